@@ -1,0 +1,151 @@
+/*
+ * insta_gb300.h -- C ABI of the GB300-native INSTA deformation + render hot path.
+ *
+ * Plain C types only (no CUDA, Eigen or torch types).  Every function returns an
+ * int status (INSTA_OK on success) and never throws; insta_last_error() gives the
+ * message of the last failure on a context.  A context is bound to one CUDA
+ * device and one stream; it is thread-compatible, not thread-safe (one host thread
+ * per context at a time).
+ *
+ * Reference interfaces these entry points replace (INSTA repository paths;
+ * "NGP/" = instant-ngp/include/neural-graphics-primitives/):
+ *   insta_canonical_set         rta::TinyMesh ctor for the canonical mesh + rta::Core::load_meshes
+ *                               adjacency and render box (src/tiny_mesh.cu:39-51,134-164,316-371;
+ *                               src/core.cu:283-304)
+ *   insta_frame_upload          rta::TinyMesh ctor for a tracked frame + BVH build and the GPU
+ *                               pointer tables (src/tiny_mesh.cu:39-51,166-178;
+ *                               instant-ngp/src/triangle_bvh.cu:548-631; src/core.cu:309-334)
+ *   insta_occupancy_from_mesh   mark_flame_density_grid + update_density_grid_mean_and_bitfield
+ *                               (instant-ngp/src/testbed_nerf.cu:364-389,2863-2878)
+ *   insta_canonical_map         rta::Core::surface_closest_point / render_deformed -> `warp`
+ *                               (src/core.cu:339-348,442-526,581-637)
+ *   insta_canonical_map_soa     the same map on bare points (index + canonical xyz)
+ *   insta_params_load           Testbed::load_snapshot parameter blob, NerfNetwork::set_params
+ *                               order (instant-ngp/src/testbed.cu:2952-3016; NGP/nerf_network.h:492-525)
+ *   insta_field_eval            NerfNetwork::inference_mixed_precision_impl (NGP/nerf_network.h:159-232)
+ *   insta_render                Testbed::render_nerf -> NerfTracer::init_rays_from_camera/trace +
+ *                               shade_kernel_nerf (instant-ngp/src/testbed_nerf.cu:2030-2244,2320-2460)
+ *   insta_march_debug           the sample positions advance_pos_nerf + generate_next_nerf_network_inputs
+ *                               emit per ray (instant-ngp/src/testbed_nerf.cu:634-686,722-795)
+ */
+#ifndef INSTA_GB300_H
+#define INSTA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define INSTA_OK 0
+#define INSTA_ERR_INVALID_ARG 1   /* bad pointer, size or index                           */
+#define INSTA_ERR_CUDA 2          /* a CUDA runtime call failed                           */
+#define INSTA_ERR_BUDGET 3        /* the context's device-memory budget would be exceeded */
+#define INSTA_ERR_NOT_READY 4     /* canonical mesh, frame or parameters missing          */
+#define INSTA_ERR_UNSUPPORTED 5   /* shape outside what the kernels implement             */
+#define INSTA_ERR_DEVICE 6        /* a kernel reported an error (stack overflow, timeout) */
+
+#define INSTA_PRECISION_FP16 0
+#define INSTA_PRECISION_BF16 1
+
+#define INSTA_FLAG_DISABLE_INTERP 0x1u   /* "disable_interp" (src/core.cu:201,495) */
+
+typedef struct insta_ctx insta_ctx;
+
+/* Hash grid + MLP shapes (configs/nerf/main.json keys).  per_level_scale <= 0 derives
+ * it as exp(log(2048 * aabb_scale / base_resolution) / (n_levels - 1))
+ * (instant-ngp/src/testbed.cu:2253-2258). */
+typedef struct {
+    uint32_t n_levels;              /* 16 */
+    uint32_t n_features_per_level;  /* 2 */
+    uint32_t log2_hashmap_size;     /* 19 */
+    uint32_t base_resolution;       /* 16 */
+    float per_level_scale;          /* 0 -> derived */
+    uint32_t aabb_scale;            /* 2 */
+    uint32_t n_extra_dims;          /* expression dims appended to the density input (0 or 16) */
+    uint32_t density_neurons;       /* 64 */
+    uint32_t density_hidden_layers; /* 1 */
+    uint32_t density_output_dims;   /* 16 */
+    uint32_t rgb_neurons;           /* 64 */
+    uint32_t rgb_hidden_layers;     /* 2 */
+    uint32_t precision;             /* INSTA_PRECISION_* */
+} insta_field_desc;
+
+/* One headless render request (Testbed::render_nerf arguments plus the avatar/frame). */
+typedef struct {
+    int32_t avatar;
+    int32_t frame;                  /* deformed frame (m_target_deform_frame) */
+    int32_t width, height;
+    float focal_length[2];          /* pixels */
+    float screen_center[2];         /* 0.5, 0.5 */
+    float camera[12];               /* 3x4 row-major [R | origin]; columns right, down, forward */
+    float cone_angle;               /* cone_angle_constant: 0 constant steps, 1/256 exponential */
+    float min_transmittance;        /* rendering_min_transmittance (0.01) */
+    uint32_t spp;                   /* sample index for the jitter sequence */
+    uint32_t snap_to_pixel_centers; /* 1 (reference default) */
+    uint32_t max_samples_per_ray;   /* 1024 */
+    uint32_t linear_colors;         /* 0: shade converts sRGB -> linear */
+    const float* extra_dims;        /* host, n_extra_dims floats, or NULL (zeros) */
+} insta_render_desc;
+
+/* -- context ---------------------------------------------------------------- */
+int insta_ctx_create(int device, void* cuda_stream, uint64_t budget_bytes, insta_ctx** out);
+int insta_ctx_destroy(insta_ctx* ctx);
+const char* insta_last_error(const insta_ctx* ctx);
+int insta_sync(insta_ctx* ctx);
+int insta_memory_used(const insta_ctx* ctx, uint64_t* bytes);
+
+/* -- avatar geometry --------------------------------------------------------- */
+/* verts f32[n_verts*3], faces i32[n_faces*3], mask u32[n_faces] (region ids, NULL = 15);
+ * host or device pointers.  Builds adjacency, canonical frames and the render box
+ * (mesh AABB inflated by 0.15 x its diagonal).  n_faces <= 16384. */
+int insta_canonical_set(insta_ctx* ctx, int avatar, const float* verts, int n_verts, const int32_t* faces, int n_faces,
+                        const uint32_t* mask);
+/* Train box (Testbed::m_aabb, unit cube by default) and render box; NULL keeps a value. */
+int insta_avatar_set_boxes(insta_ctx* ctx, int avatar, const float* train_min, const float* train_max,
+                           const float* render_min, const float* render_max);
+int insta_avatar_set_flags(insta_ctx* ctx, int avatar, uint32_t flags);
+/* Per-frame tracked mesh (same topology): f32[n_verts*3], host or device pointer. */
+int insta_frame_upload(insta_ctx* ctx, int avatar, int frame, const float* verts);
+int insta_frame_release(insta_ctx* ctx, int avatar, int frame);
+
+/* -- occupancy ---------------------------------------------------------------- */
+/* Cells (128^3, mip 0 over the unit cube) whose centre lies within `radius` of the frame's
+ * surface (nearest triangle not in region 0) become occupied; mips 1..7 are max-pooled. */
+int insta_occupancy_from_mesh(insta_ctx* ctx, int avatar, int frame, double radius);
+/* 8 mips x 128^3 bits (2 MiB), Morton order per mip; host or device pointer. */
+int insta_occupancy_set(insta_ctx* ctx, int avatar, int frame, const uint8_t* bits);
+int insta_occupancy_get(insta_ctx* ctx, int avatar, int frame, uint8_t* bits);
+
+/* -- deformation -------------------------------------------------------------- */
+/* In place on NerfCoordinate records (device pointer, stride floats each: pos[3] dt holder
+ * deformed_pos[3] dir[3] extra[n_extra]).  frame >= 0 maps every record with that frame
+ * (render_deformed); frame < 0 takes the frame from `holder` (surface_closest_point). */
+int insta_canonical_map(insta_ctx* ctx, int avatar, int frame, float* coords, uint32_t stride, uint32_t n_extra, int64_t n);
+/* Bare points (device pointers): nearest triangle id (-1 when none) and canonical xyz. */
+int insta_canonical_map_soa(insta_ctx* ctx, int avatar, int frame, const float* pts, int64_t n, int32_t* out_idx,
+                            float* out_canon);
+
+/* -- field -------------------------------------------------------------------- */
+/* FP16 parameter blob in snapshot order (density MLP, rgb MLP, hash table); host or
+ * device pointer.  n_params must equal insta_field_param_count(desc). */
+int insta_field_param_count(const insta_field_desc* desc, uint64_t* n_params);
+int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, const uint16_t* params, uint64_t n_params);
+/* out4[n][4] = (r, g, b, raw density) network outputs (device pointers). */
+int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4);
+
+/* -- render ------------------------------------------------------------------- */
+/* out_rgba f32[h*w*4] (linear RGBA, zero background), out_depth f32[h*w] (1e10 where no
+ * hit).  Host pointers: the call returns after the copy back; device pointers: asynchronous. */
+int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, float* out_depth);
+/* Network samples evaluated by the last insta_render (synchronises). */
+int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples);
+/* Per-ray sample t and dt (device pointers, [h*w][max_out]) and counts [h*w]. */
+int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out, float* out_t, float* out_dt,
+                      int32_t* out_n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

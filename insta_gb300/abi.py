@@ -1,0 +1,235 @@
+"""ctypes binding of the C ABI (include/insta_gb300.h) exported by libinsta_gb300.so.
+
+There is no CPU fallback: if the library is missing or no sm_10x GPU is
+present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libinsta_gb300.so"
+
+OK, ERR_INVALID_ARG, ERR_CUDA, ERR_BUDGET, ERR_NOT_READY, ERR_UNSUPPORTED, ERR_DEVICE = range(7)
+PRECISION_FP16, PRECISION_BF16 = 0, 1
+FLAG_DISABLE_INTERP = 1
+
+EXPORTS = [
+    "insta_ctx_create", "insta_ctx_destroy", "insta_last_error", "insta_sync", "insta_memory_used",
+    "insta_canonical_set", "insta_avatar_set_boxes", "insta_avatar_set_flags", "insta_frame_upload",
+    "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
+    "insta_canonical_map", "insta_canonical_map_soa", "insta_field_param_count", "insta_params_load",
+    "insta_field_eval", "insta_render", "insta_render_samples", "insta_march_debug",
+]
+
+
+class InstaError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[insta error {code}] {msg}")
+        self.code = code
+
+
+class FieldDesc(C.Structure):
+    _fields_ = [("n_levels", C.c_uint32), ("n_features_per_level", C.c_uint32), ("log2_hashmap_size", C.c_uint32),
+                ("base_resolution", C.c_uint32), ("per_level_scale", C.c_float), ("aabb_scale", C.c_uint32),
+                ("n_extra_dims", C.c_uint32), ("density_neurons", C.c_uint32), ("density_hidden_layers", C.c_uint32),
+                ("density_output_dims", C.c_uint32), ("rgb_neurons", C.c_uint32), ("rgb_hidden_layers", C.c_uint32),
+                ("precision", C.c_uint32)]
+
+
+class RenderDesc(C.Structure):
+    _fields_ = [("avatar", C.c_int32), ("frame", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
+                ("focal_length", C.c_float * 2), ("screen_center", C.c_float * 2), ("camera", C.c_float * 12),
+                ("cone_angle", C.c_float), ("min_transmittance", C.c_float), ("spp", C.c_uint32),
+                ("snap_to_pixel_centers", C.c_uint32), ("max_samples_per_ray", C.c_uint32), ("linear_colors", C.c_uint32),
+                ("extra_dims", C.c_void_p)]
+
+
+_lib = None
+
+
+def load(path: Path | None = None):
+    """Load the library (raises when it has not been built)."""
+    global _lib
+    if _lib is None:
+        p = Path(path) if path else LIB_PATH
+        if not p.exists():
+            raise RuntimeError(f"{p} missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        lib = C.CDLL(str(p))
+        vp, i32, i64, u32, u64 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint32, C.c_uint64
+        sig = {
+            "insta_ctx_create": [C.c_int, vp, u64, C.POINTER(vp)],
+            "insta_ctx_destroy": [vp],
+            "insta_sync": [vp],
+            "insta_memory_used": [vp, C.POINTER(u64)],
+            "insta_canonical_set": [vp, C.c_int, vp, C.c_int, vp, C.c_int, vp],
+            "insta_avatar_set_boxes": [vp, C.c_int, vp, vp, vp, vp],
+            "insta_avatar_set_flags": [vp, C.c_int, u32],
+            "insta_frame_upload": [vp, C.c_int, C.c_int, vp],
+            "insta_frame_release": [vp, C.c_int, C.c_int],
+            "insta_occupancy_from_mesh": [vp, C.c_int, C.c_int, C.c_double],
+            "insta_occupancy_set": [vp, C.c_int, C.c_int, vp],
+            "insta_occupancy_get": [vp, C.c_int, C.c_int, vp],
+            "insta_canonical_map": [vp, C.c_int, C.c_int, vp, u32, u32, i64],
+            "insta_canonical_map_soa": [vp, C.c_int, C.c_int, vp, i64, vp, vp],
+            "insta_field_param_count": [C.POINTER(FieldDesc), C.POINTER(u64)],
+            "insta_params_load": [vp, C.c_int, C.POINTER(FieldDesc), vp, u64],
+            "insta_field_eval": [vp, C.c_int, vp, u32, i64, vp],
+            "insta_render": [vp, C.POINTER(RenderDesc), vp, vp],
+            "insta_render_samples": [vp, C.POINTER(u64)],
+            "insta_march_debug": [vp, C.POINTER(RenderDesc), C.c_int, vp, vp, vp],
+        }
+        for name, args in sig.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
+        lib.insta_last_error.argtypes = [vp]
+        lib.insta_last_error.restype = C.c_char_p
+        _lib = lib
+    return _lib
+
+
+def field_desc(fc, precision: int = PRECISION_FP16) -> FieldDesc:
+    d = FieldDesc()
+    d.n_levels, d.n_features_per_level, d.log2_hashmap_size = fc.n_levels, fc.n_features, fc.log2_table
+    d.base_resolution, d.per_level_scale, d.aabb_scale = fc.base_res, fc.per_level_scale, fc.aabb_scale
+    d.n_extra_dims = fc.n_extra
+    d.density_neurons, d.density_hidden_layers, d.density_output_dims = fc.density_hidden, fc.density_layers, fc.density_out
+    d.rgb_neurons, d.rgb_hidden_layers = fc.rgb_hidden, fc.rgb_layers
+    d.precision = precision
+    return d
+
+
+def param_count(fc) -> int:
+    n = C.c_uint64(0)
+    rc = load().insta_field_param_count(C.byref(field_desc(fc)), C.byref(n))
+    if rc:
+        raise InstaError(rc, "invalid field description")
+    return int(n.value)
+
+
+def _addr(x):
+    """Address of a numpy array (host) or a torch tensor (device or host)."""
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        assert x.flags["C_CONTIGUOUS"], "arrays must be C-contiguous"
+        return C.c_void_p(x.ctypes.data)
+    if hasattr(x, "data_ptr"):
+        assert x.is_contiguous(), "tensors must be contiguous"
+        return C.c_void_p(x.data_ptr())
+    if isinstance(x, int):
+        return C.c_void_p(x)
+    raise TypeError(f"unsupported buffer type {type(x)}")
+
+
+class Context:
+    """One device, one stream, a device-memory budget; owns avatar residency."""
+
+    def __init__(self, device: int = 0, stream: int | None = None, budget_bytes: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.insta_ctx_create(device, C.c_void_p(stream) if stream else None, budget_bytes, C.byref(h))
+        if rc:
+            raise InstaError(rc, "insta_ctx_create failed (no sm_10x GPU or CUDA error)")
+        self.h = h
+
+    def _check(self, rc):
+        if rc:
+            raise InstaError(rc, self.lib.insta_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.insta_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        self._check(self.lib.insta_sync(self.h))
+
+    def memory_used(self) -> int:
+        v = C.c_uint64(0)
+        self._check(self.lib.insta_memory_used(self.h, C.byref(v)))
+        return int(v.value)
+
+    def canonical_set(self, avatar, verts, faces, mask=None):
+        v = np.ascontiguousarray(verts, dtype=np.float32)
+        f = np.ascontiguousarray(faces, dtype=np.int32)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint32)
+        self._check(self.lib.insta_canonical_set(self.h, avatar, _addr(v), len(v), _addr(f), len(f), _addr(m)))
+
+    def set_boxes(self, avatar, train=None, render=None):
+        def arr(x):
+            return None if x is None else np.ascontiguousarray(x, dtype=np.float32)
+        tmin, tmax = (None, None) if train is None else (arr(train[0]), arr(train[1]))
+        rmin, rmax = (None, None) if render is None else (arr(render[0]), arr(render[1]))
+        self._check(self.lib.insta_avatar_set_boxes(self.h, avatar, _addr(tmin), _addr(tmax), _addr(rmin), _addr(rmax)))
+
+    def set_flags(self, avatar, flags):
+        self._check(self.lib.insta_avatar_set_flags(self.h, avatar, flags))
+
+    def frame_upload(self, avatar, frame, verts):
+        v = verts if hasattr(verts, "data_ptr") else np.ascontiguousarray(verts, dtype=np.float32)
+        self._check(self.lib.insta_frame_upload(self.h, avatar, frame, _addr(v)))
+
+    def frame_release(self, avatar, frame):
+        self._check(self.lib.insta_frame_release(self.h, avatar, frame))
+
+    def occupancy_from_mesh(self, avatar, frame, radius=0.015):
+        self._check(self.lib.insta_occupancy_from_mesh(self.h, avatar, frame, float(radius)))
+
+    def occupancy_set(self, avatar, frame, bits):
+        b = np.ascontiguousarray(bits, dtype=np.uint8)
+        self._check(self.lib.insta_occupancy_set(self.h, avatar, frame, _addr(b)))
+
+    def occupancy_get(self, avatar, frame) -> np.ndarray:
+        b = np.zeros(8 * 128 ** 3 // 8, dtype=np.uint8)
+        self._check(self.lib.insta_occupancy_get(self.h, avatar, frame, _addr(b)))
+        return b
+
+    def canonical_map(self, avatar, frame, coords, stride, n_extra, n):
+        self._check(self.lib.insta_canonical_map(self.h, avatar, frame, _addr(coords), stride, n_extra, n))
+
+    def canonical_map_soa(self, avatar, frame, pts, n, out_idx, out_canon):
+        self._check(self.lib.insta_canonical_map_soa(self.h, avatar, frame, _addr(pts), n, _addr(out_idx), _addr(out_canon)))
+
+    def params_load(self, avatar, fc, params, precision=PRECISION_FP16):
+        p = params if hasattr(params, "data_ptr") else np.ascontiguousarray(params).view(np.uint16)
+        n = p.numel() if hasattr(p, "numel") else p.size
+        self._check(self.lib.insta_params_load(self.h, avatar, C.byref(field_desc(fc, precision)), _addr(p), n))
+
+    def field_eval(self, avatar, coords, stride, n, out4):
+        self._check(self.lib.insta_field_eval(self.h, avatar, _addr(coords), stride, n, _addr(out4)))
+
+    @staticmethod
+    def render_desc(avatar, frame, width, height, focal, cam, cone_angle=1 / 256, spp=0, min_transmittance=0.01,
+                    max_samples=1024, snap=True, linear_colors=False, extra_dims=None) -> RenderDesc:
+        r = RenderDesc()
+        r.avatar, r.frame, r.width, r.height = avatar, frame, width, height
+        r.focal_length[:] = [float(focal[0]), float(focal[1])]
+        r.screen_center[:] = [0.5, 0.5]
+        r.camera[:] = [float(x) for x in np.asarray(cam, dtype=np.float32).reshape(-1)]
+        r.cone_angle = float(np.float32(cone_angle))
+        r.min_transmittance = float(min_transmittance)
+        r.spp, r.snap_to_pixel_centers, r.max_samples_per_ray = spp, int(snap), max_samples
+        r.linear_colors = int(linear_colors)
+        r.extra_dims = None if extra_dims is None else extra_dims.ctypes.data
+        return r
+
+    def render(self, req: RenderDesc, out_rgba, out_depth):
+        self._check(self.lib.insta_render(self.h, C.byref(req), _addr(out_rgba), _addr(out_depth)))
+
+    def render_samples(self) -> int:
+        v = C.c_uint64(0)
+        self._check(self.lib.insta_render_samples(self.h, C.byref(v)))
+        return int(v.value)
+
+    def march_debug(self, req: RenderDesc, max_out, out_t, out_dt, out_n):
+        self._check(self.lib.insta_march_debug(self.h, C.byref(req), max_out, _addr(out_t), _addr(out_dt), _addr(out_n)))

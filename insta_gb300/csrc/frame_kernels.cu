@@ -1,0 +1,385 @@
+// frame_kernels.cu -- per-frame tracked-mesh upload on the device: triangle frame
+// records, Morton-ordered implicit 4-ary BVH (single-CTA shared-memory sort), occupancy
+// bitfield from the mesh, and the canonical-map kernels (the `warp` hook).
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace insta {
+
+// ----------------------------------------------------------------- frame records
+__device__ __forceinline__ float tri_area_rn(V3 a, V3 b, V3 c) {
+    V3 n = cross_rn(sub_rn(b, a), sub_rn(c, a));
+    return __fmul_rn(0.5f, __fsqrt_rn(dot_rn(n, n)));
+}
+
+// Triangles whose edges are almost parallel (sin^2 of the corner angle <= 1e-12) get their
+// frame built in FP64; everything else in FP32 with the reference's operation order.
+__device__ __forceinline__ bool near_degenerate(V3 e1, V3 e2) {
+    V3 n = cross_rn(e1, e2);
+    float nn = dot_rn(n, n), l1 = dot_rn(e1, e1), l2 = dot_rn(e2, e2);
+    return nn <= 1e-12f * l1 * l2;
+}
+
+struct D3 { double x, y, z; };
+__device__ __forceinline__ D3 d3cross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+__device__ __forceinline__ double d3dot(D3 a, D3 b) { return a.x * b.x + (a.y * b.y + a.z * b.z); }
+__device__ __forceinline__ D3 d3norm(D3 v) {
+    double z = d3dot(v, v);
+    if (z > 0.0) { double s = sqrt(z); return {v.x / s, v.y / s, v.z / s}; }
+    return v;
+}
+
+__device__ bool inverse4_d(const double* m, double* o) {
+    double s0 = m[0] * m[5] - m[4] * m[1], s1 = m[0] * m[6] - m[4] * m[2], s2 = m[0] * m[7] - m[4] * m[3];
+    double s3 = m[1] * m[6] - m[5] * m[2], s4 = m[1] * m[7] - m[5] * m[3], s5 = m[2] * m[7] - m[6] * m[3];
+    double c5 = m[10] * m[15] - m[14] * m[11], c4 = m[9] * m[15] - m[13] * m[11], c3 = m[9] * m[14] - m[13] * m[10];
+    double c2 = m[8] * m[15] - m[12] * m[11], c1 = m[8] * m[14] - m[12] * m[10], c0 = m[8] * m[13] - m[12] * m[9];
+    double det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    if (det == 0.0) return false;
+    double id = 1.0 / det;
+    o[0] = (m[5] * c5 - m[6] * c4 + m[7] * c3) * id;   o[1] = (-m[1] * c5 + m[2] * c4 - m[3] * c3) * id;
+    o[2] = (m[13] * s5 - m[14] * s4 + m[15] * s3) * id; o[3] = (-m[9] * s5 + m[10] * s4 - m[11] * s3) * id;
+    o[4] = (-m[4] * c5 + m[6] * c2 - m[7] * c1) * id;  o[5] = (m[0] * c5 - m[2] * c2 + m[3] * c1) * id;
+    o[6] = (-m[12] * s5 + m[14] * s2 - m[15] * s1) * id; o[7] = (m[8] * s5 - m[10] * s2 + m[11] * s1) * id;
+    o[8] = (m[4] * c4 - m[5] * c2 + m[7] * c0) * id;   o[9] = (-m[0] * c4 + m[1] * c2 - m[3] * c0) * id;
+    o[10] = (m[12] * s4 - m[13] * s2 + m[15] * s0) * id; o[11] = (-m[8] * s4 + m[9] * s2 - m[11] * s0) * id;
+    o[12] = (-m[4] * c3 + m[5] * c1 - m[6] * c0) * id; o[13] = (m[0] * c3 - m[1] * c1 + m[2] * c0) * id;
+    o[14] = (-m[12] * s3 + m[13] * s1 - m[14] * s0) * id; o[15] = (m[8] * s3 - m[9] * s1 + m[10] * s0) * id;
+    return true;
+}
+
+// TinyMesh::build_triangles (src/tiny_mesh.cu:134-164) + tri2projection (include/rta/affine.cuh:26-39)
+// for every face; `canon_area` == nullptr builds the canonical mesh (scaling 1).
+__global__ void tri_frame_kernel(int F, const float* __restrict__ verts, const int32_t* __restrict__ faces,
+                                 const uint32_t* __restrict__ mask, const float* __restrict__ canon_area,
+                                 float* __restrict__ area_out, TriFrame* __restrict__ out, int with_inverse) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    int i0 = faces[f * 3], i1 = faces[f * 3 + 1], i2 = faces[f * 3 + 2];
+    V3 a = v3(verts[i0 * 3], verts[i0 * 3 + 1], verts[i0 * 3 + 2]);
+    V3 b = v3(verts[i1 * 3], verts[i1 * 3 + 1], verts[i1 * 3 + 2]);
+    V3 c = v3(verts[i2 * 3], verts[i2 * 3 + 1], verts[i2 * 3 + 2]);
+    uint32_t m = mask ? mask[f] : 15u;
+    float area = tri_area_rn(a, b, c);
+    if (area_out) area_out[f] = area;
+    float s = canon_area ? __fmul_rn(1.0f, __fdiv_rn(area, canon_area[f])) : 1.0f;
+    V3 e1 = sub_rn(b, a), e2 = sub_rn(c, a);
+    float P[16];
+    if (!near_degenerate(e1, e2)) {
+        V3 n = normalize_rn(cross_rn(e1, e2));
+        V3 bt = normalize_rn(cross_rn(e1, n));
+        V3 tg = normalize_rn(cross_rn(bt, n));
+        float cols[3][3] = {{tg.x, bt.x, n.x}, {tg.y, bt.y, n.y}, {tg.z, bt.z, n.z}};
+        float av[3] = {a.x, a.y, a.z};
+        for (int r = 0; r < 3; ++r) {
+            for (int q = 0; q < 3; ++q) P[r * 4 + q] = m == 1u ? __fmul_rn(cols[r][q], s) : cols[r][q];
+            P[r * 4 + 3] = av[r];
+        }
+        P[12] = 0.f; P[13] = 0.f; P[14] = 0.f; P[15] = 1.f;
+        float Pi[16];
+        if (with_inverse) {
+            if (!inverse4(P, Pi))
+                for (int k = 0; k < 16; ++k) Pi[k] = (k % 5 == 0) ? 1.f : 0.f;
+            for (int r = 0; r < 4; ++r) out[f].r[3 + r] = make_float4(Pi[r * 4], Pi[r * 4 + 1], Pi[r * 4 + 2], Pi[r * 4 + 3]);
+        }
+    } else {
+        D3 A = {a.x, a.y, a.z}, E1 = {(double)b.x - a.x, (double)b.y - a.y, (double)b.z - a.z};
+        D3 E2 = {(double)c.x - a.x, (double)c.y - a.y, (double)c.z - a.z};
+        D3 n = d3norm(d3cross(E1, E2));
+        D3 bt = d3norm(d3cross(E1, n));
+        D3 tg = d3norm(d3cross(bt, n));
+        double cols[3][3] = {{tg.x, bt.x, n.x}, {tg.y, bt.y, n.y}, {tg.z, bt.z, n.z}};
+        double av[3] = {A.x, A.y, A.z}, Pd[16];
+        for (int r = 0; r < 3; ++r) {
+            for (int q = 0; q < 3; ++q) Pd[r * 4 + q] = m == 1u ? cols[r][q] * (double)s : cols[r][q];
+            Pd[r * 4 + 3] = av[r];
+        }
+        Pd[12] = 0.0; Pd[13] = 0.0; Pd[14] = 0.0; Pd[15] = 1.0;
+        for (int k = 0; k < 16; ++k) P[k] = (float)Pd[k];
+        if (with_inverse) {
+            double Pi[16];
+            if (!inverse4_d(Pd, Pi))
+                for (int k = 0; k < 16; ++k) Pi[k] = (k % 5 == 0) ? 1.0 : 0.0;
+            for (int r = 0; r < 4; ++r)
+                out[f].r[3 + r] = make_float4((float)Pi[r * 4], (float)Pi[r * 4 + 1], (float)Pi[r * 4 + 2], (float)Pi[r * 4 + 3]);
+        }
+    }
+    for (int r = 0; r < 3; ++r) out[f].r[r] = make_float4(P[r * 4], P[r * 4 + 1], P[r * 4 + 2], P[r * 4 + 3]);
+    if (!with_inverse)
+        for (int r = 0; r < 4; ++r) out[f].r[3 + r] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float cx = __fdiv_rn(__fadd_rn(__fadd_rn(a.x, b.x), c.x), 3.0f);
+    float cy = __fdiv_rn(__fadd_rn(__fadd_rn(a.y, b.y), c.y), 3.0f);
+    float cz = __fdiv_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), 3.0f);
+    out[f].r[7] = make_float4(cx, cy, cz, __uint_as_float(m));
+}
+
+// --------------------------------------------------------------- BVH build (1 CTA)
+struct BvhBuildArgs {
+    int F, n_leaves, n_levels;
+    int level_off[INSTA_MAX_LEVELS + 1];
+    int level_cnt[INSTA_MAX_LEVELS + 1];
+    const float* verts;
+    const int32_t* faces;
+    const TriFrame* frames;
+    float4* leaf_tris;
+    float4* nodes;
+    int np2;
+};
+
+__device__ __forceinline__ void box_union(float* b, const float* o) {
+    b[0] = fminf(b[0], o[0]); b[1] = fminf(b[1], o[1]); b[2] = fminf(b[2], o[2]);
+    b[3] = fmaxf(b[3], o[3]); b[4] = fmaxf(b[4], o[4]); b[5] = fmaxf(b[5], o[5]);
+}
+
+// Linear BVH: sort triangles by the 30-bit Morton code of their centroid (ties by id), then
+// group 4 consecutive triangles per leaf and 4 consecutive nodes per parent, bottom-up.
+__global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t* keys = reinterpret_cast<uint64_t*>(smem_raw);
+    __shared__ float red[6][32];
+    __shared__ float ext[6];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    // 1. centroid bounds
+    float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (int f = tid; f < a.F; f += nt) {
+        float4 c = a.frames[f].r[7];
+        lo[0] = fminf(lo[0], c.x); lo[1] = fminf(lo[1], c.y); lo[2] = fminf(lo[2], c.z);
+        hi[0] = fmaxf(hi[0], c.x); hi[1] = fmaxf(hi[1], c.y); hi[2] = fmaxf(hi[2], c.z);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+    if ((tid & 31) == 0)
+        for (int k = 0; k < 3; ++k) { red[k][tid >> 5] = lo[k]; red[3 + k][tid >> 5] = hi[k]; }
+    __syncthreads();
+    if (tid < 32) {
+        int nw = nt >> 5;
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = tid < nw ? red[k][tid] : 3.4e38f;
+            hi[k] = tid < nw ? red[3 + k][tid] : -3.4e38f;
+        }
+        for (int o = 16; o > 0; o >>= 1)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+            }
+        if (tid == 0)
+            for (int k = 0; k < 3; ++k) { ext[k] = lo[k]; float e = hi[k] - lo[k]; ext[3 + k] = e > 0.f ? 1.f / e : 0.f; }
+    }
+    __syncthreads();
+    // 2. Morton keys
+    for (int i = tid; i < a.np2; i += nt) {
+        uint64_t key = ~0ull;
+        if (i < a.F) {
+            float4 c = a.frames[i].r[7];
+            float q[3] = {(c.x - ext[0]) * ext[3], (c.y - ext[1]) * ext[4], (c.z - ext[2]) * ext[5]};
+            uint32_t v[3];
+            for (int k = 0; k < 3; ++k) v[k] = (uint32_t)fminf(fmaxf(q[k] * 1024.f, 0.f), 1023.f);
+            key = ((uint64_t)morton3d(v[0], v[1], v[2]) << 32) | (uint32_t)i;
+        }
+        keys[i] = key;
+    }
+    __syncthreads();
+    // 3. bitonic sort, ascending
+    for (int k = 2; k <= a.np2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < a.np2; i += nt) {
+                int ixj = i ^ j;
+                if (ixj > i) {
+                    uint64_t x = keys[i], y = keys[ixj];
+                    bool up = (i & k) == 0;
+                    if ((x > y) == up) { keys[i] = y; keys[ixj] = x; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // 4. leaf triangle records in sorted order
+    for (int s = tid; s < a.n_leaves * 4; s += nt) {
+        float4* dst = a.leaf_tris + (size_t)s * 3;
+        if (s < a.F) {
+            uint32_t f = (uint32_t)(keys[s] & 0xffffffffu);
+            int i0 = a.faces[f * 3], i1 = a.faces[f * 3 + 1], i2 = a.faces[f * 3 + 2];
+            const float* A = a.verts + i0 * 3; const float* B = a.verts + i1 * 3; const float* C = a.verts + i2 * 3;
+            dst[0] = make_float4(A[0], A[1], A[2], B[0]);
+            dst[1] = make_float4(B[1], B[2], C[0], C[1]);
+            dst[2] = make_float4(C[2], __uint_as_float(f), 0.f, 0.f);
+        } else {
+            dst[0] = make_float4(0.f, 0.f, 0.f, 0.f); dst[1] = dst[0]; dst[2] = dst[0];
+        }
+    }
+    __syncthreads();
+    // 5. boxes, bottom-up.  Region A (child boxes) and B (parent boxes) reuse the key buffer.
+    float* boxA = reinterpret_cast<float*>(smem_raw);
+    float* boxB = boxA + 6 * 4096;
+    for (int L = tid; L < a.n_leaves; L += nt) {
+        float b[6] = {3.4e38f, 3.4e38f, 3.4e38f, -3.4e38f, -3.4e38f, -3.4e38f};
+        for (int i = 0; i < 4; ++i) {
+            int s = L * 4 + i;
+            if (s >= a.F) break;
+            const float4* t = a.leaf_tris + (size_t)s * 3;
+            float4 q0 = t[0], q1 = t[1], q2 = t[2];
+            float pts[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+            for (int p = 0; p < 3; ++p) {
+                float pb[6] = {pts[p * 3], pts[p * 3 + 1], pts[p * 3 + 2], pts[p * 3], pts[p * 3 + 1], pts[p * 3 + 2]};
+                box_union(b, pb);
+            }
+        }
+        for (int k = 0; k < 6; ++k) boxA[L * 6 + k] = b[k];
+    }
+    __syncthreads();
+    float* child = boxA;
+    float* parent = boxB;
+    for (int lev = a.n_levels - 1; lev >= 0; --lev) {
+        int cnt = a.level_cnt[lev], ccnt = a.level_cnt[lev + 1];
+        for (int j = tid; j < cnt; j += nt) {
+            float mn[3][4], mx[3][4];
+            float nb[6] = {3.4e38f, 3.4e38f, 3.4e38f, -3.4e38f, -3.4e38f, -3.4e38f};
+            for (int i = 0; i < 4; ++i) {
+                int c = j * 4 + i;
+                if (c < ccnt) {
+                    for (int k = 0; k < 3; ++k) { mn[k][i] = child[c * 6 + k]; mx[k][i] = child[c * 6 + 3 + k]; }
+                    box_union(nb, &child[c * 6]);
+                } else {
+                    for (int k = 0; k < 3; ++k) { mn[k][i] = __int_as_float(0x7f800000); mx[k][i] = -__int_as_float(0x7f800000); }
+                }
+            }
+            float4* nd = a.nodes + ((size_t)a.level_off[lev] + j) * 6;
+            for (int k = 0; k < 3; ++k) {
+                nd[k] = make_float4(mn[k][0], mn[k][1], mn[k][2], mn[k][3]);
+                nd[3 + k] = make_float4(mx[k][0], mx[k][1], mx[k][2], mx[k][3]);
+            }
+            for (int k = 0; k < 6; ++k) parent[j * 6 + k] = nb[k];
+        }
+        __syncthreads();
+        float* t = child; child = parent; parent = t;
+    }
+}
+
+// --------------------------------------------------------------------- occupancy
+// mark_flame_density_grid (ngp/src/testbed_nerf.cu:364-389) over the deformed mesh, fused with
+// grid_to_bitfield (:585-609): one thread per bitfield byte (8 Morton-consecutive cells).
+__global__ void occupancy_kernel(FrameView fr, double radius, float bound, uint8_t* __restrict__ bits, uint32_t* err) {
+    uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= GRID3 / 8) return;
+    uint8_t out = 0;
+    for (uint32_t j = 0; j < 8; ++j) {
+        uint32_t cell = b * 8 + j;
+        uint32_t x = morton_invert(cell), y = morton_invert(cell >> 1), z = morton_invert(cell >> 2);
+        V3 p = v3(__fdiv_rn((float)x + 0.5f, 128.f), __fdiv_rn((float)y + 0.5f, 128.f), __fdiv_rn((float)z + 0.5f, 128.f));
+        NearestResult r = nearest_triangle(fr, p, bound, err);
+        if (r.id >= 0) {
+            uint32_t m;
+            load_centroid(fr.frames, (uint32_t)r.id, &m);
+            if ((double)__fsqrt_rn(r.d2) < radius && m != 0u) out |= (uint8_t)(1u << j);
+        }
+    }
+    bits[b] = out;
+}
+
+// bitfield_max_pool (:611-632) for one mip level; `next` must be zeroed.
+__global__ void maxpool_kernel(const uint8_t* __restrict__ prev, uint8_t* __restrict__ next) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= GRID3 / 64) return;
+    uint8_t bits = 0;
+    for (int j = 0; j < 8; ++j) bits |= prev[i * 8 + j] > 0 ? (uint8_t)(1u << j) : 0;
+    uint32_t x = morton_invert(i) + GRID / 8, y = morton_invert(i >> 1) + GRID / 8, z = morton_invert(i >> 2) + GRID / 8;
+    next[morton3d(x, y, z)] |= bits;
+}
+
+// ---------------------------------------------------------------- canonical map
+__global__ void canonical_map_soa_kernel(FrameView fr, DeformView dv, const float* __restrict__ pts, int64_t n,
+                                         int32_t* __restrict__ out_idx, float* __restrict__ out_canon, uint32_t* err) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    V3 p = v3(pts[i * 3], pts[i * 3 + 1], pts[i * 3 + 2]);
+    NearestResult r = nearest_triangle(fr, p, 0.f, err);
+    out_idx[i] = r.id;
+    if (r.id < 0) {
+        atomicOr(err, INSTA_DEVERR_NO_TRI);
+        out_canon[i * 3] = p.x; out_canon[i * 3 + 1] = p.y; out_canon[i * 3 + 2] = p.z;
+        return;
+    }
+    float o[3];
+    map_to_canonical(dv, fr.frames, (uint32_t)r.id, p, nullptr, o, nullptr, nullptr);
+    out_canon[i * 3] = o[0]; out_canon[i * 3 + 1] = o[1]; out_canon[i * 3 + 2] = o[2];
+}
+
+// warp (src/core.cu:442-526) in place on NerfCoordinate records (NGP/nerf.h:86-115).
+__global__ void canonical_map_coords_kernel(const FrameView* __restrict__ frames, uint32_t n_frames, DeformView dv,
+                                            float* __restrict__ coords, uint32_t stride, uint32_t n_extra, int64_t n,
+                                            int32_t frame_id, uint32_t* err) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float* c = coords + i * stride;
+    float holder = c[4];
+    if (holder < 0.f) return;
+    uint32_t fid = frame_id < 0 ? (uint32_t)holder : (uint32_t)frame_id;
+    if (fid >= n_frames) return;
+    V3 p = v3(c[0], c[1], c[2]);
+    if (!box_contains(dv.aabb_min, dv.aabb_max, p)) return;
+    const FrameView& fr = frames[fid];
+    NearestResult r = nearest_triangle(fr, p, 0.f, err);
+    if (r.id < 0) { atomicOr(err, INSTA_DEVERR_NO_TRI); return; }
+    float pos[3], dir[3], dw[3] = {c[8], c[9], c[10]};
+    uint32_t mask;
+    map_to_canonical(dv, fr.frames, (uint32_t)r.id, p, dw, pos, dir, &mask);
+    c[0] = pos[0]; c[1] = pos[1]; c[2] = pos[2];
+    c[8] = dir[0]; c[9] = dir[1]; c[10] = dir[2];
+    if (mask != 7u)
+        for (uint32_t m = 0; m < n_extra; ++m) c[stride - n_extra + m] = 1.f;
+}
+
+// ------------------------------------------------------------------- launchers
+cudaError_t launch_tri_frames(int F, const float* verts, const int32_t* faces, const uint32_t* mask, const float* canon_area,
+                              float* area_out, TriFrame* out, int with_inverse, cudaStream_t s) {
+    tri_frame_kernel<<<(F + 255) / 256, 256, 0, s>>>(F, verts, faces, mask, canon_area, area_out, out, with_inverse);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bvh_build(const FrameView& fv, int n_leaves, const float* verts, const int32_t* faces, cudaStream_t s) {
+    BvhBuildArgs a;
+    a.F = fv.n_tris; a.n_leaves = n_leaves; a.n_levels = fv.n_levels;
+    for (int k = 0; k <= INSTA_MAX_LEVELS; ++k) { a.level_off[k] = fv.level_off[k]; a.level_cnt[k] = fv.level_cnt[k]; }
+    a.verts = verts; a.faces = faces; a.frames = fv.frames;
+    a.leaf_tris = const_cast<float4*>(fv.leaf_tris); a.nodes = const_cast<float4*>(fv.nodes);
+    int np2 = 1;
+    while (np2 < fv.n_tris) np2 <<= 1;
+    if (np2 < 2) np2 = 2;
+    a.np2 = np2;
+    size_t keys_bytes = (size_t)np2 * 8;
+    size_t box_bytes = (size_t)(4096 + 1366) * 6 * 4;
+    size_t smem = keys_bytes > box_bytes ? keys_bytes : box_bytes;
+    cudaError_t e = cudaFuncSetAttribute(bvh_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    bvh_build_kernel<<<1, 1024, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_occupancy(const FrameView& fv, double radius, uint8_t* bitfield, uint32_t* err, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(bitfield + GRID3 / 8, 0, (size_t)7 * GRID3 / 8, s);
+    if (e != cudaSuccess) return e;
+    float bound = (float)(radius * radius * 1.0001);
+    occupancy_kernel<<<(GRID3 / 8 + 255) / 256, 256, 0, s>>>(fv, radius, bound, bitfield, err);
+    for (int lvl = 1; lvl < 8; ++lvl)
+        maxpool_kernel<<<(GRID3 / 64 + 255) / 256, 256, 0, s>>>(bitfield + (size_t)(lvl - 1) * GRID3 / 8, bitfield + (size_t)lvl * GRID3 / 8);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_canonical_map_soa(const FrameView& fv, const DeformView& dv, const float* pts, int64_t n, int32_t* out_idx,
+                                     float* out_canon, uint32_t* err, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    canonical_map_soa_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(fv, dv, pts, n, out_idx, out_canon, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_canonical_map_coords(const FrameView* frames_dev, uint32_t n_frames, const DeformView& dv, float* coords,
+                                        uint32_t stride, uint32_t n_extra, int64_t n, int32_t frame_id, uint32_t* err, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    canonical_map_coords_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(frames_dev, n_frames, dv, coords, stride, n_extra, n, frame_id, err);
+    return cudaGetLastError();
+}
+
+}  // namespace insta

@@ -1,0 +1,709 @@
+// insta_abi.cu -- host side of the C ABI: device residency of avatars (canonical mesh,
+// per-frame BVHs, occupancy bitfields, field parameters), argument checking and launches.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/insta_gb300.h"
+#include "device_common.cuh"
+#include "umma.cuh"
+#include "kernels.h"
+
+using namespace insta;
+
+namespace {
+
+struct Failure : std::runtime_error {
+    int code;
+    Failure(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    throw Failure(code, buf);
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) fail(INSTA_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct Frame {
+    DevBuf verts, frames, leaf_tris, nodes, bitfield;
+    FrameView view{};
+    int n_leaves = 0;
+    bool has_occupancy = false;
+};
+
+struct Field {
+    bool ready = false;
+    insta_field_desc desc{};
+    DevBuf params, image;
+    MlpPlan plan{};
+    FieldView view{};
+    uint64_t n_params = 0;
+};
+
+struct Avatar {
+    int V = 0, F = 0;
+    bool has_canon = false;
+    DevBuf faces, mask, adjacency, canon_verts, canon_area, canon_frames;
+    float render_min[3], render_max[3];
+    float train_min[3] = {0.f, 0.f, 0.f}, train_max[3] = {1.f, 1.f, 1.f};
+    uint32_t flags = 0;
+    std::map<int, Frame> frames;
+    DevBuf frame_table;
+    bool table_dirty = true;
+    uint32_t table_frames = 0;
+    Field field;
+};
+
+struct insta_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint64_t budget = 0, used = 0;
+    std::map<int, std::unique_ptr<Avatar>> avatars;
+    std::string last_error;
+    uint32_t* err_dev = nullptr;
+    uint32_t* ray_counter = nullptr;
+    unsigned long long* sample_counter = nullptr;
+    DevBuf out_rgba, out_depth, extra;
+    int sms = 0;
+    int render_ctas = 0;
+
+    void* alloc(DevBuf& b, size_t bytes) {
+        if (b.p && b.bytes >= bytes) return b.p;
+        release(b);
+        if (budget && used + bytes > budget)
+            fail(INSTA_ERR_BUDGET, "device budget exceeded: %llu + %zu > %llu bytes", (unsigned long long)used, bytes,
+                 (unsigned long long)budget);
+        CK(cudaMalloc(&b.p, bytes));
+        b.bytes = bytes;
+        used += bytes;
+        return b.p;
+    }
+    void release(DevBuf& b) {
+        if (b.p) {
+            cudaFree(b.p);
+            used -= b.bytes;
+        }
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    // Read and clear the device error word (synchronises the stream).
+    void check_device() {
+        CK(cudaStreamSynchronize(stream));
+        uint32_t e = 0;
+        CK(cudaMemcpy(&e, err_dev, sizeof(e), cudaMemcpyDeviceToHost));
+        if (e) {
+            CK(cudaMemset(err_dev, 0, sizeof(uint32_t)));
+            fail(INSTA_ERR_DEVICE, "device error word 0x%x (%s%s%s%s)", e, (e & INSTA_DEVERR_STACK) ? "stack overflow " : "",
+                 (e & INSTA_DEVERR_TIMEOUT) ? "wait timeout " : "", (e & INSTA_DEVERR_NO_TRI) ? "no triangle " : "",
+                 (e & INSTA_DEVERR_MARCH) ? "march guard" : "");
+        }
+    }
+    Avatar& avatar(int id, bool create = false) {
+        auto it = avatars.find(id);
+        if (it == avatars.end()) {
+            if (!create) fail(INSTA_ERR_NOT_READY, "avatar %d has no canonical mesh", id);
+            it = avatars.emplace(id, std::make_unique<Avatar>()).first;
+        }
+        return *it->second;
+    }
+};
+
+namespace {
+
+template <typename F>
+int guarded(insta_ctx* ctx, F&& f) {
+    if (!ctx) return INSTA_ERR_INVALID_ARG;
+    try {
+        int dev = -1;
+        cudaGetDevice(&dev);
+        if (dev != ctx->device) CK(cudaSetDevice(ctx->device));
+        f();
+        return INSTA_OK;
+    } catch (const Failure& e) {
+        ctx->last_error = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        ctx->last_error = e.what();
+        return INSTA_ERR_CUDA;
+    }
+}
+
+// TinyMesh::get_triangle_3_neighbours (src/tiny_mesh.cu:316-371): faces sharing an edge,
+// sorted by id, self removed, padded with -1 (extra entries past 3 are dropped).
+std::vector<int32_t> triangle_neighbours(const std::vector<int32_t>& faces, int F, int V) {
+    std::vector<std::vector<int32_t>> vf(V);
+    for (int f = 0; f < F; ++f)
+        for (int k = 0; k < 3; ++k) vf[faces[f * 3 + k]].push_back(f);
+    std::vector<int32_t> adj((size_t)F * 3, -1);
+    for (int f = 0; f < F; ++f) {
+        std::set<int32_t> ids;
+        const int e[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+        for (auto& ed : e) {
+            const auto& A = vf[faces[f * 3 + ed[0]]];
+            const auto& B = vf[faces[f * 3 + ed[1]]];
+            for (int32_t x : A)
+                if (std::find(B.begin(), B.end(), x) != B.end()) ids.insert(x);
+        }
+        int k = 0;
+        for (int32_t id : ids)
+            if (id != f && k < 3) adj[(size_t)f * 3 + k++] = id;
+    }
+    return adj;
+}
+
+void host_copy(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s));
+}
+
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Implicit 4-ary tree shape: leaves of 4 Morton-consecutive triangles, 4 nodes per parent.
+void tree_shape(int F, FrameView& v, int& n_leaves, int& n_internal) {
+    n_leaves = std::max(1, (F + 3) / 4);
+    std::vector<int> cnt;
+    int c = n_leaves;
+    do {
+        c = (c + 3) / 4;
+        cnt.push_back(c);
+    } while (c > 1);
+    std::reverse(cnt.begin(), cnt.end());
+    v.n_levels = (int)cnt.size();
+    if (v.n_levels > INSTA_MAX_LEVELS) fail(INSTA_ERR_UNSUPPORTED, "mesh too large for the BVH level table");
+    int off = 0;
+    for (int k = 0; k < v.n_levels; ++k) {
+        v.level_off[k] = off;
+        v.level_cnt[k] = cnt[k];
+        off += cnt[k];
+    }
+    v.level_off[v.n_levels] = off;
+    v.level_cnt[v.n_levels] = n_leaves;
+    n_internal = off;
+}
+
+float level_scale_host(float b, uint32_t base, uint32_t l) { return exp2f((float)l * log2f(b)) * (float)base - 1.0f; }
+
+struct FieldLayout {
+    uint64_t layer_off[8];
+    uint32_t layer_n[8], layer_k[8];
+    int n_density, n_rgb;
+    uint64_t table_off, total;
+    uint32_t lvl_res[INSTA_MAX_HASH_LEVELS], lvl_size[INSTA_MAX_HASH_LEVELS];
+    uint64_t lvl_off[INSTA_MAX_HASH_LEVELS];
+    float lvl_scale[INSTA_MAX_HASH_LEVELS];
+    float b;
+};
+
+FieldLayout field_layout(const insta_field_desc& d) {
+    if (d.n_levels == 0 || d.n_levels > INSTA_MAX_HASH_LEVELS) fail(INSTA_ERR_UNSUPPORTED, "n_levels must be 1..%d", INSTA_MAX_HASH_LEVELS);
+    if (d.n_features_per_level != 2) fail(INSTA_ERR_UNSUPPORTED, "n_features_per_level must be 2");
+    if (d.n_levels * 2 != 32) fail(INSTA_ERR_UNSUPPORTED, "the hash encoding must have 32 outputs (16 levels x 2)");
+    if (d.n_extra_dims != 0 && d.n_extra_dims != 16) fail(INSTA_ERR_UNSUPPORTED, "n_extra_dims must be 0 or 16");
+    if (d.density_neurons != 64 || d.rgb_neurons != 64) fail(INSTA_ERR_UNSUPPORTED, "MLP width must be 64");
+    if (d.density_output_dims != 16) fail(INSTA_ERR_UNSUPPORTED, "density_output_dims must be 16");
+    if (d.density_hidden_layers < 1 || d.density_hidden_layers > 3 || d.rgb_hidden_layers < 1 || d.rgb_hidden_layers > 4)
+        fail(INSTA_ERR_UNSUPPORTED, "hidden layer counts out of range");
+    if (d.log2_hashmap_size < 8 || d.log2_hashmap_size > 24) fail(INSTA_ERR_UNSUPPORTED, "log2_hashmap_size out of range");
+    if (d.precision > 1) fail(INSTA_ERR_UNSUPPORTED, "precision must be FP16 or BF16");
+    FieldLayout L{};
+    float b = d.per_level_scale;
+    if (!(b > 0.f)) b = expf(logf(2048.0f * (float)d.aabb_scale / (float)d.base_resolution) / (float)(d.n_levels - 1));
+    L.b = b;
+    uint64_t off = 0;
+    int li = 0;
+    uint32_t n_in = d.n_levels * 2 + d.n_extra_dims;
+    std::vector<uint32_t> w = {n_in};
+    for (uint32_t h = 0; h < d.density_hidden_layers; ++h) w.push_back(64);
+    w.push_back(16);
+    for (size_t k = 0; k + 1 < w.size(); ++k) { L.layer_off[li] = off; L.layer_n[li] = w[k + 1]; L.layer_k[li] = w[k]; off += (uint64_t)w[k + 1] * w[k]; ++li; }
+    L.n_density = li;
+    w = {32};
+    for (uint32_t h = 0; h < d.rgb_hidden_layers; ++h) w.push_back(64);
+    w.push_back(16);
+    for (size_t k = 0; k + 1 < w.size(); ++k) { L.layer_off[li] = off; L.layer_n[li] = w[k + 1]; L.layer_k[li] = w[k]; off += (uint64_t)w[k + 1] * w[k]; ++li; }
+    L.n_rgb = li - L.n_density;
+    L.table_off = off;
+    uint64_t T = 1ull << d.log2_hashmap_size, eoff = 0;
+    for (uint32_t l = 0; l < d.n_levels; ++l) {
+        float s = level_scale_host(b, d.base_resolution, l);
+        uint32_t res = (uint32_t)ceilf(s) + 1u;
+        uint64_t r3 = (uint64_t)res * res * res;
+        uint64_t sz = std::min((r3 + 7) / 8 * 8, T);
+        L.lvl_res[l] = res; L.lvl_size[l] = (uint32_t)sz; L.lvl_off[l] = eoff; L.lvl_scale[l] = s;
+        eoff += sz;
+    }
+    L.total = off + eoff * 2;
+    return L;
+}
+
+uint16_t half_to_bf16_bits(uint16_t h) {
+    // exact FP16 -> FP32, then round-to-nearest-even to BF16
+    uint32_t sign = (h >> 15) & 1u, exp = (h >> 10) & 0x1fu, man = h & 0x3ffu;
+    float f;
+    if (exp == 0) f = std::ldexp((float)man, -24);
+    else if (exp == 31) f = man ? NAN : INFINITY;
+    else f = std::ldexp((float)(man | 0x400u), (int)exp - 25);
+    if (sign) f = -f;
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40u);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+Frame& get_frame(Avatar& a, int frame) {
+    auto it = a.frames.find(frame);
+    if (it == a.frames.end()) fail(INSTA_ERR_NOT_READY, "frame %d was not uploaded", frame);
+    return it->second;
+}
+
+DeformView deform_view(const Avatar& a) {
+    DeformView dv{};
+    dv.canon = static_cast<const TriFrame*>(a.canon_frames.p);
+    dv.adjacency = static_cast<const int32_t*>(a.adjacency.p);
+    dv.disable_interp = (a.flags & INSTA_FLAG_DISABLE_INTERP) ? 1 : 0;
+    for (int k = 0; k < 3; ++k) { dv.aabb_min[k] = a.train_min[k]; dv.aabb_max[k] = a.train_max[k]; }
+    return dv;
+}
+
+RenderView render_view(const Avatar& a, const insta_render_desc& r) {
+    RenderView rv{};
+    rv.width = r.width; rv.height = r.height;
+    rv.focal[0] = r.focal_length[0]; rv.focal[1] = r.focal_length[1];
+    rv.screen_center[0] = r.screen_center[0]; rv.screen_center[1] = r.screen_center[1];
+    std::memcpy(rv.cam, r.camera, sizeof(rv.cam));
+    for (int k = 0; k < 3; ++k) {
+        rv.aabb_min[k] = a.render_min[k]; rv.aabb_max[k] = a.render_max[k];
+        rv.train_min[k] = a.train_min[k]; rv.train_max[k] = a.train_max[k];
+    }
+    rv.cone_angle = r.cone_angle;
+    rv.min_transmittance = r.min_transmittance;
+    rv.spp = r.spp;
+    rv.max_samples_per_ray = r.max_samples_per_ray ? r.max_samples_per_ray : 1024u;
+    rv.snap_to_pixel_centers = r.snap_to_pixel_centers ? 1 : 0;
+    rv.frame_id = r.frame;
+    rv.linear_colors = r.linear_colors ? 1 : 0;
+    return rv;
+}
+
+void check_request(const insta_render_desc* r) {
+    if (!r) fail(INSTA_ERR_INVALID_ARG, "null request");
+    if (r->width <= 0 || r->height <= 0 || (int64_t)r->width * r->height > (int64_t)1 << 26)
+        fail(INSTA_ERR_INVALID_ARG, "bad resolution %dx%d", r->width, r->height);
+    if (!(r->focal_length[0] > 0.f) || !(r->focal_length[1] > 0.f)) fail(INSTA_ERR_INVALID_ARG, "focal length must be positive");
+    if (r->cone_angle < 0.f) fail(INSTA_ERR_INVALID_ARG, "cone_angle must be >= 0");
+}
+
+}  // namespace
+
+extern "C" {
+
+int insta_ctx_create(int device, void* cuda_stream, uint64_t budget_bytes, insta_ctx** out) {
+    if (!out) return INSTA_ERR_INVALID_ARG;
+    *out = nullptr;
+    auto ctx = std::make_unique<insta_ctx>();
+    ctx->device = device;
+    ctx->budget = budget_bytes;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return INSTA_ERR_CUDA;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return INSTA_ERR_CUDA;
+    int major = 0, minor = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+    if (major != 10) return INSTA_ERR_UNSUPPORTED;   // tcgen05 kernels are built for sm_103a only
+    cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+    if (cuda_stream) ctx->stream = static_cast<cudaStream_t>(cuda_stream);
+    else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return INSTA_ERR_CUDA;
+        ctx->own_stream = true;
+    }
+    if (cudaMalloc(&ctx->err_dev, 64) != cudaSuccess) return INSTA_ERR_CUDA;
+    cudaMemset(ctx->err_dev, 0, 64);
+    ctx->ray_counter = ctx->err_dev + 4;
+    ctx->sample_counter = reinterpret_cast<unsigned long long*>(ctx->err_dev + 8);
+    *out = ctx.release();
+    return INSTA_OK;
+}
+
+int insta_ctx_destroy(insta_ctx* ctx) {
+    if (!ctx) return INSTA_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->avatars) {
+        Avatar& a = *kv.second;
+        for (DevBuf* b : {&a.faces, &a.mask, &a.adjacency, &a.canon_verts, &a.canon_area, &a.canon_frames, &a.frame_table,
+                          &a.field.params, &a.field.image})
+            ctx->release(*b);
+        for (auto& f : a.frames)
+            for (DevBuf* b : {&f.second.verts, &f.second.frames, &f.second.leaf_tris, &f.second.nodes, &f.second.bitfield})
+                ctx->release(*b);
+    }
+    ctx->release(ctx->out_rgba);
+    ctx->release(ctx->out_depth);
+    ctx->release(ctx->extra);
+    cudaFree(ctx->err_dev);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return INSTA_OK;
+}
+
+const char* insta_last_error(const insta_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int insta_sync(insta_ctx* ctx) {
+    return guarded(ctx, [&] { ctx->check_device(); });
+}
+
+int insta_memory_used(const insta_ctx* ctx, uint64_t* bytes) {
+    if (!ctx || !bytes) return INSTA_ERR_INVALID_ARG;
+    *bytes = ctx->used;
+    return INSTA_OK;
+}
+
+int insta_canonical_set(insta_ctx* ctx, int avatar, const float* verts, int n_verts, const int32_t* faces, int n_faces,
+                        const uint32_t* mask) {
+    return guarded(ctx, [&] {
+        if (!verts || !faces || n_verts < 3 || n_faces < 1) fail(INSTA_ERR_INVALID_ARG, "empty mesh");
+        if (n_faces > 16384) fail(INSTA_ERR_UNSUPPORTED, "n_faces %d > 16384 (single-CTA BVH build)", n_faces);
+        Avatar& a = ctx->avatar(avatar, true);
+        if (a.has_canon && (a.V != n_verts || a.F != n_faces)) fail(INSTA_ERR_INVALID_ARG, "topology change on avatar %d", avatar);
+        std::vector<int32_t> hf((size_t)n_faces * 3);
+        std::vector<float> hv((size_t)n_verts * 3);
+        CK(cudaMemcpy(hf.data(), faces, hf.size() * 4, cudaMemcpyDefault));
+        CK(cudaMemcpy(hv.data(), verts, hv.size() * 4, cudaMemcpyDefault));
+        for (int32_t i : hf)
+            if (i < 0 || i >= n_verts) fail(INSTA_ERR_INVALID_ARG, "face index %d out of range", i);
+        std::vector<uint32_t> hm((size_t)n_faces, 15u);
+        if (mask) CK(cudaMemcpy(hm.data(), mask, hm.size() * 4, cudaMemcpyDefault));
+        a.V = n_verts;
+        a.F = n_faces;
+        std::vector<int32_t> adj = triangle_neighbours(hf, n_faces, n_verts);
+        ctx->alloc(a.faces, hf.size() * 4);
+        ctx->alloc(a.mask, hm.size() * 4);
+        ctx->alloc(a.adjacency, adj.size() * 4);
+        ctx->alloc(a.canon_verts, hv.size() * 4);
+        ctx->alloc(a.canon_area, (size_t)n_faces * 4);
+        ctx->alloc(a.canon_frames, (size_t)n_faces * sizeof(TriFrame));
+        host_copy(a.faces.p, hf.data(), hf.size() * 4, ctx->stream);
+        host_copy(a.mask.p, hm.data(), hm.size() * 4, ctx->stream);
+        host_copy(a.adjacency.p, adj.data(), adj.size() * 4, ctx->stream);
+        host_copy(a.canon_verts.p, hv.data(), hv.size() * 4, ctx->stream);
+        CK(launch_tri_frames(n_faces, (const float*)a.canon_verts.p, (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p, nullptr,
+                             (float*)a.canon_area.p, (TriFrame*)a.canon_frames.p, 0, ctx->stream));
+        // TinyMesh::build_triangles render box: vertex AABB inflated by 0.15 x |diag| (src/tiny_mesh.cu:157-162)
+        float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int v = 0; v < n_verts; ++v)
+            for (int k = 0; k < 3; ++k) { mn[k] = std::min(mn[k], hv[v * 3 + k]); mx[k] = std::max(mx[k], hv[v * 3 + k]); }
+        float dx = mx[0] - mn[0], dy = mx[1] - mn[1], dz = mx[2] - mn[2];
+        float infl = sqrtf(dx * dx + (dy * dy + dz * dz)) * 0.15f;
+        for (int k = 0; k < 3; ++k) { a.render_min[k] = mn[k] - infl; a.render_max[k] = mx[k] + infl; }
+        a.has_canon = true;
+        CK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int insta_avatar_set_boxes(insta_ctx* ctx, int avatar, const float* train_min, const float* train_max, const float* render_min,
+                           const float* render_max) {
+    return guarded(ctx, [&] {
+        Avatar& a = ctx->avatar(avatar);
+        if (train_min) std::memcpy(a.train_min, train_min, 12);
+        if (train_max) std::memcpy(a.train_max, train_max, 12);
+        if (render_min) std::memcpy(a.render_min, render_min, 12);
+        if (render_max) std::memcpy(a.render_max, render_max, 12);
+        for (int k = 0; k < 3; ++k)
+            if (!(a.train_max[k] > a.train_min[k])) fail(INSTA_ERR_INVALID_ARG, "empty train box");
+    });
+}
+
+int insta_avatar_set_flags(insta_ctx* ctx, int avatar, uint32_t flags) {
+    return guarded(ctx, [&] { ctx->avatar(avatar).flags = flags; });
+}
+
+int insta_frame_upload(insta_ctx* ctx, int avatar, int frame, const float* verts) {
+    return guarded(ctx, [&] {
+        Avatar& a = ctx->avatar(avatar);
+        if (!verts || frame < 0) fail(INSTA_ERR_INVALID_ARG, "bad frame upload");
+        Frame& f = a.frames[frame];
+        int n_leaves, n_internal;
+        tree_shape(a.F, f.view, n_leaves, n_internal);
+        f.n_leaves = n_leaves;
+        ctx->alloc(f.verts, (size_t)a.V * 12);
+        ctx->alloc(f.frames, (size_t)a.F * sizeof(TriFrame));
+        ctx->alloc(f.leaf_tris, (size_t)n_leaves * 4 * 48);
+        ctx->alloc(f.nodes, (size_t)n_internal * 96);
+        host_copy(f.verts.p, verts, (size_t)a.V * 12, ctx->stream);
+        f.view.leaf_tris = static_cast<const float4*>(f.leaf_tris.p);
+        f.view.nodes = static_cast<const float4*>(f.nodes.p);
+        f.view.frames = static_cast<const TriFrame*>(f.frames.p);
+        f.view.n_tris = a.F;
+        CK(launch_tri_frames(a.F, (const float*)f.verts.p, (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
+                             (const float*)a.canon_area.p, nullptr, (TriFrame*)f.frames.p, 1, ctx->stream));
+        CK(launch_bvh_build(f.view, n_leaves, (const float*)f.verts.p, (const int32_t*)a.faces.p, ctx->stream));
+        f.has_occupancy = false;
+        a.table_dirty = true;
+    });
+}
+
+int insta_frame_release(insta_ctx* ctx, int avatar, int frame) {
+    return guarded(ctx, [&] {
+        Avatar& a = ctx->avatar(avatar);
+        auto it = a.frames.find(frame);
+        if (it == a.frames.end()) return;
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (DevBuf* b : {&it->second.verts, &it->second.frames, &it->second.leaf_tris, &it->second.nodes, &it->second.bitfield})
+            ctx->release(*b);
+        a.frames.erase(it);
+        a.table_dirty = true;
+    });
+}
+
+int insta_occupancy_from_mesh(insta_ctx* ctx, int avatar, int frame, double radius) {
+    return guarded(ctx, [&] {
+        if (!(radius > 0.0)) fail(INSTA_ERR_INVALID_ARG, "radius must be positive");
+        Avatar& a = ctx->avatar(avatar);
+        Frame& f = get_frame(a, frame);
+        ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
+        CK(launch_occupancy(f.view, radius, (uint8_t*)f.bitfield.p, ctx->err_dev, ctx->stream));
+        f.has_occupancy = true;
+    });
+}
+
+int insta_occupancy_set(insta_ctx* ctx, int avatar, int frame, const uint8_t* bits) {
+    return guarded(ctx, [&] {
+        if (!bits) fail(INSTA_ERR_INVALID_ARG, "null bitfield");
+        Frame& f = get_frame(ctx->avatar(avatar), frame);
+        ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
+        host_copy(f.bitfield.p, bits, (size_t)8 * GRID3 / 8, ctx->stream);
+        f.has_occupancy = true;
+    });
+}
+
+int insta_occupancy_get(insta_ctx* ctx, int avatar, int frame, uint8_t* bits) {
+    return guarded(ctx, [&] {
+        if (!bits) fail(INSTA_ERR_INVALID_ARG, "null bitfield");
+        Frame& f = get_frame(ctx->avatar(avatar), frame);
+        if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy", frame);
+        host_copy(bits, f.bitfield.p, (size_t)8 * GRID3 / 8, ctx->stream);
+        ctx->check_device();
+    });
+}
+
+int insta_canonical_map(insta_ctx* ctx, int avatar, int frame, float* coords, uint32_t stride, uint32_t n_extra, int64_t n) {
+    return guarded(ctx, [&] {
+        if (n < 0 || (n > 0 && !coords)) fail(INSTA_ERR_INVALID_ARG, "bad coordinate buffer");
+        if (stride < 11 + n_extra) fail(INSTA_ERR_INVALID_ARG, "stride %u < 11 + n_extra", stride);
+        Avatar& a = ctx->avatar(avatar);
+        if (n == 0) return;
+        if (a.table_dirty) {
+            int max_id = a.frames.empty() ? -1 : a.frames.rbegin()->first;
+            std::vector<FrameView> table((size_t)std::max(1, max_id + 1));
+            for (auto& fv : table) { std::memset(&fv, 0, sizeof(fv)); }
+            for (auto& kv : a.frames) table[kv.first] = kv.second.view;
+            ctx->alloc(a.frame_table, table.size() * sizeof(FrameView));
+            CK(cudaMemcpyAsync(a.frame_table.p, table.data(), table.size() * sizeof(FrameView), cudaMemcpyHostToDevice, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            a.table_frames = (uint32_t)(max_id + 1);
+            a.table_dirty = false;
+        }
+        if (frame >= 0) get_frame(a, frame);
+        for (auto& kv : a.frames) (void)kv;
+        CK(launch_canonical_map_coords((const FrameView*)a.frame_table.p, a.table_frames, deform_view(a), coords, stride, n_extra, n,
+                                       frame, ctx->err_dev, ctx->stream));
+    });
+}
+
+int insta_canonical_map_soa(insta_ctx* ctx, int avatar, int frame, const float* pts, int64_t n, int32_t* out_idx, float* out_canon) {
+    return guarded(ctx, [&] {
+        if (n < 0 || (n > 0 && (!pts || !out_idx || !out_canon))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
+        Avatar& a = ctx->avatar(avatar);
+        Frame& f = get_frame(a, frame);
+        CK(launch_canonical_map_soa(f.view, deform_view(a), pts, n, out_idx, out_canon, ctx->err_dev, ctx->stream));
+    });
+}
+
+int insta_field_param_count(const insta_field_desc* desc, uint64_t* n_params) {
+    if (!desc || !n_params) return INSTA_ERR_INVALID_ARG;
+    try {
+        *n_params = field_layout(*desc).total;
+        return INSTA_OK;
+    } catch (const Failure& e) {
+        return e.code;
+    }
+}
+
+int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, const uint16_t* params, uint64_t n_params) {
+    return guarded(ctx, [&] {
+        if (!desc || !params) fail(INSTA_ERR_INVALID_ARG, "null field description or parameters");
+        Avatar& a = ctx->avatar(avatar, true);
+        FieldLayout L = field_layout(*desc);
+        if (n_params != L.total) fail(INSTA_ERR_INVALID_ARG, "expected %llu parameters, got %llu", (unsigned long long)L.total,
+                                      (unsigned long long)n_params);
+        Field& fd = a.field;
+        fd.desc = *desc;
+        fd.n_params = n_params;
+        ctx->alloc(fd.params, n_params * 2);
+        host_copy(fd.params.p, params, n_params * 2, ctx->stream);
+        // MLP weight image in the tensor-core operand layout (umma.cuh), one tile per layer
+        std::vector<uint16_t> mlp(L.table_off);
+        CK(cudaMemcpyAsync(mlp.data(), params, L.table_off * 2, cudaMemcpyDefault, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        MlpPlan plan{};
+        plan.n_density = (uint32_t)L.n_density;
+        plan.n_rgb = (uint32_t)L.n_rgb;
+        uint32_t off = 0;
+        std::vector<uint8_t> image;
+        for (int l = 0; l < L.n_density + L.n_rgb; ++l) {
+            uint32_t N = L.layer_n[l], Kin = L.layer_k[l], K = (Kin + 15) / 16 * 16;
+            plan.layer[l] = {off, N, K};
+            image.resize(off + (size_t)N * K * 2, 0);
+            for (uint32_t n = 0; n < N; ++n)
+                for (uint32_t k = 0; k < Kin; ++k) {
+                    uint16_t w = mlp[L.layer_off[l] + (uint64_t)n * Kin + k];
+                    if (desc->precision == INSTA_PRECISION_BF16) w = half_to_bf16_bits(w);
+                    std::memcpy(&image[off + tile_offset(n, k, K)], &w, 2);
+                }
+            off += N * K * 2;
+            off = (off + 127) / 128 * 128;
+        }
+        plan.bytes = off;
+        plan.k_in = (L.layer_k[0] + 15) / 16 * 16;
+        if (plan.bytes > 64 * 1024) fail(INSTA_ERR_UNSUPPORTED, "MLP weights exceed 64 KiB of shared memory");
+        ctx->alloc(fd.image, image.size());
+        CK(cudaMemcpyAsync(fd.image.p, image.data(), image.size(), cudaMemcpyHostToDevice, ctx->stream));
+        fd.plan = plan;
+        FieldView& v = fd.view;
+        std::memset(&v, 0, sizeof(v));
+        v.table = static_cast<const uint16_t*>(fd.params.p) + L.table_off;
+        v.mlp_smem = static_cast<const uint8_t*>(fd.image.p);
+        v.mlp_smem_bytes = plan.bytes;
+        v.n_levels = desc->n_levels;
+        v.n_features = 2;
+        v.n_extra = desc->n_extra_dims;
+        for (uint32_t l = 0; l < desc->n_levels; ++l) {
+            v.level_scale[l] = L.lvl_scale[l];
+            v.level_res[l] = L.lvl_res[l];
+            v.level_size[l] = L.lvl_size[l];
+            v.level_off[l] = (uint32_t)L.lvl_off[l];
+            v.level_dense[l] = (uint64_t)L.lvl_res[l] * L.lvl_res[l] * L.lvl_res[l] <= L.lvl_size[l] ? 1 : 0;
+        }
+        v.precision = (int)desc->precision;
+        CK(cudaStreamSynchronize(ctx->stream));
+        fd.ready = true;
+        ctx->render_ctas = 0;
+    });
+}
+
+int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4) {
+    return guarded(ctx, [&] {
+        Avatar& a = ctx->avatar(avatar);
+        if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", avatar);
+        if (n < 0 || (n > 0 && (!coords || !out4))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
+        if (stride < 11 + a.field.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
+        CK(launch_field_eval(a.field.view, a.field.plan, coords, stride, n, out4, ctx->err_dev, ctx->stream));
+    });
+}
+
+int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, float* out_depth) {
+    return guarded(ctx, [&] {
+        check_request(req);
+        if (!out_rgba || !out_depth) fail(INSTA_ERR_INVALID_ARG, "null output buffers");
+        Avatar& a = ctx->avatar(req->avatar);
+        if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", req->avatar);
+        Frame& f = get_frame(a, req->frame);
+        if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", req->frame);
+        const size_t npix = (size_t)req->width * req->height;
+        bool dev_out = is_device_ptr(out_rgba) && is_device_ptr(out_depth);
+        float* rgba = out_rgba;
+        float* depth = out_depth;
+        if (!dev_out) {
+            rgba = (float*)ctx->alloc(ctx->out_rgba, npix * 16);
+            depth = (float*)ctx->alloc(ctx->out_depth, npix * 4);
+        }
+        const float* extra = nullptr;
+        if (a.field.desc.n_extra_dims) {
+            ctx->alloc(ctx->extra, 64 * 4);
+            std::vector<float> e(a.field.desc.n_extra_dims, 0.f);
+            if (req->extra_dims) std::memcpy(e.data(), req->extra_dims, e.size() * 4);
+            CK(cudaMemcpyAsync(ctx->extra.p, e.data(), e.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+            extra = (const float*)ctx->extra.p;
+        }
+        if (!ctx->render_ctas) ctx->render_ctas = render_ctas_per_sm(a.field.plan);
+        RenderLaunch L{};
+        L.rv = render_view(a, *req);
+        L.fr = f.view;
+        L.dv = deform_view(a);
+        L.fv = a.field.view;
+        L.plan = &a.field.plan;
+        L.bitfield = (const uint8_t*)f.bitfield.p;
+        L.extra_dims = extra;
+        L.out_rgba = rgba;
+        L.out_depth = depth;
+        L.ray_counter = ctx->ray_counter;
+        L.sample_counter = ctx->sample_counter;
+        L.err = ctx->err_dev;
+        L.grid = ctx->sms * ctx->render_ctas;
+        CK(cudaMemsetAsync(ctx->sample_counter, 0, sizeof(unsigned long long), ctx->stream));
+        CK(launch_render(L, ctx->stream));
+        if (!dev_out) {
+            CK(cudaMemcpyAsync(out_rgba, rgba, npix * 16, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(out_depth, depth, npix * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            ctx->check_device();
+        }
+    });
+}
+
+int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples) {
+    return guarded(ctx, [&] {
+        if (!n_samples) fail(INSTA_ERR_INVALID_ARG, "null output");
+        ctx->check_device();
+        unsigned long long v = 0;
+        CK(cudaMemcpy(&v, ctx->sample_counter, sizeof(v), cudaMemcpyDeviceToHost));
+        *n_samples = v;
+    });
+}
+
+int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out, float* out_t, float* out_dt, int32_t* out_n) {
+    return guarded(ctx, [&] {
+        check_request(req);
+        if (max_out <= 0 || !out_t || !out_dt || !out_n) fail(INSTA_ERR_INVALID_ARG, "bad output buffers");
+        Avatar& a = ctx->avatar(req->avatar);
+        Frame& f = get_frame(a, req->frame);
+        if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", req->frame);
+        CK(launch_march_debug(render_view(a, *req), (const uint8_t*)f.bitfield.p, max_out, out_t, out_dt, out_n, ctx->stream));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,289 @@
+// umma.cuh -- 5th-generation tensor-core (tcgen05) building blocks for the avatar MLPs.
+//
+// One CTA of 128 threads evaluates a 128-sample tile: thread t owns sample t, writes
+// its activation row t into a shared-memory A tile, one elected thread issues
+// tcgen05.mma (M = 128, accumulator in TMEM), and after the commit-mbarrier fires each
+// warp reads its 32 TMEM lanes back with tcgen05.ld -- lane t of the accumulator is row
+// t, i.e. the same thread's sample, so activations never cross threads.
+//
+// Operand tiles use the no-swizzle K-major canonical layout: 8-row x 16-byte core
+// matrices; core matrices adjacent along K are LBO = 128 B apart and 8-row groups are
+// SBO = (K / 8) * 128 B apart.  Element (r, k) of an R x K FP16 tile lives at byte
+//   ((r / 8) * (K / 8) + k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2.
+// Weights (B operands, [N][K] row-major = K-major) are pre-arranged in exactly this
+// layout on the host and bulk-copied into shared memory once per CTA.
+#pragma once
+
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+#include "insta_types.h"
+
+namespace insta {
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__host__ __device__ constexpr uint32_t tile_offset(uint32_t r, uint32_t k, uint32_t K) {
+    return ((r / 8) * (K / 8) + k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2;
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;          // descriptor version for tcgen05
+    return d;                        // base offset 0, relative LBO, no swizzle
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulate, A/B FP16 (or BF16), both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(uint32_t M, uint32_t N, bool bf16) {
+    return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for the mbarrier phase with the given parity: gives up after ~1 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t a = smem_addr(bar);
+    uint64_t t0 = 0;
+    for (uint32_t it = 0;; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        if (done) return true;
+        if ((it & 255u) == 0u) {
+            uint64_t now = global_ns();
+            if (t0 == 0) t0 = now;
+            else if (now - t0 > 1000000000ull) return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(slot)), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Bulk (TMA 1D) copy global -> shared, completion tracked by an mbarrier transaction count.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+
+// Layer table of the MLP weight image: byte offset, N (outputs, padded to 16) and K (inputs).
+struct MlpLayer { uint32_t off, N, K; };
+struct MlpPlan {
+    MlpLayer layer[8];
+    uint32_t n_density;   // density layers (hidden + output)
+    uint32_t n_rgb;       // rgb layers
+    uint32_t bytes;
+    uint32_t k_in;        // density input width (padded to 16)
+};
+
+// Store one FP16 row (K values, K multiple of 8) into an A tile.
+__device__ __forceinline__ void store_row(uint8_t* tile, uint32_t r, uint32_t K, const __half* v) {
+    for (uint32_t c = 0; c < K / 8; ++c) {
+        uint4 q;
+        q.x = *reinterpret_cast<const uint32_t*>(&v[c * 8 + 0]);
+        q.y = *reinterpret_cast<const uint32_t*>(&v[c * 8 + 2]);
+        q.z = *reinterpret_cast<const uint32_t*>(&v[c * 8 + 4]);
+        q.w = *reinterpret_cast<const uint32_t*>(&v[c * 8 + 6]);
+        *reinterpret_cast<uint4*>(tile + tile_offset(r, c * 8, K)) = q;
+    }
+}
+
+// Shared-memory working set of one 128-sample MLP tile.
+struct MlpSmem {
+    alignas(1024) uint8_t a_in[128 * 48 * 2];    // density input (hash features + expression dims)
+    alignas(1024) uint8_t a_h[128 * 64 * 2];     // hidden activations
+    alignas(1024) uint8_t a_rgb[128 * 32 * 2];   // density output (16) + SH (16)
+    alignas(8) uint64_t bar_mma;
+    alignas(8) uint64_t bar_load;
+    uint32_t tmem_base;
+    uint32_t mma_phase;
+    uint32_t failed;
+};
+
+// Issue one layer: all threads call, thread 0 issues the MMAs into TMEM columns [col, col+N).
+// Returns false on a timed-out wait.  Afterwards each thread reads its own lane.
+__device__ __forceinline__ bool mlp_issue(MlpSmem& sm, const uint8_t* a_tile, const uint8_t* w_smem, const MlpLayer& L,
+                                          uint32_t col, bool bf16, uint32_t& phase) {
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tc_fence_after();
+        const uint32_t idesc = idesc_f16(128, L.N, bf16);
+        const uint32_t a0 = smem_addr(a_tile), b0 = smem_addr(w_smem + L.off);
+        const uint32_t sbo = (L.K / 8) * 128;
+        for (uint32_t ks = 0; ks < L.K / 16; ++ks) {
+            uint64_t ad = smem_desc(a0 + ks * 256, 128, sbo);
+            uint64_t bd = smem_desc(b0 + ks * 256, 128, sbo);
+            umma_f16(sm.tmem_base + col, ad, bd, idesc, ks > 0 ? 1u : 0u);
+        }
+        umma_commit(&sm.bar_mma);
+    }
+    bool ok = mbar_wait(&sm.bar_mma, phase);
+    phase ^= 1u;
+    tc_fence_after();
+    return ok;
+}
+
+__device__ __forceinline__ uint32_t lane_addr(const MlpSmem& sm, uint32_t col) {
+    return sm.tmem_base + ((((uint32_t)threadIdx.x / 32u) % 4u) * 32u << 16) + col;
+}
+
+__device__ __forceinline__ __half to_act(float v, bool bf16) {
+    if (bf16) {
+        __nv_bfloat16 b = __float2bfloat16_rn(v);
+        return __ushort_as_half(__bfloat16_as_ushort(b));
+    }
+    return __float2half_rn(v);
+}
+__device__ __forceinline__ float from_act(__half h, bool bf16) {
+    if (bf16) return __bfloat162float(__ushort_as_bfloat16(__half_as_ushort(h)));
+    return __half2float(h);
+}
+
+// Hidden layer epilogue: ReLU + rounding to the activation type, streamed 16 columns at a
+// time from TMEM into this thread's row of the next A tile.
+__device__ __forceinline__ void hidden_epilogue(MlpSmem& sm, uint32_t col, uint32_t N, bool bf16) {
+    const uint32_t r = threadIdx.x;
+    for (uint32_t c = 0; c < N; c += 16) {
+        float v[16];
+        tmem_ld16(lane_addr(sm, col + c), v);
+        __half h[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) h[i] = to_act(fmaxf(v[i], 0.f), bf16);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            uint4 u;
+            u.x = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 0]);
+            u.y = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 2]);
+            u.z = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 4]);
+            u.w = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 6]);
+            *reinterpret_cast<uint4*>(sm.a_h + tile_offset(r, c + q * 8, N)) = u;
+        }
+    }
+}
+
+// Evaluate the density + colour MLPs for this thread's sample.  `feat` holds k_in
+// activations (hash features then expression dims), `sh` the 16 SH values.  Outputs
+// rgb raw (3) and density raw, each rounded to the activation type as stored.
+__device__ __forceinline__ bool mlp_eval(MlpSmem& sm, const uint8_t* w, const MlpPlan& plan, bool bf16,
+                                         const __half* feat, const __half* sh, float* rgb_raw, float& dens_raw) {
+    const uint32_t r = threadIdx.x;
+    bool ok = true;
+    store_row(sm.a_in, r, plan.k_in, feat);
+    const uint8_t* a = sm.a_in;
+    uint32_t phase = sm.mma_phase;
+    for (uint32_t l = 0; l < plan.n_density; ++l) {
+        const MlpLayer& L = plan.layer[l];
+        if (l + 1 < plan.n_density) {
+            ok &= mlp_issue(sm, a, w, L, 0, bf16, phase);
+            hidden_epilogue(sm, 0, L.N, bf16);
+            a = sm.a_h;
+        } else {
+            ok &= mlp_issue(sm, a, w, L, 64, bf16, phase);
+            float v[16];
+            tmem_ld16(lane_addr(sm, 64), v);
+            __half h[32];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) h[i] = to_act(v[i], bf16);
+            dens_raw = from_act(h[0], bf16);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) h[16 + i] = sh[i];
+            store_row(sm.a_rgb, r, 32, h);
+            a = sm.a_rgb;
+        }
+    }
+    for (uint32_t l = 0; l < plan.n_rgb; ++l) {
+        const MlpLayer& L = plan.layer[plan.n_density + l];
+        if (l + 1 < plan.n_rgb) {
+            ok &= mlp_issue(sm, a, w, L, 0, bf16, phase);
+            hidden_epilogue(sm, 0, L.N, bf16);
+            a = sm.a_h;
+        } else {
+            ok &= mlp_issue(sm, a, w, L, 64, bf16, phase);
+            float v[16];
+            tmem_ld16(lane_addr(sm, 64), v);
+            rgb_raw[0] = from_act(to_act(v[0], bf16), bf16);
+            rgb_raw[1] = from_act(to_act(v[1], bf16), bf16);
+            rgb_raw[2] = from_act(to_act(v[2], bf16), bf16);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) sm.mma_phase = phase;
+    __syncthreads();
+    return ok;
+}
+
+// CTA prologue: mbarriers, TMEM (128 columns), weight image bulk-copied into `w`.
+__device__ __forceinline__ bool mlp_setup(MlpSmem& sm, uint8_t* w, const uint8_t* w_global, uint32_t bytes) {
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.bar_mma, 1);
+        mbar_init(&sm.bar_load, 1);
+        sm.mma_phase = 0;
+        sm.failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) tmem_alloc(&sm.tmem_base, 128);
+    if (threadIdx.x == 0) bulk_load(w, w_global, bytes, &sm.bar_load);
+    bool ok = mbar_wait(&sm.bar_load, 0);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    return ok;
+}
+
+__device__ __forceinline__ void mlp_teardown(MlpSmem& sm) {
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x < 32) tmem_dealloc(sm.tmem_base, 128);
+}
+
+}  // namespace insta

@@ -1,0 +1,796 @@
+/*
+ * insta_oracle.c -- CPU restatement of INSTA's deformation + render hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, the smoke check and bench.py's
+ * CPU-baseline leg load this library, and only as the checker (or as the
+ * timed CPU baseline).  The CUDA product never links or calls it.
+ *
+ * Parity pin: the geometry primitives (distance_sq, box distance, tbn,
+ * tri2projection, the BVH traversal, the Sobol/scrambling helpers) are pinned
+ * against the reference's own headers compiled for the host (oracle/build_ref.py
+ * builds oracle/_ref/libinsta_ref.so) and against the golden vectors that
+ * script writes under tests/golden/.  The hash-grid encode, SH and MLPs have
+ * no reference source in the repository (tiny-cuda-nn is an empty
+ * submodule), so their restatement is the published method, unpinned.
+ *
+ * Build: gcc -O3 -fopenmp -ffp-contract=off -fPIC -shared (see oracle/build.py).
+ */
+#include "insta_oracle.h"
+
+#include <math.h>
+#include <float.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ---------------------------------------------------------------- halves */
+uint16_t orc_f2h(float x) { _Float16 h = (_Float16)x; uint16_t b; memcpy(&b, &h, 2); return b; }
+float orc_h2f(uint16_t b) { _Float16 h; memcpy(&h, &b, 2); return (float)h; }
+static uint16_t orc_f2bf16(float x) {
+    uint32_t u; memcpy(&u, &x, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40u);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+static float orc_bf16_to_f(uint16_t b) { uint32_t u = (uint32_t)b << 16; float f; memcpy(&f, &u, 4); return f; }
+
+/* ---------------------------------------------------------- field layout */
+/* Per-level grid scale of the multiresolution hash encoding:
+ * scale_l = b^l * N_min - 1 computed as exp2(l * log2 b) * N_min - 1 in float. */
+static float orc_level_scale(const orc_field_cfg *c, uint32_t l) {
+    return exp2f((float)l * log2f(c->per_level_scale)) * (float)c->base_res - 1.0f;
+}
+static uint32_t orc_grid_index(const uint32_t *cc, uint32_t res, uint32_t size) {
+    uint64_t r3 = (uint64_t)res * res * res;
+    uint32_t idx;
+    if (r3 <= size) idx = cc[0] + cc[1] * res + cc[2] * res * res;
+    else idx = (cc[0] * 1u) ^ (cc[1] * 2654435761u) ^ (cc[2] * 805459861u);
+    return idx % size;
+}
+
+uint64_t orc_field_layout(const orc_field_cfg *c, uint64_t *lvl_off, uint32_t *lvl_res, uint32_t *lvl_size,
+                          uint64_t *mlp_off) {
+    uint64_t n_in = (uint64_t)c->n_levels * c->n_features + c->n_extra;
+    uint64_t dens = c->density_hidden * n_in + (uint64_t)(c->density_layers - 1) * c->density_hidden * c->density_hidden
+                    + (uint64_t)c->density_out * c->density_hidden;
+    uint64_t rgb_in = c->density_out + 16;
+    uint64_t rgb = c->rgb_hidden * rgb_in + (uint64_t)(c->rgb_layers - 1) * c->rgb_hidden * c->rgb_hidden
+                   + (uint64_t)c->rgb_out_padded * c->rgb_hidden;
+    mlp_off[0] = 0;
+    mlp_off[1] = dens;
+    mlp_off[2] = dens + rgb;
+    uint64_t T = 1ull << c->log2_table, off = 0;
+    for (uint32_t l = 0; l < c->n_levels; ++l) {
+        float s = orc_level_scale(c, l);
+        uint32_t res = (uint32_t)ceilf(s) + 1u;
+        uint64_t r3 = (uint64_t)res * res * res;
+        uint64_t sz = (r3 + 7) / 8 * 8;
+        if (sz > T) sz = T;
+        lvl_off[l] = off; lvl_res[l] = res; lvl_size[l] = (uint32_t)sz;
+        off += sz;
+    }
+    return mlp_off[2] + off * c->n_features;
+}
+
+/* ------------------------------------------------- FP32 / FP64 instances */
+static void tri2projection_raw_d(const orc_tri *t, double *M);
+static int inverse4_d(const double *m, double *o);
+#define R float
+#define SFX(n) n##_f
+#define R_SQRT sqrtf
+#define R_EXP expf
+#define R_FLOOR floorf
+#define R_FABS fabsf
+#define R_IS_FLOAT 1
+#include "oracle_real.inc"
+#undef R
+#undef SFX
+#undef R_SQRT
+#undef R_EXP
+#undef R_FLOOR
+#undef R_FABS
+#undef R_IS_FLOAT
+#define R double
+#define SFX(n) n##_d
+#define R_SQRT sqrt
+#define R_EXP exp
+#define R_FLOOR floor
+#define R_FABS fabs
+#define R_IS_FLOAT 0
+#include "oracle_real.inc"
+#undef R
+#undef SFX
+
+/* ------------------------------------------------------------- geometry */
+static inline float v3dot(const float *a, const float *b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
+static inline void v3cross(const float *a, const float *b, float *o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+/* sign (NGP/common.h:191): copysignf(1, x). */
+static inline float ngp_sign(float x) { return copysignf(1.0f, x); }
+/* tcnn::clamp: val < lo ? lo : (hi < val ? hi : val). */
+static inline float clampf_(float v, float lo, float hi) { return v < lo ? lo : (hi < v ? hi : v); }
+
+/* Triangle::distance_sq (NGP/triangle.cuh:88-107). */
+float orc_tri_distance_sq(const orc_tri *t, const float *pos) {
+    float v21[3], p1[3], v32[3], p2[3], v13[3], p3[3], nor[3], tmp[3];
+    for (int k = 0; k < 3; ++k) {
+        v21[k] = t->b[k] - t->a[k]; p1[k] = pos[k] - t->a[k];
+        v32[k] = t->c[k] - t->b[k]; p2[k] = pos[k] - t->b[k];
+        v13[k] = t->a[k] - t->c[k]; p3[k] = pos[k] - t->c[k];
+    }
+    v3cross(v21, v13, nor);
+    float s = 0.0f;
+    v3cross(v21, nor, tmp); float s1 = ngp_sign(v3dot(tmp, p1));
+    v3cross(v32, nor, tmp); float s2 = ngp_sign(v3dot(tmp, p2));
+    v3cross(v13, nor, tmp); float s3 = ngp_sign(v3dot(tmp, p3));
+    s = s1 + s2 + s3;
+    if (s < 2.0f) {
+        float e[3][3], d[3];
+        const float *vv[3] = {v21, v32, v13}, *pp[3] = {p1, p2, p3};
+        for (int i = 0; i < 3; ++i) {
+            float f = clampf_(v3dot(vv[i], pp[i]) / v3dot(vv[i], vv[i]), 0.0f, 1.0f);
+            for (int k = 0; k < 3; ++k) e[i][k] = vv[i][k] * f - pp[i][k];
+            d[i] = v3dot(e[i], e[i]);
+        }
+        /* std::min({d0, d1, d2}): first smallest */
+        float m = d[0];
+        if (d[1] < m) m = d[1];
+        if (d[2] < m) m = d[2];
+        return m;
+    }
+    float nd = v3dot(nor, p1);
+    return nd * nd / v3dot(nor, nor);
+}
+
+/* BoundingBox::distance_sq (NGP/bounding_box.cuh:228-230). */
+float orc_box_distance_sq(const float *mn, const float *mx, const float *p) {
+    float d[3];
+    for (int k = 0; k < 3; ++k) {
+        float a = mn[k] - p[k], b = p[k] - mx[k];
+        float m = a < b ? b : a;   /* cwiseMax */
+        d[k] = m < 0.0f ? 0.0f : m;
+    }
+    return v3dot(d, d);
+}
+
+static inline int box_contains(const float *mn, const float *mx, const float *p) {
+    return p[0] >= mn[0] && p[0] <= mx[0] && p[1] >= mn[1] && p[1] <= mx[1] && p[2] >= mn[2] && p[2] <= mx[2];
+}
+
+/* ------------------------------------------------------------------ mesh */
+static int cmp_int(const void *a, const void *b) { int x = *(const int *)a, y = *(const int *)b; return (x > y) - (x < y); }
+
+/* TinyMesh::get_triangle_3_neighbours (src/tiny_mesh.cu:316-371): for each face, the sorted set
+ * of faces sharing one of its edges, minus itself, padded with -1 to 3 entries.  (The reference
+ * writes past slot 2 for non-manifold edges; here extra entries are dropped.)  Returns 0. */
+int orc_adjacency(const int32_t *faces, int n_faces, int n_verts, int32_t *out_adj) {
+    int *cnt = calloc((size_t)n_verts + 1, sizeof(int));
+    for (int f = 0; f < n_faces; ++f) for (int k = 0; k < 3; ++k) cnt[faces[f * 3 + k] + 1]++;
+    for (int v = 0; v < n_verts; ++v) cnt[v + 1] += cnt[v];
+    int *vf = malloc(sizeof(int) * (size_t)n_faces * 3);
+    int *fill = calloc((size_t)n_verts, sizeof(int));
+    for (int f = 0; f < n_faces; ++f)
+        for (int k = 0; k < 3; ++k) { int v = faces[f * 3 + k]; vf[cnt[v] + fill[v]++] = f; }
+    for (int f = 0; f < n_faces; ++f) {
+        int ids[256], n = 0;
+        int e[3][2] = {{faces[f * 3], faces[f * 3 + 1]}, {faces[f * 3], faces[f * 3 + 2]}, {faces[f * 3 + 1], faces[f * 3 + 2]}};
+        for (int ei = 0; ei < 3; ++ei) {
+            int va = e[ei][0], vb = e[ei][1];
+            for (int i = cnt[va]; i < cnt[va + 1]; ++i)
+                for (int j = cnt[vb]; j < cnt[vb + 1]; ++j)
+                    if (vf[i] == vf[j] && n < 256) ids[n++] = vf[i];
+        }
+        qsort(ids, (size_t)n, sizeof(int), cmp_int);
+        int k = 0, prev = -2;
+        for (int i = 0; i < 3; ++i) out_adj[f * 3 + i] = -1;
+        for (int i = 0; i < n; ++i) {
+            if (ids[i] == prev) continue;
+            prev = ids[i];
+            if (ids[i] != f && k < 3) out_adj[f * 3 + k++] = ids[i];
+        }
+    }
+    free(cnt); free(vf); free(fill);
+    return 0;
+}
+
+static float tri_area(const float *a, const float *b, const float *c) {
+    float e1[3], e2[3], n[3];
+    for (int k = 0; k < 3; ++k) { e1[k] = b[k] - a[k]; e2[k] = c[k] - a[k]; }
+    v3cross(e1, e2, n);
+    return 0.5f * sqrtf(v3dot(n, n));
+}
+
+/* TinyMesh::build_triangles (src/tiny_mesh.cu:134-164): id = face index, mask from the region map,
+ * scaling = area(deformed) / area(canonical) (1 when canon_verts == NULL). */
+void orc_build_triangles(const float *verts, const float *canon_verts, const int32_t *faces, const uint32_t *mask,
+                         int n_faces, orc_tri *out) {
+    for (int f = 0; f < n_faces; ++f) {
+        orc_tri *t = &out[f];
+        const int32_t *fc = &faces[f * 3];
+        memcpy(t->a, &verts[fc[0] * 3], 12); memcpy(t->b, &verts[fc[1] * 3], 12); memcpy(t->c, &verts[fc[2] * 3], 12);
+        t->id = (uint32_t)f;
+        t->mask_id = mask ? mask[f] : 15u;
+        float s = 1.0f;
+        if (canon_verts) {
+            float ca = tri_area(&canon_verts[fc[0] * 3], &canon_verts[fc[1] * 3], &canon_verts[fc[2] * 3]);
+            s *= tri_area(t->a, t->b, t->c) / ca;
+        }
+        t->scaling = s;
+    }
+}
+
+/* ------------------------------------------------------- nearest triangle */
+void orc_nearest_brute(const orc_tri *tris, int n_tris, const float *pts, int64_t n_pts, int32_t *out_id, float *out_d2) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < n_pts; ++i) {
+        float best = FLT_MAX; int32_t bid = -1;
+        for (int t = 0; t < n_tris; ++t) {
+            float d = orc_tri_distance_sq(&tris[t], &pts[i * 3]);
+            if (d < best || (d == best && (int32_t)tris[t].id < bid)) { best = d; bid = (int32_t)tris[t].id; }
+        }
+        out_id[i] = bid;
+        if (out_d2) out_d2[i] = best;
+    }
+}
+
+/* TriangleBvhWithBranchingFactor<4>::build (ngp/src/triangle_bvh.cu:548-631): top-down, each node
+ * splits its range twice (4 children) at the median of the max-variance centroid axis with
+ * nth_element; leaves hold <= leaf_size triangles encoded as negative ranges.  Triangles are
+ * reordered.  Returns the node count, or -1 when max_nodes is too small.  The median partition
+ * here is a deterministic introselect (std::nth_element's element order is not reproduced; only
+ * the multiset split at the median is). */
+static float centroid_axis(const orc_tri *t, int axis) { return (t->a[axis] + t->b[axis] + t->c[axis]) / 3.0f; }
+
+static void nth_split(orc_tri *v, int lo, int hi, int nth, int axis) {
+    /* quickselect on [lo, hi) so that v[nth] is the nth order statistic */
+    while (hi - lo > 1) {
+        int mid = lo + (hi - lo) / 2;
+        float pv = centroid_axis(&v[mid], axis);
+        int i = lo, j = hi - 1;
+        while (i <= j) {
+            while (centroid_axis(&v[i], axis) < pv) ++i;
+            while (pv < centroid_axis(&v[j], axis)) --j;
+            if (i <= j) { orc_tri tmp = v[i]; v[i] = v[j]; v[j] = tmp; ++i; --j; }
+        }
+        if (nth <= j) hi = j + 1;
+        else if (nth >= i) lo = i;
+        else return;
+    }
+}
+
+static void bbox_of(const orc_tri *v, int lo, int hi, float *mn, float *mx) {
+    for (int k = 0; k < 3; ++k) { mn[k] = v[lo].a[k]; mx[k] = v[lo].a[k]; }
+    for (int i = lo; i < hi; ++i) {
+        const float *pts[3] = {v[i].a, v[i].b, v[i].c};
+        for (int p = 0; p < 3; ++p)
+            for (int k = 0; k < 3; ++k) { if (pts[p][k] < mn[k]) mn[k] = pts[p][k]; if (pts[p][k] > mx[k]) mx[k] = pts[p][k]; }
+    }
+}
+
+int orc_bvh4_build(const orc_tri *tris, int n_tris, int leaf_size, orc_bvh_node *nodes, int max_nodes, orc_tri *v) {
+    memcpy(v, tris, sizeof(orc_tri) * (size_t)n_tris);
+    int n_nodes = 1;
+    bbox_of(v, 0, n_tris, nodes[0].bb_min, nodes[0].bb_max);
+    if (n_tris <= leaf_size) { nodes[0].left_idx = -1; nodes[0].right_idx = -n_tris - 1; return 1; }
+    int *stack = malloc(sizeof(int) * 3 * (size_t)(n_tris + 8));
+    int sp = 0;
+    stack[sp++] = 0; stack[sp++] = 0; stack[sp++] = n_tris;
+    while (sp > 0) {
+        int end = stack[--sp], begin = stack[--sp], node = stack[--sp];
+        int cb[4], ce[4];
+        cb[0] = begin; ce[0] = end;
+        int n_children = 1;
+        while (n_children < 4) {
+            for (int i = n_children - 1; i >= 0; --i) {
+                int b = cb[i], e = ce[i];
+                double mean[3] = {0, 0, 0}, var[3] = {0, 0, 0};
+                float meanf[3] = {0, 0, 0}, varf[3] = {0, 0, 0};
+                for (int t = b; t < e; ++t) for (int k = 0; k < 3; ++k) meanf[k] += centroid_axis(&v[t], k);
+                for (int k = 0; k < 3; ++k) meanf[k] /= (float)(e - b);
+                for (int t = b; t < e; ++t) for (int k = 0; k < 3; ++k) { float d = centroid_axis(&v[t], k) - meanf[k]; varf[k] += d * d; }
+                for (int k = 0; k < 3; ++k) varf[k] /= (float)(e - b);
+                (void)mean; (void)var;
+                int axis = 0;
+                if (varf[1] > varf[axis]) axis = 1;
+                if (varf[2] > varf[axis]) axis = 2;
+                int m = b + (e - b) / 2;
+                nth_split(v, b, e, m, axis);
+                cb[i * 2] = b; ce[i * 2 + 1] = e; ce[i * 2] = m; cb[i * 2 + 1] = m;
+            }
+            n_children *= 2;
+        }
+        nodes[node].left_idx = n_nodes;
+        for (int i = 0; i < 4; ++i) {
+            if (n_nodes >= max_nodes) { free(stack); return -1; }
+            int ci = n_nodes++;
+            bbox_of(v, cb[i], ce[i], nodes[ci].bb_min, nodes[ci].bb_max);
+            if (ce[i] - cb[i] <= leaf_size) {
+                nodes[ci].left_idx = -cb[i] - 1;
+                nodes[ci].right_idx = -ce[i] - 1;
+            } else {
+                stack[sp++] = ci; stack[sp++] = cb[i]; stack[sp++] = ce[i];
+            }
+        }
+        nodes[node].right_idx = n_nodes;
+    }
+    free(stack);
+    return n_nodes;
+}
+
+/* closest_triangle (NGP/bvh.cuh:48-96): stack traversal, children sorted by box distance with the
+ * 4-input sorting network (:28-46) so the nearest is popped first; children pushed when
+ * dist <= best.  exact == 0 reproduces the reference's leaf rule (dist <= best: the last
+ * triangle in BVH order wins ties).  exact == 1 keeps the lowest original id on ties and prunes
+ * with a small relative slack so that the result equals the brute-force minimum. */
+void orc_nearest_bvh(const orc_bvh_node *nodes, const orc_tri *sorted, const float *pts, int64_t n_pts, int exact,
+                     int32_t *out_id, float *out_d2) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t q = 0; q < n_pts; ++q) {
+        const float *p = &pts[q * 3];
+        int stack[64]; int sp = 0;
+        stack[sp++] = 0;
+        float best = FLT_MAX; int bidx = -1; int32_t bid = -1;
+        while (sp > 0) {
+            int idx = stack[--sp];
+            const orc_bvh_node *n = &nodes[idx];
+            if (n->left_idx < 0) {
+                int end = -n->right_idx - 1;
+                for (int i = -n->left_idx - 1; i < end; ++i) {
+                    float d = orc_tri_distance_sq(&sorted[i], p);
+                    if (exact) {
+                        if (d < best || (d == best && (int32_t)sorted[i].id < bid)) { best = d; bidx = i; bid = (int32_t)sorted[i].id; }
+                    } else if (d <= best) { best = d; bidx = i; bid = (int32_t)sorted[i].id; }
+                }
+            } else {
+                float cd[4]; int ci[4];
+                for (int i = 0; i < 4; ++i) { ci[i] = n->left_idx + i; cd[i] = orc_box_distance_sq(nodes[ci[i]].bb_min, nodes[ci[i]].bb_max, p); }
+                /* sorting network: compare_and_swap swaps when first < second (descending) */
+#define CAS(x, y) if (cd[x] < cd[y]) { float td = cd[x]; cd[x] = cd[y]; cd[y] = td; int ti = ci[x]; ci[x] = ci[y]; ci[y] = ti; }
+                CAS(0, 2) CAS(1, 3) CAS(0, 1) CAS(2, 3) CAS(1, 2)
+#undef CAS
+                for (int i = 0; i < 4; ++i) {
+                    float lim = exact ? best * 1.0009765625f + 1e-12f : best;
+                    if (cd[i] <= lim && sp < 64) stack[sp++] = ci[i];
+                }
+            }
+        }
+        (void)bidx;
+        out_id[q] = bid;
+        if (out_d2) out_d2[q] = best;
+    }
+}
+
+/* -------------------------------------------------- canonical map (warp) */
+static int32_t nearest_one(const orc_deform *d, const float *p) {
+    int32_t id; float d2;
+    if (d->nodes) orc_nearest_bvh(d->nodes, d->sorted, p, 1, d->bvh_exact, &id, &d2);
+    else orc_nearest_brute(d->def_tris, d->n_tris, p, 1, &id, &d2);
+    return id;
+}
+
+void orc_canonical_map_soa(const orc_deform *d, const float *pts, int64_t n, int32_t *out_idx, float *out_canon) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) {
+        int32_t id = nearest_one(d, &pts[i * 3]);
+        out_idx[i] = id;
+        if (id < 0) { memcpy(&out_canon[i * 3], &pts[i * 3], 12); continue; }
+        if (d->fp64) map_with_triangle_d(d, id, &pts[i * 3], NULL, &out_canon[i * 3], NULL);
+        else map_with_triangle_f(d, id, &pts[i * 3], NULL, &out_canon[i * 3], NULL);
+    }
+}
+
+/* warp kernel (src/core.cu:442-526) over NerfCoordinate records (NGP/nerf.h:86-115):
+ * pos[0..2], dt[3], holder[4], deformed_pos[5..7], dir[8..10], extra dims at the end.
+ * frame_id < 0 takes the frame from `holder` (surface_closest_point); this oracle holds one
+ * frame, so records naming another frame are left untouched. */
+static void map_coord(const orc_deform *d, float *c, uint32_t stride, uint32_t n_extra, int32_t frame_id, uint32_t n_frames) {
+    if (c[4] < 0.f) return;
+    uint32_t fid = frame_id < 0 ? (uint32_t)c[4] : (uint32_t)frame_id;
+    if (fid >= n_frames) return;
+    if (!box_contains(d->aabb_min, d->aabb_max, c)) return;
+    int32_t id = nearest_one(d, c);
+    if (id < 0) return;
+    float pos[3], dir[3];
+    if (d->fp64) map_with_triangle_d(d, id, c, &c[8], pos, dir);
+    else map_with_triangle_f(d, id, c, &c[8], pos, dir);
+    memcpy(c, pos, 12);
+    memcpy(&c[8], dir, 12);
+    if (d->def_tris[id].mask_id != 7u)
+        for (uint32_t m = 0; m < n_extra; ++m) c[stride - n_extra + m] = 1.f;
+}
+
+void orc_canonical_map_coords(const orc_deform *d, float *coords, uint32_t stride, uint32_t n_extra, int64_t n,
+                              int32_t frame_id, uint32_t n_frames) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) map_coord(d, &coords[i * stride], stride, n_extra, frame_id, n_frames);
+}
+
+/* ------------------------------------------------------------- occupancy */
+static uint32_t expand_bits(uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+uint32_t orc_morton3d(uint32_t x, uint32_t y, uint32_t z) { return expand_bits(x) | (expand_bits(y) << 1) | (expand_bits(z) << 2); }
+static uint32_t morton_invert(uint32_t x) {
+    x = x & 0x49249249u;
+    x = (x | (x >> 2)) & 0xc30c30c3u;
+    x = (x | (x >> 4)) & 0x0f00f00fu;
+    x = (x | (x >> 8)) & 0xff0000ffu;
+    x = (x | (x >> 16)) & 0x0000ffffu;
+    return x;
+}
+
+#define GRID 128u
+#define GRID3 (GRID * GRID * GRID)
+
+/* mark_flame_density_grid (ngp/src/testbed_nerf.cu:364-389) on the deformed mesh, then
+ * grid_to_bitfield (:585-609, threshold min(0.01, mean) which keeps exactly the marked cells)
+ * and bitfield_max_pool for mips 1..7 (:611-632).  bitfield: 8 * 128^3 / 8 bytes. */
+void orc_occupancy_from_mesh(const orc_tri *tris, int n_tris, float radius, uint8_t *bitfield) {
+    memset(bitfield, 0, GRID3 / 8 * 8);
+    orc_tri *sorted = malloc(sizeof(orc_tri) * (size_t)n_tris);
+    int max_nodes = 2 * n_tris + 16;
+    orc_bvh_node *nodes = malloc(sizeof(orc_bvh_node) * (size_t)max_nodes);
+    orc_bvh4_build(tris, n_tris, 2, nodes, max_nodes, sorted);
+    uint8_t *mark = calloc(GRID3, 1);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < (int64_t)GRID3; ++i) {
+        uint32_t x = morton_invert((uint32_t)i >> 0), y = morton_invert((uint32_t)i >> 1), z = morton_invert((uint32_t)i >> 2);
+        float p[3] = {((float)x + 0.5f) / (float)GRID, ((float)y + 0.5f) / (float)GRID, ((float)z + 0.5f) / (float)GRID};
+        for (int k = 0; k < 3; ++k) p[k] = (p[k] - 0.5f) * 1.0f + 0.5f;
+        int32_t id; float d2;
+        orc_nearest_bvh(nodes, sorted, p, 1, 1, &id, &d2);
+        if (id >= 0 && (double)sqrtf(d2) < (double)radius && tris[id].mask_id != 0u) mark[i] = 1;
+    }
+    for (uint32_t b = 0; b < GRID3 / 8; ++b) {
+        uint8_t bits = 0;
+        for (int j = 0; j < 8; ++j) bits |= mark[b * 8 + j] ? (uint8_t)(1u << j) : 0;
+        bitfield[b] = bits;
+    }
+    for (uint32_t level = 1; level < 8; ++level) {
+        const uint8_t *prev = bitfield + (size_t)(level - 1) * GRID3 / 8;
+        uint8_t *next = bitfield + (size_t)level * GRID3 / 8;
+        for (uint32_t i = 0; i < GRID3 / 64; ++i) {
+            uint8_t bits = 0;
+            for (int j = 0; j < 8; ++j) bits |= prev[i * 8 + j] > 0 ? (uint8_t)(1u << j) : 0;
+            uint32_t x = morton_invert(i >> 0) + GRID / 8, y = morton_invert(i >> 1) + GRID / 8, z = morton_invert(i >> 2) + GRID / 8;
+            next[orc_morton3d(x, y, z)] |= bits;
+        }
+    }
+    free(mark); free(nodes); free(sorted);
+}
+
+/* ------------------------------------------------- low-discrepancy jitter */
+/* Sobol direction numbers for dimensions 0 and 1 (van der Corput and the x+1 primitive
+ * polynomial), generated by the standard recurrence (NGP/random_val.cuh:159-216 uses the
+ * same sequence). */
+uint32_t orc_sobol(uint32_t index, uint32_t dim) {
+    uint32_t X = 0, v = 0x80000000u;
+    for (uint32_t bit = 0; bit < 32; ++bit) {
+        uint32_t dirn = (dim == 0) ? (0x80000000u >> bit) : v;
+        if ((index >> bit) & 1u) X ^= dirn;
+        v = v ^ (v >> 1);
+    }
+    return X;
+}
+static uint32_t hash_combine(uint32_t seed, uint32_t v) { return seed ^ (v + (seed << 6) + (seed >> 2)); }
+static uint32_t reverse_bits(uint32_t x) {
+    x = ((x & 0xaaaaaaaau) >> 1) | ((x & 0x55555555u) << 1);
+    x = ((x & 0xccccccccu) >> 2) | ((x & 0x33333333u) << 2);
+    x = ((x & 0xf0f0f0f0u) >> 4) | ((x & 0x0f0f0f0fu) << 4);
+    x = ((x & 0xff00ff00u) >> 8) | ((x & 0x00ff00ffu) << 8);
+    return (x >> 16) | (x << 16);
+}
+/* Laine-Karras style permutation (Burley 2020, "Practical Hash-based Owen Scrambling"). */
+static uint32_t lk_permutation(uint32_t x, uint32_t seed) {
+    x += seed;
+    x ^= x * 0x6c50b47cu;
+    x ^= x * 0xb82f1e52u;
+    x ^= x * 0xc7afe638u;
+    x ^= x * 0x8d22f6e6u;
+    return x;
+}
+static uint32_t owen_scramble(uint32_t x, uint32_t seed) { return reverse_bits(lk_permutation(reverse_bits(x), seed)); }
+
+/* ld_random_val (NGP/random_val.cuh:284-288). */
+float orc_ld_random_val(uint32_t index, uint32_t seed, uint32_t dim) {
+    const float S = (float)(1.0 / 4294967296.0);
+    index = owen_scramble(index, seed);
+    return (float)owen_scramble(orc_sobol(index, dim), hash_combine(seed, dim)) * S;
+}
+/* ld_random_pixel_offset (NGP/random_val.cuh:317-322). */
+void orc_ld_random_pixel_offset(uint32_t spp, float out[2]) {
+    const float S = (float)(1.0 / 4294967296.0);
+    uint32_t i0 = owen_scramble(0, 0xdeadbeefu), i1 = owen_scramble(spp, 0xdeadbeefu);
+    for (uint32_t d = 0; d < 2; ++d) {
+        float v0 = (float)owen_scramble(orc_sobol(i0, d), hash_combine(0xdeadbeefu, d)) * S;
+        float v1 = (float)owen_scramble(orc_sobol(i1, d), hash_combine(0xdeadbeefu, d)) * S;
+        float o = (0.5f - v0) + v1;
+        out[d] = o - floorf(o);
+    }
+}
+
+/* ------------------------------------------------------------------ march */
+#define SQRT3F 1.73205080757f
+#define STEPSIZE (SQRT3F / 1024.0f)
+#define MIN_CONE STEPSIZE
+#define MAX_CONE (STEPSIZE * 128.0f * 1024.0f / 128.0f)
+
+/* calc_dt (ngp/src/testbed_nerf.cu:91-93) */
+static inline float calc_dt(float t, float cone) { return clampf_(t * cone, MIN_CONE, MAX_CONE); }
+/* warp_dt / unwarp_dt (:303-311) */
+static inline float warp_dt(float dt) { float mx = MIN_CONE * 128.0f; return (dt - MIN_CONE) / (mx - MIN_CONE); }
+static inline float unwarp_dt(float dt) { float mx = MIN_CONE * 128.0f; return dt * (mx - MIN_CONE) + MIN_CONE; }
+
+/* mip_from_pos / mip_from_dt (:471-485), max_cascade = 7 */
+static inline int mip_from_pos(const float *p) {
+    float m = fabsf(p[0] - 0.5f);
+    float a1 = fabsf(p[1] - 0.5f), a2 = fabsf(p[2] - 0.5f);
+    if (a1 > m) m = a1;
+    if (a2 > m) m = a2;
+    int e; frexpf(m, &e);
+    int v = e + 1 > 0 ? e + 1 : 0;
+    return v < 6 ? v : 6;
+}
+static inline int mip_from_dt(float dt, const float *p) {
+    int mip = mip_from_pos(p);
+    dt *= 2.0f * 128.0f;
+    if (dt < 1.f) return mip;
+    int e; frexpf(dt, &e);
+    int v = e > mip ? e : mip;
+    return v < 6 ? v : 6;
+}
+/* cascaded_grid_idx_at / density_grid_occupied_at (:313-337) */
+static inline int occupied_at(const float *pos, const uint8_t *bf, int mip) {
+    float s = scalbnf(1.0f, -mip);
+    int ii[3];
+    for (int k = 0; k < 3; ++k) {
+        float q = pos[k] - 0.5f;
+        q *= s;
+        q += 0.5f;
+        int v = (int)(q * 128.0f);
+        ii[k] = v < 0 ? 0 : (v > 127 ? 127 : v);
+    }
+    uint32_t idx = orc_morton3d((uint32_t)ii[0], (uint32_t)ii[1], (uint32_t)ii[2]);
+    return (bf[idx / 8 + (size_t)mip * GRID3 / 8] >> (idx % 8)) & 1;
+}
+/* distance_to_next_voxel / advance_to_next_voxel (:186-208) */
+static inline float advance_to_next_voxel(float t, float cone, const float *pos, const float *dir, const float *idir, uint32_t res) {
+    float fr = (float)res, tt[3];
+    for (int k = 0; k < 3; ++k) {
+        float p = fr * pos[k];
+        tt[k] = (floorf(p + 0.5f + 0.5f * ngp_sign(dir[k])) - p) * idir[k];
+    }
+    float tm = tt[0] < tt[1] ? tt[0] : tt[1];
+    tm = tm < tt[2] ? tm : tt[2];
+    float dist = fmaxf(tm / fr, 0.0f);
+    float target = t + dist;
+    do { t += calc_dt(t, cone); } while (t < target);
+    return t;
+}
+
+/* BoundingBox::ray_intersect (NGP/bounding_box.cuh:163-210), returns tmin or FLT_MAX */
+static float aabb_ray_tmin(const float *mn, const float *mx, const float *o, const float *d) {
+    float tmin = (mn[0] - o[0]) / d[0], tmax = (mx[0] - o[0]) / d[0];
+    if (tmin > tmax) { float t = tmin; tmin = tmax; tmax = t; }
+    float tymin = (mn[1] - o[1]) / d[1], tymax = (mx[1] - o[1]) / d[1];
+    if (tymin > tymax) { float t = tymin; tymin = tymax; tymax = t; }
+    if (tmin > tymax || tymin > tmax) return FLT_MAX;
+    if (tymin > tmin) tmin = tymin;
+    if (tymax < tmax) tmax = tymax;
+    float tzmin = (mn[2] - o[2]) / d[2], tzmax = (mx[2] - o[2]) / d[2];
+    if (tzmin > tzmax) { float t = tzmin; tzmin = tzmax; tzmax = t; }
+    if (tmin > tzmax || tzmin > tmax) return FLT_MAX;
+    if (tzmin > tmin) tmin = tzmin;
+    return tmin;
+}
+
+typedef struct { float o[3], d[3], idir[3], t; int alive; } ray_state;
+
+/* init_rays_with_payload_kernel_nerf (:1854-1963) + pixel_to_ray (NGP/common_device.cuh:260-315)
+ * + advance_pos_nerf (:634-686) for one pixel. */
+static void ray_init(const orc_render_cfg *rc, const uint8_t *bf, int x, int y, ray_state *r) {
+    float off[2];
+    orc_ld_random_pixel_offset(rc->snap_to_pixel_centers ? 0u : rc->spp, off);
+    float u = ((float)x + off[0]) / (float)rc->width, v = ((float)y + off[1]) / (float)rc->height;
+    float dc[3] = {(u - rc->screen_center[0]) * (float)rc->width / rc->focal[0],
+                   (v - rc->screen_center[1]) * (float)rc->height / rc->focal[1], 1.0f};
+    float d[3];
+    for (int k = 0; k < 3; ++k) { const float *row = &rc->cam[k * 4]; float rr[3] = {row[0], row[1], row[2]}; d[k] = v3dot(rr, dc); }
+    float z = v3dot(d, d);
+    if (z > 0.f) { float s = sqrtf(z); d[0] /= s; d[1] /= s; d[2] /= s; }
+    for (int k = 0; k < 3; ++k) { r->o[k] = rc->cam[k * 4 + 3]; r->d[k] = d[k]; r->idir[k] = 1.0f / d[k]; }
+    float tm = aabb_ray_tmin(rc->render_aabb_min, rc->render_aabb_max, r->o, r->d);
+    float t = fmaxf(tm, 0.05f) + 1e-6f;
+    float p[3];
+    for (int k = 0; k < 3; ++k) p[k] = r->o[k] + r->d[k] * t;
+    r->alive = box_contains(rc->render_aabb_min, rc->render_aabb_max, p);
+    if (!r->alive) return;
+    uint32_t idx = (uint32_t)x + (uint32_t)rc->width * (uint32_t)y;
+    float dt = calc_dt(t, rc->cone_angle);
+    t += orc_ld_random_val(rc->spp, idx * 786433u, 0) * dt;
+    for (;;) {
+        for (int k = 0; k < 3; ++k) p[k] = r->o[k] + r->d[k] * t;
+        if (!box_contains(rc->render_aabb_min, rc->render_aabb_max, p)) { r->alive = 0; break; }
+        dt = calc_dt(t, rc->cone_angle);
+        int mip = mip_from_dt(dt, p);
+        if (!bf || occupied_at(p, bf, mip)) break;
+        uint32_t res = GRID >> mip;
+        t = advance_to_next_voxel(t, rc->cone_angle, p, r->d, r->idir, res);
+    }
+    r->t = t;
+}
+
+/* One step of generate_next_nerf_network_inputs (:760-791): march to the next occupied sample;
+ * returns 0 when the ray leaves the render box. */
+static int ray_next_sample(const orc_render_cfg *rc, const uint8_t *bf, ray_state *r, float *pos, float *dt_out, float *t_out) {
+    float t = r->t, dt = 0.f;
+    for (;;) {
+        for (int k = 0; k < 3; ++k) pos[k] = r->o[k] + r->d[k] * t;
+        if (!box_contains(rc->render_aabb_min, rc->render_aabb_max, pos)) { r->t = t; return 0; }
+        dt = calc_dt(t, rc->cone_angle);
+        int mip = mip_from_dt(dt, pos);
+        if (!bf || occupied_at(pos, bf, mip)) break;
+        uint32_t res = GRID >> mip;
+        t = advance_to_next_voxel(t, rc->cone_angle, pos, r->d, r->idir, res);
+    }
+    *dt_out = dt;
+    if (t_out) *t_out = t;
+    r->t = t + dt;
+    return 1;
+}
+
+int orc_march_ray(const orc_render_cfg *rc, const uint8_t *bf, int px, int py, int max_out, float *out_t, float *out_dt,
+                  float *out_pos) {
+    ray_state r;
+    ray_init(rc, bf, px, py, &r);
+    if (!r.alive) return 0;
+    int n = 0;
+    while (n < max_out && n < (int)rc->max_samples_per_ray) {
+        float pos[3], dt, ts;
+        if (!ray_next_sample(rc, bf, &r, pos, &dt, &ts)) break;
+        out_t[n] = ts;
+        out_dt[n] = dt;
+        memcpy(&out_pos[n * 3], pos, 12);
+        ++n;
+    }
+    return n;
+}
+
+static float srgb_to_linear(float s) { return s <= 0.04045f ? s / 12.92f : powf((s + 0.055f) / 1.055f, 2.4f); }
+static double logistic_d(double x) { return 1.0 / (1.0 + exp(-x)); }
+
+/* Full headless render of rows [row_begin, row_end): NerfTracer::trace (:2112-2244) with
+ * render_deformed (src/core.cu:610-637), NerfNetwork inference and composite_kernel_nerf
+ * (:797-1009), then shade_kernel_nerf (:1794-1827) into a zeroed frame buffer.  The result is
+ * independent of the tracer's compaction schedule, so each ray is processed to completion.
+ * Returns the number of network samples evaluated. */
+int64_t orc_render(const orc_render_cfg *rc, const orc_deform *d, const uint8_t *bf, const orc_field_cfg *fc,
+                   const uint16_t *params, const float *layer_scales, int row_begin, int row_end, float *out_rgba,
+                   float *out_depth, uint32_t *out_nsamples, int fp64) {
+    uint64_t lvl_off[64], mlp_off[3];
+    uint32_t lvl_res[64], lvl_size[64];
+    orc_field_layout(fc, lvl_off, lvl_res, lvl_size, mlp_off);
+    static const float ones[32] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
+    if (!layer_scales) layer_scales = ones;
+    const uint32_t stride = 11 + fc->n_extra;
+    const float cam_fwd[3] = {rc->cam[2], rc->cam[6], rc->cam[10]};
+    const float cam_pos[3] = {rc->cam[3], rc->cam[7], rc->cam[11]};
+    int64_t total = 0;
+    const int W = rc->width;
+    int64_t n_px = (int64_t)(row_end - row_begin) * W;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+    for (int64_t q = 0; q < n_px; ++q) {
+        int x = (int)(q % W), y = row_begin + (int)(q / W);
+        size_t pix = (size_t)(y - row_begin) * W + x;
+        float *fb = &out_rgba[pix * 4];
+        fb[0] = fb[1] = fb[2] = fb[3] = 0.f;
+        out_depth[pix] = 1e10f;
+        uint32_t ns = 0;
+        ray_state r;
+        ray_init(rc, bf, x, y, &r);
+        if (r.alive) {
+            float rgba_f[4] = {0, 0, 0, 0}, depth_f = 0.f, maxw_f = 0.f;
+            double rgba_d[4] = {0, 0, 0, 0}, depth_d = 0.0, maxw_d = 0.0;
+            while (ns < rc->max_samples_per_ray) {
+                float pos[3], dt;
+                if (!ray_next_sample(rc, bf, &r, pos, &dt, NULL)) break;
+                float coord[64];
+                for (int k = 0; k < 3; ++k) {
+                    coord[k] = (pos[k] - rc->train_aabb_min[k]) / (rc->train_aabb_max[k] - rc->train_aabb_min[k]);
+                    coord[5 + k] = coord[k];
+                    coord[8 + k] = (r.d[k] + 1.0f) * 0.5f;
+                }
+                coord[3] = warp_dt(dt);
+                coord[4] = (float)rc->frame_id;
+                for (uint32_t m = 0; m < fc->n_extra; ++m) coord[11 + m] = rc->extra_dims ? rc->extra_dims[m] : 0.f;
+                map_coord(d, coord, stride, fc->n_extra, rc->frame_id, (uint32_t)rc->frame_id + 1u);
+                ++ns;
+                float dpos[3];
+                for (int k = 0; k < 3; ++k) dpos[k] = rc->train_aabb_min[k] + coord[5 + k] * (rc->train_aabb_max[k] - rc->train_aabb_min[k]);
+                float dtu = unwarp_dt(coord[3]);
+                float dp[3] = {dpos[0] - cam_pos[0], dpos[1] - cam_pos[1], dpos[2] - cam_pos[2]};
+                int done = 0;
+                if (fp64) {
+                    double o4[4];
+                    field_one_d(fc, params, layer_scales, lvl_off, lvl_res, lvl_size, mlp_off, coord, stride, o4);
+                    double T = 1.0 - rgba_d[3];
+                    double alpha = 1.0 - exp(-exp(o4[3]) * (double)dtu);
+                    double w = alpha * T;
+                    for (int k = 0; k < 3; ++k) rgba_d[k] += logistic_d(o4[k]) * w;
+                    rgba_d[3] += w;
+                    if (w > maxw_d) { maxw_d = w; depth_d = (double)v3dot(cam_fwd, dp); }
+                    if (rgba_d[3] > 1.0 - (double)rc->min_transmittance) {
+                        double a = rgba_d[3];
+                        for (int k = 0; k < 4; ++k) rgba_d[k] /= a;
+                        done = 1;
+                    }
+                } else {
+                    float o4[4];
+                    field_one_f(fc, params, layer_scales, lvl_off, lvl_res, lvl_size, mlp_off, coord, stride, o4);
+                    float T = 1.f - rgba_f[3];
+                    float alpha = 1.f - expf(-expf(o4[3]) * dtu);
+                    float w = alpha * T;
+                    for (int k = 0; k < 3; ++k) rgba_f[k] += (1.0f / (1.0f + expf(-o4[k]))) * w;
+                    rgba_f[3] += w;
+                    if (w > maxw_f) { maxw_f = w; depth_f = v3dot(cam_fwd, dp); }
+                    if (rgba_f[3] > 1.0f - rc->min_transmittance) {
+                        float a = rgba_f[3];
+                        for (int k = 0; k < 4; ++k) rgba_f[k] /= a;
+                        done = 1;
+                    }
+                }
+                if (done) break;
+            }
+            float out4[4], dep;
+            if (fp64) { for (int k = 0; k < 4; ++k) out4[k] = (float)rgba_d[k]; dep = (float)depth_d; }
+            else { memcpy(out4, rgba_f, 16); dep = depth_f; }
+            if (out4[3] > 0.001f) {
+                if (!rc->linear_colors) for (int k = 0; k < 3; ++k) out4[k] = srgb_to_linear(out4[k]);
+                memcpy(fb, out4, 16);
+                if (out4[3] > 0.2f) out_depth[pix] = dep;
+            }
+        }
+        if (out_nsamples) out_nsamples[pix] = ns;
+        total += ns;
+    }
+    return total;
+}
+
+/* Field evaluation over NerfCoordinate records; out4[i*4 + k] = (r, g, b, raw density). */
+void orc_field_eval(const orc_field_cfg *c, const uint16_t *params, const float *layer_scales, const float *coords,
+                    uint32_t stride, int64_t n, float *out4, int fp64) {
+    uint64_t lvl_off[64], mlp_off[3];
+    uint32_t lvl_res[64], lvl_size[64];
+    orc_field_layout(c, lvl_off, lvl_res, lvl_size, mlp_off);
+    static const float ones[32] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
+    if (!layer_scales) layer_scales = ones;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) {
+        if (fp64) {
+            double o[4];
+            field_one_d(c, params, layer_scales, lvl_off, lvl_res, lvl_size, mlp_off, &coords[i * stride], stride, o);
+            for (int k = 0; k < 4; ++k) out4[i * 4 + k] = (float)o[k];
+        } else {
+            float o[4];
+            field_one_f(c, params, layer_scales, lvl_off, lvl_res, lvl_size, mlp_off, &coords[i * stride], stride, o);
+            memcpy(&out4[i * 4], o, 16);
+        }
+    }
+}

@@ -1,0 +1,138 @@
+/*
+ * insta_oracle.h -- CPU restatement of INSTA's per-sample deformation and
+ * render path.  TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke
+ * check and by bench.py's CPU-baseline leg.  The product library never links
+ * or calls anything declared here.
+ *
+ * Every function cites the reference file:line whose behaviour it restates.
+ * Paths are relative to the INSTA repository; "ngp/" abbreviates
+ * "instant-ngp/" and "NGP/" abbreviates
+ * "instant-ngp/include/neural-graphics-primitives/".
+ *
+ * Floating-point contract: compiled with -ffp-contract=off so every a*b+c is
+ * two roundings, and 3-term sums follow Eigen's halving reduction order
+ * x0 + (x1 + x2) (4-term: (x0 + x1) + (x2 + x3)).  The CUDA kernels mirror
+ * this order with __fmul_rn/__fadd_rn wherever a result must be bit-exact
+ * (squared point-triangle and point-box distances, which decide the nearest
+ * triangle index).
+ */
+#ifndef INSTA_ORACLE_H
+#define INSTA_ORACLE_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same 48-byte record as ngp::Triangle (NGP/triangle.cuh:234-238). */
+typedef struct {
+    float a[3], b[3], c[3];
+    float scaling;
+    uint32_t id;
+    uint32_t mask_id;
+} orc_tri;
+
+/* ngp::TriangleBvhNode (ngp/include/.../triangle_bvh.cuh:29-33): 32 bytes. */
+typedef struct {
+    float bb_min[3], bb_max[3];
+    int32_t left_idx, right_idx;
+} orc_bvh_node;
+
+/* ---- mesh ------------------------------------------------------------ */
+int orc_adjacency(const int32_t *faces, int n_faces, int n_verts, int32_t *out_adj);
+void orc_build_triangles(const float *verts, const float *canon_verts, const int32_t *faces,
+                         const uint32_t *mask, int n_faces, orc_tri *out);
+float orc_tri_distance_sq(const orc_tri *t, const float *p);
+float orc_box_distance_sq(const float *mn, const float *mx, const float *p);
+
+/* ---- nearest triangle -------------------------------------------------- */
+void orc_nearest_brute(const orc_tri *tris, int n_tris, const float *pts, int64_t n_pts,
+                       int32_t *out_id, float *out_d2);
+int orc_bvh4_build(const orc_tri *tris, int n_tris, int leaf_size, orc_bvh_node *out_nodes,
+                   int max_nodes, orc_tri *out_sorted);
+void orc_nearest_bvh(const orc_bvh_node *nodes, const orc_tri *sorted, const float *pts,
+                     int64_t n_pts, int exact, int32_t *out_id, float *out_d2);
+
+/* ---- deformation map --------------------------------------------------- */
+typedef struct {
+    const orc_tri *def_tris;      /* frame triangles, original order        */
+    const orc_tri *can_tris;      /* canonical triangles, original order    */
+    const int32_t *adjacency;     /* [F*3]                                  */
+    const orc_bvh_node *nodes;    /* optional BVH over def_tris (NULL: brute) */
+    const orc_tri *sorted;        /* BVH-ordered triangles                  */
+    int n_tris;
+    int disable_interp;
+    int fp64;                     /* 1: FP64 twin of the whole map          */
+    int bvh_exact;                /* 1: lowest-id ties; 0: reference `<=`   */
+    float aabb_min[3], aabb_max[3];
+} orc_deform;
+
+void orc_canonical_map_soa(const orc_deform *d, const float *pts, int64_t n,
+                           int32_t *out_idx, float *out_canon);
+void orc_canonical_map_coords(const orc_deform *d, float *coords, uint32_t stride,
+                              uint32_t n_extra, int64_t n, int32_t frame_id, uint32_t n_frames);
+
+/* ---- occupancy --------------------------------------------------------- */
+void orc_occupancy_from_mesh(const orc_tri *tris, int n_tris, float radius, uint8_t *bitfield);
+uint32_t orc_morton3d(uint32_t x, uint32_t y, uint32_t z);
+
+/* ---- field (hash grid + SH + MLPs) ------------------------------------ */
+typedef struct {
+    uint32_t n_levels, n_features, log2_table, base_res;
+    float per_level_scale;
+    uint32_t n_extra;             /* expression dims appended to the density input */
+    uint32_t density_hidden;      /* neurons (64)                           */
+    uint32_t density_layers;      /* hidden layers (1)                      */
+    uint32_t density_out;         /* 16                                     */
+    uint32_t rgb_hidden;          /* 64                                     */
+    uint32_t rgb_layers;          /* hidden layers (2)                      */
+    uint32_t rgb_out_padded;      /* 16                                     */
+    int weight_format;            /* 0 fp16, 1 bf16, 2 fp8-e4m3 (per-layer scale) */
+} orc_field_cfg;
+
+uint64_t orc_field_layout(const orc_field_cfg *c, uint64_t *level_offsets, uint32_t *level_res,
+                          uint32_t *level_size, uint64_t *mlp_params);
+void orc_field_eval(const orc_field_cfg *c, const uint16_t *params, const float *layer_scales,
+                    const float *coords, uint32_t stride, int64_t n, float *out4, int fp64);
+
+/* ---- render ------------------------------------------------------------ */
+typedef struct {
+    int width, height;
+    float focal[2];
+    float screen_center[2];
+    float cam[12];                /* 3x4 row-major: [R | origin]            */
+    float render_aabb_min[3], render_aabb_max[3];
+    float train_aabb_min[3], train_aabb_max[3];
+    float cone_angle;
+    float min_transmittance;
+    uint32_t spp;
+    uint32_t max_samples_per_ray;
+    int snap_to_pixel_centers;
+    int frame_id;
+    const float *extra_dims;      /* [n_extra] inference expression vector or NULL */
+    int linear_colors;            /* 0: shade converts sRGB -> linear       */
+} orc_render_cfg;
+
+int64_t orc_render(const orc_render_cfg *rc, const orc_deform *d, const uint8_t *bitfield,
+                   const orc_field_cfg *fc, const uint16_t *params, const float *layer_scales,
+                   int row_begin, int row_end, float *out_rgba, float *out_depth,
+                   uint32_t *out_nsamples, int fp64);
+int orc_march_ray(const orc_render_cfg *rc, const uint8_t *bitfield, int px, int py,
+                  int max_out, float *out_t, float *out_dt, float *out_pos);
+
+/* ---- low-discrepancy helpers (NGP/random_val.cuh:159-322) -------------- */
+float orc_ld_random_val(uint32_t index, uint32_t seed, uint32_t dim);
+void orc_ld_random_pixel_offset(uint32_t spp, float out[2]);
+uint32_t orc_sobol(uint32_t index, uint32_t dim);
+
+/* ---- half helpers ------------------------------------------------------ */
+uint16_t orc_f2h(float x);
+float orc_h2f(uint16_t h);
+int orc_num_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,257 @@
+"""ctypes front end of the CPU oracle (oracle/insta_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by
+bench.py's CPU-baseline leg.  It is the checker (and the timed CPU baseline),
+never the product: the library under insta_gb300/ does not import it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "insta_oracle.c"
+INC = HERE / "oracle_real.inc"
+BUILD = HERE / "_build"
+LIB = BUILD / "liboracle.so"
+
+
+def build(force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    deps = [SRC, INC, HERE / "insta_oracle.h"]
+    if force or not LIB.exists() or any(d.stat().st_mtime > LIB.stat().st_mtime for d in deps):
+        tmp = BUILD / f"liboracle.{os.getpid()}.so"
+        cmd = ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=gnu11",
+               "-Wall", "-Wno-unused-function", str(SRC), "-o", str(tmp), "-lm"]
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+class Tri(C.Structure):
+    _fields_ = [("a", C.c_float * 3), ("b", C.c_float * 3), ("c", C.c_float * 3), ("scaling", C.c_float),
+                ("id", C.c_uint32), ("mask_id", C.c_uint32)]
+
+
+class Node(C.Structure):
+    _fields_ = [("bb_min", C.c_float * 3), ("bb_max", C.c_float * 3), ("left_idx", C.c_int32), ("right_idx", C.c_int32)]
+
+
+class Deform(C.Structure):
+    _fields_ = [("def_tris", C.c_void_p), ("can_tris", C.c_void_p), ("adjacency", C.c_void_p), ("nodes", C.c_void_p),
+                ("sorted", C.c_void_p), ("n_tris", C.c_int), ("disable_interp", C.c_int), ("fp64", C.c_int),
+                ("bvh_exact", C.c_int), ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3)]
+
+
+class FieldCfg(C.Structure):
+    _fields_ = [("n_levels", C.c_uint32), ("n_features", C.c_uint32), ("log2_table", C.c_uint32), ("base_res", C.c_uint32),
+                ("per_level_scale", C.c_float), ("n_extra", C.c_uint32), ("density_hidden", C.c_uint32),
+                ("density_layers", C.c_uint32), ("density_out", C.c_uint32), ("rgb_hidden", C.c_uint32),
+                ("rgb_layers", C.c_uint32), ("rgb_out_padded", C.c_uint32), ("weight_format", C.c_int)]
+
+
+class RenderCfg(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("focal", C.c_float * 2), ("screen_center", C.c_float * 2),
+                ("cam", C.c_float * 12), ("render_aabb_min", C.c_float * 3), ("render_aabb_max", C.c_float * 3),
+                ("train_aabb_min", C.c_float * 3), ("train_aabb_max", C.c_float * 3), ("cone_angle", C.c_float),
+                ("min_transmittance", C.c_float), ("spp", C.c_uint32), ("max_samples_per_ray", C.c_uint32),
+                ("snap_to_pixel_centers", C.c_int), ("frame_id", C.c_int), ("extra_dims", C.c_void_p),
+                ("linear_colors", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(build()))
+        _lib.orc_tri_distance_sq.restype = C.c_float
+        _lib.orc_box_distance_sq.restype = C.c_float
+        _lib.orc_field_layout.restype = C.c_uint64
+        _lib.orc_render.restype = C.c_int64
+        _lib.orc_ld_random_val.restype = C.c_float
+        _lib.orc_ld_random_val.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
+        _lib.orc_sobol.restype = C.c_uint32
+        _lib.orc_sobol.argtypes = [C.c_uint32, C.c_uint32]
+        _lib.orc_morton3d.restype = C.c_uint32
+        _lib.orc_num_threads.restype = C.c_int
+        _lib.orc_occupancy_from_mesh.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_void_p]
+    return _lib
+
+
+def ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def build_triangles(verts, canon_verts, faces, mask) -> np.ndarray:
+    F = len(faces)
+    out = np.zeros(F, dtype=np.dtype([("a", "<f4", 3), ("b", "<f4", 3), ("c", "<f4", 3), ("scaling", "<f4"), ("id", "<u4"), ("mask_id", "<u4")]))
+    v = np.ascontiguousarray(verts, dtype=np.float32)
+    cv = None if canon_verts is None else np.ascontiguousarray(canon_verts, dtype=np.float32)
+    f = np.ascontiguousarray(faces, dtype=np.int32)
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint32)
+    lib().orc_build_triangles(ptr(v), ptr(cv), ptr(f), ptr(m), C.c_int(F), ptr(out))
+    return out
+
+
+def adjacency(faces, n_verts) -> np.ndarray:
+    f = np.ascontiguousarray(faces, dtype=np.int32)
+    out = np.empty((len(f), 3), dtype=np.int32)
+    lib().orc_adjacency(ptr(f), C.c_int(len(f)), C.c_int(n_verts), ptr(out))
+    return out
+
+
+def nearest_brute(tris, pts):
+    p = np.ascontiguousarray(pts, dtype=np.float32)
+    ids = np.empty(len(p), dtype=np.int32)
+    d2 = np.empty(len(p), dtype=np.float32)
+    lib().orc_nearest_brute(ptr(tris), C.c_int(len(tris)), ptr(p), C.c_int64(len(p)), ptr(ids), ptr(d2))
+    return ids, d2
+
+
+class Bvh:
+    """TriangleBvh4 restated (instant-ngp/src/triangle_bvh.cu:548-631)."""
+
+    def __init__(self, tris, leaf_size: int = 2):
+        self.tris = tris
+        max_nodes = 2 * len(tris) + 16
+        self.nodes = np.zeros(max_nodes, dtype=np.dtype([("bb_min", "<f4", 3), ("bb_max", "<f4", 3), ("l", "<i4"), ("r", "<i4")]))
+        self.sorted = np.zeros_like(tris)
+        n = lib().orc_bvh4_build(ptr(tris), C.c_int(len(tris)), C.c_int(leaf_size), ptr(self.nodes), C.c_int(max_nodes), ptr(self.sorted))
+        assert n > 0
+        self.nodes = self.nodes[:n].copy()
+
+    def nearest(self, pts, exact: bool = True):
+        p = np.ascontiguousarray(pts, dtype=np.float32)
+        ids = np.empty(len(p), dtype=np.int32)
+        d2 = np.empty(len(p), dtype=np.float32)
+        lib().orc_nearest_bvh(ptr(self.nodes), ptr(self.sorted), ptr(p), C.c_int64(len(p)), C.c_int(1 if exact else 0), ptr(ids), ptr(d2))
+        return ids, d2
+
+
+class Deformation:
+    """The deformed->canonical map of the `warp` kernel on one frame."""
+
+    def __init__(self, def_tris, can_tris, adj, bvh: Bvh | None = None, disable_interp=False, fp64=False, exact=True,
+                 aabb=((0, 0, 0), (1, 1, 1))):
+        self.keep = (def_tris, can_tris, adj, bvh)
+        d = Deform()
+        d.def_tris = def_tris.ctypes.data
+        d.can_tris = can_tris.ctypes.data
+        d.adjacency = adj.ctypes.data
+        d.nodes = bvh.nodes.ctypes.data if bvh is not None else None
+        d.sorted = bvh.sorted.ctypes.data if bvh is not None else None
+        d.n_tris = len(def_tris)
+        d.disable_interp = int(disable_interp)
+        d.fp64 = int(fp64)
+        d.bvh_exact = int(exact)
+        d.aabb_min[:] = [float(x) for x in aabb[0]]
+        d.aabb_max[:] = [float(x) for x in aabb[1]]
+        self.d = d
+
+    def map_soa(self, pts):
+        p = np.ascontiguousarray(pts, dtype=np.float32)
+        ids = np.empty(len(p), dtype=np.int32)
+        out = np.empty_like(p)
+        lib().orc_canonical_map_soa(C.byref(self.d), ptr(p), C.c_int64(len(p)), ptr(ids), ptr(out))
+        return ids, out
+
+    def map_coords(self, coords, n_extra=0, frame_id=-1, n_frames=1):
+        c = np.ascontiguousarray(coords, dtype=np.float32).copy()
+        stride = c.shape[1]
+        lib().orc_canonical_map_coords(C.byref(self.d), ptr(c), C.c_uint32(stride), C.c_uint32(n_extra), C.c_int64(len(c)),
+                                       C.c_int32(frame_id), C.c_uint32(n_frames))
+        return c
+
+
+def field_cfg(fc, weight_format: int = 0) -> FieldCfg:
+    c = FieldCfg()
+    c.n_levels, c.n_features, c.log2_table, c.base_res = fc.n_levels, fc.n_features, fc.log2_table, fc.base_res
+    c.per_level_scale = fc.per_level_scale
+    c.n_extra = fc.n_extra
+    c.density_hidden, c.density_layers, c.density_out = fc.density_hidden, fc.density_layers, fc.density_out
+    c.rgb_hidden, c.rgb_layers, c.rgb_out_padded = fc.rgb_hidden, fc.rgb_layers, fc.rgb_out_padded
+    c.weight_format = weight_format
+    return c
+
+
+def field_eval(fc, params, coords, fp64=False, weight_format=0):
+    c = np.ascontiguousarray(coords, dtype=np.float32)
+    out = np.empty((len(c), 4), dtype=np.float32)
+    cfg = field_cfg(fc, weight_format)
+    p = np.ascontiguousarray(params).view(np.uint16)
+    lib().orc_field_eval(C.byref(cfg), ptr(p), None, ptr(c), C.c_uint32(c.shape[1]), C.c_int64(len(c)), ptr(out), C.c_int(int(fp64)))
+    return out
+
+
+def occupancy(tris, radius=0.015) -> np.ndarray:
+    bits = np.zeros(8 * 128 ** 3 // 8, dtype=np.uint8)
+    lib().orc_occupancy_from_mesh(ptr(tris), C.c_int(len(tris)), C.c_double(radius), ptr(bits))
+    return bits
+
+
+def render_cfg(width, height, focal, cam, render_box, train_box=((0, 0, 0), (1, 1, 1)), cone_angle=1 / 256, spp=0,
+               min_transmittance=0.01, max_samples=1024, frame_id=0, snap=True, linear_colors=False) -> RenderCfg:
+    r = RenderCfg()
+    r.width, r.height = int(width), int(height)
+    r.focal[:] = [float(focal[0]), float(focal[1])]
+    r.screen_center[:] = [0.5, 0.5]
+    r.cam[:] = [float(x) for x in np.asarray(cam, dtype=np.float32).reshape(-1)]
+    r.render_aabb_min[:] = [float(x) for x in render_box[0]]
+    r.render_aabb_max[:] = [float(x) for x in render_box[1]]
+    r.train_aabb_min[:] = [float(x) for x in train_box[0]]
+    r.train_aabb_max[:] = [float(x) for x in train_box[1]]
+    r.cone_angle = float(np.float32(cone_angle))
+    r.min_transmittance = float(min_transmittance)
+    r.spp = spp
+    r.max_samples_per_ray = max_samples
+    r.snap_to_pixel_centers = int(snap)
+    r.frame_id = frame_id
+    r.extra_dims = None
+    r.linear_colors = int(linear_colors)
+    return r
+
+
+def render(rc: RenderCfg, deform: Deformation, bits, fc, params, rows=None, fp64=False, weight_format=0, extra_dims=None):
+    r0, r1 = (0, rc.height) if rows is None else rows
+    n = (r1 - r0) * rc.width
+    rgba = np.zeros((n, 4), dtype=np.float32)
+    depth = np.zeros(n, dtype=np.float32)
+    ns = np.zeros(n, dtype=np.uint32)
+    cfg = field_cfg(fc, weight_format)
+    p = np.ascontiguousarray(params).view(np.uint16)
+    ed = None
+    if extra_dims is not None:
+        ed = np.ascontiguousarray(extra_dims, dtype=np.float32)
+        rc.extra_dims = ed.ctypes.data
+    total = lib().orc_render(C.byref(rc), C.byref(deform.d), ptr(bits), C.byref(cfg), ptr(p), None, C.c_int(r0), C.c_int(r1),
+                             ptr(rgba), ptr(depth), ptr(ns), C.c_int(int(fp64)))
+    rc.extra_dims = None
+    return rgba, depth, ns, int(total)
+
+
+def march_ray(rc: RenderCfg, bits, px, py, max_out=1024):
+    t = np.zeros(max_out, dtype=np.float32)
+    dt = np.zeros(max_out, dtype=np.float32)
+    pos = np.zeros((max_out, 3), dtype=np.float32)
+    n = lib().orc_march_ray(C.byref(rc), ptr(bits), C.c_int(px), C.c_int(py), C.c_int(max_out), ptr(t), ptr(dt), ptr(pos))
+    return t[:n], dt[:n], pos[:n]
+
+
+def ld_random_val(index, seed, dim=0) -> float:
+    return lib().orc_ld_random_val(index, seed, dim)
+
+
+def pixel_offset(spp) -> np.ndarray:
+    out = (C.c_float * 2)()
+    lib().orc_ld_random_pixel_offset(C.c_uint32(spp), out)
+    return np.array([out[0], out[1]], dtype=np.float32)
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()

@@ -1,0 +1,251 @@
+"""Parity of the CUDA path against the CPU oracle, through the C ABI (cuda:0).
+
+Tolerances (from the task's parity bar):
+* nearest-triangle indices: bit-exact, ties to the lowest triangle id;
+* canonical coordinates: |err| <= 1e-5 x the mesh bounding-box diagonal;
+* occupancy bits and march samples (t, dt): bit-exact;
+* field outputs (FP16 network values): |err| <= 4e-3 + 1e-2 |x| (FP32 accumulation order);
+* rendered pixels: PSNR >= 45 dB against the oracle render.
+"""
+import numpy as np
+import pytest
+
+from conftest import psnr
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.fixture(scope="module")
+def gpu_avatar(ctx, avatar, frame0):
+    ctx.canonical_set(0, avatar.canonical, avatar.faces, avatar.mask)
+    ctx.frame_upload(0, 0, frame0)
+    ctx.frame_upload(0, 1, avatar.frame(avatar.frame_coeffs(1)))
+    ctx.sync()
+    return ctx
+
+
+def diag(avatar):
+    v = avatar.canonical.astype(np.float64)
+    return float(np.linalg.norm(v.max(0) - v.min(0)))
+
+
+def test_nearest_bit_exact_and_canonical(gpu_avatar, oracle, oracle_frame, avatar, frame0):
+    from insta_gb300 import synthetic as S
+    pts = S.shell_points(frame0, avatar.faces, 65536, seed=3)
+    n = len(pts)
+    idx = torch.empty(n, dtype=torch.int32, device="cuda")
+    out = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    gpu_avatar.canonical_map_soa(0, 0, dev(pts), n, idx, out)
+    gpu_avatar.sync()
+    idx, out = idx.cpu().numpy(), out.cpu().numpy()
+    brute_ids, _ = oracle.nearest_brute(oracle_frame["def"], pts[:4096])
+    assert (idx[:4096] == brute_ids).all()
+    d = oracle.Deformation(oracle_frame["def"], oracle_frame["can"], oracle_frame["adj"], oracle_frame["bvh"])
+    ref_ids, ref = d.map_soa(pts)
+    assert (idx == ref_ids).all()
+    assert np.abs(out - ref).max() <= 1e-5 * diag(avatar)
+    d64 = oracle.Deformation(oracle_frame["def"], oracle_frame["can"], oracle_frame["adj"], oracle_frame["bvh"], fp64=True)
+    _, ref64 = d64.map_soa(pts)
+    assert np.abs(out - ref64).max() <= 1e-5 * diag(avatar)
+
+
+def make_coords(pts, dirs, holder, n_extra=0, extra_val=0.25):
+    n = len(pts)
+    c = np.zeros((n, 11 + n_extra), np.float32)
+    c[:, 0:3] = pts
+    c[:, 3] = 0.1
+    c[:, 4] = holder
+    c[:, 5:8] = pts
+    c[:, 8:11] = (dirs + 1) * 0.5
+    c[:, 11:] = extra_val
+    return c
+
+
+def test_canonical_map_coords_in_place(gpu_avatar, oracle, oracle_frame, avatar, frame0):
+    """surface_closest_point / render_deformed semantics: holder-selected frame, skip rules, mask-7 expression dims."""
+    from insta_gb300 import synthetic as S
+    rng = np.random.default_rng(5)
+    pts = S.shell_points(frame0, avatar.faces, 8192, seed=4)
+    dirs = rng.normal(size=pts.shape).astype(np.float32)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    holder = np.zeros(len(pts), np.float32)
+    holder[::7] = -1.0                     # not generated -> untouched
+    pts[::11] += 5.0                       # outside the train box -> untouched
+    c = make_coords(pts, dirs, holder, n_extra=16)
+    cd = dev(c)
+    gpu_avatar.canonical_map(0, 0, cd, c.shape[1], 16, len(c))
+    gpu_avatar.sync()
+    got = cd.cpu().numpy()
+    d = oracle.Deformation(oracle_frame["def"], oracle_frame["can"], oracle_frame["adj"], oracle_frame["bvh"])
+    ref = d.map_coords(c, n_extra=16, frame_id=0, n_frames=1)
+    tol = 1e-5 * diag(avatar)
+    assert np.abs(got[:, 0:3] - ref[:, 0:3]).max() <= tol
+    assert np.abs(got[:, 8:11] - ref[:, 8:11]).max() <= 1e-5
+    assert (got[:, 3:8] == c[:, 3:8]).all()
+    assert (got[:, 11:] == ref[:, 11:]).all()
+    untouched = (holder < 0) | (np.arange(len(c)) % 11 == 0)
+    assert (got[untouched] == c[untouched]).all()
+    # at least one lips sample keeps its expression dims, others get 1.0
+    assert (got[~untouched, 11] == 1.0).any() and (got[~untouched, 11] == 0.25).any()
+
+
+def test_canonical_map_holder_selects_frame(gpu_avatar, oracle, avatar, frame0):
+    from insta_gb300 import synthetic as S
+    f1 = avatar.frame(avatar.frame_coeffs(1))
+    pts = S.shell_points(f1, avatar.faces, 2048, seed=8)
+    dirs = np.tile(np.array([[0, 0, 1]], np.float32), (len(pts), 1))
+    c = make_coords(pts, dirs, np.ones(len(pts), np.float32))
+    cd = dev(c)
+    gpu_avatar.canonical_map(0, -1, cd, 11, 0, len(c))
+    gpu_avatar.sync()
+    can = oracle.build_triangles(avatar.canonical, None, avatar.faces, avatar.mask)
+    d1 = oracle.build_triangles(f1, avatar.canonical, avatar.faces, avatar.mask)
+    adj = oracle.adjacency(avatar.faces, avatar.n_verts)
+    ref = oracle.Deformation(d1, can, adj, oracle.Bvh(d1)).map_coords(c, frame_id=-1, n_frames=2)
+    assert np.abs(cd.cpu().numpy()[:, :3] - ref[:, :3]).max() <= 1e-5 * diag(avatar)
+
+
+def test_canonical_map_empty_is_noop(gpu_avatar):
+    c = torch.zeros((0, 11), dtype=torch.float32, device="cuda")
+    gpu_avatar.canonical_map(0, 0, c, 11, 0, 0)
+    gpu_avatar.sync()
+
+
+def test_occupancy_bit_exact(gpu_avatar, oracle, oracle_frame):
+    gpu_avatar.occupancy_from_mesh(0, 0, 0.015)
+    got = gpu_avatar.occupancy_get(0, 0)
+    ref = oracle.occupancy(oracle_frame["def"], 0.015)
+    assert got.sum() > 0
+    assert (got == ref).all()
+
+
+def test_march_samples_bit_exact(gpu_avatar, oracle, oracle_frame, avatar):
+    from insta_gb300 import synthetic as S
+    gpu_avatar.occupancy_from_mesh(0, 0, 0.015)
+    W = H = 48
+    cam, focal = S.camera(10.0, width=W, height=H)
+    req = gpu_avatar.render_desc(0, 0, W, H, focal, cam)
+    M = 256
+    t = torch.zeros((W * H, M), dtype=torch.float32, device="cuda")
+    dt = torch.zeros_like(t)
+    n = torch.zeros(W * H, dtype=torch.int32, device="cuda")
+    gpu_avatar.march_debug(req, M, t, dt, n)
+    gpu_avatar.sync()
+    t, dt, n = t.cpu().numpy(), dt.cpu().numpy(), n.cpu().numpy()
+    bits = oracle.occupancy(oracle_frame["def"], 0.015)
+    rc = oracle.render_cfg(W, H, focal, cam, avatar.render_aabb())
+    total = 0
+    for i in range(W * H):
+        rt, rdt, _ = oracle.march_ray(rc, bits, i % W, i // W, M)
+        assert n[i] == len(rt), i
+        assert (t[i, :n[i]] == rt).all() and (dt[i, :n[i]] == rdt).all(), i
+        total += n[i]
+    assert total > 0
+
+
+@pytest.fixture(scope="module")
+def field_setup(gpu_avatar):
+    from insta_gb300 import synthetic as S
+    fc = S.FieldConfig()
+    params = S.field_params(fc, seed=0)
+    gpu_avatar.params_load(0, fc, params)
+    return fc, params
+
+
+def random_coords(n, seed=0, n_extra=0):
+    rng = np.random.default_rng(seed)
+    pts = rng.uniform(0.35, 0.65, size=(n, 3)).astype(np.float32)
+    dirs = rng.normal(size=(n, 3)).astype(np.float32)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    c = make_coords(pts, dirs, np.zeros(n, np.float32), n_extra=n_extra)
+    if n_extra:
+        c[:, 11:] = rng.uniform(-1, 1, size=(n, n_extra))
+    return c
+
+
+def test_field_eval_matches_oracle(gpu_avatar, field_setup, oracle):
+    fc, params = field_setup
+    c = random_coords(5000, seed=1)       # not a multiple of the 128-sample tile
+    out = torch.zeros((len(c), 4), dtype=torch.float32, device="cuda")
+    gpu_avatar.field_eval(0, dev(c), 11, len(c), out)
+    gpu_avatar.sync()
+    got = out.cpu().numpy()
+    ref = oracle.field_eval(fc, params, c)
+    err = np.abs(got - ref)
+    assert (err <= 4e-3 + 1e-2 * np.abs(ref)).all(), float(err.max())
+    ref64 = oracle.field_eval(fc, params, c, fp64=True)
+    assert np.abs(got - ref64).max() < 5e-2
+
+
+def test_field_eval_bf16(gpu_avatar, oracle):
+    from insta_gb300 import abi, synthetic as S
+    fc = S.FieldConfig()
+    params = S.field_params(fc, seed=2)
+    gpu_avatar.params_load(3, fc, params, precision=abi.PRECISION_BF16)
+    c = random_coords(1024, seed=9)
+    out = torch.zeros((len(c), 4), dtype=torch.float32, device="cuda")
+    gpu_avatar.field_eval(3, dev(c), 11, len(c), out)
+    gpu_avatar.sync()
+    ref = oracle.field_eval(fc, params, c, weight_format=1)
+    err = np.abs(out.cpu().numpy() - ref)
+    assert (err <= 3e-2 + 4e-2 * np.abs(ref)).all(), float(err.max())
+
+
+def render_pair(ctx, oracle, oracle_frame, avatar, fc, params, W, H, yaw=0.0, avatar_id=0):
+    from insta_gb300 import synthetic as S
+    cam, focal = S.camera(yaw, width=W, height=H)
+    req = ctx.render_desc(avatar_id, 0, W, H, focal, cam)
+    rgba = np.zeros((W * H, 4), np.float32)
+    depth = np.zeros(W * H, np.float32)
+    ctx.render(req, rgba, depth)
+    n = ctx.render_samples()
+    bits = oracle.occupancy(oracle_frame["def"], 0.015)
+    d = oracle.Deformation(oracle_frame["def"], oracle_frame["can"], oracle_frame["adj"], oracle_frame["bvh"])
+    rc = oracle.render_cfg(W, H, focal, cam, avatar.render_aabb())
+    r_rgba, r_depth, ns, total = oracle.render(rc, d, bits, fc, params)
+    return rgba, depth, n, r_rgba, r_depth, total
+
+
+def test_render_psnr(gpu_avatar, field_setup, oracle, oracle_frame, avatar):
+    fc, params = field_setup
+    gpu_avatar.occupancy_from_mesh(0, 0, 0.015)
+    rgba, depth, n, r_rgba, r_depth, total = render_pair(gpu_avatar, oracle, oracle_frame, avatar, fc, params, 96, 96, yaw=-12.0)
+    assert total > 1000
+    assert abs(n - total) <= max(2, total // 1000)
+    assert psnr(rgba, r_rgba) >= 45.0
+    hit = (r_rgba[:, 3] > 0.2) & (rgba[:, 3] > 0.2)
+    assert np.abs(depth[hit] - r_depth[hit]).max() < 1e-3
+
+
+def test_render_opaque_early_termination(gpu_avatar, oracle, oracle_frame, avatar):
+    """A dense field terminates rays early (composite_kernel_nerf :996-999)."""
+    from insta_gb300 import synthetic as S
+    fc = S.FieldConfig()
+    params = S.field_params(fc, seed=4, density_gain=60.0)
+    gpu_avatar.params_load(0, fc, params)
+    gpu_avatar.occupancy_from_mesh(0, 0, 0.015)
+    rgba, depth, n, r_rgba, r_depth, total = render_pair(gpu_avatar, oracle, oracle_frame, avatar, fc, params, 64, 64)
+    assert (r_rgba[:, 3] > 0.99).sum() > 100
+    assert psnr(rgba, r_rgba) >= 45.0
+    gpu_avatar.params_load(0, fc, S.field_params(fc, seed=0))
+
+
+def test_render_device_outputs(gpu_avatar, field_setup, oracle, avatar):
+    from insta_gb300 import synthetic as S
+    gpu_avatar.occupancy_from_mesh(0, 0, 0.015)
+    cam, focal = S.camera(0.0, width=32, height=32)
+    req = gpu_avatar.render_desc(0, 0, 32, 32, focal, cam)
+    rgba_h = np.zeros((32 * 32, 4), np.float32)
+    depth_h = np.zeros(32 * 32, np.float32)
+    gpu_avatar.render(req, rgba_h, depth_h)
+    rgba_d = torch.zeros((32 * 32, 4), device="cuda")
+    depth_d = torch.zeros(32 * 32, device="cuda")
+    gpu_avatar.render(req, rgba_d, depth_d)
+    gpu_avatar.sync()
+    assert (rgba_d.cpu().numpy() == rgba_h).all() and (depth_d.cpu().numpy() == depth_h).all()

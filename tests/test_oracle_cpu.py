@@ -1,0 +1,138 @@
+"""CPU checks: the oracle against itself and against properties of the reference algorithm,
+the synthetic workload, the parameter layout, and the C-ABI library's exports."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_synthetic_mesh_shape(avatar):
+    assert avatar.canonical.shape == (5122, 3)
+    assert avatar.faces.shape == (10240, 3)
+    # closed genus-0: every edge shared by exactly two faces
+    f = avatar.faces
+    e = np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), axis=1)
+    _, cnt = np.unique(e, axis=0, return_counts=True)
+    assert (cnt == 2).all()
+    assert set(np.unique(avatar.mask)) == {1, 2, 7, 15}
+
+
+def test_adjacency_matches_edge_sharing(oracle, avatar):
+    adj = oracle.adjacency(avatar.faces, avatar.n_verts)
+    assert adj.shape == (10240, 3)
+    assert (adj >= 0).all()   # closed mesh: three edge neighbours each
+    f = avatar.faces
+    for i in range(0, len(f), 997):
+        for j in adj[i]:
+            assert len(set(f[i]) & set(f[j])) == 2
+
+
+def test_bvh_exact_equals_brute_force(oracle, avatar, frame0, oracle_frame):
+    from insta_gb300 import synthetic as S
+    pts = S.shell_points(frame0, avatar.faces, 3000, seed=2)
+    bid, bd = oracle.nearest_brute(oracle_frame["def"], pts)
+    eid, ed = oracle_frame["bvh"].nearest(pts, exact=True)
+    assert (bid == eid).all() and (bd == ed).all()
+    # the reference rule (last in BVH order wins ties) gives the same distance
+    rid, rd = oracle_frame["bvh"].nearest(pts, exact=False)
+    assert (rd == bd).all()
+
+
+def test_ties_go_to_lowest_id(oracle):
+    """Duplicate and degenerate triangles: equal distances resolve to the lowest id."""
+    tri = np.array([[0.4, 0.4, 0.5], [0.6, 0.4, 0.5], [0.5, 0.6, 0.5]], np.float32)
+    verts = np.concatenate([tri, tri, [[0.5, 0.5, 0.5], [0.5, 0.5, 0.5], [0.5, 0.5, 0.5]]]).astype(np.float32)
+    faces = np.array([[3, 4, 5], [0, 1, 2], [6, 7, 8]], np.int32)   # face 0 and 1 coincide
+    tris = oracle.build_triangles(verts, None, faces, None)
+    pts = np.array([[0.5, 0.45, 0.52], [0.5, 0.45, 0.48]], np.float32)
+    ids, _ = oracle.nearest_brute(tris, pts)
+    assert (ids == 0).all()
+
+
+def test_fp64_twin_close(oracle, avatar, frame0, oracle_frame):
+    from insta_gb300 import synthetic as S
+    pts = S.shell_points(frame0, avatar.faces, 4000, seed=6)
+    d32 = oracle.Deformation(oracle_frame["def"], oracle_frame["can"], oracle_frame["adj"], oracle_frame["bvh"])
+    d64 = oracle.Deformation(oracle_frame["def"], oracle_frame["can"], oracle_frame["adj"], oracle_frame["bvh"], fp64=True)
+    _, a = d32.map_soa(pts)
+    _, b = d64.map_soa(pts)
+    assert np.abs(a - b).max() < 1e-6
+
+
+def test_identity_frame_maps_to_itself(oracle, avatar):
+    """A frame equal to the canonical mesh maps every point to itself (up to rounding)."""
+    from insta_gb300 import synthetic as S
+    can = oracle.build_triangles(avatar.canonical, None, avatar.faces, avatar.mask)
+    dtr = oracle.build_triangles(avatar.canonical, avatar.canonical, avatar.faces, avatar.mask)
+    adj = oracle.adjacency(avatar.faces, avatar.n_verts)
+    d = oracle.Deformation(dtr, can, adj, oracle.Bvh(dtr), disable_interp=True)
+    pts = S.shell_points(avatar.canonical, avatar.faces, 2000, seed=1)
+    _, out = d.map_soa(pts)
+    assert np.abs(out - pts).max() < 1e-6
+
+
+def test_layout_python_matches_oracle(oracle):
+    import ctypes as C
+    from insta_gb300 import layout, synthetic as S
+    for n_extra in (0, 16):
+        fc = S.FieldConfig(n_extra=n_extra)
+        lay = layout.field_layout(fc)
+        cfg = oracle.field_cfg(fc)
+        lo = (C.c_uint64 * 64)(); lr = (C.c_uint32 * 64)(); ls = (C.c_uint32 * 64)(); mo = (C.c_uint64 * 3)()
+        total = oracle.lib().orc_field_layout(C.byref(cfg), lo, lr, ls, mo)
+        assert total == lay.total
+        assert list(lr[:16]) == lay.level_res and list(ls[:16]) == lay.level_size
+
+
+def test_field_oracle_fp16_vs_fp64(oracle):
+    from insta_gb300 import synthetic as S
+    fc = S.FieldConfig()
+    params = S.field_params(fc, seed=0)
+    rng = np.random.default_rng(0)
+    c = np.zeros((256, 11), np.float32)
+    c[:, :3] = rng.uniform(0.35, 0.65, (256, 3))
+    c[:, 8:11] = 0.5
+    a = oracle.field_eval(fc, params, c)
+    b = oracle.field_eval(fc, params, c, fp64=True)
+    assert np.isfinite(a).all() and np.abs(a - b).max() < 5e-2
+
+
+def test_sobol_dimension_zero_is_bit_reversal(oracle):
+    lib = oracle.lib()
+    for i in (0, 1, 2, 3, 12345, 0xdeadbeef):
+        rev = int(f"{i:032b}"[::-1], 2)
+        assert lib.orc_sobol(i, 0) == rev
+    # dimension 1 direction numbers follow v_k = v_{k-1} ^ (v_{k-1} >> 1)
+    assert [lib.orc_sobol(1 << b, 1) for b in range(4)] == [0x80000000, 0xc0000000, 0xa0000000, 0xf0000000]
+
+
+def test_pixel_offset_spp0_is_centre(oracle):
+    off = oracle.pixel_offset(0)
+    assert np.abs(off - 0.5).max() < 1e-6
+
+
+def header_functions():
+    txt = (ROOT / "include" / "insta_gb300.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(insta_\w+)\s*\(", txt, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    from insta_gb300 import abi, build as B
+    lib_path = B.build()
+    lib = ctypes.CDLL(str(lib_path))
+    names = header_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(abi.EXPORTS) == names
+
+
+def test_param_count_without_gpu():
+    """insta_field_param_count is pure host code and agrees with the Python layout."""
+    from insta_gb300 import abi, layout, synthetic as S
+    fc = S.FieldConfig()
+    assert abi.param_count(fc) == layout.field_layout(fc).total
