@@ -1,0 +1,303 @@
+"""Benchmark: INSTA deformation + render hot path on GB300.
+
+Workload (one step = one frame): the 512x512 single-frame render of a tracked
+FLAME-topology-scale mesh -- device LBVH rebuild of the frame, occupancy bitfield
+from the mesh (cells within 1.5 cm), ray march with exponential stepping, per-sample
+canonical map, 16-level hash encode, density + colour MLPs (tcgen05), compositing.
+Metric: network samples per second (deform + encode + MLP), whole job.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+For N > 1 (launched by torchrun) every rank renders its own frames (replicas, no
+data-path collective); value = all ranks' samples / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "samples/s (deform+encode+MLP)"
+UNIT = "samples/s"
+WIDTH = HEIGHT = 512
+RADIUS = 0.015
+CONE = 1.0 / 256.0
+L2_FLUSH_BYTES = 512 << 20
+HASH_BYTES_PER_SAMPLE = 16 * 8 * 2 * 2            # 16 levels x 8 corners x F=2 x FP16
+MLP_FLOP_PER_SAMPLE = 2 * (32 * 64 + 64 * 16 + 32 * 64 + 64 * 64 + 64 * 3)
+KERNELS_PER_STEP = 1 + 1 + 1 + 7 + 1               # tri frames, BVH build, occupancy, 7 max-pools, render
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(rank: int):
+    from insta_gb300 import synthetic as S
+    av = S.make_avatar(0)
+    fc = S.FieldConfig()
+    params = S.field_params(fc, seed=0)
+    frames = [av.frame(av.frame_coeffs(1000 * rank + k)) for k in range(4)]
+    cams = [S.camera(yaw, width=WIDTH, height=HEIGHT) for yaw in (0.0, -8.0, 8.0, 15.0)]
+    return av, fc, params, frames, cams
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_render_rate(av, fc, params, frame, cam_focal, rows: int, threads: int | None = None):
+    """The CPU restatement of the path timed on the host cores for `rows` image rows."""
+    from oracle import oracle as O
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    cam, focal = cam_focal
+    can = O.build_triangles(av.canonical, None, av.faces, av.mask)
+    t0 = time.perf_counter()
+    dtr = O.build_triangles(frame, av.canonical, av.faces, av.mask)
+    adj = O.adjacency(av.faces, av.n_verts)
+    bvh = O.Bvh(dtr)
+    bits = O.occupancy(dtr, RADIUS)
+    setup = time.perf_counter() - t0
+    d = O.Deformation(dtr, can, adj, bvh)
+    rc = O.render_cfg(WIDTH, HEIGHT, focal, cam, av.render_aabb(), cone_angle=CONE)
+    r0 = (HEIGHT - rows) // 2
+    t0 = time.perf_counter()
+    _, _, _, total = O.render(rc, d, bits, fc, params, rows=(r0, r0 + rows))
+    dt = time.perf_counter() - t0
+    return total, dt, setup, O.num_threads()
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the path's CPU restatement on the host cores (the reference's own
+    CUDA path cannot be built: its tiny-cuda-nn and Eigen submodules are empty)."""
+    if rank != 0:
+        return
+    av, fc, params, frames, cams = workload(0)
+    rows = 32
+    for _ in range(args.warmup):
+        cpu_render_rate(av, fc, params, frames[0], cams[0], 8)
+    tot_s, tot_t = 0, 0.0
+    threads = 1
+    for k in range(args.steps):
+        s, t, _, threads = cpu_render_rate(av, fc, params, frames[k % len(frames)], cams[k % len(cams)], rows)
+        tot_s += s
+        tot_t += t
+    value = tot_s / tot_t
+    sample = f"{rows} central rows of the {WIDTH}x{HEIGHT} frame per step (encode+MLP+deform+march+composite), OpenMP"
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * tot_t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 geometry / fp16 mlp", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"render {WIDTH}x{HEIGHT}, 1 avatar, 10240-triangle tracked mesh, 16-level hash grid",
+                       "global_batch": 1, "parallelism": "cpu"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    from insta_gb300 import abi
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    av, fc, params, frames, cams = workload(rank)
+    stream = torch.cuda.Stream()
+    ctx = abi.Context(local, stream=stream.cuda_stream)
+    ctx.canonical_set(0, av.canonical, av.faces, av.mask)
+    ctx.params_load(0, fc, params)
+    frames_dev = [torch.from_numpy(f).cuda() for f in frames]
+    rgba = torch.empty((HEIGHT * WIDTH, 4), dtype=torch.float32, device="cuda")
+    depth = torch.empty(HEIGHT * WIDTH, dtype=torch.float32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    reqs = [ctx.render_desc(0, 0, WIDTH, HEIGHT, c[1], c[0], cone_angle=CONE) for c in cams]
+
+    def step(k):
+        ctx.frame_upload(0, 0, frames_dev[k % len(frames_dev)])
+        ctx.occupancy_from_mesh(0, 0, RADIUS)
+        ctx.render(reqs[k % len(reqs)], rgba, depth)
+
+    # a separate timing of the render kernel alone (the dominant kernel) on the same stream
+    def render_only(k):
+        ctx.render(reqs[k % len(reqs)], rgba, depth)
+
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup):
+            step(k)
+        ctx.sync()
+        samples_per_frame = []
+        for k in range(len(reqs)):
+            step(k)
+            samples_per_frame.append(ctx.render_samples())
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        rv = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        total_samples = 0
+        with ClockSampler(local) as clocks:
+            t_wall0 = time.perf_counter()
+            for k in range(args.steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                step(k)
+                ev[k][1].record(stream)
+                total_samples += samples_per_frame[k % len(reqs)]
+            stream.synchronize()
+            t_wall = time.perf_counter() - t_wall0
+            # render kernel alone (frame state resident), for the roofline
+            for k in range(args.steps):
+                flush.zero_()
+                rv[k][0].record(stream)
+                render_only(k)
+                rv[k][1].record(stream)
+            stream.synchronize()
+        step_ms = [a.elapsed_time(b) for a, b in ev]
+        render_ms = [a.elapsed_time(b) for a, b in rv]
+        ctx.sync()
+        # end to end through the C ABI with host buffers: H2D of the frame's vertices, D2H of RGBA + depth
+        host_rgba = torch.empty((HEIGHT * WIDTH, 4), dtype=torch.float32).pin_memory()
+        host_depth = torch.empty(HEIGHT * WIDTH, dtype=torch.float32).pin_memory()
+        host_frames = [torch.from_numpy(f).pin_memory() for f in frames]
+        e2e_samples = 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            ctx.frame_upload(0, 0, host_frames[k % len(host_frames)].numpy())
+            ctx.occupancy_from_mesh(0, 0, RADIUS)
+            ctx.render(reqs[k % len(reqs)], host_rgba.numpy(), host_depth.numpy())
+            e2e_samples += samples_per_frame[k % len(reqs)]
+        e2e_t = time.perf_counter() - t0
+
+    dev_t = sum(step_ms) / 1000.0
+    if dist:
+        t = torch.tensor([dev_t, e2e_t, float(total_samples), float(e2e_samples)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx[:2], op=dist.ReduceOp.MAX)
+        dist.all_reduce(mx[2:], op=dist.ReduceOp.SUM)
+        dev_t, e2e_t, total_samples, e2e_samples = [float(x) for x in mx.tolist()]
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    value = total_samples / dev_t
+    mean_samples = statistics.mean(samples_per_frame)
+    render_s = statistics.median(render_ms) / 1000.0
+    achieved = mean_samples * HASH_BYTES_PER_SAMPLE / render_s / 1e9
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    tflops_peak = peaks.get("bf16_tflops", 1900.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * dev_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32 geometry / fp16 mlp", "data": "synthetic",
+        "config": {"workload": f"render {WIDTH}x{HEIGHT}, 1 avatar, 10240-triangle tracked mesh rebuilt per frame, "
+                               f"occupancy from mesh (1.5 cm), 16-level hash grid T=2^19, MLPs 32-64-16 / 32-64-64-3",
+                   "global_batch": world, "samples_per_frame": mean_samples, "parallelism": f"replicas x{world}",
+                   "l2": "flushed (512 MiB write) between timed steps", "frames_per_s": args.steps * world / dev_t},
+        "roofline": {"bound": "hbm", "kernel": "render_kernel", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "basis": f"{HASH_BYTES_PER_SAMPLE} B hash-grid gathers per sample / median render-kernel time",
+                     "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"},
+        "roofline_tensor": {"achieved": mean_samples * MLP_FLOP_PER_SAMPLE / render_s / 1e12, "peak": tflops_peak,
+                            "unit": "TFLOP/s", "frac": mean_samples * MLP_FLOP_PER_SAMPLE / render_s / 1e12 / tflops_peak},
+        "render_kernel_ms": 1000.0 * render_s,
+        "e2e": {"value": e2e_samples / e2e_t, "unit": UNIT, "h2d_bytes_per_step": int(av.n_verts * 12),
+                "d2h_bytes_per_step": int(WIDTH * HEIGHT * 20)},
+        "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "clocks": clocks.summary(),
+        "wall_s_timed": t_wall,
+    }
+    if not args.no_cpu_baseline:
+        s, t, _, threads = cpu_render_rate(av, fc, params, frames[0], cams[0], 24)
+        line["cpu_baseline"] = {"value": s / t, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"24 central rows of the {WIDTH}x{HEIGHT} frame, CPU restatement, OpenMP"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

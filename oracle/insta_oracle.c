@@ -442,7 +442,7 @@ static uint32_t morton_invert(uint32_t x) {
 /* mark_flame_density_grid (ngp/src/testbed_nerf.cu:364-389) on the deformed mesh, then
  * grid_to_bitfield (:585-609, threshold min(0.01, mean) which keeps exactly the marked cells)
  * and bitfield_max_pool for mips 1..7 (:611-632).  bitfield: 8 * 128^3 / 8 bytes. */
-void orc_occupancy_from_mesh(const orc_tri *tris, int n_tris, float radius, uint8_t *bitfield) {
+void orc_occupancy_from_mesh(const orc_tri *tris, int n_tris, double radius, uint8_t *bitfield) {
     memset(bitfield, 0, GRID3 / 8 * 8);
     orc_tri *sorted = malloc(sizeof(orc_tri) * (size_t)n_tris);
     int max_nodes = 2 * n_tris + 16;
@@ -456,7 +456,7 @@ void orc_occupancy_from_mesh(const orc_tri *tris, int n_tris, float radius, uint
         for (int k = 0; k < 3; ++k) p[k] = (p[k] - 0.5f) * 1.0f + 0.5f;
         int32_t id; float d2;
         orc_nearest_bvh(nodes, sorted, p, 1, 1, &id, &d2);
-        if (id >= 0 && (double)sqrtf(d2) < (double)radius && tris[id].mask_id != 0u) mark[i] = 1;
+        if (id >= 0 && (double)sqrtf(d2) < radius && tris[id].mask_id != 0u) mark[i] = 1;
     }
     for (uint32_t b = 0; b < GRID3 / 8; ++b) {
         uint8_t bits = 0;

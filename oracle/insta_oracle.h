@@ -75,7 +75,7 @@ void orc_canonical_map_coords(const orc_deform *d, float *coords, uint32_t strid
                               uint32_t n_extra, int64_t n, int32_t frame_id, uint32_t n_frames);
 
 /* ---- occupancy --------------------------------------------------------- */
-void orc_occupancy_from_mesh(const orc_tri *tris, int n_tris, float radius, uint8_t *bitfield);
+void orc_occupancy_from_mesh(const orc_tri *tris, int n_tris, double radius, uint8_t *bitfield);
 uint32_t orc_morton3d(uint32_t x, uint32_t y, uint32_t z);
 
 /* ---- field (hash grid + SH + MLPs) ------------------------------------ */
