@@ -1,0 +1,173 @@
+// bvh.cuh -- exact nearest-triangle query over the per-frame 4-wide LBVH.
+//
+// Depth-first, nearest-child-first traversal (the order of closest_triangle,
+// NGP/bvh.cuh:48-96: child boxes sorted with the 4-input network, nearest popped
+// first).  Differences from the reference, both deliberate:
+//   * ties resolve to the lowest original triangle id (the reference keeps the last
+//     triangle in BVH order, which depends on the build);
+//   * a subtree is pruned only when its box distance exceeds best * (1 + 2^-10) + 1e-12,
+//     so a rounding-level difference between box and triangle distances can never hide
+//     the true minimum -- the result equals the brute-force minimum over all triangles.
+// The search can start from an upper bound: a known triangle (the previous sample of the
+// same ray) or a distance bound (occupancy marking).
+#pragma once
+
+#include "insta_types.h"
+
+namespace insta {
+
+struct Nearest {
+    int32_t id;     // original triangle id, -1 when nothing within the bound
+    int32_t slot;   // position in the frame's Morton-ordered triangle array
+    float d2;       // squared distance
+};
+
+__device__ __forceinline__ float prune_limit(float best) {
+    return isinf(best) ? best : __fadd_rn(__fadd_rn(best, __fmul_rn(best, 0.0009765625f)), 1e-12f);
+}
+
+// Exact squared distance of p to the triangle at Morton slot `slot`; its original id in `id`.
+__device__ __forceinline__ float slot_distance(const FrameView& fr, int32_t slot, V3 p, int32_t& id) {
+    const float4* tr = fr.leaf_tris + (size_t)slot * 3;
+    float4 q0 = __ldg(tr), q1 = __ldg(tr + 1), q2 = __ldg(tr + 2);
+    id = __float_as_int(q2.y);
+    return tri_distance_sq(v3(q0.x, q0.y, q0.z), v3(q0.w, q1.x, q1.y), v3(q1.z, q1.w, q2.x), p);
+}
+
+__device__ __forceinline__ Nearest nearest_bvh(const FrameView& fr, V3 p, float best, int32_t bid, int32_t bslot, uint32_t* err) {
+    uint32_t stack_r[INSTA_STACK];
+    float stack_d[INSTA_STACK];
+    int sp = 0;
+    stack_r[sp] = 0u;
+    stack_d[sp] = 0.f;
+    ++sp;
+    while (sp > 0) {
+        --sp;
+        const uint32_t ref = stack_r[sp];
+        if (stack_d[sp] > prune_limit(best)) continue;
+        if (ref & INSTA_LEAF_BIT) {
+            const uint32_t first = (ref & ~INSTA_LEAF_BIT) >> 3, count = ref & 7u;
+            for (uint32_t i = 0; i < count; ++i) {
+                int32_t id;
+                float d = slot_distance(fr, (int32_t)(first + i), p, id);
+                if (d < best || (d == best && (uint32_t)id < (uint32_t)bid)) { best = d; bid = id; bslot = (int32_t)(first + i); }
+            }
+            continue;
+        }
+        const float4* nd = fr.nodes + (size_t)ref * 7;
+        const float4 mnx = __ldg(nd + 0), mny = __ldg(nd + 1), mnz = __ldg(nd + 2);
+        const float4 mxx = __ldg(nd + 3), mxy = __ldg(nd + 4), mxz = __ldg(nd + 5);
+        const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
+        float cd[4];
+        uint32_t ci[4] = {(uint32_t)ch.x, (uint32_t)ch.y, (uint32_t)ch.z, (uint32_t)ch.w};
+        cd[0] = box_distance_sq(mnx.x, mny.x, mnz.x, mxx.x, mxy.x, mxz.x, p);
+        cd[1] = box_distance_sq(mnx.y, mny.y, mnz.y, mxx.y, mxy.y, mxz.y, p);
+        cd[2] = box_distance_sq(mnx.z, mny.z, mnz.z, mxx.z, mxy.z, mxz.z, p);
+        cd[3] = box_distance_sq(mnx.w, mny.w, mnz.w, mxx.w, mxy.w, mxz.w, p);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (ci[i] == 0xffffffffu) cd[i] = __int_as_float(0x7f800000);
+        // 4-input sorting network, descending (NGP/bvh.cuh:28-46): the nearest child is pushed last
+#define INSTA_CAS(x, y) if (cd[x] < cd[y]) { float td = cd[x]; cd[x] = cd[y]; cd[y] = td; uint32_t ti = ci[x]; ci[x] = ci[y]; ci[y] = ti; }
+        INSTA_CAS(0, 2) INSTA_CAS(1, 3) INSTA_CAS(0, 1) INSTA_CAS(2, 3) INSTA_CAS(1, 2)
+#undef INSTA_CAS
+        const float lim = prune_limit(best);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (ci[i] != 0xffffffffu && cd[i] <= lim) {
+                if (sp < INSTA_STACK) { stack_r[sp] = ci[i]; stack_d[sp] = cd[i]; ++sp; }
+                else if (err) atomicOr(err, INSTA_DEVERR_STACK);
+            }
+        }
+    }
+    return {bid, bslot, best};
+}
+
+// Warp-cooperative variant for spatially coherent queries (one point per lane, all 32 lanes call
+// it together).  The warp walks the union of the nodes its lanes need with one shared stack in
+// shared memory (`wstack`, INSTA_STACK entries per warp): a node is fetched once per warp, every
+// lane tests it against its own point and bound, and a child is pushed when any lane may find a
+// nearer triangle in it.  Each lane's result is exactly its own nearest triangle (the union
+// contains every node that lane's own traversal would visit); control flow stays uniform, so all
+// lanes issue together.  Lanes with active == false only ride along.
+__device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool active, uint32_t* wstack, uint32_t* err) {
+    const float INF = __int_as_float(0x7f800000);
+    float best = active ? INF : -INF;
+    int32_t bid = -1, bslot = -1;
+    float dstack[INSTA_STACK];
+    int sp = 0;
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) wstack[0] = 0u;
+    __syncwarp();
+    dstack[0] = active ? 0.f : INF;
+    sp = 1;
+    while (sp > 0) {
+        --sp;
+        const uint32_t ref = wstack[sp];
+        const bool need = dstack[sp] <= prune_limit(best);
+        if (!__any_sync(0xffffffffu, need)) continue;
+        if (ref & INSTA_LEAF_BIT) {
+            const uint32_t first = (ref & ~INSTA_LEAF_BIT) >> 3, count = ref & 7u;
+            for (uint32_t i = 0; i < count; ++i) {
+                int32_t id;
+                float d = slot_distance(fr, (int32_t)(first + i), p, id);
+                if (need && (d < best || (d == best && (uint32_t)id < (uint32_t)bid))) { best = d; bid = id; bslot = (int32_t)(first + i); }
+            }
+            continue;
+        }
+        const float4* nd = fr.nodes + (size_t)ref * 7;
+        const float4 mnx = __ldg(nd + 0), mny = __ldg(nd + 1), mnz = __ldg(nd + 2);
+        const float4 mxx = __ldg(nd + 3), mxy = __ldg(nd + 4), mxz = __ldg(nd + 5);
+        const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
+        float cd[4];
+        uint32_t ci[4] = {(uint32_t)ch.x, (uint32_t)ch.y, (uint32_t)ch.z, (uint32_t)ch.w};
+        cd[0] = box_distance_sq(mnx.x, mny.x, mnz.x, mxx.x, mxy.x, mxz.x, p);
+        cd[1] = box_distance_sq(mnx.y, mny.y, mnz.y, mxx.y, mxy.y, mxz.y, p);
+        cd[2] = box_distance_sq(mnx.z, mny.z, mnz.z, mxx.z, mxy.z, mxz.z, p);
+        cd[3] = box_distance_sq(mnx.w, mny.w, mnz.w, mxx.w, mxy.w, mxz.w, p);
+        const float lim = prune_limit(best);
+        // per child: the warp's smallest distance among lanes that need it (bits order like floats >= 0)
+        uint32_t key[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const bool want = ci[i] != 0xffffffffu && cd[i] <= lim;
+            key[i] = __reduce_min_sync(0xffffffffu, want ? __float_as_uint(cd[i]) : 0xffffffffu);
+        }
+        // push the needed children farthest-first so the warp pops the nearest next
+        uint32_t order[4] = {0, 1, 2, 3};
+#define INSTA_CASK(x, y) if (key[order[x]] < key[order[y]]) { uint32_t t = order[x]; order[x] = order[y]; order[y] = t; }
+        INSTA_CASK(0, 2) INSTA_CASK(1, 3) INSTA_CASK(0, 1) INSTA_CASK(2, 3) INSTA_CASK(1, 2)
+#undef INSTA_CASK
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint32_t c = order[i];
+            if (key[c] != 0xffffffffu) {
+                if (sp < INSTA_STACK) {
+                    __syncwarp();
+                    if ((threadIdx.x & 31) == 0) wstack[sp] = ci[c];
+                    __syncwarp();
+                    dstack[sp] = active ? cd[c] : INF;
+                    ++sp;
+                } else if (err && (threadIdx.x & 31) == 0) {
+                    atomicOr(err, INSTA_DEVERR_STACK);
+                }
+            }
+        }
+    }
+    return {bid, bslot, best};
+}
+
+// Unbounded exact nearest triangle.
+__device__ __forceinline__ Nearest nearest_triangle(const FrameView& fr, V3 p, uint32_t* err) {
+    return nearest_bvh(fr, p, __int_as_float(0x7f800000), -1, -1, err);
+}
+
+// Nearest triangle starting from the triangle at `slot` (e.g. the previous sample's).
+__device__ __forceinline__ Nearest nearest_from_slot(const FrameView& fr, V3 p, int32_t slot, uint32_t* err) {
+    if (slot < 0) return nearest_triangle(fr, p, err);
+    int32_t id;
+    float d = slot_distance(fr, slot, p, id);
+    return nearest_bvh(fr, p, d, id, slot, err);
+}
+
+}  // namespace insta

@@ -79,77 +79,11 @@ __device__ __forceinline__ float box_distance_sq(float mnx, float mny, float mnz
     return __fadd_rn(__fmul_rn(dx, dx), __fadd_rn(__fmul_rn(dy, dy), __fmul_rn(dz, dz)));
 }
 
-// -------------------------------------------------------------- nearest triangle
-// Exact nearest triangle in a per-frame implicit 4-ary BVH over Morton-ordered
-// triangles.  Ties go to the lowest original triangle id; pruning keeps a relative
-// slack of 2^-10 so a rounding-level difference between a box distance and a
-// triangle distance can never hide the true minimum.  `bound` > 0 restricts the
-// search to squared distances <= bound (returns id -1 when nothing is that close).
-struct NearestResult { int32_t id; float d2; };
+}  // namespace insta
 
-__device__ __forceinline__ float prune_limit(float best) {
-    return isinf(best) ? best : __fadd_rn(__fadd_rn(best, __fmul_rn(best, 0.0009765625f)), 1e-12f);
-}
+#include "bvh.cuh"
 
-__device__ __forceinline__ NearestResult nearest_triangle(const FrameView& fr, V3 p, float bound, uint32_t* err) {
-    float best = bound > 0.f ? bound : __int_as_float(0x7f800000);
-    int32_t bid = -1;
-    uint32_t stack_e[INSTA_STACK];
-    float stack_d[INSTA_STACK];
-    int sp = 0;
-    stack_e[sp] = 0u; stack_d[sp] = 0.f; ++sp;
-    const int D = fr.n_levels;
-    while (sp > 0) {
-        --sp;
-        uint32_t e = stack_e[sp];
-        float ed = stack_d[sp];
-        if (ed > prune_limit(best)) continue;
-        int k = (int)(e >> 24);
-        uint32_t j = e & 0xFFFFFFu;
-        if (k == D) {
-            const float4* tr = fr.leaf_tris + (size_t)j * 4 * 3;
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                uint32_t t = j * 4 + i;
-                if (t >= (uint32_t)fr.n_tris) break;
-                float4 q0 = __ldg(tr + i * 3 + 0), q1 = __ldg(tr + i * 3 + 1), q2 = __ldg(tr + i * 3 + 2);
-                int32_t id = __float_as_int(q2.y);
-                float d = tri_distance_sq(v3(q0.x, q0.y, q0.z), v3(q0.w, q1.x, q1.y), v3(q1.z, q1.w, q2.x), p);
-                if (d < best || (d == best && (uint32_t)id < (uint32_t)bid)) { best = d; bid = id; }
-            }
-        } else {
-            const float4* nd = fr.nodes + ((size_t)fr.level_off[k] + j) * 6;
-            float4 mnx = __ldg(nd + 0), mny = __ldg(nd + 1), mnz = __ldg(nd + 2);
-            float4 mxx = __ldg(nd + 3), mxy = __ldg(nd + 4), mxz = __ldg(nd + 5);
-            uint32_t child_cnt = (uint32_t)fr.level_cnt[k + 1];
-            float cd[4];
-            uint32_t ci[4];
-            cd[0] = box_distance_sq(mnx.x, mny.x, mnz.x, mxx.x, mxy.x, mxz.x, p);
-            cd[1] = box_distance_sq(mnx.y, mny.y, mnz.y, mxx.y, mxy.y, mxz.y, p);
-            cd[2] = box_distance_sq(mnx.z, mny.z, mnz.z, mxx.z, mxy.z, mxz.z, p);
-            cd[3] = box_distance_sq(mnx.w, mny.w, mnz.w, mxx.w, mxy.w, mxz.w, p);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                uint32_t cj = j * 4 + i;
-                ci[i] = ((uint32_t)(k + 1) << 24) | cj;
-                if (cj >= child_cnt) cd[i] = __int_as_float(0x7f800000);  // +inf: never pushed
-            }
-            // 4-input sorting network, descending (NGP/bvh.cuh:28-46) so the nearest pops first
-#define INSTA_CAS(x, y) if (cd[x] < cd[y]) { float td = cd[x]; cd[x] = cd[y]; cd[y] = td; uint32_t ti = ci[x]; ci[x] = ci[y]; ci[y] = ti; }
-            INSTA_CAS(0, 2) INSTA_CAS(1, 3) INSTA_CAS(0, 1) INSTA_CAS(2, 3) INSTA_CAS(1, 2)
-#undef INSTA_CAS
-            float lim = prune_limit(best);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                if (cd[i] <= lim && !isinf(cd[i])) {
-                    if (sp < INSTA_STACK) { stack_e[sp] = ci[i]; stack_d[sp] = cd[i]; ++sp; }
-                    else if (err) atomicOr(err, INSTA_DEVERR_STACK);
-                }
-            }
-        }
-    }
-    return {bid, best};
-}
+namespace insta {
 
 // ------------------------------------------------------------------ frame math
 // 4-term row product with the halving order (x0 + x1) + (x2 + x3).
@@ -491,7 +425,8 @@ __device__ __forceinline__ bool ray_next_sample(const RenderView& rv, const uint
 // 1, 2654435761, 805459861; trilinear weights; FP32 accumulation).
 __device__ __forceinline__ void hash_encode(const FieldView& fv, V3 x, float* out) {
     const __half2* table = reinterpret_cast<const __half2*>(fv.table);
-#pragma unroll 1
+    // levels unrolled by four so 32 independent gathers are in flight per thread
+#pragma unroll 4
     for (int l = 0; l < (int)fv.n_levels; ++l) {
         const float s = fv.level_scale[l];
         float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);

@@ -115,14 +115,16 @@ __global__ void tri_frame_kernel(int F, const float* __restrict__ verts, const i
 
 // --------------------------------------------------------------- BVH build (1 CTA)
 struct BvhBuildArgs {
-    int F, n_leaves, n_levels;
-    int level_off[INSTA_MAX_LEVELS + 1];
-    int level_cnt[INSTA_MAX_LEVELS + 1];
+    int F;
     const float* verts;
     const int32_t* faces;
     const TriFrame* frames;
     float4* leaf_tris;
-    float4* nodes;
+    float4* nodes;        // [max_nodes][7]
+    int2* node_range;     // scratch [max_nodes]
+    float* node_box;      // scratch [max_nodes][6]
+    int* n_nodes_out;
+    int max_nodes;
     int np2;
 };
 
@@ -131,13 +133,84 @@ __device__ __forceinline__ void box_union(float* b, const float* o) {
     b[3] = fmaxf(b[3], o[3]); b[4] = fmaxf(b[4], o[4]); b[5] = fmaxf(b[5], o[5]);
 }
 
-// Linear BVH: sort triangles by the 30-bit Morton code of their centroid (ties by id), then
-// group 4 consecutive triangles per leaf and 4 consecutive nodes per parent, bottom-up.
+// First position in [b, e) whose key has the highest bit in which keys[b] and keys[e-1] differ set:
+// the split of a binary radix tree over sorted Morton codes (Karras 2012).
+__device__ __forceinline__ int radix_split(const uint64_t* keys, int b, int e) {
+    const uint64_t x = keys[b], y = keys[e - 1];
+    if (x == y) return (b + e) >> 1;
+    const uint64_t m = 1ull << (63 - __clzll((long long)(x ^ y)));
+    int lo = b, hi = e - 1;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (keys[mid] & m) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+// Up to 4 child ranges of [b, e): split once, then split each half again if it is not a leaf.
+__device__ __forceinline__ int child_ranges(const uint64_t* keys, int b, int e, int2* out) {
+    const int m = radix_split(keys, b, e);
+    int n = 0;
+    const int2 h[2] = {make_int2(b, m), make_int2(m, e)};
+    for (int i = 0; i < 2; ++i) {
+        if (h[i].y - h[i].x > INSTA_LEAF_SIZE) {
+            const int q = radix_split(keys, h[i].x, h[i].y);
+            out[n++] = make_int2(h[i].x, q);
+            out[n++] = make_int2(q, h[i].y);
+        } else {
+            out[n++] = h[i];
+        }
+    }
+    return n;
+}
+
+// Block-wide exclusive scan of cnt[0, n) in place (1024 threads); returns the total.
+__device__ int block_scan(int* cnt, int n, int* warp_tot) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int per = (n + nt - 1) / nt;
+    const int b = tid * per, e = min(n, b + per);
+    int s = 0;
+    for (int i = b; i < e; ++i) s += cnt[i];
+    int incl = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((tid & 31) >= o) incl += v;
+    }
+    if ((tid & 31) == 31) warp_tot[tid >> 5] = incl;
+    __syncthreads();
+    if (tid < 32) {
+        int v = tid < (nt >> 5) ? warp_tot[tid] : 0;
+        int w = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, w, o);
+            if (tid >= o) w += u;
+        }
+        warp_tot[tid] = w - v;   // exclusive warp offsets
+        if (tid == 31) warp_tot[32] = w;
+    }
+    __syncthreads();
+    int run = warp_tot[tid >> 5] + incl - s;
+    for (int i = b; i < e; ++i) { int c = cnt[i]; cnt[i] = run; run += c; }
+    __syncthreads();
+    int total = warp_tot[32];
+    __syncthreads();
+    return total;
+}
+
+// LBVH: sort triangles by the 30-bit Morton code of their centroid (ties by id), build the
+// binary radix tree top-down level by level and collapse every two binary levels into one
+// 4-wide node; boxes are then filled bottom-up.  Leaves hold <= INSTA_LEAF_SIZE triangles
+// (N_PRIMITIVES_LEAF = 2 in src/tiny_mesh.cu:28-32).
 __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* keys = reinterpret_cast<uint64_t*>(smem_raw);
+    int* cnt = reinterpret_cast<int*>(smem_raw + (size_t)a.np2 * 8);   // per node of the current level
     __shared__ float red[6][32];
     __shared__ float ext[6];
+    __shared__ int warp_tot[33];
+    __shared__ int lvl_off[66];
+    __shared__ int n_levels;
     const int tid = threadIdx.x, nt = blockDim.x;
     // 1. centroid bounds
     float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
@@ -169,7 +242,7 @@ __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs a) {
             for (int k = 0; k < 3; ++k) { ext[k] = lo[k]; float e = hi[k] - lo[k]; ext[3 + k] = e > 0.f ? 1.f / e : 0.f; }
     }
     __syncthreads();
-    // 2. Morton keys
+    // 2. Morton keys (code << 32 | face id: unique)
     for (int i = tid; i < a.np2; i += nt) {
         uint64_t key = ~0ull;
         if (i < a.F) {
@@ -196,87 +269,124 @@ __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs a) {
             __syncthreads();
         }
     }
-    // 4. leaf triangle records in sorted order
-    for (int s = tid; s < a.n_leaves * 4; s += nt) {
+    // 4. triangle records in Morton order
+    for (int s = tid; s < a.F; s += nt) {
         float4* dst = a.leaf_tris + (size_t)s * 3;
-        if (s < a.F) {
-            uint32_t f = (uint32_t)(keys[s] & 0xffffffffu);
-            int i0 = a.faces[f * 3], i1 = a.faces[f * 3 + 1], i2 = a.faces[f * 3 + 2];
-            const float* A = a.verts + i0 * 3; const float* B = a.verts + i1 * 3; const float* C = a.verts + i2 * 3;
-            dst[0] = make_float4(A[0], A[1], A[2], B[0]);
-            dst[1] = make_float4(B[1], B[2], C[0], C[1]);
-            dst[2] = make_float4(C[2], __uint_as_float(f), 0.f, 0.f);
-        } else {
-            dst[0] = make_float4(0.f, 0.f, 0.f, 0.f); dst[1] = dst[0]; dst[2] = dst[0];
-        }
+        uint32_t f = (uint32_t)(keys[s] & 0xffffffffu);
+        int i0 = a.faces[f * 3], i1 = a.faces[f * 3 + 1], i2 = a.faces[f * 3 + 2];
+        const float* A = a.verts + i0 * 3; const float* B = a.verts + i1 * 3; const float* C = a.verts + i2 * 3;
+        dst[0] = make_float4(A[0], A[1], A[2], B[0]);
+        dst[1] = make_float4(B[1], B[2], C[0], C[1]);
+        dst[2] = make_float4(C[2], __uint_as_float(f), 0.f, 0.f);
+    }
+    // 5. topology, top-down, one level of 4-wide nodes at a time
+    if (tid == 0) {
+        a.node_range[0] = make_int2(0, a.F);
+        lvl_off[0] = 0;
+        lvl_off[1] = 1;
+        n_levels = 1;
     }
     __syncthreads();
-    // 5. boxes, bottom-up.  Region A (child boxes) and B (parent boxes) reuse the key buffer.
-    float* boxA = reinterpret_cast<float*>(smem_raw);
-    float* boxB = boxA + 6 * 4096;
-    for (int L = tid; L < a.n_leaves; L += nt) {
-        float b[6] = {3.4e38f, 3.4e38f, 3.4e38f, -3.4e38f, -3.4e38f, -3.4e38f};
-        for (int i = 0; i < 4; ++i) {
-            int s = L * 4 + i;
-            if (s >= a.F) break;
-            const float4* t = a.leaf_tris + (size_t)s * 3;
-            float4 q0 = t[0], q1 = t[1], q2 = t[2];
-            float pts[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
-            for (int p = 0; p < 3; ++p) {
-                float pb[6] = {pts[p * 3], pts[p * 3 + 1], pts[p * 3 + 2], pts[p * 3], pts[p * 3 + 1], pts[p * 3 + 2]};
-                box_union(b, pb);
+    for (int L = 0; L < 64; ++L) {
+        const int lb = lvl_off[L], le = lvl_off[L + 1];
+        if (lb == le) break;
+        for (int n = lb + tid; n < le; n += nt) {
+            int2 r = a.node_range[n];
+            int2 ch[4];
+            int nc = r.y - r.x > INSTA_LEAF_SIZE ? child_ranges(keys, r.x, r.y, ch) : 0;
+            if (nc == 0) { ch[0] = r; nc = 1; }   // a root that is already a leaf
+            int inner = 0;
+            for (int i = 0; i < nc; ++i) inner += (ch[i].y - ch[i].x > INSTA_LEAF_SIZE) ? 1 : 0;
+            cnt[n - lb] = inner;
+        }
+        __syncthreads();
+        const int total = block_scan(cnt, le - lb, warp_tot);
+        for (int n = lb + tid; n < le; n += nt) {
+            int2 r = a.node_range[n];
+            int2 ch[4];
+            int nc = r.y - r.x > INSTA_LEAF_SIZE ? child_ranges(keys, r.x, r.y, ch) : 0;
+            if (nc == 0) { ch[0] = r; nc = 1; }
+            int next = le + cnt[n - lb];
+            int refs[4] = {-1, -1, -1, -1};
+            for (int i = 0; i < nc; ++i) {
+                if (ch[i].y - ch[i].x > INSTA_LEAF_SIZE) {
+                    if (next < a.max_nodes) { a.node_range[next] = ch[i]; refs[i] = next; }
+                    ++next;
+                } else {
+                    refs[i] = (int)(INSTA_LEAF_BIT | ((uint32_t)ch[i].x << 3) | (uint32_t)(ch[i].y - ch[i].x));
+                }
             }
+            reinterpret_cast<int4*>(a.nodes)[(size_t)n * 7 + 6] = make_int4(refs[0], refs[1], refs[2], refs[3]);
         }
-        for (int k = 0; k < 6; ++k) boxA[L * 6 + k] = b[k];
+        __syncthreads();
+        if (tid == 0) {
+            lvl_off[L + 2] = min(le + total, a.max_nodes);
+            n_levels = L + 1;
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    float* child = boxA;
-    float* parent = boxB;
-    for (int lev = a.n_levels - 1; lev >= 0; --lev) {
-        int cnt = a.level_cnt[lev], ccnt = a.level_cnt[lev + 1];
-        for (int j = tid; j < cnt; j += nt) {
+    // 6. boxes, bottom-up
+    for (int L = n_levels - 1; L >= 0; --L) {
+        const int lb = lvl_off[L], le = lvl_off[L + 1];
+        for (int n = lb + tid; n < le; n += nt) {
+            const int4 refs = reinterpret_cast<const int4*>(a.nodes)[(size_t)n * 7 + 6];
+            const int rr[4] = {refs.x, refs.y, refs.z, refs.w};
             float mn[3][4], mx[3][4];
             float nb[6] = {3.4e38f, 3.4e38f, 3.4e38f, -3.4e38f, -3.4e38f, -3.4e38f};
             for (int i = 0; i < 4; ++i) {
-                int c = j * 4 + i;
-                if (c < ccnt) {
-                    for (int k = 0; k < 3; ++k) { mn[k][i] = child[c * 6 + k]; mx[k][i] = child[c * 6 + 3 + k]; }
-                    box_union(nb, &child[c * 6]);
-                } else {
-                    for (int k = 0; k < 3; ++k) { mn[k][i] = __int_as_float(0x7f800000); mx[k][i] = -__int_as_float(0x7f800000); }
+                float cb[6] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000),
+                               -__int_as_float(0x7f800000), -__int_as_float(0x7f800000), -__int_as_float(0x7f800000)};
+                if (rr[i] != -1) {
+                    if ((uint32_t)rr[i] & INSTA_LEAF_BIT) {
+                        const uint32_t first = ((uint32_t)rr[i] & ~(uint32_t)INSTA_LEAF_BIT) >> 3, count = (uint32_t)rr[i] & 7u;
+                        for (uint32_t t = first; t < first + count; ++t) {
+                            const float4* tr = a.leaf_tris + (size_t)t * 3;
+                            float4 q0 = tr[0], q1 = tr[1], q2 = tr[2];
+                            float pts[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+                            for (int p = 0; p < 3; ++p) {
+                                float pb[6] = {pts[p * 3], pts[p * 3 + 1], pts[p * 3 + 2], pts[p * 3], pts[p * 3 + 1], pts[p * 3 + 2]};
+                                box_union(cb, pb);
+                            }
+                        }
+                    } else {
+                        for (int k = 0; k < 6; ++k) cb[k] = a.node_box[(size_t)rr[i] * 6 + k];
+                    }
+                    box_union(nb, cb);
                 }
+                for (int k = 0; k < 3; ++k) { mn[k][i] = cb[k]; mx[k][i] = cb[3 + k]; }
             }
-            float4* nd = a.nodes + ((size_t)a.level_off[lev] + j) * 6;
+            float4* nd = a.nodes + (size_t)n * 7;
             for (int k = 0; k < 3; ++k) {
                 nd[k] = make_float4(mn[k][0], mn[k][1], mn[k][2], mn[k][3]);
                 nd[3 + k] = make_float4(mx[k][0], mx[k][1], mx[k][2], mx[k][3]);
             }
-            for (int k = 0; k < 6; ++k) parent[j * 6 + k] = nb[k];
+            for (int k = 0; k < 6; ++k) a.node_box[(size_t)n * 6 + k] = nb[k];
         }
         __syncthreads();
-        float* t = child; child = parent; parent = t;
     }
+    if (tid == 0) *a.n_nodes_out = lvl_off[n_levels];
 }
 
 // --------------------------------------------------------------------- occupancy
 // mark_flame_density_grid (ngp/src/testbed_nerf.cu:364-389) over the deformed mesh, fused with
-// grid_to_bitfield (:585-609): one thread per bitfield byte (8 Morton-consecutive cells).
-__global__ void occupancy_kernel(FrameView fr, double radius, float bound, uint8_t* __restrict__ bits, uint32_t* err) {
-    uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= GRID3 / 8) return;
-    uint8_t out = 0;
-    for (uint32_t j = 0; j < 8; ++j) {
-        uint32_t cell = b * 8 + j;
-        uint32_t x = morton_invert(cell), y = morton_invert(cell >> 1), z = morton_invert(cell >> 2);
-        V3 p = v3(__fdiv_rn((float)x + 0.5f, 128.f), __fdiv_rn((float)y + 0.5f, 128.f), __fdiv_rn((float)z + 0.5f, 128.f));
-        NearestResult r = nearest_triangle(fr, p, bound, err);
-        if (r.id >= 0) {
-            uint32_t m;
-            load_centroid(fr.frames, (uint32_t)r.id, &m);
-            if ((double)__fsqrt_rn(r.d2) < radius && m != 0u) out |= (uint8_t)(1u << j);
+// grid_to_bitfield (:585-609): one thread per bitfield byte (8 Morton-consecutive cells), each
+// cell a nearest-triangle query bounded by the marking radius.
+__global__ void __launch_bounds__(256) occupancy_kernel(FrameView fr, double radius, float bound, uint8_t* __restrict__ bits, uint32_t* err) {
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < GRID3 / 8; b += gridDim.x * blockDim.x) {
+        uint8_t out = 0;
+        for (uint32_t j = 0; j < 8; ++j) {
+            uint32_t cell = b * 8 + j;
+            uint32_t x = morton_invert(cell), y = morton_invert(cell >> 1), z = morton_invert(cell >> 2);
+            V3 p = v3(__fdiv_rn((float)x + 0.5f, 128.f), __fdiv_rn((float)y + 0.5f, 128.f), __fdiv_rn((float)z + 0.5f, 128.f));
+            Nearest r = nearest_bvh(fr, p, bound, -1, -1, err);
+            if (r.id >= 0) {
+                uint32_t m;
+                load_centroid(fr.frames, (uint32_t)r.id, &m);
+                if ((double)__fsqrt_rn(r.d2) < radius && m != 0u) out |= (uint8_t)(1u << j);
+            }
         }
+        bits[b] = out;
     }
-    bits[b] = out;
 }
 
 // bitfield_max_pool (:611-632) for one mip level; `next` must be zeroed.
@@ -290,46 +400,58 @@ __global__ void maxpool_kernel(const uint8_t* __restrict__ prev, uint8_t* __rest
 }
 
 // ---------------------------------------------------------------- canonical map
-__global__ void canonical_map_soa_kernel(FrameView fr, DeformView dv, const float* __restrict__ pts, int64_t n,
-                                         int32_t* __restrict__ out_idx, float* __restrict__ out_canon, uint32_t* err) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    V3 p = v3(pts[i * 3], pts[i * 3 + 1], pts[i * 3 + 2]);
-    NearestResult r = nearest_triangle(fr, p, 0.f, err);
-    out_idx[i] = r.id;
-    if (r.id < 0) {
-        atomicOr(err, INSTA_DEVERR_NO_TRI);
-        out_canon[i * 3] = p.x; out_canon[i * 3 + 1] = p.y; out_canon[i * 3 + 2] = p.z;
-        return;
+__global__ void __launch_bounds__(256) canonical_map_soa_kernel(FrameView fr, DeformView dv, const float* __restrict__ pts, int64_t n,
+                                                                int32_t* __restrict__ out_idx, float* __restrict__ out_canon, uint32_t* err) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        V3 p = v3(pts[i * 3], pts[i * 3 + 1], pts[i * 3 + 2]);
+        Nearest r = nearest_triangle(fr, p, err);
+        out_idx[i] = r.id;
+        if (r.id < 0) {
+            atomicOr(err, INSTA_DEVERR_NO_TRI);
+            out_canon[i * 3] = p.x; out_canon[i * 3 + 1] = p.y; out_canon[i * 3 + 2] = p.z;
+            continue;
+        }
+        float o[3];
+        map_to_canonical(dv, fr.frames, (uint32_t)r.id, p, nullptr, o, nullptr, nullptr);
+        out_canon[i * 3] = o[0]; out_canon[i * 3 + 1] = o[1]; out_canon[i * 3 + 2] = o[2];
     }
-    float o[3];
-    map_to_canonical(dv, fr.frames, (uint32_t)r.id, p, nullptr, o, nullptr, nullptr);
-    out_canon[i * 3] = o[0]; out_canon[i * 3 + 1] = o[1]; out_canon[i * 3 + 2] = o[2];
 }
 
-// warp (src/core.cu:442-526) in place on NerfCoordinate records (NGP/nerf.h:86-115).
-__global__ void canonical_map_coords_kernel(const FrameView* __restrict__ frames, uint32_t n_frames, DeformView dv,
-                                            float* __restrict__ coords, uint32_t stride, uint32_t n_extra, int64_t n,
-                                            int32_t frame_id, uint32_t* err) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float* c = coords + i * stride;
-    float holder = c[4];
-    if (holder < 0.f) return;
-    uint32_t fid = frame_id < 0 ? (uint32_t)holder : (uint32_t)frame_id;
-    if (fid >= n_frames) return;
-    V3 p = v3(c[0], c[1], c[2]);
-    if (!box_contains(dv.aabb_min, dv.aabb_max, p)) return;
-    const FrameView& fr = frames[fid];
-    NearestResult r = nearest_triangle(fr, p, 0.f, err);
-    if (r.id < 0) { atomicOr(err, INSTA_DEVERR_NO_TRI); return; }
-    float pos[3], dir[3], dw[3] = {c[8], c[9], c[10]};
-    uint32_t mask;
-    map_to_canonical(dv, fr.frames, (uint32_t)r.id, p, dw, pos, dir, &mask);
-    c[0] = pos[0]; c[1] = pos[1]; c[2] = pos[2];
-    c[8] = dir[0]; c[9] = dir[1]; c[10] = dir[2];
-    if (mask != 7u)
-        for (uint32_t m = 0; m < n_extra; ++m) c[stride - n_extra + m] = 1.f;
+// warp (src/core.cu:442-526) in place on NerfCoordinate records (NGP/nerf.h:86-115); the frame
+// is fixed (frame_id >= 0, render_deformed) or read from `holder` (surface_closest_point).
+__global__ void __launch_bounds__(256) canonical_map_coords_kernel(const FrameView* __restrict__ frames, uint32_t n_frames, DeformView dv,
+                                                                   float* __restrict__ coords, uint32_t stride, uint32_t n_extra, int64_t n,
+                                                                   int32_t frame_id, uint32_t* err) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float* c = coords + i * stride;
+        float holder = c[4];
+        if (holder < 0.f) continue;
+        uint32_t fid = frame_id < 0 ? (uint32_t)holder : (uint32_t)frame_id;
+        if (fid >= n_frames) continue;
+        V3 p = v3(c[0], c[1], c[2]);
+        if (!box_contains(dv.aabb_min, dv.aabb_max, p)) continue;
+        const FrameView& fr = frames[fid];
+        if (fr.n_tris == 0) continue;
+        Nearest r = nearest_triangle(fr, p, err);
+        if (r.id < 0) { atomicOr(err, INSTA_DEVERR_NO_TRI); continue; }
+        float pos[3], dir[3], dw[3] = {c[8], c[9], c[10]};
+        uint32_t mask;
+        map_to_canonical(dv, fr.frames, (uint32_t)r.id, p, dw, pos, dir, &mask);
+        c[0] = pos[0]; c[1] = pos[1]; c[2] = pos[2];
+        c[8] = dir[0]; c[9] = dir[1]; c[10] = dir[2];
+        if (mask != 7u)
+            for (uint32_t m = 0; m < n_extra; ++m) c[stride - n_extra + m] = 1.f;
+    }
+}
+
+static int sm_count_frames() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    return sms;
 }
 
 // ------------------------------------------------------------------- launchers
@@ -339,19 +461,22 @@ cudaError_t launch_tri_frames(int F, const float* verts, const int32_t* faces, c
     return cudaGetLastError();
 }
 
-cudaError_t launch_bvh_build(const FrameView& fv, int n_leaves, const float* verts, const int32_t* faces, cudaStream_t s) {
+size_t bvh_scratch_bytes(int F) { return (size_t)F * (sizeof(int2) + 6 * sizeof(float)) + 16; }
+
+cudaError_t launch_bvh_build(const FrameView& fv, const float* verts, const int32_t* faces, void* scratch, cudaStream_t s) {
     BvhBuildArgs a;
-    a.F = fv.n_tris; a.n_leaves = n_leaves; a.n_levels = fv.n_levels;
-    for (int k = 0; k <= INSTA_MAX_LEVELS; ++k) { a.level_off[k] = fv.level_off[k]; a.level_cnt[k] = fv.level_cnt[k]; }
+    a.F = fv.n_tris;
     a.verts = verts; a.faces = faces; a.frames = fv.frames;
-    a.leaf_tris = const_cast<float4*>(fv.leaf_tris); a.nodes = const_cast<float4*>(fv.nodes);
-    int np2 = 1;
+    a.leaf_tris = const_cast<float4*>(fv.leaf_tris);
+    a.nodes = const_cast<float4*>(fv.nodes);
+    a.max_nodes = fv.n_nodes;
+    a.node_range = reinterpret_cast<int2*>(scratch);
+    a.node_box = reinterpret_cast<float*>(reinterpret_cast<char*>(scratch) + (size_t)fv.n_tris * sizeof(int2));
+    a.n_nodes_out = reinterpret_cast<int*>(reinterpret_cast<char*>(scratch) + (size_t)fv.n_tris * (sizeof(int2) + 6 * sizeof(float)));
+    int np2 = 2;
     while (np2 < fv.n_tris) np2 <<= 1;
-    if (np2 < 2) np2 = 2;
     a.np2 = np2;
-    size_t keys_bytes = (size_t)np2 * 8;
-    size_t box_bytes = (size_t)(4096 + 1366) * 6 * 4;
-    size_t smem = keys_bytes > box_bytes ? keys_bytes : box_bytes;
+    size_t smem = (size_t)np2 * 8 + (size_t)fv.n_tris * 4 + 16;
     cudaError_t e = cudaFuncSetAttribute(bvh_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     bvh_build_kernel<<<1, 1024, smem, s>>>(a);
@@ -362,7 +487,7 @@ cudaError_t launch_occupancy(const FrameView& fv, double radius, uint8_t* bitfie
     cudaError_t e = cudaMemsetAsync(bitfield + GRID3 / 8, 0, (size_t)7 * GRID3 / 8, s);
     if (e != cudaSuccess) return e;
     float bound = (float)(radius * radius * 1.0001);
-    occupancy_kernel<<<(GRID3 / 8 + 255) / 256, 256, 0, s>>>(fv, radius, bound, bitfield, err);
+    occupancy_kernel<<<sm_count_frames() * 8, 256, 0, s>>>(fv, radius, bound, bitfield, err);
     for (int lvl = 1; lvl < 8; ++lvl)
         maxpool_kernel<<<(GRID3 / 64 + 255) / 256, 256, 0, s>>>(bitfield + (size_t)(lvl - 1) * GRID3 / 8, bitfield + (size_t)lvl * GRID3 / 8);
     return cudaGetLastError();
@@ -371,14 +496,18 @@ cudaError_t launch_occupancy(const FrameView& fv, double radius, uint8_t* bitfie
 cudaError_t launch_canonical_map_soa(const FrameView& fv, const DeformView& dv, const float* pts, int64_t n, int32_t* out_idx,
                                      float* out_canon, uint32_t* err, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    canonical_map_soa_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(fv, dv, pts, n, out_idx, out_canon, err);
+    int64_t blocks = (n + 255) / 256;
+    int grid = (int)(blocks < sm_count_frames() * 16 ? blocks : sm_count_frames() * 16);
+    canonical_map_soa_kernel<<<grid, 256, 0, s>>>(fv, dv, pts, n, out_idx, out_canon, err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_canonical_map_coords(const FrameView* frames_dev, uint32_t n_frames, const DeformView& dv, float* coords,
                                         uint32_t stride, uint32_t n_extra, int64_t n, int32_t frame_id, uint32_t* err, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    canonical_map_coords_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(frames_dev, n_frames, dv, coords, stride, n_extra, n, frame_id, err);
+    int64_t blocks = (n + 255) / 256;
+    int grid = (int)(blocks < sm_count_frames() * 16 ? blocks : sm_count_frames() * 16);
+    canonical_map_coords_kernel<<<grid, 256, 0, s>>>(frames_dev, n_frames, dv, coords, stride, n_extra, n, frame_id, err);
     return cudaGetLastError();
 }
 

@@ -14,7 +14,7 @@
 
 #include "../../include/insta_gb300.h"
 #include "device_common.cuh"
-#include "umma.cuh"
+#include "mlp_tiles.cuh"
 #include "kernels.h"
 
 using namespace insta;
@@ -51,7 +51,6 @@ struct DevBuf {
 struct Frame {
     DevBuf verts, frames, leaf_tris, nodes, bitfield;
     FrameView view{};
-    int n_leaves = 0;
     bool has_occupancy = false;
 };
 
@@ -59,9 +58,16 @@ struct Field {
     bool ready = false;
     insta_field_desc desc{};
     DevBuf params, image;
-    MlpPlan plan{};
+    TilePlan plan{};
     FieldView view{};
     uint64_t n_params = 0;
+};
+
+// Device scratch of the render wavefront, sized for the largest request seen.
+struct Wave {
+    DevBuf rays[2][4], n_round, round_base, sample_ray, samples, tiles, aux, out, out_f32, counters;
+    uint32_t cap_rays = 0;
+    uint64_t cap_samples = 0;
 };
 
 struct Avatar {
@@ -88,9 +94,10 @@ struct insta_ctx {
     uint32_t* err_dev = nullptr;
     uint32_t* ray_counter = nullptr;
     unsigned long long* sample_counter = nullptr;
-    DevBuf out_rgba, out_depth, extra;
+    DevBuf out_rgba, out_depth, extra, bvh_scratch;
+    Wave wave;
+    uint32_t* host_counters = nullptr;   // pinned: alive-ray counts read between rounds
     int sms = 0;
-    int render_ctas = 0;
 
     void* alloc(DevBuf& b, size_t bytes) {
         if (b.p && b.bytes >= bytes) return b.p;
@@ -187,29 +194,6 @@ bool is_device_ptr(const void* p) {
         return false;
     }
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
-}
-
-// Implicit 4-ary tree shape: leaves of 4 Morton-consecutive triangles, 4 nodes per parent.
-void tree_shape(int F, FrameView& v, int& n_leaves, int& n_internal) {
-    n_leaves = std::max(1, (F + 3) / 4);
-    std::vector<int> cnt;
-    int c = n_leaves;
-    do {
-        c = (c + 3) / 4;
-        cnt.push_back(c);
-    } while (c > 1);
-    std::reverse(cnt.begin(), cnt.end());
-    v.n_levels = (int)cnt.size();
-    if (v.n_levels > INSTA_MAX_LEVELS) fail(INSTA_ERR_UNSUPPORTED, "mesh too large for the BVH level table");
-    int off = 0;
-    for (int k = 0; k < v.n_levels; ++k) {
-        v.level_off[k] = off;
-        v.level_cnt[k] = cnt[k];
-        off += cnt[k];
-    }
-    v.level_off[v.n_levels] = off;
-    v.level_cnt[v.n_levels] = n_leaves;
-    n_internal = off;
 }
 
 float level_scale_host(float b, uint32_t base, uint32_t l) { return exp2f((float)l * log2f(b)) * (float)base - 1.0f; }
@@ -375,6 +359,13 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     ctx->release(ctx->out_rgba);
     ctx->release(ctx->out_depth);
     ctx->release(ctx->extra);
+    ctx->release(ctx->bvh_scratch);
+    Wave& w = ctx->wave;
+    for (int b = 0; b < 2; ++b)
+        for (int k = 0; k < 4; ++k) ctx->release(w.rays[b][k]);
+    for (DevBuf* b : {&w.n_round, &w.round_base, &w.sample_ray, &w.samples, &w.tiles, &w.aux, &w.out, &w.out_f32, &w.counters})
+        ctx->release(*b);
+    if (ctx->host_counters) cudaFreeHost(ctx->host_counters);
     cudaFree(ctx->err_dev);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -457,21 +448,22 @@ int insta_frame_upload(insta_ctx* ctx, int avatar, int frame, const float* verts
         Avatar& a = ctx->avatar(avatar);
         if (!verts || frame < 0) fail(INSTA_ERR_INVALID_ARG, "bad frame upload");
         Frame& f = a.frames[frame];
-        int n_leaves, n_internal;
-        tree_shape(a.F, f.view, n_leaves, n_internal);
-        f.n_leaves = n_leaves;
+        // an LBVH with leaves of <= 2 triangles has at most F - 1 internal nodes
+        const int max_nodes = std::max(1, a.F);
         ctx->alloc(f.verts, (size_t)a.V * 12);
         ctx->alloc(f.frames, (size_t)a.F * sizeof(TriFrame));
-        ctx->alloc(f.leaf_tris, (size_t)n_leaves * 4 * 48);
-        ctx->alloc(f.nodes, (size_t)n_internal * 96);
+        ctx->alloc(f.leaf_tris, (size_t)a.F * 48);
+        ctx->alloc(f.nodes, (size_t)max_nodes * 112);
+        ctx->alloc(ctx->bvh_scratch, bvh_scratch_bytes(a.F));
         host_copy(f.verts.p, verts, (size_t)a.V * 12, ctx->stream);
         f.view.leaf_tris = static_cast<const float4*>(f.leaf_tris.p);
         f.view.nodes = static_cast<const float4*>(f.nodes.p);
         f.view.frames = static_cast<const TriFrame*>(f.frames.p);
         f.view.n_tris = a.F;
+        f.view.n_nodes = max_nodes;
         CK(launch_tri_frames(a.F, (const float*)f.verts.p, (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
                              (const float*)a.canon_area.p, nullptr, (TriFrame*)f.frames.p, 1, ctx->stream));
-        CK(launch_bvh_build(f.view, n_leaves, (const float*)f.verts.p, (const int32_t*)a.faces.p, ctx->stream));
+        CK(launch_bvh_build(f.view, (const float*)f.verts.p, (const int32_t*)a.faces.p, ctx->bvh_scratch.p, ctx->stream));
         f.has_occupancy = false;
         a.table_dirty = true;
     });
@@ -539,7 +531,6 @@ int insta_canonical_map(insta_ctx* ctx, int avatar, int frame, float* coords, ui
             a.table_dirty = false;
         }
         if (frame >= 0) get_frame(a, frame);
-        for (auto& kv : a.frames) (void)kv;
         CK(launch_canonical_map_coords((const FrameView*)a.frame_table.p, a.table_frames, deform_view(a), coords, stride, n_extra, n,
                                        frame, ctx->err_dev, ctx->stream));
     });
@@ -576,30 +567,39 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
         fd.n_params = n_params;
         ctx->alloc(fd.params, n_params * 2);
         host_copy(fd.params.p, params, n_params * 2, ctx->stream);
-        // MLP weight image in the tensor-core operand layout (umma.cuh), one tile per layer
+        // MLP weight image in the tensor-core operand layout (umma.cuh), one B tile per operand
         std::vector<uint16_t> mlp(L.table_off);
         CK(cudaMemcpyAsync(mlp.data(), params, L.table_off * 2, cudaMemcpyDefault, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
-        MlpPlan plan{};
-        plan.n_density = (uint32_t)L.n_density;
-        plan.n_rgb = (uint32_t)L.n_rgb;
+        TilePlan plan{};
         uint32_t off = 0;
         std::vector<uint8_t> image;
-        for (int l = 0; l < L.n_density + L.n_rgb; ++l) {
-            uint32_t N = L.layer_n[l], Kin = L.layer_k[l], K = (Kin + 15) / 16 * 16;
-            plan.layer[l] = {off, N, K};
+        // copy columns [k0, k0 + K) of layer l ([N][Kin] row-major) into a [N][K] operand tile
+        auto add_tile = [&](int l, uint32_t k0, uint32_t K) -> uint32_t {
+            const uint32_t N = L.layer_n[l], Kin = L.layer_k[l];
+            const uint32_t at = off;
             image.resize(off + (size_t)N * K * 2, 0);
             for (uint32_t n = 0; n < N; ++n)
-                for (uint32_t k = 0; k < Kin; ++k) {
-                    uint16_t w = mlp[L.layer_off[l] + (uint64_t)n * Kin + k];
+                for (uint32_t k = 0; k < K && k0 + k < Kin; ++k) {
+                    uint16_t w = mlp[L.layer_off[l] + (uint64_t)n * Kin + k0 + k];
                     if (desc->precision == INSTA_PRECISION_BF16) w = half_to_bf16_bits(w);
-                    std::memcpy(&image[off + tile_offset(n, k, K)], &w, 2);
+                    std::memcpy(&image[at + tile_offset(n, k, K)], &w, 2);
                 }
-            off += N * K * 2;
-            off = (off + 127) / 128 * 128;
-        }
-        plan.bytes = off;
+            off = (off + N * K * 2 + 127) / 128 * 128;
+            return at;
+        };
         plan.k_in = (L.layer_k[0] + 15) / 16 * 16;
+        plan.n_dh = (uint32_t)L.n_density - 1;
+        for (uint32_t l = 0; l < plan.n_dh; ++l) plan.d_off[l] = add_tile((int)l, 0, l == 0 ? plan.k_in : 64);
+        plan.d_out = add_tile(L.n_density - 1, 0, 64);
+        const int r0 = L.n_density;
+        plan.r0_dens = add_tile(r0, 0, 16);
+        plan.r0_sh = add_tile(r0, 16, 16);
+        plan.n_rh = (uint32_t)L.n_rgb - 1;
+        for (uint32_t l = 1; l < plan.n_rh; ++l) plan.r_off[l] = add_tile(r0 + (int)l, 0, 64);
+        plan.r_out = add_tile(r0 + L.n_rgb - 1, 0, 64);
+        plan.bytes = off;
+        plan.tile_bytes = hash_tile_bytes(plan.k_in) + sh_tile_bytes();
         if (plan.bytes > 64 * 1024) fail(INSTA_ERR_UNSUPPORTED, "MLP weights exceed 64 KiB of shared memory");
         ctx->alloc(fd.image, image.size());
         CK(cudaMemcpyAsync(fd.image.p, image.data(), image.size(), cudaMemcpyHostToDevice, ctx->stream));
@@ -622,7 +622,6 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
         v.precision = (int)desc->precision;
         CK(cudaStreamSynchronize(ctx->stream));
         fd.ready = true;
-        ctx->render_ctas = 0;
     });
 }
 
@@ -632,7 +631,20 @@ int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t s
         if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", avatar);
         if (n < 0 || (n > 0 && (!coords || !out4))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
         if (stride < 11 + a.field.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
-        CK(launch_field_eval(a.field.view, a.field.plan, coords, stride, n, out4, ctx->err_dev, ctx->stream));
+        if (n == 0) return;
+        const TilePlan& P = a.field.plan;
+        const uint64_t tiles = ((uint64_t)n + 127) / 128;
+        Wave& w = ctx->wave;
+        ctx->alloc(w.tiles, tiles * P.tile_bytes);
+        ctx->alloc(w.out, tiles * 128 * sizeof(uint2));
+        ctx->alloc(w.out_f32, tiles * 128 * sizeof(float4));
+        CK(cudaMemsetAsync(w.tiles.p, 0, tiles * P.tile_bytes, ctx->stream));
+        CK(launch_encode_coords(a.field.view, coords, stride, n, (uint8_t*)w.tiles.p, P.tile_bytes, P.k_in, ctx->stream));
+        MlpArgs m{};
+        m.fv = a.field.view; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.steps = 1; m.n_samples = n;
+        m.out = (uint2*)w.out.p; m.out_f32 = (float4*)w.out_f32.p; m.err = ctx->err_dev;
+        CK(launch_mlp(m, (uint32_t)tiles, ctx->stream));
+        CK(launch_unpack((const uint2*)w.out.p, (const float4*)w.out_f32.p, a.field.view.precision == 1, n, (float4*)out4, ctx->stream));
     });
 }
 
@@ -660,23 +672,82 @@ int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, 
             CK(cudaMemcpyAsync(ctx->extra.p, e.data(), e.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
             extra = (const float*)ctx->extra.p;
         }
-        if (!ctx->render_ctas) ctx->render_ctas = render_ctas_per_sm(a.field.plan);
-        RenderLaunch L{};
-        L.rv = render_view(a, *req);
-        L.fr = f.view;
-        L.dv = deform_view(a);
-        L.fv = a.field.view;
-        L.plan = &a.field.plan;
-        L.bitfield = (const uint8_t*)f.bitfield.p;
-        L.extra_dims = extra;
-        L.out_rgba = rgba;
-        L.out_depth = depth;
-        L.ray_counter = ctx->ray_counter;
-        L.sample_counter = ctx->sample_counter;
-        L.err = ctx->err_dev;
-        L.grid = ctx->sms * ctx->render_ctas;
+        // scratch: two alive-ray lists, per-round samples (STEPS per ray), encoded tiles, outputs
+        const uint32_t STEPS = 32;
+        const TilePlan& P = a.field.plan;
+        Wave& w = ctx->wave;
+        const uint32_t nr = (uint32_t)npix;
+        const uint64_t cap_samples = (uint64_t)((nr + 127) / 128 * 128) * STEPS;
+        if (w.cap_rays < nr) {
+            for (int b = 0; b < 2; ++b)
+                for (int k = 0; k < 4; ++k) ctx->alloc(w.rays[b][k], (size_t)nr * 16);
+            ctx->alloc(w.n_round, (size_t)nr * 4);
+            ctx->alloc(w.round_base, (size_t)nr * 4);
+            w.cap_rays = nr;
+        }
+        ctx->alloc(w.tiles, cap_samples / 128 * P.tile_bytes);
+        ctx->alloc(w.aux, cap_samples * sizeof(float2));
+        ctx->alloc(w.samples, cap_samples * sizeof(float4));
+        ctx->alloc(w.sample_ray, cap_samples * sizeof(uint32_t));
+        ctx->alloc(w.out, cap_samples * sizeof(uint2));
+        if (a.field.view.precision == 1) ctx->alloc(w.out_f32, cap_samples * sizeof(float4));
+        ctx->alloc(w.counters, 64);
+        if (!ctx->host_counters) CK(cudaMallocHost(&ctx->host_counters, 64));
+        uint32_t* n_alive = (uint32_t*)w.counters.p;   // [0], [1]: ping-pong alive counts; [2]: samples this round
+        WaveArgs W{};
+        W.rv = render_view(a, *req);
+        W.fr = f.view;
+        W.dv = deform_view(a);
+        W.fv = a.field.view;
+        W.bitfield = (const uint8_t*)f.bitfield.p;
+        W.extra_dims = extra;
+        W.out_rgba = rgba;
+        W.out_depth = depth;
+        W.steps = STEPS;
+        W.tiles = (uint8_t*)w.tiles.p;
+        W.tile_bytes = P.tile_bytes;
+        W.k_in = P.k_in;
+        W.aux = (float2*)w.aux.p;
+        W.samples = (float4*)w.samples.p;
+        W.sample_ray = (uint32_t*)w.sample_ray.p;
+        W.round_base = (uint32_t*)w.round_base.p;
+        W.out = (const uint2*)w.out.p;
+        W.out_f32 = (const float4*)w.out_f32.p;
+        W.n_round = (uint32_t*)w.n_round.p;
+        W.sample_counter = ctx->sample_counter;
+        W.err = ctx->err_dev;
+        auto rays = [&](int b) {
+            return RayBuf{(float4*)w.rays[b][0].p, (float4*)w.rays[b][1].p, (float4*)w.rays[b][2].p, (float4*)w.rays[b][3].p};
+        };
+        MlpArgs M{};
+        M.fv = a.field.view; M.plan = P; M.tiles = W.tiles; M.steps = STEPS;
+        M.out = (uint2*)w.out.p; M.out_f32 = (float4*)w.out_f32.p; M.err = ctx->err_dev;
         CK(cudaMemsetAsync(ctx->sample_counter, 0, sizeof(unsigned long long), ctx->stream));
-        CK(launch_render(L, ctx->stream));
+        CK(cudaMemsetAsync(n_alive, 0, 8, ctx->stream));
+        W.rays_out = rays(0);
+        W.n_alive_out = n_alive;
+        CK(launch_ray_init(W, ctx->stream));
+        int cur = 0;
+        const uint32_t max_rounds = (W.rv.max_samples_per_ray + STEPS - 1) / STEPS + 1;
+        for (uint32_t round = 0; round < max_rounds; ++round) {
+            W.rays_in = rays(cur);
+            W.rays_out = rays(cur ^ 1);
+            W.n_alive_in = n_alive + cur;
+            W.n_alive_out = n_alive + (cur ^ 1);
+            CK(cudaMemsetAsync(n_alive + (cur ^ 1), 0, 4, ctx->stream));
+            CK(cudaMemsetAsync(n_alive + 2, 0, 4, ctx->stream));
+            W.n_samples_round = n_alive + 2;
+            CK(launch_march(W, ctx->stream));
+            CK(launch_deform_encode(W, ctx->stream));
+            M.n_alive = W.n_samples_round;
+            CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream));
+            CK(launch_composite(W, ctx->stream));
+            cur ^= 1;
+            // the host learns the alive count after each round; rounds stop once no ray is left
+            CK(cudaMemcpyAsync(ctx->host_counters, n_alive + cur, 4, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            if (ctx->host_counters[0] == 0) break;
+        }
         if (!dev_out) {
             CK(cudaMemcpyAsync(out_rgba, rgba, npix * 16, cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaMemcpyAsync(out_depth, depth, npix * 4, cudaMemcpyDeviceToHost, ctx->stream));

@@ -18,20 +18,20 @@ namespace insta {
 
 struct TriFrame;
 
-// Per-frame deformed mesh: implicit 4-ary BVH over Morton-ordered triangles.
-//   leaf_tris: [n_leaves*4][3] float4 -- (a.xyz, b.x) (b.yz, c.xy) (c.z, id bits, 0, 0)
-//   nodes:     [n_internal][6] float4 -- child boxes SoA: min.x[4] min.y[4] min.z[4] max.x[4] max.y[4] max.z[4]
-//   internal level k (root = 0) holds level_cnt[k] nodes starting at level_off[k];
-//   level n_levels is the leaf level (level_cnt[n_levels] = n_leaves).
-//   Children of node (k, j) are (k + 1, 4j .. 4j + 3).
+// Per-frame deformed mesh: 4-wide LBVH over Morton-ordered triangles.
+//   leaf_tris: [n_tris][3] float4 in Morton order -- (a.xyz, b.x) (b.yz, c.xy) (c.z, id bits, 0, 0)
+//   nodes:     [n_nodes][7] float4 -- child boxes SoA (min.x[4] min.y[4] min.z[4] max.x[4] max.y[4]
+//              max.z[4]) and the four child references (int bits): >= 0 internal node index,
+//              INSTA_LEAF_BIT | (first slot << 3) | count for a leaf, -1 for an empty slot.
+//   Node 0 is the root.
+#define INSTA_LEAF_BIT 0x40000000
+#define INSTA_LEAF_SIZE 2
 struct FrameView {
     const float4* leaf_tris;
     const float4* nodes;
     const TriFrame* frames;   // per original triangle, see device_common.cuh
     int n_tris;
-    int n_levels;
-    int level_off[INSTA_MAX_LEVELS + 1];
-    int level_cnt[INSTA_MAX_LEVELS + 1];
+    int n_nodes;
 };
 
 struct DeformView {

@@ -1,0 +1,175 @@
+// mlp_tiles.cuh -- the avatar MLPs on 128-sample tiles with tcgen05 (M = 128, FP32 accumulators
+// in TMEM).  Inputs arrive as ready-made operand tiles in global memory (written by the encode
+// stage in the no-swizzle K-major core-matrix layout of umma.cuh) and are moved into shared
+// memory by bulk (TMA) copies, double-buffered so tile t+1 loads while tile t computes.
+#pragma once
+
+#include "umma.cuh"
+
+namespace insta {
+
+// Weight image layout (each entry one B-operand tile, byte offset into the image):
+//   d[0 .. n_dh]      density hidden layers  (N = 64, K = k_in then 64)
+//   d_out             density output         (N = 16, K = 64)
+//   r0_dens, r0_sh    colour layer 0 split by input columns (N = 64, K = 16 each)
+//   r[0 .. n_rh-1)    further colour hidden layers (N = 64, K = 64)
+//   r_out             colour output, padded  (N = 16, K = 64)
+struct TilePlan {
+    uint32_t d_off[4];
+    uint32_t n_dh;        // density hidden layers
+    uint32_t d_out;
+    uint32_t r0_dens, r0_sh;
+    uint32_t r_off[4];
+    uint32_t n_rh;        // colour hidden layers (>= 1; the first is r0)
+    uint32_t r_out;
+    uint32_t bytes;       // image size
+    uint32_t k_in;        // density input width (32 or 48)
+    uint32_t tile_bytes;  // one input tile record: hash tile + SH tile
+};
+
+__host__ __device__ constexpr uint32_t hash_tile_bytes(uint32_t k_in) { return 128u * k_in * 2u; }
+__host__ __device__ constexpr uint32_t sh_tile_bytes() { return 128u * 16u * 2u; }
+
+struct MlpArgs {
+    FieldView fv;
+    TilePlan plan;
+    const uint8_t* tiles;
+    const uint32_t* n_alive;   // render rounds: device count of the round's samples
+    uint32_t steps;
+    int64_t n_samples;         // used when n_alive is null
+    uint2* out;                // FP16 (r, g, b, density) per sample
+    float4* out_f32;           // BF16 path: FP32 copies of the BF16-rounded values
+    uint32_t* err;
+};
+
+cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s);
+
+struct TileSmem {
+    alignas(1024) uint8_t stage[2][128 * 64 * 2];   // input tile records (hash + SH), double-buffered
+    alignas(1024) uint8_t a_h[128 * 64 * 2];        // hidden activations
+    alignas(1024) uint8_t a_dens[128 * 16 * 2];     // density-MLP output, colour input part 1
+    alignas(8) uint64_t bar_mma;
+    alignas(8) uint64_t bar_load[2];
+    uint32_t tmem_base;
+};
+
+// One MMA chain: sum over (A_i, B_i) pairs into TMEM columns [col, col + N).
+__device__ __forceinline__ bool issue_chain(TileSmem& sm, const uint8_t* const* a, const uint8_t* const* b, const uint32_t* K,
+                                            int n, uint32_t N, uint32_t col, bool bf16, uint32_t& phase) {
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tc_fence_after();
+        const uint32_t idesc = idesc_f16(128, N, bf16);
+        uint32_t acc = 0;
+        for (int i = 0; i < n; ++i) {
+            const uint32_t a0 = smem_addr(a[i]), b0 = smem_addr(b[i]);
+            const uint32_t sbo = (K[i] / 8) * 128;
+            for (uint32_t ks = 0; ks < K[i] / 16; ++ks) {
+                umma_f16(sm.tmem_base + col, smem_desc(a0 + ks * 256, 128, sbo), smem_desc(b0 + ks * 256, 128, sbo), idesc, acc);
+                acc = 1;
+            }
+        }
+        umma_commit(&sm.bar_mma);
+    }
+    bool ok = mbar_wait(&sm.bar_mma, phase);
+    phase ^= 1u;
+    tc_fence_after();
+    return ok;
+}
+
+__device__ __forceinline__ uint32_t tile_lane_addr(const TileSmem& sm, uint32_t col) {
+    return sm.tmem_base + ((((uint32_t)threadIdx.x / 32u) % 4u) * 32u << 16) + col;
+}
+
+// ReLU + rounding, TMEM -> this thread's row of a_h (K = 64).
+__device__ __forceinline__ void relu_to_ah(TileSmem& sm, bool bf16) {
+    const uint32_t r = threadIdx.x;
+#pragma unroll 1
+    for (uint32_t c = 0; c < 64; c += 16) {
+        float v[16];
+        tmem_ld16(tile_lane_addr(sm, c), v);
+        __half h[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) h[i] = to_act(fmaxf(v[i], 0.f), bf16);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            uint4 u;
+            u.x = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 0]);
+            u.y = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 2]);
+            u.z = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 4]);
+            u.w = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 6]);
+            *reinterpret_cast<uint4*>(sm.a_h + tile_offset(r, c + q * 8, 64)) = u;
+        }
+    }
+}
+
+// Both MLPs for the tile held in stage[buf]; returns this thread's (r, g, b, raw density).
+__device__ __forceinline__ bool mlp_tile(TileSmem& sm, const uint8_t* w, const TilePlan& P, int buf, bool bf16, uint32_t& phase,
+                                         float* out4) {
+    bool ok = true;
+    const uint8_t* hash = sm.stage[buf];
+    const uint8_t* sh = sm.stage[buf] + hash_tile_bytes(P.k_in);
+    const uint8_t* a;
+    const uint8_t* b;
+    uint32_t K;
+    // density hidden layers
+    a = hash; b = w + P.d_off[0]; K = P.k_in;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
+    relu_to_ah(sm, bf16);
+    for (uint32_t l = 1; l < P.n_dh; ++l) {
+        a = sm.a_h; b = w + P.d_off[l]; K = 64;
+        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
+        relu_to_ah(sm, bf16);
+    }
+    // density output (16): raw density is column 0
+    a = sm.a_h; b = w + P.d_out; K = 64;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, bf16, phase);
+    {
+        float v[16];
+        tmem_ld16(tile_lane_addr(sm, 64), v);
+        __half h[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) h[i] = to_act(v[i], bf16);
+        out4[3] = from_act(h[0], bf16);
+        store_row(sm.a_dens, threadIdx.x, 16, h);
+    }
+    // colour layer 0 = [density out | SH] split into two K = 16 operands
+    {
+        const uint8_t* as[2] = {sm.a_dens, sh};
+        const uint8_t* bs[2] = {w + P.r0_dens, w + P.r0_sh};
+        const uint32_t Ks[2] = {16, 16};
+        ok &= issue_chain(sm, as, bs, Ks, 2, 64, 0, bf16, phase);
+        relu_to_ah(sm, bf16);
+    }
+    for (uint32_t l = 1; l < P.n_rh; ++l) {
+        a = sm.a_h; b = w + P.r_off[l]; K = 64;
+        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
+        relu_to_ah(sm, bf16);
+    }
+    a = sm.a_h; b = w + P.r_out; K = 64;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, bf16, phase);
+    {
+        float v[16];
+        tmem_ld16(tile_lane_addr(sm, 64), v);
+        out4[0] = from_act(to_act(v[0], bf16), bf16);
+        out4[1] = from_act(to_act(v[1], bf16), bf16);
+        out4[2] = from_act(to_act(v[2], bf16), bf16);
+    }
+    return ok;
+}
+
+// Write one FP16 row of a tile record in global memory (K values, K multiple of 8).
+__device__ __forceinline__ void store_row_global(uint8_t* tile, uint32_t r, uint32_t K, const __half* v) {
+    for (uint32_t c = 0; c < K / 8; ++c) {
+        uint4 q;
+        q.x = *reinterpret_cast<const uint32_t*>(&v[c * 8 + 0]);
+        q.y = *reinterpret_cast<const uint32_t*>(&v[c * 8 + 2]);
+        q.z = *reinterpret_cast<const uint32_t*>(&v[c * 8 + 4]);
+        q.w = *reinterpret_cast<const uint32_t*>(&v[c * 8 + 6]);
+        *reinterpret_cast<uint4*>(tile + tile_offset(r, c * 8, K)) = q;
+    }
+}
+
+}  // namespace insta

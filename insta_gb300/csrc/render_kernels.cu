@@ -1,224 +1,340 @@
-// render_kernels.cu -- the fused render path: one persistent launch marches rays through
-// the occupancy bitfield, maps every sample to canonical space through the frame's BVH,
-// encodes it on the hash grid, runs the density and colour MLPs on tcgen05 tiles and
-// composites front to back.  Each CTA owns 128 ray slots (one per thread); the samples of
-// one iteration form the M = 128 tile of the tensor-core MLP, so no sample stream ever
-// leaves the SM.  Finished slots are refilled from a global ray counter.
+// render_kernels.cu -- the render path as a device-driven wavefront:
+//   ray_init_kernel       camera rays, render-box entry, jitter, advance to the first occupied cell
+//   march_encode_kernel   per alive ray, up to S samples: march, canonical map (BVH nodes staged in
+//                         shared memory, search seeded with the previous sample's triangle), hash
+//                         encode + SH written as ready-made tensor-core operand tiles
+//   mlp_kernel            density + colour MLPs on 128-sample tiles (tcgen05, TMEM accumulators)
+//   composite_kernel      front-to-back compositing, early termination, shading, compaction
+// Ray lists and counts stay on the device; the host only decides when to stop issuing rounds.
 #include "device_common.cuh"
-#include "umma.cuh"
+#include "mlp_tiles.cuh"
 #include "kernels.h"
 
 namespace insta {
 
 __device__ __forceinline__ float srgb_to_linear(float s) { return s <= 0.04045f ? s / 12.92f : powf((s + 0.055f) / 1.055f, 2.4f); }
 
-struct SampleIn {
-    float pos[3];     // canonical position (network input rows 0..2)
-    float dir[3];     // canonical warped direction (rows 8..10)
-    float dpos[3];    // deformed world position (for depth)
-    uint32_t mask;
-};
-
-// generate_next_nerf_network_inputs (:788) writes warp_position(pos) / warp_direction(dir);
-// the warp hook (src/core.cu:470-519) maps it to canonical space in place.
-__device__ __forceinline__ void deform_sample(const FrameView& fr, const DeformView& dv, const float* tmin, const float* tmax,
-                                              V3 pos, V3 dir, SampleIn& s, uint32_t* err) {
-    float cw[3], dw[3];
-    const float pp[3] = {pos.x, pos.y, pos.z};
-    const float dd[3] = {dir.x, dir.y, dir.z};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        cw[k] = __fdiv_rn(__fsub_rn(pp[k], tmin[k]), __fsub_rn(tmax[k], tmin[k]));
-        dw[k] = __fmul_rn(__fadd_rn(dd[k], 1.0f), 0.5f);
-        s.dpos[k] = __fadd_rn(tmin[k], __fmul_rn(cw[k], __fsub_rn(tmax[k], tmin[k])));
-        s.pos[k] = cw[k];
-        s.dir[k] = dw[k];
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
+    const uint32_t mask = __ballot_sync(0xffffffffu, pred);
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t base = 0;
+    if (mask) {
+        const int leader = __ffs(mask) - 1;
+        if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
     }
-    s.mask = 7u;   // untouched samples keep their expression dims
-    V3 p = v3(cw[0], cw[1], cw[2]);
-    if (!box_contains(dv.aabb_min, dv.aabb_max, p)) return;
-    NearestResult r = nearest_triangle(fr, p, 0.f, err);
-    if (r.id < 0) { atomicOr(err, INSTA_DEVERR_NO_TRI); return; }
-    map_to_canonical(dv, fr.frames, (uint32_t)r.id, p, dw, s.pos, s.dir, &s.mask);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
-// Network inputs of one sample, rounded to the MLP activation type (FP16 or BF16).
-__device__ __forceinline__ void build_inputs(const FieldView& fv, const float* extra_dims, const SampleIn& s, bool valid,
-                                             __half* feat, __half* sh) {
+__device__ __forceinline__ void write_pixel(const RenderView& rv, float* out_rgba, float* out_depth, uint32_t pix, float4 rgba, float depth) {
+    // shade_kernel_nerf (ngp/src/testbed_nerf.cu:1794-1827) into a zeroed frame buffer
+    if (rgba.w > 0.001f) {
+        float o[4] = {rgba.x, rgba.y, rgba.z, rgba.w};
+        if (!rv.linear_colors) for (int k = 0; k < 3; ++k) o[k] = srgb_to_linear(o[k]);
+        reinterpret_cast<float4*>(out_rgba)[pix] = make_float4(o[0], o[1], o[2], o[3]);
+        if (o[3] > 0.2f) out_depth[pix] = depth;
+    }
+}
+
+// ------------------------------------------------------------------ ray init
+__global__ void ray_init_kernel(const __grid_constant__ WaveArgs A) {
+    uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = (uint32_t)A.rv.width * (uint32_t)A.rv.height;
+    bool alive = false;
+    RayState r;
+    if (idx < n) {
+        reinterpret_cast<float4*>(A.out_rgba)[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
+        A.out_depth[idx] = 1e10f;
+        alive = ray_init(A.rv, idx % (uint32_t)A.rv.width, idx / (uint32_t)A.rv.width, A.bitfield, r);
+    }
+    uint32_t slot = warp_append(A.n_alive_out, alive);
+    if (alive) {
+        RayBuf b = A.rays_out;
+        b.a[slot] = make_float4(r.o.x, r.o.y, r.o.z, r.t);
+        b.b[slot] = make_float4(r.d.x, r.d.y, r.d.z, 0.f);
+        b.c[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+        b.d[slot] = make_float4(0.f, __uint_as_float(idx), __uint_as_float(0u), __int_as_float(-1));
+    }
+}
+
+// ------------------------------------------------------------------ march + deform + encode
+__device__ __forceinline__ void encode_sample(const FieldView& fv, const float* extra, uint32_t mask, const float* pos,
+                                              const float* dirw, uint8_t* rec, uint32_t row, uint32_t k_in) {
     const bool bf16 = fv.precision == 1;
-    float f[48], d[16];
+    float f[48];
+    hash_encode(fv, v3(pos[0], pos[1], pos[2]), f);
+    __half h[48];
 #pragma unroll
-    for (int i = 0; i < 48; ++i) f[i] = 0.f;
+    for (int i = 0; i < 32; ++i) h[i] = to_act(f[i], bf16);
+    for (uint32_t m = 0; m < fv.n_extra; ++m) h[32 + m] = to_act(mask != 7u ? 1.f : (extra ? extra[m] : 0.f), bf16);
+    store_row_global(rec, row, k_in, h);
+    float d[16];
+    sh4(dirw[0], dirw[1], dirw[2], d);
 #pragma unroll
-    for (int i = 0; i < 16; ++i) d[i] = 0.f;
-    if (valid) {
-        hash_encode(fv, v3(s.pos[0], s.pos[1], s.pos[2]), f);
-        for (uint32_t m = 0; m < fv.n_extra; ++m)
-            f[fv.n_levels * 2 + m] = s.mask != 7u ? 1.f : (extra_dims ? extra_dims[m] : 0.f);
-        sh4(s.dir[0], s.dir[1], s.dir[2], d);
-    }
-#pragma unroll
-    for (int i = 0; i < 48; ++i) feat[i] = to_act(f[i], bf16);
-#pragma unroll
-    for (int i = 0; i < 16; ++i) sh[i] = to_act(d[i], bf16);
+    for (int i = 0; i < 16; ++i) h[i] = to_act(d[i], bf16);
+    store_row_global(rec + hash_tile_bytes(k_in), row, 16, h);
 }
 
-// ------------------------------------------------------------------ render
-struct RenderArgs {
-    RenderView rv;
-    FrameView fr;
-    DeformView dv;
-    FieldView fv;
-    MlpPlan plan;
-    const uint8_t* bitfield;
-    const float* extra_dims;
-    float* out_rgba;
-    float* out_depth;
-    uint32_t* ray_counter;
-    unsigned long long* sample_counter;
-    uint32_t* err;
-};
-
-__global__ void __launch_bounds__(128) render_kernel(const __grid_constant__ RenderArgs A) {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smem_raw);
-    uint8_t* w = smem_raw + ((sizeof(MlpSmem) + 1023) & ~size_t(1023));
-    if (!mlp_setup(sm, w, A.fv.mlp_smem, A.plan.bytes)) {
-        if (threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
-        mlp_teardown(sm);
-        return;
-    }
+// One thread per alive ray: the next `steps` sample positions (generate_next_nerf_network_inputs,
+// ngp/src/testbed_nerf.cu:722-795).  The march runs twice -- count, then write -- so each ray's
+// samples land contiguously in one compacted stream (base from a warp-aggregated atomic); the
+// ray keeps (base, count) for the composite.
+__global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ WaveArgs A) {
+    const uint32_t n_alive = *A.n_alive_in;
     const RenderView& rv = A.rv;
-    const uint32_t n_rays = (uint32_t)rv.width * (uint32_t)rv.height;
-    const bool bf16 = A.fv.precision == 1;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t n_iter = (n_alive + stride - 1) / stride;
+    for (uint32_t it = 0; it < n_iter; ++it) {
+        const uint32_t r = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool valid = r < n_alive;
+        RayState ray;
+        uint32_t ns = 0, j = 0;
+        float t0 = 0.f;
+        if (valid) {
+            const float4 ra = A.rays_in.a[r], rb = A.rays_in.b[r];
+            ns = __float_as_uint(A.rays_in.d[r].z);
+            ray.o = v3(ra.x, ra.y, ra.z);
+            ray.d = v3(rb.x, rb.y, rb.z);
+            ray.idir = v3(__fdiv_rn(1.f, rb.x), __fdiv_rn(1.f, rb.y), __fdiv_rn(1.f, rb.z));
+            ray.t = t0 = ra.w;
+            for (; j < A.steps; ++j) {
+                V3 pos;
+                float dt;
+                if (ns + j >= rv.max_samples_per_ray || !ray_next_sample(rv, A.bitfield, ray, pos, dt)) break;
+            }
+        }
+        // warp-aggregated reservation of j contiguous slots
+        uint32_t incl = j;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((threadIdx.x & 31) >= (uint32_t)o) incl += v;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        uint32_t base = 0;
+        if ((threadIdx.x & 31) == 31 && total) base = atomicAdd(A.n_samples_round, total);
+        base = __shfl_sync(0xffffffffu, base, 31) + incl - j;
+        if (valid) {
+            ray.t = t0;
+            for (uint32_t k = 0; k < j; ++k) {
+                V3 pos;
+                float dt;
+                ray_next_sample(rv, A.bitfield, ray, pos, dt);
+                A.samples[base + k] = make_float4(pos.x, pos.y, pos.z, dt);
+                A.sample_ray[base + k] = r;
+            }
+            if (j == 0) ray.t = t0;
+            A.rays_in.a[r].w = ray.t;
+            A.n_round[r] = j;
+            A.round_base[r] = base;
+        }
+    }
+}
+
+// One thread per sample of the compacted stream: the warp hook (src/core.cu:470-519) on
+// warp_position(pos) / warp_direction(dir), then the hash encode and SH written as tensor-core
+// operand rows.  Neighbouring threads hold consecutive samples of a ray, so their BVH walks are
+// coherent.
+__global__ void __launch_bounds__(256, 4) deform_encode_kernel(const __grid_constant__ WaveArgs A) {
+    __shared__ uint32_t wstack[8][INSTA_STACK];
+    const uint32_t n = *A.n_samples_round;
+    const RenderView& rv = A.rv;
     const V3 cam_fwd = v3(rv.cam[2], rv.cam[6], rv.cam[10]);
     const V3 cam_pos = v3(rv.cam[3], rv.cam[7], rv.cam[11]);
-
-    int64_t pix = -1;
-    bool active = true;
-    RayState ray;
-    float rgba[4] = {0.f, 0.f, 0.f, 0.f}, depth = 0.f, maxw = 0.f;
-    uint32_t ns = 0;
-    unsigned long long local_samples = 0;
-
-    for (;;) {
-        bool has = false;
-        V3 pos = v3(0.f, 0.f, 0.f);
-        float dt = 0.f;
-        while (!has) {
-            if (pix < 0) {
-                if (!active) break;
-                uint32_t idx = atomicAdd(A.ray_counter, 1u);
-                if (idx >= n_rays) { active = false; break; }
-                reinterpret_cast<float4*>(A.out_rgba)[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
-                A.out_depth[idx] = 1e10f;
-                if (!ray_init(rv, idx % (uint32_t)rv.width, idx / (uint32_t)rv.width, A.bitfield, ray)) continue;
-                pix = idx;
-                rgba[0] = rgba[1] = rgba[2] = rgba[3] = 0.f;
-                depth = 0.f; maxw = 0.f; ns = 0;
-            }
-            if (ns < rv.max_samples_per_ray && ray_next_sample(rv, A.bitfield, ray, pos, dt)) {
-                has = true;
-            } else {
-                // shade_kernel_nerf (:1794-1827) into a zeroed frame buffer
-                if (rgba[3] > 0.001f) {
-                    float o[4] = {rgba[0], rgba[1], rgba[2], rgba[3]};
-                    if (!rv.linear_colors) for (int k = 0; k < 3; ++k) o[k] = srgb_to_linear(o[k]);
-                    reinterpret_cast<float4*>(A.out_rgba)[pix] = make_float4(o[0], o[1], o[2], o[3]);
-                    if (o[3] > 0.2f) A.out_depth[pix] = depth;
-                }
-                pix = -1;
-            }
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
+    // warps step through the stream in lockstep chunks of 32 so every lane joins the cooperative query
+    for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32u; base < n; base += n_warps * 32u) {
+        const uint32_t s = base + lane;
+        const bool valid = s < n;
+        float4 smp = make_float4(0.5f, 0.5f, 0.5f, 0.f), rb = make_float4(0.f, 0.f, 1.f, 0.f);
+        if (valid) {
+            smp = A.samples[s];
+            rb = A.rays_in.b[A.sample_ray[s]];
         }
-        if (!__syncthreads_or(has ? 1 : 0)) break;
-
-        SampleIn s;
-        if (has) deform_sample(A.fr, A.dv, rv.train_min, rv.train_max, pos, ray.d, s, A.err);
-        __half feat[48], sh[16];
-        build_inputs(A.fv, A.extra_dims, s, has, feat, sh);
-        float rgb_raw[3], dens_raw = 0.f;
-        bool ok = mlp_eval(sm, w, A.plan, bf16, feat, sh, rgb_raw, dens_raw);
-        if (__syncthreads_or(ok ? 0 : 1)) {
-            if (threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
-            break;
-        }
-        if (has) {
-            ++ns;
-            ++local_samples;
-            // composite_kernel_nerf (:840-999)
-            float T = 1.f - rgba[3];
-            float dtu = unwarp_dt(warp_dt(dt));
-            float alpha = 1.f - expf(-expf(dens_raw) * dtu);
-            float wgt = alpha * T;
+        float cw[3], dw[3], dp[3];
+        const float pp[3] = {smp.x, smp.y, smp.z}, dd[3] = {rb.x, rb.y, rb.z};
 #pragma unroll
-            for (int k = 0; k < 3; ++k) rgba[k] += (1.0f / (1.0f + expf(-rgb_raw[k]))) * wgt;
-            rgba[3] += wgt;
-            if (wgt > maxw) {
-                maxw = wgt;
-                V3 dp = v3(s.dpos[0] - cam_pos.x, s.dpos[1] - cam_pos.y, s.dpos[2] - cam_pos.z);
-                depth = dot_rn(cam_fwd, dp);
-            }
-            if (rgba[3] > 1.0f - rv.min_transmittance) {
-                float a = rgba[3];
-                for (int k = 0; k < 4; ++k) rgba[k] /= a;
-                float o[4] = {rgba[0], rgba[1], rgba[2], rgba[3]};
-                if (!rv.linear_colors) for (int k = 0; k < 3; ++k) o[k] = srgb_to_linear(o[k]);
-                reinterpret_cast<float4*>(A.out_rgba)[pix] = make_float4(o[0], o[1], o[2], o[3]);
-                if (o[3] > 0.2f) A.out_depth[pix] = depth;
-                pix = -1;
-            }
+        for (int k = 0; k < 3; ++k) {
+            cw[k] = __fdiv_rn(__fsub_rn(pp[k], rv.train_min[k]), __fsub_rn(rv.train_max[k], rv.train_min[k]));
+            dw[k] = __fmul_rn(__fadd_rn(dd[k], 1.0f), 0.5f);
+            dp[k] = __fadd_rn(rv.train_min[k], __fmul_rn(cw[k], __fsub_rn(rv.train_max[k], rv.train_min[k])));
+        }
+        float cpos[3] = {cw[0], cw[1], cw[2]}, cdir[3] = {dw[0], dw[1], dw[2]};
+        uint32_t mask = 7u;
+        const V3 p = v3(cw[0], cw[1], cw[2]);
+        const bool in_box = valid && box_contains(A.dv.aabb_min, A.dv.aabb_max, p);
+        Nearest q = nearest_warp(A.fr, p, in_box, wstack[warp], A.err);
+        if (in_box) {
+            if (q.id >= 0) map_to_canonical(A.dv, A.fr.frames, (uint32_t)q.id, p, dw, cpos, cdir, &mask);
+            else atomicOr(A.err, INSTA_DEVERR_NO_TRI);
+        }
+        if (valid) {
+            uint8_t* rec = A.tiles + (size_t)(s >> 7) * A.tile_bytes;
+            encode_sample(A.fv, A.extra_dims, mask, cpos, cdir, rec, s & 127u, A.k_in);
+            const V3 dv = v3(__fsub_rn(dp[0], cam_pos.x), __fsub_rn(dp[1], cam_pos.y), __fsub_rn(dp[2], cam_pos.z));
+            A.aux[s] = make_float2(smp.w, dot_rn(cam_fwd, dv));
         }
     }
-    // warp-aggregated sample count
-    for (int o = 16; o > 0; o >>= 1) local_samples += __shfl_xor_sync(0xffffffffu, local_samples, o);
-    if ((threadIdx.x & 31) == 0 && local_samples) atomicAdd(A.sample_counter, local_samples);
-    mlp_teardown(sm);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(A.sample_counter, (unsigned long long)n);
 }
 
-// ------------------------------------------------------------------ field eval
-struct FieldArgs {
-    FieldView fv;
-    MlpPlan plan;
-    const float* coords;
-    uint32_t stride;
-    int64_t n;
-    float* out4;
-    uint32_t* err;
-};
+// ------------------------------------------------------------------ MLP over tiles
+__device__ __forceinline__ void load_tile(TileSmem& sm, int buf, const uint8_t* src, uint32_t bytes) {
+    bulk_load(sm.stage[buf], src, bytes, &sm.bar_load[buf]);
+}
 
-// NerfNetwork::inference_mixed_precision_impl (NGP/nerf_network.h:159-232) on NerfCoordinate
-// records: out4[i] = (r, g, b, raw density) as stored by the network (FP16 values).
-__global__ void __launch_bounds__(128) field_eval_kernel(const __grid_constant__ FieldArgs A) {
+__global__ void __launch_bounds__(128) mlp_kernel(const __grid_constant__ MlpArgs A) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smem_raw);
-    uint8_t* w = smem_raw + ((sizeof(MlpSmem) + 1023) & ~size_t(1023));
-    if (!mlp_setup(sm, w, A.fv.mlp_smem, A.plan.bytes)) {
-        if (threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
-        mlp_teardown(sm);
-        return;
+    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
+    uint8_t* w = smem_raw + ((sizeof(TileSmem) + 1023) & ~size_t(1023));
+    const uint32_t n_samples = A.n_alive ? *A.n_alive : (uint32_t)A.n_samples;
+    const uint32_t n_tiles = (n_samples + 127u) / 128u;
+    if (blockIdx.x >= n_tiles) return;
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.bar_mma, 1);
+        mbar_init(&sm.bar_load[0], 1);
+        mbar_init(&sm.bar_load[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    __syncthreads();
+    if (threadIdx.x < 32) tmem_alloc(&sm.tmem_base, 128);
+    // the weight image completes phase 0 of bar_load[1]; input tiles then alternate buffers
+    if (threadIdx.x == 0) {
+        bulk_load(w, A.fv.mlp_smem, A.plan.bytes, &sm.bar_load[1]);
+        load_tile(sm, 0, A.tiles + (size_t)blockIdx.x * A.plan.tile_bytes, A.plan.tile_bytes);
+    }
+    bool ok = mbar_wait(&sm.bar_load[1], 0);   // weights
+    uint32_t load_phase[2] = {0u, 1u};          // bar_load[1] already completed one phase
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
     const bool bf16 = A.fv.precision == 1;
-    const int64_t n_tiles = (A.n + 127) / 128;
-    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        int64_t i = tile * 128 + threadIdx.x;
-        bool valid = i < A.n;
-        SampleIn s;
-        if (valid) {
-            const float* c = A.coords + i * A.stride;
-            for (int k = 0; k < 3; ++k) { s.pos[k] = c[k]; s.dir[k] = c[8 + k]; }
-            s.mask = 7u;
+    uint32_t phase = 0;
+    int buf = 0;
+    int pending = 0;   // buffer with a copy in flight: 1 + index, 0 = none
+    if (blockIdx.x < n_tiles) pending = 1;
+    for (uint32_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        ok &= mbar_wait(&sm.bar_load[buf], load_phase[buf]);
+        load_phase[buf] ^= 1u;
+        pending = 0;
+        const uint32_t next = t + gridDim.x;
+        if (next < n_tiles) {
+            if (threadIdx.x == 0) load_tile(sm, buf ^ 1, A.tiles + (size_t)next * A.plan.tile_bytes, A.plan.tile_bytes);
+            pending = 1 + (buf ^ 1);
         }
-        __half feat[48], sh[16];
-        build_inputs(A.fv, valid ? A.coords + i * A.stride + A.stride - A.fv.n_extra : nullptr, s, valid, feat, sh);
-        float rgb_raw[3], dens_raw = 0.f;
-        bool ok = mlp_eval(sm, w, A.plan, bf16, feat, sh, rgb_raw, dens_raw);
-        if (__syncthreads_or(ok ? 0 : 1)) {
-            if (threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
-            break;
+        float o4[4];
+        ok &= mlp_tile(sm, w, A.plan, buf, bf16, phase, o4);
+        const uint32_t s = t * 128u + threadIdx.x;
+        if (s < n_samples) {
+            __half2 rg = __floats2half2_rn(o4[0], o4[1]);
+            __half2 bd = __floats2half2_rn(o4[2], o4[3]);
+            uint2 u;
+            u.x = *reinterpret_cast<uint32_t*>(&rg);
+            u.y = *reinterpret_cast<uint32_t*>(&bd);
+            if (bf16) {
+                // keep BF16-rounded values exactly: store as FP32 pairs through the float outputs
+                A.out_f32[s] = make_float4(o4[0], o4[1], o4[2], o4[3]);
+            } else {
+                A.out[s] = u;
+            }
         }
-        if (valid) reinterpret_cast<float4*>(A.out4)[i] = make_float4(rgb_raw[0], rgb_raw[1], rgb_raw[2], dens_raw);
+        buf ^= 1;
+        ok = __syncthreads_and(ok ? 1 : 0) != 0;
     }
-    mlp_teardown(sm);
+    if (!ok && threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
+    // drain an outstanding prefetch (bounded wait) before the CTA's shared memory is released
+    if (pending) mbar_wait(&sm.bar_load[pending - 1], load_phase[pending - 1]);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x < 32) tmem_dealloc(sm.tmem_base, 128);
+}
+
+// ------------------------------------------------------------------ composite + compaction
+__global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
+    const uint32_t n_alive = *A.n_alive_in;
+    const RenderView& rv = A.rv;
+    const bool bf16 = A.fv.precision == 1;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t n_iter = (n_alive + stride - 1) / stride;
+    for (uint32_t it = 0; it < n_iter; ++it) {
+        const uint32_t r = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool keep = false;
+        float4 ra, rb, rc, rd;
+        if (r < n_alive) {
+            ra = A.rays_in.a[r]; rb = A.rays_in.b[r]; rc = A.rays_in.c[r]; rd = A.rays_in.d[r];
+            const uint32_t m = A.n_round[r], base = A.round_base[r];
+            bool done = m < A.steps;
+            float4 rgba = rc;
+            float depth = rd.x, maxw = rb.w;
+            uint32_t j = 0;
+            for (; j < m; ++j) {
+                const uint32_t s = base + j;
+                float o[4];
+                if (bf16) {
+                    float4 v = A.out_f32[s];
+                    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+                } else {
+                    uint2 u = A.out[s];
+                    float2 rg = __half22float2(*reinterpret_cast<__half2*>(&u.x));
+                    float2 bd = __half22float2(*reinterpret_cast<__half2*>(&u.y));
+                    o[0] = rg.x; o[1] = rg.y; o[2] = bd.x; o[3] = bd.y;
+                }
+                const float2 ax = A.aux[s];
+                // composite_kernel_nerf (ngp/src/testbed_nerf.cu:840-999)
+                const float T = 1.f - rgba.w;
+                const float dtu = unwarp_dt(warp_dt(ax.x));
+                const float alpha = 1.f - expf(-expf(o[3]) * dtu);
+                const float wgt = alpha * T;
+                rgba.x += (1.0f / (1.0f + expf(-o[0]))) * wgt;
+                rgba.y += (1.0f / (1.0f + expf(-o[1]))) * wgt;
+                rgba.z += (1.0f / (1.0f + expf(-o[2]))) * wgt;
+                rgba.w += wgt;
+                if (wgt > maxw) { maxw = wgt; depth = ax.y; }
+                if (rgba.w > 1.0f - rv.min_transmittance) {
+                    const float a = rgba.w;
+                    rgba.x /= a; rgba.y /= a; rgba.z /= a; rgba.w /= a;
+                    done = true;
+                    break;
+                }
+            }
+            const uint32_t ns = __float_as_uint(rd.z) + m;
+            if (done) {
+                write_pixel(rv, A.out_rgba, A.out_depth, __float_as_uint(rd.y), rgba, depth);
+            } else {
+                keep = true;
+                rb.w = maxw;
+                rc = rgba;
+                rd.x = depth;
+                rd.z = __uint_as_float(ns);
+            }
+        }
+        const uint32_t slot = warp_append(A.n_alive_out, keep);
+        if (keep) {
+            A.rays_out.a[slot] = ra; A.rays_out.b[slot] = rb; A.rays_out.c[slot] = rc; A.rays_out.d[slot] = rd;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ field eval (parity entry)
+__global__ void __launch_bounds__(256) encode_coords_kernel(FieldView fv, const float* __restrict__ coords, uint32_t stride,
+                                                            int64_t n, uint8_t* tiles, uint32_t tile_bytes, uint32_t k_in) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* c = coords + i * stride;
+    float pos[3] = {c[0], c[1], c[2]}, dir[3] = {c[8], c[9], c[10]};
+    uint8_t* rec = tiles + (size_t)(i >> 7) * tile_bytes;
+    encode_sample(fv, c + stride - fv.n_extra, 7u, pos, dir, rec, (uint32_t)(i & 127), k_in);
+}
+
+__global__ void unpack_outputs_kernel(const uint2* __restrict__ out, const float4* __restrict__ out_f32, int bf16, int64_t n, float4* dst) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (bf16) { dst[i] = out_f32[i]; return; }
+    uint2 u = out[i];
+    float2 rg = __half22float2(*reinterpret_cast<__half2*>(&u.x));
+    float2 bd = __half22float2(*reinterpret_cast<__half2*>(&u.y));
+    dst[i] = make_float4(rg.x, rg.y, bd.x, bd.y);
 }
 
 // ------------------------------------------------------------------ march debug
@@ -242,48 +358,59 @@ __global__ void march_debug_kernel(RenderView rv, const uint8_t* __restrict__ bf
 }
 
 // ------------------------------------------------------------------ launchers
-static size_t mlp_smem_bytes(const MlpPlan& plan) {
-    return ((sizeof(MlpSmem) + 1023) & ~size_t(1023)) + plan.bytes;
+static size_t mlp_smem_bytes(const TilePlan& p) { return ((sizeof(TileSmem) + 1023) & ~size_t(1023)) + p.bytes; }
+
+static int g_sms = 0;
+static int sm_count() {
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    return g_sms;
 }
 
-int render_ctas_per_sm(const MlpPlan& plan) {
-    size_t smem = mlp_smem_bytes(plan);
-    cudaFuncSetAttribute(render_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_kernel, 128, smem) != cudaSuccess) return 1;
-    // 128 TMEM columns per CTA: at most 4 resident CTAs share an SM's 512 columns.
-    return n < 1 ? 1 : (n > 4 ? 4 : n);
-}
-
-cudaError_t launch_render(const RenderLaunch& L, cudaStream_t s) {
-    RenderArgs a;
-    a.rv = L.rv; a.fr = L.fr; a.dv = L.dv; a.fv = L.fv; a.plan = *L.plan;
-    a.bitfield = L.bitfield; a.extra_dims = L.extra_dims;
-    a.out_rgba = L.out_rgba; a.out_depth = L.out_depth;
-    a.ray_counter = L.ray_counter; a.sample_counter = L.sample_counter; a.err = L.err;
-    size_t smem = mlp_smem_bytes(*L.plan);
-    cudaError_t e = cudaFuncSetAttribute(render_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(L.ray_counter, 0, sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
-    render_kernel<<<L.grid, 128, smem, s>>>(a);
+cudaError_t launch_ray_init(const WaveArgs& a, cudaStream_t s) {
+    uint32_t n = (uint32_t)a.rv.width * (uint32_t)a.rv.height;
+    ray_init_kernel<<<(n + 255) / 256, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_field_eval(const FieldView& fv, const MlpPlan& plan, const float* coords, uint32_t stride, int64_t n,
-                              float* out4, uint32_t* err, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    FieldArgs a;
-    a.fv = fv; a.plan = plan; a.coords = coords; a.stride = stride; a.n = n; a.out4 = out4; a.err = err;
-    size_t smem = mlp_smem_bytes(plan);
-    cudaError_t e = cudaFuncSetAttribute(field_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+cudaError_t launch_march(const WaveArgs& a, cudaStream_t s) {
+    march_kernel<<<sm_count() * 8, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_deform_encode(const WaveArgs& a, cudaStream_t s) {
+    deform_encode_kernel<<<sm_count() * 16, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s) {
+    size_t smem = mlp_smem_bytes(a.plan);
+    cudaError_t e = cudaFuncSetAttribute(mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int64_t tiles = (n + 127) / 128;
-    int grid = (int)(tiles < (int64_t)sms * 4 ? tiles : (int64_t)sms * 4);
-    field_eval_kernel<<<grid, 128, smem, s>>>(a);
+    uint32_t grid = (uint32_t)sm_count() * 2;
+    if (max_tiles < grid) grid = max_tiles ? max_tiles : 1;
+    mlp_kernel<<<grid, 128, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_composite(const WaveArgs& a, cudaStream_t s) {
+    composite_kernel<<<sm_count() * 8, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_encode_coords(const FieldView& fv, const float* coords, uint32_t stride, int64_t n, uint8_t* tiles,
+                                 uint32_t tile_bytes, uint32_t k_in, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    encode_coords_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(const uint2* out, const float4* out_f32, int bf16, int64_t n, float4* dst, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    unpack_outputs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, out_f32, bf16, n, dst);
     return cudaGetLastError();
 }
 

@@ -111,16 +111,6 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                  ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
 }
 
-// Layer table of the MLP weight image: byte offset, N (outputs, padded to 16) and K (inputs).
-struct MlpLayer { uint32_t off, N, K; };
-struct MlpPlan {
-    MlpLayer layer[8];
-    uint32_t n_density;   // density layers (hidden + output)
-    uint32_t n_rgb;       // rgb layers
-    uint32_t bytes;
-    uint32_t k_in;        // density input width (padded to 16)
-};
-
 // Store one FP16 row (K values, K multiple of 8) into an A tile.
 __device__ __forceinline__ void store_row(uint8_t* tile, uint32_t r, uint32_t K, const __half* v) {
     for (uint32_t c = 0; c < K / 8; ++c) {
@@ -133,46 +123,6 @@ __device__ __forceinline__ void store_row(uint8_t* tile, uint32_t r, uint32_t K,
     }
 }
 
-// Shared-memory working set of one 128-sample MLP tile.
-struct MlpSmem {
-    alignas(1024) uint8_t a_in[128 * 48 * 2];    // density input (hash features + expression dims)
-    alignas(1024) uint8_t a_h[128 * 64 * 2];     // hidden activations
-    alignas(1024) uint8_t a_rgb[128 * 32 * 2];   // density output (16) + SH (16)
-    alignas(8) uint64_t bar_mma;
-    alignas(8) uint64_t bar_load;
-    uint32_t tmem_base;
-    uint32_t mma_phase;
-    uint32_t failed;
-};
-
-// Issue one layer: all threads call, thread 0 issues the MMAs into TMEM columns [col, col+N).
-// Returns false on a timed-out wait.  Afterwards each thread reads its own lane.
-__device__ __forceinline__ bool mlp_issue(MlpSmem& sm, const uint8_t* a_tile, const uint8_t* w_smem, const MlpLayer& L,
-                                          uint32_t col, bool bf16, uint32_t& phase) {
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        tc_fence_after();
-        const uint32_t idesc = idesc_f16(128, L.N, bf16);
-        const uint32_t a0 = smem_addr(a_tile), b0 = smem_addr(w_smem + L.off);
-        const uint32_t sbo = (L.K / 8) * 128;
-        for (uint32_t ks = 0; ks < L.K / 16; ++ks) {
-            uint64_t ad = smem_desc(a0 + ks * 256, 128, sbo);
-            uint64_t bd = smem_desc(b0 + ks * 256, 128, sbo);
-            umma_f16(sm.tmem_base + col, ad, bd, idesc, ks > 0 ? 1u : 0u);
-        }
-        umma_commit(&sm.bar_mma);
-    }
-    bool ok = mbar_wait(&sm.bar_mma, phase);
-    phase ^= 1u;
-    tc_fence_after();
-    return ok;
-}
-
-__device__ __forceinline__ uint32_t lane_addr(const MlpSmem& sm, uint32_t col) {
-    return sm.tmem_base + ((((uint32_t)threadIdx.x / 32u) % 4u) * 32u << 16) + col;
-}
 
 __device__ __forceinline__ __half to_act(float v, bool bf16) {
     if (bf16) {
@@ -186,104 +136,5 @@ __device__ __forceinline__ float from_act(__half h, bool bf16) {
     return __half2float(h);
 }
 
-// Hidden layer epilogue: ReLU + rounding to the activation type, streamed 16 columns at a
-// time from TMEM into this thread's row of the next A tile.
-__device__ __forceinline__ void hidden_epilogue(MlpSmem& sm, uint32_t col, uint32_t N, bool bf16) {
-    const uint32_t r = threadIdx.x;
-    for (uint32_t c = 0; c < N; c += 16) {
-        float v[16];
-        tmem_ld16(lane_addr(sm, col + c), v);
-        __half h[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) h[i] = to_act(fmaxf(v[i], 0.f), bf16);
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            uint4 u;
-            u.x = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 0]);
-            u.y = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 2]);
-            u.z = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 4]);
-            u.w = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 6]);
-            *reinterpret_cast<uint4*>(sm.a_h + tile_offset(r, c + q * 8, N)) = u;
-        }
-    }
-}
-
-// Evaluate the density + colour MLPs for this thread's sample.  `feat` holds k_in
-// activations (hash features then expression dims), `sh` the 16 SH values.  Outputs
-// rgb raw (3) and density raw, each rounded to the activation type as stored.
-__device__ __forceinline__ bool mlp_eval(MlpSmem& sm, const uint8_t* w, const MlpPlan& plan, bool bf16,
-                                         const __half* feat, const __half* sh, float* rgb_raw, float& dens_raw) {
-    const uint32_t r = threadIdx.x;
-    bool ok = true;
-    store_row(sm.a_in, r, plan.k_in, feat);
-    const uint8_t* a = sm.a_in;
-    uint32_t phase = sm.mma_phase;
-    for (uint32_t l = 0; l < plan.n_density; ++l) {
-        const MlpLayer& L = plan.layer[l];
-        if (l + 1 < plan.n_density) {
-            ok &= mlp_issue(sm, a, w, L, 0, bf16, phase);
-            hidden_epilogue(sm, 0, L.N, bf16);
-            a = sm.a_h;
-        } else {
-            ok &= mlp_issue(sm, a, w, L, 64, bf16, phase);
-            float v[16];
-            tmem_ld16(lane_addr(sm, 64), v);
-            __half h[32];
-#pragma unroll
-            for (int i = 0; i < 16; ++i) h[i] = to_act(v[i], bf16);
-            dens_raw = from_act(h[0], bf16);
-#pragma unroll
-            for (int i = 0; i < 16; ++i) h[16 + i] = sh[i];
-            store_row(sm.a_rgb, r, 32, h);
-            a = sm.a_rgb;
-        }
-    }
-    for (uint32_t l = 0; l < plan.n_rgb; ++l) {
-        const MlpLayer& L = plan.layer[plan.n_density + l];
-        if (l + 1 < plan.n_rgb) {
-            ok &= mlp_issue(sm, a, w, L, 0, bf16, phase);
-            hidden_epilogue(sm, 0, L.N, bf16);
-            a = sm.a_h;
-        } else {
-            ok &= mlp_issue(sm, a, w, L, 64, bf16, phase);
-            float v[16];
-            tmem_ld16(lane_addr(sm, 64), v);
-            rgb_raw[0] = from_act(to_act(v[0], bf16), bf16);
-            rgb_raw[1] = from_act(to_act(v[1], bf16), bf16);
-            rgb_raw[2] = from_act(to_act(v[2], bf16), bf16);
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (threadIdx.x == 0) sm.mma_phase = phase;
-    __syncthreads();
-    return ok;
-}
-
-// CTA prologue: mbarriers, TMEM (128 columns), weight image bulk-copied into `w`.
-__device__ __forceinline__ bool mlp_setup(MlpSmem& sm, uint8_t* w, const uint8_t* w_global, uint32_t bytes) {
-    if (threadIdx.x == 0) {
-        mbar_init(&sm.bar_mma, 1);
-        mbar_init(&sm.bar_load, 1);
-        sm.mma_phase = 0;
-        sm.failed = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) tmem_alloc(&sm.tmem_base, 128);
-    if (threadIdx.x == 0) bulk_load(w, w_global, bytes, &sm.bar_load);
-    bool ok = mbar_wait(&sm.bar_load, 0);
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    return ok;
-}
-
-__device__ __forceinline__ void mlp_teardown(MlpSmem& sm) {
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (threadIdx.x < 32) tmem_dealloc(sm.tmem_base, 128);
-}
 
 }  // namespace insta
