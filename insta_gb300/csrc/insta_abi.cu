@@ -65,7 +65,7 @@ struct Field {
 
 // Device scratch of the render wavefront, sized for the largest request seen.
 struct Wave {
-    DevBuf rays[2][4], n_round, round_base, sample_ray, samples, tiles, aux, out, out_f32, counters;
+    DevBuf rays[2][4], n_round, sample_index, sample_ray, samples, tiles, aux, out, out_f32, counters;
     uint32_t cap_rays = 0;
     uint64_t cap_samples = 0;
 };
@@ -363,7 +363,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     Wave& w = ctx->wave;
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 4; ++k) ctx->release(w.rays[b][k]);
-    for (DevBuf* b : {&w.n_round, &w.round_base, &w.sample_ray, &w.samples, &w.tiles, &w.aux, &w.out, &w.out_f32, &w.counters})
+    for (DevBuf* b : {&w.n_round, &w.sample_index, &w.sample_ray, &w.samples, &w.tiles, &w.aux, &w.out, &w.out_f32, &w.counters})
         ctx->release(*b);
     if (ctx->host_counters) cudaFreeHost(ctx->host_counters);
     cudaFree(ctx->err_dev);
@@ -682,13 +682,13 @@ int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, 
             for (int b = 0; b < 2; ++b)
                 for (int k = 0; k < 4; ++k) ctx->alloc(w.rays[b][k], (size_t)nr * 16);
             ctx->alloc(w.n_round, (size_t)nr * 4);
-            ctx->alloc(w.round_base, (size_t)nr * 4);
             w.cap_rays = nr;
         }
         ctx->alloc(w.tiles, cap_samples / 128 * P.tile_bytes);
         ctx->alloc(w.aux, cap_samples * sizeof(float2));
         ctx->alloc(w.samples, cap_samples * sizeof(float4));
         ctx->alloc(w.sample_ray, cap_samples * sizeof(uint32_t));
+        ctx->alloc(w.sample_index, cap_samples * sizeof(uint32_t));
         ctx->alloc(w.out, cap_samples * sizeof(uint2));
         if (a.field.view.precision == 1) ctx->alloc(w.out_f32, cap_samples * sizeof(float4));
         ctx->alloc(w.counters, 64);
@@ -710,7 +710,7 @@ int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, 
         W.aux = (float2*)w.aux.p;
         W.samples = (float4*)w.samples.p;
         W.sample_ray = (uint32_t*)w.sample_ray.p;
-        W.round_base = (uint32_t*)w.round_base.p;
+        W.sample_index = (uint32_t*)w.sample_index.p;
         W.out = (const uint2*)w.out.p;
         W.out_f32 = (const float4*)w.out_f32.p;
         W.n_round = (uint32_t*)w.n_round.p;

@@ -35,7 +35,7 @@ struct WaveArgs {
     const uint32_t* n_alive_in;
     uint32_t* n_alive_out;
     uint32_t* n_round;          // samples produced this round, per alive ray
-    uint32_t* round_base;       // first sample of the ray in this round's compacted stream
+    uint32_t* sample_index;     // [steps][n_alive]: stream position of sample k of ray r
     uint32_t* sample_ray;       // per sample: its ray slot
     uint32_t* n_samples_round;  // device count of this round's samples
     uint32_t steps;             // samples per ray per round

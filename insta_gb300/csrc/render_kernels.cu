@@ -76,14 +76,18 @@ __device__ __forceinline__ void encode_sample(const FieldView& fv, const float* 
 }
 
 // One thread per alive ray: the next `steps` sample positions (generate_next_nerf_network_inputs,
-// ngp/src/testbed_nerf.cu:722-795).  The march runs twice -- count, then write -- so each ray's
-// samples land contiguously in one compacted stream (base from a warp-aggregated atomic); the
-// ray keeps (base, count) for the composite.
+// ngp/src/testbed_nerf.cu:722-795).  The march runs twice -- count, then write -- so the samples of
+// a warp's 32 neighbouring rays land in one compacted block (base from a warp-aggregated atomic),
+// ordered step-major: step k of all lanes, then step k + 1.  Neighbouring entries of the stream are
+// then the same step of adjacent pixels, which keeps the cooperative BVH queries coherent.
+// sample_index[k * n_alive + r] records where sample k of ray r went.
 __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ WaveArgs A) {
     const uint32_t n_alive = *A.n_alive_in;
     const RenderView& rv = A.rv;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_iter = (n_alive + stride - 1) / stride;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
     for (uint32_t it = 0; it < n_iter; ++it) {
         const uint32_t r = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
         const bool valid = r < n_alive;
@@ -103,29 +107,30 @@ __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ Wave
                 if (ns + j >= rv.max_samples_per_ray || !ray_next_sample(rv, A.bitfield, ray, pos, dt)) break;
             }
         }
-        // warp-aggregated reservation of j contiguous slots
-        uint32_t incl = j;
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if ((threadIdx.x & 31) >= (uint32_t)o) incl += v;
-        }
-        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t total = __reduce_add_sync(0xffffffffu, j);
+        const uint32_t max_j = __reduce_max_sync(0xffffffffu, j);
         uint32_t base = 0;
-        if ((threadIdx.x & 31) == 31 && total) base = atomicAdd(A.n_samples_round, total);
-        base = __shfl_sync(0xffffffffu, base, 31) + incl - j;
-        if (valid) {
-            ray.t = t0;
-            for (uint32_t k = 0; k < j; ++k) {
+        if (lane == 0 && total) base = atomicAdd(A.n_samples_round, total);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (valid) ray.t = t0;
+        uint32_t offset = 0;
+        for (uint32_t k = 0; k < max_j; ++k) {
+            const bool act = k < j;
+            const uint32_t m = __ballot_sync(0xffffffffu, act);
+            if (act) {
                 V3 pos;
                 float dt;
                 ray_next_sample(rv, A.bitfield, ray, pos, dt);
-                A.samples[base + k] = make_float4(pos.x, pos.y, pos.z, dt);
-                A.sample_ray[base + k] = r;
+                const uint32_t idx = base + offset + (uint32_t)__popc(m & lt_mask);
+                A.samples[idx] = make_float4(pos.x, pos.y, pos.z, dt);
+                A.sample_ray[idx] = r;
+                A.sample_index[(size_t)k * n_alive + r] = idx;
             }
-            if (j == 0) ray.t = t0;
+            offset += (uint32_t)__popc(m);
+        }
+        if (valid) {
             A.rays_in.a[r].w = ray.t;
             A.n_round[r] = j;
-            A.round_base[r] = base;
         }
     }
 }
@@ -263,13 +268,13 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
         float4 ra, rb, rc, rd;
         if (r < n_alive) {
             ra = A.rays_in.a[r]; rb = A.rays_in.b[r]; rc = A.rays_in.c[r]; rd = A.rays_in.d[r];
-            const uint32_t m = A.n_round[r], base = A.round_base[r];
+            const uint32_t m = A.n_round[r];
             bool done = m < A.steps;
             float4 rgba = rc;
             float depth = rd.x, maxw = rb.w;
             uint32_t j = 0;
             for (; j < m; ++j) {
-                const uint32_t s = base + j;
+                const uint32_t s = A.sample_index[(size_t)j * n_alive + r];
                 float o[4];
                 if (bf16) {
                     float4 v = A.out_f32[s];
