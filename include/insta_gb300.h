@@ -135,6 +135,17 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
 /* out4[n][4] = (r, g, b, raw density) network outputs (device pointers). */
 int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4);
 
+/* Same result as insta_field_eval, but the call allocates no device memory.  No counterpart
+ * in the reference: it exists for callers that must not allocate on the hot path -- code that
+ * records the work into a CUDA graph, real-time render callbacks with a fixed memory budget, or
+ * hosts that own every device allocation through their own pool.  Its working memory is a
+ * fixed array inside the library (about 2.5 MB on every GPU that loads the library, held until
+ * the process exits), so at most 16384 samples per call; larger n returns
+ * INSTA_ERR_INVALID_ARG.  The first call on a device looks the array up (make that call before
+ * any stream capture).  All calls share the array: calls whose work overlaps on the GPU (other
+ * streams, other contexts) race, so serialise them. */
+int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4);
+
 /* -- render ------------------------------------------------------------------- */
 /* out_rgba f32[h*w*4] (linear RGBA, zero background), out_depth f32[h*w] (1e10 where no
  * hit).  Host pointers: the call returns after the copy back; device pointers: asynchronous. */

@@ -21,7 +21,7 @@ EXPORTS = [
     "insta_canonical_set", "insta_avatar_set_boxes", "insta_avatar_set_flags", "insta_frame_upload",
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_field_param_count", "insta_params_load",
-    "insta_field_eval", "insta_render", "insta_render_samples", "insta_march_debug",
+    "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_samples", "insta_march_debug",
 ]
 
 
@@ -77,6 +77,7 @@ def load(path: Path | None = None):
             "insta_field_param_count": [C.POINTER(FieldDesc), C.POINTER(u64)],
             "insta_params_load": [vp, C.c_int, C.POINTER(FieldDesc), vp, u64],
             "insta_field_eval": [vp, C.c_int, vp, u32, i64, vp],
+            "insta_field_eval_static": [vp, C.c_int, vp, u32, i64, vp],
             "insta_render": [vp, C.POINTER(RenderDesc), vp, vp],
             "insta_render_samples": [vp, C.POINTER(u64)],
             "insta_march_debug": [vp, C.POINTER(RenderDesc), C.c_int, vp, vp, vp],
@@ -207,6 +208,10 @@ class Context:
 
     def field_eval(self, avatar, coords, stride, n, out4):
         self._check(self.lib.insta_field_eval(self.h, avatar, _addr(coords), stride, n, _addr(out4)))
+
+    def field_eval_static(self, avatar, coords, stride, n, out4):
+        """insta_field_eval without device allocations (n <= 16384, shared fixed scratch)."""
+        self._check(self.lib.insta_field_eval_static(self.h, avatar, _addr(coords), stride, n, _addr(out4)))
 
     @staticmethod
     def render_desc(avatar, frame, width, height, focal, cam, cone_angle=1 / 256, spp=0, min_transmittance=0.01,

@@ -648,6 +648,31 @@ int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t s
     });
 }
 
+int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4) {
+    return guarded(ctx, [&] {
+        Avatar& a = ctx->avatar(avatar);
+        if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", avatar);
+        if (n < 0 || (n > 0 && (!coords || !out4))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
+        if (n > static_max_samples())
+            fail(INSTA_ERR_INVALID_ARG, "insta_field_eval_static takes at most %lld samples per call, got %lld",
+                 (long long)static_max_samples(), (long long)n);
+        if (stride < 11 + a.field.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
+        if (n == 0) return;
+        uint8_t* tiles = nullptr;
+        uint2* out = nullptr;
+        float4* out_f32 = nullptr;
+        CK(static_scratch(ctx->device, &tiles, &out, &out_f32));
+        const TilePlan& P = a.field.plan;
+        const uint64_t n_tiles = ((uint64_t)n + 127) / 128;
+        CK(launch_encode_coords(a.field.view, coords, stride, n, tiles, P.tile_bytes, P.k_in, ctx->stream));
+        MlpArgs m{};
+        m.fv = a.field.view; m.plan = P; m.tiles = tiles; m.n_alive = nullptr; m.steps = 1; m.n_samples = n;
+        m.out = out; m.out_f32 = out_f32; m.err = ctx->err_dev;
+        CK(launch_mlp(m, (uint32_t)n_tiles, ctx->stream));
+        CK(launch_unpack(out, out_f32, a.field.view.precision == 1, n, (float4*)out4, ctx->stream));
+    });
+}
+
 int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, float* out_depth) {
     return guarded(ctx, [&] {
         check_request(req);

@@ -66,6 +66,10 @@ cudaError_t launch_composite(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_encode_coords(const FieldView& fv, const float* coords, uint32_t stride, int64_t n, uint8_t* tiles,
                                  uint32_t tile_bytes, uint32_t k_in, cudaStream_t s);
 cudaError_t launch_unpack(const uint2* out, const float4* out_f32, int bf16, int64_t n, float4* dst, cudaStream_t s);
+// Fixed device scratch of insta_field_eval_static (static_scratch.cu); first call per device looks it up.
+int64_t static_max_samples();
+cudaError_t static_scratch(int device, uint8_t** tiles, uint2** out, float4** out_f32);
+
 cudaError_t launch_march_debug(const RenderView& rv, const uint8_t* bitfield, int max_out, float* out_t, float* out_dt,
                                int32_t* out_n, cudaStream_t s);
 
