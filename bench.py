@@ -35,9 +35,15 @@ WIDTH = HEIGHT = 512
 RADIUS = 0.015
 CONE = 1.0 / 256.0
 L2_FLUSH_BYTES = 512 << 20
-HASH_BYTES_PER_SAMPLE = 16 * 8 * 2 * 2            # 16 levels x 8 corners x F=2 x FP16
+# DRAM bytes (read + write) of one deform_encode launch in a 512x512 frame, from an ncu capture
+# (profiles/deform_encode_render512.md); None until measured
+TRAFFIC_PER_FRAME = None
+# Algorithmic bytes per sample of the dominant kernel (deform_encode): hash-grid gathers
+# (16 levels x 8 corners x 2 FP16 features) + sample record, ray direction and ray index in +
+# encoded operand row (32 + 16 FP16) and (dt, depth) out.
+HASH_BYTES_PER_SAMPLE = 16 * 8 * 2 * 2
+DEFORM_ENCODE_BYTES_PER_SAMPLE = HASH_BYTES_PER_SAMPLE + 16 + 16 + 4 + (32 + 16) * 2 + 8
 MLP_FLOP_PER_SAMPLE = 2 * (32 * 64 + 64 * 16 + 32 * 64 + 64 * 64 + 64 * 3)
-KERNELS_PER_STEP = 1 + 1 + 1 + 7 + 1               # tri frames, BVH build, occupancy, 7 max-pools, render
 
 
 def dist_env():
@@ -179,10 +185,6 @@ def run_ours(args, rank, world, local):
         ctx.occupancy_from_mesh(0, 0, RADIUS)
         ctx.render(reqs[k % len(reqs)], rgba, depth)
 
-    # a separate timing of the render kernel alone (the dominant kernel) on the same stream
-    def render_only(k):
-        ctx.render(reqs[k % len(reqs)], rgba, depth)
-
     with torch.cuda.stream(stream):
         for k in range(args.warmup):
             step(k)
@@ -195,8 +197,8 @@ def run_ours(args, rank, world, local):
             dist.barrier()
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        rv = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         total_samples = 0
+        ctx.stats(reset=True)
         with ClockSampler(local) as clocks:
             t_wall0 = time.perf_counter()
             for k in range(args.steps):
@@ -207,15 +209,16 @@ def run_ours(args, rank, world, local):
                 total_samples += samples_per_frame[k % len(reqs)]
             stream.synchronize()
             t_wall = time.perf_counter() - t_wall0
-            # render kernel alone (frame state resident), for the roofline
-            for k in range(args.steps):
-                flush.zero_()
-                rv[k][0].record(stream)
-                render_only(k)
-                rv[k][1].record(stream)
-            stream.synchronize()
         step_ms = [a.elapsed_time(b) for a, b in ev]
-        render_ms = [a.elapsed_time(b) for a, b in rv]
+        launches = ctx.stats(reset=True)["kernel_launches"]
+        # per-stage device time (CUDA events recorded by the library around each stage, on this
+        # stream), in a separate pass so the timed steps above carry no extra events
+        ctx.stats_enable(True)
+        for k in range(args.steps):
+            flush.zero_()
+            step(k)
+        stages = ctx.stats(reset=True)
+        ctx.stats_enable(False)
         ctx.sync()
         # end to end through the C ABI with host buffers: H2D of the frame's vertices, D2H of RGBA + depth
         host_rgba = torch.empty((HEIGHT * WIDTH, 4), dtype=torch.float32).pin_memory()
@@ -244,8 +247,10 @@ def run_ours(args, rank, world, local):
         return
     value = total_samples / dev_t
     mean_samples = statistics.mean(samples_per_frame)
-    render_s = statistics.median(render_ms) / 1000.0
-    achieved = mean_samples * HASH_BYTES_PER_SAMPLE / render_s / 1e9
+    stage_ms = {k: v / args.steps for k, v in stages["stage_ms"].items() if stages["stage_calls"][k]}
+    de_s = stage_ms["deform_encode"] / 1000.0
+    mlp_s = stage_ms["mlp"] / 1000.0
+    achieved = mean_samples * DEFORM_ENCODE_BYTES_PER_SAMPLE / de_s / 1e9
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -261,16 +266,18 @@ def run_ours(args, rank, world, local):
                                f"occupancy from mesh (1.5 cm), 16-level hash grid T=2^19, MLPs 32-64-16 / 32-64-64-3",
                    "global_batch": world, "samples_per_frame": mean_samples, "parallelism": f"replicas x{world}",
                    "l2": "flushed (512 MiB write) between timed steps", "frames_per_s": args.steps * world / dev_t},
-        "roofline": {"bound": "hbm", "kernel": "render_kernel", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
-                     "basis": f"{HASH_BYTES_PER_SAMPLE} B hash-grid gathers per sample / median render-kernel time",
-                     "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"},
-        "roofline_tensor": {"achieved": mean_samples * MLP_FLOP_PER_SAMPLE / render_s / 1e12, "peak": tflops_peak,
-                            "unit": "TFLOP/s", "frac": mean_samples * MLP_FLOP_PER_SAMPLE / render_s / 1e12 / tflops_peak},
-        "render_kernel_ms": 1000.0 * render_s,
+        "roofline": {"bound": "hbm", "kernel": "deform_encode_kernel", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": TRAFFIC_PER_FRAME,
+                     "basis": f"{DEFORM_ENCODE_BYTES_PER_SAMPLE} B per sample (512 B hash gathers + stream in/out) "
+                              f"x samples per frame / deform_encode stage time per frame (CUDA events)",
+                     "peak_source": "MEASURED_PEAKS.json (of measured)" if peaks else "fallback"},
+        "roofline_tensor": {"kernel": "mlp_kernel", "achieved": mean_samples * MLP_FLOP_PER_SAMPLE / mlp_s / 1e12,
+                            "peak": tflops_peak, "unit": "TFLOP/s",
+                            "frac": mean_samples * MLP_FLOP_PER_SAMPLE / mlp_s / 1e12 / tflops_peak},
+        "stage_ms_per_frame": stage_ms,
         "e2e": {"value": e2e_samples / e2e_t, "unit": UNIT, "h2d_bytes_per_step": int(av.n_verts * 12),
                 "d2h_bytes_per_step": int(WIDTH * HEIGHT * 20)},
-        "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "gpu_launches": launches,
         "clocks": clocks.summary(),
         "wall_s_timed": t_wall,
     }

@@ -89,12 +89,34 @@ typedef struct {
     const float* extra_dims;        /* host, n_extra_dims floats, or NULL (zeros) */
 } insta_render_desc;
 
+/* Pipeline stages timed by insta_stats (CUDA events on the context's stream). */
+#define INSTA_STAGE_FRAME 0          /* per-frame triangle frames + LBVH build   */
+#define INSTA_STAGE_OCCUPANCY 1      /* occupancy bitfield from the mesh         */
+#define INSTA_STAGE_RAY_INIT 2
+#define INSTA_STAGE_MARCH 3
+#define INSTA_STAGE_DEFORM_ENCODE 4  /* canonical map + hash encode + SH         */
+#define INSTA_STAGE_MLP 5            /* density + colour MLPs (tensor cores)     */
+#define INSTA_STAGE_COMPOSITE 6
+#define INSTA_STAGE_CANONICAL_MAP 7  /* insta_canonical_map / _soa               */
+#define INSTA_STAGE_FIELD 8          /* insta_field_eval / _static               */
+#define INSTA_STAGE_COUNT 9
+
+typedef struct {
+    uint64_t kernel_launches;        /* kernels the library launched */
+    uint64_t last_render_samples;    /* network samples of the last insta_render */
+    float stage_ms[INSTA_STAGE_COUNT];
+    uint32_t stage_calls[INSTA_STAGE_COUNT];
+} insta_stats;
+
 /* -- context ---------------------------------------------------------------- */
 int insta_ctx_create(int device, void* cuda_stream, uint64_t budget_bytes, insta_ctx** out);
 int insta_ctx_destroy(insta_ctx* ctx);
 const char* insta_last_error(const insta_ctx* ctx);
 int insta_sync(insta_ctx* ctx);
 int insta_memory_used(const insta_ctx* ctx, uint64_t* bytes);
+/* Statistics: kernel launch count always; per-stage GPU time when stage timing is enabled. */
+int insta_stats_enable(insta_ctx* ctx, int stage_timing);
+int insta_stats_read(insta_ctx* ctx, insta_stats* out, int reset);
 
 /* -- avatar geometry --------------------------------------------------------- */
 /* verts f32[n_verts*3], faces i32[n_faces*3], mask u32[n_faces] (region ids, NULL = 15);

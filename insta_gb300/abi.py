@@ -18,6 +18,7 @@ FLAG_DISABLE_INTERP = 1
 
 EXPORTS = [
     "insta_ctx_create", "insta_ctx_destroy", "insta_last_error", "insta_sync", "insta_memory_used",
+    "insta_stats_enable", "insta_stats_read",
     "insta_canonical_set", "insta_avatar_set_boxes", "insta_avatar_set_flags", "insta_frame_upload",
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_field_param_count", "insta_params_load",
@@ -37,6 +38,14 @@ class FieldDesc(C.Structure):
                 ("n_extra_dims", C.c_uint32), ("density_neurons", C.c_uint32), ("density_hidden_layers", C.c_uint32),
                 ("density_output_dims", C.c_uint32), ("rgb_neurons", C.c_uint32), ("rgb_hidden_layers", C.c_uint32),
                 ("precision", C.c_uint32)]
+
+
+STAGES = ["frame", "occupancy", "ray_init", "march", "deform_encode", "mlp", "composite", "canonical_map", "field"]
+
+
+class Stats(C.Structure):
+    _fields_ = [("kernel_launches", C.c_uint64), ("last_render_samples", C.c_uint64),
+                ("stage_ms", C.c_float * len(STAGES)), ("stage_calls", C.c_uint32 * len(STAGES))]
 
 
 class RenderDesc(C.Structure):
@@ -64,6 +73,8 @@ def load(path: Path | None = None):
             "insta_ctx_destroy": [vp],
             "insta_sync": [vp],
             "insta_memory_used": [vp, C.POINTER(u64)],
+            "insta_stats_enable": [vp, C.c_int],
+            "insta_stats_read": [vp, C.POINTER(Stats), C.c_int],
             "insta_canonical_set": [vp, C.c_int, vp, C.c_int, vp, C.c_int, vp],
             "insta_avatar_set_boxes": [vp, C.c_int, vp, vp, vp, vp],
             "insta_avatar_set_flags": [vp, C.c_int, u32],
@@ -159,6 +170,16 @@ class Context:
         v = C.c_uint64(0)
         self._check(self.lib.insta_memory_used(self.h, C.byref(v)))
         return int(v.value)
+
+    def stats_enable(self, stage_timing: bool = True):
+        self._check(self.lib.insta_stats_enable(self.h, int(stage_timing)))
+
+    def stats(self, reset: bool = False) -> dict:
+        s = Stats()
+        self._check(self.lib.insta_stats_read(self.h, C.byref(s), int(reset)))
+        return {"kernel_launches": int(s.kernel_launches), "last_render_samples": int(s.last_render_samples),
+                "stage_ms": {n: float(s.stage_ms[i]) for i, n in enumerate(STAGES)},
+                "stage_calls": {n: int(s.stage_calls[i]) for i, n in enumerate(STAGES)}}
 
     def canonical_set(self, avatar, verts, faces, mask=None):
         v = np.ascontiguousarray(verts, dtype=np.float32)

@@ -98,6 +98,35 @@ struct insta_ctx {
     Wave wave;
     uint32_t* host_counters = nullptr;   // pinned: alive-ray counts read between rounds
     int sms = 0;
+    // statistics: kernel launches issued by the library, optional per-stage CUDA-event timing
+    uint64_t launches = 0;
+    bool timing = false;
+    std::vector<cudaEvent_t> event_pool;
+    size_t events_used = 0;
+    std::vector<std::pair<int, size_t>> timed;   // (stage, index of the start event)
+    double stage_ms[INSTA_STAGE_COUNT] = {};
+    uint32_t stage_calls[INSTA_STAGE_COUNT] = {};
+
+    cudaEvent_t next_event() {
+        if (events_used == event_pool.size()) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            event_pool.push_back(e);
+        }
+        return event_pool[events_used++];
+    }
+    void collect_timings() {
+        if (timed.empty()) return;
+        CK(cudaStreamSynchronize(stream));
+        for (auto& t : timed) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, event_pool[t.second], event_pool[t.second + 1]));
+            stage_ms[t.first] += ms;
+            stage_calls[t.first] += 1;
+        }
+        timed.clear();
+        events_used = 0;
+    }
 
     void* alloc(DevBuf& b, size_t bytes) {
         if (b.p && b.bytes >= bytes) return b.p;
@@ -141,6 +170,30 @@ struct insta_ctx {
 };
 
 namespace {
+
+// Brackets the launches of one stage: counts its kernels and, with timing on, records a CUDA
+// event pair on the context's stream around them.
+struct Stage {
+    insta_ctx* ctx;
+    int stage;
+    Stage(insta_ctx* c, int st, int kernels) : ctx(c), stage(st) {
+        ctx->launches += (uint64_t)kernels;
+        if (ctx->timing) {
+            if (ctx->events_used + 2 > 4096) ctx->collect_timings();
+            ctx->timed.push_back({stage, ctx->events_used});
+            CK(cudaEventRecord(ctx->next_event(), ctx->stream));
+        }
+    }
+    ~Stage() {
+        if (ctx->timing) {
+            if (ctx->events_used < ctx->event_pool.size() || ctx->event_pool.size() < 8192) {
+                cudaEvent_t e = nullptr;
+                try { e = ctx->next_event(); } catch (...) { return; }
+                cudaEventRecord(e, ctx->stream);
+            }
+        }
+    }
+};
 
 template <typename F>
 int guarded(insta_ctx* ctx, F&& f) {
@@ -366,6 +419,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     for (DevBuf* b : {&w.n_round, &w.sample_index, &w.sample_ray, &w.samples, &w.tiles, &w.aux, &w.out, &w.out_f32, &w.counters})
         ctx->release(*b);
     if (ctx->host_counters) cudaFreeHost(ctx->host_counters);
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     cudaFree(ctx->err_dev);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -461,6 +515,7 @@ int insta_frame_upload(insta_ctx* ctx, int avatar, int frame, const float* verts
         f.view.frames = static_cast<const TriFrame*>(f.frames.p);
         f.view.n_tris = a.F;
         f.view.n_nodes = max_nodes;
+        Stage st(ctx, INSTA_STAGE_FRAME, 2);
         CK(launch_tri_frames(a.F, (const float*)f.verts.p, (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
                              (const float*)a.canon_area.p, nullptr, (TriFrame*)f.frames.p, 1, ctx->stream));
         CK(launch_bvh_build(f.view, (const float*)f.verts.p, (const int32_t*)a.faces.p, ctx->bvh_scratch.p, ctx->stream));
@@ -488,6 +543,7 @@ int insta_occupancy_from_mesh(insta_ctx* ctx, int avatar, int frame, double radi
         Avatar& a = ctx->avatar(avatar);
         Frame& f = get_frame(a, frame);
         ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
+        Stage st(ctx, INSTA_STAGE_OCCUPANCY, 8);
         CK(launch_occupancy(f.view, radius, (uint8_t*)f.bitfield.p, ctx->err_dev, ctx->stream));
         f.has_occupancy = true;
     });
@@ -531,6 +587,7 @@ int insta_canonical_map(insta_ctx* ctx, int avatar, int frame, float* coords, ui
             a.table_dirty = false;
         }
         if (frame >= 0) get_frame(a, frame);
+        Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
         CK(launch_canonical_map_coords((const FrameView*)a.frame_table.p, a.table_frames, deform_view(a), coords, stride, n_extra, n,
                                        frame, ctx->err_dev, ctx->stream));
     });
@@ -541,6 +598,7 @@ int insta_canonical_map_soa(insta_ctx* ctx, int avatar, int frame, const float* 
         if (n < 0 || (n > 0 && (!pts || !out_idx || !out_canon))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
         Avatar& a = ctx->avatar(avatar);
         Frame& f = get_frame(a, frame);
+        Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
         CK(launch_canonical_map_soa(f.view, deform_view(a), pts, n, out_idx, out_canon, ctx->err_dev, ctx->stream));
     });
 }
@@ -639,6 +697,7 @@ int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t s
         ctx->alloc(w.out, tiles * 128 * sizeof(uint2));
         ctx->alloc(w.out_f32, tiles * 128 * sizeof(float4));
         CK(cudaMemsetAsync(w.tiles.p, 0, tiles * P.tile_bytes, ctx->stream));
+        Stage st(ctx, INSTA_STAGE_FIELD, 3);
         CK(launch_encode_coords(a.field.view, coords, stride, n, (uint8_t*)w.tiles.p, P.tile_bytes, P.k_in, ctx->stream));
         MlpArgs m{};
         m.fv = a.field.view; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.steps = 1; m.n_samples = n;
@@ -664,6 +723,7 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
         CK(static_scratch(ctx->device, &tiles, &out, &out_f32));
         const TilePlan& P = a.field.plan;
         const uint64_t n_tiles = ((uint64_t)n + 127) / 128;
+        Stage st(ctx, INSTA_STAGE_FIELD, 3);
         CK(launch_encode_coords(a.field.view, coords, stride, n, tiles, P.tile_bytes, P.k_in, ctx->stream));
         MlpArgs m{};
         m.fv = a.field.view; m.plan = P; m.tiles = tiles; m.n_alive = nullptr; m.steps = 1; m.n_samples = n;
@@ -751,7 +811,7 @@ int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, 
         CK(cudaMemsetAsync(n_alive, 0, 8, ctx->stream));
         W.rays_out = rays(0);
         W.n_alive_out = n_alive;
-        CK(launch_ray_init(W, ctx->stream));
+        { Stage st(ctx, INSTA_STAGE_RAY_INIT, 1); CK(launch_ray_init(W, ctx->stream)); }
         int cur = 0;
         const uint32_t max_rounds = (W.rv.max_samples_per_ray + STEPS - 1) / STEPS + 1;
         for (uint32_t round = 0; round < max_rounds; ++round) {
@@ -762,11 +822,11 @@ int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, 
             CK(cudaMemsetAsync(n_alive + (cur ^ 1), 0, 4, ctx->stream));
             CK(cudaMemsetAsync(n_alive + 2, 0, 4, ctx->stream));
             W.n_samples_round = n_alive + 2;
-            CK(launch_march(W, ctx->stream));
-            CK(launch_deform_encode(W, ctx->stream));
+            { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_march(W, ctx->stream)); }
+            { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 1); CK(launch_deform_encode(W, ctx->stream)); }
             M.n_alive = W.n_samples_round;
-            CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream));
-            CK(launch_composite(W, ctx->stream));
+            { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream)); }
+            { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }
             cur ^= 1;
             // the host learns the alive count after each round; rounds stop once no ray is left
             CK(cudaMemcpyAsync(ctx->host_counters, n_alive + cur, 4, cudaMemcpyDeviceToHost, ctx->stream));
@@ -788,6 +848,32 @@ int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples) {
         unsigned long long v = 0;
         CK(cudaMemcpy(&v, ctx->sample_counter, sizeof(v), cudaMemcpyDeviceToHost));
         *n_samples = v;
+    });
+}
+
+int insta_stats_enable(insta_ctx* ctx, int stage_timing) {
+    return guarded(ctx, [&] {
+        ctx->collect_timings();
+        ctx->timing = stage_timing != 0;
+    });
+}
+
+int insta_stats_read(insta_ctx* ctx, insta_stats* out, int reset) {
+    return guarded(ctx, [&] {
+        if (!out) fail(INSTA_ERR_INVALID_ARG, "null output");
+        ctx->collect_timings();
+        out->kernel_launches = ctx->launches;
+        unsigned long long v = 0;
+        CK(cudaMemcpy(&v, ctx->sample_counter, sizeof(v), cudaMemcpyDeviceToHost));
+        out->last_render_samples = v;
+        for (int k = 0; k < INSTA_STAGE_COUNT; ++k) {
+            out->stage_ms[k] = (float)ctx->stage_ms[k];
+            out->stage_calls[k] = ctx->stage_calls[k];
+        }
+        if (reset) {
+            ctx->launches = 0;
+            for (int k = 0; k < INSTA_STAGE_COUNT; ++k) { ctx->stage_ms[k] = 0.0; ctx->stage_calls[k] = 0; }
+        }
     });
 }
 

@@ -794,3 +794,26 @@ void orc_field_eval(const orc_field_cfg *c, const uint16_t *params, const float 
         }
     }
 }
+
+/* ---------------------------------------------- single-function exports (pin tests) */
+void orc_tbn(const orc_tri *t, float *m9) { tbn_f(t, m9); }
+void orc_tri2projection(const orc_tri *t, float *M16) { tri2projection_f(t, M16); }
+/* interpolate_transformation on the float path; invert applies the 4x4 inverse. */
+void orc_interpolate_transformation(const float *p, const int32_t *adj, const orc_tri *tris, uint32_t id, int invert, float *M16) {
+    float M[16];
+    blend_projection_f(p, adj, tris, &tris[id], M);
+    if (invert) { if (!inverse4_f(M, M16)) for (int k = 0; k < 16; ++k) M16[k] = (k % 5 == 0) ? 1.f : 0.f; }
+    else memcpy(M16, M, sizeof(M));
+}
+/* transform_point / transform_direction (include/rta/affine.cuh:102-116). */
+void orc_transform(const float *p, const float *dir, const float *Mw, const float *Mc, float *out_p, float *out_d) {
+    float x4[4] = {p[0], p[1], p[2], 1.f}, l4[4], o4[4];
+    for (int r = 0; r < 4; ++r) l4[r] = row4_f(&Mw[r * 4], x4);
+    for (int r = 0; r < 4; ++r) o4[r] = row4_f(&Mc[r * 4], l4);
+    for (int k = 0; k < 3; ++k) out_p[k] = o4[k];
+    float ld[3], cd[3];
+    for (int r = 0; r < 3; ++r) { float row[3] = {Mw[r * 4], Mw[r * 4 + 1], Mw[r * 4 + 2]}; ld[r] = dot3_f(row, dir); }
+    for (int r = 0; r < 3; ++r) { float row[3] = {Mc[r * 4], Mc[r * 4 + 1], Mc[r * 4 + 2]}; cd[r] = dot3_f(row, ld); }
+    normalize3_f(cd);
+    memcpy(out_d, cd, 12);
+}

@@ -127,6 +127,12 @@ float orc_ld_random_val(uint32_t index, uint32_t seed, uint32_t dim);
 void orc_ld_random_pixel_offset(uint32_t spp, float out[2]);
 uint32_t orc_sobol(uint32_t index, uint32_t dim);
 
+/* ---- single reference functions (pin tests) ----------------------------- */
+void orc_tbn(const orc_tri *t, float *m9);
+void orc_tri2projection(const orc_tri *t, float *M16);
+void orc_interpolate_transformation(const float *p, const int32_t *adj, const orc_tri *tris, uint32_t id, int invert, float *M16);
+void orc_transform(const float *p, const float *dir, const float *Mw, const float *Mc, float *out_p, float *out_d);
+
 /* ---- half helpers ------------------------------------------------------ */
 uint16_t orc_f2h(float x);
 float orc_h2f(uint16_t h);
