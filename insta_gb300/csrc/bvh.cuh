@@ -22,6 +22,15 @@ struct Nearest {
     float d2;       // squared distance
 };
 
+// Point-box squared distance for pruning only: fused multiply-adds are fine here because the
+// prune limit carries a relative slack far larger than any rounding difference.
+__device__ __forceinline__ float box_dist_fast(float mnx, float mny, float mnz, float mxx, float mxy, float mxz, V3 p) {
+    const float dx = fmaxf(fmaxf(mnx - p.x, p.x - mxx), 0.f);
+    const float dy = fmaxf(fmaxf(mny - p.y, p.y - mxy), 0.f);
+    const float dz = fmaxf(fmaxf(mnz - p.z, p.z - mxz), 0.f);
+    return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
 __device__ __forceinline__ float prune_limit(float best) {
     return isinf(best) ? best : __fadd_rn(__fadd_rn(best, __fmul_rn(best, 0.0009765625f)), 1e-12f);
 }
@@ -60,10 +69,10 @@ __device__ __forceinline__ Nearest nearest_bvh(const FrameView& fr, V3 p, float 
         const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
         float cd[4];
         uint32_t ci[4] = {(uint32_t)ch.x, (uint32_t)ch.y, (uint32_t)ch.z, (uint32_t)ch.w};
-        cd[0] = box_distance_sq(mnx.x, mny.x, mnz.x, mxx.x, mxy.x, mxz.x, p);
-        cd[1] = box_distance_sq(mnx.y, mny.y, mnz.y, mxx.y, mxy.y, mxz.y, p);
-        cd[2] = box_distance_sq(mnx.z, mny.z, mnz.z, mxx.z, mxy.z, mxz.z, p);
-        cd[3] = box_distance_sq(mnx.w, mny.w, mnz.w, mxx.w, mxy.w, mxz.w, p);
+        cd[0] = box_dist_fast(mnx.x, mny.x, mnz.x, mxx.x, mxy.x, mxz.x, p);
+        cd[1] = box_dist_fast(mnx.y, mny.y, mnz.y, mxx.y, mxy.y, mxz.y, p);
+        cd[2] = box_dist_fast(mnx.z, mny.z, mnz.z, mxx.z, mxy.z, mxz.z, p);
+        cd[3] = box_dist_fast(mnx.w, mny.w, mnz.w, mxx.w, mxy.w, mxz.w, p);
 #pragma unroll
         for (int i = 0; i < 4; ++i)
             if (ci[i] == 0xffffffffu) cd[i] = __int_as_float(0x7f800000);
@@ -90,9 +99,10 @@ __device__ __forceinline__ Nearest nearest_bvh(const FrameView& fr, V3 p, float 
 // nearer triangle in it.  Each lane's result is exactly its own nearest triangle (the union
 // contains every node that lane's own traversal would visit); control flow stays uniform, so all
 // lanes issue together.  Lanes with active == false only ride along.
-__device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool active, uint32_t* wstack, uint32_t* err) {
+__device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool active, uint32_t* wstack, uint32_t* err,
+                                                float bound = __builtin_huge_valf()) {
     const float INF = __int_as_float(0x7f800000);
-    float best = active ? INF : -INF;
+    float best = active ? bound : -INF;
     int32_t bid = -1, bslot = -1;
     float dstack[INSTA_STACK];
     int sp = 0;
@@ -121,10 +131,10 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
         const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
         float cd[4];
         uint32_t ci[4] = {(uint32_t)ch.x, (uint32_t)ch.y, (uint32_t)ch.z, (uint32_t)ch.w};
-        cd[0] = box_distance_sq(mnx.x, mny.x, mnz.x, mxx.x, mxy.x, mxz.x, p);
-        cd[1] = box_distance_sq(mnx.y, mny.y, mnz.y, mxx.y, mxy.y, mxz.y, p);
-        cd[2] = box_distance_sq(mnx.z, mny.z, mnz.z, mxx.z, mxy.z, mxz.z, p);
-        cd[3] = box_distance_sq(mnx.w, mny.w, mnz.w, mxx.w, mxy.w, mxz.w, p);
+        cd[0] = box_dist_fast(mnx.x, mny.x, mnz.x, mxx.x, mxy.x, mxz.x, p);
+        cd[1] = box_dist_fast(mnx.y, mny.y, mnz.y, mxx.y, mxy.y, mxz.y, p);
+        cd[2] = box_dist_fast(mnx.z, mny.z, mnz.z, mxx.z, mxy.z, mxz.z, p);
+        cd[3] = box_dist_fast(mnx.w, mny.w, mnz.w, mxx.w, mxy.w, mxz.w, p);
         const float lim = prune_limit(best);
         // per child: the warp's smallest distance among lanes that need it (bits order like floats >= 0)
         uint32_t key[4];

@@ -445,7 +445,10 @@ __device__ __forceinline__ void hash_encode(const FieldView& fv, V3 x, float* ou
             w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
             uint32_t cx = gx + bx, cy = gy + by, cz = gz + bz;
             uint32_t idx;
-            if (dense) idx = (cx + cy * res + cz * res * res) % size;
+            if (dense) {
+                idx = cx + cy * res + cz * res * res;
+                if (idx >= size) idx %= size;   // only cells on the far boundary wrap
+            }
             else idx = ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
             float2 e = __half22float2(__ldg(lt + idx));
             a0 = __fadd_rn(a0, __fmul_rn(w, e.x));

@@ -372,13 +372,15 @@ __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs a) {
 // grid_to_bitfield (:585-609): one thread per bitfield byte (8 Morton-consecutive cells), each
 // cell a nearest-triangle query bounded by the marking radius.
 __global__ void __launch_bounds__(256) occupancy_kernel(FrameView fr, double radius, float bound, uint8_t* __restrict__ bits, uint32_t* err) {
+    // one thread per byte: cells far from the surface leave at the root, so per-thread queries
+    // beat a shared warp traversal here (a warp's 256 Morton-consecutive cells span ~6 cm)
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < GRID3 / 8; b += gridDim.x * blockDim.x) {
         uint8_t out = 0;
         for (uint32_t j = 0; j < 8; ++j) {
-            uint32_t cell = b * 8 + j;
-            uint32_t x = morton_invert(cell), y = morton_invert(cell >> 1), z = morton_invert(cell >> 2);
-            V3 p = v3(__fdiv_rn((float)x + 0.5f, 128.f), __fdiv_rn((float)y + 0.5f, 128.f), __fdiv_rn((float)z + 0.5f, 128.f));
-            Nearest r = nearest_bvh(fr, p, bound, -1, -1, err);
+            const uint32_t cell = b * 8 + j;
+            const uint32_t x = morton_invert(cell), y = morton_invert(cell >> 1), z = morton_invert(cell >> 2);
+            const V3 p = v3(__fdiv_rn((float)x + 0.5f, 128.f), __fdiv_rn((float)y + 0.5f, 128.f), __fdiv_rn((float)z + 0.5f, 128.f));
+            const Nearest r = nearest_bvh(fr, p, bound, -1, -1, err);
             if (r.id >= 0) {
                 uint32_t m;
                 load_centroid(fr.frames, (uint32_t)r.id, &m);
