@@ -65,7 +65,8 @@ struct Field {
 
 // Device scratch of the render wavefront, sized for the largest request seen.
 struct Wave {
-    DevBuf rays[2][4], n_round, sample_index, sample_ray, samples, tiles, aux, out, out_f32, counters;
+    DevBuf rays[2][4], n_round, sample_index, sample_ray, sample_key, sample_order, sort_bins, samples, tiles, aux, out, out_f32,
+        counters;
     uint32_t cap_rays = 0;
     uint64_t cap_samples = 0;
 };
@@ -416,7 +417,8 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     Wave& w = ctx->wave;
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 4; ++k) ctx->release(w.rays[b][k]);
-    for (DevBuf* b : {&w.n_round, &w.sample_index, &w.sample_ray, &w.samples, &w.tiles, &w.aux, &w.out, &w.out_f32, &w.counters})
+    for (DevBuf* b : {&w.n_round, &w.sample_index, &w.sample_ray, &w.sample_key, &w.sample_order, &w.sort_bins, &w.samples, &w.tiles,
+                      &w.aux, &w.out, &w.out_f32, &w.counters})
         ctx->release(*b);
     if (ctx->host_counters) cudaFreeHost(ctx->host_counters);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
@@ -758,7 +760,9 @@ int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, 
             extra = (const float*)ctx->extra.p;
         }
         // scratch: two alive-ray lists, per-round samples (STEPS per ray), encoded tiles, outputs
-        const uint32_t STEPS = 32;
+        constexpr uint32_t STEPS = 32;
+        static_assert(STEPS <= (1u << (32 - kStepShift)), "step index must fit beside the ray slot");
+        static_assert((1u << 26) <= kRayMask + 1u, "ray slots (at most 2^26 pixels) must fit below the step index");
         const TilePlan& P = a.field.plan;
         Wave& w = ctx->wave;
         const uint32_t nr = (uint32_t)npix;
@@ -774,6 +778,9 @@ int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, 
         ctx->alloc(w.samples, cap_samples * sizeof(float4));
         ctx->alloc(w.sample_ray, cap_samples * sizeof(uint32_t));
         ctx->alloc(w.sample_index, cap_samples * sizeof(uint32_t));
+        ctx->alloc(w.sample_key, cap_samples * sizeof(uint32_t));
+        ctx->alloc(w.sample_order, cap_samples * sizeof(uint32_t));
+        ctx->alloc(w.sort_bins, (kSortBins + kSortBins / kSortBlock) * sizeof(uint32_t));
         ctx->alloc(w.out, cap_samples * sizeof(uint2));
         if (a.field.view.precision == 1) ctx->alloc(w.out_f32, cap_samples * sizeof(float4));
         ctx->alloc(w.counters, 64);
@@ -796,6 +803,10 @@ int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, 
         W.samples = (float4*)w.samples.p;
         W.sample_ray = (uint32_t*)w.sample_ray.p;
         W.sample_index = (uint32_t*)w.sample_index.p;
+        W.sample_key = (uint32_t*)w.sample_key.p;
+        W.sample_order = (uint32_t*)w.sample_order.p;
+        W.sort_bins = (uint32_t*)w.sort_bins.p;
+        W.sort_block_sums = W.sort_bins + kSortBins;
         W.out = (const uint2*)w.out.p;
         W.out_f32 = (const float4*)w.out_f32.p;
         W.n_round = (uint32_t*)w.n_round.p;
@@ -823,7 +834,11 @@ int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, 
             CK(cudaMemsetAsync(n_alive + 2, 0, 4, ctx->stream));
             W.n_samples_round = n_alive + 2;
             { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_march(W, ctx->stream)); }
-            { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 1); CK(launch_deform_encode(W, ctx->stream)); }
+            {
+                Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 4);
+                CK(launch_sort_samples(W, ctx->stream));
+                CK(launch_deform_encode(W, ctx->stream));
+            }
             M.n_alive = W.n_samples_round;
             { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream)); }
             { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }

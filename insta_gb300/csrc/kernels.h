@@ -22,6 +22,12 @@ struct RayBuf {
     float4* d;
 };
 
+// Samples of a round are regrouped by spatial cell before the deform stage (a counting sort over
+// a 64^3 grid spanning the frame's mesh box, Morton-ordered cells), so the 32 samples a warp
+// queries together are neighbours in space whatever rays they came from.
+constexpr uint32_t kSortBits = 18, kSortBins = 1u << kSortBits, kSortBlock = 1024;
+constexpr uint32_t kStepShift = 27, kRayMask = (1u << kStepShift) - 1u;
+
 struct WaveArgs {
     RenderView rv;
     FrameView fr;
@@ -36,7 +42,11 @@ struct WaveArgs {
     uint32_t* n_alive_out;
     uint32_t* n_round;          // samples produced this round, per alive ray
     uint32_t* sample_index;     // [steps][n_alive]: stream position of sample k of ray r
-    uint32_t* sample_ray;       // per sample: its ray slot
+    uint32_t* sample_ray;       // per sample (march order): ray slot | step k << kStepShift
+    uint32_t* sample_key;       // per sample (march order): spatial cell of the position
+    uint32_t* sample_order;     // sorted position -> march-order sample
+    uint32_t* sort_bins;        // kSortBins cell counters, then cursors
+    uint32_t* sort_block_sums;  // per 1024 cells
     uint32_t* n_samples_round;  // device count of this round's samples
     uint32_t steps;             // samples per ray per round
     uint8_t* tiles;             // encoded input tile records
@@ -61,6 +71,7 @@ cudaError_t launch_canonical_map_coords(const FrameView* frames_dev, uint32_t n_
 
 cudaError_t launch_ray_init(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_march(const WaveArgs& a, cudaStream_t s);
+cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_deform_encode(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_composite(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_encode_coords(const FieldView& fv, const float* coords, uint32_t stride, int64_t n, uint8_t* tiles,

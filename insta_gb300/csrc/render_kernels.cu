@@ -91,7 +91,8 @@ __device__ __forceinline__ void encode_sample(const FieldView& fv, const float* 
 // a warp's 32 neighbouring rays land in one compacted block (base from a warp-aggregated atomic),
 // ordered step-major: step k of all lanes, then step k + 1.  Neighbouring entries of the stream are
 // then the same step of adjacent pixels, which keeps the cooperative BVH queries coherent.
-// sample_index[k * n_alive + r] records where sample k of ray r went.
+// sample_ray packs the ray slot and the step k; the deform stage, which runs in spatially sorted
+// order, records in sample_index[k * n_alive + r] where sample k of ray r went.
 __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ WaveArgs A) {
     const uint32_t n_alive = *A.n_alive_in;
     const RenderView& rv = A.rv;
@@ -134,8 +135,7 @@ __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ Wave
                 ray_next_sample(rv, A.bitfield, ray, pos, dt);
                 const uint32_t idx = base + offset + (uint32_t)__popc(m & lt_mask);
                 A.samples[idx] = make_float4(pos.x, pos.y, pos.z, dt);
-                A.sample_ray[idx] = r;
-                A.sample_index[(size_t)k * n_alive + r] = idx;
+                A.sample_ray[idx] = r | (k << kStepShift);
             }
             offset += (uint32_t)__popc(m);
         }
@@ -146,13 +146,135 @@ __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ Wave
     }
 }
 
-// One thread per sample of the compacted stream: the warp hook (src/core.cu:470-519) on
+// ------------------------------------------------------------------ spatial sort of a round's samples
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {   // 6 bits -> every third bit
+    v &= 63u;
+    v = (v | (v << 8)) & 0x0000f00fu;
+    v = (v | (v << 4)) & 0x000c30c3u;
+    v = (v | (v << 2)) & 0x00249249u;
+    return v;
+}
+
+// Cell of a sample: 64^3 grid over the frame mesh's box (the union of the root's child boxes)
+// widened by 1/8 on each side; positions outside fall into the border cells.
+__device__ __forceinline__ uint32_t sample_cell(const FrameView& fr, float4 p) {
+    const float4* nd = fr.nodes;
+    const float4 mnx = __ldg(nd + 0), mny = __ldg(nd + 1), mnz = __ldg(nd + 2);
+    const float4 mxx = __ldg(nd + 3), mxy = __ldg(nd + 4), mxz = __ldg(nd + 5);
+    const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
+    float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    const float cmn[4][3] = {{mnx.x, mny.x, mnz.x}, {mnx.y, mny.y, mnz.y}, {mnx.z, mny.z, mnz.z}, {mnx.w, mny.w, mnz.w}};
+    const float cmx[4][3] = {{mxx.x, mxy.x, mxz.x}, {mxx.y, mxy.y, mxz.y}, {mxx.z, mxy.z, mxz.z}, {mxx.w, mxy.w, mxz.w}};
+    const int cref[4] = {ch.x, ch.y, ch.z, ch.w};
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+        if (cref[c] != -1)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], cmn[c][k]); hi[k] = fmaxf(hi[k], cmx[c][k]); }
+    const float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), fmaxf(hi[2] - lo[2], 1e-6f)) * 1.25f;
+    const float scale = 64.f / ext;
+    const float pp[3] = {p.x, p.y, p.z};
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float c = (pp[k] - (0.5f * (lo[k] + hi[k]) - 0.5f * ext)) * scale;
+        q[k] = (uint32_t)fminf(fmaxf(c, 0.f), 63.f);
+    }
+    return spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+}
+
+// Count per cell (warp-aggregated: lanes with the same cell add once) and remember each cell.
+__global__ void __launch_bounds__(256) sort_count_kernel(const __grid_constant__ WaveArgs A) {
+    const uint32_t n = *A.n_samples_round;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += stride) {
+        const uint32_t s = b + threadIdx.x;
+        const bool valid = s < n;
+        const uint32_t cell = valid ? sample_cell(A.fr, A.samples[s]) : 0xffffffffu;
+        if (valid) A.sample_key[s] = cell;
+        const uint32_t peers = __match_any_sync(0xffffffffu, cell);
+        if (valid && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(A.sort_bins + cell, (uint32_t)__popc(peers));
+    }
+}
+
+// Exclusive scan of each block of kSortBlock cell counts, in place; block totals to sort_block_sums.
+__global__ void __launch_bounds__(kSortBlock) sort_scan_kernel(uint32_t* bins, uint32_t* block_sums) {
+    __shared__ uint32_t warp_tot[kSortBlock / 32];
+    const uint32_t i = blockIdx.x * kSortBlock + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t v = bins[i];
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= (uint32_t)o) t += y;
+        }
+        warp_tot[lane] = t;   // inclusive
+    }
+    __syncthreads();
+    const uint32_t before = warp ? warp_tot[warp - 1] : 0u;
+    bins[i] = before + x - v;
+    if (threadIdx.x == kSortBlock - 1) block_sums[blockIdx.x] = before + x;
+}
+
+// Place every sample: its cell's start plus a running cursor (warp-aggregated).  Order within a
+// cell is arbitrary; each sample's result does not depend on it.
+__global__ void __launch_bounds__(256) sort_place_kernel(const __grid_constant__ WaveArgs A) {
+    constexpr uint32_t NB = kSortBins / kSortBlock;
+    __shared__ uint32_t block_off[NB];
+    static_assert(NB == 256, "one block-sum per thread");
+    {
+        const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+        __shared__ uint32_t wt[8];
+        const uint32_t v = A.sort_block_sums[threadIdx.x];
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) wt[warp] = x;
+        __syncthreads();
+        uint32_t before = 0;
+        for (uint32_t w = 0; w < warp; ++w) before += wt[w];
+        block_off[threadIdx.x] = before + x - v;
+        __syncthreads();
+    }
+    const uint32_t n = *A.n_samples_round;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += stride) {
+        const uint32_t s = b + threadIdx.x;
+        const bool valid = s < n;
+        const uint32_t cell = valid ? A.sample_key[s] : 0xffffffffu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, cell);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (valid && lane == (uint32_t)leader) base = atomicAdd(A.sort_bins + cell, (uint32_t)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (valid) A.sample_order[block_off[cell / kSortBlock] + base + (uint32_t)__popc(peers & lt_mask)] = s;
+    }
+}
+
+// One thread per sample, in spatially sorted order: the warp hook (src/core.cu:470-519) on
 // warp_position(pos) / warp_direction(dir), then the hash encode and SH written as tensor-core
-// operand rows.  Neighbouring threads hold consecutive samples of a ray, so their BVH walks are
-// coherent.
+// operand rows at the sample's sorted position.  A warp's 32 samples share a few grid cells, so
+// the cooperative BVH walk visits a small union of nodes.
 __global__ void __launch_bounds__(256, 4) deform_encode_kernel(const __grid_constant__ WaveArgs A) {
     __shared__ uint32_t wstack[8][INSTA_STACK];
     const uint32_t n = *A.n_samples_round;
+    const uint32_t n_alive = *A.n_alive_in;
     const RenderView& rv = A.rv;
     const V3 cam_fwd = v3(rv.cam[2], rv.cam[6], rv.cam[10]);
     const V3 cam_pos = v3(rv.cam[3], rv.cam[7], rv.cam[11]);
@@ -160,12 +282,15 @@ __global__ void __launch_bounds__(256, 4) deform_encode_kernel(const __grid_cons
     const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
     // warps step through the stream in lockstep chunks of 32 so every lane joins the cooperative query
     for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32u; base < n; base += n_warps * 32u) {
-        const uint32_t s = base + lane;
+        const uint32_t s = base + lane;   // position in sorted order: tile row and output slot
         const bool valid = s < n;
         float4 smp = make_float4(0.5f, 0.5f, 0.5f, 0.f), rb = make_float4(0.f, 0.f, 1.f, 0.f);
         if (valid) {
-            smp = A.samples[s];
-            rb = A.rays_in.b[A.sample_ray[s]];
+            const uint32_t m = A.sample_order[s];
+            const uint32_t rk = A.sample_ray[m];
+            smp = A.samples[m];
+            rb = A.rays_in.b[rk & kRayMask];
+            A.sample_index[(size_t)(rk >> kStepShift) * n_alive + (rk & kRayMask)] = s;
         }
         float cw[3], dw[3], dp[3];
         const float pp[3] = {smp.x, smp.y, smp.z}, dd[3] = {rb.x, rb.y, rb.z};
@@ -394,6 +519,15 @@ cudaError_t launch_ray_init(const WaveArgs& a, cudaStream_t s) {
 
 cudaError_t launch_march(const WaveArgs& a, cudaStream_t s) {
     march_kernel<<<sm_count() * 8, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(a.sort_bins, 0, kSortBins * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    sort_count_kernel<<<sm_count() * 8, 256, 0, s>>>(a);
+    sort_scan_kernel<<<kSortBins / kSortBlock, kSortBlock, 0, s>>>(a.sort_bins, a.sort_block_sums);
+    sort_place_kernel<<<sm_count() * 8, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
