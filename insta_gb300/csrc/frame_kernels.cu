@@ -369,25 +369,27 @@ __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs a) {
 
 // --------------------------------------------------------------------- occupancy
 // mark_flame_density_grid (ngp/src/testbed_nerf.cu:364-389) over the deformed mesh, fused with
-// grid_to_bitfield (:585-609): one thread per bitfield byte (8 Morton-consecutive cells), each
-// cell a nearest-triangle query bounded by the marking radius.
+// grid_to_bitfield (:585-609): one thread per cell, a nearest-triangle query bounded by the marking
+// radius; a warp covers 32 Morton-consecutive cells and writes their bits as one 32-bit word.
+// One cell per thread (not eight) spreads the few expensive cells near the surface over many warps;
+// per-thread queries beat a shared warp traversal here because most cells leave at the root.
 __global__ void __launch_bounds__(256) occupancy_kernel(FrameView fr, double radius, float bound, uint8_t* __restrict__ bits, uint32_t* err) {
-    // one thread per byte: cells far from the surface leave at the root, so per-thread queries
-    // beat a shared warp traversal here (a warp's 256 Morton-consecutive cells span ~6 cm)
-    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < GRID3 / 8; b += gridDim.x * blockDim.x) {
-        uint8_t out = 0;
-        for (uint32_t j = 0; j < 8; ++j) {
-            const uint32_t cell = b * 8 + j;
-            const uint32_t x = morton_invert(cell), y = morton_invert(cell >> 1), z = morton_invert(cell >> 2);
-            const V3 p = v3(__fdiv_rn((float)x + 0.5f, 128.f), __fdiv_rn((float)y + 0.5f, 128.f), __fdiv_rn((float)z + 0.5f, 128.f));
-            const Nearest r = nearest_bvh(fr, p, bound, -1, -1, err);
-            if (r.id >= 0) {
-                uint32_t m;
-                load_centroid(fr.frames, (uint32_t)r.id, &m);
-                if ((double)__fsqrt_rn(r.d2) < radius && m != 0u) out |= (uint8_t)(1u << j);
-            }
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32u; base < GRID3; base += n_warps * 32u) {
+        const uint32_t cell = base + lane;
+        const uint32_t x = morton_invert(cell), y = morton_invert(cell >> 1), z = morton_invert(cell >> 2);
+        const V3 p = v3(__fdiv_rn((float)x + 0.5f, 128.f), __fdiv_rn((float)y + 0.5f, 128.f), __fdiv_rn((float)z + 0.5f, 128.f));
+        const Nearest r = nearest_bvh(fr, p, bound, -1, -1, err);
+        bool on = false;
+        if (r.id >= 0) {
+            uint32_t m;
+            load_centroid(fr.frames, (uint32_t)r.id, &m);
+            on = (double)__fsqrt_rn(r.d2) < radius && m != 0u;
         }
-        bits[b] = out;
+        // bit j of byte b is cell 8b + j: the ballot word is the four bytes of this warp's cells
+        const uint32_t word = __ballot_sync(0xffffffffu, on);
+        if (lane == 0) reinterpret_cast<uint32_t*>(bits)[base >> 5] = word;
     }
 }
 
