@@ -172,7 +172,15 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
 /* out_rgba f32[h*w*4] (linear RGBA, zero background), out_depth f32[h*w] (1e10 where no
  * hit).  Host pointers: the call returns after the copy back; device pointers: asynchronous. */
 int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, float* out_depth);
-/* Network samples evaluated by the last insta_render (synchronises). */
+/* n requests rendered through one wavefront: each round marches, deforms, encodes, evaluates and
+ * composites the alive rays of every request with one set of launches.  Requests may mix avatars,
+ * frames, cameras and resolutions; their avatars must share one field layout (same
+ * insta_field_desc).  out_rgba[i] / out_depth[i] as for insta_render (host or device, per
+ * request).  Each request's pixels equal those of insta_render on that request alone.  At most
+ * 4096 requests and 2^26 pixels per batch.  No reference counterpart: render_nerf renders one
+ * view at a time (instant-ngp/src/testbed_nerf.cu:2320). */
+int insta_render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* const* out_rgba, float* const* out_depth);
+/* Network samples evaluated by the last insta_render / insta_render_batch (synchronises). */
 int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples);
 /* Per-ray sample t and dt (device pointers, [h*w][max_out]) and counts [h*w]. */
 int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out, float* out_t, float* out_dt,

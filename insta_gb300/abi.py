@@ -22,7 +22,8 @@ EXPORTS = [
     "insta_canonical_set", "insta_avatar_set_boxes", "insta_avatar_set_flags", "insta_frame_upload",
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_field_param_count", "insta_params_load",
-    "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_samples", "insta_march_debug",
+    "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_batch",
+    "insta_render_samples", "insta_march_debug",
 ]
 
 
@@ -90,6 +91,7 @@ def load(path: Path | None = None):
             "insta_field_eval": [vp, C.c_int, vp, u32, i64, vp],
             "insta_field_eval_static": [vp, C.c_int, vp, u32, i64, vp],
             "insta_render": [vp, C.POINTER(RenderDesc), vp, vp],
+            "insta_render_batch": [vp, C.POINTER(RenderDesc), C.c_int, C.POINTER(vp), C.POINTER(vp)],
             "insta_render_samples": [vp, C.POINTER(u64)],
             "insta_march_debug": [vp, C.POINTER(RenderDesc), C.c_int, vp, vp, vp],
         }
@@ -251,6 +253,14 @@ class Context:
 
     def render(self, req: RenderDesc, out_rgba, out_depth):
         self._check(self.lib.insta_render(self.h, C.byref(req), _addr(out_rgba), _addr(out_depth)))
+
+    def render_batch(self, reqs, out_rgba, out_depth):
+        """reqs: list of RenderDesc; out_rgba / out_depth: lists of buffers (one pair per request)."""
+        n = len(reqs)
+        arr = (RenderDesc * n)(*reqs)
+        pr = (C.c_void_p * n)(*[_addr(b).value for b in out_rgba])
+        pd = (C.c_void_p * n)(*[_addr(b).value for b in out_depth])
+        self._check(self.lib.insta_render_batch(self.h, arr, n, pr, pd))
 
     def render_samples(self) -> int:
         v = C.c_uint64(0)

@@ -423,8 +423,8 @@ __device__ __forceinline__ bool ray_next_sample(const RenderView& rv, const uint
 // Published multiresolution hash encoding, this library's documented table layout
 // (per-level dense index x + y*res + z*res^2 or spatial hash with primes
 // 1, 2654435761, 805459861; trilinear weights; FP32 accumulation).
-__device__ __forceinline__ void hash_encode(const FieldView& fv, V3 x, float* out) {
-    const __half2* table = reinterpret_cast<const __half2*>(fv.table);
+__device__ __forceinline__ void hash_encode(const FieldView& fv, const uint16_t* params, V3 x, float* out) {
+    const __half2* table = reinterpret_cast<const __half2*>(params);
     // levels unrolled by four so 32 independent gathers are in flight per thread
 #pragma unroll 4
     for (int l = 0; l < (int)fv.n_levels; ++l) {

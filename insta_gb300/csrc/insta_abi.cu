@@ -66,7 +66,7 @@ struct Field {
 // Device scratch of the render wavefront, sized for the largest request seen.
 struct Wave {
     DevBuf rays[2][4], n_round, sample_index, sample_ray, sample_key, sample_order, sort_bins, samples, tiles, aux, out, out_f32,
-        counters;
+        counters, req_table, req_meta;
     uint32_t cap_rays = 0;
     uint64_t cap_samples = 0;
 };
@@ -363,6 +363,204 @@ void check_request(const insta_render_desc* r) {
     if (r->cone_angle < 0.f) fail(INSTA_ERR_INVALID_ARG, "cone_angle must be >= 0");
 }
 
+// Largest number of samples one round may produce (bounds the per-sample scratch, ~160 B each).
+constexpr uint64_t kMaxRoundSamples = 32ull << 20;
+constexpr uint32_t kMaxSteps = 32;
+static_assert(kMaxSteps <= (1u << (32 - kStepShift)), "step index must fit beside the ray slot");
+static_assert((1u << 26) <= kRayMask + 1u, "ray slots (at most 2^26 pixels per batch) must fit below the step index");
+
+bool same_field_layout(const Field& a, const Field& b) {
+    return std::memcmp(&a.plan, &b.plan, sizeof(TilePlan)) == 0 && a.view.n_levels == b.view.n_levels &&
+           a.view.n_features == b.view.n_features && a.view.n_extra == b.view.n_extra && a.view.precision == b.view.precision &&
+           std::memcmp(a.view.level_scale, b.view.level_scale, sizeof(a.view.level_scale)) == 0 &&
+           std::memcmp(a.view.level_res, b.view.level_res, sizeof(a.view.level_res)) == 0 &&
+           std::memcmp(a.view.level_size, b.view.level_size, sizeof(a.view.level_size)) == 0 &&
+           std::memcmp(a.view.level_off, b.view.level_off, sizeof(a.view.level_off)) == 0 &&
+           std::memcmp(a.view.level_dense, b.view.level_dense, sizeof(a.view.level_dense)) == 0;
+}
+
+// Testbed::render_nerf for a batch of requests (avatars, frames, cameras, resolutions) through one
+// wavefront: every round marches all alive rays of all requests, sorts their samples by
+// (request, cell), runs deform + encode, the MLP tiles and the composite.  The host reads the
+// alive count between rounds (NerfTracer::trace does the same, testbed_nerf.cu:2164-2165).
+void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* const* out_rgba, float* const* out_depth) {
+    if (n <= 0 || (uint32_t)n > kMaxRequests) fail(INSTA_ERR_INVALID_ARG, "batch size %d outside 1..%u", n, kMaxRequests);
+    std::vector<ReqView> views((size_t)n);
+    const Field* field0 = nullptr;
+    uint64_t total_pix = 0, host_pix = 0;
+    uint32_t total_tiles = 0, max_spr = 0;
+    std::vector<int> on_host((size_t)n, 0);
+    for (int i = 0; i < n; ++i) {
+        const insta_render_desc* r = reqs + i;
+        check_request(r);
+        if (!out_rgba[i] || !out_depth[i]) fail(INSTA_ERR_INVALID_ARG, "null output buffers for request %d", i);
+        Avatar& a = ctx->avatar(r->avatar);
+        if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", r->avatar);
+        Frame& f = get_frame(a, r->frame);
+        if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", r->frame);
+        if (!field0) field0 = &a.field;
+        else if (!same_field_layout(*field0, a.field))
+            fail(INSTA_ERR_UNSUPPORTED, "requests of one batch must share the field layout (request %d differs)", i);
+        ReqView& v = views[(size_t)i];
+        v.rv = render_view(a, *r);
+        v.fr = f.view;
+        v.dv = deform_view(a);
+        v.table = a.field.view.table;
+        v.mlp = a.field.view.mlp_smem;
+        v.bitfield = (const uint8_t*)f.bitfield.p;
+        v.tiles_x = ((uint32_t)r->width + 7) / 8;
+        v.tile_first = total_tiles;
+        total_tiles += v.tiles_x * (((uint32_t)r->height + 3) / 4);
+        const uint64_t px = (uint64_t)r->width * r->height;
+        total_pix += px;
+        on_host[(size_t)i] = !(is_device_ptr(out_rgba[i]) && is_device_ptr(out_depth[i]));
+        if (on_host[(size_t)i]) host_pix += px;
+        max_spr = std::max(max_spr, v.rv.max_samples_per_ray);
+    }
+    if (total_pix > ((uint64_t)1 << 26)) fail(INSTA_ERR_INVALID_ARG, "a batch holds at most 2^26 pixels, got %llu", (unsigned long long)total_pix);
+    const FieldView& fv = field0->view;
+    const TilePlan& P = field0->plan;
+    Wave& w = ctx->wave;
+    const uint32_t nr = (uint32_t)total_pix;
+    // outputs: device pointers directly, host pointers through one staging buffer
+    float* stage_rgba = nullptr;
+    float* stage_depth = nullptr;
+    if (host_pix) {
+        stage_rgba = (float*)ctx->alloc(ctx->out_rgba, host_pix * 16);
+        stage_depth = (float*)ctx->alloc(ctx->out_depth, host_pix * 4);
+    }
+    // per-request expression dims (host arrays) into one device block
+    const uint32_t n_extra = fv.n_extra;
+    std::vector<float> extra;
+    if (n_extra) {
+        extra.assign((size_t)n * n_extra, 0.f);
+        for (int i = 0; i < n; ++i)
+            if (reqs[i].extra_dims) std::memcpy(extra.data() + (size_t)i * n_extra, reqs[i].extra_dims, n_extra * 4);
+        ctx->alloc(ctx->extra, extra.size() * 4);
+    }
+    {
+        uint64_t off = 0;
+        for (int i = 0; i < n; ++i) {
+            ReqView& v = views[(size_t)i];
+            if (on_host[(size_t)i]) {
+                v.out_rgba = stage_rgba + off * 4;
+                v.out_depth = stage_depth + off;
+                off += (uint64_t)reqs[i].width * reqs[i].height;
+            } else {
+                v.out_rgba = out_rgba[i];
+                v.out_depth = out_depth[i];
+            }
+            v.extra = n_extra ? (const float*)ctx->extra.p + (size_t)i * n_extra : nullptr;
+        }
+    }
+    // scratch
+    const uint64_t round_cap = std::min<uint64_t>((uint64_t)nr * kMaxSteps, kMaxRoundSamples);
+    const uint64_t cap_samples = (round_cap + (uint64_t)n * 128 + 127) / 128 * 128;
+    const uint32_t cell_bits = sort_cell_bits((uint32_t)n);
+    const uint64_t n_bins = (uint64_t)n << cell_bits;
+    if (w.cap_rays < nr) {
+        for (int b = 0; b < 2; ++b)
+            for (int k = 0; k < 4; ++k) ctx->alloc(w.rays[b][k], (size_t)nr * 16);
+        ctx->alloc(w.n_round, (size_t)nr * 4);
+        w.cap_rays = nr;
+    }
+    ctx->alloc(w.tiles, cap_samples / 128 * P.tile_bytes);
+    ctx->alloc(w.aux, cap_samples * sizeof(float2));
+    ctx->alloc(w.samples, cap_samples * sizeof(float4));
+    ctx->alloc(w.sample_ray, cap_samples * sizeof(uint32_t));
+    ctx->alloc(w.sample_index, cap_samples * sizeof(uint32_t));
+    ctx->alloc(w.sample_key, cap_samples * sizeof(uint32_t));
+    ctx->alloc(w.sample_order, cap_samples * sizeof(uint32_t));
+    ctx->alloc(w.sort_bins, (n_bins + n_bins / kSortBlock) * sizeof(uint32_t));
+    ctx->alloc(w.out, cap_samples * sizeof(uint2));
+    if (fv.precision == 1) ctx->alloc(w.out_f32, cap_samples * sizeof(float4));
+    ctx->alloc(w.counters, 64);
+    ctx->alloc(w.req_table, (size_t)n * sizeof(ReqView));
+    ctx->alloc(w.req_meta, (size_t)(n + 1) * 2 * sizeof(uint32_t));
+    if (!ctx->host_counters) CK(cudaMallocHost(&ctx->host_counters, 64));
+    if (n_extra) CK(cudaMemcpyAsync(ctx->extra.p, extra.data(), extra.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(w.req_table.p, views.data(), (size_t)n * sizeof(ReqView), cudaMemcpyHostToDevice, ctx->stream));
+    uint32_t* counters = (uint32_t*)w.counters.p;   // [0], [1]: ping-pong alive counts; [2]: round samples; [3]: padded
+    WaveArgs W{};
+    W.reqs = (const ReqView*)w.req_table.p;
+    W.n_reqs = (uint32_t)n;
+    W.cell_bits = cell_bits;
+    W.fv = fv;
+    W.tiles = (uint8_t*)w.tiles.p;
+    W.tile_bytes = P.tile_bytes;
+    W.k_in = P.k_in;
+    W.aux = (float2*)w.aux.p;
+    W.samples = (float4*)w.samples.p;
+    W.sample_ray = (uint32_t*)w.sample_ray.p;
+    W.sample_index = (uint32_t*)w.sample_index.p;
+    W.sample_key = (uint32_t*)w.sample_key.p;
+    W.sample_order = (uint32_t*)w.sample_order.p;
+    W.sort_bins = (uint32_t*)w.sort_bins.p;
+    W.sort_block_sums = W.sort_bins + n_bins;
+    W.req_start = (uint32_t*)w.req_meta.p;
+    W.req_seg = W.req_start + (n + 1);
+    W.n_samples_round = counters + 2;
+    W.n_samples_padded = counters + 3;
+    W.out = (const uint2*)w.out.p;
+    W.out_f32 = (const float4*)w.out_f32.p;
+    W.n_round = (uint32_t*)w.n_round.p;
+    W.sample_counter = ctx->sample_counter;
+    W.err = ctx->err_dev;
+    auto rays = [&](int b) {
+        return RayBuf{(float4*)w.rays[b][0].p, (float4*)w.rays[b][1].p, (float4*)w.rays[b][2].p, (float4*)w.rays[b][3].p};
+    };
+    MlpArgs M{};
+    M.fv = fv; M.plan = P; M.tiles = W.tiles;
+    M.out = (uint2*)w.out.p; M.out_f32 = (float4*)w.out_f32.p; M.err = ctx->err_dev;
+    M.n_alive = W.n_samples_padded;
+    M.seg = W.req_seg; M.reqs = W.reqs; M.n_reqs = (uint32_t)n;
+    CK(cudaMemsetAsync(ctx->sample_counter, 0, sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(counters, 0, 8, ctx->stream));
+    W.rays_out = rays(0);
+    W.n_alive_out = counters;
+    { Stage st(ctx, INSTA_STAGE_RAY_INIT, 1); CK(launch_ray_init(W, total_tiles, ctx->stream)); }
+    int cur = 0;
+    auto read_alive = [&](int b) {
+        CK(cudaMemcpyAsync(ctx->host_counters, counters + b, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        return ctx->host_counters[0];
+    };
+    // the first round's step count needs the alive count only when all pixels could not take
+    // kMaxSteps samples each; otherwise the pixel count stands in for it (no host round trip)
+    uint32_t n_alive = (uint64_t)nr * kMaxSteps <= round_cap ? nr : read_alive(cur);
+    for (uint32_t round = 0; n_alive > 0 && round < max_spr + 2; ++round) {
+        const uint32_t steps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(kMaxSteps, round_cap / n_alive));
+        W.steps = steps;
+        W.rays_in = rays(cur);
+        W.rays_out = rays(cur ^ 1);
+        W.n_alive_in = counters + cur;
+        W.n_alive_out = counters + (cur ^ 1);
+        CK(cudaMemsetAsync(counters + (cur ^ 1), 0, 4, ctx->stream));
+        CK(cudaMemsetAsync(counters + 2, 0, 4, ctx->stream));
+        { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_march(W, ctx->stream)); }
+        {
+            Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 5);
+            CK(launch_sort_samples(W, ctx->stream));
+            CK(launch_deform_encode(W, ctx->stream));
+        }
+        { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream)); }
+        { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }
+        cur ^= 1;
+        n_alive = read_alive(cur);
+    }
+    if (host_pix) {
+        uint64_t off = 0;
+        for (int i = 0; i < n; ++i) {
+            if (!on_host[(size_t)i]) continue;
+            const size_t px = (size_t)reqs[i].width * reqs[i].height;
+            CK(cudaMemcpyAsync(out_rgba[i], stage_rgba + off * 4, px * 16, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(out_depth[i], stage_depth + off, px * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            off += px;
+        }
+        ctx->check_device();
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -418,7 +616,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 4; ++k) ctx->release(w.rays[b][k]);
     for (DevBuf* b : {&w.n_round, &w.sample_index, &w.sample_ray, &w.sample_key, &w.sample_order, &w.sort_bins, &w.samples, &w.tiles,
-                      &w.aux, &w.out, &w.out_f32, &w.counters})
+                      &w.aux, &w.out, &w.out_f32, &w.counters, &w.req_table, &w.req_meta})
         ctx->release(*b);
     if (ctx->host_counters) cudaFreeHost(ctx->host_counters);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
@@ -702,7 +900,7 @@ int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t s
         Stage st(ctx, INSTA_STAGE_FIELD, 3);
         CK(launch_encode_coords(a.field.view, coords, stride, n, (uint8_t*)w.tiles.p, P.tile_bytes, P.k_in, ctx->stream));
         MlpArgs m{};
-        m.fv = a.field.view; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.steps = 1; m.n_samples = n;
+        m.fv = a.field.view; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.n_samples = n;
         m.out = (uint2*)w.out.p; m.out_f32 = (float4*)w.out_f32.p; m.err = ctx->err_dev;
         CK(launch_mlp(m, (uint32_t)tiles, ctx->stream));
         CK(launch_unpack((const uint2*)w.out.p, (const float4*)w.out_f32.p, a.field.view.precision == 1, n, (float4*)out4, ctx->stream));
@@ -728,7 +926,7 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
         Stage st(ctx, INSTA_STAGE_FIELD, 3);
         CK(launch_encode_coords(a.field.view, coords, stride, n, tiles, P.tile_bytes, P.k_in, ctx->stream));
         MlpArgs m{};
-        m.fv = a.field.view; m.plan = P; m.tiles = tiles; m.n_alive = nullptr; m.steps = 1; m.n_samples = n;
+        m.fv = a.field.view; m.plan = P; m.tiles = tiles; m.n_alive = nullptr; m.n_samples = n;
         m.out = out; m.out_f32 = out_f32; m.err = ctx->err_dev;
         CK(launch_mlp(m, (uint32_t)n_tiles, ctx->stream));
         CK(launch_unpack(out, out_f32, a.field.view.precision == 1, n, (float4*)out4, ctx->stream));
@@ -736,123 +934,13 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
 }
 
 int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, float* out_depth) {
+    return guarded(ctx, [&] { render_batch(ctx, req, 1, &out_rgba, &out_depth); });
+}
+
+int insta_render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* const* out_rgba, float* const* out_depth) {
     return guarded(ctx, [&] {
-        check_request(req);
-        if (!out_rgba || !out_depth) fail(INSTA_ERR_INVALID_ARG, "null output buffers");
-        Avatar& a = ctx->avatar(req->avatar);
-        if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", req->avatar);
-        Frame& f = get_frame(a, req->frame);
-        if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", req->frame);
-        const size_t npix = (size_t)req->width * req->height;
-        bool dev_out = is_device_ptr(out_rgba) && is_device_ptr(out_depth);
-        float* rgba = out_rgba;
-        float* depth = out_depth;
-        if (!dev_out) {
-            rgba = (float*)ctx->alloc(ctx->out_rgba, npix * 16);
-            depth = (float*)ctx->alloc(ctx->out_depth, npix * 4);
-        }
-        const float* extra = nullptr;
-        if (a.field.desc.n_extra_dims) {
-            ctx->alloc(ctx->extra, 64 * 4);
-            std::vector<float> e(a.field.desc.n_extra_dims, 0.f);
-            if (req->extra_dims) std::memcpy(e.data(), req->extra_dims, e.size() * 4);
-            CK(cudaMemcpyAsync(ctx->extra.p, e.data(), e.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-            extra = (const float*)ctx->extra.p;
-        }
-        // scratch: two alive-ray lists, per-round samples (STEPS per ray), encoded tiles, outputs
-        constexpr uint32_t STEPS = 32;
-        static_assert(STEPS <= (1u << (32 - kStepShift)), "step index must fit beside the ray slot");
-        static_assert((1u << 26) <= kRayMask + 1u, "ray slots (at most 2^26 pixels) must fit below the step index");
-        const TilePlan& P = a.field.plan;
-        Wave& w = ctx->wave;
-        const uint32_t nr = (uint32_t)npix;
-        const uint64_t cap_samples = (uint64_t)((nr + 127) / 128 * 128) * STEPS;
-        if (w.cap_rays < nr) {
-            for (int b = 0; b < 2; ++b)
-                for (int k = 0; k < 4; ++k) ctx->alloc(w.rays[b][k], (size_t)nr * 16);
-            ctx->alloc(w.n_round, (size_t)nr * 4);
-            w.cap_rays = nr;
-        }
-        ctx->alloc(w.tiles, cap_samples / 128 * P.tile_bytes);
-        ctx->alloc(w.aux, cap_samples * sizeof(float2));
-        ctx->alloc(w.samples, cap_samples * sizeof(float4));
-        ctx->alloc(w.sample_ray, cap_samples * sizeof(uint32_t));
-        ctx->alloc(w.sample_index, cap_samples * sizeof(uint32_t));
-        ctx->alloc(w.sample_key, cap_samples * sizeof(uint32_t));
-        ctx->alloc(w.sample_order, cap_samples * sizeof(uint32_t));
-        ctx->alloc(w.sort_bins, (kSortBins + kSortBins / kSortBlock) * sizeof(uint32_t));
-        ctx->alloc(w.out, cap_samples * sizeof(uint2));
-        if (a.field.view.precision == 1) ctx->alloc(w.out_f32, cap_samples * sizeof(float4));
-        ctx->alloc(w.counters, 64);
-        if (!ctx->host_counters) CK(cudaMallocHost(&ctx->host_counters, 64));
-        uint32_t* n_alive = (uint32_t*)w.counters.p;   // [0], [1]: ping-pong alive counts; [2]: samples this round
-        WaveArgs W{};
-        W.rv = render_view(a, *req);
-        W.fr = f.view;
-        W.dv = deform_view(a);
-        W.fv = a.field.view;
-        W.bitfield = (const uint8_t*)f.bitfield.p;
-        W.extra_dims = extra;
-        W.out_rgba = rgba;
-        W.out_depth = depth;
-        W.steps = STEPS;
-        W.tiles = (uint8_t*)w.tiles.p;
-        W.tile_bytes = P.tile_bytes;
-        W.k_in = P.k_in;
-        W.aux = (float2*)w.aux.p;
-        W.samples = (float4*)w.samples.p;
-        W.sample_ray = (uint32_t*)w.sample_ray.p;
-        W.sample_index = (uint32_t*)w.sample_index.p;
-        W.sample_key = (uint32_t*)w.sample_key.p;
-        W.sample_order = (uint32_t*)w.sample_order.p;
-        W.sort_bins = (uint32_t*)w.sort_bins.p;
-        W.sort_block_sums = W.sort_bins + kSortBins;
-        W.out = (const uint2*)w.out.p;
-        W.out_f32 = (const float4*)w.out_f32.p;
-        W.n_round = (uint32_t*)w.n_round.p;
-        W.sample_counter = ctx->sample_counter;
-        W.err = ctx->err_dev;
-        auto rays = [&](int b) {
-            return RayBuf{(float4*)w.rays[b][0].p, (float4*)w.rays[b][1].p, (float4*)w.rays[b][2].p, (float4*)w.rays[b][3].p};
-        };
-        MlpArgs M{};
-        M.fv = a.field.view; M.plan = P; M.tiles = W.tiles; M.steps = STEPS;
-        M.out = (uint2*)w.out.p; M.out_f32 = (float4*)w.out_f32.p; M.err = ctx->err_dev;
-        CK(cudaMemsetAsync(ctx->sample_counter, 0, sizeof(unsigned long long), ctx->stream));
-        CK(cudaMemsetAsync(n_alive, 0, 8, ctx->stream));
-        W.rays_out = rays(0);
-        W.n_alive_out = n_alive;
-        { Stage st(ctx, INSTA_STAGE_RAY_INIT, 1); CK(launch_ray_init(W, ctx->stream)); }
-        int cur = 0;
-        const uint32_t max_rounds = (W.rv.max_samples_per_ray + STEPS - 1) / STEPS + 1;
-        for (uint32_t round = 0; round < max_rounds; ++round) {
-            W.rays_in = rays(cur);
-            W.rays_out = rays(cur ^ 1);
-            W.n_alive_in = n_alive + cur;
-            W.n_alive_out = n_alive + (cur ^ 1);
-            CK(cudaMemsetAsync(n_alive + (cur ^ 1), 0, 4, ctx->stream));
-            CK(cudaMemsetAsync(n_alive + 2, 0, 4, ctx->stream));
-            W.n_samples_round = n_alive + 2;
-            { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_march(W, ctx->stream)); }
-            {
-                Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 4);
-                CK(launch_sort_samples(W, ctx->stream));
-                CK(launch_deform_encode(W, ctx->stream));
-            }
-            M.n_alive = W.n_samples_round;
-            { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream)); }
-            { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }
-            cur ^= 1;
-            // the host learns the alive count after each round; rounds stop once no ray is left
-            CK(cudaMemcpyAsync(ctx->host_counters, n_alive + cur, 4, cudaMemcpyDeviceToHost, ctx->stream));
-            CK(cudaStreamSynchronize(ctx->stream));
-            if (ctx->host_counters[0] == 0) break;
-        }
-        if (!dev_out) {
-            CK(cudaMemcpyAsync(out_rgba, rgba, npix * 16, cudaMemcpyDeviceToHost, ctx->stream));
-            CK(cudaMemcpyAsync(out_depth, depth, npix * 4, cudaMemcpyDeviceToHost, ctx->stream));
-            ctx->check_device();
-        }
+        if (!reqs || !out_rgba || !out_depth) fail(INSTA_ERR_INVALID_ARG, "null request or output arrays");
+        render_batch(ctx, reqs, n, out_rgba, out_depth);
     });
 }
 

@@ -14,7 +14,7 @@ struct TriFrame;
 struct TilePlan;
 
 // Alive-ray list, structure of arrays (float4 each):
-//   a = (origin.xyz, t)   b = (dir.xyz, max_weight)   c = rgba   d = (depth, pixel, samples so far, previous slot)
+//   a = (origin.xyz, t)   b = (dir.xyz, max_weight)   c = rgba   d = (depth, pixel, samples so far, request)
 struct RayBuf {
     float4* a;
     float4* b;
@@ -22,32 +22,59 @@ struct RayBuf {
     float4* d;
 };
 
-// Samples of a round are regrouped by spatial cell before the deform stage (a counting sort over
-// a 64^3 grid spanning the frame's mesh box, Morton-ordered cells), so the 32 samples a warp
-// queries together are neighbours in space whatever rays they came from.
-constexpr uint32_t kSortBits = 18, kSortBins = 1u << kSortBits, kSortBlock = 1024;
-constexpr uint32_t kStepShift = 27, kRayMask = (1u << kStepShift) - 1u;
-
-struct WaveArgs {
+// One render request of a batch: its camera, its frame's BVH and triangle frames, its avatar's
+// deformation data, hash table and MLP weight image, its occupancy bits and its output buffers.
+// All requests of a batch share one field layout (levels, widths), so the level tables and the
+// MLP tile plan come from the batch, and only the parameter pointers differ per request.
+struct ReqView {
     RenderView rv;
     FrameView fr;
     DeformView dv;
-    FieldView fv;
+    const uint16_t* table;
+    const uint8_t* mlp;
     const uint8_t* bitfield;
-    const float* extra_dims;
+    const float* extra;         // n_extra floats on the device, or null (zeros)
     float* out_rgba;
     float* out_depth;
+    uint32_t tile_first;        // first 8x4-pixel ray tile of this request within the batch
+    uint32_t tiles_x;           // ray tiles per image row
+};
+
+// Samples of a round are regrouped before the deform stage by a counting sort on
+// (request, spatial cell): cells are a Morton-ordered grid over each frame's mesh box, so the
+// 32 samples a warp queries together belong to one frame and are neighbours in space whatever
+// rays they came from.  Each request's run of samples is padded to a multiple of 128 so every
+// MLP tile belongs to one request (one avatar's weights).
+constexpr uint32_t kSortBlock = 1024, kMaxSortBins = 1u << 24, kMaxRequests = 4096;
+constexpr uint32_t kStepShift = 27, kRayMask = (1u << kStepShift) - 1u;
+constexpr uint32_t kNoSample = 0xffffffffu;
+
+// cell bits per request (multiple of 3, >= 12) so that n_reqs << bits stays within kMaxSortBins
+inline uint32_t sort_cell_bits(uint32_t n_reqs) {
+    uint32_t b = 18;
+    while (b > 12 && ((uint64_t)n_reqs << b) > kMaxSortBins) b -= 3;
+    return b;
+}
+
+struct WaveArgs {
+    const ReqView* reqs;        // device table, n_reqs entries
+    uint32_t n_reqs;
+    uint32_t cell_bits;         // sort cells per request = 2^cell_bits
+    FieldView fv;               // shared field layout (table / mlp pointers unused)
     RayBuf rays_in, rays_out;
     const uint32_t* n_alive_in;
     uint32_t* n_alive_out;
     uint32_t* n_round;          // samples produced this round, per alive ray
     uint32_t* sample_index;     // [steps][n_alive]: stream position of sample k of ray r
     uint32_t* sample_ray;       // per sample (march order): ray slot | step k << kStepShift
-    uint32_t* sample_key;       // per sample (march order): spatial cell of the position
-    uint32_t* sample_order;     // sorted position -> march-order sample
-    uint32_t* sort_bins;        // kSortBins cell counters, then cursors
-    uint32_t* sort_block_sums;  // per 1024 cells
+    uint32_t* sample_key;       // per sample (march order): request << cell_bits | cell
+    uint32_t* sample_order;     // sorted (padded) position -> march-order sample, kNoSample for padding
+    uint32_t* sort_bins;        // n_reqs << cell_bits counters, then cursors
+    uint32_t* sort_block_sums;  // per kSortBlock bins, then their exclusive offsets
+    uint32_t* req_start;        // [n_reqs + 1] unpadded start of each request's samples
+    uint32_t* req_seg;          // [n_reqs + 1] padded start of each request's samples
     uint32_t* n_samples_round;  // device count of this round's samples
+    uint32_t* n_samples_padded; // the same after per-request padding to 128
     uint32_t steps;             // samples per ray per round
     uint8_t* tiles;             // encoded input tile records
     uint32_t tile_bytes, k_in;
@@ -69,7 +96,7 @@ cudaError_t launch_canonical_map_soa(const FrameView& fv, const DeformView& dv, 
 cudaError_t launch_canonical_map_coords(const FrameView* frames_dev, uint32_t n_frames, const DeformView& dv, float* coords,
                                         uint32_t stride, uint32_t n_extra, int64_t n, int32_t frame_id, uint32_t* err, cudaStream_t s);
 
-cudaError_t launch_ray_init(const WaveArgs& a, cudaStream_t s);
+cudaError_t launch_ray_init(const WaveArgs& a, uint32_t total_tiles, cudaStream_t s);
 cudaError_t launch_march(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_deform_encode(const WaveArgs& a, cudaStream_t s);

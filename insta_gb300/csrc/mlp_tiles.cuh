@@ -30,13 +30,19 @@ struct TilePlan {
 __host__ __device__ constexpr uint32_t hash_tile_bytes(uint32_t k_in) { return 128u * k_in * 2u; }
 __host__ __device__ constexpr uint32_t sh_tile_bytes() { return 128u * 16u * 2u; }
 
+struct ReqView;
+
 struct MlpArgs {
     FieldView fv;
     TilePlan plan;
     const uint8_t* tiles;
-    const uint32_t* n_alive;   // render rounds: device count of the round's samples
-    uint32_t steps;
+    const uint32_t* n_alive;   // render rounds: device count of the round's (padded) samples
     int64_t n_samples;         // used when n_alive is null
+    // render batches: tile t belongs to the request r with seg[r] <= 128 t < seg[r + 1] and uses
+    // that request's weight image; null when every tile uses fv.mlp_smem
+    const uint32_t* seg;
+    const ReqView* reqs;
+    uint32_t n_reqs;
     uint2* out;                // FP16 (r, g, b, density) per sample
     float4* out_f32;           // BF16 path: FP32 copies of the BF16-rounded values
     uint32_t* err;
@@ -50,6 +56,7 @@ struct TileSmem {
     alignas(1024) uint8_t a_dens[128 * 16 * 2];     // density-MLP output, colour input part 1
     alignas(8) uint64_t bar_mma;
     alignas(8) uint64_t bar_load[2];
+    alignas(8) uint64_t bar_w;       // weight image loads
     uint32_t tmem_base;
 };
 

@@ -44,19 +44,34 @@ __device__ __forceinline__ void write_pixel(const RenderView& rv, float* out_rgb
 // union of BVH nodes (about 40% fewer than for 32x1 pixel rows).
 constexpr uint32_t kTileW = 8, kTileH = 4;
 
-__global__ void ray_init_kernel(const __grid_constant__ WaveArgs A) {
+// Request of a ray tile: the last request whose first tile is <= tile (binary search).
+__device__ __forceinline__ uint32_t request_of_tile(const ReqView* reqs, uint32_t n_reqs, uint32_t tile) {
+    uint32_t lo = 0, hi = n_reqs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&reqs[mid].tile_first) <= tile) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void ray_init_kernel(const __grid_constant__ WaveArgs A, uint32_t total_tiles) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t w = (uint32_t)A.rv.width, h = (uint32_t)A.rv.height;
-    const uint32_t tiles_x = (w + kTileW - 1) / kTileW, tiles_y = (h + kTileH - 1) / kTileH;
     const uint32_t tile = t / (kTileW * kTileH), in = t % (kTileW * kTileH);
-    const uint32_t x = (tile % tiles_x) * kTileW + in % kTileW, y = (tile / tiles_x) * kTileH + in / kTileW;
-    const uint32_t idx = y * w + x;
     bool alive = false;
     RayState r;
-    if (tile < tiles_x * tiles_y && x < w && y < h) {
-        reinterpret_cast<float4*>(A.out_rgba)[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
-        A.out_depth[idx] = 1e10f;
-        alive = ray_init(A.rv, x, y, A.bitfield, r);
+    uint32_t req = 0, idx = 0;
+    if (tile < total_tiles) {
+        req = request_of_tile(A.reqs, A.n_reqs, tile);
+        const ReqView& R = A.reqs[req];
+        const uint32_t w = (uint32_t)R.rv.width, h = (uint32_t)R.rv.height;
+        const uint32_t lt = tile - R.tile_first;
+        const uint32_t x = (lt % R.tiles_x) * kTileW + in % kTileW, y = (lt / R.tiles_x) * kTileH + in / kTileW;
+        if (x < w && y < h) {
+            idx = y * w + x;
+            reinterpret_cast<float4*>(R.out_rgba)[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
+            R.out_depth[idx] = 1e10f;
+            alive = ray_init(R.rv, x, y, R.bitfield, r);
+        }
     }
     uint32_t slot = warp_append(A.n_alive_out, alive);
     if (alive) {
@@ -64,16 +79,16 @@ __global__ void ray_init_kernel(const __grid_constant__ WaveArgs A) {
         b.a[slot] = make_float4(r.o.x, r.o.y, r.o.z, r.t);
         b.b[slot] = make_float4(r.d.x, r.d.y, r.d.z, 0.f);
         b.c[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-        b.d[slot] = make_float4(0.f, __uint_as_float(idx), __uint_as_float(0u), __int_as_float(-1));
+        b.d[slot] = make_float4(0.f, __uint_as_float(idx), __uint_as_float(0u), __uint_as_float(req));
     }
 }
 
 // ------------------------------------------------------------------ march + deform + encode
-__device__ __forceinline__ void encode_sample(const FieldView& fv, const float* extra, uint32_t mask, const float* pos,
-                                              const float* dirw, uint8_t* rec, uint32_t row, uint32_t k_in) {
+__device__ __forceinline__ void encode_sample(const FieldView& fv, const uint16_t* table, const float* extra, uint32_t mask,
+                                              const float* pos, const float* dirw, uint8_t* rec, uint32_t row, uint32_t k_in) {
     const bool bf16 = fv.precision == 1;
     float f[48];
-    hash_encode(fv, v3(pos[0], pos[1], pos[2]), f);
+    hash_encode(fv, table, v3(pos[0], pos[1], pos[2]), f);
     __half h[48];
 #pragma unroll
     for (int i = 0; i < 32; ++i) h[i] = to_act(f[i], bf16);
@@ -95,7 +110,6 @@ __device__ __forceinline__ void encode_sample(const FieldView& fv, const float* 
 // order, records in sample_index[k * n_alive + r] where sample k of ray r went.
 __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ WaveArgs A) {
     const uint32_t n_alive = *A.n_alive_in;
-    const RenderView& rv = A.rv;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_iter = (n_alive + stride - 1) / stride;
     const uint32_t lane = threadIdx.x & 31u;
@@ -106,9 +120,14 @@ __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ Wave
         RayState ray;
         uint32_t ns = 0, j = 0;
         float t0 = 0.f;
+        RenderView rv;   // the ray's request, held in registers through both march passes
+        const uint8_t* bitfield = nullptr;
         if (valid) {
-            const float4 ra = A.rays_in.a[r], rb = A.rays_in.b[r];
-            ns = __float_as_uint(A.rays_in.d[r].z);
+            const float4 ra = A.rays_in.a[r], rb = A.rays_in.b[r], rd = A.rays_in.d[r];
+            ns = __float_as_uint(rd.z);
+            const ReqView& R = A.reqs[__float_as_uint(rd.w)];
+            rv = R.rv;
+            bitfield = R.bitfield;
             ray.o = v3(ra.x, ra.y, ra.z);
             ray.d = v3(rb.x, rb.y, rb.z);
             ray.idir = v3(__fdiv_rn(1.f, rb.x), __fdiv_rn(1.f, rb.y), __fdiv_rn(1.f, rb.z));
@@ -116,7 +135,7 @@ __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ Wave
             for (; j < A.steps; ++j) {
                 V3 pos;
                 float dt;
-                if (ns + j >= rv.max_samples_per_ray || !ray_next_sample(rv, A.bitfield, ray, pos, dt)) break;
+                if (ns + j >= rv.max_samples_per_ray || !ray_next_sample(rv, bitfield, ray, pos, dt)) break;
             }
         }
         const uint32_t total = __reduce_add_sync(0xffffffffu, j);
@@ -132,7 +151,7 @@ __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ Wave
             if (act) {
                 V3 pos;
                 float dt;
-                ray_next_sample(rv, A.bitfield, ray, pos, dt);
+                ray_next_sample(rv, bitfield, ray, pos, dt);
                 const uint32_t idx = base + offset + (uint32_t)__popc(m & lt_mask);
                 A.samples[idx] = make_float4(pos.x, pos.y, pos.z, dt);
                 A.sample_ray[idx] = r | (k << kStepShift);
@@ -155,9 +174,9 @@ __device__ __forceinline__ uint32_t spread3(uint32_t v) {   // 6 bits -> every t
     return v;
 }
 
-// Cell of a sample: 64^3 grid over the frame mesh's box (the union of the root's child boxes)
-// widened by 1/8 on each side; positions outside fall into the border cells.
-__device__ __forceinline__ uint32_t sample_cell(const FrameView& fr, float4 p) {
+// Cell of a sample: a (2^(bits/3))^3 Morton grid over the frame mesh's box (the union of the
+// root's child boxes) widened by 1/8 on each side; positions outside fall into border cells.
+__device__ __forceinline__ uint32_t sample_cell(const FrameView& fr, float4 p, uint32_t bits) {
     const float4* nd = fr.nodes;
     const float4 mnx = __ldg(nd + 0), mny = __ldg(nd + 1), mnz = __ldg(nd + 2);
     const float4 mxx = __ldg(nd + 3), mxy = __ldg(nd + 4), mxz = __ldg(nd + 5);
@@ -172,33 +191,41 @@ __device__ __forceinline__ uint32_t sample_cell(const FrameView& fr, float4 p) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], cmn[c][k]); hi[k] = fmaxf(hi[k], cmx[c][k]); }
     const float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), fmaxf(hi[2] - lo[2], 1e-6f)) * 1.25f;
-    const float scale = 64.f / ext;
+    const uint32_t per_axis = 1u << (bits / 3);
+    const float scale = (float)per_axis / ext, top = (float)(per_axis - 1);
     const float pp[3] = {p.x, p.y, p.z};
     uint32_t q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const float c = (pp[k] - (0.5f * (lo[k] + hi[k]) - 0.5f * ext)) * scale;
-        q[k] = (uint32_t)fminf(fmaxf(c, 0.f), 63.f);
+        q[k] = (uint32_t)fminf(fmaxf(c, 0.f), top);
     }
     return spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
 }
 
-// Count per cell (warp-aggregated: lanes with the same cell add once) and remember each cell.
+// Count per (request, cell) bin (warp-aggregated: lanes with the same key add once) and remember
+// each sample's key.
 __global__ void __launch_bounds__(256) sort_count_kernel(const __grid_constant__ WaveArgs A) {
     const uint32_t n = *A.n_samples_round;
+    const uint32_t n_alive = *A.n_alive_in;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += stride) {
         const uint32_t s = b + threadIdx.x;
         const bool valid = s < n;
-        const uint32_t cell = valid ? sample_cell(A.fr, A.samples[s]) : 0xffffffffu;
-        if (valid) A.sample_key[s] = cell;
-        const uint32_t peers = __match_any_sync(0xffffffffu, cell);
-        if (valid && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(A.sort_bins + cell, (uint32_t)__popc(peers));
+        uint32_t key = 0xffffffffu;
+        if (valid) {
+            const uint32_t r = A.sample_ray[s] & kRayMask;
+            const uint32_t req = r < n_alive ? __float_as_uint(A.rays_in.d[r].w) : 0u;
+            key = (req << A.cell_bits) | sample_cell(A.reqs[req].fr, A.samples[s], A.cell_bits);
+            A.sample_key[s] = key;
+        }
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        if (valid && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(A.sort_bins + key, (uint32_t)__popc(peers));
     }
 }
 
-// Exclusive scan of each block of kSortBlock cell counts, in place; block totals to sort_block_sums.
+// Exclusive scan of each block of kSortBlock bin counts, in place; block totals to sort_block_sums.
 __global__ void __launch_bounds__(kSortBlock) sort_scan_kernel(uint32_t* bins, uint32_t* block_sums) {
     __shared__ uint32_t warp_tot[kSortBlock / 32];
     const uint32_t i = blockIdx.x * kSortBlock + threadIdx.x;
@@ -227,29 +254,88 @@ __global__ void __launch_bounds__(kSortBlock) sort_scan_kernel(uint32_t* bins, u
     if (threadIdx.x == kSortBlock - 1) block_sums[blockIdx.x] = before + x;
 }
 
-// Place every sample: its cell's start plus a running cursor (warp-aggregated).  Order within a
-// cell is arbitrary; each sample's result does not depend on it.
-__global__ void __launch_bounds__(256) sort_place_kernel(const __grid_constant__ WaveArgs A) {
-    constexpr uint32_t NB = kSortBins / kSortBlock;
-    __shared__ uint32_t block_off[NB];
-    static_assert(NB == 256, "one block-sum per thread");
-    {
-        const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-        __shared__ uint32_t wt[8];
-        const uint32_t v = A.sort_block_sums[threadIdx.x];
-        uint32_t x = v;
+// Block-wide exclusive scan of one value per thread (kSortBlock threads); returns the total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* before, uint32_t* warp_tot) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = warp_tot[lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= (uint32_t)o) x += y;
+            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= (uint32_t)o) t += y;
         }
-        if (lane == 31) wt[warp] = x;
-        __syncthreads();
-        uint32_t before = 0;
-        for (uint32_t w = 0; w < warp; ++w) before += wt[w];
-        block_off[threadIdx.x] = before + x - v;
-        __syncthreads();
+        warp_tot[lane] = t;
     }
+    __syncthreads();
+    *before = (warp ? warp_tot[warp - 1] : 0u) + x - v;
+    return warp_tot[31];
+}
+
+// One block: offsets of the bin blocks, each request's unpadded start and padded segment
+// (runs rounded up to 128 samples), padding markers, and the padded sample count.
+__global__ void __launch_bounds__(kSortBlock) sort_offsets_kernel(const __grid_constant__ WaveArgs A, uint32_t n_blocks) {
+    __shared__ uint32_t warp_tot[32];
+    // 1. block offsets (n_blocks <= kMaxSortBins / kSortBlock = 16 per thread)
+    const uint32_t per = (n_blocks + kSortBlock - 1) / kSortBlock;
+    const uint32_t b0 = threadIdx.x * per;
+    uint32_t local[16];
+    uint32_t sum = 0;
+    for (uint32_t k = 0; k < per; ++k) {
+        const uint32_t v = b0 + k < n_blocks ? A.sort_block_sums[b0 + k] : 0u;
+        local[k] = sum;
+        sum += v;
+    }
+    uint32_t before;
+    const uint32_t total = block_exclusive_scan(sum, &before, warp_tot);
+    for (uint32_t k = 0; k < per; ++k)
+        if (b0 + k < n_blocks) A.sort_block_sums[b0 + k] = before + local[k];
+    __syncthreads();
+    // 2. requests: start of each run (its first bin begins a bin block) and padded segments
+    const uint32_t shift = A.cell_bits - 10u;   // bins per request / kSortBlock = 2^shift
+    const uint32_t rper = (A.n_reqs + kSortBlock - 1) / kSortBlock;   // <= kMaxRequests / kSortBlock
+    const uint32_t r0 = threadIdx.x * rper;
+    uint32_t cnt[4], pad_sum = 0;
+    for (uint32_t k = 0; k < rper; ++k) {
+        const uint32_t r = r0 + k;
+        cnt[k] = 0;
+        if (r < A.n_reqs) {
+            const uint32_t st = A.sort_block_sums[r << shift];
+            const uint32_t en = r + 1 < A.n_reqs ? A.sort_block_sums[(r + 1) << shift] : total;
+            A.req_start[r] = st;
+            cnt[k] = en - st;
+        }
+        pad_sum += (cnt[k] + 127u) & ~127u;
+    }
+    uint32_t pbefore;
+    const uint32_t padded_total = block_exclusive_scan(pad_sum, &pbefore, warp_tot);
+    for (uint32_t k = 0; k < rper; ++k) {
+        const uint32_t r = r0 + k;
+        if (r < A.n_reqs) {
+            A.req_seg[r] = pbefore;
+            for (uint32_t q = pbefore + cnt[k]; q < pbefore + ((cnt[k] + 127u) & ~127u); ++q) A.sample_order[q] = kNoSample;
+        }
+        pbefore += (cnt[k] + 127u) & ~127u;
+    }
+    if (threadIdx.x == 0) {
+        A.req_seg[A.n_reqs] = padded_total;
+        A.req_start[A.n_reqs] = total;
+        *A.n_samples_padded = padded_total;
+    }
+}
+
+// Place every sample: its bin's start plus a running cursor (warp-aggregated), moved from the
+// request's unpadded start to its padded segment.  Order within a bin is arbitrary; each
+// sample's result does not depend on it.
+__global__ void __launch_bounds__(256) sort_place_kernel(const __grid_constant__ WaveArgs A) {
     const uint32_t n = *A.n_samples_round;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -257,13 +343,17 @@ __global__ void __launch_bounds__(256) sort_place_kernel(const __grid_constant__
     for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += stride) {
         const uint32_t s = b + threadIdx.x;
         const bool valid = s < n;
-        const uint32_t cell = valid ? A.sample_key[s] : 0xffffffffu;
-        const uint32_t peers = __match_any_sync(0xffffffffu, cell);
+        const uint32_t key = valid ? A.sample_key[s] : 0xffffffffu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
         const int leader = __ffs(peers) - 1;
         uint32_t base = 0;
-        if (valid && lane == (uint32_t)leader) base = atomicAdd(A.sort_bins + cell, (uint32_t)__popc(peers));
+        if (valid && lane == (uint32_t)leader) base = atomicAdd(A.sort_bins + key, (uint32_t)__popc(peers));
         base = __shfl_sync(0xffffffffu, base, leader);
-        if (valid) A.sample_order[block_off[cell / kSortBlock] + base + (uint32_t)__popc(peers & lt_mask)] = s;
+        if (valid) {
+            const uint32_t req = key >> A.cell_bits;
+            const uint32_t pos = A.sort_block_sums[key / kSortBlock] + base + (uint32_t)__popc(peers & lt_mask);
+            A.sample_order[pos - A.req_start[req] + A.req_seg[req]] = s;
+        }
     }
 }
 
@@ -273,25 +363,30 @@ __global__ void __launch_bounds__(256) sort_place_kernel(const __grid_constant__
 // the cooperative BVH walk visits a small union of nodes.
 __global__ void __launch_bounds__(256, 4) deform_encode_kernel(const __grid_constant__ WaveArgs A) {
     __shared__ uint32_t wstack[8][INSTA_STACK];
-    const uint32_t n = *A.n_samples_round;
+    const uint32_t n = *A.n_samples_padded;
     const uint32_t n_alive = *A.n_alive_in;
-    const RenderView& rv = A.rv;
-    const V3 cam_fwd = v3(rv.cam[2], rv.cam[6], rv.cam[10]);
-    const V3 cam_pos = v3(rv.cam[3], rv.cam[7], rv.cam[11]);
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
-    // warps step through the stream in lockstep chunks of 32 so every lane joins the cooperative query
+    // warps step through the stream in lockstep chunks of 32 so every lane joins the cooperative
+    // query; runs are padded to 128 per request, so a chunk never mixes requests
     for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32u; base < n; base += n_warps * 32u) {
         const uint32_t s = base + lane;   // position in sorted order: tile row and output slot
-        const bool valid = s < n;
+        const uint32_t m = A.sample_order[s];
+        const bool valid = m != kNoSample;
+        const uint32_t any = __ballot_sync(0xffffffffu, valid);
+        if (!any) continue;
+        uint32_t rk = 0, req = 0;
         float4 smp = make_float4(0.5f, 0.5f, 0.5f, 0.f), rb = make_float4(0.f, 0.f, 1.f, 0.f);
         if (valid) {
-            const uint32_t m = A.sample_order[s];
-            const uint32_t rk = A.sample_ray[m];
+            rk = A.sample_ray[m];
             smp = A.samples[m];
             rb = A.rays_in.b[rk & kRayMask];
+            req = __float_as_uint(A.rays_in.d[rk & kRayMask].w);
             A.sample_index[(size_t)(rk >> kStepShift) * n_alive + (rk & kRayMask)] = s;
         }
+        req = __shfl_sync(0xffffffffu, req, __ffs(any) - 1);
+        const ReqView& R = A.reqs[req];
+        const RenderView& rv = R.rv;
         float cw[3], dw[3], dp[3];
         const float pp[3] = {smp.x, smp.y, smp.z}, dd[3] = {rb.x, rb.y, rb.z};
 #pragma unroll
@@ -303,20 +398,22 @@ __global__ void __launch_bounds__(256, 4) deform_encode_kernel(const __grid_cons
         float cpos[3] = {cw[0], cw[1], cw[2]}, cdir[3] = {dw[0], dw[1], dw[2]};
         uint32_t mask = 7u;
         const V3 p = v3(cw[0], cw[1], cw[2]);
-        const bool in_box = valid && box_contains(A.dv.aabb_min, A.dv.aabb_max, p);
-        Nearest q = nearest_warp(A.fr, p, in_box, wstack[warp], A.err);
+        const bool in_box = valid && box_contains(R.dv.aabb_min, R.dv.aabb_max, p);
+        Nearest q = nearest_warp(R.fr, p, in_box, wstack[warp], A.err);
         if (in_box) {
-            if (q.id >= 0) map_to_canonical(A.dv, A.fr.frames, (uint32_t)q.id, p, dw, cpos, cdir, &mask);
+            if (q.id >= 0) map_to_canonical(R.dv, R.fr.frames, (uint32_t)q.id, p, dw, cpos, cdir, &mask);
             else atomicOr(A.err, INSTA_DEVERR_NO_TRI);
         }
         if (valid) {
             uint8_t* rec = A.tiles + (size_t)(s >> 7) * A.tile_bytes;
-            encode_sample(A.fv, A.extra_dims, mask, cpos, cdir, rec, s & 127u, A.k_in);
+            encode_sample(A.fv, R.table, R.extra, mask, cpos, cdir, rec, s & 127u, A.k_in);
+            const V3 cam_fwd = v3(rv.cam[2], rv.cam[6], rv.cam[10]);
+            const V3 cam_pos = v3(rv.cam[3], rv.cam[7], rv.cam[11]);
             const V3 dv = v3(__fsub_rn(dp[0], cam_pos.x), __fsub_rn(dp[1], cam_pos.y), __fsub_rn(dp[2], cam_pos.z));
             A.aux[s] = make_float2(smp.w, dot_rn(cam_fwd, dv));
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(A.sample_counter, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(A.sample_counter, (unsigned long long)*A.n_samples_round);
 }
 
 // ------------------------------------------------------------------ MLP over tiles
@@ -324,58 +421,87 @@ __device__ __forceinline__ void load_tile(TileSmem& sm, int buf, const uint8_t* 
     bulk_load(sm.stage[buf], src, bytes, &sm.bar_load[buf]);
 }
 
+// Weight image of tile t: the request whose padded run holds it (render batches), else the field's.
+__device__ __forceinline__ const uint8_t* tile_weights(const MlpArgs& A, uint32_t t) {
+    if (!A.seg) return A.fv.mlp_smem;
+    const uint32_t row = t * 128u;
+    uint32_t lo = 0, hi = A.n_reqs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(A.seg + mid) <= row) lo = mid; else hi = mid;
+    }
+    return A.reqs[lo].mlp;
+}
+
+// Each CTA takes a contiguous range of tiles (consecutive tiles mostly share a request, so the
+// weight image is reloaded only where a range crosses into another avatar's requests); input
+// tiles are double-buffered with 1-D bulk copies.
 __global__ void __launch_bounds__(128) mlp_kernel(const __grid_constant__ MlpArgs A) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
     uint8_t* w = smem_raw + ((sizeof(TileSmem) + 1023) & ~size_t(1023));
     const uint32_t n_samples = A.n_alive ? *A.n_alive : (uint32_t)A.n_samples;
     const uint32_t n_tiles = (n_samples + 127u) / 128u;
-    if (blockIdx.x >= n_tiles) return;
+    const uint32_t per = (n_tiles + gridDim.x - 1) / gridDim.x;
+    const uint32_t t0 = blockIdx.x * per, t1 = min(n_tiles, t0 + per);
+    if (t0 >= t1) return;
     if (threadIdx.x == 0) {
         mbar_init(&sm.bar_mma, 1);
         mbar_init(&sm.bar_load[0], 1);
         mbar_init(&sm.bar_load[1], 1);
+        mbar_init(&sm.bar_w, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     if (threadIdx.x < 32) tmem_alloc(&sm.tmem_base, 128);
-    // the weight image completes phase 0 of bar_load[1]; input tiles then alternate buffers
+    const uint8_t* loaded = tile_weights(A, t0);
     if (threadIdx.x == 0) {
-        bulk_load(w, A.fv.mlp_smem, A.plan.bytes, &sm.bar_load[1]);
-        load_tile(sm, 0, A.tiles + (size_t)blockIdx.x * A.plan.tile_bytes, A.plan.tile_bytes);
+        bulk_load(w, loaded, A.plan.bytes, &sm.bar_w);
+        load_tile(sm, 0, A.tiles + (size_t)t0 * A.plan.tile_bytes, A.plan.tile_bytes);
     }
-    bool ok = mbar_wait(&sm.bar_load[1], 0);   // weights
-    uint32_t load_phase[2] = {0u, 1u};          // bar_load[1] already completed one phase
+    uint32_t w_phase = 0;
+    bool ok = mbar_wait(&sm.bar_w, w_phase);
+    w_phase ^= 1u;
+    uint32_t load_phase[2] = {0u, 0u};
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const bool bf16 = A.fv.precision == 1;
     uint32_t phase = 0;
     int buf = 0;
-    int pending = 0;   // buffer with a copy in flight: 1 + index, 0 = none
-    if (blockIdx.x < n_tiles) pending = 1;
-    for (uint32_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+    int pending = 1;   // buffer with a copy in flight: 1 + index, 0 = none
+    for (uint32_t t = t0; t < t1 && ok; ++t) {
         ok &= mbar_wait(&sm.bar_load[buf], load_phase[buf]);
         load_phase[buf] ^= 1u;
         pending = 0;
-        const uint32_t next = t + gridDim.x;
-        if (next < n_tiles) {
-            if (threadIdx.x == 0) load_tile(sm, buf ^ 1, A.tiles + (size_t)next * A.plan.tile_bytes, A.plan.tile_bytes);
+        if (t + 1 < t1) {
+            if (threadIdx.x == 0) load_tile(sm, buf ^ 1, A.tiles + (size_t)(t + 1) * A.plan.tile_bytes, A.plan.tile_bytes);
             pending = 1 + (buf ^ 1);
+        }
+        const uint8_t* need = tile_weights(A, t);
+        if (need != loaded) {
+            // the previous tile's MMAs have completed (mlp_tile waited on them); swap the image
+            if (threadIdx.x == 0) bulk_load(w, need, A.plan.bytes, &sm.bar_w);
+            ok &= mbar_wait(&sm.bar_w, w_phase);
+            w_phase ^= 1u;
+            loaded = need;
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
         }
         float o4[4];
         ok &= mlp_tile(sm, w, A.plan, buf, bf16, phase, o4);
         const uint32_t s = t * 128u + threadIdx.x;
         if (s < n_samples) {
-            __half2 rg = __floats2half2_rn(o4[0], o4[1]);
-            __half2 bd = __floats2half2_rn(o4[2], o4[3]);
-            uint2 u;
-            u.x = *reinterpret_cast<uint32_t*>(&rg);
-            u.y = *reinterpret_cast<uint32_t*>(&bd);
             if (bf16) {
-                // keep BF16-rounded values exactly: store as FP32 pairs through the float outputs
+                // keep BF16-rounded values exactly: store as FP32 through the float outputs
                 A.out_f32[s] = make_float4(o4[0], o4[1], o4[2], o4[3]);
             } else {
+                __half2 rg = __floats2half2_rn(o4[0], o4[1]);
+                __half2 bd = __floats2half2_rn(o4[2], o4[3]);
+                uint2 u;
+                u.x = *reinterpret_cast<uint32_t*>(&rg);
+                u.y = *reinterpret_cast<uint32_t*>(&bd);
                 A.out[s] = u;
             }
         }
@@ -394,7 +520,6 @@ __global__ void __launch_bounds__(128) mlp_kernel(const __grid_constant__ MlpArg
 // ------------------------------------------------------------------ composite + compaction
 __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
     const uint32_t n_alive = *A.n_alive_in;
-    const RenderView& rv = A.rv;
     const bool bf16 = A.fv.precision == 1;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_iter = (n_alive + stride - 1) / stride;
@@ -404,6 +529,7 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
         float4 ra, rb, rc, rd;
         if (r < n_alive) {
             ra = A.rays_in.a[r]; rb = A.rays_in.b[r]; rc = A.rays_in.c[r]; rd = A.rays_in.d[r];
+            const ReqView& R = A.reqs[__float_as_uint(rd.w)];
             const uint32_t m = A.n_round[r];
             bool done = m < A.steps;
             float4 rgba = rc;
@@ -432,7 +558,7 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
                 rgba.z += (1.0f / (1.0f + expf(-o[2]))) * wgt;
                 rgba.w += wgt;
                 if (wgt > maxw) { maxw = wgt; depth = ax.y; }
-                if (rgba.w > 1.0f - rv.min_transmittance) {
+                if (rgba.w > 1.0f - R.rv.min_transmittance) {
                     const float a = rgba.w;
                     rgba.x /= a; rgba.y /= a; rgba.z /= a; rgba.w /= a;
                     done = true;
@@ -441,7 +567,7 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
             }
             const uint32_t ns = __float_as_uint(rd.z) + m;
             if (done) {
-                write_pixel(rv, A.out_rgba, A.out_depth, __float_as_uint(rd.y), rgba, depth);
+                write_pixel(R.rv, R.out_rgba, R.out_depth, __float_as_uint(rd.y), rgba, depth);
             } else {
                 keep = true;
                 rb.w = maxw;
@@ -465,7 +591,7 @@ __global__ void __launch_bounds__(256) encode_coords_kernel(FieldView fv, const 
     const float* c = coords + i * stride;
     float pos[3] = {c[0], c[1], c[2]}, dir[3] = {c[8], c[9], c[10]};
     uint8_t* rec = tiles + (size_t)(i >> 7) * tile_bytes;
-    encode_sample(fv, c + stride - fv.n_extra, 7u, pos, dir, rec, (uint32_t)(i & 127), k_in);
+    encode_sample(fv, fv.table, c + stride - fv.n_extra, 7u, pos, dir, rec, (uint32_t)(i & 127), k_in);
 }
 
 __global__ void unpack_outputs_kernel(const uint2* __restrict__ out, const float4* __restrict__ out_f32, int bf16, int64_t n, float4* dst) {
@@ -511,9 +637,9 @@ static int sm_count() {
     return g_sms;
 }
 
-cudaError_t launch_ray_init(const WaveArgs& a, cudaStream_t s) {
-    const uint32_t n = ((uint32_t)a.rv.width + kTileW - 1) / kTileW * kTileW * (((uint32_t)a.rv.height + kTileH - 1) / kTileH * kTileH);
-    ray_init_kernel<<<(n + 255) / 256, 256, 0, s>>>(a);
+cudaError_t launch_ray_init(const WaveArgs& a, uint32_t total_tiles, cudaStream_t s) {
+    const uint64_t n = (uint64_t)total_tiles * kTileW * kTileH;
+    ray_init_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, total_tiles);
     return cudaGetLastError();
 }
 
@@ -523,10 +649,12 @@ cudaError_t launch_march(const WaveArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(a.sort_bins, 0, kSortBins * sizeof(uint32_t), s);
+    const uint32_t n_bins = a.n_reqs << a.cell_bits;
+    cudaError_t e = cudaMemsetAsync(a.sort_bins, 0, (size_t)n_bins * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     sort_count_kernel<<<sm_count() * 8, 256, 0, s>>>(a);
-    sort_scan_kernel<<<kSortBins / kSortBlock, kSortBlock, 0, s>>>(a.sort_bins, a.sort_block_sums);
+    sort_scan_kernel<<<n_bins / kSortBlock, kSortBlock, 0, s>>>(a.sort_bins, a.sort_block_sums);
+    sort_offsets_kernel<<<1, kSortBlock, 0, s>>>(a, n_bins / kSortBlock);
     sort_place_kernel<<<sm_count() * 8, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
@@ -540,7 +668,17 @@ cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s) {
     size_t smem = mlp_smem_bytes(a.plan);
     cudaError_t e = cudaFuncSetAttribute(mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    uint32_t grid = (uint32_t)sm_count() * 2;
+    // contiguous tile ranges: exactly as many CTAs as shared memory lets reside at once (the
+    // carveout set to all-shared), at most 4 (4 x 128 TMEM columns fill an SM)
+    e = cudaFuncSetAttribute(mlp_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    int dev = 0, smem_sm = 0, reserved = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    int per_sm = smem_sm / (int)(smem + (size_t)reserved);
+    per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
+    uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
     if (max_tiles < grid) grid = max_tiles ? max_tiles : 1;
     mlp_kernel<<<grid, 128, smem, s>>>(a);
     return cudaGetLastError();

@@ -1,0 +1,120 @@
+"""Batched rendering (insta_render_batch) through the C ABI (cuda:0).
+
+A batch renders every request's rays through one wavefront.  Per-ray work does not depend on
+what else is in the batch, so each request's pixels must equal -- bit for bit -- those of
+insta_render on that request alone, whatever the mix of frames, avatars, cameras and sizes.
+One request of a mixed batch is also checked against the CPU oracle (PSNR >= 45 dB).
+"""
+import numpy as np
+import pytest
+
+from conftest import psnr
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def two_avatars(ctx):
+    """Avatar 10 (seed 0, frames 0..2) and avatar 11 (seed 1, frames 0..1), same field layout."""
+    from insta_gb300 import synthetic as S
+    fc = S.FieldConfig()
+    out = {}
+    for aid, seed, n_frames in ((10, 0, 3), (11, 1, 2)):
+        av = S.make_avatar(seed)
+        ctx.canonical_set(aid, av.canonical, av.faces, av.mask)
+        for f in range(n_frames):
+            ctx.frame_upload(aid, f, av.frame(av.frame_coeffs(f)))
+            ctx.occupancy_from_mesh(aid, f, 0.015)
+        params = S.field_params(fc, seed=seed)
+        ctx.params_load(aid, fc, params)
+        out[aid] = (av, params)
+    ctx.sync()
+    return fc, out
+
+
+def requests(ctx, specs):
+    from insta_gb300 import synthetic as S
+    reqs = []
+    for aid, frame, w, h, yaw, spp in specs:
+        cam, focal = S.camera(yaw, width=w, height=h)
+        reqs.append(ctx.render_desc(aid, frame, w, h, focal, cam, spp=spp))
+    return reqs
+
+
+SPECS = [(10, 0, 64, 48, -10.0, 0), (10, 2, 40, 40, 15.0, 1), (11, 1, 72, 56, 0.0, 0), (10, 1, 33, 29, 25.0, 3),
+         (11, 0, 48, 64, -25.0, 2)]
+
+
+def single(ctx, req):
+    rgba = np.zeros((req.width * req.height, 4), np.float32)
+    depth = np.zeros(req.width * req.height, np.float32)
+    ctx.render(req, rgba, depth)
+    return rgba, depth
+
+
+def test_batch_equals_single_renders(ctx, two_avatars):
+    reqs = requests(ctx, SPECS)
+    ref = [single(ctx, r) for r in reqs]
+    rgba = [np.full((r.width * r.height, 4), -1, np.float32) for r in reqs]
+    depth = [np.full(r.width * r.height, -1, np.float32) for r in reqs]
+    ctx.render_batch(reqs, rgba, depth)
+    for i, (a, b) in enumerate(zip(rgba, ref)):
+        assert (a == b[0]).all(), f"request {i}: rgba differs"
+        assert (depth[i] == b[1]).all(), f"request {i}: depth differs"
+    # the mix is not trivial: every request hit the avatar
+    assert all((b[0][:, 3] > 0.05).sum() > 20 for b in ref), [int((b[0][:, 3] > 0.05).sum()) for b in ref]
+
+
+def test_batch_device_outputs_and_order(ctx, two_avatars):
+    """Device outputs, and the same requests in reverse order, give the same pixels."""
+    reqs = requests(ctx, SPECS)
+    ref = [single(ctx, r) for r in reqs]
+    rgba = [torch.zeros((r.width * r.height, 4), device="cuda") for r in reqs]
+    depth = [torch.zeros(r.width * r.height, device="cuda") for r in reqs]
+    rev = list(range(len(reqs)))[::-1]
+    ctx.render_batch([reqs[i] for i in rev], [rgba[i] for i in rev], [depth[i] for i in rev])
+    ctx.sync()
+    for i in range(len(reqs)):
+        assert (rgba[i].cpu().numpy() == ref[i][0]).all()
+        assert (depth[i].cpu().numpy() == ref[i][1]).all()
+
+
+def test_batch_request_matches_oracle(ctx, two_avatars, oracle):
+    fc, avs = two_avatars
+    av, params = avs[11]
+    reqs = requests(ctx, SPECS)
+    rgba = [np.zeros((r.width * r.height, 4), np.float32) for r in reqs]
+    depth = [np.zeros(r.width * r.height, np.float32) for r in reqs]
+    ctx.render_batch(reqs, rgba, depth)
+    i = 2   # avatar 11, frame 1
+    aid, frame, w, h, yaw, spp = SPECS[i]
+    from insta_gb300 import synthetic as S
+    fr = av.frame(av.frame_coeffs(frame))
+    can = oracle.build_triangles(av.canonical, None, av.faces, av.mask)
+    dtr = oracle.build_triangles(fr, av.canonical, av.faces, av.mask)
+    adj = oracle.adjacency(av.faces, av.n_verts)
+    bvh = oracle.Bvh(dtr)
+    bits = oracle.occupancy(dtr, 0.015)
+    d = oracle.Deformation(dtr, can, adj, bvh)
+    cam, focal = S.camera(yaw, width=w, height=h)
+    rc = oracle.render_cfg(w, h, focal, cam, av.render_aabb(), spp=spp)
+    r_rgba, r_depth, ns, total = oracle.render(rc, d, bits, fc, params)
+    assert total > 500
+    assert psnr(rgba[i], r_rgba) >= 45.0
+
+
+def test_batch_rejects_mixed_layouts(ctx, two_avatars):
+    from insta_gb300 import abi, synthetic as S
+    fc2 = S.FieldConfig(n_extra=16)
+    av = S.make_avatar(2)
+    ctx.canonical_set(12, av.canonical, av.faces, av.mask)
+    ctx.frame_upload(12, 0, av.frame(av.frame_coeffs(0)))
+    ctx.occupancy_from_mesh(12, 0, 0.015)
+    ctx.params_load(12, fc2, S.field_params(fc2, seed=2))
+    reqs = requests(ctx, [(10, 0, 16, 16, 0.0, 0), (12, 0, 16, 16, 0.0, 0)])
+    rgba = [np.zeros((256, 4), np.float32) for _ in reqs]
+    depth = [np.zeros(256, np.float32) for _ in reqs]
+    with pytest.raises(abi.InstaError):
+        ctx.render_batch(reqs, rgba, depth)
