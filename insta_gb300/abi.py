@@ -20,7 +20,7 @@ EXPORTS = [
     "insta_ctx_create", "insta_ctx_destroy", "insta_last_error", "insta_sync", "insta_memory_used",
     "insta_stats_enable", "insta_stats_read",
     "insta_canonical_set", "insta_avatar_set_boxes", "insta_avatar_set_flags", "insta_frame_upload",
-    "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
+    "insta_frame_upload_batch", "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_field_param_count", "insta_params_load",
     "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_batch",
     "insta_render_samples", "insta_march_debug",
@@ -80,6 +80,7 @@ def load(path: Path | None = None):
             "insta_avatar_set_boxes": [vp, C.c_int, vp, vp, vp, vp],
             "insta_avatar_set_flags": [vp, C.c_int, u32],
             "insta_frame_upload": [vp, C.c_int, C.c_int, vp],
+            "insta_frame_upload_batch": [vp, C.c_int, vp, C.c_int, C.POINTER(vp)],
             "insta_frame_release": [vp, C.c_int, C.c_int],
             "insta_occupancy_from_mesh": [vp, C.c_int, C.c_int, C.c_double],
             "insta_occupancy_set": [vp, C.c_int, C.c_int, vp],
@@ -202,6 +203,12 @@ class Context:
     def frame_upload(self, avatar, frame, verts):
         v = verts if hasattr(verts, "data_ptr") else np.ascontiguousarray(verts, dtype=np.float32)
         self._check(self.lib.insta_frame_upload(self.h, avatar, frame, _addr(v)))
+
+    def frame_upload_batch(self, avatar, frames, verts_list):
+        vs = [v if hasattr(v, "data_ptr") else np.ascontiguousarray(v, dtype=np.float32) for v in verts_list]
+        ids = np.ascontiguousarray(frames, dtype=np.int32)
+        ptrs = (C.c_void_p * len(vs))(*[_addr(v).value for v in vs])
+        self._check(self.lib.insta_frame_upload_batch(self.h, avatar, _addr(ids), len(vs), ptrs))
 
     def frame_release(self, avatar, frame):
         self._check(self.lib.insta_frame_release(self.h, avatar, frame))

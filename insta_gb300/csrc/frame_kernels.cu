@@ -1,6 +1,8 @@
 // frame_kernels.cu -- per-frame tracked-mesh upload on the device: triangle frame
 // records, Morton-ordered implicit 4-ary BVH (single-CTA shared-memory sort), occupancy
 // bitfield from the mesh, and the canonical-map kernels (the `warp` hook).
+#include <vector>
+
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -52,9 +54,14 @@ __device__ bool inverse4_d(const double* m, double* o) {
 // for every face; `canon_area` == nullptr builds the canonical mesh (scaling 1).
 __global__ void tri_frame_kernel(int F, const float* __restrict__ verts, const int32_t* __restrict__ faces,
                                  const uint32_t* __restrict__ mask, const float* __restrict__ canon_area,
-                                 float* __restrict__ area_out, TriFrame* __restrict__ out, int with_inverse) {
+                                 float* __restrict__ area_out, TriFrame* __restrict__ out, int with_inverse,
+                                 const FrameJob* __restrict__ jobs) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
+    if (jobs) {   // a batch of frames of one avatar: frame blockIdx.y
+        verts = jobs[blockIdx.y].verts;
+        out = jobs[blockIdx.y].frames;
+    }
     int i0 = faces[f * 3], i1 = faces[f * 3 + 1], i2 = faces[f * 3 + 2];
     V3 a = v3(verts[i0 * 3], verts[i0 * 3 + 1], verts[i0 * 3 + 2]);
     V3 b = v3(verts[i1 * 3], verts[i1 * 3 + 1], verts[i1 * 3 + 2]);
@@ -202,7 +209,8 @@ __device__ int block_scan(int* cnt, int n, int* warp_tot) {
 // binary radix tree top-down level by level and collapse every two binary levels into one
 // 4-wide node; boxes are then filled bottom-up.  Leaves hold <= INSTA_LEAF_SIZE triangles
 // (N_PRIMITIVES_LEAF = 2 in src/tiny_mesh.cu:28-32).
-__global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs a) {
+__global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs one, const BvhBuildArgs* __restrict__ many) {
+    const BvhBuildArgs a = many ? many[blockIdx.x] : one;   // a batch builds one frame per CTA
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* keys = reinterpret_cast<uint64_t*>(smem_raw);
     int* cnt = reinterpret_cast<int*>(smem_raw + (size_t)a.np2 * 8);   // per node of the current level
@@ -390,6 +398,16 @@ __global__ void __launch_bounds__(256) occupancy_kernel(FrameView fr, double rad
         // bit j of byte b is cell 8b + j: the ballot word is the four bytes of this warp's cells
         const uint32_t word = __ballot_sync(0xffffffffu, on);
         if (lane == 0) reinterpret_cast<uint32_t*>(bits)[base >> 5] = word;
+        // bitfield_max_pool (:611-632) for mips 1..7 at once: a mip-l cell is occupied iff some
+        // occupied mip-0 cell maps onto it under l halvings toward the centre (x -> x / 2 + 32)
+        if (on) {
+            uint32_t cx = x, cy = y, cz = z;
+            for (uint32_t l = 1; l < 8; ++l) {
+                cx = cx / 2 + GRID / 4; cy = cy / 2 + GRID / 4; cz = cz / 2 + GRID / 4;
+                const uint32_t c = l * GRID3 + morton3d(cx, cy, cz);
+                atomicOr(reinterpret_cast<uint32_t*>(bits) + (c >> 5), 1u << (c & 31u));
+            }
+        }
     }
 }
 
@@ -461,13 +479,13 @@ static int sm_count_frames() {
 // ------------------------------------------------------------------- launchers
 cudaError_t launch_tri_frames(int F, const float* verts, const int32_t* faces, const uint32_t* mask, const float* canon_area,
                               float* area_out, TriFrame* out, int with_inverse, cudaStream_t s) {
-    tri_frame_kernel<<<(F + 255) / 256, 256, 0, s>>>(F, verts, faces, mask, canon_area, area_out, out, with_inverse);
+    tri_frame_kernel<<<(F + 255) / 256, 256, 0, s>>>(F, verts, faces, mask, canon_area, area_out, out, with_inverse, nullptr);
     return cudaGetLastError();
 }
 
 size_t bvh_scratch_bytes(int F) { return (size_t)F * (sizeof(int2) + 6 * sizeof(float)) + 16; }
 
-cudaError_t launch_bvh_build(const FrameView& fv, const float* verts, const int32_t* faces, void* scratch, cudaStream_t s) {
+static BvhBuildArgs bvh_args(const FrameView& fv, const float* verts, const int32_t* faces, void* scratch) {
     BvhBuildArgs a;
     a.F = fv.n_tris;
     a.verts = verts; a.faces = faces; a.frames = fv.frames;
@@ -480,10 +498,46 @@ cudaError_t launch_bvh_build(const FrameView& fv, const float* verts, const int3
     int np2 = 2;
     while (np2 < fv.n_tris) np2 <<= 1;
     a.np2 = np2;
-    size_t smem = (size_t)np2 * 8 + (size_t)fv.n_tris * 4 + 16;
+    return a;
+}
+
+static size_t bvh_smem(int F) {
+    int np2 = 2;
+    while (np2 < F) np2 <<= 1;
+    return (size_t)np2 * 8 + (size_t)F * 4 + 16;
+}
+
+cudaError_t launch_bvh_build(const FrameView& fv, const float* verts, const int32_t* faces, void* scratch, cudaStream_t s) {
+    const size_t smem = bvh_smem(fv.n_tris);
     cudaError_t e = cudaFuncSetAttribute(bvh_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    bvh_build_kernel<<<1, 1024, smem, s>>>(a);
+    bvh_build_kernel<<<1, 1024, smem, s>>>(bvh_args(fv, verts, faces, scratch), nullptr);
+    return cudaGetLastError();
+}
+
+size_t frame_batch_table_bytes(int n) { return (size_t)n * (sizeof(FrameJob) + sizeof(BvhBuildArgs)); }
+
+cudaError_t launch_frames_batch(int n, int F, const FrameView* views, const float* const* verts, const int32_t* faces,
+                                const uint32_t* mask, const float* canon_area, void* scratch, void* table, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    std::vector<FrameJob> jobs((size_t)n);
+    std::vector<BvhBuildArgs> args((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        jobs[(size_t)i].verts = verts[i];
+        jobs[(size_t)i].frames = const_cast<TriFrame*>(views[i].frames);
+        args[(size_t)i] = bvh_args(views[i], verts[i], faces, static_cast<char*>(scratch) + (size_t)i * bvh_scratch_bytes(F));
+    }
+    FrameJob* djobs = static_cast<FrameJob*>(table);
+    BvhBuildArgs* dargs = reinterpret_cast<BvhBuildArgs*>(static_cast<char*>(table) + (size_t)n * sizeof(FrameJob));
+    // pageable sources: the copies are staged before these calls return
+    cudaError_t e = cudaMemcpyAsync(djobs, jobs.data(), jobs.size() * sizeof(FrameJob), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dargs, args.data(), args.size() * sizeof(BvhBuildArgs), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    tri_frame_kernel<<<dim3((F + 255) / 256, n), 256, 0, s>>>(F, nullptr, faces, mask, canon_area, nullptr, nullptr, 1, djobs);
+    const size_t smem = bvh_smem(F);
+    e = cudaFuncSetAttribute(bvh_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    bvh_build_kernel<<<n, 1024, smem, s>>>(BvhBuildArgs{}, dargs);
     return cudaGetLastError();
 }
 
@@ -492,8 +546,6 @@ cudaError_t launch_occupancy(const FrameView& fv, double radius, uint8_t* bitfie
     if (e != cudaSuccess) return e;
     float bound = (float)(radius * radius * 1.0001);
     occupancy_kernel<<<sm_count_frames() * 8, 256, 0, s>>>(fv, radius, bound, bitfield, err);
-    for (int lvl = 1; lvl < 8; ++lvl)
-        maxpool_kernel<<<(GRID3 / 64 + 255) / 256, 256, 0, s>>>(bitfield + (size_t)(lvl - 1) * GRID3 / 8, bitfield + (size_t)lvl * GRID3 / 8);
     return cudaGetLastError();
 }
 

@@ -95,7 +95,7 @@ struct insta_ctx {
     uint32_t* err_dev = nullptr;
     uint32_t* ray_counter = nullptr;
     unsigned long long* sample_counter = nullptr;
-    DevBuf out_rgba, out_depth, extra, bvh_scratch;
+    DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs;
     Wave wave;
     uint32_t* host_counters = nullptr;   // pinned: alive-ray counts read between rounds
     int sms = 0;
@@ -561,6 +561,26 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
     }
 }
 
+// Device buffers and view of one uploaded frame; copies its vertices in.
+Frame& prepare_frame(insta_ctx* ctx, Avatar& a, int frame, const float* verts) {
+    Frame& f = a.frames[frame];
+    // an LBVH with leaves of <= 2 triangles has at most F - 1 internal nodes
+    const int max_nodes = std::max(1, a.F);
+    ctx->alloc(f.verts, (size_t)a.V * 12);
+    ctx->alloc(f.frames, (size_t)a.F * sizeof(TriFrame));
+    ctx->alloc(f.leaf_tris, (size_t)a.F * 48);
+    ctx->alloc(f.nodes, (size_t)max_nodes * 112);
+    host_copy(f.verts.p, verts, (size_t)a.V * 12, ctx->stream);
+    f.view.leaf_tris = static_cast<const float4*>(f.leaf_tris.p);
+    f.view.nodes = static_cast<const float4*>(f.nodes.p);
+    f.view.frames = static_cast<const TriFrame*>(f.frames.p);
+    f.view.n_tris = a.F;
+    f.view.n_nodes = max_nodes;
+    f.has_occupancy = false;
+    a.table_dirty = true;
+    return f;
+}
+
 }  // namespace
 
 extern "C" {
@@ -701,26 +721,37 @@ int insta_frame_upload(insta_ctx* ctx, int avatar, int frame, const float* verts
     return guarded(ctx, [&] {
         Avatar& a = ctx->avatar(avatar);
         if (!verts || frame < 0) fail(INSTA_ERR_INVALID_ARG, "bad frame upload");
-        Frame& f = a.frames[frame];
-        // an LBVH with leaves of <= 2 triangles has at most F - 1 internal nodes
-        const int max_nodes = std::max(1, a.F);
-        ctx->alloc(f.verts, (size_t)a.V * 12);
-        ctx->alloc(f.frames, (size_t)a.F * sizeof(TriFrame));
-        ctx->alloc(f.leaf_tris, (size_t)a.F * 48);
-        ctx->alloc(f.nodes, (size_t)max_nodes * 112);
         ctx->alloc(ctx->bvh_scratch, bvh_scratch_bytes(a.F));
-        host_copy(f.verts.p, verts, (size_t)a.V * 12, ctx->stream);
-        f.view.leaf_tris = static_cast<const float4*>(f.leaf_tris.p);
-        f.view.nodes = static_cast<const float4*>(f.nodes.p);
-        f.view.frames = static_cast<const TriFrame*>(f.frames.p);
-        f.view.n_tris = a.F;
-        f.view.n_nodes = max_nodes;
+        Frame& f = prepare_frame(ctx, a, frame, verts);
         Stage st(ctx, INSTA_STAGE_FRAME, 2);
         CK(launch_tri_frames(a.F, (const float*)f.verts.p, (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
                              (const float*)a.canon_area.p, nullptr, (TriFrame*)f.frames.p, 1, ctx->stream));
         CK(launch_bvh_build(f.view, (const float*)f.verts.p, (const int32_t*)a.faces.p, ctx->bvh_scratch.p, ctx->stream));
-        f.has_occupancy = false;
-        a.table_dirty = true;
+    });
+}
+
+int insta_frame_upload_batch(insta_ctx* ctx, int avatar, const int32_t* frames, int n, const float* const* verts) {
+    return guarded(ctx, [&] {
+        Avatar& a = ctx->avatar(avatar);
+        if (n < 0 || (n > 0 && (!frames || !verts))) fail(INSTA_ERR_INVALID_ARG, "bad frame batch");
+        if (n == 0) return;
+        std::set<int> seen;
+        for (int i = 0; i < n; ++i) {
+            if (frames[i] < 0 || !verts[i]) fail(INSTA_ERR_INVALID_ARG, "bad frame %d in batch", i);
+            if (!seen.insert(frames[i]).second) fail(INSTA_ERR_INVALID_ARG, "frame %d appears twice in the batch", frames[i]);
+        }
+        ctx->alloc(ctx->bvh_scratch, (size_t)n * bvh_scratch_bytes(a.F));
+        ctx->alloc(ctx->frame_jobs, frame_batch_table_bytes(n));
+        std::vector<FrameView> views((size_t)n);
+        std::vector<const float*> dverts((size_t)n);
+        for (int i = 0; i < n; ++i) {
+            Frame& f = prepare_frame(ctx, a, frames[i], verts[i]);
+            views[(size_t)i] = f.view;
+            dverts[(size_t)i] = (const float*)f.verts.p;
+        }
+        Stage st(ctx, INSTA_STAGE_FRAME, 2);
+        CK(launch_frames_batch(n, a.F, views.data(), dverts.data(), (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
+                               (const float*)a.canon_area.p, ctx->bvh_scratch.p, ctx->frame_jobs.p, ctx->stream));
     });
 }
 

@@ -89,6 +89,15 @@ struct WaveArgs {
 cudaError_t launch_tri_frames(int F, const float* verts, const int32_t* faces, const uint32_t* mask, const float* canon_area,
                               float* area_out, TriFrame* out, int with_inverse, cudaStream_t s);
 size_t bvh_scratch_bytes(int F);
+// A batch of frames of one avatar: per-triangle frames, then one LBVH build per CTA (frame i
+// uses scratch + i * bvh_scratch_bytes(F)); `table` holds frame_batch_table_bytes(n) device bytes.
+struct FrameJob {
+    const float* verts;
+    TriFrame* frames;
+};
+size_t frame_batch_table_bytes(int n);
+cudaError_t launch_frames_batch(int n, int F, const FrameView* views, const float* const* verts, const int32_t* faces,
+                                const uint32_t* mask, const float* canon_area, void* scratch, void* table, cudaStream_t s);
 cudaError_t launch_bvh_build(const FrameView& fv, const float* verts, const int32_t* faces, void* scratch, cudaStream_t s);
 cudaError_t launch_occupancy(const FrameView& fv, double radius, uint8_t* bitfield, uint32_t* err, cudaStream_t s);
 cudaError_t launch_canonical_map_soa(const FrameView& fv, const DeformView& dv, const float* pts, int64_t n, int32_t* out_idx,

@@ -118,3 +118,32 @@ def test_batch_rejects_mixed_layouts(ctx, two_avatars):
     depth = [np.zeros(256, np.float32) for _ in reqs]
     with pytest.raises(abi.InstaError):
         ctx.render_batch(reqs, rgba, depth)
+
+
+def test_frame_upload_batch_equals_single(ctx):
+    """A batch upload builds the same BVHs and frames: identical occupancy and canonical maps."""
+    from insta_gb300 import synthetic as S
+    av = S.make_avatar(4)
+    frames = [av.frame(av.frame_coeffs(k)) for k in range(5)]
+    for aid in (20, 21):
+        ctx.canonical_set(aid, av.canonical, av.faces, av.mask)
+    for k, v in enumerate(frames):
+        ctx.frame_upload(20, k, v)
+    ctx.frame_upload_batch(21, list(range(5)), frames)
+    pts = S.shell_points(frames[3], av.faces, 20000, seed=9)
+    outs = {}
+    for aid in (20, 21):
+        got = []
+        for k in range(5):
+            ctx.occupancy_from_mesh(aid, k, 0.015)
+            bits = ctx.occupancy_get(aid, k)
+            idx = torch.empty(len(pts), dtype=torch.int32, device="cuda")
+            can = torch.empty((len(pts), 3), device="cuda")
+            ctx.canonical_map_soa(aid, k, torch.from_numpy(pts).cuda(), len(pts), idx, can)
+            ctx.sync()
+            got.append((bits, idx.cpu().numpy(), can.cpu().numpy()))
+        outs[aid] = got
+    for k in range(5):
+        a, b = outs[20][k], outs[21][k]
+        assert (a[0] == b[0]).all() and (a[1] == b[1]).all() and (a[2] == b[2]).all(), k
+    assert outs[20][0][0].any()
