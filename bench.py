@@ -31,7 +31,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "samples/s (deform+encode+MLP)"
 UNIT = "samples/s"
-WIDTH = HEIGHT = 512
+WIDTH = HEIGHT = 512   # --width overrides (small cases for profiling)
 RADIUS = 0.015
 CONE = 1.0 / 256.0
 L2_FLUSH_BYTES = 512 << 20
@@ -198,7 +198,10 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         total_samples = 0
+        # per-stage device time: CUDA events the library records on this stream around each of
+        # its stages (a few microseconds per step), read after the timed region
         ctx.stats(reset=True)
+        ctx.stats_enable(True)
         with ClockSampler(local) as clocks:
             t_wall0 = time.perf_counter()
             for k in range(args.steps):
@@ -210,14 +213,8 @@ def run_ours(args, rank, world, local):
             stream.synchronize()
             t_wall = time.perf_counter() - t_wall0
         step_ms = [a.elapsed_time(b) for a, b in ev]
-        launches = ctx.stats(reset=True)["kernel_launches"]
-        # per-stage device time (CUDA events recorded by the library around each stage, on this
-        # stream), in a separate pass so the timed steps above carry no extra events
-        ctx.stats_enable(True)
-        for k in range(args.steps):
-            flush.zero_()
-            step(k)
         stages = ctx.stats(reset=True)
+        launches = stages["kernel_launches"]
         ctx.stats_enable(False)
         ctx.sync()
         # end to end through the C ABI with host buffers: H2D of the frame's vertices, D2H of RGBA + depth
@@ -298,7 +295,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--width", type=int, default=512, help="square render size (512 = the benchmark workload)")
     args = ap.parse_args()
+    global WIDTH, HEIGHT
+    WIDTH = HEIGHT = args.width
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)

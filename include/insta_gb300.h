@@ -99,7 +99,8 @@ typedef struct {
 #define INSTA_STAGE_COMPOSITE 6
 #define INSTA_STAGE_CANONICAL_MAP 7  /* insta_canonical_map / _soa               */
 #define INSTA_STAGE_FIELD 8          /* insta_field_eval / _static               */
-#define INSTA_STAGE_COUNT 9
+#define INSTA_STAGE_SORT 9           /* regrouping a round's samples by (request, cell) */
+#define INSTA_STAGE_COUNT 10
 
 typedef struct {
     uint64_t kernel_launches;        /* kernels the library launched */

@@ -41,7 +41,7 @@ class FieldDesc(C.Structure):
                 ("precision", C.c_uint32)]
 
 
-STAGES = ["frame", "occupancy", "ray_init", "march", "deform_encode", "mlp", "composite", "canonical_map", "field"]
+STAGES = ["frame", "occupancy", "ray_init", "march", "deform_encode", "mlp", "composite", "canonical_map", "field", "sort"]
 
 
 class Stats(C.Structure):

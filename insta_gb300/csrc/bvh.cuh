@@ -143,26 +143,30 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
             const bool want = ci[i] != 0xffffffffu && cd[i] <= lim;
             key[i] = __reduce_min_sync(0xffffffffu, want ? __float_as_uint(cd[i]) : 0xffffffffu);
         }
-        // push the needed children farthest-first so the warp pops the nearest next
-        uint32_t order[4] = {0, 1, 2, 3};
-#define INSTA_CASK(x, y) if (key[order[x]] < key[order[y]]) { uint32_t t = order[x]; order[x] = order[y]; order[y] = t; }
+        // sort the children farthest-first (keys are warp-uniform; every index is static, so the
+        // tuples stay in registers) and push the needed ones: the warp pops the nearest next
+#define INSTA_CASK(x, y)                                                                  \
+    if (key[x] < key[y]) {                                                                \
+        uint32_t tk = key[x]; key[x] = key[y]; key[y] = tk;                               \
+        uint32_t tc = ci[x]; ci[x] = ci[y]; ci[y] = tc;                                   \
+        float td = cd[x]; cd[x] = cd[y]; cd[y] = td;                                      \
+    }
         INSTA_CASK(0, 2) INSTA_CASK(1, 3) INSTA_CASK(0, 1) INSTA_CASK(2, 3) INSTA_CASK(1, 2)
 #undef INSTA_CASK
+        __syncwarp();   // every lane has read the popped entry before lane 0 overwrites it
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const uint32_t c = order[i];
-            if (key[c] != 0xffffffffu) {
+            if (key[i] != 0xffffffffu) {
                 if (sp < INSTA_STACK) {
-                    __syncwarp();
-                    if ((threadIdx.x & 31) == 0) wstack[sp] = ci[c];
-                    __syncwarp();
-                    dstack[sp] = active ? cd[c] : INF;
+                    if ((threadIdx.x & 31) == 0) wstack[sp] = ci[i];
+                    dstack[sp] = active ? cd[i] : INF;
                     ++sp;
                 } else if (err && (threadIdx.x & 31) == 0) {
                     atomicOr(err, INSTA_DEVERR_STACK);
                 }
             }
         }
+        __syncwarp();
     }
     return {bid, bslot, best};
 }

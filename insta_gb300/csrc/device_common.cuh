@@ -423,39 +423,34 @@ __device__ __forceinline__ bool ray_next_sample(const RenderView& rv, const uint
 // Published multiresolution hash encoding, this library's documented table layout
 // (per-level dense index x + y*res + z*res^2 or spatial hash with primes
 // 1, 2654435761, 805459861; trilinear weights; FP32 accumulation).
-__device__ __forceinline__ void hash_encode(const FieldView& fv, const uint16_t* params, V3 x, float* out) {
-    const __half2* table = reinterpret_cast<const __half2*>(params);
-    // levels unrolled by four so 32 independent gathers are in flight per thread
-#pragma unroll 4
-    for (int l = 0; l < (int)fv.n_levels; ++l) {
-        const float s = fv.level_scale[l];
-        float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);
-        float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
-        float rx = __fsub_rn(px, fx), ry = __fsub_rn(py, fy), rz = __fsub_rn(pz, fz);
-        uint32_t gx = (uint32_t)(int32_t)fx, gy = (uint32_t)(int32_t)fy, gz = (uint32_t)(int32_t)fz;
-        const uint32_t res = fv.level_res[l], size = fv.level_size[l];
-        const bool dense = fv.level_dense[l];
-        const __half2* lt = table + fv.level_off[l];
-        float a0 = 0.f, a1 = 0.f;
+// Level l's two features at x (trilinear over the cell's 8 corners).
+__device__ __forceinline__ void hash_level(const FieldView& fv, const __half2* table, V3 x, uint32_t l, float& a0, float& a1) {
+    const float s = fv.level_scale[l];
+    float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);
+    float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+    float rx = __fsub_rn(px, fx), ry = __fsub_rn(py, fy), rz = __fsub_rn(pz, fz);
+    uint32_t gx = (uint32_t)(int32_t)fx, gy = (uint32_t)(int32_t)fy, gz = (uint32_t)(int32_t)fz;
+    const uint32_t res = fv.level_res[l], size = fv.level_size[l];
+    const bool dense = fv.level_dense[l];
+    const __half2* lt = table + fv.level_off[l];
+    a0 = 0.f;
+    a1 = 0.f;
 #pragma unroll
-        for (uint32_t c = 0; c < 8; ++c) {
-            uint32_t bx = c & 1u, by = (c >> 1) & 1u, bz = (c >> 2) & 1u;
-            float w = bx ? rx : __fsub_rn(1.f, rx);
-            w = __fmul_rn(w, by ? ry : __fsub_rn(1.f, ry));
-            w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
-            uint32_t cx = gx + bx, cy = gy + by, cz = gz + bz;
-            uint32_t idx;
-            if (dense) {
-                idx = cx + cy * res + cz * res * res;
-                if (idx >= size) idx %= size;   // only cells on the far boundary wrap
-            }
-            else idx = ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
-            float2 e = __half22float2(__ldg(lt + idx));
-            a0 = __fadd_rn(a0, __fmul_rn(w, e.x));
-            a1 = __fadd_rn(a1, __fmul_rn(w, e.y));
+    for (uint32_t c = 0; c < 8; ++c) {
+        uint32_t bx = c & 1u, by = (c >> 1) & 1u, bz = (c >> 2) & 1u;
+        float w = bx ? rx : __fsub_rn(1.f, rx);
+        w = __fmul_rn(w, by ? ry : __fsub_rn(1.f, ry));
+        w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
+        uint32_t cx = gx + bx, cy = gy + by, cz = gz + bz;
+        uint32_t idx;
+        if (dense) {
+            idx = cx + cy * res + cz * res * res;
+            if (idx >= size) idx %= size;   // only cells on the far boundary wrap
         }
-        out[2 * l] = a0;
-        out[2 * l + 1] = a1;
+        else idx = ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
+        float2 e = __half22float2(__ldg(lt + idx));
+        a0 = __fadd_rn(a0, __fmul_rn(w, e.x));
+        a1 = __fadd_rn(a1, __fmul_rn(w, e.y));
     }
 }
 

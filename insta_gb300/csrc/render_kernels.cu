@@ -84,21 +84,48 @@ __global__ void ray_init_kernel(const __grid_constant__ WaveArgs A, uint32_t tot
 }
 
 // ------------------------------------------------------------------ march + deform + encode
+__device__ __forceinline__ uint32_t pack_act(float a, float b, bool bf16) {
+    const __half x = to_act(a, bf16), y = to_act(b, bf16);
+    return (uint32_t)__half_as_ushort(x) | ((uint32_t)__half_as_ushort(y) << 16);
+}
+
+// One sample's operand rows: hash features (+ expression dims) into the hash tile, SH of the
+// direction into the SH tile.  Four levels at a time (32 gathers in flight), each group of 8
+// values stored as one 16-byte chunk of the row, so no per-sample array is materialised.
 __device__ __forceinline__ void encode_sample(const FieldView& fv, const uint16_t* table, const float* extra, uint32_t mask,
                                               const float* pos, const float* dirw, uint8_t* rec, uint32_t row, uint32_t k_in) {
     const bool bf16 = fv.precision == 1;
-    float f[48];
-    hash_encode(fv, table, v3(pos[0], pos[1], pos[2]), f);
-    __half h[48];
+    const __half2* t2 = reinterpret_cast<const __half2*>(table);
+    const V3 x = v3(pos[0], pos[1], pos[2]);
+#pragma unroll 1
+    for (uint32_t g = 0; g < fv.n_levels / 4; ++g) {
+        float v[8];
 #pragma unroll
-    for (int i = 0; i < 32; ++i) h[i] = to_act(f[i], bf16);
-    for (uint32_t m = 0; m < fv.n_extra; ++m) h[32 + m] = to_act(mask != 7u ? 1.f : (extra ? extra[m] : 0.f), bf16);
-    store_row_global(rec, row, k_in, h);
+        for (uint32_t j = 0; j < 4; ++j) hash_level(fv, t2, x, 4 * g + j, v[2 * j], v[2 * j + 1]);
+        uint4 q;
+        q.x = pack_act(v[0], v[1], bf16); q.y = pack_act(v[2], v[3], bf16);
+        q.z = pack_act(v[4], v[5], bf16); q.w = pack_act(v[6], v[7], bf16);
+        *reinterpret_cast<uint4*>(rec + tile_offset(row, 8 * g, k_in)) = q;
+    }
+    for (uint32_t g = 0; g < fv.n_extra / 8; ++g) {
+        float v[8];
+#pragma unroll
+        for (uint32_t j = 0; j < 8; ++j) v[j] = mask != 7u ? 1.f : (extra ? __ldg(extra + 8 * g + j) : 0.f);
+        uint4 q;
+        q.x = pack_act(v[0], v[1], bf16); q.y = pack_act(v[2], v[3], bf16);
+        q.z = pack_act(v[4], v[5], bf16); q.w = pack_act(v[6], v[7], bf16);
+        *reinterpret_cast<uint4*>(rec + tile_offset(row, 2 * fv.n_levels + 8 * g, k_in)) = q;
+    }
     float d[16];
     sh4(dirw[0], dirw[1], dirw[2], d);
+    uint8_t* sh = rec + hash_tile_bytes(k_in);
 #pragma unroll
-    for (int i = 0; i < 16; ++i) h[i] = to_act(d[i], bf16);
-    store_row_global(rec + hash_tile_bytes(k_in), row, 16, h);
+    for (uint32_t g = 0; g < 2; ++g) {
+        uint4 q;
+        q.x = pack_act(d[8 * g + 0], d[8 * g + 1], bf16); q.y = pack_act(d[8 * g + 2], d[8 * g + 3], bf16);
+        q.z = pack_act(d[8 * g + 4], d[8 * g + 5], bf16); q.w = pack_act(d[8 * g + 6], d[8 * g + 7], bf16);
+        *reinterpret_cast<uint4*>(sh + tile_offset(row, 8 * g, 16)) = q;
+    }
 }
 
 // One thread per alive ray: the next `steps` sample positions (generate_next_nerf_network_inputs,
