@@ -37,10 +37,7 @@ __device__ __forceinline__ float prune_limit(float best) {
 
 // Exact squared distance of p to the triangle at Morton slot `slot`; its original id in `id`.
 __device__ __forceinline__ float slot_distance(const FrameView& fr, int32_t slot, V3 p, int32_t& id) {
-    const float4* tr = fr.leaf_tris + (size_t)slot * 3;
-    float4 q0 = __ldg(tr), q1 = __ldg(tr + 1), q2 = __ldg(tr + 2);
-    id = __float_as_int(q2.y);
-    return tri_distance_sq(v3(q0.x, q0.y, q0.z), v3(q0.w, q1.x, q1.y), v3(q1.z, q1.w, q2.x), p);
+    return tri_distance_rec(fr.leaf_tris + (size_t)slot * INSTA_TRI_F4, p, id);
 }
 
 __device__ __forceinline__ Nearest nearest_bvh(const FrameView& fr, V3 p, float best, int32_t bid, int32_t bslot, uint32_t* err) {

@@ -68,6 +68,52 @@ __device__ __forceinline__ float tri_distance_sq(V3 a, V3 b, V3 c, V3 pos) {
     return __fdiv_rn(__fmul_rn(nd, nd), dot_rn(nor, nor));
 }
 
+// Point-independent terms of tri_distance_sq for one triangle, written as INSTA_TRI_F4 float4.
+__device__ __forceinline__ void tri_record(V3 a, V3 b, V3 c, uint32_t id, float4* dst) {
+    const V3 v21 = sub_rn(b, a), v32 = sub_rn(c, b), v13 = sub_rn(a, c);
+    const V3 nor = cross_rn(v21, v13);
+    const V3 c1 = cross_rn(v21, nor), c2 = cross_rn(v32, nor), c3 = cross_rn(v13, nor);
+    dst[0] = make_float4(a.x, a.y, a.z, b.x);
+    dst[1] = make_float4(b.y, b.z, c.x, c.y);
+    dst[2] = make_float4(c.z, __uint_as_float(id), dot_rn(v21, v21), dot_rn(v32, v32));
+    dst[3] = make_float4(v21.x, v21.y, v21.z, dot_rn(v13, v13));
+    dst[4] = make_float4(v32.x, v32.y, v32.z, dot_rn(nor, nor));
+    dst[5] = make_float4(v13.x, v13.y, v13.z, nor.x);
+    dst[6] = make_float4(c1.x, c1.y, c1.z, nor.y);
+    dst[7] = make_float4(c2.x, c2.y, c2.z, nor.z);
+    dst[8] = make_float4(c3.x, c3.y, c3.z, 0.f);
+}
+
+// tri_distance_sq from a precomputed record: only the point-dependent operations remain, in the
+// same order, so the result is bit-identical.
+__device__ __forceinline__ float tri_distance_rec(const float4* tr, V3 pos, int32_t& id) {
+    const float4 q0 = __ldg(tr), q1 = __ldg(tr + 1), q2 = __ldg(tr + 2), q3 = __ldg(tr + 3), q4 = __ldg(tr + 4);
+    const float4 q5 = __ldg(tr + 5), q6 = __ldg(tr + 6), q7 = __ldg(tr + 7), q8 = __ldg(tr + 8);
+    id = __float_as_int(q2.y);
+    const V3 p1 = sub_rn(pos, v3(q0.x, q0.y, q0.z)), p2 = sub_rn(pos, v3(q0.w, q1.x, q1.y)), p3 = sub_rn(pos, v3(q1.z, q1.w, q2.x));
+    const V3 v21 = v3(q3.x, q3.y, q3.z), v32 = v3(q4.x, q4.y, q4.z), v13 = v3(q5.x, q5.y, q5.z);
+    const V3 nor = v3(q5.w, q6.w, q7.w);
+    const float s1 = sign_f(dot_rn(v3(q6.x, q6.y, q6.z), p1));
+    const float s2 = sign_f(dot_rn(v3(q7.x, q7.y, q7.z), p2));
+    const float s3 = sign_f(dot_rn(v3(q8.x, q8.y, q8.z), p3));
+    const float s = __fadd_rn(__fadd_rn(s1, s2), s3);
+    if (s < 2.0f) {
+        float f1 = clamp01_like(__fdiv_rn(dot_rn(v21, p1), q2.z), 0.f, 1.f);
+        float f2 = clamp01_like(__fdiv_rn(dot_rn(v32, p2), q2.w), 0.f, 1.f);
+        float f3 = clamp01_like(__fdiv_rn(dot_rn(v13, p3), q3.w), 0.f, 1.f);
+        V3 e1 = {__fsub_rn(__fmul_rn(v21.x, f1), p1.x), __fsub_rn(__fmul_rn(v21.y, f1), p1.y), __fsub_rn(__fmul_rn(v21.z, f1), p1.z)};
+        V3 e2 = {__fsub_rn(__fmul_rn(v32.x, f2), p2.x), __fsub_rn(__fmul_rn(v32.y, f2), p2.y), __fsub_rn(__fmul_rn(v32.z, f2), p2.z)};
+        V3 e3 = {__fsub_rn(__fmul_rn(v13.x, f3), p3.x), __fsub_rn(__fmul_rn(v13.y, f3), p3.y), __fsub_rn(__fmul_rn(v13.z, f3), p3.z)};
+        float d1 = dot_rn(e1, e1), d2 = dot_rn(e2, e2), d3 = dot_rn(e3, e3);
+        float m = d1;
+        if (d2 < m) m = d2;
+        if (d3 < m) m = d3;
+        return m;
+    }
+    const float nd = dot_rn(nor, p1);
+    return __fdiv_rn(__fmul_rn(nd, nd), q4.w);
+}
+
 // BoundingBox::distance_sq (NGP/bounding_box.cuh:228-230).
 __device__ __forceinline__ float box_distance_sq(float mnx, float mny, float mnz, float mxx, float mxy, float mxz, V3 p) {
     float ax = __fsub_rn(mnx, p.x), bx = __fsub_rn(p.x, mxx);

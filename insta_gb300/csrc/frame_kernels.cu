@@ -279,7 +279,8 @@ __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs one, const
     }
     // 4. triangle records in Morton order
     for (int s = tid; s < a.F; s += nt) {
-        float4* dst = a.leaf_tris + (size_t)s * 3;
+        // vertices and id only; tri_record_kernel fills in the rest of the record across the GPU
+        float4* dst = a.leaf_tris + (size_t)s * INSTA_TRI_F4;
         uint32_t f = (uint32_t)(keys[s] & 0xffffffffu);
         int i0 = a.faces[f * 3], i1 = a.faces[f * 3 + 1], i2 = a.faces[f * 3 + 2];
         const float* A = a.verts + i0 * 3; const float* B = a.verts + i1 * 3; const float* C = a.verts + i2 * 3;
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs one, const
                     if ((uint32_t)rr[i] & INSTA_LEAF_BIT) {
                         const uint32_t first = ((uint32_t)rr[i] & ~(uint32_t)INSTA_LEAF_BIT) >> 3, count = (uint32_t)rr[i] & 7u;
                         for (uint32_t t = first; t < first + count; ++t) {
-                            const float4* tr = a.leaf_tris + (size_t)t * 3;
+                            const float4* tr = a.leaf_tris + (size_t)t * INSTA_TRI_F4;
                             float4 q0 = tr[0], q1 = tr[1], q2 = tr[2];
                             float pts[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
                             for (int p = 0; p < 3; ++p) {
@@ -477,6 +478,18 @@ static int sm_count_frames() {
 }
 
 // ------------------------------------------------------------------- launchers
+// Completes the Morton-ordered triangle records the build left as (vertices, id): the
+// point-independent terms of the exact distance (tri_record).  A batch passes the build arguments
+// of every frame (blockIdx.y picks one).
+__global__ void tri_record_kernel(float4* __restrict__ leaf_tris, int F, const BvhBuildArgs* __restrict__ many) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (many) leaf_tris = many[blockIdx.y].leaf_tris;
+    if (s >= F) return;
+    float4* dst = leaf_tris + (size_t)s * INSTA_TRI_F4;
+    const float4 q0 = dst[0], q1 = dst[1], q2 = dst[2];
+    tri_record(v3(q0.x, q0.y, q0.z), v3(q0.w, q1.x, q1.y), v3(q1.z, q1.w, q2.x), __float_as_uint(q2.y), dst);
+}
+
 cudaError_t launch_tri_frames(int F, const float* verts, const int32_t* faces, const uint32_t* mask, const float* canon_area,
                               float* area_out, TriFrame* out, int with_inverse, cudaStream_t s) {
     tri_frame_kernel<<<(F + 255) / 256, 256, 0, s>>>(F, verts, faces, mask, canon_area, area_out, out, with_inverse, nullptr);
@@ -512,6 +525,7 @@ cudaError_t launch_bvh_build(const FrameView& fv, const float* verts, const int3
     cudaError_t e = cudaFuncSetAttribute(bvh_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     bvh_build_kernel<<<1, 1024, smem, s>>>(bvh_args(fv, verts, faces, scratch), nullptr);
+    tri_record_kernel<<<(fv.n_tris + 255) / 256, 256, 0, s>>>(const_cast<float4*>(fv.leaf_tris), fv.n_tris, nullptr);
     return cudaGetLastError();
 }
 
@@ -538,6 +552,7 @@ cudaError_t launch_frames_batch(int n, int F, const FrameView* views, const floa
     e = cudaFuncSetAttribute(bvh_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     bvh_build_kernel<<<n, 1024, smem, s>>>(BvhBuildArgs{}, dargs);
+    tri_record_kernel<<<dim3((F + 255) / 256, n), 256, 0, s>>>(nullptr, F, dargs);
     return cudaGetLastError();
 }
 

@@ -565,7 +565,7 @@ Frame& prepare_frame(insta_ctx* ctx, Avatar& a, int frame, const float* verts) {
     const int max_nodes = std::max(1, a.F);
     ctx->alloc(f.verts, (size_t)a.V * 12);
     ctx->alloc(f.frames, (size_t)a.F * sizeof(TriFrame));
-    ctx->alloc(f.leaf_tris, (size_t)a.F * 48);
+    ctx->alloc(f.leaf_tris, (size_t)a.F * INSTA_TRI_F4 * 16);
     ctx->alloc(f.nodes, (size_t)max_nodes * 112);
     host_copy(f.verts.p, verts, (size_t)a.V * 12, ctx->stream);
     f.view.leaf_tris = static_cast<const float4*>(f.leaf_tris.p);
@@ -720,7 +720,7 @@ int insta_frame_upload(insta_ctx* ctx, int avatar, int frame, const float* verts
         if (!verts || frame < 0) fail(INSTA_ERR_INVALID_ARG, "bad frame upload");
         ctx->alloc(ctx->bvh_scratch, bvh_scratch_bytes(a.F));
         Frame& f = prepare_frame(ctx, a, frame, verts);
-        Stage st(ctx, INSTA_STAGE_FRAME, 2);
+        Stage st(ctx, INSTA_STAGE_FRAME, 3);
         CK(launch_tri_frames(a.F, (const float*)f.verts.p, (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
                              (const float*)a.canon_area.p, nullptr, (TriFrame*)f.frames.p, 1, ctx->stream));
         CK(launch_bvh_build(f.view, (const float*)f.verts.p, (const int32_t*)a.faces.p, ctx->bvh_scratch.p, ctx->stream));
@@ -746,7 +746,7 @@ int insta_frame_upload_batch(insta_ctx* ctx, int avatar, const int32_t* frames, 
             views[(size_t)i] = f.view;
             dverts[(size_t)i] = (const float*)f.verts.p;
         }
-        Stage st(ctx, INSTA_STAGE_FRAME, 2);
+        Stage st(ctx, INSTA_STAGE_FRAME, 3);
         CK(launch_frames_batch(n, a.F, views.data(), dverts.data(), (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
                                (const float*)a.canon_area.p, ctx->bvh_scratch.p, ctx->frame_jobs.p, ctx->stream));
     });

@@ -19,13 +19,17 @@ namespace insta {
 struct TriFrame;
 
 // Per-frame deformed mesh: 4-wide LBVH over Morton-ordered triangles.
-//   leaf_tris: [n_tris][3] float4 in Morton order -- (a.xyz, b.x) (b.yz, c.xy) (c.z, id bits, 0, 0)
+//   leaf_tris: [n_tris][INSTA_TRI_F4] float4 in Morton order -- (a.xyz, b.x) (b.yz, c.xy)
+//              (c.z, id bits, |v21|^2, |v32|^2) (v21, |v13|^2) (v32, |n|^2) (v13, n.x)
+//              (v21 x n, n.y) (v32 x n, n.z) (v13 x n, 0): the vertices plus every point-independent
+//              term of Triangle::distance_sq, computed with the same operations (same bits)
 //   nodes:     [n_nodes][7] float4 -- child boxes SoA (min.x[4] min.y[4] min.z[4] max.x[4] max.y[4]
 //              max.z[4]) and the four child references (int bits): >= 0 internal node index,
 //              INSTA_LEAF_BIT | (first slot << 3) | count for a leaf, -1 for an empty slot.
 //   Node 0 is the root.
 #define INSTA_LEAF_BIT 0x40000000
 #define INSTA_LEAF_SIZE 2
+#define INSTA_TRI_F4 9
 struct FrameView {
     const float4* leaf_tris;
     const float4* nodes;
