@@ -17,9 +17,13 @@
  *                               instant-ngp/src/triangle_bvh.cu:548-631; src/core.cu:309-334)
  *   insta_occupancy_from_mesh   mark_flame_density_grid + update_density_grid_mean_and_bitfield
  *                               (instant-ngp/src/testbed_nerf.cu:364-389,2863-2878)
+ *   insta_density_grid_load     the snapshot's density grid -> bitfield (grid_to_bitfield +
+ *                               bitfield_max_pool, instant-ngp/src/testbed_nerf.cu:585-632)
  *   insta_canonical_map         rta::Core::surface_closest_point / render_deformed -> `warp`
  *                               (src/core.cu:339-348,442-526,581-637)
  *   insta_canonical_map_soa     the same map on bare points (index + canonical xyz)
+ *   insta_training_samples      generate_training_samples_nerf + warp (instant-ngp/src/
+ *                               testbed_nerf.cu:1105-1285,3290)
  *   insta_params_load           Testbed::load_snapshot parameter blob, NerfNetwork::set_params
  *                               order (instant-ngp/src/testbed.cu:2952-3016; NGP/nerf_network.h:492-525)
  *   insta_field_eval            NerfNetwork::inference_mixed_precision_impl (NGP/nerf_network.h:159-232)
@@ -144,6 +148,11 @@ int insta_occupancy_from_mesh(insta_ctx* ctx, int avatar, int frame, double radi
 /* 8 mips x 128^3 bits (2 MiB), Morton order per mip; host or device pointer. */
 int insta_occupancy_set(insta_ctx* ctx, int avatar, int frame, const uint8_t* bits);
 int insta_occupancy_get(insta_ctx* ctx, int avatar, int frame, uint8_t* bits);
+/* A snapshot's density grid (density_grid_binary: n_cascades x 128^3 values, Morton order per
+ * cascade; FP16 when fp16 != 0, else FP32; host or device) -> the frame's bitfield:
+ * threshold min(0.01, mean of max(v, 0) over cascade 0), then the mip max-pool
+ * (update_density_grid_mean_and_bitfield, instant-ngp/src/testbed_nerf.cu:585-632,2863-2878). */
+int insta_density_grid_load(insta_ctx* ctx, int avatar, int frame, const void* grid, uint32_t n_cascades, int fp16);
 
 /* -- deformation -------------------------------------------------------------- */
 /* In place on NerfCoordinate records (device pointer, stride floats each: pos[3] dt holder
@@ -153,6 +162,22 @@ int insta_canonical_map(insta_ctx* ctx, int avatar, int frame, float* coords, ui
 /* Bare points (device pointers): nearest triangle id (-1 when none) and canonical xyz. */
 int insta_canonical_map_soa(insta_ctx* ctx, int avatar, int frame, const float* pts, int64_t n, int32_t* out_idx,
                             float* out_canon);
+
+/* -- training samples ------------------------------------------------------------ */
+/* The training-sample entry (generate_training_samples_nerf, instant-ngp/src/testbed_nerf.cu:
+ * 1105-1285, then the warp with per-record frames, :3290 -> src/core.cu:339-348) for rays the
+ * caller drew: rays f32[n][6] (origin, unnormalised direction), image u32[n] (training image =
+ * uploaded frame id, written to `holder`), start_rand f32[n] (uniform [0,1) jitter draws),
+ * extra f32[n_images][stride - 11] or NULL.  Marches the train box through grid_frame's
+ * occupancy (<= 1024 steps per ray), reserves each ray's block of NerfCoordinate records
+ * (stride floats) atomically, and maps them to canonical space in place.  ray_indices[k] and
+ * numsteps[k] = (count, base) describe kept ray k; counters = (rays kept, samples requested);
+ * blocks past max_samples are dropped as in the reference.  All pointers are device pointers;
+ * asynchronous on the context's stream. */
+int insta_training_samples(insta_ctx* ctx, int avatar, int grid_frame, const float* rays, const uint32_t* image,
+                           const float* start_rand, const float* extra, uint32_t n_images, int64_t n_rays, float cone_angle,
+                           uint32_t max_samples, float* coords, uint32_t stride, uint32_t* ray_indices, uint32_t* numsteps,
+                           uint32_t* counters);
 
 /* -- field -------------------------------------------------------------------- */
 /* FP16 parameter blob in snapshot order (density MLP, rgb MLP, hash table); host or

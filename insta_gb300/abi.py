@@ -21,7 +21,8 @@ EXPORTS = [
     "insta_stats_enable", "insta_stats_read",
     "insta_canonical_set", "insta_avatar_set_boxes", "insta_avatar_set_flags", "insta_frame_upload",
     "insta_frame_upload_batch", "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
-    "insta_canonical_map", "insta_canonical_map_soa", "insta_field_param_count", "insta_params_load",
+    "insta_density_grid_load",
+    "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
     "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_batch",
     "insta_render_samples", "insta_march_debug",
 ]
@@ -85,8 +86,10 @@ def load(path: Path | None = None):
             "insta_occupancy_from_mesh": [vp, C.c_int, C.c_int, C.c_double],
             "insta_occupancy_set": [vp, C.c_int, C.c_int, vp],
             "insta_occupancy_get": [vp, C.c_int, C.c_int, vp],
+            "insta_density_grid_load": [vp, C.c_int, C.c_int, vp, u32, C.c_int],
             "insta_canonical_map": [vp, C.c_int, C.c_int, vp, u32, u32, i64],
             "insta_canonical_map_soa": [vp, C.c_int, C.c_int, vp, i64, vp, vp],
+            "insta_training_samples": [vp, C.c_int, C.c_int, vp, vp, vp, vp, u32, i64, C.c_float, u32, vp, u32, vp, vp, vp],
             "insta_field_param_count": [C.POINTER(FieldDesc), C.POINTER(u64)],
             "insta_params_load": [vp, C.c_int, C.POINTER(FieldDesc), vp, u64],
             "insta_field_eval": [vp, C.c_int, vp, u32, i64, vp],
@@ -224,6 +227,18 @@ class Context:
         b = np.zeros(8 * 128 ** 3 // 8, dtype=np.uint8)
         self._check(self.lib.insta_occupancy_get(self.h, avatar, frame, _addr(b)))
         return b
+
+    def density_grid_load(self, avatar, frame, grid, n_cascades):
+        """grid: float32 or float16 array/tensor [n_cascades * 128^3] (Morton order per cascade)."""
+        g = grid if hasattr(grid, "data_ptr") else np.ascontiguousarray(grid)
+        fp16 = int(str(g.dtype).endswith("float16"))
+        self._check(self.lib.insta_density_grid_load(self.h, avatar, frame, _addr(g), n_cascades, fp16))
+
+    def training_samples(self, avatar, grid_frame, rays, image, start_rand, max_samples, coords, stride, ray_indices,
+                         numsteps, counters, cone_angle=1 / 256, extra=None, n_images=0):
+        self._check(self.lib.insta_training_samples(self.h, avatar, grid_frame, _addr(rays), _addr(image), _addr(start_rand),
+                                                    _addr(extra), n_images, len(rays), float(cone_angle), max_samples,
+                                                    _addr(coords), stride, _addr(ray_indices), _addr(numsteps), _addr(counters)))
 
     def canonical_map(self, avatar, frame, coords, stride, n_extra, n):
         self._check(self.lib.insta_canonical_map(self.h, avatar, frame, _addr(coords), stride, n_extra, n))

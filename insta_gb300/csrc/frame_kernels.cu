@@ -422,6 +422,62 @@ __global__ void maxpool_kernel(const uint8_t* __restrict__ prev, uint8_t* __rest
     next[morton3d(x, y, z)] |= bits;
 }
 
+// ---------------------------------------------------------------- density grid -> bitfield
+// update_density_grid_mean_and_bitfield (ngp/src/testbed_nerf.cu:2863-2878) for a loaded grid.
+// The mean of max(v, 0) / 128^3 over cascade 0 is reduced deterministically: fixed per-block
+// trees, then one block over the block sums in index order.
+constexpr uint32_t kMeanBlocks = 1024;
+
+__global__ void __launch_bounds__(256) density_convert_kernel(const uint16_t* __restrict__ half_grid, float* __restrict__ grid, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        grid[i] = __half2float(__ushort_as_half(half_grid[i]));
+}
+
+__global__ void __launch_bounds__(256) density_mean_partial_kernel(const float* __restrict__ grid, float* __restrict__ partial) {
+    __shared__ float red[256];
+    const uint32_t per = GRID3 / kMeanBlocks;   // 2048 cells per block
+    float acc = 0.f;
+    for (uint32_t k = threadIdx.x; k < per; k += blockDim.x)
+        acc = __fadd_rn(acc, __fdiv_rn(fmaxf(grid[blockIdx.x * per + k], 0.f), (float)GRID3));
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (uint32_t o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] = __fadd_rn(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void __launch_bounds__(256) density_mean_final_kernel(float* __restrict__ partial, float* __restrict__ thresh_out) {
+    __shared__ float red[256];
+    float acc = 0.f;
+    for (uint32_t k = threadIdx.x; k < kMeanBlocks; k += blockDim.x) acc = __fadd_rn(acc, partial[k]);
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (uint32_t o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] = __fadd_rn(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) thresh_out[0] = fminf(0.01f, red[0]);   // NERF_MIN_OPTICAL_THICKNESS
+}
+
+// grid_to_bitfield (:585-609): one byte (8 Morton-consecutive cells) per thread over all mips.
+__global__ void __launch_bounds__(256) grid_to_bitfield_kernel(const float* __restrict__ grid, uint32_t n_cascades,
+                                                               const float* __restrict__ thresh, uint8_t* __restrict__ bits) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= GRID3 / 8 * 8) return;
+    uint8_t b = 0;
+    if (i < GRID3 / 8 * n_cascades) {
+        const float t = *thresh;
+        const float4 lo = reinterpret_cast<const float4*>(grid)[(size_t)i * 2];
+        const float4 hi = reinterpret_cast<const float4*>(grid)[(size_t)i * 2 + 1];
+        const float v[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+        for (int j = 0; j < 8; ++j) b |= v[j] > t ? (uint8_t)(1u << j) : (uint8_t)0;
+    }
+    bits[i] = b;
+}
+
 // ---------------------------------------------------------------- canonical map
 __global__ void __launch_bounds__(256) canonical_map_soa_kernel(FrameView fr, DeformView dv, const float* __restrict__ pts, int64_t n,
                                                                 int32_t* __restrict__ out_idx, float* __restrict__ out_canon, uint32_t* err) {
@@ -444,7 +500,8 @@ __global__ void __launch_bounds__(256) canonical_map_soa_kernel(FrameView fr, De
 // is fixed (frame_id >= 0, render_deformed) or read from `holder` (surface_closest_point).
 __global__ void __launch_bounds__(256) canonical_map_coords_kernel(const FrameView* __restrict__ frames, uint32_t n_frames, DeformView dv,
                                                                    float* __restrict__ coords, uint32_t stride, uint32_t n_extra, int64_t n,
-                                                                   int32_t frame_id, uint32_t* err) {
+                                                                   int32_t frame_id, uint32_t* err, const uint32_t* __restrict__ n_dev) {
+    if (n_dev && (int64_t)*n_dev < n) n = (int64_t)*n_dev;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         float* c = coords + i * stride;
         float holder = c[4];
@@ -564,6 +621,25 @@ cudaError_t launch_occupancy(const FrameView& fv, double radius, uint8_t* bitfie
     return cudaGetLastError();
 }
 
+size_t density_scratch_bytes(uint32_t n_cascades) { return (size_t)n_cascades * GRID3 * 4 + (kMeanBlocks + 4) * 4; }
+
+cudaError_t launch_density_grid(const void* grid, int fp16, uint32_t n_cascades, void* scratch, uint8_t* bitfield, cudaStream_t s) {
+    float* g = static_cast<float*>(scratch);
+    float* partial = g + (size_t)n_cascades * GRID3;
+    float* thresh = partial + kMeanBlocks;
+    const uint32_t n = n_cascades * GRID3;
+    cudaError_t e = cudaSuccess;
+    if (fp16) density_convert_kernel<<<sm_count_frames() * 8, 256, 0, s>>>(static_cast<const uint16_t*>(grid), g, n);
+    else e = cudaMemcpyAsync(g, grid, (size_t)n * 4, cudaMemcpyDefault, s);
+    if (e != cudaSuccess) return e;
+    density_mean_partial_kernel<<<kMeanBlocks, 256, 0, s>>>(g, partial);
+    density_mean_final_kernel<<<1, 256, 0, s>>>(partial, thresh);
+    grid_to_bitfield_kernel<<<GRID3 / 8 * 8 / 256, 256, 0, s>>>(g, n_cascades, thresh, bitfield);
+    for (int lvl = 1; lvl < 8; ++lvl)
+        maxpool_kernel<<<(GRID3 / 64 + 255) / 256, 256, 0, s>>>(bitfield + (size_t)(lvl - 1) * GRID3 / 8, bitfield + (size_t)lvl * GRID3 / 8);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_canonical_map_soa(const FrameView& fv, const DeformView& dv, const float* pts, int64_t n, int32_t* out_idx,
                                      float* out_canon, uint32_t* err, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
@@ -574,11 +650,12 @@ cudaError_t launch_canonical_map_soa(const FrameView& fv, const DeformView& dv, 
 }
 
 cudaError_t launch_canonical_map_coords(const FrameView* frames_dev, uint32_t n_frames, const DeformView& dv, float* coords,
-                                        uint32_t stride, uint32_t n_extra, int64_t n, int32_t frame_id, uint32_t* err, cudaStream_t s) {
+                                        uint32_t stride, uint32_t n_extra, int64_t n, int32_t frame_id, uint32_t* err, cudaStream_t s,
+                                        const uint32_t* n_dev) {
     if (n <= 0) return cudaSuccess;
     int64_t blocks = (n + 255) / 256;
     int grid = (int)(blocks < sm_count_frames() * 16 ? blocks : sm_count_frames() * 16);
-    canonical_map_coords_kernel<<<grid, 256, 0, s>>>(frames_dev, n_frames, dv, coords, stride, n_extra, n, frame_id, err);
+    canonical_map_coords_kernel<<<grid, 256, 0, s>>>(frames_dev, n_frames, dv, coords, stride, n_extra, n, frame_id, err, n_dev);
     return cudaGetLastError();
 }
 

@@ -95,7 +95,7 @@ struct insta_ctx {
     uint32_t* err_dev = nullptr;
     uint32_t* ray_counter = nullptr;
     unsigned long long* sample_counter = nullptr;
-    DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs;
+    DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs, density_scratch, density_stage;
     Wave wave;
     uint32_t* host_counters = nullptr;   // pinned: alive-ray counts read between rounds
     int sms = 0;
@@ -578,6 +578,20 @@ Frame& prepare_frame(insta_ctx* ctx, Avatar& a, int frame, const float* verts) {
     return f;
 }
 
+// Device table of the avatar's frame views, indexed by frame id (the `holder` lookup of warp).
+void refresh_frame_table(insta_ctx* ctx, Avatar& a) {
+    if (!a.table_dirty) return;
+    int max_id = a.frames.empty() ? -1 : a.frames.rbegin()->first;
+    std::vector<FrameView> table((size_t)std::max(1, max_id + 1));
+    for (auto& fv : table) std::memset(&fv, 0, sizeof(fv));
+    for (auto& kv : a.frames) table[kv.first] = kv.second.view;
+    ctx->alloc(a.frame_table, table.size() * sizeof(FrameView));
+    CK(cudaMemcpyAsync(a.frame_table.p, table.data(), table.size() * sizeof(FrameView), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    a.table_frames = (uint32_t)(max_id + 1);
+    a.table_dirty = false;
+}
+
 }  // namespace
 
 extern "C" {
@@ -787,6 +801,25 @@ int insta_occupancy_set(insta_ctx* ctx, int avatar, int frame, const uint8_t* bi
     });
 }
 
+int insta_density_grid_load(insta_ctx* ctx, int avatar, int frame, const void* grid, uint32_t n_cascades, int fp16) {
+    return guarded(ctx, [&] {
+        if (!grid) fail(INSTA_ERR_INVALID_ARG, "null density grid");
+        if (n_cascades < 1 || n_cascades > 8) fail(INSTA_ERR_INVALID_ARG, "n_cascades must be 1..8, got %u", n_cascades);
+        Frame& f = get_frame(ctx->avatar(avatar), frame);
+        ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
+        ctx->alloc(ctx->density_scratch, density_scratch_bytes(n_cascades));
+        const void* src = grid;
+        if (fp16 && !is_device_ptr(grid)) {
+            ctx->alloc(ctx->density_stage, (size_t)n_cascades * GRID3 * 2);
+            host_copy(ctx->density_stage.p, grid, (size_t)n_cascades * GRID3 * 2, ctx->stream);
+            src = ctx->density_stage.p;
+        }
+        Stage st(ctx, INSTA_STAGE_OCCUPANCY, fp16 ? 11 : 10);
+        CK(launch_density_grid(src, fp16, n_cascades, ctx->density_scratch.p, (uint8_t*)f.bitfield.p, ctx->stream));
+        f.has_occupancy = true;
+    });
+}
+
 int insta_occupancy_get(insta_ctx* ctx, int avatar, int frame, uint8_t* bits) {
     return guarded(ctx, [&] {
         if (!bits) fail(INSTA_ERR_INVALID_ARG, "null bitfield");
@@ -803,21 +836,43 @@ int insta_canonical_map(insta_ctx* ctx, int avatar, int frame, float* coords, ui
         if (stride < 11 + n_extra) fail(INSTA_ERR_INVALID_ARG, "stride %u < 11 + n_extra", stride);
         Avatar& a = ctx->avatar(avatar);
         if (n == 0) return;
-        if (a.table_dirty) {
-            int max_id = a.frames.empty() ? -1 : a.frames.rbegin()->first;
-            std::vector<FrameView> table((size_t)std::max(1, max_id + 1));
-            for (auto& fv : table) { std::memset(&fv, 0, sizeof(fv)); }
-            for (auto& kv : a.frames) table[kv.first] = kv.second.view;
-            ctx->alloc(a.frame_table, table.size() * sizeof(FrameView));
-            CK(cudaMemcpyAsync(a.frame_table.p, table.data(), table.size() * sizeof(FrameView), cudaMemcpyHostToDevice, ctx->stream));
-            CK(cudaStreamSynchronize(ctx->stream));
-            a.table_frames = (uint32_t)(max_id + 1);
-            a.table_dirty = false;
-        }
+        refresh_frame_table(ctx, a);
         if (frame >= 0) get_frame(a, frame);
         Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
         CK(launch_canonical_map_coords((const FrameView*)a.frame_table.p, a.table_frames, deform_view(a), coords, stride, n_extra, n,
                                        frame, ctx->err_dev, ctx->stream));
+    });
+}
+
+int insta_training_samples(insta_ctx* ctx, int avatar, int grid_frame, const float* rays, const uint32_t* image,
+                           const float* start_rand, const float* extra, uint32_t n_images, int64_t n_rays, float cone_angle,
+                           uint32_t max_samples, float* coords, uint32_t stride, uint32_t* ray_indices, uint32_t* numsteps,
+                           uint32_t* counters) {
+    return guarded(ctx, [&] {
+        if (n_rays < 0 || (n_rays > 0 && (!rays || !image || !start_rand)) || !coords || !ray_indices || !numsteps || !counters)
+            fail(INSTA_ERR_INVALID_ARG, "null buffer");
+        if (stride < 11) fail(INSTA_ERR_INVALID_ARG, "stride %u < 11", stride);
+        if (!(cone_angle >= 0.f)) fail(INSTA_ERR_INVALID_ARG, "cone_angle must be >= 0");
+        for (const void* p : {(const void*)rays, (const void*)image, (const void*)start_rand, (const void*)coords, (const void*)ray_indices,
+                              (const void*)numsteps, (const void*)counters})
+            if (n_rays > 0 && !is_device_ptr(p)) fail(INSTA_ERR_INVALID_ARG, "insta_training_samples takes device pointers");
+        Avatar& a = ctx->avatar(avatar);
+        Frame& g = get_frame(a, grid_frame);
+        if (!g.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", grid_frame);
+        refresh_frame_table(ctx, a);
+        CK(cudaMemsetAsync(counters, 0, 2 * sizeof(uint32_t), ctx->stream));
+        if (n_rays == 0) return;
+        TrainArgs T{};
+        T.rays = rays; T.image = image; T.start_rand = start_rand; T.extra = extra;
+        T.n_extra = stride - 11; T.n_images = n_images; T.n_rays = n_rays;
+        for (int k = 0; k < 3; ++k) { T.aabb_min[k] = a.train_min[k]; T.aabb_max[k] = a.train_max[k]; }
+        T.cone_angle = cone_angle; T.max_samples = max_samples; T.bitfield = (const uint8_t*)g.bitfield.p;
+        T.coords = coords; T.stride = stride; T.ray_indices = ray_indices; T.numsteps = numsteps; T.counters = counters;
+        { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_training_samples(T, ctx->stream)); }
+        // the warp with per-record frames (surface_closest_point, testbed_nerf.cu:3290)
+        Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
+        CK(launch_canonical_map_coords((const FrameView*)a.frame_table.p, a.table_frames, deform_view(a), coords, stride, stride - 11,
+                                       (int64_t)max_samples, -1, ctx->err_dev, ctx->stream, counters + 1));
     });
 }
 

@@ -100,16 +100,41 @@ cudaError_t launch_frames_batch(int n, int F, const FrameView* views, const floa
                                 const uint32_t* mask, const float* canon_area, void* scratch, void* table, cudaStream_t s);
 cudaError_t launch_bvh_build(const FrameView& fv, const float* verts, const int32_t* faces, void* scratch, cudaStream_t s);
 cudaError_t launch_occupancy(const FrameView& fv, double radius, uint8_t* bitfield, uint32_t* err, cudaStream_t s);
+// Float (or FP16) density grid [n_cascades][128^3] (Morton order) -> bitfield with mips.
+size_t density_scratch_bytes(uint32_t n_cascades);
+cudaError_t launch_density_grid(const void* grid, int fp16, uint32_t n_cascades, void* scratch, uint8_t* bitfield, cudaStream_t s);
 cudaError_t launch_canonical_map_soa(const FrameView& fv, const DeformView& dv, const float* pts, int64_t n, int32_t* out_idx,
                                      float* out_canon, uint32_t* err, cudaStream_t s);
+// n_dev (optional): a device count; records [0, min(n, *n_dev)) are mapped
 cudaError_t launch_canonical_map_coords(const FrameView* frames_dev, uint32_t n_frames, const DeformView& dv, float* coords,
-                                        uint32_t stride, uint32_t n_extra, int64_t n, int32_t frame_id, uint32_t* err, cudaStream_t s);
+                                        uint32_t stride, uint32_t n_extra, int64_t n, int32_t frame_id, uint32_t* err, cudaStream_t s,
+                                        const uint32_t* n_dev = nullptr);
 
 cudaError_t launch_ray_init(const WaveArgs& a, uint32_t total_tiles, cudaStream_t s);
 cudaError_t launch_march(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_deform_encode(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_composite(const WaveArgs& a, cudaStream_t s);
+// generate_training_samples_nerf on caller-supplied rays (see insta_training_samples).
+struct TrainArgs {
+    const float* rays;          // [n][6] origin, unnormalised direction
+    const uint32_t* image;      // [n] training image (= deformed frame id), written to `holder`
+    const float* start_rand;    // [n] uniform draw of the start jitter
+    const float* extra;         // [n_images][n_extra] or null
+    uint32_t n_extra, n_images;
+    int64_t n_rays;
+    float aabb_min[3], aabb_max[3];
+    float cone_angle;
+    uint32_t max_samples;
+    const uint8_t* bitfield;
+    float* coords;              // [max_samples][stride]
+    uint32_t stride;
+    uint32_t* ray_indices;      // [n]
+    uint32_t* numsteps;         // [n][2] (count, base)
+    uint32_t* counters;         // [2] rays kept, samples requested
+};
+cudaError_t launch_training_samples(const TrainArgs& a, cudaStream_t s);
+
 cudaError_t launch_encode_coords(const FieldView& fv, const float* coords, uint32_t stride, int64_t n, uint8_t* tiles,
                                  uint32_t tile_bytes, uint32_t k_in, cudaStream_t s);
 cudaError_t launch_unpack(const uint2* out, const float4* out_f32, int bf16, int64_t n, float4* dst, cudaStream_t s);

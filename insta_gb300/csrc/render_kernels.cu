@@ -631,6 +631,72 @@ __global__ void unpack_outputs_kernel(const uint2* __restrict__ out, const float
     dst[i] = make_float4(rg.x, rg.y, bd.x, bd.y);
 }
 
+// ------------------------------------------------------------------ training samples
+// generate_training_samples_nerf (ngp/src/testbed_nerf.cu:1105-1285) for caller-supplied rays:
+// two passes per ray (count up to NERF_STEPS = 1024 occupied steps through the train box, then
+// reserve a block atomically and write NerfCoordinate records with holder = image).
+__global__ void __launch_bounds__(256) training_samples_kernel(const __grid_constant__ TrainArgs A) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n_rays) return;
+    const float* r = A.rays + i * 6;
+    const V3 o = v3(r[0], r[1], r[2]);
+    const V3 d = normalize_rn(v3(r[3], r[4], r[5]));
+    const V3 idir = v3(__fdiv_rn(1.f, d.x), __fdiv_rn(1.f, d.y), __fdiv_rn(1.f, d.z));
+    float startt = fmaxf(aabb_ray_tmin(A.aabb_min, A.aabb_max, o, d), 0.0f);
+    startt = __fadd_rn(startt, __fmul_rn(calc_dt(startt, A.cone_angle), A.start_rand[i]));
+    uint32_t j = 0;
+    float t = startt;
+    for (int guard = 0; guard < (1 << 16) && j < 1024u; ++guard) {
+        const V3 pos = ray_at(o, d, t);
+        if (!box_contains(A.aabb_min, A.aabb_max, pos)) break;
+        const float dt = calc_dt(t, A.cone_angle);
+        const int mip = mip_from_dt(dt, pos);
+        if (occupied_at(pos, A.bitfield, mip)) { ++j; t = __fadd_rn(t, dt); }
+        else t = advance_to_next_voxel(t, A.cone_angle, pos, d, idir, GRID >> mip);
+    }
+    if (j == 0) return;
+    const uint32_t base = atomicAdd(A.counters + 1, j);
+    if (base + j > A.max_samples) {
+        // the block does not fit (dropped, as in the reference); mark the part that lies inside the
+        // buffer as unused so the warp pass skips it
+        for (uint32_t q = base; q < A.max_samples; ++q) A.coords[(size_t)q * A.stride + 4] = -1.f;
+        return;
+    }
+    const uint32_t ri = atomicAdd(A.counters + 0, 1u);
+    A.ray_indices[ri] = (uint32_t)i;
+    A.numsteps[2 * ri] = j;
+    A.numsteps[2 * ri + 1] = base;
+    const uint32_t img = A.image[i];
+    const float wd[3] = {__fmul_rn(__fadd_rn(d.x, 1.0f), 0.5f), __fmul_rn(__fadd_rn(d.y, 1.0f), 0.5f), __fmul_rn(__fadd_rn(d.z, 1.0f), 0.5f)};
+    const float* ex = (A.extra && img < A.n_images) ? A.extra + (size_t)img * A.n_extra : nullptr;
+    t = startt;
+    uint32_t w = 0;
+    for (int guard = 0; guard < (1 << 16) && w < j; ++guard) {
+        const V3 pos = ray_at(o, d, t);
+        if (!box_contains(A.aabb_min, A.aabb_max, pos)) break;
+        const float dt = calc_dt(t, A.cone_angle);
+        const int mip = mip_from_dt(dt, pos);
+        if (occupied_at(pos, A.bitfield, mip)) {
+            float* c = A.coords + (size_t)(base + w) * A.stride;
+            const float p3[3] = {pos.x, pos.y, pos.z};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float rel = __fdiv_rn(__fsub_rn(p3[k], A.aabb_min[k]), __fsub_rn(A.aabb_max[k], A.aabb_min[k]));
+                c[k] = rel;
+                c[5 + k] = rel;
+                c[8 + k] = wd[k];
+            }
+            c[3] = warp_dt(dt);
+            c[4] = (float)img;
+            for (uint32_t m = 0; m < A.n_extra; ++m) c[A.stride - A.n_extra + m] = ex ? ex[m] : 0.f;
+            ++w;
+            t = __fadd_rn(t, dt);
+        } else {
+            t = advance_to_next_voxel(t, A.cone_angle, pos, d, idir, GRID >> mip);
+        }
+    }
+}
+
 // ------------------------------------------------------------------ march debug
 __global__ void march_debug_kernel(RenderView rv, const uint8_t* __restrict__ bf, int max_out, float* out_t, float* out_dt, int32_t* out_n) {
     uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -726,6 +792,12 @@ cudaError_t launch_encode_coords(const FieldView& fv, const float* coords, uint3
 cudaError_t launch_unpack(const uint2* out, const float4* out_f32, int bf16, int64_t n, float4* dst, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     unpack_outputs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, out_f32, bf16, n, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_training_samples(const TrainArgs& a, cudaStream_t s) {
+    if (a.n_rays <= 0) return cudaSuccess;
+    training_samples_kernel<<<(unsigned)((a.n_rays + 255) / 256), 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

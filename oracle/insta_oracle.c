@@ -476,6 +476,35 @@ void orc_occupancy_from_mesh(const orc_tri *tris, int n_tris, double radius, uin
     free(mark); free(nodes); free(sorted);
 }
 
+/* update_density_grid_mean_and_bitfield (ngp/src/testbed_nerf.cu:2863-2878): the mean over
+ * cascade 0 of max(v, 0) / 128^3 (terms in float, summed in double), grid_to_bitfield (:585-609)
+ * with threshold min(0.01, mean) over the n_cascades given cascades (the bytes of the others are
+ * 0), then bitfield_max_pool (:611-632), which ORs each pooled mip into the next mip's own bits.
+ * grid: n_cascades * 128^3 floats, Morton order per cascade.  Returns the threshold. */
+float orc_density_grid_to_bitfield(const float *grid, uint32_t n_cascades, uint8_t *bitfield) {
+    double sum = 0.0;
+    for (uint32_t i = 0; i < GRID3; ++i) sum += (double)(fmaxf(grid[i], 0.f) / (float)GRID3);
+    const float mean = (float)sum;
+    const float thresh = mean < 0.01f ? mean : 0.01f;
+    for (uint32_t b = 0; b < GRID3 / 8 * 8; ++b) {
+        uint8_t bits = 0;
+        if (b < GRID3 / 8 * n_cascades)
+            for (int j = 0; j < 8; ++j) bits |= grid[(size_t)b * 8 + j] > thresh ? (uint8_t)(1u << j) : 0;
+        bitfield[b] = bits;
+    }
+    for (uint32_t level = 1; level < 8; ++level) {
+        const uint8_t *prev = bitfield + (size_t)(level - 1) * GRID3 / 8;
+        uint8_t *next = bitfield + (size_t)level * GRID3 / 8;
+        for (uint32_t i = 0; i < GRID3 / 64; ++i) {
+            uint8_t bits = 0;
+            for (int j = 0; j < 8; ++j) bits |= prev[i * 8 + j] > 0 ? (uint8_t)(1u << j) : 0;
+            uint32_t x = morton_invert(i >> 0) + GRID / 8, y = morton_invert(i >> 1) + GRID / 8, z = morton_invert(i >> 2) + GRID / 8;
+            next[orc_morton3d(x, y, z)] |= bits;
+        }
+    }
+    return thresh;
+}
+
 /* ------------------------------------------------- low-discrepancy jitter */
 /* Sobol direction numbers for dimensions 0 and 1 (van der Corput and the x+1 primitive
  * polynomial), generated by the standard recurrence (NGP/random_val.cuh:159-216 uses the
@@ -671,6 +700,67 @@ int orc_march_ray(const orc_render_cfg *rc, const uint8_t *bf, int px, int py, i
         ++n;
     }
     return n;
+}
+
+/* generate_training_samples_nerf (ngp/src/testbed_nerf.cu:1105-1285) on caller-supplied rays:
+ * rays [n][6] (origin, unnormalised direction), image[n] (written to `holder`), start_rand[n]
+ * (the uniform draw of the start jitter), extra [n_images][n_extra] or NULL.  Rays are taken in
+ * index order, so each ray's block of samples follows the previous one (the device reserves
+ * blocks with atomics in arbitrary order; compare per ray).  counters: [0] rays kept,
+ * [1] samples requested (as the reference's numsteps counter). */
+void orc_training_samples(const float *aabb_min, const float *aabb_max, float cone, const uint8_t *bf, const float *rays,
+                          const uint32_t *image, const float *start_rand, const float *extra, uint32_t n_extra, int64_t n,
+                          uint32_t max_samples, float *coords, uint32_t stride, uint32_t *ray_indices, uint32_t *numsteps,
+                          uint32_t *counters) {
+    counters[0] = counters[1] = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const float *r = rays + i * 6;
+        float o[3] = {r[0], r[1], r[2]}, d[3] = {r[3], r[4], r[5]};
+        float z = v3dot(d, d);
+        if (z > 0.f) { float sq = sqrtf(z); d[0] /= sq; d[1] /= sq; d[2] /= sq; }
+        float idir[3] = {1.0f / d[0], 1.0f / d[1], 1.0f / d[2]};
+        float startt = fmaxf(aabb_ray_tmin(aabb_min, aabb_max, o, d), 0.0f);
+        startt += calc_dt(startt, cone) * start_rand[i];
+        uint32_t j = 0;
+        float t = startt, pos[3];
+        for (int guard = 0; guard < (1 << 16) && j < 1024u; ++guard) {
+            for (int k = 0; k < 3; ++k) pos[k] = o[k] + d[k] * t;
+            if (!box_contains(aabb_min, aabb_max, pos)) break;
+            float dt = calc_dt(t, cone);
+            int mip = mip_from_dt(dt, pos);
+            if (occupied_at(pos, bf, mip)) { ++j; t += dt; }
+            else t = advance_to_next_voxel(t, cone, pos, d, idir, GRID >> mip);
+        }
+        if (j == 0) continue;
+        uint32_t base = counters[1];
+        counters[1] += j;
+        if (base + j > max_samples) continue;
+        uint32_t ri = counters[0]++;
+        ray_indices[ri] = (uint32_t)i;
+        numsteps[2 * ri] = j;
+        numsteps[2 * ri + 1] = base;
+        float wd[3];
+        for (int k = 0; k < 3; ++k) wd[k] = (d[k] + 1.0f) * 0.5f;
+        t = startt;
+        uint32_t w = 0;
+        for (int guard = 0; guard < (1 << 16) && w < j; ++guard) {
+            for (int k = 0; k < 3; ++k) pos[k] = o[k] + d[k] * t;
+            if (!box_contains(aabb_min, aabb_max, pos)) break;
+            float dt = calc_dt(t, cone);
+            int mip = mip_from_dt(dt, pos);
+            if (occupied_at(pos, bf, mip)) {
+                float *c = coords + (size_t)(base + w) * stride;
+                for (int k = 0; k < 3; ++k) { c[k] = (pos[k] - aabb_min[k]) / (aabb_max[k] - aabb_min[k]); c[5 + k] = c[k]; c[8 + k] = wd[k]; }
+                c[3] = warp_dt(dt);
+                c[4] = (float)image[i];
+                for (uint32_t m = 0; m < n_extra; ++m) c[stride - n_extra + m] = extra ? extra[(size_t)image[i] * n_extra + m] : 0.f;
+                ++w;
+                t += dt;
+            } else {
+                t = advance_to_next_voxel(t, cone, pos, d, idir, GRID >> mip);
+            }
+        }
+    }
 }
 
 static float srgb_to_linear(float s) { return s <= 0.04045f ? s / 12.92f : powf((s + 0.055f) / 1.055f, 2.4f); }

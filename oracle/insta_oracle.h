@@ -76,6 +76,7 @@ void orc_canonical_map_coords(const orc_deform *d, float *coords, uint32_t strid
 
 /* ---- occupancy --------------------------------------------------------- */
 void orc_occupancy_from_mesh(const orc_tri *tris, int n_tris, double radius, uint8_t *bitfield);
+float orc_density_grid_to_bitfield(const float *grid, uint32_t n_cascades, uint8_t *bitfield);
 uint32_t orc_morton3d(uint32_t x, uint32_t y, uint32_t z);
 
 /* ---- field (hash grid + SH + MLPs) ------------------------------------ */
@@ -121,6 +122,10 @@ int64_t orc_render(const orc_render_cfg *rc, const orc_deform *d, const uint8_t 
                    uint32_t *out_nsamples, int fp64);
 int orc_march_ray(const orc_render_cfg *rc, const uint8_t *bitfield, int px, int py,
                   int max_out, float *out_t, float *out_dt, float *out_pos);
+void orc_training_samples(const float *aabb_min, const float *aabb_max, float cone, const uint8_t *bf, const float *rays,
+                          const uint32_t *image, const float *start_rand, const float *extra, uint32_t n_extra, int64_t n,
+                          uint32_t max_samples, float *coords, uint32_t stride, uint32_t *ray_indices, uint32_t *numsteps,
+                          uint32_t *counters);
 
 /* ---- low-discrepancy helpers (NGP/random_val.cuh:159-322) -------------- */
 float orc_ld_random_val(uint32_t index, uint32_t seed, uint32_t dim);

@@ -195,6 +195,16 @@ def occupancy(tris, radius=0.015) -> np.ndarray:
     return bits
 
 
+def density_grid_to_bitfield(grid, n_cascades):
+    """Bitfield (8 mips x 128^3 bits) and threshold from a float density grid [n_cascades, 128^3]."""
+    g = np.ascontiguousarray(grid, dtype=np.float32).reshape(-1)
+    bits = np.zeros(8 * 128 ** 3 // 8, np.uint8)
+    f = lib().orc_density_grid_to_bitfield
+    f.restype = C.c_float
+    t = f(ptr(g), C.c_uint32(n_cascades), ptr(bits))
+    return bits, float(t)
+
+
 def render_cfg(width, height, focal, cam, render_box, train_box=((0, 0, 0), (1, 1, 1)), cone_angle=1 / 256, spp=0,
                min_transmittance=0.01, max_samples=1024, frame_id=0, snap=True, linear_colors=False) -> RenderCfg:
     r = RenderCfg()
@@ -241,6 +251,28 @@ def march_ray(rc: RenderCfg, bits, px, py, max_out=1024):
     pos = np.zeros((max_out, 3), dtype=np.float32)
     n = lib().orc_march_ray(C.byref(rc), ptr(bits), C.c_int(px), C.c_int(py), C.c_int(max_out), ptr(t), ptr(dt), ptr(pos))
     return t[:n], dt[:n], pos[:n]
+
+
+def training_samples(bits, rays, image, start_rand, max_samples, train_box=((0, 0, 0), (1, 1, 1)), cone_angle=1 / 256,
+                     extra=None, n_extra=0):
+    """generate_training_samples_nerf on given rays: (coords [max_samples, 11 + n_extra], ray_indices,
+    numsteps [n, 2], counters [2])."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    n = len(rays)
+    image = np.ascontiguousarray(image, np.uint32)
+    rnd = np.ascontiguousarray(start_rand, np.float32)
+    stride = 11 + n_extra
+    coords = np.zeros((max_samples, stride), np.float32)
+    ri = np.zeros(n, np.uint32)
+    ns = np.zeros((n, 2), np.uint32)
+    cnt = np.zeros(2, np.uint32)
+    mn = np.asarray(train_box[0], np.float32)
+    mx = np.asarray(train_box[1], np.float32)
+    ex = None if extra is None else np.ascontiguousarray(extra, np.float32)
+    lib().orc_training_samples(ptr(mn), ptr(mx), C.c_float(cone_angle), ptr(bits), ptr(rays), ptr(image), ptr(rnd),
+                               ptr(ex) if ex is not None else None, C.c_uint32(n_extra), C.c_int64(n),
+                               C.c_uint32(max_samples), ptr(coords), C.c_uint32(stride), ptr(ri), ptr(ns), ptr(cnt))
+    return coords, ri, ns, cnt
 
 
 def ld_random_val(index, seed, dim=0) -> float:

@@ -117,12 +117,94 @@ def test_canonical_map_empty_is_noop(gpu_avatar):
     gpu_avatar.sync()
 
 
+def test_training_samples(gpu_avatar, oracle, oracle_frame, avatar):
+    """generate_training_samples_nerf + warp with per-record frames: per kept ray, the same number
+    of samples, bit-exact march outputs (dt, holder, deformed position), canonical positions within
+    1e-5 x the bbox diagonal of the oracle's map of the record's frame."""
+    gpu_avatar.occupancy_from_mesh(0, 0, 0.015)
+    bits = oracle.occupancy(oracle_frame["def"], 0.015)
+    rng = np.random.default_rng(21)
+    n = 3000
+    c0 = np.array([0.5, 0.5, 0.5], np.float32)
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    org = c0 + u * 0.9
+    tgt = c0 + rng.normal(0, 0.06, (n, 3))
+    du = (tgt - org) * rng.uniform(0.5, 2.0, (n, 1))
+    rays = np.concatenate([org, du], 1).astype(np.float32)
+    image = rng.integers(0, 2, n).astype(np.uint32)
+    rnd = rng.random(n).astype(np.float32)
+    max_samples = 1 << 19
+    coords = torch.zeros((max_samples, 11), device="cuda")
+    ri = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ns = torch.zeros((n, 2), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(2, dtype=torch.int32, device="cuda")
+    gpu_avatar.training_samples(0, 0, dev(rays), dev(image.view(np.int32)), dev(rnd), max_samples, coords, 11, ri, ns, cnt)
+    gpu_avatar.sync()
+    c_ref, ri_ref, ns_ref, cnt_ref = oracle.training_samples(bits, rays, image, rnd, max_samples)
+    cnt = cnt.cpu().numpy().view(np.uint32)
+    assert (cnt == cnt_ref).all() and cnt[0] > 1000 and cnt[1] < max_samples
+    # the oracle's records mapped with the frame each one names
+    frames = {0: oracle_frame}
+    f1 = avatar.frame(avatar.frame_coeffs(1))
+    d1 = oracle.build_triangles(f1, avatar.canonical, avatar.faces, avatar.mask)
+    frames[1] = {"def": d1, "can": oracle_frame["can"], "adj": oracle_frame["adj"], "bvh": oracle.Bvh(d1)}
+    n_ref = int(cnt_ref[1])
+    mapped = c_ref[:n_ref].copy()
+    for h, fr in frames.items():
+        rows = mapped[:, 4] == h
+        d = oracle.Deformation(fr["def"], fr["can"], fr["adj"], fr["bvh"])
+        mapped[rows] = d.map_coords(mapped[rows], frame_id=-1, n_frames=2)
+    got = coords.cpu().numpy()
+    ri, ns = ri.cpu().numpy(), ns.cpu().numpy()
+    where = {int(i): k for k, i in enumerate(ri_ref[:cnt_ref[0]])}
+    tol = 1e-5 * diag(avatar)
+    err = 0.0
+    for k in range(int(cnt[0])):
+        i, m, b = int(ri[k]), int(ns[k, 0]), int(ns[k, 1])
+        kr = where[i]
+        assert m == int(ns_ref[kr, 0])
+        br = int(ns_ref[kr, 1])
+        g, r = got[b:b + m], mapped[br:br + m]
+        assert (g[:, 3:8] == c_ref[br:br + m, 3:8]).all()
+        err = max(err, float(np.abs(g[:, 0:3] - r[:, 0:3]).max()), float(np.abs(g[:, 8:11] - r[:, 8:11]).max()))
+    assert err <= tol
+
+
 def test_occupancy_bit_exact(gpu_avatar, oracle, oracle_frame):
     gpu_avatar.occupancy_from_mesh(0, 0, 0.015)
     got = gpu_avatar.occupancy_get(0, 0)
     ref = oracle.occupancy(oracle_frame["def"], 0.015)
     assert got.sum() > 0
     assert (got == ref).all()
+
+
+@pytest.mark.parametrize("scale,fp16", [(0.05, False), (0.05, True), (0.004, False)])
+def test_density_grid_bitfield(gpu_avatar, oracle, scale, fp16):
+    """Snapshot density grid -> bitfield (grid_to_bitfield + max-pool), two cascades.  With the
+    mean above 0.01 the threshold is exactly 0.01 and the bits are exact; below it the threshold
+    is the mean, whose last bits depend on the summation order: cells within 1e-5 of it are
+    excluded."""
+    rng = np.random.default_rng(11)
+    grid = rng.exponential(scale, size=2 * 128 ** 3).astype(np.float32)
+    grid[rng.random(grid.size) < 0.3] *= -1.0   # negative densities count as 0 in the mean
+    if fp16:
+        grid = grid.astype(np.float16)
+    gpu_avatar.density_grid_load(0, 1, grid, 2)
+    got = gpu_avatar.occupancy_get(0, 1)
+    ref, thresh = oracle.density_grid_to_bitfield(grid.astype(np.float32), 2)
+    if scale > 0.02:
+        assert thresh == np.float32(0.01)
+        assert (got == ref).all()
+    else:
+        assert thresh < 0.01
+        g32 = grid.astype(np.float32)
+        near = np.abs(g32[:128 ** 3] - thresh) <= 1e-5 * thresh
+        mip0_got = np.unpackbits(got[:128 ** 3 // 8], bitorder="little").astype(bool)
+        mip0_ref = np.unpackbits(ref[:128 ** 3 // 8], bitorder="little").astype(bool)
+        assert (mip0_got[~near] == mip0_ref[~near]).all()
+        assert mip0_ref.sum() > 1000
+    gpu_avatar.occupancy_from_mesh(0, 1, 0.015)
 
 
 def test_march_samples_bit_exact(gpu_avatar, oracle, oracle_frame, avatar):
