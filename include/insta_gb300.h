@@ -216,6 +216,46 @@ int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples);
 int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out, float* out_t, float* out_dt,
                       int32_t* out_n);
 
+/* -- serving ------------------------------------------------------------------- */
+/* A request loop on a worker thread that owns the context from insta_server_create to
+ * insta_server_destroy (load avatars -- canonical mesh, parameters -- before creating it; make no
+ * other call on the context meanwhile).  Each request renders one view of one avatar, with its
+ * own tracked-mesh frame (frame_verts, host f32[n_verts*3], copied at submit; NULL renders the
+ * already uploaded desc->frame).  Requests are admitted into request slots while slots, the
+ * pixel budget and the context's memory budget allow; the rays of admitted requests join the
+ * running wavefront at the next round, so requests that arrive while others are on the GPU run
+ * together with them (continuous batching), and a slot frees as soon as its last ray has
+ * composited.  Each request's pixels equal those of insta_render alone.  Frame ids >= 2^30 are
+ * the server's.  No reference counterpart: the reference renders one view per render_nerf call. */
+#define INSTA_REQ_QUEUED 0
+#define INSTA_REQ_RUNNING 1
+#define INSTA_REQ_DONE 2
+#define INSTA_REQ_CANCELLED 3
+#define INSTA_REQ_FAILED 4
+
+typedef struct insta_server insta_server;
+typedef struct {
+    uint32_t max_inflight;          /* request slots (1..256) */
+    uint64_t max_inflight_pixels;   /* pixels of admitted requests (<= 2^26) */
+    double occupancy_radius;        /* request frames: occupancy from the mesh (0.015) */
+} insta_server_config;
+
+int insta_server_create(insta_ctx* ctx, const insta_server_config* cfg, insta_server** out);
+/* Cancels queued requests, lets running ones finish, joins the worker. */
+int insta_server_destroy(insta_server* s);
+/* out_rgba / out_depth as for insta_render (host: filled when the request is done). */
+int insta_submit(insta_server* s, const insta_render_desc* req, const float* frame_verts, float* out_rgba, float* out_depth,
+                 uint64_t* ticket);
+/* state: INSTA_REQ_*; latency_ms (optional): submit -> done, -1 while not done. */
+int insta_poll(insta_server* s, uint64_t ticket, int* state, double* latency_ms);
+/* Blocks until the request is done, cancelled or failed (timeout_ms < 0: no limit). */
+int insta_wait(insta_server* s, uint64_t ticket, int timeout_ms, int* state);
+/* Queued: dropped before admission.  Running: finishes, its outputs are not delivered. */
+int insta_cancel(insta_server* s, uint64_t ticket);
+/* Forget a finished ticket. */
+int insta_server_release(insta_server* s, uint64_t ticket);
+const char* insta_server_error(insta_server* s, uint64_t ticket);
+
 #ifdef __cplusplus
 }
 #endif

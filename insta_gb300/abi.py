@@ -25,7 +25,15 @@ EXPORTS = [
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
     "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_batch",
     "insta_render_samples", "insta_march_debug",
+    "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
+    "insta_server_release", "insta_server_error",
 ]
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("max_inflight", C.c_uint32), ("max_inflight_pixels", C.c_uint64), ("occupancy_radius", C.c_double)]
 
 
 class InstaError(RuntimeError):
@@ -98,6 +106,14 @@ def load(path: Path | None = None):
             "insta_render_batch": [vp, C.POINTER(RenderDesc), C.c_int, C.POINTER(vp), C.POINTER(vp)],
             "insta_render_samples": [vp, C.POINTER(u64)],
             "insta_march_debug": [vp, C.POINTER(RenderDesc), C.c_int, vp, vp, vp],
+            "insta_server_create": [vp, C.POINTER(ServerConfig), C.POINTER(vp)],
+            "insta_server_destroy": [vp],
+            "insta_submit": [vp, C.POINTER(RenderDesc), vp, vp, vp, C.POINTER(u64)],
+            "insta_poll": [vp, u64, C.POINTER(C.c_int), C.POINTER(C.c_double)],
+            "insta_wait": [vp, u64, C.c_int, C.POINTER(C.c_int)],
+            "insta_cancel": [vp, u64],
+            "insta_server_release": [vp, u64],
+            "insta_server_error": [vp, u64],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)
@@ -105,6 +121,7 @@ def load(path: Path | None = None):
             fn.restype = C.c_int
         lib.insta_last_error.argtypes = [vp]
         lib.insta_last_error.restype = C.c_char_p
+        lib.insta_server_error.restype = C.c_char_p
         _lib = lib
     return _lib
 
@@ -291,3 +308,54 @@ class Context:
 
     def march_debug(self, req: RenderDesc, max_out, out_t, out_dt, out_n):
         self._check(self.lib.insta_march_debug(self.h, C.byref(req), max_out, _addr(out_t), _addr(out_dt), _addr(out_n)))
+
+
+class Server:
+    """The request loop (insta_server_*): owns `ctx` from creation to close()."""
+
+    def __init__(self, ctx: Context, max_inflight=16, max_inflight_pixels=1 << 22, occupancy_radius=0.015):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        cfg = ServerConfig(max_inflight, max_inflight_pixels, occupancy_radius)
+        h = C.c_void_p()
+        ctx._check(self.lib.insta_server_create(ctx.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, req: RenderDesc, frame_verts, out_rgba, out_depth) -> int:
+        v = None if frame_verts is None else np.ascontiguousarray(frame_verts, dtype=np.float32)
+        t = C.c_uint64(0)
+        rc = self.lib.insta_submit(self.h, C.byref(req), _addr(v), _addr(out_rgba), _addr(out_depth), C.byref(t))
+        if rc:
+            raise InstaError(rc, "insta_submit failed")
+        self._keep[t.value] = (out_rgba, out_depth)   # outputs stay alive until the ticket is released
+        return t.value
+
+    def poll(self, ticket):
+        st, lat = C.c_int(0), C.c_double(0)
+        rc = self.lib.insta_poll(self.h, ticket, C.byref(st), C.byref(lat))
+        if rc:
+            raise InstaError(rc, "insta_poll failed")
+        return st.value, lat.value
+
+    def wait(self, ticket, timeout_ms=-1) -> int:
+        st = C.c_int(0)
+        rc = self.lib.insta_wait(self.h, ticket, timeout_ms, C.byref(st))
+        if rc:
+            raise InstaError(rc, "insta_wait failed")
+        return st.value
+
+    def cancel(self, ticket):
+        self.lib.insta_cancel(self.h, ticket)
+
+    def error(self, ticket) -> str:
+        return self.lib.insta_server_error(self.h, ticket).decode()
+
+    def release(self, ticket):
+        self.lib.insta_server_release(self.h, ticket)
+        self._keep.pop(ticket, None)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.insta_server_destroy(self.h)
+            self.h = None

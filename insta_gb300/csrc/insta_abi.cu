@@ -1,7 +1,13 @@
 // insta_abi.cu -- host side of the C ABI: device residency of avatars (canonical mesh,
 // per-frame BVHs, occupancy bitfields, field parameters), argument checking and launches.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -66,7 +72,7 @@ struct Field {
 // Device scratch of the render wavefront, sized for the largest request seen.
 struct Wave {
     DevBuf rays[2][4], n_round, sample_index, sample_ray, sample_key, sample_order, sort_bins, samples, tiles, aux, out, out_f32,
-        counters, req_table, req_meta;
+        counters, req_table, req_meta, init_meta;
     uint32_t cap_rays = 0;
     uint64_t cap_samples = 0;
 };
@@ -98,6 +104,8 @@ struct insta_ctx {
     DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs, density_scratch, density_stage;
     Wave wave;
     uint32_t* host_counters = nullptr;   // pinned: alive-ray counts read between rounds
+    uint32_t* host_alive = nullptr;      // pinned: alive rays per request slot (serving)
+    uint32_t host_alive_n = 0;
     int sms = 0;
     // statistics: kernel launches issued by the library, optional per-stage CUDA-event timing
     uint64_t launches = 0;
@@ -379,17 +387,180 @@ bool same_field_layout(const Field& a, const Field& b) {
            std::memcmp(a.view.level_dense, b.view.level_dense, sizeof(a.view.level_dense)) == 0;
 }
 
+// A request's slot view: camera, frame, avatar state and output buffers (set by the caller).
+ReqView request_view(insta_ctx* ctx, const insta_render_desc& r, Avatar& a, Frame& f) {
+    ReqView v{};
+    v.rv = render_view(a, r);
+    v.fr = f.view;
+    v.dv = deform_view(a);
+    v.table = a.field.view.table;
+    v.mlp = a.field.view.mlp_smem;
+    v.bitfield = (const uint8_t*)f.bitfield.p;
+    v.tiles_x = ((uint32_t)r.width + 7) / 8;
+    v.tiles = v.tiles_x * (((uint32_t)r.height + 3) / 4);
+    return v;
+}
+
+// The render wavefront over a table of request slots (NerfTracer::trace for many views at once,
+// ngp/src/testbed_nerf.cu:2112-2244): rays of any slots can be started between rounds; each
+// round marches all alive rays, sorts their samples by (slot, cell), runs deform + encode, the
+// MLP tiles and the composite.  The host reads the alive count after each round, as trace does
+// (:2164-2165).
+struct WaveRun {
+    insta_ctx* ctx = nullptr;
+    uint32_t n_slots = 0;
+    uint64_t round_cap = 0, cap_samples = 0;
+    WaveArgs W{};
+    MlpArgs M{};
+    int cur = 0;
+    uint32_t n_alive = 0;
+    uint32_t* counters = nullptr;
+
+    RayBuf rays(int b) {
+        Wave& w = ctx->wave;
+        return RayBuf{(float4*)w.rays[b][0].p, (float4*)w.rays[b][1].p, (float4*)w.rays[b][2].p, (float4*)w.rays[b][3].p};
+    }
+
+    // Scratch for up to max_rays alive rays over n_slots slots sharing `field`'s layout.
+    void setup(insta_ctx* c, const Field& field, uint32_t slots, uint64_t max_rays, bool per_request_counts) {
+        ctx = c;
+        n_slots = slots;
+        const FieldView& fv = field.view;
+        const TilePlan& P = field.plan;
+        Wave& w = ctx->wave;
+        round_cap = std::min<uint64_t>(max_rays * kMaxSteps, kMaxRoundSamples);
+        cap_samples = (round_cap + (uint64_t)slots * 128 + 127) / 128 * 128;
+        const uint32_t cell_bits = sort_cell_bits(slots);
+        const uint64_t n_bins = (uint64_t)slots << cell_bits;
+        if (w.cap_rays < max_rays) {
+            for (int b = 0; b < 2; ++b)
+                for (int k = 0; k < 4; ++k) ctx->alloc(w.rays[b][k], (size_t)max_rays * 16);
+            ctx->alloc(w.n_round, (size_t)max_rays * 4);
+            w.cap_rays = (uint32_t)max_rays;
+        }
+        ctx->alloc(w.tiles, cap_samples / 128 * P.tile_bytes);
+        ctx->alloc(w.aux, cap_samples * sizeof(float2));
+        ctx->alloc(w.samples, cap_samples * sizeof(float4));
+        ctx->alloc(w.sample_ray, cap_samples * sizeof(uint32_t));
+        ctx->alloc(w.sample_index, cap_samples * sizeof(uint32_t));
+        ctx->alloc(w.sample_key, cap_samples * sizeof(uint32_t));
+        ctx->alloc(w.sample_order, cap_samples * sizeof(uint32_t));
+        ctx->alloc(w.sort_bins, (n_bins + n_bins / kSortBlock) * sizeof(uint32_t));
+        ctx->alloc(w.out, cap_samples * sizeof(uint2));
+        if (fv.precision == 1) ctx->alloc(w.out_f32, cap_samples * sizeof(float4));
+        ctx->alloc(w.counters, 64);
+        ctx->alloc(w.req_table, (size_t)slots * sizeof(ReqView));
+        ctx->alloc(w.req_meta, (size_t)(slots + 1) * 2 * sizeof(uint32_t) + (size_t)slots * sizeof(uint32_t));
+        ctx->alloc(w.init_meta, (size_t)(2 * slots + 1) * sizeof(uint32_t));
+        if (!ctx->host_counters) CK(cudaMallocHost(&ctx->host_counters, 64));
+        if (!ctx->host_alive || ctx->host_alive_n < slots) {
+            if (ctx->host_alive) cudaFreeHost(ctx->host_alive);
+            CK(cudaMallocHost(&ctx->host_alive, (size_t)slots * sizeof(uint32_t)));
+            ctx->host_alive_n = slots;
+        }
+        counters = (uint32_t*)w.counters.p;   // [0], [1]: ping-pong alive counts; [2]: round samples; [3]: padded
+        W = WaveArgs{};
+        W.reqs = (const ReqView*)w.req_table.p;
+        W.n_reqs = slots;
+        W.cell_bits = cell_bits;
+        W.fv = fv;
+        W.tiles = (uint8_t*)w.tiles.p;
+        W.tile_bytes = P.tile_bytes;
+        W.k_in = P.k_in;
+        W.aux = (float2*)w.aux.p;
+        W.samples = (float4*)w.samples.p;
+        W.sample_ray = (uint32_t*)w.sample_ray.p;
+        W.sample_index = (uint32_t*)w.sample_index.p;
+        W.sample_key = (uint32_t*)w.sample_key.p;
+        W.sample_order = (uint32_t*)w.sample_order.p;
+        W.sort_bins = (uint32_t*)w.sort_bins.p;
+        W.sort_block_sums = W.sort_bins + n_bins;
+        W.req_start = (uint32_t*)w.req_meta.p;
+        W.req_seg = W.req_start + (slots + 1);
+        W.req_alive = per_request_counts ? W.req_seg + (slots + 1) : nullptr;
+        W.init_tile = (const uint32_t*)w.init_meta.p;
+        W.init_slot = W.init_tile + (slots + 1);
+        W.n_samples_round = counters + 2;
+        W.n_samples_padded = counters + 3;
+        W.out = (const uint2*)w.out.p;
+        W.out_f32 = (const float4*)w.out_f32.p;
+        W.n_round = (uint32_t*)w.n_round.p;
+        W.sample_counter = ctx->sample_counter;
+        W.err = ctx->err_dev;
+        M = MlpArgs{};
+        M.fv = fv; M.plan = P; M.tiles = W.tiles;
+        M.out = (uint2*)w.out.p; M.out_f32 = (float4*)w.out_f32.p; M.err = ctx->err_dev;
+        M.n_alive = W.n_samples_padded;
+        M.seg = W.req_seg; M.reqs = W.reqs; M.n_reqs = slots;
+        cur = 0;
+        n_alive = 0;
+        CK(cudaMemsetAsync(ctx->sample_counter, 0, sizeof(unsigned long long), ctx->stream));
+        CK(cudaMemsetAsync(counters, 0, 8, ctx->stream));
+        if (W.req_alive) CK(cudaMemsetAsync(W.req_alive, 0, (size_t)slots * sizeof(uint32_t), ctx->stream));
+    }
+
+    void upload_table(const ReqView* views) {
+        CK(cudaMemcpyAsync(ctx->wave.req_table.p, views, (size_t)n_slots * sizeof(ReqView), cudaMemcpyHostToDevice, ctx->stream));
+    }
+
+    // Start the rays of the given slots, appended to the current alive list.  `tiles[k]` is slot
+    // slots[k]'s tile count.  Without read_back, the new pixels bound the alive count (no host
+    // round trip).
+    void start(const uint32_t* slots, const uint32_t* tiles, uint32_t n, bool read_back) {
+        std::vector<uint32_t> meta((size_t)2 * n + 1);
+        uint32_t total = 0;
+        for (uint32_t k = 0; k < n; ++k) { meta[k] = total; total += tiles[k]; meta[n + 1 + k] = slots[k]; }
+        meta[n] = total;
+        // init_tile then init_slot, packed for this launch
+        CK(cudaMemcpyAsync(ctx->wave.init_meta.p, meta.data(), meta.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+        W.init_tile = (const uint32_t*)ctx->wave.init_meta.p;
+        W.init_slot = W.init_tile + (n + 1);
+        W.n_init = n;
+        W.rays_out = rays(cur);
+        W.n_alive_out = counters + cur;
+        { Stage st(ctx, INSTA_STAGE_RAY_INIT, 1); CK(launch_ray_init(W, total, ctx->stream)); }
+        if (read_back) n_alive = read_alive();
+        else n_alive += total * 32u;   // upper bound: every pixel alive
+    }
+
+    uint32_t read_alive() {
+        CK(cudaMemcpyAsync(ctx->host_counters, counters + cur, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        if (W.req_alive)
+            CK(cudaMemcpyAsync(ctx->host_alive, W.req_alive, (size_t)n_slots * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        return ctx->host_counters[0];
+    }
+
+    // One round over all alive rays; afterwards n_alive (and host_alive per slot) are current.
+    void round() {
+        const uint32_t steps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(kMaxSteps, round_cap / std::max(1u, n_alive)));
+        W.steps = steps;
+        W.rays_in = rays(cur);
+        W.rays_out = rays(cur ^ 1);
+        W.n_alive_in = counters + cur;
+        W.n_alive_out = counters + (cur ^ 1);
+        CK(cudaMemsetAsync(counters + (cur ^ 1), 0, 4, ctx->stream));
+        CK(cudaMemsetAsync(counters + 2, 0, 4, ctx->stream));
+        { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_march(W, ctx->stream)); }
+        { Stage st(ctx, INSTA_STAGE_SORT, 4); CK(launch_sort_samples(W, ctx->stream)); }
+        { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 1); CK(launch_deform_encode(W, ctx->stream)); }
+        { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream)); }
+        { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }
+        cur ^= 1;
+        n_alive = read_alive();
+    }
+};
+
 // Testbed::render_nerf for a batch of requests (avatars, frames, cameras, resolutions) through one
-// wavefront: every round marches all alive rays of all requests, sorts their samples by
-// (request, cell), runs deform + encode, the MLP tiles and the composite.  The host reads the
-// alive count between rounds (NerfTracer::trace does the same, testbed_nerf.cu:2164-2165).
+// wavefront; the request slots are the batch.
 void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* const* out_rgba, float* const* out_depth) {
     if (n <= 0 || (uint32_t)n > kMaxRequests) fail(INSTA_ERR_INVALID_ARG, "batch size %d outside 1..%u", n, kMaxRequests);
     std::vector<ReqView> views((size_t)n);
     const Field* field0 = nullptr;
     uint64_t total_pix = 0, host_pix = 0;
-    uint32_t total_tiles = 0, max_spr = 0;
+    uint32_t max_spr = 0;
     std::vector<int> on_host((size_t)n, 0);
+    std::vector<uint32_t> slots((size_t)n), tiles((size_t)n);
     for (int i = 0; i < n; ++i) {
         const insta_render_desc* r = reqs + i;
         check_request(r);
@@ -401,27 +572,16 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
         if (!field0) field0 = &a.field;
         else if (!same_field_layout(*field0, a.field))
             fail(INSTA_ERR_UNSUPPORTED, "requests of one batch must share the field layout (request %d differs)", i);
-        ReqView& v = views[(size_t)i];
-        v.rv = render_view(a, *r);
-        v.fr = f.view;
-        v.dv = deform_view(a);
-        v.table = a.field.view.table;
-        v.mlp = a.field.view.mlp_smem;
-        v.bitfield = (const uint8_t*)f.bitfield.p;
-        v.tiles_x = ((uint32_t)r->width + 7) / 8;
-        v.tile_first = total_tiles;
-        total_tiles += v.tiles_x * (((uint32_t)r->height + 3) / 4);
+        views[(size_t)i] = request_view(ctx, *r, a, f);
+        slots[(size_t)i] = (uint32_t)i;
+        tiles[(size_t)i] = views[(size_t)i].tiles;
         const uint64_t px = (uint64_t)r->width * r->height;
         total_pix += px;
         on_host[(size_t)i] = !(is_device_ptr(out_rgba[i]) && is_device_ptr(out_depth[i]));
         if (on_host[(size_t)i]) host_pix += px;
-        max_spr = std::max(max_spr, v.rv.max_samples_per_ray);
+        max_spr = std::max(max_spr, views[(size_t)i].rv.max_samples_per_ray);
     }
     if (total_pix > ((uint64_t)1 << 26)) fail(INSTA_ERR_INVALID_ARG, "a batch holds at most 2^26 pixels, got %llu", (unsigned long long)total_pix);
-    const FieldView& fv = field0->view;
-    const TilePlan& P = field0->plan;
-    Wave& w = ctx->wave;
-    const uint32_t nr = (uint32_t)total_pix;
     // outputs: device pointers directly, host pointers through one staging buffer
     float* stage_rgba = nullptr;
     float* stage_depth = nullptr;
@@ -430,7 +590,7 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
         stage_depth = (float*)ctx->alloc(ctx->out_depth, host_pix * 4);
     }
     // per-request expression dims (host arrays) into one device block
-    const uint32_t n_extra = fv.n_extra;
+    const uint32_t n_extra = field0->view.n_extra;
     std::vector<float> extra;
     if (n_extra) {
         extra.assign((size_t)n * n_extra, 0.f);
@@ -453,98 +613,14 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
             v.extra = n_extra ? (const float*)ctx->extra.p + (size_t)i * n_extra : nullptr;
         }
     }
-    // scratch
-    const uint64_t round_cap = std::min<uint64_t>((uint64_t)nr * kMaxSteps, kMaxRoundSamples);
-    const uint64_t cap_samples = (round_cap + (uint64_t)n * 128 + 127) / 128 * 128;
-    const uint32_t cell_bits = sort_cell_bits((uint32_t)n);
-    const uint64_t n_bins = (uint64_t)n << cell_bits;
-    if (w.cap_rays < nr) {
-        for (int b = 0; b < 2; ++b)
-            for (int k = 0; k < 4; ++k) ctx->alloc(w.rays[b][k], (size_t)nr * 16);
-        ctx->alloc(w.n_round, (size_t)nr * 4);
-        w.cap_rays = nr;
-    }
-    ctx->alloc(w.tiles, cap_samples / 128 * P.tile_bytes);
-    ctx->alloc(w.aux, cap_samples * sizeof(float2));
-    ctx->alloc(w.samples, cap_samples * sizeof(float4));
-    ctx->alloc(w.sample_ray, cap_samples * sizeof(uint32_t));
-    ctx->alloc(w.sample_index, cap_samples * sizeof(uint32_t));
-    ctx->alloc(w.sample_key, cap_samples * sizeof(uint32_t));
-    ctx->alloc(w.sample_order, cap_samples * sizeof(uint32_t));
-    ctx->alloc(w.sort_bins, (n_bins + n_bins / kSortBlock) * sizeof(uint32_t));
-    ctx->alloc(w.out, cap_samples * sizeof(uint2));
-    if (fv.precision == 1) ctx->alloc(w.out_f32, cap_samples * sizeof(float4));
-    ctx->alloc(w.counters, 64);
-    ctx->alloc(w.req_table, (size_t)n * sizeof(ReqView));
-    ctx->alloc(w.req_meta, (size_t)(n + 1) * 2 * sizeof(uint32_t));
-    if (!ctx->host_counters) CK(cudaMallocHost(&ctx->host_counters, 64));
+    WaveRun run;
+    run.setup(ctx, *field0, (uint32_t)n, total_pix, false);
     if (n_extra) CK(cudaMemcpyAsync(ctx->extra.p, extra.data(), extra.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(w.req_table.p, views.data(), (size_t)n * sizeof(ReqView), cudaMemcpyHostToDevice, ctx->stream));
-    uint32_t* counters = (uint32_t*)w.counters.p;   // [0], [1]: ping-pong alive counts; [2]: round samples; [3]: padded
-    WaveArgs W{};
-    W.reqs = (const ReqView*)w.req_table.p;
-    W.n_reqs = (uint32_t)n;
-    W.cell_bits = cell_bits;
-    W.fv = fv;
-    W.tiles = (uint8_t*)w.tiles.p;
-    W.tile_bytes = P.tile_bytes;
-    W.k_in = P.k_in;
-    W.aux = (float2*)w.aux.p;
-    W.samples = (float4*)w.samples.p;
-    W.sample_ray = (uint32_t*)w.sample_ray.p;
-    W.sample_index = (uint32_t*)w.sample_index.p;
-    W.sample_key = (uint32_t*)w.sample_key.p;
-    W.sample_order = (uint32_t*)w.sample_order.p;
-    W.sort_bins = (uint32_t*)w.sort_bins.p;
-    W.sort_block_sums = W.sort_bins + n_bins;
-    W.req_start = (uint32_t*)w.req_meta.p;
-    W.req_seg = W.req_start + (n + 1);
-    W.n_samples_round = counters + 2;
-    W.n_samples_padded = counters + 3;
-    W.out = (const uint2*)w.out.p;
-    W.out_f32 = (const float4*)w.out_f32.p;
-    W.n_round = (uint32_t*)w.n_round.p;
-    W.sample_counter = ctx->sample_counter;
-    W.err = ctx->err_dev;
-    auto rays = [&](int b) {
-        return RayBuf{(float4*)w.rays[b][0].p, (float4*)w.rays[b][1].p, (float4*)w.rays[b][2].p, (float4*)w.rays[b][3].p};
-    };
-    MlpArgs M{};
-    M.fv = fv; M.plan = P; M.tiles = W.tiles;
-    M.out = (uint2*)w.out.p; M.out_f32 = (float4*)w.out_f32.p; M.err = ctx->err_dev;
-    M.n_alive = W.n_samples_padded;
-    M.seg = W.req_seg; M.reqs = W.reqs; M.n_reqs = (uint32_t)n;
-    CK(cudaMemsetAsync(ctx->sample_counter, 0, sizeof(unsigned long long), ctx->stream));
-    CK(cudaMemsetAsync(counters, 0, 8, ctx->stream));
-    W.rays_out = rays(0);
-    W.n_alive_out = counters;
-    { Stage st(ctx, INSTA_STAGE_RAY_INIT, 1); CK(launch_ray_init(W, total_tiles, ctx->stream)); }
-    int cur = 0;
-    auto read_alive = [&](int b) {
-        CK(cudaMemcpyAsync(ctx->host_counters, counters + b, 4, cudaMemcpyDeviceToHost, ctx->stream));
-        CK(cudaStreamSynchronize(ctx->stream));
-        return ctx->host_counters[0];
-    };
+    run.upload_table(views.data());
     // the first round's step count needs the alive count only when all pixels could not take
     // kMaxSteps samples each; otherwise the pixel count stands in for it (no host round trip)
-    uint32_t n_alive = (uint64_t)nr * kMaxSteps <= round_cap ? nr : read_alive(cur);
-    for (uint32_t round = 0; n_alive > 0 && round < max_spr + 2; ++round) {
-        const uint32_t steps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(kMaxSteps, round_cap / n_alive));
-        W.steps = steps;
-        W.rays_in = rays(cur);
-        W.rays_out = rays(cur ^ 1);
-        W.n_alive_in = counters + cur;
-        W.n_alive_out = counters + (cur ^ 1);
-        CK(cudaMemsetAsync(counters + (cur ^ 1), 0, 4, ctx->stream));
-        CK(cudaMemsetAsync(counters + 2, 0, 4, ctx->stream));
-        { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_march(W, ctx->stream)); }
-        { Stage st(ctx, INSTA_STAGE_SORT, 4); CK(launch_sort_samples(W, ctx->stream)); }
-        { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 1); CK(launch_deform_encode(W, ctx->stream)); }
-        { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream)); }
-        { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }
-        cur ^= 1;
-        n_alive = read_alive(cur);
-    }
+    run.start(slots.data(), tiles.data(), (uint32_t)n, total_pix * kMaxSteps > run.round_cap);
+    for (uint32_t round = 0; run.n_alive > 0 && round < max_spr + 2; ++round) run.round();
     if (host_pix) {
         uint64_t off = 0;
         for (int i = 0; i < n; ++i) {
@@ -647,9 +723,10 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 4; ++k) ctx->release(w.rays[b][k]);
     for (DevBuf* b : {&w.n_round, &w.sample_index, &w.sample_ray, &w.sample_key, &w.sample_order, &w.sort_bins, &w.samples, &w.tiles,
-                      &w.aux, &w.out, &w.out_f32, &w.counters, &w.req_table, &w.req_meta})
+                      &w.aux, &w.out, &w.out_f32, &w.counters, &w.req_table, &w.req_meta, &w.init_meta})
         ctx->release(*b);
     if (ctx->host_counters) cudaFreeHost(ctx->host_counters);
+    if (ctx->host_alive) cudaFreeHost(ctx->host_alive);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     cudaFree(ctx->err_dev);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
@@ -785,7 +862,7 @@ int insta_occupancy_from_mesh(insta_ctx* ctx, int avatar, int frame, double radi
         Avatar& a = ctx->avatar(avatar);
         Frame& f = get_frame(a, frame);
         ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
-        Stage st(ctx, INSTA_STAGE_OCCUPANCY, 8);
+        Stage st(ctx, INSTA_STAGE_OCCUPANCY, 1);
         CK(launch_occupancy(f.view, radius, (uint8_t*)f.bitfield.p, ctx->err_dev, ctx->stream));
         f.has_occupancy = true;
     });
@@ -1072,6 +1149,346 @@ int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out,
         if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", req->frame);
         CK(launch_march_debug(render_view(a, *req), (const uint8_t*)f.bitfield.p, max_out, out_t, out_dt, out_n, ctx->stream));
     });
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------- serving
+// A request loop over one context: render requests (each with its own tracked-mesh frame) are
+// admitted into request slots as slots and the pixel budget free up, and their rays join the
+// running wavefront at the next round -- requests that arrive while others are on the GPU overlap
+// with them on the device.  A slot is released as soon as its last ray has composited.
+namespace {
+
+using Clock = std::chrono::steady_clock;
+constexpr int kServerFrameBase = 1 << 30;   // frame ids the server uses for request frames
+
+struct ServerReq {
+    uint64_t ticket = 0;
+    insta_render_desc desc{};
+    std::vector<float> extra, verts;
+    float* out_rgba = nullptr;
+    float* out_depth = nullptr;
+    bool host_out = false;
+    int state = INSTA_REQ_QUEUED;
+    int slot = -1;
+    bool cancel = false;
+    std::string error;
+    Clock::time_point t_submit, t_start, t_done;
+};
+
+}  // namespace
+
+struct insta_server {
+    insta_ctx* ctx = nullptr;
+    insta_server_config cfg{};
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<ServerReq>> queue;
+    std::unordered_map<uint64_t, std::shared_ptr<ServerReq>> tickets;
+    bool stop = false, failed = false;
+    std::string fail_msg;
+    uint64_t next_ticket = 1;
+    uint64_t completed = 0, rounds = 0;
+    // worker-owned
+    std::vector<std::shared_ptr<ServerReq>> slot_req;
+    std::vector<ReqView> views;
+    std::vector<DevBuf> slot_rgba, slot_depth;
+    DevBuf slot_extra;
+    WaveRun run;
+    const Field* layout = nullptr;
+    uint64_t inflight_px = 0;
+    int inflight = 0;
+
+    void finish(const std::shared_ptr<ServerReq>& r, int state, const std::string& err = std::string()) {
+        std::lock_guard<std::mutex> lk(mu);
+        r->state = state;
+        r->error = err;
+        r->t_done = Clock::now();
+        ++completed;
+        cv_done.notify_all();
+    }
+
+    // Upload the admitted requests' frames, build their occupancy, fill their slots and start
+    // their rays.  A request that cannot run is finished as failed without disturbing the others.
+    void admit(std::vector<std::shared_ptr<ServerReq>>& batch) {
+        std::vector<uint32_t> slots, tiles;
+        for (auto& r : batch) {
+            try {
+                Avatar& a = ctx->avatar(r->desc.avatar);
+                if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", r->desc.avatar);
+                if (!layout) {
+                    layout = &a.field;
+                    run.setup(ctx, a.field, cfg.max_inflight, cfg.max_inflight_pixels, true);
+                    CK(cudaMemsetAsync(run.W.req_alive, 0, (size_t)cfg.max_inflight * 4, ctx->stream));
+                } else if (!same_field_layout(*layout, a.field)) {
+                    fail(INSTA_ERR_UNSUPPORTED, "the server's requests must share one field layout");
+                }
+                int frame = r->desc.frame;
+                if (!r->verts.empty()) {
+                    frame = kServerFrameBase + r->slot;
+                    ctx->alloc(ctx->bvh_scratch, bvh_scratch_bytes(a.F));
+                    Frame& f = prepare_frame(ctx, a, frame, r->verts.data());
+                    { Stage st(ctx, INSTA_STAGE_FRAME, 3);
+                      CK(launch_tri_frames(a.F, (const float*)f.verts.p, (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
+                                           (const float*)a.canon_area.p, nullptr, (TriFrame*)f.frames.p, 1, ctx->stream));
+                      CK(launch_bvh_build(f.view, (const float*)f.verts.p, (const int32_t*)a.faces.p, ctx->bvh_scratch.p, ctx->stream)); }
+                    ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
+                    { Stage st(ctx, INSTA_STAGE_OCCUPANCY, 1);
+                      CK(launch_occupancy(f.view, cfg.occupancy_radius, (uint8_t*)f.bitfield.p, ctx->err_dev, ctx->stream)); }
+                    f.has_occupancy = true;
+                }
+                Frame& f = get_frame(a, frame);
+                if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", frame);
+                insta_render_desc d = r->desc;
+                d.frame = frame;
+                ReqView v = request_view(ctx, d, a, f);
+                const size_t px = (size_t)d.width * d.height;
+                const uint32_t s = (uint32_t)r->slot;
+                if (r->host_out) {
+                    v.out_rgba = (float*)ctx->alloc(slot_rgba[s], px * 16);
+                    v.out_depth = (float*)ctx->alloc(slot_depth[s], px * 4);
+                } else {
+                    v.out_rgba = r->out_rgba;
+                    v.out_depth = r->out_depth;
+                }
+                const uint32_t n_extra = layout->view.n_extra;
+                v.extra = nullptr;
+                if (n_extra) {
+                    std::vector<float> e(n_extra, 0.f);
+                    if (!r->extra.empty()) std::memcpy(e.data(), r->extra.data(), n_extra * 4);
+                    float* dst = (float*)slot_extra.p + (size_t)s * n_extra;
+                    CK(cudaMemcpyAsync(dst, e.data(), n_extra * 4, cudaMemcpyHostToDevice, ctx->stream));
+                    CK(cudaStreamSynchronize(ctx->stream));
+                    v.extra = dst;
+                }
+                views[s] = v;
+                CK(cudaMemsetAsync(run.W.req_alive + s, 0, 4, ctx->stream));
+                slots.push_back(s);
+                tiles.push_back(v.tiles);
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    r->state = INSTA_REQ_RUNNING;
+                    r->t_start = Clock::now();
+                }
+            } catch (const Failure& e) {
+                release(r);
+                finish(r, INSTA_REQ_FAILED, e.what());
+            }
+        }
+        if (slots.empty()) return;
+        run.upload_table(views.data());
+        run.start(slots.data(), tiles.data(), (uint32_t)slots.size(), false);
+    }
+
+    void release(const std::shared_ptr<ServerReq>& r) {
+        if (r->slot < 0) return;
+        slot_req[(size_t)r->slot] = nullptr;
+        inflight_px -= (uint64_t)r->desc.width * r->desc.height;
+        --inflight;
+        r->slot = -1;
+    }
+
+    // After a round: requests whose rays have all composited are done.
+    void collect() {
+        for (size_t s = 0; s < slot_req.size(); ++s) {
+            auto r = slot_req[s];
+            if (!r || r->state != INSTA_REQ_RUNNING || ctx->host_alive[s] != 0) continue;
+            if (r->host_out && !r->cancel) {
+                const size_t px = (size_t)r->desc.width * r->desc.height;
+                CK(cudaMemcpyAsync(r->out_rgba, slot_rgba[s].p, px * 16, cudaMemcpyDeviceToHost, ctx->stream));
+                CK(cudaMemcpyAsync(r->out_depth, slot_depth[s].p, px * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            }
+            CK(cudaStreamSynchronize(ctx->stream));
+            release(r);
+            finish(r, r->cancel ? INSTA_REQ_CANCELLED : INSTA_REQ_DONE);
+        }
+    }
+
+    void loop() {
+        cudaSetDevice(ctx->device);
+        try {
+            ctx->alloc(slot_extra, (size_t)cfg.max_inflight * 64 * 4);
+            for (;;) {
+                std::vector<std::shared_ptr<ServerReq>> batch;
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    cv_work.wait(lk, [&] { return stop || inflight > 0 || !queue.empty(); });
+                    if (stop && inflight == 0) break;
+                    while (!stop && !queue.empty() && inflight < (int)cfg.max_inflight) {
+                        auto r = queue.front();
+                        const uint64_t px = (uint64_t)r->desc.width * r->desc.height;
+                        if (r->cancel) {
+                            queue.pop_front();
+                            r->state = INSTA_REQ_CANCELLED;
+                            r->t_done = Clock::now();
+                            ++completed;
+                            cv_done.notify_all();
+                            continue;
+                        }
+                        if (inflight > 0 && inflight_px + px > cfg.max_inflight_pixels) break;   // wait for pixels to free up
+                        if (ctx->budget && inflight > 0 && ctx->used + px * 20 + (8u << 20) > ctx->budget) break;   // memory
+                        queue.pop_front();
+                        size_t s = 0;
+                        while (slot_req[s]) ++s;
+                        slot_req[s] = r;
+                        r->slot = (int)s;
+                        inflight_px += px;
+                        ++inflight;
+                        batch.push_back(r);
+                    }
+                }
+                if (!batch.empty()) admit(batch);
+                if (inflight == 0) continue;
+                run.round();
+                ++rounds;
+                collect();
+            }
+        } catch (const std::exception& e) {
+            std::lock_guard<std::mutex> lk(mu);
+            failed = true;
+            fail_msg = e.what();
+            for (auto& kv : tickets)
+                if (kv.second->state == INSTA_REQ_QUEUED || kv.second->state == INSTA_REQ_RUNNING) {
+                    kv.second->state = INSTA_REQ_FAILED;
+                    kv.second->error = fail_msg;
+                    kv.second->t_done = Clock::now();
+                }
+            queue.clear();
+            cv_done.notify_all();
+        }
+    }
+};
+
+extern "C" {
+
+int insta_server_create(insta_ctx* ctx, const insta_server_config* cfg, insta_server** out) {
+    return guarded(ctx, [&] {
+        if (!cfg || !out) fail(INSTA_ERR_INVALID_ARG, "null config or output");
+        if (cfg->max_inflight < 1 || cfg->max_inflight > 256) fail(INSTA_ERR_INVALID_ARG, "max_inflight must be 1..256");
+        if (cfg->max_inflight_pixels < 1 || cfg->max_inflight_pixels > ((uint64_t)1 << 26))
+            fail(INSTA_ERR_INVALID_ARG, "max_inflight_pixels must be 1..2^26");
+        if (!(cfg->occupancy_radius > 0.0)) fail(INSTA_ERR_INVALID_ARG, "occupancy_radius must be positive");
+        auto s = std::make_unique<insta_server>();
+        s->ctx = ctx;
+        s->cfg = *cfg;
+        s->slot_req.resize(cfg->max_inflight);
+        s->views.resize(cfg->max_inflight);
+        s->slot_rgba.resize(cfg->max_inflight);
+        s->slot_depth.resize(cfg->max_inflight);
+        insta_server* raw = s.get();
+        s->worker = std::thread([raw] { raw->loop(); });
+        *out = s.release();
+    });
+}
+
+int insta_server_destroy(insta_server* s) {
+    if (!s) return INSTA_ERR_INVALID_ARG;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        for (auto& r : s->queue) { r->state = INSTA_REQ_CANCELLED; r->t_done = Clock::now(); }
+        s->queue.clear();
+    }
+    s->cv_work.notify_all();
+    if (s->worker.joinable()) s->worker.join();   // in-flight requests finish first
+    for (auto& b : s->slot_rgba) s->ctx->release(b);
+    for (auto& b : s->slot_depth) s->ctx->release(b);
+    s->ctx->release(s->slot_extra);
+    delete s;
+    return INSTA_OK;
+}
+
+int insta_submit(insta_server* s, const insta_render_desc* req, const float* frame_verts, float* out_rgba, float* out_depth,
+                 uint64_t* ticket) {
+    if (!s || !req || !out_rgba || !out_depth || !ticket) return INSTA_ERR_INVALID_ARG;
+    try {
+        check_request(req);
+    } catch (const Failure& e) {
+        return e.code;
+    }
+    if ((uint64_t)req->width * req->height > s->cfg.max_inflight_pixels) return INSTA_ERR_INVALID_ARG;
+    auto r = std::make_shared<ServerReq>();
+    r->desc = *req;
+    r->desc.extra_dims = nullptr;
+    // avatars are not added or removed while the server runs, so reading them here is safe
+    auto it = s->ctx->avatars.find(req->avatar);
+    if (it == s->ctx->avatars.end()) return INSTA_ERR_NOT_READY;
+    const Avatar& a = *it->second;
+    if (req->extra_dims && a.field.ready)
+        r->extra.assign(req->extra_dims, req->extra_dims + a.field.desc.n_extra_dims);
+    if (frame_verts) r->verts.assign(frame_verts, frame_verts + (size_t)a.V * 3);
+    r->out_rgba = out_rgba;
+    r->out_depth = out_depth;
+    r->host_out = !(is_device_ptr(out_rgba) && is_device_ptr(out_depth));
+    r->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->failed || s->stop) return INSTA_ERR_DEVICE;
+        r->ticket = s->next_ticket++;
+        s->tickets[r->ticket] = r;
+        s->queue.push_back(r);
+        *ticket = r->ticket;
+    }
+    s->cv_work.notify_one();
+    return INSTA_OK;
+}
+
+int insta_poll(insta_server* s, uint64_t ticket, int* state, double* latency_ms) {
+    if (!s || !state) return INSTA_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return INSTA_ERR_INVALID_ARG;
+    *state = it->second->state;
+    if (latency_ms) {
+        const auto& r = *it->second;
+        *latency_ms = r.state >= INSTA_REQ_DONE ? std::chrono::duration<double, std::milli>(r.t_done - r.t_submit).count() : -1.0;
+    }
+    return INSTA_OK;
+}
+
+int insta_wait(insta_server* s, uint64_t ticket, int timeout_ms, int* state) {
+    if (!s || !state) return INSTA_ERR_INVALID_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return INSTA_ERR_INVALID_ARG;
+    auto r = it->second;
+    auto done = [&] { return r->state >= INSTA_REQ_DONE; };
+    if (timeout_ms < 0) s->cv_done.wait(lk, done);
+    else s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), done);
+    *state = r->state;
+    return INSTA_OK;
+}
+
+int insta_cancel(insta_server* s, uint64_t ticket) {
+    if (!s) return INSTA_ERR_INVALID_ARG;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->tickets.find(ticket);
+        if (it == s->tickets.end()) return INSTA_ERR_INVALID_ARG;
+        it->second->cancel = true;   // queued: dropped at admission; running: finishes, outputs not delivered
+    }
+    s->cv_work.notify_one();
+    return INSTA_OK;
+}
+
+int insta_server_release(insta_server* s, uint64_t ticket) {
+    if (!s) return INSTA_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return INSTA_ERR_INVALID_ARG;
+    if (it->second->state < INSTA_REQ_DONE) return INSTA_ERR_NOT_READY;
+    s->tickets.erase(it);
+    return INSTA_OK;
+}
+
+const char* insta_server_error(insta_server* s, uint64_t ticket) {
+    if (!s) return "null server";
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it != s->tickets.end() && !it->second->error.empty()) return it->second->error.c_str();
+    return s->failed ? s->fail_msg.c_str() : "";
 }
 
 }  // extern "C"

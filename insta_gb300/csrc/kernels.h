@@ -36,8 +36,8 @@ struct ReqView {
     const float* extra;         // n_extra floats on the device, or null (zeros)
     float* out_rgba;
     float* out_depth;
-    uint32_t tile_first;        // first 8x4-pixel ray tile of this request within the batch
-    uint32_t tiles_x;           // ray tiles per image row
+    uint32_t tiles_x;           // 8x4-pixel ray tiles per image row
+    uint32_t tiles;             // ray tiles of the image
 };
 
 // Samples of a round are regrouped before the deform stage by a counting sort on
@@ -57,8 +57,14 @@ inline uint32_t sort_cell_bits(uint32_t n_reqs) {
 }
 
 struct WaveArgs {
-    const ReqView* reqs;        // device table, n_reqs entries
+    const ReqView* reqs;        // device table, n_reqs entries (request slots)
     uint32_t n_reqs;
+    // ray_init: the requests whose rays start now -- slot init_slot[k] owns ray tiles
+    // [init_tile[k], init_tile[k + 1]) of this launch
+    const uint32_t* init_tile;  // [n_init + 1]
+    const uint32_t* init_slot;  // [n_init]
+    uint32_t n_init;
+    uint32_t* req_alive;        // optional [n_reqs]: alive rays per request (ray_init adds, composite subtracts)
     uint32_t cell_bits;         // sort cells per request = 2^cell_bits
     FieldView fv;               // shared field layout (table / mlp pointers unused)
     RayBuf rays_in, rays_out;

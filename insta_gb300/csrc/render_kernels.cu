@@ -44,14 +44,23 @@ __device__ __forceinline__ void write_pixel(const RenderView& rv, float* out_rgb
 // union of BVH nodes (about 40% fewer than for 32x1 pixel rows).
 constexpr uint32_t kTileW = 8, kTileH = 4;
 
-// Request of a ray tile: the last request whose first tile is <= tile (binary search).
-__device__ __forceinline__ uint32_t request_of_tile(const ReqView* reqs, uint32_t n_reqs, uint32_t tile) {
-    uint32_t lo = 0, hi = n_reqs;
+// Entry k of the launch's init list that owns ray tile `tile`: the last k with init_tile[k] <= tile.
+__device__ __forceinline__ uint32_t init_entry(const uint32_t* init_tile, uint32_t n_init, uint32_t tile) {
+    uint32_t lo = 0, hi = n_init;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&reqs[mid].tile_first) <= tile) lo = mid; else hi = mid;
+        if (__ldg(init_tile + mid) <= tile) lo = mid; else hi = mid;
     }
     return lo;
+}
+
+// Warp-aggregated add of `delta` per lane to the counter of each lane's request (lanes may belong
+// to different requests): one atomic per distinct request in the warp.
+__device__ __forceinline__ void count_per_request(uint32_t* counters, uint32_t req, bool pred, int delta) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t key = pred ? req : 0xffffffffu;
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    if (pred && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(counters + req, (uint32_t)(delta * __popc(peers)));
 }
 
 __global__ void ray_init_kernel(const __grid_constant__ WaveArgs A, uint32_t total_tiles) {
@@ -61,10 +70,11 @@ __global__ void ray_init_kernel(const __grid_constant__ WaveArgs A, uint32_t tot
     RayState r;
     uint32_t req = 0, idx = 0;
     if (tile < total_tiles) {
-        req = request_of_tile(A.reqs, A.n_reqs, tile);
+        const uint32_t k = init_entry(A.init_tile, A.n_init, tile);
+        req = A.init_slot[k];
         const ReqView& R = A.reqs[req];
         const uint32_t w = (uint32_t)R.rv.width, h = (uint32_t)R.rv.height;
-        const uint32_t lt = tile - R.tile_first;
+        const uint32_t lt = tile - A.init_tile[k];
         const uint32_t x = (lt % R.tiles_x) * kTileW + in % kTileW, y = (lt / R.tiles_x) * kTileH + in / kTileW;
         if (x < w && y < h) {
             idx = y * w + x;
@@ -73,6 +83,7 @@ __global__ void ray_init_kernel(const __grid_constant__ WaveArgs A, uint32_t tot
             alive = ray_init(R.rv, x, y, R.bitfield, r);
         }
     }
+    if (A.req_alive) count_per_request(A.req_alive, req, alive, 1);
     uint32_t slot = warp_append(A.n_alive_out, alive);
     if (alive) {
         RayBuf b = A.rays_out;
@@ -603,6 +614,7 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
                 rd.z = __uint_as_float(ns);
             }
         }
+        if (A.req_alive) count_per_request(A.req_alive, r < n_alive ? __float_as_uint(rd.w) : 0u, r < n_alive && !keep, -1);
         const uint32_t slot = warp_append(A.n_alive_out, keep);
         if (keep) {
             A.rays_out.a[slot] = ra; A.rays_out.b[slot] = rb; A.rays_out.c[slot] = rc; A.rays_out.d[slot] = rd;
