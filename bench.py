@@ -288,6 +288,141 @@ def run_ours(args, rank, world, local):
         dist.destroy_process_group()
 
 
+def run_batch64(args):
+    """Batched expressions: one avatar, 64 tracked frames (own LBVH each, one build launch), each
+    rendered at 512x512 with its own camera yaw in [-30, 30] degrees, all rays in one wavefront.
+    One step = upload of the 64 frames + their occupancy + the batched render."""
+    import torch
+    from insta_gb300 import abi, synthetic as S
+    n = args.batch
+    av = S.make_avatar(0)
+    fc = S.FieldConfig()
+    ctx = abi.Context(0)
+    ctx.canonical_set(0, av.canonical, av.faces, av.mask)
+    ctx.params_load(0, fc, S.field_params(fc, seed=0))
+    rng = np.random.default_rng(3)
+    frames = [torch.from_numpy(av.frame(av.frame_coeffs(k))).cuda() for k in range(n)]
+    yaws = rng.uniform(-30.0, 30.0, n)
+    reqs, outs = [], []
+    for k in range(n):
+        cam, focal = S.camera(float(yaws[k]), width=WIDTH, height=HEIGHT)
+        reqs.append(ctx.render_desc(0, k, WIDTH, HEIGHT, focal, cam, cone_angle=CONE))
+        outs.append((torch.empty((WIDTH * HEIGHT, 4), device="cuda"), torch.empty(WIDTH * HEIGHT, device="cuda")))
+    ids = list(range(n))
+
+    def step():
+        ctx.frame_upload_batch(0, ids, frames)
+        for k in ids:
+            ctx.occupancy_from_mesh(0, k, RADIUS)
+        ctx.render_batch(reqs, [o[0] for o in outs], [o[1] for o in outs])
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    samples = ctx.render_samples()
+    ctx.stats(reset=True)
+    ctx.stats_enable(True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    ctx.sync()
+    dt = (time.perf_counter() - t0) / args.steps
+    st = ctx.stats(reset=True)
+    # the same frames one at a time (plain path)
+    t1 = time.perf_counter()
+    for k in ids:
+        ctx.frame_upload(0, k, frames[k])
+        ctx.occupancy_from_mesh(0, k, RADIUS)
+        ctx.render(reqs[k], outs[k][0], outs[k][1])
+    ctx.sync()
+    plain = time.perf_counter() - t1
+    line = {"workload": f"batch of {n} expressions x {WIDTH}x{HEIGHT}", "samples_per_batch": samples,
+            "ms_per_batch": dt * 1e3, "frames_per_s": n / dt, "samples_per_s": samples / dt,
+            "plain_frames_per_s": n / plain, "speedup_vs_plain": plain / dt,
+            "stage_ms_per_batch": {k: v / args.steps for k, v in st["stage_ms"].items() if st["stage_calls"][k]}}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_serve(args):
+    """Served mixed stream: 8 resident avatars, Poisson arrivals, each request a fresh expression
+    (its own frame upload, LBVH, occupancy) at a resolution drawn from {256, 512, 768, 1024}^2.
+    The batched path is the request loop (continuous batching); the plain path serves the same
+    stream one request at a time (frame upload + occupancy + render), FIFO, with its latencies
+    from the measured service times and the same arrival times."""
+    from insta_gb300 import abi, synthetic as S
+    rng = np.random.default_rng(17)
+    ctx = abi.Context(0, budget_bytes=40 << 30)
+    fc = S.FieldConfig()
+    avs = []
+    for aid in range(8):
+        av = S.make_avatar(aid)
+        ctx.canonical_set(aid, av.canonical, av.faces, av.mask)
+        ctx.params_load(aid, fc, S.field_params(fc, seed=aid))
+        avs.append(av)
+    ctx.sync()
+    n = int(args.rate * args.duration)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
+    sizes = rng.choice([256, 512, 768, 1024], n)
+    reqs = []
+    for k in range(n):
+        aid = int(rng.integers(0, 8))
+        w = int(sizes[k])
+        cam, focal = S.camera(float(rng.uniform(-30, 30)), width=w, height=w)
+        coeffs = rng.normal(0.0, 0.3, avs[aid].basis.shape[0])
+        reqs.append((ctx.render_desc(aid, -1, w, w, focal, cam, cone_angle=CONE), avs[aid].frame(coeffs)))
+    pool = {w: [(np.empty((w * w, 4), np.float32), np.empty(w * w, np.float32)) for _ in range(48)] for w in (256, 512, 768, 1024)}
+    # plain path: service time of each request alone
+    service = np.zeros(n)
+    warm = reqs[0]
+    for _ in range(3):
+        ctx.frame_upload(warm[0].avatar, 0, warm[1])
+        ctx.occupancy_from_mesh(warm[0].avatar, 0, RADIUS)
+    for k, (r, v) in enumerate(reqs):
+        o = pool[r.width][k % 48]
+        t0 = time.perf_counter()
+        ctx.frame_upload(r.avatar, 0, v)
+        ctx.occupancy_from_mesh(r.avatar, 0, RADIUS)
+        r.frame = 0
+        ctx.render(r, o[0], o[1])
+        service[k] = time.perf_counter() - t0
+        r.frame = -1
+    fin = np.zeros(n)
+    prev = 0.0
+    for k in range(n):
+        prev = max(arrivals[k], prev) + service[k]
+        fin[k] = prev
+    plain_lat = (fin - arrivals) * 1e3
+    # batched path: the request loop, submissions paced to the arrival times
+    srv = abi.Server(ctx, max_inflight=args.slots, max_inflight_pixels=args.slot_pixels)
+    tickets = []
+    t_start = time.perf_counter()
+    for k, (r, v) in enumerate(reqs):
+        while time.perf_counter() - t_start < arrivals[k]:
+            time.sleep(0.0002)
+        o = pool[r.width][k % 48]
+        if k >= 48:
+            srv.wait(tickets[k - 48])   # the output buffer's previous request is done
+        tickets.append(srv.submit(r, v, o[0], o[1]))
+    states = [srv.wait(t) for t in tickets]
+    t_end = time.perf_counter()
+    lat = np.array([srv.poll(t)[1] for t in tickets])
+    srv.close()
+    ok = sum(1 for x in states if x == abi.REQ_DONE)
+    px = float(np.mean(sizes.astype(np.float64) ** 2))
+    line = {"workload": f"served stream: 8 avatars, Poisson {args.rate} req/s over {args.duration} s, "
+                        f"sizes {{256,512,768,1024}}^2 (mean {px:.0f} px), fresh expression per request",
+            "requests": n, "done": ok,
+            "batched": {"frames_per_s": ok / (t_end - t_start), "p50_ms": float(np.percentile(lat, 50)),
+                        "p99_ms": float(np.percentile(lat, 99)), "slots": args.slots, "slot_pixels": args.slot_pixels},
+            "plain": {"frames_per_s": n / float(service.sum()), "p50_ms": float(np.percentile(plain_lat, 50)),
+                      "p99_ms": float(np.percentile(plain_lat, 99)), "mean_service_ms": float(service.mean() * 1e3)},
+            "p99_512_ms_batched": float(np.percentile(lat[sizes == 512], 99)),
+            "p99_512_ms_plain": float(np.percentile(plain_lat[sizes == 512], 99))}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -296,9 +431,20 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--width", type=int, default=512, help="square render size (512 = the benchmark workload)")
+    ap.add_argument("--workload", choices=["render", "batch", "serve"], default="render",
+                    help="render: the benchmark line; batch: 64 expressions in one wavefront; serve: request stream")
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=240.0)
+    ap.add_argument("--duration", type=float, default=30.0)
+    ap.add_argument("--slots", type=int, default=16)
+    ap.add_argument("--slot-pixels", type=int, default=6 << 20)
     args = ap.parse_args()
     global WIDTH, HEIGHT
     WIDTH = HEIGHT = args.width
+    if args.workload == "batch":
+        return run_batch64(args)
+    if args.workload == "serve":
+        return run_serve(args)
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
