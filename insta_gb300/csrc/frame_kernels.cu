@@ -1,6 +1,7 @@
 // frame_kernels.cu -- per-frame tracked-mesh upload on the device: triangle frame
 // records, Morton-ordered implicit 4-ary BVH (single-CTA shared-memory sort), occupancy
 // bitfield from the mesh, and the canonical-map kernels (the `warp` hook).
+#include <algorithm>
 #include <vector>
 
 #include "device_common.cuh"
@@ -205,6 +206,81 @@ __device__ int block_scan(int* cnt, int n, int* warp_tot) {
     return total;
 }
 
+// LSD radix sort, in shared memory, of the 64-bit keys (Morton code << 32 | face id) on their
+// high word.  The keys start in id order and every pass is stable, so the result is ordered by
+// (code, id).  8 passes of 4 bits; the active threads each own ipt consecutive keys, count their
+// digits into cnt16[digit][thread], and one block-wide exclusive scan over that digit-major table
+// gives every key its destination.  While sorting, key p lives at p + p / 16 (one 8-byte pad per
+// 16 keys keeps a thread's consecutive keys off a single bank); the keys end unpadded.  Called by
+// all 1024 threads of the block; `keys` holds np2 + np2 / 16 entries.
+__device__ __forceinline__ int padded(int p) { return p + (p >> 4); }
+
+__device__ void block_radix_sort_hi(uint64_t* keys, int np2, uint16_t* cnt16, int* warp_tot) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int active = np2 < 1024 ? np2 : 1024;
+    const int ipt = np2 / active;   // 1..16
+    const bool owns = tid < active;
+    // pad: striped, so each step moves 32 consecutive keys; reads all land before the writes
+    {
+        uint64_t v[16];
+        for (int i = 0; i < ipt; ++i) v[i] = tid < active ? keys[i * active + tid] : 0ull;
+        __syncthreads();
+        for (int i = 0; i < ipt; ++i) if (tid < active) keys[padded(i * active + tid)] = v[i];
+        __syncthreads();
+    }
+    for (int shift = 32; shift < 64; shift += 4) {
+#pragma unroll
+        for (int d = 0; d < 16; ++d) cnt16[d * 1024 + tid] = 0;
+        if (owns)
+            for (int i = 0; i < ipt; ++i) ++cnt16[(int)((keys[padded(tid * ipt + i)] >> shift) & 15u) * 1024 + tid];
+        __syncthreads();
+        // exclusive scan over the 16 x 1024 table in digit-major order, 16 entries per thread
+        uint32_t loc[16], sum = 0;
+#pragma unroll
+        for (int e = 0; e < 16; ++e) { loc[e] = sum; sum += cnt16[tid * 16 + e]; }
+        uint32_t x = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[warp] = (int)x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t t = (uint32_t)warp_tot[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            warp_tot[lane] = (int)t;
+        }
+        __syncthreads();
+        const uint32_t base = (warp ? (uint32_t)warp_tot[warp - 1] : 0u) + x - sum;
+#pragma unroll
+        for (int e = 0; e < 16; ++e) cnt16[tid * 16 + e] = (uint16_t)(base + loc[e]);
+        __syncthreads();
+        uint64_t kk[16];
+        if (owns)
+            for (int i = 0; i < ipt; ++i) kk[i] = keys[padded(tid * ipt + i)];
+        __syncthreads();   // every key is in registers before any is overwritten
+        if (owns)
+            for (int i = 0; i < ipt; ++i) {
+                const int d = (int)((kk[i] >> shift) & 15u);
+                keys[padded(cnt16[d * 1024 + tid]++)] = kk[i];
+            }
+        __syncthreads();
+    }
+    // unpad (striped)
+    {
+        uint64_t v[16];
+        for (int i = 0; i < ipt; ++i) v[i] = tid < active ? keys[padded(i * active + tid)] : 0ull;
+        __syncthreads();
+        for (int i = 0; i < ipt; ++i) if (tid < active) keys[i * active + tid] = v[i];
+        __syncthreads();
+    }
+}
+
 // LBVH: sort triangles by the 30-bit Morton code of their centroid (ties by id), build the
 // binary radix tree top-down level by level and collapse every two binary levels into one
 // 4-wide node; boxes are then filled bottom-up.  Leaves hold <= INSTA_LEAF_SIZE triangles
@@ -213,7 +289,7 @@ __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs one, const
     const BvhBuildArgs a = many ? many[blockIdx.x] : one;   // a batch builds one frame per CTA
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* keys = reinterpret_cast<uint64_t*>(smem_raw);
-    int* cnt = reinterpret_cast<int*>(smem_raw + (size_t)a.np2 * 8);   // per node of the current level
+    int* cnt = reinterpret_cast<int*>(smem_raw + (size_t)(a.np2 + a.np2 / 16) * 8);   // per node of the current level
     __shared__ float red[6][32];
     __shared__ float ext[6];
     __shared__ int warp_tot[33];
@@ -263,31 +339,10 @@ __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs one, const
         keys[i] = key;
     }
     __syncthreads();
-    // 3. bitonic sort, ascending
-    for (int k = 2; k <= a.np2; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = tid; i < a.np2; i += nt) {
-                int ixj = i ^ j;
-                if (ixj > i) {
-                    uint64_t x = keys[i], y = keys[ixj];
-                    bool up = (i & k) == 0;
-                    if ((x > y) == up) { keys[i] = y; keys[ixj] = x; }
-                }
-            }
-            __syncthreads();
-        }
-    }
-    // 4. triangle records in Morton order
-    for (int s = tid; s < a.F; s += nt) {
-        // vertices and id only; tri_record_kernel fills in the rest of the record across the GPU
-        float4* dst = a.leaf_tris + (size_t)s * INSTA_TRI_F4;
-        uint32_t f = (uint32_t)(keys[s] & 0xffffffffu);
-        int i0 = a.faces[f * 3], i1 = a.faces[f * 3 + 1], i2 = a.faces[f * 3 + 2];
-        const float* A = a.verts + i0 * 3; const float* B = a.verts + i1 * 3; const float* C = a.verts + i2 * 3;
-        dst[0] = make_float4(A[0], A[1], A[2], B[0]);
-        dst[1] = make_float4(B[1], B[2], C[0], C[1]);
-        dst[2] = make_float4(C[2], __uint_as_float(f), 0.f, 0.f);
-    }
+    // 3. sort ascending (the count region doubles as the radix counters)
+    block_radix_sort_hi(keys, a.np2, reinterpret_cast<uint16_t*>(cnt), warp_tot);
+    // 4. the face of each Morton slot; tri_record_kernel builds the records across the GPU
+    for (int s = tid; s < a.F; s += nt) a.leaf_tris[(size_t)s * INSTA_TRI_F4 + 2].y = __uint_as_float((uint32_t)(keys[s] & 0xffffffffu));
     // 5. topology, top-down, one level of 4-wide nodes at a time
     if (tid == 0) {
         a.node_range[0] = make_int2(0, a.F);
@@ -349,9 +404,11 @@ __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs one, const
                     if ((uint32_t)rr[i] & INSTA_LEAF_BIT) {
                         const uint32_t first = ((uint32_t)rr[i] & ~(uint32_t)INSTA_LEAF_BIT) >> 3, count = (uint32_t)rr[i] & 7u;
                         for (uint32_t t = first; t < first + count; ++t) {
-                            const float4* tr = a.leaf_tris + (size_t)t * INSTA_TRI_F4;
-                            float4 q0 = tr[0], q1 = tr[1], q2 = tr[2];
-                            float pts[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+                            const uint32_t f = (uint32_t)(keys[t] & 0xffffffffu);
+                            const float* A = a.verts + a.faces[f * 3] * 3;
+                            const float* B = a.verts + a.faces[f * 3 + 1] * 3;
+                            const float* Cv = a.verts + a.faces[f * 3 + 2] * 3;
+                            float pts[9] = {A[0], A[1], A[2], B[0], B[1], B[2], Cv[0], Cv[1], Cv[2]};
                             for (int p = 0; p < 3; ++p) {
                                 float pb[6] = {pts[p * 3], pts[p * 3 + 1], pts[p * 3 + 2], pts[p * 3], pts[p * 3 + 1], pts[p * 3 + 2]};
                                 box_union(cb, pb);
@@ -535,16 +592,19 @@ static int sm_count_frames() {
 }
 
 // ------------------------------------------------------------------- launchers
-// Completes the Morton-ordered triangle records the build left as (vertices, id): the
-// point-independent terms of the exact distance (tri_record).  A batch passes the build arguments
-// of every frame (blockIdx.y picks one).
-__global__ void tri_record_kernel(float4* __restrict__ leaf_tris, int F, const BvhBuildArgs* __restrict__ many) {
+// The Morton-ordered triangle records from the face id the build left in each slot: vertices
+// plus the point-independent terms of the exact distance (tri_record).  A batch passes the build
+// arguments of every frame (blockIdx.y picks one).
+__global__ void tri_record_kernel(BvhBuildArgs one, const BvhBuildArgs* __restrict__ many) {
+    const BvhBuildArgs& a = many ? many[blockIdx.y] : one;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (many) leaf_tris = many[blockIdx.y].leaf_tris;
-    if (s >= F) return;
-    float4* dst = leaf_tris + (size_t)s * INSTA_TRI_F4;
-    const float4 q0 = dst[0], q1 = dst[1], q2 = dst[2];
-    tri_record(v3(q0.x, q0.y, q0.z), v3(q0.w, q1.x, q1.y), v3(q1.z, q1.w, q2.x), __float_as_uint(q2.y), dst);
+    if (s >= a.F) return;
+    float4* dst = a.leaf_tris + (size_t)s * INSTA_TRI_F4;
+    const uint32_t f = __float_as_uint(dst[2].y);
+    const float* A = a.verts + a.faces[f * 3] * 3;
+    const float* B = a.verts + a.faces[f * 3 + 1] * 3;
+    const float* C = a.verts + a.faces[f * 3 + 2] * 3;
+    tri_record(v3(A[0], A[1], A[2]), v3(B[0], B[1], B[2]), v3(C[0], C[1], C[2]), f, dst);
 }
 
 cudaError_t launch_tri_frames(int F, const float* verts, const int32_t* faces, const uint32_t* mask, const float* canon_area,
@@ -574,15 +634,18 @@ static BvhBuildArgs bvh_args(const FrameView& fv, const float* verts, const int3
 static size_t bvh_smem(int F) {
     int np2 = 2;
     while (np2 < F) np2 <<= 1;
-    return (size_t)np2 * 8 + (size_t)F * 4 + 16;
+    // keys, then the per-node counts of the topology pass, which first serve as the 16 x 1024
+    // 16-bit radix counters
+    return (size_t)(np2 + np2 / 16) * 8 + std::max((size_t)F * 4, (size_t)16 * 1024 * 2) + 16;
 }
 
 cudaError_t launch_bvh_build(const FrameView& fv, const float* verts, const int32_t* faces, void* scratch, cudaStream_t s) {
     const size_t smem = bvh_smem(fv.n_tris);
     cudaError_t e = cudaFuncSetAttribute(bvh_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    bvh_build_kernel<<<1, 1024, smem, s>>>(bvh_args(fv, verts, faces, scratch), nullptr);
-    tri_record_kernel<<<(fv.n_tris + 255) / 256, 256, 0, s>>>(const_cast<float4*>(fv.leaf_tris), fv.n_tris, nullptr);
+    const BvhBuildArgs args = bvh_args(fv, verts, faces, scratch);
+    bvh_build_kernel<<<1, 1024, smem, s>>>(args, nullptr);
+    tri_record_kernel<<<(fv.n_tris + 255) / 256, 256, 0, s>>>(args, nullptr);
     return cudaGetLastError();
 }
 
@@ -609,7 +672,7 @@ cudaError_t launch_frames_batch(int n, int F, const FrameView* views, const floa
     e = cudaFuncSetAttribute(bvh_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     bvh_build_kernel<<<n, 1024, smem, s>>>(BvhBuildArgs{}, dargs);
-    tri_record_kernel<<<dim3((F + 255) / 256, n), 256, 0, s>>>(nullptr, F, dargs);
+    tri_record_kernel<<<dim3((F + 255) / 256, n), 256, 0, s>>>(BvhBuildArgs{}, dargs);
     return cudaGetLastError();
 }
 
