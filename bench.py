@@ -35,9 +35,9 @@ WIDTH = HEIGHT = 512   # --width overrides (small cases for profiling)
 RADIUS = 0.015
 CONE = 1.0 / 256.0
 L2_FLUSH_BYTES = 512 << 20
-# DRAM bytes (read + write) of one deform_encode launch in a 512x512 frame, from an ncu capture
-# (profiles/deform_encode_render512.md); None until measured
-TRAFFIC_PER_FRAME = None
+# DRAM bytes (read + write) of deform_encode per 512x512 frame (its two launches), from an ncu
+# capture of this workload (profiles/deform_encode_render512.md)
+TRAFFIC_PER_FRAME = 416_832_512
 # Algorithmic bytes per sample of the dominant kernel (deform_encode): hash-grid gathers
 # (16 levels x 8 corners x 2 FP16 features) + sample record, ray direction and ray index in +
 # encoded operand row (32 + 16 FP16) and (dt, depth) out.
@@ -264,9 +264,10 @@ def run_ours(args, rank, world, local):
                    "global_batch": world, "samples_per_frame": mean_samples, "parallelism": f"replicas x{world}",
                    "l2": "flushed (512 MiB write) between timed steps", "frames_per_s": args.steps * world / dev_t},
         "roofline": {"bound": "hbm", "kernel": "deform_encode_kernel", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": TRAFFIC_PER_FRAME,
+                     "frac": achieved / hbm_peak, "traffic": TRAFFIC_PER_FRAME if WIDTH == 512 else None,
                      "basis": f"{DEFORM_ENCODE_BYTES_PER_SAMPLE} B per sample (512 B hash gathers + stream in/out) "
-                              f"x samples per frame / deform_encode stage time per frame (CUDA events)",
+                              f"x samples per frame / deform_encode stage time per frame (CUDA events); per frame = "
+                              f"its 2 launches, for achieved and traffic alike",
                      "peak_source": "MEASURED_PEAKS.json (of measured)" if peaks else "fallback"},
         "roofline_tensor": {"kernel": "mlp_kernel", "achieved": mean_samples * MLP_FLOP_PER_SAMPLE / mlp_s / 1e12,
                             "peak": tflops_peak, "unit": "TFLOP/s",
