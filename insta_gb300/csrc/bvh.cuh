@@ -89,37 +89,80 @@ __device__ __forceinline__ Nearest nearest_bvh(const FrameView& fr, V3 p, float 
     return {bid, bslot, best};
 }
 
+static_assert(INSTA_LEAF_SIZE <= 2, "nearest_warp queues at most 2 x 32 tests per leaf (96-entry queue)");
+
+// Per-warp shared scratch of nearest_warp.
+struct WarpScratch {
+    uint32_t stack[INSTA_STACK];   // node references of the shared traversal stack
+    uint32_t queue[96];            // pending exact tests: Morton slot << 5 | owner lane
+    unsigned long long best[32];   // per lane: (distance bits << 32) | triangle id, the running minimum
+};
+
+// Run the first n queued exact tests, one per lane: lane t tests entry t against its owner's
+// point and folds (distance, id) into the owner's running minimum; the rest of the queue moves to
+// the front.  Returns the refreshed (best, bid) of the calling lane.
+__device__ __forceinline__ void flush_tests(const FrameView& fr, WarpScratch& ws, V3 p, uint32_t n, uint32_t& qlen,
+                                            float& best, int32_t& bid) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t e = lane < n ? ws.queue[lane] : 0u;
+    const uint32_t owner = e & 31u;
+    const V3 q = v3(__shfl_sync(0xffffffffu, p.x, owner), __shfl_sync(0xffffffffu, p.y, owner), __shfl_sync(0xffffffffu, p.z, owner));
+    if (lane < n) {
+        int32_t id;
+        const float d = slot_distance(fr, (int32_t)(e >> 5), q, id);
+        atomicMin(&ws.best[owner], ((unsigned long long)__float_as_uint(d) << 32) | (uint32_t)id);
+    }
+    const uint32_t rest = qlen - n;   // <= 63
+    const uint32_t a = lane < rest ? ws.queue[n + lane] : 0u, b = lane + 32u < rest ? ws.queue[n + 32u + lane] : 0u;
+    __syncwarp();
+    if (lane < rest) ws.queue[lane] = a;
+    if (lane + 32u < rest) ws.queue[lane + 32u] = b;
+    __syncwarp();
+    qlen = rest;
+    const unsigned long long k = ws.best[lane];
+    best = __uint_as_float((uint32_t)(k >> 32));
+    bid = (int32_t)(uint32_t)k;
+}
+
 // Warp-cooperative variant for spatially coherent queries (one point per lane, all 32 lanes call
-// it together).  The warp walks the union of the nodes its lanes need with one shared stack in
-// shared memory (`wstack`, INSTA_STACK entries per warp): a node is fetched once per warp, every
-// lane tests it against its own point and bound, and a child is pushed when any lane may find a
-// nearer triangle in it.  Each lane's result is exactly its own nearest triangle (the union
-// contains every node that lane's own traversal would visit); control flow stays uniform, so all
-// lanes issue together.  Lanes with active == false only ride along.
-__device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool active, uint32_t* wstack, uint32_t* err,
+// it together).  The warp walks the union of the nodes its lanes need with one shared stack: a
+// node is fetched once per warp, every lane tests it against its own point and bound, and a child
+// is pushed when any lane may find a nearer triangle in it.  At a leaf, the (triangle, lane) pairs
+// that lanes need are queued and run 32 at a time, one per lane, so the exact tests are not
+// replicated across lanes that do not need them.  Each lane's result is exactly its own nearest
+// triangle, ties to the lowest id (the union holds every node that lane's own traversal would
+// visit; pruning with a not yet updated bound only tests more).  Control flow stays uniform.
+// Lanes with active == false only ride along.  The slot of the result is not tracked (-1).
+__device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool active, WarpScratch& ws, uint32_t* err,
                                                 float bound = __builtin_huge_valf()) {
     const float INF = __int_as_float(0x7f800000);
+    const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
     float best = active ? bound : -INF;
-    int32_t bid = -1, bslot = -1;
+    int32_t bid = -1;
     float dstack[INSTA_STACK];
     int sp = 0;
+    uint32_t qlen = 0;
     __syncwarp();
-    if ((threadIdx.x & 31) == 0) wstack[0] = 0u;
+    ws.best[lane] = ((unsigned long long)__float_as_uint(best) << 32) | 0xffffffffull;
+    if (lane == 0) ws.stack[0] = 0u;
     __syncwarp();
     dstack[0] = active ? 0.f : INF;
     sp = 1;
     while (sp > 0) {
         --sp;
-        const uint32_t ref = wstack[sp];
+        const uint32_t ref = ws.stack[sp];
         const bool need = dstack[sp] <= prune_limit(best);
-        if (!__any_sync(0xffffffffu, need)) continue;
+        const uint32_t nm = __ballot_sync(0xffffffffu, need);
+        if (!nm) continue;
         if (ref & INSTA_LEAF_BIT) {
             const uint32_t first = (ref & ~INSTA_LEAF_BIT) >> 3, count = ref & 7u;
-            for (uint32_t i = 0; i < count; ++i) {
-                int32_t id;
-                float d = slot_distance(fr, (int32_t)(first + i), p, id);
-                if (need && (d < best || (d == best && (uint32_t)id < (uint32_t)bid))) { best = d; bid = id; bslot = (int32_t)(first + i); }
-            }
+            const uint32_t nl = __popc(nm), rank = __popc(nm & lt_mask);
+            __syncwarp();   // the popped entry has been read by every lane
+            if (need)
+                for (uint32_t i = 0; i < count; ++i) ws.queue[qlen + i * nl + rank] = ((first + i) << 5) | lane;
+            qlen += count * nl;
+            __syncwarp();
+            while (qlen >= 32u) flush_tests(fr, ws, p, 32u, qlen, best, bid);
             continue;
         }
         const float4* nd = fr.nodes + (size_t)ref * 7;
@@ -155,17 +198,18 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
         for (int i = 0; i < 4; ++i) {
             if (key[i] != 0xffffffffu) {
                 if (sp < INSTA_STACK) {
-                    if ((threadIdx.x & 31) == 0) wstack[sp] = ci[i];
+                    if (lane == 0) ws.stack[sp] = ci[i];
                     dstack[sp] = active ? cd[i] : INF;
                     ++sp;
-                } else if (err && (threadIdx.x & 31) == 0) {
+                } else if (err && lane == 0) {
                     atomicOr(err, INSTA_DEVERR_STACK);
                 }
             }
         }
         __syncwarp();
     }
-    return {bid, bslot, best};
+    if (qlen) flush_tests(fr, ws, p, qlen, qlen, best, bid);
+    return {bid, -1, best};
 }
 
 // Unbounded exact nearest triangle.

@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(256) sort_place_kernel(const __grid_constant__
 // operand rows at the sample's sorted position.  A warp's 32 samples share a few grid cells, so
 // the cooperative BVH walk visits a small union of nodes.
 __global__ void __launch_bounds__(256, 4) deform_encode_kernel(const __grid_constant__ WaveArgs A) {
-    __shared__ uint32_t wstack[8][INSTA_STACK];
+    __shared__ WarpScratch wscratch[8];
     const uint32_t n = *A.n_samples_padded;
     const uint32_t n_alive = *A.n_alive_in;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(256, 4) deform_encode_kernel(const __grid_cons
         uint32_t mask = 7u;
         const V3 p = v3(cw[0], cw[1], cw[2]);
         const bool in_box = valid && box_contains(R.dv.aabb_min, R.dv.aabb_max, p);
-        Nearest q = nearest_warp(R.fr, p, in_box, wstack[warp], A.err);
+        Nearest q = nearest_warp(R.fr, p, in_box, wscratch[warp], A.err);
         if (in_box) {
             if (q.id >= 0) map_to_canonical(R.dv, R.fr.frames, (uint32_t)q.id, p, dw, cpos, cdir, &mask);
             else atomicOr(A.err, INSTA_DEVERR_NO_TRI);
