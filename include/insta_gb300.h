@@ -52,6 +52,7 @@ extern "C" {
 
 #define INSTA_PRECISION_FP16 0
 #define INSTA_PRECISION_BF16 1
+#define INSTA_PRECISION_FP8 2            /* MLPs in E4M3: per-layer weight scale, per-row activation scale, FP32 accumulate */
 
 #define INSTA_FLAG_DISABLE_INTERP 0x1u   /* "disable_interp" (src/core.cu:201,495) */
 

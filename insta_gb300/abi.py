@@ -13,7 +13,7 @@ import numpy as np
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libinsta_gb300.so"
 
 OK, ERR_INVALID_ARG, ERR_CUDA, ERR_BUDGET, ERR_NOT_READY, ERR_UNSUPPORTED, ERR_DEVICE = range(7)
-PRECISION_FP16, PRECISION_BF16 = 0, 1
+PRECISION_FP16, PRECISION_BF16, PRECISION_FP8 = 0, 1, 2
 FLAG_DISABLE_INTERP = 1
 
 EXPORTS = [

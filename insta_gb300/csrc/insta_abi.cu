@@ -281,7 +281,7 @@ FieldLayout field_layout(const insta_field_desc& d) {
     if (d.density_hidden_layers < 1 || d.density_hidden_layers > 3 || d.rgb_hidden_layers < 1 || d.rgb_hidden_layers > 4)
         fail(INSTA_ERR_UNSUPPORTED, "hidden layer counts out of range");
     if (d.log2_hashmap_size < 8 || d.log2_hashmap_size > 24) fail(INSTA_ERR_UNSUPPORTED, "log2_hashmap_size out of range");
-    if (d.precision > 1) fail(INSTA_ERR_UNSUPPORTED, "precision must be FP16 or BF16");
+    if (d.precision > 2) fail(INSTA_ERR_UNSUPPORTED, "precision must be FP16, BF16 or FP8");
     FieldLayout L{};
     float b = d.per_level_scale;
     if (!(b > 0.f)) b = expf(logf(2048.0f * (float)d.aabb_scale / (float)d.base_resolution) / (float)(d.n_levels - 1));
@@ -311,6 +311,36 @@ FieldLayout field_layout(const insta_field_desc& d) {
     }
     L.total = off + eoff * 2;
     return L;
+}
+
+float half_to_float(uint16_t h) {
+    uint32_t sign = (h >> 15) & 1u, exp = (h >> 10) & 0x1fu, man = h & 0x3ffu;
+    float f;
+    if (exp == 0) f = std::ldexp((float)man, -24);
+    else if (exp == 31) f = man ? NAN : INFINITY;
+    else f = std::ldexp((float)(man | 0x400u), (int)exp - 25);
+    return sign ? -f : f;
+}
+
+// FP8 E4M3 encoding of x: nearest representable value, ties to even, saturating at +-448 (the
+// SATFINITE conversion of the device); NaN -> 0x7f.
+uint8_t float_to_e4m3(float x) {
+    if (x != x) return 0x7f;
+    const uint8_t sign = std::signbit(x) ? 0x80 : 0x00;
+    const float a = std::fabs(x);
+    if (a >= 448.0f) return sign | 0x7e;
+    if (a < 0.015625f) {                          // subnormals: multiples of 2^-9
+        const float m = std::nearbyint(a * 512.0f);   // 0..8; 8 is the smallest normal
+        if (m >= 8.0f) return sign | 0x08;
+        return sign | (uint8_t)m;
+    }
+    int e;
+    std::frexp(a, &e);                            // a = m 2^e, m in [0.5, 1)
+    float q = std::nearbyint(std::ldexp(a, 4 - e));   // 8..16: the leading bit and 3 mantissa bits
+    if (q >= 16.0f) { q = 8.0f; ++e; }
+    const int E = e - 1 + 7;                      // biased exponent
+    if (E > 15 || (E == 15 && q > 14.0f)) return sign | 0x7e;
+    return sign | (uint8_t)(E << 3) | (uint8_t)((int)q - 8);
 }
 
 uint16_t half_to_bf16_bits(uint16_t h) {
@@ -447,7 +477,7 @@ struct WaveRun {
         ctx->alloc(w.sample_order, cap_samples * sizeof(uint32_t));
         ctx->alloc(w.sort_bins, (n_bins + n_bins / kSortBlock) * sizeof(uint32_t));
         ctx->alloc(w.out, cap_samples * sizeof(uint2));
-        if (fv.precision == 1) ctx->alloc(w.out_f32, cap_samples * sizeof(float4));
+        if (fv.precision != 0) ctx->alloc(w.out_f32, cap_samples * sizeof(float4));
         ctx->alloc(w.counters, 64);
         ctx->alloc(w.req_table, (size_t)slots * sizeof(ReqView));
         ctx->alloc(w.req_meta, (size_t)(slots + 1) * 2 * sizeof(uint32_t) + (size_t)slots * sizeof(uint32_t));
@@ -1006,16 +1036,50 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
             off = (off + N * K * 2 + 127) / 128 * 128;
             return at;
         };
+        // FP8: one byte per weight, scaled per layer by s = max|W| / 448
+        const bool fp8 = desc->precision == INSTA_PRECISION_FP8;
+        float lscale[8] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
+        if (fp8)
+            for (int l = 0; l < L.n_density + L.n_rgb; ++l) {
+                float mx = 0.f;
+                for (uint64_t i = 0; i < (uint64_t)L.layer_n[l] * L.layer_k[l]; ++i)
+                    mx = std::max(mx, std::fabs(half_to_float(mlp[L.layer_off[l] + i])));
+                lscale[l] = mx > 0.f ? mx / 448.0f : 1.0f;
+            }
+        auto add_tile8 = [&](int l, uint32_t k0, uint32_t K) -> uint32_t {
+            const uint32_t N = L.layer_n[l], Kin = L.layer_k[l];
+            const uint32_t at = off;
+            image.resize(off + (size_t)N * K, 0);
+            for (uint32_t n = 0; n < N; ++n)
+                for (uint32_t k = 0; k < K && k0 + k < Kin; ++k)
+                    image[at + tile_offset8(n, k, K)] = float_to_e4m3(half_to_float(mlp[L.layer_off[l] + (uint64_t)n * Kin + k0 + k]) / lscale[l]);
+            off = (off + N * K + 127) / 128 * 128;
+            return at;
+        };
         plan.k_in = (L.layer_k[0] + 15) / 16 * 16;
+        plan.k8 = (L.layer_k[0] + 31) / 32 * 32;
         plan.n_dh = (uint32_t)L.n_density - 1;
-        for (uint32_t l = 0; l < plan.n_dh; ++l) plan.d_off[l] = add_tile((int)l, 0, l == 0 ? plan.k_in : 64);
-        plan.d_out = add_tile(L.n_density - 1, 0, 64);
         const int r0 = L.n_density;
-        plan.r0_dens = add_tile(r0, 0, 16);
-        plan.r0_sh = add_tile(r0, 16, 16);
         plan.n_rh = (uint32_t)L.n_rgb - 1;
-        for (uint32_t l = 1; l < plan.n_rh; ++l) plan.r_off[l] = add_tile(r0 + (int)l, 0, 64);
-        plan.r_out = add_tile(r0 + L.n_rgb - 1, 0, 64);
+        if (fp8) {
+            for (uint32_t l = 0; l < plan.n_dh; ++l) plan.d_off[l] = add_tile8((int)l, 0, l == 0 ? plan.k8 : 64);
+            plan.d_out = add_tile8(L.n_density - 1, 0, 64);
+            plan.r0_dens = plan.r0_sh = add_tile8(r0, 0, 32);   // [density out | SH] as one K = 32 operand
+            for (uint32_t l = 1; l < plan.n_rh; ++l) plan.r_off[l] = add_tile8(r0 + (int)l, 0, 64);
+            plan.r_out = add_tile8(r0 + L.n_rgb - 1, 0, 64);
+            // the scales travel with the weights (a batch may mix avatars)
+            plan.scales = off;
+            image.resize(off + sizeof(lscale), 0);
+            std::memcpy(&image[off], lscale, sizeof(lscale));
+            off = (off + (uint32_t)sizeof(lscale) + 127) / 128 * 128;
+        } else {
+            for (uint32_t l = 0; l < plan.n_dh; ++l) plan.d_off[l] = add_tile((int)l, 0, l == 0 ? plan.k_in : 64);
+            plan.d_out = add_tile(L.n_density - 1, 0, 64);
+            plan.r0_dens = add_tile(r0, 0, 16);
+            plan.r0_sh = add_tile(r0, 16, 16);
+            for (uint32_t l = 1; l < plan.n_rh; ++l) plan.r_off[l] = add_tile(r0 + (int)l, 0, 64);
+            plan.r_out = add_tile(r0 + L.n_rgb - 1, 0, 64);
+        }
         plan.bytes = off;
         plan.tile_bytes = hash_tile_bytes(plan.k_in) + sh_tile_bytes();
         if (plan.bytes > 64 * 1024) fail(INSTA_ERR_UNSUPPORTED, "MLP weights exceed 64 KiB of shared memory");
@@ -1063,7 +1127,7 @@ int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t s
         m.fv = a.field.view; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.n_samples = n;
         m.out = (uint2*)w.out.p; m.out_f32 = (float4*)w.out_f32.p; m.err = ctx->err_dev;
         CK(launch_mlp(m, (uint32_t)tiles, ctx->stream));
-        CK(launch_unpack((const uint2*)w.out.p, (const float4*)w.out_f32.p, a.field.view.precision == 1, n, (float4*)out4, ctx->stream));
+        CK(launch_unpack((const uint2*)w.out.p, (const float4*)w.out_f32.p, a.field.view.precision != 0, n, (float4*)out4, ctx->stream));
     });
 }
 
@@ -1089,7 +1153,7 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
         m.fv = a.field.view; m.plan = P; m.tiles = tiles; m.n_alive = nullptr; m.n_samples = n;
         m.out = out; m.out_f32 = out_f32; m.err = ctx->err_dev;
         CK(launch_mlp(m, (uint32_t)n_tiles, ctx->stream));
-        CK(launch_unpack(out, out_f32, a.field.view.precision == 1, n, (float4*)out4, ctx->stream));
+        CK(launch_unpack(out, out_f32, a.field.view.precision != 0, n, (float4*)out4, ctx->stream));
     });
 }
 

@@ -55,7 +55,7 @@ struct FieldView {
     uint32_t level_size[INSTA_MAX_HASH_LEVELS];
     uint32_t level_off[INSTA_MAX_HASH_LEVELS];   // in entries
     uint8_t level_dense[INSTA_MAX_HASH_LEVELS];
-    int precision;            // 0 fp16, 1 bf16
+    int precision;            // 0 fp16, 1 bf16, 2 fp8 e4m3 (weight scales inside the MLP image)
 };
 
 struct RenderView {

@@ -25,6 +25,10 @@ struct TilePlan {
     uint32_t bytes;       // image size
     uint32_t k_in;        // density input width (32 or 48)
     uint32_t tile_bytes;  // one input tile record: hash tile + SH tile
+    // FP8 image: the density input padded to k8 (multiple of 32), colour layer 0 as one K = 32
+    // tile at r0_dens ([density out | SH]); every tile stores one byte per weight
+    uint32_t k8;
+    uint32_t scales;      // FP8 image: byte offset of the 8 per-layer weight scales (float)
 };
 
 __host__ __device__ constexpr uint32_t hash_tile_bytes(uint32_t k_in) { return 128u * k_in * 2u; }
@@ -60,21 +64,25 @@ struct TileSmem {
     uint32_t tmem_base;
 };
 
-// One MMA chain: sum over (A_i, B_i) pairs into TMEM columns [col, col + N).
+// One MMA chain: sum over (A_i, B_i) pairs into TMEM columns [col, col + N).  K in elements;
+// f8: E4M3 operands (kind::f8f6f4, 32 elements per instruction), else FP16/BF16 (16 per
+// instruction).  Either way one instruction consumes 32 bytes of each row.
 __device__ __forceinline__ bool issue_chain(TileSmem& sm, const uint8_t* const* a, const uint8_t* const* b, const uint32_t* K,
-                                            int n, uint32_t N, uint32_t col, bool bf16, uint32_t& phase) {
+                                            int n, uint32_t N, uint32_t col, bool bf16, uint32_t& phase, bool f8 = false) {
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     if (threadIdx.x == 0) {
         tc_fence_after();
-        const uint32_t idesc = idesc_f16(128, N, bf16);
+        const uint32_t idesc = idesc_f16(128, N, bf16 && !f8);
         uint32_t acc = 0;
         for (int i = 0; i < n; ++i) {
             const uint32_t a0 = smem_addr(a[i]), b0 = smem_addr(b[i]);
-            const uint32_t sbo = (K[i] / 8) * 128;
-            for (uint32_t ks = 0; ks < K[i] / 16; ++ks) {
-                umma_f16(sm.tmem_base + col, smem_desc(a0 + ks * 256, 128, sbo), smem_desc(b0 + ks * 256, 128, sbo), idesc, acc);
+            const uint32_t kbytes = f8 ? K[i] : 2 * K[i];
+            const uint32_t sbo = (kbytes / 16) * 128;
+            for (uint32_t ks = 0; ks < kbytes / 32; ++ks) {
+                if (f8) umma_f8(sm.tmem_base + col, smem_desc(a0 + ks * 256, 128, sbo), smem_desc(b0 + ks * 256, 128, sbo), idesc, acc);
+                else umma_f16(sm.tmem_base + col, smem_desc(a0 + ks * 256, 128, sbo), smem_desc(b0 + ks * 256, 128, sbo), idesc, acc);
                 acc = 1;
             }
         }
@@ -164,6 +172,148 @@ __device__ __forceinline__ bool mlp_tile(TileSmem& sm, const uint8_t* w, const T
         out4[1] = from_act(to_act(v[1], bf16), bf16);
         out4[2] = from_act(to_act(v[2], bf16), bf16);
     }
+    return ok;
+}
+
+// ------------------------------------------------------------------ FP8 (E4M3) variant
+// Every layer input row gets its own scale a = max|x| / 448 (rounded to E4M3 after dividing by
+// a); weights carry a per-layer scale s; the FP32 accumulator is multiplied back by a, then s.
+__device__ __forceinline__ uint32_t e4m3x4(float a, float b, float c, float d, float inv_scale_div) {
+    (void)inv_scale_div;
+    return (uint32_t)__nv_cvt_float_to_fp8(a, __NV_SATFINITE, __NV_E4M3) |
+           ((uint32_t)__nv_cvt_float_to_fp8(b, __NV_SATFINITE, __NV_E4M3) << 8) |
+           ((uint32_t)__nv_cvt_float_to_fp8(c, __NV_SATFINITE, __NV_E4M3) << 16) |
+           ((uint32_t)__nv_cvt_float_to_fp8(d, __NV_SATFINITE, __NV_E4M3) << 24);
+}
+
+// 16 values of this thread's row, divided by `a`, as E4M3 into columns [k, k + 16) of an A tile.
+__device__ __forceinline__ void store16_e4m3(uint8_t* tile, uint32_t K, uint32_t k, const float* v, float a) {
+    float q[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) q[i] = __fdiv_rn(v[i], a);
+    uint4 u;
+    u.x = e4m3x4(q[0], q[1], q[2], q[3], 0.f);
+    u.y = e4m3x4(q[4], q[5], q[6], q[7], 0.f);
+    u.z = e4m3x4(q[8], q[9], q[10], q[11], 0.f);
+    u.w = e4m3x4(q[12], q[13], q[14], q[15], 0.f);
+    *reinterpret_cast<uint4*>(tile + tile_offset8(threadIdx.x, k, K)) = u;
+}
+
+__device__ __forceinline__ float row_scale(float mx) { return mx > 0.f ? __fdiv_rn(mx, 448.0f) : 1.0f; }
+
+// 16 FP16 values of this thread's row of a 16-bit tile (columns [k, k + 16)).
+__device__ __forceinline__ void load16_half(const uint8_t* tile, uint32_t K, uint32_t k, float* v) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const uint4 u = *reinterpret_cast<const uint4*>(tile + tile_offset(threadIdx.x, k + 8 * q, K));
+        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w[i]));
+            v[8 * q + 2 * i] = f.x;
+            v[8 * q + 2 * i + 1] = f.y;
+        }
+    }
+}
+
+// Dequantised, activated accumulator columns [c, c + 16) of this thread's row.
+__device__ __forceinline__ void acc16(TileSmem& sm, uint32_t c, float a, float s, bool relu, float* v) {
+    tmem_ld16(tile_lane_addr(sm, c), v);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        v[i] = __fmul_rn(__fmul_rn(v[i], a), s);
+        if (relu) v[i] = fmaxf(v[i], 0.f);
+    }
+}
+
+// Hidden epilogue: ReLU(acc * a * s) of 64 columns, re-quantised with a fresh row scale into
+// the hidden A tile (two passes over TMEM: max, then quantise).  Returns the new row scale.
+__device__ __forceinline__ float hidden_to_e4m3(TileSmem& sm, uint8_t* a_h8, float a, float s) {
+    float mx = 0.f;
+#pragma unroll 1
+    for (uint32_t c = 0; c < 64; c += 16) {
+        float v[16];
+        acc16(sm, c, a, s, true, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) mx = fmaxf(mx, v[i]);
+    }
+    const float na = row_scale(mx);
+#pragma unroll 1
+    for (uint32_t c = 0; c < 64; c += 16) {
+        float v[16];
+        acc16(sm, c, a, s, true, v);
+        store16_e4m3(a_h8, 64, c, v, na);
+    }
+    return na;
+}
+
+// Both MLPs in FP8 for the tile held in stage[buf]; returns this thread's (r, g, b, raw density).
+__device__ __forceinline__ bool mlp_tile8(TileSmem& sm, const uint8_t* w, const TilePlan& P, const float* ls, int buf,
+                                          uint32_t& phase, float* out4) {
+    bool ok = true;
+    const uint8_t* hash = sm.stage[buf];
+    const uint8_t* sh = sm.stage[buf] + hash_tile_bytes(P.k_in);
+    uint8_t* a_h8 = sm.a_h;            // [128][64] E4M3
+    uint8_t* a_in8 = sm.a_h + 8192;    // [128][k8 <= 64] E4M3
+    uint8_t* a_rgb8 = sm.a_dens;       // [128][32] E4M3
+    const uint8_t* a;
+    const uint8_t* b;
+    uint32_t K;
+    int li = 0;
+    // density input: the FP16 hash row (k_in values, zero-padded to k8)
+    float mx = 0.f;
+    for (uint32_t c = 0; c < P.k_in; c += 16) {
+        float v[16];
+        load16_half(hash, P.k_in, c, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fabsf(v[i]));
+    }
+    float ra = row_scale(mx);
+    for (uint32_t c = 0; c < P.k8; c += 16) {
+        float v[16];
+        if (c < P.k_in) load16_half(hash, P.k_in, c, v);
+        else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[i] = 0.f;
+        }
+        store16_e4m3(a_in8, P.k8, c, v, ra);
+    }
+    a = a_in8; b = w + P.d_off[0]; K = P.k8;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
+    ra = hidden_to_e4m3(sm, a_h8, ra, ls[li++]);
+    for (uint32_t l = 1; l < P.n_dh; ++l) {
+        a = a_h8; b = w + P.d_off[l]; K = 64;
+        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
+        ra = hidden_to_e4m3(sm, a_h8, ra, ls[li++]);
+    }
+    // density output (16): raw density is column 0; colour input = [density out | SH]
+    a = a_h8; b = w + P.d_out; K = 64;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, false, phase, true);
+    float dens[16], shv[16];
+    acc16(sm, 64, ra, ls[li++], false, dens);
+    out4[3] = dens[0];
+    load16_half(sh, 16, 0, shv);
+    mx = 0.f;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fmaxf(fabsf(dens[i]), fabsf(shv[i])));
+    ra = row_scale(mx);
+    store16_e4m3(a_rgb8, 32, 0, dens, ra);
+    store16_e4m3(a_rgb8, 32, 16, shv, ra);
+    a = a_rgb8; b = w + P.r0_dens; K = 32;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
+    ra = hidden_to_e4m3(sm, a_h8, ra, ls[li++]);
+    for (uint32_t l = 1; l < P.n_rh; ++l) {
+        a = a_h8; b = w + P.r_off[l]; K = 64;
+        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
+        ra = hidden_to_e4m3(sm, a_h8, ra, ls[li++]);
+    }
+    a = a_h8; b = w + P.r_out; K = 64;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, false, phase, true);
+    float rgb[16];
+    acc16(sm, 64, ra, ls[li++], false, rgb);
+    out4[0] = rgb[0];
+    out4[1] = rgb[1];
+    out4[2] = rgb[2];
     return ok;
 }
 

@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(128) mlp_kernel(const __grid_constant__ MlpArg
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const bool bf16 = A.fv.precision == 1;
+    const bool bf16 = A.fv.precision == 1, fp8 = A.fv.precision == 2;
     uint32_t phase = 0;
     int buf = 0;
     int pending = 1;   // buffer with a copy in flight: 1 + index, 0 = none
@@ -528,11 +528,12 @@ __global__ void __launch_bounds__(128) mlp_kernel(const __grid_constant__ MlpArg
             tc_fence_after();
         }
         float o4[4];
-        ok &= mlp_tile(sm, w, A.plan, buf, bf16, phase, o4);
+        if (fp8) ok &= mlp_tile8(sm, w, A.plan, reinterpret_cast<const float*>(w + A.plan.scales), buf, phase, o4);
+        else ok &= mlp_tile(sm, w, A.plan, buf, bf16, phase, o4);
         const uint32_t s = t * 128u + threadIdx.x;
         if (s < n_samples) {
-            if (bf16) {
-                // keep BF16-rounded values exactly: store as FP32 through the float outputs
+            if (A.fv.precision != 0) {
+                // BF16-rounded or FP8-path values kept exactly: FP32 outputs
                 A.out_f32[s] = make_float4(o4[0], o4[1], o4[2], o4[3]);
             } else {
                 __half2 rg = __floats2half2_rn(o4[0], o4[1]);
@@ -558,7 +559,7 @@ __global__ void __launch_bounds__(128) mlp_kernel(const __grid_constant__ MlpArg
 // ------------------------------------------------------------------ composite + compaction
 __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
     const uint32_t n_alive = *A.n_alive_in;
-    const bool bf16 = A.fv.precision == 1;
+    const bool f32_out = A.fv.precision != 0;   // the MLP wrote FP32 outputs
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_iter = (n_alive + stride - 1) / stride;
     for (uint32_t it = 0; it < n_iter; ++it) {
@@ -576,7 +577,7 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
             for (; j < m; ++j) {
                 const uint32_t s = A.sample_index[(size_t)j * n_alive + r];
                 float o[4];
-                if (bf16) {
+                if (f32_out) {
                     float4 v = A.out_f32[s];
                     o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
                 } else {

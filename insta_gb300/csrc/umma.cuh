@@ -17,6 +17,7 @@
 #include <cstdint>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include "insta_types.h"
 
@@ -26,6 +27,12 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)
 
 __host__ __device__ constexpr uint32_t tile_offset(uint32_t r, uint32_t k, uint32_t K) {
     return ((r / 8) * (K / 8) + k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2;
+}
+
+// The same layout for 8-bit elements: a core matrix is 8 rows x 16 one-byte elements, so with K
+// counted in bytes the byte geometry (and the descriptor strides) equal the 16-bit case.
+__host__ __device__ constexpr uint32_t tile_offset8(uint32_t r, uint32_t k, uint32_t K) {
+    return ((r / 8) * (K / 16) + k / 16) * 128 + (r % 8) * 16 + (k % 16);
 }
 
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -85,6 +92,13 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
 __device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+}
+// kind::f8f6f4 with E4M3 A and B (instruction descriptor a/b formats 0, as idesc_f16(M, N, false));
+// K = 32 per instruction.
+__device__ __forceinline__ void umma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n"
         ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
 }
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {

@@ -43,6 +43,25 @@ static uint16_t orc_f2bf16(float x) {
     return (uint16_t)(u >> 16);
 }
 static float orc_bf16_to_f(uint16_t b) { uint32_t u = (uint32_t)b << 16; float f; memcpy(&f, &u, 4); return f; }
+/* FP8 E4M3 (1 sign, 4 exponent bits with bias 7, 3 mantissa bits; largest finite 448, no
+ * infinities): x rounded to the nearest representable value, ties to even, saturating at +-448
+ * (the SATFINITE conversion); NaN stays NaN. */
+float orc_e4m3_round(float x) {
+    if (x != x) return x;
+    float a = fabsf(x);
+    if (a >= 448.0f) return copysignf(448.0f, x);
+    float q;
+    if (a < 0.015625f) {                       /* below 2^-6: subnormals, quantum 2^-9 */
+        q = nearbyintf(a * 512.0f) / 512.0f;
+    } else {
+        int e;
+        frexpf(a, &e);                         /* a = m 2^e, m in [0.5, 1): leading bit 2^(e-1) */
+        float quantum = ldexpf(1.0f, e - 4);   /* 3 mantissa bits below the leading one */
+        q = nearbyintf(a / quantum) * quantum;
+        if (q > 448.0f) q = 448.0f;
+    }
+    return copysignf(q, x);
+}
 
 /* ---------------------------------------------------------- field layout */
 /* Per-level grid scale of the multiresolution hash encoding:

@@ -141,6 +141,7 @@ void orc_transform(const float *p, const float *dir, const float *Mw, const floa
 /* ---- half helpers ------------------------------------------------------ */
 uint16_t orc_f2h(float x);
 float orc_h2f(uint16_t h);
+float orc_e4m3_round(float x);
 int orc_num_threads(void);
 
 #ifdef __cplusplus

@@ -180,12 +180,29 @@ def field_cfg(fc, weight_format: int = 0) -> FieldCfg:
     return c
 
 
-def field_eval(fc, params, coords, fp64=False, weight_format=0):
+def fp8_layer_scales(fc, params) -> np.ndarray:
+    """Per-layer FP8 weight scales max|W| / 448 (float32), in layer order (density, then colour)."""
+    from insta_gb300 import layout as _layout
+    lay = _layout.field_layout(fc)
+    w = np.ascontiguousarray(params).view(np.float16).astype(np.float32)
+    out = np.ones(8, np.float32)
+    for i, (off, n, k, _last) in enumerate(lay.layers):
+        mx = np.float32(np.abs(w[off:off + n * k]).max())
+        out[i] = mx / np.float32(448.0) if mx > 0 else np.float32(1.0)
+    return out
+
+
+def field_eval(fc, params, coords, fp64=False, weight_format=0, layer_scales=None):
+    """weight_format 2 (FP8) takes the per-layer scales (default: fp8_layer_scales)."""
     c = np.ascontiguousarray(coords, dtype=np.float32)
     out = np.empty((len(c), 4), dtype=np.float32)
     cfg = field_cfg(fc, weight_format)
     p = np.ascontiguousarray(params).view(np.uint16)
-    lib().orc_field_eval(C.byref(cfg), ptr(p), None, ptr(c), C.c_uint32(c.shape[1]), C.c_int64(len(c)), ptr(out), C.c_int(int(fp64)))
+    if weight_format == 2 and layer_scales is None:
+        layer_scales = fp8_layer_scales(fc, params)
+    ls = None if layer_scales is None else np.ascontiguousarray(layer_scales, np.float32)
+    lib().orc_field_eval(C.byref(cfg), ptr(p), ptr(ls) if ls is not None else None, ptr(c), C.c_uint32(c.shape[1]),
+                         C.c_int64(len(c)), ptr(out), C.c_int(int(fp64)))
     return out
 
 
@@ -227,7 +244,8 @@ def render_cfg(width, height, focal, cam, render_box, train_box=((0, 0, 0), (1, 
     return r
 
 
-def render(rc: RenderCfg, deform: Deformation, bits, fc, params, rows=None, fp64=False, weight_format=0, extra_dims=None):
+def render(rc: RenderCfg, deform: Deformation, bits, fc, params, rows=None, fp64=False, weight_format=0, extra_dims=None,
+           layer_scales=None):
     r0, r1 = (0, rc.height) if rows is None else rows
     n = (r1 - r0) * rc.width
     rgba = np.zeros((n, 4), dtype=np.float32)
@@ -239,7 +257,11 @@ def render(rc: RenderCfg, deform: Deformation, bits, fc, params, rows=None, fp64
     if extra_dims is not None:
         ed = np.ascontiguousarray(extra_dims, dtype=np.float32)
         rc.extra_dims = ed.ctypes.data
-    total = lib().orc_render(C.byref(rc), C.byref(deform.d), ptr(bits), C.byref(cfg), ptr(p), None, C.c_int(r0), C.c_int(r1),
+    if weight_format == 2 and layer_scales is None:
+        layer_scales = fp8_layer_scales(fc, params)
+    ls = None if layer_scales is None else np.ascontiguousarray(layer_scales, np.float32)
+    total = lib().orc_render(C.byref(rc), C.byref(deform.d), ptr(bits), C.byref(cfg), ptr(p), ptr(ls) if ls is not None else None,
+                             C.c_int(r0), C.c_int(r1),
                              ptr(rgba), ptr(depth), ptr(ns), C.c_int(int(fp64)))
     rc.extra_dims = None
     return rgba, depth, ns, int(total)

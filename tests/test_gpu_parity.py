@@ -279,6 +279,29 @@ def test_field_eval_bf16(gpu_avatar, oracle):
     assert (err <= 3e-2 + 4e-2 * np.abs(ref)).all(), float(err.max())
 
 
+def test_field_eval_fp8(gpu_avatar, oracle):
+    """FP8 E4M3 MLPs (per-layer weight scale, per-row activation scale, FP32 accumulation) against
+    the oracle's FP8 restatement.  Tensor-core accumulation order can move a re-quantised
+    activation by one E4M3 step, so the bound is statistical; the error against FP64 is reported
+    by the precision workload of bench.py."""
+    from insta_gb300 import abi, synthetic as S
+    fc = S.FieldConfig()
+    params = S.field_params(fc, seed=2)
+    gpu_avatar.params_load(5, fc, params, precision=abi.PRECISION_FP8)
+    c = random_coords(4096, seed=12)
+    out = torch.zeros((len(c), 4), dtype=torch.float32, device="cuda")
+    gpu_avatar.field_eval(5, dev(c), 11, len(c), out)
+    gpu_avatar.sync()
+    got = out.cpu().numpy()
+    ref = oracle.field_eval(fc, params, c, weight_format=2)
+    err = np.abs(got - ref)
+    assert np.isfinite(got).all()
+    assert float(err.mean()) < 5e-3, float(err.mean())
+    assert (err <= 5e-2 + 5e-2 * np.abs(ref)).mean() > 0.999, float(err.max())
+    ref16 = oracle.field_eval(fc, params, c)
+    assert np.abs(got - ref16).mean() < 5e-2
+
+
 def render_pair(ctx, oracle, oracle_frame, avatar, fc, params, W, H, yaw=0.0, avatar_id=0):
     from insta_gb300 import synthetic as S
     cam, focal = S.camera(yaw, width=W, height=H)
@@ -318,6 +341,30 @@ def test_render_opaque_early_termination(gpu_avatar, oracle, oracle_frame, avata
     assert (r_rgba[:, 3] > 0.99).sum() > 100
     assert psnr(rgba, r_rgba) >= 45.0
     gpu_avatar.params_load(0, fc, S.field_params(fc, seed=0))
+
+
+def test_render_fp8(gpu_avatar, oracle, oracle_frame, avatar):
+    """The render with FP8 MLPs against the oracle's FP8 render."""
+    from insta_gb300 import abi, synthetic as S
+    fc = S.FieldConfig()
+    params = S.field_params(fc, seed=0)
+    gpu_avatar.params_load(0, fc, params, precision=abi.PRECISION_FP8)
+    gpu_avatar.occupancy_from_mesh(0, 0, 0.015)
+    try:
+        W = H = 64
+        cam, focal = S.camera(5.0, width=W, height=H)
+        req = gpu_avatar.render_desc(0, 0, W, H, focal, cam)
+        rgba = np.zeros((W * H, 4), np.float32)
+        depth = np.zeros(W * H, np.float32)
+        gpu_avatar.render(req, rgba, depth)
+        bits = oracle.occupancy(oracle_frame["def"], 0.015)
+        d = oracle.Deformation(oracle_frame["def"], oracle_frame["can"], oracle_frame["adj"], oracle_frame["bvh"])
+        rc = oracle.render_cfg(W, H, focal, cam, avatar.render_aabb())
+        r_rgba, _, _, total = oracle.render(rc, d, bits, fc, params, weight_format=2)
+        assert total > 1000
+        assert psnr(rgba, r_rgba) >= 35.0
+    finally:
+        gpu_avatar.params_load(0, fc, params)
 
 
 def test_render_device_outputs(gpu_avatar, field_setup, oracle, avatar):
