@@ -424,6 +424,90 @@ def run_serve(args):
     ctx.close()
 
 
+def run_precision(args):
+    """Precision variants of the 1024x1024 render: MLPs in FP16 (plain), BF16 and FP8 E4M3 (per-layer
+    weight scale), FP32 accumulation; geometry FP32.  Reports per variant: device time per frame,
+    pixel error and PSNR against the host FP64 oracle on a band of central rows, PSNR against the
+    plain path, network-output error against the FP64 oracle on random field coordinates, and the
+    canonical-coordinate error of the map against the FP64 oracle."""
+    import torch
+    from insta_gb300 import abi, synthetic as S
+    from oracle import oracle as O
+    W = H = args.width if args.width != 512 else 1024
+    av = S.make_avatar(0)
+    fc = S.FieldConfig()
+    params = S.field_params(fc, seed=0)
+    frame = av.frame(av.frame_coeffs(0))
+    ctx = abi.Context(0)
+    ctx.canonical_set(0, av.canonical, av.faces, av.mask)
+    ctx.frame_upload(0, 0, frame)
+    ctx.occupancy_from_mesh(0, 0, RADIUS)
+    cam, focal = S.camera(0.0, width=W, height=H)
+    req = ctx.render_desc(0, 0, W, H, focal, cam, cone_angle=CONE)
+    # FP64 oracle references
+    can = O.build_triangles(av.canonical, None, av.faces, av.mask)
+    dtr = O.build_triangles(frame, av.canonical, av.faces, av.mask)
+    adj = O.adjacency(av.faces, av.n_verts)
+    bvh = O.Bvh(dtr)
+    bits = O.occupancy(dtr, RADIUS)
+    d64 = O.Deformation(dtr, can, adj, bvh, fp64=True)
+    rc = O.render_cfg(W, H, focal, cam, av.render_aabb(), cone_angle=CONE)
+    r0, r1 = H // 2 - args.rows // 2, H // 2 + args.rows // 2
+    ref64, _, _, _ = O.render(rc, d64, bits, fc, params, rows=(r0, r1), fp64=True)
+    rng = np.random.default_rng(5)
+    coords = np.zeros((1 << 16, 11), np.float32)
+    coords[:, :3] = rng.uniform(0.38, 0.62, (len(coords), 3))
+    dirs = rng.normal(size=(len(coords), 3))
+    coords[:, 8:11] = (dirs / np.linalg.norm(dirs, axis=1, keepdims=True) + 1) * 0.5
+    field64 = O.field_eval(fc, params, coords, fp64=True)
+    pts = S.shell_points(frame, av.faces, 1 << 18, seed=3)
+    _, can64 = d64.map_soa(pts)
+    idx = torch.empty(len(pts), dtype=torch.int32, device="cuda")
+    canon = torch.empty((len(pts), 3), device="cuda")
+    ctx.canonical_map_soa(0, 0, torch.from_numpy(pts).cuda(), len(pts), idx, canon)
+    ctx.sync()
+    diag = float(np.linalg.norm(av.canonical.max(0) - av.canonical.min(0)))
+    canon_err = float(np.abs(canon.cpu().numpy().astype(np.float64) - can64).max()) / diag
+    rgba = torch.empty((W * H, 4), device="cuda")
+    depth = torch.empty(W * H, device="cuda")
+    out = {"workload": f"precision variants, render {W}x{H}", "canonical_err_over_diag": canon_err,
+           "oracle_rows": [r0, r1], "variants": {}}
+    plain = None
+    for name, prec in (("fp16", abi.PRECISION_FP16), ("bf16", abi.PRECISION_BF16), ("fp8_e4m3", abi.PRECISION_FP8)):
+        ctx.params_load(0, fc, params, precision=prec)
+        for _ in range(args.warmup):
+            ctx.render(req, rgba, depth)
+        ctx.sync()
+        ctx.stats(reset=True)
+        ctx.stats_enable(True)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.render(req, rgba, depth)
+        ctx.sync()
+        ms = (time.perf_counter() - t0) / args.steps * 1e3
+        st = ctx.stats(reset=True)
+        ctx.stats_enable(False)
+        img = rgba.cpu().numpy()
+        band = img.reshape(H, W, 4)[r0:r1].reshape(-1, 4)
+        if plain is None:
+            plain = img.copy()
+        fo = torch.zeros((len(coords), 4), device="cuda")
+        ctx.field_eval(0, torch.from_numpy(coords).cuda(), 11, len(coords), fo)
+        ctx.sync()
+        fe = np.abs(fo.cpu().numpy().astype(np.float64) - field64)
+        mse = float(np.mean((band.astype(np.float64) - ref64) ** 2))
+        mse_plain = float(np.mean((img.astype(np.float64) - plain) ** 2))
+        out["variants"][name] = {
+            "ms_per_frame": ms, "mlp_ms": st["stage_ms"]["mlp"] / args.steps,
+            "pixel_max_abs_err_vs_fp64": float(np.abs(band - ref64).max()),
+            "psnr_vs_fp64_oracle": 10 * math.log10(1.0 / mse) if mse > 0 else float("inf"),
+            "psnr_vs_plain": 10 * math.log10(1.0 / mse_plain) if mse_plain > 0 else float("inf"),
+            "field_mean_abs_err_vs_fp64": float(fe.mean()), "field_max_abs_err_vs_fp64": float(fe.max()),
+            "density_max_abs_err_vs_fp64": float(fe[:, 3].max())}
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -432,8 +516,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--width", type=int, default=512, help="square render size (512 = the benchmark workload)")
-    ap.add_argument("--workload", choices=["render", "batch", "serve"], default="render",
-                    help="render: the benchmark line; batch: 64 expressions in one wavefront; serve: request stream")
+    ap.add_argument("--workload", choices=["render", "batch", "serve", "precision"], default="render",
+                    help="render: the benchmark line; batch: 64 expressions in one wavefront; serve: request stream; "
+                         "precision: FP16 / BF16 / FP8 MLPs at 1024x1024 against the FP64 oracle")
+    ap.add_argument("--rows", type=int, default=16, help="precision: image rows rendered by the FP64 oracle")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--rate", type=float, default=240.0)
     ap.add_argument("--duration", type=float, default=30.0)
@@ -446,6 +532,8 @@ def main():
         return run_batch64(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "precision":
+        return run_precision(args)
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -176,8 +176,9 @@ __device__ __forceinline__ bool mlp_tile(TileSmem& sm, const uint8_t* w, const T
 }
 
 // ------------------------------------------------------------------ FP8 (E4M3) variant
-// Every layer input row gets its own scale a = max|x| / 448 (rounded to E4M3 after dividing by
-// a); weights carry a per-layer scale s; the FP32 accumulator is multiplied back by a, then s.
+// Every layer input row gets its own scale a = max|x| / 448 (rounded to E4M3 after multiplying by
+// 448 / max|x|); weights carry a per-layer scale s; the FP32 accumulator is multiplied back by a,
+// then s.
 __device__ __forceinline__ uint32_t e4m3x4(float a, float b, float c, float d, float inv_scale_div) {
     (void)inv_scale_div;
     return (uint32_t)__nv_cvt_float_to_fp8(a, __NV_SATFINITE, __NV_E4M3) |
@@ -186,11 +187,12 @@ __device__ __forceinline__ uint32_t e4m3x4(float a, float b, float c, float d, f
            ((uint32_t)__nv_cvt_float_to_fp8(d, __NV_SATFINITE, __NV_E4M3) << 24);
 }
 
-// 16 values of this thread's row, divided by `a`, as E4M3 into columns [k, k + 16) of an A tile.
-__device__ __forceinline__ void store16_e4m3(uint8_t* tile, uint32_t K, uint32_t k, const float* v, float a) {
+// 16 values of this thread's row, times `inv` (448 / row max), as E4M3 into columns [k, k + 16)
+// of an A tile.
+__device__ __forceinline__ void store16_e4m3(uint8_t* tile, uint32_t K, uint32_t k, const float* v, float inv) {
     float q[16];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) q[i] = __fdiv_rn(v[i], a);
+    for (int i = 0; i < 16; ++i) q[i] = __fmul_rn(v[i], inv);
     uint4 u;
     u.x = e4m3x4(q[0], q[1], q[2], q[3], 0.f);
     u.y = e4m3x4(q[4], q[5], q[6], q[7], 0.f);
@@ -199,7 +201,9 @@ __device__ __forceinline__ void store16_e4m3(uint8_t* tile, uint32_t K, uint32_t
     *reinterpret_cast<uint4*>(tile + tile_offset8(threadIdx.x, k, K)) = u;
 }
 
+// Row scale a = max / 448 (multiplies the accumulator back) and its quantising factor 448 / max.
 __device__ __forceinline__ float row_scale(float mx) { return mx > 0.f ? __fdiv_rn(mx, 448.0f) : 1.0f; }
+__device__ __forceinline__ float row_inv(float mx) { return mx > 0.f ? __fdiv_rn(448.0f, mx) : 1.0f; }
 
 // 16 FP16 values of this thread's row of a 16-bit tile (columns [k, k + 16)).
 __device__ __forceinline__ void load16_half(const uint8_t* tile, uint32_t K, uint32_t k, float* v) {
@@ -237,14 +241,14 @@ __device__ __forceinline__ float hidden_to_e4m3(TileSmem& sm, uint8_t* a_h8, flo
 #pragma unroll
         for (int i = 0; i < 16; ++i) mx = fmaxf(mx, v[i]);
     }
-    const float na = row_scale(mx);
+    const float inv = row_inv(mx);
 #pragma unroll 1
     for (uint32_t c = 0; c < 64; c += 16) {
         float v[16];
         acc16(sm, c, a, s, true, v);
-        store16_e4m3(a_h8, 64, c, v, na);
+        store16_e4m3(a_h8, 64, c, v, inv);
     }
-    return na;
+    return row_scale(mx);
 }
 
 // Both MLPs in FP8 for the tile held in stage[buf]; returns this thread's (r, g, b, raw density).
@@ -269,6 +273,7 @@ __device__ __forceinline__ bool mlp_tile8(TileSmem& sm, const uint8_t* w, const 
         for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fabsf(v[i]));
     }
     float ra = row_scale(mx);
+    const float inv0 = row_inv(mx);
     for (uint32_t c = 0; c < P.k8; c += 16) {
         float v[16];
         if (c < P.k_in) load16_half(hash, P.k_in, c, v);
@@ -276,7 +281,7 @@ __device__ __forceinline__ bool mlp_tile8(TileSmem& sm, const uint8_t* w, const 
 #pragma unroll
             for (int i = 0; i < 16; ++i) v[i] = 0.f;
         }
-        store16_e4m3(a_in8, P.k8, c, v, ra);
+        store16_e4m3(a_in8, P.k8, c, v, inv0);
     }
     a = a_in8; b = w + P.d_off[0]; K = P.k8;
     ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
@@ -297,8 +302,8 @@ __device__ __forceinline__ bool mlp_tile8(TileSmem& sm, const uint8_t* w, const 
 #pragma unroll
     for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fmaxf(fabsf(dens[i]), fabsf(shv[i])));
     ra = row_scale(mx);
-    store16_e4m3(a_rgb8, 32, 0, dens, ra);
-    store16_e4m3(a_rgb8, 32, 16, shv, ra);
+    store16_e4m3(a_rgb8, 32, 0, dens, row_inv(mx));
+    store16_e4m3(a_rgb8, 32, 16, shv, row_inv(mx));
     a = a_rgb8; b = w + P.r0_dens; K = 32;
     ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
     ra = hidden_to_e4m3(sm, a_h8, ra, ls[li++]);
