@@ -35,8 +35,9 @@ WIDTH = HEIGHT = 512   # --width overrides (small cases for profiling)
 RADIUS = 0.015
 CONE = 1.0 / 256.0
 L2_FLUSH_BYTES = 512 << 20
-# DRAM bytes (read + write) of deform_encode per 512x512 frame (its two launches), from an ncu
-# capture of this workload (profiles/deform_encode_render512.md)
+# DRAM bytes (read + write) of the deform+encode stage per 512x512 frame (nearest_stage_kernel and
+# map_encode_kernel, two rounds each), from an ncu capture of this workload
+# (profiles/deform_encode_render512.md)
 TRAFFIC_PER_FRAME = 416_832_512
 # Algorithmic bytes per sample of the dominant kernel (deform_encode): hash-grid gathers
 # (16 levels x 8 corners x 2 FP16 features) + sample record, ray direction and ray index in +
@@ -263,7 +264,8 @@ def run_ours(args, rank, world, local):
                                f"occupancy from mesh (1.5 cm), 16-level hash grid T=2^19, MLPs 32-64-16 / 32-64-64-3",
                    "global_batch": world, "samples_per_frame": mean_samples, "parallelism": f"replicas x{world}",
                    "l2": "flushed (512 MiB write) between timed steps", "frames_per_s": args.steps * world / dev_t},
-        "roofline": {"bound": "hbm", "kernel": "deform_encode_kernel", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": "deform+encode stage (nearest_stage_kernel + map_encode_kernel)",
+                     "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": TRAFFIC_PER_FRAME if WIDTH == 512 else None,
                      "basis": f"{DEFORM_ENCODE_BYTES_PER_SAMPLE} B per sample (512 B hash gathers + stream in/out) "
                               f"x samples per frame / deform_encode stage time per frame (CUDA events); per frame = "

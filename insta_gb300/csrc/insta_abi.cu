@@ -573,7 +573,7 @@ struct WaveRun {
         CK(cudaMemsetAsync(counters + 2, 0, 4, ctx->stream));
         { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_march(W, ctx->stream)); }
         { Stage st(ctx, INSTA_STAGE_SORT, 4); CK(launch_sort_samples(W, ctx->stream)); }
-        { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 1); CK(launch_deform_encode(W, ctx->stream)); }
+        { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 2); CK(launch_deform_encode(W, ctx->stream)); }
         { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream)); }
         { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }
         cur ^= 1;

@@ -73,7 +73,7 @@ struct WaveArgs {
     uint32_t* n_round;          // samples produced this round, per alive ray
     uint32_t* sample_index;     // [steps][n_alive]: stream position of sample k of ray r
     uint32_t* sample_ray;       // per sample (march order): ray slot | step k << kStepShift
-    uint32_t* sample_key;       // per sample (march order): request << cell_bits | cell
+    uint32_t* sample_key;       // per sample: the sort key (march order), then the nearest triangle (sorted order)
     uint32_t* sample_order;     // sorted (padded) position -> march-order sample, kNoSample for padding
     uint32_t* sort_bins;        // n_reqs << cell_bits counters, then cursors
     uint32_t* sort_block_sums;  // per kSortBlock bins, then their exclusive offsets

@@ -3,8 +3,9 @@
 //   march_kernel          per alive ray, up to STEPS samples through the occupancy grid; a warp's
 //                         samples are written step-major so 32 neighbouring rays' k-th samples sit
 //                         together in the compacted sample stream
-//   deform_encode_kernel  per sample: warp-cooperative nearest triangle, deformed->canonical map,
-//                         hash encode + SH written as ready-made tensor-core operand tiles
+//   nearest_stage_kernel  per 32 sorted samples: warp-cooperative nearest triangle
+//   map_encode_kernel     per sample: deformed->canonical map, hash encode + SH written as
+//                         ready-made tensor-core operand tiles
 //   mlp_kernel            density + colour MLPs on 128-sample tiles (tcgen05, TMEM accumulators)
 //   composite_kernel      front-to-back compositing, early termination, shading, compaction
 // Ray lists and counts stay on the device; the host only decides when to stop issuing rounds.
@@ -395,34 +396,58 @@ __global__ void __launch_bounds__(256) sort_place_kernel(const __grid_constant__
     }
 }
 
-// One thread per sample, in spatially sorted order: the warp hook (src/core.cu:470-519) on
-// warp_position(pos) / warp_direction(dir), then the hash encode and SH written as tensor-core
-// operand rows at the sample's sorted position.  A warp's 32 samples share a few grid cells, so
-// the cooperative BVH walk visits a small union of nodes.
-__global__ void __launch_bounds__(256, 4) deform_encode_kernel(const __grid_constant__ WaveArgs A) {
+// The deform + encode stage, two kernels over the spatially sorted stream (split so that each
+// gets the registers and occupancy it needs):
+//   nearest_stage_kernel  a warp per 32 consecutive samples: the warp-cooperative nearest-triangle
+//                         walk (the samples share a few grid cells, so the union of visited nodes
+//                         is small); the triangle id of each sample goes to sample_key[position]
+//   map_encode_kernel     a thread per sample: the warp hook (src/core.cu:470-519) on
+//                         warp_position(pos) / warp_direction(dir) with that triangle, then the
+//                         hash encode and SH written as tensor-core operand rows at the sample's
+//                         sorted position
+__global__ void __launch_bounds__(256, 4) nearest_stage_kernel(const __grid_constant__ WaveArgs A) {
     __shared__ WarpScratch wscratch[8];
     const uint32_t n = *A.n_samples_padded;
-    const uint32_t n_alive = *A.n_alive_in;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
-    // warps step through the stream in lockstep chunks of 32 so every lane joins the cooperative
-    // query; runs are padded to 128 per request, so a chunk never mixes requests
     for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32u; base < n; base += n_warps * 32u) {
-        const uint32_t s = base + lane;   // position in sorted order: tile row and output slot
+        const uint32_t s = base + lane;
         const uint32_t m = A.sample_order[s];
         const bool valid = m != kNoSample;
         const uint32_t any = __ballot_sync(0xffffffffu, valid);
         if (!any) continue;
-        uint32_t rk = 0, req = 0;
-        float4 smp = make_float4(0.5f, 0.5f, 0.5f, 0.f), rb = make_float4(0.f, 0.f, 1.f, 0.f);
+        uint32_t req = 0;
+        float4 smp = make_float4(0.5f, 0.5f, 0.5f, 0.f);
         if (valid) {
-            rk = A.sample_ray[m];
+            const uint32_t rk = A.sample_ray[m];
             smp = A.samples[m];
-            rb = A.rays_in.b[rk & kRayMask];
             req = __float_as_uint(A.rays_in.d[rk & kRayMask].w);
-            A.sample_index[(size_t)(rk >> kStepShift) * n_alive + (rk & kRayMask)] = s;
         }
         req = __shfl_sync(0xffffffffu, req, __ffs(any) - 1);
+        const ReqView& R = A.reqs[req];
+        const RenderView& rv = R.rv;
+        const float pp[3] = {smp.x, smp.y, smp.z};
+        float cw[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) cw[k] = __fdiv_rn(__fsub_rn(pp[k], rv.train_min[k]), __fsub_rn(rv.train_max[k], rv.train_min[k]));
+        const V3 p = v3(cw[0], cw[1], cw[2]);
+        const bool in_box = valid && box_contains(R.dv.aabb_min, R.dv.aabb_max, p);
+        Nearest q = nearest_warp(R.fr, p, in_box, wscratch[warp], A.err);
+        if (valid) A.sample_key[s] = in_box ? (uint32_t)q.id : 0xfffffffeu;
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) map_encode_kernel(const __grid_constant__ WaveArgs A) {
+    const uint32_t n = *A.n_samples_padded;
+    const uint32_t n_alive = *A.n_alive_in;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const uint32_t m = A.sample_order[s];
+        if (m == kNoSample) continue;
+        const uint32_t rk = A.sample_ray[m];
+        const float4 smp = A.samples[m];
+        const float4 rb = A.rays_in.b[rk & kRayMask];
+        const uint32_t req = __float_as_uint(A.rays_in.d[rk & kRayMask].w);
+        A.sample_index[(size_t)(rk >> kStepShift) * n_alive + (rk & kRayMask)] = s;
         const ReqView& R = A.reqs[req];
         const RenderView& rv = R.rv;
         float cw[3], dw[3], dp[3];
@@ -436,20 +461,17 @@ __global__ void __launch_bounds__(256, 4) deform_encode_kernel(const __grid_cons
         float cpos[3] = {cw[0], cw[1], cw[2]}, cdir[3] = {dw[0], dw[1], dw[2]};
         uint32_t mask = 7u;
         const V3 p = v3(cw[0], cw[1], cw[2]);
-        const bool in_box = valid && box_contains(R.dv.aabb_min, R.dv.aabb_max, p);
-        Nearest q = nearest_warp(R.fr, p, in_box, wscratch[warp], A.err);
-        if (in_box) {
-            if (q.id >= 0) map_to_canonical(R.dv, R.fr.frames, (uint32_t)q.id, p, dw, cpos, cdir, &mask);
+        const uint32_t id = A.sample_key[s];
+        if (id != 0xfffffffeu) {
+            if ((int32_t)id >= 0) map_to_canonical(R.dv, R.fr.frames, id, p, dw, cpos, cdir, &mask);
             else atomicOr(A.err, INSTA_DEVERR_NO_TRI);
         }
-        if (valid) {
-            uint8_t* rec = A.tiles + (size_t)(s >> 7) * A.tile_bytes;
-            encode_sample(A.fv, R.table, R.extra, mask, cpos, cdir, rec, s & 127u, A.k_in);
-            const V3 cam_fwd = v3(rv.cam[2], rv.cam[6], rv.cam[10]);
-            const V3 cam_pos = v3(rv.cam[3], rv.cam[7], rv.cam[11]);
-            const V3 dv = v3(__fsub_rn(dp[0], cam_pos.x), __fsub_rn(dp[1], cam_pos.y), __fsub_rn(dp[2], cam_pos.z));
-            A.aux[s] = make_float2(smp.w, dot_rn(cam_fwd, dv));
-        }
+        uint8_t* rec = A.tiles + (size_t)(s >> 7) * A.tile_bytes;
+        encode_sample(A.fv, R.table, R.extra, mask, cpos, cdir, rec, s & 127u, A.k_in);
+        const V3 cam_fwd = v3(rv.cam[2], rv.cam[6], rv.cam[10]);
+        const V3 cam_pos = v3(rv.cam[3], rv.cam[7], rv.cam[11]);
+        const V3 dv = v3(__fsub_rn(dp[0], cam_pos.x), __fsub_rn(dp[1], cam_pos.y), __fsub_rn(dp[2], cam_pos.z));
+        A.aux[s] = make_float2(smp.w, dot_rn(cam_fwd, dv));
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(A.sample_counter, (unsigned long long)*A.n_samples_round);
 }
@@ -766,7 +788,8 @@ cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_deform_encode(const WaveArgs& a, cudaStream_t s) {
-    deform_encode_kernel<<<sm_count() * 16, 256, 0, s>>>(a);
+    nearest_stage_kernel<<<sm_count() * 16, 256, 0, s>>>(a);
+    map_encode_kernel<<<sm_count() * 16, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
