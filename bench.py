@@ -161,6 +161,16 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def combine_ranks(dist, dev_t, e2e_t, samples, e2e_samples, device):
+    """Replicas: the job's time is the slowest rank's (max), its work the sum over ranks."""
+    import torch
+    t = torch.tensor([dev_t, e2e_t, float(samples), float(e2e_samples)], dtype=torch.float64, device=device)
+    times, work = t[:2].clone(), t[2:].clone()
+    dist.all_reduce(times, op=dist.ReduceOp.MAX)
+    dist.all_reduce(work, op=dist.ReduceOp.SUM)
+    return float(times[0]), float(times[1]), float(work[0]), float(work[1])
+
+
 def run_ours(args, rank, world, local):
     import torch
     from insta_gb300 import abi
@@ -234,11 +244,7 @@ def run_ours(args, rank, world, local):
 
     dev_t = sum(step_ms) / 1000.0
     if dist:
-        t = torch.tensor([dev_t, e2e_t, float(total_samples), float(e2e_samples)], dtype=torch.float64, device="cuda")
-        mx = t.clone()
-        dist.all_reduce(mx[:2], op=dist.ReduceOp.MAX)
-        dist.all_reduce(mx[2:], op=dist.ReduceOp.SUM)
-        dev_t, e2e_t, total_samples, e2e_samples = [float(x) for x in mx.tolist()]
+        dev_t, e2e_t, total_samples, e2e_samples = combine_ranks(dist, dev_t, e2e_t, total_samples, e2e_samples, "cuda")
     if rank != 0:
         if dist:
             dist.destroy_process_group()
