@@ -24,10 +24,11 @@ struct Nearest {
 
 // Point-box squared distance for pruning only: fused multiply-adds are fine here because the
 // prune limit carries a relative slack far larger than any rounding difference.
+// The offset to the box is p minus p clamped into the box (zero inside).
 __device__ __forceinline__ float box_dist_fast(float mnx, float mny, float mnz, float mxx, float mxy, float mxz, V3 p) {
-    const float dx = fmaxf(fmaxf(mnx - p.x, p.x - mxx), 0.f);
-    const float dy = fmaxf(fmaxf(mny - p.y, p.y - mxy), 0.f);
-    const float dz = fmaxf(fmaxf(mnz - p.z, p.z - mxz), 0.f);
+    const float dx = p.x - fminf(fmaxf(p.x, mnx), mxx);
+    const float dy = p.y - fminf(fmaxf(p.y, mny), mxy);
+    const float dz = p.z - fminf(fmaxf(p.z, mnz), mxz);
     return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
@@ -148,10 +149,11 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
     __syncwarp();
     dstack[0] = active ? 0.f : INF;
     sp = 1;
+    float lim = prune_limit(best);   // changes only when a flush lowers best
     while (sp > 0) {
         --sp;
         const uint32_t ref = ws.stack[sp];
-        const bool need = dstack[sp] <= prune_limit(best);
+        const bool need = dstack[sp] <= lim;
         const uint32_t nm = __ballot_sync(0xffffffffu, need);
         if (!nm) continue;
         if (ref & INSTA_LEAF_BIT) {
@@ -162,7 +164,11 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
                 for (uint32_t i = 0; i < count; ++i) ws.queue[qlen + i * nl + rank] = ((first + i) << 5) | lane;
             qlen += count * nl;
             __syncwarp();
-            while (qlen >= 32u) flush_tests(fr, ws, p, 32u, qlen, best, bid);
+            if (qlen >= 32u) {
+                do flush_tests(fr, ws, p, 32u, qlen, best, bid);
+                while (qlen >= 32u);
+                lim = prune_limit(best);
+            }
             continue;
         }
         const float4* nd = fr.nodes + (size_t)ref * 7;
@@ -175,7 +181,6 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
         cd[1] = box_dist_fast(mnx.y, mny.y, mnz.y, mxx.y, mxy.y, mxz.y, p);
         cd[2] = box_dist_fast(mnx.z, mny.z, mnz.z, mxx.z, mxy.z, mxz.z, p);
         cd[3] = box_dist_fast(mnx.w, mny.w, mnz.w, mxx.w, mxy.w, mxz.w, p);
-        const float lim = prune_limit(best);
         // per child: the warp's smallest distance among lanes that need it (bits order like floats >= 0)
         uint32_t key[4];
 #pragma unroll
@@ -184,15 +189,19 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
             key[i] = __reduce_min_sync(0xffffffffu, want ? __float_as_uint(cd[i]) : 0xffffffffu);
         }
         // sort the children farthest-first (keys are warp-uniform; every index is static, so the
-        // tuples stay in registers) and push the needed ones: the warp pops the nearest next
+        // tuples stay in registers) and push the needed ones: the warp pops the nearest next.
+        // With at most one child wanted there is nothing to order.
+        const int wanted = (key[0] != 0xffffffffu) + (key[1] != 0xffffffffu) + (key[2] != 0xffffffffu) + (key[3] != 0xffffffffu);
+        if (wanted > 1) {
 #define INSTA_CASK(x, y)                                                                  \
     if (key[x] < key[y]) {                                                                \
         uint32_t tk = key[x]; key[x] = key[y]; key[y] = tk;                               \
         uint32_t tc = ci[x]; ci[x] = ci[y]; ci[y] = tc;                                   \
         float td = cd[x]; cd[x] = cd[y]; cd[y] = td;                                      \
     }
-        INSTA_CASK(0, 2) INSTA_CASK(1, 3) INSTA_CASK(0, 1) INSTA_CASK(2, 3) INSTA_CASK(1, 2)
+            INSTA_CASK(0, 2) INSTA_CASK(1, 3) INSTA_CASK(0, 1) INSTA_CASK(2, 3) INSTA_CASK(1, 2)
 #undef INSTA_CASK
+        }
         __syncwarp();   // every lane has read the popped entry before lane 0 overwrites it
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
