@@ -665,7 +665,7 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
 }
 
 // Device buffers and view of one uploaded frame; copies its vertices in.
-Frame& prepare_frame(insta_ctx* ctx, Avatar& a, int frame, const float* verts) {
+Frame& prepare_frame(insta_ctx* ctx, Avatar& a, int frame, const float* verts, cudaStream_t stream = nullptr) {
     Frame& f = a.frames[frame];
     // an LBVH with leaves of <= 2 triangles has at most F - 1 internal nodes
     const int max_nodes = std::max(1, a.F);
@@ -673,7 +673,7 @@ Frame& prepare_frame(insta_ctx* ctx, Avatar& a, int frame, const float* verts) {
     ctx->alloc(f.frames, (size_t)a.F * sizeof(TriFrame));
     ctx->alloc(f.leaf_tris, (size_t)a.F * INSTA_TRI_F4 * 16);
     ctx->alloc(f.nodes, (size_t)max_nodes * 112);
-    host_copy(f.verts.p, verts, (size_t)a.V * 12, ctx->stream);
+    host_copy(f.verts.p, verts, (size_t)a.V * 12, stream ? stream : ctx->stream);
     f.view.leaf_tris = static_cast<const float4*>(f.leaf_tris.p);
     f.view.nodes = static_cast<const float4*>(f.nodes.p);
     f.view.frames = static_cast<const TriFrame*>(f.frames.p);
@@ -1237,6 +1237,7 @@ struct ServerReq {
     int state = INSTA_REQ_QUEUED;
     int slot = -1;
     bool cancel = false;
+    bool started = false;   // its rays are in the wavefront
     std::string error;
     Clock::time_point t_submit, t_start, t_done;
 };
@@ -1264,6 +1265,11 @@ struct insta_server {
     const Field* layout = nullptr;
     uint64_t inflight_px = 0;
     int inflight = 0;
+    // admitted requests' frames are built on a second stream while the current round runs;
+    // their rays start at the next round, after `ev_ready`
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_ready = nullptr;
+    std::vector<std::shared_ptr<ServerReq>> ready;
 
     void finish(const std::shared_ptr<ServerReq>& r, int state, const std::string& err = std::string()) {
         std::lock_guard<std::mutex> lk(mu);
@@ -1274,10 +1280,11 @@ struct insta_server {
         cv_done.notify_all();
     }
 
-    // Upload the admitted requests' frames, build their occupancy, fill their slots and start
-    // their rays.  A request that cannot run is finished as failed without disturbing the others.
-    void admit(std::vector<std::shared_ptr<ServerReq>>& batch) {
-        std::vector<uint32_t> slots, tiles;
+    // Upload the admitted requests' frames and build their LBVHs (one launch per avatar, a CTA per
+    // frame) and occupancy on the side stream, and fill their slots.  A request that cannot run
+    // is finished as failed without disturbing the others.
+    void build(std::vector<std::shared_ptr<ServerReq>>& batch) {
+        std::map<int, std::vector<std::shared_ptr<ServerReq>>> by_avatar;
         for (auto& r : batch) {
             try {
                 Avatar& a = ctx->avatar(r->desc.avatar);
@@ -1285,26 +1292,49 @@ struct insta_server {
                 if (!layout) {
                     layout = &a.field;
                     run.setup(ctx, a.field, cfg.max_inflight, cfg.max_inflight_pixels, true);
-                    CK(cudaMemsetAsync(run.W.req_alive, 0, (size_t)cfg.max_inflight * 4, ctx->stream));
                 } else if (!same_field_layout(*layout, a.field)) {
                     fail(INSTA_ERR_UNSUPPORTED, "the server's requests must share one field layout");
                 }
+                if (r->verts.empty()) {
+                    Frame& f = get_frame(a, r->desc.frame);
+                    if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", r->desc.frame);
+                }
+                by_avatar[r->desc.avatar].push_back(r);
+            } catch (const Failure& e) {
+                release(r);
+                finish(r, INSTA_REQ_FAILED, e.what());
+            }
+        }
+        bool any = false;
+        for (auto& kv : by_avatar) {
+            Avatar& a = ctx->avatar(kv.first);
+            std::vector<FrameView> fviews;
+            std::vector<const float*> dverts;
+            for (auto& r : kv.second) {
+                if (r->verts.empty()) continue;
+                Frame& f = prepare_frame(ctx, a, kServerFrameBase + r->slot, r->verts.data(), side);
+                ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
+                fviews.push_back(f.view);
+                dverts.push_back((const float*)f.verts.p);
+            }
+            if (!fviews.empty()) {
+                const int n = (int)fviews.size();
+                ctx->alloc(ctx->bvh_scratch, (size_t)n * bvh_scratch_bytes(a.F));
+                ctx->alloc(ctx->frame_jobs, frame_batch_table_bytes(n));
+                CK(launch_frames_batch(n, a.F, fviews.data(), dverts.data(), (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
+                                       (const float*)a.canon_area.p, ctx->bvh_scratch.p, ctx->frame_jobs.p, side));
+                ctx->launches += 3;
+            }
+            for (auto& r : kv.second) {
                 int frame = r->desc.frame;
                 if (!r->verts.empty()) {
                     frame = kServerFrameBase + r->slot;
-                    ctx->alloc(ctx->bvh_scratch, bvh_scratch_bytes(a.F));
-                    Frame& f = prepare_frame(ctx, a, frame, r->verts.data());
-                    { Stage st(ctx, INSTA_STAGE_FRAME, 3);
-                      CK(launch_tri_frames(a.F, (const float*)f.verts.p, (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
-                                           (const float*)a.canon_area.p, nullptr, (TriFrame*)f.frames.p, 1, ctx->stream));
-                      CK(launch_bvh_build(f.view, (const float*)f.verts.p, (const int32_t*)a.faces.p, ctx->bvh_scratch.p, ctx->stream)); }
-                    ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
-                    { Stage st(ctx, INSTA_STAGE_OCCUPANCY, 1);
-                      CK(launch_occupancy(f.view, cfg.occupancy_radius, (uint8_t*)f.bitfield.p, ctx->err_dev, ctx->stream)); }
+                    Frame& f = get_frame(a, frame);
+                    CK(launch_occupancy(f.view, cfg.occupancy_radius, (uint8_t*)f.bitfield.p, ctx->err_dev, side));
+                    ctx->launches += 1;
                     f.has_occupancy = true;
                 }
                 Frame& f = get_frame(a, frame);
-                if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", frame);
                 insta_render_desc d = r->desc;
                 d.frame = frame;
                 ReqView v = request_view(ctx, d, a, f);
@@ -1323,27 +1353,38 @@ struct insta_server {
                     std::vector<float> e(n_extra, 0.f);
                     if (!r->extra.empty()) std::memcpy(e.data(), r->extra.data(), n_extra * 4);
                     float* dst = (float*)slot_extra.p + (size_t)s * n_extra;
-                    CK(cudaMemcpyAsync(dst, e.data(), n_extra * 4, cudaMemcpyHostToDevice, ctx->stream));
-                    CK(cudaStreamSynchronize(ctx->stream));
+                    // pageable source: staged before the call returns
+                    CK(cudaMemcpyAsync(dst, e.data(), n_extra * 4, cudaMemcpyHostToDevice, side));
                     v.extra = dst;
                 }
                 views[s] = v;
-                CK(cudaMemsetAsync(run.W.req_alive + s, 0, 4, ctx->stream));
-                slots.push_back(s);
-                tiles.push_back(v.tiles);
-                {
-                    std::lock_guard<std::mutex> lk(mu);
-                    r->state = INSTA_REQ_RUNNING;
-                    r->t_start = Clock::now();
-                }
-            } catch (const Failure& e) {
-                release(r);
-                finish(r, INSTA_REQ_FAILED, e.what());
+                ready.push_back(r);
+                any = true;
             }
         }
-        if (slots.empty()) return;
+        if (any) CK(cudaEventRecord(ev_ready, side));
+    }
+
+    // Start the rays of the requests built in the previous iteration (after their build).
+    void start_ready() {
+        if (ready.empty()) return;
+        CK(cudaStreamWaitEvent(ctx->stream, ev_ready, 0));
+        std::vector<uint32_t> slots, tiles;
+        for (auto& r : ready) {
+            const uint32_t s = (uint32_t)r->slot;
+            CK(cudaMemsetAsync(run.W.req_alive + s, 0, 4, ctx->stream));
+            slots.push_back(s);
+            tiles.push_back(views[s].tiles);
+        }
         run.upload_table(views.data());
         run.start(slots.data(), tiles.data(), (uint32_t)slots.size(), false);
+        std::lock_guard<std::mutex> lk(mu);
+        for (auto& r : ready) {
+            r->started = true;
+            r->state = INSTA_REQ_RUNNING;
+            r->t_start = Clock::now();
+        }
+        ready.clear();
     }
 
     void release(const std::shared_ptr<ServerReq>& r) {
@@ -1358,7 +1399,7 @@ struct insta_server {
     void collect() {
         for (size_t s = 0; s < slot_req.size(); ++s) {
             auto r = slot_req[s];
-            if (!r || r->state != INSTA_REQ_RUNNING || ctx->host_alive[s] != 0) continue;
+            if (!r || !r->started || r->state != INSTA_REQ_RUNNING || ctx->host_alive[s] != 0) continue;
             if (r->host_out && !r->cancel) {
                 const size_t px = (size_t)r->desc.width * r->desc.height;
                 CK(cudaMemcpyAsync(r->out_rgba, slot_rgba[s].p, px * 16, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1373,6 +1414,8 @@ struct insta_server {
     void loop() {
         cudaSetDevice(ctx->device);
         try {
+            CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming));
             ctx->alloc(slot_extra, (size_t)cfg.max_inflight * 64 * 4);
             for (;;) {
                 std::vector<std::shared_ptr<ServerReq>> batch;
@@ -1403,8 +1446,11 @@ struct insta_server {
                         batch.push_back(r);
                     }
                 }
-                if (!batch.empty()) admit(batch);
+                const bool had_ready = !ready.empty();
+                start_ready();
+                if (!batch.empty()) build(batch);
                 if (inflight == 0) continue;
+                if (run.n_alive == 0 && !had_ready) continue;   // only builds in flight: start them next
                 run.round();
                 ++rounds;
                 collect();
@@ -1457,6 +1503,8 @@ int insta_server_destroy(insta_server* s) {
     }
     s->cv_work.notify_all();
     if (s->worker.joinable()) s->worker.join();   // in-flight requests finish first
+    if (s->side) { cudaStreamSynchronize(s->side); cudaStreamDestroy(s->side); }
+    if (s->ev_ready) cudaEventDestroy(s->ev_ready);
     for (auto& b : s->slot_rgba) s->ctx->release(b);
     for (auto& b : s->slot_depth) s->ctx->release(b);
     s->ctx->release(s->slot_extra);
