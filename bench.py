@@ -191,19 +191,37 @@ def run_ours(args, rank, world, local):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     reqs = [ctx.render_desc(0, 0, WIDTH, HEIGHT, c[1], c[0], cone_angle=CONE) for c in cams]
 
-    def step(k):
-        ctx.frame_upload(0, 0, frames_dev[k % len(frames_dev)])
-        ctx.occupancy_from_mesh(0, 0, RADIUS)
-        ctx.render(reqs[k % len(reqs)], rgba, depth)
+    # Double-buffered frames: step k renders frame slot k % 2 (uploaded during step k - 1) and
+    # uploads the next frame (LBVH rebuild + occupancy) into the other slot on the library's side
+    # stream, where it overlaps this render.  Every step still does one upload and one render.
+    counter = {"k": 0}
+
+    def upload_next(k, src):
+        ctx.frame_upload_async(0, (k + 1) % 2, src[(k + 1) % len(src)], RADIUS)
+
+    def step(_k, src=None):
+        k = counter["k"]
+        counter["k"] += 1
+        src = src if src is not None else frames_dev
+        if k == 0:   # prime the first slot
+            ctx.frame_upload_async(0, 0, src[0], RADIUS)
+        upload_next(k, src)
+        req = reqs[k % len(reqs)]
+        req.frame = k % 2
+        ctx.render(req, rgba, depth)
+        # the step ends when both its render and the next frame's upload are done, so the timed
+        # interval holds the work of both streams
+        ctx.frame_wait(0, (k + 1) % 2)
+        return k
 
     with torch.cuda.stream(stream):
         for k in range(args.warmup):
             step(k)
         ctx.sync()
-        samples_per_frame = []
+        samples_per_frame = [0] * len(reqs)
         for k in range(len(reqs)):
-            step(k)
-            samples_per_frame.append(ctx.render_samples())
+            kk = step(k)
+            samples_per_frame[kk % len(reqs)] = ctx.render_samples()
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -218,9 +236,9 @@ def run_ours(args, rank, world, local):
             for k in range(args.steps):
                 flush.zero_()
                 ev[k][0].record(stream)
-                step(k)
+                kk = step(k)
                 ev[k][1].record(stream)
-                total_samples += samples_per_frame[k % len(reqs)]
+                total_samples += samples_per_frame[kk % len(reqs)]
             stream.synchronize()
             t_wall = time.perf_counter() - t_wall0
         step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -235,11 +253,16 @@ def run_ours(args, rank, world, local):
         e2e_samples = 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        host_np = [f.numpy() for f in host_frames]
         for k in range(args.steps):
-            ctx.frame_upload(0, 0, host_frames[k % len(host_frames)].numpy())
-            ctx.occupancy_from_mesh(0, 0, RADIUS)
-            ctx.render(reqs[k % len(reqs)], host_rgba.numpy(), host_depth.numpy())
-            e2e_samples += samples_per_frame[k % len(reqs)]
+            kk = counter["k"]
+            counter["k"] += 1
+            upload_next(kk, host_np)
+            req = reqs[kk % len(reqs)]
+            req.frame = kk % 2
+            ctx.render(req, host_rgba.numpy(), host_depth.numpy())
+            ctx.frame_wait(0, (kk + 1) % 2)
+            e2e_samples += samples_per_frame[kk % len(reqs)]
         e2e_t = time.perf_counter() - t0
 
     dev_t = sum(step_ms) / 1000.0

@@ -140,6 +140,16 @@ int insta_frame_upload(insta_ctx* ctx, int avatar, int frame, const float* verts
  * the per-triangle frames of all of them in one launch and one LBVH build per CTA, so a batch
  * of expressions builds in about the time of one.  Same result as n insta_frame_upload calls. */
 int insta_frame_upload_batch(insta_ctx* ctx, int avatar, const int32_t* frames, int n, const float* const* verts);
+/* The same upload (and, with occupancy_radius > 0, insta_occupancy_from_mesh) enqueued on a second
+ * stream of the context and returned at once: it starts after the work already queued on the
+ * context's stream and runs concurrently with later work; every later call that reads the frame
+ * waits for it.  Double-buffered frames (upload frame k+1 while frame k renders) overlap the
+ * LBVH build with rendering.  Host verts must stay unchanged until that later call when they
+ * are in pinned memory (pageable memory is copied before the call returns).  Its kernels are
+ * counted in insta_stats but not timed. */
+int insta_frame_upload_async(insta_ctx* ctx, int avatar, int frame, const float* verts, double occupancy_radius);
+/* Order the context's stream after the frame's pending asynchronous upload (no host wait). */
+int insta_frame_wait(insta_ctx* ctx, int avatar, int frame);
 int insta_frame_release(insta_ctx* ctx, int avatar, int frame);
 
 /* -- occupancy ---------------------------------------------------------------- */

@@ -20,7 +20,8 @@ EXPORTS = [
     "insta_ctx_create", "insta_ctx_destroy", "insta_last_error", "insta_sync", "insta_memory_used",
     "insta_stats_enable", "insta_stats_read",
     "insta_canonical_set", "insta_avatar_set_boxes", "insta_avatar_set_flags", "insta_frame_upload",
-    "insta_frame_upload_batch", "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
+    "insta_frame_upload_batch", "insta_frame_upload_async", "insta_frame_wait",
+    "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_density_grid_load",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
     "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_batch",
@@ -90,6 +91,8 @@ def load(path: Path | None = None):
             "insta_avatar_set_flags": [vp, C.c_int, u32],
             "insta_frame_upload": [vp, C.c_int, C.c_int, vp],
             "insta_frame_upload_batch": [vp, C.c_int, vp, C.c_int, C.POINTER(vp)],
+            "insta_frame_upload_async": [vp, C.c_int, C.c_int, vp, C.c_double],
+            "insta_frame_wait": [vp, C.c_int, C.c_int],
             "insta_frame_release": [vp, C.c_int, C.c_int],
             "insta_occupancy_from_mesh": [vp, C.c_int, C.c_int, C.c_double],
             "insta_occupancy_set": [vp, C.c_int, C.c_int, vp],
@@ -229,6 +232,14 @@ class Context:
         ids = np.ascontiguousarray(frames, dtype=np.int32)
         ptrs = (C.c_void_p * len(vs))(*[_addr(v).value for v in vs])
         self._check(self.lib.insta_frame_upload_batch(self.h, avatar, _addr(ids), len(vs), ptrs))
+
+    def frame_upload_async(self, avatar, frame, verts, occupancy_radius=0.0):
+        v = verts if hasattr(verts, "data_ptr") else np.ascontiguousarray(verts, dtype=np.float32)
+        self._keep_async = v   # the buffer must outlive the copy when it is pinned or on the device
+        self._check(self.lib.insta_frame_upload_async(self.h, avatar, frame, _addr(v), float(occupancy_radius)))
+
+    def frame_wait(self, avatar, frame):
+        self._check(self.lib.insta_frame_wait(self.h, avatar, frame))
 
     def frame_release(self, avatar, frame):
         self._check(self.lib.insta_frame_release(self.h, avatar, frame))

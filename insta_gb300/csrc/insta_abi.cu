@@ -58,6 +58,8 @@ struct Frame {
     DevBuf verts, frames, leaf_tris, nodes, bitfield;
     FrameView view{};
     bool has_occupancy = false;
+    cudaEvent_t ready = nullptr;   // insta_frame_upload_async: recorded on the side stream
+    bool pending = false;          // the main stream has not yet been made to wait for `ready`
 };
 
 struct Field {
@@ -101,7 +103,9 @@ struct insta_ctx {
     uint32_t* err_dev = nullptr;
     uint32_t* ray_counter = nullptr;
     unsigned long long* sample_counter = nullptr;
-    DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs, density_scratch, density_stage;
+    DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs, density_scratch, density_stage, side_scratch;
+    cudaStream_t side = nullptr;        // asynchronous frame uploads
+    cudaEvent_t side_mark = nullptr;    // orders a side upload after the main stream's earlier work
     Wave wave;
     uint32_t* host_counters = nullptr;   // pinned: alive-ray counts read between rounds
     uint32_t* host_alive = nullptr;      // pinned: alive rays per request slot (serving)
@@ -364,6 +368,25 @@ Frame& get_frame(Avatar& a, int frame) {
     return it->second;
 }
 
+// Make the context's stream wait for an asynchronous upload of the frame, if one is pending.
+void wait_frame(insta_ctx* ctx, Frame& f) {
+    if (!f.pending) return;
+    CK(cudaStreamWaitEvent(ctx->stream, f.ready, 0));
+    f.pending = false;
+}
+
+// The frame, with the context's stream ordered after its pending asynchronous upload.
+Frame& use_frame(insta_ctx* ctx, Avatar& a, int frame) {
+    Frame& f = get_frame(a, frame);
+    wait_frame(ctx, f);
+    return f;
+}
+
+// Every frame of the avatar (work that picks frames per record).
+void wait_all_frames(insta_ctx* ctx, Avatar& a) {
+    for (auto& kv : a.frames) wait_frame(ctx, kv.second);
+}
+
 DeformView deform_view(const Avatar& a) {
     DeformView dv{};
     dv.canon = static_cast<const TriFrame*>(a.canon_frames.p);
@@ -597,7 +620,7 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
         if (!out_rgba[i] || !out_depth[i]) fail(INSTA_ERR_INVALID_ARG, "null output buffers for request %d", i);
         Avatar& a = ctx->avatar(r->avatar);
         if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", r->avatar);
-        Frame& f = get_frame(a, r->frame);
+        Frame& f = use_frame(ctx, a, r->frame);
         if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", r->frame);
         if (!field0) field0 = &a.field;
         else if (!same_field_layout(*field0, a.field))
@@ -667,6 +690,7 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
 // Device buffers and view of one uploaded frame; copies its vertices in.
 Frame& prepare_frame(insta_ctx* ctx, Avatar& a, int frame, const float* verts, cudaStream_t stream = nullptr) {
     Frame& f = a.frames[frame];
+    if (!stream || stream == ctx->stream) wait_frame(ctx, f);   // an async upload of it still in flight
     // an LBVH with leaves of <= 2 triangles has at most F - 1 internal nodes
     const int max_nodes = std::max(1, a.F);
     ctx->alloc(f.verts, (size_t)a.V * 12);
@@ -736,6 +760,15 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     if (!ctx) return INSTA_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->side) {
+        cudaStreamSynchronize(ctx->side);
+        cudaStreamDestroy(ctx->side);
+    }
+    if (ctx->side_mark) cudaEventDestroy(ctx->side_mark);
+    ctx->release(ctx->side_scratch);
+    for (auto& kv : ctx->avatars)
+        for (auto& f : kv.second->frames)
+            if (f.second.ready) cudaEventDestroy(f.second.ready);
     for (auto& kv : ctx->avatars) {
         Avatar& a = *kv.second;
         for (DevBuf* b : {&a.faces, &a.mask, &a.adjacency, &a.canon_verts, &a.canon_area, &a.canon_frames, &a.frame_table,
@@ -873,12 +906,50 @@ int insta_frame_upload_batch(insta_ctx* ctx, int avatar, const int32_t* frames, 
     });
 }
 
+int insta_frame_upload_async(insta_ctx* ctx, int avatar, int frame, const float* verts, double occupancy_radius) {
+    return guarded(ctx, [&] {
+        Avatar& a = ctx->avatar(avatar);
+        if (!verts || frame < 0) fail(INSTA_ERR_INVALID_ARG, "bad frame upload");
+        if (occupancy_radius < 0.0) fail(INSTA_ERR_INVALID_ARG, "radius must be >= 0");
+        if (!ctx->side) {
+            CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&ctx->side_mark, cudaEventDisableTiming));
+        }
+        // after everything already queued on the context's stream (renders still reading this frame)
+        CK(cudaEventRecord(ctx->side_mark, ctx->stream));
+        CK(cudaStreamWaitEvent(ctx->side, ctx->side_mark, 0));
+        ctx->alloc(ctx->side_scratch, bvh_scratch_bytes(a.F));
+        Frame& f = prepare_frame(ctx, a, frame, verts, ctx->side);
+        CK(launch_tri_frames(a.F, (const float*)f.verts.p, (const int32_t*)a.faces.p, (const uint32_t*)a.mask.p,
+                             (const float*)a.canon_area.p, nullptr, (TriFrame*)f.frames.p, 1, ctx->side));
+        CK(launch_bvh_build(f.view, (const float*)f.verts.p, (const int32_t*)a.faces.p, ctx->side_scratch.p, ctx->side));
+        ctx->launches += 3;
+        if (occupancy_radius > 0.0) {
+            ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
+            CK(launch_occupancy(f.view, occupancy_radius, (uint8_t*)f.bitfield.p, ctx->err_dev, ctx->side));
+            ctx->launches += 1;
+            f.has_occupancy = true;
+        }
+        if (!f.ready) CK(cudaEventCreateWithFlags(&f.ready, cudaEventDisableTiming));
+        CK(cudaEventRecord(f.ready, ctx->side));
+        f.pending = true;
+    });
+}
+
+int insta_frame_wait(insta_ctx* ctx, int avatar, int frame) {
+    return guarded(ctx, [&] { use_frame(ctx, ctx->avatar(avatar), frame); });
+}
+
 int insta_frame_release(insta_ctx* ctx, int avatar, int frame) {
     return guarded(ctx, [&] {
         Avatar& a = ctx->avatar(avatar);
         auto it = a.frames.find(frame);
         if (it == a.frames.end()) return;
         CK(cudaStreamSynchronize(ctx->stream));
+        if (it->second.ready) {
+            CK(cudaEventSynchronize(it->second.ready));
+            cudaEventDestroy(it->second.ready);
+        }
         for (DevBuf* b : {&it->second.verts, &it->second.frames, &it->second.leaf_tris, &it->second.nodes, &it->second.bitfield})
             ctx->release(*b);
         a.frames.erase(it);
@@ -890,7 +961,7 @@ int insta_occupancy_from_mesh(insta_ctx* ctx, int avatar, int frame, double radi
     return guarded(ctx, [&] {
         if (!(radius > 0.0)) fail(INSTA_ERR_INVALID_ARG, "radius must be positive");
         Avatar& a = ctx->avatar(avatar);
-        Frame& f = get_frame(a, frame);
+        Frame& f = use_frame(ctx, a, frame);
         ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
         Stage st(ctx, INSTA_STAGE_OCCUPANCY, 1);
         CK(launch_occupancy(f.view, radius, (uint8_t*)f.bitfield.p, ctx->err_dev, ctx->stream));
@@ -901,7 +972,7 @@ int insta_occupancy_from_mesh(insta_ctx* ctx, int avatar, int frame, double radi
 int insta_occupancy_set(insta_ctx* ctx, int avatar, int frame, const uint8_t* bits) {
     return guarded(ctx, [&] {
         if (!bits) fail(INSTA_ERR_INVALID_ARG, "null bitfield");
-        Frame& f = get_frame(ctx->avatar(avatar), frame);
+        Frame& f = use_frame(ctx, ctx->avatar(avatar), frame);
         ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
         host_copy(f.bitfield.p, bits, (size_t)8 * GRID3 / 8, ctx->stream);
         f.has_occupancy = true;
@@ -912,7 +983,7 @@ int insta_density_grid_load(insta_ctx* ctx, int avatar, int frame, const void* g
     return guarded(ctx, [&] {
         if (!grid) fail(INSTA_ERR_INVALID_ARG, "null density grid");
         if (n_cascades < 1 || n_cascades > 8) fail(INSTA_ERR_INVALID_ARG, "n_cascades must be 1..8, got %u", n_cascades);
-        Frame& f = get_frame(ctx->avatar(avatar), frame);
+        Frame& f = use_frame(ctx, ctx->avatar(avatar), frame);
         ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
         ctx->alloc(ctx->density_scratch, density_scratch_bytes(n_cascades));
         const void* src = grid;
@@ -930,7 +1001,7 @@ int insta_density_grid_load(insta_ctx* ctx, int avatar, int frame, const void* g
 int insta_occupancy_get(insta_ctx* ctx, int avatar, int frame, uint8_t* bits) {
     return guarded(ctx, [&] {
         if (!bits) fail(INSTA_ERR_INVALID_ARG, "null bitfield");
-        Frame& f = get_frame(ctx->avatar(avatar), frame);
+        Frame& f = use_frame(ctx, ctx->avatar(avatar), frame);
         if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy", frame);
         host_copy(bits, f.bitfield.p, (size_t)8 * GRID3 / 8, ctx->stream);
         ctx->check_device();
@@ -944,7 +1015,7 @@ int insta_canonical_map(insta_ctx* ctx, int avatar, int frame, float* coords, ui
         Avatar& a = ctx->avatar(avatar);
         if (n == 0) return;
         refresh_frame_table(ctx, a);
-        if (frame >= 0) get_frame(a, frame);
+        if (frame >= 0) use_frame(ctx, a, frame); else wait_all_frames(ctx, a);
         Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
         CK(launch_canonical_map_coords((const FrameView*)a.frame_table.p, a.table_frames, deform_view(a), coords, stride, n_extra, n,
                                        frame, ctx->err_dev, ctx->stream));
@@ -964,9 +1035,10 @@ int insta_training_samples(insta_ctx* ctx, int avatar, int grid_frame, const flo
                               (const void*)numsteps, (const void*)counters})
             if (n_rays > 0 && !is_device_ptr(p)) fail(INSTA_ERR_INVALID_ARG, "insta_training_samples takes device pointers");
         Avatar& a = ctx->avatar(avatar);
-        Frame& g = get_frame(a, grid_frame);
+        Frame& g = use_frame(ctx, a, grid_frame);
         if (!g.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", grid_frame);
         refresh_frame_table(ctx, a);
+        wait_all_frames(ctx, a);   // the warp picks each record's frame
         CK(cudaMemsetAsync(counters, 0, 2 * sizeof(uint32_t), ctx->stream));
         if (n_rays == 0) return;
         TrainArgs T{};
@@ -987,7 +1059,7 @@ int insta_canonical_map_soa(insta_ctx* ctx, int avatar, int frame, const float* 
     return guarded(ctx, [&] {
         if (n < 0 || (n > 0 && (!pts || !out_idx || !out_canon))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
         Avatar& a = ctx->avatar(avatar);
-        Frame& f = get_frame(a, frame);
+        Frame& f = use_frame(ctx, a, frame);
         Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
         CK(launch_canonical_map_soa(f.view, deform_view(a), pts, n, out_idx, out_canon, ctx->err_dev, ctx->stream));
     });
@@ -1209,7 +1281,7 @@ int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out,
         check_request(req);
         if (max_out <= 0 || !out_t || !out_dt || !out_n) fail(INSTA_ERR_INVALID_ARG, "bad output buffers");
         Avatar& a = ctx->avatar(req->avatar);
-        Frame& f = get_frame(a, req->frame);
+        Frame& f = use_frame(ctx, a, req->frame);
         if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", req->frame);
         CK(launch_march_debug(render_view(a, *req), (const uint8_t*)f.bitfield.p, max_out, out_t, out_dt, out_n, ctx->stream));
     });

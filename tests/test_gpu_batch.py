@@ -147,3 +147,42 @@ def test_frame_upload_batch_equals_single(ctx):
         a, b = outs[20][k], outs[21][k]
         assert (a[0] == b[0]).all() and (a[1] == b[1]).all() and (a[2] == b[2]).all(), k
     assert outs[20][0][0].any()
+
+
+def test_frame_upload_async_double_buffered(ctx):
+    """Frames uploaded on the side stream while the previous frame renders give the same pixels as
+    synchronous uploads."""
+    from insta_gb300 import synthetic as S
+    av = S.make_avatar(6)
+    fc = S.FieldConfig()
+    params = S.field_params(fc, seed=6)
+    for aid in (30, 31):
+        ctx.canonical_set(aid, av.canonical, av.faces, av.mask)
+        ctx.params_load(aid, fc, params)
+    frames = [av.frame(av.frame_coeffs(k)) for k in range(5)]
+    W = H = 48
+    reqs = []
+    for k in range(5):
+        cam, focal = S.camera(-20.0 + 10 * k, width=W, height=H)
+        reqs.append((cam, focal))
+    ref = []
+    for k in range(5):
+        ctx.frame_upload(30, 0, frames[k])
+        ctx.occupancy_from_mesh(30, 0, 0.015)
+        r = ctx.render_desc(30, 0, W, H, reqs[k][1], reqs[k][0])
+        rgba = np.zeros((W * H, 4), np.float32)
+        depth = np.zeros(W * H, np.float32)
+        ctx.render(r, rgba, depth)
+        ref.append((rgba, depth))
+    got = []
+    ctx.frame_upload_async(31, 0, frames[0], 0.015)
+    outs = [(torch.zeros((W * H, 4), device="cuda"), torch.zeros(W * H, device="cuda")) for _ in range(5)]
+    for k in range(5):
+        if k + 1 < 5:
+            ctx.frame_upload_async(31, (k + 1) % 2, frames[k + 1], 0.015)
+        r = ctx.render_desc(31, k % 2, W, H, reqs[k][1], reqs[k][0])
+        ctx.render(r, outs[k][0], outs[k][1])
+    ctx.sync()
+    for k in range(5):
+        assert (outs[k][0].cpu().numpy() == ref[k][0]).all() and (outs[k][1].cpu().numpy() == ref[k][1]).all(), k
+    assert (ref[0][0][:, 3] > 0.05).sum() > 20
