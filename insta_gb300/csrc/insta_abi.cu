@@ -585,7 +585,9 @@ struct WaveRun {
     }
 
     // One round over all alive rays; afterwards n_alive (and host_alive per slot) are current.
-    void round() {
+    // Without read_back the host does not wait: n_alive stays an upper bound (rays only finish),
+    // and the next round's kernels take the count from the device.
+    void round(bool read_back = true) {
         const uint32_t steps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(kMaxSteps, round_cap / std::max(1u, n_alive)));
         W.steps = steps;
         W.rays_in = rays(cur);
@@ -600,7 +602,7 @@ struct WaveRun {
         { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream)); }
         { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }
         cur ^= 1;
-        n_alive = read_alive();
+        if (read_back) n_alive = read_alive();
     }
 };
 
@@ -673,7 +675,14 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
     // the first round's step count needs the alive count only when all pixels could not take
     // kMaxSteps samples each; otherwise the pixel count stands in for it (no host round trip)
     run.start(slots.data(), tiles.data(), (uint32_t)n, total_pix * kMaxSteps > run.round_cap);
-    for (uint32_t round = 0; run.n_alive > 0 && round < max_spr + 2; ++round) run.round();
+    // while every ray can take kMaxSteps samples per round, the first round is issued without a
+    // host read of its alive count (most frames finish in two rounds: one host wait, not two)
+    uint32_t round = 0;
+    if (total_pix * kMaxSteps <= run.round_cap && run.n_alive > 0) {
+        run.round(false);
+        ++round;
+    }
+    for (; run.n_alive > 0 && round < max_spr + 2; ++round) run.round();
     if (host_pix) {
         uint64_t off = 0;
         for (int i = 0; i < n; ++i) {
