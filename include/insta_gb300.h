@@ -31,6 +31,8 @@
  *                               shade_kernel_nerf (instant-ngp/src/testbed_nerf.cu:2030-2244,2320-2460)
  *   insta_march_debug           the sample positions advance_pos_nerf + generate_next_nerf_network_inputs
  *                               emit per ray (instant-ngp/src/testbed_nerf.cu:634-686,722-795)
+ *   insta_nearest_debug         the render path's warp-cooperative closest_triangle on given points
+ *                               (NGP/bvh.cuh:48-96 as called by the warp kernel, src/core.cu:470-478)
  */
 #ifndef INSTA_GB300_H
 #define INSTA_GB300_H
@@ -226,6 +228,10 @@ int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples);
 /* Per-ray sample t and dt (device pointers, [h*w][max_out]) and counts [h*w]. */
 int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out, float* out_t, float* out_dt,
                       int32_t* out_n);
+/* Nearest triangle id of each point (device pointers: pts f32[n*3] in the frame's space, out
+ * i32[n]) computed the way the render's deform stage computes it: the warp-cooperative walk over
+ * 32 consecutive points. */
+int insta_nearest_debug(insta_ctx* ctx, int avatar, int frame, const float* pts, int64_t n, int32_t* out_idx);
 
 /* -- serving ------------------------------------------------------------------- */
 /* A request loop on a worker thread that owns the context from insta_server_create to

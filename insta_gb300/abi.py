@@ -25,7 +25,7 @@ EXPORTS = [
     "insta_density_grid_load",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
     "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_batch",
-    "insta_render_samples", "insta_march_debug",
+    "insta_render_samples", "insta_march_debug", "insta_nearest_debug",
     "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
     "insta_server_release", "insta_server_error",
 ]
@@ -109,6 +109,7 @@ def load(path: Path | None = None):
             "insta_render_batch": [vp, C.POINTER(RenderDesc), C.c_int, C.POINTER(vp), C.POINTER(vp)],
             "insta_render_samples": [vp, C.POINTER(u64)],
             "insta_march_debug": [vp, C.POINTER(RenderDesc), C.c_int, vp, vp, vp],
+            "insta_nearest_debug": [vp, C.c_int, C.c_int, vp, i64, vp],
             "insta_server_create": [vp, C.POINTER(ServerConfig), C.POINTER(vp)],
             "insta_server_destroy": [vp],
             "insta_submit": [vp, C.POINTER(RenderDesc), vp, vp, vp, C.POINTER(u64)],
@@ -316,6 +317,9 @@ class Context:
         v = C.c_uint64(0)
         self._check(self.lib.insta_render_samples(self.h, C.byref(v)))
         return int(v.value)
+
+    def nearest_debug(self, avatar, frame, pts, n, out_idx):
+        self._check(self.lib.insta_nearest_debug(self.h, avatar, frame, _addr(pts), n, _addr(out_idx)))
 
     def march_debug(self, req: RenderDesc, max_out, out_t, out_dt, out_n):
         self._check(self.lib.insta_march_debug(self.h, C.byref(req), max_out, _addr(out_t), _addr(out_dt), _addr(out_n)))

@@ -1296,6 +1296,15 @@ int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out,
     });
 }
 
+int insta_nearest_debug(insta_ctx* ctx, int avatar, int frame, const float* pts, int64_t n, int32_t* out_idx) {
+    return guarded(ctx, [&] {
+        if (n < 0 || (n > 0 && (!pts || !out_idx))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
+        Avatar& a = ctx->avatar(avatar);
+        Frame& f = use_frame(ctx, a, frame);
+        CK(launch_nearest_debug(f.view, pts, n, out_idx, ctx->err_dev, ctx->stream));
+    });
+}
+
 }  // extern "C"
 
 // ------------------------------------------------------------------------------- serving

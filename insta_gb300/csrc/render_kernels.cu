@@ -205,11 +205,12 @@ __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ Wave
 }
 
 // ------------------------------------------------------------------ spatial sort of a round's samples
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {   // 6 bits -> every third bit
-    v &= 63u;
-    v = (v | (v << 8)) & 0x0000f00fu;
-    v = (v | (v << 4)) & 0x000c30c3u;
-    v = (v | (v << 2)) & 0x00249249u;
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {   // 10 bits -> every third bit
+    v &= 1023u;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
     return v;
 }
 
@@ -834,6 +835,28 @@ cudaError_t launch_unpack(const uint2* out, const float4* out_f32, int bf16, int
 cudaError_t launch_training_samples(const TrainArgs& a, cudaStream_t s) {
     if (a.n_rays <= 0) return cudaSuccess;
     training_samples_kernel<<<(unsigned)((a.n_rays + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// The deform stage's nearest-triangle query on caller points (32 consecutive points per warp).
+__global__ void __launch_bounds__(256, 4) nearest_debug_kernel(FrameView fr, const float* __restrict__ pts, int64_t n,
+                                                               int32_t* __restrict__ out, uint32_t* err) {
+    __shared__ WarpScratch wscratch[8];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const int64_t n_warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t base = ((int64_t)blockIdx.x * (blockDim.x >> 5) + warp) * 32; base < n; base += n_warps * 32) {
+        const int64_t i = base + lane;
+        const bool valid = i < n;
+        const V3 p = valid ? v3(pts[i * 3], pts[i * 3 + 1], pts[i * 3 + 2]) : v3(0.5f, 0.5f, 0.5f);
+        const Nearest q = nearest_warp(fr, p, valid, wscratch[warp], err);
+        if (valid) out[i] = q.id;
+    }
+}
+
+cudaError_t launch_nearest_debug(const FrameView& fr, const float* pts, int64_t n, int32_t* out, uint32_t* err, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
+    nearest_debug_kernel<<<(unsigned)blocks, 256, 0, s>>>(fr, pts, n, out, err);
     return cudaGetLastError();
 }
 

@@ -55,6 +55,41 @@ def test_nearest_bit_exact_and_canonical(gpu_avatar, oracle, oracle_frame, avata
     assert np.abs(out - ref64).max() <= 1e-5 * diag(avatar)
 
 
+def _morton_order(pts):
+    lo, hi = pts.min(0), pts.max(0)
+    q = np.clip(((pts - lo) / (hi - lo).max() * 1023).astype(np.int64), 0, 1023)
+    key = np.zeros(len(pts), np.int64)
+    for b in range(10):
+        for k in range(3):
+            key |= ((q[:, k] >> b) & 1) << (3 * b + k)
+    return np.argsort(key, kind="stable")
+
+
+def test_render_nearest_bit_exact(gpu_avatar, oracle, oracle_frame, avatar, frame0):
+    """The render's warp-cooperative nearest-triangle walk on points up to 2 cm off the surface,
+    as the render's samples are: a Morton-ordered block (coherent warps, as in the sorted sample
+    stream), a block in random order (wide warps: a large union of nodes) and points off the
+    vertices along their normal (vertex-nearest: several triangles at almost the same distance)."""
+    from insta_gb300 import synthetic as S
+    rng = np.random.default_rng(11)
+    shell = S.shell_points(frame0, avatar.faces, 49152, seed=5, half_width=0.02)
+    v = frame0.astype(np.float64)
+    nrm = v - v.mean(0)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    off = (v + nrm * rng.uniform(0.0, 0.02, (len(v), 1))).astype(np.float32)
+    pts = np.concatenate([shell[_morton_order(shell)][:32768], shell[32768:], off[_morton_order(off)]]).astype(np.float32)
+    n = len(pts)
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    gpu_avatar.nearest_debug(0, 0, dev(pts), n, out)
+    gpu_avatar.sync()
+    ids = out.cpu().numpy()
+    ref_ids, _ = oracle_frame["bvh"].nearest(pts)
+    assert (ids == ref_ids).all(), int((ids != ref_ids).sum())
+    pick = rng.choice(n, 4096, replace=False)
+    brute_ids, _ = oracle.nearest_brute(oracle_frame["def"], pts[pick])
+    assert (ids[pick] == brute_ids).all()
+
+
 def make_coords(pts, dirs, holder, n_extra=0, extra_val=0.25):
     n = len(pts)
     c = np.zeros((n, 11 + n_extra), np.float32)
