@@ -388,6 +388,70 @@ def run_batch64(args):
     ctx.close()
 
 
+def run_map(args):
+    """Plain canonical mapping: 1,048,576 points uniform in a 1 cm shell around the deformed
+    surface (area-weighted surface point + normal offset U(-5, 5) mm) -> nearest triangle id
+    (bit-exact) + canonical xyz, through insta_canonical_map_soa.  Device time from the library's
+    stage events; e2e adds the pinned H2D of the points and the D2H of ids + canonical xyz."""
+    import torch
+    from insta_gb300 import abi, synthetic as S
+    from oracle import oracle as O
+    n = 1 << 20
+    av = S.make_avatar(0)
+    frame = av.frame(av.frame_coeffs(0))
+    pts = S.shell_points(frame, av.faces, n, seed=0, half_width=5e-3)
+    stream = torch.cuda.Stream()
+    ctx = abi.Context(0, stream=stream.cuda_stream)
+    ctx.canonical_set(0, av.canonical, av.faces, av.mask)
+    ctx.frame_upload(0, 0, frame)
+    d_pts = torch.from_numpy(pts).cuda()
+    idx = torch.empty(n, dtype=torch.int32, device="cuda")
+    can = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.warmup)):
+            ctx.canonical_map_soa(0, 0, d_pts, n, idx, can)
+        ctx.sync()
+        ctx.stats(reset=True)
+        ctx.stats_enable(True)
+        for _ in range(args.steps):
+            flush.zero_()
+            ctx.canonical_map_soa(0, 0, d_pts, n, idx, can)
+        ctx.sync()
+        st = ctx.stats(reset=True)
+        ctx.stats_enable(False)
+        dev_ms = st["stage_ms"]["canonical_map"] / st["stage_calls"]["canonical_map"]
+        h_pts = torch.from_numpy(pts).pin_memory()
+        h_idx = torch.empty(n, dtype=torch.int32).pin_memory()
+        h_can = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            d_pts.copy_(h_pts, non_blocking=True)
+            ctx.canonical_map_soa(0, 0, d_pts, n, idx, can)
+            h_idx.copy_(idx, non_blocking=True)
+            h_can.copy_(can, non_blocking=True)
+        stream.synchronize()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+    dtr = O.build_triangles(frame, av.canonical, av.faces, av.mask)
+    bvh = O.Bvh(dtr)
+    ref_ids, _ = bvh.nearest(pts[:65536])
+    assert (h_idx.numpy()[:65536] == ref_ids).all(), "canonical map ids differ from the oracle"
+    line = {"workload": "canonical map, 1,048,576 points in a 1 cm shell, 10,240-triangle frame",
+            "points_per_s": n / (dev_ms / 1e3), "ms_per_call": dev_ms, "launches_per_call": 6,
+            "e2e": {"points_per_s": n / e2e_s, "h2d_bytes": n * 12, "d2h_bytes": n * 16}}
+    if not args.no_cpu_baseline:
+        m = 1 << 16
+        d = O.Deformation(dtr, O.build_triangles(av.canonical, None, av.faces, av.mask), O.adjacency(av.faces, av.n_verts), bvh)
+        t0 = time.perf_counter()
+        d.map_soa(pts[:m])
+        t = time.perf_counter() - t0
+        line["cpu_baseline"] = {"points_per_s": m / t, "cores": O.num_threads(), "kind": "port",
+                                "sample": f"first {m} points, oracle map_soa (BVH nearest + map), OpenMP"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_serve(args):
     """Served mixed stream: 8 resident avatars, Poisson arrivals, each request a fresh expression
     (its own frame upload, LBVH, occupancy) at a resolution drawn from {256, 512, 768, 1024}^2.
@@ -559,9 +623,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--width", type=int, default=512, help="square render size (512 = the benchmark workload)")
-    ap.add_argument("--workload", choices=["render", "batch", "serve", "precision"], default="render",
+    ap.add_argument("--workload", choices=["render", "batch", "serve", "precision", "map"], default="render",
                     help="render: the benchmark line; batch: 64 expressions in one wavefront; serve: request stream; "
-                         "precision: FP16 / BF16 / FP8 MLPs at 1024x1024 against the FP64 oracle")
+                         "precision: FP16 / BF16 / FP8 MLPs at 1024x1024 against the FP64 oracle; "
+                         "map: canonical mapping of 1M shell points")
     ap.add_argument("--rows", type=int, default=16, help="precision: image rows rendered by the FP64 oracle")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--rate", type=float, default=240.0)
@@ -577,6 +642,8 @@ def main():
         return run_serve(args)
     if args.workload == "precision":
         return run_precision(args)
+    if args.workload == "map":
+        return run_map(args)
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -103,7 +103,7 @@ struct insta_ctx {
     uint32_t* err_dev = nullptr;
     uint32_t* ray_counter = nullptr;
     unsigned long long* sample_counter = nullptr;
-    DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs, density_scratch, density_stage, side_scratch;
+    DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs, density_scratch, density_stage, side_scratch, map_scratch;
     cudaStream_t side = nullptr;        // asynchronous frame uploads
     cudaEvent_t side_mark = nullptr;    // orders a side upload after the main stream's earlier work
     Wave wave;
@@ -787,10 +787,9 @@ int insta_ctx_destroy(insta_ctx* ctx) {
             for (DevBuf* b : {&f.second.verts, &f.second.frames, &f.second.leaf_tris, &f.second.nodes, &f.second.bitfield})
                 ctx->release(*b);
     }
-    ctx->release(ctx->out_rgba);
-    ctx->release(ctx->out_depth);
-    ctx->release(ctx->extra);
-    ctx->release(ctx->bvh_scratch);
+    for (DevBuf* b : {&ctx->out_rgba, &ctx->out_depth, &ctx->extra, &ctx->bvh_scratch, &ctx->frame_jobs, &ctx->density_scratch,
+                      &ctx->density_stage, &ctx->map_scratch})
+        ctx->release(*b);
     Wave& w = ctx->wave;
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 4; ++k) ctx->release(w.rays[b][k]);
@@ -1069,8 +1068,15 @@ int insta_canonical_map_soa(insta_ctx* ctx, int avatar, int frame, const float* 
         if (n < 0 || (n > 0 && (!pts || !out_idx || !out_canon))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
         Avatar& a = ctx->avatar(avatar);
         Frame& f = use_frame(ctx, a, frame);
-        Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
-        CK(launch_canonical_map_soa(f.view, deform_view(a), pts, n, out_idx, out_canon, ctx->err_dev, ctx->stream));
+        if (n >= kMapSortedMin && n < ((int64_t)1 << 31)) {
+            ctx->alloc(ctx->map_scratch, map_sorted_scratch_bytes(n));
+            Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 6);
+            CK(launch_canonical_map_sorted(f.view, deform_view(a), pts, n, out_idx, out_canon, ctx->map_scratch.p, ctx->err_dev,
+                                           ctx->stream));
+        } else {
+            Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
+            CK(launch_canonical_map_soa(f.view, deform_view(a), pts, n, out_idx, out_canon, ctx->err_dev, ctx->stream));
+        }
     });
 }
 

@@ -111,6 +111,13 @@ size_t density_scratch_bytes(uint32_t n_cascades);
 cudaError_t launch_density_grid(const void* grid, int fp16, uint32_t n_cascades, void* scratch, uint8_t* bitfield, cudaStream_t s);
 cudaError_t launch_canonical_map_soa(const FrameView& fv, const DeformView& dv, const float* pts, int64_t n, int32_t* out_idx,
                                      float* out_canon, uint32_t* err, cudaStream_t s);
+// The same map for large point sets: points are first sorted by a 64^3 cell of the frame's box
+// (counting sort), so that the warp-cooperative nearest walk sees 32 neighbours at a time; the
+// results go back to the callers' order.  scratch: map_sorted_scratch_bytes(n) bytes.
+constexpr int64_t kMapSortedMin = 1 << 16;   // below this the per-point walk is as fast
+size_t map_sorted_scratch_bytes(int64_t n);
+cudaError_t launch_canonical_map_sorted(const FrameView& fv, const DeformView& dv, const float* pts, int64_t n, int32_t* out_idx,
+                                        float* out_canon, void* scratch, uint32_t* err, cudaStream_t s);
 // n_dev (optional): a device count; records [0, min(n, *n_dev)) are mapped
 cudaError_t launch_canonical_map_coords(const FrameView* frames_dev, uint32_t n_frames, const DeformView& dv, float* coords,
                                         uint32_t stride, uint32_t n_extra, int64_t n, int32_t frame_id, uint32_t* err, cudaStream_t s,

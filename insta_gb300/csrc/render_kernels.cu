@@ -838,6 +838,109 @@ cudaError_t launch_training_samples(const TrainArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ canonical map, sorted
+// insta_canonical_map_soa on large point sets (the warp hook of src/core.cu:442-526 on bare
+// points): a counting sort by 64^3 cell of the frame's box, the warp-cooperative nearest walk over
+// 32 sorted neighbours at a time (ids scattered back to the callers' order), then the
+// deformed->canonical map per point in the callers' order.
+constexpr uint32_t kMapCellBits = 18, kMapBins = 1u << kMapCellBits, kMapBlocks = kMapBins / kSortBlock;
+
+__global__ void __launch_bounds__(256) map_count_kernel(FrameView fr, const float* __restrict__ pts, uint32_t n,
+                                                        uint32_t* __restrict__ keys, uint32_t* __restrict__ bins) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+        const uint32_t i = b + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t key = 0xffffffffu;
+        if (valid) {
+            key = sample_cell(fr, make_float4(pts[(size_t)i * 3], pts[(size_t)i * 3 + 1], pts[(size_t)i * 3 + 2], 0.f), kMapCellBits);
+            keys[i] = key;
+        }
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        if (valid && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(bins + key, (uint32_t)__popc(peers));
+    }
+}
+
+// Exclusive scan of the kMapBlocks block totals in place (one block, one total per thread).
+__global__ void __launch_bounds__(kSortBlock) map_offsets_kernel(uint32_t* __restrict__ block_sums) {
+    __shared__ uint32_t warp_tot[32];
+    const uint32_t v = threadIdx.x < kMapBlocks ? block_sums[threadIdx.x] : 0u;
+    uint32_t before;
+    block_exclusive_scan(v, &before, warp_tot);
+    if (threadIdx.x < kMapBlocks) block_sums[threadIdx.x] = before;
+}
+
+__global__ void __launch_bounds__(256) map_place_kernel(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ bins,
+                                                        const uint32_t* __restrict__ block_sums, uint32_t* __restrict__ order) {
+    const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+        const uint32_t i = b + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t key = valid ? keys[i] : 0xffffffffu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (valid && lane == (uint32_t)leader) base = atomicAdd(bins + key, (uint32_t)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (valid) order[block_sums[key / kSortBlock] + base + __popc(peers & lt_mask)] = i;
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) map_nearest_kernel(FrameView fr, const float* __restrict__ pts, uint32_t n,
+                                                             const uint32_t* __restrict__ order, int32_t* __restrict__ out_idx,
+                                                             uint32_t* err) {
+    __shared__ WarpScratch wscratch[8];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32u; base < n; base += n_warps * 32u) {
+        const uint32_t s = base + lane;
+        const bool valid = s < n;
+        const uint32_t i = valid ? order[s] : 0u;
+        const V3 p = valid ? v3(pts[(size_t)i * 3], pts[(size_t)i * 3 + 1], pts[(size_t)i * 3 + 2]) : v3(0.5f, 0.5f, 0.5f);
+        const Nearest q = nearest_warp(fr, p, valid, wscratch[warp], err);
+        if (valid) out_idx[i] = q.id;
+    }
+}
+
+__global__ void __launch_bounds__(256) map_canon_kernel(FrameView fr, DeformView dv, const float* __restrict__ pts, uint32_t n,
+                                                        const int32_t* __restrict__ idx, float* __restrict__ out_canon, uint32_t* err) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const V3 p = v3(pts[(size_t)i * 3], pts[(size_t)i * 3 + 1], pts[(size_t)i * 3 + 2]);
+        const int32_t id = idx[i];
+        float o[3] = {p.x, p.y, p.z};
+        if (id < 0) atomicOr(err, INSTA_DEVERR_NO_TRI);
+        else map_to_canonical(dv, fr.frames, (uint32_t)id, p, nullptr, o, nullptr, nullptr);
+        out_canon[(size_t)i * 3] = o[0]; out_canon[(size_t)i * 3 + 1] = o[1]; out_canon[(size_t)i * 3 + 2] = o[2];
+    }
+}
+
+size_t map_sorted_scratch_bytes(int64_t n) { return ((size_t)n * 2 + kMapBins + kMapBlocks) * sizeof(uint32_t); }
+
+cudaError_t launch_canonical_map_sorted(const FrameView& fv, const DeformView& dv, const float* pts, int64_t n64, int32_t* out_idx,
+                                        float* out_canon, void* scratch, uint32_t* err, cudaStream_t s) {
+    if (n64 <= 0) return cudaSuccess;
+    if (n64 >= (int64_t)1 << 31) return cudaErrorInvalidValue;
+    const uint32_t n = (uint32_t)n64;
+    uint32_t* keys = static_cast<uint32_t*>(scratch);
+    uint32_t* order = keys + n;
+    uint32_t* bins = order + n;
+    uint32_t* block_sums = bins + kMapBins;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned grid = (unsigned)std::min<int64_t>((n64 + 255) / 256, (int64_t)sms * 8);
+    cudaError_t e = cudaMemsetAsync(bins, 0, kMapBins * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    map_count_kernel<<<grid, 256, 0, s>>>(fv, pts, n, keys, bins);
+    sort_scan_kernel<<<kMapBlocks, kSortBlock, 0, s>>>(bins, block_sums);
+    map_offsets_kernel<<<1, kSortBlock, 0, s>>>(block_sums);
+    map_place_kernel<<<grid, 256, 0, s>>>(keys, n, bins, block_sums, order);
+    const unsigned grid_w = (unsigned)std::min<int64_t>((n64 + 255) / 256, (int64_t)sms * 4);
+    map_nearest_kernel<<<grid_w, 256, 0, s>>>(fv, pts, n, order, out_idx, err);
+    map_canon_kernel<<<grid, 256, 0, s>>>(fv, dv, pts, n, out_idx, out_canon, err);
+    return cudaGetLastError();
+}
+
 // The deform stage's nearest-triangle query on caller points (32 consecutive points per warp).
 __global__ void __launch_bounds__(256, 4) nearest_debug_kernel(FrameView fr, const float* __restrict__ pts, int64_t n,
                                                                int32_t* __restrict__ out, uint32_t* err) {

@@ -35,9 +35,12 @@ def diag(avatar):
     return float(np.linalg.norm(v.max(0) - v.min(0)))
 
 
-def test_nearest_bit_exact_and_canonical(gpu_avatar, oracle, oracle_frame, avatar, frame0):
+@pytest.mark.parametrize("n_pts", [65536, 20000])
+def test_nearest_bit_exact_and_canonical(gpu_avatar, oracle, oracle_frame, avatar, frame0, n_pts):
+    """insta_canonical_map_soa: 65536 points take the sorted path (cell sort + warp walk), 20000
+    the per-point walk."""
     from insta_gb300 import synthetic as S
-    pts = S.shell_points(frame0, avatar.faces, 65536, seed=3)
+    pts = S.shell_points(frame0, avatar.faces, n_pts, seed=3)
     n = len(pts)
     idx = torch.empty(n, dtype=torch.int32, device="cuda")
     out = torch.empty((n, 3), dtype=torch.float32, device="cuda")
