@@ -17,6 +17,8 @@
  *                               instant-ngp/src/triangle_bvh.cu:548-631; src/core.cu:309-334)
  *   insta_occupancy_from_mesh   mark_flame_density_grid + update_density_grid_mean_and_bitfield
  *                               (instant-ngp/src/testbed_nerf.cu:364-389,2863-2878)
+ *   insta_density_grid_update   update_density_grid_nerf + warp_random_samples (instant-ngp/src/
+ *                               testbed_nerf.cu:487-583,2774-2861; src/core.cu:528-579)
  *   insta_density_grid_load     the snapshot's density grid -> bitfield (grid_to_bitfield +
  *                               bitfield_max_pool, instant-ngp/src/testbed_nerf.cu:585-632)
  *   insta_canonical_map         rta::Core::surface_closest_point / render_deformed -> `warp`
@@ -166,6 +168,43 @@ int insta_occupancy_get(insta_ctx* ctx, int avatar, int frame, uint8_t* bits);
  * threshold min(0.01, mean of max(v, 0) over cascade 0), then the mip max-pool
  * (update_density_grid_mean_and_bitfield, instant-ngp/src/testbed_nerf.cu:585-632,2863-2878). */
 int insta_density_grid_load(insta_ctx* ctx, int avatar, int frame, const void* grid, uint32_t n_cascades, int fp16);
+
+/* -- density-grid maintenance ------------------------------------------------------ */
+/* The PCG32 generator state (the pcg32 of tiny-cuda-nn, ngp's default_rng_t). */
+typedef struct insta_pcg32 {
+    uint64_t state, inc;
+} insta_pcg32;
+
+/* One update_density_grid_nerf step (instant-ngp/src/testbed_nerf.cu:2774-2861) with INSTA's
+ * surface_closest_point hook on the sample positions (warp_random_samples, src/core.cu:528-579):
+ * n_uniform samples over all cells and n_nonuniform over cells above the minimum optical
+ * thickness, each warped to the canonical space through a random one of frames 0..n_frames-1
+ * (the reference's m_meshes.size() - 1), density network at the canonical position, max splat
+ * into a fresh grid, then grid = max(grid * decay, new) (negative cells kept) and, for
+ * bitfield_frame >= 0, that frame's bitfield (update_density_grid_mean_and_bitfield).
+ * training_prep_nerf (:3427-3444) calls it with 128^3 * n_cascades uniform samples for the
+ * first 256 steps, then 128^3 / 4 * n_cascades of each kind. */
+typedef struct insta_density_update_desc {
+    float decay;                      /* density_grid_decay (0.95)                            */
+    uint32_t n_uniform, n_nonuniform;
+    uint32_t n_cascades;              /* the grid's cascades (max_cascade + 1)                */
+    float aabb_min[3], aabb_max[3];   /* Testbed::m_aabb: warp_position's box                 */
+    insta_pcg32 grid_rng;             /* density_grid_rng; on return advanced by 2^32 as the
+                                         reference's density_grid_rng.advance()              */
+    insta_pcg32 warp_rng;             /* the warp's generator (m_random_generator), read only */
+    uint32_t ema_step;                /* density_grid_ema_step; incremented on return         */
+    int n_frames;                     /* frames 0 .. n_frames - 1 (all uploaded)              */
+    int bitfield_frame;               /* frame receiving the new bitfield, or -1              */
+    float* debug_pos;                 /* optional device [n][3]: the warped sample positions  */
+    uint32_t* debug_idx;              /* optional device [n]: each sample's cell index        */
+} insta_density_update_desc;
+
+/* The avatar's float density grid (n_cascades x 128^3, Morton order; host or device pointer,
+ * NULL = zeros; cells below zero are never updated, as mark_untrained_density_grid leaves them). */
+int insta_density_grid_reset(insta_ctx* ctx, int avatar, const float* grid, uint32_t n_cascades);
+int insta_density_grid_update(insta_ctx* ctx, int avatar, insta_density_update_desc* desc);
+/* Copy the float grid out (host or device pointer, n_cascades x 128^3 floats; synchronises). */
+int insta_density_grid_read(insta_ctx* ctx, int avatar, float* out);
 
 /* -- deformation -------------------------------------------------------------- */
 /* In place on NerfCoordinate records (device pointer, stride floats each: pos[3] dt holder

@@ -22,7 +22,7 @@ EXPORTS = [
     "insta_canonical_set", "insta_avatar_set_boxes", "insta_avatar_set_flags", "insta_frame_upload",
     "insta_frame_upload_batch", "insta_frame_upload_async", "insta_frame_wait",
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
-    "insta_density_grid_load",
+    "insta_density_grid_load", "insta_density_grid_reset", "insta_density_grid_update", "insta_density_grid_read",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
     "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_batch",
     "insta_render_samples", "insta_march_debug", "insta_nearest_debug",
@@ -35,6 +35,17 @@ REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
 
 class ServerConfig(C.Structure):
     _fields_ = [("max_inflight", C.c_uint32), ("max_inflight_pixels", C.c_uint64), ("occupancy_radius", C.c_double)]
+
+
+class Pcg32State(C.Structure):
+    _fields_ = [("state", C.c_uint64), ("inc", C.c_uint64)]
+
+
+class DensityUpdateDesc(C.Structure):
+    _fields_ = [("decay", C.c_float), ("n_uniform", C.c_uint32), ("n_nonuniform", C.c_uint32), ("n_cascades", C.c_uint32),
+                ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3), ("grid_rng", Pcg32State), ("warp_rng", Pcg32State),
+                ("ema_step", C.c_uint32), ("n_frames", C.c_int32), ("bitfield_frame", C.c_int32),
+                ("debug_pos", C.c_void_p), ("debug_idx", C.c_void_p)]
 
 
 class InstaError(RuntimeError):
@@ -98,6 +109,9 @@ def load(path: Path | None = None):
             "insta_occupancy_set": [vp, C.c_int, C.c_int, vp],
             "insta_occupancy_get": [vp, C.c_int, C.c_int, vp],
             "insta_density_grid_load": [vp, C.c_int, C.c_int, vp, u32, C.c_int],
+            "insta_density_grid_reset": [vp, C.c_int, vp, u32],
+            "insta_density_grid_update": [vp, C.c_int, C.POINTER(DensityUpdateDesc)],
+            "insta_density_grid_read": [vp, C.c_int, vp],
             "insta_canonical_map": [vp, C.c_int, C.c_int, vp, u32, u32, i64],
             "insta_canonical_map_soa": [vp, C.c_int, C.c_int, vp, i64, vp, vp],
             "insta_training_samples": [vp, C.c_int, C.c_int, vp, vp, vp, vp, u32, i64, C.c_float, u32, vp, u32, vp, vp, vp],
@@ -262,6 +276,18 @@ class Context:
         g = grid if hasattr(grid, "data_ptr") else np.ascontiguousarray(grid)
         fp16 = int(str(g.dtype).endswith("float16"))
         self._check(self.lib.insta_density_grid_load(self.h, avatar, frame, _addr(g), n_cascades, fp16))
+
+    def density_grid_reset(self, avatar, n_cascades, grid=None):
+        g = None if grid is None else (grid if hasattr(grid, "data_ptr") else np.ascontiguousarray(grid, dtype=np.float32))
+        self._check(self.lib.insta_density_grid_reset(self.h, avatar, _addr(g) if g is not None else None, n_cascades))
+
+    def density_grid_update(self, avatar, desc: DensityUpdateDesc):
+        self._check(self.lib.insta_density_grid_update(self.h, avatar, C.byref(desc)))
+
+    def density_grid_read(self, avatar, n_cascades) -> np.ndarray:
+        g = np.zeros(n_cascades * 128 ** 3, dtype=np.float32)
+        self._check(self.lib.insta_density_grid_read(self.h, avatar, _addr(g)))
+        return g
 
     def training_samples(self, avatar, grid_frame, rays, image, start_rand, max_samples, coords, stride, ray_indices,
                          numsteps, counters, cone_angle=1 / 256, extra=None, n_images=0):

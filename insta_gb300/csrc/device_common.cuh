@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 
@@ -124,6 +125,41 @@ __device__ __forceinline__ float box_distance_sq(float mnx, float mny, float mnz
     float dz = az < bz ? bz : az; dz = dz < 0.f ? 0.f : dz;
     return __fadd_rn(__fmul_rn(dx, dx), __fadd_rn(__fmul_rn(dy, dy), __fmul_rn(dz, dz)));
 }
+
+// PCG32 (O'Neill's permuted congruential generator with 64-bit state, XSH-RR output), the
+// pcg32 class tiny-cuda-nn uses as default_rng_t, restated from the published algorithm:
+// LCG step with multiplier 6364136223846793005 and odd increment, output of the old state,
+// floats from the top 23 bits, and the logarithmic-time jump ahead.
+struct Pcg32 {
+    uint64_t state, inc;
+    __host__ __device__ uint32_t next_uint() {
+        const uint64_t old = state;
+        state = old * 0x5851f42d4c957f2dull + inc;
+        const uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        const uint32_t rot = (uint32_t)(old >> 59u);
+        return (xorshifted >> rot) | (xorshifted << ((~rot + 1u) & 31u));
+    }
+    __host__ __device__ float next_float() {
+        const uint32_t bits = (next_uint() >> 9) | 0x3f800000u;
+        float f;
+        memcpy(&f, &bits, 4);
+        return f - 1.0f;
+    }
+    __host__ __device__ void advance(int64_t delta_) {
+        uint64_t cur_mult = 0x5851f42d4c957f2dull, cur_plus = inc, acc_mult = 1u, acc_plus = 0u;
+        uint64_t delta = (uint64_t)delta_;
+        while (delta > 0) {
+            if (delta & 1) {
+                acc_mult *= cur_mult;
+                acc_plus = acc_plus * cur_mult + cur_plus;
+            }
+            cur_plus = (cur_mult + 1) * cur_plus;
+            cur_mult *= cur_mult;
+            delta /= 2;
+        }
+        state = acc_mult * state + acc_plus;
+    }
+};
 
 }  // namespace insta
 

@@ -535,6 +535,93 @@ __global__ void __launch_bounds__(256) grid_to_bitfield_kernel(const float* __re
     bits[i] = b;
 }
 
+// ------------------------------------------------------------- density-grid maintenance
+// update_density_grid_nerf (ngp/src/testbed_nerf.cu:2774-2861) with INSTA's deformation hook:
+//   grid_samples_kernel  generate_grid_samples_nerf_nonuniform (:487-516) for the uniform and the
+//                        non-uniform set in one launch (the reference hands both calls the same
+//                        generator state)
+//   warp_random_kernel   warp_random_samples (src/core.cu:528-579): a random tracked frame per
+//                        sample, its nearest triangle, the deformed -> canonical position
+//   (encode + MLPs)      NerfNetwork::density at the canonical positions
+//   splat_max_kernel     splat_grid_samples_nerf_max_nearest_neighbor (:518-531)
+//   ema_kernel           ema_grid_samples_nerf (:554-583): max(previous * decay, new), negative
+//                        cells (never updated) kept
+__global__ void __launch_bounds__(256) grid_samples_kernel(uint32_t n_uniform, uint32_t n_nonuniform, Pcg32 rng, uint32_t step,
+                                                           float3 aabb_min, float3 aabb_max, const float* __restrict__ grid,
+                                                           uint32_t n_cascades, float* __restrict__ coords, uint32_t stride,
+                                                           uint32_t* __restrict__ indices) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_uniform + n_nonuniform) return;
+    const bool uniform = i < n_uniform;
+    const uint32_t li = uniform ? i : i - n_uniform, ne = uniform ? n_uniform : n_nonuniform;
+    const float thresh = uniform ? -0.01f : 0.01f;   // NERF_MIN_OPTICAL_THICKNESS for the non-uniform set
+    Pcg32 r = rng;
+    r.advance((int64_t)(uint32_t)(li * 4u));
+    const uint32_t level = (uint32_t)__fmul_rn(r.next_float(), (float)n_cascades) % n_cascades;
+    uint32_t idx = 0;
+    for (uint32_t j = 0; j < 10; ++j) {
+        idx = ((li + step * ne) * 56924617u + j * 19349663u + 96925573u) % GRID3;
+        idx += level * GRID3;
+        if (grid[idx] > thresh) break;
+    }
+    const uint32_t cell = idx % GRID3;
+    const float cc[3] = {(float)morton_invert(cell), (float)morton_invert(cell >> 1), (float)morton_invert(cell >> 2)};
+    const float rr[3] = {r.next_float(), r.next_float(), r.next_float()};
+    const float scale = scalbnf(1.0f, (int)level);
+    const float mn[3] = {aabb_min.x, aabb_min.y, aabb_min.z}, mx[3] = {aabb_max.x, aabb_max.y, aabb_max.z};
+    float* c = coords + (size_t)i * stride;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float pos = __fadd_rn(__fmul_rn(__fsub_rn(__fdiv_rn(__fadd_rn(cc[k], rr[k]), (float)GRID), 0.5f), scale), 0.5f);
+        c[k] = __fdiv_rn(__fsub_rn(pos, mn[k]), __fsub_rn(mx[k], mn[k]));   // warp_position = aabb.relative_pos
+        c[8 + k] = 0.5f;                                                     // no direction (density only)
+    }
+    c[3] = 0.f;   // warp_dt(MIN_CONE_STEPSIZE)
+    c[4] = 0.f;
+    indices[i] = idx;
+}
+
+__global__ void __launch_bounds__(256) warp_random_kernel(const FrameView* __restrict__ frames, uint32_t n_frames, DeformView dv,
+                                                          float* __restrict__ coords, uint32_t stride, uint32_t n, Pcg32 rng,
+                                                          uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float* c = coords + (size_t)i * stride;
+    const V3 p = v3(c[0], c[1], c[2]);
+    Pcg32 r = rng;
+    r.advance((int64_t)(uint32_t)(i * n_frames));
+    const uint32_t fid = (uint32_t)__fmul_rn(r.next_float(), (float)n_frames);
+    if (fid >= n_frames || frames[fid].n_tris == 0) { atomicOr(err, INSTA_DEVERR_NO_TRI); return; }
+    const FrameView& fr = frames[fid];
+    const Nearest q = nearest_triangle(fr, p, err);
+    if (q.id < 0) { atomicOr(err, INSTA_DEVERR_NO_TRI); return; }
+    float o[3];
+    map_to_canonical(dv, fr.frames, (uint32_t)q.id, p, nullptr, o, nullptr, nullptr);
+    c[0] = o[0]; c[1] = o[1]; c[2] = o[2];
+}
+
+__global__ void __launch_bounds__(256) splat_max_kernel(uint32_t n, const uint32_t* __restrict__ indices, const uint2* __restrict__ out,
+                                                        const float4* __restrict__ out_f32, int f32_out, float* __restrict__ tmp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float raw;
+    if (f32_out) {
+        raw = out_f32[i].w;
+    } else {
+        const uint2 u = out[i];
+        raw = __half2float(__ushort_as_half((unsigned short)(u.y >> 16)));
+    }
+    const float thickness = __fmul_rn(__expf(raw), MIN_CONE);   // network_to_density (exponential) x the smallest step
+    atomicMax(reinterpret_cast<uint32_t*>(tmp) + indices[i], __float_as_uint(thickness));
+}
+
+__global__ void __launch_bounds__(256) ema_kernel(uint32_t n, float decay, float* __restrict__ grid, const float* __restrict__ tmp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float prev = grid[i];
+    grid[i] = prev < 0.f ? prev : fmaxf(__fmul_rn(prev, decay), tmp[i]);
+}
+
 // ---------------------------------------------------------------- canonical map
 __global__ void __launch_bounds__(256) canonical_map_soa_kernel(FrameView fr, DeformView dv, const float* __restrict__ pts, int64_t n,
                                                                 int32_t* __restrict__ out_idx, float* __restrict__ out_canon, uint32_t* err) {
@@ -700,6 +787,33 @@ cudaError_t launch_density_grid(const void* grid, int fp16, uint32_t n_cascades,
     grid_to_bitfield_kernel<<<GRID3 / 8 * 8 / 256, 256, 0, s>>>(g, n_cascades, thresh, bitfield);
     for (int lvl = 1; lvl < 8; ++lvl)
         maxpool_kernel<<<(GRID3 / 64 + 255) / 256, 256, 0, s>>>(bitfield + (size_t)(lvl - 1) * GRID3 / 8, bitfield + (size_t)lvl * GRID3 / 8);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_samples(uint32_t n_uniform, uint32_t n_nonuniform, uint64_t rng_state, uint64_t rng_inc, uint32_t step,
+                                const float* aabb_min, const float* aabb_max, const float* grid, uint32_t n_cascades, float* coords,
+                                uint32_t stride, uint32_t* indices, cudaStream_t s) {
+    const uint32_t n = n_uniform + n_nonuniform;
+    if (n == 0) return cudaSuccess;
+    Pcg32 r{rng_state, rng_inc};
+    grid_samples_kernel<<<(n + 255) / 256, 256, 0, s>>>(n_uniform, n_nonuniform, r, step, make_float3(aabb_min[0], aabb_min[1], aabb_min[2]),
+                                                        make_float3(aabb_max[0], aabb_max[1], aabb_max[2]), grid, n_cascades, coords, stride,
+                                                        indices);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_warp_random(const FrameView* frames_dev, uint32_t n_frames, const DeformView& dv, float* coords, uint32_t stride,
+                               uint32_t n, uint64_t rng_state, uint64_t rng_inc, uint32_t* err, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    Pcg32 r{rng_state, rng_inc};
+    warp_random_kernel<<<(n + 255) / 256, 256, 0, s>>>(frames_dev, n_frames, dv, coords, stride, n, r, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_splat_ema(uint32_t n, const uint32_t* indices, const uint2* out, const float4* out_f32, int f32_out, float* tmp,
+                             float* grid, uint32_t n_cells, float decay, cudaStream_t s) {
+    if (n) splat_max_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, indices, out, out_f32, f32_out, tmp);
+    ema_kernel<<<(n_cells + 255) / 256, 256, 0, s>>>(n_cells, decay, grid, tmp);
     return cudaGetLastError();
 }
 

@@ -91,6 +91,8 @@ struct Avatar {
     bool table_dirty = true;
     uint32_t table_frames = 0;
     Field field;
+    DevBuf density_grid;          // float [grid_cascades][128^3], Morton order (update_density_grid_nerf state)
+    uint32_t grid_cascades = 0;
 };
 
 struct insta_ctx {
@@ -103,7 +105,8 @@ struct insta_ctx {
     uint32_t* err_dev = nullptr;
     uint32_t* ray_counter = nullptr;
     unsigned long long* sample_counter = nullptr;
-    DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs, density_scratch, density_stage, side_scratch, map_scratch;
+    DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs, density_scratch, density_stage, side_scratch, map_scratch,
+        grid_coords, grid_idx, grid_tmp;
     cudaStream_t side = nullptr;        // asynchronous frame uploads
     cudaEvent_t side_mark = nullptr;    // orders a side upload after the main stream's earlier work
     Wave wave;
@@ -781,14 +784,14 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     for (auto& kv : ctx->avatars) {
         Avatar& a = *kv.second;
         for (DevBuf* b : {&a.faces, &a.mask, &a.adjacency, &a.canon_verts, &a.canon_area, &a.canon_frames, &a.frame_table,
-                          &a.field.params, &a.field.image})
+                          &a.field.params, &a.field.image, &a.density_grid})
             ctx->release(*b);
         for (auto& f : a.frames)
             for (DevBuf* b : {&f.second.verts, &f.second.frames, &f.second.leaf_tris, &f.second.nodes, &f.second.bitfield})
                 ctx->release(*b);
     }
     for (DevBuf* b : {&ctx->out_rgba, &ctx->out_depth, &ctx->extra, &ctx->bvh_scratch, &ctx->frame_jobs, &ctx->density_scratch,
-                      &ctx->density_stage, &ctx->map_scratch})
+                      &ctx->density_stage, &ctx->map_scratch, &ctx->grid_coords, &ctx->grid_idx, &ctx->grid_tmp})
         ctx->release(*b);
     Wave& w = ctx->wave;
     for (int b = 0; b < 2; ++b)
@@ -1003,6 +1006,95 @@ int insta_density_grid_load(insta_ctx* ctx, int avatar, int frame, const void* g
         Stage st(ctx, INSTA_STAGE_OCCUPANCY, fp16 ? 11 : 10);
         CK(launch_density_grid(src, fp16, n_cascades, ctx->density_scratch.p, (uint8_t*)f.bitfield.p, ctx->stream));
         f.has_occupancy = true;
+    });
+}
+
+int insta_density_grid_reset(insta_ctx* ctx, int avatar, const float* grid, uint32_t n_cascades) {
+    return guarded(ctx, [&] {
+        if (n_cascades < 1 || n_cascades > 8) fail(INSTA_ERR_INVALID_ARG, "n_cascades must be 1..8, got %u", n_cascades);
+        Avatar& a = ctx->avatar(avatar);
+        const size_t bytes = (size_t)n_cascades * GRID3 * sizeof(float);
+        ctx->alloc(a.density_grid, bytes);
+        a.grid_cascades = n_cascades;
+        if (grid) host_copy(a.density_grid.p, grid, bytes, ctx->stream);
+        else CK(cudaMemsetAsync(a.density_grid.p, 0, bytes, ctx->stream));
+    });
+}
+
+int insta_density_grid_read(insta_ctx* ctx, int avatar, float* out) {
+    return guarded(ctx, [&] {
+        if (!out) fail(INSTA_ERR_INVALID_ARG, "null output");
+        Avatar& a = ctx->avatar(avatar);
+        if (!a.density_grid.p) fail(INSTA_ERR_NOT_READY, "avatar %d has no density grid (insta_density_grid_reset)", avatar);
+        host_copy(out, a.density_grid.p, (size_t)a.grid_cascades * GRID3 * sizeof(float), ctx->stream);
+        ctx->check_device();
+    });
+}
+
+int insta_density_grid_update(insta_ctx* ctx, int avatar, insta_density_update_desc* d) {
+    return guarded(ctx, [&] {
+        if (!d) fail(INSTA_ERR_INVALID_ARG, "null description");
+        Avatar& a = ctx->avatar(avatar);
+        if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", avatar);
+        if (!a.density_grid.p) fail(INSTA_ERR_NOT_READY, "avatar %d has no density grid (insta_density_grid_reset)", avatar);
+        if (d->n_cascades != a.grid_cascades)
+            fail(INSTA_ERR_INVALID_ARG, "n_cascades %u differs from the grid's %u", d->n_cascades, a.grid_cascades);
+        if (a.field.desc.n_extra_dims != 0)
+            fail(INSTA_ERR_UNSUPPORTED, "the density-grid update evaluates fields without expression dims (this field has %u)",
+                 a.field.desc.n_extra_dims);
+        const uint64_t n64 = (uint64_t)d->n_uniform + d->n_nonuniform;
+        if (n64 == 0 || n64 >= (1ull << 30)) fail(INSTA_ERR_INVALID_ARG, "sample count must be 1 .. 2^30 - 1, got %llu", (unsigned long long)n64);
+        if (d->n_frames < 1) fail(INSTA_ERR_INVALID_ARG, "n_frames must be >= 1");
+        for (int k = 0; k < d->n_frames; ++k)
+            if (!a.frames.count(k)) fail(INSTA_ERR_NOT_READY, "frame %d (of the %d the warp picks from) is not uploaded", k, d->n_frames);
+        const uint32_t n = (uint32_t)n64, stride = 11;
+        refresh_frame_table(ctx, a);
+        wait_all_frames(ctx, a);
+        ctx->alloc(ctx->grid_coords, (size_t)n * stride * sizeof(float));
+        ctx->alloc(ctx->grid_idx, (size_t)n * sizeof(uint32_t));
+        ctx->alloc(ctx->grid_tmp, (size_t)d->n_cascades * GRID3 * sizeof(float));
+        float* coords = (float*)ctx->grid_coords.p;
+        uint32_t* idx = (uint32_t*)ctx->grid_idx.p;
+        const TilePlan& P = a.field.plan;
+        const uint64_t tiles = ((uint64_t)n + 127) / 128;
+        Wave& w = ctx->wave;
+        ctx->alloc(w.tiles, tiles * P.tile_bytes);
+        ctx->alloc(w.out, tiles * 128 * sizeof(uint2));
+        ctx->alloc(w.out_f32, tiles * 128 * sizeof(float4));
+        {
+            Stage st(ctx, INSTA_STAGE_OCCUPANCY, 6);
+            CK(cudaMemsetAsync(ctx->grid_tmp.p, 0, (size_t)d->n_cascades * GRID3 * sizeof(float), ctx->stream));
+            CK(launch_grid_samples(d->n_uniform, d->n_nonuniform, d->grid_rng.state, d->grid_rng.inc, d->ema_step, d->aabb_min, d->aabb_max,
+                                   (const float*)a.density_grid.p, d->n_cascades, coords, stride, idx, ctx->stream));
+            CK(launch_warp_random((const FrameView*)a.frame_table.p, (uint32_t)d->n_frames, deform_view(a), coords, stride, n,
+                                  d->warp_rng.state, d->warp_rng.inc, ctx->err_dev, ctx->stream));
+            if (d->debug_pos)
+                CK(cudaMemcpy2DAsync(d->debug_pos, 3 * sizeof(float), coords, stride * sizeof(float), 3 * sizeof(float), n,
+                                     cudaMemcpyDefault, ctx->stream));
+            if (d->debug_idx) CK(cudaMemcpyAsync(d->debug_idx, idx, (size_t)n * sizeof(uint32_t), cudaMemcpyDefault, ctx->stream));
+            CK(cudaMemsetAsync(w.tiles.p, 0, tiles * P.tile_bytes, ctx->stream));
+            CK(launch_encode_coords(a.field.view, coords, stride, n, (uint8_t*)w.tiles.p, P.tile_bytes, P.k_in, ctx->stream));
+            MlpArgs m{};
+            m.fv = a.field.view; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.n_samples = n;
+            m.out = (uint2*)w.out.p; m.out_f32 = (float4*)w.out_f32.p; m.err = ctx->err_dev;
+            CK(launch_mlp(m, (uint32_t)tiles, ctx->stream));
+            CK(launch_splat_ema(n, idx, (const uint2*)w.out.p, (const float4*)w.out_f32.p, a.field.view.precision != 0,
+                                (float*)ctx->grid_tmp.p, (float*)a.density_grid.p, d->n_cascades * GRID3, d->decay, ctx->stream));
+        }
+        if (d->bitfield_frame >= 0) {
+            Frame& f = use_frame(ctx, a, d->bitfield_frame);
+            ctx->alloc(f.bitfield, (size_t)8 * GRID3 / 8);
+            ctx->alloc(ctx->density_scratch, density_scratch_bytes(d->n_cascades));
+            Stage st(ctx, INSTA_STAGE_OCCUPANCY, 10);
+            CK(launch_density_grid(a.density_grid.p, 0, d->n_cascades, ctx->density_scratch.p, (uint8_t*)f.bitfield.p, ctx->stream));
+            f.has_occupancy = true;
+        }
+        // the reference's host-side bookkeeping after the update: ++density_grid_ema_step and
+        // density_grid_rng.advance() with pcg32's default jump of 2^32
+        d->ema_step += 1;
+        Pcg32 r{d->grid_rng.state, d->grid_rng.inc};
+        r.advance((int64_t)1 << 32);
+        d->grid_rng.state = r.state;
     });
 }
 

@@ -108,6 +108,15 @@ cudaError_t launch_bvh_build(const FrameView& fv, const float* verts, const int3
 cudaError_t launch_occupancy(const FrameView& fv, double radius, uint8_t* bitfield, uint32_t* err, cudaStream_t s);
 // Float (or FP16) density grid [n_cascades][128^3] (Morton order) -> bitfield with mips.
 size_t density_scratch_bytes(uint32_t n_cascades);
+// density-grid maintenance (update_density_grid_nerf): samples, the random-frame warp, and the
+// max splat + decay of the float grid; coords are NerfCoordinate-strided (pos 0..2, dir 8..10)
+cudaError_t launch_grid_samples(uint32_t n_uniform, uint32_t n_nonuniform, uint64_t rng_state, uint64_t rng_inc, uint32_t step,
+                                const float* aabb_min, const float* aabb_max, const float* grid, uint32_t n_cascades, float* coords,
+                                uint32_t stride, uint32_t* indices, cudaStream_t s);
+cudaError_t launch_warp_random(const FrameView* frames_dev, uint32_t n_frames, const DeformView& dv, float* coords, uint32_t stride,
+                               uint32_t n, uint64_t rng_state, uint64_t rng_inc, uint32_t* err, cudaStream_t s);
+cudaError_t launch_splat_ema(uint32_t n, const uint32_t* indices, const uint2* out, const float4* out_f32, int f32_out, float* tmp,
+                             float* grid, uint32_t n_cells, float decay, cudaStream_t s);
 cudaError_t launch_density_grid(const void* grid, int fp16, uint32_t n_cascades, void* scratch, uint8_t* bitfield, cudaStream_t s);
 cudaError_t launch_canonical_map_soa(const FrameView& fv, const DeformView& dv, const float* pts, int64_t n, int32_t* out_idx,
                                      float* out_canon, uint32_t* err, cudaStream_t s);

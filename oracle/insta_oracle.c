@@ -524,6 +524,95 @@ float orc_density_grid_to_bitfield(const float *grid, uint32_t n_cascades, uint8
     return thresh;
 }
 
+/* ------------------------------------------------ density-grid maintenance */
+uint32_t orc_pcg32_next_uint(orc_pcg32 *r) {
+    const uint64_t old = r->state;
+    r->state = old * 0x5851f42d4c957f2dull + r->inc;
+    const uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    const uint32_t rot = (uint32_t)(old >> 59u);
+    return (xorshifted >> rot) | (xorshifted << ((~rot + 1u) & 31u));
+}
+
+float orc_pcg32_next_float(orc_pcg32 *r) {
+    const uint32_t bits = (orc_pcg32_next_uint(r) >> 9) | 0x3f800000u;
+    float f;
+    memcpy(&f, &bits, 4);
+    return f - 1.0f;
+}
+
+void orc_pcg32_advance(orc_pcg32 *r, int64_t delta_) {
+    uint64_t cur_mult = 0x5851f42d4c957f2dull, cur_plus = r->inc, acc_mult = 1u, acc_plus = 0u;
+    uint64_t delta = (uint64_t)delta_;
+    while (delta > 0) {
+        if (delta & 1) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1) * cur_plus;
+        cur_mult *= cur_mult;
+        delta /= 2;
+    }
+    r->state = acc_mult * r->state + acc_plus;
+}
+
+void orc_pcg32_seed(orc_pcg32 *r, uint64_t initstate, uint64_t initseq) {
+    r->state = 0u;
+    r->inc = (initseq << 1u) | 1u;
+    orc_pcg32_next_uint(r);
+    r->state += initstate;
+    orc_pcg32_next_uint(r);
+}
+
+void orc_grid_samples(uint32_t n_uniform, uint32_t n_nonuniform, orc_pcg32 rng, uint32_t step, const float *aabb_min,
+                      const float *aabb_max, const float *grid, uint32_t n_cascades, float *out_pos, uint32_t *out_idx) {
+    const uint32_t n = n_uniform + n_nonuniform;
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+        const uint32_t i = (uint32_t)ii;
+        const int uniform = i < n_uniform;
+        const uint32_t li = uniform ? i : i - n_uniform, ne = uniform ? n_uniform : n_nonuniform;
+        const float thresh = uniform ? -0.01f : 0.01f;
+        orc_pcg32 r = rng;
+        orc_pcg32_advance(&r, (int64_t)(uint32_t)(li * 4u));
+        const uint32_t level = (uint32_t)(orc_pcg32_next_float(&r) * (float)n_cascades) % n_cascades;
+        uint32_t idx = 0;
+        for (uint32_t j = 0; j < 10; ++j) {
+            idx = ((li + step * ne) * 56924617u + j * 19349663u + 96925573u) % GRID3;
+            idx += level * GRID3;
+            if (grid[idx] > thresh) break;
+        }
+        const uint32_t cell = idx % GRID3;
+        const float cc[3] = {(float)morton_invert(cell), (float)morton_invert(cell >> 1), (float)morton_invert(cell >> 2)};
+        float rr[3];
+        for (int k = 0; k < 3; ++k) rr[k] = orc_pcg32_next_float(&r);
+        const float scale = scalbnf(1.0f, (int)level);
+        for (int k = 0; k < 3; ++k) {
+            const float pos = ((cc[k] + rr[k]) / (float)GRID - 0.5f) * scale + 0.5f;
+            out_pos[(size_t)i * 3 + k] = (pos - aabb_min[k]) / (aabb_max[k] - aabb_min[k]);
+        }
+        out_idx[i] = idx;
+    }
+}
+
+void orc_warp_random_samples(const orc_deform *frames, uint32_t n_frames, orc_pcg32 rng, float *pos, int64_t n, uint32_t *out_frame) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) {
+        orc_pcg32 r = rng;
+        orc_pcg32_advance(&r, (int64_t)(uint32_t)((uint32_t)i * n_frames));
+        const uint32_t fid = (uint32_t)(orc_pcg32_next_float(&r) * (float)n_frames);
+        if (out_frame) out_frame[i] = fid;
+        if (fid >= n_frames) continue;
+        const orc_deform *d = &frames[fid];
+        float *p = &pos[i * 3];
+        const int32_t id = nearest_one(d, p);
+        if (id < 0) continue;
+        float o[3];
+        if (d->fp64) map_with_triangle_d(d, id, p, NULL, o, NULL);
+        else map_with_triangle_f(d, id, p, NULL, o, NULL);
+        memcpy(p, o, 12);
+    }
+}
+
 /* ------------------------------------------------- low-discrepancy jitter */
 /* Sobol direction numbers for dimensions 0 and 1 (van der Corput and the x+1 primitive
  * polynomial), generated by the standard recurrence (NGP/random_val.cuh:159-216 uses the

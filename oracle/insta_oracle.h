@@ -77,6 +77,23 @@ void orc_canonical_map_coords(const orc_deform *d, float *coords, uint32_t strid
 /* ---- occupancy --------------------------------------------------------- */
 void orc_occupancy_from_mesh(const orc_tri *tris, int n_tris, double radius, uint8_t *bitfield);
 float orc_density_grid_to_bitfield(const float *grid, uint32_t n_cascades, uint8_t *bitfield);
+
+/* ---- density-grid maintenance -------------------------------------------- */
+/* PCG32 (the pcg32 of tiny-cuda-nn, absent from the reference tree: restated from O'Neill's
+ * published PCG XSH-RR 64/32 generator with its jump-ahead). */
+typedef struct { uint64_t state, inc; } orc_pcg32;
+uint32_t orc_pcg32_next_uint(orc_pcg32 *r);
+float orc_pcg32_next_float(orc_pcg32 *r);
+void orc_pcg32_advance(orc_pcg32 *r, int64_t delta);
+void orc_pcg32_seed(orc_pcg32 *r, uint64_t initstate, uint64_t initseq);
+/* generate_grid_samples_nerf_nonuniform (ngp/src/testbed_nerf.cu:487-516) for the uniform
+ * (thresh -0.01) and the non-uniform (thresh 0.01) set, both from the same generator state:
+ * out_pos [n][3] (warp_position'ed), out_idx [n]. */
+void orc_grid_samples(uint32_t n_uniform, uint32_t n_nonuniform, orc_pcg32 rng, uint32_t step, const float *aabb_min,
+                      const float *aabb_max, const float *grid, uint32_t n_cascades, float *out_pos, uint32_t *out_idx);
+/* warp_random_samples (src/core.cu:528-579): a random frame of n_frames per point, its nearest
+ * triangle, the canonical position; pos [n][3] in place; out_frame [n] (optional). */
+void orc_warp_random_samples(const orc_deform *frames, uint32_t n_frames, orc_pcg32 rng, float *pos, int64_t n, uint32_t *out_frame);
 uint32_t orc_morton3d(uint32_t x, uint32_t y, uint32_t z);
 
 /* ---- field (hash grid + SH + MLPs) ------------------------------------ */

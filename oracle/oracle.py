@@ -222,6 +222,55 @@ def density_grid_to_bitfield(grid, n_cascades):
     return bits, float(t)
 
 
+class Pcg32(C.Structure):
+    """pcg32 state (tiny-cuda-nn's default_rng_t), restated in insta_oracle.c."""
+    _fields_ = [("state", C.c_uint64), ("inc", C.c_uint64)]
+
+    @staticmethod
+    def seeded(initstate: int, initseq: int = 1) -> "Pcg32":
+        r = Pcg32()
+        lib().orc_pcg32_seed(C.byref(r), C.c_uint64(initstate), C.c_uint64(initseq))
+        return r
+
+    def copy(self) -> "Pcg32":
+        return Pcg32(self.state, self.inc)
+
+    def next_uint(self) -> int:
+        f = lib().orc_pcg32_next_uint
+        f.restype = C.c_uint32
+        return int(f(C.byref(self)))
+
+    def next_float(self) -> float:
+        f = lib().orc_pcg32_next_float
+        f.restype = C.c_float
+        return float(f(C.byref(self)))
+
+    def advance(self, delta: int = 1 << 32):
+        lib().orc_pcg32_advance(C.byref(self), C.c_int64(delta))
+
+
+def grid_samples(n_uniform, n_nonuniform, rng: Pcg32, step, aabb, grid, n_cascades):
+    """generate_grid_samples_nerf_nonuniform for both sets: positions [n, 3] and cell indices [n]."""
+    n = n_uniform + n_nonuniform
+    pos = np.zeros((n, 3), np.float32)
+    idx = np.zeros(n, np.uint32)
+    mn = np.asarray(aabb[0], np.float32)
+    mx = np.asarray(aabb[1], np.float32)
+    g = np.ascontiguousarray(grid, dtype=np.float32)
+    lib().orc_grid_samples(C.c_uint32(n_uniform), C.c_uint32(n_nonuniform), rng, C.c_uint32(step), ptr(mn), ptr(mx), ptr(g),
+                           C.c_uint32(n_cascades), ptr(pos), ptr(idx))
+    return pos, idx
+
+
+def warp_random_samples(deforms, rng: Pcg32, pos):
+    """warp_random_samples over the frames' Deformation objects: canonical positions and the frame each point took."""
+    arr = (Deform * len(deforms))(*[d.d for d in deforms])
+    p = np.ascontiguousarray(pos, dtype=np.float32).copy()
+    fr = np.zeros(len(p), np.uint32)
+    lib().orc_warp_random_samples(arr, C.c_uint32(len(deforms)), rng, ptr(p), C.c_int64(len(p)), ptr(fr))
+    return p, fr
+
+
 def render_cfg(width, height, focal, cam, render_box, train_box=((0, 0, 0), (1, 1, 1)), cone_angle=1 / 256, spp=0,
                min_transmittance=0.01, max_samples=1024, frame_id=0, snap=True, linear_colors=False) -> RenderCfg:
     r = RenderCfg()

@@ -136,3 +136,46 @@ def test_param_count_without_gpu():
     from insta_gb300 import abi, layout, synthetic as S
     fc = S.FieldConfig()
     assert abi.param_count(fc) == layout.field_layout(fc).total
+
+
+def test_pcg32_published_sequence(oracle):
+    """The pcg32 restatement (tiny-cuda-nn's default_rng_t) reproduces the PCG demo's first outputs
+    for seed 42, sequence 54, and its jump-ahead equals stepping."""
+    r = oracle.Pcg32.seeded(42, 54)
+    assert [r.next_uint() for _ in range(6)] == [0xa15c02b7, 0x7b47f409, 0xba1d3330, 0x83d2f293, 0xbfa4784b, 0xcbed606e]
+    a = oracle.Pcg32.seeded(7)
+    b = a.copy()
+    for _ in range(1000):
+        a.next_uint()
+    b.advance(1000)
+    assert (a.state, a.inc) == (b.state, b.inc)
+    c, e = oracle.Pcg32.seeded(9), oracle.Pcg32.seeded(9)
+    c.advance(1 << 32)
+    e.advance(1 << 31)
+    e.advance(1 << 31)
+    assert c.state == e.state
+    f = oracle.Pcg32.seeded(3).next_float()
+    assert 0.0 <= f < 1.0
+
+
+def test_grid_samples_land_in_their_cells(oracle):
+    """generate_grid_samples_nerf_nonuniform: every sample lies in the cell its index names (at the
+    cell's cascade scale), and non-uniform samples prefer cells above the threshold."""
+    rng = np.random.default_rng(0)
+    grid = np.where(rng.random(2 * 128 ** 3) < 0.3, 0.5, 0.0).astype(np.float32)
+    pos, idx = oracle.grid_samples(5000, 5000, oracle.Pcg32.seeded(11), 3, ((0, 0, 0), (1, 1, 1)), grid, 2)
+    level = idx // 128 ** 3
+    cell = idx % 128 ** 3
+
+    def compact(x):
+        x = x & 0x49249249
+        x = (x | (x >> 2)) & 0xc30c30c3
+        x = (x | (x >> 4)) & 0x0f00f00f
+        x = (x | (x >> 8)) & 0xff0000ff
+        return (x | (x >> 16)) & 0x0000ffff
+
+    c = np.stack([compact(cell.astype(np.int64) >> k) for k in range(3)], 1)
+    local = ((pos - 0.5) / np.exp2(level)[:, None] + 0.5) * 128
+    assert (np.floor(local + 1e-4) >= c - 1e-3).all() and (local <= c + 1 + 1e-4).all()
+    occupied = grid[idx] > 0
+    assert occupied[5000:].mean() > 0.9 and occupied[:5000].mean() < 0.45
