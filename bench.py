@@ -452,6 +452,54 @@ def run_map(args):
     ctx.close()
 
 
+def run_grid(args):
+    """Density-grid maintenance (update_density_grid_nerf with the random-frame warp) at the sizes
+    training_prep_nerf uses with 2 cascades: the first 256 steps take 128^3 x 2 uniform samples,
+    later steps 128^3 / 4 x 2 uniform + as many non-uniform.  8 tracked frames to pick from; the
+    bench field (16-level hash grid, 32-64-16 / 32-64-64-3 MLPs).  Device time from the library's
+    stage events (the update, then the bitfield of frame 0)."""
+    import torch
+    from insta_gb300 import abi, synthetic as S
+    from oracle import oracle as O
+    av = S.make_avatar(0)
+    fc = S.FieldConfig()
+    ctx = abi.Context(0)
+    ctx.canonical_set(0, av.canonical, av.faces, av.mask)
+    for k in range(8):
+        ctx.frame_upload(0, k, av.frame(av.frame_coeffs(k)))
+    ctx.params_load(0, fc, S.field_params(fc, seed=0))
+    n_casc = 2
+    ctx.density_grid_reset(0, n_casc, None)
+    grid_rng = O.Pcg32.seeded(1337)
+    warp_rng = O.Pcg32.seeded(42)
+    out = {}
+    for name, (nu, nn) in {"early (128^3 x 2 uniform)": (128 ** 3 * n_casc, 0),
+                           "later (128^3/4 x 2 uniform + non-uniform)": (128 ** 3 // 4 * n_casc, 128 ** 3 // 4 * n_casc)}.items():
+        desc = abi.DensityUpdateDesc()
+        desc.decay, desc.n_uniform, desc.n_nonuniform, desc.n_cascades = 0.95, nu, nn, n_casc
+        desc.aabb_max[:] = [1.0, 1.0, 1.0]
+        desc.grid_rng = abi.Pcg32State(grid_rng.state, grid_rng.inc)
+        desc.warp_rng = abi.Pcg32State(warp_rng.state, warp_rng.inc)
+        desc.n_frames, desc.bitfield_frame = 8, 0
+        for _ in range(max(3, args.warmup)):
+            ctx.density_grid_update(0, desc)
+        ctx.sync()
+        ctx.stats(reset=True)
+        ctx.stats_enable(True)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.density_grid_update(0, desc)
+        ctx.sync()
+        wall = (time.perf_counter() - t0) / args.steps
+        st = ctx.stats(reset=True)
+        ctx.stats_enable(False)
+        dev = st["stage_ms"]["occupancy"] / args.steps
+        out[name] = {"samples": nu + nn, "ms_per_update": dev, "wall_ms_per_update": wall * 1e3,
+                     "samples_per_s": (nu + nn) / (dev / 1e3)}
+    print(json.dumps({"workload": "density-grid update, 2 cascades, 8 frames", "results": out}), flush=True)
+    ctx.close()
+
+
 def run_serve(args):
     """Served mixed stream: 8 resident avatars, Poisson arrivals, each request a fresh expression
     (its own frame upload, LBVH, occupancy) at a resolution drawn from {256, 512, 768, 1024}^2.
@@ -623,10 +671,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--width", type=int, default=512, help="square render size (512 = the benchmark workload)")
-    ap.add_argument("--workload", choices=["render", "batch", "serve", "precision", "map"], default="render",
+    ap.add_argument("--workload", choices=["render", "batch", "serve", "precision", "map", "grid"], default="render",
                     help="render: the benchmark line; batch: 64 expressions in one wavefront; serve: request stream; "
                          "precision: FP16 / BF16 / FP8 MLPs at 1024x1024 against the FP64 oracle; "
-                         "map: canonical mapping of 1M shell points")
+                         "map: canonical mapping of 1M shell points; grid: density-grid update")
     ap.add_argument("--rows", type=int, default=16, help="precision: image rows rendered by the FP64 oracle")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--rate", type=float, default=240.0)
@@ -644,6 +692,8 @@ def main():
         return run_precision(args)
     if args.workload == "map":
         return run_map(args)
+    if args.workload == "grid":
+        return run_grid(args)
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -1062,12 +1062,26 @@ int insta_density_grid_update(insta_ctx* ctx, int avatar, insta_density_update_d
         ctx->alloc(w.out, tiles * 128 * sizeof(uint2));
         ctx->alloc(w.out_f32, tiles * 128 * sizeof(float4));
         {
-            Stage st(ctx, INSTA_STAGE_OCCUPANCY, 6);
+            Stage st(ctx, INSTA_STAGE_OCCUPANCY, (uint32_t)d->n_frames <= kMaxRequests ? 11 : 6);
             CK(cudaMemsetAsync(ctx->grid_tmp.p, 0, (size_t)d->n_cascades * GRID3 * sizeof(float), ctx->stream));
             CK(launch_grid_samples(d->n_uniform, d->n_nonuniform, d->grid_rng.state, d->grid_rng.inc, d->ema_step, d->aabb_min, d->aabb_max,
                                    (const float*)a.density_grid.p, d->n_cascades, coords, stride, idx, ctx->stream));
-            CK(launch_warp_random((const FrameView*)a.frame_table.p, (uint32_t)d->n_frames, deform_view(a), coords, stride, n,
-                                  d->warp_rng.state, d->warp_rng.inc, ctx->err_dev, ctx->stream));
+            if ((uint32_t)d->n_frames <= kMaxRequests) {
+                // the sample domain: cascade c spans 0.5 -+ 2^(c-1) of the unit cube, relative to the box
+                const float half = 0.5f * (float)(1u << (d->n_cascades - 1));
+                float lo[3], hi[3];
+                for (int k = 0; k < 3; ++k) {
+                    const float ext = d->aabb_max[k] - d->aabb_min[k];
+                    lo[k] = (0.5f - half - d->aabb_min[k]) / ext;
+                    hi[k] = (0.5f + half - d->aabb_min[k]) / ext;
+                }
+                ctx->alloc(ctx->map_scratch, warp_sorted_scratch_bytes(n, (uint32_t)d->n_frames));
+                CK(launch_warp_random_sorted((const FrameView*)a.frame_table.p, (uint32_t)d->n_frames, deform_view(a), coords, stride, n,
+                                             d->warp_rng.state, d->warp_rng.inc, lo, hi, ctx->map_scratch.p, ctx->err_dev, ctx->stream));
+            } else {
+                CK(launch_warp_random((const FrameView*)a.frame_table.p, (uint32_t)d->n_frames, deform_view(a), coords, stride, n,
+                                      d->warp_rng.state, d->warp_rng.inc, ctx->err_dev, ctx->stream));
+            }
             if (d->debug_pos)
                 CK(cudaMemcpy2DAsync(d->debug_pos, 3 * sizeof(float), coords, stride * sizeof(float), 3 * sizeof(float), n,
                                      cudaMemcpyDefault, ctx->stream));

@@ -941,6 +941,121 @@ cudaError_t launch_canonical_map_sorted(const FrameView& fv, const DeformView& d
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ density-grid warp, sorted
+// warp_random_samples (src/core.cu:528-579) for the density-grid update with the samples grouped
+// by (frame, 64^3 cell of the sample domain): the frame each sample draws decides its run, the
+// render's counting sort (runs padded to 128) orders them, and the warp-cooperative walk runs 32
+// neighbours of one frame at a time -- the grid samples lie mostly far from the mesh, where a
+// per-sample walk visits a large part of the tree and 32 neighbours share almost all of it.
+__global__ void __launch_bounds__(256) gwarp_key_kernel(uint32_t n_frames, const float* __restrict__ coords, uint32_t stride, uint32_t n,
+                                                        Pcg32 rng, float3 lo, float3 inv_ext, uint32_t cell_bits,
+                                                        uint32_t* __restrict__ keys, uint32_t* __restrict__ bins, uint32_t* __restrict__ n_round) {
+    const uint32_t lane = threadIdx.x & 31u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *n_round = n;
+    const uint32_t per_axis = 1u << (cell_bits / 3);
+    const float top = (float)(per_axis - 1);
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+        const uint32_t i = b + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t key = 0xffffffffu;
+        if (valid) {
+            Pcg32 r = rng;
+            r.advance((int64_t)(uint32_t)(i * n_frames));
+            uint32_t fid = (uint32_t)__fmul_rn(r.next_float(), (float)n_frames);
+            fid = fid < n_frames ? fid : n_frames - 1;   // next_float < 1, so fid < n_frames already
+            const float* c = coords + (size_t)i * stride;
+            const float pp[3] = {c[0], c[1], c[2]}, l[3] = {lo.x, lo.y, lo.z}, s[3] = {inv_ext.x, inv_ext.y, inv_ext.z};
+            uint32_t q[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) q[k] = (uint32_t)fminf(fmaxf((pp[k] - l[k]) * s[k] * (float)per_axis, 0.f), top);
+            key = (fid << cell_bits) | spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+            keys[i] = key;
+        }
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        if (valid && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(bins + key, (uint32_t)__popc(peers));
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) gwarp_nearest_kernel(const FrameView* __restrict__ frames, const float* __restrict__ coords,
+                                                               uint32_t stride, const uint32_t* __restrict__ order,
+                                                               const uint32_t* __restrict__ keys, const uint32_t* __restrict__ n_padded,
+                                                               uint32_t cell_bits, int32_t* __restrict__ ids, uint32_t* err) {
+    __shared__ WarpScratch wscratch[8];
+    const uint32_t n = *n_padded;   // runs padded to 128: a warp's 32 positions hold one frame
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32u; base < n; base += n_warps * 32u) {
+        const uint32_t m = order[base + lane];
+        const bool valid = m != kNoSample;
+        const uint32_t any = __ballot_sync(0xffffffffu, valid);
+        if (!any) continue;
+        const uint32_t fid = __shfl_sync(0xffffffffu, valid ? keys[m] >> cell_bits : 0u, __ffs(any) - 1);
+        const float* c = coords + (size_t)(valid ? m : 0u) * stride;
+        const V3 p = valid ? v3(c[0], c[1], c[2]) : v3(0.5f, 0.5f, 0.5f);
+        const Nearest q = nearest_warp(frames[fid], p, valid, wscratch[warp], err);
+        if (valid) ids[m] = q.id;
+    }
+}
+
+__global__ void __launch_bounds__(256) gwarp_map_kernel(const FrameView* __restrict__ frames, DeformView dv, float* __restrict__ coords,
+                                                        uint32_t stride, uint32_t n, const uint32_t* __restrict__ keys,
+                                                        const int32_t* __restrict__ ids, uint32_t cell_bits, uint32_t* err) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int32_t id = ids[i];
+        if (id < 0) { atomicOr(err, INSTA_DEVERR_NO_TRI); continue; }
+        float* c = coords + (size_t)i * stride;
+        float o[3];
+        map_to_canonical(dv, frames[keys[i] >> cell_bits].frames, (uint32_t)id, v3(c[0], c[1], c[2]), nullptr, o, nullptr, nullptr);
+        c[0] = o[0]; c[1] = o[1]; c[2] = o[2];
+    }
+}
+
+size_t warp_sorted_scratch_bytes(uint32_t n, uint32_t n_frames) {
+    const uint32_t cb = sort_cell_bits(n_frames);
+    const size_t bins = (size_t)n_frames << cb;
+    return ((size_t)n * 2 + (size_t)n + 128u * (size_t)n_frames + bins + bins / kSortBlock + 2u * (n_frames + 1u) + 2u) * sizeof(uint32_t);
+}
+
+cudaError_t launch_warp_random_sorted(const FrameView* frames_dev, uint32_t n_frames, const DeformView& dv, float* coords, uint32_t stride,
+                                      uint32_t n, uint64_t rng_state, uint64_t rng_inc, const float* dom_lo, const float* dom_hi,
+                                      void* scratch, uint32_t* err, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t cb = sort_cell_bits(n_frames);
+    const uint32_t n_bins = n_frames << cb;
+    uint32_t* keys = static_cast<uint32_t*>(scratch);
+    int32_t* ids = reinterpret_cast<int32_t*>(keys + n);
+    uint32_t* order = keys + 2 * (size_t)n;
+    uint32_t* bins = order + n + 128u * (size_t)n_frames;
+    uint32_t* block_sums = bins + n_bins;
+    uint32_t* req_start = block_sums + n_bins / kSortBlock;
+    uint32_t* req_seg = req_start + n_frames + 1;
+    uint32_t* counters = req_seg + n_frames + 1;
+    WaveArgs a{};
+    a.n_reqs = n_frames;
+    a.cell_bits = cb;
+    a.sort_bins = bins;
+    a.sort_block_sums = block_sums;
+    a.req_start = req_start;
+    a.req_seg = req_seg;
+    a.sample_order = order;
+    a.sample_key = keys;
+    a.n_samples_round = counters;
+    a.n_samples_padded = counters + 1;
+    cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)n_bins * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    Pcg32 r{rng_state, rng_inc};
+    const float3 lo = make_float3(dom_lo[0], dom_lo[1], dom_lo[2]);
+    const float3 inv = make_float3(1.f / (dom_hi[0] - dom_lo[0]), 1.f / (dom_hi[1] - dom_lo[1]), 1.f / (dom_hi[2] - dom_lo[2]));
+    const unsigned grid = (unsigned)std::min<uint32_t>((n + 255) / 256, (uint32_t)sm_count() * 8);
+    gwarp_key_kernel<<<grid, 256, 0, s>>>(n_frames, coords, stride, n, r, lo, inv, cb, keys, bins, counters);
+    sort_scan_kernel<<<n_bins / kSortBlock, kSortBlock, 0, s>>>(bins, block_sums);
+    sort_offsets_kernel<<<1, kSortBlock, 0, s>>>(a, n_bins / kSortBlock);
+    sort_place_kernel<<<sm_count() * 8, 256, 0, s>>>(a);
+    gwarp_nearest_kernel<<<sm_count() * 16, 256, 0, s>>>(frames_dev, coords, stride, order, keys, counters + 1, cb, ids, err);
+    gwarp_map_kernel<<<grid, 256, 0, s>>>(frames_dev, dv, coords, stride, n, keys, ids, cb, err);
+    return cudaGetLastError();
+}
+
 // The deform stage's nearest-triangle query on caller points (32 consecutive points per warp).
 __global__ void __launch_bounds__(256, 4) nearest_debug_kernel(FrameView fr, const float* __restrict__ pts, int64_t n,
                                                                int32_t* __restrict__ out, uint32_t* err) {
