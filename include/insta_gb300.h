@@ -33,6 +33,8 @@
  *                               shade_kernel_nerf (instant-ngp/src/testbed_nerf.cu:2030-2244,2320-2460)
  *   insta_march_debug           the sample positions advance_pos_nerf + generate_next_nerf_network_inputs
  *                               emit per ray (instant-ngp/src/testbed_nerf.cu:634-686,722-795)
+ *   insta_raycast               rta::Core::raycast_flame -> SphereTracer::trace_bvh + shade_kernel_sdf
+ *                               (src/core.cu:74-113,350-402; instant-ngp/src/testbed_sdf.cu:505-577,650-665)
  *   insta_nearest_debug         the render path's warp-cooperative closest_triangle on given points
  *                               (NGP/bvh.cuh:48-96 as called by the warp kernel, src/core.cu:470-478)
  */
@@ -109,7 +111,8 @@ typedef struct {
 #define INSTA_STAGE_CANONICAL_MAP 7  /* insta_canonical_map / _soa               */
 #define INSTA_STAGE_FIELD 8          /* insta_field_eval / _static               */
 #define INSTA_STAGE_SORT 9           /* regrouping a round's samples by (request, cell) */
-#define INSTA_STAGE_COUNT 10
+#define INSTA_STAGE_RAYCAST 10       /* insta_raycast                            */
+#define INSTA_STAGE_COUNT 11
 
 typedef struct {
     uint64_t kernel_launches;        /* kernels the library launched */
@@ -267,6 +270,16 @@ int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples);
 /* Per-ray sample t and dt (device pointers, [h*w][max_out]) and counts [h*w]. */
 int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out, float* out_t, float* out_dt,
                       int32_t* out_n);
+/* rta::Core::raycast_flame (src/core.cu:350-402): the tracked mesh of req->frame ray-traced
+ * from req's camera -- init_rays_with_payload_kernel_sdf (instant-ngp/src/testbed_sdf.cu:505-577,
+ * no slice plane, aperture or octree), the closest hit at t < 10 (TriangleBvh4::ray_intersect,
+ * instant-ngp/src/triangle_bvh.cu:271-311; ties to the lowest triangle id) and INSTA's
+ * shade_kernel_sdf (src/core.cu:74-113: three lights around the canonical centroid, or the normal
+ * as colour when color_normal != 0).  Pixels whose hit lies inside the render box get RGBA
+ * (alpha 1) and depth = the hit's z; the others keep their values.  out_tri (optional): the hit
+ * triangle id or -1.  Host or device pointers. */
+int insta_raycast(insta_ctx* ctx, const insta_render_desc* req, int color_normal, float* out_rgba, float* out_depth,
+                  int32_t* out_tri);
 /* Nearest triangle id of each point (device pointers: pts f32[n*3] in the frame's space, out
  * i32[n]) computed the way the render's deform stage computes it: the warp-cooperative walk over
  * 32 consecutive points. */

@@ -25,7 +25,7 @@ EXPORTS = [
     "insta_density_grid_load", "insta_density_grid_reset", "insta_density_grid_update", "insta_density_grid_read",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
     "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_batch",
-    "insta_render_samples", "insta_march_debug", "insta_nearest_debug",
+    "insta_render_samples", "insta_march_debug", "insta_nearest_debug", "insta_raycast",
     "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
     "insta_server_release", "insta_server_error",
 ]
@@ -62,7 +62,8 @@ class FieldDesc(C.Structure):
                 ("precision", C.c_uint32)]
 
 
-STAGES = ["frame", "occupancy", "ray_init", "march", "deform_encode", "mlp", "composite", "canonical_map", "field", "sort"]
+STAGES = ["frame", "occupancy", "ray_init", "march", "deform_encode", "mlp", "composite", "canonical_map", "field", "sort",
+          "raycast"]
 
 
 class Stats(C.Structure):
@@ -124,6 +125,7 @@ def load(path: Path | None = None):
             "insta_render_samples": [vp, C.POINTER(u64)],
             "insta_march_debug": [vp, C.POINTER(RenderDesc), C.c_int, vp, vp, vp],
             "insta_nearest_debug": [vp, C.c_int, C.c_int, vp, i64, vp],
+            "insta_raycast": [vp, C.POINTER(RenderDesc), C.c_int, vp, vp, vp],
             "insta_server_create": [vp, C.POINTER(ServerConfig), C.POINTER(vp)],
             "insta_server_destroy": [vp],
             "insta_submit": [vp, C.POINTER(RenderDesc), vp, vp, vp, C.POINTER(u64)],
@@ -343,6 +345,9 @@ class Context:
         v = C.c_uint64(0)
         self._check(self.lib.insta_render_samples(self.h, C.byref(v)))
         return int(v.value)
+
+    def raycast(self, req: RenderDesc, out_rgba, out_depth, out_tri=None, color_normal=False):
+        self._check(self.lib.insta_raycast(self.h, C.byref(req), int(color_normal), _addr(out_rgba), _addr(out_depth), _addr(out_tri)))
 
     def nearest_debug(self, avatar, frame, pts, n, out_idx):
         self._check(self.lib.insta_nearest_debug(self.h, avatar, frame, _addr(pts), n, _addr(out_idx)))

@@ -221,6 +221,85 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
     return {bid, -1, best};
 }
 
+// ------------------------------------------------------------------ ray queries
+// Triangle::ray_intersect (NGP/triangle.cuh:66-80) from a leaf record, same operations and order:
+// FLT_MAX for a miss.  v1v0 = b - a is the record's v21; v2v0 = c - a is -v13 and the triangle
+// normal (b - a) x (c - a) is -(v21 x v13), both exact negations.
+__device__ __forceinline__ float tri_ray_rec(const float4* tr, V3 ro, V3 rd, int32_t& id) {
+    const float4 q0 = __ldg(tr), q2 = __ldg(tr + 2), q3 = __ldg(tr + 3), q5 = __ldg(tr + 5), q6 = __ldg(tr + 6), q7 = __ldg(tr + 7);
+    id = __float_as_int(q2.y);
+    const V3 v1v0 = v3(q3.x, q3.y, q3.z), v2v0 = v3(-q5.x, -q5.y, -q5.z), n = v3(-q5.w, -q6.w, -q7.w);
+    const V3 rov0 = sub_rn(ro, v3(q0.x, q0.y, q0.z));
+    const V3 q = cross_rn(rov0, rd);
+    const float d = __fdiv_rn(1.0f, dot_rn(rd, n));
+    const float u = __fmul_rn(d, -dot_rn(q, v2v0));
+    const float v = __fmul_rn(d, dot_rn(q, v1v0));
+    const float t = __fmul_rn(d, -dot_rn(n, rov0));
+    if (u < 0.0f || u > 1.0f || v < 0.0f || __fadd_rn(u, v) > 1.0f || t < 0.0f) return 3.402823466e38f;
+    return t;
+}
+
+// Entry distance of a ray into a box for pruning (slab test; NaN slabs from zero direction
+// components count as inside): +inf when the ray misses it.
+__device__ __forceinline__ float box_ray_entry(float mnx, float mny, float mnz, float mxx, float mxy, float mxz, V3 o, V3 inv) {
+    const float tx1 = (mnx - o.x) * inv.x, tx2 = (mxx - o.x) * inv.x;
+    const float ty1 = (mny - o.y) * inv.y, ty2 = (mxy - o.y) * inv.y;
+    const float tz1 = (mnz - o.z) * inv.z, tz2 = (mxz - o.z) * inv.z;
+    const float tmin = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fmaxf(fminf(tz1, tz2), 0.f));
+    const float tmax = fminf(fminf(fmaxf(tx1, tx2), fmaxf(ty1, ty2)), fmaxf(tz1, tz2));
+    return tmax * 1.0001f + 1e-6f < tmin ? __int_as_float(0x7f800000) : tmin;
+}
+
+// Closest hit with t < t_max (TriangleBvh4::ray_intersect, ngp/src/triangle_bvh.cu:271-311): the
+// exact minimum of tri_ray_rec over all triangles, ties to the lowest triangle id (the reference
+// keeps the first in its BVH order).  A subtree is skipped only when its entry exceeds the
+// running minimum by the prune slack.  Returns {id or -1, Morton slot or -1, t (t_max for no hit)}.
+__device__ __forceinline__ Nearest ray_closest(const FrameView& fr, V3 o, V3 d, float t_max, uint32_t* err) {
+    const V3 inv = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    uint32_t stack[INSTA_STACK];
+    int sp = 0;
+    stack[sp++] = 0u;
+    float best = t_max;
+    int32_t bid = -1, bslot = -1;
+    while (sp > 0) {
+        const uint32_t ref = stack[--sp];
+        if (ref & INSTA_LEAF_BIT) {
+            const uint32_t first = (ref & ~INSTA_LEAF_BIT) >> 3, count = ref & 7u;
+            for (uint32_t i = 0; i < count; ++i) {
+                int32_t id;
+                const float t = tri_ray_rec(fr.leaf_tris + (size_t)(first + i) * INSTA_TRI_F4, o, d, id);
+                if (t < best || (t == best && bid >= 0 && (uint32_t)id < (uint32_t)bid)) { best = t; bid = id; bslot = (int32_t)(first + i); }
+            }
+            continue;
+        }
+        const float4* nd = fr.nodes + (size_t)ref * 7;
+        const float4 mnx = __ldg(nd + 0), mny = __ldg(nd + 1), mnz = __ldg(nd + 2);
+        const float4 mxx = __ldg(nd + 3), mxy = __ldg(nd + 4), mxz = __ldg(nd + 5);
+        const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
+        uint32_t ci[4] = {(uint32_t)ch.x, (uint32_t)ch.y, (uint32_t)ch.z, (uint32_t)ch.w};
+        float ct[4];
+        ct[0] = box_ray_entry(mnx.x, mny.x, mnz.x, mxx.x, mxy.x, mxz.x, o, inv);
+        ct[1] = box_ray_entry(mnx.y, mny.y, mnz.y, mxx.y, mxy.y, mxz.y, o, inv);
+        ct[2] = box_ray_entry(mnx.z, mny.z, mnz.z, mxx.z, mxy.z, mxz.z, o, inv);
+        ct[3] = box_ray_entry(mnx.w, mny.w, mnz.w, mxx.w, mxy.w, mxz.w, o, inv);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (ci[i] == 0xffffffffu) ct[i] = __int_as_float(0x7f800000);
+#define INSTA_CAS(x, y) if (ct[x] < ct[y]) { float td = ct[x]; ct[x] = ct[y]; ct[y] = td; uint32_t ti = ci[x]; ci[x] = ci[y]; ci[y] = ti; }
+        INSTA_CAS(0, 2) INSTA_CAS(1, 3) INSTA_CAS(0, 1) INSTA_CAS(2, 3) INSTA_CAS(1, 2)
+#undef INSTA_CAS
+        const float lim = best + best * 0.0009765625f + 1e-6f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (ci[i] != 0xffffffffu && ct[i] <= lim) {
+                if (sp < INSTA_STACK) stack[sp++] = ci[i];
+                else if (err) atomicOr(err, INSTA_DEVERR_STACK);
+            }
+        }
+    }
+    return {bid, bslot, best};
+}
+
 // Unbounded exact nearest triangle.
 __device__ __forceinline__ Nearest nearest_triangle(const FrameView& fr, V3 p, uint32_t* err) {
     return nearest_bvh(fr, p, __int_as_float(0x7f800000), -1, -1, err);

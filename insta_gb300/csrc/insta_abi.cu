@@ -91,6 +91,7 @@ struct Avatar {
     bool table_dirty = true;
     uint32_t table_frames = 0;
     Field field;
+    float center[3] = {0.f, 0.f, 0.f};   // TinyMesh::m_centorid of the canonical mesh (float sum / V)
     DevBuf density_grid;          // float [grid_cascades][128^3], Morton order (update_density_grid_nerf state)
     uint32_t grid_cascades = 0;
 };
@@ -837,6 +838,11 @@ int insta_canonical_set(insta_ctx* ctx, int avatar, const float* verts, int n_ve
         if (mask) CK(cudaMemcpy(hm.data(), mask, hm.size() * 4, cudaMemcpyDefault));
         a.V = n_verts;
         a.F = n_faces;
+        // TinyMesh::load (src/tiny_mesh.cu:62-86): centroid = float sum of the vertices / V
+        float cs[3] = {0.f, 0.f, 0.f};
+        for (int v = 0; v < n_verts; ++v)
+            for (int k = 0; k < 3; ++k) cs[k] += hv[(size_t)v * 3 + k];
+        for (int k = 0; k < 3; ++k) a.center[k] = cs[k] / (float)n_verts;
         std::vector<int32_t> adj = triangle_neighbours(hf, n_faces, n_verts);
         ctx->alloc(a.faces, hf.size() * 4);
         ctx->alloc(a.mask, hm.size() * 4);
@@ -1405,6 +1411,32 @@ int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out,
         Frame& f = use_frame(ctx, a, req->frame);
         if (!f.has_occupancy) fail(INSTA_ERR_NOT_READY, "frame %d has no occupancy bitfield", req->frame);
         CK(launch_march_debug(render_view(a, *req), (const uint8_t*)f.bitfield.p, max_out, out_t, out_dt, out_n, ctx->stream));
+    });
+}
+
+int insta_raycast(insta_ctx* ctx, const insta_render_desc* req, int color_normal, float* out_rgba, float* out_depth, int32_t* out_tri) {
+    return guarded(ctx, [&] {
+        check_request(req);
+        if (!out_rgba || !out_depth) fail(INSTA_ERR_INVALID_ARG, "null output");
+        Avatar& a = ctx->avatar(req->avatar);
+        Frame& f = use_frame(ctx, a, req->frame);
+        const size_t px = (size_t)req->width * req->height;
+        // host outputs go through device staging (pixels without a hit keep their values)
+        float* rgba = out_rgba;
+        float* depth = out_depth;
+        int32_t* tri = out_tri;
+        const bool h_rgba = !is_device_ptr(out_rgba), h_depth = !is_device_ptr(out_depth), h_tri = out_tri && !is_device_ptr(out_tri);
+        if (h_rgba) { rgba = (float*)ctx->alloc(ctx->out_rgba, px * 16); host_copy(rgba, out_rgba, px * 16, ctx->stream); }
+        if (h_depth) { depth = (float*)ctx->alloc(ctx->out_depth, px * 4); host_copy(depth, out_depth, px * 4, ctx->stream); }
+        if (h_tri) tri = (int32_t*)ctx->alloc(ctx->extra, px * 4);
+        {
+            Stage st(ctx, INSTA_STAGE_RAYCAST, 1);
+            CK(launch_raycast(render_view(a, *req), f.view, a.center, color_normal, rgba, depth, tri, ctx->err_dev, ctx->stream));
+        }
+        if (h_rgba) host_copy(out_rgba, rgba, px * 16, ctx->stream);
+        if (h_depth) host_copy(out_depth, depth, px * 4, ctx->stream);
+        if (h_tri) host_copy(out_tri, tri, px * 4, ctx->stream);
+        if (h_rgba || h_depth || h_tri) ctx->check_device();
     });
 }
 

@@ -170,6 +170,8 @@ cudaError_t launch_unpack(const uint2* out, const float4* out_f32, int bf16, int
 int64_t static_max_samples();
 cudaError_t static_scratch(int device, uint8_t** tiles, uint2** out, float4** out_f32);
 
+cudaError_t launch_raycast(const RenderView& rv, const FrameView& fr, const float* center, int color_normal, float* out_rgba,
+                           float* out_depth, int32_t* out_tri, uint32_t* err, cudaStream_t s);
 cudaError_t launch_nearest_debug(const FrameView& fr, const float* pts, int64_t n, int32_t* out, uint32_t* err, cudaStream_t s);
 cudaError_t launch_march_debug(const RenderView& rv, const uint8_t* bitfield, int max_out, float* out_t, float* out_dt,
                                int32_t* out_n, cudaStream_t s);

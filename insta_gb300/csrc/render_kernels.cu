@@ -1056,6 +1056,72 @@ cudaError_t launch_warp_random_sorted(const FrameView* frames_dev, uint32_t n_fr
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ raycast (visualisation)
+// rta::Core::raycast_flame (src/core.cu:350-402): init_rays_with_payload_kernel_sdf
+// (ngp/src/testbed_sdf.cu:505-577; no slice plane, aperture or octree), the closest hit
+// (raytrace_kernel, ngp/src/triangle_bvh.cu:150-166, hits at t < 10), INSTA's shade_kernel_sdf
+// (src/core.cu:74-113).  One thread per pixel in 8x4 tiles.
+__global__ void __launch_bounds__(256) raycast_kernel(RenderView rv, FrameView fr, float3 center, int color_normal, float* __restrict__ out_rgba,
+                                                      float* __restrict__ out_depth, int32_t* __restrict__ out_tri, uint32_t* err) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t tiles_x = ((uint32_t)rv.width + 7u) / 8u;
+    const uint32_t tile = t / 32u, in = t % 32u;
+    const uint32_t x = (tile % tiles_x) * 8u + in % 8u, y = (tile / tiles_x) * 4u + in / 8u;
+    if (x >= (uint32_t)rv.width || y >= (uint32_t)rv.height) return;
+    const uint32_t idx = x + (uint32_t)rv.width * y;
+    float off[2];
+    ld_random_pixel_offset(rv.snap_to_pixel_centers ? 0u : rv.spp, off);
+    const float u = __fdiv_rn(__fadd_rn((float)x, off[0]), (float)rv.width);
+    const float v = __fdiv_rn(__fadd_rn((float)y, off[1]), (float)rv.height);
+    const V3 dc = v3(__fdiv_rn(__fmul_rn(__fsub_rn(u, rv.screen_center[0]), (float)rv.width), rv.focal[0]),
+                     __fdiv_rn(__fmul_rn(__fsub_rn(v, rv.screen_center[1]), (float)rv.height), rv.focal[1]), 1.0f);
+    const V3 d = normalize_rn(v3(dot_rn(v3(rv.cam[0], rv.cam[1], rv.cam[2]), dc), dot_rn(v3(rv.cam[4], rv.cam[5], rv.cam[6]), dc),
+                                 dot_rn(v3(rv.cam[8], rv.cam[9], rv.cam[10]), dc)));
+    V3 o = v3(rv.cam[3], rv.cam[7], rv.cam[11]);
+    const float t0 = __fadd_rn(fmaxf(aabb_ray_tmin(rv.aabb_min, rv.aabb_max, o, d), 0.0f), 1e-6f);
+    o = v3(__fadd_rn(o.x, __fmul_rn(t0, d.x)), __fadd_rn(o.y, __fmul_rn(t0, d.y)), __fadd_rn(o.z, __fmul_rn(t0, d.z)));
+    const Nearest h = ray_closest(fr, o, d, 10.0f, err);
+    const V3 pos = v3(__fadd_rn(o.x, __fmul_rn(h.d2, d.x)), __fadd_rn(o.y, __fmul_rn(h.d2, d.y)), __fadd_rn(o.z, __fmul_rn(h.d2, d.z)));
+    if (h.id < 0 || !box_contains(rv.aabb_min, rv.aabb_max, pos)) {
+        if (out_tri) out_tri[idx] = -1;
+        return;
+    }
+    if (out_tri) out_tri[idx] = h.id;
+    // Triangle::normal() of the hit, normalised again by the shader
+    float col[3];
+    {
+        const float4* tr = fr.leaf_tris + (size_t)h.slot * INSTA_TRI_F4;
+        const float4 q0 = __ldg(tr), q1 = __ldg(tr + 1), q2 = __ldg(tr + 2);
+        const V3 a = v3(q0.x, q0.y, q0.z), b = v3(q0.w, q1.x, q1.y), c = v3(q1.z, q1.w, q2.x);
+        const V3 nrm = normalize_rn(normalize_rn(cross_rn(sub_rn(b, a), sub_rn(c, a))));
+        if (color_normal) {
+            col[0] = srgb_to_linear(__fadd_rn(__fmul_rn(0.5f, nrm.x), 0.5f));
+            col[1] = srgb_to_linear(__fadd_rn(__fmul_rn(0.5f, nrm.y), 0.5f));
+            col[2] = srgb_to_linear(__fadd_rn(__fmul_rn(0.5f, nrm.z), 0.5f));
+        } else {
+            const float lo[3][3] = {{0.f, 0.f, 1.f}, {1.5f, 0.25f, 0.5f}, {-1.5f, 0.25f, 0.5f}};
+            float cs = 0.f;
+#pragma unroll
+            for (int l = 0; l < 3; ++l) {
+                const V3 light = v3(__fadd_rn(center.x, lo[l][0]), __fadd_rn(center.y, lo[l][1]), __fadd_rn(center.z, lo[l][2]));
+                cs = __fadd_rn(cs, __fmul_rn(__fmul_rn(1.f / 3.f, fminf(1.f, fmaxf(dot_rn(nrm, light), 0.f))), 0.75f));
+            }
+            col[0] = col[1] = col[2] = srgb_to_linear(cs);
+        }
+    }
+    reinterpret_cast<float4*>(out_rgba)[idx] = make_float4(col[0], col[1], col[2], 1.0f);
+    out_depth[idx] = pos.z;
+}
+
+cudaError_t launch_raycast(const RenderView& rv, const FrameView& fr, const float* center, int color_normal, float* out_rgba,
+                           float* out_depth, int32_t* out_tri, uint32_t* err, cudaStream_t s) {
+    const uint32_t tiles = (((uint32_t)rv.width + 7u) / 8u) * (((uint32_t)rv.height + 3u) / 4u);
+    if (tiles == 0) return cudaSuccess;
+    raycast_kernel<<<(tiles * 32u + 255u) / 256u, 256, 0, s>>>(rv, fr, make_float3(center[0], center[1], center[2]), color_normal,
+                                                              out_rgba, out_depth, out_tri, err);
+    return cudaGetLastError();
+}
+
 // The deform stage's nearest-triangle query on caller points (32 consecutive points per warp).
 __global__ void __launch_bounds__(256, 4) nearest_debug_kernel(FrameView fr, const float* __restrict__ pts, int64_t n,
                                                                int32_t* __restrict__ out, uint32_t* err) {

@@ -793,6 +793,83 @@ static int ray_next_sample(const orc_render_cfg *rc, const uint8_t *bf, ray_stat
     return 1;
 }
 
+/* ------------------------------------------------------------ raycast (visualisation) */
+/* Triangle::ray_intersect (NGP/triangle.cuh:66-80), FLT_MAX for a miss. */
+static float tri_ray_t(const orc_tri *tr, const float *ro, const float *rd) {
+    float v1v0[3], v2v0[3], rov0[3];
+    for (int k = 0; k < 3; ++k) { v1v0[k] = tr->b[k] - tr->a[k]; v2v0[k] = tr->c[k] - tr->a[k]; rov0[k] = ro[k] - tr->a[k]; }
+    const float n[3] = {v1v0[1] * v2v0[2] - v1v0[2] * v2v0[1], v1v0[2] * v2v0[0] - v1v0[0] * v2v0[2], v1v0[0] * v2v0[1] - v1v0[1] * v2v0[0]};
+    const float q[3] = {rov0[1] * rd[2] - rov0[2] * rd[1], rov0[2] * rd[0] - rov0[0] * rd[2], rov0[0] * rd[1] - rov0[1] * rd[0]};
+    const float d = 1.0f / v3dot(rd, n);
+    const float u = d * -v3dot(q, v2v0);
+    const float v = d * v3dot(q, v1v0);
+    float t = d * -v3dot(n, rov0);
+    if (u < 0.0f || u > 1.0f || v < 0.0f || (u + v) > 1.0f || t < 0.0f) t = FLT_MAX;
+    return t;
+}
+
+static float srgb_to_linear_f(float s) { return s <= 0.04045f ? s / 12.92f : powf((s + 0.055f) / 1.055f, 2.4f); }
+
+/* rta::Core::raycast_flame (src/core.cu:350-402): init_rays_with_payload_kernel_sdf
+ * (ngp/src/testbed_sdf.cu:505-577, no slice plane, no octree), the closest hit of
+ * TriangleBvh4::ray_intersect (ngp/src/triangle_bvh.cu:271-311, hits at t < 10, ties to the lowest
+ * triangle id) and INSTA's shade_kernel_sdf (src/core.cu:74-113).  Pixels whose hit point is
+ * outside the render box (or without a hit) keep their values; out_tri gets -1 there. */
+void orc_raycast(const orc_render_cfg *rc, const orc_tri *tris, int n_tris, const float *center, int color_normal, float *out_rgba,
+                 float *out_depth, int32_t *out_tri) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t pix = 0; pix < (int64_t)rc->width * rc->height; ++pix) {
+        const int x = (int)(pix % rc->width), y = (int)(pix / rc->width);
+        float off[2];
+        orc_ld_random_pixel_offset(rc->snap_to_pixel_centers ? 0u : rc->spp, off);
+        const float u = ((float)x + off[0]) / (float)rc->width, v = ((float)y + off[1]) / (float)rc->height;
+        const float dc[3] = {(u - rc->screen_center[0]) * (float)rc->width / rc->focal[0],
+                             (v - rc->screen_center[1]) * (float)rc->height / rc->focal[1], 1.0f};
+        float d[3], o[3];
+        for (int k = 0; k < 3; ++k) { const float *row = &rc->cam[k * 4]; float rr[3] = {row[0], row[1], row[2]}; d[k] = v3dot(rr, dc); }
+        const float z = v3dot(d, d);
+        if (z > 0.f) { const float sz = sqrtf(z); d[0] /= sz; d[1] /= sz; d[2] /= sz; }
+        for (int k = 0; k < 3; ++k) o[k] = rc->cam[k * 4 + 3];
+        const float tm = aabb_ray_tmin(rc->render_aabb_min, rc->render_aabb_max, o, d);
+        const float t0 = fmaxf(tm, 0.0f) + 1e-6f;
+        for (int k = 0; k < 3; ++k) o[k] = o[k] + t0 * d[k];
+        float best = 10.0f;   /* MAX_DIST */
+        int32_t bid = -1;
+        for (int t = 0; t < n_tris; ++t) {
+            const float tt = tri_ray_t(&tris[t], o, d);
+            if (tt < best || (tt == best && bid >= 0 && (uint32_t)tris[t].id < (uint32_t)bid)) { best = tt; bid = (int32_t)tris[t].id; }
+        }
+        float pos[3];
+        for (int k = 0; k < 3; ++k) pos[k] = o[k] + best * d[k];
+        if (bid < 0 || !box_contains(rc->render_aabb_min, rc->render_aabb_max, pos)) { if (out_tri) out_tri[pix] = -1; continue; }
+        if (out_tri) out_tri[pix] = bid;
+        const orc_tri *tr = NULL;
+        for (int t = 0; t < n_tris; ++t) if ((int32_t)tris[t].id == bid) { tr = &tris[t]; break; }
+        float e1[3], e2[3];
+        for (int k = 0; k < 3; ++k) { e1[k] = tr->b[k] - tr->a[k]; e2[k] = tr->c[k] - tr->a[k]; }
+        float nrm[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        for (int rep = 0; rep < 2; ++rep) {   /* Triangle::normal(), then the shader's normalized() */
+            const float nz = v3dot(nrm, nrm);
+            if (nz > 0.f) { const float s = sqrtf(nz); nrm[0] /= s; nrm[1] /= s; nrm[2] /= s; }
+        }
+        float col[3];
+        if (color_normal) {
+            for (int k = 0; k < 3; ++k) col[k] = srgb_to_linear_f(0.5f * nrm[k] + 0.5f);
+        } else {
+            const float lo[3][3] = {{0.f, 0.f, 1.f}, {1.5f, 0.25f, 0.5f}, {-1.5f, 0.25f, 0.5f}};
+            float cs[3] = {0.f, 0.f, 0.f};
+            for (int l = 0; l < 3; ++l) {
+                const float light[3] = {center[0] + lo[l][0], center[1] + lo[l][1], center[2] + lo[l][2]};
+                const float w = (1 / 3.f) * fminf(1.f, fmaxf(v3dot(nrm, light), 0.f));
+                for (int k = 0; k < 3; ++k) cs[k] += w * 0.75f;
+            }
+            for (int k = 0; k < 3; ++k) col[k] = srgb_to_linear_f(cs[k]);
+        }
+        out_rgba[pix * 4 + 0] = col[0]; out_rgba[pix * 4 + 1] = col[1]; out_rgba[pix * 4 + 2] = col[2]; out_rgba[pix * 4 + 3] = 1.0f;
+        out_depth[pix] = pos[2];
+    }
+}
+
 int orc_march_ray(const orc_render_cfg *rc, const uint8_t *bf, int px, int py, int max_out, float *out_t, float *out_dt,
                   float *out_pos) {
     ray_state r;

@@ -137,6 +137,8 @@ int64_t orc_render(const orc_render_cfg *rc, const orc_deform *d, const uint8_t 
                    const orc_field_cfg *fc, const uint16_t *params, const float *layer_scales,
                    int row_begin, int row_end, float *out_rgba, float *out_depth,
                    uint32_t *out_nsamples, int fp64);
+void orc_raycast(const orc_render_cfg *rc, const orc_tri *tris, int n_tris, const float *center, int color_normal, float *out_rgba,
+                 float *out_depth, int32_t *out_tri);
 int orc_march_ray(const orc_render_cfg *rc, const uint8_t *bitfield, int px, int py,
                   int max_out, float *out_t, float *out_dt, float *out_pos);
 void orc_training_samples(const float *aabb_min, const float *aabb_max, float cone, const uint8_t *bf, const float *rays,

@@ -316,6 +316,26 @@ def render(rc: RenderCfg, deform: Deformation, bits, fc, params, rows=None, fp64
     return rgba, depth, ns, int(total)
 
 
+def raycast(rc: RenderCfg, tris, center, color_normal=False, rgba=None, depth=None):
+    """raycast_flame: (rgba [h*w, 4], depth [h*w], hit triangle id or -1 [h*w]); rgba/depth keep
+    their given values where nothing inside the render box is hit."""
+    n = rc.width * rc.height
+    rgba = np.zeros((n, 4), np.float32) if rgba is None else np.ascontiguousarray(rgba, np.float32).copy()
+    depth = np.zeros(n, np.float32) if depth is None else np.ascontiguousarray(depth, np.float32).copy()
+    tri = np.zeros(n, np.int32)
+    c = np.ascontiguousarray(center, np.float32)
+    lib().orc_raycast(C.byref(rc), ptr(tris), C.c_int(len(tris)), ptr(c), C.c_int(int(color_normal)), ptr(rgba), ptr(depth), ptr(tri))
+    return rgba, depth, tri
+
+
+def mesh_centroid(verts) -> np.ndarray:
+    """TinyMesh::m_centorid: float32 running sum of the vertices in order, divided by their count."""
+    c = np.zeros(3, np.float32)
+    for v in np.asarray(verts, np.float32):
+        c = (c + v).astype(np.float32)
+    return (c / np.float32(len(verts))).astype(np.float32)
+
+
 def march_ray(rc: RenderCfg, bits, px, py, max_out=1024):
     t = np.zeros(max_out, dtype=np.float32)
     dt = np.zeros(max_out, dtype=np.float32)

@@ -93,6 +93,47 @@ def test_render_nearest_bit_exact(gpu_avatar, oracle, oracle_frame, avatar, fram
     assert (ids[pick] == brute_ids).all()
 
 
+@pytest.mark.parametrize("yaw,color_normal", [(0.0, False), (35.0, True), (-60.0, False)])
+def test_raycast_matches_oracle(gpu_avatar, oracle, oracle_frame, avatar, yaw, color_normal):
+    """raycast_flame on the tracked frame: hit triangle ids and depths bit-exact (ties to the
+    lowest id), shaded colours within 1e-5 (powf in srgb_to_linear), untouched pixels kept."""
+    from insta_gb300 import synthetic as S
+    W = H = 128
+    cam, focal = S.camera(yaw, width=W, height=H)
+    req = gpu_avatar.render_desc(0, 0, W, H, focal, cam)
+    rgba = torch.full((W * H, 4), -1.0, dtype=torch.float32, device="cuda")
+    depth = torch.full((W * H,), -1.0, dtype=torch.float32, device="cuda")
+    tri = torch.empty(W * H, dtype=torch.int32, device="cuda")
+    gpu_avatar.raycast(req, rgba, depth, tri, color_normal=color_normal)
+    gpu_avatar.sync()
+    rc = oracle.render_cfg(W, H, focal, cam, avatar.render_aabb())
+    center = oracle.mesh_centroid(avatar.canonical)
+    o_rgba, o_depth, o_tri = oracle.raycast(rc, oracle_frame["def"], center, color_normal,
+                                            np.full((W * H, 4), -1.0, np.float32), np.full(W * H, -1.0, np.float32))
+    got_tri = tri.cpu().numpy()
+    assert (got_tri == o_tri).all(), int((got_tri != o_tri).sum())
+    hit = o_tri >= 0
+    assert hit.sum() > W * H // 10
+    assert (depth.cpu().numpy() == o_depth).all()
+    assert np.abs(rgba.cpu().numpy() - o_rgba).max() <= 1e-5
+    assert (rgba.cpu().numpy()[~hit] == -1.0).all()
+
+
+def test_raycast_host_buffers(gpu_avatar):
+    from insta_gb300 import synthetic as S
+    cam, focal = S.camera(10.0, width=64, height=48)
+    req = gpu_avatar.render_desc(0, 0, 64, 48, focal, cam)
+    rgba = np.full((64 * 48, 4), 7.0, np.float32)
+    depth = np.full(64 * 48, 7.0, np.float32)
+    d_rgba = torch.full((64 * 48, 4), 7.0, dtype=torch.float32, device="cuda")
+    d_depth = torch.full((64 * 48,), 7.0, dtype=torch.float32, device="cuda")
+    gpu_avatar.raycast(req, rgba, depth)
+    gpu_avatar.raycast(req, d_rgba, d_depth)
+    gpu_avatar.sync()
+    assert (rgba == d_rgba.cpu().numpy()).all() and (depth == d_depth.cpu().numpy()).all()
+    assert (rgba[:, 3] == 1.0).any() and (rgba[:, 3] == 7.0).any()
+
+
 def make_coords(pts, dirs, holder, n_extra=0, extra_val=0.25):
     n = len(pts)
     c = np.zeros((n, 11 + n_extra), np.float32)
