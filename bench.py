@@ -500,6 +500,50 @@ def run_grid(args):
     ctx.close()
 
 
+def run_raycast(args):
+    """raycast_flame of the 10,240-triangle tracked frame at 512^2 and 1024^2 (closest hit over the
+    frame's LBVH + shading).  Device time from the library's stage events; the CPU restatement
+    (brute-force closest hit) is timed on 8 image rows."""
+    import torch
+    from insta_gb300 import abi, synthetic as S
+    from oracle import oracle as O
+    av = S.make_avatar(0)
+    frame = av.frame(av.frame_coeffs(0))
+    ctx = abi.Context(0)
+    ctx.canonical_set(0, av.canonical, av.faces, av.mask)
+    ctx.frame_upload(0, 0, frame)
+    out = {}
+    for w in (512, 1024):
+        cam, focal = S.camera(0.0, width=w, height=w)
+        req = ctx.render_desc(0, 0, w, w, focal, cam)
+        rgba = torch.zeros((w * w, 4), device="cuda")
+        depth = torch.zeros(w * w, device="cuda")
+        for _ in range(max(3, args.warmup)):
+            ctx.raycast(req, rgba, depth)
+        ctx.sync()
+        ctx.stats(reset=True)
+        ctx.stats_enable(True)
+        for _ in range(args.steps):
+            ctx.raycast(req, rgba, depth)
+        ctx.sync()
+        st = ctx.stats(reset=True)
+        ctx.stats_enable(False)
+        ms = st["stage_ms"]["raycast"] / args.steps
+        out[f"{w}x{w}"] = {"ms_per_frame": ms, "rays_per_s": w * w / (ms / 1e3)}
+    line = {"workload": "raycast of the tracked frame (10,240 triangles)", "results": out}
+    if not args.no_cpu_baseline:
+        tris = O.build_triangles(frame, av.canonical, av.faces, av.mask)
+        cam, focal = S.camera(0.0, width=512, height=8)
+        rc = O.render_cfg(512, 8, focal, cam, av.render_aabb())
+        t0 = time.perf_counter()
+        O.raycast(rc, tris, O.mesh_centroid(av.canonical))
+        t = time.perf_counter() - t0
+        line["cpu_baseline"] = {"rays_per_s": 512 * 8 / t, "cores": O.num_threads(), "kind": "port",
+                                "sample": "512 x 8 rays, brute-force closest hit, OpenMP"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_serve(args):
     """Served mixed stream: 8 resident avatars, Poisson arrivals, each request a fresh expression
     (its own frame upload, LBVH, occupancy) at a resolution drawn from {256, 512, 768, 1024}^2.
@@ -671,10 +715,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--width", type=int, default=512, help="square render size (512 = the benchmark workload)")
-    ap.add_argument("--workload", choices=["render", "batch", "serve", "precision", "map", "grid"], default="render",
+    ap.add_argument("--workload", choices=["render", "batch", "serve", "precision", "map", "grid", "raycast"], default="render",
                     help="render: the benchmark line; batch: 64 expressions in one wavefront; serve: request stream; "
                          "precision: FP16 / BF16 / FP8 MLPs at 1024x1024 against the FP64 oracle; "
-                         "map: canonical mapping of 1M shell points; grid: density-grid update")
+                         "map: canonical mapping of 1M shell points; grid: density-grid update; raycast: mesh raycast")
     ap.add_argument("--rows", type=int, default=16, help="precision: image rows rendered by the FP64 oracle")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--rate", type=float, default=240.0)
@@ -694,6 +738,8 @@ def main():
         return run_map(args)
     if args.workload == "grid":
         return run_grid(args)
+    if args.workload == "raycast":
+        return run_raycast(args)
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
