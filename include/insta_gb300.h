@@ -262,7 +262,7 @@ int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, 
  * frames, cameras and resolutions; their avatars must share one field layout (same
  * insta_field_desc).  out_rgba[i] / out_depth[i] as for insta_render (host or device, per
  * request).  Each request's pixels equal those of insta_render on that request alone.  At most
- * 4096 requests and 2^26 pixels per batch.  No reference counterpart: render_nerf renders one
+ * 4096 requests and 2^25 pixels per batch (one round's sample buffers hold a sample per pixel).  No reference counterpart: render_nerf renders one
  * view at a time (instant-ngp/src/testbed_nerf.cu:2320). */
 int insta_render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* const* out_rgba, float* const* out_depth);
 /* Network samples evaluated by the last insta_render / insta_render_batch (synchronises). */
@@ -305,7 +305,7 @@ int insta_nearest_debug(insta_ctx* ctx, int avatar, int frame, const float* pts,
 typedef struct insta_server insta_server;
 typedef struct {
     uint32_t max_inflight;          /* request slots (1..256) */
-    uint64_t max_inflight_pixels;   /* pixels of admitted requests (<= 2^26) */
+    uint64_t max_inflight_pixels;   /* pixels of admitted requests (<= 2^25) */
     double occupancy_radius;        /* request frames: occupancy from the mesh (0.015) */
 } insta_server_config;
 

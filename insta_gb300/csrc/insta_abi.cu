@@ -422,7 +422,7 @@ RenderView render_view(const Avatar& a, const insta_render_desc& r) {
 
 void check_request(const insta_render_desc* r) {
     if (!r) fail(INSTA_ERR_INVALID_ARG, "null request");
-    if (r->width <= 0 || r->height <= 0 || (int64_t)r->width * r->height > (int64_t)1 << 26)
+    if (r->width <= 0 || r->height <= 0 || (int64_t)r->width * r->height > (int64_t)1 << 25)
         fail(INSTA_ERR_INVALID_ARG, "bad resolution %dx%d", r->width, r->height);
     if (!(r->focal_length[0] > 0.f) || !(r->focal_length[1] > 0.f)) fail(INSTA_ERR_INVALID_ARG, "focal length must be positive");
     if (r->cone_angle < 0.f) fail(INSTA_ERR_INVALID_ARG, "cone_angle must be >= 0");
@@ -640,7 +640,8 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
         if (on_host[(size_t)i]) host_pix += px;
         max_spr = std::max(max_spr, views[(size_t)i].rv.max_samples_per_ray);
     }
-    if (total_pix > ((uint64_t)1 << 26)) fail(INSTA_ERR_INVALID_ARG, "a batch holds at most 2^26 pixels, got %llu", (unsigned long long)total_pix);
+    // a round takes at least one sample per alive ray: the pixels must fit one round's buffers
+    if (total_pix > kMaxRoundSamples) fail(INSTA_ERR_INVALID_ARG, "a batch holds at most 2^25 pixels, got %llu", (unsigned long long)total_pix);
     // outputs: device pointers directly, host pointers through one staging buffer
     float* stage_rgba = nullptr;
     float* stage_depth = nullptr;
@@ -1711,8 +1712,8 @@ int insta_server_create(insta_ctx* ctx, const insta_server_config* cfg, insta_se
     return guarded(ctx, [&] {
         if (!cfg || !out) fail(INSTA_ERR_INVALID_ARG, "null config or output");
         if (cfg->max_inflight < 1 || cfg->max_inflight > 256) fail(INSTA_ERR_INVALID_ARG, "max_inflight must be 1..256");
-        if (cfg->max_inflight_pixels < 1 || cfg->max_inflight_pixels > ((uint64_t)1 << 26))
-            fail(INSTA_ERR_INVALID_ARG, "max_inflight_pixels must be 1..2^26");
+        if (cfg->max_inflight_pixels < 1 || cfg->max_inflight_pixels > kMaxRoundSamples)
+            fail(INSTA_ERR_INVALID_ARG, "max_inflight_pixels must be 1..2^25");
         if (!(cfg->occupancy_radius > 0.0)) fail(INSTA_ERR_INVALID_ARG, "occupancy_radius must be positive");
         auto s = std::make_unique<insta_server>();
         s->ctx = ctx;

@@ -34,6 +34,10 @@ def test_missing_state_and_bad_arguments():
     ctx.render(req, *out)                                                  # now it renders
     bad = ctx.render_desc(0, 0, 0, 16, focal, cam)
     assert code_of(lambda: ctx.render(bad, *out)) == 1                     # bad resolution
+    huge = ctx.render_desc(0, 0, 8192, 4097, focal, cam)                   # > 2^25 pixels: more than a round holds
+    assert code_of(lambda: ctx.render(huge, *out)) == 1
+    big = [ctx.render_desc(0, 0, 1024, 1024, focal, cam) for _ in range(33)]   # 33 Mpx in one batch
+    assert code_of(lambda: ctx.render_batch(big, [out[0]] * 33, [out[1]] * 33)) == 1
     assert code_of(lambda: ctx.occupancy_from_mesh(0, 0, -1.0)) == 1       # bad radius
     assert code_of(lambda: ctx.occupancy_get(0, 5)) == 4                   # unknown frame
     fc16 = S.FieldConfig(n_levels=8)
