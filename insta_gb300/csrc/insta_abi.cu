@@ -108,6 +108,14 @@ struct insta_ctx {
     unsigned long long* sample_counter = nullptr;
     DevBuf out_rgba, out_depth, extra, bvh_scratch, frame_jobs, density_scratch, density_stage, side_scratch, map_scratch,
         grid_coords, grid_idx, grid_tmp;
+    // the render loop as a CUDA graph (a conditional while node over pairs of rounds), rebuilt
+    // when the wavefront's buffers or limits change
+    cudaGraph_t loop_graph = nullptr;
+    cudaGraphExec_t loop_exec = nullptr;
+    std::vector<unsigned char> loop_key;
+    uint32_t* loop_state = nullptr;                 // [0] steps of the current round, [1] rounds of this launch
+    unsigned long long* loop_rounds_total = nullptr; // rounds run by graph launches (launch statistics)
+    unsigned long long loop_rounds_seen = 0;
     cudaStream_t side = nullptr;        // asynchronous frame uploads
     cudaEvent_t side_mark = nullptr;    // orders a side upload after the main stream's earlier work
     Wave wave;
@@ -588,6 +596,72 @@ struct WaveRun {
         return ctx->host_counters[0];
     }
 
+    // All remaining rounds on the device: one launch of a CUDA graph whose conditional while node
+    // runs pairs of rounds (ping-pong ray buffers) until no ray is alive or max_rounds have run.
+    // The host does not wait; n_alive is not read back.
+    void device_rounds(uint32_t max_rounds) {
+        if (!ctx->loop_state) {
+            CK(cudaMalloc(&ctx->loop_state, 64));
+            CK(cudaMemset(ctx->loop_state, 0, 64));
+            ctx->loop_rounds_total = reinterpret_cast<unsigned long long*>(ctx->loop_state + 8);
+        }
+        WaveArgs A = W, B = W;
+        A.steps_dev = B.steps_dev = ctx->loop_state;
+        A.rays_in = rays(cur); A.rays_out = rays(cur ^ 1);
+        A.n_alive_in = counters + cur; A.n_alive_out = counters + (cur ^ 1);
+        B.rays_in = rays(cur ^ 1); B.rays_out = rays(cur);
+        B.n_alive_in = counters + (cur ^ 1); B.n_alive_out = counters + cur;
+        A.n_init = B.n_init = 0; A.init_tile = B.init_tile = nullptr; A.init_slot = B.init_slot = nullptr;
+        A.steps = B.steps = 0;
+        std::vector<unsigned char> key(sizeof(WaveArgs) * 2 + sizeof(MlpArgs) + 16);
+        std::memcpy(key.data(), &A, sizeof(WaveArgs));
+        std::memcpy(key.data() + sizeof(WaveArgs), &B, sizeof(WaveArgs));
+        std::memcpy(key.data() + 2 * sizeof(WaveArgs), &M, sizeof(MlpArgs));
+        std::memcpy(key.data() + 2 * sizeof(WaveArgs) + sizeof(MlpArgs), &round_cap, 8);
+        std::memcpy(key.data() + 2 * sizeof(WaveArgs) + sizeof(MlpArgs) + 8, &max_rounds, 4);
+        const uint32_t grid_tiles = (uint32_t)(cap_samples / 128);
+        std::memcpy(key.data() + 2 * sizeof(WaveArgs) + sizeof(MlpArgs) + 12, &grid_tiles, 4);
+        if (!ctx->loop_exec || key != ctx->loop_key) {
+            if (ctx->loop_exec) { cudaGraphExecDestroy(ctx->loop_exec); ctx->loop_exec = nullptr; }
+            if (ctx->loop_graph) { cudaGraphDestroy(ctx->loop_graph); ctx->loop_graph = nullptr; }
+            cudaGraph_t g;
+            CK(cudaGraphCreate(&g, 0));
+            ctx->loop_graph = g;
+            cudaGraphConditionalHandle cond;
+            CK(cudaGraphConditionalHandleCreate(&cond, g, 1u, cudaGraphCondAssignDefault));
+            cudaGraphNodeParams cp{};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = cond;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node;
+            CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            // the body by capture: two rounds, then the condition
+            CK(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+            cudaError_t e = cudaSuccess;
+            for (int half = 0; half < 2 && e == cudaSuccess; ++half) {
+                const WaveArgs& R = half ? B : A;
+                if (e == cudaSuccess) e = launch_round_begin(R.n_alive_in, R.n_alive_out, R.n_samples_round, ctx->loop_state, round_cap, kMaxSteps,
+                                                             ctx->stream);
+                if (e == cudaSuccess) e = launch_march(R, ctx->stream);
+                if (e == cudaSuccess) e = launch_sort_samples(R, ctx->stream);
+                if (e == cudaSuccess) e = launch_deform_encode(R, ctx->stream);
+                if (e == cudaSuccess) e = launch_mlp(M, grid_tiles, ctx->stream);
+                if (e == cudaSuccess) e = launch_composite(R, ctx->stream);
+            }
+            if (e == cudaSuccess) e = launch_round_end(B.n_alive_out, ctx->loop_state + 1, ctx->loop_rounds_total, max_rounds, cond, ctx->stream);
+            cudaGraph_t captured = nullptr;
+            const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &captured);
+            CK(e);
+            CK(e2);
+            CK(cudaGraphInstantiate(&ctx->loop_exec, g, 0));
+            ctx->loop_key = key;
+        }
+        CK(cudaMemsetAsync(ctx->loop_state + 1, 0, 4, ctx->stream));
+        CK(cudaGraphLaunch(ctx->loop_exec, ctx->stream));   // its kernels are counted from the device's round total
+    }
+
     // One round over all alive rays; afterwards n_alive (and host_alive per slot) are current.
     // Without read_back the host does not wait: n_alive stays an upper bound (rays only finish),
     // and the next round's kernels take the count from the device.
@@ -683,11 +757,17 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
     // while every ray can take kMaxSteps samples per round, the first round is issued without a
     // host read of its alive count (most frames finish in two rounds: one host wait, not two)
     uint32_t round = 0;
-    if (total_pix * kMaxSteps <= run.round_cap && run.n_alive > 0) {
-        run.round(false);
-        ++round;
+    if (!ctx->timing && run.n_alive > 0) {
+        // the whole loop on the device (one CUDA-graph launch); per-stage timing needs the
+        // host-driven rounds below, which run the same kernels
+        run.device_rounds(max_spr + 2);
+    } else {
+        if (total_pix * kMaxSteps <= run.round_cap && run.n_alive > 0) {
+            run.round(false);
+            ++round;
+        }
+        for (; run.n_alive > 0 && round < max_spr + 2; ++round) run.round();
     }
-    for (; run.n_alive > 0 && round < max_spr + 2; ++round) run.round();
     if (host_pix) {
         uint64_t off = 0;
         for (int i = 0; i < n; ++i) {
@@ -779,6 +859,9 @@ int insta_ctx_destroy(insta_ctx* ctx) {
         cudaStreamDestroy(ctx->side);
     }
     if (ctx->side_mark) cudaEventDestroy(ctx->side_mark);
+    if (ctx->loop_exec) cudaGraphExecDestroy(ctx->loop_exec);
+    if (ctx->loop_graph) cudaGraphDestroy(ctx->loop_graph);
+    if (ctx->loop_state) cudaFree(ctx->loop_state);
     ctx->release(ctx->side_scratch);
     for (auto& kv : ctx->avatars)
         for (auto& f : kv.second->frames)
@@ -1389,6 +1472,14 @@ int insta_stats_read(insta_ctx* ctx, insta_stats* out, int reset) {
     return guarded(ctx, [&] {
         if (!out) fail(INSTA_ERR_INVALID_ARG, "null output");
         ctx->collect_timings();
+        if (ctx->loop_rounds_total) {
+            // graph-run rounds: 10 kernels per round plus the loop condition per pair of rounds
+            unsigned long long total = 0;
+            CK(cudaMemcpy(&total, ctx->loop_rounds_total, sizeof(total), cudaMemcpyDeviceToHost));
+            const unsigned long long d = total - ctx->loop_rounds_seen;
+            ctx->launches += d * 10ull + d / 2ull;
+            ctx->loop_rounds_seen = total;
+        }
         out->kernel_launches = ctx->launches;
         unsigned long long v = 0;
         CK(cudaMemcpy(&v, ctx->sample_counter, sizeof(v), cudaMemcpyDeviceToHost));

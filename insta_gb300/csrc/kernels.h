@@ -82,6 +82,7 @@ struct WaveArgs {
     uint32_t* n_samples_round;  // device count of this round's samples
     uint32_t* n_samples_padded; // the same after per-request padding to 128
     uint32_t steps;             // samples per ray per round
+    const uint32_t* steps_dev;  // when set: the round's step count, written on the device (graph rounds)
     uint8_t* tiles;             // encoded input tile records
     uint32_t tile_bytes, k_in;
     float4* samples;            // per sample: (pos.xyz, dt) from the march
@@ -170,6 +171,13 @@ cudaError_t launch_unpack(const uint2* out, const float4* out_f32, int bf16, int
 int64_t static_max_samples();
 cudaError_t static_scratch(int device, uint8_t** tiles, uint2** out, float4** out_f32);
 
+// Device-driven rounds for the CUDA-graph render loop: round_begin sets a round's step count from
+// its alive count and clears the counters it appends to; round_end (after two rounds) counts them
+// and sets the loop's condition: rays alive and rounds left.
+cudaError_t launch_round_begin(const uint32_t* n_alive_in, uint32_t* n_alive_out, uint32_t* n_samples_round, uint32_t* steps,
+                               uint64_t round_cap, uint32_t max_steps, cudaStream_t s);
+cudaError_t launch_round_end(const uint32_t* n_alive, uint32_t* rounds, unsigned long long* rounds_total, uint32_t max_rounds,
+                             cudaGraphConditionalHandle cond, cudaStream_t s);
 cudaError_t launch_raycast(const RenderView& rv, const FrameView& fr, const float* center, int color_normal, float* out_rgba,
                            float* out_depth, int32_t* out_tri, uint32_t* err, cudaStream_t s);
 cudaError_t launch_nearest_debug(const FrameView& fr, const float* pts, int64_t n, int32_t* out, uint32_t* err, cudaStream_t s);

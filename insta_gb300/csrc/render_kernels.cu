@@ -149,6 +149,7 @@ __device__ __forceinline__ void encode_sample(const FieldView& fv, const uint16_
 // order, records in sample_index[k * n_alive + r] where sample k of ray r went.
 __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ WaveArgs A) {
     const uint32_t n_alive = *A.n_alive_in;
+    const uint32_t steps = A.steps_dev ? *A.steps_dev : A.steps;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_iter = (n_alive + stride - 1) / stride;
     const uint32_t lane = threadIdx.x & 31u;
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ Wave
             ray.d = v3(rb.x, rb.y, rb.z);
             ray.idir = v3(__fdiv_rn(1.f, rb.x), __fdiv_rn(1.f, rb.y), __fdiv_rn(1.f, rb.z));
             ray.t = t0 = ra.w;
-            for (; j < A.steps; ++j) {
+            for (; j < steps; ++j) {
                 V3 pos;
                 float dt;
                 if (ns + j >= rv.max_samples_per_ray || !ray_next_sample(rv, bitfield, ray, pos, dt)) break;
@@ -582,6 +583,7 @@ __global__ void __launch_bounds__(128) mlp_kernel(const __grid_constant__ MlpArg
 // ------------------------------------------------------------------ composite + compaction
 __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
     const uint32_t n_alive = *A.n_alive_in;
+    const uint32_t steps = A.steps_dev ? *A.steps_dev : A.steps;
     const bool f32_out = A.fv.precision != 0;   // the MLP wrote FP32 outputs
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_iter = (n_alive + stride - 1) / stride;
@@ -593,7 +595,7 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
             ra = A.rays_in.a[r]; rb = A.rays_in.b[r]; rc = A.rays_in.c[r]; rd = A.rays_in.d[r];
             const ReqView& R = A.reqs[__float_as_uint(rd.w)];
             const uint32_t m = A.n_round[r];
-            bool done = m < A.steps;
+            bool done = m < steps;
             float4 rgba = rc;
             float depth = rd.x, maxw = rb.w;
             uint32_t j = 0;
@@ -811,6 +813,35 @@ cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s) {
     uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
     if (max_tiles < grid) grid = max_tiles ? max_tiles : 1;
     mlp_kernel<<<grid, 128, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+__global__ void round_begin_kernel(const uint32_t* n_alive_in, uint32_t* n_alive_out, uint32_t* n_samples_round, uint32_t* steps,
+                                   uint64_t round_cap, uint32_t max_steps) {
+    const uint64_t n = *n_alive_in;
+    const uint64_t per = round_cap / (n > 0 ? n : 1);
+    *steps = (uint32_t)(per < 1 ? 1 : (per > max_steps ? max_steps : per));
+    *n_alive_out = 0u;
+    *n_samples_round = 0u;
+}
+
+__global__ void round_end_kernel(const uint32_t* n_alive, uint32_t* rounds, unsigned long long* rounds_total, uint32_t max_rounds,
+                                 cudaGraphConditionalHandle cond) {
+    const uint32_t r = *rounds + 2u;
+    *rounds = r;
+    *rounds_total += 2ull;
+    cudaGraphSetConditional(cond, (*n_alive > 0u && r < max_rounds) ? 1u : 0u);
+}
+
+cudaError_t launch_round_begin(const uint32_t* n_alive_in, uint32_t* n_alive_out, uint32_t* n_samples_round, uint32_t* steps,
+                               uint64_t round_cap, uint32_t max_steps, cudaStream_t s) {
+    round_begin_kernel<<<1, 1, 0, s>>>(n_alive_in, n_alive_out, n_samples_round, steps, round_cap, max_steps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_round_end(const uint32_t* n_alive, uint32_t* rounds, unsigned long long* rounds_total, uint32_t max_rounds,
+                             cudaGraphConditionalHandle cond, cudaStream_t s) {
+    round_end_kernel<<<1, 1, 0, s>>>(n_alive, rounds, rounds_total, max_rounds, cond);
     return cudaGetLastError();
 }
 
