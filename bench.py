@@ -217,6 +217,8 @@ def run_ours(args, rank, world, local):
         ctx.frame_wait(0, (k + 1) % 2)
         return k
 
+    if args.stage_timing:   # every render with per-stage events: host-driven rounds (for kernel-level profiles)
+        ctx.stats_enable(True)
     clocks = ClockSampler(local).__enter__()
     with torch.cuda.stream(stream):
         # settle: untimed steps for SETTLE_S so the SM clock has left its idle state before the
@@ -256,6 +258,7 @@ def run_ours(args, rank, world, local):
         # per-stage device time (untimed pass, same frames and kernels): with stage timing on the
         # library records CUDA events around each stage and drives the rounds from the host
         ctx.stats_enable(True)
+        ctx.stats(reset=True)
         for k in range(args.steps):
             flush.zero_()
             step(k)
@@ -310,7 +313,9 @@ def run_ours(args, rank, world, local):
                                f"occupancy from mesh (1.5 cm), 16-level hash grid T=2^19, MLPs 32-64-16 / 32-64-64-3",
                    "global_batch": world, "samples_per_frame": mean_samples, "parallelism": f"replicas x{world}",
                    "l2": "flushed (512 MiB write) between timed steps", "frames_per_s": args.steps * world / dev_t,
-                   "settle_s": SETTLE_S},
+                   "settle_s": SETTLE_S,
+                   "render_loop": "host-driven rounds with per-stage events" if args.stage_timing else
+                                  "one CUDA-graph launch per frame (conditional while node over the rounds)"},
         "roofline": {"bound": "hbm", "kernel": "deform+encode stage (nearest_stage_kernel + map_encode_kernel)",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": TRAFFIC_PER_FRAME if WIDTH == 512 else None,
@@ -725,6 +730,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--stage-timing", action="store_true",
+                    help="per-stage CUDA events on every render (host-driven rounds instead of the CUDA-graph loop; "
+                         "for kernel-level profiles)")
     ap.add_argument("--width", type=int, default=512, help="square render size (512 = the benchmark workload)")
     ap.add_argument("--workload", choices=["render", "batch", "serve", "precision", "map", "grid", "raycast"], default="render",
                     help="render: the benchmark line; batch: 64 expressions in one wavefront; serve: request stream; "
