@@ -174,6 +174,40 @@ def test_canonical_map_coords_in_place(gpu_avatar, oracle, oracle_frame, avatar,
     assert (got[~untouched, 11] == 1.0).any() and (got[~untouched, 11] == 0.25).any()
 
 
+@pytest.mark.parametrize("variant", ["all_torso", "disable_interp", "boundary"])
+def test_canonical_map_mask_variants(ctx, oracle, variant):
+    """The warp's branches on other meshes: every triangle region 15 (rigid frames, expression
+    dims reset everywhere), the disable-interp flag (rigid frames for face triangles too), and a
+    mesh with a boundary region (mask 0)."""
+    from insta_gb300 import abi, synthetic as S
+    av = S.make_avatar(3, with_boundary=variant == "boundary")
+    mask = np.full(av.n_faces, S.MASK_TORSO, np.uint32) if variant == "all_torso" else av.mask
+    aid = {"all_torso": 10, "disable_interp": 11, "boundary": 12}[variant]
+    fr = av.frame(av.frame_coeffs(2))
+    ctx.canonical_set(aid, av.canonical, av.faces, mask)
+    if variant == "disable_interp":
+        ctx.set_flags(aid, abi.FLAG_DISABLE_INTERP)
+    ctx.frame_upload(aid, 0, fr)
+    rng = np.random.default_rng(9)
+    pts = S.shell_points(fr, av.faces, 20000, seed=8)
+    dirs = rng.normal(size=pts.shape).astype(np.float32)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    c = make_coords(pts, dirs, np.zeros(len(pts), np.float32), n_extra=16)
+    cd = dev(c)
+    ctx.canonical_map(aid, 0, cd, c.shape[1], 16, len(c))
+    ctx.sync()
+    got = cd.cpu().numpy()
+    can = oracle.build_triangles(av.canonical, None, av.faces, mask)
+    dtr = oracle.build_triangles(fr, av.canonical, av.faces, mask)
+    d = oracle.Deformation(dtr, can, oracle.adjacency(av.faces, av.n_verts), oracle.Bvh(dtr), disable_interp=variant == "disable_interp")
+    ref = d.map_coords(c, n_extra=16, frame_id=0, n_frames=1)
+    assert np.abs(got[:, 0:3] - ref[:, 0:3]).max() <= 1e-5 * diag(av)
+    assert np.abs(got[:, 8:11] - ref[:, 8:11]).max() <= 1e-5
+    assert (got[:, 11:] == ref[:, 11:]).all()
+    if variant == "all_torso":
+        assert (got[:, 11:] == 1.0).all()
+
+
 def test_canonical_map_holder_selects_frame(gpu_avatar, oracle, avatar, frame0):
     from insta_gb300 import synthetic as S
     f1 = avatar.frame(avatar.frame_coeffs(1))
@@ -254,6 +288,21 @@ def test_occupancy_bit_exact(gpu_avatar, oracle, oracle_frame):
     gpu_avatar.occupancy_from_mesh(0, 0, 0.015)
     got = gpu_avatar.occupancy_get(0, 0)
     ref = oracle.occupancy(oracle_frame["def"], 0.015)
+    assert got.sum() > 0
+    assert (got == ref).all()
+
+
+def test_occupancy_bit_exact_with_boundary_region(ctx, oracle):
+    """mark_flame_density_grid skips cells whose nearest triangle lies in region 0 (boundary)."""
+    from insta_gb300 import synthetic as S
+    av = S.make_avatar(4, with_boundary=True)
+    assert (av.mask == S.MASK_BOUNDARY).any()
+    fr = av.frame(av.frame_coeffs(3))
+    ctx.canonical_set(13, av.canonical, av.faces, av.mask)
+    ctx.frame_upload(13, 0, fr)
+    ctx.occupancy_from_mesh(13, 0, 0.015)
+    got = ctx.occupancy_get(13, 0)
+    ref = oracle.occupancy(oracle.build_triangles(fr, av.canonical, av.faces, av.mask), 0.015)
     assert got.sum() > 0
     assert (got == ref).all()
 
