@@ -8,8 +8,7 @@
 //   * a subtree is pruned only when its box distance exceeds best * (1 + 2^-10) + 1e-12,
 //     so a rounding-level difference between box and triangle distances can never hide
 //     the true minimum -- the result equals the brute-force minimum over all triangles.
-// The search can start from an upper bound: a known triangle (the previous sample of the
-// same ray) or a distance bound (occupancy marking).
+// The search can start from a distance bound (occupancy marking).
 #pragma once
 
 #include "insta_types.h"
@@ -305,12 +304,5 @@ __device__ __forceinline__ Nearest nearest_triangle(const FrameView& fr, V3 p, u
     return nearest_bvh(fr, p, __int_as_float(0x7f800000), -1, -1, err);
 }
 
-// Nearest triangle starting from the triangle at `slot` (e.g. the previous sample's).
-__device__ __forceinline__ Nearest nearest_from_slot(const FrameView& fr, V3 p, int32_t slot, uint32_t* err) {
-    if (slot < 0) return nearest_triangle(fr, p, err);
-    int32_t id;
-    float d = slot_distance(fr, slot, p, id);
-    return nearest_bvh(fr, p, d, id, slot, err);
-}
 
 }  // namespace insta

@@ -115,16 +115,6 @@ __device__ __forceinline__ float tri_distance_rec(const float4* tr, V3 pos, int3
     return __fdiv_rn(__fmul_rn(nd, nd), q4.w);
 }
 
-// BoundingBox::distance_sq (NGP/bounding_box.cuh:228-230).
-__device__ __forceinline__ float box_distance_sq(float mnx, float mny, float mnz, float mxx, float mxy, float mxz, V3 p) {
-    float ax = __fsub_rn(mnx, p.x), bx = __fsub_rn(p.x, mxx);
-    float ay = __fsub_rn(mny, p.y), by = __fsub_rn(p.y, mxy);
-    float az = __fsub_rn(mnz, p.z), bz = __fsub_rn(p.z, mxz);
-    float dx = ax < bx ? bx : ax; dx = dx < 0.f ? 0.f : dx;
-    float dy = ay < by ? by : ay; dy = dy < 0.f ? 0.f : dy;
-    float dz = az < bz ? bz : az; dz = dz < 0.f ? 0.f : dz;
-    return __fadd_rn(__fmul_rn(dx, dx), __fadd_rn(__fmul_rn(dy, dy), __fmul_rn(dz, dz)));
-}
 
 // PCG32 (O'Neill's permuted congruential generator with 64-bit state, XSH-RR output), the
 // pcg32 class tiny-cuda-nn uses as default_rng_t, restated from the published algorithm:
