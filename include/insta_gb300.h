@@ -257,6 +257,11 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
 /* out_rgba f32[h*w*4] (linear RGBA, zero background), out_depth f32[h*w] (1e10 where no
  * hit).  Host pointers: the call returns after the copy back; device pointers: asynchronous. */
 int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, float* out_depth);
+/* insta_render without waiting for host outputs: the copy back of a frame runs on the context's
+ * copy stream (page-locked host buffers let it overlap the next render); the buffers hold the
+ * frame after insta_sync or any later call that synchronises.  Device outputs: as insta_render.
+ * No reference counterpart (render_nerf writes into its own render buffer). */
+int insta_render_async(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, float* out_depth);
 /* n requests rendered through one wavefront: each round marches, deforms, encodes, evaluates and
  * composites the alive rays of every request with one set of launches.  Requests may mix avatars,
  * frames, cameras and resolutions; their avatars must share one field layout (same

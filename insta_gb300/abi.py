@@ -24,7 +24,7 @@ EXPORTS = [
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_density_grid_load", "insta_density_grid_reset", "insta_density_grid_update", "insta_density_grid_read",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
-    "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_batch",
+    "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_async", "insta_render_batch",
     "insta_render_samples", "insta_march_debug", "insta_nearest_debug", "insta_raycast",
     "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
     "insta_server_release", "insta_server_error",
@@ -121,6 +121,7 @@ def load(path: Path | None = None):
             "insta_field_eval": [vp, C.c_int, vp, u32, i64, vp],
             "insta_field_eval_static": [vp, C.c_int, vp, u32, i64, vp],
             "insta_render": [vp, C.POINTER(RenderDesc), vp, vp],
+            "insta_render_async": [vp, C.POINTER(RenderDesc), vp, vp],
             "insta_render_batch": [vp, C.POINTER(RenderDesc), C.c_int, C.POINTER(vp), C.POINTER(vp)],
             "insta_render_samples": [vp, C.POINTER(u64)],
             "insta_march_debug": [vp, C.POINTER(RenderDesc), C.c_int, vp, vp, vp],
@@ -332,6 +333,10 @@ class Context:
 
     def render(self, req: RenderDesc, out_rgba, out_depth):
         self._check(self.lib.insta_render(self.h, C.byref(req), _addr(out_rgba), _addr(out_depth)))
+
+    def render_async(self, req: RenderDesc, out_rgba, out_depth):
+        """insta_render_async: host outputs are complete after sync()."""
+        self._check(self.lib.insta_render_async(self.h, C.byref(req), _addr(out_rgba), _addr(out_depth)))
 
     def render_batch(self, reqs, out_rgba, out_depth):
         """reqs: list of RenderDesc; out_rgba / out_depth: lists of buffers (one pair per request)."""

@@ -116,6 +116,13 @@ struct insta_ctx {
     uint32_t* loop_state = nullptr;                 // [0] steps of the current round, [1] rounds of this launch
     unsigned long long* loop_rounds_total = nullptr; // rounds run by graph launches (launch statistics)
     unsigned long long loop_rounds_seen = 0;
+    // insta_render_async with host outputs: double-buffered device staging, copied back on a
+    // copy stream while the next render runs
+    cudaStream_t copy = nullptr;
+    DevBuf async_rgba[2], async_depth[2];
+    cudaEvent_t async_free[2] = {nullptr, nullptr}, async_done = nullptr;
+    bool async_used[2] = {false, false};
+    int async_next = 0;
     cudaStream_t side = nullptr;        // asynchronous frame uploads
     cudaEvent_t side_mark = nullptr;    // orders a side upload after the main stream's earlier work
     Wave wave;
@@ -175,6 +182,7 @@ struct insta_ctx {
     // Read and clear the device error word (synchronises the stream).
     void check_device() {
         CK(cudaStreamSynchronize(stream));
+        if (copy) CK(cudaStreamSynchronize(copy));
         uint32_t e = 0;
         CK(cudaMemcpy(&e, err_dev, sizeof(e), cudaMemcpyDeviceToHost));
         if (e) {
@@ -686,7 +694,8 @@ struct WaveRun {
 
 // Testbed::render_nerf for a batch of requests (avatars, frames, cameras, resolutions) through one
 // wavefront; the request slots are the batch.
-void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* const* out_rgba, float* const* out_depth) {
+void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* const* out_rgba, float* const* out_depth,
+                  bool async_host = false) {
     if (n <= 0 || (uint32_t)n > kMaxRequests) fail(INSTA_ERR_INVALID_ARG, "batch size %d outside 1..%u", n, kMaxRequests);
     std::vector<ReqView> views((size_t)n);
     const Field* field0 = nullptr;
@@ -719,7 +728,19 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
     // outputs: device pointers directly, host pointers through one staging buffer
     float* stage_rgba = nullptr;
     float* stage_depth = nullptr;
-    if (host_pix) {
+    int async_k = -1;
+    if (host_pix && async_host) {
+        // the staging pair the copy stream released last; the render waits for its copy to end
+        async_k = ctx->async_next;
+        if (!ctx->copy) {
+            CK(cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking));
+            for (int k = 0; k < 2; ++k) CK(cudaEventCreateWithFlags(&ctx->async_free[k], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&ctx->async_done, cudaEventDisableTiming));
+        }
+        if (ctx->async_used[async_k]) CK(cudaStreamWaitEvent(ctx->stream, ctx->async_free[async_k], 0));
+        stage_rgba = (float*)ctx->alloc(ctx->async_rgba[async_k], host_pix * 16);
+        stage_depth = (float*)ctx->alloc(ctx->async_depth[async_k], host_pix * 4);
+    } else if (host_pix) {
         stage_rgba = (float*)ctx->alloc(ctx->out_rgba, host_pix * 16);
         stage_depth = (float*)ctx->alloc(ctx->out_depth, host_pix * 4);
     }
@@ -769,15 +790,27 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
         for (; run.n_alive > 0 && round < max_spr + 2; ++round) run.round();
     }
     if (host_pix) {
+        cudaStream_t cs = ctx->stream;
+        if (async_k >= 0) {
+            CK(cudaEventRecord(ctx->async_done, ctx->stream));
+            CK(cudaStreamWaitEvent(ctx->copy, ctx->async_done, 0));
+            cs = ctx->copy;
+        }
         uint64_t off = 0;
         for (int i = 0; i < n; ++i) {
             if (!on_host[(size_t)i]) continue;
             const size_t px = (size_t)reqs[i].width * reqs[i].height;
-            CK(cudaMemcpyAsync(out_rgba[i], stage_rgba + off * 4, px * 16, cudaMemcpyDeviceToHost, ctx->stream));
-            CK(cudaMemcpyAsync(out_depth[i], stage_depth + off, px * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(out_rgba[i], stage_rgba + off * 4, px * 16, cudaMemcpyDeviceToHost, cs));
+            CK(cudaMemcpyAsync(out_depth[i], stage_depth + off, px * 4, cudaMemcpyDeviceToHost, cs));
             off += px;
         }
-        ctx->check_device();
+        if (async_k >= 0) {
+            CK(cudaEventRecord(ctx->async_free[async_k], ctx->copy));
+            ctx->async_used[async_k] = true;
+            ctx->async_next = async_k ^ 1;
+        } else {
+            ctx->check_device();
+        }
     }
 }
 
@@ -859,6 +892,16 @@ int insta_ctx_destroy(insta_ctx* ctx) {
         cudaStreamDestroy(ctx->side);
     }
     if (ctx->side_mark) cudaEventDestroy(ctx->side_mark);
+    if (ctx->copy) {
+        cudaStreamSynchronize(ctx->copy);
+        cudaStreamDestroy(ctx->copy);
+        for (int k = 0; k < 2; ++k) {
+            cudaEventDestroy(ctx->async_free[k]);
+            ctx->release(ctx->async_rgba[k]);
+            ctx->release(ctx->async_depth[k]);
+        }
+        cudaEventDestroy(ctx->async_done);
+    }
     if (ctx->loop_exec) cudaGraphExecDestroy(ctx->loop_exec);
     if (ctx->loop_graph) cudaGraphDestroy(ctx->loop_graph);
     if (ctx->loop_state) cudaFree(ctx->loop_state);
@@ -1442,6 +1485,10 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
 
 int insta_render(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, float* out_depth) {
     return guarded(ctx, [&] { render_batch(ctx, req, 1, &out_rgba, &out_depth); });
+}
+
+int insta_render_async(insta_ctx* ctx, const insta_render_desc* req, float* out_rgba, float* out_depth) {
+    return guarded(ctx, [&] { render_batch(ctx, req, 1, &out_rgba, &out_depth, true); });
 }
 
 int insta_render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* const* out_rgba, float* const* out_depth) {

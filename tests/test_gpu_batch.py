@@ -186,3 +186,32 @@ def test_frame_upload_async_double_buffered(ctx):
     for k in range(5):
         assert (outs[k][0].cpu().numpy() == ref[k][0]).all() and (outs[k][1].cpu().numpy() == ref[k][1]).all(), k
     assert (ref[0][0][:, 3] > 0.05).sum() > 20
+
+
+def test_render_async_host_outputs_match_render(ctx, avatar):
+    """insta_render_async: three frames in a row into page-locked host buffers (the two device
+    staging pairs alternate) equal the synchronous renders once the context is synchronised."""
+    from insta_gb300 import synthetic as S
+    fc = S.FieldConfig()
+    ctx.canonical_set(14, avatar.canonical, avatar.faces, avatar.mask)
+    ctx.params_load(14, fc, S.field_params(fc, seed=6))
+    for k in range(3):
+        ctx.frame_upload(14, k, avatar.frame(avatar.frame_coeffs(30 + k)))
+        ctx.occupancy_from_mesh(14, k, 0.015)
+    reqs = []
+    for k in range(3):
+        cam, focal = S.camera(-10.0 + 10.0 * k, width=80, height=64)
+        reqs.append(ctx.render_desc(14, k, 80, 64, focal, cam))
+    sync_out = []
+    for r in reqs:
+        rgba, depth = np.zeros((80 * 64, 4), np.float32), np.zeros(80 * 64, np.float32)
+        ctx.render(r, rgba, depth)
+        sync_out.append((rgba, depth))
+    pinned = [(torch.zeros((80 * 64, 4), dtype=torch.float32).pin_memory(), torch.zeros(80 * 64, dtype=torch.float32).pin_memory())
+              for _ in range(3)]
+    for r, (a, b) in zip(reqs, pinned):
+        ctx.render_async(r, a.numpy(), b.numpy())
+    ctx.sync()
+    for (a, b), (ra, rb) in zip(pinned, sync_out):
+        assert (a.numpy() == ra).all() and (b.numpy() == rb).all()
+    assert sync_out[0][0][:, 3].max() > 0.05
