@@ -441,6 +441,25 @@ def run_map(args):
         st = ctx.stats(reset=True)
         ctx.stats_enable(False)
         dev_ms = st["stage_ms"]["canonical_map"] / st["stage_calls"]["canonical_map"]
+        # the same points as NerfCoordinate records through the render_deformed hook (frame 0)
+        rec = np.zeros((n, 11), np.float32)
+        rec[:, :3] = pts
+        rec[:, 8:11] = 0.5
+        d_rec0 = torch.from_numpy(rec).cuda()
+        d_rec = torch.empty_like(d_rec0)
+        for _ in range(3):
+            d_rec.copy_(d_rec0)
+            ctx.canonical_map(0, 0, d_rec, 11, 0, n)
+        ctx.sync()
+        ctx.stats(reset=True)
+        ctx.stats_enable(True)
+        for _ in range(args.steps):
+            d_rec.copy_(d_rec0)
+            ctx.canonical_map(0, 0, d_rec, 11, 0, n)
+        ctx.sync()
+        st = ctx.stats(reset=True)
+        ctx.stats_enable(False)
+        coords_ms = st["stage_ms"]["canonical_map"] / st["stage_calls"]["canonical_map"]
         h_pts = torch.from_numpy(pts).pin_memory()
         h_idx = torch.empty(n, dtype=torch.int32).pin_memory()
         h_can = torch.empty((n, 3), dtype=torch.float32).pin_memory()
@@ -459,6 +478,7 @@ def run_map(args):
     assert (h_idx.numpy()[:65536] == ref_ids).all(), "canonical map ids differ from the oracle"
     line = {"workload": "canonical map, 1,048,576 points in a 1 cm shell, 10,240-triangle frame",
             "points_per_s": n / (dev_ms / 1e3), "ms_per_call": dev_ms, "launches_per_call": 6,
+            "records_ms_per_call": coords_ms, "records_per_s": n / (coords_ms / 1e3),
             "e2e": {"points_per_s": n / e2e_s, "h2d_bytes": n * 12, "d2h_bytes": n * 16}}
     if not args.no_cpu_baseline:
         m = 1 << 16

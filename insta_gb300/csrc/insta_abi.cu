@@ -1263,9 +1263,20 @@ int insta_canonical_map(insta_ctx* ctx, int avatar, int frame, float* coords, ui
         if (n == 0) return;
         refresh_frame_table(ctx, a);
         if (frame >= 0) use_frame(ctx, a, frame); else wait_all_frames(ctx, a);
-        Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
-        CK(launch_canonical_map_coords((const FrameView*)a.frame_table.p, a.table_frames, deform_view(a), coords, stride, n_extra, n,
-                                       frame, ctx->err_dev, ctx->stream));
+        const bool sorted = n >= kMapSortedMin && n < ((int64_t)1 << 30) && (frame >= 0 || a.table_frames <= kMaxRequests);
+        if (sorted) {
+            // render_deformed (fixed frame) sorts by cell; surface_closest_point by (holder frame, cell)
+            const uint32_t n_frames = frame >= 0 ? 1u : a.table_frames;
+            const FrameView* frames = (const FrameView*)a.frame_table.p + (frame >= 0 ? frame : 0);
+            ctx->alloc(ctx->map_scratch, warp_sorted_scratch_bytes((uint32_t)n, n_frames));
+            Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 6);
+            CK(launch_canonical_map_coords_sorted(frames, n_frames, frame >= 0, deform_view(a), coords, stride, n_extra, (uint32_t)n,
+                                                  ctx->map_scratch.p, ctx->err_dev, ctx->stream));
+        } else {
+            Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
+            CK(launch_canonical_map_coords((const FrameView*)a.frame_table.p, a.table_frames, deform_view(a), coords, stride, n_extra, n,
+                                           frame, ctx->err_dev, ctx->stream));
+        }
     });
 }
 

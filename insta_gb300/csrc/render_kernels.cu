@@ -384,13 +384,14 @@ __global__ void __launch_bounds__(256) sort_place_kernel(const __grid_constant__
     for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += stride) {
         const uint32_t s = b + threadIdx.x;
         const bool valid = s < n;
-        const uint32_t key = valid ? A.sample_key[s] : 0xffffffffu;
+        uint32_t key = valid ? A.sample_key[s] : 0xffffffffu;
+        const bool placed = key != 0xffffffffu;   // unsorted records (skipped by the caller) carry no key
         const uint32_t peers = __match_any_sync(0xffffffffu, key);
         const int leader = __ffs(peers) - 1;
         uint32_t base = 0;
-        if (valid && lane == (uint32_t)leader) base = atomicAdd(A.sort_bins + key, (uint32_t)__popc(peers));
+        if (placed && lane == (uint32_t)leader) base = atomicAdd(A.sort_bins + key, (uint32_t)__popc(peers));
         base = __shfl_sync(0xffffffffu, base, leader);
-        if (valid) {
+        if (placed) {
             const uint32_t req = key >> A.cell_bits;
             const uint32_t pos = A.sort_block_sums[key / kSortBlock] + base + (uint32_t)__popc(peers & lt_mask);
             A.sample_order[pos - A.req_start[req] + A.req_seg[req]] = s;
@@ -1039,6 +1040,95 @@ __global__ void __launch_bounds__(256) gwarp_map_kernel(const FrameView* __restr
         map_to_canonical(dv, frames[keys[i] >> cell_bits].frames, (uint32_t)id, v3(c[0], c[1], c[2]), nullptr, o, nullptr, nullptr);
         c[0] = o[0]; c[1] = o[1]; c[2] = o[2];
     }
+}
+
+// The warp hook on NerfCoordinate records in bulk (insta_canonical_map, src/core.cu:442-526):
+// the records the hook maps (holder >= 0, a known frame, inside the train box) are sorted by
+// (frame, 64^3 cell of the train box) and walked 32 neighbours at a time; the others keep no key
+// and stay untouched.
+__global__ void __launch_bounds__(256) coords_key_kernel(const FrameView* __restrict__ frames, uint32_t n_frames, int fixed, DeformView dv,
+                                                         const float* __restrict__ coords, uint32_t stride, uint32_t n, uint32_t cell_bits,
+                                                         uint32_t* __restrict__ keys, uint32_t* __restrict__ bins, uint32_t* __restrict__ n_round) {
+    const uint32_t lane = threadIdx.x & 31u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *n_round = n;
+    const uint32_t per_axis = 1u << (cell_bits / 3);
+    const float top = (float)(per_axis - 1);
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+        const uint32_t i = b + threadIdx.x;
+        uint32_t key = 0xffffffffu;
+        if (i < n) {
+            const float* c = coords + (size_t)i * stride;
+            const float holder = c[4];
+            const V3 p = v3(c[0], c[1], c[2]);
+            const uint32_t fid = fixed ? 0u : (uint32_t)holder;
+            if (holder >= 0.f && fid < n_frames && box_contains(dv.aabb_min, dv.aabb_max, p) && frames[fid].n_tris > 0) {
+                const float pp[3] = {p.x, p.y, p.z};
+                uint32_t q[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    q[k] = (uint32_t)fminf(fmaxf((pp[k] - dv.aabb_min[k]) / (dv.aabb_max[k] - dv.aabb_min[k]) * (float)per_axis, 0.f), top);
+                key = (fid << cell_bits) | spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+            }
+            keys[i] = key;
+        }
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        if (key != 0xffffffffu && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(bins + key, (uint32_t)__popc(peers));
+    }
+}
+
+__global__ void __launch_bounds__(256) coords_map_kernel(const FrameView* __restrict__ frames, DeformView dv, float* __restrict__ coords,
+                                                         uint32_t stride, uint32_t n_extra, uint32_t n, const uint32_t* __restrict__ keys,
+                                                         const int32_t* __restrict__ ids, uint32_t cell_bits, uint32_t* err) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t key = keys[i];
+        if (key == 0xffffffffu) continue;
+        const int32_t id = ids[i];
+        if (id < 0) { atomicOr(err, INSTA_DEVERR_NO_TRI); continue; }
+        float* c = coords + (size_t)i * stride;
+        float pos[3], dir[3], dw[3] = {c[8], c[9], c[10]};
+        uint32_t mask;
+        map_to_canonical(dv, frames[key >> cell_bits].frames, (uint32_t)id, v3(c[0], c[1], c[2]), dw, pos, dir, &mask);
+        c[0] = pos[0]; c[1] = pos[1]; c[2] = pos[2];
+        c[8] = dir[0]; c[9] = dir[1]; c[10] = dir[2];
+        if (mask != 7u)
+            for (uint32_t m = 0; m < n_extra; ++m) c[stride - n_extra + m] = 1.f;
+    }
+}
+
+cudaError_t launch_canonical_map_coords_sorted(const FrameView* frames_dev, uint32_t n_frames, int fixed, const DeformView& dv, float* coords,
+                                               uint32_t stride, uint32_t n_extra, uint32_t n, void* scratch, uint32_t* err, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t cb = sort_cell_bits(n_frames);
+    const uint32_t n_bins = n_frames << cb;
+    uint32_t* keys = static_cast<uint32_t*>(scratch);
+    int32_t* ids = reinterpret_cast<int32_t*>(keys + n);
+    uint32_t* order = keys + 2 * (size_t)n;
+    uint32_t* bins = order + n + 128u * (size_t)n_frames;
+    uint32_t* block_sums = bins + n_bins;
+    uint32_t* req_start = block_sums + n_bins / kSortBlock;
+    uint32_t* req_seg = req_start + n_frames + 1;
+    uint32_t* counters = req_seg + n_frames + 1;
+    WaveArgs a{};
+    a.n_reqs = n_frames;
+    a.cell_bits = cb;
+    a.sort_bins = bins;
+    a.sort_block_sums = block_sums;
+    a.req_start = req_start;
+    a.req_seg = req_seg;
+    a.sample_order = order;
+    a.sample_key = keys;
+    a.n_samples_round = counters;
+    a.n_samples_padded = counters + 1;
+    cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)n_bins * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)std::min<uint32_t>((n + 255) / 256, (uint32_t)sm_count() * 8);
+    coords_key_kernel<<<grid, 256, 0, s>>>(frames_dev, n_frames, fixed, dv, coords, stride, n, cb, keys, bins, counters);
+    sort_scan_kernel<<<n_bins / kSortBlock, kSortBlock, 0, s>>>(bins, block_sums);
+    sort_offsets_kernel<<<1, kSortBlock, 0, s>>>(a, n_bins / kSortBlock);
+    sort_place_kernel<<<sm_count() * 8, 256, 0, s>>>(a);
+    gwarp_nearest_kernel<<<sm_count() * 16, 256, 0, s>>>(frames_dev, coords, stride, order, keys, counters + 1, cb, ids, err);
+    coords_map_kernel<<<grid, 256, 0, s>>>(frames_dev, dv, coords, stride, n_extra, n, keys, ids, cb, err);
+    return cudaGetLastError();
 }
 
 size_t warp_sorted_scratch_bytes(uint32_t n, uint32_t n_frames) {

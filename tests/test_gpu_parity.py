@@ -224,6 +224,44 @@ def test_canonical_map_holder_selects_frame(gpu_avatar, oracle, avatar, frame0):
     assert np.abs(cd.cpu().numpy()[:, :3] - ref[:, :3]).max() <= 1e-5 * diag(avatar)
 
 
+@pytest.mark.parametrize("fixed", [True, False])
+def test_canonical_map_sorted_paths(gpu_avatar, oracle, oracle_frame, avatar, frame0, fixed):
+    """insta_canonical_map on 70,000 records takes the (frame, cell)-sorted walk: render_deformed
+    (fixed frame 0) and surface_closest_point (holder frames 0 and 1), with skipped records
+    (holder -1, outside the train box) left untouched."""
+    from insta_gb300 import synthetic as S
+    rng = np.random.default_rng(12)
+    f1 = avatar.frame(avatar.frame_coeffs(1))
+    n = 70000
+    holder = rng.integers(0, 2, n).astype(np.float32)
+    holder[rng.random(n) < 0.05] = -1.0
+    pts = np.where((holder == 1)[:, None], S.shell_points(f1, avatar.faces, n, seed=13), S.shell_points(frame0, avatar.faces, n, seed=14))
+    pts[rng.random(n) < 0.03] += 3.0
+    dirs = rng.normal(size=(n, 3)).astype(np.float32)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    c = make_coords(pts.astype(np.float32), dirs, holder, n_extra=4)
+    cd = dev(c)
+    gpu_avatar.canonical_map(0, 0 if fixed else -1, cd, c.shape[1], 4, n)
+    gpu_avatar.sync()
+    got = cd.cpu().numpy()
+    can, adj = oracle_frame["can"], oracle_frame["adj"]
+    d0 = oracle.Deformation(oracle_frame["def"], can, adj, oracle_frame["bvh"])
+    if fixed:
+        ref = d0.map_coords(c, n_extra=4, frame_id=0, n_frames=1)
+    else:
+        dt1 = oracle.build_triangles(f1, avatar.canonical, avatar.faces, avatar.mask)
+        d1 = oracle.Deformation(dt1, can, adj, oracle.Bvh(dt1))
+        ref = c.copy()
+        for h, d in ((0, d0), (1, d1)):
+            sel = holder == h
+            ref[sel] = d.map_coords(c[sel], n_extra=4, frame_id=-1, n_frames=2)
+    assert np.abs(got[:, 0:3] - ref[:, 0:3]).max() <= 1e-5 * diag(avatar)
+    assert np.abs(got[:, 8:11] - ref[:, 8:11]).max() <= 1e-5
+    assert (got[:, 11:] == ref[:, 11:]).all() and (got[:, 3:8] == c[:, 3:8]).all()
+    skipped = (holder < 0) | (np.abs(pts - 0.5).max(1) > 0.5)
+    assert skipped.any() and (got[skipped] == c[skipped]).all()
+
+
 def test_canonical_map_empty_is_noop(gpu_avatar):
     c = torch.zeros((0, 11), dtype=torch.float32, device="cuda")
     gpu_avatar.canonical_map(0, 0, c, 11, 0, 0)
