@@ -496,6 +496,36 @@ def test_render_psnr(gpu_avatar, field_setup, oracle, oracle_frame, avatar):
     assert ((r_rgba[:, 3] > 0.2) == (rgba[:, 3] > 0.2)).mean() > 0.999
 
 
+@pytest.mark.parametrize("variant", ["uniform_steps", "jitter", "max_samples", "odd_size", "linear_colors"])
+def test_render_variants(gpu_avatar, field_setup, oracle, oracle_frame, avatar, variant):
+    """Render options against the oracle: cone angle 0 (uniform steps, aabb_scale 1), sub-pixel
+    jitter (spp 3, no snapping), a per-ray sample cap of 8, a ragged 37x23 frame, linear colours."""
+    from insta_gb300 import synthetic as S
+    fc, params = field_setup
+    gpu_avatar.occupancy_from_mesh(0, 0, 0.015)
+    W, H = (37, 23) if variant == "odd_size" else (64, 48)
+    opts = {"uniform_steps": dict(cone_angle=0.0), "jitter": dict(spp=3, snap=False), "max_samples": dict(max_samples=8),
+            "odd_size": {}, "linear_colors": dict(linear_colors=True)}[variant]
+    cam, focal = S.camera(7.0, width=W, height=H)
+    req = gpu_avatar.render_desc(0, 0, W, H, focal, cam, **opts)
+    rgba = np.zeros((W * H, 4), np.float32)
+    depth = np.zeros(W * H, np.float32)
+    gpu_avatar.render(req, rgba, depth)
+    n = gpu_avatar.render_samples()
+    bits = oracle.occupancy(oracle_frame["def"], 0.015)
+    d = oracle.Deformation(oracle_frame["def"], oracle_frame["can"], oracle_frame["adj"], oracle_frame["bvh"])
+    ro = dict(opts)
+    if "max_samples" in ro:
+        ro["max_samples"] = ro.pop("max_samples")
+    rc = oracle.render_cfg(W, H, focal, cam, avatar.render_aabb(), **ro)
+    r_rgba, r_depth, ns, total = oracle.render(rc, d, bits, fc, params)
+    assert total > 100
+    assert abs(n - total) <= max(2, total // 1000)
+    assert psnr(rgba, r_rgba) >= 45.0
+    if variant == "max_samples":
+        assert ns.max() <= 8
+
+
 def test_render_opaque_early_termination(gpu_avatar, oracle, oracle_frame, avatar):
     """A dense field terminates rays early (composite_kernel_nerf :996-999)."""
     from insta_gb300 import synthetic as S
