@@ -29,6 +29,8 @@
  *   insta_params_load           Testbed::load_snapshot parameter blob, NerfNetwork::set_params
  *                               order (instant-ngp/src/testbed.cu:2952-3016; NGP/nerf_network.h:492-525)
  *   insta_field_eval            NerfNetwork::inference_mixed_precision_impl (NGP/nerf_network.h:159-232)
+ *   insta_field_backward        NerfNetwork's forward/backward for training (NGP/nerf_network.h:296-383)
+ *   insta_adam_step             the Adam optimizer of the trainer (configs/nerf/main.json)
  *   insta_render                Testbed::render_nerf -> NerfTracer::init_rays_from_camera/trace +
  *                               shade_kernel_nerf (instant-ngp/src/testbed_nerf.cu:2030-2244,2320-2460)
  *   insta_march_debug           the sample positions advance_pos_nerf + generate_next_nerf_network_inputs
@@ -252,6 +254,24 @@ int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t s
  * any stream capture).  All calls share the array: calls whose work overlaps on the GPU (other
  * streams, other contexts) race, so serialise them. */
 int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4);
+
+/* -- training side of the field ----------------------------------------------- */
+/* NerfNetwork's backward (NGP/nerf_network.h:296-383, the tiny-cuda-nn side of train_nerf_step):
+ * for n NerfCoordinate records (canonical position, direction, expression dims; device
+ * pointers) and the loss gradient w.r.t. each record's outputs dl_dout f32[n][4] (raw r, g, b,
+ * raw density), ADD the gradient of every parameter to grad f32[n_params] (snapshot order:
+ * density MLP, colour MLP, hash table).  FP32 throughout from the FP32 master weights (the FP16
+ * parameters at the first call after insta_params_load).  out4 (optional) gets the outputs of
+ * that FP32 forward; with dl_dout = grad = NULL only the forward runs.  n < 2^24. */
+int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, const float* dl_dout, float* grad,
+                         float* out4);
+/* Adam (configs/nerf/main.json nests it in an Ema): w -= lr * m_hat / (sqrt(v_hat) + eps) with
+ * g + l2_reg * w, bias-corrected moments; the FP32 master weights and moments stay on the
+ * device, the field's FP16 parameters and weight image are rewritten. */
+typedef struct insta_adam_config {
+    float learning_rate, beta1, beta2, epsilon, l2_reg;
+} insta_adam_config;
+int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_adam_config* cfg);
 
 /* -- render ------------------------------------------------------------------- */
 /* out_rgba f32[h*w*4] (linear RGBA, zero background), out_depth f32[h*w] (1e10 where no

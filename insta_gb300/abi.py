@@ -24,7 +24,7 @@ EXPORTS = [
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_density_grid_load", "insta_density_grid_reset", "insta_density_grid_update", "insta_density_grid_read",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
-    "insta_field_eval", "insta_field_eval_static", "insta_render", "insta_render_async", "insta_render_batch",
+    "insta_field_eval", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_render", "insta_render_async", "insta_render_batch",
     "insta_render_samples", "insta_march_debug", "insta_nearest_debug", "insta_raycast",
     "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
     "insta_server_release", "insta_server_error",
@@ -46,6 +46,11 @@ class DensityUpdateDesc(C.Structure):
                 ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3), ("grid_rng", Pcg32State), ("warp_rng", Pcg32State),
                 ("ema_step", C.c_uint32), ("n_frames", C.c_int32), ("bitfield_frame", C.c_int32),
                 ("debug_pos", C.c_void_p), ("debug_idx", C.c_void_p)]
+
+
+class AdamConfig(C.Structure):
+    _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
+                ("l2_reg", C.c_float)]
 
 
 class InstaError(RuntimeError):
@@ -120,6 +125,8 @@ def load(path: Path | None = None):
             "insta_params_load": [vp, C.c_int, C.POINTER(FieldDesc), vp, u64],
             "insta_field_eval": [vp, C.c_int, vp, u32, i64, vp],
             "insta_field_eval_static": [vp, C.c_int, vp, u32, i64, vp],
+            "insta_field_backward": [vp, C.c_int, vp, u32, i64, vp, vp, vp],
+            "insta_adam_step": [vp, C.c_int, vp, C.POINTER(AdamConfig)],
             "insta_render": [vp, C.POINTER(RenderDesc), vp, vp],
             "insta_render_async": [vp, C.POINTER(RenderDesc), vp, vp],
             "insta_render_batch": [vp, C.POINTER(RenderDesc), C.c_int, C.POINTER(vp), C.POINTER(vp)],
@@ -315,6 +322,14 @@ class Context:
     def field_eval_static(self, avatar, coords, stride, n, out4):
         """insta_field_eval without device allocations (n <= 16384, shared fixed scratch)."""
         self._check(self.lib.insta_field_eval_static(self.h, avatar, _addr(coords), stride, n, _addr(out4)))
+
+    def field_backward(self, avatar, coords, stride, n, dl_dout=None, grad=None, out4=None):
+        """insta_field_backward: ADDS d(sum dl_dout . out)/d(params) into grad (f32, snapshot order)."""
+        self._check(self.lib.insta_field_backward(self.h, avatar, _addr(coords), stride, n, _addr(dl_dout), _addr(grad), _addr(out4)))
+
+    def adam_step(self, avatar, grad, learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6):
+        cfg = AdamConfig(learning_rate, beta1, beta2, epsilon, l2_reg)
+        self._check(self.lib.insta_adam_step(self.h, avatar, _addr(grad), C.byref(cfg)))
 
     @staticmethod
     def render_desc(avatar, frame, width, height, focal, cam, cone_angle=1 / 256, spp=0, min_transmittance=0.01,

@@ -16,7 +16,7 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 OUT_DIR = HERE / "_lib"
 LIB = OUT_DIR / "libinsta_gb300.so"
-SOURCES = ["insta_abi.cu", "frame_kernels.cu", "render_kernels.cu", "static_scratch.cu"]
+SOURCES = ["insta_abi.cu", "frame_kernels.cu", "render_kernels.cu", "static_scratch.cu", "train_kernels.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -62,7 +62,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
             if r.returncode:
                 raise RuntimeError(f"nvcc failed: {' '.join(cmd)}")
     if force or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + ["-lcudart", "-lcublas"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
             sys.stderr.write(r.stdout + r.stderr)

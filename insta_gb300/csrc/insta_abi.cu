@@ -18,6 +18,8 @@
 #include <string>
 #include <vector>
 
+#include <cublas_v2.h>
+
 #include "../../include/insta_gb300.h"
 #include "device_common.cuh"
 #include "mlp_tiles.cuh"
@@ -69,6 +71,11 @@ struct Field {
     TilePlan plan{};
     FieldView view{};
     uint64_t n_params = 0;
+    // training: FP32 master weights (from the FP16 parameters at the first backward after a
+    // load), Adam moments, the optimizer's step count and its FP16 output
+    DevBuf w32, adam_m, adam_v, w16;
+    bool w32_valid = false;
+    uint32_t adam_step = 0;
 };
 
 // Device scratch of the render wavefront, sized for the largest request seen.
@@ -123,6 +130,9 @@ struct insta_ctx {
     cudaEvent_t async_free[2] = {nullptr, nullptr}, async_done = nullptr;
     bool async_used[2] = {false, false};
     int async_next = 0;
+    cublasHandle_t blas = nullptr;      // the training side's GEMMs
+    DevBuf train_scratch;
+    bool keep_master = false;           // a parameter reload from the optimizer keeps the FP32 master weights
     cudaStream_t side = nullptr;        // asynchronous frame uploads
     cudaEvent_t side_mark = nullptr;    // orders a side upload after the main stream's earlier work
     Wave wave;
@@ -902,6 +912,8 @@ int insta_ctx_destroy(insta_ctx* ctx) {
         }
         cudaEventDestroy(ctx->async_done);
     }
+    if (ctx->blas) cublasDestroy(ctx->blas);
+    ctx->release(ctx->train_scratch);
     if (ctx->loop_exec) cudaGraphExecDestroy(ctx->loop_exec);
     if (ctx->loop_graph) cudaGraphDestroy(ctx->loop_graph);
     if (ctx->loop_state) cudaFree(ctx->loop_state);
@@ -912,7 +924,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     for (auto& kv : ctx->avatars) {
         Avatar& a = *kv.second;
         for (DevBuf* b : {&a.faces, &a.mask, &a.adjacency, &a.canon_verts, &a.canon_area, &a.canon_frames, &a.frame_table,
-                          &a.field.params, &a.field.image, &a.density_grid})
+                          &a.field.params, &a.field.image, &a.density_grid, &a.field.w32, &a.field.adam_m, &a.field.adam_v, &a.field.w16})
             ctx->release(*b);
         for (auto& f : a.frames)
             for (DevBuf* b : {&f.second.verts, &f.second.frames, &f.second.leaf_tris, &f.second.nodes, &f.second.bitfield})
@@ -1350,6 +1362,10 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
         Field& fd = a.field;
         fd.desc = *desc;
         fd.n_params = n_params;
+        if (!ctx->keep_master) {
+            fd.w32_valid = false;
+            fd.adam_step = 0;
+        }
         ctx->alloc(fd.params, n_params * 2);
         host_copy(fd.params.p, params, n_params * 2, ctx->stream);
         // MLP weight image in the tensor-core operand layout (umma.cuh), one B tile per operand
@@ -1465,6 +1481,76 @@ int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t s
         m.out = (uint2*)w.out.p; m.out_f32 = (float4*)w.out_f32.p; m.err = ctx->err_dev;
         CK(launch_mlp(m, (uint32_t)tiles, ctx->stream));
         CK(launch_unpack((const uint2*)w.out.p, (const float4*)w.out_f32.p, a.field.view.precision != 0, n, (float4*)out4, ctx->stream));
+    });
+}
+
+namespace {
+TrainShape train_shape(const Field& fd) {
+    const FieldLayout L = field_layout(fd.desc);
+    TrainShape t{};
+    t.kd = L.layer_k[0];
+    t.n_density = L.n_density;
+    t.n_rgb = L.n_rgb;
+    for (int l = 0; l < 8; ++l) t.layer_off[l] = L.layer_off[l];
+    t.table_off = L.table_off;
+    return t;
+}
+
+void ensure_master(insta_ctx* ctx, Field& fd) {
+    if (fd.w32_valid) return;
+    ctx->alloc(fd.w32, fd.n_params * 4);
+    CK(launch_half_to_float(fd.n_params, fd.params.p, (float*)fd.w32.p, ctx->stream));
+    fd.w32_valid = true;
+}
+}  // namespace
+
+int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, const float* dl_dout, float* grad,
+                         float* out4) {
+    return guarded(ctx, [&] {
+        Avatar& a = ctx->avatar(avatar);
+        Field& fd = a.field;
+        if (!fd.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", avatar);
+        if (n < 0 || n >= ((int64_t)1 << 24)) fail(INSTA_ERR_INVALID_ARG, "sample count must be 0 .. 2^24 - 1");
+        if (n > 0 && (!coords || (!out4 && !(dl_dout && grad)))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
+        if ((dl_dout == nullptr) != (grad == nullptr)) fail(INSTA_ERR_INVALID_ARG, "output gradients and parameter gradients go together");
+        if (stride < 11 + fd.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
+        if (n == 0) return;
+        if (!ctx->blas && cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) fail(INSTA_ERR_CUDA, "cublasCreate failed");
+        ensure_master(ctx, fd);
+        const TrainShape t = train_shape(fd);
+        ctx->alloc(ctx->train_scratch, train_scratch_floats(t, (uint32_t)n) * 4);
+        Stage st(ctx, INSTA_STAGE_FIELD, 8 + 2 * (t.n_density + t.n_rgb));
+        CK(launch_field_train(ctx->blas, fd.view, t, (const float*)fd.w32.p, coords, stride, (uint32_t)n, dl_dout, out4, grad,
+                              (float*)ctx->train_scratch.p, ctx->stream));
+    });
+}
+
+int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_adam_config* cfg) {
+    return guarded(ctx, [&] {
+        if (!grad || !cfg) fail(INSTA_ERR_INVALID_ARG, "null gradient or configuration");
+        Avatar& a = ctx->avatar(avatar);
+        Field& fd = a.field;
+        if (!fd.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", avatar);
+        ensure_master(ctx, fd);
+        if (fd.adam_step == 0) {
+            ctx->alloc(fd.adam_m, fd.n_params * 4);
+            ctx->alloc(fd.adam_v, fd.n_params * 4);
+            CK(cudaMemsetAsync(fd.adam_m.p, 0, fd.n_params * 4, ctx->stream));
+            CK(cudaMemsetAsync(fd.adam_v.p, 0, fd.n_params * 4, ctx->stream));
+        }
+        ctx->alloc(fd.w16, fd.n_params * 2);
+        const uint32_t step = ++fd.adam_step;
+        {
+            Stage st(ctx, INSTA_STAGE_FIELD, 1);
+            CK(launch_adam(fd.n_params, (float*)fd.w32.p, (float*)fd.adam_m.p, (float*)fd.adam_v.p, grad, cfg->learning_rate, cfg->beta1,
+                           cfg->beta2, cfg->epsilon, cfg->l2_reg, step, (__half*)fd.w16.p, ctx->stream));
+        }
+        // the new FP16 parameters: the field's buffer and weight image (the master stays FP32)
+        const insta_field_desc desc = fd.desc;
+        ctx->keep_master = true;
+        const int rc = insta_params_load(ctx, avatar, &desc, (const uint16_t*)fd.w16.p, fd.n_params);
+        ctx->keep_master = false;
+        if (rc != INSTA_OK) fail(rc, "%s", ctx->last_error.c_str());
     });
 }
 

@@ -182,6 +182,21 @@ cudaError_t launch_round_begin(const uint32_t* n_alive_in, uint32_t* n_alive_out
                                uint64_t round_cap, uint32_t max_steps, cudaStream_t s);
 cudaError_t launch_round_end(const uint32_t* n_alive, uint32_t* rounds, unsigned long long* rounds_total, uint32_t max_rounds,
                              cudaGraphConditionalHandle cond, cudaStream_t s);
+// The field's training side (train_kernels.cu): forward with saved activations, output
+// gradients -> parameter gradients (FP32, snapshot order), Adam.
+struct TrainShape {
+    uint32_t kd;                 // density MLP input width (32 + expression dims)
+    int n_density, n_rgb;        // layers of each MLP
+    uint64_t layer_off[8];       // offsets of the layers' [n_out][n_in] weights in the parameters
+    uint64_t table_off;          // offset of the hash table ([entries][2])
+};
+size_t train_scratch_floats(const TrainShape& t, uint32_t n);
+cudaError_t launch_field_train(struct cublasContext* h, const FieldView& fv, const TrainShape& t, const float* w32, const float* coords,
+                               uint32_t stride, uint32_t n, const float* dl_dout, float* out4, float* grad, float* scratch,
+                               cudaStream_t s);
+cudaError_t launch_adam(size_t n, float* w, float* m, float* v, const float* g, float lr, float b1, float b2, float eps, float l2,
+                        uint32_t step, __half* w16, cudaStream_t s);
+cudaError_t launch_half_to_float(size_t n, const void* a, float* b, cudaStream_t s);
 cudaError_t launch_raycast(const RenderView& rv, const FrameView& fr, const float* center, int color_normal, float* out_rgba,
                            float* out_depth, int32_t* out_tri, uint32_t* err, cudaStream_t s);
 cudaError_t launch_nearest_debug(const FrameView& fr, const float* pts, int64_t n, int32_t* out, uint32_t* err, cudaStream_t s);

@@ -1070,6 +1070,143 @@ void orc_field_eval(const orc_field_cfg *c, const uint16_t *params, const float 
     }
 }
 
+/* NerfNetwork's backward (NGP/nerf_network.h:296-383) in FP64 from the FP16 parameters: for each
+ * record the forward with its activations, then the gradient of sum_i dl_dout[i] . out4[i]
+ * w.r.t. every parameter, ADDED to grad[n_params] (snapshot order).  Single-threaded. */
+static void layer_fwd_d(const uint16_t *W, const double *x, int n_in, int n_out, double *y, int relu) {
+    for (int o = 0; o < n_out; ++o) {
+        double acc = 0;
+        for (int i = 0; i < n_in; ++i) acc += (double)orc_h2f(W[(size_t)o * n_in + i]) * x[i];
+        y[o] = (relu && acc < 0) ? 0 : acc;
+    }
+}
+/* dy -> dx = W^T dy, dW += dy x^T; relu mask of x applied by the caller */
+static void layer_bwd_d(const uint16_t *W, const double *x, int n_in, int n_out, const double *dy, double *dx, double *dW) {
+    for (int i = 0; i < n_in; ++i) dx[i] = 0;
+    for (int o = 0; o < n_out; ++o) {
+        if (dy[o] == 0) continue;
+        for (int i = 0; i < n_in; ++i) {
+            dx[i] += (double)orc_h2f(W[(size_t)o * n_in + i]) * dy[o];
+            dW[(size_t)o * n_in + i] += dy[o] * x[i];
+        }
+    }
+}
+
+void orc_field_backward(const orc_field_cfg *c, const uint16_t *params, const float *coords, uint32_t stride, int64_t n,
+                        const float *dl_dout, double *grad, float *out4) {
+    uint64_t lvl_off[64], mlp_off[3];
+    uint32_t lvl_res[64], lvl_size[64];
+    orc_field_layout(c, lvl_off, lvl_res, lvl_size, mlp_off);
+    const uint16_t *table = params + mlp_off[2];
+    const uint32_t F = c->n_features, n_enc = c->n_levels * F, n_in = n_enc + c->n_extra;
+    const uint32_t H = c->density_hidden, HR = c->rgb_hidden, DO = c->density_out, RI = c->density_out + 16;
+    for (int64_t s = 0; s < n; ++s) {
+        const float *coord = &coords[s * stride];
+        double feat[256], hd[4][128], dens[64], rin[128], hr[5][128], rgb[64];
+        uint32_t cidx[64][8];
+        double cw[64][8];
+        for (uint32_t l = 0; l < c->n_levels; ++l) {
+            const float scale = orc_level_scale(c, l);
+            float pos[3], fr[3];
+            uint32_t g[3];
+            for (int k = 0; k < 3; ++k) {
+                pos[k] = fmaf(coord[k], scale, 0.5f);
+                float fl = floorf(pos[k]);
+                fr[k] = pos[k] - fl;
+                g[k] = (uint32_t)(int32_t)fl;
+            }
+            double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (uint32_t corner = 0; corner < 8; ++corner) {
+                double w = 1;
+                uint32_t cc[3];
+                for (int k = 0; k < 3; ++k) {
+                    uint32_t bit = (corner >> k) & 1u;
+                    cc[k] = g[k] + bit;
+                    w = w * (bit ? (double)fr[k] : 1.0 - (double)fr[k]);
+                }
+                uint32_t idx = orc_grid_index(cc, lvl_res[l], lvl_size[l]);
+                cidx[l][corner] = idx;
+                cw[l][corner] = w;
+                const uint16_t *e = table + (lvl_off[l] + (uint64_t)idx) * F;
+                for (uint32_t f = 0; f < F; ++f) acc[f] += w * (double)orc_h2f(e[f]);
+            }
+            for (uint32_t f = 0; f < F; ++f) feat[l * F + f] = acc[f];
+        }
+        const float *extra = coord + stride - c->n_extra;
+        for (uint32_t k = 0; k < c->n_extra; ++k) feat[n_enc + k] = extra[k];
+        /* density MLP */
+        const uint16_t *Wd[8];
+        const uint16_t *W = params + mlp_off[0];
+        const double *x = feat;
+        uint32_t k_in = n_in;
+        for (uint32_t h = 0; h < c->density_layers; ++h) {
+            Wd[h] = W;
+            layer_fwd_d(W, x, (int)k_in, (int)H, hd[h], 1);
+            W += (size_t)H * k_in;
+            x = hd[h];
+            k_in = H;
+        }
+        Wd[c->density_layers] = W;
+        layer_fwd_d(W, x, (int)H, (int)DO, dens, 0);
+        /* SH */
+        double X = (double)coord[8] * 2 - 1, Y = (double)coord[9] * 2 - 1, Z = (double)coord[10] * 2 - 1;
+        double xx = X * X, yy = Y * Y, zz = Z * Z, sh[16];
+        sh[0] = 0.28209479177387814; sh[1] = -0.48860251190291987 * Y; sh[2] = 0.48860251190291987 * Z;
+        sh[3] = -0.48860251190291987 * X; sh[4] = 1.0925484305920792 * X * Y; sh[5] = -1.0925484305920792 * Y * Z;
+        sh[6] = 0.94617469575755997 * zz - 0.31539156525251999; sh[7] = -1.0925484305920792 * X * Z;
+        sh[8] = 0.54627421529603959 * (xx - yy); sh[9] = 0.59004358992664352 * Y * (-3 * xx + yy);
+        sh[10] = 2.8906114426405538 * X * Y * Z; sh[11] = 0.45704579946446572 * Y * (1 - 5 * zz);
+        sh[12] = 0.3731763325901154 * Z * (5 * zz - 3); sh[13] = 0.45704579946446572 * X * (1 - 5 * zz);
+        sh[14] = 1.4453057213202769 * Z * (xx - yy); sh[15] = 0.59004358992664352 * X * (-xx + 3 * yy);
+        for (uint32_t k = 0; k < DO; ++k) rin[k] = dens[k];
+        for (uint32_t k = 0; k < 16; ++k) rin[DO + k] = sh[k];
+        /* colour MLP */
+        const uint16_t *Wr[8];
+        W = params + mlp_off[1];
+        x = rin;
+        k_in = RI;
+        for (uint32_t h = 0; h < c->rgb_layers; ++h) {
+            Wr[h] = W;
+            layer_fwd_d(W, x, (int)k_in, (int)HR, hr[h], 1);
+            W += (size_t)HR * k_in;
+            x = hr[h];
+            k_in = HR;
+        }
+        Wr[c->rgb_layers] = W;
+        layer_fwd_d(W, x, (int)HR, (int)c->rgb_out_padded, rgb, 0);
+        if (out4) { out4[s * 4] = (float)rgb[0]; out4[s * 4 + 1] = (float)rgb[1]; out4[s * 4 + 2] = (float)rgb[2]; out4[s * 4 + 3] = (float)dens[0]; }
+        if (!dl_dout || !grad) continue;
+        /* backward */
+        double dy[128], dx[256];
+        for (uint32_t k = 0; k < c->rgb_out_padded; ++k) dy[k] = k < 3 ? (double)dl_dout[s * 4 + k] : 0.0;
+        uint32_t n_out = c->rgb_out_padded;
+        for (int h = (int)c->rgb_layers; h >= 0; --h) {
+            const double *xin = h == 0 ? rin : hr[h - 1];
+            const uint32_t kk = h == 0 ? RI : HR;
+            layer_bwd_d(Wr[h], xin, (int)kk, (int)n_out, dy, dx, grad + (Wr[h] - params));
+            if (h > 0) for (uint32_t i = 0; i < kk; ++i) dy[i] = hr[h - 1][i] > 0 ? dx[i] : 0.0;
+            else for (uint32_t i = 0; i < kk; ++i) dy[i] = dx[i];
+            n_out = kk;
+        }
+        /* dy = dL/d rin; density output gradient = rows 0..DO-1, plus the raw density's own */
+        dy[0] += (double)dl_dout[s * 4 + 3];
+        n_out = DO;
+        for (int h = (int)c->density_layers; h >= 0; --h) {
+            const double *xin = h == 0 ? feat : hd[h - 1];
+            const uint32_t kk = h == 0 ? n_in : H;
+            layer_bwd_d(Wd[h], xin, (int)kk, (int)n_out, dy, dx, grad + (Wd[h] - params));
+            if (h > 0) for (uint32_t i = 0; i < kk; ++i) dy[i] = hd[h - 1][i] > 0 ? dx[i] : 0.0;
+            else for (uint32_t i = 0; i < kk; ++i) dy[i] = dx[i];
+            n_out = kk;
+        }
+        /* hash table */
+        double *gt = grad + mlp_off[2];
+        for (uint32_t l = 0; l < c->n_levels; ++l)
+            for (uint32_t corner = 0; corner < 8; ++corner)
+                for (uint32_t f = 0; f < F; ++f) gt[(lvl_off[l] + (uint64_t)cidx[l][corner]) * F + f] += cw[l][corner] * dy[l * F + f];
+    }
+}
+
 /* ---------------------------------------------- single-function exports (pin tests) */
 void orc_tbn(const orc_tri *t, float *m9) { tbn_f(t, m9); }
 void orc_tri2projection(const orc_tri *t, float *M16) { tri2projection_f(t, M16); }

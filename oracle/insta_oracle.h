@@ -137,6 +137,8 @@ int64_t orc_render(const orc_render_cfg *rc, const orc_deform *d, const uint8_t 
                    const orc_field_cfg *fc, const uint16_t *params, const float *layer_scales,
                    int row_begin, int row_end, float *out_rgba, float *out_depth,
                    uint32_t *out_nsamples, int fp64);
+void orc_field_backward(const orc_field_cfg *c, const uint16_t *params, const float *coords, uint32_t stride, int64_t n,
+                        const float *dl_dout, double *grad, float *out4);
 void orc_raycast(const orc_render_cfg *rc, const orc_tri *tris, int n_tris, const float *center, int color_normal, float *out_rgba,
                  float *out_depth, int32_t *out_tri);
 int orc_march_ray(const orc_render_cfg *rc, const uint8_t *bitfield, int px, int py,

@@ -206,6 +206,20 @@ def field_eval(fc, params, coords, fp64=False, weight_format=0, layer_scales=Non
     return out
 
 
+def field_backward(fc, params, coords, dl_dout=None):
+    """NerfNetwork backward in FP64: (gradient of sum(dl_dout * out) w.r.t. every parameter
+    [float64, snapshot order], the FP64 forward's outputs [n, 4])."""
+    c = np.ascontiguousarray(coords, dtype=np.float32)
+    cfg = field_cfg(fc, 0)
+    p = np.ascontiguousarray(params).view(np.uint16)
+    grad = np.zeros(p.size, np.float64)
+    out = np.zeros((len(c), 4), np.float32)
+    g = None if dl_dout is None else np.ascontiguousarray(dl_dout, np.float32)
+    lib().orc_field_backward(C.byref(cfg), ptr(p), ptr(c), C.c_uint32(c.shape[1]), C.c_int64(len(c)),
+                             ptr(g) if g is not None else None, ptr(grad) if g is not None else None, ptr(out))
+    return grad, out
+
+
 def occupancy(tris, radius=0.015) -> np.ndarray:
     bits = np.zeros(8 * 128 ** 3 // 8, dtype=np.uint8)
     lib().orc_occupancy_from_mesh(ptr(tris), C.c_int(len(tris)), C.c_double(radius), ptr(bits))

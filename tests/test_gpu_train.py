@@ -1,0 +1,163 @@
+"""Training side of the field (insta_field_backward, insta_adam_step) through the C ABI (cuda:0).
+
+Oracle: the FP64 forward/backward of the same network (oracle.field_backward), itself checked
+against finite differences on the CPU.  Tolerances:
+* FP32 forward outputs: |err| <= 1e-4 + 1e-4 |x| against the FP64 forward;
+* parameter gradients: per layer and for the hash table, ||g - ref|| <= 1e-3 ||ref|| (FP32
+  GEMMs and atomics against FP64; a ReLU that flips on a pre-activation within rounding of 0
+  moves one sample's share, which the norm absorbs), and every entry within 1e-2 of the
+  block's largest gradient;
+* Adam: the FP16 parameters it writes give field outputs within the field parity tolerance
+  (4e-3 + 1e-2 |x|) of the oracle run on a NumPy FP32 Adam of the same gradient.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+AVATAR = 21
+
+
+def coords(n, seed, n_extra=16):
+    rng = np.random.default_rng(seed)
+    c = np.zeros((n, 11 + n_extra), np.float32)
+    c[:, :3] = rng.uniform(0.3, 0.7, size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    c[:, 8:11] = (d / np.linalg.norm(d, axis=1, keepdims=True) + 1) * 0.5
+    c[:, 11:] = rng.uniform(-1, 1, size=(n, n_extra))
+    return c
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.fixture()
+def field(ctx):
+    from insta_gb300 import layout as L, synthetic as S
+    fc = S.FieldConfig(n_extra=16)
+    params = S.field_params(fc, seed=5)
+    ctx.params_load(AVATAR, fc, params)
+    return fc, params, L.field_layout(fc)
+
+
+def blocks(lay):
+    out = [(off, off + n_out * n_in) for (off, n_out, n_in, _) in lay.mlp_layers(1.0)]
+    return out + [(lay.table_offset, lay.total)]
+
+
+def test_backward_matches_oracle(ctx, field, oracle):
+    fc, params, lay = field
+    n = 3000                                   # not a multiple of any tile or block
+    c = coords(n, seed=1)
+    g_out = np.random.default_rng(2).normal(size=(n, 4)).astype(np.float32)
+    grad = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    ctx.field_backward(AVATAR, dev(c), c.shape[1], n, dev(g_out), grad, out)
+    ctx.sync()
+    ref_g, ref_out = oracle.field_backward(fc, params, c, g_out)
+    got_out = out.cpu().numpy()
+    assert np.abs(got_out - ref_out).max() <= 1e-4 + 1e-4 * np.abs(ref_out).max()
+    g = grad.cpu().numpy().astype(np.float64)
+    for lo, hi in blocks(lay):
+        a, b = g[lo:hi], ref_g[lo:hi]
+        assert np.linalg.norm(b) > 0, (lo, hi)
+        assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(b), (lo, hi, np.linalg.norm(a - b) / np.linalg.norm(b))
+        assert np.abs(a - b).max() <= 1e-2 * np.abs(b).max(), (lo, hi)
+    # the table gradient touches exactly the entries the samples' corners reach
+    touched_ref = ref_g[lay.table_offset:] != 0
+    assert ((g[lay.table_offset:] != 0) <= touched_ref).all()
+
+
+def test_backward_accumulates_and_forward_only(ctx, field, oracle):
+    fc, params, lay = field
+    n = 700
+    c = dev(coords(n, seed=3))
+    g_out = dev(np.random.default_rng(4).normal(size=(n, 4)).astype(np.float32))
+    g1 = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    ctx.field_backward(AVATAR, c, 27, n, g_out, g1)
+    g2 = g1.clone()
+    ctx.field_backward(AVATAR, c, 27, n, g_out, g2)      # adds a second copy
+    out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    ctx.field_backward(AVATAR, c, 27, n, None, None, out)  # forward only
+    ctx.sync()
+    a, b = g1.cpu().numpy(), g2.cpu().numpy()
+    assert np.allclose(b, 2 * a, rtol=1e-5, atol=1e-7 * np.abs(a).max())
+    ref_out = oracle.field_backward(fc, params, c.cpu().numpy())[1]
+    assert np.abs(out.cpu().numpy() - ref_out).max() <= 1e-4 + 1e-4 * np.abs(ref_out).max()
+
+
+def numpy_adam(w, g, steps, lr, b1, b2, eps, l2):
+    w = w.astype(np.float32).copy()
+    m = np.zeros_like(w)
+    v = np.zeros_like(w)
+    for t in range(1, steps + 1):
+        gi = g + np.float32(l2) * w
+        m = np.float32(b1) * m + np.float32(1 - b1) * gi
+        v = np.float32(b2) * v + np.float32(1 - b2) * gi * gi
+        c1, c2 = np.float32(1 - b1 ** t), np.float32(1 - b2 ** t)
+        w = w - np.float32(lr) * (m / c1) / (np.sqrt(v / c2) + np.float32(eps))
+    return w
+
+
+def test_adam_matches_numpy(ctx, field, oracle):
+    fc, params, lay = field
+    n = 2000
+    c = coords(n, seed=6)
+    g_out = np.random.default_rng(7).normal(size=(n, 4)).astype(np.float32)
+    grad = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    ctx.field_backward(AVATAR, dev(c), 27, n, dev(g_out), grad)
+    cfg = dict(learning_rate=1e-2, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6)
+    ctx.adam_step(AVATAR, grad, **cfg)
+    ctx.adam_step(AVATAR, grad, **cfg)          # second step: the moments carry over
+    cq = coords(1500, seed=8)
+    out = torch.zeros((len(cq), 4), dtype=torch.float32, device="cuda")
+    ctx.field_eval(AVATAR, dev(cq), 27, len(cq), out)
+    ctx.sync()
+    g = grad.cpu().numpy()
+    w_new = numpy_adam(params.astype(np.float32), g, 2, cfg["learning_rate"], cfg["beta1"], cfg["beta2"], cfg["epsilon"],
+                       cfg["l2_reg"]).astype(np.float16)
+    ref = oracle.field_eval(fc, w_new, cq)
+    before = oracle.field_eval(fc, params, cq)
+    got = out.cpu().numpy()
+    assert np.abs(ref - before).max() > 0.05          # the step moved the field
+    err = np.abs(got - ref)
+    assert (err <= 4e-3 + 1e-2 * np.abs(ref)).all(), float(err.max())
+
+
+def test_regression_loss_decreases(ctx, field):
+    """A few hundred Adam steps fitting fixed targets with an L2 loss: the backward's sign and
+    scale, and the optimizer state across steps, together reduce the loss by 10x."""
+    fc, params, lay = field
+    n = 4096
+    c = dev(coords(n, seed=9))
+    target = dev(np.random.default_rng(10).uniform(-1, 1, size=(n, 4)).astype(np.float32))
+    out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    grad = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    losses = []
+    for step in range(200):
+        ctx.field_backward(AVATAR, c, 27, n, None, None, out)
+        diff = out - target
+        losses.append(float((diff * diff).mean()))
+        grad.zero_()
+        ctx.field_backward(AVATAR, c, 27, n, (2.0 / diff.numel()) * diff, grad)
+        ctx.adam_step(AVATAR, grad, learning_rate=1e-2)
+    ctx.sync()
+    assert np.isfinite(losses).all() and losses[-1] < 0.1 * losses[0], (losses[0], losses[-1])
+
+
+def test_argument_errors(ctx, field):
+    from insta_gb300 import abi
+    fc, params, lay = field
+    c = dev(coords(16, seed=0))
+    g = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    with pytest.raises(abi.InstaError):
+        ctx.field_backward(AVATAR, c, 27, 16, dev(np.zeros((16, 4), np.float32)), None)   # gradients without a target
+    with pytest.raises(abi.InstaError):
+        ctx.field_backward(AVATAR, c, 11, 16, None, None, torch.zeros((16, 4), device="cuda"))   # stride < 11 + 16
+    with pytest.raises(abi.InstaError):
+        ctx.field_backward(55, c, 27, 16, None, None, torch.zeros((16, 4), device="cuda"))   # no field on avatar 55
+    with pytest.raises(abi.InstaError):
+        ctx.adam_step(55, g)

@@ -179,3 +179,42 @@ def test_grid_samples_land_in_their_cells(oracle):
     assert (np.floor(local + 1e-4) >= c - 1e-3).all() and (local <= c + 1 + 1e-4).all()
     occupied = grid[idx] > 0
     assert occupied[5000:].mean() > 0.9 and occupied[:5000].mean() < 0.45
+
+
+def test_field_backward_oracle_matches_finite_differences(oracle):
+    """The FP64 backward of the field (the oracle for insta_field_backward) against central
+    differences of its own forward: the field is piecewise linear in every single parameter
+    (trilinear hash weights, ReLU MLPs), so a difference over a step that flips no ReLU is exact
+    up to the FP32 rounding of the outputs."""
+    from insta_gb300 import synthetic as S
+    fc = S.FieldConfig(n_extra=16)
+    params = S.field_params(fc, seed=3)
+    rng = np.random.default_rng(4)
+    n = 6
+    c = np.zeros((n, 11 + 16), np.float32)
+    c[:, :3] = rng.uniform(0.35, 0.65, (n, 3))
+    d = rng.normal(size=(n, 3))
+    c[:, 8:11] = (d / np.linalg.norm(d, axis=1, keepdims=True) + 1) * 0.5
+    c[:, 11:] = rng.uniform(-1, 1, (n, 16))
+    g_out = rng.normal(size=(n, 4)).astype(np.float32)
+    grad, out = oracle.field_backward(fc, params, c, g_out)
+    np.testing.assert_allclose(out, oracle.field_eval(fc, params, c, fp64=True), rtol=1e-6, atol=1e-6)
+    from insta_gb300 import layout as L
+    table_off = L.field_layout(fc).table_offset
+    w16 = np.ascontiguousarray(params).view(np.uint16).view(np.float16)
+    nz_table = table_off + np.flatnonzero(grad[table_off:])
+    picks = np.concatenate([rng.choice(table_off, 40, replace=False), rng.choice(nz_table, 40, replace=False)])
+
+    def loss(p):
+        return float((oracle.field_backward(fc, p.view(np.uint16), c)[1].astype(np.float64) * g_out).sum())
+
+    checked = 0
+    for i in picks:
+        hi, lo = w16.copy(), w16.copy()
+        hi[i] = np.float16(float(w16[i]) + 0.002)
+        lo[i] = np.float16(float(w16[i]) - 0.002)
+        step = float(hi[i]) - float(lo[i])
+        fd = (loss(hi) - loss(lo)) / step
+        assert abs(fd - grad[i]) <= 2e-3 + 2e-2 * abs(grad[i]), (int(i), fd, grad[i])
+        checked += 1
+    assert checked == 80 and np.abs(grad[nz_table]).max() > 0
