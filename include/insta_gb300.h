@@ -31,6 +31,8 @@
  *   insta_field_eval            NerfNetwork::inference_mixed_precision_impl (NGP/nerf_network.h:159-232)
  *   insta_field_backward        NerfNetwork's forward/backward for training (NGP/nerf_network.h:296-383)
  *   insta_adam_step             the Adam optimizer of the trainer (configs/nerf/main.json)
+ *   insta_train_loss            compute_loss_kernel_train_nerf + fill_rollover (instant-ngp/src/
+ *                               testbed_nerf.cu:1305-1644,3298-3362)
  *   insta_render                Testbed::render_nerf -> NerfTracer::init_rays_from_camera/trace +
  *                               shade_kernel_nerf (instant-ngp/src/testbed_nerf.cu:2030-2244,2320-2460)
  *   insta_march_debug           the sample positions advance_pos_nerf + generate_next_nerf_network_inputs
@@ -272,6 +274,59 @@ typedef struct insta_adam_config {
     float learning_rate, beta1, beta2, epsilon, l2_reg;
 } insta_adam_config;
 int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_adam_config* cfg);
+
+/* Training loss: compute_loss_kernel_train_nerf (instant-ngp/src/testbed_nerf.cu:1305-1644) for
+ * the rays of insta_training_samples, then tiny-cuda-nn's fill_rollover(_and_rescale) as
+ * train_nerf_step runs them (:3298-3362).  Per kept ray k: composite the raw network outputs of
+ * its samples (logistic rgb, exponential density, stop below transmittance 1e-4), add the
+ * background when the ray ran to its end, take the loss against the ray's target, reserve the
+ * ray's compacted block (atomic on numsteps_counter, cut at max_samples_compacted), rewrite
+ * numsteps[k] = (compacted count, compacted base), copy the block's records to coords_out and
+ * write dL/d(raw output) f32[4] per compacted sample (colour, density, depth and beta terms, the
+ * density regularisers).  With target_batch_size > 0 the compacted arrays are then filled to
+ * target_batch_size by repeating them, the repeated gradients scaled by compacted / target.
+ * Loss types use the reference's ELossType numbering. */
+#define INSTA_LOSS_L2 0
+#define INSTA_LOSS_L1 1
+#define INSTA_LOSS_MAPE 2
+#define INSTA_LOSS_SMAPE 3
+#define INSTA_LOSS_HUBER 4
+#define INSTA_LOSS_LOG_L1 5
+#define INSTA_LOSS_RELATIVE_L2 6
+typedef struct insta_train_loss_desc {
+    uint32_t n_rays;                  /* rays per batch: losses and gradients are divided by it   */
+    uint32_t max_rays;                /* size of the ray arrays below (the sample call's n)       */
+    uint32_t max_samples_compacted;   /* capacity of coords_out / dloss_doutput                    */
+    uint32_t target_batch_size;       /* 0 = no rollover, else <= max_samples_compacted           */
+    float aabb_min[3], aabb_max[3];   /* the train box (unwarp_position)                          */
+    int32_t loss_type, depth_loss_type;
+    int32_t srgb_targets;             /* EColorSpace::SRGB (1) or Linear (0)                      */
+    int32_t train_in_linear_colors;
+    float loss_scale;                 /* LOSS_SCALE, 128 in the reference                          */
+    float depth_supervision_lambda, seg_mask_supervision_lambda, near_distance, beta;
+    int32_t penalize_density;
+    uint32_t stride;                  /* floats per NerfCoordinate record                          */
+    /* per original ray (indexed through ray_indices, like insta_training_samples' rays) */
+    const float* rays;                /* f32[6]: origin, unnormalised direction                    */
+    const float* target;              /* f32[4]: the image sample (linear rgb, alpha)              */
+    const float* background;          /* f32[3] sRGB background (random_bg_color draw) or NULL = 0 */
+    const float* exposure;            /* f32[3] exposure (log2 scale) or NULL = 0                  */
+    const float* depth;               /* f32 depth image sample or NULL (no depth supervision)     */
+    const int32_t* seg_mask;          /* i32 segmentation id or NULL (no segmentation rules)       */
+    const float* mean_density;        /* the density grid's mean (1 float) or NULL (no L1 term)    */
+    /* insta_training_samples' outputs and the network's */
+    const uint32_t* rays_counter;     /* rays kept (counters[0])                                   */
+    const uint32_t* ray_indices;
+    uint32_t* numsteps;               /* [max_rays][2] in: (count, base); out: compacted           */
+    const float* coords;              /* the sample records                                        */
+    const float* network_output;      /* f32[samples][4] raw rgb + raw density                     */
+    uint32_t* numsteps_counter;       /* compacted samples (zeroed by the caller)                  */
+    float* coords_out;                /* [max_samples_compacted][stride]                            */
+    float* dloss_doutput;             /* f32[max_samples_compacted][4]                              */
+    float* loss_output;               /* f32[max_rays] per-ray loss / n_rays, or NULL               */
+} insta_train_loss_desc;
+/* All pointers are device pointers; asynchronous on the context's stream. */
+int insta_train_loss(insta_ctx* ctx, const insta_train_loss_desc* desc);
 
 /* -- render ------------------------------------------------------------------- */
 /* out_rgba f32[h*w*4] (linear RGBA, zero background), out_depth f32[h*w] (1e10 where no

@@ -24,7 +24,7 @@ EXPORTS = [
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_density_grid_load", "insta_density_grid_reset", "insta_density_grid_update", "insta_density_grid_read",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
-    "insta_field_eval", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_render", "insta_render_async", "insta_render_batch",
+    "insta_field_eval", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_train_loss", "insta_render", "insta_render_async", "insta_render_batch",
     "insta_render_samples", "insta_march_debug", "insta_nearest_debug", "insta_raycast",
     "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
     "insta_server_release", "insta_server_error",
@@ -51,6 +51,23 @@ class DensityUpdateDesc(C.Structure):
 class AdamConfig(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
                 ("l2_reg", C.c_float)]
+
+
+LOSS_TYPES = {"l2": 0, "l1": 1, "mape": 2, "smape": 3, "huber": 4, "logl1": 5, "relativel2": 6}
+
+
+class TrainLossDesc(C.Structure):
+    _fields_ = [("n_rays", C.c_uint32), ("max_rays", C.c_uint32), ("max_samples_compacted", C.c_uint32),
+                ("target_batch_size", C.c_uint32), ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3),
+                ("loss_type", C.c_int32), ("depth_loss_type", C.c_int32), ("srgb_targets", C.c_int32),
+                ("train_in_linear_colors", C.c_int32), ("loss_scale", C.c_float), ("depth_supervision_lambda", C.c_float),
+                ("seg_mask_supervision_lambda", C.c_float), ("near_distance", C.c_float), ("beta", C.c_float),
+                ("penalize_density", C.c_int32), ("stride", C.c_uint32),
+                ("rays", C.c_void_p), ("target", C.c_void_p), ("background", C.c_void_p), ("exposure", C.c_void_p),
+                ("depth", C.c_void_p), ("seg_mask", C.c_void_p), ("mean_density", C.c_void_p), ("rays_counter", C.c_void_p),
+                ("ray_indices", C.c_void_p), ("numsteps", C.c_void_p), ("coords", C.c_void_p), ("network_output", C.c_void_p),
+                ("numsteps_counter", C.c_void_p), ("coords_out", C.c_void_p), ("dloss_doutput", C.c_void_p),
+                ("loss_output", C.c_void_p)]
 
 
 class InstaError(RuntimeError):
@@ -127,6 +144,7 @@ def load(path: Path | None = None):
             "insta_field_eval_static": [vp, C.c_int, vp, u32, i64, vp],
             "insta_field_backward": [vp, C.c_int, vp, u32, i64, vp, vp, vp],
             "insta_adam_step": [vp, C.c_int, vp, C.POINTER(AdamConfig)],
+            "insta_train_loss": [vp, C.POINTER(TrainLossDesc)],
             "insta_render": [vp, C.POINTER(RenderDesc), vp, vp],
             "insta_render_async": [vp, C.POINTER(RenderDesc), vp, vp],
             "insta_render_batch": [vp, C.POINTER(RenderDesc), C.c_int, C.POINTER(vp), C.POINTER(vp)],
@@ -330,6 +348,27 @@ class Context:
     def adam_step(self, avatar, grad, learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6):
         cfg = AdamConfig(learning_rate, beta1, beta2, epsilon, l2_reg)
         self._check(self.lib.insta_adam_step(self.h, avatar, _addr(grad), C.byref(cfg)))
+
+    _LOSS_PTRS = ("rays", "target", "background", "exposure", "depth", "seg_mask", "mean_density", "rays_counter", "ray_indices",
+                  "numsteps", "coords", "network_output", "numsteps_counter", "coords_out", "dloss_doutput", "loss_output")
+
+    def train_loss(self, **kw):
+        """insta_train_loss: keyword arguments are insta_train_loss_desc's fields (buffers as
+        device tensors); loss_type / depth_loss_type also accept names ("huber", "l2", ...)."""
+        d = TrainLossDesc()
+        d.loss_scale, d.seg_mask_supervision_lambda = 128.0, 1.0
+        d.aabb_max[:] = [1.0, 1.0, 1.0]
+        for k, v in kw.items():
+            if k in self._LOSS_PTRS:
+                a = _addr(v)
+                setattr(d, k, a.value if a is not None else None)
+            elif k in ("aabb_min", "aabb_max"):
+                getattr(d, k)[:] = [float(x) for x in v]
+            elif k in ("loss_type", "depth_loss_type") and isinstance(v, str):
+                setattr(d, k, LOSS_TYPES[v.lower()])
+            else:
+                setattr(d, k, v)
+        self._check(self.lib.insta_train_loss(self.h, C.byref(d)))
 
     @staticmethod
     def render_desc(avatar, frame, width, height, focal, cam, cone_angle=1 / 256, spp=0, min_transmittance=0.01,

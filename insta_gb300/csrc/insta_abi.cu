@@ -1554,6 +1554,31 @@ int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_a
     });
 }
 
+int insta_train_loss(insta_ctx* ctx, const insta_train_loss_desc* d) {
+    return guarded(ctx, [&] {
+        if (!d) fail(INSTA_ERR_INVALID_ARG, "null loss description");
+        if (d->max_rays >= (1u << 26) || d->max_samples_compacted >= (1u << 28)) fail(INSTA_ERR_INVALID_ARG, "batch too large");
+        if (d->n_rays == 0) fail(INSTA_ERR_INVALID_ARG, "n_rays must be positive");
+        if (d->target_batch_size > d->max_samples_compacted) fail(INSTA_ERR_INVALID_ARG, "target_batch_size exceeds max_samples_compacted");
+        if (d->stride < 11) fail(INSTA_ERR_INVALID_ARG, "stride too small");
+        if (d->loss_type < 0 || d->loss_type > 6 || d->depth_loss_type < 0 || d->depth_loss_type > 6)
+            fail(INSTA_ERR_INVALID_ARG, "unknown loss type");
+        if (!d->numsteps_counter || !d->rays_counter) fail(INSTA_ERR_INVALID_ARG, "null counters");
+        if (d->max_rays == 0) {
+            if (d->target_batch_size > 0 && !(d->coords_out && d->dloss_doutput)) fail(INSTA_ERR_INVALID_ARG, "null output buffers");
+        } else if (!d->rays || !d->target || !d->ray_indices || !d->numsteps || !d->coords || !d->network_output || !d->coords_out ||
+                   !d->dloss_doutput) {
+            fail(INSTA_ERR_INVALID_ARG, "null buffers");
+        }
+        if (((uintptr_t)d->network_output | (uintptr_t)d->dloss_doutput) & 15)
+            fail(INSTA_ERR_INVALID_ARG, "network_output and dloss_doutput must be 16-byte aligned");
+        {
+            Stage st(ctx, INSTA_STAGE_FIELD, d->target_batch_size > 0 ? 3 : 1);
+            CK(launch_train_loss(*d, ctx->stream));
+        }
+    });
+}
+
 int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4) {
     return guarded(ctx, [&] {
         Avatar& a = ctx->avatar(avatar);

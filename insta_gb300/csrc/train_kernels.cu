@@ -13,6 +13,7 @@
 // layers).
 #include <cublas_v2.h>
 
+#include "../../include/insta_gb300.h"
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -130,6 +131,201 @@ __global__ void __launch_bounds__(256) adam_kernel(size_t n, float* __restrict__
 
 __global__ void __launch_bounds__(256) half_to_float_kernel(size_t n, const __half* __restrict__ a, float* __restrict__ b) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) b[i] = __half2float(a[i]);
+}
+
+// ---- training loss (compute_loss_kernel_train_nerf, testbed_nerf.cu:1305-1644) ----------------
+
+__device__ __forceinline__ float tl_srgb_to_linear(float s) { return s <= 0.04045f ? s / 12.92f : powf((s + 0.055f) / 1.055f, 2.4f); }
+__device__ __forceinline__ float tl_linear_to_srgb(float l) { return l < 0.0031308f ? 12.92f * l : 1.055f * powf(l, 0.41666f) - 0.055f; }
+__device__ __forceinline__ float tl_logistic(float x) { return 1.f / (1.f + __expf(-x)); }
+
+// loss_and_gradient (testbed_nerf.cu:116-180,1288-1303) of one channel
+__device__ __forceinline__ void tl_loss(int type, float target, float pred, float& loss, float& grad) {
+    const float d = pred - target;
+    switch (type) {
+        case 1: loss = fabsf(d); grad = copysignf(1.f, d); break;                                          // L1
+        case 2: { const float f = 1.f / (fabsf(pred) + 1e-2f); loss = fabsf(d) * f; grad = copysignf(f, d); } break;   // MAPE
+        case 3: { const float f = 1.f / (0.5f * (fabsf(pred) + fabsf(target)) + 1e-2f); loss = fabsf(d) * f; grad = copysignf(f, d); } break;
+        case 4: {                                                                                           // Huber(0.1) / 5
+            const float a = 0.1f, ad = fabsf(d);
+            loss = ad > a ? ad - 0.5f * a : 0.5f / a * d * d;
+            grad = ad > a ? (d > 0 ? 1.f : -1.f) : d / a;
+            loss /= 5.f;
+            grad /= 5.f;
+        } break;
+        case 5: { const float q = fabsf(d) + 1.f; loss = logf(q); grad = copysignf(1.f / q, d); } break;   // LogL1
+        case 6: { const float f = 1.f / (pred * pred + 1e-2f); loss = d * d * f; grad = 2.f * d * f; } break;   // RelativeL2
+        default: loss = d * d; grad = 2.f * d; break;                                                        // L2
+    }
+}
+
+struct TrainLossArgs {
+    uint32_t n_rays, max_rays, max_compacted, stride;
+    float aabb_min[3], aabb_diag[3];
+    int loss_type, depth_loss_type, srgb, linear_train, penalize;
+    float loss_scale, depth_lambda, seg_lambda, near_distance, beta;
+    const float *rays, *target, *background, *exposure, *depth, *mean_density;
+    const int32_t* seg_mask;
+    const uint32_t *rays_counter, *ray_indices;
+    uint32_t* numsteps;
+    const float *coords, *out;
+    uint32_t* counter;
+    float *coords_out, *dloss, *loss_out;
+};
+
+// One thread per kept ray: the two passes over the ray's samples of the reference kernel.
+__global__ void __launch_bounds__(128) train_loss_kernel(TrainLossArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= min(*a.rays_counter, a.max_rays)) return;
+    const uint32_t numsteps = a.numsteps[2 * i], base = a.numsteps[2 * i + 1];
+    const uint32_t ray = a.ray_indices[i];
+    const float* R = a.rays + (size_t)ray * 6;
+    const float ox = R[0], oy = R[1], oz = R[2];
+    const float* cin = a.coords + (size_t)base * a.stride;
+    const float* nout = a.out + (size_t)base * 4;
+    const float mx = MIN_CONE * 128.0f;
+    float T = 1.f, rgb_ray[3] = {0.f, 0.f, 0.f}, depth_ray = 0.f;
+    uint32_t cn = 0;
+    for (; cn < numsteps; ++cn) {
+        if (T < 1e-4f) break;
+        const float4 o = *reinterpret_cast<const float4*>(nout + (size_t)cn * 4);
+        const float* c = cin + (size_t)cn * a.stride;
+        const float px = a.aabb_min[0] + c[5] * a.aabb_diag[0], py = a.aabb_min[1] + c[6] * a.aabb_diag[1],
+                    pz = a.aabb_min[2] + c[7] * a.aabb_diag[2];
+        const float dt = c[3] * (mx - MIN_CONE) + MIN_CONE;
+        const float dx = px - ox, dy = py - oy, dz = pz - oz;
+        const float cur_depth = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float density = __expf(o.w);
+        const float alpha = 1.f - __expf(-density * dt);
+        const float w = alpha * T;
+        rgb_ray[0] += w * tl_logistic(o.x);
+        rgb_ray[1] += w * tl_logistic(o.y);
+        rgb_ray[2] += w * tl_logistic(o.z);
+        depth_ray += w * cur_depth;
+        T *= (1.f - alpha);
+    }
+    const float T_ray = T;
+    // target colour and background (random_bg_color draw in sRGB, linearised)
+    float bg[3], tgt[3];
+    const float* ts = a.target + (size_t)ray * 4;
+    const float ta = ts[3];
+    float ex[3] = {1.f, 1.f, 1.f};
+    for (int k = 0; k < 3; ++k) {
+        bg[k] = tl_srgb_to_linear(a.background ? a.background[(size_t)ray * 3 + k] : 0.f);
+        if (a.exposure) ex[k] = expf(0.6931471805599453f * a.exposure[(size_t)ray * 3 + k]);
+    }
+    if (a.linear_train || !a.srgb) {
+        for (int k = 0; k < 3; ++k) tgt[k] = ex[k] * ts[k] + (1.f - ta) * bg[k];
+        if (!a.linear_train)
+            for (int k = 0; k < 3; ++k) { tgt[k] = tl_linear_to_srgb(tgt[k]); bg[k] = tl_linear_to_srgb(bg[k]); }
+    } else {
+        for (int k = 0; k < 3; ++k) bg[k] = tl_linear_to_srgb(bg[k]);
+        if (ta > 0.f)
+            for (int k = 0; k < 3; ++k) tgt[k] = tl_linear_to_srgb(ex[k] * ts[k] / ta) * ta + (1.f - ta) * bg[k];
+        else
+            for (int k = 0; k < 3; ++k) tgt[k] = bg[k];
+    }
+    if (cn == numsteps)
+        for (int k = 0; k < 3; ++k) rgb_ray[k] += T * bg[k];
+    // compacted block
+    const uint32_t cbase = atomicAdd(a.counter, cn);
+    const uint32_t ccount = min(a.max_compacted - min(a.max_compacted, cbase), cn);
+    a.numsteps[2 * i] = ccount;
+    a.numsteps[2 * i + 1] = cbase;
+    if (ccount == 0) return;
+    float seg_sup = 1.f, depth_lambda = a.depth_lambda;
+    if (a.seg_mask) {
+        const int m = a.seg_mask[ray];
+        if (m == 120 || m == 130 || m == 140) seg_sup = a.seg_lambda;
+        if (m <= 90 || m > 250) depth_lambda = 0.f;
+        if (ta < 0.001f) depth_lambda = 0.f;
+    }
+    const float dn = sqrtf(R[3] * R[3] + R[4] * R[4] + R[5] * R[5]);
+    const float target_depth = dn * ((depth_lambda > 0.f && a.depth) ? a.depth[ray] : -1.f);
+    float dl, dg;
+    tl_loss(a.depth_loss_type, target_depth, depth_ray, dl, dg);
+    const float depth_grad = (target_depth > 0.f ? dg : 0.f) * depth_lambda;
+    float lgrad[3], lsum = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        float l, g;
+        tl_loss(a.loss_type, tgt[k], rgb_ray[k], l, g);
+        lgrad[k] = g * seg_sup;
+        lsum += l;
+    }
+    if (a.loss_out) a.loss_out[i] = (lsum / 3.f) / (float)a.n_rays;
+    const float loss_scale = a.loss_scale / (float)a.n_rays;
+    const float l1_density = (a.mean_density && *a.mean_density < 0.01f) ? 1e-4f : 0.f;
+    // second pass: the per-sample gradients, and the records copied to their compacted block
+    float rgb2[3] = {0.f, 0.f, 0.f}, depth2 = 0.f;
+    T = 1.f;
+    float* cout = a.coords_out + (size_t)cbase * a.stride;
+    float* dout = a.dloss + (size_t)cbase * 4;
+    for (uint32_t j = 0; j < ccount; ++j) {
+        const float* c = cin + (size_t)j * a.stride;
+        float* co = cout + (size_t)j * a.stride;
+        for (uint32_t k = 0; k < a.stride; ++k) co[k] = c[k];
+        const float px = a.aabb_min[0] + c[5] * a.aabb_diag[0], py = a.aabb_min[1] + c[6] * a.aabb_diag[1],
+                    pz = a.aabb_min[2] + c[7] * a.aabb_diag[2];
+        const float dx = px - ox, dy = py - oy, dz = pz - oz;
+        const float depth = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float dt = c[3] * (mx - MIN_CONE) + MIN_CONE;
+        const float4 o = *reinterpret_cast<const float4*>(nout + (size_t)j * 4);
+        const float rgb[3] = {tl_logistic(o.x), tl_logistic(o.y), tl_logistic(o.z)};
+        const float density = __expf(o.w);
+        const float alpha = 1.f - __expf(-density * dt);
+        const float w = alpha * T;
+        for (int k = 0; k < 3; ++k) rgb2[k] += w * rgb[k];
+        depth2 += w * depth;
+        T *= (1.f - alpha);
+        float d4[4], dot = 0.f;
+        for (int k = 0; k < 3; ++k) {
+            const float suffix = rgb_ray[k] - rgb2[k];
+            d4[k] = loss_scale * ((w * lgrad[k]) * (rgb[k] * (1.f - rgb[k])));   // logistic: no output L2 term
+            dot += lgrad[k] * (T * rgb[k] - suffix);
+        }
+        const float dd = __expf(fminf(fmaxf(o.w, -15.f), 15.f));
+        const float depth_sup = depth_grad * (T * depth - (depth_ray - depth2));
+        const float beta_sup = dt / (T_ray - 1.f + 1e-3f);
+        float dmlp = dd * (dt * (dot + depth_sup) + a.beta * beta_sup);
+        if (a.penalize) dmlp += (ta <= 0.01f) ? w : 0.f;
+        d4[3] = loss_scale * dmlp + (o.w < 0.f ? -l1_density : 0.f) + (o.w > -10.f && depth < a.near_distance ? 1e-4f : 0.f);
+        *reinterpret_cast<float4*>(dout + (size_t)j * 4) = make_float4(d4[0], d4[1], d4[2], d4[3]);
+    }
+}
+
+// tiny-cuda-nn fill_rollover / fill_rollover_and_rescale: entries [count*width, total*width) repeat
+// the first count*width entries; the repeated gradients are scaled by count / total.
+__global__ void __launch_bounds__(256) rollover_kernel(size_t total, uint32_t width, const uint32_t* __restrict__ counter, uint32_t cap,
+                                                       float* __restrict__ data, int rescale, uint32_t n_total) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t cnt = min(*counter, cap);
+    const size_t have = (size_t)cnt * width;
+    if (cnt == 0 || i < have || i >= total) return;
+    float v = data[i % have];
+    if (rescale) v = v * (float)cnt / (float)n_total;
+    data[i] = v;
+}
+
+cudaError_t launch_train_loss(const ::insta_train_loss_desc& d, cudaStream_t s) {
+    TrainLossArgs a{};
+    a.n_rays = d.n_rays; a.max_rays = d.max_rays; a.max_compacted = d.max_samples_compacted; a.stride = d.stride;
+    for (int k = 0; k < 3; ++k) { a.aabb_min[k] = d.aabb_min[k]; a.aabb_diag[k] = d.aabb_max[k] - d.aabb_min[k]; }
+    a.loss_type = d.loss_type; a.depth_loss_type = d.depth_loss_type; a.srgb = d.srgb_targets; a.linear_train = d.train_in_linear_colors;
+    a.penalize = d.penalize_density; a.loss_scale = d.loss_scale; a.depth_lambda = d.depth_supervision_lambda;
+    a.seg_lambda = d.seg_mask_supervision_lambda; a.near_distance = d.near_distance; a.beta = d.beta;
+    a.rays = d.rays; a.target = d.target; a.background = d.background; a.exposure = d.exposure; a.depth = d.depth;
+    a.mean_density = d.mean_density; a.seg_mask = d.seg_mask; a.rays_counter = d.rays_counter; a.ray_indices = d.ray_indices;
+    a.numsteps = d.numsteps; a.coords = d.coords; a.out = d.network_output; a.counter = d.numsteps_counter;
+    a.coords_out = d.coords_out; a.dloss = d.dloss_doutput; a.loss_out = d.loss_output;
+    if (d.max_rays > 0) train_loss_kernel<<<(d.max_rays + 127) / 128, 128, 0, s>>>(a);
+    if (d.target_batch_size > 0) {
+        const size_t nd = (size_t)d.target_batch_size * 4, nc = (size_t)d.target_batch_size * d.stride;
+        rollover_kernel<<<(unsigned)((nd + 255) / 256), 256, 0, s>>>(nd, 4, d.numsteps_counter, d.max_samples_compacted, d.dloss_doutput, 1,
+                                                                       d.target_batch_size);
+        rollover_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(nc, d.stride, d.numsteps_counter, d.max_samples_compacted, d.coords_out, 0,
+                                                                       d.target_batch_size);
+    }
+    return cudaGetLastError();
 }
 
 static unsigned grid_for(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 152 * 32); }

@@ -1207,6 +1207,130 @@ void orc_field_backward(const orc_field_cfg *c, const uint16_t *params, const fl
     }
 }
 
+/* compute_loss_kernel_train_nerf (instant-ngp/src/testbed_nerf.cu:1305-1644) for rays in order
+ * 0..n_kept-1, logistic rgb / exponential density, no error map, envmap, exposure gradient or
+ * importance sampling (pdfs 1); then tiny-cuda-nn's fill_rollover(_and_rescale) restated from
+ * its published source (train_nerf_step, :3349-3357): entries past the compacted count repeat the
+ * compacted ones, the repeated gradients scaled by count / target.  Loss functions :116-180,
+ * :1288-1303.  Single-threaded; the compacted bases follow ray order. */
+static void loss_1(int type, float target, float pred, float *loss, float *grad) {
+    const float d = pred - target;
+    switch (type) {
+    case 1: *loss = fabsf(d); *grad = copysignf(1.f, d); break;
+    case 2: { float f = 1.f / (fabsf(pred) + 1e-2f); *loss = fabsf(d) * f; *grad = copysignf(f, d); } break;
+    case 3: { float f = 1.f / (0.5f * (fabsf(pred) + fabsf(target)) + 1e-2f); *loss = fabsf(d) * f; *grad = copysignf(f, d); } break;
+    case 4: { float a = 0.1f, ad = fabsf(d);
+              *loss = (ad > a ? ad - 0.5f * a : 0.5f / a * d * d) / 5.f;
+              *grad = (ad > a ? (d > 0 ? 1.f : -1.f) : d / a) / 5.f; } break;
+    case 5: { float q = fabsf(d) + 1.f; *loss = logf(q); *grad = copysignf(1.f / q, d); } break;
+    case 6: { float f = 1.f / (pred * pred + 1e-2f); *loss = d * d * f; *grad = 2.f * d * f; } break;
+    default: *loss = d * d; *grad = 2.f * d; break;
+    }
+}
+static float lin_to_srgb_f(float l) { return l < 0.0031308f ? 12.92f * l : 1.055f * powf(l, 0.41666f) - 0.055f; }
+static float logistic_f(float x) { return 1.f / (1.f + expf(-x)); }
+
+void orc_train_loss(const orc_train_loss_cfg *c, uint32_t n_kept, const float *rays, const float *target, const float *background,
+                    const float *exposure, const float *depth_img, const int32_t *seg_mask, const float *mean_density,
+                    const uint32_t *ray_indices, uint32_t *numsteps, const float *coords, const float *nout, uint32_t *counter,
+                    float *coords_out, float *dloss, float *loss_out) {
+    const float mx = MIN_CONE * 128.0f;
+    float diag[3];
+    for (int k = 0; k < 3; ++k) diag[k] = c->aabb_max[k] - c->aabb_min[k];
+    for (uint32_t i = 0; i < n_kept; ++i) {
+        const uint32_t ns = numsteps[2 * i], base = numsteps[2 * i + 1], ray = ray_indices[i];
+        const float *R = rays + (size_t)ray * 6;
+        const float *cin = coords + (size_t)base * c->stride, *o4 = nout + (size_t)base * 4;
+        float T = 1.f, rgb_ray[3] = {0, 0, 0}, depth_ray = 0.f;
+        uint32_t cn = 0;
+        for (; cn < ns; ++cn) {
+            if (T < 1e-4f) break;
+            const float *cc = cin + (size_t)cn * c->stride, *o = o4 + (size_t)cn * 4;
+            float p[3], dd = 0.f;
+            for (int k = 0; k < 3; ++k) { p[k] = c->aabb_min[k] + cc[5 + k] * diag[k]; float t = p[k] - R[k]; dd += t * t; }
+            const float dt = cc[3] * (mx - MIN_CONE) + MIN_CONE, cur = sqrtf(dd);
+            const float alpha = 1.f - expf(-expf(o[3]) * dt), w = alpha * T;
+            for (int k = 0; k < 3; ++k) rgb_ray[k] += w * logistic_f(o[k]);
+            depth_ray += w * cur;
+            T *= 1.f - alpha;
+        }
+        const float T_ray = T;
+        const float *ts = target + (size_t)ray * 4, ta = ts[3];
+        float bg[3], tgt[3], ex[3] = {1.f, 1.f, 1.f};
+        for (int k = 0; k < 3; ++k) {
+            bg[k] = srgb_to_linear_f(background ? background[(size_t)ray * 3 + k] : 0.f);
+            if (exposure) ex[k] = expf(0.6931471805599453f * exposure[(size_t)ray * 3 + k]);
+        }
+        if (c->train_in_linear_colors || !c->srgb_targets) {
+            for (int k = 0; k < 3; ++k) tgt[k] = ex[k] * ts[k] + (1.f - ta) * bg[k];
+            if (!c->train_in_linear_colors) for (int k = 0; k < 3; ++k) { tgt[k] = lin_to_srgb_f(tgt[k]); bg[k] = lin_to_srgb_f(bg[k]); }
+        } else {
+            for (int k = 0; k < 3; ++k) bg[k] = lin_to_srgb_f(bg[k]);
+            for (int k = 0; k < 3; ++k) tgt[k] = ta > 0.f ? lin_to_srgb_f(ex[k] * ts[k] / ta) * ta + (1.f - ta) * bg[k] : bg[k];
+        }
+        if (cn == ns) for (int k = 0; k < 3; ++k) rgb_ray[k] += T * bg[k];
+        const uint32_t cbase = *counter;
+        *counter += cn;
+        const uint32_t mc = c->max_samples_compacted;
+        const uint32_t ccount = (mc - (cbase < mc ? cbase : mc)) < cn ? (mc - (cbase < mc ? cbase : mc)) : cn;
+        numsteps[2 * i] = ccount;
+        numsteps[2 * i + 1] = cbase;
+        if (ccount == 0) continue;
+        float seg_sup = 1.f, dl = c->depth_supervision_lambda;
+        if (seg_mask) {
+            const int m = seg_mask[ray];
+            if (m == 120 || m == 130 || m == 140) seg_sup = c->seg_mask_supervision_lambda;
+            if (m <= 90 || m > 250) dl = 0.f;
+            if (ta < 0.001f) dl = 0.f;
+        }
+        const float dn = sqrtf(R[3] * R[3] + R[4] * R[4] + R[5] * R[5]);
+        const float td = dn * ((dl > 0.f && depth_img) ? depth_img[ray] : -1.f);
+        float l_, g_;
+        loss_1(c->depth_loss_type, td, depth_ray, &l_, &g_);
+        const float depth_grad = (td > 0.f ? g_ : 0.f) * dl;
+        float lg[3], ls = 0.f;
+        for (int k = 0; k < 3; ++k) { loss_1(c->loss_type, tgt[k], rgb_ray[k], &l_, &g_); lg[k] = g_ * seg_sup; ls += l_; }
+        if (loss_out) loss_out[i] = (ls / 3.f) / (float)c->n_rays;
+        const float scale = c->loss_scale / (float)c->n_rays;
+        const float l1d = (mean_density && *mean_density < 0.01f) ? 1e-4f : 0.f;
+        float rgb2[3] = {0, 0, 0}, depth2 = 0.f;
+        T = 1.f;
+        for (uint32_t j = 0; j < ccount; ++j) {
+            const float *cc = cin + (size_t)j * c->stride, *o = o4 + (size_t)j * 4;
+            memcpy(coords_out + (size_t)(cbase + j) * c->stride, cc, sizeof(float) * c->stride);
+            float p[3], dd = 0.f;
+            for (int k = 0; k < 3; ++k) { p[k] = c->aabb_min[k] + cc[5 + k] * diag[k]; float t = p[k] - R[k]; dd += t * t; }
+            const float depth = sqrtf(dd), dt = cc[3] * (mx - MIN_CONE) + MIN_CONE;
+            float rgb[3];
+            for (int k = 0; k < 3; ++k) rgb[k] = logistic_f(o[k]);
+            const float alpha = 1.f - expf(-expf(o[3]) * dt), w = alpha * T;
+            for (int k = 0; k < 3; ++k) rgb2[k] += w * rgb[k];
+            depth2 += w * depth;
+            T *= 1.f - alpha;
+            float *d4 = dloss + (size_t)(cbase + j) * 4, dot = 0.f;
+            for (int k = 0; k < 3; ++k) {
+                d4[k] = scale * ((w * lg[k]) * (rgb[k] * (1.f - rgb[k])));
+                dot += lg[k] * (T * rgb[k] - (rgb_ray[k] - rgb2[k]));
+            }
+            const float ddens = expf(o[3] < -15.f ? -15.f : (o[3] > 15.f ? 15.f : o[3]));
+            const float dsup = depth_grad * (T * depth - (depth_ray - depth2));
+            const float bsup = dt / (T_ray - 1.f + 1e-3f);
+            float dm = ddens * (dt * (dot + dsup) + c->beta * bsup);
+            if (c->penalize_density) dm += ta <= 0.01f ? w : 0.f;
+            d4[3] = scale * dm + (o[3] < 0.f ? -l1d : 0.f) + (o[3] > -10.f && depth < c->near_distance ? 1e-4f : 0.f);
+        }
+    }
+    if (c->target_batch_size > 0) {
+        const uint32_t cnt = *counter < c->max_samples_compacted ? *counter : c->max_samples_compacted;
+        if (cnt > 0)
+            for (uint32_t s = cnt; s < c->target_batch_size; ++s) {
+                const uint32_t from = s % cnt;
+                for (int k = 0; k < 4; ++k) dloss[(size_t)s * 4 + k] = dloss[(size_t)from * 4 + k] * (float)cnt / (float)c->target_batch_size;
+                memcpy(coords_out + (size_t)s * c->stride, coords_out + (size_t)from * c->stride, sizeof(float) * c->stride);
+            }
+    }
+}
+
 /* ---------------------------------------------- single-function exports (pin tests) */
 void orc_tbn(const orc_tri *t, float *m9) { tbn_f(t, m9); }
 void orc_tri2projection(const orc_tri *t, float *M16) { tri2projection_f(t, M16); }

@@ -137,6 +137,16 @@ int64_t orc_render(const orc_render_cfg *rc, const orc_deform *d, const uint8_t 
                    const orc_field_cfg *fc, const uint16_t *params, const float *layer_scales,
                    int row_begin, int row_end, float *out_rgba, float *out_depth,
                    uint32_t *out_nsamples, int fp64);
+typedef struct {
+    uint32_t n_rays, max_samples_compacted, target_batch_size, stride;
+    float aabb_min[3], aabb_max[3];
+    int loss_type, depth_loss_type, srgb_targets, train_in_linear_colors, penalize_density;
+    float loss_scale, depth_supervision_lambda, seg_mask_supervision_lambda, near_distance, beta;
+} orc_train_loss_cfg;
+void orc_train_loss(const orc_train_loss_cfg *c, uint32_t n_kept, const float *rays, const float *target, const float *background,
+                    const float *exposure, const float *depth_img, const int32_t *seg_mask, const float *mean_density,
+                    const uint32_t *ray_indices, uint32_t *numsteps, const float *coords, const float *nout, uint32_t *counter,
+                    float *coords_out, float *dloss, float *loss_out);
 void orc_field_backward(const orc_field_cfg *c, const uint16_t *params, const float *coords, uint32_t stride, int64_t n,
                         const float *dl_dout, double *grad, float *out4);
 void orc_raycast(const orc_render_cfg *rc, const orc_tri *tris, int n_tris, const float *center, int color_normal, float *out_rgba,

@@ -220,6 +220,42 @@ def field_backward(fc, params, coords, dl_dout=None):
     return grad, out
 
 
+class TrainLossCfg(C.Structure):
+    _fields_ = [("n_rays", C.c_uint32), ("max_samples_compacted", C.c_uint32), ("target_batch_size", C.c_uint32),
+                ("stride", C.c_uint32), ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3), ("loss_type", C.c_int),
+                ("depth_loss_type", C.c_int), ("srgb_targets", C.c_int), ("train_in_linear_colors", C.c_int),
+                ("penalize_density", C.c_int), ("loss_scale", C.c_float), ("depth_supervision_lambda", C.c_float),
+                ("seg_mask_supervision_lambda", C.c_float), ("near_distance", C.c_float), ("beta", C.c_float)]
+
+
+def train_loss(cfg: dict, rays, target, ray_indices, numsteps, coords, network_output, background=None, exposure=None,
+               depth=None, seg_mask=None, mean_density=None):
+    """compute_loss_kernel_train_nerf + fill_rollover over the kept rays in order.  cfg keys are
+    TrainLossCfg's fields.  Returns (numsteps out, compacted counter, coords_out, dloss, loss)."""
+    c = TrainLossCfg()
+    for k, v in cfg.items():
+        if k in ("aabb_min", "aabb_max"):
+            getattr(c, k)[:] = [float(x) for x in v]
+        else:
+            setattr(c, k, v)
+    f32 = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)
+    rays, target, coords, network_output = f32(rays), f32(target), f32(coords), f32(network_output)
+    background, exposure, depth = f32(background), f32(exposure), f32(depth)
+    seg = None if seg_mask is None else np.ascontiguousarray(seg_mask, np.int32)
+    md = None if mean_density is None else np.array([mean_density], np.float32)
+    idx = np.ascontiguousarray(ray_indices, np.uint32)
+    ns = np.ascontiguousarray(numsteps, np.uint32).copy()
+    counter = np.zeros(1, np.uint32)
+    cap = int(c.max_samples_compacted)
+    coords_out = np.zeros((cap, int(c.stride)), np.float32)
+    dloss = np.zeros((cap, 4), np.float32)
+    loss = np.zeros(len(idx), np.float32)
+    p = lambda a: None if a is None else ptr(a)
+    lib().orc_train_loss(C.byref(c), C.c_uint32(len(idx)), ptr(rays), ptr(target), p(background), p(exposure), p(depth), p(seg), p(md),
+                         ptr(idx), ptr(ns), ptr(coords), ptr(network_output), ptr(counter), ptr(coords_out), ptr(dloss), ptr(loss))
+    return ns, int(counter[0]), coords_out, dloss, loss
+
+
 def occupancy(tris, radius=0.015) -> np.ndarray:
     bits = np.zeros(8 * 128 ** 3 // 8, dtype=np.uint8)
     lib().orc_occupancy_from_mesh(ptr(tris), C.c_int(len(tris)), C.c_double(radius), ptr(bits))

@@ -1,4 +1,5 @@
-"""Training side of the field (insta_field_backward, insta_adam_step) through the C ABI (cuda:0).
+"""Training side of the field (insta_field_backward, insta_adam_step, insta_train_loss) through the
+C ABI (cuda:0).
 
 Oracle: the FP64 forward/backward of the same network (oracle.field_backward), itself checked
 against finite differences on the CPU.  Tolerances:
@@ -8,7 +9,10 @@ against finite differences on the CPU.  Tolerances:
   moves one sample's share, which the norm absorbs), and every entry within 1e-2 of the
   block's largest gradient;
 * Adam: the FP16 parameters it writes give field outputs within the field parity tolerance
-  (4e-3 + 1e-2 |x|) of the oracle run on a NumPy FP32 Adam of the same gradient.
+  (4e-3 + 1e-2 |x|) of the oracle run on a NumPy FP32 Adam of the same gradient;
+* loss: per kept ray the same compacted count and records (bit-exact), gradients within
+  1e-5 of the batch's largest + 1e-4 relative, per-ray losses 1e-5 relative (the kernel's
+  __expf against the oracle's expf).
 """
 import numpy as np
 import pytest
@@ -161,3 +165,101 @@ def test_argument_errors(ctx, field):
         ctx.field_backward(55, c, 27, 16, None, None, torch.zeros((16, 4), device="cuda"))   # no field on avatar 55
     with pytest.raises(abi.InstaError):
         ctx.adam_step(55, g)
+
+
+def run_loss(ctx, b, cfg, mean_density=None, extra=None):
+    """insta_train_loss on device copies of a synthetic batch; returns host arrays."""
+    n = len(b["ray_indices"])
+    cap = cfg["max_samples_compacted"]
+    as_dev = lambda v: dev(v.view(np.int32) if v.dtype == np.uint32 else v)   # torch has no general uint32
+    d = {k: as_dev(v) for k, v in b.items()}
+    d.update({k: as_dev(v) for k, v in (extra or {}).items()})
+    ns = d["numsteps"].clone()
+    counter = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rays_counter = torch.tensor([n], dtype=torch.int32, device="cuda")
+    cout = torch.zeros((cap, cfg["stride"]), dtype=torch.float32, device="cuda")
+    dloss = torch.zeros((cap, 4), dtype=torch.float32, device="cuda")
+    loss = torch.zeros(n, dtype=torch.float32, device="cuda")
+    md = None if mean_density is None else torch.tensor([mean_density], dtype=torch.float32, device="cuda")
+    kw = {k: v for k, v in cfg.items()}
+    kw.update(d)
+    kw.update(numsteps=ns, numsteps_counter=counter, rays_counter=rays_counter, coords_out=cout, dloss_doutput=dloss,
+              loss_output=loss, mean_density=md, max_rays=n)
+    ctx.train_loss(**kw)
+    ctx.sync()
+    return ns.cpu().numpy().view(np.uint32), int(counter.item()), cout.cpu().numpy(), dloss.cpu().numpy(), loss.cpu().numpy()
+
+
+def check_blocks(got, ref, n_kept):
+    """Per kept ray: same compacted count, same records, gradients within 1e-5 of the batch's
+    largest plus 1e-4 relative (__expf against the oracle's expf), losses to 1e-5 relative."""
+    ns, cnt, cout, dloss, loss = got
+    rns, rcnt, rcout, rdloss, rloss = ref
+    assert cnt == rcnt
+    scale = np.abs(rdloss).max()
+    for k in range(n_kept):
+        c, base, rbase = int(ns[k, 0]), int(ns[k, 1]), int(rns[k, 1])
+        assert c == int(rns[k, 0]), k
+        np.testing.assert_array_equal(cout[base:base + c], rcout[rbase:rbase + c])
+        err = np.abs(dloss[base:base + c] - rdloss[rbase:rbase + c])
+        assert (err <= 1e-5 * scale + 1e-4 * np.abs(rdloss[rbase:rbase + c])).all(), (k, float(err.max()))
+    np.testing.assert_allclose(loss, rloss, rtol=1e-5, atol=1e-9)
+
+
+@pytest.mark.parametrize("loss_type,srgb,linear", [(4, 1, 0), (0, 0, 0), (1, 1, 1), (6, 1, 0)])
+def test_train_loss_matches_oracle(ctx, oracle, loss_type, srgb, linear):
+    from conftest import loss_cfg, train_loss_batch
+    b = train_loss_batch(3000, seed=loss_type, stride=27)
+    cfg = loss_cfg(n_rays=4096, stride=27, loss_type=loss_type, srgb_targets=srgb, train_in_linear_colors=linear, loss_scale=128.0)
+    got = run_loss(ctx, b, cfg)
+    ref = oracle.train_loss(cfg, **b)
+    check_blocks(got, ref, 3000)
+
+
+def test_train_loss_all_terms(ctx, oracle):
+    """Depth supervision, segmentation rules, beta, density penalty, near-distance and mean-density
+    regularisers, exposure; dense rays that stop early on transmittance."""
+    from conftest import loss_cfg, train_loss_batch
+    n = 2000
+    b = train_loss_batch(n, seed=7, stride=27, max_steps=60)
+    rng = np.random.default_rng(8)
+    b["network_output"][::2, 3] += 5.0                      # opaque stretches: early termination
+    extra = dict(depth=rng.uniform(0.2, 2.0, n).astype(np.float32),
+                 seg_mask=rng.choice([0, 100, 120, 130, 140, 255], n).astype(np.int32),
+                 exposure=rng.uniform(-0.5, 0.5, (n, 3)).astype(np.float32))
+    b["target"][::5, 3] = 0.0                                # transparent targets (density penalty)
+    cfg = loss_cfg(n_rays=n, stride=27, loss_type=4, depth_loss_type=1, loss_scale=128.0, depth_supervision_lambda=1.25,
+                   seg_mask_supervision_lambda=40.0, near_distance=0.4, beta=0.05, penalize_density=1)
+    got = run_loss(ctx, {**b, **extra}, cfg, mean_density=0.005)
+    ref = oracle.train_loss(cfg, **b, **extra, mean_density=0.005)
+    check_blocks(got, ref, n)
+    assert int(got[0][:, 0].sum()) < int(b["numsteps"][:, 0].sum())     # some rays stopped early
+
+
+def test_train_loss_cap_and_rollover(ctx, oracle):
+    """max_samples_compacted cuts the batch (which ray is cut depends on the atomic order), the
+    rest is filled to target_batch_size by repetition with the repeated gradients rescaled."""
+    from conftest import loss_cfg, train_loss_batch
+    b = train_loss_batch(1000, seed=11, stride=27)
+    total = int(b["numsteps"][:, 0].sum())
+    cap = total // 2
+    cfg_cut = loss_cfg(n_rays=1000, stride=27, max_samples_compacted=cap, target_batch_size=cap)
+    ns, cnt, cout, dloss, _ = run_loss(ctx, b, cfg_cut)
+    assert cnt == total and int(ns[:, 0].sum()) == cap
+    rns, _, rcout, rdloss, _ = oracle.train_loss(loss_cfg(n_rays=1000, stride=27), **b)
+    scale = np.abs(rdloss).max()
+    for k in range(1000):
+        c, base, rbase = int(ns[k, 0]), int(ns[k, 1]), int(rns[k, 1])
+        assert c <= int(rns[k, 0])
+        if c:
+            np.testing.assert_array_equal(cout[base:base + c], rcout[rbase:rbase + c])
+            assert np.abs(dloss[base:base + c] - rdloss[rbase:rbase + c]).max() <= 1e-5 * scale + 1e-4 * np.abs(rdloss).max()
+    # rollover past a count below the target: the tail repeats the head
+    b2 = train_loss_batch(200, seed=12, stride=27)
+    t2 = int(b2["numsteps"][:, 0].sum())
+    tgt = t2 + 777
+    ns2, cnt2, cout2, dloss2, _ = run_loss(ctx, b2, loss_cfg(n_rays=200, stride=27, max_samples_compacted=tgt, target_batch_size=tgt))
+    assert cnt2 == t2
+    src = np.arange(t2, tgt) % t2
+    np.testing.assert_array_equal(cout2[t2:tgt], cout2[src])
+    np.testing.assert_allclose(dloss2[t2:tgt], dloss2[src] * np.float32(t2 / tgt), rtol=1e-6, atol=0)

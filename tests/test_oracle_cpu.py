@@ -218,3 +218,56 @@ def test_field_backward_oracle_matches_finite_differences(oracle):
         assert abs(fd - grad[i]) <= 2e-3 + 2e-2 * abs(grad[i]), (int(i), fd, grad[i])
         checked += 1
     assert checked == 80 and np.abs(grad[nz_table]).max() > 0
+
+
+@pytest.mark.parametrize("loss_type,srgb", [(0, 1), (4, 0), (0, 0)])
+def test_train_loss_oracle_gradients_match_finite_differences(oracle, loss_type, srgb):
+    from conftest import loss_cfg, train_loss_batch
+    """dL/d(raw output) of the loss kernel is the derivative of its own per-ray losses: with
+    loss_scale 1 and the regularisers off, dloss = 3 d(sum of loss_output)/d(output) (the loss is
+    the channel mean divided by n_rays, the gradient the channel sum divided by n_rays)."""
+    b = train_loss_batch(16, seed=loss_type + 10 * srgb)
+    cfg = loss_cfg(n_rays=16, loss_type=loss_type, srgb_targets=srgb)
+    ns, cnt, _, dloss, loss = oracle.train_loss(cfg, **b)
+    assert cnt == int(b["numsteps"][:, 0].sum())
+    out = b["network_output"].astype(np.float64)
+    rng = np.random.default_rng(1)
+    picks = rng.choice(len(out), 30, replace=False)
+    for s in picks:
+        for ch in range(4):
+            vals = []
+            for h in (+1e-2, -1e-2):
+                o2 = out.copy()
+                o2[s, ch] += h
+                vals.append(float(oracle.train_loss(cfg, **{**b, "network_output": o2})[4].astype(np.float64).sum()))
+            fd = 3 * (vals[0] - vals[1]) / 2e-2
+            # the kernel writes each ray's block at its compacted base; rays are compacted in kept order
+            k = int(np.searchsorted(b["numsteps"][:, 1], s, side="right") - 1)
+            j = s - int(b["numsteps"][k, 1])
+            an = float(dloss[int(ns[k, 1]) + j, ch])
+            assert abs(fd - an) <= 2e-4 + 2e-2 * abs(an), (s, ch, fd, an)
+
+
+def test_train_loss_oracle_compaction_and_rollover(oracle):
+    """Blocks past max_samples_compacted are cut (the ray that crosses it keeps its prefix), the
+    compacted arrays are filled to target_batch_size by repetition, the repeated gradients scaled
+    by count / target."""
+    from conftest import loss_cfg, train_loss_batch
+    b = train_loss_batch(40, seed=5)
+    total = int(b["numsteps"][:, 0].sum())
+    cap = total * 2 // 3
+    ns, cnt, cout, dloss, _ = oracle.train_loss(loss_cfg(n_rays=40, max_samples_compacted=cap, target_batch_size=cap), **b)
+    assert cnt == total and int(ns[:, 0].sum()) == cap
+    ref_ns, _, ref_cout, ref_dloss, _ = oracle.train_loss(loss_cfg(n_rays=40), **b)
+    for k in range(40):
+        c, base = int(ns[k, 0]), int(ns[k, 1])
+        assert base == int(ref_ns[k, 1])
+        if c:
+            np.testing.assert_array_equal(dloss[base:base + c], ref_dloss[base:base + c])
+            np.testing.assert_array_equal(cout[base:base + c], ref_cout[base:base + c])
+    ns2, _, cout2, dloss2, _ = oracle.train_loss(loss_cfg(n_rays=40, max_samples_compacted=2 * total, target_batch_size=2 * total - 5),
+                                                 **b)
+    n = 2 * total - 5
+    src = np.arange(total, n) % total
+    np.testing.assert_array_equal(cout2[total:n], cout2[src])
+    np.testing.assert_allclose(dloss2[total:n], dloss2[src] * np.float32(total / n), rtol=1e-6)
