@@ -540,6 +540,68 @@ def run_grid(args):
     ctx.close()
 
 
+def run_train(args):
+    """One training step of the field (Testbed::train_nerf_step as insta_gb300.train.TrainStep
+    runs it): 4096 rays per batch through the tracked frame's occupancy, the field evaluated on
+    every march sample, the loss over the rays, backward over the 2^18-sample compacted batch
+    (rollover-filled), Adam.  The bench field with 16 expression dims.  Device time per stage
+    from the library's events, wall time per step with the step's one counter read-back."""
+    import torch
+    from insta_gb300 import abi, synthetic as S
+    from insta_gb300.train import TrainConfig, TrainStep
+    av = S.make_avatar(0)
+    fc = S.FieldConfig(n_extra=16)
+    ctx = abi.Context(0)
+    ctx.canonical_set(0, av.canonical, av.faces, av.mask)
+    ctx.frame_upload(0, 0, av.frame(av.frame_coeffs(0)))
+    ctx.occupancy_from_mesh(0, 0, 0.015)
+    ctx.params_load(0, fc, S.field_params(fc, seed=0))
+    cfg = TrainConfig(n_rays_per_batch=4096, target_batch_size=1 << 18, max_samples=1 << 20)
+    ts = TrainStep(ctx, 0, fc, cfg)
+    rng = np.random.default_rng(0)
+    n = cfg.n_rays_per_batch
+
+    def batch():
+        c0 = np.array([0.5, 0.5, 0.5], np.float32)
+        u = rng.normal(size=(n, 3))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        org = c0 + u * 0.9
+        tgt = c0 + rng.normal(0, 0.05, (n, 3))
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        return (dev(np.concatenate([org, tgt - org], 1).astype(np.float32)), dev(np.zeros(n, np.int32)),
+                dev(rng.random(n).astype(np.float32)), dev(rng.uniform(0, 1, (n, 4)).astype(np.float32)),
+                dev(rng.uniform(0, 1, (n, 3)).astype(np.float32)), dev(rng.uniform(-1, 1, (1, 16)).astype(np.float32)))
+
+    batches = [batch() for _ in range(4)]
+
+    def step(k):
+        r, img, rnd, tgt, bg, ex = batches[k % len(batches)]
+        return ts.step(0, r, img, rnd, tgt, background=bg, extra=ex, n_images=1)
+
+    for k in range(max(3, args.warmup)):
+        step(k)
+    ctx.sync()
+    ctx.stats(reset=True)
+    ctx.stats_enable(True)
+    samples = 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        samples += step(k)["samples"]
+    ctx.sync()
+    wall = (time.perf_counter() - t0) / args.steps
+    st = ctx.stats(reset=True)
+    ctx.stats_enable(False)
+    stage = {k: v / args.steps for k, v in st["stage_ms"].items() if v > 0}
+    dev_ms = sum(stage.values())
+    line = {"workload": "training step: 4096 rays, 2^18-sample batch, field with 16 expression dims",
+            "ms_per_step_device": dev_ms, "ms_per_step_wall": wall * 1e3, "stage_ms_per_step": stage,
+            "march_samples_per_step": samples / args.steps,
+            "trained_samples_per_s_device": cfg.target_batch_size / (dev_ms / 1e3),
+            "rays_per_s_wall": n / wall}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_raycast(args):
     """raycast_flame of the 10,240-triangle tracked frame at 512^2 and 1024^2 (closest hit over the
     frame's LBVH + shading).  Device time from the library's stage events; the CPU restatement
@@ -758,7 +820,7 @@ def main():
                     help="per-stage CUDA events on every render (host-driven rounds instead of the CUDA-graph loop; "
                          "for kernel-level profiles)")
     ap.add_argument("--width", type=int, default=512, help="square render size (512 = the benchmark workload)")
-    ap.add_argument("--workload", choices=["render", "batch", "serve", "precision", "map", "grid", "raycast"], default="render",
+    ap.add_argument("--workload", choices=["render", "batch", "serve", "precision", "map", "grid", "raycast", "train"], default="render",
                     help="render: the benchmark line; batch: 64 expressions in one wavefront; serve: request stream; "
                          "precision: FP16 / BF16 / FP8 MLPs at 1024x1024 against the FP64 oracle; "
                          "map: canonical mapping of 1M shell points; grid: density-grid update; raycast: mesh raycast")
@@ -781,6 +843,8 @@ def main():
         return run_map(args)
     if args.workload == "grid":
         return run_grid(args)
+    if args.workload == "train":
+        return run_train(args)
     if args.workload == "raycast":
         return run_raycast(args)
     rank, world, local = dist_env()

@@ -116,7 +116,8 @@ typedef struct {
 #define INSTA_STAGE_FIELD 8          /* insta_field_eval / _static               */
 #define INSTA_STAGE_SORT 9           /* regrouping a round's samples by (request, cell) */
 #define INSTA_STAGE_RAYCAST 10       /* insta_raycast                            */
-#define INSTA_STAGE_COUNT 11
+#define INSTA_STAGE_TRAIN 11         /* insta_train_loss, field_backward, adam   */
+#define INSTA_STAGE_COUNT 12
 
 typedef struct {
     uint64_t kernel_launches;        /* kernels the library launched */

@@ -85,7 +85,7 @@ class FieldDesc(C.Structure):
 
 
 STAGES = ["frame", "occupancy", "ray_init", "march", "deform_encode", "mlp", "composite", "canonical_map", "field", "sort",
-          "raycast"]
+          "raycast", "train"]
 
 
 class Stats(C.Structure):

@@ -1519,7 +1519,7 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
         ensure_master(ctx, fd);
         const TrainShape t = train_shape(fd);
         ctx->alloc(ctx->train_scratch, train_scratch_floats(t, (uint32_t)n) * 4);
-        Stage st(ctx, INSTA_STAGE_FIELD, 8 + 2 * (t.n_density + t.n_rgb));
+        Stage st(ctx, INSTA_STAGE_TRAIN, 8 + 2 * (t.n_density + t.n_rgb));
         CK(launch_field_train(ctx->blas, fd.view, t, (const float*)fd.w32.p, coords, stride, (uint32_t)n, dl_dout, out4, grad,
                               (float*)ctx->train_scratch.p, ctx->stream));
     });
@@ -1541,7 +1541,7 @@ int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_a
         ctx->alloc(fd.w16, fd.n_params * 2);
         const uint32_t step = ++fd.adam_step;
         {
-            Stage st(ctx, INSTA_STAGE_FIELD, 1);
+            Stage st(ctx, INSTA_STAGE_TRAIN, 1);
             CK(launch_adam(fd.n_params, (float*)fd.w32.p, (float*)fd.adam_m.p, (float*)fd.adam_v.p, grad, cfg->learning_rate, cfg->beta1,
                            cfg->beta2, cfg->epsilon, cfg->l2_reg, step, (__half*)fd.w16.p, ctx->stream));
         }
@@ -1573,7 +1573,7 @@ int insta_train_loss(insta_ctx* ctx, const insta_train_loss_desc* d) {
         if (((uintptr_t)d->network_output | (uintptr_t)d->dloss_doutput) & 15)
             fail(INSTA_ERR_INVALID_ARG, "network_output and dloss_doutput must be 16-byte aligned");
         {
-            Stage st(ctx, INSTA_STAGE_FIELD, d->target_batch_size > 0 ? 3 : 1);
+            Stage st(ctx, INSTA_STAGE_TRAIN, d->target_batch_size > 0 ? 3 : 1);
             CK(launch_train_loss(*d, ctx->stream));
         }
     });

@@ -81,10 +81,13 @@ def test_backward_accumulates_and_forward_only(ctx, field, oracle):
     c = dev(coords(n, seed=3))
     g_out = dev(np.random.default_rng(4).normal(size=(n, 4)).astype(np.float32))
     g1 = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()                             # torch's stream -> the context's stream
     ctx.field_backward(AVATAR, c, 27, n, g_out, g1)
+    ctx.sync()
     g2 = g1.clone()
-    ctx.field_backward(AVATAR, c, 27, n, g_out, g2)      # adds a second copy
     out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    ctx.field_backward(AVATAR, c, 27, n, g_out, g2)      # adds a second copy
     ctx.field_backward(AVATAR, c, 27, n, None, None, out)  # forward only
     ctx.sync()
     a, b = g1.cpu().numpy(), g2.cpu().numpy()
@@ -142,13 +145,17 @@ def test_regression_loss_decreases(ctx, field):
     grad = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
     losses = []
     for step in range(200):
+        torch.cuda.synchronize()                         # the context's stream is not torch's
         ctx.field_backward(AVATAR, c, 27, n, None, None, out)
+        ctx.sync()
         diff = out - target
         losses.append(float((diff * diff).mean()))
         grad.zero_()
-        ctx.field_backward(AVATAR, c, 27, n, (2.0 / diff.numel()) * diff, grad)
+        dl = (2.0 / diff.numel()) * diff
+        torch.cuda.synchronize()
+        ctx.field_backward(AVATAR, c, 27, n, dl, grad)
         ctx.adam_step(AVATAR, grad, learning_rate=1e-2)
-    ctx.sync()
+        ctx.sync()
     assert np.isfinite(losses).all() and losses[-1] < 0.1 * losses[0], (losses[0], losses[-1])
 
 
@@ -185,6 +192,7 @@ def run_loss(ctx, b, cfg, mean_density=None, extra=None):
     kw.update(d)
     kw.update(numsteps=ns, numsteps_counter=counter, rays_counter=rays_counter, coords_out=cout, dloss_doutput=dloss,
               loss_output=loss, mean_density=md, max_rays=n)
+    torch.cuda.synchronize()                             # buffers filled on torch's stream
     ctx.train_loss(**kw)
     ctx.sync()
     return ns.cpu().numpy().view(np.uint32), int(counter.item()), cout.cpu().numpy(), dloss.cpu().numpy(), loss.cpu().numpy()
@@ -263,3 +271,36 @@ def test_train_loss_cap_and_rollover(ctx, oracle):
     src = np.arange(t2, tgt) % t2
     np.testing.assert_array_equal(cout2[t2:tgt], cout2[src])
     np.testing.assert_allclose(dloss2[t2:tgt], dloss2[src] * np.float32(t2 / tgt), rtol=1e-6, atol=0)
+
+
+def test_train_step_fits_a_constant_colour(ctx, avatar, frame0):
+    """insta_gb300.train.TrainStep: training samples -> field evaluation -> loss -> backward ->
+    Adam, 80 steps towards an opaque constant-colour target, lowers the batch loss 4x."""
+    from insta_gb300 import synthetic as S
+    from insta_gb300.train import TrainConfig, TrainStep
+    aid = 22
+    ctx.canonical_set(aid, avatar.canonical, avatar.faces, avatar.mask)
+    ctx.frame_upload(aid, 0, frame0)
+    ctx.occupancy_from_mesh(aid, 0, 0.015)
+    fc = S.FieldConfig()
+    ctx.params_load(aid, fc, S.field_params(fc, seed=2))
+    cfg = TrainConfig(n_rays_per_batch=4096, target_batch_size=1 << 16, max_samples=1 << 19)
+    cfg.adam["learning_rate"] = 1e-2
+    ts = TrainStep(ctx, aid, fc, cfg)
+    rng = np.random.default_rng(3)
+    n = cfg.n_rays_per_batch
+    target = dev(np.tile(np.array([[0.8, 0.3, 0.2, 1.0]], np.float32), (n, 1)))
+    image = dev(np.zeros(n, np.int32))
+    losses, kept = [], []
+    for step in range(80):
+        c0 = np.array([0.5, 0.5, 0.5], np.float32)
+        u = rng.normal(size=(n, 3))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        org = c0 + u * 0.9
+        tgt = c0 + rng.normal(0, 0.05, (n, 3))
+        rays = dev(np.concatenate([org, tgt - org], 1).astype(np.float32))
+        info = ts.step(0, rays, image, dev(rng.random(n).astype(np.float32)), target)
+        kept.append(info["rays_kept"])
+        losses.append(ts.loss_value())
+    assert min(kept) > n // 2
+    assert np.isfinite(losses).all() and np.mean(losses[-5:]) < 0.25 * np.mean(losses[:5]), (losses[:5], losses[-5:])
