@@ -263,9 +263,11 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
  * for n NerfCoordinate records (canonical position, direction, expression dims; device
  * pointers) and the loss gradient w.r.t. each record's outputs dl_dout f32[n][4] (raw r, g, b,
  * raw density), ADD the gradient of every parameter to grad f32[n_params] (snapshot order:
- * density MLP, colour MLP, hash table).  FP32 throughout from the FP32 master weights (the FP16
- * parameters at the first call after insta_params_load).  out4 (optional) gets the outputs of
- * that FP32 forward; with dl_dout = grad = NULL only the forward runs.  n < 2^24. */
+ * density MLP, colour MLP, hash table; 8-byte aligned).  FP32 arithmetic; the MLP weights come
+ * from the FP32 master copy (the FP16 parameters widened at the first call after
+ * insta_params_load), the hash table from the FP16 parameters as the forward pass reads them.
+ * out4 (optional) gets the outputs of that FP32 forward; with dl_dout = grad = NULL only the
+ * forward runs.  n < 2^24. */
 int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, const float* dl_dout, float* grad,
                          float* out4);
 /* Adam (configs/nerf/main.json nests it in an Ema): w -= lr * m_hat / (sqrt(v_hat) + eps) with

@@ -132,6 +132,7 @@ struct insta_ctx {
     int async_next = 0;
     cublasHandle_t blas = nullptr;      // the training side's GEMMs
     DevBuf train_scratch;
+    DevBuf loss_scratch;     // insta_train_loss: each kept ray's block start before compaction
     bool keep_master = false;           // a parameter reload from the optimizer keeps the FP32 master weights
     cudaStream_t side = nullptr;        // asynchronous frame uploads
     cudaEvent_t side_mark = nullptr;    // orders a side upload after the main stream's earlier work
@@ -914,6 +915,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     }
     if (ctx->blas) cublasDestroy(ctx->blas);
     ctx->release(ctx->train_scratch);
+    ctx->release(ctx->loss_scratch);
     if (ctx->loop_exec) cudaGraphExecDestroy(ctx->loop_exec);
     if (ctx->loop_graph) cudaGraphDestroy(ctx->loop_graph);
     if (ctx->loop_state) cudaFree(ctx->loop_state);
@@ -1514,6 +1516,7 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
         if (n > 0 && (!coords || (!out4 && !(dl_dout && grad)))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
         if ((dl_dout == nullptr) != (grad == nullptr)) fail(INSTA_ERR_INVALID_ARG, "output gradients and parameter gradients go together");
         if (stride < 11 + fd.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
+        if ((uintptr_t)grad & 7) fail(INSTA_ERR_INVALID_ARG, "grad must be 8-byte aligned");   // paired table atomics
         if (n == 0) return;
         if (!ctx->blas && cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) fail(INSTA_ERR_CUDA, "cublasCreate failed");
         ensure_master(ctx, fd);
@@ -1573,8 +1576,9 @@ int insta_train_loss(insta_ctx* ctx, const insta_train_loss_desc* d) {
         if (((uintptr_t)d->network_output | (uintptr_t)d->dloss_doutput) & 15)
             fail(INSTA_ERR_INVALID_ARG, "network_output and dloss_doutput must be 16-byte aligned");
         {
-            Stage st(ctx, INSTA_STAGE_TRAIN, d->target_batch_size > 0 ? 3 : 1);
-            CK(launch_train_loss(*d, ctx->stream));
+            ctx->alloc(ctx->loss_scratch, (size_t)std::max(d->max_rays, 1u) * 4);
+            Stage st(ctx, INSTA_STAGE_TRAIN, (d->max_rays > 0 ? 2 : 0) + (d->target_batch_size > 0 ? 2 : 0));
+            CK(launch_train_loss(*d, (uint32_t*)ctx->loss_scratch.p, ctx->stream));
         }
     });
 }

@@ -866,7 +866,9 @@ cudaError_t launch_unpack(const uint2* out, const float4* out_f32, int bf16, int
 
 cudaError_t launch_training_samples(const TrainArgs& a, cudaStream_t s) {
     if (a.n_rays <= 0) return cudaSuccess;
-    training_samples_kernel<<<(unsigned)((a.n_rays + 255) / 256), 256, 0, s>>>(a);
+    // one ray per thread; small batches (a few thousand rays) in 32-thread blocks so that they spread over every SM
+    const int threads = a.n_rays < 152 * 128 ? 32 : 128;
+    training_samples_kernel<<<(unsigned)((a.n_rays + threads - 1) / threads), threads, 0, s>>>(a);
     return cudaGetLastError();
 }
 

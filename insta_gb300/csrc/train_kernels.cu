@@ -105,8 +105,7 @@ __global__ void __launch_bounds__(256) hash_backward_kernel(FieldView fv, const 
             } else {
                 idx = ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
             }
-            atomicAdd(lt + (size_t)idx * 2, w * g0);
-            atomicAdd(lt + (size_t)idx * 2 + 1, w * g1);
+            atomicAdd(reinterpret_cast<float2*>(lt) + idx, make_float2(w * g0, w * g1));   // one 8-byte reduction per corner
         }
     }
 }
@@ -171,10 +170,11 @@ struct TrainLossArgs {
     const float *coords, *out;
     uint32_t* counter;
     float *coords_out, *dloss, *loss_out;
+    uint32_t* base_in;   // each kept ray's block start before compaction (for the copy kernel)
 };
 
 // One thread per kept ray: the two passes over the ray's samples of the reference kernel.
-__global__ void __launch_bounds__(128) train_loss_kernel(TrainLossArgs a) {
+__global__ void __launch_bounds__(32) train_loss_kernel(TrainLossArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= min(*a.rays_counter, a.max_rays)) return;
     const uint32_t numsteps = a.numsteps[2 * i], base = a.numsteps[2 * i + 1];
@@ -232,6 +232,7 @@ __global__ void __launch_bounds__(128) train_loss_kernel(TrainLossArgs a) {
     const uint32_t ccount = min(a.max_compacted - min(a.max_compacted, cbase), cn);
     a.numsteps[2 * i] = ccount;
     a.numsteps[2 * i + 1] = cbase;
+    a.base_in[i] = base;
     if (ccount == 0) return;
     float seg_sup = 1.f, depth_lambda = a.depth_lambda;
     if (a.seg_mask) {
@@ -258,12 +259,9 @@ __global__ void __launch_bounds__(128) train_loss_kernel(TrainLossArgs a) {
     // second pass: the per-sample gradients, and the records copied to their compacted block
     float rgb2[3] = {0.f, 0.f, 0.f}, depth2 = 0.f;
     T = 1.f;
-    float* cout = a.coords_out + (size_t)cbase * a.stride;
     float* dout = a.dloss + (size_t)cbase * 4;
     for (uint32_t j = 0; j < ccount; ++j) {
         const float* c = cin + (size_t)j * a.stride;
-        float* co = cout + (size_t)j * a.stride;
-        for (uint32_t k = 0; k < a.stride; ++k) co[k] = c[k];
         const float px = a.aabb_min[0] + c[5] * a.aabb_diag[0], py = a.aabb_min[1] + c[6] * a.aabb_diag[1],
                     pz = a.aabb_min[2] + c[7] * a.aabb_diag[2];
         const float dx = px - ox, dy = py - oy, dz = pz - oz;
@@ -293,6 +291,20 @@ __global__ void __launch_bounds__(128) train_loss_kernel(TrainLossArgs a) {
     }
 }
 
+// The records of each kept ray's compacted block, copied after the loss kernel has placed the
+// block: one warp per ray, the block's floats are contiguous on both sides (coalesced).
+__global__ void __launch_bounds__(256) compact_copy_kernel(const uint32_t* __restrict__ rays_counter, uint32_t max_rays,
+                                                           const uint32_t* __restrict__ numsteps_in, const uint32_t* __restrict__ numsteps,
+                                                           uint32_t stride, const float* __restrict__ coords, float* __restrict__ coords_out) {
+    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (k >= min(*rays_counter, max_rays)) return;
+    const uint32_t count = numsteps[2 * k], cbase = numsteps[2 * k + 1], base = numsteps_in[k];
+    const size_t nf = (size_t)count * stride;
+    const float* src = coords + (size_t)base * stride;
+    float* dst = coords_out + (size_t)cbase * stride;
+    for (size_t f = lane; f < nf; f += 32) dst[f] = src[f];
+}
+
 // tiny-cuda-nn fill_rollover / fill_rollover_and_rescale: entries [count*width, total*width) repeat
 // the first count*width entries; the repeated gradients are scaled by count / total.
 __global__ void __launch_bounds__(256) rollover_kernel(size_t total, uint32_t width, const uint32_t* __restrict__ counter, uint32_t cap,
@@ -306,7 +318,7 @@ __global__ void __launch_bounds__(256) rollover_kernel(size_t total, uint32_t wi
     data[i] = v;
 }
 
-cudaError_t launch_train_loss(const ::insta_train_loss_desc& d, cudaStream_t s) {
+cudaError_t launch_train_loss(const ::insta_train_loss_desc& d, uint32_t* base_scratch, cudaStream_t s) {
     TrainLossArgs a{};
     a.n_rays = d.n_rays; a.max_rays = d.max_rays; a.max_compacted = d.max_samples_compacted; a.stride = d.stride;
     for (int k = 0; k < 3; ++k) { a.aabb_min[k] = d.aabb_min[k]; a.aabb_diag[k] = d.aabb_max[k] - d.aabb_min[k]; }
@@ -316,8 +328,13 @@ cudaError_t launch_train_loss(const ::insta_train_loss_desc& d, cudaStream_t s) 
     a.rays = d.rays; a.target = d.target; a.background = d.background; a.exposure = d.exposure; a.depth = d.depth;
     a.mean_density = d.mean_density; a.seg_mask = d.seg_mask; a.rays_counter = d.rays_counter; a.ray_indices = d.ray_indices;
     a.numsteps = d.numsteps; a.coords = d.coords; a.out = d.network_output; a.counter = d.numsteps_counter;
-    a.coords_out = d.coords_out; a.dloss = d.dloss_doutput; a.loss_out = d.loss_output;
-    if (d.max_rays > 0) train_loss_kernel<<<(d.max_rays + 127) / 128, 128, 0, s>>>(a);
+    a.coords_out = d.coords_out; a.dloss = d.dloss_doutput; a.loss_out = d.loss_output; a.base_in = base_scratch;
+    if (d.max_rays > 0) {
+        // one ray per thread in 32-thread blocks: a batch of a few thousand rays spreads over every SM
+        train_loss_kernel<<<(d.max_rays + 31) / 32, 32, 0, s>>>(a);
+        compact_copy_kernel<<<(unsigned)(((size_t)d.max_rays * 32 + 255) / 256), 256, 0, s>>>(d.rays_counter, d.max_rays, base_scratch,
+                                                                                               d.numsteps, d.stride, d.coords, d.coords_out);
+    }
     if (d.target_batch_size > 0) {
         const size_t nd = (size_t)d.target_batch_size * 4, nc = (size_t)d.target_batch_size * d.stride;
         rollover_kernel<<<(unsigned)((nd + 255) / 256), 256, 0, s>>>(nd, 4, d.numsteps_counter, d.max_samples_compacted, d.dloss_doutput, 1,
