@@ -1302,6 +1302,7 @@ int insta_training_samples(insta_ctx* ctx, int avatar, int grid_frame, const flo
         if (n_rays < 0 || (n_rays > 0 && (!rays || !image || !start_rand)) || !coords || !ray_indices || !numsteps || !counters)
             fail(INSTA_ERR_INVALID_ARG, "null buffer");
         if (stride < 11) fail(INSTA_ERR_INVALID_ARG, "stride %u < 11", stride);
+        if (max_samples >= (1u << 30)) fail(INSTA_ERR_INVALID_ARG, "max_samples must be below 2^30");
         if (!(cone_angle >= 0.f)) fail(INSTA_ERR_INVALID_ARG, "cone_angle must be >= 0");
         for (const void* p : {(const void*)rays, (const void*)image, (const void*)start_rand, (const void*)coords, (const void*)ray_indices,
                               (const void*)numsteps, (const void*)counters})
@@ -1320,10 +1321,18 @@ int insta_training_samples(insta_ctx* ctx, int avatar, int grid_frame, const flo
         T.cone_angle = cone_angle; T.max_samples = max_samples; T.bitfield = (const uint8_t*)g.bitfield.p;
         T.coords = coords; T.stride = stride; T.ray_indices = ray_indices; T.numsteps = numsteps; T.counters = counters;
         { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_training_samples(T, ctx->stream)); }
-        // the warp with per-record frames (surface_closest_point, testbed_nerf.cu:3290)
-        Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
-        CK(launch_canonical_map_coords((const FrameView*)a.frame_table.p, a.table_frames, deform_view(a), coords, stride, stride - 11,
-                                       (int64_t)max_samples, -1, ctx->err_dev, ctx->stream, counters + 1));
+        // the warp with per-record frames (surface_closest_point, testbed_nerf.cu:3290): large sample
+        // buffers take the (frame, cell)-sorted warp walk over the records the march wrote
+        if (max_samples >= kMapSortedMin && a.table_frames <= kMaxRequests) {
+            ctx->alloc(ctx->map_scratch, warp_sorted_scratch_bytes(max_samples, a.table_frames));
+            Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 6);
+            CK(launch_canonical_map_coords_sorted((const FrameView*)a.frame_table.p, a.table_frames, 0, deform_view(a), coords, stride,
+                                                  stride - 11, max_samples, ctx->map_scratch.p, ctx->err_dev, ctx->stream, counters + 1));
+        } else {
+            Stage st(ctx, INSTA_STAGE_CANONICAL_MAP, 1);
+            CK(launch_canonical_map_coords((const FrameView*)a.frame_table.p, a.table_frames, deform_view(a), coords, stride, stride - 11,
+                                           (int64_t)max_samples, -1, ctx->err_dev, ctx->stream, counters + 1));
+        }
     });
 }
 

@@ -127,7 +127,8 @@ cudaError_t launch_warp_random_sorted(const FrameView* frames_dev, uint32_t n_fr
 // insta_canonical_map on many records: (frame, cell)-sorted warp walk; fixed != 0: frames_dev is
 // the one frame (n_frames 1) and holder only gates; scratch: warp_sorted_scratch_bytes(n, n_frames)
 cudaError_t launch_canonical_map_coords_sorted(const FrameView* frames_dev, uint32_t n_frames, int fixed, const DeformView& dv, float* coords,
-                                               uint32_t stride, uint32_t n_extra, uint32_t n, void* scratch, uint32_t* err, cudaStream_t s);
+                                               uint32_t stride, uint32_t n_extra, uint32_t n, void* scratch, uint32_t* err, cudaStream_t s,
+                                               const uint32_t* n_dev = nullptr);   // optional device count: records past it untouched
 cudaError_t launch_splat_ema(uint32_t n, const uint32_t* indices, const uint2* out, const float4* out_f32, int f32_out, float* tmp,
                              float* grid, uint32_t n_cells, float decay, cudaStream_t s);
 cudaError_t launch_density_grid(const void* grid, int fp16, uint32_t n_cascades, void* scratch, uint8_t* bitfield, cudaStream_t s);

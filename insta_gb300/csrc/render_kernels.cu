@@ -1050,15 +1050,17 @@ __global__ void __launch_bounds__(256) gwarp_map_kernel(const FrameView* __restr
 // and stay untouched.
 __global__ void __launch_bounds__(256) coords_key_kernel(const FrameView* __restrict__ frames, uint32_t n_frames, int fixed, DeformView dv,
                                                          const float* __restrict__ coords, uint32_t stride, uint32_t n, uint32_t cell_bits,
-                                                         uint32_t* __restrict__ keys, uint32_t* __restrict__ bins, uint32_t* __restrict__ n_round) {
+                                                         uint32_t* __restrict__ keys, uint32_t* __restrict__ bins, uint32_t* __restrict__ n_round,
+                                                         const uint32_t* __restrict__ n_dev) {
     const uint32_t lane = threadIdx.x & 31u;
     if (blockIdx.x == 0 && threadIdx.x == 0) *n_round = n;
+    const uint32_t n_live = n_dev ? min(n, *n_dev) : n;   // records past a device count get no key
     const uint32_t per_axis = 1u << (cell_bits / 3);
     const float top = (float)(per_axis - 1);
     for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
         const uint32_t i = b + threadIdx.x;
         uint32_t key = 0xffffffffu;
-        if (i < n) {
+        if (i < n_live) {
             const float* c = coords + (size_t)i * stride;
             const float holder = c[4];
             const V3 p = v3(c[0], c[1], c[2]);
@@ -1071,8 +1073,8 @@ __global__ void __launch_bounds__(256) coords_key_kernel(const FrameView* __rest
                     q[k] = (uint32_t)fminf(fmaxf((pp[k] - dv.aabb_min[k]) / (dv.aabb_max[k] - dv.aabb_min[k]) * (float)per_axis, 0.f), top);
                 key = (fid << cell_bits) | spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
             }
-            keys[i] = key;
         }
+        if (i < n) keys[i] = key;
         const uint32_t peers = __match_any_sync(0xffffffffu, key);
         if (key != 0xffffffffu && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(bins + key, (uint32_t)__popc(peers));
     }
@@ -1098,7 +1100,8 @@ __global__ void __launch_bounds__(256) coords_map_kernel(const FrameView* __rest
 }
 
 cudaError_t launch_canonical_map_coords_sorted(const FrameView* frames_dev, uint32_t n_frames, int fixed, const DeformView& dv, float* coords,
-                                               uint32_t stride, uint32_t n_extra, uint32_t n, void* scratch, uint32_t* err, cudaStream_t s) {
+                                               uint32_t stride, uint32_t n_extra, uint32_t n, void* scratch, uint32_t* err, cudaStream_t s,
+                                               const uint32_t* n_dev) {
     if (n == 0) return cudaSuccess;
     const uint32_t cb = sort_cell_bits(n_frames);
     const uint32_t n_bins = n_frames << cb;
@@ -1124,7 +1127,7 @@ cudaError_t launch_canonical_map_coords_sorted(const FrameView* frames_dev, uint
     cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)n_bins * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)std::min<uint32_t>((n + 255) / 256, (uint32_t)sm_count() * 8);
-    coords_key_kernel<<<grid, 256, 0, s>>>(frames_dev, n_frames, fixed, dv, coords, stride, n, cb, keys, bins, counters);
+    coords_key_kernel<<<grid, 256, 0, s>>>(frames_dev, n_frames, fixed, dv, coords, stride, n, cb, keys, bins, counters, n_dev);
     sort_scan_kernel<<<n_bins / kSortBlock, kSortBlock, 0, s>>>(bins, block_sums);
     sort_offsets_kernel<<<1, kSortBlock, 0, s>>>(a, n_bins / kSortBlock);
     sort_place_kernel<<<sm_count() * 8, 256, 0, s>>>(a);

@@ -73,24 +73,28 @@ __global__ void __launch_bounds__(256) train_density_grad_kernel(uint32_t n, con
 }
 
 // Hash encode backward: every corner's trilinear weight times the encoding gradient, added into
-// the table gradient (FP32, [entries][2] like the table).
+// the table gradient (FP32, [entries][2] like the table, one 8-byte reduction per entry).
+// Samples arrive in ray order, so neighbouring lanes of a warp often hit the same corner (every
+// coarse level, and fine levels along short steps): lanes with equal entries in a row are summed
+// first (a segmented scan over the warp) and only the last lane of each run adds to memory.
 __global__ void __launch_bounds__(256) hash_backward_kernel(FieldView fv, const float* __restrict__ coords, uint32_t stride, uint32_t n,
                                                             const float* __restrict__ dxd, uint32_t kd, float* __restrict__ gtable) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float* c = coords + (size_t)i * stride;
+    constexpr uint32_t FULL = 0xffffffffu;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31u;
+    if ((i & ~31u) >= n) return;   // whole warps past the end leave; the rest stay for the shuffles
+    const bool valid = i < n;
+    const float* c = coords + (size_t)(valid ? i : 0) * stride;
     const V3 x = v3(c[0], c[1], c[2]);
-    const float* dg = dxd + (size_t)i * kd;
+    const float* dg = dxd + (size_t)(valid ? i : 0) * kd;
     for (uint32_t l = 0; l < fv.n_levels; ++l) {
-        const float g0 = dg[2 * l], g1 = dg[2 * l + 1];
-        if (g0 == 0.f && g1 == 0.f) continue;
+        const float g0 = valid ? dg[2 * l] : 0.f, g1 = valid ? dg[2 * l + 1] : 0.f;
         const float s = fv.level_scale[l];
         const float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);
         const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
         const float rx = __fsub_rn(px, fx), ry = __fsub_rn(py, fy), rz = __fsub_rn(pz, fz);
         const uint32_t gx = (uint32_t)(int32_t)fx, gy = (uint32_t)(int32_t)fy, gz = (uint32_t)(int32_t)fz;
         const uint32_t res = fv.level_res[l], size = fv.level_size[l];
-        float* lt = gtable + (size_t)fv.level_off[l] * 2;
+        float2* lt = reinterpret_cast<float2*>(gtable + (size_t)fv.level_off[l] * 2);
 #pragma unroll
         for (uint32_t cc = 0; cc < 8; ++cc) {
             const uint32_t bx = cc & 1u, by = (cc >> 1) & 1u, bz = (cc >> 2) & 1u;
@@ -105,7 +109,20 @@ __global__ void __launch_bounds__(256) hash_backward_kernel(FieldView fv, const 
             } else {
                 idx = ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
             }
-            atomicAdd(reinterpret_cast<float2*>(lt) + idx, make_float2(w * g0, w * g1));   // one 8-byte reduction per corner
+            if (!valid) idx = FULL;
+            float vx = w * g0, vy = w * g1;
+            const uint32_t prev = __shfl_up_sync(FULL, idx, 1), next = __shfl_down_sync(FULL, idx, 1);
+            const uint32_t heads = __ballot_sync(FULL, lane == 0 || prev != idx);
+            if (heads != FULL) {
+                // segmented inclusive scan: the run of this lane starts at the highest head at or below it
+                const uint32_t start = 31u - __clz(heads & (FULL >> (31u - lane)));
+#pragma unroll
+                for (uint32_t d = 1; d < 32; d <<= 1) {
+                    const float ox = __shfl_up_sync(FULL, vx, d), oy = __shfl_up_sync(FULL, vy, d);
+                    if (lane >= start + d) { vx += ox; vy += oy; }
+                }
+            }
+            if (valid && (lane == 31 || next != idx) && (vx != 0.f || vy != 0.f)) atomicAdd(lt + idx, make_float2(vx, vy));
         }
     }
 }
