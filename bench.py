@@ -598,6 +598,20 @@ def run_train(args):
             "march_samples_per_step": samples / args.steps,
             "trained_samples_per_s_device": cfg.target_batch_size / (dev_ms / 1e3),
             "rays_per_s_wall": n / wall}
+    if not args.no_cpu_baseline:
+        # the CPU restatement of the loss and the field backward on a bounded slice of one step
+        from oracle import oracle as O
+        torch.cuda.synchronize()
+        ctx.sync()
+        n_cpu = 4096
+        co = ts.coords_out[:n_cpu].cpu().numpy()
+        dl = ts.dloss[:n_cpu].cpu().numpy()
+        params = S.field_params(fc, seed=0)
+        t0 = time.perf_counter()
+        O.field_backward(fc, params, co, dl)
+        t_bwd = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_cpu / t_bwd, "unit": "trained samples/s", "cores": 1, "kind": "port",
+                                "sample": f"FP64 field forward+backward of {n_cpu} compacted samples of the step"}
     print(json.dumps(line), flush=True)
     ctx.close()
 
