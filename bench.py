@@ -594,6 +594,7 @@ def run_train(args):
     stage = {k: v / args.steps for k, v in st["stage_ms"].items() if v > 0}
     dev_ms = sum(stage.values())
     line = {"workload": "training step: 4096 rays, 2^18-sample batch, field with 16 expression dims",
+            "train_math": "TF32 tensor-core layer products, FP32 accumulation" if cfg.tf32 else "FP32",
             "ms_per_step_device": dev_ms, "ms_per_step_wall": wall * 1e3, "stage_ms_per_step": stage,
             "march_samples_per_step": samples / args.steps,
             "trained_samples_per_s_device": cfg.target_batch_size / (dev_ms / 1e3),

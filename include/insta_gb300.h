@@ -31,6 +31,7 @@
  *   insta_field_eval            NerfNetwork::inference_mixed_precision_impl (NGP/nerf_network.h:159-232)
  *   insta_field_backward        NerfNetwork's forward/backward for training (NGP/nerf_network.h:296-383)
  *   insta_adam_step             the Adam optimizer of the trainer (configs/nerf/main.json)
+ *   insta_train_set_math        FP32 or TF32 layer products of the backward
  *   insta_train_loss            compute_loss_kernel_train_nerf + fill_rollover (instant-ngp/src/
  *                               testbed_nerf.cu:1305-1644,3298-3362)
  *   insta_render                Testbed::render_nerf -> NerfTracer::init_rays_from_camera/trace +
@@ -270,6 +271,11 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
  * forward runs.  n < 2^24. */
 int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, const float* dl_dout, float* grad,
                          float* out4);
+/* Arithmetic of the backward's layer products: FP32 (default) or TF32 tensor-core GEMMs (inputs
+ * rounded to TF32, FP32 accumulation; still finer than the reference's FP16 training arithmetic). */
+#define INSTA_TRAIN_MATH_FP32 0
+#define INSTA_TRAIN_MATH_TF32 1
+int insta_train_set_math(insta_ctx* ctx, int math);
 /* Adam (configs/nerf/main.json nests it in an Ema): w -= lr * m_hat / (sqrt(v_hat) + eps) with
  * g + l2_reg * w, bias-corrected moments; the FP32 master weights and moments stay on the
  * device, the field's FP16 parameters and weight image are rewritten. */

@@ -24,7 +24,7 @@ EXPORTS = [
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_density_grid_load", "insta_density_grid_reset", "insta_density_grid_update", "insta_density_grid_read",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
-    "insta_field_eval", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_train_loss", "insta_render", "insta_render_async", "insta_render_batch",
+    "insta_field_eval", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_train_loss", "insta_train_set_math", "insta_render", "insta_render_async", "insta_render_batch",
     "insta_render_samples", "insta_march_debug", "insta_nearest_debug", "insta_raycast",
     "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
     "insta_server_release", "insta_server_error",
@@ -145,6 +145,7 @@ def load(path: Path | None = None):
             "insta_field_backward": [vp, C.c_int, vp, u32, i64, vp, vp, vp],
             "insta_adam_step": [vp, C.c_int, vp, C.POINTER(AdamConfig)],
             "insta_train_loss": [vp, C.POINTER(TrainLossDesc)],
+            "insta_train_set_math": [vp, C.c_int],
             "insta_render": [vp, C.POINTER(RenderDesc), vp, vp],
             "insta_render_async": [vp, C.POINTER(RenderDesc), vp, vp],
             "insta_render_batch": [vp, C.POINTER(RenderDesc), C.c_int, C.POINTER(vp), C.POINTER(vp)],
@@ -344,6 +345,10 @@ class Context:
     def field_backward(self, avatar, coords, stride, n, dl_dout=None, grad=None, out4=None):
         """insta_field_backward: ADDS d(sum dl_dout . out)/d(params) into grad (f32, snapshot order)."""
         self._check(self.lib.insta_field_backward(self.h, avatar, _addr(coords), stride, n, _addr(dl_dout), _addr(grad), _addr(out4)))
+
+    def train_set_math(self, tf32: bool):
+        """insta_train_set_math: TF32 tensor-core layer products in the backward (else FP32)."""
+        self._check(self.lib.insta_train_set_math(self.h, 1 if tf32 else 0))
 
     def adam_step(self, avatar, grad, learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6):
         cfg = AdamConfig(learning_rate, beta1, beta2, epsilon, l2_reg)

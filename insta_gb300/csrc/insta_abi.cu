@@ -131,6 +131,7 @@ struct insta_ctx {
     bool async_used[2] = {false, false};
     int async_next = 0;
     cublasHandle_t blas = nullptr;      // the training side's GEMMs
+    bool train_tf32 = false;            // insta_train_set_math: TF32 tensor-core GEMMs
     DevBuf train_scratch;
     DevBuf loss_scratch;     // insta_train_loss: each kept ray's block start before compaction
     bool keep_master = false;           // a parameter reload from the optimizer keeps the FP32 master weights
@@ -1527,13 +1528,26 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
         if (stride < 11 + fd.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
         if ((uintptr_t)grad & 7) fail(INSTA_ERR_INVALID_ARG, "grad must be 8-byte aligned");   // paired table atomics
         if (n == 0) return;
-        if (!ctx->blas && cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) fail(INSTA_ERR_CUDA, "cublasCreate failed");
+        if (!ctx->blas) {
+            if (cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) fail(INSTA_ERR_CUDA, "cublasCreate failed");
+            if (cublasSetMathMode(ctx->blas, ctx->train_tf32 ? CUBLAS_TF32_TENSOR_OP_MATH : CUBLAS_DEFAULT_MATH) != CUBLAS_STATUS_SUCCESS)
+                fail(INSTA_ERR_CUDA, "cublasSetMathMode failed");
+        }
         ensure_master(ctx, fd);
         const TrainShape t = train_shape(fd);
         ctx->alloc(ctx->train_scratch, train_scratch_floats(t, (uint32_t)n) * 4);
         Stage st(ctx, INSTA_STAGE_TRAIN, 8 + 2 * (t.n_density + t.n_rgb));
         CK(launch_field_train(ctx->blas, fd.view, t, (const float*)fd.w32.p, coords, stride, (uint32_t)n, dl_dout, out4, grad,
                               (float*)ctx->train_scratch.p, ctx->stream));
+    });
+}
+
+int insta_train_set_math(insta_ctx* ctx, int math) {
+    return guarded(ctx, [&] {
+        if (math != INSTA_TRAIN_MATH_FP32 && math != INSTA_TRAIN_MATH_TF32) fail(INSTA_ERR_INVALID_ARG, "unknown training math %d", math);
+        ctx->train_tf32 = math == INSTA_TRAIN_MATH_TF32;
+        if (ctx->blas && cublasSetMathMode(ctx->blas, ctx->train_tf32 ? CUBLAS_TF32_TENSOR_OP_MATH : CUBLAS_DEFAULT_MATH) != CUBLAS_STATUS_SUCCESS)
+            fail(INSTA_ERR_CUDA, "cublasSetMathMode failed");
     });
 }
 

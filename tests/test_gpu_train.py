@@ -75,6 +75,32 @@ def test_backward_matches_oracle(ctx, field, oracle):
     assert ((g[lay.table_offset:] != 0) <= touched_ref).all()
 
 
+def test_backward_tf32(ctx, field, oracle):
+    """insta_train_set_math(TF32): layer products on tensor cores with TF32 inputs (10-bit
+    mantissa, the reference trains in FP16) and FP32 accumulation: outputs within 5e-3 of the
+    largest, per-block gradient norms within 5e-2 of the FP64 oracle (a weight gradient sums
+    thousands of products of both signs, so TF32 input rounding shows at the percent level there:
+    2 % measured on the first layer)."""
+    fc, params, lay = field
+    n = 3000
+    c = coords(n, seed=11)
+    g_out = np.random.default_rng(12).normal(size=(n, 4)).astype(np.float32)
+    grad = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    ctx.train_set_math(True)
+    try:
+        ctx.field_backward(AVATAR, dev(c), c.shape[1], n, dev(g_out), grad, out)
+        ctx.sync()
+    finally:
+        ctx.train_set_math(False)
+    ref_g, ref_out = oracle.field_backward(fc, params, c, g_out)
+    assert np.abs(out.cpu().numpy() - ref_out).max() <= 5e-3 * np.abs(ref_out).max()
+    g = grad.cpu().numpy().astype(np.float64)
+    for lo, hi in blocks(lay):
+        a, b = g[lo:hi], ref_g[lo:hi]
+        assert np.linalg.norm(a - b) <= 5e-2 * np.linalg.norm(b), (lo, hi, np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
 def test_backward_accumulates_and_forward_only(ctx, field, oracle):
     fc, params, lay = field
     n = 700
@@ -274,8 +300,9 @@ def test_train_loss_cap_and_rollover(ctx, oracle):
 
 
 def test_train_step_fits_a_constant_colour(ctx, avatar, frame0):
-    """insta_gb300.train.TrainStep: training samples -> field evaluation -> loss -> backward ->
-    Adam, 80 steps towards an opaque constant-colour target, lowers the batch loss 4x."""
+    """insta_gb300.train.TrainStep (TF32 backward): training samples -> field evaluation -> loss
+    -> backward -> Adam, 80 steps towards an opaque constant-colour target, lowers the batch loss
+    4x."""
     from insta_gb300 import synthetic as S
     from insta_gb300.train import TrainConfig, TrainStep
     aid = 22
@@ -302,5 +329,6 @@ def test_train_step_fits_a_constant_colour(ctx, avatar, frame0):
         info = ts.step(0, rays, image, dev(rng.random(n).astype(np.float32)), target)
         kept.append(info["rays_kept"])
         losses.append(ts.loss_value())
+    ctx.train_set_math(False)
     assert min(kept) > n // 2
     assert np.isfinite(losses).all() and np.mean(losses[-5:]) < 0.25 * np.mean(losses[:5]), (losses[:5], losses[-5:])
