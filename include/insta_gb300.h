@@ -264,9 +264,8 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
  * for n NerfCoordinate records (canonical position, direction, expression dims; device
  * pointers) and the loss gradient w.r.t. each record's outputs dl_dout f32[n][4] (raw r, g, b,
  * raw density), ADD the gradient of every parameter to grad f32[n_params] (snapshot order:
- * density MLP, colour MLP, hash table; 8-byte aligned).  FP32 arithmetic; the MLP weights come
- * from the FP32 master copy (the FP16 parameters widened at the first call after
- * insta_params_load), the hash table from the FP16 parameters as the forward pass reads them.
+ * density MLP, colour MLP, hash table; 8-byte aligned).  FP32 arithmetic on the FP32 master
+ * weights (the FP16 parameters widened at the first call after insta_params_load).
  * out4 (optional) gets the outputs of that FP32 forward; with dl_dout = grad = NULL only the
  * forward runs.  n < 2^24. */
 int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, const float* dl_dout, float* grad,
@@ -278,9 +277,14 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
 int insta_train_set_math(insta_ctx* ctx, int math);
 /* Adam (configs/nerf/main.json nests it in an Ema): w -= lr * m_hat / (sqrt(v_hat) + eps) with
  * g + l2_reg * w, bias-corrected moments; the FP32 master weights and moments stay on the
- * device, the field's FP16 parameters and weight image are rewritten. */
+ * device, the field's FP16 parameters and weight image are rewritten.  ema_decay > 0 adds the
+ * Ema wrapper: a bias-corrected exponential average of the weights,
+ * e_t = (decay (1 - decay^(t-1)) e_(t-1) + (1 - decay) w_t) / (1 - decay^t), becomes the field's
+ * parameters (what rendering and insta_field_eval read), while the training forward of
+ * insta_field_backward keeps reading the raw master weights. */
 typedef struct insta_adam_config {
     float learning_rate, beta1, beta2, epsilon, l2_reg;
+    float ema_decay;   /* 0: no Ema; configs/nerf/main.json: 0.95 */
 } insta_adam_config;
 int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_adam_config* cfg);
 

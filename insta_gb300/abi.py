@@ -50,7 +50,7 @@ class DensityUpdateDesc(C.Structure):
 
 class AdamConfig(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
-                ("l2_reg", C.c_float)]
+                ("l2_reg", C.c_float), ("ema_decay", C.c_float)]
 
 
 LOSS_TYPES = {"l2": 0, "l1": 1, "mape": 2, "smape": 3, "huber": 4, "logl1": 5, "relativel2": 6}
@@ -350,8 +350,9 @@ class Context:
         """insta_train_set_math: TF32 tensor-core layer products in the backward (else FP32)."""
         self._check(self.lib.insta_train_set_math(self.h, 1 if tf32 else 0))
 
-    def adam_step(self, avatar, grad, learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6):
-        cfg = AdamConfig(learning_rate, beta1, beta2, epsilon, l2_reg)
+    def adam_step(self, avatar, grad, learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6, ema_decay=0.0):
+        """insta_adam_step; ema_decay > 0 adds the Ema wrapper (its average becomes the field's parameters)."""
+        cfg = AdamConfig(learning_rate, beta1, beta2, epsilon, l2_reg, ema_decay)
         self._check(self.lib.insta_adam_step(self.h, avatar, _addr(grad), C.byref(cfg)))
 
     _LOSS_PTRS = ("rays", "target", "background", "exposure", "depth", "seg_mask", "mean_density", "rays_counter", "ray_indices",

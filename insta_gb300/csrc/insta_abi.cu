@@ -73,9 +73,10 @@ struct Field {
     uint64_t n_params = 0;
     // training: FP32 master weights (from the FP16 parameters at the first backward after a
     // load), Adam moments, the optimizer's step count and its FP16 output
-    DevBuf w32, adam_m, adam_v, w16;
+    DevBuf w32, adam_m, adam_v, w16, ema;
     bool w32_valid = false;
     uint32_t adam_step = 0;
+    uint32_t ema_step = 0;   // steps averaged into `ema` (0: no running average yet)
 };
 
 // Device scratch of the render wavefront, sized for the largest request seen.
@@ -927,7 +928,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     for (auto& kv : ctx->avatars) {
         Avatar& a = *kv.second;
         for (DevBuf* b : {&a.faces, &a.mask, &a.adjacency, &a.canon_verts, &a.canon_area, &a.canon_frames, &a.frame_table,
-                          &a.field.params, &a.field.image, &a.density_grid, &a.field.w32, &a.field.adam_m, &a.field.adam_v, &a.field.w16})
+                          &a.field.params, &a.field.image, &a.density_grid, &a.field.w32, &a.field.adam_m, &a.field.adam_v, &a.field.w16, &a.field.ema})
             ctx->release(*b);
         for (auto& f : a.frames)
             for (DevBuf* b : {&f.second.verts, &f.second.frames, &f.second.leaf_tris, &f.second.nodes, &f.second.bitfield})
@@ -1377,6 +1378,7 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
         if (!ctx->keep_master) {
             fd.w32_valid = false;
             fd.adam_step = 0;
+            fd.ema_step = 0;
         }
         ctx->alloc(fd.params, n_params * 2);
         host_copy(fd.params.p, params, n_params * 2, ctx->stream);
@@ -1564,12 +1566,22 @@ int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_a
             CK(cudaMemsetAsync(fd.adam_m.p, 0, fd.n_params * 4, ctx->stream));
             CK(cudaMemsetAsync(fd.adam_v.p, 0, fd.n_params * 4, ctx->stream));
         }
+        if (!(cfg->ema_decay >= 0.f && cfg->ema_decay < 1.f)) fail(INSTA_ERR_INVALID_ARG, "ema_decay must be in [0, 1)");
         ctx->alloc(fd.w16, fd.n_params * 2);
         const uint32_t step = ++fd.adam_step;
+        float* ema = nullptr;
+        if (cfg->ema_decay > 0.f) {
+            ctx->alloc(fd.ema, fd.n_params * 4);
+            ema = (float*)fd.ema.p;
+            ++fd.ema_step;
+        } else {
+            fd.ema_step = 0;   // a step without the Ema restarts its average
+        }
         {
             Stage st(ctx, INSTA_STAGE_TRAIN, 1);
             CK(launch_adam(fd.n_params, (float*)fd.w32.p, (float*)fd.adam_m.p, (float*)fd.adam_v.p, grad, cfg->learning_rate, cfg->beta1,
-                           cfg->beta2, cfg->epsilon, cfg->l2_reg, step, (__half*)fd.w16.p, ctx->stream));
+                           cfg->beta2, cfg->epsilon, cfg->l2_reg, step, ema, cfg->ema_decay, fd.ema_step, (__half*)fd.w16.p,
+                           ctx->stream));
         }
         // the new FP16 parameters: the field's buffer and weight image (the master stays FP32)
         const insta_field_desc desc = fd.desc;

@@ -8,9 +8,9 @@
 //   backward   dX = W^T dY, then the ReLU mask of the layer's input
 //   weights    dW += dY X^T
 // The hash encode and its backward (scatter-add of each corner's weighted gradient into the
-// table, FP32 atomics) and the elementwise steps are kernels here.  Values are FP32 from the
-// FP16 parameters; the forward is that of the field evaluation in FP32 (no FP16 rounding between
-// layers).
+// table, FP32 atomics) and the elementwise steps are kernels here.  Values are FP32 from the FP32
+// master weights (the FP16 parameters at first); the forward is that of the field evaluation in
+// FP32 (no FP16 rounding between layers).
 #include <cublas_v2.h>
 
 #include "../../include/insta_gb300.h"
@@ -19,19 +19,51 @@
 
 namespace insta {
 
+// One level of the hash encoding from the FP32 master table ([entries][2] floats), the same
+// index arithmetic and summation order as hash_level.
+__device__ __forceinline__ void hash_level_f32(const FieldView& fv, const float2* __restrict__ table, V3 x, uint32_t l, float& a0, float& a1) {
+    const float s = fv.level_scale[l];
+    const float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);
+    const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+    const float rx = __fsub_rn(px, fx), ry = __fsub_rn(py, fy), rz = __fsub_rn(pz, fz);
+    const uint32_t gx = (uint32_t)(int32_t)fx, gy = (uint32_t)(int32_t)fy, gz = (uint32_t)(int32_t)fz;
+    const uint32_t res = fv.level_res[l], size = fv.level_size[l];
+    const float2* lt = table + fv.level_off[l];
+    a0 = 0.f;
+    a1 = 0.f;
+#pragma unroll
+    for (uint32_t c = 0; c < 8; ++c) {
+        const uint32_t bx = c & 1u, by = (c >> 1) & 1u, bz = (c >> 2) & 1u;
+        float w = bx ? rx : __fsub_rn(1.f, rx);
+        w = __fmul_rn(w, by ? ry : __fsub_rn(1.f, ry));
+        w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
+        const uint32_t cx = gx + bx, cy = gy + by, cz = gz + bz;
+        uint32_t idx;
+        if (fv.level_dense[l]) {
+            idx = cx + cy * res + cz * res * res;
+            if (idx >= size) idx %= size;
+        } else {
+            idx = ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
+        }
+        const float2 e = __ldg(lt + idx);
+        a0 = __fadd_rn(a0, __fmul_rn(w, e.x));
+        a1 = __fadd_rn(a1, __fmul_rn(w, e.y));
+    }
+}
+
 // Encode: X_d[:, 0:32] = hash encoding, X_d[:, 32:32+n_extra] = the record's expression dims,
 // X_r[:, 16:32] = SH of the direction (X_r[:, 0:16] is filled by the density MLP's output).
-__global__ void __launch_bounds__(256) train_encode_kernel(FieldView fv, const float* __restrict__ coords, uint32_t stride, uint32_t n,
-                                                           float* __restrict__ xd, uint32_t kd, float* __restrict__ xr) {
+__global__ void __launch_bounds__(256) train_encode_kernel(FieldView fv, const float2* __restrict__ table32, const float* __restrict__ coords,
+                                                           uint32_t stride, uint32_t n, float* __restrict__ xd, uint32_t kd,
+                                                           float* __restrict__ xr) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* c = coords + (size_t)i * stride;
-    const __half2* table = reinterpret_cast<const __half2*>(fv.table);
     const V3 p = v3(c[0], c[1], c[2]);
     float* x = xd + (size_t)i * kd;
     for (uint32_t l = 0; l < fv.n_levels; ++l) {
         float a0, a1;
-        hash_level(fv, table, p, l, a0, a1);
+        hash_level_f32(fv, table32, p, l, a0, a1);
         x[2 * l] = a0;
         x[2 * l + 1] = a1;
     }
@@ -129,10 +161,13 @@ __global__ void __launch_bounds__(256) hash_backward_kernel(FieldView fv, const 
 
 // Adam (the optimizer the INSTA configuration nests in its Ema, configs/nerf/main.json): FP32
 // master weights, first and second moments, L2 regularisation added to the gradient, bias
-// correction; the FP16 parameters are written back.
+// correction.  With an Ema (ema != nullptr) the bias-corrected running average of the weights
+// (e_old scaled by decay * debias_old, plus (1 - decay) w, over debias_new) is kept in FP32 and
+// written as the FP16 parameters; without one the weights themselves are.
 __global__ void __launch_bounds__(256) adam_kernel(size_t n, float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                                                    const float* __restrict__ g, float lr, float b1, float b2, float eps, float l2,
-                                                   float c1, float c2, __half* __restrict__ w16) {
+                                                   float c1, float c2, float* __restrict__ ema, float decay, float debias_old,
+                                                   float debias_new, __half* __restrict__ w16) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const float gi = g[i] + l2 * w[i];
         const float mi = b1 * m[i] + (1.f - b1) * gi;
@@ -141,7 +176,13 @@ __global__ void __launch_bounds__(256) adam_kernel(size_t n, float* __restrict__
         v[i] = vi;
         const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
         w[i] = wi;
-        w16[i] = __float2half_rn(wi);
+        float out = wi;
+        if (ema) {
+            // the first averaged step is the weights themselves (debias_old = 0)
+            if (debias_old > 0.f) out = (ema[i] * (decay * debias_old) + (1.f - decay) * wi) / debias_new;
+            ema[i] = out;
+        }
+        w16[i] = __float2half_rn(out);
     }
 }
 
@@ -414,7 +455,8 @@ cudaError_t launch_field_train(cublasHandle_t h, const FieldView& fv, const Trai
     for (int l = 0; l + 1 < t.n_rgb; ++l) { dhr[l] = p; p += (size_t)64 * n; }
     float* dyr = p; p += (size_t)16 * n;
 
-    train_encode_kernel<<<(n + 255) / 256, 256, 0, s>>>(fv, coords, stride, n, xd, t.kd, xr);
+    train_encode_kernel<<<(n + 255) / 256, 256, 0, s>>>(fv, reinterpret_cast<const float2*>(w32 + t.table_off), coords, stride, n, xd, t.kd,
+                                                        xr);
     bool okb = true;
     // density MLP: hidden layers then the 16 outputs into X_r rows 0..15
     const float* in = xd;
@@ -472,9 +514,10 @@ cudaError_t launch_field_train(cublasHandle_t h, const FieldView& fv, const Trai
 }
 
 cudaError_t launch_adam(size_t n, float* w, float* m, float* v, const float* g, float lr, float b1, float b2, float eps, float l2,
-                        uint32_t step, __half* w16, cudaStream_t s) {
+                        uint32_t step, float* ema, float decay, uint32_t ema_step, __half* w16, cudaStream_t s) {
     const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
-    adam_kernel<<<grid_for(n), 256, 0, s>>>(n, w, m, v, g, lr, b1, b2, eps, l2, c1, c2, w16);
+    const float debias_old = 1.f - powf(decay, (float)(ema_step - 1u)), debias_new = 1.f - powf(decay, (float)ema_step);
+    adam_kernel<<<grid_for(n), 256, 0, s>>>(n, w, m, v, g, lr, b1, b2, eps, l2, c1, c2, ema, decay, debias_old, debias_new, w16);
     return cudaGetLastError();
 }
 

@@ -3,6 +3,8 @@
 
     insta_training_samples   generate_training_samples_nerf + surface_closest_point (:3252-3293)
     insta_field_eval         inference_mixed_precision on the uncompacted records   (:3295)
+                             (with the Ema: the FP32 forward of insta_field_backward,
+                             the training weights rather than the averaged ones)
     insta_train_loss         compute_loss_kernel_train_nerf + fill_rollover          (:3298-3357)
     insta_field_backward     forward + backward on the compacted batch, gradients
                              overwritten (EGradientMode::Overwrite)                  (:3364-3368)
@@ -13,8 +15,9 @@ the way the reference's sampler does (device tensors, complete on torch's curren
 step() is called; the context runs on its own stream and step() orders torch's work before
 it).  Each step reads the two sample counters back to the host (the reference reads its
 counters back too, one step later), so that the field evaluation covers exactly the records
-the march wrote.  Not built: the Ema wrapper of the optimizer, error-map importance sampling,
-camera / exposure / extra-dims optimisation.
+the march wrote.  The optimizer is Adam in the configuration's Ema wrapper (decay 0.95): the
+field renders with the averaged weights.  Not built: error-map importance sampling, camera /
+exposure / extra-dims optimisation.
 """
 from __future__ import annotations
 
@@ -28,7 +31,7 @@ from . import layout as _layout
 
 @dataclass
 class TrainConfig:
-    """configs/nerf/main.json-style settings (loss Huber, Adam 1.75e-3, beta 0.9/0.99)."""
+    """configs/nerf/main.json-style settings (loss Huber, Ema(0.95) of Adam 1.75e-3, beta 0.9/0.99)."""
     n_rays_per_batch: int = 4096
     target_batch_size: int = 1 << 18
     max_samples: int = 1 << 20
@@ -46,7 +49,8 @@ class TrainConfig:
     aabb_min: tuple = (0.0, 0.0, 0.0)
     aabb_max: tuple = (1.0, 1.0, 1.0)
     tf32: bool = True                  # TF32 tensor-core layer products in the backward
-    adam: dict = field(default_factory=lambda: dict(learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6))
+    adam: dict = field(default_factory=lambda: dict(learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6,
+                                                    ema_decay=0.95))
 
 
 class TrainStep:
@@ -98,7 +102,13 @@ class TrainStep:
         n_kept, n_samples = (int(x) for x in self.counters_host.numpy().view(np.uint32))
         n_samples = min(n_samples, cfg.max_samples)
         if n_samples > 0:
-            ctx.field_eval(self.avatar, self.coords, self.stride, n_samples, self.out)
+            # the loss reads the training weights (inference_mixed_precision with
+            # use_inference_params = false): with an Ema those are the FP32 masters, not the field's
+            # averaged parameters; without one the field's FP16 parameters are the same weights
+            if cfg.adam.get("ema_decay", 0.0) > 0.0:
+                ctx.field_backward(self.avatar, self.coords, self.stride, n_samples, None, None, self.out)
+            else:
+                ctx.field_eval(self.avatar, self.coords, self.stride, n_samples, self.out)
         ctx.train_loss(n_rays=n, max_rays=n, max_samples_compacted=cfg.target_batch_size,
                        target_batch_size=cfg.target_batch_size, aabb_min=cfg.aabb_min, aabb_max=cfg.aabb_max,
                        loss_type=cfg.loss_type, depth_loss_type=cfg.depth_loss_type, srgb_targets=int(cfg.srgb_targets),

@@ -160,6 +160,50 @@ def test_adam_matches_numpy(ctx, field, oracle):
     assert (err <= 4e-3 + 1e-2 * np.abs(ref)).all(), float(err.max())
 
 
+def test_adam_ema_matches_numpy(ctx, field, oracle):
+    """Adam inside the Ema wrapper (decay 0.95, 3 steps): the field's parameters -- what
+    insta_field_eval and rendering read -- are the bias-corrected average of the weights, within the
+    field parity tolerance of the oracle on a NumPy FP32 Adam + Ema; the training forward keeps
+    the raw weights (FP16-rounded for the oracle, hence the same tolerance)."""
+    fc, params, lay = field
+    n = 2000
+    c = coords(n, seed=13)
+    g_out = np.random.default_rng(14).normal(size=(n, 4)).astype(np.float32)
+    grad = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    ctx.field_backward(AVATAR, dev(c), 27, n, dev(g_out), grad)
+    cfg = dict(learning_rate=1e-2, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6)
+    decay = 0.95
+    for _ in range(3):
+        ctx.adam_step(AVATAR, grad, ema_decay=decay, **cfg)
+    cq = coords(1500, seed=15)
+    inf_out = torch.zeros((len(cq), 4), dtype=torch.float32, device="cuda")
+    train_out = torch.zeros((len(cq), 4), dtype=torch.float32, device="cuda")
+    dq = dev(cq)
+    ctx.field_eval(AVATAR, dq, 27, len(cq), inf_out)
+    ctx.field_backward(AVATAR, dq, 27, len(cq), None, None, train_out)
+    ctx.sync()
+    g = grad.cpu().numpy()
+    w = params.astype(np.float32)
+    m = np.zeros_like(w)
+    v = np.zeros_like(w)
+    e = None
+    for t in range(1, 4):
+        gi = g + np.float32(cfg["l2_reg"]) * w
+        m = np.float32(0.9) * m + np.float32(0.1) * gi
+        v = np.float32(0.99) * v + np.float32(0.01) * gi * gi
+        w = w - np.float32(1e-2) * (m / np.float32(1 - 0.9 ** t)) / (np.sqrt(v / np.float32(1 - 0.99 ** t)) + np.float32(1e-15))
+        if e is None:
+            e = w.copy()
+        else:
+            e = (e * np.float32(decay * (1 - decay ** (t - 1))) + np.float32(1 - decay) * w) / np.float32(1 - decay ** t)
+    ref_inf = oracle.field_eval(fc, e.astype(np.float16), cq)
+    ref_train = oracle.field_eval(fc, w.astype(np.float16), cq)
+    got_inf, got_train = inf_out.cpu().numpy(), train_out.cpu().numpy()
+    assert np.abs(ref_inf - ref_train).max() > 0.02                     # the average differs from the weights
+    assert (np.abs(got_inf - ref_inf) <= 4e-3 + 1e-2 * np.abs(ref_inf)).all(), float(np.abs(got_inf - ref_inf).max())
+    assert (np.abs(got_train - ref_train) <= 4e-3 + 1e-2 * np.abs(ref_train)).all(), float(np.abs(got_train - ref_train).max())
+
+
 def test_regression_loss_decreases(ctx, field):
     """A few hundred Adam steps fitting fixed targets with an L2 loss: the backward's sign and
     scale, and the optimizer state across steps, together reduce the loss by 10x."""
