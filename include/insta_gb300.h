@@ -29,6 +29,7 @@
  *   insta_params_load           Testbed::load_snapshot parameter blob, NerfNetwork::set_params
  *                               order (instant-ngp/src/testbed.cu:2952-3016; NGP/nerf_network.h:492-525)
  *   insta_field_eval            NerfNetwork::inference_mixed_precision_impl (NGP/nerf_network.h:159-232)
+ *   insta_field_eval_training   the same with the training weights (use_inference_params = false)
  *   insta_field_backward        NerfNetwork's forward/backward for training (NGP/nerf_network.h:296-383)
  *   insta_adam_step             the Adam optimizer of the trainer (configs/nerf/main.json)
  *   insta_train_set_math        FP32 or TF32 layer products of the backward
@@ -247,6 +248,10 @@ int insta_field_param_count(const insta_field_desc* desc, uint64_t* n_params);
 int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, const uint16_t* params, uint64_t n_params);
 /* out4[n][4] = (r, g, b, raw density) network outputs (device pointers). */
 int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4);
+/* The same evaluation with the training weights (inference_mixed_precision with
+ * use_inference_params = false, ngp/src/testbed_nerf.cu:3295): differs from insta_field_eval only
+ * while insta_adam_step runs with an Ema, whose average is then the field's parameters. */
+int insta_field_eval_training(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4);
 
 /* Same result as insta_field_eval, but the call allocates no device memory.  No counterpart
  * in the reference: it exists for callers that must not allocate on the hot path -- code that

@@ -24,7 +24,7 @@ EXPORTS = [
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_density_grid_load", "insta_density_grid_reset", "insta_density_grid_update", "insta_density_grid_read",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
-    "insta_field_eval", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_train_loss", "insta_train_set_math", "insta_render", "insta_render_async", "insta_render_batch",
+    "insta_field_eval", "insta_field_eval_training", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_train_loss", "insta_train_set_math", "insta_render", "insta_render_async", "insta_render_batch",
     "insta_render_samples", "insta_march_debug", "insta_nearest_debug", "insta_raycast",
     "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
     "insta_server_release", "insta_server_error",
@@ -142,6 +142,7 @@ def load(path: Path | None = None):
             "insta_params_load": [vp, C.c_int, C.POINTER(FieldDesc), vp, u64],
             "insta_field_eval": [vp, C.c_int, vp, u32, i64, vp],
             "insta_field_eval_static": [vp, C.c_int, vp, u32, i64, vp],
+            "insta_field_eval_training": [vp, C.c_int, vp, u32, i64, vp],
             "insta_field_backward": [vp, C.c_int, vp, u32, i64, vp, vp, vp],
             "insta_adam_step": [vp, C.c_int, vp, C.POINTER(AdamConfig)],
             "insta_train_loss": [vp, C.POINTER(TrainLossDesc)],
@@ -337,6 +338,10 @@ class Context:
 
     def field_eval(self, avatar, coords, stride, n, out4):
         self._check(self.lib.insta_field_eval(self.h, avatar, _addr(coords), stride, n, _addr(out4)))
+
+    def field_eval_training(self, avatar, coords, stride, n, out4):
+        """insta_field_eval_training: the training weights (differ from field_eval under an Ema)."""
+        self._check(self.lib.insta_field_eval_training(self.h, avatar, _addr(coords), stride, n, _addr(out4)))
 
     def field_eval_static(self, avatar, coords, stride, n, out4):
         """insta_field_eval without device allocations (n <= 16384, shared fixed scratch)."""

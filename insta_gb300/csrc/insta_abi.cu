@@ -74,6 +74,11 @@ struct Field {
     // training: FP32 master weights (from the FP16 parameters at the first backward after a
     // load), Adam moments, the optimizer's step count and its FP16 output
     DevBuf w32, adam_m, adam_v, w16, ema;
+    // with an Ema the field's parameters are the average; the training weights' own FP16 copy,
+    // weight image and view serve insta_field_eval_training
+    DevBuf train_params, train_image, w16_train;
+    FieldView train_view{};
+    bool train_valid = false;
     bool w32_valid = false;
     uint32_t adam_step = 0;
     uint32_t ema_step = 0;   // steps averaged into `ema` (0: no running average yet)
@@ -928,7 +933,8 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     for (auto& kv : ctx->avatars) {
         Avatar& a = *kv.second;
         for (DevBuf* b : {&a.faces, &a.mask, &a.adjacency, &a.canon_verts, &a.canon_area, &a.canon_frames, &a.frame_table,
-                          &a.field.params, &a.field.image, &a.density_grid, &a.field.w32, &a.field.adam_m, &a.field.adam_v, &a.field.w16, &a.field.ema})
+                          &a.field.params, &a.field.image, &a.density_grid, &a.field.w32, &a.field.adam_m, &a.field.adam_v, &a.field.w16, &a.field.ema, &a.field.train_params,
+                          &a.field.train_image, &a.field.w16_train})
             ctx->release(*b);
         for (auto& f : a.frames)
             for (DevBuf* b : {&f.second.verts, &f.second.frames, &f.second.leaf_tris, &f.second.nodes, &f.second.bitfield})
@@ -1379,6 +1385,7 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
             fd.w32_valid = false;
             fd.adam_step = 0;
             fd.ema_step = 0;
+            fd.train_valid = false;
         }
         ctx->alloc(fd.params, n_params * 2);
         host_copy(fd.params.p, params, n_params * 2, ctx->stream);
@@ -1474,10 +1481,10 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
     });
 }
 
-int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4) {
-    return guarded(ctx, [&] {
-        Avatar& a = ctx->avatar(avatar);
-        if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", avatar);
+namespace {
+void field_eval_view(insta_ctx* ctx, Avatar& a, const FieldView& fv, const float* coords, uint32_t stride, int64_t n, float* out4) {
+    {
+        if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar has no field parameters");
         if (n < 0 || (n > 0 && (!coords || !out4))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
         if (stride < 11 + a.field.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
         if (n == 0) return;
@@ -1489,12 +1496,27 @@ int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t s
         ctx->alloc(w.out_f32, tiles * 128 * sizeof(float4));
         CK(cudaMemsetAsync(w.tiles.p, 0, tiles * P.tile_bytes, ctx->stream));
         Stage st(ctx, INSTA_STAGE_FIELD, 3);
-        CK(launch_encode_coords(a.field.view, coords, stride, n, (uint8_t*)w.tiles.p, P.tile_bytes, P.k_in, ctx->stream));
+        CK(launch_encode_coords(fv, coords, stride, n, (uint8_t*)w.tiles.p, P.tile_bytes, P.k_in, ctx->stream));
         MlpArgs m{};
-        m.fv = a.field.view; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.n_samples = n;
+        m.fv = fv; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.n_samples = n;
         m.out = (uint2*)w.out.p; m.out_f32 = (float4*)w.out_f32.p; m.err = ctx->err_dev;
         CK(launch_mlp(m, (uint32_t)tiles, ctx->stream));
-        CK(launch_unpack((const uint2*)w.out.p, (const float4*)w.out_f32.p, a.field.view.precision != 0, n, (float4*)out4, ctx->stream));
+        CK(launch_unpack((const uint2*)w.out.p, (const float4*)w.out_f32.p, fv.precision != 0, n, (float4*)out4, ctx->stream));
+    }
+}
+}  // namespace
+
+int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4) {
+    return guarded(ctx, [&] {
+        Avatar& a = ctx->avatar(avatar);
+        field_eval_view(ctx, a, a.field.view, coords, stride, n, out4);
+    });
+}
+
+int insta_field_eval_training(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4) {
+    return guarded(ctx, [&] {
+        Avatar& a = ctx->avatar(avatar);
+        field_eval_view(ctx, a, a.field.train_valid ? a.field.train_view : a.field.view, coords, stride, n, out4);
     });
 }
 
@@ -1577,11 +1599,26 @@ int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_a
         } else {
             fd.ema_step = 0;   // a step without the Ema restarts its average
         }
+        if (ema) ctx->alloc(fd.w16_train, fd.n_params * 2);
         {
             Stage st(ctx, INSTA_STAGE_TRAIN, 1);
             CK(launch_adam(fd.n_params, (float*)fd.w32.p, (float*)fd.adam_m.p, (float*)fd.adam_v.p, grad, cfg->learning_rate, cfg->beta1,
                            cfg->beta2, cfg->epsilon, cfg->l2_reg, step, ema, cfg->ema_decay, fd.ema_step, (__half*)fd.w16.p,
-                           ctx->stream));
+                           ema ? (__half*)fd.w16_train.p : nullptr, ctx->stream));
+        }
+        if (ema) {
+            // the training weights' parameters and image: loaded like any parameters, then moved aside
+            const insta_field_desc d0 = fd.desc;
+            ctx->keep_master = true;
+            const int rc0 = insta_params_load(ctx, avatar, &d0, (const uint16_t*)fd.w16_train.p, fd.n_params);
+            ctx->keep_master = false;
+            if (rc0 != INSTA_OK) fail(rc0, "%s", ctx->last_error.c_str());
+            std::swap(fd.params, fd.train_params);
+            std::swap(fd.image, fd.train_image);
+            fd.train_view = fd.view;
+            fd.train_valid = true;
+        } else {
+            fd.train_valid = false;
         }
         // the new FP16 parameters: the field's buffer and weight image (the master stays FP32)
         const insta_field_desc desc = fd.desc;

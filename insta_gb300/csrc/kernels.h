@@ -198,7 +198,7 @@ cudaError_t launch_field_train(struct cublasContext* h, const FieldView& fv, con
                                uint32_t stride, uint32_t n, const float* dl_dout, float* out4, float* grad, float* scratch,
                                cudaStream_t s);
 cudaError_t launch_adam(size_t n, float* w, float* m, float* v, const float* g, float lr, float b1, float b2, float eps, float l2,
-                        uint32_t step, float* ema, float decay, uint32_t ema_step, __half* w16, cudaStream_t s);
+                        uint32_t step, float* ema, float decay, uint32_t ema_step, __half* w16, __half* w16_train, cudaStream_t s);
 cudaError_t launch_half_to_float(size_t n, const void* a, float* b, cudaStream_t s);
 cudaError_t launch_train_loss(const ::insta_train_loss_desc& d, uint32_t* base_scratch, cudaStream_t s);
 cudaError_t launch_raycast(const RenderView& rv, const FrameView& fr, const float* center, int color_normal, float* out_rgba,

@@ -163,11 +163,12 @@ __global__ void __launch_bounds__(256) hash_backward_kernel(FieldView fv, const 
 // master weights, first and second moments, L2 regularisation added to the gradient, bias
 // correction.  With an Ema (ema != nullptr) the bias-corrected running average of the weights
 // (e_old scaled by decay * debias_old, plus (1 - decay) w, over debias_new) is kept in FP32 and
-// written as the FP16 parameters; without one the weights themselves are.
+// written as the FP16 parameters (the weights themselves to w16_train); without one the weights
+// themselves are the FP16 parameters.
 __global__ void __launch_bounds__(256) adam_kernel(size_t n, float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                                                    const float* __restrict__ g, float lr, float b1, float b2, float eps, float l2,
                                                    float c1, float c2, float* __restrict__ ema, float decay, float debias_old,
-                                                   float debias_new, __half* __restrict__ w16) {
+                                                   float debias_new, __half* __restrict__ w16, __half* __restrict__ w16_train) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const float gi = g[i] + l2 * w[i];
         const float mi = b1 * m[i] + (1.f - b1) * gi;
@@ -183,6 +184,7 @@ __global__ void __launch_bounds__(256) adam_kernel(size_t n, float* __restrict__
             ema[i] = out;
         }
         w16[i] = __float2half_rn(out);
+        if (w16_train) w16_train[i] = __float2half_rn(wi);
     }
 }
 
@@ -514,10 +516,10 @@ cudaError_t launch_field_train(cublasHandle_t h, const FieldView& fv, const Trai
 }
 
 cudaError_t launch_adam(size_t n, float* w, float* m, float* v, const float* g, float lr, float b1, float b2, float eps, float l2,
-                        uint32_t step, float* ema, float decay, uint32_t ema_step, __half* w16, cudaStream_t s) {
+                        uint32_t step, float* ema, float decay, uint32_t ema_step, __half* w16, __half* w16_train, cudaStream_t s) {
     const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
     const float debias_old = 1.f - powf(decay, (float)(ema_step - 1u)), debias_new = 1.f - powf(decay, (float)ema_step);
-    adam_kernel<<<grid_for(n), 256, 0, s>>>(n, w, m, v, g, lr, b1, b2, eps, l2, c1, c2, ema, decay, debias_old, debias_new, w16);
+    adam_kernel<<<grid_for(n), 256, 0, s>>>(n, w, m, v, g, lr, b1, b2, eps, l2, c1, c2, ema, decay, debias_old, debias_new, w16, w16_train);
     return cudaGetLastError();
 }
 

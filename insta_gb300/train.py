@@ -2,9 +2,8 @@
 (instant-ngp/src/testbed_nerf.cu:3170-3380) as INSTA runs it.
 
     insta_training_samples   generate_training_samples_nerf + surface_closest_point (:3252-3293)
-    insta_field_eval         inference_mixed_precision on the uncompacted records   (:3295)
-                             (with the Ema: the FP32 forward of insta_field_backward,
-                             the training weights rather than the averaged ones)
+    insta_field_eval_training  inference_mixed_precision on the uncompacted records with the
+                             training weights (not the Ema's average)                 (:3295)
     insta_train_loss         compute_loss_kernel_train_nerf + fill_rollover          (:3298-3357)
     insta_field_backward     forward + backward on the compacted batch, gradients
                              overwritten (EGradientMode::Overwrite)                  (:3364-3368)
@@ -103,12 +102,8 @@ class TrainStep:
         n_samples = min(n_samples, cfg.max_samples)
         if n_samples > 0:
             # the loss reads the training weights (inference_mixed_precision with
-            # use_inference_params = false): with an Ema those are the FP32 masters, not the field's
-            # averaged parameters; without one the field's FP16 parameters are the same weights
-            if cfg.adam.get("ema_decay", 0.0) > 0.0:
-                ctx.field_backward(self.avatar, self.coords, self.stride, n_samples, None, None, self.out)
-            else:
-                ctx.field_eval(self.avatar, self.coords, self.stride, n_samples, self.out)
+            # use_inference_params = false), not the Ema's average
+            ctx.field_eval_training(self.avatar, self.coords, self.stride, n_samples, self.out)
         ctx.train_loss(n_rays=n, max_rays=n, max_samples_compacted=cfg.target_batch_size,
                        target_batch_size=cfg.target_batch_size, aabb_min=cfg.aabb_min, aabb_max=cfg.aabb_max,
                        loss_type=cfg.loss_type, depth_loss_type=cfg.depth_loss_type, srgb_targets=int(cfg.srgb_targets),

@@ -179,8 +179,10 @@ def test_adam_ema_matches_numpy(ctx, field, oracle):
     inf_out = torch.zeros((len(cq), 4), dtype=torch.float32, device="cuda")
     train_out = torch.zeros((len(cq), 4), dtype=torch.float32, device="cuda")
     dq = dev(cq)
+    tc_out = torch.zeros((len(cq), 4), dtype=torch.float32, device="cuda")
     ctx.field_eval(AVATAR, dq, 27, len(cq), inf_out)
     ctx.field_backward(AVATAR, dq, 27, len(cq), None, None, train_out)
+    ctx.field_eval_training(AVATAR, dq, 27, len(cq), tc_out)
     ctx.sync()
     g = grad.cpu().numpy()
     w = params.astype(np.float32)
@@ -202,6 +204,8 @@ def test_adam_ema_matches_numpy(ctx, field, oracle):
     assert np.abs(ref_inf - ref_train).max() > 0.02                     # the average differs from the weights
     assert (np.abs(got_inf - ref_inf) <= 4e-3 + 1e-2 * np.abs(ref_inf)).all(), float(np.abs(got_inf - ref_inf).max())
     assert (np.abs(got_train - ref_train) <= 4e-3 + 1e-2 * np.abs(ref_train)).all(), float(np.abs(got_train - ref_train).max())
+    got_tc = tc_out.cpu().numpy()   # the tensor-core evaluation of the training weights' FP16 copy
+    assert (np.abs(got_tc - ref_train) <= 4e-3 + 1e-2 * np.abs(ref_train)).all(), float(np.abs(got_tc - ref_train).max())
 
 
 def test_regression_loss_decreases(ctx, field):
