@@ -1482,41 +1482,40 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
 }
 
 namespace {
-void field_eval_view(insta_ctx* ctx, Avatar& a, const FieldView& fv, const float* coords, uint32_t stride, int64_t n, float* out4) {
-    {
-        if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar has no field parameters");
-        if (n < 0 || (n > 0 && (!coords || !out4))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
-        if (stride < 11 + a.field.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
-        if (n == 0) return;
-        const TilePlan& P = a.field.plan;
-        const uint64_t tiles = ((uint64_t)n + 127) / 128;
-        Wave& w = ctx->wave;
-        ctx->alloc(w.tiles, tiles * P.tile_bytes);
-        ctx->alloc(w.out, tiles * 128 * sizeof(uint2));
-        ctx->alloc(w.out_f32, tiles * 128 * sizeof(float4));
-        CK(cudaMemsetAsync(w.tiles.p, 0, tiles * P.tile_bytes, ctx->stream));
-        Stage st(ctx, INSTA_STAGE_FIELD, 3);
-        CK(launch_encode_coords(fv, coords, stride, n, (uint8_t*)w.tiles.p, P.tile_bytes, P.k_in, ctx->stream));
-        MlpArgs m{};
-        m.fv = fv; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.n_samples = n;
-        m.out = (uint2*)w.out.p; m.out_f32 = (float4*)w.out_f32.p; m.err = ctx->err_dev;
-        CK(launch_mlp(m, (uint32_t)tiles, ctx->stream));
-        CK(launch_unpack((const uint2*)w.out.p, (const float4*)w.out_f32.p, fv.precision != 0, n, (float4*)out4, ctx->stream));
-    }
+void field_eval_view(insta_ctx* ctx, int avatar, Avatar& a, const FieldView& fv, const float* coords, uint32_t stride, int64_t n,
+                     float* out4) {
+    if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", avatar);
+    if (n < 0 || (n > 0 && (!coords || !out4))) fail(INSTA_ERR_INVALID_ARG, "bad buffers");
+    if (stride < 11 + a.field.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
+    if (n == 0) return;
+    const TilePlan& P = a.field.plan;
+    const uint64_t tiles = ((uint64_t)n + 127) / 128;
+    Wave& w = ctx->wave;
+    ctx->alloc(w.tiles, tiles * P.tile_bytes);
+    ctx->alloc(w.out, tiles * 128 * sizeof(uint2));
+    ctx->alloc(w.out_f32, tiles * 128 * sizeof(float4));
+    CK(cudaMemsetAsync(w.tiles.p, 0, tiles * P.tile_bytes, ctx->stream));
+    Stage st(ctx, INSTA_STAGE_FIELD, 3);
+    CK(launch_encode_coords(fv, coords, stride, n, (uint8_t*)w.tiles.p, P.tile_bytes, P.k_in, ctx->stream));
+    MlpArgs m{};
+    m.fv = fv; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.n_samples = n;
+    m.out = (uint2*)w.out.p; m.out_f32 = (float4*)w.out_f32.p; m.err = ctx->err_dev;
+    CK(launch_mlp(m, (uint32_t)tiles, ctx->stream));
+    CK(launch_unpack((const uint2*)w.out.p, (const float4*)w.out_f32.p, fv.precision != 0, n, (float4*)out4, ctx->stream));
 }
 }  // namespace
 
 int insta_field_eval(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4) {
     return guarded(ctx, [&] {
         Avatar& a = ctx->avatar(avatar);
-        field_eval_view(ctx, a, a.field.view, coords, stride, n, out4);
+        field_eval_view(ctx, avatar, a, a.field.view, coords, stride, n, out4);
     });
 }
 
 int insta_field_eval_training(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, float* out4) {
     return guarded(ctx, [&] {
         Avatar& a = ctx->avatar(avatar);
-        field_eval_view(ctx, a, a.field.train_valid ? a.field.train_view : a.field.view, coords, stride, n, out4);
+        field_eval_view(ctx, avatar, a, a.field.train_valid ? a.field.train_view : a.field.view, coords, stride, n, out4);
     });
 }
 

@@ -233,6 +233,21 @@ struct TrainLossArgs {
     uint32_t* base_in;   // each kept ray's block start before compaction (for the copy kernel)
 };
 
+// The fields of one sample the loss reads: dt (warped), the deformed position, the raw outputs.
+struct TlSample {
+    float4 o;
+    float c3, c5, c6, c7;
+};
+__device__ __forceinline__ TlSample tl_load(const float* c, const float* out) {
+    TlSample t;
+    t.o = *reinterpret_cast<const float4*>(out);
+    t.c3 = c[3];
+    t.c5 = c[5];
+    t.c6 = c[6];
+    t.c7 = c[7];
+    return t;
+}
+
 // One thread per kept ray: the two passes over the ray's samples of the reference kernel.
 __global__ void __launch_bounds__(32) train_loss_kernel(TrainLossArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -246,23 +261,35 @@ __global__ void __launch_bounds__(32) train_loss_kernel(TrainLossArgs a) {
     const float mx = MIN_CONE * 128.0f;
     float T = 1.f, rgb_ray[3] = {0.f, 0.f, 0.f}, depth_ray = 0.f;
     uint32_t cn = 0;
-    for (; cn < numsteps; ++cn) {
-        if (T < 1e-4f) break;
-        const float4 o = *reinterpret_cast<const float4*>(nout + (size_t)cn * 4);
-        const float* c = cin + (size_t)cn * a.stride;
-        const float px = a.aabb_min[0] + c[5] * a.aabb_diag[0], py = a.aabb_min[1] + c[6] * a.aabb_diag[1],
-                    pz = a.aabb_min[2] + c[7] * a.aabb_diag[2];
-        const float dt = c[3] * (mx - MIN_CONE) + MIN_CONE;
-        const float dx = px - ox, dy = py - oy, dz = pz - oz;
-        const float cur_depth = sqrtf(dx * dx + dy * dy + dz * dz);
-        const float density = __expf(o.w);
-        const float alpha = 1.f - __expf(-density * dt);
-        const float w = alpha * T;
-        rgb_ray[0] += w * tl_logistic(o.x);
-        rgb_ray[1] += w * tl_logistic(o.y);
-        rgb_ray[2] += w * tl_logistic(o.z);
-        depth_ray += w * cur_depth;
-        T *= (1.f - alpha);
+    bool stop = false;
+    // four samples' fields are loaded before they are used (a few thousand rays give each SM about
+    // one warp, so the loads' latency is hidden only by having several in flight); the arithmetic
+    // and its order are those of the one-sample loop
+    for (uint32_t j0 = 0; j0 < numsteps && !stop; j0 += 4u) {
+        TlSample sm[4];
+#pragma unroll
+        for (uint32_t u = 0; u < 4u; ++u)
+            if (j0 + u < numsteps) sm[u] = tl_load(cin + (size_t)(j0 + u) * a.stride, nout + (size_t)(j0 + u) * 4);
+#pragma unroll
+        for (uint32_t u = 0; u < 4u; ++u) {
+            if (j0 + u >= numsteps) break;
+            if (T < 1e-4f) { stop = true; break; }
+            const float4 o = sm[u].o;
+            const float px = a.aabb_min[0] + sm[u].c5 * a.aabb_diag[0], py = a.aabb_min[1] + sm[u].c6 * a.aabb_diag[1],
+                        pz = a.aabb_min[2] + sm[u].c7 * a.aabb_diag[2];
+            const float dt = sm[u].c3 * (mx - MIN_CONE) + MIN_CONE;
+            const float dx = px - ox, dy = py - oy, dz = pz - oz;
+            const float cur_depth = sqrtf(dx * dx + dy * dy + dz * dz);
+            const float density = __expf(o.w);
+            const float alpha = 1.f - __expf(-density * dt);
+            const float w = alpha * T;
+            rgb_ray[0] += w * tl_logistic(o.x);
+            rgb_ray[1] += w * tl_logistic(o.y);
+            rgb_ray[2] += w * tl_logistic(o.z);
+            depth_ray += w * cur_depth;
+            T *= (1.f - alpha);
+            ++cn;
+        }
     }
     const float T_ray = T;
     // target colour and background (random_bg_color draw in sRGB, linearised)
@@ -320,34 +347,43 @@ __global__ void __launch_bounds__(32) train_loss_kernel(TrainLossArgs a) {
     float rgb2[3] = {0.f, 0.f, 0.f}, depth2 = 0.f;
     T = 1.f;
     float* dout = a.dloss + (size_t)cbase * 4;
-    for (uint32_t j = 0; j < ccount; ++j) {
-        const float* c = cin + (size_t)j * a.stride;
-        const float px = a.aabb_min[0] + c[5] * a.aabb_diag[0], py = a.aabb_min[1] + c[6] * a.aabb_diag[1],
-                    pz = a.aabb_min[2] + c[7] * a.aabb_diag[2];
-        const float dx = px - ox, dy = py - oy, dz = pz - oz;
-        const float depth = sqrtf(dx * dx + dy * dy + dz * dz);
-        const float dt = c[3] * (mx - MIN_CONE) + MIN_CONE;
-        const float4 o = *reinterpret_cast<const float4*>(nout + (size_t)j * 4);
-        const float rgb[3] = {tl_logistic(o.x), tl_logistic(o.y), tl_logistic(o.z)};
-        const float density = __expf(o.w);
-        const float alpha = 1.f - __expf(-density * dt);
-        const float w = alpha * T;
-        for (int k = 0; k < 3; ++k) rgb2[k] += w * rgb[k];
-        depth2 += w * depth;
-        T *= (1.f - alpha);
-        float d4[4], dot = 0.f;
-        for (int k = 0; k < 3; ++k) {
-            const float suffix = rgb_ray[k] - rgb2[k];
-            d4[k] = loss_scale * ((w * lgrad[k]) * (rgb[k] * (1.f - rgb[k])));   // logistic: no output L2 term
-            dot += lgrad[k] * (T * rgb[k] - suffix);
+    for (uint32_t j0 = 0; j0 < ccount; j0 += 4u) {
+        TlSample sm2[4];
+#pragma unroll
+        for (uint32_t u = 0; u < 4u; ++u)
+            if (j0 + u < ccount) sm2[u] = tl_load(cin + (size_t)(j0 + u) * a.stride, nout + (size_t)(j0 + u) * 4);
+#pragma unroll
+        for (uint32_t u = 0; u < 4u; ++u) {
+            const uint32_t j = j0 + u;
+            if (j >= ccount) break;
+            const TlSample& q = sm2[u];
+            const float px = a.aabb_min[0] + q.c5 * a.aabb_diag[0], py = a.aabb_min[1] + q.c6 * a.aabb_diag[1],
+                        pz = a.aabb_min[2] + q.c7 * a.aabb_diag[2];
+            const float dx = px - ox, dy = py - oy, dz = pz - oz;
+            const float depth = sqrtf(dx * dx + dy * dy + dz * dz);
+            const float dt = q.c3 * (mx - MIN_CONE) + MIN_CONE;
+            const float4 o = q.o;
+            const float rgb[3] = {tl_logistic(o.x), tl_logistic(o.y), tl_logistic(o.z)};
+            const float density = __expf(o.w);
+            const float alpha = 1.f - __expf(-density * dt);
+            const float w = alpha * T;
+            for (int k = 0; k < 3; ++k) rgb2[k] += w * rgb[k];
+            depth2 += w * depth;
+            T *= (1.f - alpha);
+            float d4[4], dot = 0.f;
+            for (int k = 0; k < 3; ++k) {
+                const float suffix = rgb_ray[k] - rgb2[k];
+                d4[k] = loss_scale * ((w * lgrad[k]) * (rgb[k] * (1.f - rgb[k])));   // logistic: no output L2 term
+                dot += lgrad[k] * (T * rgb[k] - suffix);
+            }
+            const float dd = __expf(fminf(fmaxf(o.w, -15.f), 15.f));
+            const float depth_sup = depth_grad * (T * depth - (depth_ray - depth2));
+            const float beta_sup = dt / (T_ray - 1.f + 1e-3f);
+            float dmlp = dd * (dt * (dot + depth_sup) + a.beta * beta_sup);
+            if (a.penalize) dmlp += (ta <= 0.01f) ? w : 0.f;
+            d4[3] = loss_scale * dmlp + (o.w < 0.f ? -l1_density : 0.f) + (o.w > -10.f && depth < a.near_distance ? 1e-4f : 0.f);
+            *reinterpret_cast<float4*>(dout + (size_t)j * 4) = make_float4(d4[0], d4[1], d4[2], d4[3]);
         }
-        const float dd = __expf(fminf(fmaxf(o.w, -15.f), 15.f));
-        const float depth_sup = depth_grad * (T * depth - (depth_ray - depth2));
-        const float beta_sup = dt / (T_ray - 1.f + 1e-3f);
-        float dmlp = dd * (dt * (dot + depth_sup) + a.beta * beta_sup);
-        if (a.penalize) dmlp += (ta <= 0.01f) ? w : 0.f;
-        d4[3] = loss_scale * dmlp + (o.w < 0.f ? -l1_density : 0.f) + (o.w > -10.f && depth < a.near_distance ? 1e-4f : 0.f);
-        *reinterpret_cast<float4*>(dout + (size_t)j * 4) = make_float4(d4[0], d4[1], d4[2], d4[3]);
     }
 }
 
