@@ -380,3 +380,36 @@ def test_train_step_fits_a_constant_colour(ctx, avatar, frame0):
     ctx.train_set_math(False)
     assert min(kept) > n // 2
     assert np.isfinite(losses).all() and np.mean(losses[-5:]) < 0.25 * np.mean(losses[:5]), (losses[:5], losses[-5:])
+
+
+def test_empty_and_invalid_training_calls(ctx, field):
+    """Edge cases: no kept rays (nothing written, the rollover leaves the buffers alone), zero
+    samples to the backward, and the arguments the entry points reject."""
+    from insta_gb300 import abi
+    fc, params, lay = field
+    cap = 64
+    zero = torch.zeros(1, dtype=torch.int32, device="cuda")
+    counter = torch.zeros(1, dtype=torch.int32, device="cuda")
+    cout = torch.full((cap, 27), 7.0, device="cuda")
+    dloss = torch.full((cap, 4), 7.0, device="cuda")
+    one = torch.zeros((1, 27), device="cuda")
+    torch.cuda.synchronize()
+    ctx.train_loss(n_rays=16, max_rays=16, max_samples_compacted=cap, target_batch_size=cap, stride=27, rays=torch.zeros((16, 6), device="cuda"),
+                   target=torch.zeros((16, 4), device="cuda"), rays_counter=zero, ray_indices=torch.zeros(16, dtype=torch.int32, device="cuda"),
+                   numsteps=torch.zeros((16, 2), dtype=torch.int32, device="cuda"), coords=one, network_output=torch.zeros((1, 4), device="cuda"),
+                   numsteps_counter=counter, coords_out=cout, dloss_doutput=dloss)
+    g = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    ctx.field_backward(AVATAR, one, 27, 0, torch.zeros((1, 4), device="cuda"), g)   # n = 0: nothing to do
+    ctx.sync()
+    assert int(counter.item()) == 0 and bool((cout == 7.0).all()) and bool((dloss == 7.0).all()) and float(g.abs().sum()) == 0.0
+    with pytest.raises(abi.InstaError):
+        ctx.train_loss(n_rays=0, max_rays=0, max_samples_compacted=cap, stride=27, rays_counter=zero, numsteps_counter=counter)
+    with pytest.raises(abi.InstaError):
+        ctx.train_loss(n_rays=1, max_rays=0, max_samples_compacted=cap, target_batch_size=cap + 1, stride=27, rays_counter=zero,
+                       numsteps_counter=counter, coords_out=cout, dloss_doutput=dloss)
+    with pytest.raises(abi.InstaError):
+        ctx.train_loss(n_rays=1, max_rays=0, max_samples_compacted=cap, loss_type=9, stride=27, rays_counter=zero, numsteps_counter=counter)
+    with pytest.raises(abi.InstaError):
+        ctx.adam_step(AVATAR, g, ema_decay=1.0)
+    with pytest.raises(abi.InstaError):
+        ctx._check(ctx.lib.insta_train_set_math(ctx.h, 7))
