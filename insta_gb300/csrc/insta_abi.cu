@@ -140,6 +140,7 @@ struct insta_ctx {
     bool train_tf32 = false;            // insta_train_set_math: TF32 tensor-core GEMMs
     DevBuf train_scratch;
     DevBuf loss_scratch;     // insta_train_loss: each kept ray's block start before compaction
+    DevBuf train_t;          // insta_training_samples: each ray's sample positions t
     bool keep_master = false;           // a parameter reload from the optimizer keeps the FP32 master weights
     cudaStream_t side = nullptr;        // asynchronous frame uploads
     cudaEvent_t side_mark = nullptr;    // orders a side upload after the main stream's earlier work
@@ -923,6 +924,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     if (ctx->blas) cublasDestroy(ctx->blas);
     ctx->release(ctx->train_scratch);
     ctx->release(ctx->loss_scratch);
+    ctx->release(ctx->train_t);
     if (ctx->loop_exec) cudaGraphExecDestroy(ctx->loop_exec);
     if (ctx->loop_graph) cudaGraphDestroy(ctx->loop_graph);
     if (ctx->loop_state) cudaFree(ctx->loop_state);
@@ -1328,7 +1330,12 @@ int insta_training_samples(insta_ctx* ctx, int avatar, int grid_frame, const flo
         for (int k = 0; k < 3; ++k) { T.aabb_min[k] = a.train_min[k]; T.aabb_max[k] = a.train_max[k]; }
         T.cone_angle = cone_angle; T.max_samples = max_samples; T.bitfield = (const uint8_t*)g.bitfield.p;
         T.coords = coords; T.stride = stride; T.ray_indices = ray_indices; T.numsteps = numsteps; T.counters = counters;
-        { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_training_samples(T, ctx->stream)); }
+        float* tbuf = nullptr;
+        if (n_rays <= kTrainMarchOnceMaxRays) {
+            ctx->alloc(ctx->train_t, (size_t)n_rays * 1024 * 4);
+            tbuf = (float*)ctx->train_t.p;
+        }
+        { Stage st(ctx, INSTA_STAGE_MARCH, tbuf ? 2 : 1); CK(launch_training_samples(T, tbuf, ctx->stream)); }
         // the warp with per-record frames (surface_closest_point, testbed_nerf.cu:3290): large sample
         // buffers take the (frame, cell)-sorted warp walk over the records the march wrote
         if (max_samples >= kMapSortedMin && a.table_frames <= kMaxRequests) {

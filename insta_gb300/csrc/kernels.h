@@ -169,7 +169,9 @@ struct TrainArgs {
     uint32_t* numsteps;         // [n][2] (count, base)
     uint32_t* counters;         // [2] rays kept, samples requested
 };
-cudaError_t launch_training_samples(const TrainArgs& a, cudaStream_t s);
+// tbuf (optional, [n_rays][1024] floats): the march runs once and a warp per kept ray writes the records
+cudaError_t launch_training_samples(const TrainArgs& a, float* tbuf, cudaStream_t s);
+constexpr int64_t kTrainMarchOnceMaxRays = 1 << 16;   // larger batches march twice (no per-ray buffer)
 
 cudaError_t launch_encode_coords(const FieldView& fv, const float* coords, uint32_t stride, int64_t n, uint8_t* tiles,
                                  uint32_t tile_bytes, uint32_t k_in, cudaStream_t s);

@@ -736,6 +736,72 @@ __global__ void __launch_bounds__(256) training_samples_kernel(const __grid_cons
     }
 }
 
+// The same training march run once: the counting pass keeps each occupied sample's t (at most 1024
+// per ray) and reserves the ray's block, then a warp per kept ray writes the records from those t
+// with the write pass's arithmetic -- the records depend only on t and the ray -- so the records
+// are bit-identical to training_samples_kernel's.
+__global__ void __launch_bounds__(256) training_march_kernel(const __grid_constant__ TrainArgs A, float* __restrict__ tbuf) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n_rays) return;
+    const float* r = A.rays + i * 6;
+    const V3 o = v3(r[0], r[1], r[2]);
+    const V3 d = normalize_rn(v3(r[3], r[4], r[5]));
+    const V3 idir = v3(__fdiv_rn(1.f, d.x), __fdiv_rn(1.f, d.y), __fdiv_rn(1.f, d.z));
+    float startt = fmaxf(aabb_ray_tmin(A.aabb_min, A.aabb_max, o, d), 0.0f);
+    startt = __fadd_rn(startt, __fmul_rn(calc_dt(startt, A.cone_angle), A.start_rand[i]));
+    float* tr = tbuf + (size_t)i * 1024u;
+    uint32_t j = 0;
+    float t = startt;
+    for (int guard = 0; guard < (1 << 16) && j < 1024u; ++guard) {
+        const V3 pos = ray_at(o, d, t);
+        if (!box_contains(A.aabb_min, A.aabb_max, pos)) break;
+        const float dt = calc_dt(t, A.cone_angle);
+        const int mip = mip_from_dt(dt, pos);
+        if (occupied_at(pos, A.bitfield, mip)) { tr[j] = t; ++j; t = __fadd_rn(t, dt); }
+        else t = advance_to_next_voxel(t, A.cone_angle, pos, d, idir, GRID >> mip);
+    }
+    if (j == 0) return;
+    const uint32_t base = atomicAdd(A.counters + 1, j);
+    if (base + j > A.max_samples) {
+        for (uint32_t q = base; q < A.max_samples; ++q) A.coords[(size_t)q * A.stride + 4] = -1.f;
+        return;
+    }
+    const uint32_t ri = atomicAdd(A.counters + 0, 1u);
+    A.ray_indices[ri] = (uint32_t)i;
+    A.numsteps[2 * ri] = j;
+    A.numsteps[2 * ri + 1] = base;
+}
+
+__global__ void __launch_bounds__(256) training_write_kernel(const __grid_constant__ TrainArgs A, const float* __restrict__ tbuf) {
+    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if ((int64_t)k >= min((int64_t)A.counters[0], A.n_rays)) return;
+    const uint32_t i = A.ray_indices[k], j = A.numsteps[2 * k], base = A.numsteps[2 * k + 1];
+    const float* r = A.rays + (size_t)i * 6;
+    const V3 o = v3(r[0], r[1], r[2]);
+    const V3 d = normalize_rn(v3(r[3], r[4], r[5]));
+    const uint32_t img = A.image[i];
+    const float wd[3] = {__fmul_rn(__fadd_rn(d.x, 1.0f), 0.5f), __fmul_rn(__fadd_rn(d.y, 1.0f), 0.5f), __fmul_rn(__fadd_rn(d.z, 1.0f), 0.5f)};
+    const float* ex = (A.extra && img < A.n_images) ? A.extra + (size_t)img * A.n_extra : nullptr;
+    const float* tr = tbuf + (size_t)i * 1024u;
+    for (uint32_t w = lane; w < j; w += 32u) {
+        const float t = tr[w];
+        const V3 pos = ray_at(o, d, t);
+        const float dt = calc_dt(t, A.cone_angle);
+        float* c = A.coords + (size_t)(base + w) * A.stride;
+        const float p3[3] = {pos.x, pos.y, pos.z};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float rel = __fdiv_rn(__fsub_rn(p3[q], A.aabb_min[q]), __fsub_rn(A.aabb_max[q], A.aabb_min[q]));
+            c[q] = rel;
+            c[5 + q] = rel;
+            c[8 + q] = wd[q];
+        }
+        c[3] = warp_dt(dt);
+        c[4] = (float)img;
+        for (uint32_t m = 0; m < A.n_extra; ++m) c[A.stride - A.n_extra + m] = ex ? ex[m] : 0.f;
+    }
+}
+
 // ------------------------------------------------------------------ march debug
 __global__ void march_debug_kernel(RenderView rv, const uint8_t* __restrict__ bf, int max_out, float* out_t, float* out_dt, int32_t* out_n) {
     uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -864,11 +930,17 @@ cudaError_t launch_unpack(const uint2* out, const float4* out_f32, int bf16, int
     return cudaGetLastError();
 }
 
-cudaError_t launch_training_samples(const TrainArgs& a, cudaStream_t s) {
+cudaError_t launch_training_samples(const TrainArgs& a, float* tbuf, cudaStream_t s) {
     if (a.n_rays <= 0) return cudaSuccess;
     // one ray per thread; small batches (a few thousand rays) in 32-thread blocks so that they spread over every SM
     const int threads = a.n_rays < 152 * 128 ? 32 : 128;
-    training_samples_kernel<<<(unsigned)((a.n_rays + threads - 1) / threads), threads, 0, s>>>(a);
+    const unsigned blocks = (unsigned)((a.n_rays + threads - 1) / threads);
+    if (tbuf) {
+        training_march_kernel<<<blocks, threads, 0, s>>>(a, tbuf);
+        training_write_kernel<<<(unsigned)((a.n_rays * 32 + 255) / 256), 256, 0, s>>>(a, tbuf);
+    } else {
+        training_samples_kernel<<<blocks, threads, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 
