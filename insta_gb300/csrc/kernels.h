@@ -52,11 +52,14 @@ constexpr uint32_t kStepShift = 27, kRayMask = (1u << kStepShift) - 1u;
 constexpr uint32_t kNoSample = 0xffffffffu;
 
 // cell bits per request (multiple of 3, >= 12) so that n_reqs << bits stays within kMaxSortBins
-inline uint32_t sort_cell_bits(uint32_t n_reqs) {
-    uint32_t b = 18;
+inline uint32_t sort_cell_bits(uint32_t n_reqs, uint32_t start = 18) {
+    uint32_t b = start;
     while (b > 12 && ((uint64_t)n_reqs << b) > kMaxSortBins) b -= 3;
     return b;
 }
+// record and point sets (canonical map, density-grid warp): 128^3 cells where the bins allow --
+// their points are spread through each cell, unlike a render's neighbouring rays
+inline uint32_t map_cell_bits(uint32_t n_frames) { return sort_cell_bits(n_frames, 21); }
 
 struct WaveArgs {
     const ReqView* reqs;        // device table, n_reqs entries (request slots)

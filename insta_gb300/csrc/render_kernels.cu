@@ -1175,7 +1175,7 @@ cudaError_t launch_canonical_map_coords_sorted(const FrameView* frames_dev, uint
                                                uint32_t stride, uint32_t n_extra, uint32_t n, void* scratch, uint32_t* err, cudaStream_t s,
                                                const uint32_t* n_dev) {
     if (n == 0) return cudaSuccess;
-    const uint32_t cb = sort_cell_bits(n_frames);
+    const uint32_t cb = map_cell_bits(n_frames);
     const uint32_t n_bins = n_frames << cb;
     uint32_t* keys = static_cast<uint32_t*>(scratch);
     int32_t* ids = reinterpret_cast<int32_t*>(keys + n);
@@ -1209,7 +1209,7 @@ cudaError_t launch_canonical_map_coords_sorted(const FrameView* frames_dev, uint
 }
 
 size_t warp_sorted_scratch_bytes(uint32_t n, uint32_t n_frames) {
-    const uint32_t cb = sort_cell_bits(n_frames);
+    const uint32_t cb = map_cell_bits(n_frames);
     const size_t bins = (size_t)n_frames << cb;
     return ((size_t)n * 2 + (size_t)n + 128u * (size_t)n_frames + bins + bins / kSortBlock + 2u * (n_frames + 1u) + 2u) * sizeof(uint32_t);
 }
@@ -1218,7 +1218,7 @@ cudaError_t launch_warp_random_sorted(const FrameView* frames_dev, uint32_t n_fr
                                       uint32_t n, uint64_t rng_state, uint64_t rng_inc, const float* dom_lo, const float* dom_hi,
                                       void* scratch, uint32_t* err, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    const uint32_t cb = sort_cell_bits(n_frames);
+    const uint32_t cb = map_cell_bits(n_frames);
     const uint32_t n_bins = n_frames << cb;
     uint32_t* keys = static_cast<uint32_t*>(scratch);
     int32_t* ids = reinterpret_cast<int32_t*>(keys + n);
