@@ -40,8 +40,8 @@ class TrainConfig:
     srgb_targets: bool = True
     train_in_linear_colors: bool = False
     loss_scale: float = 128.0
-    depth_supervision_lambda: float = 0.0
-    seg_mask_supervision_lambda: float = 40.0
+    depth_supervision_lambda: float = 1.25   # "depth_weight"; no depth term without depth samples
+    seg_mask_supervision_lambda: float = 40.0   # "seg_weight"
     near_distance: float = 0.2
     beta: float = 0.0
     penalize_density: bool = False
@@ -77,6 +77,7 @@ class TrainStep:
         self.grad = torch.zeros(_layout.field_layout(fc).total, dtype=torch.float32, **dev)
         self.counters_host = torch.zeros(2, dtype=torch.int32, pin_memory=True)
         self.n_steps = 0
+        self._last_kept = 0
         ctx.train_set_math(cfg.tf32)
 
     def step(self, grid_frame: int, rays, image, start_rand, target, background=None, extra=None, n_images: int = 0,
