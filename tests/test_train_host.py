@@ -25,6 +25,9 @@ class FakeLib:
     def insta_last_error(self, h):
         return b"unknown training math"
 
+    def insta_ctx_destroy(self, h):
+        return 0
+
 
 def fake_context():
     from insta_gb300 import abi
