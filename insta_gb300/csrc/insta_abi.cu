@@ -86,7 +86,7 @@ struct Field {
 
 // Device scratch of the render wavefront, sized for the largest request seen.
 struct Wave {
-    DevBuf rays[2][4], n_round, sample_index, sample_ray, sample_key, sample_order, sort_bins, samples, tiles, aux, out, out_f32,
+    DevBuf rays[2][4], n_round, sample_index, sample_ray, sample_key, sample_order, sort_bins, samples, march_t, tiles, aux, out, out_f32,
         counters, req_table, req_meta, init_meta;
     uint32_t cap_rays = 0;
     uint64_t cap_samples = 0;
@@ -533,6 +533,7 @@ struct WaveRun {
         ctx->alloc(w.tiles, cap_samples / 128 * P.tile_bytes);
         ctx->alloc(w.aux, cap_samples * sizeof(float2));
         ctx->alloc(w.samples, cap_samples * sizeof(float4));
+        ctx->alloc(w.march_t, cap_samples * sizeof(float));
         ctx->alloc(w.sample_ray, cap_samples * sizeof(uint32_t));
         ctx->alloc(w.sample_index, cap_samples * sizeof(uint32_t));
         ctx->alloc(w.sample_key, cap_samples * sizeof(uint32_t));
@@ -561,6 +562,7 @@ struct WaveRun {
         W.k_in = P.k_in;
         W.aux = (float2*)w.aux.p;
         W.samples = (float4*)w.samples.p;
+        W.march_t = (float*)w.march_t.p;
         W.sample_ray = (uint32_t*)w.sample_ray.p;
         W.sample_index = (uint32_t*)w.sample_index.p;
         W.sample_key = (uint32_t*)w.sample_key.p;
@@ -948,7 +950,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     Wave& w = ctx->wave;
     for (int b = 0; b < 2; ++b)
         for (int k = 0; k < 4; ++k) ctx->release(w.rays[b][k]);
-    for (DevBuf* b : {&w.n_round, &w.sample_index, &w.sample_ray, &w.sample_key, &w.sample_order, &w.sort_bins, &w.samples, &w.tiles,
+    for (DevBuf* b : {&w.n_round, &w.sample_index, &w.sample_ray, &w.sample_key, &w.sample_order, &w.sort_bins, &w.samples, &w.march_t, &w.tiles,
                       &w.aux, &w.out, &w.out_f32, &w.counters, &w.req_table, &w.req_meta, &w.init_meta})
         ctx->release(*b);
     if (ctx->host_counters) cudaFreeHost(ctx->host_counters);

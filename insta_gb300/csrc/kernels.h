@@ -91,6 +91,7 @@ struct WaveArgs {
     uint8_t* tiles;             // encoded input tile records
     uint32_t tile_bytes, k_in;
     float4* samples;            // per sample: (pos.xyz, dt) from the march
+    float* march_t;             // [step][n_alive] the t of each ray's samples of the round (march scratch)
     float2* aux;                // per sample: (dt, depth candidate)
     const uint2* out;           // per sample: FP16 (r, g, b, density)
     const float4* out_f32;      // per sample when the MLP runs in BF16

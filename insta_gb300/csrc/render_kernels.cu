@@ -141,9 +141,10 @@ __device__ __forceinline__ void encode_sample(const FieldView& fv, const uint16_
 }
 
 // One thread per alive ray: the next `steps` sample positions (generate_next_nerf_network_inputs,
-// ngp/src/testbed_nerf.cu:722-795).  The march runs twice -- count, then write -- so the samples of
-// a warp's 32 neighbouring rays land in one compacted block (base from a warp-aggregated atomic),
-// ordered step-major: step k of all lanes, then step k + 1.  Neighbouring entries of the stream are
+// ngp/src/testbed_nerf.cu:722-795).  The march counts the samples, keeping each one's t; then the
+// write pass places them -- position and step rebuilt from t -- so the samples of a warp's 32
+// neighbouring rays land in one compacted block (base from a warp-aggregated atomic), ordered
+// step-major: step k of all lanes, then step k + 1.  Neighbouring entries of the stream are
 // then the same step of adjacent pixels, which keeps the cooperative BVH queries coherent.
 // sample_ray packs the ray slot and the step k; the deform stage, which runs in spatially sorted
 // order, records in sample_index[k * n_alive + r] where sample k of ray r went.
@@ -174,8 +175,9 @@ __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ Wave
             ray.t = t0 = ra.w;
             for (; j < steps; ++j) {
                 V3 pos;
-                float dt;
-                if (ns + j >= rv.max_samples_per_ray || !ray_next_sample(rv, bitfield, ray, pos, dt)) break;
+                float dt, ts;
+                if (ns + j >= rv.max_samples_per_ray || !ray_next_sample(rv, bitfield, ray, pos, dt, &ts)) break;
+                A.march_t[(size_t)j * n_alive + r] = ts;   // the write pass rebuilds the sample from its t
             }
         }
         const uint32_t total = __reduce_add_sync(0xffffffffu, j);
@@ -189,9 +191,12 @@ __global__ void __launch_bounds__(256) march_kernel(const __grid_constant__ Wave
             const bool act = k < j;
             const uint32_t m = __ballot_sync(0xffffffffu, act);
             if (act) {
-                V3 pos;
-                float dt;
-                ray_next_sample(rv, bitfield, ray, pos, dt);
+                // position and step of the sample at ts, as ray_next_sample produced them; the ray
+                // then continues from ts + dt, where ray_next_sample leaves it
+                const float ts = A.march_t[(size_t)k * n_alive + r];
+                const V3 pos = ray_at(ray.o, ray.d, ts);
+                const float dt = calc_dt(ts, rv.cone_angle);
+                ray.t = __fadd_rn(ts, dt);
                 const uint32_t idx = base + offset + (uint32_t)__popc(m & lt_mask);
                 A.samples[idx] = make_float4(pos.x, pos.y, pos.z, dt);
                 A.sample_ray[idx] = r | (k << kStepShift);
