@@ -678,7 +678,8 @@ __global__ void unpack_outputs_kernel(const uint2* __restrict__ out, const float
 // ------------------------------------------------------------------ training samples
 // generate_training_samples_nerf (ngp/src/testbed_nerf.cu:1105-1285) for caller-supplied rays:
 // two passes per ray (count up to NERF_STEPS = 1024 occupied steps through the train box, then
-// reserve a block atomically and write NerfCoordinate records with holder = image).
+// reserve a block atomically and write NerfCoordinate records with holder = image).  Batches of
+// up to kTrainMarchOnceMaxRays rays take training_march_kernel + training_write_kernel instead.
 __global__ void __launch_bounds__(256) training_samples_kernel(const __grid_constant__ TrainArgs A) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.n_rays) return;
