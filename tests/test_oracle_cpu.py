@@ -271,3 +271,57 @@ def test_train_loss_oracle_compaction_and_rollover(oracle):
     src = np.arange(total, n) % total
     np.testing.assert_array_equal(cout2[total:n], cout2[src])
     np.testing.assert_allclose(dloss2[total:n], dloss2[src] * np.float32(total / n), rtol=1e-6)
+
+
+def _np_loss_forward(cfg, b, k):
+    """Per-ray loss of compute_loss_kernel_train_nerf (instant-ngp/src/testbed_nerf.cu:1305-1460),
+    restated independently in NumPy float64 for kept ray k: composite with the transmittance stop,
+    background added when the ray ran out, target from the image sample, loss mean / n_rays."""
+    mn, mx = np.array(cfg["aabb_min"], np.float64), np.array(cfg["aabb_max"], np.float64)
+    min_cone = np.sqrt(3.0) / 1024.0
+    count, base = (int(x) for x in b["numsteps"][k])
+    ray = int(b["ray_indices"][k])
+    T, rgb = 1.0, np.zeros(3)
+    n = 0
+    for j in range(count):
+        if T < 1e-4:
+            break
+        c = b["coords"][base + j].astype(np.float64)
+        o = b["network_output"][base + j].astype(np.float64)
+        dt = c[3] * (min_cone * 128 - min_cone) + min_cone
+        alpha = 1.0 - np.exp(-np.exp(o[3]) * dt)
+        rgb += alpha * T / (1.0 + np.exp(-o[:3]))
+        T *= 1.0 - alpha
+        n += 1
+    s2l = lambda s: np.where(s <= 0.04045, s / 12.92, ((s + 0.055) / 1.055) ** 2.4)
+    l2s = lambda l: np.where(l < 0.0031308, 12.92 * l, 1.055 * np.power(np.maximum(l, 0), 0.41666) - 0.055)
+    bg = s2l(b["background"][ray].astype(np.float64))
+    tex = b["target"][ray].astype(np.float64)
+    if cfg["train_in_linear_colors"] or not cfg["srgb_targets"]:
+        tgt = tex[:3] + (1 - tex[3]) * bg
+        if not cfg["train_in_linear_colors"]:
+            tgt, bg = l2s(tgt), l2s(bg)
+    else:
+        bg = l2s(bg)
+        tgt = l2s(tex[:3] / tex[3]) * tex[3] + (1 - tex[3]) * bg if tex[3] > 0 else bg
+    if n == count:
+        rgb = rgb + T * bg
+    d = rgb - tgt
+    if cfg["loss_type"] == 4:   # Huber(0.1) / 5
+        ad = np.abs(d)
+        loss = np.where(ad > 0.1, ad - 0.05, 0.5 / 0.1 * d * d) / 5
+    else:                       # L2
+        loss = d * d
+    return loss.mean() / cfg["n_rays"]
+
+
+@pytest.mark.parametrize("loss_type,srgb,linear", [(0, 1, 0), (4, 1, 0), (0, 0, 0), (4, 1, 1)])
+def test_train_loss_oracle_matches_numpy_restatement(oracle, loss_type, srgb, linear):
+    from conftest import loss_cfg, train_loss_batch
+    b = train_loss_batch(24, seed=30 + loss_type + srgb, max_steps=40)
+    b["network_output"][::3, 3] += 4.0          # some rays reach the transmittance stop
+    b["target"][1::4, 3] = 0.0                  # transparent samples: the target is the background
+    cfg = loss_cfg(n_rays=24, loss_type=loss_type, srgb_targets=srgb, train_in_linear_colors=linear)
+    _, _, _, _, loss = oracle.train_loss(cfg, **b)
+    ref = np.array([_np_loss_forward(cfg, b, k) for k in range(24)])
+    np.testing.assert_allclose(loss, ref, rtol=2e-4, atol=1e-9)
