@@ -325,3 +325,86 @@ def test_train_loss_oracle_matches_numpy_restatement(oracle, loss_type, srgb, li
     _, _, _, _, loss = oracle.train_loss(cfg, **b)
     ref = np.array([_np_loss_forward(cfg, b, k) for k in range(24)])
     np.testing.assert_allclose(loss, ref, rtol=2e-4, atol=1e-9)
+
+
+def _np_loss_gradients(cfg, b, k, extra, mean_density):
+    """dL/d(raw output) of compute_loss_kernel_train_nerf's second pass (instant-ngp/src/
+    testbed_nerf.cu:1465-1560) for kept ray k, restated in NumPy float64 with every term on:
+    colour (L2), depth supervision (L1) with the segmentation rules, beta, density penalty,
+    near-distance and mean-density regularisers."""
+    mn, mx = np.array(cfg["aabb_min"], np.float64), np.array(cfg["aabb_max"], np.float64)
+    min_cone = np.sqrt(3.0) / 1024.0
+    count, base = (int(x) for x in b["numsteps"][k])
+    ray = int(b["ray_indices"][k])
+    R = b["rays"][ray].astype(np.float64)
+    samples = []
+    T, rgb_ray, depth_ray = 1.0, np.zeros(3), 0.0
+    for j in range(count):
+        if T < 1e-4:
+            break
+        c = b["coords"][base + j].astype(np.float64)
+        o = b["network_output"][base + j].astype(np.float64)
+        pos = mn + c[5:8] * (mx - mn)
+        depth = np.linalg.norm(pos - R[:3])
+        dt = c[3] * (min_cone * 128 - min_cone) + min_cone
+        alpha = 1.0 - np.exp(-np.exp(o[3]) * dt)
+        rgb = 1.0 / (1.0 + np.exp(-o[:3]))
+        w = alpha * T
+        rgb_ray += w * rgb
+        depth_ray += w * depth
+        T *= 1.0 - alpha
+        samples.append((o, rgb, depth, dt, alpha))
+    T_ray = T
+    tex = b["target"][ray].astype(np.float64)
+    bg = np.zeros(3)
+    tgt = tex[:3] + (1 - tex[3]) * bg          # trained in linear colours, black background
+    if len(samples) == count:
+        rgb_ray = rgb_ray + T * bg
+    seg, lam = 1.0, cfg["depth_supervision_lambda"]
+    m = int(extra["seg_mask"][ray])
+    if m in (120, 130, 140):
+        seg = cfg["seg_mask_supervision_lambda"]
+    if m <= 90 or m > 250 or tex[3] < 0.001:
+        lam = 0.0
+    target_depth = np.linalg.norm(R[3:]) * (extra["depth"][ray] if lam > 0 else -1.0)
+    depth_grad = (np.sign(depth_ray - target_depth) if target_depth > 0 else 0.0) * lam
+    lg = 2.0 * (rgb_ray - tgt) * seg
+    scale = cfg["loss_scale"] / cfg["n_rays"]
+    l1 = 1e-4 if mean_density < 0.01 else 0.0
+    out, T, rgb2, depth2 = [], 1.0, np.zeros(3), 0.0
+    for o, rgb, depth, dt, alpha in samples:
+        w = alpha * T
+        rgb2 += w * rgb
+        depth2 += w * depth
+        T *= 1.0 - alpha
+        suffix = rgb_ray - rgb2
+        d = np.zeros(4)
+        d[:3] = scale * (w * lg) * rgb * (1 - rgb)
+        dmlp = np.exp(np.clip(o[3], -15, 15)) * (dt * (lg @ (T * rgb - suffix) + depth_grad * (T * depth - (depth_ray - depth2)))
+                                                 + cfg["beta"] * dt / (T_ray - 1 + 1e-3))
+        if cfg["penalize_density"] and tex[3] <= 0.01:
+            dmlp += w
+        d[3] = scale * dmlp + (-l1 if o[3] < 0 else 0.0) + (1e-4 if (o[3] > -10 and depth < cfg["near_distance"]) else 0.0)
+        out.append(d)
+    return np.array(out).reshape(-1, 4)
+
+
+def test_train_loss_oracle_gradients_match_numpy_all_terms(oracle):
+    from conftest import loss_cfg, train_loss_batch
+    n = 20
+    b = train_loss_batch(n, seed=41, max_steps=30)
+    b["background"] = np.zeros((n, 3), np.float32)
+    b["target"][::5, 3] = 0.0
+    rng = np.random.default_rng(42)
+    extra = dict(depth=rng.uniform(0.2, 2.0, n).astype(np.float32),
+                 seg_mask=np.array([0, 100, 120, 130, 140, 255, 91, 250] * 3, np.int32)[:n])
+    cfg = loss_cfg(n_rays=n, loss_type=0, depth_loss_type=1, srgb_targets=0, train_in_linear_colors=1, loss_scale=128.0,
+                   depth_supervision_lambda=1.25,
+                   seg_mask_supervision_lambda=40.0, near_distance=0.6, beta=0.05, penalize_density=1)
+    ns, _, _, dloss, _ = oracle.train_loss(cfg, **b, **extra, mean_density=0.005)
+    for k in range(n):
+        ref = _np_loss_gradients(cfg, b, k, extra, 0.005)
+        c, base = int(ns[k, 0]), int(ns[k, 1])
+        assert c == len(ref)
+        got = dloss[base:base + c].astype(np.float64)
+        np.testing.assert_allclose(got, ref, rtol=2e-3, atol=1e-6 * max(1.0, np.abs(ref).max()))
