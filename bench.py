@@ -37,8 +37,7 @@ CONE = 1.0 / 256.0
 L2_FLUSH_BYTES = 512 << 20
 SETTLE_S = 0.5   # untimed steps before the warm-up, long enough for the SM clock to ramp
 # DRAM bytes (read + write) of the deform+encode stage per 512x512 frame (nearest_stage_kernel and
-# map_encode_kernel, two rounds each), from an ncu capture of this workload
-# (profiles/deform_encode_render512.md)
+# map_encode_kernel, two rounds each), from an ncu capture of this workload's kernels
 TRAFFIC_PER_FRAME = 428_134_656
 # Algorithmic bytes per sample of the dominant kernel (deform_encode): hash-grid gathers
 # (16 levels x 8 corners x 2 FP16 features) + sample record, ray direction and ray index in +

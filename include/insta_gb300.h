@@ -104,6 +104,8 @@ typedef struct {
     uint32_t max_samples_per_ray;   /* 1024 */
     uint32_t linear_colors;         /* 0: shade converts sRGB -> linear */
     const float* extra_dims;        /* host, n_extra_dims floats, or NULL (zeros) */
+    uint32_t* out_samples;          /* device u32[h*w] or NULL: samples composited into each pixel
+                                       (the ray's NerfPayload::n_steps when it finished) */
 } insta_render_desc;
 
 /* Pipeline stages timed by insta_stats (CUDA events on the context's stream). */
@@ -280,16 +282,21 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
 #define INSTA_TRAIN_MATH_FP32 0
 #define INSTA_TRAIN_MATH_TF32 1
 int insta_train_set_math(insta_ctx* ctx, int math);
-/* Adam (configs/nerf/main.json nests it in an Ema): w -= lr * m_hat / (sqrt(v_hat) + eps) with
- * g + l2_reg * w, bias-corrected moments; the FP32 master weights and moments stay on the
- * device, the field's FP16 parameters and weight image are rewritten.  ema_decay > 0 adds the
- * Ema wrapper: a bias-corrected exponential average of the weights,
+/* Adam (configs/nerf/main.json nests it in an Ema), as tiny-cuda-nn's Adam steps it: the gradient
+ * is divided by loss_scale first (LOSS_SCALE, 128 in train_nerf_step); the MLP weights get
+ * g + l2_reg * w and step every call; hash-table entries get no L2 term, and an entry whose
+ * gradient is exactly zero is skipped (weights, moments and its own step count unchanged);
+ * w -= lr sqrt(1 - beta2^t) / (1 - beta1^t) * m / (sqrt(v) + eps), t the parameter's step count.
+ * The FP32 master weights, moments and table step counts stay on the device; the field's FP16
+ * parameters and weight image are rewritten.  ema_decay > 0 adds the Ema wrapper: a
+ * bias-corrected exponential average of the weights,
  * e_t = (decay (1 - decay^(t-1)) e_(t-1) + (1 - decay) w_t) / (1 - decay^t), becomes the field's
  * parameters (what rendering and insta_field_eval read), while the training forward of
  * insta_field_backward keeps reading the raw master weights. */
 typedef struct insta_adam_config {
     float learning_rate, beta1, beta2, epsilon, l2_reg;
-    float ema_decay;   /* 0: no Ema; configs/nerf/main.json: 0.95 */
+    float ema_decay;    /* 0: no Ema; configs/nerf/main.json: 0.95 */
+    float loss_scale;   /* factor the gradients carry (128 from insta_train_loss's LOSS_SCALE); 0 reads as 1 */
 } insta_adam_config;
 int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_adam_config* cfg);
 
@@ -365,6 +372,27 @@ int insta_render_async(insta_ctx* ctx, const insta_render_desc* req, float* out_
 int insta_render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* const* out_rgba, float* const* out_depth);
 /* Network samples evaluated by the last insta_render / insta_render_batch (synchronises). */
 int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples);
+
+/* Launch shapes of the render wavefront, per context.  NerfTracer::trace fixes its own
+ * (MIN/MAX_STEPS_INBETWEEN_COMPACTION 1/8 and n_steps_between_compaction = clamp(N0 / n_alive),
+ * instant-ngp/src/testbed_nerf.cu:67-68,2172); here each round takes
+ * clamp(round budget / n_alive, 1, max_steps_per_round) samples per alive ray.  A zero field keeps
+ * the built-in choice.  Results do not depend on these (every sample's arithmetic is the same;
+ * rays composite their samples in order): only speed does. */
+typedef struct insta_tuning {
+    uint32_t max_steps_per_round;   /* 1..32 (built-in 32) */
+    uint32_t sort_cell_bits;        /* 12, 15, 18 or 21: Morton cells of a round's (request, cell) sort (built-in 18 = 64^3) */
+    uint32_t mlp_ctas_per_sm;       /* 1..4 resident MLP CTAs per SM (built-in: as many as shared memory allows) */
+    uint32_t deform_blocks_per_sm;  /* 1..64 blocks per SM of the deform + encode stage (built-in 16) */
+} insta_tuning;
+int insta_tuning_set(insta_ctx* ctx, const insta_tuning* t);
+int insta_tuning_get(insta_ctx* ctx, insta_tuning* t);
+/* The autotuner: times insta_render_batch on the given requests (device outputs it allocates)
+ * for candidate launch shapes -- coordinate descent over the four fields above, each candidate the
+ * median of `repeats` timed renders after one untimed one (CUDA events on the context's stream) --
+ * then keeps the fastest with insta_tuning_set and returns it in *best (best_ms: its time per
+ * batch).  No reference counterpart. */
+int insta_autotune(insta_ctx* ctx, const insta_render_desc* reqs, int n, int repeats, insta_tuning* best, float* best_ms);
 /* Per-ray sample t and dt (device pointers, [h*w][max_out]) and counts [h*w]. */
 int insta_march_debug(insta_ctx* ctx, const insta_render_desc* req, int max_out, float* out_t, float* out_dt,
                       int32_t* out_n);

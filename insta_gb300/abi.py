@@ -25,7 +25,8 @@ EXPORTS = [
     "insta_density_grid_load", "insta_density_grid_reset", "insta_density_grid_update", "insta_density_grid_read",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
     "insta_field_eval", "insta_field_eval_training", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_train_loss", "insta_train_set_math", "insta_render", "insta_render_async", "insta_render_batch",
-    "insta_render_samples", "insta_march_debug", "insta_nearest_debug", "insta_raycast",
+    "insta_render_samples", "insta_tuning_set", "insta_tuning_get", "insta_autotune", "insta_march_debug", "insta_nearest_debug",
+    "insta_raycast",
     "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
     "insta_server_release", "insta_server_error",
 ]
@@ -50,7 +51,7 @@ class DensityUpdateDesc(C.Structure):
 
 class AdamConfig(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
-                ("l2_reg", C.c_float), ("ema_decay", C.c_float)]
+                ("l2_reg", C.c_float), ("ema_decay", C.c_float), ("loss_scale", C.c_float)]
 
 
 LOSS_TYPES = {"l2": 0, "l1": 1, "mape": 2, "smape": 3, "huber": 4, "logl1": 5, "relativel2": 6}
@@ -98,7 +99,12 @@ class RenderDesc(C.Structure):
                 ("focal_length", C.c_float * 2), ("screen_center", C.c_float * 2), ("camera", C.c_float * 12),
                 ("cone_angle", C.c_float), ("min_transmittance", C.c_float), ("spp", C.c_uint32),
                 ("snap_to_pixel_centers", C.c_uint32), ("max_samples_per_ray", C.c_uint32), ("linear_colors", C.c_uint32),
-                ("extra_dims", C.c_void_p)]
+                ("extra_dims", C.c_void_p), ("out_samples", C.c_void_p)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("max_steps_per_round", C.c_uint32), ("sort_cell_bits", C.c_uint32), ("mlp_ctas_per_sm", C.c_uint32),
+                ("deform_blocks_per_sm", C.c_uint32)]
 
 
 _lib = None
@@ -151,6 +157,9 @@ def load(path: Path | None = None):
             "insta_render_async": [vp, C.POINTER(RenderDesc), vp, vp],
             "insta_render_batch": [vp, C.POINTER(RenderDesc), C.c_int, C.POINTER(vp), C.POINTER(vp)],
             "insta_render_samples": [vp, C.POINTER(u64)],
+            "insta_tuning_set": [vp, C.POINTER(Tuning)],
+            "insta_tuning_get": [vp, C.POINTER(Tuning)],
+            "insta_autotune": [vp, C.POINTER(RenderDesc), C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_float)],
             "insta_march_debug": [vp, C.POINTER(RenderDesc), C.c_int, vp, vp, vp],
             "insta_nearest_debug": [vp, C.c_int, C.c_int, vp, i64, vp],
             "insta_raycast": [vp, C.POINTER(RenderDesc), C.c_int, vp, vp, vp],
@@ -355,9 +364,11 @@ class Context:
         """insta_train_set_math: TF32 tensor-core layer products in the backward (else FP32)."""
         self._check(self.lib.insta_train_set_math(self.h, 1 if tf32 else 0))
 
-    def adam_step(self, avatar, grad, learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6, ema_decay=0.0):
-        """insta_adam_step; ema_decay > 0 adds the Ema wrapper (its average becomes the field's parameters)."""
-        cfg = AdamConfig(learning_rate, beta1, beta2, epsilon, l2_reg, ema_decay)
+    def adam_step(self, avatar, grad, learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6, ema_decay=0.0,
+                  loss_scale=1.0):
+        """insta_adam_step; ema_decay > 0 adds the Ema wrapper (its average becomes the field's parameters);
+        loss_scale is the factor the gradient carries (128 for gradients from insta_train_loss)."""
+        cfg = AdamConfig(learning_rate, beta1, beta2, epsilon, l2_reg, ema_decay, loss_scale)
         self._check(self.lib.insta_adam_step(self.h, avatar, _addr(grad), C.byref(cfg)))
 
     _LOSS_PTRS = ("rays", "target", "background", "exposure", "depth", "seg_mask", "mean_density", "rays_counter", "ray_indices",
@@ -383,7 +394,7 @@ class Context:
 
     @staticmethod
     def render_desc(avatar, frame, width, height, focal, cam, cone_angle=1 / 256, spp=0, min_transmittance=0.01,
-                    max_samples=1024, snap=True, linear_colors=False, extra_dims=None) -> RenderDesc:
+                    max_samples=1024, snap=True, linear_colors=False, extra_dims=None, out_samples=None) -> RenderDesc:
         r = RenderDesc()
         r.avatar, r.frame, r.width, r.height = avatar, frame, width, height
         r.focal_length[:] = [float(focal[0]), float(focal[1])]
@@ -394,6 +405,7 @@ class Context:
         r.spp, r.snap_to_pixel_centers, r.max_samples_per_ray = spp, int(snap), max_samples
         r.linear_colors = int(linear_colors)
         r.extra_dims = None if extra_dims is None else extra_dims.ctypes.data
+        r.out_samples = None if out_samples is None else _addr(out_samples).value
         return r
 
     def render(self, req: RenderDesc, out_rgba, out_depth):
@@ -410,6 +422,24 @@ class Context:
         pr = (C.c_void_p * n)(*[_addr(b).value for b in out_rgba])
         pd = (C.c_void_p * n)(*[_addr(b).value for b in out_depth])
         self._check(self.lib.insta_render_batch(self.h, arr, n, pr, pd))
+
+    def tuning_set(self, max_steps_per_round=0, sort_cell_bits=0, mlp_ctas_per_sm=0, deform_blocks_per_sm=0):
+        """insta_tuning_set: the wavefront's launch shapes (0 keeps a field's built-in choice)."""
+        t = Tuning(max_steps_per_round, sort_cell_bits, mlp_ctas_per_sm, deform_blocks_per_sm)
+        self._check(self.lib.insta_tuning_set(self.h, C.byref(t)))
+
+    def tuning_get(self) -> dict:
+        t = Tuning()
+        self._check(self.lib.insta_tuning_get(self.h, C.byref(t)))
+        return {f: int(getattr(t, f)) for f, _ in Tuning._fields_}
+
+    def autotune(self, reqs, repeats=3):
+        """insta_autotune over a list of RenderDesc; returns (tuning dict, ms per batch)."""
+        n = len(reqs)
+        arr = (RenderDesc * n)(*reqs)
+        t, ms = Tuning(), C.c_float(0)
+        self._check(self.lib.insta_autotune(self.h, arr, n, repeats, C.byref(t), C.byref(ms)))
+        return {f: int(getattr(t, f)) for f, _ in Tuning._fields_}, float(ms.value)
 
     def render_samples(self) -> int:
         v = C.c_uint64(0)

@@ -73,7 +73,7 @@ struct Field {
     uint64_t n_params = 0;
     // training: FP32 master weights (from the FP16 parameters at the first backward after a
     // load), Adam moments, the optimizer's step count and its FP16 output
-    DevBuf w32, adam_m, adam_v, w16, ema;
+    DevBuf w32, adam_m, adam_v, adam_steps, w16, ema;   // adam_steps: per hash-table entry
     // with an Ema the field's parameters are the average; the training weights' own FP16 copy,
     // weight image and view serve insta_field_eval_training
     DevBuf train_params, train_image, w16_train;
@@ -149,6 +149,9 @@ struct insta_ctx {
     uint32_t* host_alive = nullptr;      // pinned: alive rays per request slot (serving)
     uint32_t host_alive_n = 0;
     int sms = 0;
+    // launch shapes of the render wavefront (insta_tuning_set / insta_autotune); zero = built-in
+    insta_tuning tune{};
+    DevBuf tune_rgba, tune_depth;   // insta_autotune's device outputs
     // statistics: kernel launches issued by the library, optional per-stage CUDA-event timing
     uint64_t launches = 0;
     bool timing = false;
@@ -461,12 +464,17 @@ void check_request(const insta_render_desc* r) {
         fail(INSTA_ERR_INVALID_ARG, "bad resolution %dx%d", r->width, r->height);
     if (!(r->focal_length[0] > 0.f) || !(r->focal_length[1] > 0.f)) fail(INSTA_ERR_INVALID_ARG, "focal length must be positive");
     if (r->cone_angle < 0.f) fail(INSTA_ERR_INVALID_ARG, "cone_angle must be >= 0");
+    if (r->out_samples && !is_device_ptr(r->out_samples)) fail(INSTA_ERR_INVALID_ARG, "out_samples must be device memory");
 }
 
 // Largest number of samples one round may produce (bounds the per-sample scratch, ~160 B each).
 constexpr uint64_t kMaxRoundSamples = 32ull << 20;
 constexpr uint32_t kMaxSteps = 32;
 static_assert(kMaxSteps <= (1u << (32 - kStepShift)), "step index must fit beside the ray slot");
+
+// The wavefront's launch shapes under the context's tuning (zero fields: built-in choices).
+uint32_t tune_steps(const insta_ctx* ctx) { return ctx->tune.max_steps_per_round ? ctx->tune.max_steps_per_round : kMaxSteps; }
+uint32_t tune_cell_bits(const insta_ctx* ctx) { return ctx->tune.sort_cell_bits ? ctx->tune.sort_cell_bits : 18u; }
 static_assert((1u << 26) <= kRayMask + 1u, "ray slots (at most 2^26 pixels per batch) must fit below the step index");
 
 bool same_field_layout(const Field& a, const Field& b) {
@@ -488,6 +496,7 @@ ReqView request_view(insta_ctx* ctx, const insta_render_desc& r, Avatar& a, Fram
     v.table = a.field.view.table;
     v.mlp = a.field.view.mlp_smem;
     v.bitfield = (const uint8_t*)f.bitfield.p;
+    v.out_samples = r.out_samples;
     v.tiles_x = ((uint32_t)r.width + 7) / 8;
     v.tiles = v.tiles_x * (((uint32_t)r.height + 3) / 4);
     return v;
@@ -501,6 +510,7 @@ ReqView request_view(insta_ctx* ctx, const insta_render_desc& r, Avatar& a, Fram
 struct WaveRun {
     insta_ctx* ctx = nullptr;
     uint32_t n_slots = 0;
+    uint32_t steps_max = kMaxSteps;   // samples per alive ray per round, at most
     uint64_t round_cap = 0, cap_samples = 0;
     WaveArgs W{};
     MlpArgs M{};
@@ -520,9 +530,10 @@ struct WaveRun {
         const FieldView& fv = field.view;
         const TilePlan& P = field.plan;
         Wave& w = ctx->wave;
-        round_cap = std::min<uint64_t>(max_rays * kMaxSteps, kMaxRoundSamples);
+        steps_max = tune_steps(ctx);
+        round_cap = std::min<uint64_t>(max_rays * steps_max, kMaxRoundSamples);
         cap_samples = (round_cap + (uint64_t)slots * 128 + 127) / 128 * 128;
-        const uint32_t cell_bits = sort_cell_bits(slots);
+        const uint32_t cell_bits = sort_cell_bits(slots, tune_cell_bits(ctx));
         const uint64_t n_bins = (uint64_t)slots << cell_bits;
         if (w.cap_rays < max_rays) {
             for (int b = 0; b < 2; ++b)
@@ -642,7 +653,7 @@ struct WaveRun {
         B.n_alive_in = counters + (cur ^ 1); B.n_alive_out = counters + cur;
         A.n_init = B.n_init = 0; A.init_tile = B.init_tile = nullptr; A.init_slot = B.init_slot = nullptr;
         A.steps = B.steps = 0;
-        std::vector<unsigned char> key(sizeof(WaveArgs) * 2 + sizeof(MlpArgs) + 16);
+        std::vector<unsigned char> key(sizeof(WaveArgs) * 2 + sizeof(MlpArgs) + 16 + sizeof(insta_tuning));
         std::memcpy(key.data(), &A, sizeof(WaveArgs));
         std::memcpy(key.data() + sizeof(WaveArgs), &B, sizeof(WaveArgs));
         std::memcpy(key.data() + 2 * sizeof(WaveArgs), &M, sizeof(MlpArgs));
@@ -650,6 +661,7 @@ struct WaveRun {
         std::memcpy(key.data() + 2 * sizeof(WaveArgs) + sizeof(MlpArgs) + 8, &max_rounds, 4);
         const uint32_t grid_tiles = (uint32_t)(cap_samples / 128);
         std::memcpy(key.data() + 2 * sizeof(WaveArgs) + sizeof(MlpArgs) + 12, &grid_tiles, 4);
+        std::memcpy(key.data() + 2 * sizeof(WaveArgs) + sizeof(MlpArgs) + 16, &ctx->tune, sizeof(insta_tuning));
         if (!ctx->loop_exec || key != ctx->loop_key) {
             if (ctx->loop_exec) { cudaGraphExecDestroy(ctx->loop_exec); ctx->loop_exec = nullptr; }
             if (ctx->loop_graph) { cudaGraphDestroy(ctx->loop_graph); ctx->loop_graph = nullptr; }
@@ -671,12 +683,12 @@ struct WaveRun {
             cudaError_t e = cudaSuccess;
             for (int half = 0; half < 2 && e == cudaSuccess; ++half) {
                 const WaveArgs& R = half ? B : A;
-                if (e == cudaSuccess) e = launch_round_begin(R.n_alive_in, R.n_alive_out, R.n_samples_round, ctx->loop_state, round_cap, kMaxSteps,
+                if (e == cudaSuccess) e = launch_round_begin(R.n_alive_in, R.n_alive_out, R.n_samples_round, ctx->loop_state, round_cap, steps_max,
                                                              ctx->stream);
                 if (e == cudaSuccess) e = launch_march(R, ctx->stream);
                 if (e == cudaSuccess) e = launch_sort_samples(R, ctx->stream);
-                if (e == cudaSuccess) e = launch_deform_encode(R, ctx->stream);
-                if (e == cudaSuccess) e = launch_mlp(M, grid_tiles, ctx->stream);
+                if (e == cudaSuccess) e = launch_deform_encode(R, ctx->tune.deform_blocks_per_sm, ctx->stream);
+                if (e == cudaSuccess) e = launch_mlp(M, grid_tiles, ctx->stream, ctx->tune.mlp_ctas_per_sm);
                 if (e == cudaSuccess) e = launch_composite(R, ctx->stream);
             }
             if (e == cudaSuccess) e = launch_round_end(B.n_alive_out, ctx->loop_state + 1, ctx->loop_rounds_total, max_rounds, cond, ctx->stream);
@@ -695,7 +707,7 @@ struct WaveRun {
     // Without read_back the host does not wait: n_alive stays an upper bound (rays only finish),
     // and the next round's kernels take the count from the device.
     void round(bool read_back = true) {
-        const uint32_t steps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(kMaxSteps, round_cap / std::max(1u, n_alive)));
+        const uint32_t steps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(steps_max, round_cap / std::max(1u, n_alive)));
         W.steps = steps;
         W.rays_in = rays(cur);
         W.rays_out = rays(cur ^ 1);
@@ -705,8 +717,8 @@ struct WaveRun {
         CK(cudaMemsetAsync(counters + 2, 0, 4, ctx->stream));
         { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_march(W, ctx->stream)); }
         { Stage st(ctx, INSTA_STAGE_SORT, 4); CK(launch_sort_samples(W, ctx->stream)); }
-        { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 2); CK(launch_deform_encode(W, ctx->stream)); }
-        { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream)); }
+        { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 2); CK(launch_deform_encode(W, ctx->tune.deform_blocks_per_sm, ctx->stream)); }
+        { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream, ctx->tune.mlp_ctas_per_sm)); }
         { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }
         cur ^= 1;
         if (read_back) n_alive = read_alive();
@@ -794,9 +806,9 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
     if (n_extra) CK(cudaMemcpyAsync(ctx->extra.p, extra.data(), extra.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     run.upload_table(views.data());
     // the first round's step count needs the alive count only when all pixels could not take
-    // kMaxSteps samples each; otherwise the pixel count stands in for it (no host round trip)
-    run.start(slots.data(), tiles.data(), (uint32_t)n, total_pix * kMaxSteps > run.round_cap);
-    // while every ray can take kMaxSteps samples per round, the first round is issued without a
+    // steps_max samples each; otherwise the pixel count stands in for it (no host round trip)
+    run.start(slots.data(), tiles.data(), (uint32_t)n, total_pix * run.steps_max > run.round_cap);
+    // while every ray can take steps_max samples per round, the first round is issued without a
     // host read of its alive count (most frames finish in two rounds: one host wait, not two)
     uint32_t round = 0;
     if (!ctx->timing && run.n_alive > 0) {
@@ -804,7 +816,7 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
         // host-driven rounds below, which run the same kernels
         run.device_rounds(max_spr + 2);
     } else {
-        if (total_pix * kMaxSteps <= run.round_cap && run.n_alive > 0) {
+        if (total_pix * run.steps_max <= run.round_cap && run.n_alive > 0) {
             run.round(false);
             ++round;
         }
@@ -937,7 +949,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     for (auto& kv : ctx->avatars) {
         Avatar& a = *kv.second;
         for (DevBuf* b : {&a.faces, &a.mask, &a.adjacency, &a.canon_verts, &a.canon_area, &a.canon_frames, &a.frame_table,
-                          &a.field.params, &a.field.image, &a.density_grid, &a.field.w32, &a.field.adam_m, &a.field.adam_v, &a.field.w16, &a.field.ema, &a.field.train_params,
+                          &a.field.params, &a.field.image, &a.density_grid, &a.field.w32, &a.field.adam_m, &a.field.adam_v, &a.field.adam_steps, &a.field.w16, &a.field.ema, &a.field.train_params,
                           &a.field.train_image, &a.field.w16_train})
             ctx->release(*b);
         for (auto& f : a.frames)
@@ -1590,13 +1602,18 @@ int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_a
         Field& fd = a.field;
         if (!fd.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", avatar);
         ensure_master(ctx, fd);
+        if (!(cfg->ema_decay >= 0.f && cfg->ema_decay < 1.f)) fail(INSTA_ERR_INVALID_ARG, "ema_decay must be in [0, 1)");
+        if (!(cfg->loss_scale >= 0.f) || isinf(cfg->loss_scale)) fail(INSTA_ERR_INVALID_ARG, "loss_scale must be finite and >= 0");
+        const float loss_scale = cfg->loss_scale > 0.f ? cfg->loss_scale : 1.f;
+        const uint64_t n_matrix = field_layout(fd.desc).table_off;
         if (fd.adam_step == 0) {
             ctx->alloc(fd.adam_m, fd.n_params * 4);
             ctx->alloc(fd.adam_v, fd.n_params * 4);
+            ctx->alloc(fd.adam_steps, (fd.n_params - n_matrix) * 4);
             CK(cudaMemsetAsync(fd.adam_m.p, 0, fd.n_params * 4, ctx->stream));
             CK(cudaMemsetAsync(fd.adam_v.p, 0, fd.n_params * 4, ctx->stream));
+            CK(cudaMemsetAsync(fd.adam_steps.p, 0, (fd.n_params - n_matrix) * 4, ctx->stream));
         }
-        if (!(cfg->ema_decay >= 0.f && cfg->ema_decay < 1.f)) fail(INSTA_ERR_INVALID_ARG, "ema_decay must be in [0, 1)");
         ctx->alloc(fd.w16, fd.n_params * 2);
         const uint32_t step = ++fd.adam_step;
         float* ema = nullptr;
@@ -1610,8 +1627,9 @@ int insta_adam_step(insta_ctx* ctx, int avatar, const float* grad, const insta_a
         if (ema) ctx->alloc(fd.w16_train, fd.n_params * 2);
         {
             Stage st(ctx, INSTA_STAGE_TRAIN, 1);
-            CK(launch_adam(fd.n_params, (float*)fd.w32.p, (float*)fd.adam_m.p, (float*)fd.adam_v.p, grad, cfg->learning_rate, cfg->beta1,
-                           cfg->beta2, cfg->epsilon, cfg->l2_reg, step, ema, cfg->ema_decay, fd.ema_step, (__half*)fd.w16.p,
+            CK(launch_adam(fd.n_params, n_matrix, (float*)fd.w32.p, (float*)fd.adam_m.p, (float*)fd.adam_v.p, (uint32_t*)fd.adam_steps.p,
+                           grad, loss_scale, cfg->learning_rate, cfg->beta1, cfg->beta2, cfg->epsilon, cfg->l2_reg, step, ema,
+                           cfg->ema_decay, fd.ema_step, (__half*)fd.w16.p,
                            ema ? (__half*)fd.w16_train.p : nullptr, ctx->stream));
         }
         if (ema) {
@@ -1711,6 +1729,99 @@ int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples) {
         unsigned long long v = 0;
         CK(cudaMemcpy(&v, ctx->sample_counter, sizeof(v), cudaMemcpyDeviceToHost));
         *n_samples = v;
+    });
+}
+
+int insta_tuning_set(insta_ctx* ctx, const insta_tuning* t) {
+    return guarded(ctx, [&] {
+        if (!t) fail(INSTA_ERR_INVALID_ARG, "null tuning");
+        if (t->max_steps_per_round > kMaxSteps) fail(INSTA_ERR_INVALID_ARG, "max_steps_per_round must be 0..%u", kMaxSteps);
+        if (t->sort_cell_bits && (t->sort_cell_bits < 12 || t->sort_cell_bits > 21 || t->sort_cell_bits % 3))
+            fail(INSTA_ERR_INVALID_ARG, "sort_cell_bits must be 0 or one of 12, 15, 18, 21");
+        if (t->mlp_ctas_per_sm > 4) fail(INSTA_ERR_INVALID_ARG, "mlp_ctas_per_sm must be 0..4");
+        if (t->deform_blocks_per_sm > 64) fail(INSTA_ERR_INVALID_ARG, "deform_blocks_per_sm must be 0..64");
+        ctx->tune = *t;
+    });
+}
+
+int insta_tuning_get(insta_ctx* ctx, insta_tuning* t) {
+    return guarded(ctx, [&] {
+        if (!t) fail(INSTA_ERR_INVALID_ARG, "null output");
+        *t = ctx->tune;
+    });
+}
+
+int insta_autotune(insta_ctx* ctx, const insta_render_desc* reqs, int n, int repeats, insta_tuning* best, float* best_ms) {
+    return guarded(ctx, [&] {
+        if (!reqs || n <= 0 || (uint32_t)n > kMaxRequests) fail(INSTA_ERR_INVALID_ARG, "bad request list");
+        if (repeats < 1 || repeats > 64) fail(INSTA_ERR_INVALID_ARG, "repeats must be 1..64");
+        uint64_t px = 0;
+        for (int i = 0; i < n; ++i) {
+            check_request(reqs + i);
+            px += (uint64_t)reqs[i].width * reqs[i].height;
+        }
+        ctx->alloc(ctx->tune_rgba, px * 16);
+        ctx->alloc(ctx->tune_depth, px * 4);
+        std::vector<float*> o_rgba((size_t)n), o_depth((size_t)n);
+        {
+            uint64_t off = 0;
+            for (int i = 0; i < n; ++i) {
+                o_rgba[(size_t)i] = (float*)ctx->tune_rgba.p + off * 4;
+                o_depth[(size_t)i] = (float*)ctx->tune_depth.p + off;
+                off += (uint64_t)reqs[i].width * reqs[i].height;
+            }
+        }
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        const bool timing = ctx->timing;
+        ctx->timing = false;   // the timed path: the whole loop as one graph launch
+        auto time_one = [&](const insta_tuning& t) {
+            ctx->tune = t;
+            render_batch(ctx, reqs, n, o_rgba.data(), o_depth.data());   // untimed: graph (re)built
+            std::vector<float> ms((size_t)repeats);
+            for (int k = 0; k < repeats; ++k) {
+                CK(cudaEventRecord(e0, ctx->stream));
+                render_batch(ctx, reqs, n, o_rgba.data(), o_depth.data());
+                CK(cudaEventRecord(e1, ctx->stream));
+                CK(cudaEventSynchronize(e1));
+                CK(cudaEventElapsedTime(&ms[(size_t)k], e0, e1));
+            }
+            std::sort(ms.begin(), ms.end());
+            return ms[ms.size() / 2];
+        };
+        insta_tuning cur = ctx->tune;
+        float cur_ms = 0.f;
+        try {
+            cur_ms = time_one(cur);
+            const std::vector<uint32_t> cands[4] = {{8, 16, 24, 32}, {15, 18, 21}, {1, 2, 3, 4}, {8, 12, 16, 24}};
+            for (int pass = 0; pass < 2; ++pass) {
+                bool moved = false;
+                for (int f = 0; f < 4; ++f) {
+                    for (uint32_t v : cands[f]) {
+                        insta_tuning t = cur;
+                        uint32_t* field = f == 0 ? &t.max_steps_per_round : f == 1 ? &t.sort_cell_bits : f == 2 ? &t.mlp_ctas_per_sm
+                                                                                                       : &t.deform_blocks_per_sm;
+                        if (*field == v) continue;
+                        *field = v;
+                        const float ms = time_one(t);
+                        if (ms < cur_ms * 0.99f) { cur = t; cur_ms = ms; moved = true; }
+                    }
+                }
+                if (!moved) break;
+            }
+        } catch (...) {
+            ctx->timing = timing;
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        ctx->timing = timing;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ctx->tune = cur;
+        if (best) *best = cur;
+        if (best_ms) *best_ms = cur_ms;
     });
 }
 

@@ -38,6 +38,7 @@ struct ReqView {
     const float* extra;         // n_extra floats on the device, or null (zeros)
     float* out_rgba;
     float* out_depth;
+    uint32_t* out_samples;      // device: samples composited per pixel, or null
     uint32_t tiles_x;           // 8x4-pixel ray tiles per image row
     uint32_t tiles;             // ray tiles of the image
 };
@@ -153,7 +154,7 @@ cudaError_t launch_canonical_map_coords(const FrameView* frames_dev, uint32_t n_
 cudaError_t launch_ray_init(const WaveArgs& a, uint32_t total_tiles, cudaStream_t s);
 cudaError_t launch_march(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s);
-cudaError_t launch_deform_encode(const WaveArgs& a, cudaStream_t s);
+cudaError_t launch_deform_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s);
 cudaError_t launch_composite(const WaveArgs& a, cudaStream_t s);
 // generate_training_samples_nerf on caller-supplied rays (see insta_training_samples).
 struct TrainArgs {
@@ -203,8 +204,9 @@ size_t train_scratch_floats(const TrainShape& t, uint32_t n);
 cudaError_t launch_field_train(struct cublasContext* h, const FieldView& fv, const TrainShape& t, const float* w32, const float* coords,
                                uint32_t stride, uint32_t n, const float* dl_dout, float* out4, float* grad, float* scratch,
                                cudaStream_t s);
-cudaError_t launch_adam(size_t n, float* w, float* m, float* v, const float* g, float lr, float b1, float b2, float eps, float l2,
-                        uint32_t step, float* ema, float decay, uint32_t ema_step, __half* w16, __half* w16_train, cudaStream_t s);
+cudaError_t launch_adam(size_t n, size_t n_matrix, float* w, float* m, float* v, uint32_t* table_steps, const float* g, float loss_scale,
+                        float lr, float b1, float b2, float eps, float l2, uint32_t step, float* ema, float decay, uint32_t ema_step,
+                        __half* w16, __half* w16_train, cudaStream_t s);
 cudaError_t launch_half_to_float(size_t n, const void* a, float* b, cudaStream_t s);
 cudaError_t launch_train_loss(const ::insta_train_loss_desc& d, uint32_t* base_scratch, cudaStream_t s);
 cudaError_t launch_raycast(const RenderView& rv, const FrameView& fr, const float* center, int color_normal, float* out_rgba,

@@ -52,7 +52,8 @@ struct MlpArgs {
     uint32_t* err;
 };
 
-cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s);
+// ctas_per_sm: 0 = as many as shared memory lets reside (at most 4)
+cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm = 0);
 
 struct TileSmem {
     alignas(1024) uint8_t stage[2][128 * 64 * 2];   // input tile records (hash + SH), double-buffered

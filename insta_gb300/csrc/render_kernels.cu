@@ -81,6 +81,7 @@ __global__ void ray_init_kernel(const __grid_constant__ WaveArgs A, uint32_t tot
             idx = y * w + x;
             reinterpret_cast<float4*>(R.out_rgba)[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
             R.out_depth[idx] = 1e10f;
+            if (R.out_samples) R.out_samples[idx] = 0u;
             alive = ray_init(R.rv, x, y, R.bitfield, r);
         }
     }
@@ -604,7 +605,7 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
             bool done = m < steps;
             float4 rgba = rc;
             float depth = rd.x, maxw = rb.w;
-            uint32_t j = 0;
+            uint32_t j = 0, used = m;   // samples composited this round
             for (; j < m; ++j) {
                 const uint32_t s = A.sample_index[(size_t)j * n_alive + r];
                 float o[4];
@@ -632,12 +633,14 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
                     const float a = rgba.w;
                     rgba.x /= a; rgba.y /= a; rgba.z /= a; rgba.w /= a;
                     done = true;
+                    used = j + 1;
                     break;
                 }
             }
             const uint32_t ns = __float_as_uint(rd.z) + m;
             if (done) {
                 write_pixel(R.rv, R.out_rgba, R.out_depth, __float_as_uint(rd.y), rgba, depth);
+                if (R.out_samples) R.out_samples[__float_as_uint(rd.y)] = __float_as_uint(rd.z) + used;
             } else {
                 keep = true;
                 rb.w = maxw;
@@ -863,13 +866,14 @@ cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_deform_encode(const WaveArgs& a, cudaStream_t s) {
-    nearest_stage_kernel<<<sm_count() * 16, 256, 0, s>>>(a);
-    map_encode_kernel<<<sm_count() * 16, 256, 0, s>>>(a);
+cudaError_t launch_deform_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s) {
+    const uint32_t bps = blocks_per_sm ? blocks_per_sm : 16u;
+    nearest_stage_kernel<<<sm_count() * bps, 256, 0, s>>>(a);
+    map_encode_kernel<<<sm_count() * bps, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s) {
+cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm) {
     size_t smem = mlp_smem_bytes(a.plan);
     cudaError_t e = cudaFuncSetAttribute(mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -883,6 +887,7 @@ cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s) {
     cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
     int per_sm = smem_sm / (int)(smem + (size_t)reserved);
     per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
+    if (ctas_per_sm && (int)ctas_per_sm < per_sm) per_sm = (int)ctas_per_sm;
     uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
     if (max_tiles < grid) grid = max_tiles ? max_tiles : 1;
     mlp_kernel<<<grid, 128, smem, s>>>(a);

@@ -159,24 +159,43 @@ __global__ void __launch_bounds__(256) hash_backward_kernel(FieldView fv, const 
     }
 }
 
-// Adam (the optimizer the INSTA configuration nests in its Ema, configs/nerf/main.json): FP32
-// master weights, first and second moments, L2 regularisation added to the gradient, bias
-// correction.  With an Ema (ema != nullptr) the bias-corrected running average of the weights
-// (e_old scaled by decay * debias_old, plus (1 - decay) w, over debias_new) is kept in FP32 and
-// written as the FP16 parameters (the weights themselves to w16_train); without one the weights
-// themselves are the FP16 parameters.
-__global__ void __launch_bounds__(256) adam_kernel(size_t n, float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                                                   const float* __restrict__ g, float lr, float b1, float b2, float eps, float l2,
-                                                   float c1, float c2, float* __restrict__ ema, float decay, float debias_old,
-                                                   float debias_new, __half* __restrict__ w16, __half* __restrict__ w16_train) {
+// Adam (the optimizer the INSTA configuration nests in its Ema, configs/nerf/main.json), in the
+// form tiny-cuda-nn's Adam takes (absent here, restated from its published behaviour): the
+// gradient is first divided by the loss scale the loss kernel multiplied in (LOSS_SCALE, 128 in
+// train_nerf_step); the MLP weights (the first n_matrix parameters, "matrix" parameters) get the
+// L2 term l2 * w and step every call; a hash-table entry whose gradient is exactly zero is left
+// alone (weights, moments and its own step count unchanged: sparse updates of the table), and
+// no L2 term is added to table entries.  The step uses the bias correction folded into the rate
+// (Kingma & Ba, "Adam", sec. 2: lr_t = lr sqrt(1 - b2^t) / (1 - b1^t), w -= lr_t m / (sqrt(v) + eps))
+// with t the parameter's own step count.  With an Ema (ema != nullptr) the bias-corrected running
+// average of the weights (e_old scaled by decay * debias_old, plus (1 - decay) w, over debias_new)
+// is kept in FP32 for every parameter and written as the FP16 parameters (the weights themselves
+// to w16_train); without one the weights themselves are the FP16 parameters.
+__global__ void __launch_bounds__(256) adam_kernel(size_t n, size_t n_matrix, float* __restrict__ w, float* __restrict__ m,
+                                                   float* __restrict__ v, uint32_t* __restrict__ table_steps,
+                                                   const float* __restrict__ g, float inv_loss_scale, float lr, float b1, float b2,
+                                                   float eps, float l2, float lr_matrix, float* __restrict__ ema, float decay,
+                                                   float debias_old, float debias_new, __half* __restrict__ w16,
+                                                   __half* __restrict__ w16_train) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const float gi = g[i] + l2 * w[i];
-        const float mi = b1 * m[i] + (1.f - b1) * gi;
-        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
-        m[i] = mi;
-        v[i] = vi;
-        const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-        w[i] = wi;
+        float gi = g[i] * inv_loss_scale;
+        float wi = w[i];
+        const bool matrix = i < n_matrix;
+        if (matrix || gi != 0.f) {
+            float lr_t = lr_matrix;
+            if (matrix) {
+                gi += l2 * wi;
+            } else {
+                const uint32_t t = ++table_steps[i - n_matrix];
+                lr_t = lr * sqrtf(1.f - powf(b2, (float)t)) / (1.f - powf(b1, (float)t));
+            }
+            const float mi = b1 * m[i] + (1.f - b1) * gi;
+            const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+            m[i] = mi;
+            v[i] = vi;
+            wi = wi - lr_t * mi / (sqrtf(vi) + eps);
+            w[i] = wi;
+        }
         float out = wi;
         if (ema) {
             // the first averaged step is the weights themselves (debias_old = 0)
@@ -551,11 +570,13 @@ cudaError_t launch_field_train(cublasHandle_t h, const FieldView& fv, const Trai
     return okb ? cudaGetLastError() : cudaErrorUnknown;
 }
 
-cudaError_t launch_adam(size_t n, float* w, float* m, float* v, const float* g, float lr, float b1, float b2, float eps, float l2,
-                        uint32_t step, float* ema, float decay, uint32_t ema_step, __half* w16, __half* w16_train, cudaStream_t s) {
-    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+cudaError_t launch_adam(size_t n, size_t n_matrix, float* w, float* m, float* v, uint32_t* table_steps, const float* g, float loss_scale,
+                        float lr, float b1, float b2, float eps, float l2, uint32_t step, float* ema, float decay, uint32_t ema_step,
+                        __half* w16, __half* w16_train, cudaStream_t s) {
+    const float lr_matrix = lr * sqrtf(1.f - powf(b2, (float)step)) / (1.f - powf(b1, (float)step));
     const float debias_old = 1.f - powf(decay, (float)(ema_step - 1u)), debias_new = 1.f - powf(decay, (float)ema_step);
-    adam_kernel<<<grid_for(n), 256, 0, s>>>(n, w, m, v, g, lr, b1, b2, eps, l2, c1, c2, ema, decay, debias_old, debias_new, w16, w16_train);
+    adam_kernel<<<grid_for(n), 256, 0, s>>>(n, n_matrix, w, m, v, table_steps, g, 1.f / loss_scale, lr, b1, b2, eps, l2, lr_matrix, ema,
+                                            decay, debias_old, debias_new, w16, w16_train);
     return cudaGetLastError();
 }
 

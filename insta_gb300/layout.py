@@ -5,7 +5,7 @@ parameter vector out as: density MLP, rgb MLP, position (hash-grid)
 encoding, direction encoding (spherical harmonics, no parameters).  The
 tiny-cuda-nn internals of each block are not in the reference repository, so
 this library fixes its own block layout and the C++ side
-(``insta_gb300/csrc/field_layout.h``) computes the same offsets:
+(``field_layout`` in ``insta_gb300/csrc/insta_abi.cu``) computes the same offsets:
 
 * MLP layer ``k``: row-major ``[n_out][n_in]`` FP16 matrix, no bias;
 * hash level ``l``: ``scale_l = exp2(l * log2(b)) * N_min - 1`` (float),

@@ -210,6 +210,12 @@ class Snapshot:
     training_step: int = 0
     loss: float = 0.0
     config: dict = field(default_factory=dict)  # the network configuration (without "snapshot")
+    bounding_radius: float = 1.0               # Testbed::m_bounding_radius (testbed.h:488)
+    # the trainer's batch counters (Testbed::Nerf::Training::Counters, testbed.h:581-584), which
+    # load_snapshot reads without a default (testbed.cu:2975-2977)
+    rays_per_batch: int = 1 << 12
+    measured_batch_size: int = 0
+    measured_batch_size_before_compaction: int = 0
 
     @property
     def n_cascades(self) -> int:
@@ -264,16 +270,22 @@ def read_snapshot(src) -> Snapshot:
             raise ValueError("incompatible number of grid cascades")
         grid = g if g.size else None
     nerf = snap.get("nerf", {})
+    rgb = nerf.get("rgb", {})
     cfg = {k: v for k, v in doc.items() if k != "snapshot"}
     unit = {"min": [0.0, 0.0, 0.0], "max": [1.0, 1.0, 1.0]}
     return Snapshot(params=params, density_grid=grid, aabb=_box(snap.get("aabb", unit)), render_aabb=_box(snap.get("render_aabb", unit)),
                     aabb_scale=int(nerf.get("aabb_scale", 1)), training_step=int(snap.get("training_step", 0)),
-                    loss=float(snap.get("loss", 0.0)), config=cfg)
+                    loss=float(snap.get("loss", 0.0)), config=cfg, bounding_radius=float(snap.get("bounding_radius", 1.0)),
+                    rays_per_batch=int(rgb.get("rays_per_batch", 1 << 12)),
+                    measured_batch_size=int(rgb.get("measured_batch_size", 0)),
+                    measured_batch_size_before_compaction=int(rgb.get("measured_batch_size_before_compaction", 0)))
 
 
 def write_snapshot(dst, s: Snapshot) -> bytes:
-    """Testbed::save_snapshot's layout (FP16 parameters); returns the bytes and writes them to dst
-    when it is a path."""
+    """Testbed::save_snapshot's layout (FP16 parameters; testbed.cu:2916-2950): every key that
+    Testbed::load_snapshot reads (testbed.cu:2952-3016) is written, an empty density_grid_binary
+    standing for a grid that was never populated, as the reference allows.  Returns the bytes and
+    writes them to dst when it is a path."""
     snap = {
         "version": SNAPSHOT_FORMAT_VERSION,
         "params_type": "__half",
@@ -281,11 +293,14 @@ def write_snapshot(dst, s: Snapshot) -> bytes:
         "params_binary": np.ascontiguousarray(s.params, np.float16).tobytes(),
         "density_grid_size": GRID,
         "density_grid_binary": b"" if s.density_grid is None else np.ascontiguousarray(s.density_grid, np.float16).tobytes(),
-        "nerf": {"aabb_scale": int(s.aabb_scale)},
+        "nerf": {"aabb_scale": int(s.aabb_scale),
+                 "rgb": {"rays_per_batch": int(s.rays_per_batch), "measured_batch_size": int(s.measured_batch_size),
+                         "measured_batch_size_before_compaction": int(s.measured_batch_size_before_compaction)}},
         "training_step": int(s.training_step),
         "loss": float(s.loss),
         "aabb": {"min": [float(x) for x in s.aabb[0]], "max": [float(x) for x in s.aabb[1]]},
         "render_aabb": {"min": [float(x) for x in s.render_aabb[0]], "max": [float(x) for x in s.render_aabb[1]]},
+        "bounding_radius": float(s.bounding_radius),
     }
     doc = dict(s.config)
     doc["snapshot"] = snap

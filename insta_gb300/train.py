@@ -119,7 +119,7 @@ class TrainStep:
                        loss_output=self.loss)
         if n_samples > 0:
             ctx.field_backward(self.avatar, self.coords_out, self.stride, cfg.target_batch_size, self.dloss, self.grad)
-            ctx.adam_step(self.avatar, self.grad, **cfg.adam)
+            ctx.adam_step(self.avatar, self.grad, loss_scale=cfg.loss_scale, **cfg.adam)
         self.n_steps += 1
         self._last_kept = n_kept
         return {"rays_kept": n_kept, "samples": n_samples}

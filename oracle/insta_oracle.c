@@ -722,6 +722,17 @@ static inline float advance_to_next_voxel(float t, float cone, const float *pos,
     return t;
 }
 
+/* The march helpers above behind the C ABI, for the pin against the reference's own
+ * (oracle/ref_march_probe.cpp). */
+float orc_probe_calc_dt(float t, float cone) { return calc_dt(t, cone); }
+float orc_probe_warp_dt(float dt) { return warp_dt(dt); }
+float orc_probe_unwarp_dt(float dt) { return unwarp_dt(dt); }
+int orc_probe_mip_from_dt(float dt, const float *pos) { return mip_from_dt(dt, pos); }
+int orc_probe_occupied_at(const float *pos, const uint8_t *bf, int mip) { return occupied_at(pos, bf, mip); }
+float orc_probe_advance_to_next_voxel(float t, float cone, const float *pos, const float *dir, const float *idir, uint32_t res) {
+    return advance_to_next_voxel(t, cone, pos, dir, idir, res);
+}
+
 /* BoundingBox::ray_intersect (NGP/bounding_box.cuh:163-210), returns tmin or FLT_MAX */
 static float aabb_ray_tmin(const float *mn, const float *mx, const float *o, const float *d) {
     float tmin = (mn[0] - o[0]) / d[0], tmax = (mx[0] - o[0]) / d[0];

@@ -168,6 +168,14 @@ void orc_tbn(const orc_tri *t, float *m9);
 void orc_tri2projection(const orc_tri *t, float *M16);
 void orc_interpolate_transformation(const float *p, const int32_t *adj, const orc_tri *tris, uint32_t id, int invert, float *M16);
 void orc_transform(const float *p, const float *dir, const float *Mw, const float *Mc, float *out_p, float *out_d);
+/* march helpers (calc_dt, warp_dt / unwarp_dt, mip_from_dt, density_grid_occupied_at,
+ * advance_to_next_voxel of ngp/src/testbed_nerf.cu) */
+float orc_probe_calc_dt(float t, float cone);
+float orc_probe_warp_dt(float dt);
+float orc_probe_unwarp_dt(float dt);
+int orc_probe_mip_from_dt(float dt, const float *pos);
+int orc_probe_occupied_at(const float *pos, const uint8_t *bf, int mip);
+float orc_probe_advance_to_next_voxel(float t, float cone, const float *pos, const float *dir, const float *idir, uint32_t res);
 
 /* ---- half helpers ------------------------------------------------------ */
 uint16_t orc_f2h(float x);

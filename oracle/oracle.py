@@ -81,6 +81,14 @@ def lib():
         _lib.orc_morton3d.restype = C.c_uint32
         _lib.orc_num_threads.restype = C.c_int
         _lib.orc_occupancy_from_mesh.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_void_p]
+        for n in ("orc_probe_calc_dt", "orc_probe_warp_dt", "orc_probe_unwarp_dt", "orc_probe_advance_to_next_voxel"):
+            getattr(_lib, n).restype = C.c_float
+        _lib.orc_probe_calc_dt.argtypes = [C.c_float, C.c_float]
+        _lib.orc_probe_warp_dt.argtypes = [C.c_float]
+        _lib.orc_probe_unwarp_dt.argtypes = [C.c_float]
+        _lib.orc_probe_mip_from_dt.argtypes = [C.c_float, C.c_void_p]
+        _lib.orc_probe_occupied_at.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        _lib.orc_probe_advance_to_next_voxel.argtypes = [C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]
     return _lib
 
 
@@ -428,3 +436,60 @@ def pixel_offset(spp) -> np.ndarray:
 
 def num_threads() -> int:
     return lib().orc_num_threads()
+
+
+# ------------------------------------------------------------------ march helpers (pin tests)
+def march_bitfield() -> np.ndarray:
+    """A fixed, seed-free 8-mip occupancy bitfield for the march-helper pins: byte i is a
+    multiplicative hash of i (about half the bits set)."""
+    i = np.arange(8 * 128 ** 3 // 8, dtype=np.uint64)
+    return ((i * np.uint64(2654435761)) >> np.uint64(13)).astype(np.uint8)
+
+
+def march_helpers(lib_, cases: dict, bitfield: np.ndarray) -> dict:
+    """Run the march helpers of one library (the oracle's orc_probe_* or the reference's ref_*)
+    over the input arrays in `cases`; returns their outputs."""
+    pre = "orc_probe_" if hasattr(lib_, "orc_probe_calc_dt") else "ref_"
+    f = lambda n: getattr(lib_, pre + ("density_grid_occupied_at" if n == "occupied_at" and pre == "ref_" else n))
+    out = {}
+    out["calc_dt"] = np.array([f("calc_dt")(C.c_float(t), C.c_float(c)) for t, c in zip(cases["dt_t"], cases["dt_cone"])], np.float32)
+    out["warp_dt"] = np.array([f("warp_dt")(C.c_float(x)) for x in cases["warp_in"]], np.float32)
+    out["unwarp_dt"] = np.array([f("unwarp_dt")(C.c_float(x)) for x in cases["unwarp_in"]], np.float32)
+    mp = np.ascontiguousarray(cases["mip_pos"], np.float32)
+    out["mip_from_dt"] = np.array([f("mip_from_dt")(C.c_float(d), ptr(mp[i])) for i, d in enumerate(cases["mip_dt"])], np.int32)
+    op = np.ascontiguousarray(cases["occ_pos"], np.float32)
+    out["occupied_at"] = np.array([f("occupied_at")(ptr(op[i]), ptr(bitfield), int(m)) for i, m in enumerate(cases["occ_mip"])], np.int32)
+    ap, ad, ai = (np.ascontiguousarray(cases[k], np.float32) for k in ("adv_pos", "adv_dir", "adv_idir"))
+    out["advance"] = np.array([f("advance_to_next_voxel")(C.c_float(t), C.c_float(c), ptr(ap[i]), ptr(ad[i]), ptr(ai[i]), C.c_uint32(int(r)))
+                               for i, (t, c, r) in enumerate(zip(cases["adv_t"], cases["adv_cone"], cases["adv_res"]))], np.float32)
+    return out
+
+
+def march_cases(rng) -> dict:
+    """Seeded inputs for the march-helper pins: step sizes around both clamps, positions over all
+    cascades, rays in every direction octant (including axis-parallel ones) at every grid level."""
+    n = 2000
+    min_cone, max_cone = np.float32(1.73205080757 / 1024), np.float32(1.73205080757 / 1024 * 128)
+    t = np.concatenate([rng.uniform(0, 4, n // 2), np.exp(rng.uniform(np.log(1e-3), np.log(150.0), n // 2))]).astype(np.float32)
+    cone = rng.choice(np.array([0.0, 1 / 256, 1 / 128, 0.02], np.float32), n)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[np.arange(n // 10), rng.integers(0, 3, n // 10)] = 0.0   # a zero component: axis-parallel slabs
+    d /= np.maximum(np.linalg.norm(d, axis=1, keepdims=True), 1e-12)
+    with np.errstate(divide="ignore"):
+        idir = (np.float32(1) / d).astype(np.float32)
+    # occupancy lookups inside each mip's box [0.5 - 2^(m-1), 0.5 + 2^(m-1)] (the march never
+    # leaves it), a few just outside where the index is clamped
+    occ_mip = rng.integers(0, 8, n).astype(np.int32)
+    half = np.ldexp(0.5, occ_mip).astype(np.float64)[:, None]
+    occ_pos = (0.5 + rng.uniform(-1.0, 1.0, (n, 3)) * half * np.where(rng.random((n, 1)) < 0.02, 1.004, 0.999)).astype(np.float32)
+    return {
+        "dt_t": t, "dt_cone": cone,
+        "warp_in": rng.uniform(min_cone, max_cone, n).astype(np.float32),
+        "unwarp_in": rng.uniform(0, 1, n).astype(np.float32),
+        "mip_pos": rng.uniform(-1.5, 2.5, (n, 3)).astype(np.float32),
+        "mip_dt": np.exp(rng.uniform(np.log(1e-4), np.log(2.0), n)).astype(np.float32),
+        "occ_pos": occ_pos, "occ_mip": occ_mip,
+        "adv_t": rng.uniform(0.05, 2.0, n).astype(np.float32), "adv_cone": rng.choice(np.array([0.0, 1 / 256], np.float32), n),
+        "adv_pos": rng.uniform(0.0, 1.0, (n, 3)).astype(np.float32), "adv_dir": d, "adv_idir": idir,
+        "adv_res": rng.choice(np.array([128, 64, 32, 16, 8, 4, 2, 1], np.uint32), n),
+    }

@@ -1,12 +1,16 @@
-"""Generate tests/golden/reference_geometry.npz from the reference's own headers.
+"""Generate tests/golden/reference_geometry.npz and tests/golden/reference_march.npz from the
+reference's own code.
 
 Runs oracle/_ref/libinsta_ref.so -- Triangle::distance_sq, BoundingBox::distance_sq,
 Triangle::tbn, tri2projection, interpolate_transformation, transform_point/direction,
 closest_triangle, sobol, ld_random_val and ld_random_pixel_offset compiled for the host from
-the INSTA sources (oracle/build_ref.py) -- on seeded inputs and stores inputs and outputs.
+the INSTA headers, and the march helpers of instant-ngp/src/testbed_nerf.cu (calc_dt,
+warp_dt / unwarp_dt, mip_from_dt, density_grid_occupied_at, advance_to_next_voxel) compiled from
+the text of that file (oracle/build_ref.py) -- on seeded inputs and stores inputs and outputs.
 The oracle is then checked against these vectors on machines without the INSTA sources.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # both files
+    python tests/golden/make_golden.py --march    # reference_march.npz only
 """
 from __future__ import annotations
 
@@ -22,6 +26,7 @@ sys.path.insert(0, str(ROOT))
 from oracle import build_ref, oracle as O  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "reference_geometry.npz"
+OUT_MARCH = Path(__file__).resolve().parent / "reference_march.npz"
 F32P = C.POINTER(C.c_float)
 
 
@@ -33,6 +38,16 @@ def ref_lib():
     lib.ref_sobol.restype = C.c_uint32
     lib.ref_sobol.argtypes = [C.c_uint32, C.c_uint32]
     lib.ref_closest_triangle.restype = C.c_int
+    for n in ("ref_calc_dt", "ref_warp_dt", "ref_unwarp_dt", "ref_advance_to_next_voxel", "ref_distance_to_next_voxel",
+              "ref_calc_cone_angle"):
+        getattr(lib, n).restype = C.c_float
+    lib.ref_calc_dt.argtypes = [C.c_float, C.c_float]
+    lib.ref_warp_dt.argtypes = [C.c_float]
+    lib.ref_unwarp_dt.argtypes = [C.c_float]
+    lib.ref_calc_cone_angle.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float]
+    lib.ref_mip_from_dt.argtypes = [C.c_float, C.c_void_p]
+    lib.ref_density_grid_occupied_at.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+    lib.ref_advance_to_next_voxel.argtypes = [C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]
     return lib
 
 
@@ -126,5 +141,21 @@ def main():
     print(OUT, OUT.stat().st_size, "bytes")
 
 
+def march_main(lib=None):
+    """The march helpers on seeded inputs (oracle.march_cases) over oracle.march_bitfield()."""
+    lib = lib or ref_lib()
+    cases = O.march_cases(np.random.default_rng(77))
+    out = O.march_helpers(lib, cases, O.march_bitfield())
+    g = dict(cases)
+    g.update({"ref_" + k: v for k, v in out.items()})
+    # calc_cone_angle returns the constant whatever the cosine and focal length (:82-89)
+    g["cone_ref"] = np.array([lib.ref_calc_cone_angle(c, 1000.0, 1000.0, k) for c, k in zip(cases["warp_in"], cases["dt_cone"])],
+                             np.float32)
+    np.savez_compressed(OUT_MARCH, **g)
+    print(OUT_MARCH, OUT_MARCH.stat().st_size, "bytes")
+
+
 if __name__ == "__main__":
-    main()
+    if "--march" not in sys.argv:
+        main()
+    march_main()

@@ -18,6 +18,7 @@ STRUCTS = {
     "insta_adam_config": "AdamConfig",
     "insta_train_loss_desc": "TrainLossDesc",
     "insta_server_config": "ServerConfig",
+    "insta_tuning": "Tuning",
 }
 
 

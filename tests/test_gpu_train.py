@@ -122,36 +122,60 @@ def test_backward_accumulates_and_forward_only(ctx, field, oracle):
     assert np.abs(out.cpu().numpy() - ref_out).max() <= 1e-4 + 1e-4 * np.abs(ref_out).max()
 
 
-def numpy_adam(w, g, steps, lr, b1, b2, eps, l2):
+def numpy_adam(w, g, steps, lr, b1, b2, eps, l2, n_matrix, loss_scale=1.0, decay=None):
+    """FP32 NumPy restatement of insta_adam_step: gradient / loss_scale; L2 and a step every call
+    for the first n_matrix (MLP) parameters; table entries with a zero gradient skipped, the others
+    counting their own steps; lr sqrt(1 - b2^t) / (1 - b1^t) * m / (sqrt(v) + eps).  With decay the
+    Ema's bias-corrected average is returned beside the weights."""
     w = w.astype(np.float32).copy()
     m = np.zeros_like(w)
     v = np.zeros_like(w)
+    t_tab = np.zeros(w.size - n_matrix, np.int64)
+    e = None
     for t in range(1, steps + 1):
-        gi = g + np.float32(l2) * w
-        m = np.float32(b1) * m + np.float32(1 - b1) * gi
-        v = np.float32(b2) * v + np.float32(1 - b2) * gi * gi
-        c1, c2 = np.float32(1 - b1 ** t), np.float32(1 - b2 ** t)
-        w = w - np.float32(lr) * (m / c1) / (np.sqrt(v / c2) + np.float32(eps))
-    return w
+        gi = (g / np.float32(loss_scale)).astype(np.float32)
+        upd = np.ones(w.size, bool)
+        upd[n_matrix:] = gi[n_matrix:] != 0
+        gi[:n_matrix] += np.float32(l2) * w[:n_matrix]
+        t_tab[upd[n_matrix:]] += 1
+        tt = np.concatenate([np.full(n_matrix, t), np.maximum(t_tab, 1)]).astype(np.float64)
+        lr_t = (lr * np.sqrt(1 - b2 ** tt) / (1 - b1 ** tt)).astype(np.float32)
+        m_new = np.float32(b1) * m + np.float32(1 - b1) * gi
+        v_new = np.float32(b2) * v + np.float32(1 - b2) * gi * gi
+        w_new = w - lr_t * m_new / (np.sqrt(v_new) + np.float32(eps))
+        m, v, w = np.where(upd, m_new, m), np.where(upd, v_new, v), np.where(upd, w_new, w)
+        if decay is not None:
+            e = w.copy() if e is None else (e * np.float32(decay * (1 - decay ** (t - 1))) + np.float32(1 - decay) * w) / np.float32(1 - decay ** t)
+    return w if decay is None else (w, e)
 
 
-def test_adam_matches_numpy(ctx, field, oracle):
+@pytest.mark.parametrize("loss_scale", [1.0, 128.0])
+def test_adam_matches_numpy(ctx, field, oracle, loss_scale):
+    """Two Adam steps on a gradient that touches only part of the hash table (2000 points): the
+    field outputs match the oracle on a NumPy FP32 restatement; with loss_scale 128 the gradient
+    carries the factor, so the step equals the unscaled one; untouched table entries (zero
+    gradient) keep their values, the MLP weights all move."""
     fc, params, lay = field
     n = 2000
     c = coords(n, seed=6)
     g_out = np.random.default_rng(7).normal(size=(n, 4)).astype(np.float32)
     grad = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
-    ctx.field_backward(AVATAR, dev(c), 27, n, dev(g_out), grad)
+    ctx.field_backward(AVATAR, dev(c), 27, n, dev(g_out * np.float32(loss_scale)), grad)
     cfg = dict(learning_rate=1e-2, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6)
-    ctx.adam_step(AVATAR, grad, **cfg)
-    ctx.adam_step(AVATAR, grad, **cfg)          # second step: the moments carry over
+    ctx.adam_step(AVATAR, grad, loss_scale=loss_scale, **cfg)
+    ctx.adam_step(AVATAR, grad, loss_scale=loss_scale, **cfg)          # second step: the moments carry over
     cq = coords(1500, seed=8)
     out = torch.zeros((len(cq), 4), dtype=torch.float32, device="cuda")
     ctx.field_eval(AVATAR, dev(cq), 27, len(cq), out)
     ctx.sync()
     g = grad.cpu().numpy()
-    w_new = numpy_adam(params.astype(np.float32), g, 2, cfg["learning_rate"], cfg["beta1"], cfg["beta2"], cfg["epsilon"],
-                       cfg["l2_reg"]).astype(np.float16)
+    n_matrix = lay.table_offset
+    tab_zero = g[n_matrix:] == 0
+    assert tab_zero.any() and not tab_zero.all()
+    w32 = numpy_adam(params.astype(np.float32), g, 2, cfg["learning_rate"], cfg["beta1"], cfg["beta2"], cfg["epsilon"],
+                     cfg["l2_reg"], n_matrix, loss_scale)
+    assert np.array_equal(w32[n_matrix:][tab_zero], params.astype(np.float32)[n_matrix:][tab_zero])
+    w_new = w32.astype(np.float16)
     ref = oracle.field_eval(fc, w_new, cq)
     before = oracle.field_eval(fc, params, cq)
     got = out.cpu().numpy()
@@ -185,19 +209,8 @@ def test_adam_ema_matches_numpy(ctx, field, oracle):
     ctx.field_eval_training(AVATAR, dq, 27, len(cq), tc_out)
     ctx.sync()
     g = grad.cpu().numpy()
-    w = params.astype(np.float32)
-    m = np.zeros_like(w)
-    v = np.zeros_like(w)
-    e = None
-    for t in range(1, 4):
-        gi = g + np.float32(cfg["l2_reg"]) * w
-        m = np.float32(0.9) * m + np.float32(0.1) * gi
-        v = np.float32(0.99) * v + np.float32(0.01) * gi * gi
-        w = w - np.float32(1e-2) * (m / np.float32(1 - 0.9 ** t)) / (np.sqrt(v / np.float32(1 - 0.99 ** t)) + np.float32(1e-15))
-        if e is None:
-            e = w.copy()
-        else:
-            e = (e * np.float32(decay * (1 - decay ** (t - 1))) + np.float32(1 - decay) * w) / np.float32(1 - decay ** t)
+    w, e = numpy_adam(params.astype(np.float32), g, 3, cfg["learning_rate"], cfg["beta1"], cfg["beta2"], cfg["epsilon"],
+                      cfg["l2_reg"], lay.table_offset, decay=decay)
     ref_inf = oracle.field_eval(fc, e.astype(np.float16), cq)
     ref_train = oracle.field_eval(fc, w.astype(np.float16), cq)
     got_inf, got_train = inf_out.cpu().numpy(), train_out.cpu().numpy()

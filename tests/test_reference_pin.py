@@ -151,3 +151,49 @@ def test_live_reference_distance_and_traversal(oracle, ref):
         slot = ref.ref_closest_triangle(p(bvh.nodes), p(bvh.sorted), p(q[i]), C.byref(d))
         assert bvh.sorted["id"][slot] == ids[i]
         assert np.float32(np.sqrt(d2[i])) == np.float32(d.value)
+
+
+# ---------------------------------------------------------------- march helpers
+# calc_dt, warp_dt / unwarp_dt, mip_from_dt, density_grid_occupied_at and advance_to_next_voxel
+# (instant-ngp/src/testbed_nerf.cu:91-93,186-208,300-337,471-485) compiled from the reference
+# file's own text (oracle/ref_march_probe.cpp): the oracle's restatement, which the GPU march is
+# tested against bit for bit, must reproduce them bit for bit.
+GOLDEN_MARCH = Path(__file__).resolve().parent / "golden" / "reference_march.npz"
+MARCH_KEYS = ("calc_dt", "warp_dt", "unwarp_dt", "mip_from_dt", "occupied_at", "advance")
+
+
+def _bits(a):
+    a = np.asarray(a)
+    return a.view(np.uint32) if a.dtype == np.float32 else a
+
+
+def test_golden_march_helpers_bit_exact(oracle):
+    g = dict(np.load(GOLDEN_MARCH))
+    ours = oracle.march_helpers(oracle.lib(), g, oracle.march_bitfield())
+    for k in MARCH_KEYS:
+        assert (_bits(ours[k]) == _bits(g["ref_" + k])).all(), k
+    # the cases reach both clamps of calc_dt, every mip and every grid level of the DDA
+    dt = g["ref_calc_dt"]
+    assert (dt == dt.min()).sum() > 50 and (dt == dt.max()).sum() >= 10 and abs(dt.max() / dt.min() - 1024) < 1e-2
+    assert set(np.unique(g["ref_mip_from_dt"])) == set(range(7))
+    assert 0.2 < g["ref_occupied_at"].mean() < 0.8
+    # calc_cone_angle is the constant (the pixel-size variant is commented out in the reference)
+    assert (g["cone_ref"] == g["dt_cone"]).all()
+
+
+def test_live_reference_march_helpers(oracle, ref):
+    from oracle import oracle as O
+    for n in ("ref_calc_dt", "ref_warp_dt", "ref_unwarp_dt", "ref_advance_to_next_voxel"):
+        getattr(ref, n).restype = C.c_float
+    ref.ref_calc_dt.argtypes = [C.c_float, C.c_float]
+    ref.ref_warp_dt.argtypes = [C.c_float]
+    ref.ref_unwarp_dt.argtypes = [C.c_float]
+    ref.ref_mip_from_dt.argtypes = [C.c_float, C.c_void_p]
+    ref.ref_density_grid_occupied_at.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+    ref.ref_advance_to_next_voxel.argtypes = [C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]
+    cases = O.march_cases(np.random.default_rng(123))
+    bf = O.march_bitfield()
+    a = O.march_helpers(oracle.lib(), cases, bf)
+    b = O.march_helpers(ref, cases, bf)
+    for k in MARCH_KEYS:
+        assert (_bits(a[k]) == _bits(b[k])).all(), k

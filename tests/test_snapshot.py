@@ -72,3 +72,32 @@ def test_snapshot_fp32_params_and_errors():
         SN.read_snapshot(SN.packb(doc))
     with pytest.raises(ValueError):
         SN.read_snapshot(SN.packb({"encoding": {}}))
+
+
+# Every key Testbed::load_snapshot (instant-ngp/src/testbed.cu:2952-3016) reads from the snapshot
+# block, the ones without a default (operator[]) and the ones with (value()); the trainer's
+# deserialize reads params_binary.
+LOAD_SNAPSHOT_KEYS = [("version",), ("aabb",), ("render_aabb",), ("bounding_radius",), ("density_grid_size",),
+                      ("nerf", "rgb", "rays_per_batch"), ("nerf", "rgb", "measured_batch_size"),
+                      ("nerf", "rgb", "measured_batch_size_before_compaction"), ("nerf", "aabb_scale"),
+                      ("density_grid_binary",), ("training_step",), ("loss",), ("params_binary",)]
+
+
+@pytest.mark.parametrize("with_grid", [False, True])
+def test_written_snapshot_has_every_key_load_snapshot_reads(with_grid):
+    rng = np.random.default_rng(1)
+    s = SN.Snapshot(params=rng.normal(size=64).astype(np.float16),
+                    density_grid=rng.random(128 ** 3).astype(np.float16) if with_grid else None,
+                    aabb=(np.zeros(3, np.float32), np.ones(3, np.float32)), render_aabb=(np.zeros(3, np.float32), np.ones(3, np.float32)),
+                    aabb_scale=2, bounding_radius=0.75, rays_per_batch=4096, measured_batch_size=200000,
+                    measured_batch_size_before_compaction=250000)
+    doc = SN.unpackb(SN.write_snapshot(None, s))
+    for key in LOAD_SNAPSHOT_KEYS:
+        node = doc["snapshot"]
+        for k in key:
+            assert k in node, key
+            node = node[k]
+    r = SN.read_snapshot(SN.write_snapshot(None, s))
+    assert (r.bounding_radius, r.rays_per_batch, r.measured_batch_size, r.measured_batch_size_before_compaction) == \
+        (0.75, 4096, 200000, 250000)
+    assert (r.density_grid is not None) == with_grid
