@@ -187,6 +187,7 @@ def run_ours(args, rank, world, local):
     ctx = abi.Context(local, stream=stream.cuda_stream)
     ctx.canonical_set(0, av.canonical, av.faces, av.mask)
     ctx.params_load(0, fc, params)
+    apply_tuning(ctx, args)
     frames_dev = [torch.from_numpy(f).cuda() for f in frames]
     rgba = torch.empty((HEIGHT * WIDTH, 4), dtype=torch.float32, device="cuda")
     depth = torch.empty(HEIGHT * WIDTH, dtype=torch.float32, device="cuda")
@@ -216,6 +217,12 @@ def run_ours(args, rank, world, local):
         ctx.frame_wait(0, (k + 1) % 2)
         return k
 
+    tuning_note = None
+    if args.autotune:   # untimed: the library's autotuner picks the launch shapes on this frame
+        ctx.frame_upload(0, 0, frames[0])
+        ctx.occupancy_from_mesh(0, 0, RADIUS)
+        tuned, tuned_ms = ctx.autotune([reqs[0]], repeats=3)
+        tuning_note = {"autotuned": tuned, "ms_per_frame_at_tuning": tuned_ms}
     if args.stage_timing:   # every render with per-stage events: host-driven rounds (for kernel-level profiles)
         ctx.stats_enable(True)
     clocks = ClockSampler(local).__enter__()
@@ -335,6 +342,7 @@ def run_ours(args, rank, world, local):
         "gpu_launches": launches,
         "clocks": clock_summary,
         "wall_s_timed": t_wall,
+        "tuning": dict(ctx.tuning_get(), **(tuning_note or {})),
     }
     if not args.no_cpu_baseline:
         s, t, _, threads = cpu_render_rate(av, fc, params, frames[0], cams[0], 24)
@@ -405,6 +413,13 @@ def run_batch64(args):
             "stage_ms_per_batch": {k: v / args.steps for k, v in st["stage_ms"].items() if st["stage_calls"][k]}}
     print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def apply_tuning(ctx, args):
+    """--tune k=v,...: the render wavefront's launch shapes through insta_tuning_set."""
+    if args.tune:
+        kv = dict(item.split("=") for item in args.tune.split(",") if item)
+        ctx.tuning_set(**{k: int(v) for k, v in kv.items()})
 
 
 def run_map(args):
@@ -839,6 +854,8 @@ def main():
                          "precision: FP16 / BF16 / FP8 MLPs at 1024x1024 against the FP64 oracle; "
                          "map: canonical mapping of 1M shell points; grid: density-grid update; raycast: mesh raycast")
     ap.add_argument("--rows", type=int, default=16, help="precision: image rows rendered by the FP64 oracle")
+    ap.add_argument("--tune", default="", help="launch shapes, e.g. max_steps_per_round=16,bvh_top_nodes=21 (insta_tuning_set)")
+    ap.add_argument("--autotune", action="store_true", help="render: run insta_autotune on the frame before the warm-up")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--rate", type=float, default=240.0)
     ap.add_argument("--duration", type=float, default=30.0)

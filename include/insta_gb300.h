@@ -384,6 +384,8 @@ typedef struct insta_tuning {
     uint32_t sort_cell_bits;        /* 12, 15, 18 or 21: Morton cells of a round's (request, cell) sort (built-in 18 = 64^3) */
     uint32_t mlp_ctas_per_sm;       /* 1..4 resident MLP CTAs per SM (built-in: as many as shared memory allows) */
     uint32_t deform_blocks_per_sm;  /* 1..64 blocks per SM of the deform + encode stage (built-in 16) */
+    uint32_t bvh_top_nodes;         /* 0, 5 or 21: top levels of each frame's tree that every warp of the
+                                       nearest-triangle stage copies into shared memory (built-in 0) */
 } insta_tuning;
 int insta_tuning_set(insta_ctx* ctx, const insta_tuning* t);
 int insta_tuning_get(insta_ctx* ctx, insta_tuning* t);

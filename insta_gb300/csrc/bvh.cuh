@@ -54,6 +54,7 @@ __device__ __forceinline__ Nearest nearest_bvh(const FrameView& fr, V3 p, float 
         if (ref & INSTA_LEAF_BIT) {
             const uint32_t first = (ref & ~INSTA_LEAF_BIT) >> 3, count = ref & 7u;
             for (uint32_t i = 0; i < count; ++i) {
+                if (leaf_bound_sq(fr.leaf_bounds + (size_t)(first + i) * 2, p) > prune_limit(best)) continue;
                 int32_t id;
                 float d = slot_distance(fr, (int32_t)(first + i), p, id);
                 if (d < best || (d == best && (uint32_t)id < (uint32_t)bid)) { best = d; bid = id; bslot = (int32_t)(first + i); }
@@ -133,8 +134,11 @@ __device__ __forceinline__ void flush_tests(const FrameView& fr, WarpScratch& ws
 // triangle, ties to the lowest id (the union holds every node that lane's own traversal would
 // visit; pruning with a not yet updated bound only tests more).  Control flow stays uniform.
 // Lanes with active == false only ride along.  The slot of the result is not tracked (-1).
+// `top`: when not null, the warp's shared-memory copy of the frame's first n_top nodes (the top
+// levels: nodes are numbered level by level, see stage_top_nodes); those are read from there.
 __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool active, WarpScratch& ws, uint32_t* err,
-                                                float bound = __builtin_huge_valf()) {
+                                                float bound = __builtin_huge_valf(), const float4* top = nullptr,
+                                                uint32_t n_top = 0) {
     const float INF = __int_as_float(0x7f800000);
     const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
     float best = active ? bound : -INF;
@@ -156,12 +160,16 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
         const uint32_t nm = __ballot_sync(0xffffffffu, need);
         if (!nm) continue;
         if (ref & INSTA_LEAF_BIT) {
+            // a lane queues a triangle of the leaf only when the triangle's bounding disk may
+            // hold a point nearer than its prune limit (leaf_bound_sq)
             const uint32_t first = (ref & ~INSTA_LEAF_BIT) >> 3, count = ref & 7u;
-            const uint32_t nl = __popc(nm), rank = __popc(nm & lt_mask);
             __syncwarp();   // the popped entry has been read by every lane
-            if (need)
-                for (uint32_t i = 0; i < count; ++i) ws.queue[qlen + i * nl + rank] = ((first + i) << 5) | lane;
-            qlen += count * nl;
+            for (uint32_t i = 0; i < count; ++i) {
+                const bool want = need && leaf_bound_sq(fr.leaf_bounds + (size_t)(first + i) * 2, p) <= lim;
+                const uint32_t m = __ballot_sync(0xffffffffu, want);
+                if (want) ws.queue[qlen + __popc(m & lt_mask)] = ((first + i) << 5) | lane;
+                qlen += __popc(m);
+            }
             __syncwarp();
             if (qlen >= 32u) {
                 do flush_tests(fr, ws, p, 32u, qlen, best, bid);
@@ -170,10 +178,18 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
             }
             continue;
         }
-        const float4* nd = fr.nodes + (size_t)ref * 7;
-        const float4 mnx = __ldg(nd + 0), mny = __ldg(nd + 1), mnz = __ldg(nd + 2);
-        const float4 mxx = __ldg(nd + 3), mxy = __ldg(nd + 4), mxz = __ldg(nd + 5);
-        const int4 ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
+        float4 mnx, mny, mnz, mxx, mxy, mxz;
+        int4 ch;
+        if (ref < n_top) {   // warp-uniform: the staged top levels
+            const float4* nd = top + (size_t)ref * 7;
+            mnx = nd[0]; mny = nd[1]; mnz = nd[2]; mxx = nd[3]; mxy = nd[4]; mxz = nd[5];
+            ch = reinterpret_cast<const int4*>(nd)[6];
+        } else {
+            const float4* nd = fr.nodes + (size_t)ref * 7;
+            mnx = __ldg(nd + 0); mny = __ldg(nd + 1); mnz = __ldg(nd + 2);
+            mxx = __ldg(nd + 3); mxy = __ldg(nd + 4); mxz = __ldg(nd + 5);
+            ch = __ldg(reinterpret_cast<const int4*>(nd + 6));
+        }
         float cd[4];
         uint32_t ci[4] = {(uint32_t)ch.x, (uint32_t)ch.y, (uint32_t)ch.z, (uint32_t)ch.w};
         cd[0] = box_dist_fast(mnx.x, mny.x, mnz.x, mxx.x, mxy.x, mxz.x, p);

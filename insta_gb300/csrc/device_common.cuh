@@ -85,6 +85,52 @@ __device__ __forceinline__ void tri_record(V3 a, V3 b, V3 c, uint32_t id, float4
     dst[8] = make_float4(c3.x, c3.y, c3.z, 0.f);
 }
 
+// The bounding disk of a triangle (FrameView::leaf_bounds), in FP64: centre = centroid, radius =
+// the largest vertex distance from it, widened by 2^-16 relative + 2e-7 absolute so that the FP32
+// centre and radius still enclose every vertex, with the rounding of p - centre in FP32 (below
+// 1e-7 for coordinates of order one) to spare; unit normal of (b - a) x (c - a), zero for a
+// degenerate triangle (the disk is then the sphere of the same radius).
+__device__ __forceinline__ void tri_bound(const float* A, const float* B, const float* C, float4* dst) {
+    double c[3], n[3], r2 = 0.0;
+    for (int k = 0; k < 3; ++k) c[k] = ((double)A[k] + (double)B[k] + (double)C[k]) / 3.0;
+    const float* v[3] = {A, B, C};
+    for (int i = 0; i < 3; ++i) {
+        double d2 = 0.0;
+        for (int k = 0; k < 3; ++k) d2 += ((double)v[i][k] - c[k]) * ((double)v[i][k] - c[k]);
+        r2 = fmax(r2, d2);
+    }
+    const double e1[3] = {(double)B[0] - A[0], (double)B[1] - A[1], (double)B[2] - A[2]};
+    const double e2[3] = {(double)C[0] - A[0], (double)C[1] - A[1], (double)C[2] - A[2]};
+    n[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    n[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    n[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    const double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    const double inv = nn > 0.0 ? 1.0 / nn : 0.0;
+    const double r = sqrt(r2) * (1.0 + 1.0 / 65536.0) + 2e-7;
+    dst[0] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)r);
+    dst[1] = make_float4((float)(n[0] * inv), (float)(n[1] * inv), (float)(n[2] * inv), 0.f);
+}
+
+// A lower bound on the squared distance from p to the triangle of a leaf_bounds entry: with
+// v = p - centre, h = n.v the signed distance to the triangle's plane and l = |v - h n| the
+// distance of p's projection from the centre, the triangle lies within the disk of the radius
+// around the centre, so d^2 >= h^2 + max(l - radius, 0)^2.  In FP32: |h| is reduced by 2e-7
+// (the rounding of v and of the stored normal, for coordinates of order one and distances below
+// 0.1), the radius carries its own margin, and the result is shrunk by 2^-12 relative, which
+// covers the rounding of l where the radius matters (l >= radius, millimetres); so the bound
+// stays below the exact squared distance, and a triangle it skips (bound > prune limit) cannot
+// reach the running minimum.
+__device__ __forceinline__ float leaf_bound_sq(const float4* b, V3 p) {
+    const float4 b0 = __ldg(b), b1 = __ldg(b + 1);
+    const float vx = p.x - b0.x, vy = p.y - b0.y, vz = p.z - b0.z;
+    const float h = fmaf(b1.x, vx, fmaf(b1.y, vy, b1.z * vz));
+    const float vv = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+    const float l = sqrtf(fmaxf(fmaf(-h, h, vv), 0.f));
+    const float ex = fmaxf(l - b0.w, 0.f);
+    const float hs = fmaxf(fabsf(h) - 2e-7f, 0.f);
+    return fmaf(hs, hs, ex * ex) * (1.0f - 1.0f / 4096.0f);
+}
+
 // tri_distance_sq from a precomputed record: only the point-dependent operations remain, in the
 // same order, so the result is bit-identical.
 __device__ __forceinline__ float tri_distance_rec(const float4* tr, V3 pos, int32_t& id) {

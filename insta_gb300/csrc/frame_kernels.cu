@@ -692,6 +692,7 @@ __global__ void tri_record_kernel(BvhBuildArgs one, const BvhBuildArgs* __restri
     const float* B = a.verts + a.faces[f * 3 + 1] * 3;
     const float* C = a.verts + a.faces[f * 3 + 2] * 3;
     tri_record(v3(A[0], A[1], A[2]), v3(B[0], B[1], B[2]), v3(C[0], C[1], C[2]), f, dst);
+    tri_bound(A, B, C, a.leaf_tris + (size_t)a.F * INSTA_TRI_F4 + (size_t)s * 2);
 }
 
 cudaError_t launch_tri_frames(int F, const float* verts, const int32_t* faces, const uint32_t* mask, const float* canon_area,

@@ -591,6 +591,7 @@ struct WaveRun {
         W.out_f32 = (const float4*)w.out_f32.p;
         W.n_round = (uint32_t*)w.n_round.p;
         W.sample_counter = ctx->sample_counter;
+        W.top_nodes = ctx->tune.bvh_top_nodes;
         W.err = ctx->err_dev;
         M = MlpArgs{};
         M.fv = fv; M.plan = P; M.tiles = W.tiles;
@@ -855,10 +856,11 @@ Frame& prepare_frame(insta_ctx* ctx, Avatar& a, int frame, const float* verts, c
     const int max_nodes = std::max(1, a.F);
     ctx->alloc(f.verts, (size_t)a.V * 12);
     ctx->alloc(f.frames, (size_t)a.F * sizeof(TriFrame));
-    ctx->alloc(f.leaf_tris, (size_t)a.F * INSTA_TRI_F4 * 16);
+    ctx->alloc(f.leaf_tris, (size_t)a.F * (INSTA_TRI_F4 + 2) * 16);   // records, then the bounding disks
     ctx->alloc(f.nodes, (size_t)max_nodes * 112);
     host_copy(f.verts.p, verts, (size_t)a.V * 12, stream ? stream : ctx->stream);
     f.view.leaf_tris = static_cast<const float4*>(f.leaf_tris.p);
+    f.view.leaf_bounds = f.view.leaf_tris + (size_t)a.F * INSTA_TRI_F4;
     f.view.nodes = static_cast<const float4*>(f.nodes.p);
     f.view.frames = static_cast<const TriFrame*>(f.frames.p);
     f.view.n_tris = a.F;
@@ -1740,6 +1742,8 @@ int insta_tuning_set(insta_ctx* ctx, const insta_tuning* t) {
             fail(INSTA_ERR_INVALID_ARG, "sort_cell_bits must be 0 or one of 12, 15, 18, 21");
         if (t->mlp_ctas_per_sm > 4) fail(INSTA_ERR_INVALID_ARG, "mlp_ctas_per_sm must be 0..4");
         if (t->deform_blocks_per_sm > 64) fail(INSTA_ERR_INVALID_ARG, "deform_blocks_per_sm must be 0..64");
+        if (t->bvh_top_nodes != 0 && t->bvh_top_nodes != 5 && t->bvh_top_nodes != 21)
+            fail(INSTA_ERR_INVALID_ARG, "bvh_top_nodes must be 0, 5 or 21");
         ctx->tune = *t;
     });
 }
@@ -1794,14 +1798,14 @@ int insta_autotune(insta_ctx* ctx, const insta_render_desc* reqs, int n, int rep
         float cur_ms = 0.f;
         try {
             cur_ms = time_one(cur);
-            const std::vector<uint32_t> cands[4] = {{8, 16, 24, 32}, {15, 18, 21}, {1, 2, 3, 4}, {8, 12, 16, 24}};
+            const std::vector<uint32_t> cands[5] = {{8, 16, 24, 32}, {15, 18, 21}, {1, 2, 3, 4}, {8, 12, 16, 24}, {0, 5, 21}};
             for (int pass = 0; pass < 2; ++pass) {
                 bool moved = false;
-                for (int f = 0; f < 4; ++f) {
+                for (int f = 0; f < 5; ++f) {
                     for (uint32_t v : cands[f]) {
                         insta_tuning t = cur;
                         uint32_t* field = f == 0 ? &t.max_steps_per_round : f == 1 ? &t.sort_cell_bits : f == 2 ? &t.mlp_ctas_per_sm
-                                                                                                       : &t.deform_blocks_per_sm;
+                                        : f == 3 ? &t.deform_blocks_per_sm : &t.bvh_top_nodes;
                         if (*field == v) continue;
                         *field = v;
                         const float ms = time_one(t);

@@ -32,6 +32,10 @@ struct TriFrame;
 #define INSTA_TRI_F4 9
 struct FrameView {
     const float4* leaf_tris;
+    // [n_tris][2] float4 per Morton slot, the triangle's bounding disk: (centre, radius), (unit
+    // normal, 0) -- every point of the triangle lies in the plane through the centre with that
+    // normal, within the radius of the centre (leaf_bound_sq)
+    const float4* leaf_bounds;
     const float4* nodes;
     const TriFrame* frames;   // per original triangle, see device_common.cuh
     int n_tris;

@@ -97,6 +97,7 @@ struct WaveArgs {
     const uint2* out;           // per sample: FP16 (r, g, b, density)
     const float4* out_f32;      // per sample when the MLP runs in BF16
     unsigned long long* sample_counter;
+    uint32_t top_nodes;         // nearest stage: top tree nodes each warp stages in shared memory (0: none)
     uint32_t* err;
 };
 

@@ -414,11 +414,28 @@ __global__ void __launch_bounds__(256) sort_place_kernel(const __grid_constant__
 //                         warp_position(pos) / warp_direction(dir) with that triangle, then the
 //                         hash encode and SH written as tensor-core operand rows at the sample's
 //                         sorted position
+// With A.top_nodes > 0 each warp keeps a shared-memory copy of the first top_nodes nodes of its
+// frame's tree (the top levels: nodes are numbered level by level), brought in by one bulk copy
+// (cp.async.bulk, completion on the warp's mbarrier) whenever the warp moves to another frame;
+// the walk reads those nodes from shared memory and the rest through the L1.
 __global__ void __launch_bounds__(256, 4) nearest_stage_kernel(const __grid_constant__ WaveArgs A) {
     __shared__ WarpScratch wscratch[8];
+    __shared__ alignas(8) uint64_t top_bar[8];
+    extern __shared__ __align__(128) float4 top_dyn[];   // [8][top_nodes * 7]
     const uint32_t n = *A.n_samples_padded;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
+    float4* top = top_dyn + (size_t)warp * A.top_nodes * 7;
+    const float4* staged = nullptr;   // the nodes array whose top levels `top` holds
+    uint32_t n_top = 0, top_phase = 0;
+    bool top_ok = A.top_nodes > 0;    // false after a copy that did not complete in time
+    if (top_ok) {
+        if (lane == 0) {
+            mbar_init(&top_bar[warp], 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncwarp();
+    }
     for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32u; base < n; base += n_warps * 32u) {
         const uint32_t s = base + lane;
         const uint32_t m = A.sample_order[s];
@@ -441,9 +458,28 @@ __global__ void __launch_bounds__(256, 4) nearest_stage_kernel(const __grid_cons
         for (int k = 0; k < 3; ++k) cw[k] = __fdiv_rn(__fsub_rn(pp[k], rv.train_min[k]), __fsub_rn(rv.train_max[k], rv.train_min[k]));
         const V3 p = v3(cw[0], cw[1], cw[2]);
         const bool in_box = valid && box_contains(R.dv.aabb_min, R.dv.aabb_max, p);
-        Nearest q = nearest_warp(R.fr, p, in_box, wscratch[warp], A.err);
+        if (top_ok && R.fr.nodes != staged) {
+            const uint32_t k = min(A.top_nodes, (uint32_t)R.fr.n_nodes);   // never past the node array
+            __syncwarp();   // every lane is done reading the previous copy
+            if (lane == 0) {
+                fence_async_smem();
+                bulk_load(top, R.fr.nodes, k * 112u, &top_bar[warp]);
+            }
+            top_ok = mbar_wait(&top_bar[warp], top_phase);
+            if (top_ok) {
+                top_phase ^= 1u;
+                staged = R.fr.nodes;
+                n_top = k;
+            } else {
+                n_top = 0;
+                if (lane == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
+            }
+        }
+        Nearest q = nearest_warp(R.fr, p, in_box, wscratch[warp], A.err, __builtin_huge_valf(), top, n_top);
         if (valid) A.sample_key[s] = in_box ? (uint32_t)q.id : 0xfffffffeu;
     }
+    // a copy that timed out may still land: wait for it (bounded) before the CTA's shared memory goes
+    if (A.top_nodes > 0 && !top_ok) mbar_wait(&top_bar[warp], top_phase);
 }
 
 __global__ void __launch_bounds__(256, 4) map_encode_kernel(const __grid_constant__ WaveArgs A) {
@@ -868,7 +904,7 @@ cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s) {
 
 cudaError_t launch_deform_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s) {
     const uint32_t bps = blocks_per_sm ? blocks_per_sm : 16u;
-    nearest_stage_kernel<<<sm_count() * bps, 256, 0, s>>>(a);
+    nearest_stage_kernel<<<sm_count() * bps, 256, (size_t)8 * a.top_nodes * 112u, s>>>(a);
     map_encode_kernel<<<sm_count() * bps, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
