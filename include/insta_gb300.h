@@ -128,6 +128,9 @@ typedef struct {
     uint64_t last_render_samples;    /* network samples of the last insta_render */
     float stage_ms[INSTA_STAGE_COUNT];
     uint32_t stage_calls[INSTA_STAGE_COUNT];
+    /* render nearest-triangle walk, counted while stage timing is on (per 32-sample warp walk):
+       walks, inner nodes visited, leaves visited, bounding-disk tests, exact triangle tests */
+    uint64_t walk_warps, walk_inner_nodes, walk_leaves, walk_bound_tests, walk_exact_tests;
 } insta_stats;
 
 /* -- context ---------------------------------------------------------------- */
@@ -381,16 +384,19 @@ int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples);
  * rays composite their samples in order): only speed does. */
 typedef struct insta_tuning {
     uint32_t max_steps_per_round;   /* 1..32 (built-in 32) */
-    uint32_t sort_cell_bits;        /* 12, 15, 18 or 21: Morton cells of a round's (request, cell) sort (built-in 18 = 64^3) */
+    uint32_t sort_cell_bits;        /* 12, 15, 18 or 21: Morton cells of a round's (request, cell) sort
+                                       (built-in 18 = 64^3 per request, fewer when requests x cells > 4 Mi) */
     uint32_t mlp_ctas_per_sm;       /* 1..4 resident MLP CTAs per SM (built-in: as many as shared memory allows) */
     uint32_t deform_blocks_per_sm;  /* 1..64 blocks per SM of the deform + encode stage (built-in 16) */
     uint32_t bvh_top_nodes;         /* 0, 5 or 21: top levels of each frame's tree that every warp of the
                                        nearest-triangle stage copies into shared memory (built-in 0) */
+    uint32_t fused_field_stage;     /* 1: deform + encode + MLP as one kernel (FP16 / BF16 fields);
+                                       0 (built-in, faster on GB300): encode to global operand tiles, then the MLP */
 } insta_tuning;
 int insta_tuning_set(insta_ctx* ctx, const insta_tuning* t);
 int insta_tuning_get(insta_ctx* ctx, insta_tuning* t);
 /* The autotuner: times insta_render_batch on the given requests (device outputs it allocates)
- * for candidate launch shapes -- coordinate descent over the four fields above, each candidate the
+ * for candidate launch shapes -- coordinate descent over the fields above, each candidate the
  * median of `repeats` timed renders after one untimed one (CUDA events on the context's stream) --
  * then keeps the fastest with insta_tuning_set and returns it in *best (best_ms: its time per
  * batch).  No reference counterpart. */
@@ -435,6 +441,8 @@ typedef struct {
     uint32_t max_inflight;          /* request slots (1..256) */
     uint64_t max_inflight_pixels;   /* pixels of admitted requests (<= 2^25) */
     double occupancy_radius;        /* request frames: occupancy from the mesh (0.015) */
+    uint32_t rounds_per_launch;     /* rounds run as one CUDA-graph launch between admission points
+                                       (even; 0 = 2); with per-stage timing on, rounds are host-driven */
 } insta_server_config;
 
 int insta_server_create(insta_ctx* ctx, const insta_server_config* cfg, insta_server** out);

@@ -6,11 +6,13 @@ present, the calls raise.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
 
-LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libinsta_gb300.so"
+# the in-tree build; INSTA_GB300_LIB selects another build of the same library
+LIB_PATH = Path(os.environ.get("INSTA_GB300_LIB", Path(__file__).resolve().parent / "_lib" / "libinsta_gb300.so"))
 
 OK, ERR_INVALID_ARG, ERR_CUDA, ERR_BUDGET, ERR_NOT_READY, ERR_UNSUPPORTED, ERR_DEVICE = range(7)
 PRECISION_FP16, PRECISION_BF16, PRECISION_FP8 = 0, 1, 2
@@ -35,7 +37,8 @@ REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
 
 
 class ServerConfig(C.Structure):
-    _fields_ = [("max_inflight", C.c_uint32), ("max_inflight_pixels", C.c_uint64), ("occupancy_radius", C.c_double)]
+    _fields_ = [("max_inflight", C.c_uint32), ("max_inflight_pixels", C.c_uint64), ("occupancy_radius", C.c_double),
+                ("rounds_per_launch", C.c_uint32)]
 
 
 class Pcg32State(C.Structure):
@@ -91,7 +94,9 @@ STAGES = ["frame", "occupancy", "ray_init", "march", "deform_encode", "mlp", "co
 
 class Stats(C.Structure):
     _fields_ = [("kernel_launches", C.c_uint64), ("last_render_samples", C.c_uint64),
-                ("stage_ms", C.c_float * len(STAGES)), ("stage_calls", C.c_uint32 * len(STAGES))]
+                ("stage_ms", C.c_float * len(STAGES)), ("stage_calls", C.c_uint32 * len(STAGES)),
+                ("walk_warps", C.c_uint64), ("walk_inner_nodes", C.c_uint64), ("walk_leaves", C.c_uint64),
+                ("walk_bound_tests", C.c_uint64), ("walk_exact_tests", C.c_uint64)]
 
 
 class RenderDesc(C.Structure):
@@ -104,7 +109,7 @@ class RenderDesc(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("max_steps_per_round", C.c_uint32), ("sort_cell_bits", C.c_uint32), ("mlp_ctas_per_sm", C.c_uint32),
-                ("deform_blocks_per_sm", C.c_uint32), ("bvh_top_nodes", C.c_uint32)]
+                ("deform_blocks_per_sm", C.c_uint32), ("bvh_top_nodes", C.c_uint32), ("fused_field_stage", C.c_uint32)]
 
 
 _lib = None
@@ -259,7 +264,8 @@ class Context:
         self._check(self.lib.insta_stats_read(self.h, C.byref(s), int(reset)))
         return {"kernel_launches": int(s.kernel_launches), "last_render_samples": int(s.last_render_samples),
                 "stage_ms": {n: float(s.stage_ms[i]) for i, n in enumerate(STAGES)},
-                "stage_calls": {n: int(s.stage_calls[i]) for i, n in enumerate(STAGES)}}
+                "stage_calls": {n: int(s.stage_calls[i]) for i, n in enumerate(STAGES)},
+                "walk": {k: int(getattr(s, "walk_" + k)) for k in ("warps", "inner_nodes", "leaves", "bound_tests", "exact_tests")}}
 
     def canonical_set(self, avatar, verts, faces, mask=None):
         v = np.ascontiguousarray(verts, dtype=np.float32)
@@ -423,9 +429,10 @@ class Context:
         pd = (C.c_void_p * n)(*[_addr(b).value for b in out_depth])
         self._check(self.lib.insta_render_batch(self.h, arr, n, pr, pd))
 
-    def tuning_set(self, max_steps_per_round=0, sort_cell_bits=0, mlp_ctas_per_sm=0, deform_blocks_per_sm=0, bvh_top_nodes=0):
+    def tuning_set(self, max_steps_per_round=0, sort_cell_bits=0, mlp_ctas_per_sm=0, deform_blocks_per_sm=0, bvh_top_nodes=0,
+                   fused_field_stage=0):
         """insta_tuning_set: the wavefront's launch shapes (0 keeps a field's built-in choice)."""
-        t = Tuning(max_steps_per_round, sort_cell_bits, mlp_ctas_per_sm, deform_blocks_per_sm, bvh_top_nodes)
+        t = Tuning(max_steps_per_round, sort_cell_bits, mlp_ctas_per_sm, deform_blocks_per_sm, bvh_top_nodes, fused_field_stage)
         self._check(self.lib.insta_tuning_set(self.h, C.byref(t)))
 
     def tuning_get(self) -> dict:
@@ -459,10 +466,10 @@ class Context:
 class Server:
     """The request loop (insta_server_*): owns `ctx` from creation to close()."""
 
-    def __init__(self, ctx: Context, max_inflight=16, max_inflight_pixels=1 << 22, occupancy_radius=0.015):
+    def __init__(self, ctx: Context, max_inflight=16, max_inflight_pixels=1 << 22, occupancy_radius=0.015, rounds_per_launch=0):
         self.ctx = ctx
         self.lib = ctx.lib
-        cfg = ServerConfig(max_inflight, max_inflight_pixels, occupancy_radius)
+        cfg = ServerConfig(max_inflight, max_inflight_pixels, occupancy_radius, rounds_per_launch)
         h = C.c_void_p()
         ctx._check(self.lib.insta_server_create(ctx.h, C.byref(cfg), C.byref(h)))
         self.h = h

@@ -136,9 +136,12 @@ __device__ __forceinline__ void flush_tests(const FrameView& fr, WarpScratch& ws
 // Lanes with active == false only ride along.  The slot of the result is not tracked (-1).
 // `top`: when not null, the warp's shared-memory copy of the frame's first n_top nodes (the top
 // levels: nodes are numbered level by level, see stage_top_nodes); those are read from there.
+// `stats`: when not null, lane 0 adds the walk's counts (walks, inner nodes, leaves, bounding-disk
+// tests, exact tests) to stats[0..4].
 __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool active, WarpScratch& ws, uint32_t* err,
                                                 float bound = __builtin_huge_valf(), const float4* top = nullptr,
-                                                uint32_t n_top = 0) {
+                                                uint32_t n_top = 0, unsigned long long* stats = nullptr) {
+    uint32_t c_inner = 0, c_leaf = 0, c_bound = 0, c_exact = 0;
     const float INF = __int_as_float(0x7f800000);
     const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
     float best = active ? bound : -INF;
@@ -164,11 +167,14 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
             // hold a point nearer than its prune limit (leaf_bound_sq)
             const uint32_t first = (ref & ~INSTA_LEAF_BIT) >> 3, count = ref & 7u;
             __syncwarp();   // the popped entry has been read by every lane
+            ++c_leaf;
+            c_bound += count * (uint32_t)__popc(nm);
             for (uint32_t i = 0; i < count; ++i) {
                 const bool want = need && leaf_bound_sq(fr.leaf_bounds + (size_t)(first + i) * 2, p) <= lim;
                 const uint32_t m = __ballot_sync(0xffffffffu, want);
                 if (want) ws.queue[qlen + __popc(m & lt_mask)] = ((first + i) << 5) | lane;
                 qlen += __popc(m);
+                c_exact += (uint32_t)__popc(m);
             }
             __syncwarp();
             if (qlen >= 32u) {
@@ -178,6 +184,7 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
             }
             continue;
         }
+        ++c_inner;
         float4 mnx, mny, mnz, mxx, mxy, mxz;
         int4 ch;
         if (ref < n_top) {   // warp-uniform: the staged top levels
@@ -233,6 +240,13 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
         __syncwarp();
     }
     if (qlen) flush_tests(fr, ws, p, qlen, qlen, best, bid);
+    if (stats && lane == 0) {
+        atomicAdd(stats + 0, 1ull);
+        atomicAdd(stats + 1, (unsigned long long)c_inner);
+        atomicAdd(stats + 2, (unsigned long long)c_leaf);
+        atomicAdd(stats + 3, (unsigned long long)c_bound);
+        atomicAdd(stats + 4, (unsigned long long)c_exact);
+    }
     return {bid, -1, best};
 }
 

@@ -542,6 +542,20 @@ __device__ __forceinline__ bool ray_next_sample(const RenderView& rv, const uint
 // (per-level dense index x + y*res + z*res^2 or spatial hash with primes
 // 1, 2654435761, 805459861; trilinear weights; FP32 accumulation).
 // Level l's two features at x (trilinear over the cell's 8 corners).
+__device__ __forceinline__ float2 half2_bits(uint32_t b) {
+    __half2 h;
+    memcpy(&h, &b, 4);
+    return __half22float2(h);
+}
+
+// Trilinear interpolation of level l's two features at x (the published multiresolution hash
+// encoding: dense index x + y res + z res^2 for levels whose grid fits the table, else the spatial
+// hash x ^ y * 2654435761 ^ z * 805459861).  The eight corners are summed in the order
+// (x, y, z) = 000, 100, 010, 110, 001, 101, 011, 111.  Dense levels (the coarse ones) fetch the
+// two x-neighbours of each (y, z) pair together: one 8-byte load when the pair starts on an even
+// entry (level offsets are multiples of 8 entries), else two 4-byte loads; the values and their
+// order are unchanged.  (Measured on the 512x512 frame: 8-byte pairs ~2 % faster than per-corner
+// loads; 16-byte groups and L2 evict_last cache hints on the dense levels were slower.)
 __device__ __forceinline__ void hash_level(const FieldView& fv, const __half2* table, V3 x, uint32_t l, float& a0, float& a1) {
     const float s = fv.level_scale[l];
     float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);
@@ -553,6 +567,35 @@ __device__ __forceinline__ void hash_level(const FieldView& fv, const __half2* t
     const __half2* lt = table + fv.level_off[l];
     a0 = 0.f;
     a1 = 0.f;
+    if (dense) {
+#pragma unroll
+        for (uint32_t c2 = 0; c2 < 4; ++c2) {
+            const uint32_t by = c2 & 1u, bz = c2 >> 1;
+            uint32_t i0 = gx + (gy + by) * res + (gz + bz) * res * res;
+            uint32_t i1 = i0 + 1u;
+            if (i0 >= size) i0 %= size;   // only cells on the far boundary wrap
+            if (i1 >= size) i1 %= size;
+            float2 e0, e1;
+            if (i1 == i0 + 1u && (i0 & 1u) == 0u) {
+                const uint2 u = __ldg(reinterpret_cast<const uint2*>(lt + i0));
+                e0 = half2_bits(u.x);
+                e1 = half2_bits(u.y);
+            } else {
+                e0 = __half22float2(__ldg(lt + i0));
+                e1 = __half22float2(__ldg(lt + i1));
+            }
+            const float wy = by ? ry : __fsub_rn(1.f, ry);
+            float w = __fmul_rn(__fsub_rn(1.f, rx), wy);
+            w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
+            a0 = __fadd_rn(a0, __fmul_rn(w, e0.x));
+            a1 = __fadd_rn(a1, __fmul_rn(w, e0.y));
+            w = __fmul_rn(rx, wy);
+            w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
+            a0 = __fadd_rn(a0, __fmul_rn(w, e1.x));
+            a1 = __fadd_rn(a1, __fmul_rn(w, e1.y));
+        }
+        return;
+    }
 #pragma unroll
     for (uint32_t c = 0; c < 8; ++c) {
         uint32_t bx = c & 1u, by = (c >> 1) & 1u, bz = (c >> 2) & 1u;
@@ -560,12 +603,7 @@ __device__ __forceinline__ void hash_level(const FieldView& fv, const __half2* t
         w = __fmul_rn(w, by ? ry : __fsub_rn(1.f, ry));
         w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
         uint32_t cx = gx + bx, cy = gy + by, cz = gz + bz;
-        uint32_t idx;
-        if (dense) {
-            idx = cx + cy * res + cz * res * res;
-            if (idx >= size) idx %= size;   // only cells on the far boundary wrap
-        }
-        else idx = ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
+        const uint32_t idx = ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
         float2 e = __half22float2(__ldg(lt + idx));
         a0 = __fadd_rn(a0, __fmul_rn(w, e.x));
         a1 = __fadd_rn(a1, __fmul_rn(w, e.y));

@@ -129,6 +129,8 @@ struct insta_ctx {
     uint32_t* loop_state = nullptr;                 // [0] steps of the current round, [1] rounds of this launch
     unsigned long long* loop_rounds_total = nullptr; // rounds run by graph launches (launch statistics)
     unsigned long long loop_rounds_seen = 0;
+    uint32_t loop_round_kernels = 10;                // kernels per graph-run round (9 with the fused field stage)
+    unsigned long long* walk_stats = nullptr;        // nearest-walk counters while stage timing is on
     // insta_render_async with host outputs: double-buffered device staging, copied back on a
     // copy stream while the next render runs
     cudaStream_t copy = nullptr;
@@ -474,7 +476,14 @@ static_assert(kMaxSteps <= (1u << (32 - kStepShift)), "step index must fit besid
 
 // The wavefront's launch shapes under the context's tuning (zero fields: built-in choices).
 uint32_t tune_steps(const insta_ctx* ctx) { return ctx->tune.max_steps_per_round ? ctx->tune.max_steps_per_round : kMaxSteps; }
-uint32_t tune_cell_bits(const insta_ctx* ctx) { return ctx->tune.sort_cell_bits ? ctx->tune.sort_cell_bits : 18u; }
+// Built-in sort grid: 64^3 cells per request while the bins stay within 4 Mi (a round's
+// counting sort clears and scans them), else 32^3 (16^3 beyond 128 request slots).
+uint32_t tune_cell_bits(const insta_ctx* ctx, uint32_t slots) {
+    if (ctx->tune.sort_cell_bits) return ctx->tune.sort_cell_bits;
+    uint32_t b = 18u;
+    while (b > 12u && ((uint64_t)slots << b) > (4ull << 20)) b -= 3u;
+    return b;
+}
 static_assert((1u << 26) <= kRayMask + 1u, "ray slots (at most 2^26 pixels per batch) must fit below the step index");
 
 bool same_field_layout(const Field& a, const Field& b) {
@@ -518,6 +527,9 @@ struct WaveRun {
     uint32_t n_alive = 0;
     uint32_t* counters = nullptr;
 
+    // deform + encode + MLP as one kernel: FP16 / BF16 fields when the tuning asks for it
+    bool fused_field() const { return W.fv.precision != 2 && ctx->tune.fused_field_stage; }
+
     RayBuf rays(int b) {
         Wave& w = ctx->wave;
         return RayBuf{(float4*)w.rays[b][0].p, (float4*)w.rays[b][1].p, (float4*)w.rays[b][2].p, (float4*)w.rays[b][3].p};
@@ -533,7 +545,7 @@ struct WaveRun {
         steps_max = tune_steps(ctx);
         round_cap = std::min<uint64_t>(max_rays * steps_max, kMaxRoundSamples);
         cap_samples = (round_cap + (uint64_t)slots * 128 + 127) / 128 * 128;
-        const uint32_t cell_bits = sort_cell_bits(slots, tune_cell_bits(ctx));
+        const uint32_t cell_bits = sort_cell_bits(slots, tune_cell_bits(ctx, slots));
         const uint64_t n_bins = (uint64_t)slots << cell_bits;
         if (w.cap_rays < max_rays) {
             for (int b = 0; b < 2; ++b)
@@ -592,6 +604,11 @@ struct WaveRun {
         W.n_round = (uint32_t*)w.n_round.p;
         W.sample_counter = ctx->sample_counter;
         W.top_nodes = ctx->tune.bvh_top_nodes;
+        if (ctx->timing && !ctx->walk_stats) {
+            CK(cudaMalloc(&ctx->walk_stats, 8 * sizeof(unsigned long long)));
+            CK(cudaMemset(ctx->walk_stats, 0, 8 * sizeof(unsigned long long)));
+        }
+        W.walk_stats = ctx->timing ? ctx->walk_stats : nullptr;
         W.err = ctx->err_dev;
         M = MlpArgs{};
         M.fv = fv; M.plan = P; M.tiles = W.tiles;
@@ -688,8 +705,13 @@ struct WaveRun {
                                                              ctx->stream);
                 if (e == cudaSuccess) e = launch_march(R, ctx->stream);
                 if (e == cudaSuccess) e = launch_sort_samples(R, ctx->stream);
-                if (e == cudaSuccess) e = launch_deform_encode(R, ctx->tune.deform_blocks_per_sm, ctx->stream);
-                if (e == cudaSuccess) e = launch_mlp(M, grid_tiles, ctx->stream, ctx->tune.mlp_ctas_per_sm);
+                if (fused_field()) {
+                    if (e == cudaSuccess) e = launch_nearest_stage(R, ctx->tune.deform_blocks_per_sm, ctx->stream);
+                    if (e == cudaSuccess) e = launch_field_fused(R, M, grid_tiles, ctx->stream, ctx->tune.mlp_ctas_per_sm);
+                } else {
+                    if (e == cudaSuccess) e = launch_deform_encode(R, ctx->tune.deform_blocks_per_sm, ctx->stream);
+                    if (e == cudaSuccess) e = launch_mlp(M, grid_tiles, ctx->stream, ctx->tune.mlp_ctas_per_sm);
+                }
                 if (e == cudaSuccess) e = launch_composite(R, ctx->stream);
             }
             if (e == cudaSuccess) e = launch_round_end(B.n_alive_out, ctx->loop_state + 1, ctx->loop_rounds_total, max_rounds, cond, ctx->stream);
@@ -700,6 +722,7 @@ struct WaveRun {
             CK(cudaGraphInstantiate(&ctx->loop_exec, g, 0));
             ctx->loop_key = key;
         }
+        ctx->loop_round_kernels = fused_field() ? 9u : 10u;
         CK(cudaMemsetAsync(ctx->loop_state + 1, 0, 4, ctx->stream));
         CK(cudaGraphLaunch(ctx->loop_exec, ctx->stream));   // its kernels are counted from the device's round total
     }
@@ -718,13 +741,29 @@ struct WaveRun {
         CK(cudaMemsetAsync(counters + 2, 0, 4, ctx->stream));
         { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_march(W, ctx->stream)); }
         { Stage st(ctx, INSTA_STAGE_SORT, 4); CK(launch_sort_samples(W, ctx->stream)); }
-        { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 2); CK(launch_deform_encode(W, ctx->tune.deform_blocks_per_sm, ctx->stream)); }
-        { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream, ctx->tune.mlp_ctas_per_sm)); }
+        if (fused_field()) {
+            // the nearest-triangle walk under the deform stage, the fused deform + encode + MLP kernel under the MLP stage
+            { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 1); CK(launch_nearest_stage(W, ctx->tune.deform_blocks_per_sm, ctx->stream)); }
+            { Stage st(ctx, INSTA_STAGE_MLP, 1);
+              CK(launch_field_fused(W, M, (uint32_t)(cap_samples / 128), ctx->stream, ctx->tune.mlp_ctas_per_sm)); }
+        } else {
+            { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 2); CK(launch_deform_encode(W, ctx->tune.deform_blocks_per_sm, ctx->stream)); }
+            { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream, ctx->tune.mlp_ctas_per_sm)); }
+        }
         { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }
         cur ^= 1;
         if (read_back) n_alive = read_alive();
     }
 };
+
+// The context's copy stream for device -> host output copies and the events of the
+// double-buffered insta_render_async staging, created together on first use.
+void ensure_copy_stream(insta_ctx* ctx) {
+    if (ctx->copy) return;
+    CK(cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) CK(cudaEventCreateWithFlags(&ctx->async_free[k], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->async_done, cudaEventDisableTiming));
+}
 
 // Testbed::render_nerf for a batch of requests (avatars, frames, cameras, resolutions) through one
 // wavefront; the request slots are the batch.
@@ -766,11 +805,7 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
     if (host_pix && async_host) {
         // the staging pair the copy stream released last; the render waits for its copy to end
         async_k = ctx->async_next;
-        if (!ctx->copy) {
-            CK(cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking));
-            for (int k = 0; k < 2; ++k) CK(cudaEventCreateWithFlags(&ctx->async_free[k], cudaEventDisableTiming));
-            CK(cudaEventCreateWithFlags(&ctx->async_done, cudaEventDisableTiming));
-        }
+        ensure_copy_stream(ctx);
         if (ctx->async_used[async_k]) CK(cudaStreamWaitEvent(ctx->stream, ctx->async_free[async_k], 0));
         stage_rgba = (float*)ctx->alloc(ctx->async_rgba[async_k], host_pix * 16);
         stage_depth = (float*)ctx->alloc(ctx->async_depth[async_k], host_pix * 4);
@@ -944,6 +979,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     if (ctx->loop_exec) cudaGraphExecDestroy(ctx->loop_exec);
     if (ctx->loop_graph) cudaGraphDestroy(ctx->loop_graph);
     if (ctx->loop_state) cudaFree(ctx->loop_state);
+    if (ctx->walk_stats) cudaFree(ctx->walk_stats);
     ctx->release(ctx->side_scratch);
     for (auto& kv : ctx->avatars)
         for (auto& f : kv.second->frames)
@@ -1744,6 +1780,7 @@ int insta_tuning_set(insta_ctx* ctx, const insta_tuning* t) {
         if (t->deform_blocks_per_sm > 64) fail(INSTA_ERR_INVALID_ARG, "deform_blocks_per_sm must be 0..64");
         if (t->bvh_top_nodes != 0 && t->bvh_top_nodes != 5 && t->bvh_top_nodes != 21)
             fail(INSTA_ERR_INVALID_ARG, "bvh_top_nodes must be 0, 5 or 21");
+        if (t->fused_field_stage > 1) fail(INSTA_ERR_INVALID_ARG, "fused_field_stage must be 0 or 1");
         ctx->tune = *t;
     });
 }
@@ -1798,14 +1835,14 @@ int insta_autotune(insta_ctx* ctx, const insta_render_desc* reqs, int n, int rep
         float cur_ms = 0.f;
         try {
             cur_ms = time_one(cur);
-            const std::vector<uint32_t> cands[5] = {{8, 16, 24, 32}, {15, 18, 21}, {1, 2, 3, 4}, {8, 12, 16, 24}, {0, 5, 21}};
+            const std::vector<uint32_t> cands[6] = {{8, 16, 24, 32}, {15, 18, 21}, {1, 2, 3, 4}, {8, 12, 16, 24}, {0, 5, 21}, {0, 1}};
             for (int pass = 0; pass < 2; ++pass) {
                 bool moved = false;
-                for (int f = 0; f < 5; ++f) {
+                for (int f = 0; f < 6; ++f) {
                     for (uint32_t v : cands[f]) {
                         insta_tuning t = cur;
                         uint32_t* field = f == 0 ? &t.max_steps_per_round : f == 1 ? &t.sort_cell_bits : f == 2 ? &t.mlp_ctas_per_sm
-                                        : f == 3 ? &t.deform_blocks_per_sm : &t.bvh_top_nodes;
+                                        : f == 3 ? &t.deform_blocks_per_sm : f == 4 ? &t.bvh_top_nodes : &t.fused_field_stage;
                         if (*field == v) continue;
                         *field = v;
                         const float ms = time_one(t);
@@ -1841,11 +1878,11 @@ int insta_stats_read(insta_ctx* ctx, insta_stats* out, int reset) {
         if (!out) fail(INSTA_ERR_INVALID_ARG, "null output");
         ctx->collect_timings();
         if (ctx->loop_rounds_total) {
-            // graph-run rounds: 10 kernels per round plus the loop condition per pair of rounds
+            // graph-run rounds: loop_round_kernels per round plus the loop condition per pair of rounds
             unsigned long long total = 0;
             CK(cudaMemcpy(&total, ctx->loop_rounds_total, sizeof(total), cudaMemcpyDeviceToHost));
             const unsigned long long d = total - ctx->loop_rounds_seen;
-            ctx->launches += d * 10ull + d / 2ull;
+            ctx->launches += d * ctx->loop_round_kernels + d / 2ull;
             ctx->loop_rounds_seen = total;
         }
         out->kernel_launches = ctx->launches;
@@ -1856,9 +1893,17 @@ int insta_stats_read(insta_ctx* ctx, insta_stats* out, int reset) {
             out->stage_ms[k] = (float)ctx->stage_ms[k];
             out->stage_calls[k] = ctx->stage_calls[k];
         }
+        unsigned long long walk[8] = {};
+        if (ctx->walk_stats) CK(cudaMemcpy(walk, ctx->walk_stats, sizeof(walk), cudaMemcpyDeviceToHost));
+        out->walk_warps = walk[0];
+        out->walk_inner_nodes = walk[1];
+        out->walk_leaves = walk[2];
+        out->walk_bound_tests = walk[3];
+        out->walk_exact_tests = walk[4];
         if (reset) {
             ctx->launches = 0;
             for (int k = 0; k < INSTA_STAGE_COUNT; ++k) { ctx->stage_ms[k] = 0.0; ctx->stage_calls[k] = 0; }
+            if (ctx->walk_stats) CK(cudaMemset(ctx->walk_stats, 0, 8 * sizeof(unsigned long long)));
         }
     });
 }
@@ -1932,6 +1977,7 @@ struct ServerReq {
     int slot = -1;
     bool cancel = false;
     bool started = false;   // its rays are in the wavefront
+    bool copying = false;   // rays done; its host outputs are being copied back (copy stream)
     std::string error;
     Clock::time_point t_submit, t_start, t_done;
 };
@@ -1964,6 +2010,9 @@ struct insta_server {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_ready = nullptr;
     std::vector<std::shared_ptr<ServerReq>> ready;
+    // output copies back to the host on the context's copy stream, after the rounds (ev_rounds)
+    cudaEvent_t ev_rounds = nullptr;
+    std::vector<cudaEvent_t> slot_copied;
 
     void finish(const std::shared_ptr<ServerReq>& r, int state, const std::string& err = std::string()) {
         std::lock_guard<std::mutex> lk(mu);
@@ -2089,20 +2138,53 @@ struct insta_server {
         r->slot = -1;
     }
 
-    // After a round: requests whose rays have all composited are done.
+    // After a round: requests whose rays have all composited are done.  Host outputs are copied
+    // back on the copy stream (page-locked host buffers let the copies overlap the next rounds);
+    // such a request keeps its slot until its copy has landed (poll_copies).
     void collect() {
+        bool any_copy = false;
         for (size_t s = 0; s < slot_req.size(); ++s) {
             auto r = slot_req[s];
-            if (!r || !r->started || r->state != INSTA_REQ_RUNNING || ctx->host_alive[s] != 0) continue;
+            if (!r || !r->started || r->copying || r->state != INSTA_REQ_RUNNING || ctx->host_alive[s] != 0) continue;
             if (r->host_out && !r->cancel) {
+                if (!any_copy) {
+                    CK(cudaEventRecord(ev_rounds, ctx->stream));
+                    CK(cudaStreamWaitEvent(ctx->copy, ev_rounds, 0));
+                    any_copy = true;
+                }
                 const size_t px = (size_t)r->desc.width * r->desc.height;
-                CK(cudaMemcpyAsync(r->out_rgba, slot_rgba[s].p, px * 16, cudaMemcpyDeviceToHost, ctx->stream));
-                CK(cudaMemcpyAsync(r->out_depth, slot_depth[s].p, px * 4, cudaMemcpyDeviceToHost, ctx->stream));
+                CK(cudaMemcpyAsync(r->out_rgba, slot_rgba[s].p, px * 16, cudaMemcpyDeviceToHost, ctx->copy));
+                CK(cudaMemcpyAsync(r->out_depth, slot_depth[s].p, px * 4, cudaMemcpyDeviceToHost, ctx->copy));
+                CK(cudaEventRecord(slot_copied[s], ctx->copy));
+                r->copying = true;
+                continue;
             }
-            CK(cudaStreamSynchronize(ctx->stream));
             release(r);
             finish(r, r->cancel ? INSTA_REQ_CANCELLED : INSTA_REQ_DONE);
         }
+        poll_copies(false);
+    }
+
+    // Requests whose output copies have landed are done; `wait_one` blocks for the oldest copy
+    // when nothing else is left to run.
+    void poll_copies(bool wait_one) {
+        for (size_t s = 0; s < slot_req.size(); ++s) {
+            auto r = slot_req[s];
+            if (!r || !r->copying) continue;
+            cudaError_t q = wait_one ? cudaEventSynchronize(slot_copied[s]) : cudaEventQuery(slot_copied[s]);
+            if (q == cudaErrorNotReady) continue;
+            CK(q);
+            wait_one = false;
+            r->copying = false;
+            release(r);
+            finish(r, INSTA_REQ_DONE);
+        }
+    }
+
+    bool any_copying() const {
+        for (auto& r : slot_req)
+            if (r && r->copying) return true;
+        return false;
     }
 
     void loop() {
@@ -2110,6 +2192,10 @@ struct insta_server {
         try {
             CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
             CK(cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&ev_rounds, cudaEventDisableTiming));
+            ensure_copy_stream(ctx);
+            slot_copied.resize(cfg.max_inflight);
+            for (auto& e : slot_copied) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
             ctx->alloc(slot_extra, (size_t)cfg.max_inflight * 64 * 4);
             for (;;) {
                 std::vector<std::shared_ptr<ServerReq>> batch;
@@ -2144,9 +2230,24 @@ struct insta_server {
                 start_ready();
                 if (!batch.empty()) build(batch);
                 if (inflight == 0) continue;
-                if (run.n_alive == 0 && !had_ready) continue;   // only builds in flight: start them next
-                run.round();
-                ++rounds;
+                if (run.n_alive == 0 && !had_ready) {
+                    // nothing to march: either frames still building (start them next) or only
+                    // output copies in flight (wait for the oldest)
+                    if (ready.empty() && batch.empty() && any_copying()) poll_copies(true);
+                    continue;
+                }
+                if (ctx->timing) {
+                    run.round();
+                    ++rounds;
+                } else {
+                    // the rounds up to the next admission point as one CUDA-graph launch (a
+                    // conditional while node stopping early when no ray is alive), then one host
+                    // read of the alive counts
+                    const uint32_t k = cfg.rounds_per_launch ? cfg.rounds_per_launch : 2u;
+                    run.device_rounds(k);
+                    run.n_alive = run.read_alive();
+                    rounds += k;
+                }
                 collect();
             }
         } catch (const std::exception& e) {
@@ -2174,6 +2275,7 @@ int insta_server_create(insta_ctx* ctx, const insta_server_config* cfg, insta_se
         if (cfg->max_inflight_pixels < 1 || cfg->max_inflight_pixels > kMaxRoundSamples)
             fail(INSTA_ERR_INVALID_ARG, "max_inflight_pixels must be 1..2^25");
         if (!(cfg->occupancy_radius > 0.0)) fail(INSTA_ERR_INVALID_ARG, "occupancy_radius must be positive");
+        if (cfg->rounds_per_launch % 2 || cfg->rounds_per_launch > 64) fail(INSTA_ERR_INVALID_ARG, "rounds_per_launch must be even, 0..64");
         auto s = std::make_unique<insta_server>();
         s->ctx = ctx;
         s->cfg = *cfg;
@@ -2199,6 +2301,9 @@ int insta_server_destroy(insta_server* s) {
     if (s->worker.joinable()) s->worker.join();   // in-flight requests finish first
     if (s->side) { cudaStreamSynchronize(s->side); cudaStreamDestroy(s->side); }
     if (s->ev_ready) cudaEventDestroy(s->ev_ready);
+    if (s->ctx->copy) cudaStreamSynchronize(s->ctx->copy);
+    if (s->ev_rounds) cudaEventDestroy(s->ev_rounds);
+    for (auto& e : s->slot_copied) cudaEventDestroy(e);
     for (auto& b : s->slot_rgba) s->ctx->release(b);
     for (auto& b : s->slot_depth) s->ctx->release(b);
     s->ctx->release(s->slot_extra);

@@ -12,8 +12,9 @@ namespace insta {
 
 struct TriFrame;
 
-// Tile plan of the MLP weight image (see mlp_tiles.cuh); plain data shared with the host.
+// Tile plan of the MLP weight image and the MLP launch arguments (see mlp_tiles.cuh).
 struct TilePlan;
+struct MlpArgs;
 
 // Alive-ray list, structure of arrays (float4 each):
 //   a = (origin.xyz, t)   b = (dir.xyz, max_weight)   c = rgba   d = (depth, pixel, samples so far, request)
@@ -98,6 +99,7 @@ struct WaveArgs {
     const float4* out_f32;      // per sample when the MLP runs in BF16
     unsigned long long* sample_counter;
     uint32_t top_nodes;         // nearest stage: top tree nodes each warp stages in shared memory (0: none)
+    unsigned long long* walk_stats;  // nearest stage: walk counters (see nearest_warp), or null
     uint32_t* err;
 };
 
@@ -156,6 +158,9 @@ cudaError_t launch_ray_init(const WaveArgs& a, uint32_t total_tiles, cudaStream_
 cudaError_t launch_march(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_deform_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s);
+cudaError_t launch_nearest_stage(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s);
+// deform + encode + MLP in one kernel after launch_nearest_stage (FP16 / BF16 fields)
+cudaError_t launch_field_fused(const WaveArgs& a, const MlpArgs& m, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm);
 cudaError_t launch_composite(const WaveArgs& a, cudaStream_t s);
 // generate_training_samples_nerf on caller-supplied rays (see insta_training_samples).
 struct TrainArgs {

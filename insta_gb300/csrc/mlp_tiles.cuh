@@ -68,7 +68,8 @@ struct TileSmem {
 // One MMA chain: sum over (A_i, B_i) pairs into TMEM columns [col, col + N).  K in elements;
 // f8: E4M3 operands (kind::f8f6f4, 32 elements per instruction), else FP16/BF16 (16 per
 // instruction).  Either way one instruction consumes 32 bytes of each row.
-__device__ __forceinline__ bool issue_chain(TileSmem& sm, const uint8_t* const* a, const uint8_t* const* b, const uint32_t* K,
+template <typename Smem>
+__device__ __forceinline__ bool issue_chain(Smem& sm, const uint8_t* const* a, const uint8_t* const* b, const uint32_t* K,
                                             int n, uint32_t N, uint32_t col, bool bf16, uint32_t& phase, bool f8 = false) {
     fence_async_smem();
     tc_fence_before();
@@ -176,6 +177,138 @@ __device__ __forceinline__ bool mlp_tile(TileSmem& sm, const uint8_t* w, const T
     return ok;
 }
 
+// ------------------------------------------------------------------ fused tiles (256 threads)
+// Shared memory of the fused deform + encode + MLP kernel: one 128-sample tile at a time per CTA,
+// encoded in place by the CTA's own threads (two per sample), so the operand rows never leave the
+// SM.  a_h first carries the deform stage's hand-off to the encode (canonical position, direction
+// and region of each row); the hash rows of `stage` are dead once density layer 0 has run and then
+// hold the density output rows (colour input part 1).
+struct FusedSmem {
+    alignas(1024) uint8_t stage[128 * 64 * 2];   // hash rows [128][k_in], then SH rows [128][16]
+    alignas(1024) uint8_t a_h[128 * 64 * 2];     // hidden activations
+    alignas(8) uint64_t bar_mma;
+    alignas(8) uint64_t bar_w;
+    uint32_t tmem_base;
+};
+
+// Shared memory of the 256-thread MLP kernel over ready-made operand tiles: the tile record is
+// brought in by two bulk copies -- its hash rows once density layer 0 of the previous tile has run,
+// its SH rows once colour layer 0 has -- so the next tile loads while this one computes.
+// Dynamic shared memory, in 1 KiB-aligned pieces sized by the tile plan: control block, a_h
+// [128][64], the tile record (tile_bytes), a_dens [128][16], the weight image.
+struct Mlp2Ctl {
+    uint64_t bar_mma;
+    uint64_t bar_load;   // both parts of the next tile (two arrivals)
+    uint64_t bar_w;
+    uint32_t tmem_base;
+};
+struct Mlp2View {
+    uint64_t& bar_mma;
+    uint32_t& tmem_base;
+    uint8_t* stage;
+    uint8_t* a_h;
+    uint8_t* a_dens;
+    uint8_t* w;
+};
+__host__ __device__ constexpr uint32_t mlp2_round(uint32_t b) { return (b + 1023u) & ~1023u; }
+__host__ __device__ constexpr uint32_t mlp2_xch_off() { return 1024u; }   // FP8: [2][128] row maxima
+__host__ __device__ constexpr uint32_t mlp2_a_h_off() { return 2048u; }
+__host__ __device__ constexpr uint32_t mlp2_stage_off() { return 2048u + 128u * 64u * 2u; }
+__host__ __device__ constexpr uint32_t mlp2_dens_off(uint32_t tile_bytes) { return mlp2_stage_off() + mlp2_round(tile_bytes); }
+__host__ __device__ constexpr uint32_t mlp2_w_off(uint32_t tile_bytes) { return mlp2_dens_off(tile_bytes) + 128u * 16u * 2u; }
+
+struct NoHook {
+    __device__ void operator()() const {}
+};
+
+template <typename Smem>
+__device__ __forceinline__ uint32_t fused_lane_addr(const Smem& sm, uint32_t col) {
+    return sm.tmem_base + ((((uint32_t)threadIdx.x / 32u) % 4u) * 32u << 16) + col;
+}
+
+// ReLU + rounding of 64 accumulator columns into a_h; warpgroup g (threads 128 g ...) takes
+// columns [32 g, 32 g + 32) of its row (TMEM lane quarter = warp % 4).
+template <typename Smem>
+__device__ __forceinline__ void relu_to_ah2(Smem& sm, bool bf16) {
+    const uint32_t r = threadIdx.x & 127u, c0 = (threadIdx.x >> 7) * 32u;
+#pragma unroll 1
+    for (uint32_t c = c0; c < c0 + 32u; c += 16) {
+        float v[16];
+        tmem_ld16(fused_lane_addr(sm, c), v);
+        __half h[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) h[i] = to_act(fmaxf(v[i], 0.f), bf16);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            uint4 u;
+            u.x = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 0]);
+            u.y = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 2]);
+            u.z = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 4]);
+            u.w = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 6]);
+            *reinterpret_cast<uint4*>(sm.a_h + tile_offset(r, c + q * 8, 64)) = u;
+        }
+    }
+}
+
+// Both MLPs (FP16 or BF16) with 256 threads on the tile in sm.stage; warpgroup 0 returns its
+// row's (r, g, b, raw density).  The arithmetic is mlp_tile's: the same operand tiles,
+// instruction sequence and roundings, so the outputs are the same bits.  hash_free / sh_free run
+// (all threads) as soon as the tensor core is done with the hash rows / the SH rows.
+template <typename Smem, typename HashFree = NoHook, typename ShFree = NoHook>
+__device__ __forceinline__ bool mlp256(Smem& sm, uint8_t* a_dens, const uint8_t* w, const TilePlan& P, bool bf16, uint32_t& phase,
+                                       float* out4, HashFree hash_free = HashFree(), ShFree sh_free = ShFree()) {
+    bool ok = true;
+    const uint8_t* hash = sm.stage;
+    const uint8_t* sh = sm.stage + hash_tile_bytes(P.k_in);
+    const bool wg0 = threadIdx.x < 128u;
+    const uint8_t* a;
+    const uint8_t* b;
+    uint32_t K;
+    a = hash; b = w + P.d_off[0]; K = P.k_in;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
+    hash_free();
+    relu_to_ah2(sm, bf16);
+    for (uint32_t l = 1; l < P.n_dh; ++l) {
+        a = sm.a_h; b = w + P.d_off[l]; K = 64;
+        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
+        relu_to_ah2(sm, bf16);
+    }
+    a = sm.a_h; b = w + P.d_out; K = 64;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, bf16, phase);
+    if (wg0) {
+        float v[16];
+        tmem_ld16(fused_lane_addr(sm, 64), v);
+        __half h[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) h[i] = to_act(v[i], bf16);
+        out4[3] = from_act(h[0], bf16);
+        store_row(a_dens, threadIdx.x, 16, h);
+    }
+    {
+        const uint8_t* as[2] = {a_dens, sh};
+        const uint8_t* bs[2] = {w + P.r0_dens, w + P.r0_sh};
+        const uint32_t Ks[2] = {16, 16};
+        ok &= issue_chain(sm, as, bs, Ks, 2, 64, 0, bf16, phase);
+        sh_free();
+        relu_to_ah2(sm, bf16);
+    }
+    for (uint32_t l = 1; l < P.n_rh; ++l) {
+        a = sm.a_h; b = w + P.r_off[l]; K = 64;
+        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
+        relu_to_ah2(sm, bf16);
+    }
+    a = sm.a_h; b = w + P.r_out; K = 64;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, bf16, phase);
+    if (wg0) {
+        float v[16];
+        tmem_ld16(fused_lane_addr(sm, 64), v);
+        out4[0] = from_act(to_act(v[0], bf16), bf16);
+        out4[1] = from_act(to_act(v[1], bf16), bf16);
+        out4[2] = from_act(to_act(v[2], bf16), bf16);
+    }
+    return ok;
+}
+
 // ------------------------------------------------------------------ FP8 (E4M3) variant
 // Every layer input row gets its own scale a = max|x| / 448 (rounded to E4M3 after multiplying by
 // 448 / max|x|); weights carry a per-layer scale s; the FP32 accumulator is multiplied back by a,
@@ -202,6 +335,19 @@ __device__ __forceinline__ void store16_e4m3(uint8_t* tile, uint32_t K, uint32_t
     *reinterpret_cast<uint4*>(tile + tile_offset8(threadIdx.x, k, K)) = u;
 }
 
+// The same for row r (threads other than r's own 128-thread layout).
+__device__ __forceinline__ void store16_e4m3_row(uint8_t* tile, uint32_t K, uint32_t k, const float* v, float inv, uint32_t r) {
+    float q[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) q[i] = __fmul_rn(v[i], inv);
+    uint4 u;
+    u.x = e4m3x4(q[0], q[1], q[2], q[3], 0.f);
+    u.y = e4m3x4(q[4], q[5], q[6], q[7], 0.f);
+    u.z = e4m3x4(q[8], q[9], q[10], q[11], 0.f);
+    u.w = e4m3x4(q[12], q[13], q[14], q[15], 0.f);
+    *reinterpret_cast<uint4*>(tile + tile_offset8(r, k, K)) = u;
+}
+
 // Row scale a = max / 448 (multiplies the accumulator back) and its quantising factor 448 / max.
 __device__ __forceinline__ float row_scale(float mx) { return mx > 0.f ? __fdiv_rn(mx, 448.0f) : 1.0f; }
 __device__ __forceinline__ float row_inv(float mx) { return mx > 0.f ? __fdiv_rn(448.0f, mx) : 1.0f; }
@@ -211,6 +357,20 @@ __device__ __forceinline__ void load16_half(const uint8_t* tile, uint32_t K, uin
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
         const uint4 u = *reinterpret_cast<const uint4*>(tile + tile_offset(threadIdx.x, k + 8 * q, K));
+        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w[i]));
+            v[8 * q + 2 * i] = f.x;
+            v[8 * q + 2 * i + 1] = f.y;
+        }
+    }
+}
+
+__device__ __forceinline__ void load16_half_row(const uint8_t* tile, uint32_t K, uint32_t k, float* v, uint32_t r) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const uint4 u = *reinterpret_cast<const uint4*>(tile + tile_offset(r, k + 8 * q, K));
         const uint32_t w[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -333,6 +493,137 @@ __device__ __forceinline__ void store_row_global(uint8_t* tile, uint32_t r, uint
         q.w = *reinterpret_cast<const uint32_t*>(&v[c * 8 + 6]);
         *reinterpret_cast<uint4*>(tile + tile_offset(r, c * 8, K)) = q;
     }
+}
+
+}  // namespace insta
+
+namespace insta {
+
+// ------------------------------------------------------------------ FP8 with 256 threads
+// The FP8 chain of mlp_tile8 with the row work split between the warpgroups: each quantises half
+// of a row's columns; the row maximum that sets the row scale is exchanged through `xch`
+// ([2][128] floats), so both halves use the same scale and the values are those of mlp_tile8.
+__device__ __forceinline__ float row_max2(float* xch, float m) {
+    const uint32_t r = threadIdx.x & 127u, g = threadIdx.x >> 7;
+    xch[g * 128u + r] = m;
+    __syncthreads();
+    const float o = xch[(g ^ 1u) * 128u + r];
+    __syncthreads();   // the buffer is reused by the next exchange
+    return fmaxf(m, o);
+}
+
+template <typename Smem>
+__device__ __forceinline__ float hidden_to_e4m3_2(Smem& sm, float* xch, uint8_t* a_h8, float a, float s) {
+    const uint32_t c0 = (threadIdx.x >> 7) * 32u;
+    float mx = 0.f;
+#pragma unroll 1
+    for (uint32_t c = c0; c < c0 + 32u; c += 16) {
+        float v[16];
+        tmem_ld16(fused_lane_addr(sm, c), v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fmaxf(__fmul_rn(__fmul_rn(v[i], a), s), 0.f));
+    }
+    mx = row_max2(xch, mx);
+    const float inv = row_inv(mx);
+#pragma unroll 1
+    for (uint32_t c = c0; c < c0 + 32u; c += 16) {
+        float v[16];
+        tmem_ld16(fused_lane_addr(sm, c), v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = fmaxf(__fmul_rn(__fmul_rn(v[i], a), s), 0.f);
+        store16_e4m3_row(a_h8, 64, c, v, inv, threadIdx.x & 127u);
+    }
+    return row_scale(mx);
+}
+
+template <typename Smem, typename HashFree = NoHook, typename ShFree = NoHook>
+__device__ __forceinline__ bool mlp256_8(Smem& sm, float* xch, uint8_t* a_rgb8, const uint8_t* w, const TilePlan& P, const float* ls,
+                                         uint32_t& phase, float* out4, HashFree hash_free = HashFree(), ShFree sh_free = ShFree()) {
+    bool ok = true;
+    const uint32_t r = threadIdx.x & 127u, g = threadIdx.x >> 7;
+    const bool wg0 = g == 0u;
+    const uint8_t* hash = sm.stage;
+    const uint8_t* sh = sm.stage + hash_tile_bytes(P.k_in);
+    uint8_t* a_h8 = sm.a_h;            // [128][64] E4M3
+    uint8_t* a_in8 = sm.a_h + 8192;    // [128][k8 <= 64] E4M3
+    const uint8_t* a;
+    const uint8_t* b;
+    uint32_t K;
+    int li = 0;
+    // density input: the FP16 hash row (k_in values, zero-padded to k8), half the columns each
+    const uint32_t half = P.k8 / 2u, c0 = g * half;
+    float mx = 0.f;
+    for (uint32_t c = c0; c < c0 + half; c += 16) {
+        if (c >= P.k_in) continue;
+        float v[16];
+        load16_half_row(hash, P.k_in, c, v, r);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fabsf(v[i]));
+    }
+    mx = row_max2(xch, mx);
+    float ra = row_scale(mx);
+    const float inv0 = row_inv(mx);
+    for (uint32_t c = c0; c < c0 + half; c += 16) {
+        float v[16];
+        if (c < P.k_in) load16_half_row(hash, P.k_in, c, v, r);
+        else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[i] = 0.f;
+        }
+        store16_e4m3_row(a_in8, P.k8, c, v, inv0, r);
+    }
+    a = a_in8; b = w + P.d_off[0]; K = P.k8;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
+    hash_free();
+    ra = hidden_to_e4m3_2(sm, xch, a_h8, ra, ls[li++]);
+    for (uint32_t l = 1; l < P.n_dh; ++l) {
+        a = a_h8; b = w + P.d_off[l]; K = 64;
+        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
+        ra = hidden_to_e4m3_2(sm, xch, a_h8, ra, ls[li++]);
+    }
+    // density output (16): raw density is column 0; colour input = [density out | SH] (warpgroup 0)
+    a = a_h8; b = w + P.d_out; K = 64;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, false, phase, true);
+    float dens[16], shv[16];
+    mx = 0.f;
+    if (wg0) {
+        float v[16];
+        tmem_ld16(fused_lane_addr(sm, 64), v);
+        const float sd = ls[li];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dens[i] = __fmul_rn(__fmul_rn(v[i], ra), sd);
+        out4[3] = dens[0];
+        load16_half_row(sh, 16, 0, shv, r);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fmaxf(fabsf(dens[i]), fabsf(shv[i])));
+    }
+    ++li;
+    mx = row_max2(xch, mx);
+    ra = row_scale(mx);
+    if (wg0) {
+        store16_e4m3_row(a_rgb8, 32, 0, dens, row_inv(mx), r);
+        store16_e4m3_row(a_rgb8, 32, 16, shv, row_inv(mx), r);
+    }
+    a = a_rgb8; b = w + P.r0_dens; K = 32;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
+    sh_free();
+    ra = hidden_to_e4m3_2(sm, xch, a_h8, ra, ls[li++]);
+    for (uint32_t l = 1; l < P.n_rh; ++l) {
+        a = a_h8; b = w + P.r_off[l]; K = 64;
+        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
+        ra = hidden_to_e4m3_2(sm, xch, a_h8, ra, ls[li++]);
+    }
+    a = a_h8; b = w + P.r_out; K = 64;
+    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, false, phase, true);
+    if (wg0) {
+        float v[16];
+        tmem_ld16(fused_lane_addr(sm, 64), v);
+        const float so = ls[li];
+        out4[0] = __fmul_rn(__fmul_rn(v[0], ra), so);
+        out4[1] = __fmul_rn(__fmul_rn(v[1], ra), so);
+        out4[2] = __fmul_rn(__fmul_rn(v[2], ra), so);
+    }
+    return ok;
 }
 
 }  // namespace insta

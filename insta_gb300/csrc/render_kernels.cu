@@ -102,16 +102,17 @@ __device__ __forceinline__ uint32_t pack_act(float a, float b, bool bf16) {
     return (uint32_t)__half_as_ushort(x) | ((uint32_t)__half_as_ushort(y) << 16);
 }
 
-// One sample's operand rows: hash features (+ expression dims) into the hash tile, SH of the
-// direction into the SH tile.  Four levels at a time (32 gathers in flight), each group of 8
-// values stored as one 16-byte chunk of the row, so no per-sample array is materialised.
-__device__ __forceinline__ void encode_sample(const FieldView& fv, const uint16_t* table, const float* extra, uint32_t mask,
-                                              const float* pos, const float* dirw, uint8_t* rec, uint32_t row, uint32_t k_in) {
+// Parts of one sample's operand rows: hash features of level groups [g0, g1) (four levels, 32
+// gathers in flight, per group, each group of 8 values stored as one 16-byte chunk of the row),
+// the expression dims, and SH of the direction into the SH tile.  No per-sample array is
+// materialised.
+__device__ __forceinline__ void encode_levels(const FieldView& fv, const uint16_t* table, const float* pos, uint8_t* rec, uint32_t row,
+                                              uint32_t k_in, uint32_t g0, uint32_t g1) {
     const bool bf16 = fv.precision == 1;
     const __half2* t2 = reinterpret_cast<const __half2*>(table);
     const V3 x = v3(pos[0], pos[1], pos[2]);
 #pragma unroll 1
-    for (uint32_t g = 0; g < fv.n_levels / 4; ++g) {
+    for (uint32_t g = g0; g < g1; ++g) {
         float v[8];
 #pragma unroll
         for (uint32_t j = 0; j < 4; ++j) hash_level(fv, t2, x, 4 * g + j, v[2 * j], v[2 * j + 1]);
@@ -120,6 +121,9 @@ __device__ __forceinline__ void encode_sample(const FieldView& fv, const uint16_
         q.z = pack_act(v[4], v[5], bf16); q.w = pack_act(v[6], v[7], bf16);
         *reinterpret_cast<uint4*>(rec + tile_offset(row, 8 * g, k_in)) = q;
     }
+}
+__device__ __forceinline__ void encode_extra(const FieldView& fv, const float* extra, uint32_t mask, uint8_t* rec, uint32_t row, uint32_t k_in) {
+    const bool bf16 = fv.precision == 1;
     for (uint32_t g = 0; g < fv.n_extra / 8; ++g) {
         float v[8];
 #pragma unroll
@@ -129,6 +133,9 @@ __device__ __forceinline__ void encode_sample(const FieldView& fv, const uint16_
         q.z = pack_act(v[4], v[5], bf16); q.w = pack_act(v[6], v[7], bf16);
         *reinterpret_cast<uint4*>(rec + tile_offset(row, 2 * fv.n_levels + 8 * g, k_in)) = q;
     }
+}
+__device__ __forceinline__ void encode_sh(const FieldView& fv, const float* dirw, uint8_t* rec, uint32_t row, uint32_t k_in) {
+    const bool bf16 = fv.precision == 1;
     float d[16];
     sh4(dirw[0], dirw[1], dirw[2], d);
     uint8_t* sh = rec + hash_tile_bytes(k_in);
@@ -139,6 +146,15 @@ __device__ __forceinline__ void encode_sample(const FieldView& fv, const uint16_
         q.z = pack_act(d[8 * g + 4], d[8 * g + 5], bf16); q.w = pack_act(d[8 * g + 6], d[8 * g + 7], bf16);
         *reinterpret_cast<uint4*>(sh + tile_offset(row, 8 * g, 16)) = q;
     }
+}
+
+// One sample's operand rows: hash features (+ expression dims) into the hash tile, SH of the
+// direction into the SH tile.
+__device__ __forceinline__ void encode_sample(const FieldView& fv, const uint16_t* table, const float* extra, uint32_t mask,
+                                              const float* pos, const float* dirw, uint8_t* rec, uint32_t row, uint32_t k_in) {
+    encode_levels(fv, table, pos, rec, row, k_in, 0, fv.n_levels / 4);
+    encode_extra(fv, extra, mask, rec, row, k_in);
+    encode_sh(fv, dirw, rec, row, k_in);
 }
 
 // One thread per alive ray: the next `steps` sample positions (generate_next_nerf_network_inputs,
@@ -475,11 +491,48 @@ __global__ void __launch_bounds__(256, 4) nearest_stage_kernel(const __grid_cons
                 if (lane == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
             }
         }
-        Nearest q = nearest_warp(R.fr, p, in_box, wscratch[warp], A.err, __builtin_huge_valf(), top, n_top);
+        Nearest q = nearest_warp(R.fr, p, in_box, wscratch[warp], A.err, __builtin_huge_valf(), top, n_top, A.walk_stats);
         if (valid) A.sample_key[s] = in_box ? (uint32_t)q.id : 0xfffffffeu;
     }
     // a copy that timed out may still land: wait for it (bounded) before the CTA's shared memory goes
     if (A.top_nodes > 0 && !top_ok) mbar_wait(&top_bar[warp], top_phase);
+}
+
+// The deform half of the stage for sorted position s holding march-order sample m: the warp hook
+// (src/core.cu:470-519) on warp_position(pos) / warp_direction(dir) with the nearest triangle the
+// nearest stage left in sample_key[s]; records where the sample went (sample_index) and its
+// (dt, depth candidate) for the composite.  Returns the request slot.
+__device__ __forceinline__ uint32_t deform_sample(const WaveArgs& A, uint32_t s, uint32_t m, uint32_t n_alive, float* cpos, float* cdir,
+                                                  uint32_t& mask) {
+    const uint32_t rk = A.sample_ray[m];
+    const float4 smp = A.samples[m];
+    const float4 rb = A.rays_in.b[rk & kRayMask];
+    const uint32_t req = __float_as_uint(A.rays_in.d[rk & kRayMask].w);
+    A.sample_index[(size_t)(rk >> kStepShift) * n_alive + (rk & kRayMask)] = s;
+    const ReqView& R = A.reqs[req];
+    const RenderView& rv = R.rv;
+    float cw[3], dw[3], dp[3];
+    const float pp[3] = {smp.x, smp.y, smp.z}, dd[3] = {rb.x, rb.y, rb.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        cw[k] = __fdiv_rn(__fsub_rn(pp[k], rv.train_min[k]), __fsub_rn(rv.train_max[k], rv.train_min[k]));
+        dw[k] = __fmul_rn(__fadd_rn(dd[k], 1.0f), 0.5f);
+        dp[k] = __fadd_rn(rv.train_min[k], __fmul_rn(cw[k], __fsub_rn(rv.train_max[k], rv.train_min[k])));
+    }
+    cpos[0] = cw[0]; cpos[1] = cw[1]; cpos[2] = cw[2];
+    cdir[0] = dw[0]; cdir[1] = dw[1]; cdir[2] = dw[2];
+    mask = 7u;
+    const V3 p = v3(cw[0], cw[1], cw[2]);
+    const uint32_t id = A.sample_key[s];
+    if (id != 0xfffffffeu) {
+        if ((int32_t)id >= 0) map_to_canonical(R.dv, R.fr.frames, id, p, dw, cpos, cdir, &mask);
+        else atomicOr(A.err, INSTA_DEVERR_NO_TRI);
+    }
+    const V3 cam_fwd = v3(rv.cam[2], rv.cam[6], rv.cam[10]);
+    const V3 cam_pos = v3(rv.cam[3], rv.cam[7], rv.cam[11]);
+    const V3 dv = v3(__fsub_rn(dp[0], cam_pos.x), __fsub_rn(dp[1], cam_pos.y), __fsub_rn(dp[2], cam_pos.z));
+    A.aux[s] = make_float2(smp.w, dot_rn(cam_fwd, dv));
+    return req;
 }
 
 __global__ void __launch_bounds__(256, 4) map_encode_kernel(const __grid_constant__ WaveArgs A) {
@@ -488,35 +541,12 @@ __global__ void __launch_bounds__(256, 4) map_encode_kernel(const __grid_constan
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         const uint32_t m = A.sample_order[s];
         if (m == kNoSample) continue;
-        const uint32_t rk = A.sample_ray[m];
-        const float4 smp = A.samples[m];
-        const float4 rb = A.rays_in.b[rk & kRayMask];
-        const uint32_t req = __float_as_uint(A.rays_in.d[rk & kRayMask].w);
-        A.sample_index[(size_t)(rk >> kStepShift) * n_alive + (rk & kRayMask)] = s;
+        float cpos[3], cdir[3];
+        uint32_t mask;
+        const uint32_t req = deform_sample(A, s, m, n_alive, cpos, cdir, mask);
         const ReqView& R = A.reqs[req];
-        const RenderView& rv = R.rv;
-        float cw[3], dw[3], dp[3];
-        const float pp[3] = {smp.x, smp.y, smp.z}, dd[3] = {rb.x, rb.y, rb.z};
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            cw[k] = __fdiv_rn(__fsub_rn(pp[k], rv.train_min[k]), __fsub_rn(rv.train_max[k], rv.train_min[k]));
-            dw[k] = __fmul_rn(__fadd_rn(dd[k], 1.0f), 0.5f);
-            dp[k] = __fadd_rn(rv.train_min[k], __fmul_rn(cw[k], __fsub_rn(rv.train_max[k], rv.train_min[k])));
-        }
-        float cpos[3] = {cw[0], cw[1], cw[2]}, cdir[3] = {dw[0], dw[1], dw[2]};
-        uint32_t mask = 7u;
-        const V3 p = v3(cw[0], cw[1], cw[2]);
-        const uint32_t id = A.sample_key[s];
-        if (id != 0xfffffffeu) {
-            if ((int32_t)id >= 0) map_to_canonical(R.dv, R.fr.frames, id, p, dw, cpos, cdir, &mask);
-            else atomicOr(A.err, INSTA_DEVERR_NO_TRI);
-        }
         uint8_t* rec = A.tiles + (size_t)(s >> 7) * A.tile_bytes;
         encode_sample(A.fv, R.table, R.extra, mask, cpos, cdir, rec, s & 127u, A.k_in);
-        const V3 cam_fwd = v3(rv.cam[2], rv.cam[6], rv.cam[10]);
-        const V3 cam_pos = v3(rv.cam[3], rv.cam[7], rv.cam[11]);
-        const V3 dv = v3(__fsub_rn(dp[0], cam_pos.x), __fsub_rn(dp[1], cam_pos.y), __fsub_rn(dp[2], cam_pos.z));
-        A.aux[s] = make_float2(smp.w, dot_rn(cam_fwd, dv));
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(A.sample_counter, (unsigned long long)*A.n_samples_round);
 }
@@ -526,16 +556,21 @@ __device__ __forceinline__ void load_tile(TileSmem& sm, int buf, const uint8_t* 
     bulk_load(sm.stage[buf], src, bytes, &sm.bar_load[buf]);
 }
 
-// Weight image of tile t: the request whose padded run holds it (render batches), else the field's.
-__device__ __forceinline__ const uint8_t* tile_weights(const MlpArgs& A, uint32_t t) {
-    if (!A.seg) return A.fv.mlp_smem;
+// Request slot of tile t: the request whose padded run holds it (render batches; 0 otherwise).
+__device__ __forceinline__ uint32_t tile_request(const MlpArgs& A, uint32_t t) {
+    if (!A.seg) return 0;
     const uint32_t row = t * 128u;
     uint32_t lo = 0, hi = A.n_reqs;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         if (__ldg(A.seg + mid) <= row) lo = mid; else hi = mid;
     }
-    return A.reqs[lo].mlp;
+    return lo;
+}
+
+// Weight image of tile t: its request's (render batches), else the field's.
+__device__ __forceinline__ const uint8_t* tile_weights(const MlpArgs& A, uint32_t t) {
+    return A.seg ? A.reqs[tile_request(A, t)].mlp : A.fv.mlp_smem;
 }
 
 // Each CTA takes a contiguous range of tiles (consecutive tiles mostly share a request, so the
@@ -617,6 +652,201 @@ __global__ void __launch_bounds__(128) mlp_kernel(const __grid_constant__ MlpArg
     if (!ok && threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
     // drain an outstanding prefetch (bounded wait) before the CTA's shared memory is released
     if (pending) mbar_wait(&sm.bar_load[pending - 1], load_phase[pending - 1]);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x < 32) tmem_dealloc(sm.tmem_base, 128);
+}
+
+// The MLPs over ready-made operand tiles in global memory, 256 threads per CTA: each
+// CTA takes a contiguous range of tiles (consecutive tiles mostly share a request, so the weight
+// image is reloaded only where a range crosses into another avatar's requests); tile t + 1's
+// hash rows are bulk-copied in as soon as tile t's density layer 0 has run, its SH rows as soon
+// as colour layer 0 has, so the copies overlap the chain; the epilogues split the accumulator
+// columns between the two warpgroups (FP8: each warpgroup re-quantises half of a row, the row
+// maximum exchanged through shared memory).  Same arithmetic as mlp_kernel.
+__global__ void __launch_bounds__(256) mlp256_kernel(const __grid_constant__ MlpArgs A) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    Mlp2Ctl& ctl = *reinterpret_cast<Mlp2Ctl*>(smem_raw);
+    Mlp2View sm{ctl.bar_mma, ctl.tmem_base, smem_raw + mlp2_stage_off(), smem_raw + mlp2_a_h_off(),
+                smem_raw + mlp2_dens_off(A.plan.tile_bytes), smem_raw + mlp2_w_off(A.plan.tile_bytes)};
+    uint8_t* w = sm.w;
+    const uint32_t n_samples = A.n_alive ? *A.n_alive : (uint32_t)A.n_samples;
+    const uint32_t n_tiles = (n_samples + 127u) / 128u;
+    const uint32_t per = (n_tiles + gridDim.x - 1) / gridDim.x;
+    const uint32_t t0 = blockIdx.x * per, t1 = min(n_tiles, t0 + per);
+    if (t0 >= t1) return;
+    const uint32_t hash_bytes = hash_tile_bytes(A.plan.k_in), sh_bytes = sh_tile_bytes();
+    if (threadIdx.x == 0) {
+        mbar_init(&ctl.bar_mma, 1);
+        mbar_init(&ctl.bar_load, 2);
+        mbar_init(&ctl.bar_w, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) tmem_alloc(&ctl.tmem_base, 128);
+    const uint8_t* loaded = tile_weights(A, t0);
+    if (threadIdx.x == 0) {
+        bulk_load(w, loaded, A.plan.bytes, &ctl.bar_w);
+        const uint8_t* src = A.tiles + (size_t)t0 * A.plan.tile_bytes;
+        bulk_load(sm.stage, src, hash_bytes, &ctl.bar_load);
+        bulk_load(sm.stage + hash_bytes, src + hash_bytes, sh_bytes, &ctl.bar_load);
+    }
+    uint32_t w_phase = 0, load_phase = 0, phase = 0;
+    bool ok = mbar_wait(&ctl.bar_w, w_phase);
+    w_phase ^= 1u;
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const bool bf16 = A.fv.precision == 1, fp8 = A.fv.precision == 2;
+    float* xch = reinterpret_cast<float*>(smem_raw + mlp2_xch_off());
+    bool pending = true;   // a tile's copies are in flight
+    for (uint32_t t = t0; t < t1 && ok; ++t) {
+        ok &= mbar_wait(&ctl.bar_load, load_phase);
+        load_phase ^= 1u;
+        pending = false;
+        const uint8_t* need = tile_weights(A, t);
+        if (need != loaded) {
+            // the previous tile's MMAs have completed (mlp256 waited on them); swap the image
+            if (threadIdx.x == 0) bulk_load(w, need, A.plan.bytes, &ctl.bar_w);
+            ok &= mbar_wait(&ctl.bar_w, w_phase);
+            w_phase ^= 1u;
+            loaded = need;
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+        }
+        const bool next = t + 1 < t1;
+        const uint8_t* nsrc = A.tiles + (size_t)(t + 1) * A.plan.tile_bytes;
+        auto hash_free = [&] {
+            if (next && threadIdx.x == 0) bulk_load(sm.stage, nsrc, hash_bytes, &ctl.bar_load);
+        };
+        auto sh_free = [&] {
+            if (next && threadIdx.x == 0) bulk_load(sm.stage + hash_bytes, nsrc + hash_bytes, sh_bytes, &ctl.bar_load);
+        };
+        pending = next;
+        float o4[4];
+        if (fp8) ok &= mlp256_8(sm, xch, sm.a_dens, w, A.plan, reinterpret_cast<const float*>(w + A.plan.scales), phase, o4, hash_free, sh_free);
+        else ok &= mlp256(sm, sm.a_dens, w, A.plan, bf16, phase, o4, hash_free, sh_free);
+        const uint32_t s = t * 128u + threadIdx.x;
+        if (threadIdx.x < 128u && s < n_samples) {
+            if (A.fv.precision != 0) {
+                A.out_f32[s] = make_float4(o4[0], o4[1], o4[2], o4[3]);
+            } else {
+                __half2 rg = __floats2half2_rn(o4[0], o4[1]);
+                __half2 bd = __floats2half2_rn(o4[2], o4[3]);
+                uint2 u;
+                u.x = *reinterpret_cast<uint32_t*>(&rg);
+                u.y = *reinterpret_cast<uint32_t*>(&bd);
+                A.out[s] = u;
+            }
+        }
+        ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
+    // drain the copies of a tile that will not run (bounded wait) before shared memory is released
+    if (pending) mbar_wait(&ctl.bar_load, load_phase);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x < 32) tmem_dealloc(ctl.tmem_base, 128);
+}
+
+// ------------------------------------------------------------------ fused deform + encode + MLP
+// The stage after the nearest-triangle walk in one launch over the sorted stream (FP16 / BF16
+// MLPs): a CTA of 256 threads takes a contiguous range of 128-sample tiles.  Per tile, warpgroup 0
+// runs the deform half (deform_sample, a sample per thread) and hands canonical position,
+// direction and region to the encode through shared memory; both warpgroups encode (half the hash
+// levels each, SH and expression dims split between them) straight into the tile's operand rows
+// in shared memory; then the MLP chain runs on the tensor cores (mlp256: one thread issues,
+// the epilogues split the accumulator columns between the warpgroups).  Several CTAs per SM
+// overlap one CTA's gathers with another's MMAs, and the operand rows never go to global memory.
+// Same arithmetic as map_encode_kernel + mlp_kernel, so the outputs are the same bits.
+__global__ void __launch_bounds__(256, 4) field_tile_kernel(const __grid_constant__ WaveArgs A, const __grid_constant__ MlpArgs M) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    FusedSmem& sm = *reinterpret_cast<FusedSmem*>(smem_raw);
+    uint8_t* w = smem_raw + ((sizeof(FusedSmem) + 1023) & ~size_t(1023));
+    const uint32_t n_samples = *A.n_samples_padded;
+    const uint32_t n_alive = *A.n_alive_in;
+    const uint32_t n_tiles = (n_samples + 127u) / 128u;
+    const uint32_t per = (n_tiles + gridDim.x - 1) / gridDim.x;
+    const uint32_t t0 = blockIdx.x * per, t1 = min(n_tiles, t0 + per);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(A.sample_counter, (unsigned long long)*A.n_samples_round);
+    if (t0 >= t1) return;
+    const uint32_t r = threadIdx.x & 127u, wg = threadIdx.x >> 7;
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.bar_mma, 1);
+        mbar_init(&sm.bar_w, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) tmem_alloc(&sm.tmem_base, 128);
+    const uint8_t* loaded = tile_weights(M, t0);
+    if (threadIdx.x == 0) bulk_load(w, loaded, M.plan.bytes, &sm.bar_w);
+    uint32_t w_phase = 0, phase = 0;
+    bool ok = mbar_wait(&sm.bar_w, w_phase);
+    w_phase ^= 1u;
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const bool bf16 = A.fv.precision == 1;
+    const uint32_t ng = A.fv.n_levels / 4, half = ng / 2;   // level groups; warpgroup 0 takes [0, half)
+    float4* hand = reinterpret_cast<float4*>(sm.a_h);      // [128][2]: (position, region), (direction, valid)
+    for (uint32_t t = t0; t < t1 && ok; ++t) {
+        const uint32_t req = tile_request(M, t);
+        const uint8_t* need = M.seg ? M.reqs[req].mlp : M.fv.mlp_smem;
+        if (need != loaded) {
+            // the previous tile's MMAs have completed (mlp256 waited on them); swap the image
+            if (threadIdx.x == 0) bulk_load(w, need, M.plan.bytes, &sm.bar_w);
+            ok &= mbar_wait(&sm.bar_w, w_phase);
+            w_phase ^= 1u;
+            loaded = need;
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+        }
+        const uint32_t s = t * 128u + r;
+        if (wg == 0) {
+            const uint32_t m = A.sample_order[s];
+            float cpos[3] = {0.f, 0.f, 0.f}, cdir[3] = {0.5f, 0.5f, 0.5f};
+            uint32_t mask = 7u;
+            if (m != kNoSample) deform_sample(A, s, m, n_alive, cpos, cdir, mask);
+            hand[r * 2] = make_float4(cpos[0], cpos[1], cpos[2], __uint_as_float(mask));
+            hand[r * 2 + 1] = make_float4(cdir[0], cdir[1], cdir[2], __uint_as_float(m != kNoSample ? 1u : 0u));
+        }
+        __syncthreads();
+        const float4 h0 = hand[r * 2], h1 = hand[r * 2 + 1];
+        {
+            // padding rows are encoded at a fixed point; their outputs are never read
+            const ReqView& R = A.reqs[req];
+            const float cpos[3] = {h0.x, h0.y, h0.z}, cdir[3] = {h1.x, h1.y, h1.z};
+            if (wg == 0) {
+                encode_levels(A.fv, R.table, cpos, sm.stage, r, A.k_in, 0, half);
+                encode_sh(A.fv, cdir, sm.stage, r, A.k_in);
+            } else {
+                encode_levels(A.fv, R.table, cpos, sm.stage, r, A.k_in, half, ng);
+                encode_extra(A.fv, R.extra, __float_as_uint(h0.w), sm.stage, r, A.k_in);
+            }
+        }
+        // mlp256's first chain fences these generic writes for the tensor core and syncs the CTA;
+        // the density output rows go to the hash rows, dead once density layer 0 has run
+        float o4[4];
+        ok &= mlp256(sm, sm.stage, w, M.plan, bf16, phase, o4);
+        if (wg == 0 && __float_as_uint(h1.w) != 0u) {
+            if (A.fv.precision != 0) {
+                M.out_f32[s] = make_float4(o4[0], o4[1], o4[2], o4[3]);
+            } else {
+                __half2 rg = __floats2half2_rn(o4[0], o4[1]);
+                __half2 bd = __floats2half2_rn(o4[2], o4[3]);
+                uint2 u;
+                u.x = *reinterpret_cast<uint32_t*>(&rg);
+                u.y = *reinterpret_cast<uint32_t*>(&bd);
+                M.out[s] = u;
+            }
+        }
+        ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -902,14 +1132,62 @@ cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_deform_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s) {
+cudaError_t launch_nearest_stage(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s) {
     const uint32_t bps = blocks_per_sm ? blocks_per_sm : 16u;
     nearest_stage_kernel<<<sm_count() * bps, 256, (size_t)8 * a.top_nodes * 112u, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_deform_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s) {
+    const uint32_t bps = blocks_per_sm ? blocks_per_sm : 16u;
+    cudaError_t e = launch_nearest_stage(a, blocks_per_sm, s);
+    if (e != cudaSuccess) return e;
     map_encode_kernel<<<sm_count() * bps, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
+cudaError_t launch_field_fused(const WaveArgs& a, const MlpArgs& m, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm) {
+    const size_t smem = ((sizeof(FusedSmem) + 1023) & ~size_t(1023)) + m.plan.bytes;
+    cudaError_t e = cudaFuncSetAttribute(field_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, smem_sm = 0, reserved = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    // as many CTAs as shared memory lets reside, at most 4 (4 x 128 TMEM columns fill an SM)
+    int per_sm = smem_sm / (int)(smem + (size_t)reserved);
+    per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
+    if (ctas_per_sm && (int)ctas_per_sm < per_sm) per_sm = (int)ctas_per_sm;
+    // the shared-memory carveout just large enough for them: the rest stays L1 for the gathers
+    const int pct = (int)((100 * (size_t)per_sm * (smem + (size_t)reserved) + (size_t)smem_sm - 1) / (size_t)smem_sm);
+    e = cudaFuncSetAttribute(field_tile_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct > 100 ? 100 : pct);
+    if (e != cudaSuccess) return e;
+    uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
+    if (max_tiles < grid) grid = max_tiles ? max_tiles : 1;
+    field_tile_kernel<<<grid, 256, smem, s>>>(a, m);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm) {
+    {
+        // the 256-thread kernel (mlp_kernel, 128 threads, double-buffered tiles, is kept for comparison)
+        const size_t smem2 = (size_t)mlp2_w_off(a.plan.tile_bytes) + a.plan.bytes;
+        cudaError_t e = cudaFuncSetAttribute(mlp256_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(mlp256_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
+        int dev = 0, smem_sm = 0, reserved = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+        int per_sm = smem_sm / (int)(smem2 + (size_t)reserved);
+        per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
+        if (ctas_per_sm && (int)ctas_per_sm < per_sm) per_sm = (int)ctas_per_sm;
+        uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
+        if (max_tiles < grid) grid = max_tiles ? max_tiles : 1;
+        mlp256_kernel<<<grid, 256, smem2, s>>>(a);
+        return cudaGetLastError();
+    }
     size_t smem = mlp_smem_bytes(a.plan);
     cudaError_t e = cudaFuncSetAttribute(mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -12,8 +12,9 @@ multi-round alive lists are exercised the way the benchmark exercises them:
   render, per-pixel composited sample counts equal to the oracle's march (rays whose early
   termination flips on rounding aside, < 0.1 %), depths within 1e-3 where both are opaque;
 * the same frame with at most 3 samples per ray per round (so the rays span up to tens of rounds
-  and the alive lists are compacted every round): bit-identical to the default schedule and to
-  the host-driven rounds -- a sample's arithmetic never depends on how rays are grouped;
+  and the alive lists are compacted every round), other launch shapes, staged tree tops, and the
+  split deform + encode / MLP kernels: bit-identical to the default schedule and to the
+  host-driven rounds -- a sample's arithmetic never depends on how rays are grouped;
 * the whole 1024x1024 frame with FP16, BF16 and FP8 E4M3 MLPs (the precision workload) against
   the oracle's restatement of each format, and a 32-row band against the FP64 oracle.
 """
@@ -140,8 +141,11 @@ def test_render_512_multi_round_bit_identical(full, frame512):
     h_rgba, h_depth, h_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(max_steps_per_round=5), host_rounds=True)
     assert np.array_equal(h_rgba, rgba) and np.array_equal(h_depth, depth) and np.array_equal(h_counts, counts)
     s_rgba, s_depth, s_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(sort_cell_bits=15, mlp_ctas_per_sm=1,
-                                                                          deform_blocks_per_sm=8))
+                                                                          deform_blocks_per_sm=8, bvh_top_nodes=21))
     assert np.array_equal(s_rgba, rgba) and np.array_equal(s_depth, depth) and np.array_equal(s_counts, counts)
+    # the deform + encode + MLP stage as one kernel, against encode to global tiles + MLP (default)
+    f_rgba, f_depth, f_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(fused_field_stage=1, bvh_top_nodes=5))
+    assert np.array_equal(f_rgba, rgba) and np.array_equal(f_depth, depth) and np.array_equal(f_counts, counts)
 
 
 @pytest.mark.parametrize("precision,min_psnr", [(0, 45.0), (1, 45.0), (2, 35.0)])
