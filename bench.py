@@ -38,13 +38,14 @@ L2_FLUSH_BYTES = 512 << 20
 SETTLE_S = 0.5   # untimed steps before the warm-up, long enough for the SM clock to ramp
 # DRAM bytes (read + write) of the deform+encode stage per 512x512 frame (nearest_stage_kernel and
 # map_encode_kernel, two rounds each), from an ncu capture of this workload's kernels
-TRAFFIC_PER_FRAME = 428_134_656
+TRAFFIC_PER_FRAME = 431_540_000
 # Algorithmic bytes per sample of the dominant kernel (deform_encode): hash-grid gathers
 # (16 levels x 8 corners x 2 FP16 features) + sample record, ray direction and ray index in +
 # encoded operand row (32 + 16 FP16) and (dt, depth) out.
 HASH_BYTES_PER_SAMPLE = 16 * 8 * 2 * 2
 DEFORM_ENCODE_BYTES_PER_SAMPLE = HASH_BYTES_PER_SAMPLE + 16 + 16 + 4 + (32 + 16) * 2 + 8
 MLP_FLOP_PER_SAMPLE = 2 * (32 * 64 + 64 * 16 + 32 * 64 + 64 * 64 + 64 * 3)
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 
 def dist_env():
@@ -305,9 +306,15 @@ def run_ours(args, rank, world, local):
     value = total_samples / dev_t
     mean_samples = statistics.mean(samples_per_frame)
     stage_ms = {k: v / args.steps for k, v in stages["stage_ms"].items() if stages["stage_calls"][k]}
-    de_s = stage_ms["deform_encode"] / 1000.0
+    # deform + encode = the nearest-triangle walk (its own stage) + the map and hash encode
+    near_s = stage_ms.get("nearest", 0.0) / 1000.0
+    de_s = near_s + stage_ms.get("deform_encode", 0.0) / 1000.0
     mlp_s = stage_ms["mlp"] / 1000.0
     achieved = mean_samples * DEFORM_ENCODE_BYTES_PER_SAMPLE / de_s / 1e9
+    # the walk's FP32 work from its counters (the stage-timing pass): 4 child boxes per inner node
+    # for all 32 lanes at 12 FLOP, 15 FLOP per bounding-disk test, 60 per exact triangle test
+    walk = stages["walk"]
+    walk_flop = (walk["inner_nodes"] * 4 * 32 * 12 + walk["bound_tests"] * 15 + walk["exact_tests"] * 60) / args.steps
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -329,11 +336,21 @@ def run_ours(args, rank, world, local):
         "roofline": {"bound": "hbm", "kernel": "deform+encode stage (nearest_stage_kernel + map_encode_kernel)",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": TRAFFIC_PER_FRAME if WIDTH == 512 else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's launches for one "
+                                       "512x512 frame, captured separately (not measured in this run)",
                      "basis": f"{DEFORM_ENCODE_BYTES_PER_SAMPLE} B per sample (512 B hash gathers + stream in/out) "
                               f"x samples per frame / deform_encode stage time per frame (CUDA events); per frame = "
                               f"its 2 launches, for achieved and traffic alike",
                      "peak_source": "MEASURED_PEAKS.json (of measured)" if peaks else "fallback"},
-        "roofline_tensor": {"kernel": "mlp_kernel", "achieved": mean_samples * MLP_FLOP_PER_SAMPLE / mlp_s / 1e12,
+        "roofline_fp32": {"kernel": "nearest_stage_kernel (warp-cooperative exact nearest triangle)",
+                          "achieved": walk_flop / near_s / 1e12 if near_s else None, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
+                          "frac": walk_flop / near_s / 1e12 / FP32_PEAK_TFLOPS if near_s else None,
+                          "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 x 2.07 GHz)",
+                          "per_warp_walk": {"inner_nodes": walk["inner_nodes"] / max(walk["warps"], 1),
+                                            "leaves": walk["leaves"] / max(walk["warps"], 1)},
+                          "per_sample": {"bound_tests": walk["bound_tests"] / args.steps / mean_samples,
+                                         "exact_tests": walk["exact_tests"] / args.steps / mean_samples}},
+        "roofline_tensor": {"kernel": "mlp256_kernel", "achieved": mean_samples * MLP_FLOP_PER_SAMPLE / mlp_s / 1e12,
                             "peak": tflops_peak, "unit": "TFLOP/s",
                             "frac": mean_samples * MLP_FLOP_PER_SAMPLE / mlp_s / 1e12 / tflops_peak},
         "stage_ms_per_frame": stage_ms,

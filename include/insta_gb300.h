@@ -113,7 +113,7 @@ typedef struct {
 #define INSTA_STAGE_OCCUPANCY 1      /* occupancy bitfield from the mesh         */
 #define INSTA_STAGE_RAY_INIT 2
 #define INSTA_STAGE_MARCH 3
-#define INSTA_STAGE_DEFORM_ENCODE 4  /* canonical map + hash encode + SH         */
+#define INSTA_STAGE_DEFORM_ENCODE 4  /* canonical map + hash encode + SH (after NEAREST) */
 #define INSTA_STAGE_MLP 5            /* density + colour MLPs (tensor cores)     */
 #define INSTA_STAGE_COMPOSITE 6
 #define INSTA_STAGE_CANONICAL_MAP 7  /* insta_canonical_map / _soa               */
@@ -121,7 +121,8 @@ typedef struct {
 #define INSTA_STAGE_SORT 9           /* regrouping a round's samples by (request, cell) */
 #define INSTA_STAGE_RAYCAST 10       /* insta_raycast                            */
 #define INSTA_STAGE_TRAIN 11         /* insta_train_loss, field_backward, adam   */
-#define INSTA_STAGE_COUNT 12
+#define INSTA_STAGE_NEAREST 12       /* the render's nearest-triangle walk, before DEFORM_ENCODE */
+#define INSTA_STAGE_COUNT 13
 
 typedef struct {
     uint64_t kernel_launches;        /* kernels the library launched */

@@ -89,7 +89,7 @@ class FieldDesc(C.Structure):
 
 
 STAGES = ["frame", "occupancy", "ray_init", "march", "deform_encode", "mlp", "composite", "canonical_map", "field", "sort",
-          "raycast", "train"]
+          "raycast", "train", "nearest"]
 
 
 class Stats(C.Structure):

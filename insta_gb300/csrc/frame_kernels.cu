@@ -283,8 +283,9 @@ __device__ void block_radix_sort_hi(uint64_t* keys, int np2, uint16_t* cnt16, in
 
 // LBVH: sort triangles by the 30-bit Morton code of their centroid (ties by id), build the
 // binary radix tree top-down level by level and collapse every two binary levels into one
-// 4-wide node; boxes are then filled bottom-up.  Leaves hold <= INSTA_LEAF_SIZE triangles
-// (N_PRIMITIVES_LEAF = 2 in src/tiny_mesh.cu:28-32).
+// 4-wide node; boxes are then filled bottom-up.  Leaves hold <= INSTA_LEAF_SIZE triangles (the
+// reference's build uses N_PRIMITIVES_LEAF = 2, src/tiny_mesh.cu:28-32; query results do not
+// depend on the structure).
 __global__ void __launch_bounds__(1024) bvh_build_kernel(BvhBuildArgs one, const BvhBuildArgs* __restrict__ many) {
     const BvhBuildArgs a = many ? many[blockIdx.x] : one;   // a batch builds one frame per CTA
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -741,13 +741,13 @@ struct WaveRun {
         CK(cudaMemsetAsync(counters + 2, 0, 4, ctx->stream));
         { Stage st(ctx, INSTA_STAGE_MARCH, 1); CK(launch_march(W, ctx->stream)); }
         { Stage st(ctx, INSTA_STAGE_SORT, 4); CK(launch_sort_samples(W, ctx->stream)); }
+        { Stage st(ctx, INSTA_STAGE_NEAREST, 1); CK(launch_nearest_stage(W, ctx->tune.deform_blocks_per_sm, ctx->stream)); }
         if (fused_field()) {
-            // the nearest-triangle walk under the deform stage, the fused deform + encode + MLP kernel under the MLP stage
-            { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 1); CK(launch_nearest_stage(W, ctx->tune.deform_blocks_per_sm, ctx->stream)); }
-            { Stage st(ctx, INSTA_STAGE_MLP, 1);
-              CK(launch_field_fused(W, M, (uint32_t)(cap_samples / 128), ctx->stream, ctx->tune.mlp_ctas_per_sm)); }
+            // the fused deform + encode + MLP kernel under the MLP stage
+            Stage st(ctx, INSTA_STAGE_MLP, 1);
+            CK(launch_field_fused(W, M, (uint32_t)(cap_samples / 128), ctx->stream, ctx->tune.mlp_ctas_per_sm));
         } else {
-            { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 2); CK(launch_deform_encode(W, ctx->tune.deform_blocks_per_sm, ctx->stream)); }
+            { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 1); CK(launch_map_encode(W, ctx->tune.deform_blocks_per_sm, ctx->stream)); }
             { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream, ctx->tune.mlp_ctas_per_sm)); }
         }
         { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }

@@ -28,7 +28,7 @@ struct TriFrame;
 //              INSTA_LEAF_BIT | (first slot << 3) | count for a leaf, -1 for an empty slot.
 //   Node 0 is the root.
 #define INSTA_LEAF_BIT 0x40000000
-#define INSTA_LEAF_SIZE 2
+#define INSTA_LEAF_SIZE 4   // triangles per leaf at most (the reference's N_PRIMITIVES_LEAF is 2; see bvh.cuh)
 #define INSTA_TRI_F4 9
 struct FrameView {
     const float4* leaf_tris;

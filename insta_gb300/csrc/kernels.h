@@ -159,6 +159,7 @@ cudaError_t launch_march(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_sort_samples(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_deform_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s);
 cudaError_t launch_nearest_stage(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s);
+cudaError_t launch_map_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s);
 // deform + encode + MLP in one kernel after launch_nearest_stage (FP16 / BF16 fields)
 cudaError_t launch_field_fused(const WaveArgs& a, const MlpArgs& m, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm);
 cudaError_t launch_composite(const WaveArgs& a, cudaStream_t s);

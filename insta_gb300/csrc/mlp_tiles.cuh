@@ -90,7 +90,12 @@ __device__ __forceinline__ bool issue_chain(Smem& sm, const uint8_t* const* a, c
         }
         umma_commit(&sm.bar_mma);
     }
-    bool ok = mbar_wait(&sm.bar_mma, phase);
+    // warp 0 waits for the chain's commit; the others sleep at the barrier instead of polling the
+    // mbarrier (their issue slots go to the other CTAs' epilogues), then order their TMEM reads
+    // after it
+    bool ok = true;
+    if (threadIdx.x < 32u) ok = mbar_wait(&sm.bar_mma, phase);
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
     phase ^= 1u;
     tc_fence_after();
     return ok;
@@ -235,18 +240,12 @@ __device__ __forceinline__ void relu_to_ah2(Smem& sm, bool bf16) {
     for (uint32_t c = c0; c < c0 + 32u; c += 16) {
         float v[16];
         tmem_ld16(fused_lane_addr(sm, c), v);
-        __half h[16];
+        uint32_t p[8];   // ReLU, then both values of a pair rounded by one packed conversion
 #pragma unroll
-        for (int i = 0; i < 16; ++i) h[i] = to_act(fmaxf(v[i], 0.f), bf16);
+        for (int i = 0; i < 8; ++i) p[i] = pack2_act(fmaxf(v[2 * i], 0.f), fmaxf(v[2 * i + 1], 0.f), bf16);
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            uint4 u;
-            u.x = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 0]);
-            u.y = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 2]);
-            u.z = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 4]);
-            u.w = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 6]);
-            *reinterpret_cast<uint4*>(sm.a_h + tile_offset(r, c + q * 8, 64)) = u;
-        }
+        for (int q = 0; q < 2; ++q)
+            *reinterpret_cast<uint4*>(sm.a_h + tile_offset(r, c + q * 8, 64)) = make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
     }
 }
 

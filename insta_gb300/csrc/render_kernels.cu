@@ -97,10 +97,7 @@ __global__ void ray_init_kernel(const __grid_constant__ WaveArgs A, uint32_t tot
 }
 
 // ------------------------------------------------------------------ march + deform + encode
-__device__ __forceinline__ uint32_t pack_act(float a, float b, bool bf16) {
-    const __half x = to_act(a, bf16), y = to_act(b, bf16);
-    return (uint32_t)__half_as_ushort(x) | ((uint32_t)__half_as_ushort(y) << 16);
-}
+__device__ __forceinline__ uint32_t pack_act(float a, float b, bool bf16) { return pack2_act(a, b, bf16); }
 
 // Parts of one sample's operand rows: hash features of level groups [g0, g1) (four levels, 32
 // gathers in flight, per group, each group of 8 values stored as one 16-byte chunk of the row),
@@ -665,7 +662,8 @@ __global__ void __launch_bounds__(128) mlp_kernel(const __grid_constant__ MlpArg
 // as colour layer 0 has, so the copies overlap the chain; the epilogues split the accumulator
 // columns between the two warpgroups (FP8: each warpgroup re-quantises half of a row, the row
 // maximum exchanged through shared memory).  Same arithmetic as mlp_kernel.
-__global__ void __launch_bounds__(256) mlp256_kernel(const __grid_constant__ MlpArgs A) {
+template <bool FP8>
+__global__ void __launch_bounds__(256, 4) mlp256_kernel(const __grid_constant__ MlpArgs A) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     Mlp2Ctl& ctl = *reinterpret_cast<Mlp2Ctl*>(smem_raw);
     Mlp2View sm{ctl.bar_mma, ctl.tmem_base, smem_raw + mlp2_stage_off(), smem_raw + mlp2_a_h_off(),
@@ -698,7 +696,7 @@ __global__ void __launch_bounds__(256) mlp256_kernel(const __grid_constant__ Mlp
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const bool bf16 = A.fv.precision == 1, fp8 = A.fv.precision == 2;
+    const bool bf16 = A.fv.precision == 1;
     float* xch = reinterpret_cast<float*>(smem_raw + mlp2_xch_off());
     bool pending = true;   // a tile's copies are in flight
     for (uint32_t t = t0; t < t1 && ok; ++t) {
@@ -726,7 +724,7 @@ __global__ void __launch_bounds__(256) mlp256_kernel(const __grid_constant__ Mlp
         };
         pending = next;
         float o4[4];
-        if (fp8) ok &= mlp256_8(sm, xch, sm.a_dens, w, A.plan, reinterpret_cast<const float*>(w + A.plan.scales), phase, o4, hash_free, sh_free);
+        if constexpr (FP8) ok &= mlp256_8(sm, xch, sm.a_dens, w, A.plan, reinterpret_cast<const float*>(w + A.plan.scales), phase, o4, hash_free, sh_free);
         else ok &= mlp256(sm, sm.a_dens, w, A.plan, bf16, phase, o4, hash_free, sh_free);
         const uint32_t s = t * 128u + threadIdx.x;
         if (threadIdx.x < 128u && s < n_samples) {
@@ -1138,12 +1136,16 @@ cudaError_t launch_nearest_stage(const WaveArgs& a, uint32_t blocks_per_sm, cuda
     return cudaGetLastError();
 }
 
-cudaError_t launch_deform_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s) {
+cudaError_t launch_map_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s) {
     const uint32_t bps = blocks_per_sm ? blocks_per_sm : 16u;
-    cudaError_t e = launch_nearest_stage(a, blocks_per_sm, s);
-    if (e != cudaSuccess) return e;
     map_encode_kernel<<<sm_count() * bps, 256, 0, s>>>(a);
     return cudaGetLastError();
+}
+
+cudaError_t launch_deform_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s) {
+    cudaError_t e = launch_nearest_stage(a, blocks_per_sm, s);
+    if (e != cudaSuccess) return e;
+    return launch_map_encode(a, blocks_per_sm, s);
 }
 
 cudaError_t launch_field_fused(const WaveArgs& a, const MlpArgs& m, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm) {
@@ -1172,9 +1174,11 @@ cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uin
     {
         // the 256-thread kernel (mlp_kernel, 128 threads, double-buffered tiles, is kept for comparison)
         const size_t smem2 = (size_t)mlp2_w_off(a.plan.tile_bytes) + a.plan.bytes;
-        cudaError_t e = cudaFuncSetAttribute(mlp256_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+        const bool fp8 = a.fv.precision == 2;
+        const void* fn = fp8 ? (const void*)mlp256_kernel<true> : (const void*)mlp256_kernel<false>;
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
         if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(mlp256_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
         int dev = 0, smem_sm = 0, reserved = 0;
         cudaGetDevice(&dev);
@@ -1185,7 +1189,8 @@ cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uin
         if (ctas_per_sm && (int)ctas_per_sm < per_sm) per_sm = (int)ctas_per_sm;
         uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
         if (max_tiles < grid) grid = max_tiles ? max_tiles : 1;
-        mlp256_kernel<<<grid, 256, smem2, s>>>(a);
+        if (fp8) mlp256_kernel<true><<<grid, 256, smem2, s>>>(a);
+        else mlp256_kernel<false><<<grid, 256, smem2, s>>>(a);
         return cudaGetLastError();
     }
     size_t smem = mlp_smem_bytes(a.plan);

@@ -145,6 +145,16 @@ __device__ __forceinline__ __half to_act(float v, bool bf16) {
     }
     return __float2half_rn(v);
 }
+// Two FP32 values rounded to the activation type (round to nearest even, as to_act) and packed,
+// a in the low half: one packed conversion instruction.
+__device__ __forceinline__ uint32_t pack2_act(float a, float b, bool bf16) {
+    if (bf16) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        return *reinterpret_cast<const uint32_t*>(&h);
+    }
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
 __device__ __forceinline__ float from_act(__half h, bool bf16) {
     if (bf16) return __bfloat162float(__ushort_as_bfloat16(__half_as_ushort(h)));
     return __half2float(h);
