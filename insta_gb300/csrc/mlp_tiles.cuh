@@ -55,16 +55,6 @@ struct MlpArgs {
 // ctas_per_sm: 0 = as many as shared memory lets reside (at most 4)
 cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm = 0);
 
-struct TileSmem {
-    alignas(1024) uint8_t stage[2][128 * 64 * 2];   // input tile records (hash + SH), double-buffered
-    alignas(1024) uint8_t a_h[128 * 64 * 2];        // hidden activations
-    alignas(1024) uint8_t a_dens[128 * 16 * 2];     // density-MLP output, colour input part 1
-    alignas(8) uint64_t bar_mma;
-    alignas(8) uint64_t bar_load[2];
-    alignas(8) uint64_t bar_w;       // weight image loads
-    uint32_t tmem_base;
-};
-
 // One MMA chain: sum over (A_i, B_i) pairs into TMEM columns [col, col + N).  K in elements;
 // f8: E4M3 operands (kind::f8f6f4, 32 elements per instruction), else FP16/BF16 (16 per
 // instruction).  Either way one instruction consumes 32 bytes of each row.
@@ -98,87 +88,6 @@ __device__ __forceinline__ bool issue_chain(Smem& sm, const uint8_t* const* a, c
     ok = __syncthreads_and(ok ? 1 : 0) != 0;
     phase ^= 1u;
     tc_fence_after();
-    return ok;
-}
-
-__device__ __forceinline__ uint32_t tile_lane_addr(const TileSmem& sm, uint32_t col) {
-    return sm.tmem_base + ((((uint32_t)threadIdx.x / 32u) % 4u) * 32u << 16) + col;
-}
-
-// ReLU + rounding, TMEM -> this thread's row of a_h (K = 64).
-__device__ __forceinline__ void relu_to_ah(TileSmem& sm, bool bf16) {
-    const uint32_t r = threadIdx.x;
-#pragma unroll 1
-    for (uint32_t c = 0; c < 64; c += 16) {
-        float v[16];
-        tmem_ld16(tile_lane_addr(sm, c), v);
-        __half h[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) h[i] = to_act(fmaxf(v[i], 0.f), bf16);
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            uint4 u;
-            u.x = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 0]);
-            u.y = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 2]);
-            u.z = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 4]);
-            u.w = *reinterpret_cast<const uint32_t*>(&h[q * 8 + 6]);
-            *reinterpret_cast<uint4*>(sm.a_h + tile_offset(r, c + q * 8, 64)) = u;
-        }
-    }
-}
-
-// Both MLPs for the tile held in stage[buf]; returns this thread's (r, g, b, raw density).
-__device__ __forceinline__ bool mlp_tile(TileSmem& sm, const uint8_t* w, const TilePlan& P, int buf, bool bf16, uint32_t& phase,
-                                         float* out4) {
-    bool ok = true;
-    const uint8_t* hash = sm.stage[buf];
-    const uint8_t* sh = sm.stage[buf] + hash_tile_bytes(P.k_in);
-    const uint8_t* a;
-    const uint8_t* b;
-    uint32_t K;
-    // density hidden layers
-    a = hash; b = w + P.d_off[0]; K = P.k_in;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
-    relu_to_ah(sm, bf16);
-    for (uint32_t l = 1; l < P.n_dh; ++l) {
-        a = sm.a_h; b = w + P.d_off[l]; K = 64;
-        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
-        relu_to_ah(sm, bf16);
-    }
-    // density output (16): raw density is column 0
-    a = sm.a_h; b = w + P.d_out; K = 64;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, bf16, phase);
-    {
-        float v[16];
-        tmem_ld16(tile_lane_addr(sm, 64), v);
-        __half h[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) h[i] = to_act(v[i], bf16);
-        out4[3] = from_act(h[0], bf16);
-        store_row(sm.a_dens, threadIdx.x, 16, h);
-    }
-    // colour layer 0 = [density out | SH] split into two K = 16 operands
-    {
-        const uint8_t* as[2] = {sm.a_dens, sh};
-        const uint8_t* bs[2] = {w + P.r0_dens, w + P.r0_sh};
-        const uint32_t Ks[2] = {16, 16};
-        ok &= issue_chain(sm, as, bs, Ks, 2, 64, 0, bf16, phase);
-        relu_to_ah(sm, bf16);
-    }
-    for (uint32_t l = 1; l < P.n_rh; ++l) {
-        a = sm.a_h; b = w + P.r_off[l]; K = 64;
-        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
-        relu_to_ah(sm, bf16);
-    }
-    a = sm.a_h; b = w + P.r_out; K = 64;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, bf16, phase);
-    {
-        float v[16];
-        tmem_ld16(tile_lane_addr(sm, 64), v);
-        out4[0] = from_act(to_act(v[0], bf16), bf16);
-        out4[1] = from_act(to_act(v[1], bf16), bf16);
-        out4[2] = from_act(to_act(v[2], bf16), bf16);
-    }
     return ok;
 }
 
@@ -250,8 +159,8 @@ __device__ __forceinline__ void relu_to_ah2(Smem& sm, bool bf16) {
 }
 
 // Both MLPs (FP16 or BF16) with 256 threads on the tile in sm.stage; warpgroup 0 returns its
-// row's (r, g, b, raw density).  The arithmetic is mlp_tile's: the same operand tiles,
-// instruction sequence and roundings, so the outputs are the same bits.  hash_free / sh_free run
+// row's (r, g, b, raw density): the density MLP's hidden layers (ReLU), its 16 outputs (raw
+// density in column 0) rounded to the activation type, then the colour MLP on [those | SH].  hash_free / sh_free run
 // (all threads) as soon as the tensor core is done with the hash rows / the SH rows.
 template <typename Smem, typename HashFree = NoHook, typename ShFree = NoHook>
 __device__ __forceinline__ bool mlp256(Smem& sm, uint8_t* a_dens, const uint8_t* w, const TilePlan& P, bool bf16, uint32_t& phase,
@@ -312,59 +221,30 @@ __device__ __forceinline__ bool mlp256(Smem& sm, uint8_t* a_dens, const uint8_t*
 // Every layer input row gets its own scale a = max|x| / 448 (rounded to E4M3 after multiplying by
 // 448 / max|x|); weights carry a per-layer scale s; the FP32 accumulator is multiplied back by a,
 // then s.
-__device__ __forceinline__ uint32_t e4m3x4(float a, float b, float c, float d, float inv_scale_div) {
-    (void)inv_scale_div;
-    return (uint32_t)__nv_cvt_float_to_fp8(a, __NV_SATFINITE, __NV_E4M3) |
-           ((uint32_t)__nv_cvt_float_to_fp8(b, __NV_SATFINITE, __NV_E4M3) << 8) |
-           ((uint32_t)__nv_cvt_float_to_fp8(c, __NV_SATFINITE, __NV_E4M3) << 16) |
-           ((uint32_t)__nv_cvt_float_to_fp8(d, __NV_SATFINITE, __NV_E4M3) << 24);
+// Four values to E4M3 (round to nearest even, saturating to the finite range), a in the lowest
+// byte: two packed conversions of two values each.
+__device__ __forceinline__ uint32_t e4m3x4(float a, float b, float c, float d) {
+    const uint32_t lo = (uint32_t)__nv_cvt_float2_to_fp8x2(make_float2(a, b), __NV_SATFINITE, __NV_E4M3);
+    const uint32_t hi = (uint32_t)__nv_cvt_float2_to_fp8x2(make_float2(c, d), __NV_SATFINITE, __NV_E4M3);
+    return (lo & 0xffffu) | (hi << 16);
 }
 
-// 16 values of this thread's row, times `inv` (448 / row max), as E4M3 into columns [k, k + 16)
-// of an A tile.
-__device__ __forceinline__ void store16_e4m3(uint8_t* tile, uint32_t K, uint32_t k, const float* v, float inv) {
-    float q[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) q[i] = __fmul_rn(v[i], inv);
-    uint4 u;
-    u.x = e4m3x4(q[0], q[1], q[2], q[3], 0.f);
-    u.y = e4m3x4(q[4], q[5], q[6], q[7], 0.f);
-    u.z = e4m3x4(q[8], q[9], q[10], q[11], 0.f);
-    u.w = e4m3x4(q[12], q[13], q[14], q[15], 0.f);
-    *reinterpret_cast<uint4*>(tile + tile_offset8(threadIdx.x, k, K)) = u;
-}
-
-// The same for row r (threads other than r's own 128-thread layout).
+// 16 values of row r, times `inv` (448 / row max), as E4M3 into columns [k, k + 16) of an A tile.
 __device__ __forceinline__ void store16_e4m3_row(uint8_t* tile, uint32_t K, uint32_t k, const float* v, float inv, uint32_t r) {
     float q[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) q[i] = __fmul_rn(v[i], inv);
     uint4 u;
-    u.x = e4m3x4(q[0], q[1], q[2], q[3], 0.f);
-    u.y = e4m3x4(q[4], q[5], q[6], q[7], 0.f);
-    u.z = e4m3x4(q[8], q[9], q[10], q[11], 0.f);
-    u.w = e4m3x4(q[12], q[13], q[14], q[15], 0.f);
+    u.x = e4m3x4(q[0], q[1], q[2], q[3]);
+    u.y = e4m3x4(q[4], q[5], q[6], q[7]);
+    u.z = e4m3x4(q[8], q[9], q[10], q[11]);
+    u.w = e4m3x4(q[12], q[13], q[14], q[15]);
     *reinterpret_cast<uint4*>(tile + tile_offset8(r, k, K)) = u;
 }
 
 // Row scale a = max / 448 (multiplies the accumulator back) and its quantising factor 448 / max.
 __device__ __forceinline__ float row_scale(float mx) { return mx > 0.f ? __fdiv_rn(mx, 448.0f) : 1.0f; }
 __device__ __forceinline__ float row_inv(float mx) { return mx > 0.f ? __fdiv_rn(448.0f, mx) : 1.0f; }
-
-// 16 FP16 values of this thread's row of a 16-bit tile (columns [k, k + 16)).
-__device__ __forceinline__ void load16_half(const uint8_t* tile, uint32_t K, uint32_t k, float* v) {
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const uint4 u = *reinterpret_cast<const uint4*>(tile + tile_offset(threadIdx.x, k + 8 * q, K));
-        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w[i]));
-            v[8 * q + 2 * i] = f.x;
-            v[8 * q + 2 * i + 1] = f.y;
-        }
-    }
-}
 
 __device__ __forceinline__ void load16_half_row(const uint8_t* tile, uint32_t K, uint32_t k, float* v, uint32_t r) {
 #pragma unroll
@@ -378,108 +258,6 @@ __device__ __forceinline__ void load16_half_row(const uint8_t* tile, uint32_t K,
             v[8 * q + 2 * i + 1] = f.y;
         }
     }
-}
-
-// Dequantised, activated accumulator columns [c, c + 16) of this thread's row.
-__device__ __forceinline__ void acc16(TileSmem& sm, uint32_t c, float a, float s, bool relu, float* v) {
-    tmem_ld16(tile_lane_addr(sm, c), v);
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        v[i] = __fmul_rn(__fmul_rn(v[i], a), s);
-        if (relu) v[i] = fmaxf(v[i], 0.f);
-    }
-}
-
-// Hidden epilogue: ReLU(acc * a * s) of 64 columns, re-quantised with a fresh row scale into
-// the hidden A tile (two passes over TMEM: max, then quantise).  Returns the new row scale.
-__device__ __forceinline__ float hidden_to_e4m3(TileSmem& sm, uint8_t* a_h8, float a, float s) {
-    float mx = 0.f;
-#pragma unroll 1
-    for (uint32_t c = 0; c < 64; c += 16) {
-        float v[16];
-        acc16(sm, c, a, s, true, v);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) mx = fmaxf(mx, v[i]);
-    }
-    const float inv = row_inv(mx);
-#pragma unroll 1
-    for (uint32_t c = 0; c < 64; c += 16) {
-        float v[16];
-        acc16(sm, c, a, s, true, v);
-        store16_e4m3(a_h8, 64, c, v, inv);
-    }
-    return row_scale(mx);
-}
-
-// Both MLPs in FP8 for the tile held in stage[buf]; returns this thread's (r, g, b, raw density).
-__device__ __forceinline__ bool mlp_tile8(TileSmem& sm, const uint8_t* w, const TilePlan& P, const float* ls, int buf,
-                                          uint32_t& phase, float* out4) {
-    bool ok = true;
-    const uint8_t* hash = sm.stage[buf];
-    const uint8_t* sh = sm.stage[buf] + hash_tile_bytes(P.k_in);
-    uint8_t* a_h8 = sm.a_h;            // [128][64] E4M3
-    uint8_t* a_in8 = sm.a_h + 8192;    // [128][k8 <= 64] E4M3
-    uint8_t* a_rgb8 = sm.a_dens;       // [128][32] E4M3
-    const uint8_t* a;
-    const uint8_t* b;
-    uint32_t K;
-    int li = 0;
-    // density input: the FP16 hash row (k_in values, zero-padded to k8)
-    float mx = 0.f;
-    for (uint32_t c = 0; c < P.k_in; c += 16) {
-        float v[16];
-        load16_half(hash, P.k_in, c, v);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fabsf(v[i]));
-    }
-    float ra = row_scale(mx);
-    const float inv0 = row_inv(mx);
-    for (uint32_t c = 0; c < P.k8; c += 16) {
-        float v[16];
-        if (c < P.k_in) load16_half(hash, P.k_in, c, v);
-        else {
-#pragma unroll
-            for (int i = 0; i < 16; ++i) v[i] = 0.f;
-        }
-        store16_e4m3(a_in8, P.k8, c, v, inv0);
-    }
-    a = a_in8; b = w + P.d_off[0]; K = P.k8;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
-    ra = hidden_to_e4m3(sm, a_h8, ra, ls[li++]);
-    for (uint32_t l = 1; l < P.n_dh; ++l) {
-        a = a_h8; b = w + P.d_off[l]; K = 64;
-        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
-        ra = hidden_to_e4m3(sm, a_h8, ra, ls[li++]);
-    }
-    // density output (16): raw density is column 0; colour input = [density out | SH]
-    a = a_h8; b = w + P.d_out; K = 64;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, false, phase, true);
-    float dens[16], shv[16];
-    acc16(sm, 64, ra, ls[li++], false, dens);
-    out4[3] = dens[0];
-    load16_half(sh, 16, 0, shv);
-    mx = 0.f;
-#pragma unroll
-    for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fmaxf(fabsf(dens[i]), fabsf(shv[i])));
-    ra = row_scale(mx);
-    store16_e4m3(a_rgb8, 32, 0, dens, row_inv(mx));
-    store16_e4m3(a_rgb8, 32, 16, shv, row_inv(mx));
-    a = a_rgb8; b = w + P.r0_dens; K = 32;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
-    ra = hidden_to_e4m3(sm, a_h8, ra, ls[li++]);
-    for (uint32_t l = 1; l < P.n_rh; ++l) {
-        a = a_h8; b = w + P.r_off[l]; K = 64;
-        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
-        ra = hidden_to_e4m3(sm, a_h8, ra, ls[li++]);
-    }
-    a = a_h8; b = w + P.r_out; K = 64;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, false, phase, true);
-    float rgb[16];
-    acc16(sm, 64, ra, ls[li++], false, rgb);
-    out4[0] = rgb[0];
-    out4[1] = rgb[1];
-    out4[2] = rgb[2];
-    return ok;
 }
 
 // Write one FP16 row of a tile record in global memory (K values, K multiple of 8).
@@ -499,9 +277,9 @@ __device__ __forceinline__ void store_row_global(uint8_t* tile, uint32_t r, uint
 namespace insta {
 
 // ------------------------------------------------------------------ FP8 with 256 threads
-// The FP8 chain of mlp_tile8 with the row work split between the warpgroups: each quantises half
-// of a row's columns; the row maximum that sets the row scale is exchanged through `xch`
-// ([2][128] floats), so both halves use the same scale and the values are those of mlp_tile8.
+// The FP8 chain with the row work split between the warpgroups: each quantises half of a row's
+// columns; the row maximum that sets the row scale is exchanged through `xch` ([2][128] floats),
+// so both halves use the same scale.
 __device__ __forceinline__ float row_max2(float* xch, float m) {
     const uint32_t r = threadIdx.x & 127u, g = threadIdx.x >> 7;
     xch[g * 128u + r] = m;

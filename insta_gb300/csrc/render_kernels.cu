@@ -6,7 +6,7 @@
 //   nearest_stage_kernel  per 32 sorted samples: warp-cooperative nearest triangle
 //   map_encode_kernel     per sample: deformed->canonical map, hash encode + SH written as
 //                         ready-made tensor-core operand tiles
-//   mlp_kernel            density + colour MLPs on 128-sample tiles (tcgen05, TMEM accumulators)
+//   mlp256_kernel         density + colour MLPs on 128-sample tiles (tcgen05, TMEM accumulators)
 //   composite_kernel      front-to-back compositing, early termination, shading, compaction
 // Ray lists and counts stay on the device; the host only decides when to stop issuing rounds.
 #include "device_common.cuh"
@@ -549,10 +549,6 @@ __global__ void __launch_bounds__(256, 4) map_encode_kernel(const __grid_constan
 }
 
 // ------------------------------------------------------------------ MLP over tiles
-__device__ __forceinline__ void load_tile(TileSmem& sm, int buf, const uint8_t* src, uint32_t bytes) {
-    bulk_load(sm.stage[buf], src, bytes, &sm.bar_load[buf]);
-}
-
 // Request slot of tile t: the request whose padded run holds it (render batches; 0 otherwise).
 __device__ __forceinline__ uint32_t tile_request(const MlpArgs& A, uint32_t t) {
     if (!A.seg) return 0;
@@ -570,98 +566,13 @@ __device__ __forceinline__ const uint8_t* tile_weights(const MlpArgs& A, uint32_
     return A.seg ? A.reqs[tile_request(A, t)].mlp : A.fv.mlp_smem;
 }
 
-// Each CTA takes a contiguous range of tiles (consecutive tiles mostly share a request, so the
-// weight image is reloaded only where a range crosses into another avatar's requests); input
-// tiles are double-buffered with 1-D bulk copies.
-__global__ void __launch_bounds__(128) mlp_kernel(const __grid_constant__ MlpArgs A) {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
-    uint8_t* w = smem_raw + ((sizeof(TileSmem) + 1023) & ~size_t(1023));
-    const uint32_t n_samples = A.n_alive ? *A.n_alive : (uint32_t)A.n_samples;
-    const uint32_t n_tiles = (n_samples + 127u) / 128u;
-    const uint32_t per = (n_tiles + gridDim.x - 1) / gridDim.x;
-    const uint32_t t0 = blockIdx.x * per, t1 = min(n_tiles, t0 + per);
-    if (t0 >= t1) return;
-    if (threadIdx.x == 0) {
-        mbar_init(&sm.bar_mma, 1);
-        mbar_init(&sm.bar_load[0], 1);
-        mbar_init(&sm.bar_load[1], 1);
-        mbar_init(&sm.bar_w, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) tmem_alloc(&sm.tmem_base, 128);
-    const uint8_t* loaded = tile_weights(A, t0);
-    if (threadIdx.x == 0) {
-        bulk_load(w, loaded, A.plan.bytes, &sm.bar_w);
-        load_tile(sm, 0, A.tiles + (size_t)t0 * A.plan.tile_bytes, A.plan.tile_bytes);
-    }
-    uint32_t w_phase = 0;
-    bool ok = mbar_wait(&sm.bar_w, w_phase);
-    w_phase ^= 1u;
-    uint32_t load_phase[2] = {0u, 0u};
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const bool bf16 = A.fv.precision == 1, fp8 = A.fv.precision == 2;
-    uint32_t phase = 0;
-    int buf = 0;
-    int pending = 1;   // buffer with a copy in flight: 1 + index, 0 = none
-    for (uint32_t t = t0; t < t1 && ok; ++t) {
-        ok &= mbar_wait(&sm.bar_load[buf], load_phase[buf]);
-        load_phase[buf] ^= 1u;
-        pending = 0;
-        if (t + 1 < t1) {
-            if (threadIdx.x == 0) load_tile(sm, buf ^ 1, A.tiles + (size_t)(t + 1) * A.plan.tile_bytes, A.plan.tile_bytes);
-            pending = 1 + (buf ^ 1);
-        }
-        const uint8_t* need = tile_weights(A, t);
-        if (need != loaded) {
-            // the previous tile's MMAs have completed (mlp_tile waited on them); swap the image
-            if (threadIdx.x == 0) bulk_load(w, need, A.plan.bytes, &sm.bar_w);
-            ok &= mbar_wait(&sm.bar_w, w_phase);
-            w_phase ^= 1u;
-            loaded = need;
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
-        }
-        float o4[4];
-        if (fp8) ok &= mlp_tile8(sm, w, A.plan, reinterpret_cast<const float*>(w + A.plan.scales), buf, phase, o4);
-        else ok &= mlp_tile(sm, w, A.plan, buf, bf16, phase, o4);
-        const uint32_t s = t * 128u + threadIdx.x;
-        if (s < n_samples) {
-            if (A.fv.precision != 0) {
-                // BF16-rounded or FP8-path values kept exactly: FP32 outputs
-                A.out_f32[s] = make_float4(o4[0], o4[1], o4[2], o4[3]);
-            } else {
-                __half2 rg = __floats2half2_rn(o4[0], o4[1]);
-                __half2 bd = __floats2half2_rn(o4[2], o4[3]);
-                uint2 u;
-                u.x = *reinterpret_cast<uint32_t*>(&rg);
-                u.y = *reinterpret_cast<uint32_t*>(&bd);
-                A.out[s] = u;
-            }
-        }
-        buf ^= 1;
-        ok = __syncthreads_and(ok ? 1 : 0) != 0;
-    }
-    if (!ok && threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
-    // drain an outstanding prefetch (bounded wait) before the CTA's shared memory is released
-    if (pending) mbar_wait(&sm.bar_load[pending - 1], load_phase[pending - 1]);
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (threadIdx.x < 32) tmem_dealloc(sm.tmem_base, 128);
-}
-
 // The MLPs over ready-made operand tiles in global memory, 256 threads per CTA: each
 // CTA takes a contiguous range of tiles (consecutive tiles mostly share a request, so the weight
 // image is reloaded only where a range crosses into another avatar's requests); tile t + 1's
 // hash rows are bulk-copied in as soon as tile t's density layer 0 has run, its SH rows as soon
 // as colour layer 0 has, so the copies overlap the chain; the epilogues split the accumulator
 // columns between the two warpgroups (FP8: each warpgroup re-quantises half of a row, the row
-// maximum exchanged through shared memory).  Same arithmetic as mlp_kernel.
+// maximum exchanged through shared memory).
 template <bool FP8>
 __global__ void __launch_bounds__(256, 4) mlp256_kernel(const __grid_constant__ MlpArgs A) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -759,7 +670,7 @@ __global__ void __launch_bounds__(256, 4) mlp256_kernel(const __grid_constant__ 
 // in shared memory; then the MLP chain runs on the tensor cores (mlp256: one thread issues,
 // the epilogues split the accumulator columns between the warpgroups).  Several CTAs per SM
 // overlap one CTA's gathers with another's MMAs, and the operand rows never go to global memory.
-// Same arithmetic as map_encode_kernel + mlp_kernel, so the outputs are the same bits.
+// Same arithmetic as map_encode_kernel + mlp256_kernel, so the outputs are the same bits.
 __global__ void __launch_bounds__(256, 4) field_tile_kernel(const __grid_constant__ WaveArgs A, const __grid_constant__ MlpArgs M) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     FusedSmem& sm = *reinterpret_cast<FusedSmem*>(smem_raw);
@@ -1096,7 +1007,6 @@ __global__ void march_debug_kernel(RenderView rv, const uint8_t* __restrict__ bf
 }
 
 // ------------------------------------------------------------------ launchers
-static size_t mlp_smem_bytes(const TilePlan& p) { return ((sizeof(TileSmem) + 1023) & ~size_t(1023)) + p.bytes; }
 
 static int g_sms = 0;
 static int sm_count() {
@@ -1171,45 +1081,26 @@ cudaError_t launch_field_fused(const WaveArgs& a, const MlpArgs& m, uint32_t max
 }
 
 cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm) {
-    {
-        // the 256-thread kernel (mlp_kernel, 128 threads, double-buffered tiles, is kept for comparison)
-        const size_t smem2 = (size_t)mlp2_w_off(a.plan.tile_bytes) + a.plan.bytes;
-        const bool fp8 = a.fv.precision == 2;
-        const void* fn = fp8 ? (const void*)mlp256_kernel<true> : (const void*)mlp256_kernel<false>;
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
-        if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-        if (e != cudaSuccess) return e;
-        int dev = 0, smem_sm = 0, reserved = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
-        int per_sm = smem_sm / (int)(smem2 + (size_t)reserved);
-        per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
-        if (ctas_per_sm && (int)ctas_per_sm < per_sm) per_sm = (int)ctas_per_sm;
-        uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
-        if (max_tiles < grid) grid = max_tiles ? max_tiles : 1;
-        if (fp8) mlp256_kernel<true><<<grid, 256, smem2, s>>>(a);
-        else mlp256_kernel<false><<<grid, 256, smem2, s>>>(a);
-        return cudaGetLastError();
-    }
-    size_t smem = mlp_smem_bytes(a.plan);
-    cudaError_t e = cudaFuncSetAttribute(mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = (size_t)mlp2_w_off(a.plan.tile_bytes) + a.plan.bytes;
+    const bool fp8 = a.fv.precision == 2;
+    const void* fn = fp8 ? (const void*)mlp256_kernel<true> : (const void*)mlp256_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    // contiguous tile ranges: exactly as many CTAs as shared memory lets reside at once (the
-    // carveout set to all-shared), at most 4 (4 x 128 TMEM columns fill an SM)
-    e = cudaFuncSetAttribute(mlp_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     int dev = 0, smem_sm = 0, reserved = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    // contiguous tile ranges: as many CTAs as shared memory lets reside at once (the carveout set
+    // to all-shared), at most 4 (4 x 128 TMEM columns fill an SM)
     int per_sm = smem_sm / (int)(smem + (size_t)reserved);
     per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
     if (ctas_per_sm && (int)ctas_per_sm < per_sm) per_sm = (int)ctas_per_sm;
     uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
     if (max_tiles < grid) grid = max_tiles ? max_tiles : 1;
-    mlp_kernel<<<grid, 128, smem, s>>>(a);
+    if (fp8) mlp256_kernel<true><<<grid, 256, smem, s>>>(a);
+    else mlp256_kernel<false><<<grid, 256, smem, s>>>(a);
     return cudaGetLastError();
 }
 
