@@ -587,7 +587,8 @@ def run_train(args):
     ctx.frame_upload(0, 0, av.frame(av.frame_coeffs(0)))
     ctx.occupancy_from_mesh(0, 0, 0.015)
     ctx.params_load(0, fc, S.field_params(fc, seed=0))
-    cfg = TrainConfig(n_rays_per_batch=4096, target_batch_size=1 << 18, max_samples=1 << 20)
+    cfg = TrainConfig(n_rays_per_batch=4096, target_batch_size=1 << 18, max_samples=1 << 20, tf32=args.train_math != "fp32",
+                      tcgen05=args.train_math == "tcgen05")
     ts = TrainStep(ctx, 0, fc, cfg)
     rng = np.random.default_rng(0)
     n = cfg.n_rays_per_batch
@@ -625,7 +626,9 @@ def run_train(args):
     stage = {k: v / args.steps for k, v in st["stage_ms"].items() if v > 0}
     dev_ms = sum(stage.values())
     line = {"workload": "training step: 4096 rays, 2^18-sample batch, field with 16 expression dims",
-            "train_math": "TF32 tensor-core layer products, FP32 accumulation" if cfg.tf32 else "FP32",
+            "train_math": {"tcgen05": "tcgen05 kernel: FP16 operands, FP32 accumulation in TMEM",
+                           "tf32": "TF32 tensor-core layer products (cuBLAS), FP32 accumulation",
+                           "fp32": "FP32 layer products (cuBLAS)"}[args.train_math],
             "ms_per_step_device": dev_ms, "ms_per_step_wall": wall * 1e3, "stage_ms_per_step": stage,
             "march_samples_per_step": samples / args.steps,
             "trained_samples_per_s_device": cfg.target_batch_size / (dev_ms / 1e3),
@@ -912,6 +915,7 @@ def main():
     ap.add_argument("--rows", type=int, default=16, help="precision: image rows rendered by the FP64 oracle")
     ap.add_argument("--tune", default="", help="launch shapes, e.g. max_steps_per_round=16,bvh_top_nodes=21 (insta_tuning_set)")
     ap.add_argument("--autotune", action="store_true", help="render: run insta_autotune on the frame before the warm-up")
+    ap.add_argument("--train-math", choices=["tcgen05", "tf32", "fp32"], default="tf32", help="train: the backward's layer products")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--rate", type=float, default=240.0)
     ap.add_argument("--duration", type=float, default=30.0)

@@ -285,6 +285,10 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
  * rounded to TF32, FP32 accumulation; still finer than the reference's FP16 training arithmetic). */
 #define INSTA_TRAIN_MATH_FP32 0
 #define INSTA_TRAIN_MATH_TF32 1
+/* The library's own tcgen05 kernel: per 128-sample tile the forward (activations kept in shared
+ * memory) and the backward (input and weight gradients) as FP16 tensor-core products with FP32
+ * accumulation -- the arithmetic class of tiny-cuda-nn's FP16 fully fused MLP training. */
+#define INSTA_TRAIN_MATH_TCGEN05 2
 int insta_train_set_math(insta_ctx* ctx, int math);
 /* Adam (configs/nerf/main.json nests it in an Ema), as tiny-cuda-nn's Adam steps it: the gradient
  * is divided by loss_scale first (LOSS_SCALE, 128 in train_nerf_step); the MLP weights get

@@ -366,9 +366,10 @@ class Context:
         """insta_field_backward: ADDS d(sum dl_dout . out)/d(params) into grad (f32, snapshot order)."""
         self._check(self.lib.insta_field_backward(self.h, avatar, _addr(coords), stride, n, _addr(dl_dout), _addr(grad), _addr(out4)))
 
-    def train_set_math(self, tf32: bool):
-        """insta_train_set_math: TF32 tensor-core layer products in the backward (else FP32)."""
-        self._check(self.lib.insta_train_set_math(self.h, 1 if tf32 else 0))
+    def train_set_math(self, tf32, tcgen05=False):
+        """insta_train_set_math: TF32 tensor-core layer products in the backward (else FP32), or with
+        tcgen05=True the library's own tcgen05 kernel (FP16 operands, FP32 accumulation)."""
+        self._check(self.lib.insta_train_set_math(self.h, 2 if tcgen05 else (1 if tf32 else 0)))
 
     def adam_step(self, avatar, grad, learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6, ema_decay=0.0,
                   loss_scale=1.0):

@@ -140,6 +140,8 @@ struct insta_ctx {
     int async_next = 0;
     cublasHandle_t blas = nullptr;      // the training side's GEMMs
     bool train_tf32 = false;            // insta_train_set_math: TF32 tensor-core GEMMs
+    bool train_tc = false;              // insta_train_set_math: the library's tcgen05 layer products
+    DevBuf train_images;                // their weight images (rebuilt from the FP32 masters per call)
     DevBuf train_scratch;
     DevBuf loss_scratch;     // insta_train_loss: each kept ray's block start before compaction
     DevBuf train_t;          // insta_training_samples: each ray's sample positions t
@@ -1590,6 +1592,64 @@ TrainShape train_shape(const Field& fd) {
     return t;
 }
 
+// The tcgen05 training plan of a field: weight-image tiles (forward B tiles, and W^T for the input
+// gradients), TMEM columns of the weight-gradient accumulators (from column 96, 32-aligned), and
+// the shared-memory layout.  False when the field does not fit one CTA (shared memory, TMEM).
+bool train_mlp_plan(const FieldLayout& L, TrainMlpPlan& P, TrainImageList& I) {
+    P = TrainMlpPlan{};
+    I = TrainImageList{};
+    const int nl = L.n_density + L.n_rgb;
+    if (nl > 8 || L.n_density < 2 || L.n_rgb < 2) return false;
+    P.n_density = (uint32_t)L.n_density;
+    P.n_rgb = (uint32_t)L.n_rgb;
+    P.kd = L.layer_k[0];
+    if (P.kd % 16 || P.kd > 64) return false;
+    uint32_t off = 0, col = 96;
+    auto add = [&](uint32_t n, uint32_t k, uint64_t w_off, uint32_t rows, uint32_t cols, uint32_t col0, uint32_t tr) {
+        TrainImageTile& T = I.tile[I.n_tiles++];
+        T = TrainImageTile{off, n, k, w_off, rows, cols, 0u, col0, tr};
+        const uint32_t at = off;
+        off = (off + n * k * 2 + 127) / 128 * 128;
+        return at;
+    };
+    for (int l = 0; l < nl; ++l) {
+        TrainMlpLayer& Y = P.layer[l];
+        Y.n_out = L.layer_n[l];
+        Y.n_in = L.layer_k[l];
+        if (Y.n_in > 64 || (Y.n_out != 16 && Y.n_out != 64)) return false;
+        Y.k_pad = (Y.n_in + 15) / 16 * 16;
+        Y.w_off = L.layer_off[l];
+        Y.n_out_real = l == nl - 1 ? 3u : Y.n_out;
+        if (l == L.n_density) {
+            Y.fwd_img = add(Y.n_out, 16, Y.w_off, Y.n_out, Y.n_in, 0, 0);
+            Y.fwd_img2 = add(Y.n_out, 16, Y.w_off, Y.n_out, Y.n_in, 16, 0);
+            Y.bwd_n = 16;   // only the density-output part of the colour input has a gradient to pass on
+        } else {
+            Y.fwd_img = add(Y.n_out, Y.k_pad, Y.w_off, Y.n_out, Y.n_in, 0, 0);
+            Y.bwd_n = Y.k_pad;
+        }
+        Y.bwd_img = add(Y.bwd_n, Y.n_out, Y.w_off, Y.n_out, Y.n_in, 0, 1);
+        Y.kp_blk = Y.n_in <= 32 ? 32u : 64u;
+        Y.dw_col = col;
+        col = (col + Y.n_out + 31) / 32 * 32;
+    }
+    if (col > 512) return false;
+    P.img_bytes = off;
+    auto r1k = [](uint32_t b) { return (b + 1023u) & ~1023u; };
+    uint32_t o = 1024;
+    P.s_img = o; o = r1k(o + P.img_bytes);
+    P.s_x = o; o = r1k(o + 128 * P.kd * 2);
+    P.s_sh = o; o += 128 * 16 * 2;
+    for (int k = 0; k < nl - 2; ++k) { P.s_kept[k] = o; o += 128 * 64 * 2; }
+    P.s_dens = o; o += 128 * 16 * 2;
+    P.s_dy = o; o += 128 * 64 * 2;
+    P.s_bt = o; o += 64 * 128 * 2;
+    P.s_at32 = o; o += 128 * 128 * 2;
+    P.s_at64 = o; o += 128 * 128 * 2;
+    P.smem_bytes = o;
+    return o <= 227u * 1024u;
+}
+
 void ensure_master(insta_ctx* ctx, Field& fd) {
     if (fd.w32_valid) return;
     ctx->alloc(fd.w32, fd.n_params * 4);
@@ -1610,6 +1670,20 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
         if (stride < 11 + fd.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
         if ((uintptr_t)grad & 7) fail(INSTA_ERR_INVALID_ARG, "grad must be 8-byte aligned");   // paired table atomics
         if (n == 0) return;
+        if (ctx->train_tc) {
+            ensure_master(ctx, fd);
+            const TrainShape t = train_shape(fd);
+            TrainMlpPlan plan;
+            TrainImageList images;
+            if (!train_mlp_plan(field_layout(fd.desc), plan, images))
+                fail(INSTA_ERR_UNSUPPORTED, "the field's MLPs do not fit the tcgen05 training kernel; use INSTA_TRAIN_MATH_TF32");
+            ctx->alloc(ctx->train_images, plan.img_bytes);
+            ctx->alloc(ctx->train_scratch, ((size_t)2 * t.kd + 32) * (size_t)n * 4);
+            Stage st(ctx, INSTA_STAGE_TRAIN, (dl_dout && grad) ? 4 : 3);
+            CK(launch_field_train_tc(fd.view, t, plan, images, (uint8_t*)ctx->train_images.p, (const float*)fd.w32.p, coords, stride,
+                                     (uint32_t)n, dl_dout, out4, grad, (float*)ctx->train_scratch.p, ctx->err_dev, ctx->stream));
+            return;
+        }
         if (!ctx->blas) {
             if (cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) fail(INSTA_ERR_CUDA, "cublasCreate failed");
             if (cublasSetMathMode(ctx->blas, ctx->train_tf32 ? CUBLAS_TF32_TENSOR_OP_MATH : CUBLAS_DEFAULT_MATH) != CUBLAS_STATUS_SUCCESS)
@@ -1626,8 +1700,10 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
 
 int insta_train_set_math(insta_ctx* ctx, int math) {
     return guarded(ctx, [&] {
-        if (math != INSTA_TRAIN_MATH_FP32 && math != INSTA_TRAIN_MATH_TF32) fail(INSTA_ERR_INVALID_ARG, "unknown training math %d", math);
+        if (math != INSTA_TRAIN_MATH_FP32 && math != INSTA_TRAIN_MATH_TF32 && math != INSTA_TRAIN_MATH_TCGEN05)
+            fail(INSTA_ERR_INVALID_ARG, "unknown training math %d", math);
         ctx->train_tf32 = math == INSTA_TRAIN_MATH_TF32;
+        ctx->train_tc = math == INSTA_TRAIN_MATH_TCGEN05;
         if (ctx->blas && cublasSetMathMode(ctx->blas, ctx->train_tf32 ? CUBLAS_TF32_TENSOR_OP_MATH : CUBLAS_DEFAULT_MATH) != CUBLAS_STATUS_SUCCESS)
             fail(INSTA_ERR_CUDA, "cublasSetMathMode failed");
     });

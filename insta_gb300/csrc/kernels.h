@@ -208,6 +208,52 @@ struct TrainShape {
     uint64_t table_off;          // offset of the hash table ([entries][2])
 };
 size_t train_scratch_floats(const TrainShape& t, uint32_t n);
+
+// The layer products of training on tcgen05 (train_mlp.cu).  Layers in parameter order: the
+// density MLP (hidden layers, then its 16 outputs), then the colour MLP (hidden layers, then its
+// 16 padded outputs).
+struct TrainMlpLayer {
+    uint32_t n_out, n_in, k_pad;   // forward N, input width, forward K (n_in rounded to 16)
+    uint64_t w_off;                // the layer's [n_out][n_in] weights in the parameters
+    uint32_t fwd_img, fwd_img2;    // image offsets of the forward B tile(s) (colour layer 0: two K = 16 halves)
+    uint32_t bwd_img, bwd_n;       // image offset of W^T (N = bwd_n, K = n_out) for dX
+    uint32_t kp_blk;               // input width padded to 32 or 64: the weight gradient's row block
+    uint32_t dw_col;               // TMEM column of the weight-gradient accumulator (n_out columns)
+    uint32_t n_out_real;           // output rows that carry gradient (3 for the colour output)
+};
+struct TrainMlpPlan {
+    TrainMlpLayer layer[8];
+    uint32_t n_density, n_rgb, kd;
+    uint32_t img_bytes;
+    uint32_t s_img, s_x, s_sh, s_kept[8], s_dens, s_dy, s_bt, s_at32, s_at64, smem_bytes;   // s_at64 = s_at32 + 32 KiB
+};
+struct TrainMlpArgs {
+    TrainMlpPlan plan;
+    const uint8_t* images;   // the weight images (device), img_bytes
+    const float* xd;         // [n][kd] encoding
+    const float* xr;         // [n][32]: columns 16..31 SH
+    const float* dl_dout;    // [n][4] or null (forward only)
+    float* out4;             // [n][4] or null
+    float* dxd;              // [n][kd] dL/d encoding
+    float* grad;             // parameter gradients (added to)
+    uint32_t n;
+    uint32_t* err;
+};
+struct TrainImageTile {
+    uint32_t dst, n, k;                      // N x K FP16 tile at image byte offset dst
+    uint64_t w_off;
+    uint32_t rows, cols, row0, col0, transpose;
+};
+struct TrainImageList {
+    TrainImageTile tile[17];
+    uint32_t n_tiles;
+};
+cudaError_t launch_train_mlp(const TrainMlpArgs& a, const TrainImageList& images, const float* w32, uint8_t* img_dev, cudaStream_t s);
+// insta_field_backward with INSTA_TRAIN_MATH_TCGEN05: encode (FP32 master table), the tcgen05 layer
+// products, then the hash-table backward; scratch (2 kd + 32) n floats.
+cudaError_t launch_field_train_tc(const FieldView& fv, const TrainShape& t, const TrainMlpPlan& plan, const TrainImageList& images,
+                                  uint8_t* img_dev, const float* w32, const float* coords, uint32_t stride, uint32_t n,
+                                  const float* dl_dout, float* out4, float* grad, float* scratch, uint32_t* err, cudaStream_t s);
 cudaError_t launch_field_train(struct cublasContext* h, const FieldView& fv, const TrainShape& t, const float* w32, const float* coords,
                                uint32_t stride, uint32_t n, const float* dl_dout, float* out4, float* grad, float* scratch,
                                cudaStream_t s);

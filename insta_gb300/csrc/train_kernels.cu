@@ -570,6 +570,33 @@ cudaError_t launch_field_train(cublasHandle_t h, const FieldView& fv, const Trai
     return okb ? cudaGetLastError() : cudaErrorUnknown;
 }
 
+cudaError_t launch_field_train_tc(const FieldView& fv, const TrainShape& t, const TrainMlpPlan& plan, const TrainImageList& images,
+                                  uint8_t* img_dev, const float* w32, const float* coords, uint32_t stride, uint32_t n,
+                                  const float* dl_dout, float* out4, float* grad, float* scratch, uint32_t* err, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    float* xd = scratch;
+    float* xr = xd + (size_t)t.kd * n;
+    float* dxd = xr + (size_t)32 * n;
+    train_encode_kernel<<<(n + 255) / 256, 256, 0, s>>>(fv, reinterpret_cast<const float2*>(w32 + t.table_off), coords, stride, n, xd, t.kd,
+                                                        xr);
+    const bool bwd = dl_dout && grad;
+    TrainMlpArgs a{};
+    a.plan = plan;
+    a.images = img_dev;
+    a.xd = xd;
+    a.xr = xr;
+    a.dl_dout = bwd ? dl_dout : nullptr;
+    a.out4 = out4;
+    a.dxd = dxd;
+    a.grad = grad;
+    a.n = n;
+    a.err = err;
+    cudaError_t e = launch_train_mlp(a, images, w32, img_dev, s);
+    if (e != cudaSuccess || !bwd) return e;
+    hash_backward_kernel<<<(n + 255) / 256, 256, 0, s>>>(fv, coords, stride, n, dxd, t.kd, grad + t.table_off);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_adam(size_t n, size_t n_matrix, float* w, float* m, float* v, uint32_t* table_steps, const float* g, float loss_scale,
                         float lr, float b1, float b2, float eps, float l2, uint32_t step, float* ema, float decay, uint32_t ema_step,
                         __half* w16, __half* w16_train, cudaStream_t s) {

@@ -48,6 +48,7 @@ class TrainConfig:
     aabb_min: tuple = (0.0, 0.0, 0.0)
     aabb_max: tuple = (1.0, 1.0, 1.0)
     tf32: bool = True                  # TF32 tensor-core layer products in the backward
+    tcgen05: bool = False              # the library's tcgen05 training kernel (FP16 operands) instead
     adam: dict = field(default_factory=lambda: dict(learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6,
                                                     ema_decay=0.95))
 
@@ -78,7 +79,7 @@ class TrainStep:
         self.counters_host = torch.zeros(2, dtype=torch.int32, pin_memory=True)
         self.n_steps = 0
         self._last_kept = 0
-        ctx.train_set_math(cfg.tf32)
+        ctx.train_set_math(cfg.tf32, tcgen05=cfg.tcgen05)
 
     def step(self, grid_frame: int, rays, image, start_rand, target, background=None, extra=None, n_images: int = 0,
              depth=None, seg_mask=None, mean_density=None, exposure=None) -> dict:

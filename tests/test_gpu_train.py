@@ -101,6 +101,39 @@ def test_backward_tf32(ctx, field, oracle):
         assert np.linalg.norm(a - b) <= 5e-2 * np.linalg.norm(b), (lo, hi, np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
+@pytest.mark.parametrize("n", [3000, 77, 128 * 152 * 2 + 5])
+def test_backward_tcgen05(ctx, field, oracle, n):
+    """insta_train_set_math(TCGEN05): the library's tcgen05 kernel, FP16 operands (encoding, kept
+    activations, output gradients, weights) with FP32 accumulation, the arithmetic class of the
+    reference's FP16 fused MLP training: outputs within 5e-3 of the largest, per-block gradient
+    norms within 5e-2 of the FP64 oracle.  Sizes: ragged, one partial tile, and more tiles than
+    CTAs (each CTA keeps its weight-gradient accumulators in TMEM over several tiles)."""
+    fc, params, lay = field
+    c = coords(n, seed=21 + n)
+    g_out = np.random.default_rng(22 + n).normal(size=(n, 4)).astype(np.float32)
+    grad = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    ctx.train_set_math(False, tcgen05=True)
+    try:
+        ctx.field_backward(AVATAR, dev(c), c.shape[1], n, dev(g_out), grad, out)
+        ctx.sync()
+        out_fwd = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        ctx.field_backward(AVATAR, dev(c), c.shape[1], n, None, None, out_fwd)   # forward only
+        ctx.sync()
+    finally:
+        ctx.train_set_math(False)
+    ref_g, ref_out = oracle.field_backward(fc, params, c, g_out)
+    got = out.cpu().numpy()
+    assert np.abs(got - ref_out).max() <= 5e-3 * np.abs(ref_out).max()
+    assert np.array_equal(out_fwd.cpu().numpy(), got)
+    g = grad.cpu().numpy().astype(np.float64)
+    for lo, hi in blocks(lay):
+        a, b = g[lo:hi], ref_g[lo:hi]
+        assert np.linalg.norm(a - b) <= 5e-2 * np.linalg.norm(b), (lo, hi, np.linalg.norm(a - b) / np.linalg.norm(b))
+    touched_ref = ref_g[lay.table_offset:] != 0
+    assert ((g[lay.table_offset:] != 0) <= touched_ref).all()
+
+
 def test_backward_accumulates_and_forward_only(ctx, field, oracle):
     fc, params, lay = field
     n = 700

@@ -20,7 +20,7 @@ class FakeLib:
 
     def insta_train_set_math(self, h, math):
         self.calls.append({"math": math})
-        return 0 if math in (0, 1) else 1
+        return 0 if math in (0, 1, 2) else 1
 
     def insta_last_error(self, h):
         return b"unknown training math"
@@ -59,7 +59,8 @@ def test_train_set_math_passes_and_rejects():
     ctx = fake_context()
     ctx.train_set_math(True)
     ctx.train_set_math(False)
-    assert [c["math"] for c in ctx.lib.calls] == [1, 0]
+    ctx.train_set_math(False, tcgen05=True)
+    assert [c["math"] for c in ctx.lib.calls] == [1, 0, 2]
     with pytest.raises(abi.InstaError):
         ctx._check(ctx.lib.insta_train_set_math(ctx.h, 7))
 
