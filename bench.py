@@ -915,7 +915,7 @@ def main():
     ap.add_argument("--rows", type=int, default=16, help="precision: image rows rendered by the FP64 oracle")
     ap.add_argument("--tune", default="", help="launch shapes, e.g. max_steps_per_round=16,bvh_top_nodes=21 (insta_tuning_set)")
     ap.add_argument("--autotune", action="store_true", help="render: run insta_autotune on the frame before the warm-up")
-    ap.add_argument("--train-math", choices=["tcgen05", "tf32", "fp32"], default="tf32", help="train: the backward's layer products")
+    ap.add_argument("--train-math", choices=["tcgen05", "tf32", "fp32"], default="tcgen05", help="train: the backward's layer products")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--rate", type=float, default=240.0)
     ap.add_argument("--duration", type=float, default=30.0)

@@ -357,9 +357,53 @@ typedef struct insta_train_loss_desc {
     float* coords_out;                /* [max_samples_compacted][stride]                            */
     float* dloss_doutput;             /* f32[max_samples_compacted][4]                              */
     float* loss_output;               /* f32[max_rays] per-ray loss / n_rays, or NULL               */
+    /* importance sampling and the error map (compute_loss_kernel_train_nerf,
+     * instant-ngp/src/testbed_nerf.cu:1411-1416,1494-1536; train_nerf_step runs it with
+     * accumulate_error = true, :3248,3333).  Per original ray, as insta_training_pixels writes them. */
+    const float* pdf;                 /* f32 img_pdf * xy_pdf the ray's loss is divided by, or NULL = 1 */
+    float* error_map;                 /* f32[n_images][res_y][res_x]: each kept ray's mean loss added
+                                         bilinearly at its image position, or NULL = off             */
+    uint32_t error_map_res[2];        /* x, y (each >= 2, no larger than the images)                 */
+    const float* image_xy;            /* f32[2] position in [0, 1]^2 of the ray's pixel              */
+    const uint32_t* image_index;      /* the ray's training image                                     */
 } insta_train_loss_desc;
 /* All pointers are device pointers; asynchronous on the context's stream. */
 int insta_train_loss(insta_ctx* ctx, const insta_train_loss_desc* desc);
+
+/* The training batch's image and pixel draws of generate_training_samples_nerf and
+ * compute_loss_kernel_train_nerf (instant-ngp/src/testbed_nerf.cu:1140-1144,1406-1420): per ray i
+ * the image image_idx(i, ...) (evenly spread, or from cdf_img with ld_random_val(i + n_rays_total,
+ * 0xdeadbeef) when the error-map CDFs are given), the step's pcg32 advanced by 8 i, the pixel
+ * position nerf_random_image_pos_training (two draws, through sample_cdf_2d when the CDFs are
+ * given, optionally snapped to pixel centres), then the random background colour draw
+ * (random_val_3d, sRGB).  The caller turns (image, xy) into camera rays. */
+typedef struct insta_training_pixels_desc {
+    uint32_t n_rays;                  /* rays of the batch                                         */
+    uint32_t n_rays_total;            /* rays drawn by the earlier steps                           */
+    uint32_t n_images;
+    const int32_t* resolution;        /* [n_images][2] image width, height (device)                 */
+    int32_t snap_to_pixel_centers;
+    uint64_t rng_state, rng_inc;      /* the step's pcg32 (m_rng)                                   */
+    const float* cdf_x_cond_y;        /* insta_error_map_cdf's outputs, or all NULL = uniform       */
+    const float* cdf_y;
+    const float* cdf_img;
+    uint32_t cdf_res[2];              /* x, y of the error map the CDFs were built from             */
+    uint32_t* out_image;              /* [n_rays]                                                   */
+    float* out_xy;                    /* [n_rays][2]                                                */
+    float* out_pdf;                   /* [n_rays] img_pdf * xy_pdf, or NULL                          */
+    float* out_background;            /* [n_rays][3] random_bg_color draw (sRGB), or NULL           */
+} insta_training_pixels_desc;
+int insta_training_pixels(insta_ctx* ctx, const insta_training_pixels_desc* desc);
+
+/* The error map's sampling distributions (construct_cdf_2d, construct_cdf_1d and the image CDF of
+ * train_nerf_step, instant-ngp/src/testbed_nerf.cu:1967-2020,3010-3041): per image and row the
+ * conditional CDF over x (mixed with 1 % uniform), per image the CDF over rows (1 %), and over the
+ * images the CDF with 10 % uniform.  error_map f32[n_images][res_y][res_x] in; cdf_x_cond_y
+ * (same shape), cdf_y [n_images][res_y], cdf_img [n_images] and pmf_img [n_images] (or NULL) out.
+ * Device pointers, asynchronous; the reference builds the image CDF on the host, here one device
+ * thread runs the same loop. */
+int insta_error_map_cdf(insta_ctx* ctx, const float* error_map, uint32_t n_images, uint32_t res_x, uint32_t res_y,
+                        float* cdf_x_cond_y, float* cdf_y, float* cdf_img, float* pmf_img);
 
 /* -- render ------------------------------------------------------------------- */
 /* out_rgba f32[h*w*4] (linear RGBA, zero background), out_depth f32[h*w] (1e10 where no

@@ -26,7 +26,7 @@ EXPORTS = [
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_density_grid_load", "insta_density_grid_reset", "insta_density_grid_update", "insta_density_grid_read",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
-    "insta_field_eval", "insta_field_eval_training", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_train_loss", "insta_train_set_math", "insta_render", "insta_render_async", "insta_render_batch",
+    "insta_field_eval", "insta_field_eval_training", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_train_loss", "insta_training_pixels", "insta_error_map_cdf", "insta_train_set_math", "insta_render", "insta_render_async", "insta_render_batch",
     "insta_render_samples", "insta_tuning_set", "insta_tuning_get", "insta_autotune", "insta_march_debug", "insta_nearest_debug",
     "insta_raycast",
     "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
@@ -71,7 +71,15 @@ class TrainLossDesc(C.Structure):
                 ("depth", C.c_void_p), ("seg_mask", C.c_void_p), ("mean_density", C.c_void_p), ("rays_counter", C.c_void_p),
                 ("ray_indices", C.c_void_p), ("numsteps", C.c_void_p), ("coords", C.c_void_p), ("network_output", C.c_void_p),
                 ("numsteps_counter", C.c_void_p), ("coords_out", C.c_void_p), ("dloss_doutput", C.c_void_p),
-                ("loss_output", C.c_void_p)]
+                ("loss_output", C.c_void_p), ("pdf", C.c_void_p), ("error_map", C.c_void_p), ("error_map_res", C.c_uint32 * 2),
+                ("image_xy", C.c_void_p), ("image_index", C.c_void_p)]
+
+
+class TrainingPixelsDesc(C.Structure):
+    _fields_ = [("n_rays", C.c_uint32), ("n_rays_total", C.c_uint32), ("n_images", C.c_uint32), ("resolution", C.c_void_p),
+                ("snap_to_pixel_centers", C.c_int32), ("rng_state", C.c_uint64), ("rng_inc", C.c_uint64),
+                ("cdf_x_cond_y", C.c_void_p), ("cdf_y", C.c_void_p), ("cdf_img", C.c_void_p), ("cdf_res", C.c_uint32 * 2),
+                ("out_image", C.c_void_p), ("out_xy", C.c_void_p), ("out_pdf", C.c_void_p), ("out_background", C.c_void_p)]
 
 
 class InstaError(RuntimeError):
@@ -157,6 +165,8 @@ def load(path: Path | None = None):
             "insta_field_backward": [vp, C.c_int, vp, u32, i64, vp, vp, vp],
             "insta_adam_step": [vp, C.c_int, vp, C.POINTER(AdamConfig)],
             "insta_train_loss": [vp, C.POINTER(TrainLossDesc)],
+            "insta_training_pixels": [vp, C.POINTER(TrainingPixelsDesc)],
+            "insta_error_map_cdf": [vp, vp, u32, u32, u32, vp, vp, vp, vp],
             "insta_train_set_math": [vp, C.c_int],
             "insta_render": [vp, C.POINTER(RenderDesc), vp, vp],
             "insta_render_async": [vp, C.POINTER(RenderDesc), vp, vp],
@@ -379,7 +389,8 @@ class Context:
         self._check(self.lib.insta_adam_step(self.h, avatar, _addr(grad), C.byref(cfg)))
 
     _LOSS_PTRS = ("rays", "target", "background", "exposure", "depth", "seg_mask", "mean_density", "rays_counter", "ray_indices",
-                  "numsteps", "coords", "network_output", "numsteps_counter", "coords_out", "dloss_doutput", "loss_output")
+                  "numsteps", "coords", "network_output", "numsteps_counter", "coords_out", "dloss_doutput", "loss_output", "pdf",
+                  "error_map", "image_xy", "image_index")
 
     def train_loss(self, **kw):
         """insta_train_loss: keyword arguments are insta_train_loss_desc's fields (buffers as
@@ -393,11 +404,35 @@ class Context:
                 setattr(d, k, a.value if a is not None else None)
             elif k in ("aabb_min", "aabb_max"):
                 getattr(d, k)[:] = [float(x) for x in v]
+            elif k == "error_map_res":
+                d.error_map_res[:] = [int(x) for x in v]
             elif k in ("loss_type", "depth_loss_type") and isinstance(v, str):
                 setattr(d, k, LOSS_TYPES[v.lower()])
             else:
                 setattr(d, k, v)
         self._check(self.lib.insta_train_loss(self.h, C.byref(d)))
+
+    def training_pixels(self, n_rays, n_images, rng_state, rng_inc, out_image, out_xy, out_pdf=None, out_background=None,
+                        n_rays_total=0, resolution=None, snap=False, cdfs=None, cdf_res=(0, 0)):
+        """insta_training_pixels: the batch's image and pixel draws (device buffers); cdfs =
+        (cdf_x_cond_y, cdf_y, cdf_img) from error_map_cdf, or None for uniform draws."""
+        d = TrainingPixelsDesc()
+        d.n_rays, d.n_rays_total, d.n_images = n_rays, n_rays_total, n_images
+        d.resolution = None if resolution is None else _addr(resolution).value
+        d.snap_to_pixel_centers = int(snap)
+        d.rng_state, d.rng_inc = rng_state, rng_inc
+        if cdfs is not None:
+            d.cdf_x_cond_y, d.cdf_y, d.cdf_img = (_addr(a).value for a in cdfs)
+        d.cdf_res[:] = [int(x) for x in cdf_res]
+        d.out_image, d.out_xy = _addr(out_image).value, _addr(out_xy).value
+        d.out_pdf = None if out_pdf is None else _addr(out_pdf).value
+        d.out_background = None if out_background is None else _addr(out_background).value
+        self._check(self.lib.insta_training_pixels(self.h, C.byref(d)))
+
+    def error_map_cdf(self, error_map, n_images, res_x, res_y, cdf_x_cond_y, cdf_y, cdf_img, pmf_img=None):
+        """insta_error_map_cdf on device buffers."""
+        self._check(self.lib.insta_error_map_cdf(self.h, _addr(error_map), n_images, res_x, res_y, _addr(cdf_x_cond_y), _addr(cdf_y),
+                                                 _addr(cdf_img), _addr(pmf_img)))
 
     @staticmethod
     def render_desc(avatar, frame, width, height, focal, cam, cone_angle=1 / 256, spp=0, min_transmittance=0.01,

@@ -1787,11 +1787,43 @@ int insta_train_loss(insta_ctx* ctx, const insta_train_loss_desc* d) {
         }
         if (((uintptr_t)d->network_output | (uintptr_t)d->dloss_doutput) & 15)
             fail(INSTA_ERR_INVALID_ARG, "network_output and dloss_doutput must be 16-byte aligned");
+        if (d->error_map) {
+            if (!d->image_xy || !d->image_index) fail(INSTA_ERR_INVALID_ARG, "the error map needs image_xy and image_index");
+            if (d->error_map_res[0] < 2 || d->error_map_res[1] < 2 || (uint64_t)d->error_map_res[0] * d->error_map_res[1] > (1ull << 26))
+                fail(INSTA_ERR_INVALID_ARG, "error_map_res must be at least 2 x 2 and at most 2^26 cells");
+            if ((uintptr_t)d->image_xy & 7) fail(INSTA_ERR_INVALID_ARG, "image_xy must be 8-byte aligned");
+        }
         {
             ctx->alloc(ctx->loss_scratch, (size_t)std::max(d->max_rays, 1u) * 4);
             Stage st(ctx, INSTA_STAGE_TRAIN, (d->max_rays > 0 ? 2 : 0) + (d->target_batch_size > 0 ? 2 : 0));
             CK(launch_train_loss(*d, (uint32_t*)ctx->loss_scratch.p, ctx->stream));
         }
+    });
+}
+
+int insta_training_pixels(insta_ctx* ctx, const insta_training_pixels_desc* d) {
+    return guarded(ctx, [&] {
+        if (!d) fail(INSTA_ERR_INVALID_ARG, "null description");
+        if (d->n_rays == 0) return;
+        if (d->n_images == 0) fail(INSTA_ERR_INVALID_ARG, "n_images must be positive");
+        if (!d->out_image || !d->out_xy) fail(INSTA_ERR_INVALID_ARG, "null outputs");
+        if (d->snap_to_pixel_centers && !d->resolution) fail(INSTA_ERR_INVALID_ARG, "snapping needs the image resolutions");
+        const bool cdf = d->cdf_x_cond_y || d->cdf_y || d->cdf_img;
+        if (cdf && !(d->cdf_x_cond_y && d->cdf_y && d->cdf_img)) fail(INSTA_ERR_INVALID_ARG, "give all three CDFs or none");
+        if (cdf && (d->cdf_res[0] == 0 || d->cdf_res[1] == 0)) fail(INSTA_ERR_INVALID_ARG, "cdf_res must be positive");
+        Stage st(ctx, INSTA_STAGE_TRAIN, 1);
+        CK(launch_training_pixels(*d, ctx->stream));
+    });
+}
+
+int insta_error_map_cdf(insta_ctx* ctx, const float* error_map, uint32_t n_images, uint32_t res_x, uint32_t res_y, float* cdf_x_cond_y,
+                        float* cdf_y, float* cdf_img, float* pmf_img) {
+    return guarded(ctx, [&] {
+        if (n_images == 0 || res_x == 0 || res_y == 0) fail(INSTA_ERR_INVALID_ARG, "empty error map");
+        if (n_images > 65535u) fail(INSTA_ERR_INVALID_ARG, "at most 65535 images");
+        if (!error_map || !cdf_x_cond_y || !cdf_y || !cdf_img) fail(INSTA_ERR_INVALID_ARG, "null buffers");
+        Stage st(ctx, INSTA_STAGE_TRAIN, 3);
+        CK(launch_error_map_cdf(error_map, n_images, res_x, res_y, cdf_x_cond_y, cdf_y, cdf_img, pmf_img, ctx->stream));
     });
 }
 

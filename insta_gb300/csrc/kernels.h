@@ -7,6 +7,7 @@
 #include "insta_types.h"
 
 struct insta_train_loss_desc;   // include/insta_gb300.h
+struct insta_training_pixels_desc;
 
 namespace insta {
 
@@ -262,6 +263,9 @@ cudaError_t launch_adam(size_t n, size_t n_matrix, float* w, float* m, float* v,
                         __half* w16, __half* w16_train, cudaStream_t s);
 cudaError_t launch_half_to_float(size_t n, const void* a, float* b, cudaStream_t s);
 cudaError_t launch_train_loss(const ::insta_train_loss_desc& d, uint32_t* base_scratch, cudaStream_t s);
+cudaError_t launch_training_pixels(const ::insta_training_pixels_desc& d, cudaStream_t s);
+cudaError_t launch_error_map_cdf(const float* em, uint32_t n_images, uint32_t w, uint32_t h, float* cdf_x, float* cdf_y, float* cdf_img,
+                                 float* pmf_img, cudaStream_t s);
 cudaError_t launch_raycast(const RenderView& rv, const FrameView& fr, const float* center, int color_normal, float* out_rgba,
                            float* out_depth, int32_t* out_tri, uint32_t* err, cudaStream_t s);
 cudaError_t launch_nearest_debug(const FrameView& fr, const float* pts, int64_t n, int32_t* out, uint32_t* err, cudaStream_t s);

@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(256, 4) nearest_stage_kernel(const __grid_cons
                 fence_async_smem();
                 bulk_load(top, R.fr.nodes, k * 112u, &top_bar[warp]);
             }
-            top_ok = mbar_wait(&top_bar[warp], top_phase);
+            top_ok = __all_sync(0xffffffffu, mbar_wait(&top_bar[warp], top_phase));   // warp-uniform
             if (top_ok) {
                 top_phase ^= 1u;
                 staged = R.fr.nodes;
@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(256, 4) mlp256_kernel(const __grid_constant__ 
     bool ok = mbar_wait(&ctl.bar_w, w_phase);
     w_phase ^= 1u;
     tc_fence_before();
-    __syncthreads();
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;   // uniform: the tile loop holds CTA barriers
     tc_fence_after();
     const bool bf16 = A.fv.precision == 1;
     float* xch = reinterpret_cast<float*>(smem_raw + mlp2_xch_off());
@@ -696,7 +696,7 @@ __global__ void __launch_bounds__(256, 4) field_tile_kernel(const __grid_constan
     bool ok = mbar_wait(&sm.bar_w, w_phase);
     w_phase ^= 1u;
     tc_fence_before();
-    __syncthreads();
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;   // uniform: the tile loop holds CTA barriers
     tc_fence_after();
     const bool bf16 = A.fv.precision == 1;
     const uint32_t ng = A.fv.n_levels / 4, half = ng / 2;   // level groups; warpgroup 0 takes [0, half)

@@ -250,6 +250,11 @@ struct TrainLossArgs {
     uint32_t* counter;
     float *coords_out, *dloss, *loss_out;
     uint32_t* base_in;   // each kept ray's block start before compaction (for the copy kernel)
+    const float* pdf;    // per ray img_pdf * xy_pdf, or null (1)
+    float* error_map;    // [images][res_y][res_x] or null
+    uint32_t em_res[2];
+    const float* image_xy;
+    const uint32_t* image_index;
 };
 
 // The fields of one sample the loss reads: dt (warped), the deformed position, the raw outputs.
@@ -353,13 +358,33 @@ __global__ void __launch_bounds__(32) train_loss_kernel(TrainLossArgs a) {
     tl_loss(a.depth_loss_type, target_depth, depth_ray, dl, dg);
     const float depth_grad = (target_depth > 0.f ? dg : 0.f) * depth_lambda;
     float lgrad[3], lsum = 0.f;
+    const float pdf = a.pdf ? a.pdf[ray] : 1.f;
     for (int k = 0; k < 3; ++k) {
         float l, g;
         tl_loss(a.loss_type, tgt[k], rgb_ray[k], l, g);
         lgrad[k] = g * seg_sup;
-        lsum += l;
+        lsum += a.pdf ? __fdiv_rn(l, pdf) : l;   // lg.loss /= img_pdf * xy_pdf
     }
-    if (a.loss_out) a.loss_out[i] = (lsum / 3.f) / (float)a.n_rays;
+    const float mean_loss = lsum / 3.f;
+    if (a.loss_out) a.loss_out[i] = mean_loss / (float)a.n_rays;
+    if (a.error_map) {
+        // the ray's mean loss splatted bilinearly at its image position (texel centres at +0.5);
+        // the reference clamps the cell by the image resolution - 2, which equals the map's own
+        // bound while the map is no larger than the image
+        const float rx = (float)a.em_res[0], ry = (float)a.em_res[1];
+        const float2 xy = *reinterpret_cast<const float2*>(a.image_xy + (size_t)ray * 2);
+        const float px = fminf(fmaxf(fmaf(xy.x, rx, -0.5f), 0.f), __fsub_rn(rx, 1.0001f));
+        const float py = fminf(fmaxf(fmaf(xy.y, ry, -0.5f), 0.f), __fsub_rn(ry, 1.0001f));
+        const int ix0 = (int)px, iy0 = (int)py;
+        const float wx = __fsub_rn(px, (float)ix0), wy = __fsub_rn(py, (float)iy0);
+        const int ix = min(max(ix0, 0), (int)a.em_res[0] - 2), iy = min(max(iy0, 0), (int)a.em_res[1] - 2);
+        float* em = a.error_map + (size_t)a.image_index[ray] * a.em_res[0] * a.em_res[1];
+        const float ux = __fsub_rn(1.f, wx), uy = __fsub_rn(1.f, wy);
+        atomicAdd(em + (size_t)iy * a.em_res[0] + ix, __fmul_rn(__fmul_rn(ux, uy), mean_loss));
+        atomicAdd(em + (size_t)iy * a.em_res[0] + ix + 1, __fmul_rn(__fmul_rn(wx, uy), mean_loss));
+        atomicAdd(em + (size_t)(iy + 1) * a.em_res[0] + ix, __fmul_rn(__fmul_rn(ux, wy), mean_loss));
+        atomicAdd(em + (size_t)(iy + 1) * a.em_res[0] + ix + 1, __fmul_rn(__fmul_rn(wx, wy), mean_loss));
+    }
     const float loss_scale = a.loss_scale / (float)a.n_rays;
     const float l1_density = (a.mean_density && *a.mean_density < 0.01f) ? 1e-4f : 0.f;
     // second pass: the per-sample gradients, and the records copied to their compacted block
@@ -444,6 +469,8 @@ cudaError_t launch_train_loss(const ::insta_train_loss_desc& d, uint32_t* base_s
     a.mean_density = d.mean_density; a.seg_mask = d.seg_mask; a.rays_counter = d.rays_counter; a.ray_indices = d.ray_indices;
     a.numsteps = d.numsteps; a.coords = d.coords; a.out = d.network_output; a.counter = d.numsteps_counter;
     a.coords_out = d.coords_out; a.dloss = d.dloss_doutput; a.loss_out = d.loss_output; a.base_in = base_scratch;
+    a.pdf = d.pdf; a.error_map = d.error_map; a.em_res[0] = d.error_map_res[0]; a.em_res[1] = d.error_map_res[1];
+    a.image_xy = d.image_xy; a.image_index = d.image_index;
     if (d.max_rays > 0) {
         // one ray per thread in 32-thread blocks: a batch of a few thousand rays spreads over every SM
         train_loss_kernel<<<(d.max_rays + 31) / 32, 32, 0, s>>>(a);
@@ -457,6 +484,146 @@ cudaError_t launch_train_loss(const ::insta_train_loss_desc& d, uint32_t* base_s
         rollover_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(nc, d.stride, d.numsteps_counter, d.max_samples_compacted, d.coords_out, 0,
                                                                        d.target_batch_size);
     }
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ image / pixel draws, error map
+constexpr float kMinPdf = 0.01f;                // construct_cdf_2d / _1d
+constexpr float kMinPmf = 0.1f;                 // the image CDF of train_nerf_step
+constexpr float kUniformFraction = 0.5f;        // sample_cdf_2d's uniform share
+
+// binary_search (instant-ngp/include/neural-graphics-primitives/common.h:195-218): the first index
+// whose value is not below val, clamped to length - 1.
+__device__ __forceinline__ uint32_t cdf_search(float val, const float* __restrict__ data, uint32_t length) {
+    uint32_t first = 0, count = length;
+    while (count > 0) {
+        const uint32_t step = count / 2, it = first + step;
+        if (data[it] < val) { first = it + 1; count -= step + 1; }
+        else count = step;
+    }
+    return min(first, length - 1);
+}
+
+// image_idx, nerf_random_image_pos_training (sample_cdf_2d) and the background draw per ray.
+__global__ void __launch_bounds__(256) training_pixels_kernel(const ::insta_training_pixels_desc d) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n_rays) return;
+    const uint32_t ni = d.n_images;
+    uint32_t img;
+    float img_pdf = 1.f;
+    if (d.cdf_img) {
+        const float u = ld_random_val(i + d.n_rays_total, 0xdeadbeefu, 0u);
+        img = cdf_search(u, d.cdf_img, ni);
+        const float prev = img > 0 ? d.cdf_img[img - 1] : 0.f;
+        img_pdf = __fmul_rn(__fsub_rn(d.cdf_img[img], prev), (float)ni);
+    } else {
+        img = ((i + d.n_rays_total) * ni / d.n_rays) % ni;
+    }
+    Pcg32 rng{d.rng_state, d.rng_inc};
+    rng.advance((int64_t)i * 8);   // N_MAX_RANDOM_SAMPLES_PER_RAY
+    float sx = rng.next_float();
+    float sy = rng.next_float();
+    float xy_pdf = 1.f;
+    if (d.cdf_x_cond_y) {
+        if (sx < kUniformFraction) {
+            sx = __fdiv_rn(sx, kUniformFraction);
+        } else {
+            sx = __fdiv_rn(__fsub_rn(sx, kUniformFraction), __fsub_rn(1.f, kUniformFraction));
+            const uint32_t rx = d.cdf_res[0], ry = d.cdf_res[1];
+            const float* cy = d.cdf_y + (size_t)img * ry;
+            const uint32_t y = cdf_search(sy, cy, ry);
+            float prev = y > 0 ? cy[y - 1] : 0.f;
+            const float pmf_y = __fsub_rn(cy[y], prev);
+            sy = __fdiv_rn(__fsub_rn(sy, prev), pmf_y);
+            const float* cx = d.cdf_x_cond_y + ((size_t)img * ry + y) * rx;
+            const uint32_t x = cdf_search(sx, cx, rx);
+            prev = x > 0 ? cx[x - 1] : 0.f;
+            const float pmf_x = __fsub_rn(cx[x], prev);
+            sx = __fdiv_rn(__fsub_rn(sx, prev), pmf_x);
+            xy_pdf = __fmul_rn(__fmul_rn(pmf_x, pmf_y), (float)(rx * ry));
+            sx = __fdiv_rn(__fadd_rn((float)x, sx), (float)rx);
+            sy = __fdiv_rn(__fadd_rn((float)y, sy), (float)ry);
+        }
+    }
+    if (d.snap_to_pixel_centers) {
+        const int w = d.resolution[2 * img], h = d.resolution[2 * img + 1];
+        const int px = min(max((int)__fmul_rn(sx, (float)w), 0), w - 1), py = min(max((int)__fmul_rn(sy, (float)h), 0), h - 1);
+        sx = __fdiv_rn(__fadd_rn((float)px, 0.5f), (float)w);
+        sy = __fdiv_rn(__fadd_rn((float)py, 0.5f), (float)h);
+    }
+    d.out_image[i] = img;
+    d.out_xy[2 * i] = sx;
+    d.out_xy[2 * i + 1] = sy;
+    if (d.out_pdf) d.out_pdf[i] = __fmul_rn(img_pdf, xy_pdf);
+    if (d.out_background) {
+        const float b0 = rng.next_float(), b1 = rng.next_float(), b2 = rng.next_float();
+        d.out_background[3 * i] = b0;
+        d.out_background[3 * i + 1] = b1;
+        d.out_background[3 * i + 2] = b2;
+    }
+}
+
+// construct_cdf_2d: a thread per (row, image).  The normalisation's multiply-add is one fused
+// operation, as nvcc contracts it in the reference's kernel.
+__global__ void __launch_bounds__(256) cdf_rows_kernel(uint32_t n_images, uint32_t h, uint32_t w, const float* __restrict__ data,
+                                                      float* __restrict__ cdf_x, float* __restrict__ cdf_y) {
+    const uint32_t y = blockIdx.x * blockDim.x + threadIdx.x, img = blockIdx.y;
+    if (y >= h || img >= n_images) return;
+    const size_t off = ((size_t)img * h + y) * w;
+    float cum = 0.f;
+    for (uint32_t x = 0; x < w; ++x) {
+        cum = __fadd_rn(cum, __fadd_rn(data[off + x], 1e-10f));
+        cdf_x[off + x] = cum;
+    }
+    cdf_y[(size_t)img * h + y] = cum;
+    const float norm = __frcp_rn(cum);
+    for (uint32_t x = 0; x < w; ++x)
+        cdf_x[off + x] = fmaf(__fmul_rn(1.f - kMinPdf, cdf_x[off + x]), norm, __fdiv_rn(__fmul_rn(kMinPdf, (float)(x + 1)), (float)w));
+}
+
+// construct_cdf_1d (a thread per image), then one thread: the image CDF with its PMF.
+__global__ void __launch_bounds__(256) cdf_cols_kernel(uint32_t n_images, uint32_t h, float* __restrict__ cdf_y, float* __restrict__ cdf_img) {
+    const uint32_t img = blockIdx.x * blockDim.x + threadIdx.x;
+    if (img >= n_images) return;
+    float* cy = cdf_y + (size_t)img * h;
+    float cum = 0.f;
+    for (uint32_t y = 0; y < h; ++y) {
+        cum = __fadd_rn(cum, cy[y]);
+        cy[y] = cum;
+    }
+    cdf_img[img] = cum;
+    const float norm = __frcp_rn(cum);
+    for (uint32_t y = 0; y < h; ++y) cy[y] = fmaf(__fmul_rn(1.f - kMinPdf, cy[y]), norm, __fdiv_rn(__fmul_rn(kMinPdf, (float)(y + 1)), (float)h));
+}
+
+// The image CDF, which the reference computes on the host (separate multiply and add: the host
+// build has no fused multiply-add), here in one device thread with the same operations.
+__global__ void cdf_images_kernel(uint32_t n_images, float* __restrict__ cdf_img, float* __restrict__ pmf_img) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    float cum = 0.f;
+    for (uint32_t i = 0; i < n_images; ++i) cum = __fadd_rn(cum, cdf_img[i]);
+    const float norm = __fdiv_rn(1.f, cum);
+    float run = 0.f;
+    const float n = (float)n_images;
+    for (uint32_t i = 0; i < n_images; ++i) {
+        const float v = cdf_img[i];
+        run = __fadd_rn(run, v);
+        if (pmf_img) pmf_img[i] = __fadd_rn(__fmul_rn(__fmul_rn(1.f - kMinPmf, v), norm), __fdiv_rn(kMinPmf, n));
+        cdf_img[i] = __fadd_rn(__fmul_rn(__fmul_rn(1.f - kMinPmf, run), norm), __fdiv_rn(__fmul_rn(kMinPmf, (float)(i + 1)), n));
+    }
+}
+
+cudaError_t launch_training_pixels(const ::insta_training_pixels_desc& d, cudaStream_t s) {
+    if (d.n_rays == 0) return cudaSuccess;
+    training_pixels_kernel<<<(d.n_rays + 255) / 256, 256, 0, s>>>(d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_error_map_cdf(const float* em, uint32_t n_images, uint32_t w, uint32_t h, float* cdf_x, float* cdf_y, float* cdf_img,
+                                 float* pmf_img, cudaStream_t s) {
+    cdf_rows_kernel<<<dim3((h + 255) / 256, n_images), 256, 0, s>>>(n_images, h, w, em, cdf_x, cdf_y);
+    cdf_cols_kernel<<<(n_images + 255) / 256, 256, 0, s>>>(n_images, h, cdf_y, cdf_img);
+    cdf_images_kernel<<<1, 32, 0, s>>>(n_images, cdf_img, pmf_img);
     return cudaGetLastError();
 }
 

@@ -47,8 +47,8 @@ class TrainConfig:
     penalize_density: bool = False
     aabb_min: tuple = (0.0, 0.0, 0.0)
     aabb_max: tuple = (1.0, 1.0, 1.0)
-    tf32: bool = True                  # TF32 tensor-core layer products in the backward
-    tcgen05: bool = False              # the library's tcgen05 training kernel (FP16 operands) instead
+    tcgen05: bool = True               # the library's tcgen05 training kernel (FP16 operands, FP32 accumulation)
+    tf32: bool = True                  # without it: TF32 tensor-core (else FP32) cuBLAS layer products
     adam: dict = field(default_factory=lambda: dict(learning_rate=1.75e-3, beta1=0.9, beta2=0.99, epsilon=1e-15, l2_reg=1e-6,
                                                     ema_decay=0.95))
 

@@ -1300,8 +1300,34 @@ void orc_train_loss(const orc_train_loss_cfg *c, uint32_t n_kept, const float *r
         loss_1(c->depth_loss_type, td, depth_ray, &l_, &g_);
         const float depth_grad = (td > 0.f ? g_ : 0.f) * dl;
         float lg[3], ls = 0.f;
-        for (int k = 0; k < 3; ++k) { loss_1(c->loss_type, tgt[k], rgb_ray[k], &l_, &g_); lg[k] = g_ * seg_sup; ls += l_; }
-        if (loss_out) loss_out[i] = (ls / 3.f) / (float)c->n_rays;
+        /* lg.loss /= img_pdf * xy_pdf (testbed_nerf.cu:1494) */
+        for (int k = 0; k < 3; ++k) {
+            loss_1(c->loss_type, tgt[k], rgb_ray[k], &l_, &g_);
+            lg[k] = g_ * seg_sup;
+            ls += c->pdf ? l_ / c->pdf[ray] : l_;
+        }
+        const float mean_loss = ls / 3.f;
+        if (loss_out) loss_out[i] = mean_loss / (float)c->n_rays;
+        if (c->error_map) {
+            /* testbed_nerf.cu:1510-1536: bilinear deposit at the ray's image position (xy * res - 0.5
+             * is one fused multiply-add in the reference's nvcc build) */
+            const float rx = (float)c->error_map_res[0], ry = (float)c->error_map_res[1];
+            const float *xy = c->image_xy + (size_t)ray * 2;
+            float px = fmaf(xy[0], rx, -0.5f), py = fmaf(xy[1], ry, -0.5f);
+            px = px > 0.f ? px : 0.f; px = px < rx - 1.0001f ? px : rx - 1.0001f;
+            py = py > 0.f ? py : 0.f; py = py < ry - 1.0001f ? py : ry - 1.0001f;
+            int ix = (int)px, iy = (int)py;
+            const float wx = px - (float)ix, wy = py - (float)iy;
+            const int mxx = (int)c->error_map_res[0] - 2, mxy = (int)c->error_map_res[1] - 2;
+            ix = ix < mxx ? ix : mxx; ix = ix > 0 ? ix : 0;
+            iy = iy < mxy ? iy : mxy; iy = iy > 0 ? iy : 0;
+            float *em = c->error_map + (size_t)c->image_index[ray] * c->error_map_res[0] * c->error_map_res[1];
+            const size_t w = c->error_map_res[0];
+            em[(size_t)iy * w + ix] += (1.f - wx) * (1.f - wy) * mean_loss;
+            em[(size_t)iy * w + ix + 1] += wx * (1.f - wy) * mean_loss;
+            em[(size_t)(iy + 1) * w + ix] += (1.f - wx) * wy * mean_loss;
+            em[(size_t)(iy + 1) * w + ix + 1] += wx * wy * mean_loss;
+        }
         const float scale = c->loss_scale / (float)c->n_rays;
         const float l1d = (mean_density && *mean_density < 0.01f) ? 1e-4f : 0.f;
         float rgb2[3] = {0, 0, 0}, depth2 = 0.f;
@@ -1363,4 +1389,104 @@ void orc_transform(const float *p, const float *dir, const float *Mw, const floa
     for (int r = 0; r < 3; ++r) { float row[3] = {Mc[r * 4], Mc[r * 4 + 1], Mc[r * 4 + 2]}; cd[r] = dot3_f(row, ld); }
     normalize3_f(cd);
     memcpy(out_d, cd, 12);
+}
+
+/* ---- image / pixel draws and the error map's CDFs --------------------------------------- */
+/* binary_search (NGP/common.h:195-218) */
+static uint32_t cdf_search(float val, const float *data, uint32_t length) {
+    uint32_t first = 0, count = length;
+    while (count > 0) {
+        const uint32_t step = count / 2, it = first + step;
+        if (data[it] < val) { first = it + 1; count -= step + 1; }
+        else count = step;
+    }
+    return first < length - 1 ? first : length - 1;
+}
+
+void orc_training_pixels(uint32_t n_rays, uint32_t n_rays_total, uint32_t n_images, const int32_t *resolution, int snap,
+                         orc_pcg32 rng0, const float *cdf_x_cond_y, const float *cdf_y, const float *cdf_img, const uint32_t *cdf_res,
+                         uint32_t *out_image, float *out_xy, float *out_pdf, float *out_background) {
+    for (uint32_t i = 0; i < n_rays; ++i) {
+        uint32_t img;
+        float img_pdf = 1.f;
+        if (cdf_img) { /* image_idx with the CDF (testbed_nerf.cu:1082-1094) */
+            const float u = orc_ld_random_val(i + n_rays_total, 0xdeadbeefu, 0);
+            img = cdf_search(u, cdf_img, n_images);
+            const float prev = img > 0 ? cdf_img[img - 1] : 0.f;
+            img_pdf = (cdf_img[img] - prev) * (float)n_images;
+        } else {
+            img = ((i + n_rays_total) * n_images / n_rays) % n_images;
+        }
+        orc_pcg32 rng = rng0;
+        orc_pcg32_advance(&rng, (int64_t)i * 8);
+        float sx = orc_pcg32_next_float(&rng);
+        float sy = orc_pcg32_next_float(&rng);
+        float xy_pdf = 1.f;
+        if (cdf_x_cond_y) { /* sample_cdf_2d (testbed_nerf.cu:1013-1043) */
+            if (sx < 0.5f) {
+                sx /= 0.5f;
+            } else {
+                sx = (sx - 0.5f) / (1.0f - 0.5f);
+                const uint32_t rx = cdf_res[0], ry = cdf_res[1];
+                const float *cy = cdf_y + (size_t)img * ry;
+                const uint32_t y = cdf_search(sy, cy, ry);
+                float prev = y > 0 ? cy[y - 1] : 0.f;
+                const float pmf_y = cy[y] - prev;
+                sy = (sy - prev) / pmf_y;
+                const float *cx = cdf_x_cond_y + ((size_t)img * ry + y) * rx;
+                const uint32_t x = cdf_search(sx, cx, rx);
+                prev = x > 0 ? cx[x - 1] : 0.f;
+                const float pmf_x = cx[x] - prev;
+                sx = (sx - prev) / pmf_x;
+                xy_pdf = pmf_x * pmf_y * (float)(rx * ry);
+                sx = ((float)x + sx) / (float)rx;
+                sy = ((float)y + sy) / (float)ry;
+            }
+        }
+        if (snap) { /* nerf_random_image_pos_training's pixel-centre snap (testbed_nerf.cu:1076-1078) */
+            const int w = resolution[2 * img], h = resolution[2 * img + 1];
+            int px = (int)(sx * (float)w), py = (int)(sy * (float)h);
+            px = px > 0 ? px : 0; px = px < w - 1 ? px : w - 1;
+            py = py > 0 ? py : 0; py = py < h - 1 ? py : h - 1;
+            sx = ((float)px + 0.5f) / (float)w;
+            sy = ((float)py + 0.5f) / (float)h;
+        }
+        out_image[i] = img;
+        out_xy[2 * i] = sx;
+        out_xy[2 * i + 1] = sy;
+        if (out_pdf) out_pdf[i] = img_pdf * xy_pdf;
+        if (out_background) /* train_with_random_bg_color: random_val_3d after the position */
+            for (int k = 0; k < 3; ++k) out_background[3 * i + k] = orc_pcg32_next_float(&rng);
+    }
+}
+
+void orc_error_map_cdf(const float *em, uint32_t n_images, uint32_t w, uint32_t h, float *cdf_x, float *cdf_y, float *cdf_img,
+                       float *pmf_img) {
+    const float a = 1.0f - 0.01f, b = 1.0f - 0.1f;
+    for (uint32_t img = 0; img < n_images; ++img) {
+        for (uint32_t y = 0; y < h; ++y) { /* construct_cdf_2d */
+            const size_t off = ((size_t)img * h + y) * w;
+            float cum = 0.f;
+            for (uint32_t x = 0; x < w; ++x) { cum += em[off + x] + 1e-10f; cdf_x[off + x] = cum; }
+            cdf_y[(size_t)img * h + y] = cum;
+            const float norm = 1.0f / cum;
+            for (uint32_t x = 0; x < w; ++x) cdf_x[off + x] = fmaf(a * cdf_x[off + x], norm, 0.01f * (float)(x + 1) / (float)w);
+        }
+        float *cy = cdf_y + (size_t)img * h; /* construct_cdf_1d */
+        float cum = 0.f;
+        for (uint32_t y = 0; y < h; ++y) { cum += cy[y]; cy[y] = cum; }
+        cdf_img[img] = cum;
+        const float norm = 1.0f / cum;
+        for (uint32_t y = 0; y < h; ++y) cy[y] = fmaf(a * cy[y], norm, 0.01f * (float)(y + 1) / (float)h);
+    }
+    float cum = 0.f; /* the image CDF (host code of train_nerf_step) */
+    for (uint32_t i = 0; i < n_images; ++i) cum += cdf_img[i];
+    const float norm = 1.0f / cum;
+    float run = 0.f;
+    for (uint32_t i = 0; i < n_images; ++i) {
+        const float v = cdf_img[i];
+        run += v;
+        if (pmf_img) pmf_img[i] = b * v * norm + 0.1f / (float)n_images;
+        cdf_img[i] = b * run * norm + 0.1f * (float)(i + 1) / (float)n_images;
+    }
 }

@@ -142,7 +142,22 @@ typedef struct {
     float aabb_min[3], aabb_max[3];
     int loss_type, depth_loss_type, srgb_targets, train_in_linear_colors, penalize_density;
     float loss_scale, depth_supervision_lambda, seg_mask_supervision_lambda, near_distance, beta;
+    /* importance-sampling pdf and the error map (per original ray; NULL = off) */
+    const float *pdf;
+    float *error_map;
+    uint32_t error_map_res[2];
+    const float *image_xy;
+    const uint32_t *image_index;
 } orc_train_loss_cfg;
+/* image_idx + nerf_random_image_pos_training + the background draw (testbed_nerf.cu:1013-1105,
+ * 1140-1144, 1406-1420) for rays [0, n_rays). */
+void orc_training_pixels(uint32_t n_rays, uint32_t n_rays_total, uint32_t n_images, const int32_t *resolution, int snap,
+                         orc_pcg32 rng, const float *cdf_x_cond_y, const float *cdf_y, const float *cdf_img, const uint32_t *cdf_res,
+                         uint32_t *out_image, float *out_xy, float *out_pdf, float *out_background);
+/* construct_cdf_2d, construct_cdf_1d and the image CDF of train_nerf_step (testbed_nerf.cu:1967-2020,
+ * 3024-3041). */
+void orc_error_map_cdf(const float *error_map, uint32_t n_images, uint32_t res_x, uint32_t res_y, float *cdf_x_cond_y,
+                       float *cdf_y, float *cdf_img, float *pmf_img);
 void orc_train_loss(const orc_train_loss_cfg *c, uint32_t n_kept, const float *rays, const float *target, const float *background,
                     const float *exposure, const float *depth_img, const int32_t *seg_mask, const float *mean_density,
                     const uint32_t *ray_indices, uint32_t *numsteps, const float *coords, const float *nout, uint32_t *counter,

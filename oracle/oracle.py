@@ -233,19 +233,33 @@ class TrainLossCfg(C.Structure):
                 ("stride", C.c_uint32), ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3), ("loss_type", C.c_int),
                 ("depth_loss_type", C.c_int), ("srgb_targets", C.c_int), ("train_in_linear_colors", C.c_int),
                 ("penalize_density", C.c_int), ("loss_scale", C.c_float), ("depth_supervision_lambda", C.c_float),
-                ("seg_mask_supervision_lambda", C.c_float), ("near_distance", C.c_float), ("beta", C.c_float)]
+                ("seg_mask_supervision_lambda", C.c_float), ("near_distance", C.c_float), ("beta", C.c_float),
+                ("pdf", C.c_void_p), ("error_map", C.c_void_p), ("error_map_res", C.c_uint32 * 2), ("image_xy", C.c_void_p),
+                ("image_index", C.c_void_p)]
 
 
 def train_loss(cfg: dict, rays, target, ray_indices, numsteps, coords, network_output, background=None, exposure=None,
-               depth=None, seg_mask=None, mean_density=None):
+               depth=None, seg_mask=None, mean_density=None, pdf=None, error_map=None, image_xy=None, image_index=None):
     """compute_loss_kernel_train_nerf + fill_rollover over the kept rays in order.  cfg keys are
-    TrainLossCfg's fields.  Returns (numsteps out, compacted counter, coords_out, dloss, loss)."""
+    TrainLossCfg's fields.  Returns (numsteps out, compacted counter, coords_out, dloss, loss); with
+    error_map (f32[n_images][res_y][res_x], added to in place) the kept rays' mean losses are
+    deposited into it."""
     c = TrainLossCfg()
     for k, v in cfg.items():
         if k in ("aabb_min", "aabb_max"):
             getattr(c, k)[:] = [float(x) for x in v]
         else:
             setattr(c, k, v)
+    keep = []
+    if pdf is not None:
+        keep.append(np.ascontiguousarray(pdf, np.float32))
+        c.pdf = keep[-1].ctypes.data
+    if error_map is not None:
+        assert error_map.dtype == np.float32 and error_map.flags.c_contiguous and error_map.ndim == 3
+        c.error_map = error_map.ctypes.data
+        c.error_map_res[0], c.error_map_res[1] = error_map.shape[2], error_map.shape[1]
+        keep += [np.ascontiguousarray(image_xy, np.float32), np.ascontiguousarray(image_index, np.uint32)]
+        c.image_xy, c.image_index = keep[-2].ctypes.data, keep[-1].ctypes.data
     f32 = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)
     rays, target, coords, network_output = f32(rays), f32(target), f32(coords), f32(network_output)
     background, exposure, depth = f32(background), f32(exposure), f32(depth)
@@ -262,6 +276,37 @@ def train_loss(cfg: dict, rays, target, ray_indices, numsteps, coords, network_o
     lib().orc_train_loss(C.byref(c), C.c_uint32(len(idx)), ptr(rays), ptr(target), p(background), p(exposure), p(depth), p(seg), p(md),
                          ptr(idx), ptr(ns), ptr(coords), ptr(network_output), ptr(counter), ptr(coords_out), ptr(dloss), ptr(loss))
     return ns, int(counter[0]), coords_out, dloss, loss
+
+
+def training_pixels(n_rays, n_rays_total, n_images, rng, resolution=None, snap=False, cdfs=None, cdf_res=(0, 0)):
+    """image_idx + nerf_random_image_pos_training + the background draw per ray: (image u32[n],
+    xy f32[n][2], pdf f32[n], background f32[n][3]).  cdfs = (cdf_x_cond_y, cdf_y, cdf_img) or None."""
+    img = np.zeros(n_rays, np.uint32)
+    xy = np.zeros((n_rays, 2), np.float32)
+    pdf = np.zeros(n_rays, np.float32)
+    bg = np.zeros((n_rays, 3), np.float32)
+    res = None if resolution is None else np.ascontiguousarray(resolution, np.int32)
+    cx = cy = ci = None
+    if cdfs is not None:
+        cx, cy, ci = (np.ascontiguousarray(a, np.float32) for a in cdfs)
+    cr = np.array(cdf_res, np.uint32)
+    p = lambda a: None if a is None else ptr(a)
+    lib().orc_training_pixels(C.c_uint32(n_rays), C.c_uint32(n_rays_total), C.c_uint32(n_images), p(res), C.c_int(int(snap)), rng,
+                              p(cx), p(cy), p(ci), ptr(cr), ptr(img), ptr(xy), ptr(pdf), ptr(bg))
+    return img, xy, pdf, bg
+
+
+def error_map_cdf(error_map):
+    """construct_cdf_2d / _1d and the image CDF of an error map f32[n_images][res_y][res_x]:
+    (cdf_x_cond_y, cdf_y, cdf_img, pmf_img)."""
+    em = np.ascontiguousarray(error_map, np.float32)
+    n, h, w = em.shape
+    cx = np.zeros_like(em)
+    cy = np.zeros((n, h), np.float32)
+    ci = np.zeros(n, np.float32)
+    pm = np.zeros(n, np.float32)
+    lib().orc_error_map_cdf(ptr(em), C.c_uint32(n), C.c_uint32(w), C.c_uint32(h), ptr(cx), ptr(cy), ptr(ci), ptr(pm))
+    return cx, cy, ci, pm
 
 
 def occupancy(tris, radius=0.015) -> np.ndarray:

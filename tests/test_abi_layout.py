@@ -19,6 +19,7 @@ STRUCTS = {
     "insta_train_loss_desc": "TrainLossDesc",
     "insta_server_config": "ServerConfig",
     "insta_tuning": "Tuning",
+    "insta_training_pixels_desc": "TrainingPixelsDesc",
 }
 
 

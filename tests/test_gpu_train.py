@@ -294,8 +294,9 @@ def test_argument_errors(ctx, field):
         ctx.adam_step(55, g)
 
 
-def run_loss(ctx, b, cfg, mean_density=None, extra=None):
-    """insta_train_loss on device copies of a synthetic batch; returns host arrays."""
+def run_loss(ctx, b, cfg, mean_density=None, extra=None, **more):
+    """insta_train_loss on device copies of a synthetic batch; returns host arrays.  `more` goes
+    to the description as given (device tensors, error_map_res)."""
     n = len(b["ray_indices"])
     cap = cfg["max_samples_compacted"]
     as_dev = lambda v: dev(v.view(np.int32) if v.dtype == np.uint32 else v)   # torch has no general uint32
@@ -312,6 +313,7 @@ def run_loss(ctx, b, cfg, mean_density=None, extra=None):
     kw.update(d)
     kw.update(numsteps=ns, numsteps_counter=counter, rays_counter=rays_counter, coords_out=cout, dloss_doutput=dloss,
               loss_output=loss, mean_density=md, max_rays=n)
+    kw.update(more)
     torch.cuda.synchronize()                             # buffers filled on torch's stream
     ctx.train_loss(**kw)
     ctx.sync()
@@ -391,6 +393,69 @@ def test_train_loss_cap_and_rollover(ctx, oracle):
     src = np.arange(t2, tgt) % t2
     np.testing.assert_array_equal(cout2[t2:tgt], cout2[src])
     np.testing.assert_allclose(dloss2[t2:tgt], dloss2[src] * np.float32(t2 / tgt), rtol=1e-6, atol=0)
+
+
+def test_train_loss_error_map_and_pdf(ctx, oracle):
+    """The error map of compute_loss_kernel_train_nerf: each kept ray's mean loss (divided by its
+    importance-sampling pdf) splatted bilinearly at its image position, rays at the corners of
+    the image included.  Deposits are atomic additions in any order: the map agrees with the
+    oracle's to 1e-5 of its largest cell; blocks, gradients and losses as in the other tests."""
+    from conftest import loss_cfg, train_loss_batch
+    n, n_img, rx, ry = 2500, 3, 37, 23
+    b = train_loss_batch(n, seed=21, stride=27)
+    rng = np.random.default_rng(22)
+    xy = rng.uniform(0, 1, (n, 2)).astype(np.float32)
+    xy[:5] = [[0, 0], [1, 1], [0, 1], [1, 0], [0.5, 0.5]]
+    img = rng.integers(0, n_img, n).astype(np.uint32)
+    pdf = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    cfg = loss_cfg(n_rays=n, stride=27, loss_type=4, loss_scale=128.0)
+    em_dev = torch.zeros((n_img, ry, rx), dtype=torch.float32, device="cuda")
+    got = run_loss(ctx, b, cfg, extra=dict(image_xy=xy, image_index=img, pdf=pdf), error_map=em_dev, error_map_res=(rx, ry))
+    em_ref = np.zeros((n_img, ry, rx), np.float32)
+    ref = oracle.train_loss(cfg, **b, pdf=pdf, error_map=em_ref, image_xy=xy, image_index=img)
+    check_blocks(got, ref, n)
+    em = em_dev.cpu().numpy()
+    assert np.abs(em - em_ref).max() <= 1e-5 * np.abs(em_ref).max()
+    assert ((em != 0) == (em_ref != 0)).all()
+
+
+@pytest.mark.parametrize("mode", ["uniform", "cdf", "cdf_snap"])
+def test_training_pixels_and_cdf_match_oracle(ctx, oracle, mode):
+    """insta_error_map_cdf and insta_training_pixels against the oracle bit for bit: the CDFs,
+    then per ray the image (evenly spread or from cdf_img with the low-discrepancy draw), the
+    position (pcg32 sub-stream, sample_cdf_2d, pixel-centre snap), the pdf and the background
+    draw."""
+    n, n_img, total, w, h = 5000, 7, 12345, 37, 23
+    res = np.array([[640, 480], [512, 512], [37, 23], [1, 1], [1024, 768], [3, 2], [256, 256]], np.int32)
+    rng = oracle.Pcg32.seeded(1337, 11)
+    cdfs = None
+    if mode != "uniform":
+        em = np.random.default_rng(4).gamma(0.5, 1.0, (n_img, h, w)).astype(np.float32)
+        em[3] = 0.0
+        rcx, rcy, rci, rpm = oracle.error_map_cdf(em)
+        cx = torch.zeros((n_img, h, w), dtype=torch.float32, device="cuda")
+        cy = torch.zeros((n_img, h), dtype=torch.float32, device="cuda")
+        ci = torch.zeros(n_img, dtype=torch.float32, device="cuda")
+        pm = torch.zeros(n_img, dtype=torch.float32, device="cuda")
+        ctx.error_map_cdf(dev(em), n_img, w, h, cx, cy, ci, pm)
+        ctx.sync()
+        for g, r in ((cx, rcx), (cy, rcy), (ci, rci), (pm, rpm)):
+            np.testing.assert_array_equal(g.cpu().numpy(), r)
+        cdfs = (cx, cy, ci)
+    snap = mode == "cdf_snap"
+    out_img = torch.zeros(n, dtype=torch.int32, device="cuda")
+    out_xy = torch.zeros((n, 2), dtype=torch.float32, device="cuda")
+    out_pdf = torch.zeros(n, dtype=torch.float32, device="cuda")
+    out_bg = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+    ctx.training_pixels(n, n_img, rng.state, rng.inc, out_img, out_xy, out_pdf, out_bg, n_rays_total=total, resolution=dev(res),
+                        snap=snap, cdfs=cdfs, cdf_res=(w, h))
+    ctx.sync()
+    ri, rxy, rpdf, rbg = oracle.training_pixels(n, total, n_img, rng, resolution=res, snap=snap,
+                                                cdfs=None if cdfs is None else (rcx, rcy, rci), cdf_res=(w, h))
+    np.testing.assert_array_equal(out_img.cpu().numpy().view(np.uint32), ri)
+    np.testing.assert_array_equal(out_xy.cpu().numpy(), rxy)
+    np.testing.assert_array_equal(out_pdf.cpu().numpy(), rpdf)
+    np.testing.assert_array_equal(out_bg.cpu().numpy(), rbg)
 
 
 def test_train_step_fits_a_constant_colour(ctx, avatar, frame0):
