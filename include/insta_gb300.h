@@ -275,12 +275,36 @@ int insta_field_eval_static(insta_ctx* ctx, int avatar, const float* coords, uin
  * for n NerfCoordinate records (canonical position, direction, expression dims; device
  * pointers) and the loss gradient w.r.t. each record's outputs dl_dout f32[n][4] (raw r, g, b,
  * raw density), ADD the gradient of every parameter to grad f32[n_params] (snapshot order:
- * density MLP, colour MLP, hash table; 8-byte aligned).  FP32 arithmetic on the FP32 master
- * weights (the FP16 parameters widened at the first call after insta_params_load).
+ * density MLP, colour MLP, hash table; 8-byte aligned).  On the FP32 master weights (the FP16
+ * parameters widened at the first call after insta_params_load); the layer products in the
+ * arithmetic insta_train_set_math selects (FP32 by default).
  * out4 (optional) gets the outputs of that FP32 forward; with dl_dout = grad = NULL only the
  * forward runs.  n < 2^24. */
 int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, const float* dl_dout, float* grad,
                          float* out4);
+/* insta_field_backward that also writes the gradient w.r.t. each record's expression dims,
+ * dl_dextra f32[n][n_extra_dims] (NULL = none): the extra-dims part of the input gradient
+ * NerfNetwork's backward returns when train_nerf_step prepares input gradients
+ * (instant-ngp/src/testbed_nerf.cu:3364-3380).  Needs dl_dout and grad. */
+int insta_field_backward_ex(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, const float* dl_dout,
+                            float* grad, float* out4, float* dl_dextra);
+
+/* compute_extra_dims_gradient_train_nerf (instant-ngp/src/testbed_nerf.cu:1756-1791): every kept
+ * ray's compacted samples' expression-dim gradients summed into its training image's row of
+ * extra_dims_gradient.  Each ray's samples are summed first, then added to the image's row
+ * (the reference adds sample by sample; the sums differ by rounding only). */
+typedef struct insta_extra_dims_gradient_desc {
+    uint32_t max_rays;                /* size of the ray arrays                                     */
+    uint32_t n_extra_dims;
+    uint32_t n_images;
+    const uint32_t* rays_counter;     /* rays kept (counters[0])                                    */
+    const uint32_t* ray_indices;
+    const uint32_t* numsteps;         /* [max_rays][2] compacted (count, base) as insta_train_loss leaves them */
+    const uint32_t* image_index;      /* per original ray                                           */
+    const float* dl_dextra;           /* f32[compacted samples][n_extra_dims] (insta_field_backward_ex) */
+    float* extra_dims_gradient;       /* f32[n_images][n_extra_dims], added to                      */
+} insta_extra_dims_gradient_desc;
+int insta_extra_dims_gradient(insta_ctx* ctx, const insta_extra_dims_gradient_desc* desc);
 /* Arithmetic of the backward's layer products: FP32 (default) or TF32 tensor-core GEMMs (inputs
  * rounded to TF32, FP32 accumulation; still finer than the reference's FP16 training arithmetic). */
 #define INSTA_TRAIN_MATH_FP32 0

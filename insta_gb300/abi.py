@@ -26,7 +26,7 @@ EXPORTS = [
     "insta_frame_release", "insta_occupancy_from_mesh", "insta_occupancy_set", "insta_occupancy_get",
     "insta_density_grid_load", "insta_density_grid_reset", "insta_density_grid_update", "insta_density_grid_read",
     "insta_canonical_map", "insta_canonical_map_soa", "insta_training_samples", "insta_field_param_count", "insta_params_load",
-    "insta_field_eval", "insta_field_eval_training", "insta_field_eval_static", "insta_field_backward", "insta_adam_step", "insta_train_loss", "insta_training_pixels", "insta_error_map_cdf", "insta_train_set_math", "insta_render", "insta_render_async", "insta_render_batch",
+    "insta_field_eval", "insta_field_eval_training", "insta_field_eval_static", "insta_field_backward", "insta_field_backward_ex", "insta_extra_dims_gradient", "insta_adam_step", "insta_train_loss", "insta_training_pixels", "insta_error_map_cdf", "insta_train_set_math", "insta_render", "insta_render_async", "insta_render_batch",
     "insta_render_samples", "insta_tuning_set", "insta_tuning_get", "insta_autotune", "insta_march_debug", "insta_nearest_debug",
     "insta_raycast",
     "insta_server_create", "insta_server_destroy", "insta_submit", "insta_poll", "insta_wait", "insta_cancel",
@@ -73,6 +73,12 @@ class TrainLossDesc(C.Structure):
                 ("numsteps_counter", C.c_void_p), ("coords_out", C.c_void_p), ("dloss_doutput", C.c_void_p),
                 ("loss_output", C.c_void_p), ("pdf", C.c_void_p), ("error_map", C.c_void_p), ("error_map_res", C.c_uint32 * 2),
                 ("image_xy", C.c_void_p), ("image_index", C.c_void_p)]
+
+
+class ExtraDimsGradientDesc(C.Structure):
+    _fields_ = [("max_rays", C.c_uint32), ("n_extra_dims", C.c_uint32), ("n_images", C.c_uint32), ("rays_counter", C.c_void_p),
+                ("ray_indices", C.c_void_p), ("numsteps", C.c_void_p), ("image_index", C.c_void_p), ("dl_dextra", C.c_void_p),
+                ("extra_dims_gradient", C.c_void_p)]
 
 
 class TrainingPixelsDesc(C.Structure):
@@ -163,6 +169,8 @@ def load(path: Path | None = None):
             "insta_field_eval_static": [vp, C.c_int, vp, u32, i64, vp],
             "insta_field_eval_training": [vp, C.c_int, vp, u32, i64, vp],
             "insta_field_backward": [vp, C.c_int, vp, u32, i64, vp, vp, vp],
+            "insta_field_backward_ex": [vp, C.c_int, vp, u32, i64, vp, vp, vp, vp],
+            "insta_extra_dims_gradient": [vp, C.POINTER(ExtraDimsGradientDesc)],
             "insta_adam_step": [vp, C.c_int, vp, C.POINTER(AdamConfig)],
             "insta_train_loss": [vp, C.POINTER(TrainLossDesc)],
             "insta_training_pixels": [vp, C.POINTER(TrainingPixelsDesc)],
@@ -372,9 +380,15 @@ class Context:
         """insta_field_eval without device allocations (n <= 16384, shared fixed scratch)."""
         self._check(self.lib.insta_field_eval_static(self.h, avatar, _addr(coords), stride, n, _addr(out4)))
 
-    def field_backward(self, avatar, coords, stride, n, dl_dout=None, grad=None, out4=None):
-        """insta_field_backward: ADDS d(sum dl_dout . out)/d(params) into grad (f32, snapshot order)."""
-        self._check(self.lib.insta_field_backward(self.h, avatar, _addr(coords), stride, n, _addr(dl_dout), _addr(grad), _addr(out4)))
+    def field_backward(self, avatar, coords, stride, n, dl_dout=None, grad=None, out4=None, dl_dextra=None):
+        """insta_field_backward: ADDS d(sum dl_dout . out)/d(params) into grad (f32, snapshot order);
+        with dl_dextra (f32[n][n_extra]) insta_field_backward_ex also writes the expression-dim
+        gradients."""
+        if dl_dextra is None:
+            self._check(self.lib.insta_field_backward(self.h, avatar, _addr(coords), stride, n, _addr(dl_dout), _addr(grad), _addr(out4)))
+        else:
+            self._check(self.lib.insta_field_backward_ex(self.h, avatar, _addr(coords), stride, n, _addr(dl_dout), _addr(grad), _addr(out4),
+                                                         _addr(dl_dextra)))
 
     def train_set_math(self, tf32, tcgen05=False):
         """insta_train_set_math: TF32 tensor-core layer products in the backward (else FP32), or with
@@ -428,6 +442,17 @@ class Context:
         d.out_pdf = None if out_pdf is None else _addr(out_pdf).value
         d.out_background = None if out_background is None else _addr(out_background).value
         self._check(self.lib.insta_training_pixels(self.h, C.byref(d)))
+
+    def extra_dims_gradient(self, max_rays, n_extra_dims, n_images, rays_counter, ray_indices, numsteps, image_index, dl_dextra,
+                            extra_dims_gradient):
+        """insta_extra_dims_gradient on device buffers (per kept ray its samples' expression-dim
+        gradients summed into its image's row, added to)."""
+        d = ExtraDimsGradientDesc()
+        d.max_rays, d.n_extra_dims, d.n_images = max_rays, n_extra_dims, n_images
+        for k, v in (("rays_counter", rays_counter), ("ray_indices", ray_indices), ("numsteps", numsteps), ("image_index", image_index),
+                     ("dl_dextra", dl_dextra), ("extra_dims_gradient", extra_dims_gradient)):
+            setattr(d, k, _addr(v).value)
+        self._check(self.lib.insta_extra_dims_gradient(self.h, C.byref(d)))
 
     def error_map_cdf(self, error_map, n_images, res_x, res_y, cdf_x_cond_y, cdf_y, cdf_img, pmf_img=None):
         """insta_error_map_cdf on device buffers."""

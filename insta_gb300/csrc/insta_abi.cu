@@ -1660,6 +1660,11 @@ void ensure_master(insta_ctx* ctx, Field& fd) {
 
 int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, const float* dl_dout, float* grad,
                          float* out4) {
+    return insta_field_backward_ex(ctx, avatar, coords, stride, n, dl_dout, grad, out4, nullptr);
+}
+
+int insta_field_backward_ex(insta_ctx* ctx, int avatar, const float* coords, uint32_t stride, int64_t n, const float* dl_dout,
+                            float* grad, float* out4, float* dl_dextra) {
     return guarded(ctx, [&] {
         Avatar& a = ctx->avatar(avatar);
         Field& fd = a.field;
@@ -1669,7 +1674,9 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
         if ((dl_dout == nullptr) != (grad == nullptr)) fail(INSTA_ERR_INVALID_ARG, "output gradients and parameter gradients go together");
         if (stride < 11 + fd.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
         if ((uintptr_t)grad & 7) fail(INSTA_ERR_INVALID_ARG, "grad must be 8-byte aligned");   // paired table atomics
+        if (dl_dextra && !(dl_dout && grad)) fail(INSTA_ERR_INVALID_ARG, "dl_dextra needs the backward (dl_dout and grad)");
         if (n == 0) return;
+        const int extra_k = (dl_dextra && fd.desc.n_extra_dims) ? 1 : 0;
         if (ctx->train_tc) {
             ensure_master(ctx, fd);
             const TrainShape t = train_shape(fd);
@@ -1679,9 +1686,9 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
                 fail(INSTA_ERR_UNSUPPORTED, "the field's MLPs do not fit the tcgen05 training kernel; use INSTA_TRAIN_MATH_TF32");
             ctx->alloc(ctx->train_images, plan.img_bytes);
             ctx->alloc(ctx->train_scratch, ((size_t)2 * t.kd + 32) * (size_t)n * 4);
-            Stage st(ctx, INSTA_STAGE_TRAIN, (dl_dout && grad) ? 4 : 3);
+            Stage st(ctx, INSTA_STAGE_TRAIN, ((dl_dout && grad) ? 4 : 3) + extra_k);
             CK(launch_field_train_tc(fd.view, t, plan, images, (uint8_t*)ctx->train_images.p, (const float*)fd.w32.p, coords, stride,
-                                     (uint32_t)n, dl_dout, out4, grad, (float*)ctx->train_scratch.p, ctx->err_dev, ctx->stream));
+                                     (uint32_t)n, dl_dout, out4, grad, (float*)ctx->train_scratch.p, ctx->err_dev, ctx->stream, dl_dextra));
             return;
         }
         if (!ctx->blas) {
@@ -1692,9 +1699,9 @@ int insta_field_backward(insta_ctx* ctx, int avatar, const float* coords, uint32
         ensure_master(ctx, fd);
         const TrainShape t = train_shape(fd);
         ctx->alloc(ctx->train_scratch, train_scratch_floats(t, (uint32_t)n) * 4);
-        Stage st(ctx, INSTA_STAGE_TRAIN, 8 + 2 * (t.n_density + t.n_rgb));
+        Stage st(ctx, INSTA_STAGE_TRAIN, 8 + 2 * (t.n_density + t.n_rgb) + extra_k);
         CK(launch_field_train(ctx->blas, fd.view, t, (const float*)fd.w32.p, coords, stride, (uint32_t)n, dl_dout, out4, grad,
-                              (float*)ctx->train_scratch.p, ctx->stream));
+                              (float*)ctx->train_scratch.p, ctx->stream, dl_dextra));
     });
 }
 
@@ -1813,6 +1820,18 @@ int insta_training_pixels(insta_ctx* ctx, const insta_training_pixels_desc* d) {
         if (cdf && (d->cdf_res[0] == 0 || d->cdf_res[1] == 0)) fail(INSTA_ERR_INVALID_ARG, "cdf_res must be positive");
         Stage st(ctx, INSTA_STAGE_TRAIN, 1);
         CK(launch_training_pixels(*d, ctx->stream));
+    });
+}
+
+int insta_extra_dims_gradient(insta_ctx* ctx, const insta_extra_dims_gradient_desc* d) {
+    return guarded(ctx, [&] {
+        if (!d) fail(INSTA_ERR_INVALID_ARG, "null description");
+        if (d->max_rays == 0 || d->n_extra_dims == 0) return;
+        if (d->n_extra_dims > 256 || d->max_rays >= (1u << 26)) fail(INSTA_ERR_INVALID_ARG, "sizes out of range");
+        if (!d->rays_counter || !d->ray_indices || !d->numsteps || !d->image_index || !d->dl_dextra || !d->extra_dims_gradient)
+            fail(INSTA_ERR_INVALID_ARG, "null buffers");
+        Stage st(ctx, INSTA_STAGE_TRAIN, 1);
+        CK(launch_extra_dims_gradient(*d, ctx->stream));
     });
 }
 

@@ -8,6 +8,7 @@
 
 struct insta_train_loss_desc;   // include/insta_gb300.h
 struct insta_training_pixels_desc;
+struct insta_extra_dims_gradient_desc;
 
 namespace insta {
 
@@ -254,10 +255,12 @@ cudaError_t launch_train_mlp(const TrainMlpArgs& a, const TrainImageList& images
 // products, then the hash-table backward; scratch (2 kd + 32) n floats.
 cudaError_t launch_field_train_tc(const FieldView& fv, const TrainShape& t, const TrainMlpPlan& plan, const TrainImageList& images,
                                   uint8_t* img_dev, const float* w32, const float* coords, uint32_t stride, uint32_t n,
-                                  const float* dl_dout, float* out4, float* grad, float* scratch, uint32_t* err, cudaStream_t s);
+                                  const float* dl_dout, float* out4, float* grad, float* scratch, uint32_t* err, cudaStream_t s,
+                                  float* dl_dextra = nullptr);
 cudaError_t launch_field_train(struct cublasContext* h, const FieldView& fv, const TrainShape& t, const float* w32, const float* coords,
                                uint32_t stride, uint32_t n, const float* dl_dout, float* out4, float* grad, float* scratch,
-                               cudaStream_t s);
+                               cudaStream_t s, float* dl_dextra = nullptr);
+cudaError_t launch_extra_dims_gradient(const ::insta_extra_dims_gradient_desc& d, cudaStream_t s);
 cudaError_t launch_adam(size_t n, size_t n_matrix, float* w, float* m, float* v, uint32_t* table_steps, const float* g, float loss_scale,
                         float lr, float b1, float b2, float eps, float l2, uint32_t step, float* ema, float decay, uint32_t ema_step,
                         __half* w16, __half* w16_train, cudaStream_t s);

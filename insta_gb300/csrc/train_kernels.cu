@@ -656,9 +656,48 @@ static cublasStatus_t wgrad(cublasHandle_t h, const float* X, uint32_t ldx, uint
     return cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_T, (int)n_in, (int)n_out, (int)n, &one, X, (int)ldx, dY, (int)lddy, &one, dW, (int)n_in);
 }
 
+// The expression-dim columns of the density MLP's input gradient (after the 2 n_levels hash
+// features), per sample.
+__global__ void __launch_bounds__(256) extra_grad_kernel(uint32_t n, const float* __restrict__ dxd, uint32_t kd, uint32_t first,
+                                                         uint32_t n_extra, float* __restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)n * n_extra) return;
+    const size_t s = i / n_extra, k = i % n_extra;
+    out[i] = dxd[s * kd + first + k];
+}
+
+static cudaError_t launch_extra_grad(const FieldView& fv, const TrainShape& t, uint32_t n, const float* dxd, float* out, cudaStream_t s) {
+    const uint32_t ne = fv.n_extra;
+    if (!out || ne == 0) return cudaSuccess;
+    extra_grad_kernel<<<(unsigned)(((size_t)n * ne + 255) / 256), 256, 0, s>>>(n, dxd, t.kd, 2u * fv.n_levels, ne, out);
+    return cudaGetLastError();
+}
+
+// compute_extra_dims_gradient_train_nerf: a thread per (kept ray, dim) sums the ray's samples,
+// then one addition into the ray's image row.
+__global__ void __launch_bounds__(256) extra_dims_gradient_kernel(const ::insta_extra_dims_gradient_desc d) {
+    const uint32_t ne = d.n_extra_dims;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = (uint32_t)(t / ne), k = (uint32_t)(t % ne);
+    if (i >= min(*d.rays_counter, d.max_rays)) return;
+    const uint32_t count = d.numsteps[2 * i], base = d.numsteps[2 * i + 1];
+    if (count == 0) return;
+    const float* g = d.dl_dextra + (size_t)base * ne + k;
+    float sum = 0.f;
+    for (uint32_t j = 0; j < count; ++j) sum += g[(size_t)j * ne];
+    atomicAdd(d.extra_dims_gradient + (size_t)d.image_index[d.ray_indices[i]] * ne + k, sum);
+}
+
+cudaError_t launch_extra_dims_gradient(const ::insta_extra_dims_gradient_desc& d, cudaStream_t s) {
+    const size_t threads = (size_t)d.max_rays * d.n_extra_dims;
+    if (threads == 0) return cudaSuccess;
+    extra_dims_gradient_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(d);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_field_train(cublasHandle_t h, const FieldView& fv, const TrainShape& t, const float* w32, const float* coords,
                                uint32_t stride, uint32_t n, const float* dl_dout, float* out4, float* grad, float* scratch,
-                               cudaStream_t s) {
+                               cudaStream_t s, float* dl_dextra) {
     if (n == 0) return cudaSuccess;
     if (cublasSetStream(h, s) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
     // activations: X_d [kd x n], H_d[l] [64 x n], X_r [32 x n] (rows 0..15 = density output), H_r[l] [64 x n], Y_r [16 x n]
@@ -734,12 +773,14 @@ cudaError_t launch_field_train(cublasHandle_t h, const FieldView& fv, const Trai
         dout = dx; lddout = k; n_out = k;
     }
     hash_backward_kernel<<<(n + 255) / 256, 256, 0, s>>>(fv, coords, stride, n, dxd, t.kd, grad + t.table_off);
-    return okb ? cudaGetLastError() : cudaErrorUnknown;
+    if (!okb) return cudaErrorUnknown;
+    return launch_extra_grad(fv, t, n, dxd, dl_dextra, s);
 }
 
 cudaError_t launch_field_train_tc(const FieldView& fv, const TrainShape& t, const TrainMlpPlan& plan, const TrainImageList& images,
                                   uint8_t* img_dev, const float* w32, const float* coords, uint32_t stride, uint32_t n,
-                                  const float* dl_dout, float* out4, float* grad, float* scratch, uint32_t* err, cudaStream_t s) {
+                                  const float* dl_dout, float* out4, float* grad, float* scratch, uint32_t* err, cudaStream_t s,
+                                  float* dl_dextra) {
     if (n == 0) return cudaSuccess;
     float* xd = scratch;
     float* xr = xd + (size_t)t.kd * n;
@@ -761,7 +802,7 @@ cudaError_t launch_field_train_tc(const FieldView& fv, const TrainShape& t, cons
     cudaError_t e = launch_train_mlp(a, images, w32, img_dev, s);
     if (e != cudaSuccess || !bwd) return e;
     hash_backward_kernel<<<(n + 255) / 256, 256, 0, s>>>(fv, coords, stride, n, dxd, t.kd, grad + t.table_off);
-    return cudaGetLastError();
+    return launch_extra_grad(fv, t, n, dxd, dl_dextra, s);
 }
 
 cudaError_t launch_adam(size_t n, size_t n_matrix, float* w, float* m, float* v, uint32_t* table_steps, const float* g, float loss_scale,

@@ -1105,6 +1105,11 @@ static void layer_bwd_d(const uint16_t *W, const double *x, int n_in, int n_out,
 
 void orc_field_backward(const orc_field_cfg *c, const uint16_t *params, const float *coords, uint32_t stride, int64_t n,
                         const float *dl_dout, double *grad, float *out4) {
+    orc_field_backward_ex(c, params, coords, stride, n, dl_dout, grad, out4, NULL);
+}
+
+void orc_field_backward_ex(const orc_field_cfg *c, const uint16_t *params, const float *coords, uint32_t stride, int64_t n,
+                           const float *dl_dout, double *grad, float *out4, double *dl_dextra) {
     uint64_t lvl_off[64], mlp_off[3];
     uint32_t lvl_res[64], lvl_size[64];
     orc_field_layout(c, lvl_off, lvl_res, lvl_size, mlp_off);
@@ -1210,6 +1215,9 @@ void orc_field_backward(const orc_field_cfg *c, const uint16_t *params, const fl
             else for (uint32_t i = 0; i < kk; ++i) dy[i] = dx[i];
             n_out = kk;
         }
+        /* dy = dL/d density input: the hash features, then the expression dims */
+        if (dl_dextra)
+            for (uint32_t k = 0; k < c->n_extra; ++k) dl_dextra[(size_t)s * c->n_extra + k] = dy[n_enc + k];
         /* hash table */
         double *gt = grad + mlp_off[2];
         for (uint32_t l = 0; l < c->n_levels; ++l)
@@ -1219,8 +1227,8 @@ void orc_field_backward(const orc_field_cfg *c, const uint16_t *params, const fl
 }
 
 /* compute_loss_kernel_train_nerf (instant-ngp/src/testbed_nerf.cu:1305-1644) for rays in order
- * 0..n_kept-1, logistic rgb / exponential density, no error map, envmap, exposure gradient or
- * importance sampling (pdfs 1); then tiny-cuda-nn's fill_rollover(_and_rescale) restated from
+ * 0..n_kept-1, logistic rgb / exponential density, with the optional importance-sampling pdf and
+ * error map (no envmap, sharpness grid or exposure gradient); then tiny-cuda-nn's fill_rollover(_and_rescale) restated from
  * its published source (train_nerf_step, :3349-3357): entries past the compacted count repeat the
  * compacted ones, the repeated gradients scaled by count / target.  Loss functions :116-180,
  * :1288-1303.  Single-threaded; the compacted bases follow ray order. */

@@ -164,6 +164,9 @@ void orc_train_loss(const orc_train_loss_cfg *c, uint32_t n_kept, const float *r
                     float *coords_out, float *dloss, float *loss_out);
 void orc_field_backward(const orc_field_cfg *c, const uint16_t *params, const float *coords, uint32_t stride, int64_t n,
                         const float *dl_dout, double *grad, float *out4);
+/* ... and, when dl_dextra is given, the gradient w.r.t. each record's expression dims [n][n_extra]. */
+void orc_field_backward_ex(const orc_field_cfg *c, const uint16_t *params, const float *coords, uint32_t stride, int64_t n,
+                           const float *dl_dout, double *grad, float *out4, double *dl_dextra);
 void orc_raycast(const orc_render_cfg *rc, const orc_tri *tris, int n_tris, const float *center, int color_normal, float *out_rgba,
                  float *out_depth, int32_t *out_tri);
 int orc_march_ray(const orc_render_cfg *rc, const uint8_t *bitfield, int px, int py,

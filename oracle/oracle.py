@@ -214,18 +214,21 @@ def field_eval(fc, params, coords, fp64=False, weight_format=0, layer_scales=Non
     return out
 
 
-def field_backward(fc, params, coords, dl_dout=None):
+def field_backward(fc, params, coords, dl_dout=None, extra_grad=False):
     """NerfNetwork backward in FP64: (gradient of sum(dl_dout * out) w.r.t. every parameter
-    [float64, snapshot order], the FP64 forward's outputs [n, 4])."""
+    [float64, snapshot order], the FP64 forward's outputs [n, 4]); with extra_grad also the
+    gradient w.r.t. each record's expression dims [n, n_extra] (float64)."""
     c = np.ascontiguousarray(coords, dtype=np.float32)
     cfg = field_cfg(fc, 0)
     p = np.ascontiguousarray(params).view(np.uint16)
     grad = np.zeros(p.size, np.float64)
     out = np.zeros((len(c), 4), np.float32)
     g = None if dl_dout is None else np.ascontiguousarray(dl_dout, np.float32)
-    lib().orc_field_backward(C.byref(cfg), ptr(p), ptr(c), C.c_uint32(c.shape[1]), C.c_int64(len(c)),
-                             ptr(g) if g is not None else None, ptr(grad) if g is not None else None, ptr(out))
-    return grad, out
+    dx = np.zeros((len(c), max(1, int(cfg.n_extra))), np.float64) if extra_grad else None
+    lib().orc_field_backward_ex(C.byref(cfg), ptr(p), ptr(c), C.c_uint32(c.shape[1]), C.c_int64(len(c)),
+                                ptr(g) if g is not None else None, ptr(grad) if g is not None else None, ptr(out),
+                                ptr(dx) if dx is not None else None)
+    return (grad, out, dx[:, :int(cfg.n_extra)]) if extra_grad else (grad, out)
 
 
 class TrainLossCfg(C.Structure):

@@ -134,6 +134,52 @@ def test_backward_tcgen05(ctx, field, oracle, n):
     assert ((g[lay.table_offset:] != 0) <= touched_ref).all()
 
 
+@pytest.mark.parametrize("tcgen05", [False, True])
+def test_extra_dims_gradient(ctx, field, oracle, tcgen05):
+    """insta_field_backward_ex's expression-dim gradients against the FP64 oracle (FP32 products:
+    within 1e-4 of the largest; tcgen05's FP16 operands: norm within 5e-2), then
+    insta_extra_dims_gradient: each kept ray's samples summed into its image's row, against a
+    float64 sum of the same per-sample gradients (1e-5 of the largest row)."""
+    fc, params, lay = field
+    n = 3000
+    c = coords(n, seed=31)
+    g_out = np.random.default_rng(32).normal(size=(n, 4)).astype(np.float32)
+    grad = torch.zeros(lay.total, dtype=torch.float32, device="cuda")
+    dx = torch.zeros((n, 16), dtype=torch.float32, device="cuda")
+    ctx.train_set_math(False, tcgen05=tcgen05)
+    try:
+        ctx.field_backward(AVATAR, dev(c), c.shape[1], n, dev(g_out), grad, None, dl_dextra=dx)
+        ctx.sync()
+    finally:
+        ctx.train_set_math(False)
+    _, _, ref_dx = oracle.field_backward(fc, params, c, g_out, extra_grad=True)
+    got = dx.cpu().numpy().astype(np.float64)
+    if tcgen05:
+        assert np.linalg.norm(got - ref_dx) <= 5e-2 * np.linalg.norm(ref_dx)
+    else:
+        assert np.abs(got - ref_dx).max() <= 1e-4 * np.abs(ref_dx).max()
+    # per image sums over kept rays' compacted blocks (rays in a shuffled order, some empty)
+    rng = np.random.default_rng(33)
+    n_rays, n_img = 400, 5
+    counts = rng.integers(0, 15, n_rays).astype(np.uint32)
+    counts[0] = 0
+    total = int(counts.sum())
+    assert total <= n
+    bases = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint32)
+    perm = rng.permutation(n_rays).astype(np.uint32)
+    img = rng.integers(0, n_img, n_rays).astype(np.uint32)
+    kept = n_rays - 7                                          # the last rays were not kept
+    out = torch.zeros((n_img, 16), dtype=torch.float32, device="cuda")
+    i32 = lambda a: dev(a.view(np.int32))
+    ctx.extra_dims_gradient(n_rays, 16, n_img, i32(np.array([kept], np.uint32)), i32(perm), i32(np.stack([counts, bases], 1)), i32(img),
+                            dx, out)
+    ctx.sync()
+    ref = np.zeros((n_img, 16), np.float64)
+    for i in range(kept):
+        ref[img[perm[i]]] += got[bases[i]:bases[i] + counts[i]].sum(0)
+    assert np.abs(out.cpu().numpy() - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
 def test_backward_accumulates_and_forward_only(ctx, field, oracle):
     fc, params, lay = field
     n = 700

@@ -220,6 +220,37 @@ def test_field_backward_oracle_matches_finite_differences(oracle):
     assert checked == 80 and np.abs(grad[nz_table]).max() > 0
 
 
+def test_extra_dims_gradient_oracle_matches_finite_differences(oracle):
+    """The oracle's gradient w.r.t. the expression dims (the input gradient train_nerf_step asks
+    for when it optimises them) against central differences of the FP64 forward: the field is
+    piecewise linear in each input dim, so a step that flips no ReLU gives the slope up to the
+    FP32 rounding of the outputs."""
+    from insta_gb300 import synthetic as S
+    fc = S.FieldConfig(n_extra=16)
+    params = S.field_params(fc, seed=3)
+    rng = np.random.default_rng(9)
+    n = 5
+    c = np.zeros((n, 11 + 16), np.float32)
+    c[:, :3] = rng.uniform(0.35, 0.65, (n, 3))
+    d = rng.normal(size=(n, 3))
+    c[:, 8:11] = (d / np.linalg.norm(d, axis=1, keepdims=True) + 1) * 0.5
+    c[:, 11:] = rng.uniform(-1, 1, (n, 16))
+    g_out = rng.normal(size=(n, 4)).astype(np.float32)
+    _, _, dx = oracle.field_backward(fc, params, c, g_out, extra_grad=True)
+    assert dx.shape == (n, 16) and np.abs(dx).max() > 0
+    def f(s_, k, h):
+        c2 = c[s_:s_ + 1].copy()
+        c2[0, 11 + k] = np.float32(c2[0, 11 + k] + np.float32(h))
+        return float((oracle.field_eval(fc, params, c2, fp64=True).astype(np.float64) * g_out[s_]).sum()), float(c2[0, 11 + k])
+
+    for s_ in range(n):
+        for k in range(0, 16, 3):
+            (fp, xp), (f0, x0), (fm, xm) = f(s_, k, 5e-4), f(s_, k, 0.0), f(s_, k, -5e-4)
+            # central, right and left slopes: a ReLU kink inside one side leaves the other exact
+            slopes = [(fp - fm) / (xp - xm), (fp - f0) / (xp - x0), (f0 - fm) / (x0 - xm)]
+            assert min(abs(v - dx[s_, k]) for v in slopes) <= 2e-3 + 2e-2 * abs(dx[s_, k]), (s_, k, slopes, dx[s_, k])
+
+
 @pytest.mark.parametrize("loss_type,srgb", [(0, 1), (4, 0), (0, 0)])
 def test_train_loss_oracle_gradients_match_finite_differences(oracle, loss_type, srgb):
     from conftest import loss_cfg, train_loss_batch
