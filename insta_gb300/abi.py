@@ -123,7 +123,8 @@ class RenderDesc(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("max_steps_per_round", C.c_uint32), ("sort_cell_bits", C.c_uint32), ("mlp_ctas_per_sm", C.c_uint32),
-                ("deform_blocks_per_sm", C.c_uint32), ("bvh_top_nodes", C.c_uint32), ("fused_field_stage", C.c_uint32)]
+                ("deform_blocks_per_sm", C.c_uint32), ("bvh_top_nodes", C.c_uint32), ("fused_field_stage", C.c_uint32),
+                ("mlp_slots", C.c_uint32)]
 
 
 _lib = None
@@ -491,9 +492,9 @@ class Context:
         self._check(self.lib.insta_render_batch(self.h, arr, n, pr, pd))
 
     def tuning_set(self, max_steps_per_round=0, sort_cell_bits=0, mlp_ctas_per_sm=0, deform_blocks_per_sm=0, bvh_top_nodes=0,
-                   fused_field_stage=0):
+                   fused_field_stage=0, mlp_slots=0):
         """insta_tuning_set: the wavefront's launch shapes (0 keeps a field's built-in choice)."""
-        t = Tuning(max_steps_per_round, sort_cell_bits, mlp_ctas_per_sm, deform_blocks_per_sm, bvh_top_nodes, fused_field_stage)
+        t = Tuning(max_steps_per_round, sort_cell_bits, mlp_ctas_per_sm, deform_blocks_per_sm, bvh_top_nodes, fused_field_stage, mlp_slots)
         self._check(self.lib.insta_tuning_set(self.h, C.byref(t)))
 
     def tuning_get(self) -> dict:

@@ -16,7 +16,7 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 OUT_DIR = HERE / "_lib"
 LIB = OUT_DIR / "libinsta_gb300.so"
-SOURCES = ["insta_abi.cu", "frame_kernels.cu", "render_kernels.cu", "static_scratch.cu", "train_kernels.cu", "train_mlp.cu"]
+SOURCES = ["insta_abi.cu", "frame_kernels.cu", "render_kernels.cu", "static_scratch.cu", "train_kernels.cu", "train_mlp.cu", "mlp_slots.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -712,7 +712,7 @@ struct WaveRun {
                     if (e == cudaSuccess) e = launch_field_fused(R, M, grid_tiles, ctx->stream, ctx->tune.mlp_ctas_per_sm);
                 } else {
                     if (e == cudaSuccess) e = launch_deform_encode(R, ctx->tune.deform_blocks_per_sm, ctx->stream);
-                    if (e == cudaSuccess) e = launch_mlp(M, grid_tiles, ctx->stream, ctx->tune.mlp_ctas_per_sm);
+                    if (e == cudaSuccess) e = launch_mlp(M, grid_tiles, ctx->stream, ctx->tune.mlp_ctas_per_sm, ctx->tune.mlp_slots);
                 }
                 if (e == cudaSuccess) e = launch_composite(R, ctx->stream);
             }
@@ -750,7 +750,7 @@ struct WaveRun {
             CK(launch_field_fused(W, M, (uint32_t)(cap_samples / 128), ctx->stream, ctx->tune.mlp_ctas_per_sm));
         } else {
             { Stage st(ctx, INSTA_STAGE_DEFORM_ENCODE, 1); CK(launch_map_encode(W, ctx->tune.deform_blocks_per_sm, ctx->stream)); }
-            { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream, ctx->tune.mlp_ctas_per_sm)); }
+            { Stage st(ctx, INSTA_STAGE_MLP, 1); CK(launch_mlp(M, (uint32_t)(cap_samples / 128), ctx->stream, ctx->tune.mlp_ctas_per_sm, ctx->tune.mlp_slots)); }
         }
         { Stage st(ctx, INSTA_STAGE_COMPOSITE, 1); CK(launch_composite(W, ctx->stream)); }
         cur ^= 1;
@@ -841,6 +841,14 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
     }
     WaveRun run;
     run.setup(ctx, *field0, (uint32_t)n, total_pix, false);
+    {
+        // one weight image for every request (one avatar, or avatars sharing one): the MLP stage
+        // can keep it resident once per SM
+        bool same = true;
+        for (int i = 1; i < n; ++i) same = same && views[(size_t)i].mlp == views[0].mlp;
+        run.M.single = same ? views[0].mlp : nullptr;
+        run.M.batch = n > 1 ? 1u : 0u;
+    }
     if (n_extra) CK(cudaMemcpyAsync(ctx->extra.p, extra.data(), extra.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     run.upload_table(views.data());
     // the first round's step count needs the alive count only when all pixels could not take
@@ -1908,6 +1916,7 @@ int insta_tuning_set(insta_ctx* ctx, const insta_tuning* t) {
         if (t->bvh_top_nodes != 0 && t->bvh_top_nodes != 5 && t->bvh_top_nodes != 21)
             fail(INSTA_ERR_INVALID_ARG, "bvh_top_nodes must be 0, 5 or 21");
         if (t->fused_field_stage > 1) fail(INSTA_ERR_INVALID_ARG, "fused_field_stage must be 0 or 1");
+        if (t->mlp_slots > 7) fail(INSTA_ERR_INVALID_ARG, "mlp_slots must be 0..7");
         ctx->tune = *t;
     });
 }
@@ -1962,14 +1971,16 @@ int insta_autotune(insta_ctx* ctx, const insta_render_desc* reqs, int n, int rep
         float cur_ms = 0.f;
         try {
             cur_ms = time_one(cur);
-            const std::vector<uint32_t> cands[6] = {{8, 16, 24, 32}, {15, 18, 21}, {1, 2, 3, 4}, {8, 12, 16, 24}, {0, 5, 21}, {0, 1}};
+            const std::vector<uint32_t> cands[7] = {{8, 16, 24, 32}, {15, 18, 21}, {1, 2, 3, 4}, {8, 12, 16, 24}, {0, 5, 21}, {0, 1},
+                                                    {1, 7}};
             for (int pass = 0; pass < 2; ++pass) {
                 bool moved = false;
-                for (int f = 0; f < 6; ++f) {
+                for (int f = 0; f < 7; ++f) {
                     for (uint32_t v : cands[f]) {
                         insta_tuning t = cur;
                         uint32_t* field = f == 0 ? &t.max_steps_per_round : f == 1 ? &t.sort_cell_bits : f == 2 ? &t.mlp_ctas_per_sm
-                                        : f == 3 ? &t.deform_blocks_per_sm : f == 4 ? &t.bvh_top_nodes : &t.fused_field_stage;
+                                        : f == 3 ? &t.deform_blocks_per_sm : f == 4 ? &t.bvh_top_nodes : f == 5 ? &t.fused_field_stage
+                                        : &t.mlp_slots;
                         if (*field == v) continue;
                         *field = v;
                         const float ms = time_one(t);

@@ -1,0 +1,239 @@
+// mlp_slots.cu -- the avatar MLPs over ready-made operand tiles with several tiles in flight per
+// SM: one persistent CTA per SM holds the weight image once, and up to kMaxSlots tile slots, each
+// a warpgroup of 128 threads (one sample row per thread) with its own shared-memory tile, its own
+// 64 TMEM columns and its own chain (one thread issues the layer's MMAs, one warp waits on the
+// commit, the slot's named barrier releases the others, the epilogue converts the accumulator
+// into the next layer's operand rows).  The slots synchronise only within themselves, so one
+// slot's epilogue overlaps the others' MMAs; compared with mlp256_kernel (four CTAs of 256
+// threads per SM, each with its own copy of the weights) more tiles are in flight per SM.  Same
+// arithmetic and rounding as mlp256_kernel (FP16 / BF16): NerfNetwork::
+// inference_mixed_precision_impl's density and colour MLPs (NGP/nerf_network.h:159-232).
+//
+// Per slot s: full[s] completes when the tile record has landed (two bulk copies: hash rows, SH
+// rows), done[s] at the commit of the slot's current layer.  The record's hash rows and the
+// hidden activations share one 16 KiB buffer: the activations are written only after the layer
+// that read the hash rows completed, and the next record is copied in once the tile's last layer
+// has completed.  Every wait is bounded (about a second), after which the kernel sets
+// INSTA_DEVERR_TIMEOUT and the slot leaves.
+#include <cstdint>
+
+#include "device_common.cuh"
+#include "mlp_tiles.cuh"
+#include "kernels.h"
+
+namespace insta {
+
+namespace {
+
+constexpr uint32_t kMaxSlots = 7;
+constexpr uint32_t kSlotBytes = 24576;   // [0, 16 KiB) hash rows, then activations; SH rows; density rows
+constexpr uint32_t kCtlBytes = 1024;
+
+struct SlotCtl {
+    uint64_t full[kMaxSlots];
+    uint64_t done[kMaxSlots];
+    uint64_t bar_w;
+    uint32_t tmem_base;
+};
+
+// The slot's 128 threads meet at named barrier `id`; true when every thread passed true.
+__device__ __forceinline__ bool slot_sync_and(uint32_t id, bool v) {
+    uint32_t r;
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n barrier.cta.red.and.pred q, %2, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+                 : "=r"(r) : "r"(v ? 1u : 0u), "r"(id) : "memory");
+    return r != 0;
+}
+
+// Layer l of the chain: n_dh density hidden layers, the density output (N = 16), n_rh colour
+// hidden layers (the first over [density output | SH]), the colour output (N = 16).
+struct LayerOps {
+    const uint8_t* a[2];
+    const uint8_t* b[2];
+    uint32_t k[2];
+    int n_ops;
+    uint32_t n;
+};
+
+__device__ __forceinline__ LayerOps layer_ops(const TilePlan& P, const uint8_t* w, const uint8_t* stage, const uint8_t* sh,
+                                              const uint8_t* dens, uint32_t l) {
+    LayerOps o{};
+    o.n_ops = 1;
+    o.n = 64;
+    o.a[0] = stage;
+    o.k[0] = 64;
+    if (l < P.n_dh) {
+        o.b[0] = w + P.d_off[l];
+        if (l == 0) o.k[0] = P.k_in;
+    } else if (l == P.n_dh) {
+        o.b[0] = w + P.d_out;
+        o.n = 16;
+    } else if (l == P.n_dh + 1) {
+        o.n_ops = 2;
+        o.a[0] = dens; o.b[0] = w + P.r0_dens; o.k[0] = 16;
+        o.a[1] = sh; o.b[1] = w + P.r0_sh; o.k[1] = 16;
+    } else if (l < P.n_dh + 1 + P.n_rh) {
+        o.b[0] = w + P.r_off[l - (P.n_dh + 1)];
+    } else {
+        o.b[0] = w + P.r_out;
+        o.n = 16;
+    }
+    return o;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __grid_constant__ MlpArgs A, const uint8_t* wimg,
+                                                                      uint32_t n_slots) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    SlotCtl& ctl = *reinterpret_cast<SlotCtl*>(smem);
+    uint8_t* slots = smem + kCtlBytes;
+    uint8_t* w = slots + n_slots * kSlotBytes;
+    const TilePlan& P = A.plan;
+    const uint32_t n_samples = A.n_alive ? *A.n_alive : (uint32_t)A.n_samples;
+    const uint32_t n_tiles = (n_samples + 127u) / 128u;
+    const uint32_t stride = gridDim.x * n_slots;
+    const uint32_t n_layers = P.n_dh + P.n_rh + 2u;
+    const uint32_t hash_bytes = hash_tile_bytes(P.k_in), sh_bytes = sh_tile_bytes();
+    const bool bf16 = A.fv.precision == 1;
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t s = threadIdx.x >> 7, r = threadIdx.x & 127u, bar_id = 1u + s;
+    if (threadIdx.x == 0) {
+        for (uint32_t k = 0; k < n_slots; ++k) {
+            mbar_init(&ctl.full[k], 2);
+            mbar_init(&ctl.done[k], 1);
+        }
+        mbar_init(&ctl.bar_w, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // 64 columns per slot, allocated as a power of two
+    const uint32_t tmem_cols = n_slots <= 2u ? 128u : (n_slots <= 4u ? 256u : 512u);
+    if (warp == 0) tmem_alloc(&ctl.tmem_base, tmem_cols);
+    if (threadIdx.x == 0) bulk_load(w, wimg, P.bytes, &ctl.bar_w);
+    bool ok = mbar_wait(&ctl.bar_w, 0);
+    tc_fence_before();
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    tc_fence_after();
+    const uint32_t tmem = ctl.tmem_base;
+
+    uint8_t* st = slots + s * kSlotBytes;
+    uint8_t* sh = st + 16384;
+    uint8_t* dens = st + 20480;
+    const uint32_t col0 = tmem + ((warp & 3u) * 32u << 16) + s * 64u;
+    const bool waiter = (warp & 3u) == 0;   // the slot's first warp waits on the mbarriers
+    uint32_t n_done = 0, n_loads = 0, n_used = 0;
+    uint32_t t = blockIdx.x * n_slots + s;
+    auto load = [&](uint32_t tt) {
+        const uint8_t* src = A.tiles + (size_t)tt * P.tile_bytes;
+        bulk_load(st, src, hash_bytes, &ctl.full[s]);
+        bulk_load(sh, src + hash_bytes, sh_bytes, &ctl.full[s]);
+    };
+    if (t < n_tiles && ok) {
+        if (r == 0) load(t);
+        ++n_loads;
+    }
+    for (; t < n_tiles && ok; t += stride) {
+        float o4[4] = {0.f, 0.f, 0.f, 0.f};
+        for (uint32_t l = 0; l < n_layers; ++l) {
+            // operands: the record (layer 0) or the rows the previous epilogue wrote
+            fence_async_smem();
+            tc_fence_before();
+            bool wok = true;
+            if (l == 0 && waiter) wok = mbar_wait(&ctl.full[s], n_used & 1u);
+            if (l == 0) ++n_used;
+            ok = slot_sync_and(bar_id, wok);
+            if (!ok) break;
+            tc_fence_after();
+            if (r == 0) {
+                const LayerOps o = layer_ops(P, w, st, sh, dens, l);
+                const uint32_t idesc = idesc_f16(128, o.n, bf16);
+                uint32_t acc = 0;
+                for (int i = 0; i < o.n_ops; ++i) {
+                    const uint32_t a0 = smem_addr(o.a[i]), b0 = smem_addr(o.b[i]);
+                    const uint32_t sbo = (o.k[i] / 8u) * 128u;
+                    for (uint32_t ks = 0; ks < o.k[i] / 16u; ++ks) {
+                        umma_f16(tmem + s * 64u, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, acc);
+                        acc = 1;
+                    }
+                }
+                umma_commit(&ctl.done[s]);
+            }
+            wok = true;
+            if (waiter) wok = mbar_wait(&ctl.done[s], n_done & 1u);
+            ++n_done;
+            ok = slot_sync_and(bar_id, wok);
+            if (!ok) break;
+            tc_fence_after();
+            if (l + 1 == n_layers && r == 0 && t + stride < n_tiles) load(t + stride);   // this tile's MMAs are done
+            if (l + 1 == n_layers && t + stride < n_tiles) ++n_loads;
+            if (l == P.n_dh) {
+                float v[16];
+                tmem_ld16(col0, v);
+                __half h[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) h[i] = to_act(v[i], bf16);
+                o4[3] = from_act(h[0], bf16);
+                store_row(dens, r, 16, h);
+            } else if (l + 1 == n_layers) {
+                float v[16];
+                tmem_ld16(col0, v);
+                o4[0] = from_act(to_act(v[0], bf16), bf16);
+                o4[1] = from_act(to_act(v[1], bf16), bf16);
+                o4[2] = from_act(to_act(v[2], bf16), bf16);
+            } else {
+                // ReLU, rounding to the activation type, into the activation rows (K = 64)
+#pragma unroll 1
+                for (uint32_t c = 0; c < 64u; c += 32u) {
+                    float v[32];
+                    tmem_ld32(col0 + c, v);
+                    uint32_t p[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) p[i] = pack2_act(fmaxf(v[2 * i], 0.f), fmaxf(v[2 * i + 1], 0.f), bf16);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        *reinterpret_cast<uint4*>(st + tile_offset(r, c + q * 8u, 64)) =
+                            make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+                }
+            }
+        }
+        const uint32_t row = t * 128u + r;
+        if (ok && row < n_samples) {
+            if (A.fv.precision != 0) {
+                A.out_f32[row] = make_float4(o4[0], o4[1], o4[2], o4[3]);
+            } else {
+                const __half2 rg = __floats2half2_rn(o4[0], o4[1]);
+                const __half2 bd = __floats2half2_rn(o4[2], o4[3]);
+                A.out[row] = make_uint2(*reinterpret_cast<const uint32_t*>(&rg), *reinterpret_cast<const uint32_t*>(&bd));
+            }
+        }
+    }
+    // a record whose copies were issued but not consumed (after a timeout): wait for them
+    // (bounded) before shared memory is released
+    if (r == 0 && n_loads > n_used) mbar_wait(&ctl.full[s], (n_loads - 1u) & 1u);
+    if (!ok && r == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, tmem_cols);
+}
+
+uint32_t mlp_slots_for(const TilePlan& P, int smem_optin) {
+    if (P.k_in > 64u) return 0;
+    const long avail = (long)smem_optin - (long)kCtlBytes - (long)((P.bytes + 1023u) & ~1023u);
+    long n = avail / (long)kSlotBytes;
+    if (n > (long)kMaxSlots) n = kMaxSlots;
+    return n < 2 ? 0u : (uint32_t)n;
+}
+
+cudaError_t launch_mlp_slots(const MlpArgs& a, const uint8_t* image, uint32_t n_slots, uint32_t max_tiles, int n_sms, cudaStream_t s) {
+    const size_t smem = kCtlBytes + (size_t)n_slots * kSlotBytes + a.plan.bytes;
+    cudaError_t e = cudaFuncSetAttribute(mlp_slots_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    uint32_t grid = (uint32_t)n_sms;
+    const uint32_t need = (max_tiles + n_slots - 1) / n_slots;
+    if (need < grid) grid = need ? need : 1;
+    mlp_slots_kernel<<<grid, n_slots * 128, smem, s>>>(a, image, n_slots);
+    return cudaGetLastError();
+}
+
+}  // namespace insta

@@ -67,6 +67,26 @@ def test_batch_equals_single_renders(ctx, two_avatars):
     assert all((b[0][:, 3] > 0.05).sum() > 20 for b in ref), [int((b[0][:, 3] > 0.05).sum()) for b in ref]
 
 
+@pytest.mark.parametrize("slots", [0, 3, 7])
+def test_one_avatar_batch_equals_single_renders(ctx, two_avatars, slots):
+    """A batch whose requests all use one avatar's weights runs the MLP stage with the weights
+    resident once per SM (the tile-slot kernel: by default for such batches, or forced with 3 or 7
+    slots): each request's pixels still equal insta_render alone, bit for bit."""
+    reqs = requests(ctx, [s for s in SPECS if s[0] == 10] + [(10, 0, 96, 80, 5.0, 0)])
+    ref = [single(ctx, r) for r in reqs]
+    rgba = [np.full((r.width * r.height, 4), -1, np.float32) for r in reqs]
+    depth = [np.full(r.width * r.height, -1, np.float32) for r in reqs]
+    before = ctx.tuning_get()
+    ctx.tuning_set(mlp_slots=slots)
+    try:
+        ctx.render_batch(reqs, rgba, depth)
+    finally:
+        ctx.tuning_set(**before)
+    for i, (a, b) in enumerate(zip(rgba, ref)):
+        assert (a == b[0]).all(), f"request {i}: rgba differs"
+        assert (depth[i] == b[1]).all(), f"request {i}: depth differs"
+
+
 def test_batch_device_outputs_and_order(ctx, two_avatars):
     """Device outputs, and the same requests in reverse order, give the same pixels."""
     reqs = requests(ctx, SPECS)

@@ -143,6 +143,10 @@ def test_render_512_multi_round_bit_identical(full, frame512):
     s_rgba, s_depth, s_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(sort_cell_bits=15, mlp_ctas_per_sm=1,
                                                                           deform_blocks_per_sm=8, bvh_top_nodes=21))
     assert np.array_equal(s_rgba, rgba) and np.array_equal(s_depth, depth) and np.array_equal(s_counts, counts)
+    # the MLP stage with the weights resident once per SM (tile slots), against one copy per CTA
+    for n_slots in (7, 2):
+        k_rgba, k_depth, k_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(mlp_slots=n_slots))
+        assert np.array_equal(k_rgba, rgba) and np.array_equal(k_depth, depth) and np.array_equal(k_counts, counts)
     # the deform + encode + MLP stage as one kernel, against encode to global tiles + MLP (default)
     f_rgba, f_depth, f_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(fused_field_stage=1, bvh_top_nodes=5))
     assert np.array_equal(f_rgba, rgba) and np.array_equal(f_depth, depth) and np.array_equal(f_counts, counts)
