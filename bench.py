@@ -828,6 +828,7 @@ def run_precision(args):
     params = S.field_params(fc, seed=0)
     frame = av.frame(av.frame_coeffs(0))
     ctx = abi.Context(0)
+    apply_tuning(ctx, args)
     ctx.canonical_set(0, av.canonical, av.faces, av.mask)
     ctx.frame_upload(0, 0, frame)
     ctx.occupancy_from_mesh(0, 0, RADIUS)

@@ -465,11 +465,12 @@ typedef struct insta_tuning {
                                        nearest-triangle stage copies into shared memory (built-in 0) */
     uint32_t fused_field_stage;     /* 1: deform + encode + MLP as one kernel (FP16 / BF16 fields);
                                        0 (built-in, faster on GB300): encode to global operand tiles, then the MLP */
-    uint32_t mlp_slots;             /* MLP stage of FP16 / BF16 fields whose tiles share one weight image:
-                                       2..7 = one persistent CTA per SM with that many 128-sample tile slots
-                                       sharing one copy of the weights; 1 = several CTAs per SM, each with its
-                                       own copy (mlp_ctas_per_sm); 0 = built-in: slots for batches of two or
-                                       more requests on one weight image (measured faster there), else CTAs */
+    uint32_t mlp_slots;             /* MLP stage where every tile uses one weight image: 2..7 = one
+                                       persistent CTA per SM with that many 128-sample tile slots sharing one
+                                       copy of the weights (one sample row per thread); 1 = several CTAs per
+                                       SM, each with its own copy (mlp_ctas_per_sm); 0 = built-in: slots for
+                                       FP8 fields and for batches of two or more requests on one weight image
+                                       (measured faster there), else CTAs */
 } insta_tuning;
 int insta_tuning_set(insta_ctx* ctx, const insta_tuning* t);
 int insta_tuning_get(insta_ctx* ctx, insta_tuning* t);

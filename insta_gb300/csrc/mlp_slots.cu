@@ -26,7 +26,9 @@ namespace insta {
 namespace {
 
 constexpr uint32_t kMaxSlots = 7;
-constexpr uint32_t kSlotBytes = 24576;   // [0, 16 KiB) hash rows, then activations; SH rows; density rows
+constexpr uint32_t kSlotBytes = 24576;    // FP16 / BF16: [0, 16 KiB) hash rows, then activations; SH rows; density rows
+constexpr uint32_t kSlotBytes8 = 32768;   // FP8: hash rows (FP16); SH rows (FP16); E4M3 layer input; E4M3 colour input
+__host__ __device__ constexpr uint32_t slot_bytes(bool fp8) { return fp8 ? kSlotBytes8 : kSlotBytes; }
 constexpr uint32_t kCtlBytes = 1024;
 
 struct SlotCtl {
@@ -80,14 +82,65 @@ __device__ __forceinline__ LayerOps layer_ops(const TilePlan& P, const uint8_t* 
     return o;
 }
 
+// FP8 layer l: A the E4M3 layer input (density input padded to k8, then 64-wide hidden rows) or
+// the [density output | SH] rows; the image stores colour layer 0 as one K = 32 tile at r0_dens.
+__device__ __forceinline__ LayerOps layer_ops8(const TilePlan& P, const uint8_t* w, const uint8_t* a8, const uint8_t* rgb8, uint32_t l) {
+    LayerOps o{};
+    o.n_ops = 1;
+    o.n = 64;
+    o.a[0] = a8;
+    o.k[0] = 64;
+    if (l < P.n_dh) {
+        o.b[0] = w + P.d_off[l];
+        if (l == 0) o.k[0] = P.k8;
+    } else if (l == P.n_dh) {
+        o.b[0] = w + P.d_out;
+        o.n = 16;
+    } else if (l == P.n_dh + 1) {
+        o.a[0] = rgb8; o.b[0] = w + P.r0_dens; o.k[0] = 32;
+    } else if (l < P.n_dh + 1 + P.n_rh) {
+        o.b[0] = w + P.r_off[l - (P.n_dh + 1)];
+    } else {
+        o.b[0] = w + P.r_out;
+        o.n = 16;
+    }
+    return o;
+}
+
+// A 64-wide FP8 hidden layer's epilogue for the thread's own row: dequantise (input row scale a,
+// layer weight scale sw), ReLU, the row maximum (the whole row is this thread's, no exchange),
+// E4M3 with the new row scale into a8 (K = 64).  Returns the new row scale.
+__device__ __forceinline__ float hidden8_row(uint32_t col0, uint8_t* a8, float a, float sw, uint32_t r) {
+    float mx = 0.f;
+#pragma unroll 1
+    for (uint32_t c = 0; c < 64u; c += 32u) {
+        float v[32];
+        tmem_ld32(col0 + c, v);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) mx = fmaxf(mx, fmaxf(__fmul_rn(__fmul_rn(v[i], a), sw), 0.f));
+    }
+    const float inv = row_inv(mx);
+#pragma unroll 1
+    for (uint32_t c = 0; c < 64u; c += 32u) {
+        float v[32];
+        tmem_ld32(col0 + c, v);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = fmaxf(__fmul_rn(__fmul_rn(v[i], a), sw), 0.f);
+        store16_e4m3_row(a8, 64, c, v, inv, r);
+        store16_e4m3_row(a8, 64, c + 16u, v + 16, inv, r);
+    }
+    return row_scale(mx);
+}
+
 }  // namespace
 
+template <bool FP8>
 __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __grid_constant__ MlpArgs A, const uint8_t* wimg,
                                                                       uint32_t n_slots) {
     extern __shared__ __align__(1024) uint8_t smem[];
     SlotCtl& ctl = *reinterpret_cast<SlotCtl*>(smem);
     uint8_t* slots = smem + kCtlBytes;
-    uint8_t* w = slots + n_slots * kSlotBytes;
+    uint8_t* w = slots + n_slots * slot_bytes(FP8);
     const TilePlan& P = A.plan;
     const uint32_t n_samples = A.n_alive ? *A.n_alive : (uint32_t)A.n_samples;
     const uint32_t n_tiles = (n_samples + 127u) / 128u;
@@ -116,9 +169,10 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
     tc_fence_after();
     const uint32_t tmem = ctl.tmem_base;
 
-    uint8_t* st = slots + s * kSlotBytes;
+    uint8_t* st = slots + s * slot_bytes(FP8);
     uint8_t* sh = st + 16384;
-    uint8_t* dens = st + 20480;
+    uint8_t* dens = st + 20480;   // FP16 / BF16 density rows; FP8: the E4M3 layer input
+    uint8_t* rgb8 = st + 28672;   // FP8: E4M3 [density output | SH] rows
     const uint32_t col0 = tmem + ((warp & 3u) * 32u << 16) + s * 64u;
     const bool waiter = (warp & 3u) == 0;   // the slot's first warp waits on the mbarriers
     uint32_t n_done = 0, n_loads = 0, n_used = 0;
@@ -134,65 +188,144 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
     }
     for (; t < n_tiles && ok; t += stride) {
         float o4[4] = {0.f, 0.f, 0.f, 0.f};
-        for (uint32_t l = 0; l < n_layers; ++l) {
-            // operands: the record (layer 0) or the rows the previous epilogue wrote
-            fence_async_smem();
-            tc_fence_before();
-            bool wok = true;
-            if (l == 0 && waiter) wok = mbar_wait(&ctl.full[s], n_used & 1u);
-            if (l == 0) ++n_used;
-            ok = slot_sync_and(bar_id, wok);
-            if (!ok) break;
-            tc_fence_after();
-            if (r == 0) {
-                const LayerOps o = layer_ops(P, w, st, sh, dens, l);
-                const uint32_t idesc = idesc_f16(128, o.n, bf16);
-                uint32_t acc = 0;
-                for (int i = 0; i < o.n_ops; ++i) {
-                    const uint32_t a0 = smem_addr(o.a[i]), b0 = smem_addr(o.b[i]);
-                    const uint32_t sbo = (o.k[i] / 8u) * 128u;
-                    for (uint32_t ks = 0; ks < o.k[i] / 16u; ++ks) {
-                        umma_f16(tmem + s * 64u, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, acc);
-                        acc = 1;
+        if constexpr (FP8) {
+            const float* ls = reinterpret_cast<const float*>(w + P.scales);
+            float ra = 1.f;
+            for (int l = -1; l < (int)n_layers; ++l) {
+                fence_async_smem();
+                tc_fence_before();
+                bool wok = true;
+                if (l == -1 && waiter) wok = mbar_wait(&ctl.full[s], n_used & 1u);
+                if (l == -1) ++n_used;
+                ok = slot_sync_and(bar_id, wok);
+                if (!ok) break;
+                tc_fence_after();
+                if (l == -1) {
+                    // the density input: the FP16 hash row, E4M3 with its own row scale, zero-padded to k8
+                    float mx = 0.f;
+                    for (uint32_t c = 0; c < P.k_in; c += 16u) {
+                        float v[16];
+                        load16_half_row(st, P.k_in, c, v, r);
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fabsf(v[i]));
                     }
+                    ra = row_scale(mx);
+                    const float inv = row_inv(mx);
+                    for (uint32_t c = 0; c < P.k8; c += 16u) {
+                        float v[16];
+                        if (c < P.k_in) {
+                            load16_half_row(st, P.k_in, c, v, r);
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < 16; ++i) v[i] = 0.f;
+                        }
+                        store16_e4m3_row(dens, P.k8, c, v, inv, r);
+                    }
+                    continue;
                 }
-                umma_commit(&ctl.done[s]);
+                if (l == (int)P.n_dh + 1 && r == 0 && t + stride < n_tiles) load(t + stride);   // hash and SH rows are read
+                if (l == (int)P.n_dh + 1 && t + stride < n_tiles) ++n_loads;
+                if (r == 0) {
+                    const LayerOps o = layer_ops8(P, w, dens, rgb8, (uint32_t)l);
+                    const uint32_t idesc = idesc_f16(128, o.n, false);
+                    const uint32_t a0 = smem_addr(o.a[0]), b0 = smem_addr(o.b[0]);
+                    const uint32_t sbo = (o.k[0] / 16u) * 128u;
+                    for (uint32_t ks = 0; ks < o.k[0] / 32u; ++ks)
+                        umma_f8(tmem + s * 64u, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, ks ? 1u : 0u);
+                    umma_commit(&ctl.done[s]);
+                }
+                wok = true;
+                if (waiter) wok = mbar_wait(&ctl.done[s], n_done & 1u);
+                ++n_done;
+                ok = slot_sync_and(bar_id, wok);
+                if (!ok) break;
+                tc_fence_after();
+                const float sw = ls[l];
+                if (l == (int)P.n_dh) {
+                    float v[16], sv[16];
+                    tmem_ld16(col0, v);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) v[i] = __fmul_rn(__fmul_rn(v[i], ra), sw);
+                    o4[3] = v[0];
+                    load16_half_row(sh, 16, 0, sv, r);
+                    float mx = 0.f;
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fmaxf(fabsf(v[i]), fabsf(sv[i])));
+                    ra = row_scale(mx);
+                    const float inv = row_inv(mx);
+                    store16_e4m3_row(rgb8, 32, 0, v, inv, r);
+                    store16_e4m3_row(rgb8, 32, 16, sv, inv, r);
+                } else if (l + 1 == (int)n_layers) {
+                    float v[16];
+                    tmem_ld16(col0, v);
+                    o4[0] = __fmul_rn(__fmul_rn(v[0], ra), sw);
+                    o4[1] = __fmul_rn(__fmul_rn(v[1], ra), sw);
+                    o4[2] = __fmul_rn(__fmul_rn(v[2], ra), sw);
+                } else {
+                    ra = hidden8_row(col0, dens, ra, sw, r);
+                }
             }
-            wok = true;
-            if (waiter) wok = mbar_wait(&ctl.done[s], n_done & 1u);
-            ++n_done;
-            ok = slot_sync_and(bar_id, wok);
-            if (!ok) break;
-            tc_fence_after();
-            if (l + 1 == n_layers && r == 0 && t + stride < n_tiles) load(t + stride);   // this tile's MMAs are done
-            if (l + 1 == n_layers && t + stride < n_tiles) ++n_loads;
-            if (l == P.n_dh) {
-                float v[16];
-                tmem_ld16(col0, v);
-                __half h[16];
-#pragma unroll
-                for (int i = 0; i < 16; ++i) h[i] = to_act(v[i], bf16);
-                o4[3] = from_act(h[0], bf16);
-                store_row(dens, r, 16, h);
-            } else if (l + 1 == n_layers) {
-                float v[16];
-                tmem_ld16(col0, v);
-                o4[0] = from_act(to_act(v[0], bf16), bf16);
-                o4[1] = from_act(to_act(v[1], bf16), bf16);
-                o4[2] = from_act(to_act(v[2], bf16), bf16);
-            } else {
-                // ReLU, rounding to the activation type, into the activation rows (K = 64)
-#pragma unroll 1
-                for (uint32_t c = 0; c < 64u; c += 32u) {
-                    float v[32];
-                    tmem_ld32(col0 + c, v);
-                    uint32_t p[16];
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) p[i] = pack2_act(fmaxf(v[2 * i], 0.f), fmaxf(v[2 * i + 1], 0.f), bf16);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        *reinterpret_cast<uint4*>(st + tile_offset(r, c + q * 8u, 64)) =
-                            make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+        } else {
+            for (uint32_t l = 0; l < n_layers; ++l) {
+                // operands: the record (layer 0) or the rows the previous epilogue wrote
+                fence_async_smem();
+                tc_fence_before();
+                bool wok = true;
+                if (l == 0 && waiter) wok = mbar_wait(&ctl.full[s], n_used & 1u);
+                if (l == 0) ++n_used;
+                ok = slot_sync_and(bar_id, wok);
+                if (!ok) break;
+                tc_fence_after();
+                if (r == 0) {
+                    const LayerOps o = layer_ops(P, w, st, sh, dens, l);
+                    const uint32_t idesc = idesc_f16(128, o.n, bf16);
+                    uint32_t acc = 0;
+                    for (int i = 0; i < o.n_ops; ++i) {
+                        const uint32_t a0 = smem_addr(o.a[i]), b0 = smem_addr(o.b[i]);
+                        const uint32_t sbo = (o.k[i] / 8u) * 128u;
+                        for (uint32_t ks = 0; ks < o.k[i] / 16u; ++ks) {
+                            umma_f16(tmem + s * 64u, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, acc);
+                            acc = 1;
+                        }
+                    }
+                    umma_commit(&ctl.done[s]);
+                }
+                wok = true;
+                if (waiter) wok = mbar_wait(&ctl.done[s], n_done & 1u);
+                ++n_done;
+                ok = slot_sync_and(bar_id, wok);
+                if (!ok) break;
+                tc_fence_after();
+                if (l + 1 == n_layers && r == 0 && t + stride < n_tiles) load(t + stride);   // this tile's MMAs are done
+                if (l + 1 == n_layers && t + stride < n_tiles) ++n_loads;
+                if (l == P.n_dh) {
+                    float v[16];
+                    tmem_ld16(col0, v);
+                    __half h[16];
+    #pragma unroll
+                    for (int i = 0; i < 16; ++i) h[i] = to_act(v[i], bf16);
+                    o4[3] = from_act(h[0], bf16);
+                    store_row(dens, r, 16, h);
+                } else if (l + 1 == n_layers) {
+                    float v[16];
+                    tmem_ld16(col0, v);
+                    o4[0] = from_act(to_act(v[0], bf16), bf16);
+                    o4[1] = from_act(to_act(v[1], bf16), bf16);
+                    o4[2] = from_act(to_act(v[2], bf16), bf16);
+                } else {
+                    // ReLU, rounding to the activation type, into the activation rows (K = 64)
+    #pragma unroll 1
+                    for (uint32_t c = 0; c < 64u; c += 32u) {
+                        float v[32];
+                        tmem_ld32(col0 + c, v);
+                        uint32_t p[16];
+    #pragma unroll
+                        for (int i = 0; i < 16; ++i) p[i] = pack2_act(fmaxf(v[2 * i], 0.f), fmaxf(v[2 * i + 1], 0.f), bf16);
+    #pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            *reinterpret_cast<uint4*>(st + tile_offset(r, c + q * 8u, 64)) =
+                                make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+                    }
                 }
             }
         }
@@ -217,22 +350,25 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
     if (warp == 0) tmem_dealloc(tmem, tmem_cols);
 }
 
-uint32_t mlp_slots_for(const TilePlan& P, int smem_optin) {
-    if (P.k_in > 64u) return 0;
+uint32_t mlp_slots_for(const TilePlan& P, int smem_optin, bool fp8) {
+    if (P.k_in > 64u || (fp8 && P.k8 > 64u)) return 0;
     const long avail = (long)smem_optin - (long)kCtlBytes - (long)((P.bytes + 1023u) & ~1023u);
-    long n = avail / (long)kSlotBytes;
+    long n = avail / (long)slot_bytes(fp8);
     if (n > (long)kMaxSlots) n = kMaxSlots;
     return n < 2 ? 0u : (uint32_t)n;
 }
 
 cudaError_t launch_mlp_slots(const MlpArgs& a, const uint8_t* image, uint32_t n_slots, uint32_t max_tiles, int n_sms, cudaStream_t s) {
-    const size_t smem = kCtlBytes + (size_t)n_slots * kSlotBytes + a.plan.bytes;
-    cudaError_t e = cudaFuncSetAttribute(mlp_slots_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const bool fp8 = a.fv.precision == 2;
+    const size_t smem = kCtlBytes + (size_t)n_slots * slot_bytes(fp8) + a.plan.bytes;
+    const void* fn = fp8 ? (const void*)mlp_slots_kernel<true> : (const void*)mlp_slots_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     uint32_t grid = (uint32_t)n_sms;
     const uint32_t need = (max_tiles + n_slots - 1) / n_slots;
     if (need < grid) grid = need ? need : 1;
-    mlp_slots_kernel<<<grid, n_slots * 128, smem, s>>>(a, image, n_slots);
+    if (fp8) mlp_slots_kernel<true><<<grid, n_slots * 128, smem, s>>>(a, image, n_slots);
+    else mlp_slots_kernel<false><<<grid, n_slots * 128, smem, s>>>(a, image, n_slots);
     return cudaGetLastError();
 }
 

@@ -57,12 +57,12 @@ struct MlpArgs {
 };
 
 // slots (insta_tuning.mlp_slots): 2..7 = mlp_slots_kernel with that many slots where every tile
-// uses one weight image (FP16 / BF16); 1 = mlp256_kernel; 0 = mlp_slots_kernel for render batches
-// on one weight image, else mlp256_kernel.  ctas_per_sm: mlp256_kernel's resident CTAs per SM
+// uses one weight image; 1 = mlp256_kernel; 0 = mlp_slots_kernel for FP8 fields and for render
+// batches on one weight image, else mlp256_kernel.  ctas_per_sm: mlp256_kernel's resident CTAs per SM
 // (0 = as many as shared memory lets reside, at most 4).
 cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm = 0, uint32_t slots = 0);
 // mlp_slots.cu: slots that fit the opt-in shared memory (0 = the kernel does not apply), launch
-uint32_t mlp_slots_for(const TilePlan& P, int smem_optin);
+uint32_t mlp_slots_for(const TilePlan& P, int smem_optin, bool fp8);
 cudaError_t launch_mlp_slots(const MlpArgs& a, const uint8_t* image, uint32_t n_slots, uint32_t max_tiles, int n_sms, cudaStream_t s);
 
 // One MMA chain: sum over (A_i, B_i) pairs into TMEM columns [col, col + N).  K in elements;

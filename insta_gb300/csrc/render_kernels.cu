@@ -1084,12 +1084,12 @@ cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uin
     const size_t smem = (size_t)mlp2_w_off(a.plan.tile_bytes) + a.plan.bytes;
     const bool fp8 = a.fv.precision == 2;
     const uint8_t* image = a.seg ? a.single : a.fv.mlp_smem;
-    const bool want_slots = slots >= 2 || (slots == 0 && a.seg && a.batch);
-    if (!fp8 && image && want_slots) {
+    const bool want_slots = slots >= 2 || (slots == 0 && (fp8 || (a.seg && a.batch)));
+    if (image && want_slots) {
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        uint32_t n_slots = mlp_slots_for(a.plan, optin);
+        uint32_t n_slots = mlp_slots_for(a.plan, optin, fp8);
         if (slots >= 2 && slots < n_slots) n_slots = slots;
         if (n_slots) return launch_mlp_slots(a, image, n_slots, max_tiles, sm_count(), s);
     }

@@ -152,6 +152,22 @@ def test_render_512_multi_round_bit_identical(full, frame512):
     assert np.array_equal(f_rgba, rgba) and np.array_equal(f_depth, depth) and np.array_equal(f_counts, counts)
 
 
+@pytest.mark.parametrize("precision", [1, 2])
+def test_mlp_slots_equal_ctas_bf16_fp8(full, precision):
+    """BF16 and FP8 E4M3 MLPs: the tile-slot kernel (weights resident once per SM, one row per
+    thread, the FP8 row scale without an exchange) gives the same bits as the per-CTA kernel."""
+    ctx, fc, params = full
+    ctx.params_load(AV, fc, params, precision=precision)
+    try:
+        a = render_gpu(ctx, 256, 256, yaw=-8.0, tuning=dict(mlp_slots=1))
+        b = render_gpu(ctx, 256, 256, yaw=-8.0, tuning=dict(mlp_slots=6))
+    finally:
+        ctx.params_load(AV, fc, params)
+    assert (a[0][:, 3] > 0.05).sum() > 1000
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
+
+
 @pytest.mark.parametrize("precision,min_psnr", [(0, 45.0), (1, 45.0), (2, 35.0)])
 def test_render_1024_precision(full, oracle, avatar, deform, bits, precision, min_psnr):
     """1024x1024: FP16 (the plain path), BF16, FP8 E4M3 MLPs against the oracle's restatement of
