@@ -109,16 +109,19 @@ __device__ __forceinline__ LayerOps layer_ops8(const TilePlan& P, const uint8_t*
 
 // A 64-wide FP8 hidden layer's epilogue for the thread's own row: dequantise (input row scale a,
 // layer weight scale sw), ReLU, the row maximum (the whole row is this thread's, no exchange),
-// E4M3 with the new row scale into a8 (K = 64).  Returns the new row scale.
+// E4M3 with the new row scale into a8 (K = 64).  Returns the new row scale.  The maximum is taken
+// over the raw accumulator values and dequantised once: v -> round(round(v a) sw) is monotone for
+// positive scales, so this is the maximum of the dequantised values, bit for bit.
 __device__ __forceinline__ float hidden8_row(uint32_t col0, uint8_t* a8, float a, float sw, uint32_t r) {
-    float mx = 0.f;
+    float raw = -__int_as_float(0x7f800000);
 #pragma unroll 1
     for (uint32_t c = 0; c < 64u; c += 32u) {
         float v[32];
         tmem_ld32(col0 + c, v);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) mx = fmaxf(mx, fmaxf(__fmul_rn(__fmul_rn(v[i], a), sw), 0.f));
+        for (int i = 0; i < 32; ++i) raw = fmaxf(raw, v[i]);
     }
+    const float mx = fmaxf(__fmul_rn(__fmul_rn(raw, a), sw), 0.f);
     const float inv = row_inv(mx);
 #pragma unroll 1
     for (uint32_t c = 0; c < 64u; c += 32u) {

@@ -299,17 +299,21 @@ __device__ __forceinline__ float row_max2(float* xch, float m) {
     return fmaxf(m, o);
 }
 
+// (The maximum is taken over the raw accumulator values and dequantised once: v ->
+// round(round(v a) s) is monotone for positive scales, so this is the maximum of the dequantised
+// values, bit for bit.)
 template <typename Smem>
 __device__ __forceinline__ float hidden_to_e4m3_2(Smem& sm, float* xch, uint8_t* a_h8, float a, float s) {
     const uint32_t c0 = (threadIdx.x >> 7) * 32u;
-    float mx = 0.f;
+    float raw = -__int_as_float(0x7f800000);
 #pragma unroll 1
     for (uint32_t c = c0; c < c0 + 32u; c += 16) {
         float v[16];
         tmem_ld16(fused_lane_addr(sm, c), v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fmaxf(__fmul_rn(__fmul_rn(v[i], a), s), 0.f));
+        for (int i = 0; i < 16; ++i) raw = fmaxf(raw, v[i]);
     }
+    float mx = fmaxf(__fmul_rn(__fmul_rn(raw, a), s), 0.f);
     mx = row_max2(xch, mx);
     const float inv = row_inv(mx);
 #pragma unroll 1
