@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
                         tmem_ld32(col0 + c, v);
                         uint32_t p[16];
     #pragma unroll
-                        for (int i = 0; i < 16; ++i) p[i] = pack2_act(fmaxf(v[2 * i], 0.f), fmaxf(v[2 * i + 1], 0.f), bf16);
+                        for (int i = 0; i < 16; ++i) p[i] = pack2_relu(v[2 * i], v[2 * i + 1], bf16);
     #pragma unroll
                         for (int q = 0; q < 4; ++q)
                             *reinterpret_cast<uint4*>(st + tile_offset(r, c + q * 8u, 64)) =

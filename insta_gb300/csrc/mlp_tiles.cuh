@@ -161,7 +161,7 @@ __device__ __forceinline__ void relu_to_ah2(Smem& sm, bool bf16) {
         tmem_ld16(fused_lane_addr(sm, c), v);
         uint32_t p[8];   // ReLU, then both values of a pair rounded by one packed conversion
 #pragma unroll
-        for (int i = 0; i < 8; ++i) p[i] = pack2_act(fmaxf(v[2 * i], 0.f), fmaxf(v[2 * i + 1], 0.f), bf16);
+        for (int i = 0; i < 8; ++i) p[i] = pack2_relu(v[2 * i], v[2 * i + 1], bf16);
 #pragma unroll
         for (int q = 0; q < 2; ++q)
             *reinterpret_cast<uint4*>(sm.a_h + tile_offset(r, c + q * 8, 64)) = make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);

@@ -171,6 +171,15 @@ __device__ __forceinline__ uint32_t pack2_act(float a, float b, bool bf16) {
     const __half2 h = __floats2half2_rn(a, b);
     return *reinterpret_cast<const uint32_t*>(&h);
 }
+// ReLU and the rounding of pack2_act in one packed conversion (cvt.rn.relu: negative results
+// become zero), a in the low half.  Same bits as pack2_act(fmaxf(a, 0), fmaxf(b, 0)) for every
+// non-NaN input.
+__device__ __forceinline__ uint32_t pack2_relu(float a, float b, bool bf16) {
+    uint32_t r;
+    if (bf16) asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+    else asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+    return r;
+}
 __device__ __forceinline__ float from_act(__half h, bool bf16) {
     if (bf16) return __bfloat162float(__ushort_as_bfloat16(__half_as_ushort(h)));
     return __half2float(h);
