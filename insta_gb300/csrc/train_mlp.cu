@@ -172,9 +172,14 @@ __device__ __forceinline__ void epi64(uint32_t tmem_base, uint32_t col, uint8_t*
     for (uint32_t c = c0; c < c0 + 32u; c += 16) {
         float v[16];
         tmem_ld16(lane_addr(tmem_base, col + c), v);
-        if (relu) {
+        if (relu) {   // ReLU inside the packed conversion (cvt.rn.relu)
+            uint32_t p[8];
 #pragma unroll
-            for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
+            for (int i = 0; i < 8; ++i) p[i] = pack2_relu(v[2 * i], v[2 * i + 1], false);
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+                *reinterpret_cast<uint4*>(dst + tile_offset(r, c + 8 * q, 64)) = make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+            continue;
         }
         if (mask) {
             float m[16];
