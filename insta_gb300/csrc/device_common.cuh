@@ -565,8 +565,11 @@ __device__ __forceinline__ void hash_level(const FieldView& fv, const __half2* t
     const uint32_t res = fv.level_res[l], size = fv.level_size[l];
     const bool dense = fv.level_dense[l];
     const __half2* lt = table + fv.level_off[l];
-    a0 = 0.f;
-    a1 = 0.f;
+    // The weights and the weighted sum run as packed FP32 pairs (the two x-neighbours' weights,
+    // the two features), each half with the rounding of the scalar operations, in the same order:
+    // w = (wx * wy) * wz, then a += w * e corner by corner.
+    const float2 wx = make_float2(__fsub_rn(1.f, rx), rx);
+    float2 acc = make_float2(0.f, 0.f);
     if (dense) {
 #pragma unroll
         for (uint32_t c2 = 0; c2 < 4; ++c2) {
@@ -584,30 +587,28 @@ __device__ __forceinline__ void hash_level(const FieldView& fv, const __half2* t
                 e0 = __half22float2(__ldg(lt + i0));
                 e1 = __half22float2(__ldg(lt + i1));
             }
-            const float wy = by ? ry : __fsub_rn(1.f, ry);
-            float w = __fmul_rn(__fsub_rn(1.f, rx), wy);
-            w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
-            a0 = __fadd_rn(a0, __fmul_rn(w, e0.x));
-            a1 = __fadd_rn(a1, __fmul_rn(w, e0.y));
-            w = __fmul_rn(rx, wy);
-            w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
-            a0 = __fadd_rn(a0, __fmul_rn(w, e1.x));
-            a1 = __fadd_rn(a1, __fmul_rn(w, e1.y));
+            const float wy = by ? ry : __fsub_rn(1.f, ry), wz = bz ? rz : __fsub_rn(1.f, rz);
+            const float2 w = __fmul2_rn(__fmul2_rn(wx, make_float2(wy, wy)), make_float2(wz, wz));
+            acc = __fadd2_rn(acc, __fmul2_rn(make_float2(w.x, w.x), e0));
+            acc = __fadd2_rn(acc, __fmul2_rn(make_float2(w.y, w.y), e1));
         }
+        a0 = acc.x;
+        a1 = acc.y;
         return;
     }
 #pragma unroll
-    for (uint32_t c = 0; c < 8; ++c) {
-        uint32_t bx = c & 1u, by = (c >> 1) & 1u, bz = (c >> 2) & 1u;
-        float w = bx ? rx : __fsub_rn(1.f, rx);
-        w = __fmul_rn(w, by ? ry : __fsub_rn(1.f, ry));
-        w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
-        uint32_t cx = gx + bx, cy = gy + by, cz = gz + bz;
-        const uint32_t idx = ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
-        float2 e = __half22float2(__ldg(lt + idx));
-        a0 = __fadd_rn(a0, __fmul_rn(w, e.x));
-        a1 = __fadd_rn(a1, __fmul_rn(w, e.y));
+    for (uint32_t c2 = 0; c2 < 4; ++c2) {
+        const uint32_t by = c2 & 1u, bz = c2 >> 1;
+        const float wy = by ? ry : __fsub_rn(1.f, ry), wz = bz ? rz : __fsub_rn(1.f, rz);
+        const float2 w = __fmul2_rn(__fmul2_rn(wx, make_float2(wy, wy)), make_float2(wz, wz));
+        const uint32_t hyz = ((gy + by) * 2654435761u) ^ ((gz + bz) * 805459861u);
+        const uint32_t idx0 = (gx ^ hyz) & (size - 1u), idx1 = ((gx + 1u) ^ hyz) & (size - 1u);
+        const float2 e0 = __half22float2(__ldg(lt + idx0)), e1 = __half22float2(__ldg(lt + idx1));
+        acc = __fadd2_rn(acc, __fmul2_rn(make_float2(w.x, w.x), e0));
+        acc = __fadd2_rn(acc, __fmul2_rn(make_float2(w.y, w.y), e1));
     }
+    a0 = acc.x;
+    a1 = acc.y;
 }
 
 // Real spherical harmonics up to degree 4 of the unwarped direction (16 values).
