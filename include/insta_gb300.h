@@ -388,6 +388,7 @@ typedef struct insta_train_loss_desc {
     float* error_map;                 /* f32[n_images][res_y][res_x]: each kept ray's mean loss added
                                          bilinearly at its image position, or NULL = off             */
     uint32_t error_map_res[2];        /* x, y (each >= 2, no larger than the images)                 */
+    uint32_t error_map_images;        /* images of the error map; rays of other images deposit nothing */
     const float* image_xy;            /* f32[2] position in [0, 1]^2 of the ray's pixel              */
     const uint32_t* image_index;      /* the ray's training image                                     */
 } insta_train_loss_desc;

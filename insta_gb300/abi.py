@@ -72,7 +72,7 @@ class TrainLossDesc(C.Structure):
                 ("ray_indices", C.c_void_p), ("numsteps", C.c_void_p), ("coords", C.c_void_p), ("network_output", C.c_void_p),
                 ("numsteps_counter", C.c_void_p), ("coords_out", C.c_void_p), ("dloss_doutput", C.c_void_p),
                 ("loss_output", C.c_void_p), ("pdf", C.c_void_p), ("error_map", C.c_void_p), ("error_map_res", C.c_uint32 * 2),
-                ("image_xy", C.c_void_p), ("image_index", C.c_void_p)]
+                ("error_map_images", C.c_uint32), ("image_xy", C.c_void_p), ("image_index", C.c_void_p)]
 
 
 class ExtraDimsGradientDesc(C.Structure):

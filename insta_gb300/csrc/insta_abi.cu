@@ -1806,6 +1806,7 @@ int insta_train_loss(insta_ctx* ctx, const insta_train_loss_desc* d) {
             if (!d->image_xy || !d->image_index) fail(INSTA_ERR_INVALID_ARG, "the error map needs image_xy and image_index");
             if (d->error_map_res[0] < 2 || d->error_map_res[1] < 2 || (uint64_t)d->error_map_res[0] * d->error_map_res[1] > (1ull << 26))
                 fail(INSTA_ERR_INVALID_ARG, "error_map_res must be at least 2 x 2 and at most 2^26 cells");
+            if (d->error_map_images == 0) fail(INSTA_ERR_INVALID_ARG, "error_map_images must be positive");
             if ((uintptr_t)d->image_xy & 7) fail(INSTA_ERR_INVALID_ARG, "image_xy must be 8-byte aligned");
         }
         {

@@ -252,7 +252,7 @@ struct TrainLossArgs {
     uint32_t* base_in;   // each kept ray's block start before compaction (for the copy kernel)
     const float* pdf;    // per ray img_pdf * xy_pdf, or null (1)
     float* error_map;    // [images][res_y][res_x] or null
-    uint32_t em_res[2];
+    uint32_t em_res[2], em_images;
     const float* image_xy;
     const uint32_t* image_index;
 };
@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(32) train_loss_kernel(TrainLossArgs a) {
     }
     const float mean_loss = lsum / 3.f;
     if (a.loss_out) a.loss_out[i] = mean_loss / (float)a.n_rays;
-    if (a.error_map) {
+    if (a.error_map && a.image_index[ray] < a.em_images) {
         // the ray's mean loss splatted bilinearly at its image position (texel centres at +0.5);
         // the reference clamps the cell by the image resolution - 2, which equals the map's own
         // bound while the map is no larger than the image
@@ -470,6 +470,7 @@ cudaError_t launch_train_loss(const ::insta_train_loss_desc& d, uint32_t* base_s
     a.numsteps = d.numsteps; a.coords = d.coords; a.out = d.network_output; a.counter = d.numsteps_counter;
     a.coords_out = d.coords_out; a.dloss = d.dloss_doutput; a.loss_out = d.loss_output; a.base_in = base_scratch;
     a.pdf = d.pdf; a.error_map = d.error_map; a.em_res[0] = d.error_map_res[0]; a.em_res[1] = d.error_map_res[1];
+    a.em_images = d.error_map_images;
     a.image_xy = d.image_xy; a.image_index = d.image_index;
     if (d.max_rays > 0) {
         // one ray per thread in 32-thread blocks: a batch of a few thousand rays spreads over every SM
@@ -681,11 +682,12 @@ __global__ void __launch_bounds__(256) extra_dims_gradient_kernel(const ::insta_
     const uint32_t i = (uint32_t)(t / ne), k = (uint32_t)(t % ne);
     if (i >= min(*d.rays_counter, d.max_rays)) return;
     const uint32_t count = d.numsteps[2 * i], base = d.numsteps[2 * i + 1];
-    if (count == 0) return;
+    const uint32_t img = d.image_index[d.ray_indices[i]];
+    if (count == 0 || img >= d.n_images) return;   // rays of images outside the gradient add nothing
     const float* g = d.dl_dextra + (size_t)base * ne + k;
     float sum = 0.f;
     for (uint32_t j = 0; j < count; ++j) sum += g[(size_t)j * ne];
-    atomicAdd(d.extra_dims_gradient + (size_t)d.image_index[d.ray_indices[i]] * ne + k, sum);
+    atomicAdd(d.extra_dims_gradient + (size_t)img * ne + k, sum);
 }
 
 cudaError_t launch_extra_dims_gradient(const ::insta_extra_dims_gradient_desc& d, cudaStream_t s) {

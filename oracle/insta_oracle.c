@@ -1316,7 +1316,7 @@ void orc_train_loss(const orc_train_loss_cfg *c, uint32_t n_kept, const float *r
         }
         const float mean_loss = ls / 3.f;
         if (loss_out) loss_out[i] = mean_loss / (float)c->n_rays;
-        if (c->error_map) {
+        if (c->error_map && c->image_index[ray] < c->error_map_images) {
             /* testbed_nerf.cu:1510-1536: bilinear deposit at the ray's image position (xy * res - 0.5
              * is one fused multiply-add in the reference's nvcc build) */
             const float rx = (float)c->error_map_res[0], ry = (float)c->error_map_res[1];

@@ -146,6 +146,7 @@ typedef struct {
     const float *pdf;
     float *error_map;
     uint32_t error_map_res[2];
+    uint32_t error_map_images;
     const float *image_xy;
     const uint32_t *image_index;
 } orc_train_loss_cfg;

@@ -237,8 +237,8 @@ class TrainLossCfg(C.Structure):
                 ("depth_loss_type", C.c_int), ("srgb_targets", C.c_int), ("train_in_linear_colors", C.c_int),
                 ("penalize_density", C.c_int), ("loss_scale", C.c_float), ("depth_supervision_lambda", C.c_float),
                 ("seg_mask_supervision_lambda", C.c_float), ("near_distance", C.c_float), ("beta", C.c_float),
-                ("pdf", C.c_void_p), ("error_map", C.c_void_p), ("error_map_res", C.c_uint32 * 2), ("image_xy", C.c_void_p),
-                ("image_index", C.c_void_p)]
+                ("pdf", C.c_void_p), ("error_map", C.c_void_p), ("error_map_res", C.c_uint32 * 2),
+                ("error_map_images", C.c_uint32), ("image_xy", C.c_void_p), ("image_index", C.c_void_p)]
 
 
 def train_loss(cfg: dict, rays, target, ray_indices, numsteps, coords, network_output, background=None, exposure=None,
@@ -261,6 +261,7 @@ def train_loss(cfg: dict, rays, target, ray_indices, numsteps, coords, network_o
         assert error_map.dtype == np.float32 and error_map.flags.c_contiguous and error_map.ndim == 3
         c.error_map = error_map.ctypes.data
         c.error_map_res[0], c.error_map_res[1] = error_map.shape[2], error_map.shape[1]
+        c.error_map_images = error_map.shape[0]
         keep += [np.ascontiguousarray(image_xy, np.float32), np.ascontiguousarray(image_index, np.uint32)]
         c.image_xy, c.image_index = keep[-2].ctypes.data, keep[-1].ctypes.data
     f32 = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)

@@ -168,6 +168,7 @@ def test_extra_dims_gradient(ctx, field, oracle, tcgen05):
     bases = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint32)
     perm = rng.permutation(n_rays).astype(np.uint32)
     img = rng.integers(0, n_img, n_rays).astype(np.uint32)
+    img[perm[3]] = n_img + 2                                   # a ray of an image outside the gradient adds nothing
     kept = n_rays - 7                                          # the last rays were not kept
     out = torch.zeros((n_img, 16), dtype=torch.float32, device="cuda")
     i32 = lambda a: dev(a.view(np.int32))
@@ -176,7 +177,8 @@ def test_extra_dims_gradient(ctx, field, oracle, tcgen05):
     ctx.sync()
     ref = np.zeros((n_img, 16), np.float64)
     for i in range(kept):
-        ref[img[perm[i]]] += got[bases[i]:bases[i] + counts[i]].sum(0)
+        if img[perm[i]] < n_img:
+            ref[img[perm[i]]] += got[bases[i]:bases[i] + counts[i]].sum(0)
     assert np.abs(out.cpu().numpy() - ref).max() <= 1e-5 * np.abs(ref).max()
 
 
@@ -456,7 +458,9 @@ def test_train_loss_error_map_and_pdf(ctx, oracle):
     pdf = rng.uniform(0.5, 2.0, n).astype(np.float32)
     cfg = loss_cfg(n_rays=n, stride=27, loss_type=4, loss_scale=128.0)
     em_dev = torch.zeros((n_img, ry, rx), dtype=torch.float32, device="cuda")
-    got = run_loss(ctx, b, cfg, extra=dict(image_xy=xy, image_index=img, pdf=pdf), error_map=em_dev, error_map_res=(rx, ry))
+    img[7] = n_img + 4                                   # an image outside the map deposits nothing
+    got = run_loss(ctx, b, cfg, extra=dict(image_xy=xy, image_index=img, pdf=pdf), error_map=em_dev, error_map_res=(rx, ry),
+                   error_map_images=n_img)
     em_ref = np.zeros((n_img, ry, rx), np.float32)
     ref = oracle.train_loss(cfg, **b, pdf=pdf, error_map=em_ref, image_xy=xy, image_index=img)
     check_blocks(got, ref, n)
