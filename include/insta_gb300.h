@@ -31,10 +31,17 @@
  *   insta_field_eval            NerfNetwork::inference_mixed_precision_impl (NGP/nerf_network.h:159-232)
  *   insta_field_eval_training   the same with the training weights (use_inference_params = false)
  *   insta_field_backward        NerfNetwork's forward/backward for training (NGP/nerf_network.h:296-383)
+ *   insta_field_backward_ex     the same, also returning the expression-dim input gradients
+ *                               (instant-ngp/src/testbed_nerf.cu:3364-3380)
+ *   insta_extra_dims_gradient   compute_extra_dims_gradient_train_nerf (instant-ngp/src/testbed_nerf.cu:1756-1791)
  *   insta_adam_step             the Adam optimizer of the trainer (configs/nerf/main.json)
- *   insta_train_set_math        FP32 or TF32 layer products of the backward
- *   insta_train_loss            compute_loss_kernel_train_nerf + fill_rollover (instant-ngp/src/
- *                               testbed_nerf.cu:1305-1644,3298-3362)
+ *   insta_train_set_math        FP32, TF32 or the library's tcgen05 layer products of the backward
+ *   insta_train_loss            compute_loss_kernel_train_nerf (with the error map) + fill_rollover
+ *                               (instant-ngp/src/testbed_nerf.cu:1305-1644,3298-3362)
+ *   insta_training_pixels       image_idx + nerf_random_image_pos_training + the background draw of
+ *                               generate_training_samples_nerf (instant-ngp/src/testbed_nerf.cu:1013-1105,1140-1144)
+ *   insta_error_map_cdf         construct_cdf_2d / construct_cdf_1d + the image CDF of train_nerf_step
+ *                               (instant-ngp/src/testbed_nerf.cu:1967-2020,3010-3041)
  *   insta_render                Testbed::render_nerf -> NerfTracer::init_rays_from_camera/trace +
  *                               shade_kernel_nerf (instant-ngp/src/testbed_nerf.cu:2030-2244,2320-2460)
  *   insta_march_debug           the sample positions advance_pos_nerf + generate_next_nerf_network_inputs
