@@ -1612,10 +1612,10 @@ bool train_mlp_plan(const FieldLayout& L, TrainMlpPlan& P, TrainImageList& I) {
     P.n_rgb = (uint32_t)L.n_rgb;
     P.kd = L.layer_k[0];
     if (P.kd % 16 || P.kd > 64) return false;
-    uint32_t off = 0, col = 96;
-    auto add = [&](uint32_t n, uint32_t k, uint64_t w_off, uint32_t rows, uint32_t cols, uint32_t col0, uint32_t tr) {
+    uint32_t off = 0, col = 128;   // TMEM: columns 0..127 the two slots' working accumulators
+    auto add = [&](uint32_t n, uint32_t k, uint64_t w_off, uint32_t rows, uint32_t cols, uint32_t tr) {
         TrainImageTile& T = I.tile[I.n_tiles++];
-        T = TrainImageTile{off, n, k, w_off, rows, cols, 0u, col0, tr};
+        T = TrainImageTile{off, n, k, w_off, rows, cols, 0u, 0u, tr};
         const uint32_t at = off;
         off = (off + n * k * 2 + 127) / 128 * 128;
         return at;
@@ -1625,19 +1625,14 @@ bool train_mlp_plan(const FieldLayout& L, TrainMlpPlan& P, TrainImageList& I) {
         Y.n_out = L.layer_n[l];
         Y.n_in = L.layer_k[l];
         if (Y.n_in > 64 || (Y.n_out != 16 && Y.n_out != 64)) return false;
+        if (l == L.n_density && Y.n_in != 32) return false;   // the colour input [density output | SH]
         Y.k_pad = (Y.n_in + 15) / 16 * 16;
         Y.w_off = L.layer_off[l];
         Y.n_out_real = l == nl - 1 ? 3u : Y.n_out;
-        if (l == L.n_density) {
-            Y.fwd_img = add(Y.n_out, 16, Y.w_off, Y.n_out, Y.n_in, 0, 0);
-            Y.fwd_img2 = add(Y.n_out, 16, Y.w_off, Y.n_out, Y.n_in, 16, 0);
-            Y.bwd_n = 16;   // only the density-output part of the colour input has a gradient to pass on
-        } else {
-            Y.fwd_img = add(Y.n_out, Y.k_pad, Y.w_off, Y.n_out, Y.n_in, 0, 0);
-            Y.bwd_n = Y.k_pad;
-        }
-        Y.bwd_img = add(Y.bwd_n, Y.n_out, Y.w_off, Y.n_out, Y.n_in, 0, 1);
-        Y.kp_blk = Y.n_in <= 32 ? 32u : 64u;
+        Y.fwd_img = add(Y.n_out, Y.k_pad, Y.w_off, Y.n_out, Y.n_in, 0);
+        // only the density-output part of the colour input has a gradient to pass on
+        Y.bwd_n = l == L.n_density ? 16u : Y.k_pad;
+        Y.bwd_img = add(Y.bwd_n, Y.n_out, Y.w_off, Y.n_out, Y.n_in, 1);
         Y.dw_col = col;
         col = (col + Y.n_out + 31) / 32 * 32;
     }
@@ -1646,14 +1641,13 @@ bool train_mlp_plan(const FieldLayout& L, TrainMlpPlan& P, TrainImageList& I) {
     auto r1k = [](uint32_t b) { return (b + 1023u) & ~1023u; };
     uint32_t o = 1024;
     P.s_img = o; o = r1k(o + P.img_bytes);
-    P.s_x = o; o = r1k(o + 128 * P.kd * 2);
-    P.s_sh = o; o += 128 * 16 * 2;
-    for (int k = 0; k < nl - 2; ++k) { P.s_kept[k] = o; o += 128 * 64 * 2; }
-    P.s_dens = o; o += 128 * 16 * 2;
-    P.s_dy = o; o += 128 * 64 * 2;
-    P.s_bt = o; o += 64 * 128 * 2;
-    P.s_at32 = o; o += 128 * 128 * 2;
-    P.s_at64 = o; o += 128 * 128 * 2;
+    for (int s = 0; s < 2; ++s) {
+        P.s_x[s] = o; o = r1k(o + 128 * P.kd * 2);
+        P.s_rin[s] = o; o += 128 * 32 * 2;
+        for (int k = 0; k < nl - 2; ++k) { P.s_kept[s][k] = o; o += 128 * 64 * 2; }
+        P.s_dy[s] = o; o += 128 * 64 * 2;
+    }
+    o += 16384;   // tail
     P.smem_bytes = o;
     return o <= 227u * 1024u;
 }

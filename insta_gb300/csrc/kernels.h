@@ -217,17 +217,20 @@ size_t train_scratch_floats(const TrainShape& t, uint32_t n);
 struct TrainMlpLayer {
     uint32_t n_out, n_in, k_pad;   // forward N, input width, forward K (n_in rounded to 16)
     uint64_t w_off;                // the layer's [n_out][n_in] weights in the parameters
-    uint32_t fwd_img, fwd_img2;    // image offsets of the forward B tile(s) (colour layer 0: two K = 16 halves)
+    uint32_t fwd_img;              // image offset of the forward B tile (N = n_out, K = k_pad)
     uint32_t bwd_img, bwd_n;       // image offset of W^T (N = bwd_n, K = n_out) for dX
-    uint32_t kp_blk;               // input width padded to 32 or 64: the weight gradient's row block
     uint32_t dw_col;               // TMEM column of the weight-gradient accumulator (n_out columns)
     uint32_t n_out_real;           // output rows that carry gradient (3 for the colour output)
 };
+// Shared memory: the weight images, then per tile slot (two) the density input [128][kd], the
+// colour input [128][32], the kept hidden outputs [128][64] and dY [128][64], then a tail that
+// the MN-major weight-gradient operands may read past the last tile without leaving the block's
+// shared memory.
 struct TrainMlpPlan {
     TrainMlpLayer layer[8];
     uint32_t n_density, n_rgb, kd;
     uint32_t img_bytes;
-    uint32_t s_img, s_x, s_sh, s_kept[8], s_dens, s_dy, s_bt, s_at32, s_at64, smem_bytes;   // s_at64 = s_at32 + 32 KiB
+    uint32_t s_img, s_x[2], s_rin[2], s_kept[2][6], s_dy[2], smem_bytes;
 };
 struct TrainMlpArgs {
     TrainMlpPlan plan;

@@ -4,17 +4,24 @@
 // operands and FP32 accumulation in TMEM, the activations kept in shared memory between the
 // forward and the backward, the ReLU derivatives applied in the epilogues.
 //
-// Per tile (one persistent CTA of 256 threads per SM, the whole TMEM allocated):
+// One persistent CTA per SM (the whole TMEM allocated) takes two tiles at a time and pipelines
+// them: 512 epilogue threads alternate between the two tiles' epilogues, and one more warp issues
+// each tile's next MMAs as soon as that tile's epilogue has written their operands, so the tensor
+// core runs one tile's step while the epilogue threads work on the other's.  One thread issues
+// every MMA, so the two tiles' additions into the shared weight-gradient accumulators happen in
+// issue order.
+//
+// Per tile, steps 0 .. n-1 are the forward and n .. 2n-1 the backward of the n layers:
 //   forward   X -> H_1 .. H_n -> D (density MLP), [D | SH] -> C_1 .. C_m -> Y (colour MLP), every
 //             hidden output rounded to FP16 and kept in shared memory;
 //   backward  for each layer from the last: dX = dY W (M = 128 samples) into TMEM, masked by the
 //             layer input's ReLU (X > 0) in the epilogue, and dW^T += X^T dY.  The weight
-//             gradient contracts over samples, so its M is the layer's input width; to keep
-//             M = 128 the tile's samples are split into 128 / K_in blocks and A = X^T is laid
-//             out block-diagonally ([X_1^T 0; 0 X_2^T] for K_in = 64): row block b of the
-//             accumulator sums the samples of block b, and the blocks are added when the
-//             accumulators are flushed.  The dW accumulators stay in TMEM over all the tiles a
-//             CTA takes and are added to the gradient once at the end.
+//             gradient contracts over the tile's samples: its A operand is the layer's input
+//             tile read as an MN-major matrix (features along M, samples along K) and its B
+//             operand the dY tile read the same way, so neither is transposed in shared memory.
+//             With M = 128 the accumulator rows past the layer's input width hold products of
+//             neighbouring data and are never read.  The dW accumulators stay in TMEM over all
+//             the tiles a CTA takes and are added to the gradient once at the end.
 //   dX of the first layer goes to global memory (FP32) for the hash-table backward.
 #include <cstdint>
 
@@ -26,60 +33,35 @@ namespace insta {
 
 namespace {
 
-constexpr uint32_t kThreads = 256;
+constexpr uint32_t kEpiThreads = 512;              // four warpgroups: each epilogue splits a row's columns four ways
+constexpr uint32_t kThreads = kEpiThreads + 32;    // and one warp that issues the MMAs
 
 struct TrainCtl {
-    uint64_t bar_mma;
+    uint64_t bar_mma[2];   // per tile slot: the MMA warp's commit of the slot's current step
+    uint64_t opready[2];   // per tile slot: the epilogue threads have written the next step's operands
     uint64_t bar_w;
     uint32_t tmem_base;
 };
+
+// The epilogue threads (not the MMA warp) meet at named barrier 1; true when every one passed true.
+__device__ __forceinline__ bool epi_sync_and(bool v) {
+    uint32_t r;
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n barrier.cta.red.and.pred q, 1, %2, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+                 : "=r"(r) : "r"(v ? 1u : 0u), "n"(kEpiThreads) : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 
 __device__ __forceinline__ uint32_t lane_addr(uint32_t tmem_base, uint32_t col) {
     return tmem_base + ((((uint32_t)threadIdx.x / 32u) % 4u) * 32u << 16) + col;
 }
 
-// One chain of MMAs into TMEM column `col` (N columns), A and B K-major no-swizzle tiles in shared
-// memory with their own K (so their own 8-row-group stride).  `acc` = accumulate into what is
-// there already for the first instruction.
-struct Mma {
-    const uint8_t* a;
-    uint32_t a_k;   // K of the A tile (elements)
-    const uint8_t* b;
-    uint32_t b_k;   // K of the B tile
-    uint32_t k0;    // first K element of this product in both tiles
-    uint32_t k;     // K elements of this product (multiple of 16)
-    uint32_t n;     // N
-    uint32_t col;   // TMEM column of the accumulator
-    bool acc;
-};
-
-__device__ __forceinline__ void issue(uint32_t tmem_base, const Mma& m) {
-    const uint32_t idesc = idesc_f16(128, m.n, false);
-    const uint32_t a0 = smem_addr(m.a), b0 = smem_addr(m.b);
-    const uint32_t sbo_a = (m.a_k / 8) * 128, sbo_b = (m.b_k / 8) * 128;
-    for (uint32_t ks = 0; ks < m.k / 16; ++ks) {
-        const uint32_t kb = (m.k0 / 16 + ks) * 256;   // two core matrices (16 elements) per step
-        umma_f16(tmem_base + m.col, smem_desc(a0 + kb, 128, sbo_a), smem_desc(b0 + kb, 128, sbo_b), idesc, (m.acc || ks) ? 1u : 0u);
-    }
-}
-
-// Run up to two chains, then wait for them: the generic-proxy writes of the operands are fenced
-// for the tensor core, one thread issues, warp 0 waits on the commit, the CTA syncs.
-__device__ __forceinline__ bool run(TrainCtl& ctl, const Mma* ms, int n, uint32_t& phase) {
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        tc_fence_after();
-        for (int i = 0; i < n; ++i) issue(ctl.tmem_base, ms[i]);
-        umma_commit(&ctl.bar_mma);
-    }
-    bool ok = true;
-    if (threadIdx.x < 32u) ok = mbar_wait(&ctl.bar_mma, phase);
-    ok = __syncthreads_and(ok ? 1 : 0) != 0;
-    phase ^= 1u;
-    tc_fence_after();
-    return ok;
+// Instruction descriptor of the weight-gradient product: FP16, both operands MN-major.
+__host__ __device__ constexpr uint32_t idesc_f16_mn(uint32_t M, uint32_t N) {
+    return idesc_f16(M, N, false) | (1u << 15) | (1u << 16);
 }
 
 __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
@@ -113,63 +95,13 @@ __device__ __forceinline__ void load16(const uint8_t* tile, uint32_t K, uint32_t
     }
 }
 
-// Core-matrix transposes (a core matrix: 8 rows of 16 bytes, 8 x 8 FP16): a warp moves four at a
-// time with one ldmatrix.trans / stmatrix pair, lane l addressing row l % 8 of matrix l / 8 in
-// both; the registers carry the transposed fragments, so the stored matrix is the loaded one
-// transposed.  Conflict-free: each group of 8 lanes reads or writes 128 contiguous bytes.
-__device__ __forceinline__ void cm_transpose4(uint32_t src_row, uint32_t dst_row) {
-    uint32_t r0, r1, r2, r3;
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(src_row) : "memory");
-    asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1,%2,%3,%4};" ::"r"(dst_row), "r"(r0), "r"(r1), "r"(r2), "r"(r3)
-                 : "memory");
-}
-
-// Job j (of n_jobs, a multiple of 4) moves core matrix map(j).src to map(j).dst transposed (byte
-// offsets from the tiles' shared-memory addresses); each warp takes four jobs per step.
-template <typename Map>
-__device__ __forceinline__ void cm_transpose(uint32_t src_base, uint32_t dst_base, uint32_t n_jobs, Map map) {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    for (uint32_t g = warp * 4u; g < n_jobs; g += 4u * (kThreads / 32u)) {
-        uint32_t so, d_o;
-        map(g + (lane >> 3), so, d_o);
-        cm_transpose4(src_base + so + (lane & 7u) * 16u, dst_base + d_o + (lane & 7u) * 16u);
-    }
-}
-
-// dst[n rows][K = 128 samples] <- src[128 samples][K = n] transposed (n a multiple of 8).
-__device__ __forceinline__ void transpose_rows(uint8_t* dst, const uint8_t* src, uint32_t n) {
-    const uint32_t gk = n / 8u;
-    cm_transpose(smem_addr(src), smem_addr(dst), 16u * gk, [gk](uint32_t j, uint32_t& so, uint32_t& d_o) {
-        const uint32_t i = j & 15u, c = j >> 4;   // sample group, output group
-        so = (i * gk + c) * 128u;
-        d_o = (c * 16u + i) * 128u;
-    });
-}
-
-// Block-diagonal X^T: dst[128 rows][K = 128 samples], row b * kp + f = feature f of the samples of
-// block b ([b kp, b kp + kp)), from src[128 samples][K = src_k] columns [0, width) placed at
-// features [f0, f0 + width).  Only the diagonal blocks are written: the rest of dst stays zero
-// (cleared once per launch; each kp has its own dst), and features a narrower layer does not
-// write hold another layer's values, which only reach accumulator rows that are never read.
-__device__ __forceinline__ void transpose_blocks(uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t src_k, uint32_t kp,
-                                                 uint32_t f0 = 0) {
-    const uint32_t gw = width / 8u, gs = src_k / 8u, gb = kp / 8u, g0 = f0 / 8u;
-    cm_transpose(smem_addr(src), smem_addr(dst), 16u * gw, [=](uint32_t j, uint32_t& so, uint32_t& d_o) {
-        const uint32_t i = j & 15u, c = j >> 4;   // sample group, feature group
-        const uint32_t b = (8u * i) / kp;
-        so = (i * gs + c) * 128u;
-        d_o = ((b * gb + g0 + c) * 16u + i) * 128u;
-    });
-}
-
-// Epilogue of a 64-wide accumulator at column `col`: warpgroup g takes columns [32 g, 32 g + 32)
-// of its row; optionally ReLU (forward) or the mask of a kept ReLU output (backward), FP16 into
-// the K = 64 tile `dst`.
+// Epilogue of a 64-wide accumulator at column `col`: warpgroup g takes columns [16 g, 16 g + 16)
+// of its row; ReLU (forward) or the mask of a kept ReLU output (backward), FP16 into the K = 64
+// tile `dst`.
 __device__ __forceinline__ void epi64(uint32_t tmem_base, uint32_t col, uint8_t* dst, bool relu, const uint8_t* mask) {
-    const uint32_t r = threadIdx.x & 127u, c0 = (threadIdx.x >> 7) * 32u;
-#pragma unroll 1
-    for (uint32_t c = c0; c < c0 + 32u; c += 16) {
+    const uint32_t r = threadIdx.x & 127u, c0 = (threadIdx.x >> 7) * 16u;
+    {
+        const uint32_t c = c0;
         float v[16];
         tmem_ld16(lane_addr(tmem_base, col + c), v);
         if (relu) {   // ReLU inside the packed conversion (cvt.rn.relu)
@@ -179,7 +111,7 @@ __device__ __forceinline__ void epi64(uint32_t tmem_base, uint32_t col, uint8_t*
 #pragma unroll
             for (int q = 0; q < 2; ++q)
                 *reinterpret_cast<uint4*>(dst + tile_offset(r, c + 8 * q, 64)) = make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
-            continue;
+            return;
         }
         if (mask) {
             float m[16];
@@ -191,6 +123,33 @@ __device__ __forceinline__ void epi64(uint32_t tmem_base, uint32_t col, uint8_t*
     }
 }
 
+// Shared-memory tiles of one slot.
+struct SlotTiles {
+    uint8_t* x;       // [128][kd] density input
+    uint8_t* rin;     // [128][32] colour input: density output (columns 0..15), SH (16..31)
+    uint8_t* kept[6]; // [128][64] hidden outputs
+    uint8_t* dy;      // [128][<= 64] gradient w.r.t. the current layer's output
+};
+
+__device__ __forceinline__ SlotTiles slot_tiles(uint8_t* smem, const TrainMlpPlan& P, uint32_t s) {
+    SlotTiles t;
+    t.x = smem + P.s_x[s];
+    t.rin = smem + P.s_rin[s];
+    for (int k = 0; k < 6; ++k) t.kept[k] = smem + P.s_kept[s][k];
+    t.dy = smem + P.s_dy[s];
+    return t;
+}
+
+// The input tile of layer l and its K (its width as a K-major operand).
+__device__ __forceinline__ const uint8_t* layer_input(const TrainMlpPlan& P, const SlotTiles& T, int l, uint32_t& k) {
+    const int nd = (int)P.n_density;
+    if (l == 0) { k = P.kd; return T.x; }
+    if (l < nd) { k = 64; return T.kept[l - 1]; }
+    if (l == nd) { k = 32; return T.rin; }
+    k = 64;
+    return T.kept[l - 2];
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_constant__ TrainMlpArgs A) {
@@ -198,24 +157,20 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
     const TrainMlpPlan& P = A.plan;
     TrainCtl& ctl = *reinterpret_cast<TrainCtl*>(smem);
     uint8_t* img = smem + P.s_img;
-    uint8_t* xt = smem + P.s_x;      // [128][kd] layer input of the density MLP
-    uint8_t* sh = smem + P.s_sh;     // [128][16] SH of the direction
-    uint8_t* dens = smem + P.s_dens; // [128][16] density output (colour input part 1)
-    uint8_t* dy = smem + P.s_dy;     // [128][<= 64] gradient w.r.t. the current layer's output
-    uint8_t* bt = smem + P.s_bt;     // [<= 64][128] the same transposed (B of the weight gradient)
-    uint8_t* at32 = smem + P.s_at32; // [128][128] block-diagonal X^T (A of the weight gradient), blocks of 32
-    uint8_t* at64 = smem + P.s_at64; // the same with blocks of 64
     const uint32_t r = threadIdx.x & 127u, wg = threadIdx.x >> 7;
-    const uint32_t n_tiles = (A.n + 127u) / 128u;
+    const uint32_t n_tiles = (A.n + 127u) / 128u, n_pairs = (n_tiles + 1u) / 2u;
     const bool backward = A.dl_dout != nullptr;
+    const int nd = (int)P.n_density, nl = (int)(P.n_density + P.n_rgb);
+    const int n_steps = backward ? 2 * nl : nl;
     if (threadIdx.x == 0) {
-        mbar_init(&ctl.bar_mma, 1);
+        mbar_init(&ctl.bar_mma[0], 1);
+        mbar_init(&ctl.bar_mma[1], 1);
+        mbar_init(&ctl.opready[0], kEpiThreads);
+        mbar_init(&ctl.opready[1], kEpiThreads);
         mbar_init(&ctl.bar_w, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < 2u * 128u * 128u * 2u / 16u; i += kThreads)   // both X^T tiles (adjacent)
-        reinterpret_cast<uint4*>(at32)[i] = make_uint4(0u, 0u, 0u, 0u);
     if (threadIdx.x < 32) tmem_alloc(&ctl.tmem_base, 512);
     if (threadIdx.x == 0) bulk_load(img, A.images, P.img_bytes, &ctl.bar_w);
     bool ok = mbar_wait(&ctl.bar_w, 0);
@@ -223,157 +178,230 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
     ok = __syncthreads_and(ok ? 1 : 0) != 0;   // uniform: the tile loop holds CTA barriers
     tc_fence_after();
     const uint32_t tmem = ctl.tmem_base;
-    uint32_t phase = 0;
-    bool first = true;   // the weight-gradient accumulators start from zero at the CTA's first tile
-    const int nd = (int)P.n_density, nl = (int)(P.n_density + P.n_rgb);
-    for (uint32_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
-        const uint32_t s = t * 128u + r;
-        const bool valid = s < A.n;
-        // ---- inputs: the encoding (FP32 -> FP16) split by columns, SH by warpgroup 0
-        {
-            const uint32_t half = P.kd / 2u;
-            for (uint32_t c = wg * half; c < wg * half + half; c += 8) {
-                float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                if (valid) {
-                    const float4* src = reinterpret_cast<const float4*>(A.xd + (size_t)s * P.kd + c);
-                    const float4 p0 = __ldg(src), p1 = __ldg(src + 1);
-                    v[0] = p0.x; v[1] = p0.y; v[2] = p0.z; v[3] = p0.w; v[4] = p1.x; v[5] = p1.y; v[6] = p1.z; v[7] = p1.w;
-                }
-                *reinterpret_cast<uint4*>(xt + tile_offset(r, c, P.kd)) =
-                    make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]), pack_h2(v[6], v[7]));
+    const SlotTiles T[2] = {slot_tiles(smem, P, 0), slot_tiles(smem, P, 1)};
+    uint32_t phase[2] = {0u, 0u}, ready_phase[2] = {0u, 0u};
+    uint32_t dw_started = 0;   // layers whose weight-gradient accumulator holds a value (the issuing thread's)
+    const bool mma_warp = threadIdx.x >= kEpiThreads;
+
+    // The MMAs of step k of slot s, then its commit (the MMA warp's first thread, once the slot's
+    // operands are published).
+    auto issue = [&](uint32_t s, int k) {
+        if (threadIdx.x != kEpiThreads) return;
+        const SlotTiles& S = T[s];
+        const uint32_t d_col = tmem + s * 64u;
+        if (k < nl) {
+            const TrainMlpLayer& L = P.layer[k];
+            uint32_t ka;
+            const uint8_t* a = layer_input(P, S, k, ka);
+            const uint32_t idesc = idesc_f16(128, L.n_out, false);
+            const uint32_t a0 = smem_addr(a), b0 = smem_addr(img + L.fwd_img);
+            for (uint32_t ks = 0; ks < L.k_pad / 16u; ++ks)
+                umma_f16(d_col, smem_desc(a0 + ks * 256u, 128, (ka / 8u) * 128u), smem_desc(b0 + ks * 256u, 128, (L.k_pad / 8u) * 128u),
+                         idesc, ks ? 1u : 0u);
+        } else {
+            const int l = 2 * nl - 1 - k;
+            const TrainMlpLayer& L = P.layer[l];
+            // dX = dY W: A = dY (K-major, K = n_out), B = the W^T image (N = bwd_n, K = n_out)
+            {
+                const uint32_t idesc = idesc_f16(128, L.bwd_n, false);
+                const uint32_t a0 = smem_addr(S.dy), b0 = smem_addr(img + L.bwd_img), sbo = (L.n_out / 8u) * 128u;
+                for (uint32_t ks = 0; ks < L.n_out / 16u; ++ks)
+                    umma_f16(d_col, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, ks ? 1u : 0u);
             }
-            if (wg == 0) {
-                float v[16];
+            // dW^T += X^T dY: A = the layer's input tile as an MN-major operand (features along M,
+            // one core matrix of 8 features every 128 B; samples along K, one group of 8 rows every
+            // (w / 8) * 128 B), B = dY the same way; K = 128 samples, 16 per instruction
+            {
+                uint32_t w;
+                const uint8_t* x = layer_input(P, S, l, w);
+                const uint32_t idesc = idesc_f16_mn(128, L.n_out);
+                const uint32_t a0 = smem_addr(x), b0 = smem_addr(S.dy);
+                const uint32_t kgrp_a = (w / 8u) * 128u, kgrp_b = (L.n_out / 8u) * 128u;
+                const bool acc0 = (dw_started >> l) & 1u;
+                for (uint32_t ks = 0; ks < 8u; ++ks)
+                    umma_f16(tmem + L.dw_col, smem_desc(a0 + ks * 2u * kgrp_a, kgrp_a, 128), smem_desc(b0 + ks * 2u * kgrp_b, kgrp_b, 128),
+                             idesc, (acc0 || ks) ? 1u : 0u);
+                dw_started |= 1u << l;
+            }
+        }
+        umma_commit(&ctl.bar_mma[s]);
+    };
+    // Epilogue threads: wait (warp 0 polls, bounded) for slot s's commit, then release the others.
+    auto epi_wait = [&](uint32_t s) -> bool {
+        bool w = true;
+        if (threadIdx.x < 32u) w = mbar_wait(&ctl.bar_mma[s], phase[s]);
+        phase[s] ^= 1u;
+        w = epi_sync_and(w);
+        tc_fence_after();
+        return w;
+    };
+    // Epilogue threads: publish slot s's operands for its next step to the MMA warp.
+    auto publish = [&](uint32_t s) {
+        fence_async_smem();
+        tc_fence_before();
+        mbar_arrive(&ctl.opready[s]);
+    };
+    // The MMA warp: wait (bounded) until slot s's operands are published.
+    auto mma_wait = [&](uint32_t s) -> bool {
+        const bool w = __all_sync(0xffffffffu, mbar_wait(&ctl.opready[s], ready_phase[s]));
+        ready_phase[s] ^= 1u;
+        tc_fence_after();
+        return w;
+    };
+    // The inputs of tile t into slot s: the encoding (FP32 -> FP16) in 8-column chunks dealt to
+    // the four warpgroups, SH by warpgroups 0 and 1 into the colour input's columns 16..31.
+    auto stage = [&](uint32_t s, uint32_t t) {
+        const SlotTiles& S = T[s];
+        const uint32_t row = t * 128u + r;
+        const bool valid = row < A.n;
+        for (uint32_t c = wg * 8u; c < P.kd; c += 32u) {
+            float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (valid) {
+                const float4* src = reinterpret_cast<const float4*>(A.xd + (size_t)row * P.kd + c);
+                const float4 p0 = __ldg(src), p1 = __ldg(src + 1);
+                v[0] = p0.x; v[1] = p0.y; v[2] = p0.z; v[3] = p0.w; v[4] = p1.x; v[5] = p1.y; v[6] = p1.z; v[7] = p1.w;
+            }
+            *reinterpret_cast<uint4*>(S.x + tile_offset(r, c, P.kd)) =
+                make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]), pack_h2(v[6], v[7]));
+        }
+        if (wg < 2) {
+            float v[8];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] = valid ? __ldg(A.xr + (size_t)s * 32 + 16 + i) : 0.f;
-                store16(sh, 16, r, 0, v);
-            }
+            for (int i = 0; i < 8; ++i) v[i] = valid ? __ldg(A.xr + (size_t)row * 32 + 16 + 8 * wg + i) : 0.f;
+            *reinterpret_cast<uint4*>(S.rin + tile_offset(r, 16u + 8u * wg, 32)) =
+                make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]), pack_h2(v[6], v[7]));
         }
-        // ---- forward, the hidden outputs kept
-        Mma m{};
-        for (int l = 0; l < nd - 1; ++l) {
-            const TrainMlpLayer& L = P.layer[l];
-            m = Mma{l == 0 ? xt : smem + P.s_kept[l - 1], l == 0 ? P.kd : 64u, img + L.fwd_img, L.k_pad, 0, L.k_pad, 64, 0, false};
-            ok &= run(ctl, &m, 1, phase);
-            epi64(tmem, 0, smem + P.s_kept[l], true, nullptr);
-        }
-        {
-            const TrainMlpLayer& L = P.layer[nd - 1];
-            m = Mma{nd > 1 ? smem + P.s_kept[nd - 2] : xt, nd > 1 ? 64u : P.kd, img + L.fwd_img, L.k_pad, 0, L.k_pad, 16, 64, false};
-            ok &= run(ctl, &m, 1, phase);
-            if (wg == 0) {
-                float v[16];
-                tmem_ld16(lane_addr(tmem, 64), v);
-                store16(dens, 16, r, 0, v);
-                if (A.out4 && valid) A.out4[(size_t)s * 4 + 3] = __half2float(__float2half_rn(v[0]));
-            }
-        }
-        {
-            const TrainMlpLayer& L = P.layer[nd];
-            const Mma ms[2] = {Mma{dens, 16, img + L.fwd_img, 16, 0, 16, 64, 0, false},
-                               Mma{sh, 16, img + L.fwd_img2, 16, 0, 16, 64, 0, true}};
-            ok &= run(ctl, ms, 2, phase);
-            epi64(tmem, 0, smem + P.s_kept[nd - 1], true, nullptr);
-        }
-        for (int l = nd + 1; l < nl - 1; ++l) {
-            const TrainMlpLayer& L = P.layer[l];
-            m = Mma{smem + P.s_kept[l - 2], 64, img + L.fwd_img, 64, 0, 64, 64, 0, false};
-            ok &= run(ctl, &m, 1, phase);
-            epi64(tmem, 0, smem + P.s_kept[l - 1], true, nullptr);
-        }
-        {
-            const TrainMlpLayer& L = P.layer[nl - 1];
-            m = Mma{smem + P.s_kept[nl - 3], 64, img + L.fwd_img, 64, 0, 64, 16, 64, false};
-            ok &= run(ctl, &m, 1, phase);
-            if (wg == 0 && A.out4) {   // warp-uniform: tcgen05.ld is a whole-warp instruction
-                float v[16];
-                tmem_ld16(lane_addr(tmem, 64), v);
-                if (valid) {
-                    float* o = A.out4 + (size_t)s * 4;
-                    o[0] = __half2float(__float2half_rn(v[0]));
-                    o[1] = __half2float(__float2half_rn(v[1]));
-                    o[2] = __half2float(__float2half_rn(v[2]));
-                }
-            }
-        }
-        if (!backward) continue;
-        // ---- backward.  dY of the colour output: dL/d raw rgb (columns 3..15 zero)
-        if (wg == 0) {
-            float v[16];
-#pragma unroll
-            for (int i = 0; i < 16; ++i) v[i] = (valid && i < 3) ? __ldg(A.dl_dout + (size_t)s * 4 + i) : 0.f;
-            store16(dy, 16, r, 0, v);
-        }
-        // layers from the last: input tile X (kept), its width, dY width = the layer's n_out
-        for (int l = nl - 1; l >= 0; --l) {
-            const TrainMlpLayer& L = P.layer[l];
-            const uint8_t* x;
-            uint32_t xk, xw;
-            if (l == 0) { x = xt; xk = P.kd; xw = P.kd; }
-            else if (l < nd) { x = smem + P.s_kept[l - 1]; xk = 64; xw = 64; }
-            else if (l == nd) { x = nullptr; xk = 32; xw = 32; }   // [density output | SH]
-            else { x = smem + P.s_kept[l - 2]; xk = 64; xw = 64; }
-            __syncthreads();   // dy complete (the previous epilogue or the output gradient)
-            transpose_rows(bt, dy, L.n_out);
-            uint8_t* at = L.kp_blk == 32u ? at32 : at64;
-            if (x) {
-                transpose_blocks(at, x, xw, xk, L.kp_blk);
-            } else {
-                // colour layer 0 (blocks of 32): features 0..15 the density output, 16..31 SH
-                transpose_blocks(at, dens, 16, 16, 32);
-                transpose_blocks(at, sh, 16, 16, 32, 16);
-            }
-            // dX = dY W (into columns 0..), dW^T += X^T dY (its own columns)
-            const Mma ms[2] = {Mma{dy, L.n_out, img + L.bwd_img, L.n_out, 0, L.n_out, L.bwd_n, 0, false},
-                               Mma{at, 128, bt, 128, 0, 128, L.n_out, L.dw_col, !first}};
-            ok &= run(ctl, ms, 2, phase);
-            if (l == 0) {
-                // dL/d encoding, FP32, for the hash-table backward (warpgroup g: half the columns)
-                const uint32_t half = P.kd / 2u;
-                for (uint32_t c = wg * half; c < wg * half + half; c += 8) {
+    };
+    // The epilogue of step k of slot s (tile t).  Warp-uniform conditions only around the TMEM
+    // loads (whole-warp instructions); `valid` guards stores alone.
+    auto epilogue = [&](uint32_t s, uint32_t t, int k) {
+        const SlotTiles& S = T[s];
+        const uint32_t col = s * 64u;
+        const uint32_t row = t * 128u + r;
+        const bool valid = row < A.n;
+        if (k < nl) {
+            if (k < nd - 1) {
+                epi64(tmem, col, S.kept[k], true, nullptr);
+            } else if (k == nd - 1) {
+                if (wg == 0) {   // density output: the colour input's columns 0..15, the raw density
                     float v[16];
-                    tmem_ld16(lane_addr(tmem, c & ~15u), v);   // 16 columns; use the 8 of this chunk
+                    tmem_ld16(lane_addr(tmem, col), v);
+                    store16(S.rin, 32, r, 0, v);
+                    if (A.out4 && valid) A.out4[(size_t)row * 4 + 3] = __half2float(__float2half_rn(v[0]));
+                }
+            } else if (k < nl - 1) {
+                epi64(tmem, col, S.kept[k - 1], true, nullptr);
+            } else if (wg == 0) {   // colour output; and the output gradient dL/d raw rgb (columns 3..15 zero)
+                if (A.out4) {
+                    float v[16];
+                    tmem_ld16(lane_addr(tmem, col), v);
                     if (valid) {
-                        float4* d = reinterpret_cast<float4*>(A.dxd + (size_t)s * P.kd + c);
-                        const uint32_t o = c & 15u;
-                        d[0] = make_float4(v[o], v[o + 1], v[o + 2], v[o + 3]);
-                        d[1] = make_float4(v[o + 4], v[o + 5], v[o + 6], v[o + 7]);
+                        float* o = A.out4 + (size_t)row * 4;
+                        o[0] = __half2float(__float2half_rn(v[0]));
+                        o[1] = __half2float(__float2half_rn(v[1]));
+                        o[2] = __half2float(__float2half_rn(v[2]));
                     }
                 }
-            } else if (l == nd) {
-                // dL/d density output = the colour input's first 16 gradients + the raw density's own
-                if (wg == 0) {
+                if (backward) {
                     float v[16];
-                    tmem_ld16(lane_addr(tmem, 0), v);
-                    if (valid) v[0] += __ldg(A.dl_dout + (size_t)s * 4 + 3);
-                    store16(dy, 16, r, 0, v);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) v[i] = (valid && i < 3) ? __ldg(A.dl_dout + (size_t)row * 4 + i) : 0.f;
+                    store16(S.dy, 16, r, 0, v);
                 }
-            } else {
-                // the input is a kept ReLU output: mask
-                const uint8_t* mk = l < nd ? smem + P.s_kept[l - 1] : smem + P.s_kept[l - 2];
-                epi64(tmem, 0, dy, false, mk);
+            }
+            return;
+        }
+        const int l = 2 * nl - 1 - k;
+        if (l == 0) {
+            // dL/d encoding, FP32, for the hash-table backward (8-column chunks dealt to the warpgroups)
+            for (uint32_t c = wg * 8u; c < P.kd; c += 32u) {
+                float v[16];
+                tmem_ld16(lane_addr(tmem, col + (c & ~15u)), v);   // 16 columns; use the 8 of this chunk
+                if (valid) {
+                    float4* d = reinterpret_cast<float4*>(A.dxd + (size_t)row * P.kd + c);
+                    const uint32_t o = c & 15u;
+                    d[0] = make_float4(v[o], v[o + 1], v[o + 2], v[o + 3]);
+                    d[1] = make_float4(v[o + 4], v[o + 5], v[o + 6], v[o + 7]);
+                }
+            }
+        } else if (l == nd) {
+            // dL/d density output = the colour input's first 16 gradients + the raw density's own
+            if (wg == 0) {
+                float v[16];
+                tmem_ld16(lane_addr(tmem, col), v);
+                if (valid) v[0] += __ldg(A.dl_dout + (size_t)row * 4 + 3);
+                store16(S.dy, 16, r, 0, v);
+            }
+        } else {
+            // the layer's input is a kept ReLU output: mask
+            uint32_t w;
+            const uint8_t* mk = layer_input(P, S, l, w);
+            epi64(tmem, col, S.dy, false, mk);
+        }
+    };
+
+    // Tile pairs (2p, 2p + 1); slot 1 idles for an odd last tile.  Per step the epilogue threads
+    // take slot 0's epilogue, publish its operands, take slot 1's; the MMA warp issues each slot's
+    // next step as soon as it is published.  Every pair starts at a CTA barrier (staging done, the
+    // previous pair finished on both sides, the outcome so far agreed).
+    for (uint32_t p = blockIdx.x; p < n_pairs; p += gridDim.x) {
+        const uint32_t ta = 2u * p, tb = 2u * p + 1u;
+        const bool has_b = tb < n_tiles;
+        if (!mma_warp) {
+            stage(0, ta);
+            if (has_b) stage(1, tb);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        ok = __syncthreads_and(ok ? 1 : 0) != 0;
+        tc_fence_after();
+        if (!ok) break;
+        if (mma_warp) {
+            issue(0, 0);
+            if (has_b) issue(1, 0);
+            for (int k = 0; k + 1 < n_steps && ok; ++k) {
+                ok = mma_wait(0);
+                if (!ok) break;
+                issue(0, k + 1);
+                if (has_b) {
+                    ok = mma_wait(1);
+                    if (!ok) break;
+                    issue(1, k + 1);
+                }
+            }
+        } else {
+            for (int k = 0; k < n_steps; ++k) {
+                ok = epi_wait(0);
+                if (!ok) break;
+                epilogue(0, ta, k);
+                if (k + 1 < n_steps) publish(0);
+                if (has_b) {
+                    ok = epi_wait(1);
+                    if (!ok) break;
+                    epilogue(1, tb, k);
+                    if (k + 1 < n_steps) publish(1);
+                }
             }
         }
-        first = false;
     }
     if (!ok && threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    // ---- flush the weight gradients: accumulator row b * kp + f = feature f of sample block b
-    if (backward && ok && !first) {
+    // ---- flush the weight gradients: accumulator row f = input feature f, column o = output o.
+    // dw_started is thread 0's; the flush runs when the backward ran on at least one tile.
+    if (backward && ok && !mma_warp && n_tiles > blockIdx.x * 2u) {
         for (int l = 0; l < nl; ++l) {
             const TrainMlpLayer& L = P.layer[l];
-            const uint32_t f = r % L.kp_blk;
-            const uint32_t cols = L.n_out, c0 = cols == 64u ? wg * 32u : 0u, c1 = cols == 64u ? c0 + 32u : (wg == 0 ? 16u : 0u);
+            const uint32_t cols = L.n_out, c0 = cols == 64u ? wg * 16u : 0u, c1 = cols == 64u ? c0 + 16u : (wg == 0 ? 16u : 0u);
             for (uint32_t c = c0; c < c1; c += 16) {
                 float v[16];
                 tmem_ld16(lane_addr(tmem, L.dw_col + c), v);
-                if (f < L.n_in) {
+                if (r < L.n_in) {
                     float* g = A.grad + L.w_off;
 #pragma unroll
                     for (int i = 0; i < 16; ++i)
-                        if (c + i < L.n_out_real) atomicAdd(g + (size_t)(c + i) * L.n_in + f, v[i]);
+                        if (c + i < L.n_out_real) atomicAdd(g + (size_t)(c + i) * L.n_in + r, v[i]);
                 }
             }
         }
@@ -405,8 +433,8 @@ cudaError_t launch_train_mlp(const TrainMlpArgs& a, const TrainImageList& images
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint32_t tiles = (a.n + 127u) / 128u;
-    train_mlp_kernel<<<tiles < (uint32_t)sms ? tiles : (uint32_t)sms, kThreads, a.plan.smem_bytes, s>>>(a);
+    const uint32_t pairs = ((a.n + 127u) / 128u + 1u) / 2u;
+    train_mlp_kernel<<<pairs < (uint32_t)sms ? pairs : (uint32_t)sms, kThreads, a.plan.smem_bytes, s>>>(a);
     return cudaGetLastError();
 }
 
