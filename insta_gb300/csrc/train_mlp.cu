@@ -123,32 +123,25 @@ __device__ __forceinline__ void epi64(uint32_t tmem_base, uint32_t col, uint8_t*
     }
 }
 
-// Shared-memory tiles of one slot.
-struct SlotTiles {
-    uint8_t* x;       // [128][kd] density input
-    uint8_t* rin;     // [128][32] colour input: density output (columns 0..15), SH (16..31)
-    uint8_t* kept[6]; // [128][64] hidden outputs
-    uint8_t* dy;      // [128][<= 64] gradient w.r.t. the current layer's output
+// Shared-memory tiles of slot s, addressed through the plan (constant-bank offsets) so that no
+// per-slot table of pointers goes to local memory.
+struct Tiles {
+    uint8_t* smem;
+    const TrainMlpPlan& P;
+    __device__ __forceinline__ uint8_t* x(uint32_t s) const { return smem + P.s_x[s]; }         // [128][kd] density input
+    __device__ __forceinline__ uint8_t* rin(uint32_t s) const { return smem + P.s_rin[s]; }     // [128][32] density output | SH
+    __device__ __forceinline__ uint8_t* kept(uint32_t s, int k) const { return smem + P.s_kept[s][k]; }   // [128][64]
+    __device__ __forceinline__ uint8_t* dy(uint32_t s) const { return smem + P.s_dy[s]; }       // [128][<= 64] dL/d output
+    // The input tile of layer l and its K (its width as a K-major operand).
+    __device__ __forceinline__ const uint8_t* input(uint32_t s, int l, uint32_t& k) const {
+        const int nd = (int)P.n_density;
+        if (l == 0) { k = P.kd; return x(s); }
+        if (l < nd) { k = 64; return kept(s, l - 1); }
+        if (l == nd) { k = 32; return rin(s); }
+        k = 64;
+        return kept(s, l - 2);
+    }
 };
-
-__device__ __forceinline__ SlotTiles slot_tiles(uint8_t* smem, const TrainMlpPlan& P, uint32_t s) {
-    SlotTiles t;
-    t.x = smem + P.s_x[s];
-    t.rin = smem + P.s_rin[s];
-    for (int k = 0; k < 6; ++k) t.kept[k] = smem + P.s_kept[s][k];
-    t.dy = smem + P.s_dy[s];
-    return t;
-}
-
-// The input tile of layer l and its K (its width as a K-major operand).
-__device__ __forceinline__ const uint8_t* layer_input(const TrainMlpPlan& P, const SlotTiles& T, int l, uint32_t& k) {
-    const int nd = (int)P.n_density;
-    if (l == 0) { k = P.kd; return T.x; }
-    if (l < nd) { k = 64; return T.kept[l - 1]; }
-    if (l == nd) { k = 32; return T.rin; }
-    k = 64;
-    return T.kept[l - 2];
-}
 
 }  // namespace
 
@@ -178,8 +171,8 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
     ok = __syncthreads_and(ok ? 1 : 0) != 0;   // uniform: the tile loop holds CTA barriers
     tc_fence_after();
     const uint32_t tmem = ctl.tmem_base;
-    const SlotTiles T[2] = {slot_tiles(smem, P, 0), slot_tiles(smem, P, 1)};
-    uint32_t phase[2] = {0u, 0u}, ready_phase[2] = {0u, 0u};
+    const Tiles T{smem, P};
+    uint32_t phase = 0u, ready_phase = 0u;   // bit s: the parity to wait for on slot s's barrier
     uint32_t dw_started = 0;   // layers whose weight-gradient accumulator holds a value (the issuing thread's)
     const bool mma_warp = threadIdx.x >= kEpiThreads;
 
@@ -187,12 +180,11 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
     // operands are published).
     auto issue = [&](uint32_t s, int k) {
         if (threadIdx.x != kEpiThreads) return;
-        const SlotTiles& S = T[s];
         const uint32_t d_col = tmem + s * 64u;
         if (k < nl) {
             const TrainMlpLayer& L = P.layer[k];
             uint32_t ka;
-            const uint8_t* a = layer_input(P, S, k, ka);
+            const uint8_t* a = T.input(s, k, ka);
             const uint32_t idesc = idesc_f16(128, L.n_out, false);
             const uint32_t a0 = smem_addr(a), b0 = smem_addr(img + L.fwd_img);
             for (uint32_t ks = 0; ks < L.k_pad / 16u; ++ks)
@@ -204,7 +196,7 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
             // dX = dY W: A = dY (K-major, K = n_out), B = the W^T image (N = bwd_n, K = n_out)
             {
                 const uint32_t idesc = idesc_f16(128, L.bwd_n, false);
-                const uint32_t a0 = smem_addr(S.dy), b0 = smem_addr(img + L.bwd_img), sbo = (L.n_out / 8u) * 128u;
+                const uint32_t a0 = smem_addr(T.dy(s)), b0 = smem_addr(img + L.bwd_img), sbo = (L.n_out / 8u) * 128u;
                 for (uint32_t ks = 0; ks < L.n_out / 16u; ++ks)
                     umma_f16(d_col, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, ks ? 1u : 0u);
             }
@@ -213,9 +205,9 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
             // (w / 8) * 128 B), B = dY the same way; K = 128 samples, 16 per instruction
             {
                 uint32_t w;
-                const uint8_t* x = layer_input(P, S, l, w);
+                const uint8_t* x = T.input(s, l, w);
                 const uint32_t idesc = idesc_f16_mn(128, L.n_out);
-                const uint32_t a0 = smem_addr(x), b0 = smem_addr(S.dy);
+                const uint32_t a0 = smem_addr(x), b0 = smem_addr(T.dy(s));
                 const uint32_t kgrp_a = (w / 8u) * 128u, kgrp_b = (L.n_out / 8u) * 128u;
                 const bool acc0 = (dw_started >> l) & 1u;
                 for (uint32_t ks = 0; ks < 8u; ++ks)
@@ -229,8 +221,8 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
     // Epilogue threads: wait (warp 0 polls, bounded) for slot s's commit, then release the others.
     auto epi_wait = [&](uint32_t s) -> bool {
         bool w = true;
-        if (threadIdx.x < 32u) w = mbar_wait(&ctl.bar_mma[s], phase[s]);
-        phase[s] ^= 1u;
+        if (threadIdx.x < 32u) w = mbar_wait(&ctl.bar_mma[s], (phase >> s) & 1u);
+        phase ^= 1u << s;
         w = epi_sync_and(w);
         tc_fence_after();
         return w;
@@ -243,15 +235,14 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
     };
     // The MMA warp: wait (bounded) until slot s's operands are published.
     auto mma_wait = [&](uint32_t s) -> bool {
-        const bool w = __all_sync(0xffffffffu, mbar_wait(&ctl.opready[s], ready_phase[s]));
-        ready_phase[s] ^= 1u;
+        const bool w = __all_sync(0xffffffffu, mbar_wait(&ctl.opready[s], (ready_phase >> s) & 1u));
+        ready_phase ^= 1u << s;
         tc_fence_after();
         return w;
     };
     // The inputs of tile t into slot s: the encoding (FP32 -> FP16) in 8-column chunks dealt to
     // the four warpgroups, SH by warpgroups 0 and 1 into the colour input's columns 16..31.
     auto stage = [&](uint32_t s, uint32_t t) {
-        const SlotTiles& S = T[s];
         const uint32_t row = t * 128u + r;
         const bool valid = row < A.n;
         for (uint32_t c = wg * 8u; c < P.kd; c += 32u) {
@@ -261,36 +252,35 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
                 const float4 p0 = __ldg(src), p1 = __ldg(src + 1);
                 v[0] = p0.x; v[1] = p0.y; v[2] = p0.z; v[3] = p0.w; v[4] = p1.x; v[5] = p1.y; v[6] = p1.z; v[7] = p1.w;
             }
-            *reinterpret_cast<uint4*>(S.x + tile_offset(r, c, P.kd)) =
+            *reinterpret_cast<uint4*>(T.x(s) + tile_offset(r, c, P.kd)) =
                 make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]), pack_h2(v[6], v[7]));
         }
         if (wg < 2) {
             float v[8];
 #pragma unroll
             for (int i = 0; i < 8; ++i) v[i] = valid ? __ldg(A.xr + (size_t)row * 32 + 16 + 8 * wg + i) : 0.f;
-            *reinterpret_cast<uint4*>(S.rin + tile_offset(r, 16u + 8u * wg, 32)) =
+            *reinterpret_cast<uint4*>(T.rin(s) + tile_offset(r, 16u + 8u * wg, 32)) =
                 make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]), pack_h2(v[6], v[7]));
         }
     };
     // The epilogue of step k of slot s (tile t).  Warp-uniform conditions only around the TMEM
     // loads (whole-warp instructions); `valid` guards stores alone.
     auto epilogue = [&](uint32_t s, uint32_t t, int k) {
-        const SlotTiles& S = T[s];
         const uint32_t col = s * 64u;
         const uint32_t row = t * 128u + r;
         const bool valid = row < A.n;
         if (k < nl) {
             if (k < nd - 1) {
-                epi64(tmem, col, S.kept[k], true, nullptr);
+                epi64(tmem, col, T.kept(s, k), true, nullptr);
             } else if (k == nd - 1) {
                 if (wg == 0) {   // density output: the colour input's columns 0..15, the raw density
                     float v[16];
                     tmem_ld16(lane_addr(tmem, col), v);
-                    store16(S.rin, 32, r, 0, v);
+                    store16(T.rin(s), 32, r, 0, v);
                     if (A.out4 && valid) A.out4[(size_t)row * 4 + 3] = __half2float(__float2half_rn(v[0]));
                 }
             } else if (k < nl - 1) {
-                epi64(tmem, col, S.kept[k - 1], true, nullptr);
+                epi64(tmem, col, T.kept(s, k - 1), true, nullptr);
             } else if (wg == 0) {   // colour output; and the output gradient dL/d raw rgb (columns 3..15 zero)
                 if (A.out4) {
                     float v[16];
@@ -306,7 +296,7 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
                     float v[16];
 #pragma unroll
                     for (int i = 0; i < 16; ++i) v[i] = (valid && i < 3) ? __ldg(A.dl_dout + (size_t)row * 4 + i) : 0.f;
-                    store16(S.dy, 16, r, 0, v);
+                    store16(T.dy(s), 16, r, 0, v);
                 }
             }
             return;
@@ -317,11 +307,11 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
             for (uint32_t c = wg * 8u; c < P.kd; c += 32u) {
                 float v[16];
                 tmem_ld16(lane_addr(tmem, col + (c & ~15u)), v);   // 16 columns; use the 8 of this chunk
-                if (valid) {
+                if (valid) {   // static register indices: the chunk's half of the 16 columns
                     float4* d = reinterpret_cast<float4*>(A.dxd + (size_t)row * P.kd + c);
-                    const uint32_t o = c & 15u;
-                    d[0] = make_float4(v[o], v[o + 1], v[o + 2], v[o + 3]);
-                    d[1] = make_float4(v[o + 4], v[o + 5], v[o + 6], v[o + 7]);
+                    const bool hi = (c & 8u) != 0u;
+                    d[0] = hi ? make_float4(v[8], v[9], v[10], v[11]) : make_float4(v[0], v[1], v[2], v[3]);
+                    d[1] = hi ? make_float4(v[12], v[13], v[14], v[15]) : make_float4(v[4], v[5], v[6], v[7]);
                 }
             }
         } else if (l == nd) {
@@ -330,13 +320,13 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
                 float v[16];
                 tmem_ld16(lane_addr(tmem, col), v);
                 if (valid) v[0] += __ldg(A.dl_dout + (size_t)row * 4 + 3);
-                store16(S.dy, 16, r, 0, v);
+                store16(T.dy(s), 16, r, 0, v);
             }
         } else {
             // the layer's input is a kept ReLU output: mask
             uint32_t w;
-            const uint8_t* mk = layer_input(P, S, l, w);
-            epi64(tmem, col, S.dy, false, mk);
+            const uint8_t* mk = T.input(s, l, w);
+            epi64(tmem, col, T.dy(s), false, mk);
         }
     };
 
