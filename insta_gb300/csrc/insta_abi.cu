@@ -1911,7 +1911,7 @@ int insta_tuning_set(insta_ctx* ctx, const insta_tuning* t) {
         if (t->bvh_top_nodes != 0 && t->bvh_top_nodes != 5 && t->bvh_top_nodes != 21)
             fail(INSTA_ERR_INVALID_ARG, "bvh_top_nodes must be 0, 5 or 21");
         if (t->fused_field_stage > 1) fail(INSTA_ERR_INVALID_ARG, "fused_field_stage must be 0 or 1");
-        if (t->mlp_slots > 7) fail(INSTA_ERR_INVALID_ARG, "mlp_slots must be 0..7");
+        if (t->mlp_slots > 8) fail(INSTA_ERR_INVALID_ARG, "mlp_slots must be 0..8");
         ctx->tune = *t;
     });
 }
@@ -1967,7 +1967,7 @@ int insta_autotune(insta_ctx* ctx, const insta_render_desc* reqs, int n, int rep
         try {
             cur_ms = time_one(cur);
             const std::vector<uint32_t> cands[7] = {{8, 16, 24, 32}, {15, 18, 21}, {1, 2, 3, 4}, {8, 12, 16, 24}, {0, 5, 21}, {0, 1},
-                                                    {1, 7}};
+                                                    {1, 7, 8}};
             for (int pass = 0; pass < 2; ++pass) {
                 bool moved = false;
                 for (int f = 0; f < 7; ++f) {

@@ -46,6 +46,10 @@ __device__ __forceinline__ bool slot_sync_and(uint32_t id, bool v) {
     return r != 0;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // Layer l of the chain: n_dh density hidden layers, the density output (N = 16), n_rh colour
 // hidden layers (the first over [density output | SH]), the colour output (N = 16).
 struct LayerOps {
@@ -351,6 +355,259 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
     __syncthreads();
     tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, tmem_cols);
+}
+
+// ------------------------------------------------------------------ tile pairs, warp-specialised
+// FP16 / BF16 MLPs with two tiles per CTA: 256 epilogue threads (two warpgroups splitting each
+// row's 64 columns, as mlp256_kernel) alternate between the two tiles' epilogues and publish each
+// tile's next operands on an mbarrier; one more warp issues that tile's next layer at once and
+// loads the tile records.  The tensor core runs one tile's layer while the epilogue threads
+// convert the other's, and the epilogue threads never wait on the issuing thread.  Hidden
+// activations stay in TMEM as the next layer's A operand; 256 TMEM columns and a copy of the
+// weights per CTA, two CTAs per SM.  Same arithmetic as mlp256_kernel (bit for bit); measured
+// slower than it on the render (0.18 vs 0.13 ms per 512x512 frame): a tuning choice
+// (insta_tuning.mlp_slots = 8).
+namespace {
+constexpr uint32_t kPairEpi = 256;
+constexpr uint32_t kPairThreads = kPairEpi + 32;
+
+struct PairCtl {
+    uint64_t full[2];      // the tile record has landed (two bulk copies)
+    uint64_t done[2];      // the commit of the slot's current layer
+    uint64_t opready[2];   // the epilogue threads have written the slot's next operands
+    uint64_t bar_w;
+    uint32_t tmem_base;
+};
+
+// The epilogue threads meet at named barrier 1; true when every one passed true.
+__device__ __forceinline__ bool pair_sync_and(bool v) {
+    uint32_t r;
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n barrier.cta.red.and.pred q, 1, %2, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+                 : "=r"(r) : "r"(v ? 1u : 0u), "n"(kPairEpi) : "memory");
+    return r != 0;
+}
+}  // namespace
+
+__global__ void __launch_bounds__(kPairThreads, 2) mlp_pairs_kernel(const __grid_constant__ MlpArgs A, const uint8_t* wimg) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    PairCtl& ctl = *reinterpret_cast<PairCtl*>(smem);
+    const TilePlan& P = A.plan;
+    uint8_t* w = smem + kCtlBytes;
+    uint8_t* slot0 = w + ((P.bytes + 1023u) & ~1023u);
+    const uint32_t n_samples = A.n_alive ? *A.n_alive : (uint32_t)A.n_samples;
+    const uint32_t n_tiles = (n_samples + 127u) / 128u, n_pairs = (n_tiles + 1u) / 2u;
+    const uint32_t n_layers = P.n_dh + P.n_rh + 2u;
+    const uint32_t hash_bytes = hash_tile_bytes(P.k_in), sh_bytes = sh_tile_bytes();
+    const bool bf16 = A.fv.precision == 1;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const bool mma_warp = threadIdx.x >= kPairEpi;
+    const uint32_t r = threadIdx.x & 127u, c0 = ((threadIdx.x >> 7) & 1u) * 32u;   // epilogue: row, first column
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(&ctl.full[k], 2);
+            mbar_init(&ctl.done[k], 1);
+            mbar_init(&ctl.opready[k], kPairEpi);
+        }
+        mbar_init(&ctl.bar_w, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (warp == 0) tmem_alloc(&ctl.tmem_base, 256);
+    if (threadIdx.x == 0) bulk_load(w, wimg, P.bytes, &ctl.bar_w);
+    bool ok = mbar_wait(&ctl.bar_w, 0);
+    tc_fence_before();
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    tc_fence_after();
+    const uint32_t tmem = ctl.tmem_base;
+    auto stage_of = [&](uint32_t s) { return slot0 + s * kSlotBytes; };   // hash rows, then activations
+    uint32_t full_phase = 0u, done_phase = 0u, ready_phase = 0u;          // bit s: slot s's parity
+    float dens0 = 0.f, dens1 = 0.f;                                        // per slot: the row's density output
+
+    // The MMA warp: issue layer l of slot s (lane 0), then its commit.
+    // Slot s's TMEM: accumulator columns [128 s, 128 s + 64), the hidden activations as the next
+    // layer's A operand at 128 s + 64 (32 columns).  Layer 0 (hash rows) and colour layer 0
+    // ([density output | SH] rows) read A from shared memory.
+    auto issue = [&](uint32_t s, uint32_t l) {
+        if (lane != 0) return;
+        uint8_t* st = stage_of(s);
+        const LayerOps o = layer_ops(P, w, st, st + 16384, st + 20480, l);
+        const uint32_t idesc = idesc_f16(128, o.n, bf16);
+        const uint32_t d = tmem + s * 128u;
+        if (l != 0 && l != P.n_dh + 1) {
+            const uint32_t b0 = smem_addr(o.b[0]);
+            for (uint32_t ks = 0; ks < 4u; ++ks)
+                umma_f16_ts(d, d + 64u + ks * 8u, smem_desc(b0 + ks * 256u, 128, 8u * 128u), idesc, ks ? 1u : 0u);
+        } else {
+            uint32_t acc = 0;
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                if (i >= o.n_ops) break;
+                const uint32_t a0 = smem_addr(o.a[i]), b0 = smem_addr(o.b[i]);
+                const uint32_t sbo = (o.k[i] / 8u) * 128u;
+                for (uint32_t ks = 0; ks < o.k[i] / 16u; ++ks) {
+                    umma_f16(d, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, acc);
+                    acc = 1;
+                }
+            }
+        }
+        umma_commit(&ctl.done[s]);
+    };
+    // (the parity advances only on success: a record still in flight is waited for at the end)
+    auto mma_wait = [&](uint64_t* bar, uint32_t& bits, uint32_t s) -> bool {
+        const bool v = __all_sync(0xffffffffu, mbar_wait(bar, (bits >> s) & 1u));
+        if (v) bits ^= 1u << s;
+        tc_fence_after();
+        return v;
+    };
+    uint32_t pending = 0u;   // MMA warp, bit s: slot s's record copies issued, not yet seen landed
+    // The epilogue threads: wait for slot s's commit (warp 0 polls), then release the others.
+    auto epi_wait = [&](uint32_t s) -> bool {
+        bool v = true;
+        if (threadIdx.x < 32u) v = mbar_wait(&ctl.done[s], (done_phase >> s) & 1u);
+        done_phase ^= 1u << s;
+        v = pair_sync_and(v);
+        tc_fence_after();
+        return v;
+    };
+    // The epilogue of layer l of slot s (tile t): ReLU into the activation rows, the density
+    // output into the density rows, or the outputs.
+    auto epilogue = [&](uint32_t s, uint32_t t, uint32_t l) {
+        uint8_t* st = stage_of(s);
+        const uint32_t col = tmem + (((warp & 3u) * 32u) << 16) + s * 128u;
+        const bool wg0 = threadIdx.x < 128u;
+        if (l == P.n_dh) {
+            if (wg0) {
+                float v[16];
+                tmem_ld16(col, v);
+                __half h[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) h[i] = to_act(v[i], bf16);
+                const float d = from_act(h[0], bf16);
+                if (s == 0) dens0 = d; else dens1 = d;
+                store_row(st + 20480, r, 16, h);
+            }
+        } else if (l + 1 == n_layers) {
+            if (wg0) {
+                float v[16];
+                tmem_ld16(col, v);
+                const uint32_t row = t * 128u + r;
+                if (row < n_samples) {
+                    const float o0 = from_act(to_act(v[0], bf16), bf16), o1 = from_act(to_act(v[1], bf16), bf16);
+                    const float o2 = from_act(to_act(v[2], bf16), bf16), o3 = s == 0 ? dens0 : dens1;
+                    if (A.fv.precision != 0) {
+                        A.out_f32[row] = make_float4(o0, o1, o2, o3);
+                    } else {
+                        const __half2 rg = __floats2half2_rn(o0, o1), bd = __floats2half2_rn(o2, o3);
+                        A.out[row] = make_uint2(*reinterpret_cast<const uint32_t*>(&rg), *reinterpret_cast<const uint32_t*>(&bd));
+                    }
+                }
+            }
+        } else {
+#pragma unroll 1
+            for (uint32_t c = c0; c < c0 + 32u; c += 16) {
+                float v[16];
+                tmem_ld16(col + c, v);
+                uint32_t p8[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) p8[i] = pack2_relu(v[2 * i], v[2 * i + 1], bf16);
+                tmem_st8(col + 64u + c / 2u, p8);
+            }
+            tmem_st_wait();
+        }
+    };
+
+    for (uint32_t p = blockIdx.x; p < n_pairs; p += gridDim.x) {
+        const uint32_t ta = 2u * p, tb = 2u * p + 1u;
+        const bool has_b = tb < n_tiles;
+        // both slots' buffers and TMEM columns are free: the previous pair finished on both sides
+        tc_fence_before();
+        ok = __syncthreads_and(ok ? 1 : 0) != 0;
+        tc_fence_after();
+        if (!ok) break;
+        if (mma_warp) {
+            if (lane == 0) {
+                for (uint32_t s = 0; s < (has_b ? 2u : 1u); ++s) {
+                    const uint8_t* src = A.tiles + (size_t)(2u * p + s) * P.tile_bytes;
+                    bulk_load(stage_of(s), src, hash_bytes, &ctl.full[s]);
+                    bulk_load(stage_of(s) + 16384, src + hash_bytes, sh_bytes, &ctl.full[s]);
+                }
+            }
+            pending = has_b ? 3u : 1u;
+            ok = mma_wait(&ctl.full[0], full_phase, 0);
+            if (ok) {
+                pending &= ~1u;
+                issue(0, 0);
+            }
+            if (ok && has_b) {
+                ok = mma_wait(&ctl.full[1], full_phase, 1);
+                if (ok) {
+                    pending &= ~2u;
+                    issue(1, 0);
+                }
+            }
+            for (uint32_t l = 0; l + 1 < n_layers && ok; ++l) {
+                ok = mma_wait(&ctl.opready[0], ready_phase, 0);
+                if (!ok) break;
+                issue(0, l + 1);
+                if (has_b) {
+                    ok = mma_wait(&ctl.opready[1], ready_phase, 1);
+                    if (!ok) break;
+                    issue(1, l + 1);
+                }
+            }
+        } else {
+            for (uint32_t l = 0; l < n_layers; ++l) {
+                ok = epi_wait(0);
+                if (!ok) break;
+                epilogue(0, ta, l);
+                if (l + 1 < n_layers) {
+                    fence_async_smem();
+                    tc_fence_before();
+                    mbar_arrive(&ctl.opready[0]);
+                }
+                if (has_b) {
+                    ok = epi_wait(1);
+                    if (!ok) break;
+                    epilogue(1, tb, l);
+                    if (l + 1 < n_layers) {
+                        fence_async_smem();
+                        tc_fence_before();
+                        mbar_arrive(&ctl.opready[1]);
+                    }
+                }
+            }
+        }
+    }
+    // records whose copies were issued but not seen landed (after a timeout): wait for them
+    // (bounded) before shared memory is released
+    if (mma_warp && lane == 0)
+        for (uint32_t s = 0; s < 2u; ++s)
+            if ((pending >> s) & 1u) mbar_wait(&ctl.full[s], (full_phase >> s) & 1u);
+    if (!ok && (threadIdx.x == 0 || (mma_warp && lane == 0))) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 256);
+}
+
+cudaError_t launch_mlp_pairs(const MlpArgs& a, const uint8_t* image, uint32_t max_tiles, int n_sms, uint32_t ctas_per_sm, cudaStream_t s) {
+    const size_t smem = kCtlBytes + ((a.plan.bytes + 1023u) & ~1023u) + 2u * kSlotBytes;
+    cudaError_t e = cudaFuncSetAttribute(mlp_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(mlp_pairs_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    int dev = 0, smem_sm = 0, reserved = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    int per_sm = smem_sm / (int)(smem + (size_t)reserved);
+    per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm);   // 2 x 256 TMEM columns
+    if (ctas_per_sm && (int)ctas_per_sm < per_sm) per_sm = (int)ctas_per_sm;
+    uint32_t grid = (uint32_t)n_sms * (uint32_t)per_sm;
+    const uint32_t pairs = (max_tiles + 1u) / 2u;
+    if (pairs < grid) grid = pairs ? pairs : 1;
+    mlp_pairs_kernel<<<grid, kPairThreads, smem, s>>>(a, image);
+    return cudaGetLastError();
 }
 
 uint32_t mlp_slots_for(const TilePlan& P, int smem_optin, bool fp8) {

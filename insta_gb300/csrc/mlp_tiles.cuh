@@ -57,13 +57,15 @@ struct MlpArgs {
 };
 
 // slots (insta_tuning.mlp_slots): 2..7 = mlp_slots_kernel with that many slots where every tile
-// uses one weight image; 1 = mlp256_kernel; 0 = mlp_slots_kernel for FP8 fields and for render
-// batches on one weight image, else mlp256_kernel.  ctas_per_sm: mlp256_kernel's resident CTAs per SM
+// uses one weight image; 8 = mlp_pairs_kernel there (FP16 / BF16); 1 = mlp256_kernel; 0 =
+// mlp_slots_kernel for FP8 fields and for render batches on one weight image, else mlp256_kernel.  ctas_per_sm: mlp256_kernel's resident CTAs per SM
 // (0 = as many as shared memory lets reside, at most 4).
 cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm = 0, uint32_t slots = 0);
 // mlp_slots.cu: slots that fit the opt-in shared memory (0 = the kernel does not apply), launch
 uint32_t mlp_slots_for(const TilePlan& P, int smem_optin, bool fp8);
 cudaError_t launch_mlp_slots(const MlpArgs& a, const uint8_t* image, uint32_t n_slots, uint32_t max_tiles, int n_sms, cudaStream_t s);
+// mlp_slots.cu: FP16 / BF16, two tiles per CTA with an MMA-issuing warp
+cudaError_t launch_mlp_pairs(const MlpArgs& a, const uint8_t* image, uint32_t max_tiles, int n_sms, uint32_t ctas_per_sm, cudaStream_t s);
 
 // One MMA chain: sum over (A_i, B_i) pairs into TMEM columns [col, col + N).  K in elements;
 // f8: E4M3 operands (kind::f8f6f4, 32 elements per instruction), else FP16/BF16 (16 per
@@ -93,6 +95,39 @@ __device__ __forceinline__ bool issue_chain(Smem& sm, const uint8_t* const* a, c
     // warp 0 waits for the chain's commit; the others sleep at the barrier instead of polling the
     // mbarrier (their issue slots go to the other CTAs' epilogues), then order their TMEM reads
     // after it
+    bool ok = true;
+    if (threadIdx.x < 32u) ok = mbar_wait(&sm.bar_mma, phase);
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    phase ^= 1u;
+    tc_fence_after();
+    return ok;
+}
+
+// TMEM columns of the 256-thread kernels (128 allocated per CTA): the 64-wide accumulator, the
+// 16-wide output-layer accumulator, and a hidden layer's activations as the next layer's A
+// operand (64 FP16/BF16 values per row = 32 columns).
+constexpr uint32_t kTmemAcc16 = 64u, kTmemA = 96u;
+
+// The same chain with A = the activations in TMEM (kTmemA, K = 64) and B from shared memory.
+// Either way one instruction consumes 32 bytes of each row (8 TMEM columns of A).
+template <typename Smem>
+__device__ __forceinline__ bool issue_chain_ts(Smem& sm, const uint8_t* b, uint32_t N, uint32_t col, bool bf16, uint32_t& phase,
+                                               bool f8 = false) {
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tc_fence_after();
+        const uint32_t idesc = idesc_f16(128, N, bf16 && !f8);
+        const uint32_t b0 = smem_addr(b);
+        if (f8) {
+            for (uint32_t ks = 0; ks < 2u; ++ks)
+                umma_f8_ts(sm.tmem_base + col, sm.tmem_base + kTmemA + ks * 8u, smem_desc(b0 + ks * 256u, 128, 4u * 128u), idesc, ks ? 1u : 0u);
+        } else {
+            for (uint32_t ks = 0; ks < 4u; ++ks)
+                umma_f16_ts(sm.tmem_base + col, sm.tmem_base + kTmemA + ks * 8u, smem_desc(b0 + ks * 256u, 128, 8u * 128u), idesc, ks ? 1u : 0u);
+        }
+        umma_commit(&sm.bar_mma);
+    }
     bool ok = true;
     if (threadIdx.x < 32u) ok = mbar_wait(&sm.bar_mma, phase);
     ok = __syncthreads_and(ok ? 1 : 0) != 0;
@@ -150,11 +185,12 @@ __device__ __forceinline__ uint32_t fused_lane_addr(const Smem& sm, uint32_t col
     return sm.tmem_base + ((((uint32_t)threadIdx.x / 32u) % 4u) * 32u << 16) + col;
 }
 
-// ReLU + rounding of 64 accumulator columns into a_h; warpgroup g (threads 128 g ...) takes
-// columns [32 g, 32 g + 32) of its row (TMEM lane quarter = warp % 4).
+// ReLU + rounding of 64 accumulator columns into the next layer's A operand in TMEM (kTmemA);
+// warpgroup g (threads 128 g ...) takes columns [32 g, 32 g + 32) of its row (TMEM lane quarter =
+// warp % 4), i.e. A columns [16 g, 16 g + 16).
 template <typename Smem>
-__device__ __forceinline__ void relu_to_ah2(Smem& sm, bool bf16) {
-    const uint32_t r = threadIdx.x & 127u, c0 = (threadIdx.x >> 7) * 32u;
+__device__ __forceinline__ void relu_to_tmem_a(Smem& sm, bool bf16) {
+    const uint32_t c0 = (threadIdx.x >> 7) * 32u;
 #pragma unroll 1
     for (uint32_t c = c0; c < c0 + 32u; c += 16) {
         float v[16];
@@ -162,10 +198,9 @@ __device__ __forceinline__ void relu_to_ah2(Smem& sm, bool bf16) {
         uint32_t p[8];   // ReLU, then both values of a pair rounded by one packed conversion
 #pragma unroll
         for (int i = 0; i < 8; ++i) p[i] = pack2_relu(v[2 * i], v[2 * i + 1], bf16);
-#pragma unroll
-        for (int q = 0; q < 2; ++q)
-            *reinterpret_cast<uint4*>(sm.a_h + tile_offset(r, c + q * 8, 64)) = make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+        tmem_st8(fused_lane_addr(sm, kTmemA + c / 2u), p);
     }
+    tmem_st_wait();
 }
 
 // Both MLPs (FP16 or BF16) with 256 threads on the tile in sm.stage; warpgroup 0 returns its
@@ -185,17 +220,15 @@ __device__ __forceinline__ bool mlp256(Smem& sm, uint8_t* a_dens, const uint8_t*
     a = hash; b = w + P.d_off[0]; K = P.k_in;
     ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
     hash_free();
-    relu_to_ah2(sm, bf16);
+    relu_to_tmem_a(sm, bf16);
     for (uint32_t l = 1; l < P.n_dh; ++l) {
-        a = sm.a_h; b = w + P.d_off[l]; K = 64;
-        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
-        relu_to_ah2(sm, bf16);
+        ok &= issue_chain_ts(sm, w + P.d_off[l], 64, 0, bf16, phase);
+        relu_to_tmem_a(sm, bf16);
     }
-    a = sm.a_h; b = w + P.d_out; K = 64;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, bf16, phase);
+    ok &= issue_chain_ts(sm, w + P.d_out, 16, kTmemAcc16, bf16, phase);
     if (wg0) {
         float v[16];
-        tmem_ld16(fused_lane_addr(sm, 64), v);
+        tmem_ld16(fused_lane_addr(sm, kTmemAcc16), v);
         __half h[16];
 #pragma unroll
         for (int i = 0; i < 16; ++i) h[i] = to_act(v[i], bf16);
@@ -208,18 +241,16 @@ __device__ __forceinline__ bool mlp256(Smem& sm, uint8_t* a_dens, const uint8_t*
         const uint32_t Ks[2] = {16, 16};
         ok &= issue_chain(sm, as, bs, Ks, 2, 64, 0, bf16, phase);
         sh_free();
-        relu_to_ah2(sm, bf16);
+        relu_to_tmem_a(sm, bf16);
     }
     for (uint32_t l = 1; l < P.n_rh; ++l) {
-        a = sm.a_h; b = w + P.r_off[l]; K = 64;
-        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, bf16, phase);
-        relu_to_ah2(sm, bf16);
+        ok &= issue_chain_ts(sm, w + P.r_off[l], 64, 0, bf16, phase);
+        relu_to_tmem_a(sm, bf16);
     }
-    a = sm.a_h; b = w + P.r_out; K = 64;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, bf16, phase);
+    ok &= issue_chain_ts(sm, w + P.r_out, 16, kTmemAcc16, bf16, phase);
     if (wg0) {
         float v[16];
-        tmem_ld16(fused_lane_addr(sm, 64), v);
+        tmem_ld16(fused_lane_addr(sm, kTmemAcc16), v);
         out4[0] = from_act(to_act(v[0], bf16), bf16);
         out4[1] = from_act(to_act(v[1], bf16), bf16);
         out4[2] = from_act(to_act(v[2], bf16), bf16);
@@ -303,7 +334,7 @@ __device__ __forceinline__ float row_max2(float* xch, float m) {
 // round(round(v a) s) is monotone for positive scales, so this is the maximum of the dequantised
 // values, bit for bit.)
 template <typename Smem>
-__device__ __forceinline__ float hidden_to_e4m3_2(Smem& sm, float* xch, uint8_t* a_h8, float a, float s) {
+__device__ __forceinline__ float hidden_to_e4m3_2(Smem& sm, float* xch, float a, float s) {
     const uint32_t c0 = (threadIdx.x >> 7) * 32u;
     float raw = -__int_as_float(0x7f800000);
 #pragma unroll 1
@@ -321,9 +352,12 @@ __device__ __forceinline__ float hidden_to_e4m3_2(Smem& sm, float* xch, uint8_t*
         float v[16];
         tmem_ld16(fused_lane_addr(sm, c), v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = fmaxf(__fmul_rn(__fmul_rn(v[i], a), s), 0.f);
-        store16_e4m3_row(a_h8, 64, c, v, inv, threadIdx.x & 127u);
+        for (int i = 0; i < 16; ++i) v[i] = __fmul_rn(fmaxf(__fmul_rn(__fmul_rn(v[i], a), s), 0.f), inv);
+        // E4M3 into the next layer's A operand in TMEM: 4 values per column
+        tmem_st4(fused_lane_addr(sm, kTmemA + c / 4u), e4m3x4(v[0], v[1], v[2], v[3]), e4m3x4(v[4], v[5], v[6], v[7]),
+                 e4m3x4(v[8], v[9], v[10], v[11]), e4m3x4(v[12], v[13], v[14], v[15]));
     }
+    tmem_st_wait();
     return row_scale(mx);
 }
 
@@ -335,7 +369,6 @@ __device__ __forceinline__ bool mlp256_8(Smem& sm, float* xch, uint8_t* a_rgb8, 
     const bool wg0 = g == 0u;
     const uint8_t* hash = sm.stage;
     const uint8_t* sh = sm.stage + hash_tile_bytes(P.k_in);
-    uint8_t* a_h8 = sm.a_h;            // [128][64] E4M3
     uint8_t* a_in8 = sm.a_h + 8192;    // [128][k8 <= 64] E4M3
     const uint8_t* a;
     const uint8_t* b;
@@ -366,20 +399,18 @@ __device__ __forceinline__ bool mlp256_8(Smem& sm, float* xch, uint8_t* a_rgb8, 
     a = a_in8; b = w + P.d_off[0]; K = P.k8;
     ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
     hash_free();
-    ra = hidden_to_e4m3_2(sm, xch, a_h8, ra, ls[li++]);
+    ra = hidden_to_e4m3_2(sm, xch, ra, ls[li++]);
     for (uint32_t l = 1; l < P.n_dh; ++l) {
-        a = a_h8; b = w + P.d_off[l]; K = 64;
-        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
-        ra = hidden_to_e4m3_2(sm, xch, a_h8, ra, ls[li++]);
+        ok &= issue_chain_ts(sm, w + P.d_off[l], 64, 0, false, phase, true);
+        ra = hidden_to_e4m3_2(sm, xch, ra, ls[li++]);
     }
     // density output (16): raw density is column 0; colour input = [density out | SH] (warpgroup 0)
-    a = a_h8; b = w + P.d_out; K = 64;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, false, phase, true);
+    ok &= issue_chain_ts(sm, w + P.d_out, 16, kTmemAcc16, false, phase, true);
     float dens[16], shv[16];
     mx = 0.f;
     if (wg0) {
         float v[16];
-        tmem_ld16(fused_lane_addr(sm, 64), v);
+        tmem_ld16(fused_lane_addr(sm, kTmemAcc16), v);
         const float sd = ls[li];
 #pragma unroll
         for (int i = 0; i < 16; ++i) dens[i] = __fmul_rn(__fmul_rn(v[i], ra), sd);
@@ -398,17 +429,15 @@ __device__ __forceinline__ bool mlp256_8(Smem& sm, float* xch, uint8_t* a_rgb8, 
     a = a_rgb8; b = w + P.r0_dens; K = 32;
     ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
     sh_free();
-    ra = hidden_to_e4m3_2(sm, xch, a_h8, ra, ls[li++]);
+    ra = hidden_to_e4m3_2(sm, xch, ra, ls[li++]);
     for (uint32_t l = 1; l < P.n_rh; ++l) {
-        a = a_h8; b = w + P.r_off[l]; K = 64;
-        ok &= issue_chain(sm, &a, &b, &K, 1, 64, 0, false, phase, true);
-        ra = hidden_to_e4m3_2(sm, xch, a_h8, ra, ls[li++]);
+        ok &= issue_chain_ts(sm, w + P.r_off[l], 64, 0, false, phase, true);
+        ra = hidden_to_e4m3_2(sm, xch, ra, ls[li++]);
     }
-    a = a_h8; b = w + P.r_out; K = 64;
-    ok &= issue_chain(sm, &a, &b, &K, 1, 16, 64, false, phase, true);
+    ok &= issue_chain_ts(sm, w + P.r_out, 16, kTmemAcc16, false, phase, true);
     if (wg0) {
         float v[16];
-        tmem_ld16(fused_lane_addr(sm, 64), v);
+        tmem_ld16(fused_lane_addr(sm, kTmemAcc16), v);
         const float so = ls[li];
         out4[0] = __fmul_rn(__fmul_rn(v[0], ra), so);
         out4[1] = __fmul_rn(__fmul_rn(v[1], ra), so);

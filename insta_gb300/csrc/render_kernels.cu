@@ -1084,7 +1084,8 @@ cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uin
     const size_t smem = (size_t)mlp2_w_off(a.plan.tile_bytes) + a.plan.bytes;
     const bool fp8 = a.fv.precision == 2;
     const uint8_t* image = a.seg ? a.single : a.fv.mlp_smem;
-    const bool want_slots = slots >= 2 || (slots == 0 && (fp8 || (a.seg && a.batch)));
+    if (image && slots == 8 && !fp8 && a.plan.k_in <= 64u) return launch_mlp_pairs(a, image, max_tiles, sm_count(), ctas_per_sm, s);
+    const bool want_slots = (slots >= 2 && slots <= 7) || (slots == 0 && (fp8 || (a.seg && a.batch)));
     if (image && want_slots) {
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);

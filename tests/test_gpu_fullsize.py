@@ -143,8 +143,9 @@ def test_render_512_multi_round_bit_identical(full, frame512):
     s_rgba, s_depth, s_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(sort_cell_bits=15, mlp_ctas_per_sm=1,
                                                                           deform_blocks_per_sm=8, bvh_top_nodes=21))
     assert np.array_equal(s_rgba, rgba) and np.array_equal(s_depth, depth) and np.array_equal(s_counts, counts)
-    # the MLP stage with the weights resident once per SM (tile slots), against one copy per CTA
-    for n_slots in (7, 2):
+    # the MLP stage with the weights resident once per SM (tile slots), and as CTAs of two tiles
+    # with an MMA-issuing warp (8), against one copy per CTA
+    for n_slots in (7, 2, 8):
         k_rgba, k_depth, k_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(mlp_slots=n_slots))
         assert np.array_equal(k_rgba, rgba) and np.array_equal(k_depth, depth) and np.array_equal(k_counts, counts)
     # the deform + encode + MLP stage as one kernel, against encode to global tiles + MLP (default)
@@ -161,11 +162,12 @@ def test_mlp_slots_equal_ctas_bf16_fp8(full, precision):
     try:
         a = render_gpu(ctx, 256, 256, yaw=-8.0, tuning=dict(mlp_slots=1))
         b = render_gpu(ctx, 256, 256, yaw=-8.0, tuning=dict(mlp_slots=6))
+        c = render_gpu(ctx, 256, 256, yaw=-8.0, tuning=dict(mlp_slots=8))   # two-tile CTAs (FP8: per-CTA kernel)
     finally:
         ctx.params_load(AV, fc, params)
     assert (a[0][:, 3] > 0.05).sum() > 1000
-    for x, y in zip(a[:3], b[:3]):
-        assert np.array_equal(x, y)
+    for x, y, z in zip(a[:3], b[:3], c[:3]):
+        assert np.array_equal(x, y) and np.array_equal(x, z)
 
 
 @pytest.mark.parametrize("precision,min_psnr", [(0, 45.0), (1, 45.0), (2, 35.0)])
