@@ -10,11 +10,12 @@
 // inference_mixed_precision_impl's density and colour MLPs (NGP/nerf_network.h:159-232).
 //
 // Per slot s: full[s] completes when the tile record has landed (two bulk copies: hash rows, SH
-// rows), done[s] at the commit of the slot's current layer.  The record's hash rows and the
-// hidden activations share one 16 KiB buffer: the activations are written only after the layer
-// that read the hash rows completed, and the next record is copied in once the tile's last layer
-// has completed.  Every wait is bounded (about a second), after which the kernel sets
-// INSTA_DEVERR_TIMEOUT and the slot leaves.
+// rows), done[s] at the commit of the slot's current layer.  Hidden activations stay in TMEM as
+// the next layer's A operand (after the slots' accumulators: 32 columns per slot for FP16 / BF16,
+// 16 for E4M3, so at most 5 / 6 slots fit the 512 columns); only layer 0 (hash rows) and colour
+// layer 0 ([density output | SH] rows) read A from shared memory, and the next record is copied
+// in once colour layer 0 has completed.  Every wait is bounded (about a second), after which the
+// kernel sets INSTA_DEVERR_TIMEOUT and the slot leaves.
 #include <cstdint>
 
 #include "device_common.cuh"
@@ -26,6 +27,9 @@ namespace insta {
 namespace {
 
 constexpr uint32_t kMaxSlots = 7;
+// TMEM columns of the hidden activations per slot (A operand, 64 values per row)
+__host__ __device__ constexpr uint32_t a_cols(bool fp8) { return fp8 ? 16u : 32u; }
+__host__ __device__ constexpr uint32_t max_slots_tmem(bool fp8) { return 512u / (64u + a_cols(fp8)); }
 constexpr uint32_t kSlotBytes = 24576;    // FP16 / BF16: [0, 16 KiB) hash rows, then activations; SH rows; density rows
 constexpr uint32_t kSlotBytes8 = 32768;   // FP8: hash rows (FP16); SH rows (FP16); E4M3 layer input; E4M3 colour input
 __host__ __device__ constexpr uint32_t slot_bytes(bool fp8) { return fp8 ? kSlotBytes8 : kSlotBytes; }
@@ -116,7 +120,7 @@ __device__ __forceinline__ LayerOps layer_ops8(const TilePlan& P, const uint8_t*
 // E4M3 with the new row scale into a8 (K = 64).  Returns the new row scale.  The maximum is taken
 // over the raw accumulator values and dequantised once: v -> round(round(v a) sw) is monotone for
 // positive scales, so this is the maximum of the dequantised values, bit for bit.
-__device__ __forceinline__ float hidden8_row(uint32_t col0, uint8_t* a8, float a, float sw, uint32_t r) {
+__device__ __forceinline__ float hidden8_row(uint32_t col0, uint32_t acol, float a, float sw) {
     float raw = -__int_as_float(0x7f800000);
 #pragma unroll 1
     for (uint32_t c = 0; c < 64u; c += 32u) {
@@ -132,17 +136,20 @@ __device__ __forceinline__ float hidden8_row(uint32_t col0, uint8_t* a8, float a
         float v[32];
         tmem_ld32(col0 + c, v);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = fmaxf(__fmul_rn(__fmul_rn(v[i], a), sw), 0.f);
-        store16_e4m3_row(a8, 64, c, v, inv, r);
-        store16_e4m3_row(a8, 64, c + 16u, v + 16, inv, r);
+        for (int i = 0; i < 32; ++i) v[i] = __fmul_rn(fmaxf(__fmul_rn(__fmul_rn(v[i], a), sw), 0.f), inv);
+        uint32_t q[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) q[i] = e4m3x4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+        tmem_st8(acol + c / 4u, q);   // the next layer's A operand: 4 values per column
     }
+    tmem_st_wait();
     return row_scale(mx);
 }
 
 }  // namespace
 
 template <bool FP8>
-__global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __grid_constant__ MlpArgs A, const uint8_t* wimg,
+__global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel(const __grid_constant__ MlpArgs A, const uint8_t* wimg,
                                                                       uint32_t n_slots) {
     extern __shared__ __align__(1024) uint8_t smem[];
     SlotCtl& ctl = *reinterpret_cast<SlotCtl*>(smem);
@@ -166,8 +173,9 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    // 64 columns per slot, allocated as a power of two
-    const uint32_t tmem_cols = n_slots <= 2u ? 128u : (n_slots <= 4u ? 256u : 512u);
+    // 64 accumulator columns per slot, then the slots' activation columns, allocated as a power of two
+    const uint32_t used_cols = n_slots * (64u + a_cols(FP8));
+    const uint32_t tmem_cols = used_cols <= 128u ? 128u : (used_cols <= 256u ? 256u : 512u);
     if (warp == 0) tmem_alloc(&ctl.tmem_base, tmem_cols);
     if (threadIdx.x == 0) bulk_load(w, wimg, P.bytes, &ctl.bar_w);
     bool ok = mbar_wait(&ctl.bar_w, 0);
@@ -181,6 +189,8 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
     uint8_t* dens = st + 20480;   // FP16 / BF16 density rows; FP8: the E4M3 layer input
     uint8_t* rgb8 = st + 28672;   // FP8: E4M3 [density output | SH] rows
     const uint32_t col0 = tmem + ((warp & 3u) * 32u << 16) + s * 64u;
+    const uint32_t a_col = n_slots * 64u + s * a_cols(FP8);            // the slot's A operand columns
+    const uint32_t acol0 = tmem + ((warp & 3u) * 32u << 16) + a_col;   // ... at this thread's lane
     const bool waiter = (warp & 3u) == 0;   // the slot's first warp waits on the mbarriers
     uint32_t n_done = 0, n_loads = 0, n_used = 0;
     uint32_t t = blockIdx.x * n_slots + s;
@@ -237,8 +247,13 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
                     const uint32_t idesc = idesc_f16(128, o.n, false);
                     const uint32_t a0 = smem_addr(o.a[0]), b0 = smem_addr(o.b[0]);
                     const uint32_t sbo = (o.k[0] / 16u) * 128u;
-                    for (uint32_t ks = 0; ks < o.k[0] / 32u; ++ks)
-                        umma_f8(tmem + s * 64u, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, ks ? 1u : 0u);
+                    if (l == 0 || l == (int)P.n_dh + 1) {
+                        for (uint32_t ks = 0; ks < o.k[0] / 32u; ++ks)
+                            umma_f8(tmem + s * 64u, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, ks ? 1u : 0u);
+                    } else {   // A = the hidden activations in TMEM (K = 64)
+                        for (uint32_t ks = 0; ks < 2u; ++ks)
+                            umma_f8_ts(tmem + s * 64u, tmem + a_col + ks * 8u, smem_desc(b0 + ks * 256u, 128, sbo), idesc, ks ? 1u : 0u);
+                    }
                     umma_commit(&ctl.done[s]);
                 }
                 wok = true;
@@ -269,7 +284,7 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
                     o4[1] = __fmul_rn(__fmul_rn(v[1], ra), sw);
                     o4[2] = __fmul_rn(__fmul_rn(v[2], ra), sw);
                 } else {
-                    ra = hidden8_row(col0, dens, ra, sw, r);
+                    ra = hidden8_row(col0, acol0, ra, sw);
                 }
             }
         } else {
@@ -286,14 +301,20 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
                 if (r == 0) {
                     const LayerOps o = layer_ops(P, w, st, sh, dens, l);
                     const uint32_t idesc = idesc_f16(128, o.n, bf16);
-                    uint32_t acc = 0;
-                    for (int i = 0; i < o.n_ops; ++i) {
-                        const uint32_t a0 = smem_addr(o.a[i]), b0 = smem_addr(o.b[i]);
-                        const uint32_t sbo = (o.k[i] / 8u) * 128u;
-                        for (uint32_t ks = 0; ks < o.k[i] / 16u; ++ks) {
-                            umma_f16(tmem + s * 64u, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, acc);
-                            acc = 1;
+                    if (l == 0 || l == P.n_dh + 1) {
+                        uint32_t acc = 0;
+                        for (int i = 0; i < o.n_ops; ++i) {
+                            const uint32_t a0 = smem_addr(o.a[i]), b0 = smem_addr(o.b[i]);
+                            const uint32_t sbo = (o.k[i] / 8u) * 128u;
+                            for (uint32_t ks = 0; ks < o.k[i] / 16u; ++ks) {
+                                umma_f16(tmem + s * 64u, smem_desc(a0 + ks * 256u, 128, sbo), smem_desc(b0 + ks * 256u, 128, sbo), idesc, acc);
+                                acc = 1;
+                            }
                         }
+                    } else {   // A = the hidden activations in TMEM (K = 64)
+                        const uint32_t b0 = smem_addr(o.b[0]);
+                        for (uint32_t ks = 0; ks < 4u; ++ks)
+                            umma_f16_ts(tmem + s * 64u, tmem + a_col + ks * 8u, smem_desc(b0 + ks * 256u, 128, 8u * 128u), idesc, ks ? 1u : 0u);
                     }
                     umma_commit(&ctl.done[s]);
                 }
@@ -303,8 +324,9 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
                 ok = slot_sync_and(bar_id, wok);
                 if (!ok) break;
                 tc_fence_after();
-                if (l + 1 == n_layers && r == 0 && t + stride < n_tiles) load(t + stride);   // this tile's MMAs are done
-                if (l + 1 == n_layers && t + stride < n_tiles) ++n_loads;
+                // hash and SH rows are read once colour layer 0 has completed
+                if (l == P.n_dh + 1 && r == 0 && t + stride < n_tiles) load(t + stride);
+                if (l == P.n_dh + 1 && t + stride < n_tiles) ++n_loads;
                 if (l == P.n_dh) {
                     float v[16];
                     tmem_ld16(col0, v);
@@ -320,7 +342,8 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
                     o4[1] = from_act(to_act(v[1], bf16), bf16);
                     o4[2] = from_act(to_act(v[2], bf16), bf16);
                 } else {
-                    // ReLU, rounding to the activation type, into the activation rows (K = 64)
+                    // ReLU, rounding to the activation type, into the next layer's A operand in
+                    // TMEM (two values per column)
     #pragma unroll 1
                     for (uint32_t c = 0; c < 64u; c += 32u) {
                         float v[32];
@@ -328,11 +351,10 @@ __global__ void __launch_bounds__(kMaxSlots * 128, 1) mlp_slots_kernel(const __g
                         uint32_t p[16];
     #pragma unroll
                         for (int i = 0; i < 16; ++i) p[i] = pack2_relu(v[2 * i], v[2 * i + 1], bf16);
-    #pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            *reinterpret_cast<uint4*>(st + tile_offset(r, c + q * 8u, 64)) =
-                                make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+                        tmem_st8(acol0 + c / 2u, p);
+                        tmem_st8(acol0 + c / 2u + 8u, p + 8);
                     }
+                    tmem_st_wait();
                 }
             }
         }
@@ -614,7 +636,7 @@ uint32_t mlp_slots_for(const TilePlan& P, int smem_optin, bool fp8) {
     if (P.k_in > 64u || (fp8 && P.k8 > 64u)) return 0;
     const long avail = (long)smem_optin - (long)kCtlBytes - (long)((P.bytes + 1023u) & ~1023u);
     long n = avail / (long)slot_bytes(fp8);
-    if (n > (long)kMaxSlots) n = kMaxSlots;
+    if (n > (long)max_slots_tmem(fp8)) n = max_slots_tmem(fp8);
     return n < 2 ? 0u : (uint32_t)n;
 }
 
