@@ -82,7 +82,8 @@ typedef struct insta_ctx insta_ctx;
  * (instant-ngp/src/testbed.cu:2253-2258). */
 typedef struct {
     uint32_t n_levels;              /* 16 */
-    uint32_t n_features_per_level;  /* 2 */
+    uint32_t n_features_per_level;  /* 2 (the benchmark field), 4 or 8 (INSTA's configs/nerf/main.json);
+                                       n_levels x n_features_per_level a multiple of 8 in 16..128 */
     uint32_t log2_hashmap_size;     /* 19 */
     uint32_t base_resolution;       /* 16 */
     float per_level_scale;          /* 0 -> derived */

@@ -611,6 +611,62 @@ __device__ __forceinline__ void hash_level(const FieldView& fv, const __half2* t
     a1 = acc.y;
 }
 
+// Level l's F = 4 or 8 features at x: the corners, weights and summation order of hash_level,
+// each corner's F FP16 values in one 8-byte (F = 4) or 16-byte (F = 8) load; entry i of the
+// level starts at FP16 element (level_off + i) F (16-byte aligned for F = 8: the table follows the
+// MLP weights, whose sizes are multiples of 16 elements).
+template <int F>
+__device__ __forceinline__ void hash_level_wide(const FieldView& fv, const __half2* table, V3 x, uint32_t l, float* out) {
+    static_assert(F == 4 || F == 8, "4 or 8 features per level");
+    const float s = fv.level_scale[l];
+    const float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);
+    const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+    const float rx = __fsub_rn(px, fx), ry = __fsub_rn(py, fy), rz = __fsub_rn(pz, fz);
+    const uint32_t gx = (uint32_t)(int32_t)fx, gy = (uint32_t)(int32_t)fy, gz = (uint32_t)(int32_t)fz;
+    const uint32_t res = fv.level_res[l], size = fv.level_size[l];
+    const bool dense = fv.level_dense[l];
+    const __half2* lt = table + (size_t)fv.level_off[l] * (F / 2);
+    const float2 wx = make_float2(__fsub_rn(1.f, rx), rx);
+    float2 acc[F / 2];
+#pragma unroll
+    for (int q = 0; q < F / 2; ++q) acc[q] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (uint32_t c2 = 0; c2 < 4; ++c2) {
+        const uint32_t by = c2 & 1u, bz = c2 >> 1;
+        uint32_t i0, i1;
+        if (dense) {
+            i0 = gx + (gy + by) * res + (gz + bz) * res * res;
+            i1 = i0 + 1u;
+            if (i0 >= size) i0 %= size;   // only cells on the far boundary wrap
+            if (i1 >= size) i1 %= size;
+        } else {
+            const uint32_t hyz = ((gy + by) * 2654435761u) ^ ((gz + bz) * 805459861u);
+            i0 = (gx ^ hyz) & (size - 1u);
+            i1 = ((gx + 1u) ^ hyz) & (size - 1u);
+        }
+        uint32_t e0[F / 2], e1[F / 2];
+        if constexpr (F == 8) {
+            const uint4 u0 = __ldg(reinterpret_cast<const uint4*>(lt + (size_t)i0 * 4u));
+            const uint4 u1 = __ldg(reinterpret_cast<const uint4*>(lt + (size_t)i1 * 4u));
+            e0[0] = u0.x; e0[1] = u0.y; e0[2] = u0.z; e0[3] = u0.w;
+            e1[0] = u1.x; e1[1] = u1.y; e1[2] = u1.z; e1[3] = u1.w;
+        } else {
+            const uint2 u0 = __ldg(reinterpret_cast<const uint2*>(lt + (size_t)i0 * 2u));
+            const uint2 u1 = __ldg(reinterpret_cast<const uint2*>(lt + (size_t)i1 * 2u));
+            e0[0] = u0.x; e0[1] = u0.y;
+            e1[0] = u1.x; e1[1] = u1.y;
+        }
+        const float wy = by ? ry : __fsub_rn(1.f, ry), wz = bz ? rz : __fsub_rn(1.f, rz);
+        const float2 w = __fmul2_rn(__fmul2_rn(wx, make_float2(wy, wy)), make_float2(wz, wz));
+#pragma unroll
+        for (int q = 0; q < F / 2; ++q) acc[q] = __fadd2_rn(acc[q], __fmul2_rn(make_float2(w.x, w.x), half2_bits(e0[q])));
+#pragma unroll
+        for (int q = 0; q < F / 2; ++q) acc[q] = __fadd2_rn(acc[q], __fmul2_rn(make_float2(w.y, w.y), half2_bits(e1[q])));
+    }
+#pragma unroll
+    for (int q = 0; q < F / 2; ++q) { out[2 * q] = acc[q].x; out[2 * q + 1] = acc[q].y; }
+}
+
 // Real spherical harmonics up to degree 4 of the unwarped direction (16 values).
 __device__ __forceinline__ void sh4(float dx, float dy, float dz, float* out) {
     float x = __fsub_rn(__fmul_rn(dx, 2.f), 1.f), y = __fsub_rn(__fmul_rn(dy, 2.f), 1.f), z = __fsub_rn(__fmul_rn(dz, 2.f), 1.f);

@@ -323,8 +323,11 @@ struct FieldLayout {
 
 FieldLayout field_layout(const insta_field_desc& d) {
     if (d.n_levels == 0 || d.n_levels > INSTA_MAX_HASH_LEVELS) fail(INSTA_ERR_UNSUPPORTED, "n_levels must be 1..%d", INSTA_MAX_HASH_LEVELS);
-    if (d.n_features_per_level != 2) fail(INSTA_ERR_UNSUPPORTED, "n_features_per_level must be 2");
-    if (d.n_levels * 2 != 32) fail(INSTA_ERR_UNSUPPORTED, "the hash encoding must have 32 outputs (16 levels x 2)");
+    const uint32_t F = d.n_features_per_level;
+    if (F != 2 && F != 4 && F != 8) fail(INSTA_ERR_UNSUPPORTED, "n_features_per_level must be 2, 4 or 8");
+    // the encode writes 8-feature groups (four levels of two, two of four, one of eight)
+    if ((d.n_levels * F) % 8 != 0 || d.n_levels * F < 16 || d.n_levels * F > 128)
+        fail(INSTA_ERR_UNSUPPORTED, "n_levels x n_features_per_level must be a multiple of 8 in 16..128");
     if (d.n_extra_dims != 0 && d.n_extra_dims != 16) fail(INSTA_ERR_UNSUPPORTED, "n_extra_dims must be 0 or 16");
     if (d.density_neurons != 64 || d.rgb_neurons != 64) fail(INSTA_ERR_UNSUPPORTED, "MLP width must be 64");
     if (d.density_output_dims != 16) fail(INSTA_ERR_UNSUPPORTED, "density_output_dims must be 16");
@@ -338,7 +341,7 @@ FieldLayout field_layout(const insta_field_desc& d) {
     L.b = b;
     uint64_t off = 0;
     int li = 0;
-    uint32_t n_in = d.n_levels * 2 + d.n_extra_dims;
+    uint32_t n_in = d.n_levels * F + d.n_extra_dims;
     std::vector<uint32_t> w = {n_in};
     for (uint32_t h = 0; h < d.density_hidden_layers; ++h) w.push_back(64);
     w.push_back(16);
@@ -359,7 +362,7 @@ FieldLayout field_layout(const insta_field_desc& d) {
         L.lvl_res[l] = res; L.lvl_size[l] = (uint32_t)sz; L.lvl_off[l] = eoff; L.lvl_scale[l] = s;
         eoff += sz;
     }
-    L.total = off + eoff * 2;
+    L.total = off + eoff * F;
     return L;
 }
 
@@ -530,7 +533,9 @@ struct WaveRun {
     uint32_t* counters = nullptr;
 
     // deform + encode + MLP as one kernel: FP16 / BF16 fields when the tuning asks for it
-    bool fused_field() const { return W.fv.precision != 2 && ctx->tune.fused_field_stage; }
+    // (the fused kernel's 16 KiB tile holds the hash rows and the SH rows: at most 48 + 16 columns;
+    // it encodes two features per level)
+    bool fused_field() const { return W.fv.precision != 2 && W.fv.n_features == 2 && W.k_in <= 48u && ctx->tune.fused_field_stage; }
 
     RayBuf rays(int b) {
         Wave& w = ctx->wave;
@@ -1501,6 +1506,8 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
         };
         plan.k_in = (L.layer_k[0] + 15) / 16 * 16;
         plan.k8 = (L.layer_k[0] + 31) / 32 * 32;
+        // the E4M3 density input rows of the per-CTA kernel take one 16 KiB buffer: 128 B per row
+        if (fp8 && plan.k8 > 128) fail(INSTA_ERR_UNSUPPORTED, "FP8 fields take at most 128 density inputs (got %u)", L.layer_k[0]);
         plan.n_dh = (uint32_t)L.n_density - 1;
         const int r0 = L.n_density;
         plan.n_rh = (uint32_t)L.n_rgb - 1;
@@ -1535,7 +1542,7 @@ int insta_params_load(insta_ctx* ctx, int avatar, const insta_field_desc* desc, 
         v.mlp_smem = static_cast<const uint8_t*>(fd.image.p);
         v.mlp_smem_bytes = plan.bytes;
         v.n_levels = desc->n_levels;
-        v.n_features = 2;
+        v.n_features = desc->n_features_per_level;
         v.n_extra = desc->n_extra_dims;
         for (uint32_t l = 0; l < desc->n_levels; ++l) {
             v.level_scale[l] = L.lvl_scale[l];
@@ -1676,6 +1683,8 @@ int insta_field_backward_ex(insta_ctx* ctx, int avatar, const float* coords, uin
         if ((dl_dout == nullptr) != (grad == nullptr)) fail(INSTA_ERR_INVALID_ARG, "output gradients and parameter gradients go together");
         if (stride < 11 + fd.desc.n_extra_dims) fail(INSTA_ERR_INVALID_ARG, "stride too small");
         if ((uintptr_t)grad & 7) fail(INSTA_ERR_INVALID_ARG, "grad must be 8-byte aligned");   // paired table atomics
+        if (fd.desc.n_features_per_level >= 4 && ((uintptr_t)grad & 15))
+            fail(INSTA_ERR_INVALID_ARG, "grad must be 16-byte aligned for 4 or 8 features per level");   // 16-byte table atomics
         if (dl_dextra && !(dl_dout && grad)) fail(INSTA_ERR_INVALID_ARG, "dl_dextra needs the backward (dl_dout and grad)");
         if (n == 0) return;
         const int extra_k = (dl_dextra && fd.desc.n_extra_dims) ? 1 : 0;

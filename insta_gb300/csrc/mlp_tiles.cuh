@@ -369,7 +369,7 @@ __device__ __forceinline__ bool mlp256_8(Smem& sm, float* xch, uint8_t* a_rgb8, 
     const bool wg0 = g == 0u;
     const uint8_t* hash = sm.stage;
     const uint8_t* sh = sm.stage + hash_tile_bytes(P.k_in);
-    uint8_t* a_in8 = sm.a_h + 8192;    // [128][k8 <= 64] E4M3
+    uint8_t* a_in8 = sm.a_h;           // [128][k8 <= 128] E4M3 (the hidden layers' inputs stay in TMEM)
     const uint8_t* a;
     const uint8_t* b;
     uint32_t K;

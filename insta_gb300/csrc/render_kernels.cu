@@ -99,10 +99,13 @@ __global__ void ray_init_kernel(const __grid_constant__ WaveArgs A, uint32_t tot
 // ------------------------------------------------------------------ march + deform + encode
 __device__ __forceinline__ uint32_t pack_act(float a, float b, bool bf16) { return pack2_act(a, b, bf16); }
 
-// Parts of one sample's operand rows: hash features of level groups [g0, g1) (four levels, 32
-// gathers in flight, per group, each group of 8 values stored as one 16-byte chunk of the row),
-// the expression dims, and SH of the direction into the SH tile.  No per-sample array is
-// materialised.
+// Parts of one sample's operand rows: hash features of 8-feature groups [g0, g1) (four levels of
+// two features, two of four, or one of eight per group; each group stored as one 16-byte chunk
+// of the row), the expression dims, and SH of the direction into the SH tile.  No per-sample
+// array is materialised.
+__device__ __forceinline__ uint32_t feature_groups(const FieldView& fv) { return fv.n_levels * fv.n_features / 8u; }
+// F = fv.n_features (2, 4 or 8), a template parameter so that each kernel holds one variant.
+template <int F>
 __device__ __forceinline__ void encode_levels(const FieldView& fv, const uint16_t* table, const float* pos, uint8_t* rec, uint32_t row,
                                               uint32_t k_in, uint32_t g0, uint32_t g1) {
     const bool bf16 = fv.precision == 1;
@@ -111,14 +114,22 @@ __device__ __forceinline__ void encode_levels(const FieldView& fv, const uint16_
 #pragma unroll 1
     for (uint32_t g = g0; g < g1; ++g) {
         float v[8];
+        if constexpr (F == 8) {
+            hash_level_wide<8>(fv, t2, x, g, v);
+        } else if constexpr (F == 4) {
+            hash_level_wide<4>(fv, t2, x, 2 * g, v);
+            hash_level_wide<4>(fv, t2, x, 2 * g + 1, v + 4);
+        } else {
 #pragma unroll
-        for (uint32_t j = 0; j < 4; ++j) hash_level(fv, t2, x, 4 * g + j, v[2 * j], v[2 * j + 1]);
+            for (uint32_t j = 0; j < 4; ++j) hash_level(fv, t2, x, 4 * g + j, v[2 * j], v[2 * j + 1]);
+        }
         uint4 q;
         q.x = pack_act(v[0], v[1], bf16); q.y = pack_act(v[2], v[3], bf16);
         q.z = pack_act(v[4], v[5], bf16); q.w = pack_act(v[6], v[7], bf16);
         *reinterpret_cast<uint4*>(rec + tile_offset(row, 8 * g, k_in)) = q;
     }
 }
+template <int F>
 __device__ __forceinline__ void encode_extra(const FieldView& fv, const float* extra, uint32_t mask, uint8_t* rec, uint32_t row, uint32_t k_in) {
     const bool bf16 = fv.precision == 1;
     for (uint32_t g = 0; g < fv.n_extra / 8; ++g) {
@@ -128,7 +139,7 @@ __device__ __forceinline__ void encode_extra(const FieldView& fv, const float* e
         uint4 q;
         q.x = pack_act(v[0], v[1], bf16); q.y = pack_act(v[2], v[3], bf16);
         q.z = pack_act(v[4], v[5], bf16); q.w = pack_act(v[6], v[7], bf16);
-        *reinterpret_cast<uint4*>(rec + tile_offset(row, 2 * fv.n_levels + 8 * g, k_in)) = q;
+        *reinterpret_cast<uint4*>(rec + tile_offset(row, fv.n_levels * F + 8 * g, k_in)) = q;
     }
 }
 __device__ __forceinline__ void encode_sh(const FieldView& fv, const float* dirw, uint8_t* rec, uint32_t row, uint32_t k_in) {
@@ -147,10 +158,11 @@ __device__ __forceinline__ void encode_sh(const FieldView& fv, const float* dirw
 
 // One sample's operand rows: hash features (+ expression dims) into the hash tile, SH of the
 // direction into the SH tile.
+template <int F>
 __device__ __forceinline__ void encode_sample(const FieldView& fv, const uint16_t* table, const float* extra, uint32_t mask,
                                               const float* pos, const float* dirw, uint8_t* rec, uint32_t row, uint32_t k_in) {
-    encode_levels(fv, table, pos, rec, row, k_in, 0, fv.n_levels / 4);
-    encode_extra(fv, extra, mask, rec, row, k_in);
+    encode_levels<F>(fv, table, pos, rec, row, k_in, 0, feature_groups(fv));
+    encode_extra<F>(fv, extra, mask, rec, row, k_in);
     encode_sh(fv, dirw, rec, row, k_in);
 }
 
@@ -532,6 +544,7 @@ __device__ __forceinline__ uint32_t deform_sample(const WaveArgs& A, uint32_t s,
     return req;
 }
 
+template <int F>
 __global__ void __launch_bounds__(256, 4) map_encode_kernel(const __grid_constant__ WaveArgs A) {
     const uint32_t n = *A.n_samples_padded;
     const uint32_t n_alive = *A.n_alive_in;
@@ -543,7 +556,7 @@ __global__ void __launch_bounds__(256, 4) map_encode_kernel(const __grid_constan
         const uint32_t req = deform_sample(A, s, m, n_alive, cpos, cdir, mask);
         const ReqView& R = A.reqs[req];
         uint8_t* rec = A.tiles + (size_t)(s >> 7) * A.tile_bytes;
-        encode_sample(A.fv, R.table, R.extra, mask, cpos, cdir, rec, s & 127u, A.k_in);
+        encode_sample<F>(A.fv, R.table, R.extra, mask, cpos, cdir, rec, s & 127u, A.k_in);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(A.sample_counter, (unsigned long long)*A.n_samples_round);
 }
@@ -699,7 +712,7 @@ __global__ void __launch_bounds__(256, 4) field_tile_kernel(const __grid_constan
     ok = __syncthreads_and(ok ? 1 : 0) != 0;   // uniform: the tile loop holds CTA barriers
     tc_fence_after();
     const bool bf16 = A.fv.precision == 1;
-    const uint32_t ng = A.fv.n_levels / 4, half = ng / 2;   // level groups; warpgroup 0 takes [0, half)
+    const uint32_t ng = feature_groups(A.fv), half = ng / 2;   // feature groups; warpgroup 0 takes [0, half)
     float4* hand = reinterpret_cast<float4*>(sm.a_h);      // [128][2]: (position, region), (direction, valid)
     for (uint32_t t = t0; t < t1 && ok; ++t) {
         const uint32_t req = tile_request(M, t);
@@ -730,11 +743,11 @@ __global__ void __launch_bounds__(256, 4) field_tile_kernel(const __grid_constan
             const ReqView& R = A.reqs[req];
             const float cpos[3] = {h0.x, h0.y, h0.z}, cdir[3] = {h1.x, h1.y, h1.z};
             if (wg == 0) {
-                encode_levels(A.fv, R.table, cpos, sm.stage, r, A.k_in, 0, half);
+                encode_levels<2>(A.fv, R.table, cpos, sm.stage, r, A.k_in, 0, half);
                 encode_sh(A.fv, cdir, sm.stage, r, A.k_in);
             } else {
-                encode_levels(A.fv, R.table, cpos, sm.stage, r, A.k_in, half, ng);
-                encode_extra(A.fv, R.extra, __float_as_uint(h0.w), sm.stage, r, A.k_in);
+                encode_levels<2>(A.fv, R.table, cpos, sm.stage, r, A.k_in, half, ng);
+                encode_extra<2>(A.fv, R.extra, __float_as_uint(h0.w), sm.stage, r, A.k_in);
             }
         }
         // mlp256's first chain fences these generic writes for the tensor core and syncs the CTA;
@@ -833,6 +846,7 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
 }
 
 // ------------------------------------------------------------------ field eval (parity entry)
+template <int F>
 __global__ void __launch_bounds__(256) encode_coords_kernel(FieldView fv, const float* __restrict__ coords, uint32_t stride,
                                                             int64_t n, uint8_t* tiles, uint32_t tile_bytes, uint32_t k_in) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -840,7 +854,7 @@ __global__ void __launch_bounds__(256) encode_coords_kernel(FieldView fv, const 
     const float* c = coords + i * stride;
     float pos[3] = {c[0], c[1], c[2]}, dir[3] = {c[8], c[9], c[10]};
     uint8_t* rec = tiles + (size_t)(i >> 7) * tile_bytes;
-    encode_sample(fv, fv.table, c + stride - fv.n_extra, 7u, pos, dir, rec, (uint32_t)(i & 127), k_in);
+    encode_sample<F>(fv, fv.table, c + stride - fv.n_extra, 7u, pos, dir, rec, (uint32_t)(i & 127), k_in);
 }
 
 __global__ void unpack_outputs_kernel(const uint2* __restrict__ out, const float4* __restrict__ out_f32, int bf16, int64_t n, float4* dst) {
@@ -1048,7 +1062,10 @@ cudaError_t launch_nearest_stage(const WaveArgs& a, uint32_t blocks_per_sm, cuda
 
 cudaError_t launch_map_encode(const WaveArgs& a, uint32_t blocks_per_sm, cudaStream_t s) {
     const uint32_t bps = blocks_per_sm ? blocks_per_sm : 16u;
-    map_encode_kernel<<<sm_count() * bps, 256, 0, s>>>(a);
+    const unsigned grid = sm_count() * bps;
+    if (a.fv.n_features == 8) map_encode_kernel<8><<<grid, 256, 0, s>>>(a);
+    else if (a.fv.n_features == 4) map_encode_kernel<4><<<grid, 256, 0, s>>>(a);
+    else map_encode_kernel<2><<<grid, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -1152,7 +1169,10 @@ cudaError_t launch_composite(const WaveArgs& a, cudaStream_t s) {
 cudaError_t launch_encode_coords(const FieldView& fv, const float* coords, uint32_t stride, int64_t n, uint8_t* tiles,
                                  uint32_t tile_bytes, uint32_t k_in, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    encode_coords_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in);
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    if (fv.n_features == 8) encode_coords_kernel<8><<<grid, 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in);
+    else if (fv.n_features == 4) encode_coords_kernel<4><<<grid, 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in);
+    else encode_coords_kernel<2><<<grid, 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in);
     return cudaGetLastError();
 }
 

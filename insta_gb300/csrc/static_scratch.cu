@@ -10,9 +10,10 @@
 namespace insta {
 
 // Largest batch insta_field_eval_static accepts, and the scratch it needs: encoded input
-// tiles (up to 48 + 16 FP16 columns per sample) plus packed FP16 and FP32 network outputs.
+// tiles (up to 144 + 16 FP16 columns per sample: 128 hash features, 16 expression dims, SH) plus
+// packed FP16 and FP32 network outputs.
 constexpr int64_t kStaticMaxSamples = 16384;
-constexpr size_t kStaticTileBytes = (size_t)kStaticMaxSamples / 128 * (128 * (48 + 16) * 2);
+constexpr size_t kStaticTileBytes = (size_t)kStaticMaxSamples / 128 * (128 * (144 + 16) * 2);
 constexpr size_t kStaticOutBytes = (size_t)kStaticMaxSamples * sizeof(uint2);
 constexpr size_t kStaticOutF32Bytes = (size_t)kStaticMaxSamples * sizeof(float4);
 constexpr size_t kStaticBytes = kStaticTileBytes + kStaticOutBytes + kStaticOutF32Bytes;

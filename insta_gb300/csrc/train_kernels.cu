@@ -19,6 +19,48 @@
 
 namespace insta {
 
+// Table index of corner (cx, cy, cz) of level l: dense x + y res + z res^2 (wrapping on the far
+// boundary), else the spatial hash.
+__device__ __forceinline__ uint32_t corner_index(const FieldView& fv, uint32_t l, uint32_t cx, uint32_t cy, uint32_t cz) {
+    const uint32_t res = fv.level_res[l], size = fv.level_size[l];
+    if (fv.level_dense[l]) {
+        uint32_t idx = cx + cy * res + cz * res * res;
+        if (idx >= size) idx %= size;
+        return idx;
+    }
+    return ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
+}
+
+// One level of the hash encoding from the FP32 master table ([entries][F] floats, F = 4 or 8),
+// the same index arithmetic and summation order as hash_level / hash_level_wide.
+template <int F>
+__device__ __forceinline__ void hash_level_f32_wide(const FieldView& fv, const float* __restrict__ table, V3 x, uint32_t l, float* a) {
+    const float s = fv.level_scale[l];
+    const float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);
+    const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+    const float rx = __fsub_rn(px, fx), ry = __fsub_rn(py, fy), rz = __fsub_rn(pz, fz);
+    const uint32_t gx = (uint32_t)(int32_t)fx, gy = (uint32_t)(int32_t)fy, gz = (uint32_t)(int32_t)fz;
+    const float4* lt = reinterpret_cast<const float4*>(table + (size_t)fv.level_off[l] * F);
+#pragma unroll
+    for (int f = 0; f < F; ++f) a[f] = 0.f;
+#pragma unroll
+    for (uint32_t c = 0; c < 8; ++c) {
+        const uint32_t bx = c & 1u, by = (c >> 1) & 1u, bz = (c >> 2) & 1u;
+        float w = bx ? rx : __fsub_rn(1.f, rx);
+        w = __fmul_rn(w, by ? ry : __fsub_rn(1.f, ry));
+        w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
+        const uint32_t idx = corner_index(fv, l, gx + bx, gy + by, gz + bz);
+#pragma unroll
+        for (int q = 0; q < F / 4; ++q) {
+            const float4 e = __ldg(lt + (size_t)idx * (F / 4) + q);
+            a[4 * q + 0] = __fadd_rn(a[4 * q + 0], __fmul_rn(w, e.x));
+            a[4 * q + 1] = __fadd_rn(a[4 * q + 1], __fmul_rn(w, e.y));
+            a[4 * q + 2] = __fadd_rn(a[4 * q + 2], __fmul_rn(w, e.z));
+            a[4 * q + 3] = __fadd_rn(a[4 * q + 3], __fmul_rn(w, e.w));
+        }
+    }
+}
+
 // One level of the hash encoding from the FP32 master table ([entries][2] floats), the same
 // index arithmetic and summation order as hash_level.
 __device__ __forceinline__ void hash_level_f32(const FieldView& fv, const float2* __restrict__ table, V3 x, uint32_t l, float& a0, float& a1) {
@@ -61,13 +103,20 @@ __global__ void __launch_bounds__(256) train_encode_kernel(FieldView fv, const f
     const float* c = coords + (size_t)i * stride;
     const V3 p = v3(c[0], c[1], c[2]);
     float* x = xd + (size_t)i * kd;
+    const uint32_t F = fv.n_features;
     for (uint32_t l = 0; l < fv.n_levels; ++l) {
-        float a0, a1;
-        hash_level_f32(fv, table32, p, l, a0, a1);
-        x[2 * l] = a0;
-        x[2 * l + 1] = a1;
+        if (F == 8) {
+            hash_level_f32_wide<8>(fv, reinterpret_cast<const float*>(table32), p, l, x + 8 * l);
+        } else if (F == 4) {
+            hash_level_f32_wide<4>(fv, reinterpret_cast<const float*>(table32), p, l, x + 4 * l);
+        } else {
+            float a0, a1;
+            hash_level_f32(fv, table32, p, l, a0, a1);
+            x[2 * l] = a0;
+            x[2 * l + 1] = a1;
+        }
     }
-    for (uint32_t m = 0; m < fv.n_extra; ++m) x[2 * fv.n_levels + m] = c[stride - fv.n_extra + m];
+    for (uint32_t m = 0; m < fv.n_extra; ++m) x[F * fv.n_levels + m] = c[stride - fv.n_extra + m];
     float sh[16];
     sh4(c[8], c[9], c[10], sh);
     float* r = xr + (size_t)i * 32 + 16;
@@ -102,6 +151,65 @@ __global__ void __launch_bounds__(256) train_out_kernel(uint32_t n, const float*
 __global__ void __launch_bounds__(256) train_density_grad_kernel(uint32_t n, const float* __restrict__ g, float* __restrict__ dxr) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dxr[(size_t)i * 32] += g[(size_t)i * 4 + 3];
+}
+
+// Hash encode backward for F = 4 or 8 features per level: the corner weights of
+// hash_backward_kernel times the F gradients, runs of equal entries within a warp summed first
+// (the same segmented scan), one or two 16-byte reductions per entry and run.
+template <int F>
+__global__ void __launch_bounds__(256) hash_backward_wide_kernel(FieldView fv, const float* __restrict__ coords, uint32_t stride, uint32_t n,
+                                                                 const float* __restrict__ dxd, uint32_t kd, float* __restrict__ gtable) {
+    constexpr uint32_t FULL = 0xffffffffu;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31u;
+    if ((i & ~31u) >= n) return;   // whole warps past the end leave; the rest stay for the shuffles
+    const bool valid = i < n;
+    const float* c = coords + (size_t)(valid ? i : 0) * stride;
+    const V3 x = v3(c[0], c[1], c[2]);
+    const float* dg = dxd + (size_t)(valid ? i : 0) * kd;
+    for (uint32_t l = 0; l < fv.n_levels; ++l) {
+        float g[F];
+#pragma unroll
+        for (int f = 0; f < F; ++f) g[f] = valid ? dg[F * l + f] : 0.f;
+        const float s = fv.level_scale[l];
+        const float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);
+        const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+        const float rx = __fsub_rn(px, fx), ry = __fsub_rn(py, fy), rz = __fsub_rn(pz, fz);
+        const uint32_t gx = (uint32_t)(int32_t)fx, gy = (uint32_t)(int32_t)fy, gz = (uint32_t)(int32_t)fz;
+        float4* lt = reinterpret_cast<float4*>(gtable + (size_t)fv.level_off[l] * F);
+#pragma unroll 1
+        for (uint32_t cc = 0; cc < 8; ++cc) {
+            const uint32_t bx = cc & 1u, by = (cc >> 1) & 1u, bz = (cc >> 2) & 1u;
+            float w = bx ? rx : __fsub_rn(1.f, rx);
+            w = __fmul_rn(w, by ? ry : __fsub_rn(1.f, ry));
+            w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
+            uint32_t idx = corner_index(fv, l, gx + bx, gy + by, gz + bz);
+            if (!valid) idx = FULL;
+            float v[F];
+            bool any = false;
+#pragma unroll
+            for (int f = 0; f < F; ++f) v[f] = w * g[f];
+            const uint32_t prev = __shfl_up_sync(FULL, idx, 1), next = __shfl_down_sync(FULL, idx, 1);
+            const uint32_t heads = __ballot_sync(FULL, lane == 0 || prev != idx);
+            if (heads != FULL) {
+                const uint32_t start = 31u - __clz(heads & (FULL >> (31u - lane)));
+#pragma unroll
+                for (uint32_t d = 1; d < 32; d <<= 1) {
+#pragma unroll
+                    for (int f = 0; f < F; ++f) {
+                        const float o = __shfl_up_sync(FULL, v[f], d);
+                        if (lane >= start + d) v[f] += o;
+                    }
+                }
+            }
+#pragma unroll
+            for (int f = 0; f < F; ++f) any |= v[f] != 0.f;
+            if (valid && (lane == 31 || next != idx) && any) {
+#pragma unroll
+                for (int q = 0; q < F / 4; ++q)
+                    atomicAdd(lt + (size_t)idx * (F / 4) + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
+            }
+        }
+    }
 }
 
 // Hash encode backward: every corner's trilinear weight times the encoding gradient, added into
@@ -157,6 +265,14 @@ __global__ void __launch_bounds__(256) hash_backward_kernel(FieldView fv, const 
             if (valid && (lane == 31 || next != idx) && (vx != 0.f || vy != 0.f)) atomicAdd(lt + idx, make_float2(vx, vy));
         }
     }
+}
+
+void launch_hash_backward(const FieldView& fv, const float* coords, uint32_t stride, uint32_t n, const float* dxd, uint32_t kd,
+                          float* gtable, cudaStream_t s) {
+    const unsigned blocks = (n + 255) / 256;
+    if (fv.n_features == 8) hash_backward_wide_kernel<8><<<blocks, 256, 0, s>>>(fv, coords, stride, n, dxd, kd, gtable);
+    else if (fv.n_features == 4) hash_backward_wide_kernel<4><<<blocks, 256, 0, s>>>(fv, coords, stride, n, dxd, kd, gtable);
+    else hash_backward_kernel<<<blocks, 256, 0, s>>>(fv, coords, stride, n, dxd, kd, gtable);
 }
 
 // Adam (the optimizer the INSTA configuration nests in its Ema, configs/nerf/main.json), in the
@@ -670,7 +786,7 @@ __global__ void __launch_bounds__(256) extra_grad_kernel(uint32_t n, const float
 static cudaError_t launch_extra_grad(const FieldView& fv, const TrainShape& t, uint32_t n, const float* dxd, float* out, cudaStream_t s) {
     const uint32_t ne = fv.n_extra;
     if (!out || ne == 0) return cudaSuccess;
-    extra_grad_kernel<<<(unsigned)(((size_t)n * ne + 255) / 256), 256, 0, s>>>(n, dxd, t.kd, 2u * fv.n_levels, ne, out);
+    extra_grad_kernel<<<(unsigned)(((size_t)n * ne + 255) / 256), 256, 0, s>>>(n, dxd, t.kd, fv.n_features * fv.n_levels, ne, out);
     return cudaGetLastError();
 }
 
@@ -774,7 +890,7 @@ cudaError_t launch_field_train(cublasHandle_t h, const FieldView& fv, const Trai
         if (l > 0) relu_back_kernel<<<grid_for((size_t)64 * n), 256, 0, s>>>(dx, hd[l - 1], (size_t)64 * n);
         dout = dx; lddout = k; n_out = k;
     }
-    hash_backward_kernel<<<(n + 255) / 256, 256, 0, s>>>(fv, coords, stride, n, dxd, t.kd, grad + t.table_off);
+    launch_hash_backward(fv, coords, stride, n, dxd, t.kd, grad + t.table_off, s);
     if (!okb) return cudaErrorUnknown;
     return launch_extra_grad(fv, t, n, dxd, dl_dextra, s);
 }
@@ -803,7 +919,7 @@ cudaError_t launch_field_train_tc(const FieldView& fv, const TrainShape& t, cons
     a.err = err;
     cudaError_t e = launch_train_mlp(a, images, w32, img_dev, s);
     if (e != cudaSuccess || !bwd) return e;
-    hash_backward_kernel<<<(n + 255) / 256, 256, 0, s>>>(fv, coords, stride, n, dxd, t.kd, grad + t.table_off);
+    launch_hash_backward(fv, coords, stride, n, dxd, t.kd, grad + t.table_off, s);
     return launch_extra_grad(fv, t, n, dxd, dl_dextra, s);
 }
 

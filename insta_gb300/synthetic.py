@@ -228,6 +228,14 @@ class FieldConfig:
         return float(f(np.exp(f(np.log(f(2048.0) * f(self.aabb_scale) / f(self.base_res))) / f(self.n_levels - 1))))
 
 
+def insta_field_config() -> FieldConfig:
+    """The field INSTA trains with its shipped configuration (configs/nerf/main.json: 16 levels of
+    8 features, 2^18 entries per level, base resolution 16; 16 expression dims appended to the
+    density input ("exp_params"); density MLP 2 hidden layers of 64, 16 outputs; colour MLP 3
+    hidden layers of 64)."""
+    return FieldConfig(n_levels=16, n_features=8, log2_table=18, base_res=16, n_extra=16, density_layers=2, rgb_layers=3)
+
+
 def field_params(cfg: FieldConfig, seed: int = 0, density_gain: float = 1.0) -> np.ndarray:
     """FP16 parameter blob in snapshot order: density MLP, rgb MLP, hash table
     (NerfNetwork::set_params, NGP/nerf_network.h:492-525).  Each MLP layer is a

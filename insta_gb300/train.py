@@ -79,7 +79,11 @@ class TrainStep:
         self.counters_host = torch.zeros(2, dtype=torch.int32, pin_memory=True)
         self.n_steps = 0
         self._last_kept = 0
-        ctx.train_set_math(cfg.tf32, tcgen05=cfg.tcgen05)
+        # the tcgen05 training kernel holds a field of at most 64 density inputs and 8 layers in one
+        # CTA (wider fields, e.g. INSTA's 16 x 8 features + 16 expression dims, take the TF32 products)
+        n_in = fc.n_levels * fc.n_features + fc.n_extra
+        self.tcgen05 = cfg.tcgen05 and n_in <= 64 and fc.density_layers + fc.rgb_layers + 2 <= 8
+        ctx.train_set_math(cfg.tf32, tcgen05=self.tcgen05)
 
     def step(self, grid_frame: int, rays, image, start_rand, target, background=None, extra=None, n_images: int = 0,
              depth=None, seg_mask=None, mean_density=None, exposure=None) -> dict:

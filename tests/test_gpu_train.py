@@ -508,21 +508,26 @@ def test_training_pixels_and_cdf_match_oracle(ctx, oracle, mode):
     np.testing.assert_array_equal(out_bg.cpu().numpy(), rbg)
 
 
-def test_train_step_fits_a_constant_colour(ctx, avatar, frame0):
-    """insta_gb300.train.TrainStep (TF32 backward): training samples -> field evaluation -> loss
-    -> backward -> Adam, 80 steps towards an opaque constant-colour target, lowers the batch loss
-    4x."""
+@pytest.mark.parametrize("layout", ["benchmark", "insta"])
+def test_train_step_fits_a_constant_colour(ctx, avatar, frame0, layout):
+    """insta_gb300.train.TrainStep: training samples -> field evaluation -> loss -> backward ->
+    Adam, 80 steps towards an opaque constant-colour target, lowers the batch loss 4x (INSTA's wider
+    field gets there within its first steps, so against the first step's loss); for the
+    benchmark field (tcgen05 layer products) and INSTA's shipped one (16 levels x 8 features, 16
+    expression dims, 2 + 3 hidden layers: TF32 layer products, 16-byte table reductions)."""
     from insta_gb300 import synthetic as S
     from insta_gb300.train import TrainConfig, TrainStep
-    aid = 22
+    aid = 22 if layout == "benchmark" else 23
     ctx.canonical_set(aid, avatar.canonical, avatar.faces, avatar.mask)
     ctx.frame_upload(aid, 0, frame0)
     ctx.occupancy_from_mesh(aid, 0, 0.015)
-    fc = S.FieldConfig()
+    fc = S.FieldConfig() if layout == "benchmark" else S.insta_field_config()
     ctx.params_load(aid, fc, S.field_params(fc, seed=2))
     cfg = TrainConfig(n_rays_per_batch=4096, target_batch_size=1 << 16, max_samples=1 << 19)
     cfg.adam["learning_rate"] = 1e-2
     ts = TrainStep(ctx, aid, fc, cfg)
+    assert ts.tcgen05 == (layout == "benchmark")
+    extra = dev(np.linspace(-0.5, 0.5, fc.n_extra, dtype=np.float32).reshape(1, -1)) if fc.n_extra else None
     rng = np.random.default_rng(3)
     n = cfg.n_rays_per_batch
     target = dev(np.tile(np.array([[0.8, 0.3, 0.2, 1.0]], np.float32), (n, 1)))
@@ -535,12 +540,14 @@ def test_train_step_fits_a_constant_colour(ctx, avatar, frame0):
         org = c0 + u * 0.9
         tgt = c0 + rng.normal(0, 0.05, (n, 3))
         rays = dev(np.concatenate([org, tgt - org], 1).astype(np.float32))
-        info = ts.step(0, rays, image, dev(rng.random(n).astype(np.float32)), target)
+        info = ts.step(0, rays, image, dev(rng.random(n).astype(np.float32)), target, extra=extra, n_images=1 if extra is not None else 0)
         kept.append(info["rays_kept"])
         losses.append(ts.loss_value())
     ctx.train_set_math(False)
     assert min(kept) > n // 2
-    assert np.isfinite(losses).all() and np.mean(losses[-5:]) < 0.25 * np.mean(losses[:5]), (losses[:5], losses[-5:])
+    assert np.isfinite(losses).all() and np.mean(losses[-5:]) < 0.25 * losses[0], (losses[:5], losses[-5:])
+    if layout == "benchmark":
+        assert np.mean(losses[-5:]) < 0.25 * np.mean(losses[:5]), (losses[:5], losses[-5:])
 
 
 def test_empty_and_invalid_training_calls(ctx, field):

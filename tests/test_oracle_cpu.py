@@ -132,10 +132,17 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_param_count_without_gpu():
-    """insta_field_param_count is pure host code and agrees with the Python layout."""
+    """insta_field_param_count is pure host code and agrees with the Python layout: the benchmark
+    field, INSTA's shipped layout (16 levels x 8 features, 16 expression dims, 2 + 3 hidden layers)
+    and 4 features per level; layouts the kernels do not take are rejected."""
     from insta_gb300 import abi, layout, synthetic as S
-    fc = S.FieldConfig()
-    assert abi.param_count(fc) == layout.field_layout(fc).total
+    for fc in (S.FieldConfig(), S.insta_field_config(), S.FieldConfig(n_levels=12, n_features=4, n_extra=16)):
+        assert abi.param_count(fc) == layout.field_layout(fc).total
+    assert S.insta_field_config().n_levels * S.insta_field_config().n_features == 128
+    for bad in (S.FieldConfig(n_features=1), S.FieldConfig(n_features=16, n_levels=16), S.FieldConfig(n_levels=6, n_features=2),
+                S.FieldConfig(n_levels=18, n_features=8)):
+        with pytest.raises(abi.InstaError):
+            abi.param_count(bad)
 
 
 def test_pcg32_published_sequence(oracle):

@@ -54,6 +54,12 @@ def test_snapshot_round_trip(tmp_path):
     fc = r.field_config()
     assert (fc.n_levels, fc.n_features, fc.log2_table, fc.base_res, fc.n_extra) == (16, 8, 18, 16, 16)
     assert (fc.density_hidden, fc.density_layers, fc.density_out, fc.rgb_hidden, fc.rgb_layers, fc.aabb_scale) == (64, 2, 16, 64, 3, 2)
+    # that is INSTA's shipped field, and the library takes it
+    from insta_gb300 import abi, layout, synthetic as S
+    want = S.insta_field_config()
+    assert (fc.n_levels, fc.n_features, fc.log2_table, fc.n_extra, fc.density_layers, fc.rgb_layers) == \
+        (want.n_levels, want.n_features, want.log2_table, want.n_extra, want.density_layers, want.rgb_layers)
+    assert abi.param_count(fc) == layout.field_layout(fc).total
 
 
 def test_snapshot_fp32_params_and_errors():
