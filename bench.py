@@ -39,13 +39,40 @@ SETTLE_S = 0.5   # untimed steps before the warm-up, long enough for the SM cloc
 # DRAM bytes (read + write) of the deform+encode stage per 512x512 frame (nearest_stage_kernel and
 # map_encode_kernel, two rounds each), from an ncu capture of this workload's kernels
 TRAFFIC_PER_FRAME = 431_540_000
-# Algorithmic bytes per sample of the dominant kernel (deform_encode): hash-grid gathers
-# (16 levels x 8 corners x 2 FP16 features) + sample record, ray direction and ray index in +
-# encoded operand row (32 + 16 FP16) and (dt, depth) out.
-HASH_BYTES_PER_SAMPLE = 16 * 8 * 2 * 2
-DEFORM_ENCODE_BYTES_PER_SAMPLE = HASH_BYTES_PER_SAMPLE + 16 + 16 + 4 + (32 + 16) * 2 + 8
-MLP_FLOP_PER_SAMPLE = 2 * (32 * 64 + 64 * 16 + 32 * 64 + 64 * 64 + 64 * 3)
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+FIELD = "benchmark"   # --field: the benchmark's 16 x 2 field, or INSTA's shipped 16 x 8 one
+
+
+def field_config():
+    from insta_gb300 import synthetic as S
+    return S.FieldConfig() if FIELD == "benchmark" else S.insta_field_config()
+
+
+def hash_bytes_per_sample(fc) -> int:
+    """Hash-grid gathers: levels x 8 corners x features x 2 B (FP16)."""
+    return fc.n_levels * 8 * fc.n_features * 2
+
+
+def deform_encode_bytes_per_sample(fc) -> int:
+    """Algorithmic bytes per sample of the dominant stage (deform + encode): the hash gathers +
+    sample record, ray direction and ray index in + the encoded operand row (hash features,
+    expression dims, 16 SH, FP16) and (dt, depth) out.  652 B for the benchmark field."""
+    return hash_bytes_per_sample(fc) + 16 + 16 + 4 + (fc.n_levels * fc.n_features + fc.n_extra + 16) * 2 + 8
+
+
+def mlp_flop_per_sample(fc) -> int:
+    """Unpadded MLP FLOP per sample: 18,816 for the benchmark field (32-64-16 / 32-64-64-3)."""
+    n_in = fc.n_levels * fc.n_features + fc.n_extra
+    macs = n_in * 64 + 64 * 64 * (fc.density_layers - 1) + 64 * 16 + 32 * 64 + 64 * 64 * (fc.rgb_layers - 1) + 64 * 3
+    return 2 * macs
+
+
+def field_label(fc) -> str:
+    if FIELD == "benchmark":
+        return "16-level hash grid T=2^19, MLPs 32-64-16 / 32-64-64-3"
+    n_in = fc.n_levels * fc.n_features + fc.n_extra
+    return (f"INSTA's shipped field: {fc.n_levels}-level hash grid x {fc.n_features} features T=2^{fc.log2_table} + "
+            f"{fc.n_extra} expression dims, MLPs {n_in}-64x{fc.density_layers}-16 / 32-64x{fc.rgb_layers}-3")
 
 
 def dist_env():
@@ -58,7 +85,7 @@ def dist_env():
 def workload(rank: int):
     from insta_gb300 import synthetic as S
     av = S.make_avatar(0)
-    fc = S.FieldConfig()
+    fc = field_config()
     params = S.field_params(fc, seed=0)
     frames = [av.frame(av.frame_coeffs(1000 * rank + k)) for k in range(4)]
     cams = [S.camera(yaw, width=WIDTH, height=HEIGHT) for yaw in (0.0, -8.0, 8.0, 15.0)]
@@ -157,7 +184,7 @@ def run_reference(args, rank, world):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000 * tot_t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32 geometry / fp16 mlp", "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"render {WIDTH}x{HEIGHT}, 1 avatar, 10240-triangle tracked mesh, 16-level hash grid",
+            "config": {"workload": f"render {WIDTH}x{HEIGHT}, 1 avatar, 10240-triangle tracked mesh, {field_label(fc)}",
                        "global_batch": 1, "parallelism": "cpu"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -310,7 +337,8 @@ def run_ours(args, rank, world, local):
     near_s = stage_ms.get("nearest", 0.0) / 1000.0
     de_s = near_s + stage_ms.get("deform_encode", 0.0) / 1000.0
     mlp_s = stage_ms["mlp"] / 1000.0
-    achieved = mean_samples * DEFORM_ENCODE_BYTES_PER_SAMPLE / de_s / 1e9
+    de_bytes, mlp_flop = deform_encode_bytes_per_sample(fc), mlp_flop_per_sample(fc)
+    achieved = mean_samples * de_bytes / de_s / 1e9
     # the walk's FP32 work from its counters (the stage-timing pass): 4 child boxes per inner node
     # for all 32 lanes at 12 FLOP, 15 FLOP per bounding-disk test, 60 per exact triangle test
     walk = stages["walk"]
@@ -327,7 +355,7 @@ def run_ours(args, rank, world, local):
         "ms_per_step": 1000.0 * dev_t / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32 geometry / fp16 mlp", "data": "synthetic",
         "config": {"workload": f"render {WIDTH}x{HEIGHT}, 1 avatar, 10240-triangle tracked mesh rebuilt per frame, "
-                               f"occupancy from mesh (1.5 cm), 16-level hash grid T=2^19, MLPs 32-64-16 / 32-64-64-3",
+                               f"occupancy from mesh (1.5 cm), {field_label(fc)}",
                    "global_batch": world, "samples_per_frame": mean_samples, "parallelism": f"replicas x{world}",
                    "l2": "flushed (512 MiB write) between timed steps", "frames_per_s": args.steps * world / dev_t,
                    "settle_s": SETTLE_S,
@@ -335,10 +363,10 @@ def run_ours(args, rank, world, local):
                                   "one CUDA-graph launch per frame (conditional while node over the rounds)"},
         "roofline": {"bound": "hbm", "kernel": "deform+encode stage (nearest_stage_kernel + map_encode_kernel)",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": TRAFFIC_PER_FRAME if WIDTH == 512 else None,
+                     "frac": achieved / hbm_peak, "traffic": TRAFFIC_PER_FRAME if WIDTH == 512 and FIELD == "benchmark" else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's launches for one "
                                        "512x512 frame, captured separately (not measured in this run)",
-                     "basis": f"{DEFORM_ENCODE_BYTES_PER_SAMPLE} B per sample (512 B hash gathers + stream in/out) "
+                     "basis": f"{de_bytes} B per sample ({hash_bytes_per_sample(fc)} B hash gathers + stream in/out) "
                               f"x samples per frame / deform_encode stage time per frame (CUDA events); per frame = "
                               f"its 2 launches, for achieved and traffic alike",
                      "peak_source": "MEASURED_PEAKS.json (of measured)" if peaks else "fallback"},
@@ -350,9 +378,9 @@ def run_ours(args, rank, world, local):
                                             "leaves": walk["leaves"] / max(walk["warps"], 1)},
                           "per_sample": {"bound_tests": walk["bound_tests"] / args.steps / mean_samples,
                                          "exact_tests": walk["exact_tests"] / args.steps / mean_samples}},
-        "roofline_tensor": {"kernel": "mlp256_kernel", "achieved": mean_samples * MLP_FLOP_PER_SAMPLE / mlp_s / 1e12,
-                            "peak": tflops_peak, "unit": "TFLOP/s",
-                            "frac": mean_samples * MLP_FLOP_PER_SAMPLE / mlp_s / 1e12 / tflops_peak},
+        "roofline_tensor": {"kernel": "mlp256_kernel", "achieved": mean_samples * mlp_flop / mlp_s / 1e12,
+                            "peak": tflops_peak, "unit": "TFLOP/s", "flop_per_sample": mlp_flop,
+                            "frac": mean_samples * mlp_flop / mlp_s / 1e12 / tflops_peak},
         "stage_ms_per_frame": stage_ms,
         "e2e": {"value": e2e_samples / e2e_t, "unit": UNIT, "h2d_bytes_per_step": int(av.n_verts * 12),
                 "d2h_bytes_per_step": int(WIDTH * HEIGHT * 20)},
@@ -581,7 +609,7 @@ def run_train(args):
     from insta_gb300 import abi, synthetic as S
     from insta_gb300.train import TrainConfig, TrainStep
     av = S.make_avatar(0)
-    fc = S.FieldConfig(n_extra=16)
+    fc = S.FieldConfig(n_extra=16) if FIELD == "benchmark" else S.insta_field_config()
     ctx = abi.Context(0)
     ctx.canonical_set(0, av.canonical, av.faces, av.mask)
     ctx.frame_upload(0, 0, av.frame(av.frame_coeffs(0)))
@@ -625,10 +653,10 @@ def run_train(args):
     ctx.stats_enable(False)
     stage = {k: v / args.steps for k, v in st["stage_ms"].items() if v > 0}
     dev_ms = sum(stage.values())
-    line = {"workload": "training step: 4096 rays, 2^18-sample batch, field with 16 expression dims",
+    line = {"workload": "training step: 4096 rays, 2^18-sample batch, " + ("field with 16 expression dims" if FIELD == "benchmark" else field_label(fc)),
             "train_math": {"tcgen05": "tcgen05 kernel: FP16 operands, FP32 accumulation in TMEM",
                            "tf32": "TF32 tensor-core layer products (cuBLAS), FP32 accumulation",
-                           "fp32": "FP32 layer products (cuBLAS)"}[args.train_math],
+                           "fp32": "FP32 layer products (cuBLAS)"}["tcgen05" if ts.tcgen05 else ("fp32" if args.train_math == "fp32" else "tf32")],
             "ms_per_step_device": dev_ms, "ms_per_step_wall": wall * 1e3, "stage_ms_per_step": stage,
             "march_samples_per_step": samples / args.steps,
             "trained_samples_per_s_device": cfg.target_batch_size / (dev_ms / 1e3),
@@ -917,14 +945,17 @@ def main():
     ap.add_argument("--tune", default="", help="launch shapes, e.g. max_steps_per_round=16,bvh_top_nodes=21 (insta_tuning_set)")
     ap.add_argument("--autotune", action="store_true", help="render: run insta_autotune on the frame before the warm-up")
     ap.add_argument("--train-math", choices=["tcgen05", "tf32", "fp32"], default="tcgen05", help="train: the backward's layer products")
+    ap.add_argument("--field", choices=["benchmark", "insta"], default="benchmark",
+                    help="render / reference arm: the benchmark's 16 x 2 field or INSTA's shipped 16 x 8 one (16 expression dims)")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--rate", type=float, default=240.0)
     ap.add_argument("--duration", type=float, default=30.0)
     ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--slot-pixels", type=int, default=6 << 20)
     args = ap.parse_args()
-    global WIDTH, HEIGHT
+    global WIDTH, HEIGHT, FIELD
     WIDTH = HEIGHT = args.width
+    FIELD = args.field
     if args.workload == "batch":
         return run_batch64(args)
     if args.workload == "serve":
