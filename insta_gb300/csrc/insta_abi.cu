@@ -1688,6 +1688,10 @@ int insta_field_backward_ex(insta_ctx* ctx, int avatar, const float* coords, uin
         if (dl_dextra && !(dl_dout && grad)) fail(INSTA_ERR_INVALID_ARG, "dl_dextra needs the backward (dl_dout and grad)");
         if (n == 0) return;
         const int extra_k = (dl_dextra && fd.desc.n_extra_dims) ? 1 : 0;
+        // the encode reads the FP16 copy of the training weights (under an Ema the field's own
+        // parameters are the average)
+        FieldView tv = fd.view;
+        if (fd.train_valid) tv.table = fd.train_view.table;
         if (ctx->train_tc) {
             ensure_master(ctx, fd);
             const TrainShape t = train_shape(fd);
@@ -1698,7 +1702,7 @@ int insta_field_backward_ex(insta_ctx* ctx, int avatar, const float* coords, uin
             ctx->alloc(ctx->train_images, plan.img_bytes);
             ctx->alloc(ctx->train_scratch, ((size_t)2 * t.kd + 32) * (size_t)n * 4);
             Stage st(ctx, INSTA_STAGE_TRAIN, ((dl_dout && grad) ? 4 : 3) + extra_k);
-            CK(launch_field_train_tc(fd.view, t, plan, images, (uint8_t*)ctx->train_images.p, (const float*)fd.w32.p, coords, stride,
+            CK(launch_field_train_tc(tv, t, plan, images, (uint8_t*)ctx->train_images.p, (const float*)fd.w32.p, coords, stride,
                                      (uint32_t)n, dl_dout, out4, grad, (float*)ctx->train_scratch.p, ctx->err_dev, ctx->stream, dl_dextra));
             return;
         }
@@ -1711,7 +1715,7 @@ int insta_field_backward_ex(insta_ctx* ctx, int avatar, const float* coords, uin
         const TrainShape t = train_shape(fd);
         ctx->alloc(ctx->train_scratch, train_scratch_floats(t, (uint32_t)n) * 4);
         Stage st(ctx, INSTA_STAGE_TRAIN, 8 + 2 * (t.n_density + t.n_rgb) + extra_k);
-        CK(launch_field_train(ctx->blas, fd.view, t, (const float*)fd.w32.p, coords, stride, (uint32_t)n, dl_dout, out4, grad,
+        CK(launch_field_train(ctx->blas, tv, t, (const float*)fd.w32.p, coords, stride, (uint32_t)n, dl_dout, out4, grad,
                               (float*)ctx->train_scratch.p, ctx->stream, dl_dextra));
     });
 }

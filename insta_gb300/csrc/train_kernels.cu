@@ -8,9 +8,10 @@
 //   backward   dX = W^T dY, then the ReLU mask of the layer's input
 //   weights    dW += dY X^T
 // The hash encode and its backward (scatter-add of each corner's weighted gradient into the
-// table, FP32 atomics) and the elementwise steps are kernels here.  Values are FP32 from the FP32
-// master weights (the FP16 parameters at first); the forward is that of the field evaluation in
-// FP32 (no FP16 rounding between layers).
+// table, FP32 atomics) and the elementwise steps are kernels here.  The encode gathers the FP16
+// copy of the training weights' table (as tiny-cuda-nn's mixed-precision training forward does);
+// the layer products take the FP32 master weights (FP32 / TF32 products) or their FP16 images
+// (the tcgen05 kernel); features and activations stay FP32 (no FP16 rounding between layers).
 #include <cublas_v2.h>
 
 #include "../../include/insta_gb300.h"
@@ -31,89 +32,32 @@ __device__ __forceinline__ uint32_t corner_index(const FieldView& fv, uint32_t l
     return ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
 }
 
-// One level of the hash encoding from the FP32 master table ([entries][F] floats, F = 4 or 8),
-// the same index arithmetic and summation order as hash_level / hash_level_wide.
+// Encode: X_d[:, 0:E] = hash encoding (E = levels x features), X_d[:, E:E+n_extra] = the record's
+// expression dims, X_r[:, 16:32] = SH of the direction (X_r[:, 0:16] is filled by the density
+// MLP's output).  The table entries come from fv.table: the FP16 copy of the training weights, as
+// tiny-cuda-nn's mixed-precision training forward reads its half-precision grid (the FP32 master
+// weights stay with the optimizer); the same gathers, weights and summation order as the render's
+// encode (hash_level / hash_level_wide), the features kept in FP32.
 template <int F>
-__device__ __forceinline__ void hash_level_f32_wide(const FieldView& fv, const float* __restrict__ table, V3 x, uint32_t l, float* a) {
-    const float s = fv.level_scale[l];
-    const float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);
-    const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
-    const float rx = __fsub_rn(px, fx), ry = __fsub_rn(py, fy), rz = __fsub_rn(pz, fz);
-    const uint32_t gx = (uint32_t)(int32_t)fx, gy = (uint32_t)(int32_t)fy, gz = (uint32_t)(int32_t)fz;
-    const float4* lt = reinterpret_cast<const float4*>(table + (size_t)fv.level_off[l] * F);
-#pragma unroll
-    for (int f = 0; f < F; ++f) a[f] = 0.f;
-#pragma unroll
-    for (uint32_t c = 0; c < 8; ++c) {
-        const uint32_t bx = c & 1u, by = (c >> 1) & 1u, bz = (c >> 2) & 1u;
-        float w = bx ? rx : __fsub_rn(1.f, rx);
-        w = __fmul_rn(w, by ? ry : __fsub_rn(1.f, ry));
-        w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
-        const uint32_t idx = corner_index(fv, l, gx + bx, gy + by, gz + bz);
-#pragma unroll
-        for (int q = 0; q < F / 4; ++q) {
-            const float4 e = __ldg(lt + (size_t)idx * (F / 4) + q);
-            a[4 * q + 0] = __fadd_rn(a[4 * q + 0], __fmul_rn(w, e.x));
-            a[4 * q + 1] = __fadd_rn(a[4 * q + 1], __fmul_rn(w, e.y));
-            a[4 * q + 2] = __fadd_rn(a[4 * q + 2], __fmul_rn(w, e.z));
-            a[4 * q + 3] = __fadd_rn(a[4 * q + 3], __fmul_rn(w, e.w));
-        }
-    }
-}
-
-// One level of the hash encoding from the FP32 master table ([entries][2] floats), the same
-// index arithmetic and summation order as hash_level.
-__device__ __forceinline__ void hash_level_f32(const FieldView& fv, const float2* __restrict__ table, V3 x, uint32_t l, float& a0, float& a1) {
-    const float s = fv.level_scale[l];
-    const float px = fmaf(x.x, s, 0.5f), py = fmaf(x.y, s, 0.5f), pz = fmaf(x.z, s, 0.5f);
-    const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
-    const float rx = __fsub_rn(px, fx), ry = __fsub_rn(py, fy), rz = __fsub_rn(pz, fz);
-    const uint32_t gx = (uint32_t)(int32_t)fx, gy = (uint32_t)(int32_t)fy, gz = (uint32_t)(int32_t)fz;
-    const uint32_t res = fv.level_res[l], size = fv.level_size[l];
-    const float2* lt = table + fv.level_off[l];
-    a0 = 0.f;
-    a1 = 0.f;
-#pragma unroll
-    for (uint32_t c = 0; c < 8; ++c) {
-        const uint32_t bx = c & 1u, by = (c >> 1) & 1u, bz = (c >> 2) & 1u;
-        float w = bx ? rx : __fsub_rn(1.f, rx);
-        w = __fmul_rn(w, by ? ry : __fsub_rn(1.f, ry));
-        w = __fmul_rn(w, bz ? rz : __fsub_rn(1.f, rz));
-        const uint32_t cx = gx + bx, cy = gy + by, cz = gz + bz;
-        uint32_t idx;
-        if (fv.level_dense[l]) {
-            idx = cx + cy * res + cz * res * res;
-            if (idx >= size) idx %= size;
-        } else {
-            idx = ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
-        }
-        const float2 e = __ldg(lt + idx);
-        a0 = __fadd_rn(a0, __fmul_rn(w, e.x));
-        a1 = __fadd_rn(a1, __fmul_rn(w, e.y));
-    }
-}
-
-// Encode: X_d[:, 0:32] = hash encoding, X_d[:, 32:32+n_extra] = the record's expression dims,
-// X_r[:, 16:32] = SH of the direction (X_r[:, 0:16] is filled by the density MLP's output).
-__global__ void __launch_bounds__(256) train_encode_kernel(FieldView fv, const float2* __restrict__ table32, const float* __restrict__ coords,
-                                                           uint32_t stride, uint32_t n, float* __restrict__ xd, uint32_t kd,
-                                                           float* __restrict__ xr) {
+__global__ void __launch_bounds__(256) train_encode_kernel(FieldView fv, const float* __restrict__ coords, uint32_t stride, uint32_t n,
+                                                           float* __restrict__ xd, uint32_t kd, float* __restrict__ xr) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* c = coords + (size_t)i * stride;
     const V3 p = v3(c[0], c[1], c[2]);
+    const __half2* t2 = reinterpret_cast<const __half2*>(fv.table);
     float* x = xd + (size_t)i * kd;
-    const uint32_t F = fv.n_features;
     for (uint32_t l = 0; l < fv.n_levels; ++l) {
-        if (F == 8) {
-            hash_level_f32_wide<8>(fv, reinterpret_cast<const float*>(table32), p, l, x + 8 * l);
-        } else if (F == 4) {
-            hash_level_f32_wide<4>(fv, reinterpret_cast<const float*>(table32), p, l, x + 4 * l);
-        } else {
+        if constexpr (F == 2) {
             float a0, a1;
-            hash_level_f32(fv, table32, p, l, a0, a1);
+            hash_level(fv, t2, p, l, a0, a1);
             x[2 * l] = a0;
             x[2 * l + 1] = a1;
+        } else {
+            float a[F];
+            hash_level_wide<F>(fv, t2, p, l, a);
+#pragma unroll
+            for (int f = 0; f < F; ++f) x[F * l + f] = a[f];
         }
     }
     for (uint32_t m = 0; m < fv.n_extra; ++m) x[F * fv.n_levels + m] = c[stride - fv.n_extra + m];
@@ -122,6 +66,14 @@ __global__ void __launch_bounds__(256) train_encode_kernel(FieldView fv, const f
     float* r = xr + (size_t)i * 32 + 16;
 #pragma unroll
     for (int k = 0; k < 16; ++k) r[k] = sh[k];
+}
+
+static void launch_train_encode(const FieldView& fv, const float* coords, uint32_t stride, uint32_t n, float* xd, uint32_t kd, float* xr,
+                                cudaStream_t s) {
+    const unsigned blocks = (n + 255) / 256;
+    if (fv.n_features == 8) train_encode_kernel<8><<<blocks, 256, 0, s>>>(fv, coords, stride, n, xd, kd, xr);
+    else if (fv.n_features == 4) train_encode_kernel<4><<<blocks, 256, 0, s>>>(fv, coords, stride, n, xd, kd, xr);
+    else train_encode_kernel<2><<<blocks, 256, 0, s>>>(fv, coords, stride, n, xd, kd, xr);
 }
 
 __global__ void __launch_bounds__(256) relu_kernel(float* __restrict__ h, size_t count) {
@@ -836,8 +788,7 @@ cudaError_t launch_field_train(cublasHandle_t h, const FieldView& fv, const Trai
     for (int l = 0; l + 1 < t.n_rgb; ++l) { dhr[l] = p; p += (size_t)64 * n; }
     float* dyr = p; p += (size_t)16 * n;
 
-    train_encode_kernel<<<(n + 255) / 256, 256, 0, s>>>(fv, reinterpret_cast<const float2*>(w32 + t.table_off), coords, stride, n, xd, t.kd,
-                                                        xr);
+    launch_train_encode(fv, coords, stride, n, xd, t.kd, xr, s);
     bool okb = true;
     // density MLP: hidden layers then the 16 outputs into X_r rows 0..15
     const float* in = xd;
@@ -903,8 +854,7 @@ cudaError_t launch_field_train_tc(const FieldView& fv, const TrainShape& t, cons
     float* xd = scratch;
     float* xr = xd + (size_t)t.kd * n;
     float* dxd = xr + (size_t)32 * n;
-    train_encode_kernel<<<(n + 255) / 256, 256, 0, s>>>(fv, reinterpret_cast<const float2*>(w32 + t.table_off), coords, stride, n, xd, t.kd,
-                                                        xr);
+    launch_train_encode(fv, coords, stride, n, xd, t.kd, xr, s);
     const bool bwd = dl_dout && grad;
     TrainMlpArgs a{};
     a.plan = plan;
