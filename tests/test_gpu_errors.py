@@ -40,8 +40,8 @@ def test_missing_state_and_bad_arguments():
     assert code_of(lambda: ctx.render_batch(big, [out[0]] * 33, [out[1]] * 33)) == 1
     assert code_of(lambda: ctx.occupancy_from_mesh(0, 0, -1.0)) == 1       # bad radius
     assert code_of(lambda: ctx.occupancy_get(0, 5)) == 4                   # unknown frame
-    fc16 = S.FieldConfig(n_levels=8)
-    assert code_of(lambda: ctx.params_load(1, fc16, np.zeros(10, np.float16))) == 5   # unsupported shape
+    fc12 = S.FieldConfig(n_levels=6)     # 12 hash features: not whole 8-feature groups
+    assert code_of(lambda: ctx.params_load(1, fc12, np.zeros(10, np.float16))) == 5   # unsupported shape
     ctx.close()
 
 
