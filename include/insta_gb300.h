@@ -465,7 +465,7 @@ int insta_render_samples(insta_ctx* ctx, uint64_t* n_samples);
  * the built-in choice.  Results do not depend on these (every sample's arithmetic is the same;
  * rays composite their samples in order): only speed does. */
 typedef struct insta_tuning {
-    uint32_t max_steps_per_round;   /* 1..32 (built-in 32) */
+    uint32_t max_steps_per_round;   /* 1..128 (built-in 64) */
     uint32_t sort_cell_bits;        /* 12, 15, 18 or 21: Morton cells of a round's (request, cell) sort
                                        (built-in 18 = 64^3 per request, fewer when requests x cells > 4 Mi) */
     uint32_t mlp_ctas_per_sm;       /* 1..4 resident MLP CTAs per SM (built-in: as many as shared memory allows) */

@@ -474,13 +474,18 @@ void check_request(const insta_render_desc* r) {
     if (r->out_samples && !is_device_ptr(r->out_samples)) fail(INSTA_ERR_INVALID_ARG, "out_samples must be device memory");
 }
 
-// Largest number of samples one round may produce (bounds the per-sample scratch, ~160 B each).
+// Largest number of samples one round may produce (bounds the per-sample scratch, ~160 B each),
+// and the most pixels (ray slots) one batch may hold.
 constexpr uint64_t kMaxRoundSamples = 32ull << 20;
-constexpr uint32_t kMaxSteps = 32;
+constexpr uint64_t kMaxBatchPixels = 1ull << 25;
+// Samples per alive ray per round: at most kMaxSteps, built-in kDefaultSteps.  With 64 a 512x512
+// frame of the benchmark finishes in one round (a second round of the few long rays ran at low
+// occupancy: 1.89 -> 1.76 ms per frame); the round budget caps it for large batches.
+constexpr uint32_t kMaxSteps = 128, kDefaultSteps = 64;
 static_assert(kMaxSteps <= (1u << (32 - kStepShift)), "step index must fit beside the ray slot");
 
 // The wavefront's launch shapes under the context's tuning (zero fields: built-in choices).
-uint32_t tune_steps(const insta_ctx* ctx) { return ctx->tune.max_steps_per_round ? ctx->tune.max_steps_per_round : kMaxSteps; }
+uint32_t tune_steps(const insta_ctx* ctx) { return ctx->tune.max_steps_per_round ? ctx->tune.max_steps_per_round : kDefaultSteps; }
 // Built-in sort grid: 64^3 cells per request while the bins stay within 4 Mi (a round's
 // counting sort clears and scans them), else 32^3 (16^3 beyond 128 request slots).
 uint32_t tune_cell_bits(const insta_ctx* ctx, uint32_t slots) {
@@ -489,7 +494,7 @@ uint32_t tune_cell_bits(const insta_ctx* ctx, uint32_t slots) {
     while (b > 12u && ((uint64_t)slots << b) > (4ull << 20)) b -= 3u;
     return b;
 }
-static_assert((1u << 26) <= kRayMask + 1u, "ray slots (at most 2^26 pixels per batch) must fit below the step index");
+static_assert(kMaxBatchPixels <= (uint64_t)kRayMask + 1u, "ray slots (at most 2^25 pixels per batch) must fit below the step index");
 
 bool same_field_layout(const Field& a, const Field& b) {
     return std::memcmp(&a.plan, &b.plan, sizeof(TilePlan)) == 0 && a.view.n_levels == b.view.n_levels &&
@@ -524,7 +529,7 @@ ReqView request_view(insta_ctx* ctx, const insta_render_desc& r, Avatar& a, Fram
 struct WaveRun {
     insta_ctx* ctx = nullptr;
     uint32_t n_slots = 0;
-    uint32_t steps_max = kMaxSteps;   // samples per alive ray per round, at most
+    uint32_t steps_max = kDefaultSteps;   // samples per alive ray per round, at most
     uint64_t round_cap = 0, cap_samples = 0;
     WaveArgs W{};
     MlpArgs M{};
@@ -804,7 +809,7 @@ void render_batch(insta_ctx* ctx, const insta_render_desc* reqs, int n, float* c
         max_spr = std::max(max_spr, views[(size_t)i].rv.max_samples_per_ray);
     }
     // a round takes at least one sample per alive ray: the pixels must fit one round's buffers
-    if (total_pix > kMaxRoundSamples) fail(INSTA_ERR_INVALID_ARG, "a batch holds at most 2^25 pixels, got %llu", (unsigned long long)total_pix);
+    if (total_pix > kMaxBatchPixels) fail(INSTA_ERR_INVALID_ARG, "a batch holds at most 2^25 pixels, got %llu", (unsigned long long)total_pix);
     // outputs: device pointers directly, host pointers through one staging buffer
     float* stage_rgba = nullptr;
     float* stage_depth = nullptr;
@@ -1979,7 +1984,7 @@ int insta_autotune(insta_ctx* ctx, const insta_render_desc* reqs, int n, int rep
         float cur_ms = 0.f;
         try {
             cur_ms = time_one(cur);
-            const std::vector<uint32_t> cands[7] = {{8, 16, 24, 32}, {15, 18, 21}, {1, 2, 3, 4}, {8, 12, 16, 24}, {0, 5, 21}, {0, 1},
+            const std::vector<uint32_t> cands[7] = {{8, 16, 32, 64, 96, 128}, {15, 18, 21}, {1, 2, 3, 4}, {8, 12, 16, 24}, {0, 5, 21}, {0, 1},
                                                     {1, 7, 8}};
             for (int pass = 0; pass < 2; ++pass) {
                 bool moved = false;
@@ -2418,7 +2423,7 @@ int insta_server_create(insta_ctx* ctx, const insta_server_config* cfg, insta_se
     return guarded(ctx, [&] {
         if (!cfg || !out) fail(INSTA_ERR_INVALID_ARG, "null config or output");
         if (cfg->max_inflight < 1 || cfg->max_inflight > 256) fail(INSTA_ERR_INVALID_ARG, "max_inflight must be 1..256");
-        if (cfg->max_inflight_pixels < 1 || cfg->max_inflight_pixels > kMaxRoundSamples)
+        if (cfg->max_inflight_pixels < 1 || cfg->max_inflight_pixels > kMaxBatchPixels)
             fail(INSTA_ERR_INVALID_ARG, "max_inflight_pixels must be 1..2^25");
         if (!(cfg->occupancy_radius > 0.0)) fail(INSTA_ERR_INVALID_ARG, "occupancy_radius must be positive");
         if (cfg->rounds_per_launch % 2 || cfg->rounds_per_launch > 64) fail(INSTA_ERR_INVALID_ARG, "rounds_per_launch must be even, 0..64");

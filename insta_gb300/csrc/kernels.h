@@ -52,7 +52,7 @@ struct ReqView {
 // rays they came from.  Each request's run of samples is padded to a multiple of 128 so every
 // MLP tile belongs to one request (one avatar's weights).
 constexpr uint32_t kSortBlock = 1024, kMaxSortBins = 1u << 24, kMaxRequests = 4096;
-constexpr uint32_t kStepShift = 27, kRayMask = (1u << kStepShift) - 1u;
+constexpr uint32_t kStepShift = 25, kRayMask = (1u << kStepShift) - 1u;
 constexpr uint32_t kNoSample = 0xffffffffu;
 
 // cell bits per request (multiple of 3, >= 12) so that n_reqs << bits stays within kMaxSortBins

@@ -140,6 +140,8 @@ def test_render_512_multi_round_bit_identical(full, frame512):
     assert np.array_equal(m_rgba, rgba) and np.array_equal(m_depth, depth) and np.array_equal(m_counts, counts)
     h_rgba, h_depth, h_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(max_steps_per_round=5), host_rounds=True)
     assert np.array_equal(h_rgba, rgba) and np.array_equal(h_depth, depth) and np.array_equal(h_counts, counts)
+    w_rgba, w_depth, w_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(max_steps_per_round=64))   # the longest rounds
+    assert np.array_equal(w_rgba, rgba) and np.array_equal(w_depth, depth) and np.array_equal(w_counts, counts)
     s_rgba, s_depth, s_counts, _ = render_gpu(ctx, 512, 512, tuning=dict(sort_cell_bits=15, mlp_ctas_per_sm=1,
                                                                           deform_blocks_per_sm=8, bvh_top_nodes=21))
     assert np.array_equal(s_rgba, rgba) and np.array_equal(s_depth, depth) and np.array_equal(s_counts, counts)
