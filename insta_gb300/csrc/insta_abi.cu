@@ -479,8 +479,9 @@ void check_request(const insta_render_desc* r) {
 constexpr uint64_t kMaxRoundSamples = 32ull << 20;
 constexpr uint64_t kMaxBatchPixels = 1ull << 25;
 // Samples per alive ray per round: at most kMaxSteps, built-in kDefaultSteps.  With 64 a 512x512
-// frame of the benchmark finishes in one round (a second round of the few long rays ran at low
-// occupancy: 1.89 -> 1.76 ms per frame); the round budget caps it for large batches.
+// frame of the benchmark takes nearly all of its samples in the first round (with 32, a second
+// round of about a tenth of them ran at low occupancy: 1.89 -> 1.76 ms per frame); the round
+// budget caps it for large batches.
 constexpr uint32_t kMaxSteps = 128, kDefaultSteps = 64;
 static_assert(kMaxSteps <= (1u << (32 - kStepShift)), "step index must fit beside the ray slot");
 
