@@ -101,6 +101,7 @@ constexpr uint32_t kWarpQueue = 32u * (INSTA_LEAF_SIZE + 1);   // < 32 pending +
 // Per-warp shared scratch of nearest_warp.
 struct WarpScratch {
     uint32_t stack[INSTA_STACK];   // node references of the shared traversal stack
+    uint32_t skey[INSTA_STACK];    // per entry: the smallest box distance (bits) of the lanes that pushed it
     uint32_t queue[kWarpQueue];    // pending exact tests: Morton slot << 5 | owner lane
     unsigned long long best[32];   // per lane: (distance bits << 32) | triangle id, the running minimum
 };
@@ -137,7 +138,11 @@ __device__ __forceinline__ void flush_tests(const FrameView& fr, WarpScratch& ws
 // Warp-cooperative variant for spatially coherent queries (one point per lane, all 32 lanes call
 // it together).  The warp walks the union of the nodes its lanes need with one shared stack: a
 // node is fetched once per warp, every lane tests it against its own point and bound, and a child
-// is pushed when any lane may find a nearer triangle in it.  At a leaf, the (triangle, lane) pairs
+// is pushed when any lane may find a nearer triangle in it.  The stack holds, beside each node,
+// the smallest box distance among the lanes that wanted it (warp-uniform, in shared memory): a
+// popped node is skipped when that exceeds every lane's current prune limit, so no per-lane
+// distances are kept (no local-memory stack; measured on the 512x512 frame: 6 % more inner nodes,
+// nearest stage 0.965 -> 0.920 ms).  At a leaf, the (triangle, lane) pairs
 // that lanes need are queued and run 32 at a time, one per lane, so the exact tests are not
 // replicated across lanes that do not need them.  Each lane's result is exactly its own nearest
 // triangle, ties to the lowest id (the union holds every node that lane's own traversal would
@@ -155,22 +160,22 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
     const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
     float best = active ? bound : -INF;
     int32_t bid = -1;
-    float dstack[INSTA_STACK];
     int sp = 0;
     uint32_t qlen = 0;
     __syncwarp();
     ws.best[lane] = ((unsigned long long)__float_as_uint(best) << 32) | 0xffffffffull;
-    if (lane == 0) ws.stack[0] = 0u;
+    if (lane == 0) { ws.stack[0] = 0u; ws.skey[0] = 0u; }
     __syncwarp();
-    dstack[0] = active ? 0.f : INF;
     sp = 1;
     float lim = prune_limit(best);   // changes only when a flush lowers best
+    // the warp's largest prune limit (bits; limits are >= 0, inactive lanes count as 0)
+    uint32_t lim_max = __reduce_max_sync(0xffffffffu, active ? __float_as_uint(lim) : 0u);
     while (sp > 0) {
         --sp;
         const uint32_t ref = ws.stack[sp];
-        const bool need = dstack[sp] <= lim;
+        if (ws.skey[sp] > lim_max) continue;   // no lane can find anything nearer below it
+        const bool need = active;
         const uint32_t nm = __ballot_sync(0xffffffffu, need);
-        if (!nm) continue;
         if (ref & INSTA_LEAF_BIT) {
             // a lane queues a triangle of the leaf only when the triangle's bounding disk may
             // hold a point nearer than its prune limit (leaf_bound_sq)
@@ -190,6 +195,7 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
                 do flush_tests(fr, ws, p, 32u, qlen, best, bid);
                 while (qlen >= 32u);
                 lim = prune_limit(best);
+                lim_max = __reduce_max_sync(0xffffffffu, active ? __float_as_uint(lim) : 0u);
             }
             continue;
         }
@@ -238,8 +244,7 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
         for (int i = 0; i < 4; ++i) {
             if (key[i] != 0xffffffffu) {
                 if (sp < INSTA_STACK) {
-                    if (lane == 0) ws.stack[sp] = ci[i];
-                    dstack[sp] = active ? cd[i] : INF;
+                    if (lane == 0) { ws.stack[sp] = ci[i]; ws.skey[sp] = key[i]; }
                     ++sp;
                 } else if (err && lane == 0) {
                     atomicOr(err, INSTA_DEVERR_STACK);
