@@ -226,7 +226,7 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
             key[i] = __reduce_min_sync(0xffffffffu, want ? __float_as_uint(cd[i]) : 0xffffffffu);
         }
         // sort the children farthest-first (keys are warp-uniform; every index is static, so the
-        // tuples stay in registers) and push the needed ones: the warp pops the nearest next.
+        // pairs stay in registers) and push the needed ones: the warp pops the nearest next.
         // With at most one child wanted there is nothing to order.
         const int wanted = (key[0] != 0xffffffffu) + (key[1] != 0xffffffffu) + (key[2] != 0xffffffffu) + (key[3] != 0xffffffffu);
         if (wanted > 1) {
@@ -234,7 +234,6 @@ __device__ __forceinline__ Nearest nearest_warp(const FrameView& fr, V3 p, bool 
     if (key[x] < key[y]) {                                                                \
         uint32_t tk = key[x]; key[x] = key[y]; key[y] = tk;                               \
         uint32_t tc = ci[x]; ci[x] = ci[y]; ci[y] = tc;                                   \
-        float td = cd[x]; cd[x] = cd[y]; cd[y] = td;                                      \
     }
             INSTA_CASK(0, 2) INSTA_CASK(1, 3) INSTA_CASK(0, 1) INSTA_CASK(2, 3) INSTA_CASK(1, 2)
 #undef INSTA_CASK
