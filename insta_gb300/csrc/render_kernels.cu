@@ -794,19 +794,31 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
             float4 rgba = rc;
             float depth = rd.x, maxw = rb.w;
             uint32_t j = 0, used = m;   // samples composited this round
-            for (; j < m; ++j) {
-                const uint32_t s = A.sample_index[(size_t)j * n_alive + r];
-                float o[4];
+            // The loads run ahead of the arithmetic: the next sample's outputs and the sorted
+            // position of the one after are in flight while this sample is composited (loads
+            // past an early termination are dropped unused).
+            auto load = [&](uint32_t s, float4& v, float2& ax) {
                 if (f32_out) {
-                    float4 v = A.out_f32[s];
-                    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+                    v = A.out_f32[s];
                 } else {
-                    uint2 u = A.out[s];
-                    float2 rg = __half22float2(*reinterpret_cast<__half2*>(&u.x));
-                    float2 bd = __half22float2(*reinterpret_cast<__half2*>(&u.y));
-                    o[0] = rg.x; o[1] = rg.y; o[2] = bd.x; o[3] = bd.y;
+                    const uint2 u = A.out[s];
+                    const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+                    const float2 bd = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+                    v = make_float4(rg.x, rg.y, bd.x, bd.y);
                 }
-                const float2 ax = A.aux[s];
+                ax = A.aux[s];
+            };
+            float4 v_next = make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 ax_next = make_float2(0.f, 0.f);
+            uint32_t s_after = 0;
+            if (m > 0) load(A.sample_index[r], v_next, ax_next);
+            if (m > 1) s_after = A.sample_index[(size_t)n_alive + r];
+            for (; j < m; ++j) {
+                const float4 v = v_next;
+                const float2 ax = ax_next;
+                if (j + 1 < m) load(s_after, v_next, ax_next);
+                if (j + 2 < m) s_after = A.sample_index[(size_t)(j + 2) * n_alive + r];
+                const float o[4] = {v.x, v.y, v.z, v.w};
                 // composite_kernel_nerf (ngp/src/testbed_nerf.cu:840-999)
                 const float T = 1.f - rgba.w;
                 const float dtu = unwarp_dt(warp_dt(ax.x));
