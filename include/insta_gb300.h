@@ -203,8 +203,9 @@ typedef struct insta_pcg32 {
  * surface_closest_point hook on the sample positions (warp_random_samples, src/core.cu:528-579):
  * n_uniform samples over all cells and n_nonuniform over cells above the minimum optical
  * thickness, each warped to the canonical space through a random one of frames 0..n_frames-1
- * (the reference's m_meshes.size() - 1), density network at the canonical position, max splat
- * into a fresh grid, then grid = max(grid * decay, new) (negative cells kept) and, for
+ * (the reference's m_meshes.size() - 1), density network at the canonical position (a field
+ * with expression dims gets 1 in each of them, as NerfNetwork::density feeds them,
+ * NGP/nerf_network.h:107-127,401-410), max splat into a fresh grid, then grid = max(grid * decay, new) (negative cells kept) and, for
  * bitfield_frame >= 0, that frame's bitfield (update_density_grid_mean_and_bitfield).
  * training_prep_nerf (:3427-3444) calls it with 128^3 * n_cascades uniform samples for the
  * first 256 steps, then 128^3 / 4 * n_cascades of each kind. */

@@ -1269,9 +1269,6 @@ int insta_density_grid_update(insta_ctx* ctx, int avatar, insta_density_update_d
         if (!a.density_grid.p) fail(INSTA_ERR_NOT_READY, "avatar %d has no density grid (insta_density_grid_reset)", avatar);
         if (d->n_cascades != a.grid_cascades)
             fail(INSTA_ERR_INVALID_ARG, "n_cascades %u differs from the grid's %u", d->n_cascades, a.grid_cascades);
-        if (a.field.desc.n_extra_dims != 0)
-            fail(INSTA_ERR_UNSUPPORTED, "the density-grid update evaluates fields without expression dims (this field has %u)",
-                 a.field.desc.n_extra_dims);
         const uint64_t n64 = (uint64_t)d->n_uniform + d->n_nonuniform;
         if (n64 == 0 || n64 >= (1ull << 30)) fail(INSTA_ERR_INVALID_ARG, "sample count must be 1 .. 2^30 - 1, got %llu", (unsigned long long)n64);
         if (d->n_frames < 1) fail(INSTA_ERR_INVALID_ARG, "n_frames must be >= 1");
@@ -1317,7 +1314,9 @@ int insta_density_grid_update(insta_ctx* ctx, int avatar, insta_density_update_d
                                      cudaMemcpyDefault, ctx->stream));
             if (d->debug_idx) CK(cudaMemcpyAsync(d->debug_idx, idx, (size_t)n * sizeof(uint32_t), cudaMemcpyDefault, ctx->stream));
             CK(cudaMemsetAsync(w.tiles.p, 0, tiles * P.tile_bytes, ctx->stream));
-            CK(launch_encode_coords(a.field.view, coords, stride, n, (uint8_t*)w.tiles.p, P.tile_bytes, P.k_in, ctx->stream));
+            // a field with expression dims gets 1 in each of them (NerfNetwork::density,
+            // NGP/nerf_network.h:107-127,401-410: the per-sample random code is disabled there)
+            CK(launch_encode_coords(a.field.view, coords, stride, n, (uint8_t*)w.tiles.p, P.tile_bytes, P.k_in, ctx->stream, true));
             MlpArgs m{};
             m.fv = a.field.view; m.plan = P; m.tiles = (const uint8_t*)w.tiles.p; m.n_alive = nullptr; m.n_samples = n;
             m.out = (uint2*)w.out.p; m.out_f32 = (float4*)w.out_f32.p; m.err = ctx->err_dev;

@@ -187,8 +187,10 @@ struct TrainArgs {
 cudaError_t launch_training_samples(const TrainArgs& a, float* tbuf, cudaStream_t s);
 constexpr int64_t kTrainMarchOnceMaxRays = 1 << 16;   // larger batches march twice (no per-ray buffer)
 
+// extra_ones: every expression dim 1 instead of the records' last n_extra floats (the density-grid
+// update's density evaluation)
 cudaError_t launch_encode_coords(const FieldView& fv, const float* coords, uint32_t stride, int64_t n, uint8_t* tiles,
-                                 uint32_t tile_bytes, uint32_t k_in, cudaStream_t s);
+                                 uint32_t tile_bytes, uint32_t k_in, cudaStream_t s, bool extra_ones = false);
 cudaError_t launch_unpack(const uint2* out, const float4* out_f32, int bf16, int64_t n, float4* dst, cudaStream_t s);
 // Fixed device scratch of insta_field_eval_static (static_scratch.cu); first call per device looks it up.
 int64_t static_max_samples();

@@ -858,15 +858,18 @@ __global__ void composite_kernel(const __grid_constant__ WaveArgs A) {
 }
 
 // ------------------------------------------------------------------ field eval (parity entry)
+// mask: 7 = the expression dims from the record's last n_extra floats; any other value = every
+// expression dim 1 (the density-grid update, as NerfNetwork::density feeds them,
+// NGP/nerf_network.h:107-127,401-410).
 template <int F>
 __global__ void __launch_bounds__(256) encode_coords_kernel(FieldView fv, const float* __restrict__ coords, uint32_t stride,
-                                                            int64_t n, uint8_t* tiles, uint32_t tile_bytes, uint32_t k_in) {
+                                                            int64_t n, uint8_t* tiles, uint32_t tile_bytes, uint32_t k_in, uint32_t mask) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* c = coords + i * stride;
     float pos[3] = {c[0], c[1], c[2]}, dir[3] = {c[8], c[9], c[10]};
     uint8_t* rec = tiles + (size_t)(i >> 7) * tile_bytes;
-    encode_sample<F>(fv, fv.table, c + stride - fv.n_extra, 7u, pos, dir, rec, (uint32_t)(i & 127), k_in);
+    encode_sample<F>(fv, fv.table, mask == 7u ? c + stride - fv.n_extra : nullptr, mask, pos, dir, rec, (uint32_t)(i & 127), k_in);
 }
 
 __global__ void unpack_outputs_kernel(const uint2* __restrict__ out, const float4* __restrict__ out_f32, int bf16, int64_t n, float4* dst) {
@@ -1179,12 +1182,13 @@ cudaError_t launch_composite(const WaveArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_encode_coords(const FieldView& fv, const float* coords, uint32_t stride, int64_t n, uint8_t* tiles,
-                                 uint32_t tile_bytes, uint32_t k_in, cudaStream_t s) {
+                                 uint32_t tile_bytes, uint32_t k_in, cudaStream_t s, bool extra_ones) {
     if (n <= 0) return cudaSuccess;
     const unsigned grid = (unsigned)((n + 255) / 256);
-    if (fv.n_features == 8) encode_coords_kernel<8><<<grid, 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in);
-    else if (fv.n_features == 4) encode_coords_kernel<4><<<grid, 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in);
-    else encode_coords_kernel<2><<<grid, 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in);
+    const uint32_t mask = extra_ones ? 0u : 7u;
+    if (fv.n_features == 8) encode_coords_kernel<8><<<grid, 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in, mask);
+    else if (fv.n_features == 4) encode_coords_kernel<4><<<grid, 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in, mask);
+    else encode_coords_kernel<2><<<grid, 256, 0, s>>>(fv, coords, stride, n, tiles, tile_bytes, k_in, mask);
     return cudaGetLastError();
 }
 

@@ -23,14 +23,15 @@ N_CASCADES = 2
 MIN_CONE = np.float32(1.73205080757) / np.float32(1024)
 
 
-@pytest.fixture(scope="module")
-def grid_avatar(ctx, avatar):
+@pytest.fixture(scope="module", params=["benchmark", "insta"])
+def grid_avatar(ctx, avatar, request):
+    """The benchmark field and INSTA's shipped one (16 levels x 8 features, expression dims)."""
     from insta_gb300 import synthetic as S
     ctx.canonical_set(AVATAR, avatar.canonical, avatar.faces, avatar.mask)
     frames = [avatar.frame(avatar.frame_coeffs(20 + k)) for k in range(3)]
     for k, f in enumerate(frames):
         ctx.frame_upload(AVATAR, k, f)
-    fc = S.FieldConfig()
+    fc = S.FieldConfig() if request.param == "benchmark" else S.insta_field_config()
     params = S.field_params(fc, seed=4)
     ctx.params_load(AVATAR, fc, params)
     ctx.sync()
@@ -90,9 +91,11 @@ def test_density_grid_update(ctx, oracle, avatar, grid_avatar):
     assert np.abs(pos - wpos).max() <= 1e-5 * diag
 
     # splat + decay
-    coords = np.zeros((n, 11), np.float32)
+    # (a field with expression dims gets 1 in each, NerfNetwork::density's fill)
+    coords = np.zeros((n, 11 + fc.n_extra), np.float32)
     coords[:, :3] = wpos
     coords[:, 8:11] = 0.5
+    coords[:, 11:] = 1.0
     raw = oracle.field_eval(fc, params, coords)[:, 3]
     thick = (np.exp(raw.astype(np.float64)) * np.float64(MIN_CONE)).astype(np.float32)
     tmp = np.zeros_like(grid0)
