@@ -126,14 +126,16 @@ struct insta_ctx {
     cudaGraph_t loop_graph = nullptr;
     cudaGraphExec_t loop_exec = nullptr;
     std::vector<unsigned char> loop_key;
-    uint32_t* loop_state = nullptr;                 // [0] steps of the current round, [1] rounds of this launch
-    unsigned long long* loop_rounds_total = nullptr; // rounds run by graph launches (launch statistics)
+    uint32_t* loop_state = nullptr;                 // [0] steps of the current round, [1] rounds of this launch,
+                                                    // [2] whether the body's second round ran
+    unsigned long long* loop_rounds_total = nullptr; // rounds (low 40 bits) and loop iterations of graph launches
     unsigned long long loop_rounds_seen = 0;
     uint32_t loop_round_kernels = 10;                // kernels per graph-run round (9 with the fused field stage)
     unsigned long long* walk_stats = nullptr;        // nearest-walk counters while stage timing is on
     // insta_render_async with host outputs: double-buffered device staging, copied back on a
     // copy stream while the next render runs
     cudaStream_t copy = nullptr;
+    cudaStream_t capture = nullptr;                 // captures the conditional second round of the graph body
     DevBuf async_rgba[2], async_depth[2];
     cudaEvent_t async_free[2] = {nullptr, nullptr}, async_done = nullptr;
     bool async_used[2] = {false, false};
@@ -709,25 +711,62 @@ struct WaveRun {
             cudaGraphNode_t node;
             CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
             cudaGraph_t body = cp.conditional.phGraph_out[0];
-            // the body by capture: two rounds, then the condition
-            CK(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-            cudaError_t e = cudaSuccess;
-            for (int half = 0; half < 2 && e == cudaSuccess; ++half) {
-                const WaveArgs& R = half ? B : A;
-                if (e == cudaSuccess) e = launch_round_begin(R.n_alive_in, R.n_alive_out, R.n_samples_round, ctx->loop_state, round_cap, steps_max,
-                                                             ctx->stream);
-                if (e == cudaSuccess) e = launch_march(R, ctx->stream);
-                if (e == cudaSuccess) e = launch_sort_samples(R, ctx->stream);
+            if (!ctx->capture) CK(cudaStreamCreateWithFlags(&ctx->capture, cudaStreamNonBlocking));
+            // one round's kernels on stream st
+            auto round_kernels = [&](const WaveArgs& R, cudaStream_t st) -> cudaError_t {
+                cudaError_t e = launch_round_begin(R.n_alive_in, R.n_alive_out, R.n_samples_round, ctx->loop_state, round_cap, steps_max, st);
+                if (e == cudaSuccess) e = launch_march(R, st);
+                if (e == cudaSuccess) e = launch_sort_samples(R, st);
                 if (fused_field()) {
-                    if (e == cudaSuccess) e = launch_nearest_stage(R, ctx->tune.deform_blocks_per_sm, ctx->stream);
-                    if (e == cudaSuccess) e = launch_field_fused(R, M, grid_tiles, ctx->stream, ctx->tune.mlp_ctas_per_sm);
+                    if (e == cudaSuccess) e = launch_nearest_stage(R, ctx->tune.deform_blocks_per_sm, st);
+                    if (e == cudaSuccess) e = launch_field_fused(R, M, grid_tiles, st, ctx->tune.mlp_ctas_per_sm);
                 } else {
-                    if (e == cudaSuccess) e = launch_deform_encode(R, ctx->tune.deform_blocks_per_sm, ctx->stream);
-                    if (e == cudaSuccess) e = launch_mlp(M, grid_tiles, ctx->stream, ctx->tune.mlp_ctas_per_sm, ctx->tune.mlp_slots);
+                    if (e == cudaSuccess) e = launch_deform_encode(R, ctx->tune.deform_blocks_per_sm, st);
+                    if (e == cudaSuccess) e = launch_mlp(M, grid_tiles, st, ctx->tune.mlp_ctas_per_sm, ctx->tune.mlp_slots);
                 }
-                if (e == cudaSuccess) e = launch_composite(R, ctx->stream);
+                if (e == cudaSuccess) e = launch_composite(R, st);
+                return e;
+            };
+            // The body by capture: round A; round B under a conditional IF node that
+            // round_mid_kernel sets only when rays are still alive (a frame whose rays all finish
+            // in round A launches none of B's kernels); then the loop condition.
+            CK(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+            cudaGraphConditionalHandle if_cond{};
+            cudaError_t e = cudaGraphConditionalHandleCreate(&if_cond, body, 0u, 0u);
+            if (e == cudaSuccess) e = round_kernels(A, ctx->stream);
+            if (e == cudaSuccess) e = launch_round_mid(A.n_alive_out, B.n_alive_out, ctx->loop_state + 2, if_cond, ctx->stream);
+            cudaGraph_t if_body = nullptr;
+            if (e == cudaSuccess) {
+                cudaStreamCaptureStatus status;
+                cudaGraph_t capturing = nullptr;
+                const cudaGraphNode_t* deps = nullptr;
+                size_t n_deps = 0;
+                e = cudaStreamGetCaptureInfo(ctx->stream, &status, nullptr, &capturing, &deps, nullptr, &n_deps);
+                if (e == cudaSuccess) {
+                    cudaGraphNodeParams ip{};
+                    ip.type = cudaGraphNodeTypeConditional;
+                    ip.conditional.handle = if_cond;
+                    ip.conditional.type = cudaGraphCondTypeIf;
+                    ip.conditional.size = 1;
+                    cudaGraphNode_t if_node = nullptr;
+                    e = cudaGraphAddNode(&if_node, capturing, deps, nullptr, n_deps, &ip);
+                    if (e == cudaSuccess) {
+                        if_body = ip.conditional.phGraph_out[0];
+                        e = cudaStreamUpdateCaptureDependencies(ctx->stream, &if_node, nullptr, 1, cudaStreamSetCaptureDependencies);
+                    }
+                }
             }
-            if (e == cudaSuccess) e = launch_round_end(B.n_alive_out, ctx->loop_state + 1, ctx->loop_rounds_total, max_rounds, cond, ctx->stream);
+            if (e == cudaSuccess) {
+                e = cudaStreamBeginCaptureToGraph(ctx->capture, if_body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+                if (e == cudaSuccess) {
+                    const cudaError_t eb = round_kernels(B, ctx->capture);
+                    cudaGraph_t captured_b = nullptr;
+                    const cudaError_t ee = cudaStreamEndCapture(ctx->capture, &captured_b);
+                    e = eb != cudaSuccess ? eb : ee;
+                }
+            }
+            if (e == cudaSuccess)
+                e = launch_round_end(B.n_alive_out, ctx->loop_state + 1, ctx->loop_state + 2, ctx->loop_rounds_total, max_rounds, cond, ctx->stream);
             cudaGraph_t captured = nullptr;
             const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &captured);
             CK(e);
@@ -1000,6 +1039,7 @@ int insta_ctx_destroy(insta_ctx* ctx) {
     if (ctx->loop_exec) cudaGraphExecDestroy(ctx->loop_exec);
     if (ctx->loop_graph) cudaGraphDestroy(ctx->loop_graph);
     if (ctx->loop_state) cudaFree(ctx->loop_state);
+    if (ctx->capture) cudaStreamDestroy(ctx->capture);
     if (ctx->walk_stats) cudaFree(ctx->walk_stats);
     ctx->release(ctx->side_scratch);
     for (auto& kv : ctx->avatars)
@@ -2029,11 +2069,12 @@ int insta_stats_read(insta_ctx* ctx, insta_stats* out, int reset) {
         if (!out) fail(INSTA_ERR_INVALID_ARG, "null output");
         ctx->collect_timings();
         if (ctx->loop_rounds_total) {
-            // graph-run rounds: loop_round_kernels per round plus the loop condition per pair of rounds
+            // graph-run rounds: loop_round_kernels per round, plus the mid and end kernels per loop
+            // iteration (the device total holds rounds in its low 40 bits, iterations above)
             unsigned long long total = 0;
             CK(cudaMemcpy(&total, ctx->loop_rounds_total, sizeof(total), cudaMemcpyDeviceToHost));
             const unsigned long long d = total - ctx->loop_rounds_seen;
-            ctx->launches += d * ctx->loop_round_kernels + d / 2ull;
+            ctx->launches += (d & ((1ull << 40) - 1ull)) * ctx->loop_round_kernels + (d >> 40) * 2ull;
             ctx->loop_rounds_seen = total;
         }
         out->kernel_launches = ctx->launches;

@@ -197,12 +197,17 @@ int64_t static_max_samples();
 cudaError_t static_scratch(int device, uint8_t** tiles, uint2** out, float4** out_f32);
 
 // Device-driven rounds for the CUDA-graph render loop: round_begin sets a round's step count from
-// its alive count and clears the counters it appends to; round_end (after two rounds) counts them
+// its alive count and clears the counters it appends to; round_end (after the body's rounds) counts them
 // and sets the loop's condition: rays alive and rounds left.
 cudaError_t launch_round_begin(const uint32_t* n_alive_in, uint32_t* n_alive_out, uint32_t* n_samples_round, uint32_t* steps,
                                uint64_t round_cap, uint32_t max_steps, cudaStream_t s);
-cudaError_t launch_round_end(const uint32_t* n_alive, uint32_t* rounds, unsigned long long* rounds_total, uint32_t max_rounds,
-                             cudaGraphConditionalHandle cond, cudaStream_t s);
+// Between the two rounds of the loop body: the second round's IF condition (rays left alive by
+// the first), and b_ran for round_end's count; clears the second round's output count when it is
+// skipped.
+cudaError_t launch_round_mid(const uint32_t* a_alive_out, uint32_t* b_alive_out, uint32_t* b_ran, cudaGraphConditionalHandle c,
+                             cudaStream_t s);
+cudaError_t launch_round_end(const uint32_t* n_alive, uint32_t* rounds, const uint32_t* b_ran, unsigned long long* rounds_total,
+                             uint32_t max_rounds, cudaGraphConditionalHandle cond, cudaStream_t s);
 // The field's training side (train_kernels.cu): forward with saved activations, output
 // gradients -> parameter gradients (FP32, snapshot order), Adam.
 struct TrainShape {

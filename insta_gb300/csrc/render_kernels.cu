@@ -1156,11 +1156,22 @@ __global__ void round_begin_kernel(const uint32_t* n_alive_in, uint32_t* n_alive
     *n_samples_round = 0u;
 }
 
-__global__ void round_end_kernel(const uint32_t* n_alive, uint32_t* rounds, unsigned long long* rounds_total, uint32_t max_rounds,
-                                 cudaGraphConditionalHandle cond) {
-    const uint32_t r = *rounds + 2u;
+// Between the body's two rounds: the second runs only when the first left rays alive; when it
+// does not, its output count (the first round's input count, consumed) is cleared so that the
+// loop condition and the host see no ray alive.
+__global__ void round_mid_kernel(const uint32_t* a_alive_out, uint32_t* b_alive_out, uint32_t* b_ran, cudaGraphConditionalHandle c) {
+    const bool more = *a_alive_out > 0u;
+    if (!more) *b_alive_out = 0u;
+    *b_ran = more ? 1u : 0u;
+    cudaGraphSetConditional(c, more ? 1u : 0u);
+}
+
+__global__ void round_end_kernel(const uint32_t* n_alive, uint32_t* rounds, const uint32_t* b_ran, unsigned long long* rounds_total,
+                                 uint32_t max_rounds, cudaGraphConditionalHandle cond) {
+    const uint32_t ran = 1u + *b_ran;
+    const uint32_t r = *rounds + ran;
     *rounds = r;
-    *rounds_total += 2ull;
+    *rounds_total += (unsigned long long)ran + (1ull << 40);   // rounds in the low 40 bits, loop iterations above
     cudaGraphSetConditional(cond, (*n_alive > 0u && r < max_rounds) ? 1u : 0u);
 }
 
@@ -1170,9 +1181,15 @@ cudaError_t launch_round_begin(const uint32_t* n_alive_in, uint32_t* n_alive_out
     return cudaGetLastError();
 }
 
-cudaError_t launch_round_end(const uint32_t* n_alive, uint32_t* rounds, unsigned long long* rounds_total, uint32_t max_rounds,
-                             cudaGraphConditionalHandle cond, cudaStream_t s) {
-    round_end_kernel<<<1, 1, 0, s>>>(n_alive, rounds, rounds_total, max_rounds, cond);
+cudaError_t launch_round_mid(const uint32_t* a_alive_out, uint32_t* b_alive_out, uint32_t* b_ran, cudaGraphConditionalHandle c,
+                             cudaStream_t s) {
+    round_mid_kernel<<<1, 1, 0, s>>>(a_alive_out, b_alive_out, b_ran, c);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_round_end(const uint32_t* n_alive, uint32_t* rounds, const uint32_t* b_ran, unsigned long long* rounds_total,
+                             uint32_t max_rounds, cudaGraphConditionalHandle cond, cudaStream_t s) {
+    round_end_kernel<<<1, 1, 0, s>>>(n_alive, rounds, b_ran, rounds_total, max_rounds, cond);
     return cudaGetLastError();
 }
 
