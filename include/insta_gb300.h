@@ -480,8 +480,9 @@ typedef struct insta_tuning {
                                        copy of the weights (one sample row per thread); 1 = several CTAs per
                                        SM, each with its own copy (mlp_ctas_per_sm); 8 = FP16 / BF16 only:
                                        CTAs of two tiles each, an MMA-issuing warp and two epilogue warpgroups;
-                                       0 = built-in: slots for FP8 fields and for batches of two or more
-                                       requests on one weight image (measured faster there), else CTAs */
+                                       0 = built-in: slots for FP8 fields, for batches of two or more
+                                       requests on one weight image and for encodings wider than 64
+                                       (measured faster there), else CTAs */
 } insta_tuning;
 int insta_tuning_set(insta_ctx* ctx, const insta_tuning* t);
 int insta_tuning_get(insta_ctx* ctx, insta_tuning* t);

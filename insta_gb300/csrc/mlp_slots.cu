@@ -30,9 +30,16 @@ constexpr uint32_t kMaxSlots = 7;
 // TMEM columns of the hidden activations per slot (A operand, 64 values per row)
 __host__ __device__ constexpr uint32_t a_cols(bool fp8) { return fp8 ? 16u : 32u; }
 __host__ __device__ constexpr uint32_t max_slots_tmem(bool fp8) { return 512u / (64u + a_cols(fp8)); }
-constexpr uint32_t kSlotBytes = 24576;    // FP16 / BF16: [0, 16 KiB) hash rows, then activations; SH rows; density rows
+constexpr uint32_t kSlotBytes = 24576;    // FP16 / BF16 up to 64 density inputs: [0, 16 KiB) hash rows; SH rows; density rows
 constexpr uint32_t kSlotBytes8 = 32768;   // FP8: hash rows (FP16); SH rows (FP16); E4M3 layer input; E4M3 colour input
-__host__ __device__ constexpr uint32_t slot_bytes(bool fp8) { return fp8 ? kSlotBytes8 : kSlotBytes; }
+// FP16 / BF16 slots hold the hash rows in max(16 KiB, the hash tile rounded to 1 KiB), then 4 KiB
+// of SH rows and 4 KiB of density rows (wider encodings: 128 hash features + 16 expression dims
+// take 36 KiB); FP8 slots take at most 64 density inputs.
+__host__ __device__ inline uint32_t hash_region(const TilePlan& P, bool fp8) {
+    const uint32_t h = (hash_tile_bytes(P.k_in) + 1023u) & ~1023u;
+    return fp8 || h < 16384u ? 16384u : h;
+}
+__host__ __device__ inline uint32_t slot_bytes(const TilePlan& P, bool fp8) { return fp8 ? kSlotBytes8 : hash_region(P, false) + 8192u; }
 constexpr uint32_t kCtlBytes = 1024;
 
 struct SlotCtl {
@@ -154,8 +161,8 @@ __global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel
     extern __shared__ __align__(1024) uint8_t smem[];
     SlotCtl& ctl = *reinterpret_cast<SlotCtl*>(smem);
     uint8_t* slots = smem + kCtlBytes;
-    uint8_t* w = slots + n_slots * slot_bytes(FP8);
     const TilePlan& P = A.plan;
+    uint8_t* w = slots + n_slots * slot_bytes(P, FP8);
     const uint32_t n_samples = A.n_alive ? *A.n_alive : (uint32_t)A.n_samples;
     const uint32_t n_tiles = (n_samples + 127u) / 128u;
     const uint32_t stride = gridDim.x * n_slots;
@@ -184,9 +191,9 @@ __global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel
     tc_fence_after();
     const uint32_t tmem = ctl.tmem_base;
 
-    uint8_t* st = slots + s * slot_bytes(FP8);
-    uint8_t* sh = st + 16384;
-    uint8_t* dens = st + 20480;   // FP16 / BF16 density rows; FP8: the E4M3 layer input
+    uint8_t* st = slots + s * slot_bytes(P, FP8);
+    uint8_t* sh = st + hash_region(P, FP8);
+    uint8_t* dens = sh + 4096;    // FP16 / BF16 density rows; FP8: the E4M3 layer input
     uint8_t* rgb8 = st + 28672;   // FP8: E4M3 [density output | SH] rows
     const uint32_t col0 = tmem + ((warp & 3u) * 32u << 16) + s * 64u;
     const uint32_t a_col = n_slots * 64u + s * a_cols(FP8);            // the slot's A operand columns
@@ -633,16 +640,16 @@ cudaError_t launch_mlp_pairs(const MlpArgs& a, const uint8_t* image, uint32_t ma
 }
 
 uint32_t mlp_slots_for(const TilePlan& P, int smem_optin, bool fp8) {
-    if (P.k_in > 64u || (fp8 && P.k8 > 64u)) return 0;
+    if (fp8 && (P.k_in > 64u || P.k8 > 64u)) return 0;
     const long avail = (long)smem_optin - (long)kCtlBytes - (long)((P.bytes + 1023u) & ~1023u);
-    long n = avail / (long)slot_bytes(fp8);
+    long n = avail / (long)slot_bytes(P, fp8);
     if (n > (long)max_slots_tmem(fp8)) n = max_slots_tmem(fp8);
     return n < 2 ? 0u : (uint32_t)n;
 }
 
 cudaError_t launch_mlp_slots(const MlpArgs& a, const uint8_t* image, uint32_t n_slots, uint32_t max_tiles, int n_sms, cudaStream_t s) {
     const bool fp8 = a.fv.precision == 2;
-    const size_t smem = kCtlBytes + (size_t)n_slots * slot_bytes(fp8) + a.plan.bytes;
+    const size_t smem = kCtlBytes + (size_t)n_slots * slot_bytes(a.plan, fp8) + a.plan.bytes;
     const void* fn = fp8 ? (const void*)mlp_slots_kernel<true> : (const void*)mlp_slots_kernel<false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

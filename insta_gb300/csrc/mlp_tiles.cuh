@@ -58,7 +58,8 @@ struct MlpArgs {
 
 // slots (insta_tuning.mlp_slots): 2..7 = mlp_slots_kernel with that many slots where every tile
 // uses one weight image; 8 = mlp_pairs_kernel there (FP16 / BF16); 1 = mlp256_kernel; 0 =
-// mlp_slots_kernel for FP8 fields and for render batches on one weight image, else mlp256_kernel.  ctas_per_sm: mlp256_kernel's resident CTAs per SM
+// mlp_slots_kernel for FP8 fields, for render batches on one weight image and for encodings
+// wider than 64, else mlp256_kernel.  ctas_per_sm: mlp256_kernel's resident CTAs per SM
 // (0 = as many as shared memory lets reside, at most 4).
 cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uint32_t ctas_per_sm = 0, uint32_t slots = 0);
 // mlp_slots.cu: slots that fit the opt-in shared memory (0 = the kernel does not apply), launch

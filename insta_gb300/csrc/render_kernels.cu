@@ -1117,7 +1117,9 @@ cudaError_t launch_mlp(const MlpArgs& a, uint32_t max_tiles, cudaStream_t s, uin
     const bool fp8 = a.fv.precision == 2;
     const uint8_t* image = a.seg ? a.single : a.fv.mlp_smem;
     if (image && slots == 8 && !fp8 && a.plan.k_in <= 64u) return launch_mlp_pairs(a, image, max_tiles, sm_count(), ctas_per_sm, s);
-    const bool want_slots = (slots >= 2 && slots <= 7) || (slots == 0 && (fp8 || (a.seg && a.batch)));
+    // built in: slots for FP8, for batches on one weight image, and for encodings wider than 64
+    // (the per-CTA kernel fits two CTAs per SM there; four slots share one copy of the weights)
+    const bool want_slots = (slots >= 2 && slots <= 7) || (slots == 0 && (fp8 || (a.seg && a.batch) || a.plan.k_in > 64u));
     if (image && want_slots) {
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);

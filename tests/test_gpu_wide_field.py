@@ -103,6 +103,29 @@ def test_wide_field_render_psnr(ctx, wide, oracle, oracle_frame, avatar):
     assert psnr(rgba, r_rgba) >= 45.0
 
 
+def test_wide_field_mlp_kernels_equal(ctx, wide):
+    """INSTA's field through the tile-slot MLP kernel (slots sized for the 144-wide encoding) and
+    the per-CTA kernel: the same bits."""
+    from insta_gb300 import synthetic as S
+    aid, fc, params = wide["insta"]
+    W = H = 96
+    extra = np.linspace(-1, 1, 16).astype(np.float32)
+    cam, focal = S.camera(8.0, width=W, height=H)
+    req = ctx.render_desc(aid, 0, W, H, focal, cam, extra_dims=extra)
+    outs = []
+    for slots in (1, 4):
+        rgba = np.zeros((W * H, 4), np.float32)
+        depth = np.zeros(W * H, np.float32)
+        ctx.tuning_set(mlp_slots=slots)
+        try:
+            ctx.render(req, rgba, depth)
+        finally:
+            ctx.tuning_set()
+        outs.append((rgba, depth))
+    assert (outs[0][0][:, 3] > 0.01).sum() > 100
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
 @pytest.mark.parametrize("kind", ["insta", "f4"])
 def test_wide_field_backward_matches_oracle(ctx, wide, oracle, kind):
     """FP32 layer products (cuBLAS) and the 4- / 8-feature table backward (16-byte reductions)
