@@ -93,12 +93,12 @@ __device__ __forceinline__ bool issue_chain(Smem& sm, const uint8_t* const* a, c
         }
         umma_commit(&sm.bar_mma);
     }
-    // warp 0 waits for the chain's commit; the others sleep at the barrier instead of polling the
-    // mbarrier (their issue slots go to the other CTAs' epilogues), then order their TMEM reads
-    // after it
-    bool ok = true;
-    if (threadIdx.x < 32u) ok = mbar_wait(&sm.bar_mma, phase);
-    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    // every thread waits for the chain's commit on the mbarrier (try_wait suspends the warp until
+    // the phase completes, so no CTA barrier is needed after it; measured 0.128 -> 0.124 ms per
+    // 512x512 frame against warp 0 polling and a CTA barrier), then orders its TMEM reads after
+    // it.  A wait that gives up makes only that thread's result false: the tile loop agrees on it
+    // at its closing barrier.
+    const bool ok = mbar_wait(&sm.bar_mma, phase);
     phase ^= 1u;
     tc_fence_after();
     return ok;
@@ -129,9 +129,7 @@ __device__ __forceinline__ bool issue_chain_ts(Smem& sm, const uint8_t* b, uint3
         }
         umma_commit(&sm.bar_mma);
     }
-    bool ok = true;
-    if (threadIdx.x < 32u) ok = mbar_wait(&sm.bar_mma, phase);
-    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    const bool ok = mbar_wait(&sm.bar_mma, phase);
     phase ^= 1u;
     tc_fence_after();
     return ok;
