@@ -1,9 +1,10 @@
 // mlp_slots.cu -- the avatar MLPs over ready-made operand tiles with several tiles in flight per
 // SM: one persistent CTA per SM holds the weight image once, and up to kMaxSlots tile slots, each
 // a warpgroup of 128 threads (one sample row per thread) with its own shared-memory tile, its own
-// 64 TMEM columns and its own chain (one thread issues the layer's MMAs, one warp waits on the
-// commit, the slot's named barrier releases the others, the epilogue converts the accumulator
-// into the next layer's operand rows).  The slots synchronise only within themselves, so one
+// 64 TMEM columns and its own chain (one thread issues the layer's MMAs, every thread of the slot
+// waits on the commit mbarrier -- the slot's named barrier is taken once per layer, before the
+// issue, and also agrees on the waits' outcome --, the epilogue converts the accumulator into the
+// next layer's operand).  The slots synchronise only within themselves, so one
 // slot's epilogue overlaps the others' MMAs; compared with mlp256_kernel (four CTAs of 256
 // threads per SM, each with its own copy of the weights) more tiles are in flight per SM.  Same
 // arithmetic and rounding as mlp256_kernel (FP16 / BF16): NerfNetwork::
@@ -210,6 +211,7 @@ __global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel
         if (r == 0) load(t);
         ++n_loads;
     }
+    bool dok = true;   // this thread's commit waits since the slot's last agreement
     for (; t < n_tiles && ok; t += stride) {
         float o4[4] = {0.f, 0.f, 0.f, 0.f};
         if constexpr (FP8) {
@@ -221,7 +223,7 @@ __global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel
                 bool wok = true;
                 if (l == -1 && waiter) wok = mbar_wait(&ctl.full[s], n_used & 1u);
                 if (l == -1) ++n_used;
-                ok = slot_sync_and(bar_id, wok);
+                ok = slot_sync_and(bar_id, wok && dok);
                 if (!ok) break;
                 tc_fence_after();
                 if (l == -1) {
@@ -263,11 +265,8 @@ __global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel
                     }
                     umma_commit(&ctl.done[s]);
                 }
-                wok = true;
-                if (waiter) wok = mbar_wait(&ctl.done[s], n_done & 1u);
+                dok = mbar_wait(&ctl.done[s], n_done & 1u) && dok;   // every thread; agreed at the next sync
                 ++n_done;
-                ok = slot_sync_and(bar_id, wok);
-                if (!ok) break;
                 tc_fence_after();
                 const float sw = ls[l];
                 if (l == (int)P.n_dh) {
@@ -302,7 +301,7 @@ __global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel
                 bool wok = true;
                 if (l == 0 && waiter) wok = mbar_wait(&ctl.full[s], n_used & 1u);
                 if (l == 0) ++n_used;
-                ok = slot_sync_and(bar_id, wok);
+                ok = slot_sync_and(bar_id, wok && dok);
                 if (!ok) break;
                 tc_fence_after();
                 if (r == 0) {
@@ -325,11 +324,8 @@ __global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel
                     }
                     umma_commit(&ctl.done[s]);
                 }
-                wok = true;
-                if (waiter) wok = mbar_wait(&ctl.done[s], n_done & 1u);
+                dok = mbar_wait(&ctl.done[s], n_done & 1u) && dok;   // every thread; agreed at the next sync
                 ++n_done;
-                ok = slot_sync_and(bar_id, wok);
-                if (!ok) break;
                 tc_fence_after();
                 // hash and SH rows are read once colour layer 0 has completed
                 if (l == P.n_dh + 1 && r == 0 && t + stride < n_tiles) load(t + stride);
@@ -376,6 +372,7 @@ __global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel
             }
         }
     }
+    ok = slot_sync_and(bar_id, ok && dok);
     // a record whose copies were issued but not consumed (after a timeout): wait for them
     // (bounded) before shared memory is released
     if (r == 0 && n_loads > n_used) mbar_wait(&ctl.full[s], (n_loads - 1u) & 1u);
