@@ -267,6 +267,7 @@ __global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel
                 }
                 dok = mbar_wait(&ctl.done[s], n_done & 1u) && dok;   // every thread; agreed at the next sync
                 ++n_done;
+                __syncwarp();   // the TMEM loads below are warp-collective
                 tc_fence_after();
                 const float sw = ls[l];
                 if (l == (int)P.n_dh) {
@@ -326,6 +327,7 @@ __global__ void __launch_bounds__(max_slots_tmem(FP8) * 128, 1) mlp_slots_kernel
                 }
                 dok = mbar_wait(&ctl.done[s], n_done & 1u) && dok;   // every thread; agreed at the next sync
                 ++n_done;
+                __syncwarp();   // the TMEM loads below are warp-collective
                 tc_fence_after();
                 // hash and SH rows are read once colour layer 0 has completed
                 if (l == P.n_dh + 1 && r == 0 && t + stride < n_tiles) load(t + stride);

@@ -100,6 +100,7 @@ __device__ __forceinline__ bool issue_chain(Smem& sm, const uint8_t* const* a, c
     // at its closing barrier.
     const bool ok = mbar_wait(&sm.bar_mma, phase);
     phase ^= 1u;
+    __syncwarp();   // the epilogue's TMEM loads are warp-collective
     tc_fence_after();
     return ok;
 }
@@ -131,6 +132,7 @@ __device__ __forceinline__ bool issue_chain_ts(Smem& sm, const uint8_t* b, uint3
     }
     const bool ok = mbar_wait(&sm.bar_mma, phase);
     phase ^= 1u;
+    __syncwarp();   // the epilogue's TMEM loads are warp-collective
     tc_fence_after();
     return ok;
 }

@@ -43,14 +43,6 @@ struct TrainCtl {
     uint32_t tmem_base;
 };
 
-// The epilogue threads (not the MMA warp) meet at named barrier 1; true when every one passed true.
-__device__ __forceinline__ bool epi_sync_and(bool v) {
-    uint32_t r;
-    asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n barrier.cta.red.and.pred q, 1, %2, p;\n selp.u32 %0, 1, 0, q;\n}\n"
-                 : "=r"(r) : "r"(v ? 1u : 0u), "n"(kEpiThreads) : "memory");
-    return r != 0;
-}
-
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
@@ -218,12 +210,15 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
         }
         umma_commit(&ctl.bar_mma[s]);
     };
-    // Epilogue threads: wait (warp 0 polls, bounded) for slot s's commit, then release the others.
+    // Epilogue threads: each waits (bounded) for slot s's commit itself.  The commit orders the
+    // MMAs' reads of the published tiles before any thread's next epilogue overwrites them, and no
+    // thread can run a phase ahead: the next commit needs every epilogue thread's publish.  A wait
+    // that gives up makes only that thread's flag false; the pair loop agrees on it at the next CTA
+    // barrier, and the thread skips its later waits meanwhile (bounded work, results discarded).
     auto epi_wait = [&](uint32_t s) -> bool {
-        bool w = true;
-        if (threadIdx.x < 32u) w = mbar_wait(&ctl.bar_mma[s], (phase >> s) & 1u);
+        const bool w = mbar_wait(&ctl.bar_mma[s], (phase >> s) & 1u);
         phase ^= 1u << s;
-        w = epi_sync_and(w);
+        __syncwarp();   // the epilogue's TMEM loads are warp-collective
         tc_fence_after();
         return w;
     };
@@ -361,23 +356,21 @@ __global__ void __launch_bounds__(kThreads, 1) train_mlp_kernel(const __grid_con
             }
         } else {
             for (int k = 0; k < n_steps; ++k) {
-                ok = epi_wait(0);
-                if (!ok) break;
+                ok = ok && epi_wait(0);
                 epilogue(0, ta, k);
                 if (k + 1 < n_steps) publish(0);
                 if (has_b) {
-                    ok = epi_wait(1);
-                    if (!ok) break;
+                    ok = ok && epi_wait(1);
                     epilogue(1, tb, k);
                     if (k + 1 < n_steps) publish(1);
                 }
             }
         }
     }
-    if (!ok && threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
     tc_fence_before();
-    __syncthreads();
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;   // the flush below runs on all epilogue threads or none
     tc_fence_after();
+    if (!ok && threadIdx.x == 0) atomicOr(A.err, INSTA_DEVERR_TIMEOUT);
     // ---- flush the weight gradients: accumulator row f = input feature f, column o = output o.
     // dw_started is thread 0's; the flush runs when the backward ran on at least one tile.
     if (backward && ok && !mma_warp && n_tiles > blockIdx.x * 2u) {
