@@ -800,7 +800,8 @@ def run_serve(args):
     ctx.sync()
 
     def serve(order_arrivals, count):
-        srv = abi.Server(ctx, max_inflight=args.slots, max_inflight_pixels=args.slot_pixels, rounds_per_launch=2)
+        srv = abi.Server(ctx, max_inflight=args.slots, max_inflight_pixels=args.slot_pixels, rounds_per_launch=2,
+                         round_samples=args.round_samples)
         tickets = []
         t_s = time.perf_counter()
         for k in range(count):
@@ -831,7 +832,8 @@ def run_serve(args):
                         "capacity_frames_per_s": batched_capacity, "frames_per_s": ok / span,
                         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                         "p99_512_ms": float(np.percentile(lat[sizes == 512], 99)),
-                        "slots": args.slots, "slot_pixels": args.slot_pixels, "rounds_per_launch": 2, "tuning": tuned},
+                        "slots": args.slots, "slot_pixels": args.slot_pixels, "rounds_per_launch": 2,
+                        "round_samples": args.round_samples or (32 << 20), "tuning": tuned},
             "plain": {"precision": "fp16 mlp, fp32 geometry", "capacity_frames_per_s": plain_capacity, "frames_per_s": n / plain_span,
                       "p50_ms": float(np.percentile(plain_lat, 50)), "p99_ms": float(np.percentile(plain_lat, 99)),
                       "p99_512_ms": float(np.percentile(plain_lat[sizes == 512], 99))},
@@ -952,6 +954,7 @@ def main():
     ap.add_argument("--duration", type=float, default=30.0)
     ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--slot-pixels", type=int, default=6 << 20)
+    ap.add_argument("--round-samples", type=int, default=0, help="served stream: samples per round at most (0 = 2^25)")
     args = ap.parse_args()
     global WIDTH, HEIGHT, FIELD
     WIDTH = HEIGHT = args.width

@@ -534,6 +534,10 @@ typedef struct {
     double occupancy_radius;        /* request frames: occupancy from the mesh (0.015) */
     uint32_t rounds_per_launch;     /* rounds run as one CUDA-graph launch between admission points
                                        (even; 0 = 2); with per-stage timing on, rounds are host-driven */
+    uint64_t round_samples;         /* samples marched per round at most (2^16..2^25; 0 = 2^25;
+                                       raised to max_inflight_pixels): a smaller budget gives
+                                       shorter rounds, so arriving requests join sooner, at more
+                                       rounds per ray */
 } insta_server_config;
 
 int insta_server_create(insta_ctx* ctx, const insta_server_config* cfg, insta_server** out);

@@ -38,7 +38,7 @@ REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
 
 class ServerConfig(C.Structure):
     _fields_ = [("max_inflight", C.c_uint32), ("max_inflight_pixels", C.c_uint64), ("occupancy_radius", C.c_double),
-                ("rounds_per_launch", C.c_uint32)]
+                ("rounds_per_launch", C.c_uint32), ("round_samples", C.c_uint64)]
 
 
 class Pcg32State(C.Structure):
@@ -528,10 +528,11 @@ class Context:
 class Server:
     """The request loop (insta_server_*): owns `ctx` from creation to close()."""
 
-    def __init__(self, ctx: Context, max_inflight=16, max_inflight_pixels=1 << 22, occupancy_radius=0.015, rounds_per_launch=0):
+    def __init__(self, ctx: Context, max_inflight=16, max_inflight_pixels=1 << 22, occupancy_radius=0.015, rounds_per_launch=0,
+                 round_samples=0):
         self.ctx = ctx
         self.lib = ctx.lib
-        cfg = ServerConfig(max_inflight, max_inflight_pixels, occupancy_radius, rounds_per_launch)
+        cfg = ServerConfig(max_inflight, max_inflight_pixels, occupancy_radius, rounds_per_launch, round_samples)
         h = C.c_void_p()
         ctx._check(self.lib.insta_server_create(ctx.h, C.byref(cfg), C.byref(h)))
         self.h = h

@@ -551,14 +551,17 @@ struct WaveRun {
     }
 
     // Scratch for up to max_rays alive rays over n_slots slots sharing `field`'s layout.
-    void setup(insta_ctx* c, const Field& field, uint32_t slots, uint64_t max_rays, bool per_request_counts) {
+    void setup(insta_ctx* c, const Field& field, uint32_t slots, uint64_t max_rays, bool per_request_counts,
+               uint64_t max_round_samples = kMaxRoundSamples) {
         ctx = c;
         n_slots = slots;
         const FieldView& fv = field.view;
         const TilePlan& P = field.plan;
         Wave& w = ctx->wave;
         steps_max = tune_steps(ctx);
-        round_cap = std::min<uint64_t>(max_rays * steps_max, kMaxRoundSamples);
+        // at least one sample per alive ray fits a round: the march takes max(1, cap / alive) steps
+        // per ray and writes into buffers of cap_samples (max_rays <= 2^25 = kMaxRoundSamples)
+        round_cap = std::min<uint64_t>(max_rays * steps_max, std::max(max_rays, std::min(max_round_samples, kMaxRoundSamples)));
         cap_samples = (round_cap + (uint64_t)slots * 128 + 127) / 128 * 128;
         const uint32_t cell_bits = sort_cell_bits(slots, tune_cell_bits(ctx, slots));
         const uint64_t n_bins = (uint64_t)slots << cell_bits;
@@ -2226,7 +2229,8 @@ struct insta_server {
                 if (!a.field.ready) fail(INSTA_ERR_NOT_READY, "avatar %d has no field parameters", r->desc.avatar);
                 if (!layout) {
                     layout = &a.field;
-                    run.setup(ctx, a.field, cfg.max_inflight, cfg.max_inflight_pixels, true);
+                    run.setup(ctx, a.field, cfg.max_inflight, cfg.max_inflight_pixels, true,
+                              cfg.round_samples ? cfg.round_samples : kMaxRoundSamples);
                 } else if (!same_field_layout(*layout, a.field)) {
                     fail(INSTA_ERR_UNSUPPORTED, "the server's requests must share one field layout");
                 }
@@ -2468,6 +2472,8 @@ int insta_server_create(insta_ctx* ctx, const insta_server_config* cfg, insta_se
             fail(INSTA_ERR_INVALID_ARG, "max_inflight_pixels must be 1..2^25");
         if (!(cfg->occupancy_radius > 0.0)) fail(INSTA_ERR_INVALID_ARG, "occupancy_radius must be positive");
         if (cfg->rounds_per_launch % 2 || cfg->rounds_per_launch > 64) fail(INSTA_ERR_INVALID_ARG, "rounds_per_launch must be even, 0..64");
+        if (cfg->round_samples && (cfg->round_samples < (1ull << 16) || cfg->round_samples > kMaxRoundSamples))
+            fail(INSTA_ERR_INVALID_ARG, "round_samples must be 0 or 2^16..2^25");
         auto s = std::make_unique<insta_server>();
         s->ctx = ctx;
         s->cfg = *cfg;

@@ -89,6 +89,27 @@ def test_server_alone_equals_in_the_mix(serve_ctx):
     assert torch.equal(alone[0], mix[0][0]) and torch.equal(alone[1], mix[0][1])
 
 
+def test_server_short_rounds_equal_single_renders(serve_ctx):
+    """A round budget of 2^16 samples (many short rounds, a few steps per ray each): the same
+    pixels as insta_render alone; budgets outside 2^16..2^25 are refused."""
+    from insta_gb300 import abi
+    ctx, avatars = serve_ctx
+    reqs = make_requests(ctx, avatars, 6, seed=3)
+    outs = [(np.full((r.width * r.height, 4), -1, np.float32), np.full(r.width * r.height, -1, np.float32)) for r, _ in reqs]
+    srv = abi.Server(ctx, max_inflight=4, max_inflight_pixels=2 * 64 * 64, round_samples=1 << 16)
+    tickets = [srv.submit(r, v, o[0], o[1]) for (r, v), o in zip(reqs, outs)]
+    states = [srv.wait(t, 60000) for t in tickets]
+    srv.close()
+    assert states == [abi.REQ_DONE] * len(tickets), states
+    for (r, v), (rgba, depth) in zip(reqs, outs):
+        ref_rgba, ref_depth = single_render(ctx, r, v)
+        assert (rgba == ref_rgba).all() and (depth == ref_depth).all()
+    for bad in (1000, (1 << 25) + 1):
+        with pytest.raises(abi.InstaError) as e:
+            abi.Server(ctx, max_inflight=2, max_inflight_pixels=1 << 16, round_samples=bad)
+        assert e.value.code == abi.ERR_INVALID_ARG
+
+
 def test_server_cancel_queued(serve_ctx):
     from insta_gb300 import abi, synthetic as S
     ctx, avatars = serve_ctx
