@@ -617,6 +617,7 @@ struct WaveRun {
         W.init_slot = W.init_tile + (slots + 1);
         W.n_samples_round = counters + 2;
         W.n_samples_padded = counters + 3;
+        W.nearest_work = counters + 4;
         W.out = (const uint2*)w.out.p;
         W.out_f32 = (const float4*)w.out_f32.p;
         W.n_round = (uint32_t*)w.n_round.p;
@@ -636,7 +637,7 @@ struct WaveRun {
         cur = 0;
         n_alive = 0;
         CK(cudaMemsetAsync(ctx->sample_counter, 0, sizeof(unsigned long long), ctx->stream));
-        CK(cudaMemsetAsync(counters, 0, 8, ctx->stream));
+        CK(cudaMemsetAsync(counters, 0, 24, ctx->stream));   // alive counts, round counts, nearest-stage work
         if (W.req_alive) CK(cudaMemsetAsync(W.req_alive, 0, (size_t)slots * sizeof(uint32_t), ctx->stream));
     }
 

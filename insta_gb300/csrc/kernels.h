@@ -102,6 +102,7 @@ struct WaveArgs {
     unsigned long long* sample_counter;
     uint32_t top_nodes;         // nearest stage: top tree nodes each warp stages in shared memory (0: none)
     unsigned long long* walk_stats;  // nearest stage: walk counters (see nearest_warp), or null
+    uint32_t* nearest_work;     // nearest stage: [0] next 32-sample chunk, [1] warps finished (zero between launches)
     uint32_t* err;
 };
 

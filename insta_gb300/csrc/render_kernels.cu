@@ -461,7 +461,13 @@ __global__ void __launch_bounds__(256, 4) nearest_stage_kernel(const __grid_cons
         }
         __syncwarp();
     }
-    for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32u; base < n; base += n_warps * 32u) {
+    // 32-sample chunks are handed out by a device cursor (walk costs vary from chunk to chunk, so
+    // a fixed share per warp leaves SMs idle at the end); the last warp to finish resets it
+    for (;;) {
+        uint32_t chunk = 0;
+        if (lane == 0) chunk = atomicAdd(A.nearest_work, 1u);
+        const uint32_t base = __shfl_sync(0xffffffffu, chunk, 0) * 32u;
+        if (base >= n) break;
         const uint32_t s = base + lane;
         const uint32_t m = A.sample_order[s];
         const bool valid = m != kNoSample;
@@ -505,6 +511,14 @@ __global__ void __launch_bounds__(256, 4) nearest_stage_kernel(const __grid_cons
     }
     // a copy that timed out may still land: wait for it (bounded) before the CTA's shared memory goes
     if (A.top_nodes > 0 && !top_ok) mbar_wait(&top_bar[warp], top_phase);
+    if (lane == 0) {
+        __threadfence();   // this warp's last cursor increment before its count
+        if (atomicAdd(A.nearest_work + 1, 1u) == n_warps - 1u) {
+            A.nearest_work[0] = 0u;
+            A.nearest_work[1] = 0u;
+            __threadfence();
+        }
+    }
 }
 
 // The deform half of the stage for sorted position s holding march-order sample m: the warp hook
